@@ -1,0 +1,221 @@
+"""ctypes mirror of include/epic_gb300.h and numpy-backed storage for its structs.
+
+The structs carry what the reference's timestep() reads from the globals `grid`, `planet`
+and `var` (include/epic_datatypes.h:238-627); the arrays keep the reference memory layout
+X(k,j,i) = base[i + (j+1)*(ni+2) + k*(ni+2)*(nj+3)] (include/epic.h:407-449).
+"""
+from __future__ import annotations
+
+import ctypes as C
+from dataclasses import dataclass, field
+
+import numpy as np
+
+EPIC_STEP_PROGS_AND_SYNC_DIAGS = 0
+EPIC_SYNC_DIAGS_ONLY = 1
+EPIC_UV_AB3 = 0
+EPIC_UV_LEAPFROG = 1
+EPIC_PREC_FP64 = 0
+EPIC_PREC_MIXED = 1
+
+_dp = C.POINTER(C.c_double)
+
+
+class EpicGrid(C.Structure):
+    _fields_ = [
+        ("ni", C.c_int32), ("nj", C.c_int32), ("nk", C.c_int32), ("dt", C.c_int32),
+        ("uv_scheme", C.c_int32), ("k_sigma", C.c_int32), ("k_sponge", C.c_int32),
+        ("newt_cool_on", C.c_int32), ("newt_cool_adjust", C.c_int32), ("drag_v", C.c_int32),
+        ("drag_zonal_avg", C.c_int32), ("jtp", C.c_int32),
+        ("dln", C.c_double), ("dlt", C.c_double), ("dy0", C.c_double),
+        ("globe_latbot", C.c_double), ("globe_lattop", C.c_double), ("press0", C.c_double),
+        ("topo_scale", C.c_double), ("prandtl", C.c_double), ("tau_drag", C.c_double),
+        ("nudiv_nondim", C.c_double),
+        ("zeta0", C.c_double), ("zeta1", C.c_double), ("hybrid_alpha", C.c_double),
+        ("sigma_sigma", C.c_double),
+        ("nu", C.c_double * 9),
+        ("re", C.c_double), ("rp", C.c_double), ("cp", C.c_double), ("rgas", C.c_double),
+        ("kappa", C.c_double), ("kinvisc", C.c_double), ("lat0", C.c_double), ("hs_kf", C.c_double),
+        ("lon", _dp), ("lat", _dp), ("rln", _dp), ("rlt", _dp), ("f", _dp), ("m", _dp), ("n", _dp),
+        ("mn", _dp), ("g", _dp), ("sigmatheta", _dp), ("dsgth", _dp), ("dsgth_inv", _dp),
+        ("h_min", _dp), ("t_sponge_inv", _dp),
+    ]
+
+
+FIELD_NAMES_3D = ["hdry", "theta", "p3", "h3", "p2", "theta2", "t2", "t3", "rho2", "rho3", "exner3",
+                  "gz3", "mont3", "heat3", "pv3", "ri2", "div_uv3", "w3", "dzdt3", "u_spinup"]
+PROGNOSTIC = ["u", "v", "hdry", "theta"]
+
+
+class EpicFields(C.Structure):
+    _fields_ = ([(n, _dp) for n in ["u", "v", "dudt", "dvdt"]]
+                + [(n, _dp) for n in FIELD_NAMES_3D]
+                + [("gz_surface", _dp),
+                   ("it_zero", C.c_int32), ("it_minus1", C.c_int32), ("it_minus2", C.c_int32),
+                   ("pad0", C.c_int32), ("itime", C.c_int64), ("model_time", C.c_int64)])
+
+
+class EpicHsParams(C.Structure):
+    _fields_ = [("ni", C.c_int32), ("nj", C.c_int32), ("nk", C.c_int32), ("dt", C.c_int32),
+                ("uv_scheme", C.c_int32), ("pad0", C.c_int32),
+                ("ptop", C.c_double), ("pbot", C.c_double), ("p_sigma", C.c_double),
+                ("nu_nondim", C.c_double * 9), ("nudiv_nondim", C.c_double), ("lat0", C.c_double)]
+
+
+def _ptr(a: np.ndarray):
+    assert a.dtype == np.float64 and a.flags["C_CONTIGUOUS"]
+    return a.ctypes.data_as(_dp)
+
+
+@dataclass
+class Layout:
+    ni: int
+    nj: int
+    nk: int
+
+    @property
+    def shape3(self):
+        return (self.nk + 2, self.nj + 3, self.ni + 2)
+
+    @property
+    def shape2(self):
+        return (self.nj + 3, self.ni + 2)
+
+    @property
+    def n3(self):
+        return (self.nk + 2) * (self.nj + 3) * (self.ni + 2)
+
+    def interior(self, a3: np.ndarray, kind: str = "h"):
+        """View of the cells a field's update loops cover (k rows 1..nk, j per grid, i 1..ni).
+
+        kind 'h': h/u grid j = 0..nj; 'v': v grid j = 1..nj; 'w': interfaces k = 0..nk.
+        a3 has shape (..., nk+2, nj+3, ni+2); array index j+1 holds row j.
+        """
+        if kind == "h":
+            return a3[..., 1:self.nk + 1, 1:self.nj + 2, 1:self.ni + 1]
+        if kind == "v":
+            return a3[..., 1:self.nk + 1, 2:self.nj + 2, 1:self.ni + 1]
+        if kind == "uv":   # u, v interfaces the time step updates: k = 1..nk-1
+            return a3[..., 1:self.nk, 1:self.nj + 2, 1:self.ni + 1]
+        if kind == "vv":
+            return a3[..., 1:self.nk, 2:self.nj + 2, 1:self.ni + 1]
+        if kind == "w":
+            return a3[..., 0:self.nk + 1, 1:self.nj + 2, 1:self.ni + 1]
+        raise ValueError(kind)
+
+
+class GridArrays:
+    """Owns the 1-D arrays an EpicGrid points at."""
+
+    def __init__(self, ni: int, nj: int, nk: int, k_sponge: int = 0):
+        self.layout = Layout(ni, nj, nk)
+        nj1, ni1, nk1 = 2 * (nj + 1) + 1, 2 * (ni + 1) + 1, 2 * (nk + 1) + 1
+        self.arrays = {
+            "lon": np.zeros(ni1), "lat": np.zeros(nj1), "rln": np.zeros(nj1), "rlt": np.zeros(nj1),
+            "f": np.zeros(nj1), "m": np.zeros(nj1), "n": np.zeros(nj1), "mn": np.zeros(nj1),
+            "g": np.zeros(nj1), "sigmatheta": np.zeros(nk1), "dsgth": np.zeros(nk1),
+            "dsgth_inv": np.zeros(nk1), "h_min": np.zeros(nk + 2), "t_sponge_inv": np.zeros(k_sponge + 1),
+        }
+        self.p_ref = np.zeros(nk1)
+        self.theta_ref = np.zeros(nk1)
+        self.struct = EpicGrid()
+        for k, a in self.arrays.items():
+            setattr(self.struct, k, _ptr(a))
+
+    def __getattr__(self, name):
+        arrays = self.__dict__.get("arrays", {})
+        if name in arrays:
+            return arrays[name]
+        raise AttributeError(name)
+
+    def scalars(self) -> dict:
+        out = {}
+        for name, typ in EpicGrid._fields_:
+            if typ is _dp:
+                continue
+            v = getattr(self.struct, name)
+            out[name] = list(v) if name == "nu" else v
+        return out
+
+
+class Fields:
+    """Owns numpy storage for every EpicFields pointer, in the reference layout."""
+
+    def __init__(self, ni: int, nj: int, nk: int, uv_scheme: int):
+        self.layout = Layout(ni, nj, nk)
+        self.uv_scheme = uv_scheme
+        nvp, ntp = (1, 3) if uv_scheme == EPIC_UV_AB3 else (2, 1)
+        s3 = self.layout.shape3
+        self.arrays = {
+            "u": np.zeros((nvp,) + s3), "v": np.zeros((nvp,) + s3),
+            "dudt": np.zeros((ntp,) + s3), "dvdt": np.zeros((ntp,) + s3),
+        }
+        for n in FIELD_NAMES_3D:
+            self.arrays[n] = np.zeros(s3)
+        self.arrays["gz_surface"] = np.zeros(self.layout.shape2)
+        self.struct = EpicFields()
+        for k, a in self.arrays.items():
+            setattr(self.struct, k, _ptr(a))
+        self.struct.it_zero, self.struct.it_minus1, self.struct.it_minus2 = 0, 1, 2
+
+    def __getattr__(self, name):
+        arrays = self.__dict__.get("arrays", {})
+        if name in arrays:
+            return arrays[name]
+        raise AttributeError(name)
+
+    def copy(self) -> "Fields":
+        out = Fields(self.layout.ni, self.layout.nj, self.layout.nk, self.uv_scheme)
+        for k, a in self.arrays.items():
+            out.arrays[k][...] = a
+        for name in ("it_zero", "it_minus1", "it_minus2", "itime", "model_time"):
+            setattr(out.struct, name, getattr(self.struct, name))
+        return out
+
+    def wind(self, name: str) -> np.ndarray:
+        """Current value plane of u or v (grid.it_uv: plane 0 for AB3, IT_ZERO for leapfrog)."""
+        a = self.arrays[name]
+        return a[0] if self.uv_scheme == EPIC_UV_AB3 else a[self.struct.it_zero]
+
+    def tendency(self, name: str) -> np.ndarray:
+        """Most recent tendency plane of u or v."""
+        a = self.arrays[name]
+        if self.uv_scheme == EPIC_UV_AB3:
+            return a[self.struct.it_minus1]   # after the step's index rotation
+        return a[0]
+
+
+@dataclass
+class HSConfig:
+    """A synthetic Held-Suarez run: grid shape, time step, scheme and dissipation."""
+    ni: int = 64
+    nj: int = 32
+    nk: int = 10
+    dt: int = 300
+    uv_scheme: int = EPIC_UV_AB3
+    nu4: float = 0.5
+    nu6: float = 0.0
+    nu8: float = 0.0
+    nudiv: float = 0.0
+    ptop: float = 10.0
+    pbot: float = 1.0e5
+    p_sigma: float = 900.0e2
+    lat0: float = 45.0
+    seed: int = 0
+    noise_k: float = 0.1
+    extra: dict = field(default_factory=dict)
+
+    def params(self) -> EpicHsParams:
+        p = EpicHsParams()
+        p.ni, p.nj, p.nk, p.dt, p.uv_scheme = self.ni, self.nj, self.nk, self.dt, self.uv_scheme
+        p.ptop, p.pbot, p.p_sigma = self.ptop, self.pbot, self.p_sigma
+        for i in range(9):
+            p.nu_nondim[i] = 0.0
+        p.nu_nondim[4], p.nu_nondim[6], p.nu_nondim[8] = self.nu4, self.nu6, self.nu8
+        p.nudiv_nondim = self.nudiv
+        p.lat0 = self.lat0
+        return p
+
+    @property
+    def cells(self) -> int:
+        return self.ni * self.nj * self.nk

@@ -1,0 +1,393 @@
+// Host-side Held-Suarez grid and initial-state construction (no GPU).
+//
+// Restates, for planet "held_suarez" on the full globe, the grid set-up that the reference's
+// `initial` program performs and that `epic` repeats at start-up:
+//   geometry        set_lonlat / set_fmn / set_gravity   src/shared/epic_funcs_diag.c:1324-1633
+//   dsgth           set_dsgth                            src/shared/epic_funcs_diag.c:1639-1686
+//   vertical grid   p_ref, k_sigma, sigmatheta, h_min    src/shared/epic_initial.c:1758-2006
+//   viscosity       set_max_nu / init_viscosity          src/shared/epic_subgrid.c:82-199
+//   AB3/leapfrog start flags                             src/shared/epic_initial.c:1301-1330
+//   HDRY from P3    get_h                                src/shared/epic_main.c:290-297
+// The temperature sounding t_vs_p.held_suarez is replaced by the analytic Held-Suarez
+// equilibrium profile at 45 degrees (temp_eq, src/shared/epic_sensible_heating.c:394-406).
+// Compiled with -ffp-contract=off so the same bits come out on x86-64 and aarch64 hosts.
+#include <cmath>
+#include <cstdint>
+#include <cstring>
+#include <cfloat>
+#include <string>
+#include <vector>
+#include "epic_gb300.h"
+#include "epic_common.h"
+
+namespace {
+
+constexpr double kDeg = M_PI / 180.0;
+constexpr double kHsKappa = 0.2857;
+constexpr double kHsRgas = 286.86;
+constexpr double kHsCp = 1004.0;
+constexpr double kHsRe = 6371.e+3;
+constexpr double kHsOmega = 7.2921e-5;
+constexpr double kHsGM = 0.39860e+15;
+constexpr double kHsJ2 = 1082.636e-6;
+constexpr double kHsKinvisc = 14.60e-6;
+constexpr double kAlphaBoundary = 0.5;   // ALPHA_BOUNDARY, epic_initial.c:110
+constexpr double kPress0 = 1.e+5;        // grid.press0, epic_initial.c:242
+
+struct Coord {  // the hybrid-coordinate constants get_sigma ... return_sigmatheta read
+  double zeta0, zeta1, alpha, sigma_sigma;
+};
+
+// get_sigma, epic_funcs_diag.c:1751-1756
+inline double get_sigma(double pbot, double p, double ptop) { return log(p / pbot) / log(ptop / pbot); }
+// get_p_sigma, epic_funcs_diag.c:1765-1770
+inline double get_p_sigma(double pbot, double sigma, double ptop) { return pbot * exp(sigma * log(ptop / pbot)); }
+// g_sigma, epic_funcs_diag.c:1300-1314
+inline double g_sigma(const Coord &c, double sigma) {
+  const double coeff = 1. / (1 - exp(-c.alpha * (1. - c.sigma_sigma)));
+  if (sigma <= c.sigma_sigma) return 0.;
+  if (sigma >= 1.) return 1.;
+  return coeff * (1. - exp(-c.alpha * (sigma - c.sigma_sigma)));
+}
+// f_sigma, epic_funcs_diag.c:1271-1289
+inline double f_sigma(const Coord &c, double sigma) {
+  if (sigma < 0.) return c.zeta0;
+  if (sigma <= c.sigma_sigma) return c.zeta0 + sigma * (c.zeta1 - c.zeta0);
+  if (sigma < 1.) return (1. - g_sigma(c, sigma)) * (c.zeta0 + sigma * (c.zeta1 - c.zeta0));
+  return 0.;
+}
+// return_sigmatheta, epic_funcs_diag.c:1238-1260 (p > pbot is an error there; callers never pass it)
+inline double return_sigmatheta(const Coord &c, double theta, double p, double pbot, double ptop) {
+  if (p <= ptop) return theta;
+  const double sigma = get_sigma(pbot, p, ptop);
+  return f_sigma(c, sigma) + g_sigma(c, sigma) * theta;
+}
+// fcmp, epic_funcs_util.c:4275-4330 (binary64 epsilon)
+inline int fcmp(double x1, double x2) {
+  int exponent;
+  frexp(fabs(x1) > fabs(x2) ? x1 : x2, &exponent);
+  const double delta = ldexp(DBL_EPSILON, exponent);
+  const double difference = x1 - x2;
+  if (difference > delta) return 1;
+  if (difference < -delta) return -1;
+  return 0;
+}
+// onto_kk for P2_INDEX at a layer, epic_funcs_diag.c:2601-2618
+inline double layer_pressure(double topval, double botval, double kappa) {
+  if (fcmp(botval, topval) == 0) return .5 * (botval + topval);
+  const double kappap1 = kappa + 1.;
+  return pow((pow(botval, kappap1) - pow(topval, kappap1)) / (kappap1 * (botval - topval)), 1. / kappa);
+}
+// Held-Suarez equilibrium temperature, temp_eq, epic_sensible_heating.c:394-406
+inline double hs_temp_eq(double lat_deg, double p, double kappa) {
+  double cos2 = cos(lat_deg * kDeg);
+  cos2 *= cos2;
+  const double sin2 = 1. - cos2;
+  const double p_p0 = p / (1000. * 100.);
+  double ans = (315. - 60. * sin2 - 10. * log(p_p0) * cos2) * pow(p_p0, kappa);
+  return ans > 200. ? ans : 200.;
+}
+inline double hs_theta_eq(double lat_deg, double p, double kappa) {
+  return hs_temp_eq(lat_deg, p, kappa) * pow(kPress0 / p, kappa);
+}
+
+// SplitMix64, one independent stream value per (seed, counter).
+inline uint64_t splitmix64(uint64_t x) {
+  x += 0x9E3779B97F4A7C15ull;
+  x = (x ^ (x >> 30)) * 0xBF58476D1CE4E5B9ull;
+  x = (x ^ (x >> 27)) * 0x94D049BB133111EBull;
+  return x ^ (x >> 31);
+}
+inline double unit_open(uint64_t x) {  // (0, 1]
+  return ((double)(x >> 11) + 1.0) * (1.0 / 9007199254740992.0);
+}
+// Standard normal for cell `counter` of stream `seed` (Box-Muller on two SplitMix64 draws).
+inline double gauss(uint64_t seed, uint64_t counter) {
+  const uint64_t base = splitmix64(seed * 0xD1B54A32D192ED03ull + 0x632BE59BD9B4E019ull);
+  const double u1 = unit_open(splitmix64(base ^ (2 * counter)));
+  const double u2 = unit_open(splitmix64(base ^ (2 * counter + 1)));
+  return sqrt(-2. * log(u1)) * cos(2. * M_PI * u2);
+}
+
+}  // namespace
+
+extern "C" int epic_hs_grid_build(const epic_hs_params *p, epic_grid *g, double *p_ref, double *theta_ref) {
+  using epic::set_error;
+  if (!p || !g || !p_ref || !theta_ref) return set_error(EPIC_ERR_ARG, "epic_hs_grid_build: NULL argument");
+  const int ni = p->ni, nj = p->nj, nk = p->nk;
+  if (ni < 4 || (ni & (ni - 1)) != 0) return set_error(EPIC_ERR_ARG, "ni=%d must be a power of 2 >= 4", ni);
+  if (nj < 3 || nk < 3) return set_error(EPIC_ERR_ARG, "nj=%d, nk=%d too small", nj, nk);
+  if (p->dt <= 0) return set_error(EPIC_ERR_ARG, "dt=%d", p->dt);
+  if (p->uv_scheme != EPIC_UV_AB3 && p->uv_scheme != EPIC_UV_LEAPFROG) return set_error(EPIC_ERR_ARG, "uv_scheme=%d", p->uv_scheme);
+  double *lon = const_cast<double *>(g->lon), *lat = const_cast<double *>(g->lat);
+  double *rln = const_cast<double *>(g->rln), *rlt = const_cast<double *>(g->rlt);
+  double *fc = const_cast<double *>(g->f), *m = const_cast<double *>(g->m), *n = const_cast<double *>(g->n);
+  double *mn = const_cast<double *>(g->mn), *grav = const_cast<double *>(g->g);
+  double *sgth = const_cast<double *>(g->sigmatheta), *dsgth = const_cast<double *>(g->dsgth);
+  double *dsgth_inv = const_cast<double *>(g->dsgth_inv), *h_min = const_cast<double *>(g->h_min);
+  double *t_sponge_inv = const_cast<double *>(g->t_sponge_inv);
+  if (!lon || !lat || !rln || !rlt || !fc || !m || !n || !mn || !grav || !sgth || !dsgth || !dsgth_inv || !h_min || !t_sponge_inv)
+    return set_error(EPIC_ERR_ARG, "epic_hs_grid_build: grid array pointer is NULL");
+
+  g->ni = ni; g->nj = nj; g->nk = nk; g->dt = p->dt; g->uv_scheme = p->uv_scheme;
+  g->k_sponge = 0;               // held_suarez forces k_sponge = 0, epic_initial.c:1252-1254
+  g->newt_cool_on = 1;           // epic_initial.c:473-475
+  g->newt_cool_adjust = 0; g->prandtl = 0.;     // :488-490
+  g->tau_drag = 1.e+20; g->drag_v = 0; g->drag_zonal_avg = 0;
+  g->topo_scale = 1.;            // :1406-1408
+  g->press0 = kPress0;
+  g->zeta0 = 260.; g->zeta1 = 700.; g->hybrid_alpha = 50.;   // :1593-1601
+  g->globe_latbot = -90.; g->globe_lattop = 90.;
+  g->re = kHsRe; g->rp = kHsRe; g->cp = kHsCp; g->rgas = kHsRgas; g->kappa = kHsKappa; g->kinvisc = kHsKinvisc;
+  g->lat0 = p->lat0 > 0. ? p->lat0 : 45.;
+  g->hs_kf = 1. / (24. * 60. * 60.);
+  g->nudiv_nondim = p->nudiv_nondim;
+
+  // Longitude/latitude spacing, epic_initial.c:1145-1150, 1198.
+  const double lonbot = -180., lontop = 180.;
+  g->dln = (lontop - lonbot) / ni;
+  g->dlt = 180. / ((nj + 1) + sqrt(.5) + sqrt(.5));
+
+  // set_lonlat, epic_funcs_diag.c:1324-1413 (globe with both poles).
+  lon[0] = lonbot - g->dln;
+  for (int ii = 1; ii <= 2 * (ni + 1); ii++) lon[ii] = lon[ii - 1] + g->dln * .5;
+  lat[0] = -90. + g->dlt * sqrt(.5);
+  for (int jj = 1; jj <= 2 * (nj + 1); jj++) lat[jj] = lat[jj - 1] + g->dlt * .5;
+  lat[0] = -90.;
+  lat[2 * (nj + 1)] = 90.;
+  {
+    int jjn = 2 * (nj + 1), jjs = 0;
+    while (lat[jjs] < 0. && lat[jjn] > 0.) {
+      for (; jjs < jjn; jjs++) {
+        if (fabs(lat[jjs] + lat[jjn]) < 1.e-3) {
+          lat[jjn--] = -lat[jjs++];
+          break;
+        }
+      }
+    }
+  }
+
+  // set_fmn, epic_funcs_diag.c:1424-1598 (globe).
+  {
+    const double omega = kHsOmega, re = g->re, rp = g->rp;
+    const double dlnr = g->dln * kDeg, dltr = g->dlt * kDeg;
+    for (int jj = 1; jj < 2 * (nj + 1); jj++) {
+      const double la = kDeg * lat[jj];
+      const double r_ln = re / sqrt(1. + pow(rp / re * tan(la), 2.));
+      const double r_lt = r_ln / (cos(la) * (pow(sin(la), 2.) + pow(re / rp * cos(la), 2.)));
+      rln[jj] = r_ln; rlt[jj] = r_lt;
+      fc[jj] = 2. * omega * sin(la);
+      m[jj] = 1. / (r_ln * dlnr);
+      n[jj] = 1. / (r_lt * dltr);
+      mn[jj] = m[jj] * n[jj];
+    }
+    double la = kDeg * lat[0];
+    rln[0] = 0.; rlt[0] = re * re / rp; fc[0] = 2. * omega * sin(la);
+    n[1] /= 1. + sqrt(.5);
+    mn[1] = n[1] * n[1] / (.5 * dlnr);
+    mn[0] = 2. * mn[1];
+    const int jn = 2 * (nj + 1);
+    la = kDeg * lat[jn];
+    rln[jn] = 0.; rlt[jn] = re * re / rp; fc[jn] = 2. * omega * sin(la);
+    n[jn - 1] /= 1. + sqrt(.5);
+    mn[jn - 1] = n[jn - 1] * n[jn - 1] / (.5 * dlnr);
+    mn[jn] = 2. * mn[jn - 1];
+    // m[0], n[0], m[jn], n[jn] stay 0 as in the calloc'ed reference arrays.
+    m[0] = n[0] = m[jn] = n[jn] = 0.;
+    // dy0 at LAT0 (the reference hard-codes 45 degrees here as well).
+    const double lat0 = 45. * kDeg;
+    const double r_ln = re / sqrt(1. + pow(rp / re * tan(lat0), 2.));
+    const double r_lt = r_ln / (cos(lat0) * (pow(sin(lat0), 2.) + pow(re / rp * cos(lat0), 2.)));
+    g->dy0 = r_lt * g->dlt * kDeg;
+  }
+
+  // set_gravity, epic_funcs_diag.c:1607-1633.
+  {
+    const double a = g->re, b = g->rp;
+    const double spin_factor = (kHsOmega * a) * (kHsOmega * a) * (a / kHsGM);
+    const double ge = (1. + 1.5 * kHsJ2 - spin_factor) * kHsGM / (a * a);
+    const double gp = (1. - 3. * (a / b) * (a / b) * kHsJ2) * kHsGM / (b * b);
+    for (int jj = 0; jj <= 2 * (nj + 1); jj++) {
+      double s2 = sin(lat[jj] * kDeg); s2 *= s2;
+      double c2 = cos(lat[jj] * kDeg); c2 *= c2;
+      grav[jj] = (a * ge * c2 + b * gp * s2) / sqrt(a * a * c2 + b * b * s2);
+    }
+  }
+
+  // grid.jtp: first h-row within dlt/2 of the equator, epic_initial.c:1434-1440.
+  g->jtp = 0;
+  for (int J = 0; J <= nj; J++) {
+    if (fabs(lat[2 * J + 1] - 0.) <= .5 * g->dlt) { g->jtp = J; break; }
+  }
+
+  // Vertical grid, epic_initial.c:1758-2006 (terrestrial, SPACING_LOGP_W_BOUNDARIES).
+  const int KHI = nk;
+  const double ptop = p->ptop > 0. ? p->ptop : 10.;
+  const double pbot = p->pbot > 0. ? p->pbot : 1.e+5;
+  const double p_sigma = p->p_sigma > 0. ? p->p_sigma : 900. * 100.;
+  const double lat_ref = 45.;
+  for (int kk = 0; kk <= 2 * (nk + 1); kk++) { p_ref[kk] = 0.; theta_ref[kk] = 0.; sgth[kk] = 0.; }
+  Coord c{g->zeta0, g->zeta1, g->hybrid_alpha, 0.};
+  p_ref[1] = ptop;
+  p_ref[2 * KHI + 1] = pbot;
+  theta_ref[1] = hs_theta_eq(lat_ref, ptop, kHsKappa);
+  theta_ref[2 * KHI + 1] = hs_theta_eq(lat_ref, pbot, kHsKappa);
+  const double sgth_top = theta_ref[1];
+  const double sgth_bot = return_sigmatheta(c, theta_ref[2 * KHI + 1], pbot, pbot, ptop);
+  sgth[0] = sgth[1] = sgth_top;
+  sgth[2 * KHI + 1] = sgth_bot;
+  {
+    const int nk_sponge = g->k_sponge;
+    const int nk_pbl = nk / 5;
+    const int nk_reg = nk - nk_pbl - nk_sponge;
+    const double dlnp = log(pbot / ptop) /
+                        ((1. - pow(1. + kAlphaBoundary, -nk_sponge)) / kAlphaBoundary + (double)nk_reg +
+                         (1. - pow(1. + kAlphaBoundary, -nk_pbl)) / kAlphaBoundary);
+    p_ref[2 * 1 + 1] = p_ref[1] * exp(dlnp * pow(1. + kAlphaBoundary, -nk_sponge));
+    for (int K = 2; K <= g->k_sponge; K++)
+      p_ref[2 * K + 1] = p_ref[2 * (K - 1) + 1] * pow(p_ref[2 * (K - 1) + 1] / p_ref[2 * (K - 2) + 1], 1. + kAlphaBoundary);
+    for (int K = g->k_sponge + 1; K <= nk - nk_pbl; K++) p_ref[2 * K + 1] = p_ref[2 * (K - 1) + 1] * exp(dlnp);
+    for (int K = nk - nk_pbl + 1; K < nk; K++)
+      p_ref[2 * K + 1] = p_ref[2 * (K - 1) + 1] * pow(p_ref[2 * (K - 1) + 1] / p_ref[2 * (K - 2) + 1], 1. / (1. + kAlphaBoundary));
+    for (int K = 1; K <= KHI; K++) p_ref[2 * K] = layer_pressure(p_ref[2 * K - 1], p_ref[2 * K + 1], kHsKappa);
+  }
+  // k_sigma: layer whose top is nearest p_sigma, epic_initial.c:1905-1923.
+  {
+    int k_sigma = -1;
+    double best = DBL_MAX;
+    for (int K = 1; K <= KHI; K++) {
+      const double d = fabs(p_ref[2 * (K - 1) + 1] - p_sigma);
+      if (d < best) { k_sigma = K; best = d; }
+    }
+    if (k_sigma < 2) return set_error(EPIC_ERR_ARG, "k_sigma=%d < 2 (nk too small for p_sigma)", k_sigma);
+    g->k_sigma = k_sigma;
+  }
+  c.sigma_sigma = get_sigma(p_ref[2 * KHI + 1], p_ref[2 * (g->k_sigma - 1) + 1], p_ref[1]);
+  for (int kk = 2; kk < 2 * KHI + 1; kk++) theta_ref[kk] = hs_theta_eq(lat_ref, p_ref[kk], kHsKappa);
+  for (int kk = 2; kk < 2 * KHI + 1; kk++) sgth[kk] = return_sigmatheta(c, theta_ref[kk], p_ref[kk], pbot, ptop);
+  g->sigma_sigma = (sgth[2 * g->k_sigma - 1] - g->zeta0) / (g->zeta1 - g->zeta0);
+
+  // set_dsgth, epic_funcs_diag.c:1639-1686.
+  for (int kk = 0; kk <= 2 * (nk + 1); kk++) { dsgth[kk] = 0.; dsgth_inv[kk] = 0.; }
+  for (int K = 0; K <= KHI; K++) {
+    const int kk = 2 * K;
+    if (K == 0) dsgth[kk + 1] = sgth[kk + 1] - sgth[kk + 2];
+    else if (K == KHI) dsgth[kk + 1] = sgth[kk] - sgth[kk + 1];
+    else dsgth[kk + 1] = sgth[kk] - sgth[kk + 2];
+    if (!(dsgth[kk + 1] > 0.)) return set_error(EPIC_ERR_MODEL, "dsgth[%d]=%g <= 0", kk + 1, dsgth[kk + 1]);
+    dsgth_inv[kk + 1] = 1. / dsgth[kk + 1];
+  }
+  for (int K = 1; K <= KHI; K++) {
+    const int kk = 2 * K;
+    dsgth[kk] = sgth[kk - 1] - sgth[kk + 1];
+    if (!(dsgth[kk] > 0.)) return set_error(EPIC_ERR_MODEL, "dsgth[%d]=%g <= 0", kk, dsgth[kk]);
+    dsgth_inv[kk] = 1. / dsgth[kk];
+  }
+
+  // h_min, epic_initial.c:2001-2006.
+  {
+    const double tmp = 0.02 / grav[2 * g->jtp + 1];
+    for (int K = 1; K <= KHI; K++)
+      h_min[K] = tmp * (p_ref[2 * K + 1] - p_ref[2 * (K - 1) + 1]) * dsgth_inv[2 * K];
+    h_min[0] = h_min[1];
+    h_min[KHI + 1] = 0.;
+  }
+  t_sponge_inv[0] = 0.;  // k_sponge = 0: set_sponge() leaves the (harness-allocated) entry at 0
+
+  // init_viscosity, epic_subgrid.c:169-199, with set_max_nu, :82-158.
+  {
+    double max_nu[9];
+    epic::set_max_nu(g->dt, g->dy0, g->uv_scheme, max_nu);
+    for (int i = 0; i < 9; i++) g->nu[i] = 0.;
+    g->nu[2] = g->kinvisc < max_nu[2] ? g->kinvisc : max_nu[2];
+    for (int ii = 4; ii <= 8; ii += 2) g->nu[ii] = p->nu_nondim[ii] * max_nu[ii];
+  }
+  return EPIC_OK;
+}
+
+extern "C" int epic_hs_initial_state(const epic_grid *g, const epic_hs_params *p, uint64_t seed, double noise_k,
+                                     epic_fields *f) {
+  using epic::set_error;
+  if (!g || !p || !f) return set_error(EPIC_ERR_ARG, "epic_hs_initial_state: NULL argument");
+  if (!f->u || !f->v || !f->dudt || !f->dvdt || !f->hdry || !f->theta || !f->p3 || !f->gz_surface || !f->u_spinup)
+    return set_error(EPIC_ERR_ARG, "epic_hs_initial_state: required field pointer is NULL");
+  const epic::Layout L(g->ni, g->nj, g->nk);
+  const int ni = g->ni, nj = g->nj, nk = g->nk, KHI = nk;
+  Coord c{g->zeta0, g->zeta1, g->hybrid_alpha, g->sigma_sigma};
+  const double *sgth = g->sigmatheta;
+  const double p_top = p->ptop > 0. ? p->ptop : 10.;
+  const double p_bot = p->pbot > 0. ? p->pbot : 1.e+5;
+
+  f->it_zero = 0; f->it_minus1 = 1; f->it_minus2 = 2;
+  f->itime = 0; f->model_time = 0;
+
+  // Horizontally uniform column at rest, as the reference's own Held-Suarez runs start from a
+  // single sounding (init_with_u with u_scale = 0, src/shared/epic_funcs_init.c:1514-1662):
+  // P3 on the sigmatheta interfaces of the 45-degree equilibrium profile, found by bisection
+  // of return_sigmatheta(theta_eq(p), p) = sigmatheta[2K+1] above the pure-sigma region and
+  // from get_p_sigma() inside it; THETA = theta_eq(P3).  Seeded N(0, noise_k^2) noise is then
+  // added to THETA where it is prognostic (K >= k_sigma-1).
+  const int ksig = g->k_sigma;
+  const double la = 45.;
+  std::vector<double> pcol(KHI + 1), thcol(KHI + 1);
+  pcol[0] = p_top;
+  pcol[KHI] = p_bot;
+  for (int K = ksig - 1; K < KHI; K++) {
+    const double sigma = (sgth[2 * K + 1] - g->zeta0) / (g->zeta1 - g->zeta0);
+    pcol[K] = get_p_sigma(p_bot, sigma, p_top);
+  }
+  for (int K = 1; K < ksig - 1; K++) {
+    const double target = sgth[2 * K + 1];
+    double lo = log(p_top), hi = log(pcol[ksig - 1]);
+    for (int it = 0; it < 200; it++) {
+      const double mid = .5 * (lo + hi);
+      const double pm = exp(mid);
+      const double v = return_sigmatheta(c, hs_theta_eq(la, pm, g->kappa), pm, p_bot, p_top) - target;
+      if (v > 0.) lo = mid; else hi = mid;   // sigmatheta decreases downward
+      if (hi - lo < 1.e-15) break;
+    }
+    pcol[K] = exp(.5 * (lo + hi));
+  }
+  for (int K = 0; K <= KHI; K++) thcol[K] = hs_theta_eq(la, pcol[K], g->kappa);
+  for (int J = 0; J <= nj; J++) {
+    for (int I = 1; I <= ni; I++) {
+      for (int K = 0; K <= KHI; K++) {
+        f->p3[L.at(K, J, I)] = pcol[K];
+        double th = thcol[K];
+        if (K >= ksig - 1 && noise_k > 0.) {
+          const uint64_t counter = ((uint64_t)K * (uint64_t)(nj + 1) + (uint64_t)J) * (uint64_t)ni + (uint64_t)(I - 1);
+          th += noise_k * gauss(seed, counter);
+        }
+        f->theta[L.at(K, J, I)] = th;
+      }
+    }
+  }
+  // HDRY = get_h(P3) in the layers, epic_main.c:290-297 with get_h, epic_funcs_diag.c:1780-1853.
+  for (int K = 1; K <= KHI; K++)
+    for (int J = 0; J <= nj; J++)
+      for (int I = 1; I <= ni; I++)
+        f->hdry[L.at(K, J, I)] = (f->p3[L.at(K, J, I)] - f->p3[L.at(K - 1, J, I)]) / (g->g[2 * J + 1] * g->dsgth[2 * K]);
+  // Zonal periodicity of everything that was filled (bc_lateral, src/single/s_epic_functions.c:39-87).
+  double *fields3[] = {f->p3, f->theta, f->hdry};
+  for (double *a : fields3) L.periodic3(a);
+  // Rest state; time-scheme start flags.
+  const int64_t n3 = L.n3;
+  if (g->uv_scheme == EPIC_UV_AB3) {
+    for (int K = 1; K <= KHI; K++)
+      for (int J = 0; J <= nj; J++)
+        for (int I = 1; I <= ni; I++) {
+          f->dudt[2 * n3 + L.at(K, J, I)] = DBL_MAX;   // IT_MINUS2
+          f->dudt[1 * n3 + L.at(K, J, I)] = DBL_MAX;   // IT_MINUS1
+          f->dvdt[2 * n3 + L.at(K, J, I)] = DBL_MAX;
+          f->dvdt[1 * n3 + L.at(K, J, I)] = DBL_MAX;
+        }
+  } else {
+    // Leapfrog: the reference flags the whole IT_MINUS1 plane (epic_initial.c:1316-1325), which
+    // leaves DBL_MAX in V's polar row after the first step.  Only the two cells that
+    // leapfrog_step and timeplane_bookkeeping test are flagged here
+    // (U at (KLO,JLO,ILO), V at (KLO,JFIRST,ILO)); the rest of IT_MINUS1 copies IT_ZERO.
+    f->u[n3 + L.at(1, 0, 1)] = DBL_MAX;
+    f->v[n3 + L.at(1, 1, 1)] = DBL_MAX;
+  }
+  return EPIC_OK;
+}

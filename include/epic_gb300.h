@@ -1,0 +1,194 @@
+/*
+ * epic_gb300.h -- C ABI of the GB300 dynamical core for EPIC's single-processor timestep().
+ *
+ * The reference entry point this library replaces is
+ *
+ *     void timestep(planetspec *planet, int action, EPIC_FLOAT **Buff2D);
+ *         include/epic.h:654-656, defined at src/shared/epic_timestep.c:62
+ *
+ * which reads the globals `grid` (gridspec, include/epic_datatypes.h:279-394), `planet`
+ * (planetspec, :238-274) and `var` (variablespec, :550-627).  This ABI carries the same
+ * information through plain structs of scalars and host pointers:
+ *
+ *   epic_grid    the gridspec/planetspec scalars and 1-D grid arrays timestep() reads,
+ *   epic_fields  host views of the variablespec 3-D arrays in the reference memory layout
+ *                X(k,j,i) = base[i + (j+1)*(ni+2) + k*(ni+2)*(nj+3)], k = 0..nk+1,
+ *                j = -1..nj+1, i = 0..ni+1 (include/epic.h:407-449; wind time planes
+ *                are consecutive blocks of (ni+2)*(nj+3)*(nk+2) doubles, :407-411).
+ *
+ * All arithmetic types are IEEE binary64 unless a function says otherwise.  Every function
+ * returns 0 on success or a negative EPIC_ERR_* code; epic_last_error() gives the text.
+ * Nothing here calls exit(): the reference's epic_error() (src/shared/epic_funcs_io.c:4872)
+ * becomes an error code plus message.
+ */
+#ifndef EPIC_GB300_H
+#define EPIC_GB300_H
+
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* timestep() actions, include/epic.h:294-295 */
+#define EPIC_STEP_PROGS_AND_SYNC_DIAGS 0
+#define EPIC_SYNC_DIAGS_ONLY           1
+
+/* grid.uv_timestep_scheme, src/shared/epic_timestep.c:242,262 */
+#define EPIC_UV_AB3      0   /* "3rd-order Adams-Bashforth"   */
+#define EPIC_UV_LEAPFROG 1   /* "Leapfrog (Asselin filtered)" */
+
+/* Precision forms accepted by epic_model_create(). */
+#define EPIC_PREC_FP64  0    /* every kernel in binary64 (the drop-in form)                    */
+#define EPIC_PREC_MIXED 1    /* stencils/advection/hyperviscosity in binary32, vertical sums,
+                                updates and global sums in binary64                           */
+
+/* Error codes. */
+#define EPIC_OK               0
+#define EPIC_ERR_ARG         -1   /* bad argument or unsupported configuration              */
+#define EPIC_ERR_CUDA        -2   /* CUDA runtime error                                     */
+#define EPIC_ERR_NOMEM       -3   /* device or host allocation failed                       */
+#define EPIC_ERR_MODEL       -4   /* a model check failed (the reference would epic_error)  */
+#define EPIC_ERR_STATE       -5   /* call order violated (e.g. step before upload)          */
+
+/*
+ * Scalars and 1-D arrays of `grid` and `planet` that the step reads.  Array lengths follow
+ * make_arrays() (src/shared/epic_funcs_diag.c:577-1074): half-level index jj = 0..2*(nj+1),
+ * ii = 0..2*(ni+1), kk = 0..2*(nk+1).  Only the full globe (latbot = -90, lattop = 90) with
+ * Held-Suarez physics (planet "held_suarez", x_h2 = 0, ideal gas, nq = 0, turbulence "off",
+ * Hsu advection) is supported; anything else returns EPIC_ERR_ARG.
+ */
+typedef struct epic_grid {
+  int32_t ni, nj, nk;          /* grid.ni, grid.nj, grid.nk                                     */
+  int32_t dt;                  /* grid.dt [s]                                                   */
+  int32_t uv_scheme;           /* EPIC_UV_AB3 or EPIC_UV_LEAPFROG                               */
+  int32_t k_sigma;             /* grid.k_sigma                                                  */
+  int32_t k_sponge;            /* grid.k_sponge                                                 */
+  int32_t newt_cool_on;        /* grid.newt_cool_on                                             */
+  int32_t newt_cool_adjust;    /* grid.newt_cool_adjust                                         */
+  int32_t drag_v;              /* grid.drag_v                                                   */
+  int32_t drag_zonal_avg;      /* grid.drag_zonal_avg                                           */
+  int32_t jtp;                 /* grid.jtp                                                      */
+  double  dln, dlt, dy0;       /* grid.dln, grid.dlt [deg], grid.dy0 [m]                        */
+  double  globe_latbot, globe_lattop;
+  double  press0;              /* grid.press0 [Pa]                                              */
+  double  topo_scale, prandtl, tau_drag, nudiv_nondim;
+  double  zeta0, zeta1, hybrid_alpha, sigma_sigma;
+  double  nu[9];               /* grid.nu[0..MAX_NU_ORDER]                                      */
+  double  re, rp;              /* planet->re, planet->rp [m]                                    */
+  double  cp, rgas, kappa;     /* planet->cp, planet->rgas, planet->kappa                       */
+  double  kinvisc;             /* planet->kinvisc                                               */
+  double  lat0;                /* filter/taper latitude [deg]; the reference's LAT0 is 45      */
+  double  hs_kf;               /* Held-Suarez PBL drag rate k_f [1/s]; the reference hard-codes
+                                  HELD_SUAREZ_PBL_NU0 = 1/86400 (epic_timestep.c:1292)         */
+  const double *lon;           /* [2*(ni+1)+1]                                                  */
+  const double *lat, *rln, *rlt, *f, *m, *n, *mn, *g;   /* [2*(nj+1)+1]                         */
+  const double *sigmatheta, *dsgth, *dsgth_inv;         /* [2*(nk+1)+1]                         */
+  const double *h_min;         /* [nk+2]                                                        */
+  const double *t_sponge_inv;  /* [k_sponge+1]                                                  */
+} epic_grid;
+
+/*
+ * Host views of `var`.  AB3: u, v hold 1 value plane and dudt, dvdt 3 tendency planes;
+ * leapfrog: u, v hold 2 value planes and dudt, dvdt 1 plane (make_arrays, epic_funcs_diag.c:686-711).
+ * With nq = 0 the reference aliases P3 = PDRY3, H2 = HDRY, H3 = HDRY3 (:891-927); here p3
+ * and h3 are the only copies.  Any pointer may be NULL on download to skip that field.
+ */
+typedef struct epic_fields {
+  double *u, *v, *dudt, *dvdt;
+  double *hdry, *theta;
+  double *p3, *h3, *p2, *theta2, *t2, *t3, *rho2, *rho3, *exner3;
+  double *gz3, *mont3, *heat3, *pv3, *ri2, *div_uv3, *w3, *dzdt3, *u_spinup;
+  double *gz_surface;          /* 2-D: [(nj+3)*(ni+2)]                                          */
+  int32_t it_zero, it_minus1, it_minus2;  /* IT_ZERO, IT_MINUS1, IT_MINUS2 (include/epic.h:303) */
+  int32_t pad0;
+  int64_t itime;               /* grid.itime                                                    */
+  int64_t model_time;          /* var.model_time [s]                                            */
+} epic_fields;
+
+typedef struct epic_model epic_model;
+
+/*
+ * Allocate device state for one grid on the current CUDA device and upload the grid
+ * arrays (the first-call work of timestep(), epic_timestep.c:88-101, plus the static
+ * initialisation blocks of zonal_filter, d2dy2 and the hyperviscosity routines).
+ */
+int  epic_model_create(const epic_grid *grid, int32_t precision, epic_model **out);
+void epic_model_destroy(epic_model *m);
+
+/* Copy host `var` into the device state (no kernel runs). */
+int  epic_model_upload(epic_model *m, const epic_fields *f);
+
+/*
+ * timestep(planet, action, Buff2D), src/shared/epic_timestep.c:62-390, on the device state.
+ * Asynchronous on the model's stream; errors found by kernels surface on the next
+ * epic_model_sync() or download.
+ */
+int  epic_model_timestep(epic_model *m, int32_t action);
+
+/*
+ * nsteps calls of timestep(STEP_PROGS_AND_SYNC_DIAGS) with grid.itime advancing by one
+ * after each, as the driver loop does (src/shared/epic_main.c:336-427).  Replays a captured
+ * CUDA graph of one step when possible.
+ */
+int  epic_model_run(epic_model *m, int32_t nsteps);
+
+/* Wait for queued work and report any device-side model error. */
+int  epic_model_sync(epic_model *m);
+
+/* Copy the device state back into host `var` (called before var_write()). */
+int  epic_model_download(epic_model *m, epic_fields *f);
+
+/*
+ * End-to-end form of the drop-in: upload f, run nsteps (after a SYNC_DIAGS_ONLY call when
+ * prime != 0), download into f.  This is what a reference-side timestep() wrapper does.
+ */
+int  epic_model_step_host(epic_model *m, epic_fields *f, int32_t prime, int32_t nsteps);
+
+/* Device stream the model runs on (a cudaStream_t), for callers that interleave work. */
+void *epic_model_stream(epic_model *m);
+
+/* Bytes of device memory the model holds. */
+int64_t epic_model_device_bytes(const epic_model *m);
+
+/* Text of the last error on this thread. */
+const char *epic_last_error(void);
+
+/*
+ * Host-side synthetic Held-Suarez set-up (no GPU needed).  These restate the grid
+ * construction of the reference's `initial` program for planet "held_suarez"
+ * (src/shared/epic_initial.c:1140-2006) and the geometry routines set_lonlat, set_fmn,
+ * set_gravity, set_dsgth (src/shared/epic_funcs_diag.c:1324-1686), with the temperature
+ * sounding replaced by the analytic Held-Suarez equilibrium profile at 45 degrees.
+ *
+ * epic_hs_grid_build fills *grid; every array pointer in *grid must already point at
+ * caller-owned storage of the lengths documented in epic_grid (lon, lat, ... h_min,
+ * t_sponge_inv).  p_ref and theta_ref (length 2*(nk+1)+1) receive grid.p_ref/theta_ref.
+ */
+typedef struct epic_hs_params {
+  int32_t ni, nj, nk, dt;
+  int32_t uv_scheme;
+  int32_t pad0;
+  double  ptop, pbot, p_sigma; /* [Pa]; reference HS defaults 10, 1e5, 9e4 */
+  double  nu_nondim[9];        /* grid.nu_nondim; HS runs use nu[4] = 0.5, the rest 0 */
+  double  nudiv_nondim;
+  double  lat0;                /* 45 reproduces the reference's LAT0 */
+} epic_hs_params;
+
+int epic_hs_grid_build(const epic_hs_params *p, epic_grid *grid, double *p_ref, double *theta_ref);
+
+/*
+ * Seeded initial state: rest (U = V = 0), P3 on the sigmatheta interfaces from the
+ * Held-Suarez equilibrium temperature of each latitude row, theta noise N(0, noise_k^2)
+ * in the pure-sigma region (k >= k_sigma-1), HDRY = get_h(P3), GZ_SURFACE = 0,
+ * U_SPINUP = 0, and the first-step flags of the chosen time scheme
+ * (src/shared/epic_initial.c:1301-1330).  Fields f must point at zeroed storage.
+ */
+int epic_hs_initial_state(const epic_grid *grid, const epic_hs_params *p, uint64_t seed, double noise_k,
+                          epic_fields *f);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* EPIC_GB300_H */
