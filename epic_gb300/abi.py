@@ -35,7 +35,7 @@ class EpicGrid(C.Structure):
         ("sigma_sigma", C.c_double),
         ("nu", C.c_double * 9),
         ("re", C.c_double), ("rp", C.c_double), ("cp", C.c_double), ("rgas", C.c_double),
-        ("kappa", C.c_double), ("kinvisc", C.c_double), ("lat0", C.c_double), ("hs_kf", C.c_double),
+        ("kappa", C.c_double), ("cpr", C.c_double), ("kinvisc", C.c_double), ("lat0", C.c_double), ("hs_kf", C.c_double),
         ("lon", _dp), ("lat", _dp), ("rln", _dp), ("rlt", _dp), ("f", _dp), ("m", _dp), ("n", _dp),
         ("mn", _dp), ("g", _dp), ("sigmatheta", _dp), ("dsgth", _dp), ("dsgth_inv", _dp),
         ("h_min", _dp), ("t_sponge_inv", _dp),

@@ -138,7 +138,7 @@ extern "C" int epic_hs_grid_build(const epic_hs_params *p, epic_grid *g, double 
   g->press0 = kPress0;
   g->zeta0 = 260.; g->zeta1 = 700.; g->hybrid_alpha = 50.;   // :1593-1601
   g->globe_latbot = -90.; g->globe_lattop = 90.;
-  g->re = kHsRe; g->rp = kHsRe; g->cp = kHsCp; g->rgas = kHsRgas; g->kappa = kHsKappa; g->kinvisc = kHsKinvisc;
+  g->re = kHsRe; g->rp = kHsRe; g->cp = kHsCp; g->rgas = kHsRgas; g->kappa = kHsKappa; g->cpr = 3.5; g->kinvisc = kHsKinvisc;
   g->lat0 = p->lat0 > 0. ? p->lat0 : 45.;
   g->hs_kf = 1. / (24. * 60. * 60.);
   g->nudiv_nondim = p->nudiv_nondim;
@@ -194,8 +194,8 @@ extern "C" int epic_hs_grid_build(const epic_hs_params *p, epic_grid *g, double 
     mn[jn] = 2. * mn[jn - 1];
     // m[0], n[0], m[jn], n[jn] stay 0 as in the calloc'ed reference arrays.
     m[0] = n[0] = m[jn] = n[jn] = 0.;
-    // dy0 at LAT0 (the reference hard-codes 45 degrees here as well).
-    const double lat0 = 45. * kDeg;
+    // dy0 at the filter latitude (LAT0 = 45 degrees in the reference).
+    const double lat0 = g->lat0 * kDeg;
     const double r_ln = re / sqrt(1. + pow(rp / re * tan(lat0), 2.));
     const double r_lt = r_ln / (cos(lat0) * (pow(sin(lat0), 2.) + pow(re / rp * cos(lat0), 2.)));
     g->dy0 = r_lt * g->dlt * kDeg;

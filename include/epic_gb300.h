@@ -77,6 +77,7 @@ typedef struct epic_grid {
   double  nu[9];               /* grid.nu[0..MAX_NU_ORDER]                                      */
   double  re, rp;              /* planet->re, planet->rp [m]                                    */
   double  cp, rgas, kappa;     /* planet->cp, planet->rgas, planet->kappa                       */
+  double  cpr;                 /* planet->cpr, low-temperature cp/rgas (thermo_setup)           */
   double  kinvisc;             /* planet->kinvisc                                               */
   double  lat0;                /* filter/taper latitude [deg]; the reference's LAT0 is 45      */
   double  hs_kf;               /* Held-Suarez PBL drag rate k_f [1/s]; the reference hard-codes

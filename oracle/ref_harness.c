@@ -45,7 +45,7 @@ int ref_init(const epic_grid *g, const epic_fields *f) {
   planet = (planetspec *)malloc(sizeof(planetspec));
   *planet = held_suarez;
   if (planet->re != g->re || planet->rp != g->rp || planet->cp != g->cp || planet->rgas != g->rgas ||
-      planet->kappa != g->kappa || planet->kinvisc != g->kinvisc)
+      planet->kappa != g->kappa || planet->cpr != g->cpr || planet->kinvisc != g->kinvisc)
     return -2;
 
   /* What var_read(SIZE_DATA) and (POST_SIZE_DATA) supply for a held_suarez epic.nc. */
