@@ -1,0 +1,142 @@
+"""GB300-native drop-in for the EPIC single-processor timestep().
+
+The compute path is the CUDA library epic_gb300/_lib/libepic_gb300.so (C ABI in
+include/epic_gb300.h).  This package only loads it and mirrors the reference's calling
+interface in Python:
+
+    timestep(planet, action, Buff2D)   src/shared/epic_timestep.c:62   ->  Model.timestep(action)
+    the epic driver's step loop        src/shared/epic_main.c:336-427  ->  Model.run(nsteps)
+    var_write's need for host data     src/shared/epic_funcs_io.c:1361 ->  Model.download()
+
+There is no CPU fallback: if the library is missing or no GPU is present, Model() raises.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+
+import numpy as np
+
+from .abi import (EPIC_PREC_FP64, EPIC_PREC_MIXED, EPIC_STEP_PROGS_AND_SYNC_DIAGS, EPIC_SYNC_DIAGS_ONLY,
+                  EPIC_UV_AB3, EPIC_UV_LEAPFROG, EpicFields, EpicGrid, EpicHsParams, Fields, GridArrays,
+                  HSConfig, Layout)
+
+_HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(_HERE, "_lib", "libepic_gb300.so")
+_lib = None
+
+
+class EpicError(RuntimeError):
+    """A C-ABI call returned an error code (the reference would have called epic_error())."""
+
+
+def load_library(path: str | None = None) -> C.CDLL:
+    """Load (once) and return the CUDA library; raises if it has not been built."""
+    global _lib
+    if _lib is not None:
+        return _lib
+    p = path or LIB_PATH
+    if not os.path.exists(p):
+        raise EpicError(f"{p} is missing: build it with `python -c 'import __graft_entry__ as g; g.build()'`")
+    lib = C.CDLL(p)
+    lib.epic_last_error.restype = C.c_char_p
+    lib.epic_model_create.argtypes = [C.POINTER(EpicGrid), C.c_int32, C.POINTER(C.c_void_p)]
+    lib.epic_model_destroy.argtypes = [C.c_void_p]
+    lib.epic_model_destroy.restype = None
+    for name in ("epic_model_upload", "epic_model_download"):
+        getattr(lib, name).argtypes = [C.c_void_p, C.POINTER(EpicFields)]
+    lib.epic_model_timestep.argtypes = [C.c_void_p, C.c_int32]
+    lib.epic_model_run.argtypes = [C.c_void_p, C.c_int32]
+    lib.epic_model_run_stage.argtypes = [C.c_void_p, C.c_int32]
+    lib.epic_model_sync.argtypes = [C.c_void_p]
+    lib.epic_model_step_host.argtypes = [C.c_void_p, C.POINTER(EpicFields), C.c_int32, C.c_int32]
+    lib.epic_model_stream.argtypes = [C.c_void_p]
+    lib.epic_model_stream.restype = C.c_void_p
+    lib.epic_model_device_bytes.argtypes = [C.c_void_p]
+    lib.epic_model_device_bytes.restype = C.c_int64
+    lib.epic_hs_grid_build.argtypes = [C.POINTER(EpicHsParams), C.POINTER(EpicGrid), C.POINTER(C.c_double),
+                                       C.POINTER(C.c_double)]
+    lib.epic_hs_initial_state.argtypes = [C.POINTER(EpicGrid), C.POINTER(EpicHsParams), C.c_uint64, C.c_double,
+                                          C.POINTER(EpicFields)]
+    _lib = lib
+    return lib
+
+
+def _check(rc: int, what: str) -> None:
+    if rc != 0:
+        msg = load_library().epic_last_error().decode(errors="replace")
+        raise EpicError(f"{what} failed ({rc}): {msg}")
+
+
+def hs_setup(cfg: HSConfig) -> tuple[GridArrays, Fields]:
+    """Synthetic Held-Suarez grid and initial state (host only; no GPU needed)."""
+    lib = load_library()
+    ga = GridArrays(cfg.ni, cfg.nj, cfg.nk)
+    p = cfg.params()
+    dp = C.POINTER(C.c_double)
+    _check(lib.epic_hs_grid_build(C.byref(p), C.byref(ga.struct), ga.p_ref.ctypes.data_as(dp),
+                                  ga.theta_ref.ctypes.data_as(dp)), "epic_hs_grid_build")
+    f = Fields(cfg.ni, cfg.nj, cfg.nk, cfg.uv_scheme)
+    _check(lib.epic_hs_initial_state(C.byref(ga.struct), C.byref(p), C.c_uint64(cfg.seed), C.c_double(cfg.noise_k),
+                                     C.byref(f.struct)), "epic_hs_initial_state")
+    return ga, f
+
+
+class Model:
+    """One device-resident EPIC grid on the current GPU."""
+
+    def __init__(self, grid: GridArrays, precision: int = EPIC_PREC_FP64):
+        self.lib = load_library()
+        self.grid = grid
+        self.layout = grid.layout
+        self.uv_scheme = grid.struct.uv_scheme
+        self._h = C.c_void_p()
+        _check(self.lib.epic_model_create(C.byref(grid.struct), precision, C.byref(self._h)), "epic_model_create")
+
+    def close(self) -> None:
+        if self._h:
+            self.lib.epic_model_destroy(self._h)
+            self._h = C.c_void_p()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def upload(self, f: Fields) -> None:
+        _check(self.lib.epic_model_upload(self._h, C.byref(f.struct)), "epic_model_upload")
+
+    def download(self, f: Fields | None = None) -> Fields:
+        if f is None:
+            f = Fields(self.layout.ni, self.layout.nj, self.layout.nk, self.uv_scheme)
+        _check(self.lib.epic_model_download(self._h, C.byref(f.struct)), "epic_model_download")
+        return f
+
+    def timestep(self, action: int = EPIC_STEP_PROGS_AND_SYNC_DIAGS) -> None:
+        _check(self.lib.epic_model_timestep(self._h, action), "epic_model_timestep")
+
+    def run(self, nsteps: int) -> None:
+        _check(self.lib.epic_model_run(self._h, nsteps), "epic_model_run")
+
+    def run_stage(self, stage: int) -> None:
+        _check(self.lib.epic_model_run_stage(self._h, stage), "epic_model_run_stage")
+
+    def sync(self) -> None:
+        _check(self.lib.epic_model_sync(self._h), "epic_model_sync")
+
+    def step_host(self, f: Fields, nsteps: int, prime: bool = False) -> None:
+        _check(self.lib.epic_model_step_host(self._h, C.byref(f.struct), int(prime), nsteps), "epic_model_step_host")
+
+    @property
+    def stream(self) -> int:
+        return self.lib.epic_model_stream(self._h) or 0
+
+    @property
+    def device_bytes(self) -> int:
+        return int(self.lib.epic_model_device_bytes(self._h))
+
+
+__all__ = ["Model", "hs_setup", "load_library", "EpicError", "HSConfig", "Fields", "GridArrays", "Layout",
+           "EPIC_PREC_FP64", "EPIC_PREC_MIXED", "EPIC_STEP_PROGS_AND_SYNC_DIAGS", "EPIC_SYNC_DIAGS_ONLY",
+           "EPIC_UV_AB3", "EPIC_UV_LEAPFROG", "LIB_PATH", "np"]

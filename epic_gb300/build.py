@@ -1,0 +1,75 @@
+"""Build the in-tree CUDA library epic_gb300/_lib/libepic_gb300.so for sm_103a.
+
+nvcc compiles each translation unit in parallel (one -gencode, -lineinfo) and links one
+shared library with the C ABI of include/epic_gb300.h.  Host code is compiled with
+-ffp-contract=off so the host-side set-up gives the same bits on x86-64 and aarch64.
+"""
+from __future__ import annotations
+
+import concurrent.futures as cf
+import os
+import shutil
+import subprocess
+import sys
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+ROOT = os.path.dirname(HERE)
+SRC = os.path.join(HERE, "csrc")
+OUT = os.path.join(HERE, "_lib")
+LIB = os.path.join(OUT, "libepic_gb300.so")
+SOURCES = ["epic_model.cu", "k_filter.cu", "k_column.cu", "k_stencil.cu", "epic_setup.cpp"]
+ARCH = "-gencode=arch=compute_103a,code=sm_103a"
+
+
+def _nvcc() -> str:
+    for cand in (os.environ.get("NVCC"), shutil.which("nvcc"), "/usr/local/cuda/bin/nvcc"):
+        if cand and os.path.exists(cand):
+            return cand
+    raise RuntimeError("nvcc not found")
+
+
+def _flags() -> list[str]:
+    return ["-O3", "-std=c++17", ARCH, "-lineinfo", "-Xcompiler", "-fPIC,-ffp-contract=off",
+            "-I" + os.path.join(ROOT, "include"), "-I" + SRC, "--expt-relaxed-constexpr"]
+
+
+def _compile(src: str) -> str:
+    obj = os.path.join(OUT, os.path.basename(src) + ".o")
+    deps = [os.path.join(SRC, src)] + [os.path.join(SRC, h) for h in os.listdir(SRC) if h.endswith((".h", ".cuh"))]
+    deps.append(os.path.join(ROOT, "include", "epic_gb300.h"))
+    if os.path.exists(obj) and all(os.path.getmtime(obj) >= os.path.getmtime(d) for d in deps):
+        return obj
+    cmd = [_nvcc(), *_flags(), "-c", os.path.join(SRC, src), "-o", obj]
+    r = subprocess.run(cmd, capture_output=True, text=True)
+    if r.returncode != 0:
+        raise RuntimeError(f"nvcc failed for {src}:\n{r.stderr}")
+    return obj
+
+
+def build(verbose: bool = False) -> str:
+    os.makedirs(OUT, exist_ok=True)
+    with cf.ThreadPoolExecutor(max_workers=len(SOURCES)) as ex:
+        objs = list(ex.map(_compile, SOURCES))
+    if not os.path.exists(LIB) or any(os.path.getmtime(o) > os.path.getmtime(LIB) for o in objs):
+        cmd = [_nvcc(), ARCH, "-shared", "-cudart", "static", "-o", LIB, *objs]
+        r = subprocess.run(cmd, capture_output=True, text=True)
+        if r.returncode != 0:
+            raise RuntimeError(f"link failed:\n{r.stderr}")
+    if verbose:
+        print(LIB)
+    return LIB
+
+
+def build_oracle(with_reference: bool = True) -> None:
+    """Compile the oracle's CPU restatement, and the reference harness where its sources exist."""
+    oracle = os.path.join(ROOT, "oracle")
+    subprocess.run(["make", "-s", "-C", oracle, "port"], check=True)
+    ref = os.environ.get("EPIC_REFERENCE_DIR", "/root/reference")
+    if with_reference and os.path.isdir(os.path.join(ref, "src", "shared")):
+        subprocess.run(["make", "-s", "-j8", "-C", oracle, "ref", f"REF={ref}"], check=True)
+
+
+if __name__ == "__main__":
+    build(verbose=True)
+    build_oracle()
+    sys.exit(0)

@@ -1,0 +1,202 @@
+// Device-side model description and the pointwise helpers every kernel shares.
+//
+// All device arrays keep the reference layout X(k,j,i) = base[i + (j+1)*iadim + k*n2]
+// (include/epic.h:407-449), so host upload/download are plain copies.
+#pragma once
+#include <cuda_runtime.h>
+#include <cstdint>
+#include <cfloat>
+
+#define EPIC_MAX_NK 126      // column kernels keep per-column arrays of nk+2 entries
+#define EPIC_MAX_NI 1024     // row kernels keep one row of ni entries in shared memory
+
+namespace epic {
+
+// Time-plane indices and step counters live on the device so that one captured CUDA graph
+// serves every step (the reference rotates IT_ZERO/IT_MINUS1/IT_MINUS2 on the host,
+// src/shared/epic_timestep.c:257-274).
+struct Ctl {
+  int it_zero, it_minus1, it_minus2;
+  int it_uv, it_uv_dis, it_uv_tend;
+  long long itime, model_time;
+  int err_code, err_k, err_j, err_i;   // first model error (0 = none)
+  double err_val;
+  double ab[2][3];                     // Adams-Bashforth coefficients chosen for u, v this step
+  int lf_first[2];                     // leapfrog: forward (Euler) first step for u, v
+};
+
+enum ErrCode { ERR_NONE = 0, ERR_GZ_MONOTONE = 1, ERR_CALC_W_P = 2, ERR_PCHIP_X = 3, ERR_NONFINITE = 4 };
+
+struct DevModel {
+  // sizes
+  int ni, nj, nk, iadim, jadim, kadim;
+  long long n2, n3;
+  int nvp, ntp;
+  // scalars
+  int uv_scheme, k_sigma, k_sponge, newt_cool_on, drag_v, drag_zonal_avg, rayleigh_on;
+  double dt, press0, topo_scale, prandtl, tau_drag, nudiv;
+  double zeta0, zeta1, alpha, sigma_sigma, g_coeff;   // g_coeff = 1/(1-exp(-alpha*(1-sigma_sigma)))
+  double kappa, cp, cpr, rgas, mu_dry, hs_kf, lat0, m0, eps13;
+  double coef[9], nu[9];
+  // 1-D grid arrays (device copies)
+  const double *lon, *lat, *rln, *rlt, *f, *m, *n, *mn, *grav, *mn_inv;
+  const double *sgth, *dsgth, *dsgth_inv, *h_min, *t_sponge_inv;
+  const double *high_lat_h, *high_lat_pv;   // [(nj+3)*(ni+2)] 2-D like the reference
+  const double *h_coef, *v_coef;            // d2dy2 coefficients, 3 per row
+  const double *tw;                         // FFT twiddles: N/2 for the half-length FFT, N+1 for the split
+  // state
+  double *u, *v, *dudt, *dvdt, *hdry, *theta, *p3, *h3, *p2, *theta2, *t2, *t3, *rho2, *rho3, *exner3;
+  double *gz3, *mont3, *heat3, *pv3, *ri2, *div_uv3, *w3, *dzdt3, *u_spinup, *gz_surface;
+  // scratch
+  double *gz, *unity, *old, *work0, *work1, *work2, *work3, *ptable;
+  Ctl *ctl;
+
+  __host__ __device__ __forceinline__ long long at(int k, int j, int i) const {
+    return (long long)i + (long long)(j + 1) * iadim + (long long)k * n2;
+  }
+  __host__ __device__ __forceinline__ long long at2(int j, int i) const { return (long long)i + (long long)(j + 1) * iadim; }
+};
+
+// ---- pointwise helpers: restatements of the reference routines named beside each ----
+
+__device__ __forceinline__ double dmaxr(double x, double y) { return x > y ? x : y; }   // MAX, include/epic.h:144
+__device__ __forceinline__ double dminr(double x, double y) { return x < y ? x : y; }   // MIN, include/epic.h:138
+
+// fcmp, src/shared/epic_funcs_util.c:4275-4330
+__device__ __forceinline__ int fcmp(double x1, double x2) {
+  int e;
+  frexp(fabs(x1) > fabs(x2) ? x1 : x2, &e);
+  const double delta = ldexp(DBL_EPSILON, e);
+  const double d = x1 - x2;
+  return d > delta ? 1 : (d < -delta ? -1 : 0);
+}
+
+// get_sigma / get_p_sigma / g_sigma / f_sigma / return_sigmatheta, epic_funcs_diag.c:1238-1314,1751-1770
+__device__ __forceinline__ double get_sigma(double pbot, double p, double ptop) { return log(p / pbot) / log(ptop / pbot); }
+__device__ __forceinline__ double get_p_sigma(double pbot, double sigma, double ptop) { return pbot * exp(sigma * log(ptop / pbot)); }
+__device__ __forceinline__ double g_sigma(const DevModel &M, double s) {
+  if (s <= M.sigma_sigma) return 0.;
+  if (s >= 1.) return 1.;
+  return M.g_coeff * (1. - exp(-M.alpha * (s - M.sigma_sigma)));
+}
+__device__ __forceinline__ double f_sigma(const DevModel &M, double s) {
+  if (s < 0.) return M.zeta0;
+  if (s <= M.sigma_sigma) return M.zeta0 + s * (M.zeta1 - M.zeta0);
+  if (s < 1.) return (1. - g_sigma(M, s)) * (M.zeta0 + s * (M.zeta1 - M.zeta0));
+  return 0.;
+}
+__device__ __forceinline__ double return_sigmatheta(const DevModel &M, double theta, double p, double pbot, double ptop) {
+  if (p <= ptop) return theta;
+  const double s = get_sigma(pbot, p, ptop);
+  return f_sigma(M, s) + g_sigma(M, s) * theta;
+}
+// return_temp (x_h2 = 0), return_density (ideal gas), return_enthalpy (cpr*T*rgas)
+__device__ __forceinline__ double return_temp(const DevModel &M, double p, double theta) { return theta * pow(p / M.press0, M.kappa); }
+__device__ __forceinline__ double return_density(double p, double t, double mu) { return p * mu / (8.314472e+3 * t); }
+__device__ __forceinline__ double return_enthalpy(const DevModel &M, double t) { return (M.cpr * t) * M.rgas; }
+// onto_kk(P2_INDEX) at a layer, epic_funcs_diag.c:2601-2618
+__device__ __forceinline__ double layer_p(const DevModel &M, double top, double bot) {
+  if (fcmp(bot, top) == 0) return .5 * (bot + top);
+  const double kp1 = M.kappa + 1.;
+  return pow((pow(bot, kp1) - pow(top, kp1)) / (kp1 * (bot - top)), 1. / M.kappa);
+}
+
+struct Trip { double x, y, z; };
+
+__device__ __forceinline__ double pchst(double a, double b) {
+  if (a == 0.0) return 0.0;
+  if (a < 0.0) return b < 0.0 ? 1.0 : (b == 0.0 ? 0.0 : -1.0);
+  return b < 0.0 ? -1.0 : (b == 0.0 ? 0.0 : 1.0);
+}
+// spline_pchip (Fritsch-Carlson PCHIM slopes), epic_funcs_util.c:721-845; returns false if x not increasing
+__device__ __forceinline__ bool spline_pchip(int n, Trip *t) {
+  for (int i = 1; i < n; i++)
+    if (t[i].x <= t[i - 1].x) return false;
+  double h1 = t[1].x - t[0].x;
+  double del1 = (t[1].y - t[0].y) / h1;
+  if (n == 2) { t[0].z = del1; t[1].z = del1; return true; }
+  double h2 = t[2].x - t[1].x;
+  double del2 = (t[2].y - t[1].y) / h2;
+  double hsum = h1 + h2;
+  double w1 = (h1 + hsum) / hsum, w2 = -h1 / hsum;
+  t[0].z = w1 * del1 + w2 * del2;
+  if (pchst(t[0].z, del1) <= 0.0) t[0].z = 0.0;
+  else if (pchst(del1, del2) < 0.0) {
+    const double dmx = 3.0 * del1;
+    if (fabs(dmx) < fabs(t[0].z)) t[0].z = dmx;
+  }
+  for (int i = 2; i <= n - 1; i++) {
+    if (2 < i) {
+      h1 = h2;
+      h2 = t[i].x - t[i - 1].x;
+      hsum = h1 + h2;
+      del1 = del2;
+      del2 = (t[i].y - t[i - 1].y) / h2;
+    }
+    t[i - 1].z = 0.0;
+    if (pchst(del1, del2) > 0.0) {
+      const double hsumt3 = 3.0 * hsum;
+      w1 = (hsum + h1) / hsumt3;
+      w2 = (hsum + h2) / hsumt3;
+      const double dmx = dmaxr(fabs(del1), fabs(del2)), dmn = dminr(fabs(del1), fabs(del2));
+      t[i - 1].z = dmn / (w1 * (del1 / dmx) + w2 * (del2 / dmx));
+    }
+  }
+  w1 = -h2 / hsum;
+  w2 = (h2 + hsum) / hsum;
+  t[n - 1].z = w1 * del1 + w2 * del2;
+  if (pchst(t[n - 1].z, del2) <= 0.0) t[n - 1].z = 0.0;
+  else if (pchst(del1, del2) < 0.0) {
+    const double dmx = 3.0 * del2;
+    if (fabs(dmx) < fabs(t[n - 1].z)) t[n - 1].z = dmx;
+  }
+  return true;
+}
+// splint_pchip, epic_funcs_util.c:926-946
+__device__ __forceinline__ double splint_pchip(double xx, const Trip *t, double h) {
+  const double delta = (t[1].y - t[0].y) / h;
+  const double del1 = (t[0].z - delta) / h;
+  const double del2 = (t[1].z - delta) / h;
+  const double c3 = (del1 + del2) / h;
+  const double c2 = -(del1 + del1 + del2);
+  const double x = xx - t[0].x;
+  return t[0].y + x * (t[0].z + x * (c2 + x * c3));
+}
+// find_place_in_table (ascending tables only), epic_funcs_util.c:2908-2967
+__device__ __forceinline__ int find_place_in_table(int n, const Trip *t, double x, double *dx) {
+  if (fcmp(x, t[0].x) <= 0) { *dx = t[1].x - t[0].x; return 0; }
+  if (fcmp(x, t[n - 1].x) >= 0) { *dx = t[n - 1].x - t[n - 2].x; return n - 2; }
+  int il = -1, iu = n;
+  while (iu - il > 1) {
+    const int im = (iu + il) >> 1;
+    if (fcmp(x, t[im].x) >= 0) il = im; else iu = im;
+  }
+  *dx = t[il + 1].x - t[il].x;
+  return il;
+}
+
+// Record the first model error (the reference would epic_error() and exit).
+__device__ __forceinline__ void flag_error(Ctl *c, int code, int k, int j, int i, double v) {
+  if (atomicCAS(&c->err_code, 0, code) == 0) {
+    c->err_k = k; c->err_j = j; c->err_i = i; c->err_val = v;
+  }
+}
+
+// Zonal periodicity of one row: pads i = 0 and i = ni+1 (bc_lateral, src/single/s_epic_functions.c:55-59).
+// Called by the thread that owns interior cell i after it wrote the final value.
+__device__ __forceinline__ void write_with_pads(double *a, const DevModel &M, long long rowbase, int i, double val) {
+  a[rowbase + i] = val;
+  if (i == M.ni) a[rowbase] = val;
+  if (i == 1) a[rowbase + M.ni + 1] = val;
+}
+
+}  // namespace epic
+
+// Kernel launch helpers.
+#define EPIC_CUDA_CHECK(x)                                                     \
+  do {                                                                         \
+    cudaError_t e_ = (x);                                                      \
+    if (e_ != cudaSuccess) return epic::set_error(EPIC_ERR_CUDA, "%s: %s (%s:%d)", #x, cudaGetErrorString(e_), __FILE__, __LINE__); \
+  } while (0)
+
+inline unsigned epic_blocks(long long n, int threads) { return (unsigned)((n + threads - 1) / threads); }

@@ -1,0 +1,485 @@
+// Host side of the GB300 timestep(): device state, the step sequence, CUDA-graph replay and
+// the C ABI of include/epic_gb300.h.
+#include <cmath>
+#include <cstdio>
+#include <cstdlib>
+#include <cstring>
+#include <vector>
+#include "device_common.cuh"
+#include "kernels.h"
+#include "epic_common.h"
+#include "epic_gb300.h"
+
+using epic::Ctl;
+using epic::DevModel;
+using epic::set_error;
+
+struct epic_model {
+  epic_grid g;
+  DevModel d;
+  int precision;
+  cudaStream_t stream = nullptr;
+  char *pool = nullptr;
+  size_t pool_bytes = 0;
+  bool uploaded = false;
+  cudaGraphExec_t run_graph = nullptr;
+  bool graph_failed = false;
+};
+
+namespace {
+
+constexpr double kDeg = M_PI / 180.;
+
+// Tables the reference builds in the initialisation blocks of its routines.
+struct HostTables {
+  std::vector<double> high_lat_h, high_lat_pv, h_coef, v_coef, mn_inv, tw;
+  double m0 = 0., coef[9] = {0}, max_nu[9] = {0}, eps13 = 0.;
+};
+
+// zonal_filter's HIGH_LAT_H / HIGH_LAT_PV tables, src/shared/epic_adjust.c:132-241.
+void filter_tables(const epic_grid &g, const epic::Layout &L, HostTables &T) {
+  const double lat0 = g.lat0 * kDeg, re = g.re, rp = g.rp;
+  const double rln0 = re / sqrt(1. + pow(rp / re * tan(lat0), 2.));
+  const double rlt0 = rln0 / (cos(lat0) * (pow(sin(lat0), 2.) + pow(re / rp * cos(lat0), 2.)));
+  const double m0 = 1. / (rln0 * g.dln * kDeg);
+  const double n0 = 1. / (rlt0 * g.dlt * kDeg);
+  T.m0 = m0;
+  T.high_lat_h.assign(L.n2, 0.);
+  T.high_lat_pv.assign(L.n2, 0.);
+  auto fill = [&](std::vector<double> &hl, int J, int jj) {
+    hl[L.at2(J, 1)] = 1.;
+    const double r = g.mn[jj] / (g.m[jj] * g.n[jj]);
+    double tmp0 = (g.n[jj] / n0) / (g.m[jj] / m0);
+    tmp0 = pow(tmp0, 2.);
+    for (int I = 2; I <= g.ni / 2 + 1; I++) {
+      double tmp1 = sin((I - 1) * (g.dln) * kDeg / 2.);
+      tmp1 = pow(tmp1, -2.);
+      tmp1 *= r * tmp0;
+      tmp1 = (tmp1 < 1.) ? tmp1 : 1.;
+      hl[L.at2(J, I)] = tmp1;
+    }
+  };
+  for (int J = 0; J <= g.nj; J++) fill(T.high_lat_h, J, 2 * J + 1);
+  for (int J = 1; J <= g.nj; J++) fill(T.high_lat_pv, J, 2 * J);
+}
+
+// d2dy2's 3-point coefficients (a Legendre fit; one-sided at the ends), epic_subgrid.c:1049-1141.
+void d2dy2_coef(double r2_inv, double l0, double l1, double l2, int where, double *c) {
+  const double lat[3] = {l0 * kDeg, l1 * kDeg, l2 * kDeg};
+  const double s0 = sin(lat[0]), s1 = sin(lat[1]), s2 = sin(lat[2]);
+  if (where == 0) {
+    c[0] = r2_inv * (1. + s0 * (-3. * s0 + s1 + s2)) / ((s1 - s0) * .5 * (s2 - s0));
+    c[1] = -r2_inv * 2. * (cos(2. * lat[0]) + s0 * s2) / ((s1 - s0) * (s2 - s1));
+    c[2] = r2_inv * (cos(2. * lat[0]) + s0 * s1) / (.5 * (s2 - s0) * (s2 - s1));
+  } else if (where == 2) {
+    c[0] = r2_inv * (cos(2. * lat[2]) + s1 * s2) / ((s1 - s0) * .5 * (s2 - s0));
+    c[1] = -r2_inv * 2. * (cos(2. * lat[2]) + s0 * s2) / ((s1 - s0) * (s2 - s1));
+    c[2] = r2_inv * (1. + s2 * (s0 + s1 - 3. * s2)) / (.5 * (s2 - s0) * (s2 - s1));
+  } else {
+    c[0] = r2_inv * (cos(2. * lat[1]) + s1 * s2) / ((s1 - s0) * .5 * (s2 - s0));
+    c[1] = -r2_inv * 2. * (1. + s1 * (s0 - 3. * s1 + s2)) / ((s1 - s0) * (s2 - s1));
+    c[2] = r2_inv * (cos(2. * lat[1]) + s0 * s1) / (.5 * (s2 - s0) * (s2 - s1));
+  }
+}
+
+void visc_tables(const epic_grid &g, HostTables &T) {
+  epic::set_max_nu(g.dt, g.dy0, g.uv_scheme, T.max_nu);
+  double nu[9];
+  for (int i = 0; i < 9; i++) nu[i] = g.nu[i];
+  nu[2] = 0.;   // the hyperviscosity routines zero grid.nu[2] (epic_subgrid.c:651, :879)
+  for (int itmp2 = 2; itmp2 <= 8; itmp2 += 2) {
+    T.coef[itmp2] = nu[itmp2] > 0. ? nu[itmp2] : 0.01 * T.max_nu[itmp2];
+    for (int itmp = 2; itmp < itmp2; itmp += 2) T.coef[itmp2] /= T.coef[itmp];
+  }
+  const int nj = g.nj;
+  T.h_coef.assign(3 * (nj + 2), 0.);
+  T.v_coef.assign(3 * (nj + 2), 0.);
+  auto r2 = [&](int jj) { double r = g.rlt[jj]; return 1. / (r * r); };
+  d2dy2_coef(r2(1), g.lat[1], g.lat[3], g.lat[5], 0, &T.h_coef[0]);
+  for (int J = 1; J < nj; J++) d2dy2_coef(r2(2 * J + 1), g.lat[2 * J - 1], g.lat[2 * J + 1], g.lat[2 * J + 3], 1, &T.h_coef[3 * J]);
+  d2dy2_coef(r2(2 * nj + 1), g.lat[2 * nj - 3], g.lat[2 * nj - 1], g.lat[2 * nj + 1], 2, &T.h_coef[3 * nj]);
+  d2dy2_coef(r2(0), g.lat[0], g.lat[2], g.lat[4], 0, &T.v_coef[0]);
+  for (int J = 1; J <= nj; J++) d2dy2_coef(r2(2 * J), g.lat[2 * J - 2], g.lat[2 * J], g.lat[2 * J + 2], 1, &T.v_coef[3 * J]);
+  const int J = nj + 1;
+  d2dy2_coef(r2(2 * J), g.lat[2 * J - 4], g.lat[2 * J - 2], g.lat[2 * J], 2, &T.v_coef[3 * J]);
+}
+
+double cube_root_machine_eps() {
+  // machine_epsilon, epic_funcs_util.c:1247-1265, then pow(eps, 1/3) as calc_w uses it
+  volatile double eps = 1.;
+  while (1. + eps != 1.) eps *= .5;
+  eps *= 2.;
+  return pow((double)eps, 1. / 3.);
+}
+
+template <typename T>
+T *carve(char *&p, size_t count) {
+  T *r = reinterpret_cast<T *>(p);
+  p += ((count * sizeof(T) + 255) / 256) * 256;
+  return r;
+}
+
+int check_launch(const char *what) {
+  cudaError_t e = cudaGetLastError();
+  if (e != cudaSuccess) return set_error(EPIC_ERR_CUDA, "%s: %s", what, cudaGetErrorString(e));
+  return EPIC_OK;
+}
+
+// One reference-function stage of the step, in the reference's call order.
+int run_stage(epic_model *m, int stage) {
+  DevModel &M = m->d;
+  cudaStream_t s = m->stream;
+  using namespace epic;
+  switch (stage) {
+    case 0: launch_zero_tend(M, s); break;
+    case 1: launch_source_sink(M, s); break;
+    case 2: launch_calc_w(M, s); break;
+    case 3: launch_uv_core(M, s); break;
+    case 4: launch_uv_drag(M, s); break;
+    case 5:
+      launch_meridional_hyperviscosity(M, 2, M.hdry, PL_NONE, s);
+      launch_zonal_hyperviscosity(M, 2, M.hdry, PL_NONE, s);
+      launch_restore_mass(M, s);
+      launch_meridional_hyperviscosity(M, 3, M.theta, PL_NONE, s);
+      launch_zonal_hyperviscosity(M, 3, M.theta, PL_NONE, s);
+      break;
+    case 6:
+      launch_advection_prep(M, 0, s);
+      launch_hsu_vertical(M, M.unity, 0, s);
+      launch_hsu_meridional(M, M.unity, 0, s);
+      launch_hsu_zonal(M, M.unity, 0, 1, s);
+      launch_advection_prep(M, 1, s);
+      launch_hsu_vertical(M, M.theta, 1, s);
+      launch_hsu_meridional(M, M.theta, 1, s);
+      launch_hsu_zonal(M, M.theta, 0, M.k_sigma - 1, s);
+      launch_advection_prep(M, 2, s);
+      launch_hsu_vertical(M, M.hdry, 2, s);
+      launch_hsu_meridional(M, M.hdry, 2, s);
+      launch_hsu_zonal(M, M.hdry, 1, 1, s);
+      launch_restore_mass(M, s);
+      launch_set_p2etc(M, 0, s);
+      break;
+    case 7: launch_store_pgrad_vars(M, s); break;
+    case 8:
+      cudaMemcpyAsync(M.gz, M.gz3, M.n3 * sizeof(double), cudaMemcpyDeviceToDevice, s);
+      launch_filter_planes(M, M.gz, PL_NONE, M.gz, 0, M.nk, 0, s);
+      launch_gz_monotone(M, s);
+      break;
+    case 9:
+      launch_varz_filter(M, M.dudt, PL_UV_TEND, 0, 1, M.nk, s);
+      launch_varz_filter(M, M.dvdt, PL_UV_TEND, 1, 1, M.nk, s);
+      break;
+    case 10:
+      launch_varz_filter(M, M.hdry, PL_NONE, 2, 1, M.nk, s);
+      launch_restore_mass(M, s);
+      launch_varz_filter(M, M.theta, PL_NONE, 3, M.k_sigma - 1, M.nk, s);
+      break;
+    case 11: launch_set_p2etc(M, 1, s); break;
+    case 12: launch_uv_pgrad(M, s); break;
+    case 13: launch_divergence_damping(M, s); break;
+    case 14: launch_uv_update(M, s); break;
+    case 15:
+      launch_meridional_hyperviscosity(M, 0, M.u, PL_UV, s);
+      launch_meridional_hyperviscosity(M, 1, M.v, PL_UV, s);
+      launch_zonal_hyperviscosity(M, 0, M.u, PL_UV, s);
+      launch_zonal_hyperviscosity(M, 1, M.v, PL_UV, s);
+      break;
+    case 16: launch_store_diag(M, s); break;
+    case 17: launch_calc_heating(M, s); break;
+    case 18: launch_set_p2etc(M, 0, s); break;
+    default: return set_error(EPIC_ERR_ARG, "unknown stage %d", stage);
+  }
+  return check_launch("stage launch");
+}
+
+int enqueue_step(epic_model *m) {
+  static const int step[] = {0, 1, 2, 3, 4, 5, 6, 7, 8, 9, 10, 11, 7, 12, 13, 14, 15, 16, 17};
+  for (int st : step) {
+    int rc = run_stage(m, st);
+    if (rc) return rc;
+  }
+  return EPIC_OK;
+}
+
+int enqueue_sync(epic_model *m) {
+  static const int sync[] = {11, 7, 16, 17, 2};
+  for (int st : sync) {
+    int rc = run_stage(m, st);
+    if (rc) return rc;
+  }
+  return EPIC_OK;
+}
+
+int read_ctl(epic_model *m, Ctl &c) {
+  EPIC_CUDA_CHECK(cudaMemcpyAsync(&c, m->d.ctl, sizeof(Ctl), cudaMemcpyDeviceToHost, m->stream));
+  EPIC_CUDA_CHECK(cudaStreamSynchronize(m->stream));
+  return EPIC_OK;
+}
+
+int model_error(const Ctl &c) {
+  if (c.err_code == 0) return EPIC_OK;
+  static const char *what[] = {"", "store_pgrad_vars: GZ3 not monotonic", "calc_w: p2 >= p4",
+                               "zonal_filter: spline_pchip x not increasing", "non-finite value"};
+  return set_error(EPIC_ERR_MODEL, "%s at (k=%d, j=%d, i=%d), value %g", c.err_code < 5 ? what[c.err_code] : "model error",
+                   c.err_k, c.err_j, c.err_i, c.err_val);
+}
+
+}  // namespace
+
+extern "C" const char *epic_last_error(void) { return epic::error_buffer(); }
+
+extern "C" int epic_model_create(const epic_grid *g, int32_t precision, epic_model **out) {
+  if (!g || !out) return set_error(EPIC_ERR_ARG, "epic_model_create: NULL argument");
+  *out = nullptr;
+  if (precision != EPIC_PREC_FP64) return set_error(EPIC_ERR_ARG, "precision form %d not available", precision);
+  if (g->ni < 4 || (g->ni & (g->ni - 1)) || g->ni > EPIC_MAX_NI) return set_error(EPIC_ERR_ARG, "ni=%d: need a power of 2 in [4,%d]", g->ni, EPIC_MAX_NI);
+  if (g->nj < 3 || g->nk < 3 || g->nk > EPIC_MAX_NK) return set_error(EPIC_ERR_ARG, "nj=%d nk=%d out of range", g->nj, g->nk);
+  if (g->globe_latbot != -90. || g->globe_lattop != 90.) return set_error(EPIC_ERR_ARG, "only the full globe is supported");
+  if (g->k_sigma < 2 || g->k_sigma > g->nk) return set_error(EPIC_ERR_ARG, "k_sigma=%d out of range", g->k_sigma);
+  if (g->k_sponge != 0 || g->newt_cool_adjust) return set_error(EPIC_ERR_ARG, "k_sponge > 0 and newt_cool_adjust are not supported");
+  if ((g->newt_cool_on && g->prandtl > 0.) || (g->tau_drag > 0. && g->tau_drag < 1.e+20))
+    return set_error(EPIC_ERR_ARG, "zonal Rayleigh drag (prandtl/tau_drag) is not supported");
+  if (g->uv_scheme != EPIC_UV_AB3 && g->uv_scheme != EPIC_UV_LEAPFROG) return set_error(EPIC_ERR_ARG, "uv_scheme=%d", g->uv_scheme);
+  const char *ptrs[] = {(const char *)g->lon, (const char *)g->lat, (const char *)g->rln, (const char *)g->rlt, (const char *)g->f,
+                        (const char *)g->m, (const char *)g->n, (const char *)g->mn, (const char *)g->g, (const char *)g->sigmatheta,
+                        (const char *)g->dsgth, (const char *)g->dsgth_inv, (const char *)g->h_min, (const char *)g->t_sponge_inv};
+  for (const char *p : ptrs)
+    if (!p) return set_error(EPIC_ERR_ARG, "epic_model_create: grid array pointer is NULL");
+
+  epic_model *m = new epic_model();
+  m->g = *g;
+  m->precision = precision;
+  const epic::Layout L(g->ni, g->nj, g->nk);
+  DevModel &d = m->d;
+  d.ni = g->ni; d.nj = g->nj; d.nk = g->nk;
+  d.iadim = L.iadim; d.jadim = L.jadim; d.kadim = L.kadim;
+  d.n2 = L.n2; d.n3 = L.n3;
+  d.nvp = g->uv_scheme == EPIC_UV_AB3 ? 1 : 2;
+  d.ntp = g->uv_scheme == EPIC_UV_AB3 ? 3 : 1;
+  d.uv_scheme = g->uv_scheme; d.k_sigma = g->k_sigma; d.k_sponge = g->k_sponge; d.newt_cool_on = g->newt_cool_on;
+  d.drag_v = g->drag_v; d.drag_zonal_avg = g->drag_zonal_avg; d.rayleigh_on = 0;
+  d.dt = (double)g->dt; d.press0 = g->press0; d.topo_scale = g->topo_scale; d.prandtl = g->prandtl; d.tau_drag = g->tau_drag;
+  d.zeta0 = g->zeta0; d.zeta1 = g->zeta1; d.alpha = g->hybrid_alpha; d.sigma_sigma = g->sigma_sigma;
+  d.g_coeff = 1. / (1 - exp(-g->hybrid_alpha * (1. - g->sigma_sigma)));
+  d.kappa = g->kappa; d.cp = g->cp; d.cpr = g->cpr; d.rgas = g->rgas;
+  d.mu_dry = 1. / (g->rgas / 8.314472e+3);
+  d.hs_kf = g->hs_kf; d.lat0 = g->lat0;
+
+  HostTables T;
+  filter_tables(*g, L, T);
+  visc_tables(*g, T);
+  d.m0 = T.m0;
+  d.eps13 = cube_root_machine_eps();
+  for (int i = 0; i < 9; i++) { d.coef[i] = T.coef[i]; d.nu[i] = g->nu[i]; }
+  d.nu[2] = 0.;
+  d.nudiv = g->nudiv_nondim * T.max_nu[2];
+  const int nj1 = 2 * (g->nj + 1) + 1, ni1 = 2 * (g->ni + 1) + 1, nk1 = 2 * (g->nk + 1) + 1;
+  T.mn_inv.resize(nj1);
+  for (int i = 0; i < nj1; i++) T.mn_inv[i] = 1. / g->mn[i];
+  T.tw.assign(epic::twiddle_doubles(g->ni), 0.);
+  epic::fill_twiddles(g->ni, T.tw.data());
+
+  // One pool for everything: state, scratch, tables.
+  const size_t n3 = (size_t)L.n3, n2 = (size_t)L.n2;
+  const size_t n_state3 = 2 * d.nvp + 2 * d.ntp + 20;   // u,v planes + tendencies + 20 single fields
+  const size_t n_scratch3 = 7;                          // gz, unity, old, work0..3
+  auto rnd = [](size_t b) { return ((b + 255) / 256) * 256; };
+  size_t bytes = rnd(sizeof(Ctl)) + (n_state3 + n_scratch3) * rnd(n3 * 8) + 3 * rnd(n2 * 8) + rnd((size_t)(g->nj + 3) * (g->nk + 2) * 3 * 8) +
+                 rnd(ni1 * 8) + 10 * rnd(nj1 * 8) + 3 * rnd(nk1 * 8) + rnd((g->nk + 2) * 8) + rnd((g->k_sponge + 1) * 8) +
+                 2 * rnd(3 * (g->nj + 2) * 8) + rnd(T.tw.size() * 8) + 4096;
+  cudaError_t e = cudaStreamCreateWithFlags(&m->stream, cudaStreamNonBlocking);
+  if (e != cudaSuccess) { delete m; return set_error(EPIC_ERR_CUDA, "cudaStreamCreate: %s", cudaGetErrorString(e)); }
+  e = cudaMalloc(&m->pool, bytes);
+  if (e != cudaSuccess) {
+    cudaStreamDestroy(m->stream);
+    delete m;
+    return set_error(EPIC_ERR_NOMEM, "cudaMalloc(%zu): %s", bytes, cudaGetErrorString(e));
+  }
+  m->pool_bytes = bytes;
+  cudaMemsetAsync(m->pool, 0, bytes, m->stream);
+  char *p = m->pool;
+  d.ctl = carve<Ctl>(p, 1);
+  d.u = carve<double>(p, d.nvp * n3); d.v = carve<double>(p, d.nvp * n3);
+  d.dudt = carve<double>(p, d.ntp * n3); d.dvdt = carve<double>(p, d.ntp * n3);
+  double **f3[] = {&d.hdry, &d.theta, &d.p3, &d.h3, &d.p2, &d.theta2, &d.t2, &d.t3, &d.rho2, &d.rho3, &d.exner3, &d.gz3, &d.mont3,
+                   &d.heat3, &d.pv3, &d.ri2, &d.div_uv3, &d.w3, &d.dzdt3, &d.u_spinup};
+  for (double **q : f3) *q = carve<double>(p, n3);
+  double **s3[] = {&d.gz, &d.unity, &d.old, &d.work0, &d.work1, &d.work2, &d.work3};
+  for (double **q : s3) *q = carve<double>(p, n3);
+  d.gz_surface = carve<double>(p, n2);
+  double *hlh = carve<double>(p, n2), *hlpv = carve<double>(p, n2);
+  d.ptable = carve<double>(p, (size_t)(g->nj + 3) * (g->nk + 2) * 3);
+  double *lon = carve<double>(p, ni1);
+  double *j1[10];
+  for (int i = 0; i < 10; i++) j1[i] = carve<double>(p, nj1);
+  double *sg = carve<double>(p, nk1), *ds = carve<double>(p, nk1), *dsi = carve<double>(p, nk1);
+  double *hmin = carve<double>(p, g->nk + 2), *tsp = carve<double>(p, g->k_sponge + 1);
+  double *hc = carve<double>(p, 3 * (g->nj + 2)), *vc = carve<double>(p, 3 * (g->nj + 2));
+  double *tw = carve<double>(p, T.tw.size());
+  if ((size_t)(p - m->pool) > bytes) {
+    epic_model_destroy(m);
+    return set_error(EPIC_ERR_NOMEM, "internal pool layout overflow");
+  }
+  auto up = [&](double *dst, const double *src, size_t n) {
+    return cudaMemcpyAsync(dst, src, n * sizeof(double), cudaMemcpyHostToDevice, m->stream);
+  };
+  up(lon, g->lon, ni1);
+  const double *src1[10] = {g->lat, g->rln, g->rlt, g->f, g->m, g->n, g->mn, g->g, T.mn_inv.data(), nullptr};
+  for (int i = 0; i < 9; i++) up(j1[i], src1[i], nj1);
+  up(sg, g->sigmatheta, nk1); up(ds, g->dsgth, nk1); up(dsi, g->dsgth_inv, nk1);
+  up(hmin, g->h_min, g->nk + 2); up(tsp, g->t_sponge_inv, g->k_sponge + 1);
+  up(hlh, T.high_lat_h.data(), n2); up(hlpv, T.high_lat_pv.data(), n2);
+  up(hc, T.h_coef.data(), T.h_coef.size()); up(vc, T.v_coef.data(), T.v_coef.size());
+  up(tw, T.tw.data(), T.tw.size());
+  d.lon = lon; d.lat = j1[0]; d.rln = j1[1]; d.rlt = j1[2]; d.f = j1[3]; d.m = j1[4]; d.n = j1[5]; d.mn = j1[6]; d.grav = j1[7];
+  d.mn_inv = j1[8];
+  d.sgth = sg; d.dsgth = ds; d.dsgth_inv = dsi; d.h_min = hmin; d.t_sponge_inv = tsp;
+  d.high_lat_h = hlh; d.high_lat_pv = hlpv; d.h_coef = hc; d.v_coef = vc; d.tw = tw;
+  epic::filter_kernels_init(g->ni);
+  e = cudaStreamSynchronize(m->stream);
+  if (e != cudaSuccess) {
+    epic_model_destroy(m);
+    return set_error(EPIC_ERR_CUDA, "epic_model_create: %s", cudaGetErrorString(e));
+  }
+  *out = m;
+  return EPIC_OK;
+}
+
+extern "C" void epic_model_destroy(epic_model *m) {
+  if (!m) return;
+  if (m->run_graph) cudaGraphExecDestroy(m->run_graph);
+  if (m->stream) cudaStreamSynchronize(m->stream);
+  if (m->pool) cudaFree(m->pool);
+  if (m->stream) cudaStreamDestroy(m->stream);
+  delete m;
+}
+
+extern "C" int epic_model_upload(epic_model *m, const epic_fields *f) {
+  if (!m || !f) return set_error(EPIC_ERR_ARG, "epic_model_upload: NULL argument");
+  if (!f->u || !f->v || !f->dudt || !f->dvdt || !f->hdry || !f->theta || !f->p3 || !f->gz_surface || !f->u_spinup)
+    return set_error(EPIC_ERR_ARG, "epic_model_upload: a required field pointer is NULL");
+  DevModel &d = m->d;
+  const size_t b3 = (size_t)d.n3 * sizeof(double);
+  cudaStream_t s = m->stream;
+  EPIC_CUDA_CHECK(cudaMemcpyAsync(d.u, f->u, d.nvp * b3, cudaMemcpyHostToDevice, s));
+  EPIC_CUDA_CHECK(cudaMemcpyAsync(d.v, f->v, d.nvp * b3, cudaMemcpyHostToDevice, s));
+  EPIC_CUDA_CHECK(cudaMemcpyAsync(d.dudt, f->dudt, d.ntp * b3, cudaMemcpyHostToDevice, s));
+  EPIC_CUDA_CHECK(cudaMemcpyAsync(d.dvdt, f->dvdt, d.ntp * b3, cudaMemcpyHostToDevice, s));
+  const double *src[] = {f->hdry, f->theta, f->p3, f->h3, f->p2, f->theta2, f->t2, f->t3, f->rho2, f->rho3, f->exner3, f->gz3,
+                         f->mont3, f->heat3, f->pv3, f->ri2, f->div_uv3, f->w3, f->dzdt3, f->u_spinup};
+  double *dst[] = {d.hdry, d.theta, d.p3, d.h3, d.p2, d.theta2, d.t2, d.t3, d.rho2, d.rho3, d.exner3, d.gz3,
+                   d.mont3, d.heat3, d.pv3, d.ri2, d.div_uv3, d.w3, d.dzdt3, d.u_spinup};
+  for (int i = 0; i < 20; i++)
+    if (src[i]) EPIC_CUDA_CHECK(cudaMemcpyAsync(dst[i], src[i], b3, cudaMemcpyHostToDevice, s));
+  EPIC_CUDA_CHECK(cudaMemcpyAsync(d.gz_surface, f->gz_surface, (size_t)d.n2 * sizeof(double), cudaMemcpyHostToDevice, s));
+  Ctl c;
+  memset(&c, 0, sizeof(c));
+  c.it_zero = f->it_zero; c.it_minus1 = f->it_minus1; c.it_minus2 = f->it_minus2;
+  c.itime = f->itime; c.model_time = f->model_time;
+  // timeplane_bookkeeping, epic_funcs_diag.c:7086-7124
+  if (d.uv_scheme == EPIC_UV_AB3) {
+    c.it_uv = 0; c.it_uv_dis = 0; c.it_uv_tend = c.it_zero;
+  } else {
+    c.it_uv = c.it_zero;
+    const double flag = f->u[(size_t)c.it_minus1 * d.n3 + d.at(1, 0, 1)];
+    c.it_uv_dis = flag == DBL_MAX ? c.it_zero : c.it_minus1;
+    c.it_uv_tend = 0;
+  }
+  EPIC_CUDA_CHECK(cudaMemcpyAsync(d.ctl, &c, sizeof(Ctl), cudaMemcpyHostToDevice, s));
+  EPIC_CUDA_CHECK(cudaStreamSynchronize(s));
+  m->uploaded = true;
+  return EPIC_OK;
+}
+
+extern "C" int epic_model_timestep(epic_model *m, int32_t action) {
+  if (!m) return set_error(EPIC_ERR_ARG, "epic_model_timestep: NULL model");
+  if (!m->uploaded) return set_error(EPIC_ERR_STATE, "timestep before upload");
+  if (action == EPIC_STEP_PROGS_AND_SYNC_DIAGS) return enqueue_step(m);
+  if (action == EPIC_SYNC_DIAGS_ONLY) return enqueue_sync(m);
+  return set_error(EPIC_ERR_ARG, "unrecognized action=%d", action);
+}
+
+extern "C" int epic_model_run_stage(epic_model *m, int32_t stage) {
+  if (!m) return set_error(EPIC_ERR_ARG, "epic_model_run_stage: NULL model");
+  if (!m->uploaded) return set_error(EPIC_ERR_STATE, "stage before upload");
+  return run_stage(m, stage);
+}
+
+extern "C" int epic_model_run(epic_model *m, int32_t nsteps) {
+  if (!m) return set_error(EPIC_ERR_ARG, "epic_model_run: NULL model");
+  if (!m->uploaded) return set_error(EPIC_ERR_STATE, "run before upload");
+  if (nsteps <= 0) return EPIC_OK;
+  if (!m->run_graph && !m->graph_failed) {
+    cudaGraph_t graph = nullptr;
+    if (cudaStreamBeginCapture(m->stream, cudaStreamCaptureModeThreadLocal) == cudaSuccess) {
+      int rc = enqueue_step(m);
+      if (!rc) rc = epic::launch_itime_advance(m->d, m->stream);
+      cudaError_t e = cudaStreamEndCapture(m->stream, &graph);
+      if (rc == EPIC_OK && e == cudaSuccess && graph) {
+        if (cudaGraphInstantiate(&m->run_graph, graph, 0) != cudaSuccess) m->run_graph = nullptr;
+      }
+      if (graph) cudaGraphDestroy(graph);
+    }
+    cudaGetLastError();
+    if (!m->run_graph) m->graph_failed = true;
+  }
+  for (int s = 0; s < nsteps; s++) {
+    if (m->run_graph) {
+      EPIC_CUDA_CHECK(cudaGraphLaunch(m->run_graph, m->stream));
+    } else {
+      int rc = enqueue_step(m);
+      if (rc) return rc;
+      epic::launch_itime_advance(m->d, m->stream);
+    }
+  }
+  return check_launch("epic_model_run");
+}
+
+extern "C" int epic_model_sync(epic_model *m) {
+  if (!m) return set_error(EPIC_ERR_ARG, "epic_model_sync: NULL model");
+  EPIC_CUDA_CHECK(cudaStreamSynchronize(m->stream));
+  Ctl c;
+  int rc = read_ctl(m, c);
+  if (rc) return rc;
+  return model_error(c);
+}
+
+extern "C" int epic_model_download(epic_model *m, epic_fields *f) {
+  if (!m || !f) return set_error(EPIC_ERR_ARG, "epic_model_download: NULL argument");
+  DevModel &d = m->d;
+  const size_t b3 = (size_t)d.n3 * sizeof(double);
+  cudaStream_t s = m->stream;
+  if (f->u) EPIC_CUDA_CHECK(cudaMemcpyAsync(f->u, d.u, d.nvp * b3, cudaMemcpyDeviceToHost, s));
+  if (f->v) EPIC_CUDA_CHECK(cudaMemcpyAsync(f->v, d.v, d.nvp * b3, cudaMemcpyDeviceToHost, s));
+  if (f->dudt) EPIC_CUDA_CHECK(cudaMemcpyAsync(f->dudt, d.dudt, d.ntp * b3, cudaMemcpyDeviceToHost, s));
+  if (f->dvdt) EPIC_CUDA_CHECK(cudaMemcpyAsync(f->dvdt, d.dvdt, d.ntp * b3, cudaMemcpyDeviceToHost, s));
+  double *dst[] = {f->hdry, f->theta, f->p3, f->h3, f->p2, f->theta2, f->t2, f->t3, f->rho2, f->rho3, f->exner3, f->gz3,
+                   f->mont3, f->heat3, f->pv3, f->ri2, f->div_uv3, f->w3, f->dzdt3, f->u_spinup};
+  const double *src[] = {d.hdry, d.theta, d.p3, d.h3, d.p2, d.theta2, d.t2, d.t3, d.rho2, d.rho3, d.exner3, d.gz3,
+                         d.mont3, d.heat3, d.pv3, d.ri2, d.div_uv3, d.w3, d.dzdt3, d.u_spinup};
+  for (int i = 0; i < 20; i++)
+    if (dst[i]) EPIC_CUDA_CHECK(cudaMemcpyAsync(dst[i], src[i], b3, cudaMemcpyDeviceToHost, s));
+  if (f->gz_surface) EPIC_CUDA_CHECK(cudaMemcpyAsync(f->gz_surface, d.gz_surface, (size_t)d.n2 * sizeof(double), cudaMemcpyDeviceToHost, s));
+  Ctl c;
+  int rc = read_ctl(m, c);
+  if (rc) return rc;
+  f->it_zero = c.it_zero; f->it_minus1 = c.it_minus1; f->it_minus2 = c.it_minus2;
+  f->itime = c.itime; f->model_time = c.model_time;
+  return model_error(c);
+}
+
+extern "C" int epic_model_step_host(epic_model *m, epic_fields *f, int32_t prime, int32_t nsteps) {
+  int rc = epic_model_upload(m, f);
+  if (rc) return rc;
+  if (prime) {
+    rc = epic_model_timestep(m, EPIC_SYNC_DIAGS_ONLY);
+    if (rc) return rc;
+  }
+  rc = epic_model_run(m, nsteps);
+  if (rc) return rc;
+  return epic_model_download(m, f);
+}
+
+extern "C" void *epic_model_stream(epic_model *m) { return m ? (void *)m->stream : nullptr; }
+
+extern "C" int64_t epic_model_device_bytes(const epic_model *m) { return m ? (int64_t)m->pool_bytes : 0; }

@@ -1,0 +1,777 @@
+// Horizontal stencil kernels and the time update.  Each kernel restates the reference routine
+// named in its comment; thread = one (k, j, i) cell unless stated otherwise.
+#include "device_common.cuh"
+#include "kernels.h"
+#include "epic_common.h"
+#include "epic_gb300.h"
+
+namespace epic {
+
+// Cell index helpers for 3-D launches over k in [k0, k0+nk), j in [j0, j0+nj), i in 1..ni.
+struct Cell { int k, j, i; };
+__device__ __forceinline__ bool cell3(const DevModel &M, int k0, int nkk, int j0, int njj, Cell &c) {
+  const long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  const long long tot = (long long)nkk * njj * M.ni;
+  if (t >= tot) return false;
+  c.i = 1 + (int)(t % M.ni);
+  const long long r = t / M.ni;
+  c.j = j0 + (int)(r % njj);
+  c.k = k0 + (int)(r / njj);
+  return true;
+}
+static inline unsigned cells_blocks(const DevModel &M, int nkk, int njj, int th) {
+  return epic_blocks((long long)nkk * njj * M.ni, th);
+}
+__device__ __forceinline__ int wrap_i(const DevModel &M, int i) { return i == 0 ? M.ni : (i == M.ni + 1 ? 1 : i); }
+
+// memset of DUDT, DVDT(it_uv_tend), epic_timestep.c:107-108
+__global__ void k_zero_tend(DevModel M) {
+  const long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= M.n3) return;
+  const long long off = plane_offset(M, PL_UV_TEND);
+  M.dudt[off + t] = 0.;
+  M.dvdt[off + t] = 0.;
+}
+
+// ---------------------------------------------------------------------------------------------
+// uv_core, epic_timestep.c:628-762, with get_kin (Suarez-Takacs blend for the Sadourney scheme,
+// epic_funcs_diag.c:2694-2847) and the PV averages of include/epic_pv_schemes.h:48-61.
+// ---------------------------------------------------------------------------------------------
+
+__device__ __forceinline__ double kin_at(const DevModel &M, const double *Uk, const double *Vk, int j, int i) {
+  const int jj = 2 * j;
+  double u2 = Uk[M.at2(j, i)], u4 = Uk[M.at2(j, i + 1)], v2 = Vk[M.at2(j, i)], v4 = Vk[M.at2(j + 1, i)];
+  const double kin_c = (u2 * u2 + u4 * u4 + M.mn[jj + 1] * (v2 * v2 * M.mn_inv[jj] + v4 * v4 * M.mn_inv[jj + 2])) * .25;
+  if (j == 0 || j == M.nj) return kin_c;
+  u2 = .5 * (Uk[M.at2(j + 1, i)] + Uk[M.at2(j - 1, i)]);
+  u4 = .5 * (Uk[M.at2(j + 1, i + 1)] + Uk[M.at2(j - 1, i + 1)]);
+  v2 = .5 * (Vk[M.at2(j, i + 1)] + Vk[M.at2(j, i - 1)]);
+  v4 = .5 * (Vk[M.at2(j + 1, i + 1)] + Vk[M.at2(j + 1, i - 1)]);
+  const double kin_s = (u2 * u2 + u4 * u4 + M.mn[jj + 1] * (v2 * v2 * M.mn_inv[jj] + v4 * v4 * M.mn_inv[jj + 2])) * .25;
+  return (5. / 6.) * kin_c + (1. / 6.) * kin_s;
+}
+// UH(j,i) for j = 0..nj (0 above), periodic in i
+__device__ __forceinline__ double uh_at(const DevModel &M, const double *Uk, const double *Hk, int j, int i) {
+  if (j < 0 || j > M.nj) return 0.;
+  i = wrap_i(M, i);
+  const double havg = .5 * (Hk[M.at2(j, i)] + Hk[M.at2(j, i - 1)]);
+  return Uk[M.at2(j, i)] * havg * (1. / M.n[2 * j + 1]);
+}
+// VH(j,i) for j = 1..nj (0 at the poles), periodic in i
+__device__ __forceinline__ double vh_at(const DevModel &M, const double *Vk, const double *Hk, int j, int i) {
+  if (j < 1 || j > M.nj) return 0.;
+  i = wrap_i(M, i);
+  const double havg = .5 * (Hk[M.at2(j, i)] + Hk[M.at2(j - 1, i)]);
+  return Vk[M.at2(j, i)] * havg * (1. / M.m[2 * j]);
+}
+
+// Kinetic energy per mass on the h grid, planes k = 1..nk-1, into work0 (with pads).
+__global__ void k_uv_kin(DevModel M) {
+  Cell c;
+  if (!cell3(M, 1, M.nk - 1, 0, M.nj + 1, c)) return;
+  const long long off = plane_offset(M, PL_UV);
+  const double *Uk = M.u + off + c.k * M.n2, *Vk = M.v + off + c.k * M.n2;
+  write_with_pads(M.work0, M, M.at(c.k, c.j, 0), c.i, kin_at(M, Uk, Vk, c.j, c.i));
+}
+
+// DVDT += (PV*UH terms + KIN(j-1)-KIN(j))*n, then the vertical advection of V.
+__global__ void k_uv_core_v(DevModel M) {
+  Cell c;
+  if (!cell3(M, 1, M.nk - 1, 1, M.nj, c)) return;
+  const int k = c.k, j = c.j, i = c.i;
+  const long long off = plane_offset(M, PL_UV);
+  const double *U = M.u + off, *V = M.v + off;
+  const double *Uk = U + k * M.n2, *Hk = M.h3 + k * M.n2;
+  const double *PV = M.pv3 + k * M.n2, *KIN = M.work0 + k * M.n2;
+  double *D = M.dvdt + plane_offset(M, PL_UV_TEND);
+  auto pv = [&](int jj, int ii) { return PV[M.at2(jj, ii)]; };
+  const double ga = (pv(j, i) + pv(j, i + 1) + pv(j + 1, i + 1));
+  const double de = (pv(j, i) + pv(j + 1, i) + pv(j, i + 1));
+  const double al = (pv(j - 1, i) + pv(j, i) + pv(j, i + 1));
+  const double be = (pv(j, i) + pv(j, i + 1) + pv(j - 1, i + 1));
+  const double core = ((-ga * uh_at(M, Uk, Hk, j, i + 1) - de * uh_at(M, Uk, Hk, j, i) - al * uh_at(M, Uk, Hk, j - 1, i) -
+                        be * uh_at(M, Uk, Hk, j - 1, i + 1)) * (1. / 12.) +
+                       KIN[M.at2(j - 1, i)] - KIN[M.at2(j, i)]) * M.n[2 * j];
+  const long long x = M.at(k, j, i);
+  double d = D[x] + core;
+  const int kk = 2 * k + 1;
+  d -= .5 * (M.w3[x] + M.w3[M.at(k, j - 1, i)]) * (V[M.at(k - 1, j, i)] - V[M.at(k + 1, j, i)]) / (M.sgth[kk - 2] - M.sgth[kk + 2]);
+  D[x] = d;
+}
+
+// DUDT += (PV*VH terms + KIN(i-1)-KIN(i))*m with the filtered KIN, then the vertical advection of U.
+__global__ void k_uv_core_u(DevModel M) {
+  Cell c;
+  if (!cell3(M, 1, M.nk - 1, 0, M.nj + 1, c)) return;
+  const int k = c.k, j = c.j, i = c.i;
+  const long long off = plane_offset(M, PL_UV);
+  const double *U = M.u + off, *V = M.v + off;
+  const double *Vk = V + k * M.n2, *Hk = M.h3 + k * M.n2;
+  const double *PV = M.pv3 + k * M.n2, *KIN = M.work0 + k * M.n2;
+  double *D = M.dudt + plane_offset(M, PL_UV_TEND);
+  auto pv = [&](int jj, int ii) { return PV[M.at2(jj, ii)]; };
+  const double al = (pv(j, i) + pv(j + 1, i) + pv(j + 1, i + 1));
+  const double be = (pv(j + 1, i - 1) + pv(j + 1, i) + pv(j, i));
+  const double ga = (pv(j, i - 1) + pv(j, i) + pv(j + 1, i));
+  const double de = (pv(j, i) + pv(j + 1, i) + pv(j, i + 1));
+  const double core = ((al * vh_at(M, Vk, Hk, j + 1, i) + be * vh_at(M, Vk, Hk, j + 1, i - 1) + ga * vh_at(M, Vk, Hk, j, i - 1) +
+                        de * vh_at(M, Vk, Hk, j, i)) * (1. / 12.) +
+                       KIN[M.at2(j, i - 1)] - KIN[M.at2(j, i)]) * M.m[2 * j + 1];
+  const long long x = M.at(k, j, i);
+  double d = D[x] + core;
+  const int kk = 2 * k + 1;
+  d -= .5 * (M.w3[x] + M.w3[M.at(k, j, i - 1)]) * (U[M.at(k - 1, j, i)] - U[M.at(k + 1, j, i)]) / (M.sgth[kk - 2] - M.sgth[kk + 2]);
+  D[x] = d;
+}
+
+// ---------------------------------------------------------------------------------------------
+// uv_pgrad_finite_volume, epic_timestep.c:909-1273
+// ---------------------------------------------------------------------------------------------
+
+// Pole boundary rows of GZ3 (zonal means of the adjacent row), epic_timestep.c:930-998.
+// One block per k; thread 0 sums in the reference order.
+__global__ void k_gz_pole_rows(DevModel M) {
+  const int k = blockIdx.x;
+  __shared__ double avg[2];
+  if (threadIdx.x < 2) {
+    const int j = threadIdx.x == 0 ? 0 : M.nj;
+    double tmp = 0.;
+    for (int i = 1; i <= M.ni; i++) tmp += M.gz3[M.at(k, j, i)];
+    avg[threadIdx.x] = tmp / M.ni;
+  }
+  __syncthreads();
+  for (int i = threadIdx.x; i <= M.ni + 1; i += blockDim.x) {
+    M.gz3[M.at(k, -1, i)] = avg[0];
+    M.gz3[M.at(k, M.nj + 1, i)] = avg[1];
+  }
+}
+
+struct LonFace { double zbse, zbne, ztse, ztne, zbe, zte, pbe, pte, east, ln; };
+
+// East face of the u control volume at column i (the quantities the reference carries
+// from one i to the next).
+__device__ __forceinline__ LonFace lon_face(const DevModel &M, int k, int j, int i) {
+  const double *G = M.gz3, *P = M.p2;
+  auto gz = [&](int kk, int jj, int ii) { return G[M.at(kk, jj, ii)]; };
+  LonFace f;
+  f.ln = M.lon[2 * i + 1] * (M_PI / 180.);
+  f.zbse = .25 * (gz(k, j, i) + gz(k, j - 1, i) + gz(k + 1, j, i) + gz(k + 1, j - 1, i));
+  f.zbne = .25 * (gz(k, j, i) + gz(k, j + 1, i) + gz(k + 1, j, i) + gz(k + 1, j + 1, i));
+  f.ztse = .25 * (gz(k, j, i) + gz(k, j - 1, i) + gz(k - 1, j, i) + gz(k - 1, j - 1, i));
+  f.ztne = .25 * (gz(k, j, i) + gz(k, j + 1, i) + gz(k - 1, j, i) + gz(k - 1, j + 1, i));
+  f.zbe = .5 * (gz(k, j, i) + gz(k + 1, j, i));
+  f.zte = .5 * (gz(k, j, i) + gz(k - 1, j, i));
+  f.pbe = P[M.at(k + 1, j, i)];
+  f.pte = P[M.at(k, j, i)];
+  const double a1 = f.ztne + f.ztse, b1 = f.ztne * f.ztse, a2 = f.zbne + f.zbse, b2 = f.zbne * f.zbse;
+  const double terms1 = a1 * a1 - b1 - (a2 * a2 - b2);
+  const double terms2 = 3. * (a1 - a2);
+  f.east = (-terms1 * (f.pbe - f.pte) + terms2 * (f.zte * f.pbe - f.zbe * f.pte)) / (f.zte - f.zbe);
+  return f;
+}
+
+__global__ void k_pgrad_lon(DevModel M) {
+  Cell c;
+  if (!cell3(M, 1, M.nk - 1, 0, M.nj + 1, c)) return;
+  const int k = c.k, j = c.j, i = c.i;
+  const double DLOGZ_TOL = 1.e-2;
+  const LonFace w = lon_face(M, k, j, i - 1), e = lon_face(M, k, j, i);
+  const double rho = .5 * (M.rho3[M.at(k, j, i)] + M.rho3[M.at(k, j, i - 1)]);
+  const double rlns = M.rln[2 * j], rlnn = M.rln[2 * j + 2];
+  double a1 = e.ztne + e.ztse, a2 = w.ztne + w.ztse;
+  double terms2 = 3. * (a1 - a2), top, bottom;
+  if (fabs(2. * (e.zte - w.zte) / (e.zte + w.zte - e.zbe - w.zbe)) > DLOGZ_TOL) {
+    const double b1 = e.ztne * e.ztse, b2 = w.ztne * w.ztse;
+    const double terms1 = a1 * a1 - b1 - (a2 * a2 - b2);
+    top = (-terms1 * (w.pte - e.pte) + terms2 * (e.zte * w.pte - w.zte * e.pte)) / (e.zte - w.zte);
+  } else {
+    top = .5 * (w.pte + e.pte) * terms2;
+  }
+  a1 = e.zbne + e.zbse;
+  a2 = w.zbne + w.zbse;
+  terms2 = 3. * (a1 - a2);
+  if (fabs(2. * (e.zbe - w.zbe) / (e.zte + w.zte - e.zbe - w.zbe)) > DLOGZ_TOL) {
+    const double b1 = e.zbne * e.zbse, b2 = w.zbne * w.zbse;
+    const double terms1 = a1 * a1 - b1 - (a2 * a2 - b2);
+    bottom = (-terms1 * (w.pbe - e.pbe) + terms2 * (e.zbe * w.pbe - w.zbe * e.pbe)) / (e.zbe - w.zbe);
+  } else {
+    bottom = .5 * (w.pbe + e.pbe) * terms2;
+  }
+  double pgflon = top - bottom + 0. - 0. + w.east - e.east;
+  const double dzn = e.ztne - e.zbne + w.ztne - w.zbne;
+  const double dzs = e.ztse - e.zbse + w.ztse - w.zbse;
+  pgflon /= (e.ln - w.ln) * rho * (rlns * (dzs + .5 * dzn) + rlnn * (dzn + .5 * dzs));
+  M.dudt[plane_offset(M, PL_UV_TEND) + M.at(k, j, i)] += pgflon;
+}
+
+struct LatFace { double zbnw, zbne, ztnw, ztne, zbn, ztn, pbn, ptn, north, rln, lt; };
+
+// North face of the v control volume at row j.
+__device__ __forceinline__ LatFace lat_face(const DevModel &M, int k, int j, int i) {
+  const double *G = M.gz3, *P = M.p2;
+  auto gz = [&](int kk, int jj, int ii) { return G[M.at(kk, jj, ii)]; };
+  LatFace f;
+  f.rln = M.rln[2 * j + 1];
+  f.lt = M.lat[2 * j + 1] * (M_PI / 180.);
+  f.zbnw = .25 * (gz(k, j, i) + gz(k, j, i - 1) + gz(k + 1, j, i) + gz(k + 1, j, i - 1));
+  f.zbne = .25 * (gz(k, j, i) + gz(k, j, i + 1) + gz(k + 1, j, i) + gz(k + 1, j, i + 1));
+  f.ztnw = .25 * (gz(k, j, i) + gz(k, j, i - 1) + gz(k - 1, j, i) + gz(k - 1, j, i - 1));
+  f.ztne = .25 * (gz(k, j, i) + gz(k, j, i + 1) + gz(k - 1, j, i) + gz(k - 1, j, i + 1));
+  f.zbn = .5 * (gz(k, j, i) + gz(k + 1, j, i));
+  f.ztn = .5 * (gz(k, j, i) + gz(k - 1, j, i));
+  f.pbn = P[M.at(k + 1, j, i)];
+  f.ptn = P[M.at(k, j, i)];
+  const double a1 = f.ztne + f.ztnw, b1 = f.ztne * f.ztnw, a2 = f.zbne + f.zbnw, b2 = f.zbne * f.zbnw;
+  const double terms1 = a1 * a1 - b1 - (a2 * a2 - b2);
+  const double terms2 = 3. * (a1 - a2);
+  f.north = f.rln * (-terms1 * (f.pbn - f.ptn) + terms2 * (f.ztn * f.pbn - f.zbn * f.ptn)) / (f.ztn - f.zbn);
+  return f;
+}
+
+__global__ void k_pgrad_lat(DevModel M) {
+  Cell c;
+  if (!cell3(M, 1, M.nk - 1, 1, M.nj, c)) return;
+  const int k = c.k, j = c.j, i = c.i;
+  const double DLOGZ_TOL = 1.e-2;
+  const LatFace s = lat_face(M, k, j - 1, i), n = lat_face(M, k, j, i);
+  const double *G = M.gz3, *P = M.p2;
+  auto gz = [&](int kk, int jj, int ii) { return G[M.at(kk, jj, ii)]; };
+  auto pp = [&](int kk, int jj, int ii) { return P[M.at(kk, jj, ii)]; };
+  const double rho = .5 * (M.rho3[M.at(k, j, i)] + M.rho3[M.at(k, j - 1, i)]);
+  const double rlt = M.rlt[2 * j];
+  const double rlns = s.rln, rlnn = n.rln;
+  const double south = s.north, north = n.north;
+  // s-face values carried over from row j-1: zbsw = zbnw(j-1), zbse = zbne(j-1), ...
+  const double zbsw = s.zbnw, zbse = s.zbne, ztsw = s.ztnw, ztse = s.ztne;
+  const double zbs = s.zbn, zts = s.ztn, pbs = s.pbn, pts = s.ptn;
+  double a1, a2, b1, b2, b3, terms1, terms2;
+  const double zbe = .125 * (gz(k, j, i) + gz(k, j, i + 1) + gz(k, j - 1, i) + gz(k, j - 1, i + 1) + gz(k + 1, j, i) +
+                             gz(k + 1, j, i + 1) + gz(k + 1, j - 1, i) + gz(k + 1, j - 1, i + 1));
+  const double zte = .125 * (gz(k - 1, j, i) + gz(k - 1, j, i + 1) + gz(k - 1, j - 1, i) + gz(k - 1, j - 1, i + 1) + gz(k, j, i) +
+                             gz(k, j, i + 1) + gz(k, j - 1, i) + gz(k, j - 1, i + 1));
+  const double pbe = .25 * (pp(k + 1, j, i) + pp(k + 1, j, i + 1) + pp(k + 1, j - 1, i) + pp(k + 1, j - 1, i + 1));
+  const double pte = .25 * (pp(k, j, i) + pp(k, j, i + 1) + pp(k, j - 1, i) + pp(k, j - 1, i + 1));
+  a1 = n.ztne + ztse; b1 = n.ztne * ztse; a2 = n.zbne + zbse; b2 = n.zbne * zbse;
+  terms1 = a1 * a1 - b1 - (a2 * a2 - b2);
+  terms2 = 3. * (a1 - a2);
+  const double east = .5 * (rlns - rlnn) * (-terms1 * (pbe - pte) + terms2 * (zte * pbe - zbe * pte)) / (zte - zbe);
+  const double zbw = .125 * (gz(k, j, i) + gz(k, j, i - 1) + gz(k, j - 1, i) + gz(k, j - 1, i - 1) + gz(k + 1, j, i) +
+                             gz(k + 1, j, i - 1) + gz(k + 1, j - 1, i) + gz(k + 1, j - 1, i - 1));
+  const double ztw = .125 * (gz(k - 1, j, i) + gz(k - 1, j, i - 1) + gz(k - 1, j - 1, i) + gz(k - 1, j - 1, i - 1) + gz(k, j, i) +
+                             gz(k, j, i - 1) + gz(k, j - 1, i) + gz(k, j - 1, i - 1));
+  const double pbw = .25 * (pp(k + 1, j, i) + pp(k + 1, j, i - 1) + pp(k + 1, j - 1, i) + pp(k + 1, j - 1, i - 1));
+  const double ptw = .25 * (pp(k, j, i) + pp(k, j, i - 1) + pp(k, j - 1, i) + pp(k, j - 1, i - 1));
+  a1 = n.ztnw + ztsw; b1 = n.ztnw * ztsw; a2 = n.zbnw + zbsw; b2 = n.zbnw * zbsw;
+  terms1 = a1 * a1 - b1 - (a2 * a2 - b2);
+  terms2 = 3. * (a1 - a2);
+  const double west = .5 * (rlns - rlnn) * (-terms1 * (pbw - ptw) + terms2 * (ztw * pbw - zbw * ptw)) / (ztw - zbw);
+  double top, bottom;
+  a1 = n.ztne + n.ztnw; a2 = ztse + ztsw;
+  terms2 = 3. * (a1 - a2);
+  if (fabs(2. * (n.ztn - zts) / (n.ztn + zts - n.zbn - zbs)) > DLOGZ_TOL) {
+    b1 = n.ztne * n.ztnw; b2 = ztse * ztsw; b3 = n.ztne * ztse + n.ztnw * ztsw;
+    terms1 = a1 * a1 - b1 - (a2 * a2 - b2);
+    top = .5 * ((n.ptn - pts) * ((rlnn + rlns) * terms1 + (rlnn - rlns) * (b1 + b2 - b3)) + (rlnn + rlns) * terms2 * (n.ztn * pts - zts * n.ptn)) /
+          (n.ztn - zts);
+  } else {
+    top = .25 * (rlnn + rlns) * (pts + n.ptn) * terms2;
+  }
+  a1 = n.zbne + n.zbnw; a2 = zbse + zbsw;
+  terms2 = 3. * (a1 - a2);
+  if (fabs(2. * (n.zbn - zbs) / (n.ztn + zts - n.zbn - zbs)) > DLOGZ_TOL) {
+    b1 = n.zbne * n.zbnw; b2 = zbse * zbsw; b3 = n.zbne * zbse + n.zbnw * zbsw;
+    terms1 = a1 * a1 - b1 - (a2 * a2 - b2);
+    bottom = .5 * ((n.pbn - pbs) * ((rlnn + rlns) * terms1 + (rlnn - rlns) * (b1 + b2 - b3)) + (rlnn + rlns) * terms2 * (n.zbn * pbs - zbs * n.pbn)) /
+             (n.zbn - zbs);
+  } else {
+    bottom = .25 * (rlnn + rlns) * (pbs + n.pbn) * terms2;
+  }
+  double pgflat = top - bottom + south - (north + west + east);
+  const double dzn = n.ztne - n.zbne + n.ztnw - n.zbnw;
+  const double dzs = ztse - zbse + ztsw - zbsw;
+  pgflat /= (n.lt - s.lt) * rho * rlt * (rlns * (dzs + .5 * dzn) + rlnn * (dzn + .5 * dzs));
+  M.dvdt[plane_offset(M, PL_UV_TEND) + M.at(k, j, i)] += pgflat;
+}
+
+// ---------------------------------------------------------------------------------------------
+// Meridional pass of hsu_advection, epic_flux.c:1060-1310.  kind: 0/1 interface (unity,
+// THETA), 2 = HDRY (v averaged to the layer).  Four launches over all planes k0..nk.
+// ---------------------------------------------------------------------------------------------
+
+__device__ __forceinline__ void vmp(const DevModel &M, const double *V, int kind, int k, int j, int i, double &vm, double &vp) {
+  double v2d;
+  if (j < 0 || j > M.nj + 1) { vm = vp = 0.; return; }
+  if (kind == 2) v2d = (j >= 1 && j <= M.nj) ? .5 * (V[M.at(k, j, i)] + V[M.at(k - 1, j, i)]) : 0.;
+  else v2d = V[M.at(k, j, i)];
+  const double mi = (fabs(M.lat[2 * j]) == 90.) ? 0. : 1. / M.m[2 * j];
+  vm = dminr(0., v2d * mi);
+  vp = dmaxr(0., v2d * mi);
+}
+
+__global__ void k_hsu_merid_pred(DevModel M, const double *A, int kind, int k0) {
+  Cell c;
+  if (!cell3(M, k0, M.nk - k0 + 1, 0, M.nj + 2, c)) return;   // rows 0..nj+1
+  const double *V = M.v + plane_offset(M, PL_UV);
+  double ff = 0.;
+  if (c.j >= 1 && c.j <= M.nj) {
+    double vm, vp;
+    vmp(M, V, kind, c.k, c.j, c.i, vm, vp);
+    ff = vp * A[M.at(c.k, c.j - 1, c.i)] + vm * A[M.at(c.k, c.j, c.i)];
+  }
+  write_with_pads(M.work1, M, M.at(c.k, c.j, 0), c.i, ff);
+}
+
+__global__ void k_hsu_merid_apred(DevModel M, const double *A, int k0) {
+  Cell c;
+  if (!cell3(M, k0, M.nk - k0 + 1, 0, M.nj + 1, c)) return;
+  const double *FF = M.work1;
+  const long long x = M.at(c.k, c.j, c.i);
+  const double da = (FF[x] - FF[M.at(c.k, c.j + 1, c.i)]) * M.mn[2 * c.j + 1] * M.dt;
+  write_with_pads(M.work2, M, M.at(c.k, c.j, 0), c.i, A[x] + da);
+}
+
+__global__ void k_hsu_merid_corr(DevModel M, const double *A, int kind, int k0) {
+  Cell c;
+  if (!cell3(M, k0, M.nk - k0 + 1, 0, M.nj + 2, c)) return;
+  const int k = c.k, j = c.j, i = c.i, nj = M.nj;
+  double ffv = 0.;
+  if (j >= 1 && j <= nj) {
+    const double ep = 1.e-10, DT = M.dt;
+    const double a_min = kind == 2 ? M.h_min[k] : 0.;
+    const double *V = M.v + plane_offset(M, PL_UV);
+    const double *AP = M.work2;
+    auto a = [&](int jj) { return A[M.at(k, jj, i)]; };
+    auto ap = [&](int jj) { return AP[M.at(k, jj, i)]; };
+    auto diff1 = [&](int jj) { return jj == 0 ? 0. : ap(jj) - a(jj - 1); };
+    auto diff2 = [&](int jj) { return jj == nj ? 0. : ap(jj) - a(jj + 1); };
+    auto aaa = [&](int jj) {
+      double t;
+      if (jj == 0) t = fabs(-a(0) + a(1)) + ep;
+      else if (jj == nj) t = fabs(a(nj - 1) - a(nj)) + ep;
+      else t = fabs(a(jj - 1) - 2. * a(jj) + a(jj + 1)) + ep;
+      return t * t;
+    };
+    double vm, vp, vmm, vpm, vmp1, vpp1;
+    vmp(M, V, kind, k, j, i, vm, vp);
+    vmp(M, V, kind, k, j - 1, i, vmm, vpm);
+    vmp(M, V, kind, k, j + 1, i, vmp1, vpp1);
+    ffv = .5 * (vp * (ap(j) + a(j - 1)) + vm * (ap(j - 1) + a(j)));
+    const double vhatp = sqrt(vp * vpm);
+    const double vhatm = -sqrt(vm * vmp1);
+    const double mu = (vp - vm) * M.mn[2 * j] * DT;
+    const double al = (1. + mu) / 6.;
+    const double am1 = aaa(j - 1), a0 = aaa(j);
+    const double prod = (a(j - 1) - a_min) * (a(j) - a_min);
+    double gap = am1 / (am1 + prod); gap = gap * gap;
+    double gam = a0 / (a0 + prod); gam = gam * gam;
+    const double bep = 1. + (1. / (2. * al) - 1.) * gap;
+    const double bem = 1. + (1. / (2. * al) - 1.) * gam;
+    ffv += -al * (vp * bep * diff1(j) - vhatp * (1. - gap) * diff1(j - 1) + vm * bem * diff2(j - 1) - vhatm * (1. - gam) * diff2(j));
+  }
+  write_with_pads(M.work3, M, M.at(k, j, 0), i, ffv);
+}
+
+__global__ void k_hsu_merid_update(DevModel M, double *A, int k0) {
+  Cell c;
+  if (!cell3(M, k0, M.nk - k0 + 1, 0, M.nj + 1, c)) return;
+  const double *FF = M.work3;
+  const long long x = M.at(c.k, c.j, c.i);
+  const double da = (FF[x] - FF[M.at(c.k, c.j + 1, c.i)]) * M.mn[2 * c.j + 1] * M.dt;
+  write_with_pads(A, M, M.at(c.k, c.j, 0), c.i, A[x] + da);
+}
+
+// ---------------------------------------------------------------------------------------------
+// Hyperviscosity, epic_subgrid.c:590-1232
+// ---------------------------------------------------------------------------------------------
+
+// d2dy2 of planes k0..k1 of src into dst (coefficients per row from the init block, :1049-1141).
+__global__ void k_d2dy2(DevModel M, const double *src, int src_sel, double *dst, int vgrid, double diff_coef, int k0, int nkk) {
+  Cell c;
+  const int nrows = vgrid ? M.nj + 2 : M.nj + 1;   // v: j = 0..nj+1, h: j = 0..nj
+  if (!cell3(M, k0, nkk, 0, nrows, c)) return;
+  src += plane_offset(M, src_sel);
+  const int k = c.k, j = c.j, i = c.i, nj = M.nj;
+  const double *cf = (vgrid ? M.v_coef : M.h_coef) + 3 * j;
+  const double a0 = diff_coef * cf[0], a1 = diff_coef * cf[1], a2 = diff_coef * cf[2];
+  auto h = [&](int jj) { return src[M.at(k, jj, i)]; };
+  double d;
+  const int jlast = vgrid ? nj + 1 : nj;
+  if (j == 0) d = a0 * h(0) + a1 * h(1) + a2 * h(2);
+  else if (j == jlast) d = a0 * h(j - 2) + a1 * h(j - 1) + a2 * h(j);
+  else d = a0 * h(j - 1) + a1 * h(j) + a2 * h(j + 1);
+  write_with_pads(dst, M, M.at(k, j, 0), i, d);
+}
+
+// A += dt*sign*D over the rows the reference updates (v: 1..nj, h: 0..nj).
+__global__ void k_visc_apply(DevModel M, double *A, int sel, const double *D, int vgrid, double sign, int k0, int nkk) {
+  Cell c;
+  if (!cell3(M, k0, nkk, vgrid ? 1 : 0, vgrid ? M.nj : M.nj + 1, c)) return;
+  A += plane_offset(M, sel);
+  const long long x = M.at(c.k, c.j, c.i);
+  write_with_pads(A, M, M.at(c.k, c.j, 0), c.i, A[x] + M.dt * sign * D[x]);
+}
+
+// zonal_hyperviscosity for one row (block), epic_subgrid.c:715-808.
+__global__ void k_zonal_visc(DevModel M, double *A, int sel, int jbot, int jhalf, int k0) {
+  extern __shared__ double sm[];
+  const int ni = M.ni;
+  const int j = jbot + (int)blockIdx.x;
+  const int k = k0 + (int)blockIdx.y;
+  A += plane_offset(M, sel);
+  const long long base = M.at(k, j, 0);
+  double *a = sm, *hh = a + (ni + 2), *d = hh + (ni + 2);
+  __shared__ double mean;
+  for (int i = threadIdx.x; i <= ni + 1; i += blockDim.x) { a[i] = A[base + i]; hh[i] = a[i]; }
+  __syncthreads();
+  const bool taper = fabs(M.lat[2 * j + jhalf]) > M.lat0;
+  const double mm = M.m[2 * j + jhalf];
+  double sign = 1.;
+  bool any_applied = false;
+  for (int itmp = 2; itmp <= 8; itmp += 2) {
+    const double dc = taper ? M.coef[itmp] * M.m0 * M.m0 : M.coef[itmp] * mm * mm;
+    for (int i = threadIdx.x + 1; i <= ni; i += blockDim.x) d[i] = dc * (hh[i - 1] - 2. * hh[i] + hh[i + 1]);
+    __syncthreads();
+    if (threadIdx.x == 0) {
+      d[ni + 1] = d[1];
+      d[0] = d[ni];
+      double fm = 0.;
+      for (int i = 1; i <= ni; i++) fm += d[i];
+      mean = fm / ni;
+    }
+    __syncthreads();
+    for (int i = threadIdx.x; i <= ni + 1; i += blockDim.x) d[i] -= mean;
+    __syncthreads();
+    if (M.nu[itmp] > 0.) {
+      for (int i = threadIdx.x + 1; i <= ni; i += blockDim.x) a[i] += M.dt * sign * d[i];
+      any_applied = true;
+    }
+    sign = -sign;
+    double rest = 0.;
+    for (int q = itmp + 2; q <= 8; q += 2) rest += M.nu[q];
+    if (!(rest > 0.)) break;
+    for (int i = threadIdx.x; i <= ni + 1; i += blockDim.x) hh[i] = d[i];   // swap roles
+    __syncthreads();
+  }
+  __syncthreads();
+  if (any_applied)
+    for (int i = threadIdx.x + 1; i <= ni; i += blockDim.x) write_with_pads(A, M, base, i, a[i]);
+}
+
+// ---------------------------------------------------------------------------------------------
+// divergence, vorticity, store_diag (epic_funcs_diag.c:3963-4445) and the Richardson number
+// ---------------------------------------------------------------------------------------------
+
+// DIV(j,i) of (UU, VV) on planes k0.., divergence() :4064-4117
+__device__ __forceinline__ double div_at(const DevModel &M, const double *UU, const double *VV, int k, int j, int i) {
+  const int jj = 2 * j + 1;
+  const double n_inv = 1. / M.n[jj];
+  const double mn1 = M.mn[jj];
+  const double m2j_inv = (j == 0) ? 0. : 1. / M.m[jj - 1];
+  const double m2jp2_inv = (j == M.nj) ? 0. : 1. / M.m[jj + 1];
+  return mn1 * ((UU[M.at(k, j, i + 1)] * n_inv - UU[M.at(k, j, i)] * n_inv) + (VV[M.at(k, j + 1, i)] * m2jp2_inv - VV[M.at(k, j, i)] * m2j_inv));
+}
+
+__global__ void k_divergence(DevModel M, const double *UU, const double *VV, int vsel, double *DI, int k0, int nkk) {
+  Cell c;
+  if (!cell3(M, k0, nkk, 0, M.nj + 1, c)) return;
+  VV += plane_offset(M, vsel);
+  write_with_pads(DI, M, M.at(c.k, c.j, 0), c.i, div_at(M, UU, VV, c.k, c.j, c.i));
+}
+
+// Interior potential vorticity, vorticity(ON_SIGMATHETA, POTENTIAL) :4168-4186, planes 0..nk.
+__global__ void k_pv_interior(DevModel M, const double *VV) {
+  Cell c;
+  if (!cell3(M, 0, M.nk + 1, 1, M.nj, c)) return;
+  const int k = c.k, j = c.j, i = c.i;
+  const double *UU = M.u + plane_offset(M, PL_UV);
+  const double *HH = M.h3;
+  const double f2j = M.f[2 * j], m2j = M.m[2 * j], n2j = M.n[2 * j];
+  const double m_m1_inv = 1. / M.m[2 * j - 1], m_p1_inv = 1. / M.m[2 * j + 1];
+  const double mn_m1_inv = 1. / M.mn[2 * j - 1], mn_p1_inv = 1. / M.mn[2 * j + 1];
+  const double mn_pv = .5 / (mn_m1_inv + mn_p1_inv);
+  const double ze = m2j * ((VV[M.at(k, j, i)] - VV[M.at(k, j, i - 1)]) +
+                           n2j * (UU[M.at(k, j - 1, i)] * m_m1_inv - UU[M.at(k, j, i)] * m_p1_inv));
+  double pv = (ze + f2j);
+  const double h_pv = ((HH[M.at(k, j, i)] + HH[M.at(k, j, i - 1)]) * mn_p1_inv + (HH[M.at(k, j - 1, i)] + HH[M.at(k, j - 1, i - 1)]) * mn_m1_inv) * mn_pv;
+  pv /= h_pv;
+  write_with_pads(M.pv3, M, M.at(k, j, 0), i, pv);
+}
+
+// Polar potential vorticity from the circulation of the adjacent u row, :4279-4341.
+// One block per plane; thread 0 forms the sums in the reference order.
+__global__ void k_pv_poles(DevModel M) {
+  const int k = blockIdx.x;
+  const double *UU = M.u + plane_offset(M, PL_UV);
+  const double *HH = M.h3;
+  __shared__ double pole[2];
+  if (threadIdx.x == 0) {
+    double ze = 0., h = 0.;
+    for (int i = 1; i <= M.ni; i++) ze -= UU[M.at(k, 0, i)];
+    ze *= M.mn[0] / ((M.m[1]) * (double)(M.ni));
+    for (int i = 1; i <= M.ni; i++) h += HH[M.at(k, 0, i)];
+    h /= (double)(M.ni);
+    pole[0] = (ze + M.f[0]) / h;
+    const int J = M.nj;
+    ze = 0.; h = 0.;
+    for (int i = 1; i <= M.ni; i++) ze += UU[M.at(k, J, i)];
+    ze *= M.mn[2 * (J + 1)] / (M.m[2 * J + 1] * (double)(M.ni));
+    for (int i = 1; i <= M.ni; i++) h += HH[M.at(k, J, i)];
+    h /= (double)(M.ni);
+    pole[1] = (ze + M.f[2 * (J + 1)]) / h;
+  }
+  __syncthreads();
+  for (int i = threadIdx.x; i <= M.ni + 1; i += blockDim.x) {
+    M.pv3[M.at(k, 0, i)] = pole[0];
+    M.pv3[M.at(k, M.nj + 1, i)] = pole[1];
+  }
+}
+
+// Richardson number in the layers, get_richardson/get_brunt2 (:2885-3156).  The V term of
+// dvdz2 keeps the reference's sign slip (:3127-3128); only dudz2 decides the 1e6 branch.
+__global__ void k_ri2(DevModel M) {
+  Cell c;
+  if (!cell3(M, 1, M.nk, 0, M.nj + 1, c)) return;
+  const int k = c.k, j = c.j, i = c.i;
+  const long long off = plane_offset(M, PL_UV);
+  const double *U = M.u + off, *V = M.v + off;
+  double dudz2 = .5 * (U[M.at(k - 1, j, i)] + U[M.at(k - 1, j, i + 1)] - U[M.at(k, j, i)] - U[M.at(k, j, i + 1)]);
+  double dvdz2 = .5 * (V[M.at(k - 1, j, i)] + V[M.at(k - 1, j + 1, i)] - V[M.at(k, j, i)] + V[M.at(k, j + 1, i)]);
+  dudz2 *= dudz2;
+  dvdz2 *= dvdz2;
+  double ri;
+  if (fcmp(dudz2, 0.) != 0) {
+    const long long x = M.at(k, j, i);
+    const double pressure = M.p2[x], temperature = M.t2[x], density = M.rho2[x];
+    const double cp = 1004., mu = M.mu_dry;
+    const double deltap = 0.001 * pressure, deltaT = 0.001 * temperature;
+    const double drho_dp_T = (return_density(pressure + deltap, temperature, mu) - return_density(pressure - deltap, temperature, mu)) / (2. * deltap);
+    const double drho_dT_p = (return_density(pressure, temperature + deltaT, mu) - return_density(pressure, temperature - deltaT, mu)) / (2. * deltaT);
+    const double Drho_Dp = (M.rho3[x] - M.rho3[M.at(k - 1, j, i)]) / (M.p3[x] - M.p3[M.at(k - 1, j, i)]);
+    const double g = M.grav[2 * j + 1];
+    const double brunt2 = g * g * (Drho_Dp - drho_dp_T + temperature / (cp * density * density) * drho_dT_p * drho_dT_p);
+    ri = brunt2 / (dudz2 + dvdz2);
+  } else {
+    ri = 1.e+6;
+  }
+  write_with_pads(M.ri2, M, M.at(k, j, 0), i, ri);
+}
+
+// divergence_damping apply step, epic_subgrid.c:1857-1881 (DIV from k_divergence in work2).
+__global__ void k_divdamp_apply(DevModel M, double nudiv) {
+  const long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  const long long per = (long long)(M.nk - 1) * (M.nj + 1) * M.ni;
+  if (t >= 2 * per) return;
+  const int isv = t >= per;
+  const long long r = isv ? t - per : t;
+  const int i = 1 + (int)(r % M.ni);
+  const int j = (int)((r / M.ni) % (M.nj + 1));
+  const int k = 1 + (int)(r / ((long long)M.ni * (M.nj + 1)));
+  const double *DIV = M.work2;
+  const long long off = plane_offset(M, PL_UV_TEND);
+  if (!isv) {
+    const double coef = (M.lat[2 * j + 1] > M.lat0) ? nudiv * M.m0 : nudiv * M.m[2 * j + 1];
+    M.dudt[off + M.at(k, j, i)] += coef * (DIV[M.at(k, j, i)] - DIV[M.at(k, j, i - 1)]);
+  } else if (j >= 1) {
+    const double coef = nudiv * M.n[2 * j];
+    M.dvdt[off + M.at(k, j, i)] += coef * (DIV[M.at(k, j, i)] - DIV[M.at(k, j - 1, i)]);
+  }
+}
+
+// ---------------------------------------------------------------------------------------------
+// Time update: adams_bashforth_step / leapfrog_step (epic_timestep.c:406-615), the index
+// rotation (:257-274) and timeplane_bookkeeping (epic_funcs_diag.c:7086-7124).
+// ---------------------------------------------------------------------------------------------
+
+__global__ void k_uv_decide(DevModel M) {
+  Ctl *c = M.ctl;
+  for (int w = 0; w < 2; w++) {
+    const double *val = w == 0 ? M.u : M.v, *ten = w == 0 ? M.dudt : M.dvdt;
+    const int jlo = w == 0 ? 0 : 1;
+    const long long cell = M.at(1, jlo, 1);
+    if (M.uv_scheme == EPIC_UV_AB3) {
+      double *ab = c->ab[w];
+      if (ten[(long long)c->it_minus2 * M.n3 + cell] == DBL_MAX) {
+        if (ten[(long long)c->it_minus1 * M.n3 + cell] == DBL_MAX) { ab[0] = 1.; ab[1] = 0.; ab[2] = 0.; }
+        else { ab[0] = 3. / 2.; ab[1] = -1. / 2.; ab[2] = 0.; }
+      } else { ab[0] = 23. / 12.; ab[1] = -16. / 12.; ab[2] = 5. / 12.; }
+    } else {
+      c->lf_first[w] = val[(long long)c->it_minus1 * M.n3 + cell] == DBL_MAX;
+    }
+  }
+}
+
+__global__ void k_uv_update(DevModel M) {
+  const long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  const long long per = (long long)(M.nk - 1) * (M.nj + 1) * M.ni;
+  if (t >= 2 * per) return;
+  const int w = t >= per;
+  const long long r = w ? t - per : t;
+  const int i = 1 + (int)(r % M.ni);
+  const int j = (int)((r / M.ni) % (M.nj + 1));
+  const int k = 1 + (int)(r / ((long long)M.ni * (M.nj + 1)));
+  if (w == 1 && j == 0) return;   // v is updated for j = 1..nj
+  const Ctl *c = M.ctl;
+  double *val = w == 0 ? M.u : M.v;
+  const double *ten = w == 0 ? M.dudt : M.dvdt;
+  const long long x = M.at(k, j, i), base = M.at(k, j, 0);
+  const double DT = M.dt;
+  if (M.uv_scheme == EPIC_UV_AB3) {
+    const double *ab = c->ab[w];
+    double *X = val + (long long)c->it_uv * M.n3;
+    const double v = X[x] + DT * (ab[0] * ten[(long long)c->it_zero * M.n3 + x] + ab[1] * ten[(long long)c->it_minus1 * M.n3 + x] +
+                                  ab[2] * ten[(long long)c->it_minus2 * M.n3 + x]);
+    write_with_pads(X, M, base, i, v);
+  } else {
+    double *X0 = val + (long long)c->it_zero * M.n3, *Xm1 = val + (long long)c->it_minus1 * M.n3;
+    const double d = ten[(long long)c->it_uv_tend * M.n3 + x];
+    if (c->lf_first[w]) {
+      write_with_pads(Xm1, M, base, i, X0[x] + DT * d);
+    } else {
+      const double old_filtered = Xm1[x], present = X0[x];
+      const double new_leap = old_filtered + 2. * DT * d;
+      write_with_pads(Xm1, M, base, i, new_leap);
+      write_with_pads(X0, M, base, i, present * (1. - 2. * 0.06) + 0.06 * (old_filtered + new_leap));
+    }
+  }
+}
+
+__global__ void k_uv_rotate(DevModel M) {
+  Ctl *c = M.ctl;
+  if (M.uv_scheme == EPIC_UV_AB3) {
+    const int itmp = c->it_minus2;
+    c->it_minus2 = c->it_minus1;
+    c->it_minus1 = c->it_zero;
+    c->it_zero = itmp;
+    c->it_uv = 0;
+    c->it_uv_dis = 0;
+    c->it_uv_tend = c->it_zero;
+  } else {
+    const int itmp = c->it_minus1;
+    c->it_minus1 = c->it_zero;
+    c->it_zero = itmp;
+    c->it_uv = c->it_zero;
+    c->it_uv_dis = (M.u[(long long)c->it_minus1 * M.n3 + M.at(1, 0, 1)] == DBL_MAX) ? c->it_zero : c->it_minus1;
+    c->it_uv_tend = 0;
+  }
+  c->model_time += (long long)M.dt;
+}
+
+__global__ void k_itime_advance(DevModel M) { M.ctl->itime += 1; }
+
+// ---- launchers ----
+
+int launch_zero_tend(const DevModel &M, cudaStream_t s) {
+  k_zero_tend<<<epic_blocks(M.n3, 256), 256, 0, s>>>(M);
+  return 0;
+}
+
+int launch_uv_core(const DevModel &M, cudaStream_t s) {
+  k_uv_kin<<<cells_blocks(M, M.nk - 1, M.nj + 1, 128), 128, 0, s>>>(M);
+  k_uv_core_v<<<cells_blocks(M, M.nk - 1, M.nj, 128), 128, 0, s>>>(M);
+  launch_filter_planes(M, M.work0, PL_NONE, M.work0, 1, M.nk - 1, 0, s);
+  k_uv_core_u<<<cells_blocks(M, M.nk - 1, M.nj + 1, 128), 128, 0, s>>>(M);
+  return 0;
+}
+
+int launch_uv_pgrad(const DevModel &M, cudaStream_t s) {
+  k_gz_pole_rows<<<M.nk + 1, 128, 0, s>>>(M);
+  k_pgrad_lon<<<cells_blocks(M, M.nk - 1, M.nj + 1, 128), 128, 0, s>>>(M);
+  k_pgrad_lat<<<cells_blocks(M, M.nk - 1, M.nj, 128), 128, 0, s>>>(M);
+  return 0;
+}
+
+int launch_hsu_meridional(const DevModel &M, double *buff, int kind, cudaStream_t s) {
+  const int k0 = kind == 1 ? M.k_sigma - 1 : 1;
+  const int nkk = M.nk - k0 + 1;
+  k_hsu_merid_pred<<<cells_blocks(M, nkk, M.nj + 2, 128), 128, 0, s>>>(M, buff, kind, k0);
+  k_hsu_merid_apred<<<cells_blocks(M, nkk, M.nj + 1, 128), 128, 0, s>>>(M, buff, k0);
+  k_hsu_merid_corr<<<cells_blocks(M, nkk, M.nj + 2, 128), 128, 0, s>>>(M, buff, kind, k0);
+  k_hsu_merid_update<<<cells_blocks(M, nkk, M.nj + 1, 128), 128, 0, s>>>(M, buff, k0);
+  return 0;
+}
+
+// index: 0 = U, 1 = V, 2 = HDRY, 3 = THETA
+static void visc_krange(const DevModel &M, int index, int &k0, int &k1) {
+  k0 = 1;
+  k1 = M.nk;
+  if (index == 0 || index == 1) k1 = M.nk - 1;
+  if (index == 3) k0 = M.k_sigma - 1;
+}
+
+int launch_meridional_hyperviscosity(const DevModel &M, int index, double *var, int sel, cudaStream_t s) {
+  double rest4 = M.nu[4] + M.nu[6] + M.nu[8];
+  if (!(rest4 > 0.)) return 0;
+  int k0, k1;
+  visc_krange(M, index, k0, k1);
+  const int nkk = k1 - k0 + 1;
+  const int vgrid = index == 1;
+  const int nrows = vgrid ? M.nj + 2 : M.nj + 1;
+  // The first second-derivative reads the (possibly time-plane selected) field itself; later
+  // ones ping-pong between two scratch volumes, as hh and d2dy2var do in the reference.
+  double *cur_src = var;
+  int src_sel = sel;
+  double *bufs[2] = {M.work1, M.work2};
+  int which = 0;
+  double sign = 1.;
+  for (int itmp = 2; itmp <= 8; itmp += 2) {
+    double *dst = bufs[which];
+    k_d2dy2<<<cells_blocks(M, nkk, nrows, 128), 128, 0, s>>>(M, cur_src, src_sel, dst, vgrid, M.coef[itmp], k0, nkk);
+    src_sel = PL_NONE;
+    if (M.nu[itmp] > 0.) {
+      launch_filter_planes(M, dst, PL_NONE, dst, k0, nkk, vgrid, s);
+      k_visc_apply<<<cells_blocks(M, nkk, vgrid ? M.nj : M.nj + 1, 128), 128, 0, s>>>(M, var, sel, dst, vgrid, sign, k0, nkk);
+    }
+    sign = -sign;
+    double rest = 0.;
+    for (int q = itmp + 2; q <= 8; q += 2) rest += M.nu[q];
+    if (!(rest > 0.)) break;
+    cur_src = dst;
+    which ^= 1;
+  }
+  return 0;
+}
+
+int launch_zonal_hyperviscosity(const DevModel &M, int index, double *var, int sel, cudaStream_t s) {
+  if (M.ni < 2 || !(M.nu[4] + M.nu[6] + M.nu[8] > 0.)) return 0;
+  int k0, k1;
+  visc_krange(M, index, k0, k1);
+  const int jbot = index == 1 ? 1 : 0, jhalf = index == 1 ? 0 : 1;
+  dim3 grid(M.nj - jbot + 1, k1 - k0 + 1);
+  const size_t smem = 3 * (size_t)(M.ni + 2) * sizeof(double);
+  k_zonal_visc<<<grid, M.ni >= 256 ? 128 : 64, smem, s>>>(M, var, sel, jbot, jhalf, k0);
+  return 0;
+}
+
+int launch_divergence_damping(const DevModel &M, cudaStream_t s) {
+  if (M.nudiv == 0.) return 0;
+  launch_filter_planes(M, M.u, PL_UV_DIS, M.work1, 1, M.nk - 1, 0, s);
+  k_divergence<<<cells_blocks(M, M.nk - 1, M.nj + 1, 128), 128, 0, s>>>(M, M.work1, M.v, PL_UV_DIS, M.work2, 1, M.nk - 1);
+  k_divdamp_apply<<<epic_blocks(2LL * (M.nk - 1) * (M.nj + 1) * M.ni, 128), 128, 0, s>>>(M, M.nudiv);
+  return 0;
+}
+
+int launch_uv_update(const DevModel &M, cudaStream_t s) {
+  k_uv_decide<<<1, 1, 0, s>>>(M);
+  k_uv_update<<<epic_blocks(2LL * (M.nk - 1) * (M.nj + 1) * M.ni, 128), 128, 0, s>>>(M);
+  k_uv_rotate<<<1, 1, 0, s>>>(M);
+  return 0;
+}
+
+int launch_store_diag(const DevModel &M, cudaStream_t s) {
+  // PV3: filtered copy of V (v rows), then the interior and polar values.
+  launch_filter_planes(M, M.v, PL_UV, M.work1, 0, M.nk + 1, 1, s);
+  k_pv_interior<<<cells_blocks(M, M.nk + 1, M.nj, 128), 128, 0, s>>>(M, M.work1);
+  k_pv_poles<<<M.nk + 1, 128, 0, s>>>(M);
+  // DIV_UV3 from a filtered copy of U.
+  launch_filter_planes(M, M.u, PL_UV, M.work2, 0, M.nk + 1, 0, s);
+  k_divergence<<<cells_blocks(M, M.nk + 1, M.nj + 1, 128), 128, 0, s>>>(M, M.work2, M.v, PL_UV, M.div_uv3, 0, M.nk + 1);
+  k_ri2<<<cells_blocks(M, M.nk, M.nj + 1, 128), 128, 0, s>>>(M);
+  return 0;
+}
+
+int launch_itime_advance(const DevModel &M, cudaStream_t s) {
+  k_itime_advance<<<1, 1, 0, s>>>(M);
+  return 0;
+}
+
+}  // namespace epic

@@ -1,0 +1,54 @@
+// Launchers of the step kernels (each returns 0; launch errors surface through cudaGetLastError).
+#pragma once
+#include <cuda_runtime.h>
+#include "device_common.cuh"
+
+namespace epic {
+
+// Which time plane of a wind array a kernel works on; the index itself lives in Ctl so that
+// one captured graph serves every step.
+enum PlaneSel { PL_NONE = 0, PL_UV = 1, PL_UV_DIS = 2, PL_UV_TEND = 3 };
+
+__device__ __forceinline__ long long plane_offset(const DevModel &M, int sel) {
+  const Ctl *c = M.ctl;
+  switch (sel) {
+    case PL_UV: return (long long)c->it_uv * M.n3;
+    case PL_UV_DIS: return (long long)c->it_uv_dis * M.n3;
+    case PL_UV_TEND: return (long long)c->it_uv_tend * M.n3;
+    default: return 0;
+  }
+}
+
+// k_filter.cu -- zonal filter (epic_adjust.c) and the zonal pass of hsu_advection
+int launch_filter_planes(const DevModel &M, const double *src, int src_sel, double *dst, int k0, int nplanes, int vgrid, cudaStream_t s);
+int launch_varz_filter(const DevModel &M, double *buff, int sel, int index, int kstart, int kend, cudaStream_t s);
+int launch_hsu_zonal(const DevModel &M, double *buff, int kind, int kstart, cudaStream_t s);
+int filter_kernels_init(int ni);
+size_t twiddle_doubles(int ni);
+void fill_twiddles(int ni, double *tw);
+
+// k_column.cu -- vertical (column) work
+int launch_source_sink(const DevModel &M, cudaStream_t s);
+int launch_calc_w(const DevModel &M, cudaStream_t s);
+int launch_uv_drag(const DevModel &M, cudaStream_t s);
+int launch_hsu_vertical(const DevModel &M, double *buff, int kind, cudaStream_t s);
+int launch_restore_mass(const DevModel &M, cudaStream_t s);
+int launch_set_p2etc(const DevModel &M, int update_theta, cudaStream_t s);
+int launch_store_pgrad_vars(const DevModel &M, cudaStream_t s);
+int launch_gz_monotone(const DevModel &M, cudaStream_t s);
+int launch_calc_heating(const DevModel &M, cudaStream_t s);
+int launch_advection_prep(const DevModel &M, int phase, cudaStream_t s);
+
+// k_stencil.cu -- horizontal stencils and the time update
+int launch_zero_tend(const DevModel &M, cudaStream_t s);
+int launch_uv_core(const DevModel &M, cudaStream_t s);
+int launch_uv_pgrad(const DevModel &M, cudaStream_t s);
+int launch_hsu_meridional(const DevModel &M, double *buff, int kind, cudaStream_t s);
+int launch_meridional_hyperviscosity(const DevModel &M, int index, double *var, int sel, cudaStream_t s);
+int launch_zonal_hyperviscosity(const DevModel &M, int index, double *var, int sel, cudaStream_t s);
+int launch_divergence_damping(const DevModel &M, cudaStream_t s);
+int launch_uv_update(const DevModel &M, cudaStream_t s);
+int launch_store_diag(const DevModel &M, cudaStream_t s);
+int launch_itime_advance(const DevModel &M, cudaStream_t s);
+
+}  // namespace epic

@@ -134,6 +134,16 @@ int  epic_model_timestep(epic_model *m, int32_t action);
  */
 int  epic_model_run(epic_model *m, int32_t nsteps);
 
+/*
+ * Test hook: enqueue one stage of the step (the stage numbering of oracle/epic_port.h:
+ * 0 zero tendencies, 1 source_sink, 2 calc_w, 3 uv_core, 4 uv_drag, 5 scalar hyperviscosity,
+ * 6 advection, 7 store_pgrad_vars, 8 filtered GZ, 9 3-D filter of DUDT/DVDT, 10 3-D filter of
+ * HDRY/THETA, 11 set_p2etc(UPDATE_THETA), 12 uv_pgrad, 13 divergence damping, 14 u/v time
+ * update, 15 u/v hyperviscosity, 16 store_diag, 17 calc_heating, 18 set_p2etc(DONT_UPDATE)).
+ * It has no counterpart in the reference, which only exposes the whole step.
+ */
+int  epic_model_run_stage(epic_model *m, int32_t stage);
+
 /* Wait for queued work and report any device-side model error. */
 int  epic_model_sync(epic_model *m);
 

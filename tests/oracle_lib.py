@@ -1,0 +1,174 @@
+"""ctypes access to the oracle (test infrastructure only).
+
+Two oracles live under oracle/:
+  libepicport.so  the CPU restatement of the reference step (oracle/epic_port.c), built from
+                  committed sources anywhere (also on the GPU host);
+  libepicref.so   the reference's own step compiled from its sources (oracle/Makefile `ref`),
+                  only where the reference tree is present.  It keeps static state, so each
+                  model runs in a fresh spawned process.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import multiprocessing as mp
+import os
+import subprocess
+
+import numpy as np
+
+from epic_gb300.abi import EPIC_STEP_PROGS_AND_SYNC_DIAGS, EPIC_SYNC_DIAGS_ONLY, EpicFields, EpicGrid, Fields, GridArrays
+
+ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+ORACLE = os.path.join(ROOT, "oracle")
+PORT_LIB = os.path.join(ORACLE, "_build", "libepicport.so")
+REF_LIB = os.path.join(ORACLE, "_ref", "libepicref.so")
+REFERENCE_DIR = os.environ.get("EPIC_REFERENCE_DIR", "/root/reference")
+
+_port = None
+
+
+def build_port() -> str:
+    subprocess.run(["make", "-s", "-C", ORACLE, "port"], check=True)
+    return PORT_LIB
+
+
+def reference_available() -> bool:
+    if os.path.exists(REF_LIB):
+        return True
+    if not os.path.isdir(os.path.join(REFERENCE_DIR, "src", "shared")):
+        return False
+    r = subprocess.run(["make", "-s", "-j8", "-C", ORACLE, "ref", f"REF={REFERENCE_DIR}"], capture_output=True)
+    return r.returncode == 0 and os.path.exists(REF_LIB)
+
+
+def port_lib() -> C.CDLL:
+    global _port
+    if _port is None:
+        build_port()
+        lib = C.CDLL(PORT_LIB)
+        lib.ep_create.restype = C.c_void_p
+        lib.ep_create.argtypes = [C.POINTER(EpicGrid)]
+        lib.ep_destroy.argtypes = [C.c_void_p]
+        lib.ep_destroy.restype = None
+        for n in ("ep_upload", "ep_download"):
+            getattr(lib, n).argtypes = [C.c_void_p, C.POINTER(EpicFields)]
+        for n in ("ep_timestep", "ep_run", "ep_stage"):
+            getattr(lib, n).argtypes = [C.c_void_p, C.c_int]
+        lib.ep_error.restype = C.c_char_p
+        lib.ep_error.argtypes = [C.c_void_p]
+        lib.ep_create_error.restype = C.c_char_p
+        _port = lib
+    return _port
+
+
+class Port:
+    """The CPU restatement of the step on one grid."""
+
+    def __init__(self, grid: GridArrays):
+        self.lib = port_lib()
+        self.layout = grid.layout
+        self.uv_scheme = grid.struct.uv_scheme
+        h = self.lib.ep_create(C.byref(grid.struct))
+        if not h:
+            raise RuntimeError("ep_create: " + self.lib.ep_create_error().decode())
+        self.h = C.c_void_p(h)
+
+    def _chk(self, rc, what):
+        if rc:
+            raise RuntimeError(f"{what}: {self.lib.ep_error(self.h).decode()}")
+
+    def upload(self, f: Fields):
+        self._chk(self.lib.ep_upload(self.h, C.byref(f.struct)), "ep_upload")
+
+    def download(self) -> Fields:
+        f = Fields(self.layout.ni, self.layout.nj, self.layout.nk, self.uv_scheme)
+        self._chk(self.lib.ep_download(self.h, C.byref(f.struct)), "ep_download")
+        return f
+
+    def timestep(self, action=EPIC_STEP_PROGS_AND_SYNC_DIAGS):
+        self._chk(self.lib.ep_timestep(self.h, action), "ep_timestep")
+
+    def run(self, n: int):
+        self._chk(self.lib.ep_run(self.h, n), "ep_run")
+
+    def stage(self, s: int):
+        self._chk(self.lib.ep_stage(self.h, s), "ep_stage")
+
+    def __del__(self):
+        try:
+            self.lib.ep_destroy(self.h)
+        except Exception:
+            pass
+
+
+def fields_to_dict(f: Fields) -> dict:
+    d = {k: v.copy() for k, v in f.arrays.items()}
+    for n in ("it_zero", "it_minus1", "it_minus2", "itime", "model_time"):
+        d[n] = int(getattr(f.struct, n))
+    return d
+
+
+def dict_to_fields(d: dict, ni, nj, nk, uv_scheme) -> Fields:
+    f = Fields(ni, nj, nk, uv_scheme)
+    for k in f.arrays:
+        f.arrays[k][...] = d[k]
+    for n in ("it_zero", "it_minus1", "it_minus2", "itime", "model_time"):
+        setattr(f.struct, n, int(d[n]))
+    return f
+
+
+def _ref_worker(grid_arrays: dict, grid_scalars: dict, fields: dict, dims, schedule, q):
+    """Run the reference harness in this (fresh) process; schedule = [('sync'|'step', n), ...]."""
+    try:
+        ni, nj, nk, scheme = dims
+        ga = GridArrays(ni, nj, nk)
+        for k, v in grid_arrays.items():
+            ga.arrays[k][...] = v
+        for k, v in grid_scalars.items():
+            if k == "nu":
+                for i in range(9):
+                    ga.struct.nu[i] = v[i]
+            else:
+                setattr(ga.struct, k, v)
+        f = dict_to_fields(fields, ni, nj, nk, scheme)
+        lib = C.CDLL(REF_LIB)
+        rc = lib.ref_init(C.byref(ga.struct), C.byref(f.struct))
+        if rc:
+            raise RuntimeError(f"ref_init {rc}")
+        geo = (C.c_double * 8)()
+        lib.ref_geometry_maxdiff(geo)
+        out = []
+        for what, n in schedule:
+            if what == "sync":
+                lib.ref_timestep(EPIC_SYNC_DIAGS_ONLY)
+            else:
+                lib.ref_run(n)
+            g = Fields(ni, nj, nk, scheme)
+            lib.ref_get(C.byref(g.struct))
+            out.append(fields_to_dict(g))
+        q.put(("ok", list(geo), out))
+    except Exception as e:  # pragma: no cover - reported to the parent
+        q.put(("err", repr(e), None))
+
+
+def run_reference(ga: GridArrays, f: Fields, schedule) -> tuple[list, list]:
+    """Snapshots of the reference after each schedule entry, computed in a spawned process."""
+    ctx = mp.get_context("spawn")
+    q = ctx.Queue()
+    dims = (ga.layout.ni, ga.layout.nj, ga.layout.nk, f.uv_scheme)
+    p = ctx.Process(target=_ref_worker, args=({k: v.copy() for k, v in ga.arrays.items()}, ga.scalars(),
+                                               fields_to_dict(f), dims, schedule, q))
+    p.start()
+    status, geo, out = q.get(timeout=1800)
+    p.join(60)
+    if status != "ok":
+        raise RuntimeError(geo)
+    return geo, out
+
+
+def rel_l2(a: np.ndarray, b: np.ndarray) -> float:
+    a = np.asarray(a, dtype=np.float64)
+    b = np.asarray(b, dtype=np.float64)
+    den = np.linalg.norm(b.ravel())
+    num = np.linalg.norm((a - b).ravel())
+    return float(num / den) if den > 0 else float(num)
