@@ -1,0 +1,331 @@
+"""Throughput of the GB300 EPIC timestep() on a synthetic Held-Suarez state.
+
+    python bench.py [--gpus N] [--steps K] [--warmup W] [--impl gb300|reference]
+                    [--workload hs256|hs512|hs128|hs64] [--no-cpu-baseline]
+
+A step is one timestep(STEP_PROGS_AND_SYNC_DIAGS) of the whole grid.  The default workload
+is 256 x 128 x 32 at dt = 60 s (the shape of the plain-FP64 256x128x32 run); its state
+(~37 FP64 3-D arrays, 0.35 GB) is larger than the 129 MB L2, so no flush is needed between
+steps.  value = cell-steps/s (cells = ni*nj*nk) with the state resident in HBM, timed with
+CUDA events on the model's stream; e2e = the same metric through the C ABI with the state
+in pinned host memory, uploaded and downloaded every step (what a reference-side
+timestep() wrapper over host-owned `var` costs).
+
+--impl reference times the reference's CPU implementation of the step (the oracle's
+restatement, bit-identical to the reference build) on every host core as independent
+replicas.  For N > 1 each GPU runs its own replica (the step does not shard).
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import multiprocessing as mp
+import os
+import statistics
+import subprocess
+import sys
+import tempfile
+import time
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+WORKLOADS = {
+    # name: (ni, nj, nk, dt)
+    "hs64": (64, 32, 10, 300),
+    "hs128": (128, 64, 20, 300),
+    "hs256": (256, 128, 32, 60),
+    "hs512": (512, 256, 40, 75),
+}
+METRIC = "cell-steps/s"
+
+
+def _workload_cfg(name, seed=0):
+    from epic_gb300 import HSConfig
+    ni, nj, nk, dt = WORKLOADS[name]
+    return HSConfig(ni=ni, nj=nj, nk=nk, dt=dt, seed=seed)
+
+
+def algorithmic_bytes_per_step(cfg, word=8):
+    """Compulsory HBM traffic of one AB3 step: U, V, HDRY, THETA and the two older tendency
+    planes of U and V read once; U, V, HDRY, THETA and the new tendencies written once."""
+    return 14 * word * cfg.ni * (cfg.nj + 1) * cfg.nk
+
+
+# ---------------------------------------------------------------------------------------------
+# clocks during the timed region
+# ---------------------------------------------------------------------------------------------
+
+class ClockSampler:
+    QUERY = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,clocks_event_reasons.hw_slowdown,"
+             "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,"
+             "clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, gpu_index: int):
+        self.gpu = gpu_index
+        self.proc = None
+        self.path = None
+
+    def __enter__(self):
+        fd, self.path = tempfile.mkstemp(suffix=".csv")
+        os.close(fd)
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.gpu), f"--query-gpu={self.QUERY}", "--format=csv,noheader,nounits",
+                                          "-lms", "100"], stdout=open(self.path, "w"), stderr=subprocess.DEVNULL)
+        except OSError:
+            self.proc = None
+        time.sleep(0.25)
+        return self
+
+    def __exit__(self, *a):
+        if self.proc:
+            self.proc.terminate()
+            try:
+                self.proc.wait(5)
+            except subprocess.TimeoutExpired:
+                self.proc.kill()
+
+    def summary(self):
+        out = {"sm_mhz": None, "sm_max_mhz": None, "reasons": [], "samples": 0}
+        if not self.path or not os.path.exists(self.path):
+            return out
+        sm, mx, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for line in open(self.path):
+            parts = [p.strip() for p in line.split(",")]
+            if len(parts) < 9:
+                continue
+            try:
+                sm.append(float(parts[1]))
+                mx.append(float(parts[2]))
+            except ValueError:
+                continue
+            for n, v in zip(names, parts[5:9]):
+                if v.lower() == "active":
+                    reasons.add(n)
+        os.unlink(self.path)
+        if sm:
+            out.update(sm_mhz=statistics.median(sm), sm_max_mhz=max(mx), reasons=sorted(reasons), samples=len(sm))
+        return out
+
+
+# ---------------------------------------------------------------------------------------------
+# CPU side: the oracle's restatement of the reference step
+# ---------------------------------------------------------------------------------------------
+
+def _cpu_replica(name, seed, nsteps, warm, q):
+    sys.path.insert(0, os.path.join(ROOT, "tests"))
+    from oracle_lib import Port
+    from epic_gb300 import EPIC_SYNC_DIAGS_ONLY, hs_setup
+    cfg = _workload_cfg(name, seed)
+    ga, f = hs_setup(cfg)
+    p = Port(ga)
+    p.upload(f)
+    p.timestep(EPIC_SYNC_DIAGS_ONLY)
+    p.run(warm)
+    t0 = time.perf_counter()
+    p.run(nsteps)
+    q.put(time.perf_counter() - t0)
+
+
+def cpu_reference(name, nsteps, warm, procs):
+    """Aggregate cell-steps/s of `procs` independent single-threaded replicas of the reference step."""
+    sys.path.insert(0, os.path.join(ROOT, "tests"))
+    from oracle_lib import build_port
+    build_port()
+    ctx = mp.get_context("spawn")
+    q = ctx.Queue()
+    ps = [ctx.Process(target=_cpu_replica, args=(name, s, nsteps, warm, q)) for s in range(procs)]
+    for p in ps:
+        p.start()
+    times = [q.get(timeout=3600) for _ in ps]
+    for p in ps:
+        p.join()
+    cfg = _workload_cfg(name)
+    return sum(cfg.cells * nsteps / t for t in times), max(times)
+
+
+# ---------------------------------------------------------------------------------------------
+# GPU side
+# ---------------------------------------------------------------------------------------------
+
+def _dist():
+    ws = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return ws, rank, local
+
+
+def run_gpu(args):
+    import torch
+    from epic_gb300 import EPIC_SYNC_DIAGS_ONLY, Model, hs_setup
+    ws, rank, local = _dist()
+    torch.cuda.set_device(local)
+    if ws > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl")
+    cfg = _workload_cfg(args.workload, seed=rank)
+    ga, f = hs_setup(cfg)
+    model = Model(ga)
+    model.upload(f)
+    model.timestep(EPIC_SYNC_DIAGS_ONLY)
+    stream = torch.cuda.ExternalStream(model.stream)
+    for _ in range(args.warmup):
+        model.run(1)
+    model.sync()
+
+    def barrier():
+        torch.cuda.synchronize()
+        if ws > 1:
+            import torch.distributed as dist
+            dist.barrier()
+
+    # device-resident throughput
+    ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    barrier()
+    with ClockSampler(local) as clk:
+        ev0.record(stream)
+        for _ in range(args.steps):
+            model.run(1)
+        ev1.record(stream)
+        ev1.synchronize()
+    model.sync()
+    barrier()
+    ms = ev0.elapsed_time(ev1)
+    if ws > 1:
+        import torch.distributed as dist
+        t = torch.tensor([ms], device="cuda")
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        ms = float(t.item())
+    ms_step = ms / args.steps
+    value = ws * cfg.cells * args.steps / (ms / 1e3)
+    clocks = clk.summary()
+
+    # dominant kernel, timed alone with events: the vertical Hsu advection stage
+    roof = kernel_roofline(model, cfg, stream, torch)
+
+    # end to end through the C ABI with pinned host state
+    host = model.download().copy(pinned=True)
+    e2e_steps = max(1, min(args.steps, 5))
+    barrier()
+    t0 = time.perf_counter()
+    for _ in range(e2e_steps):
+        model.step_host(host, 1, prime=False)
+    torch.cuda.synchronize()
+    e2e_s = (time.perf_counter() - t0) / e2e_steps
+    e2e_val = ws * cfg.cells / e2e_s
+    launches = model.kernels_per_step * args.steps
+
+    out = None
+    if rank == 0:
+        peaks = _peaks()
+        out = {
+            "metric": METRIC, "value": value, "unit": "cell-steps/s", "n_gpus": ws, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": ms_step, "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+            "config": {"workload": f"Held-Suarez {cfg.ni}x{cfg.nj}x{cfg.nk}, dt={cfg.dt}s, AB3, nu4=0.5 max, "
+                                   f"FP64 drop-in form", "ni": cfg.ni, "nj": cfg.nj, "nk": cfg.nk, "dt": cfg.dt,
+                       "precision": "fp64", "parallelism": f"replicas{ws}",
+                       "l2": f"state {model.device_bytes / 1e9:.2f} GB > 129 MB L2; no flush needed",
+                       "state": "horizontally uniform HS equilibrium column at rest + seeded 0.1 K theta noise"},
+            "clocks": clocks,
+            "e2e": {"value": e2e_val, "unit": "cell-steps/s", "h2d_bytes_per_step": host.nbytes,
+                    "d2h_bytes_per_step": host.nbytes},
+            "gpu_launches": launches,
+            "roofline": roof,
+            "step_roofline": {"bound": "hbm", "algorithmic_bytes_per_step": algorithmic_bytes_per_step(cfg),
+                              "achieved_gbs": algorithmic_bytes_per_step(cfg) / (ms_step / 1e3) / 1e9,
+                              "peak_gbs": peaks.get("hbm_gbs")},
+        }
+        if peaks.get("hbm_gbs"):
+            out["step_roofline"]["frac"] = out["step_roofline"]["achieved_gbs"] / peaks["hbm_gbs"]
+    model.close()
+    if ws > 1:
+        import torch.distributed as dist
+        dist.destroy_process_group()
+    return out
+
+
+def _peaks():
+    p = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    if os.path.exists(p):
+        d = json.load(open(p))
+        d["source"] = "measured"
+        return d
+    return {"hbm_gbs": 6800.0, "bf16_tflops": 1900.0, "source": "fallback"}
+
+
+def kernel_roofline(model, cfg, stream, torch):
+    """Stage 6 (advection: the three Hsu predictor-corrector advections) timed alone.
+
+    Algorithmic bytes per launch: each advected field (unity, THETA, HDRY) is read and written
+    once, plus U, V, W3 read once: 6 reads + 3 writes of one FP64 3-D field
+    (ni*(nj+1)*nk cells)."""
+    peaks = _peaks()
+    n = 5
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    state = model.download()
+    model.run_stage(6)
+    model.sync()
+    model.upload(state)
+    torch.cuda.synchronize()
+    e0.record(stream)
+    for _ in range(n):
+        model.run_stage(6)
+    e1.record(stream)
+    e1.synchronize()
+    model.upload(state)
+    model.sync()
+    dur = e0.elapsed_time(e1) / n / 1e3
+    cells = cfg.ni * (cfg.nj + 1) * cfg.nk
+    alg = 9 * 8 * cells
+    ach = alg / dur / 1e9
+    return {"kernel": "advection (hsu_advection of unity, THETA, HDRY)", "bound": "hbm", "achieved": ach,
+            "peak": peaks["hbm_gbs"], "unit": "GB/s", "frac": ach / peaks["hbm_gbs"],
+            "peak_source": peaks["source"] + " (burst copy)", "algorithmic_bytes": alg, "launch_ms": dur * 1e3,
+            "traffic": None}
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=20)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
+    ap.add_argument("--workload", default="hs256", choices=sorted(WORKLOADS))
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--cpu-steps", type=int, default=3)
+    args = ap.parse_args()
+    ws, rank, _ = _dist()
+
+    if args.impl == "reference":
+        if rank != 0:
+            return
+        procs = os.cpu_count() or 1
+        steps = max(1, min(args.steps, 3))
+        val, wall = cpu_reference(args.workload, steps, 0, procs)
+        cfg = _workload_cfg(args.workload)
+        line = {"impl": "reference", "metric": METRIC, "value": val, "unit": "cell-steps/s", "n_gpus": args.gpus,
+                "steps": steps, "warmup": args.warmup, "ms_per_step": wall / steps * 1e3, "higher_is_better": True,
+                "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+                "config": {"workload": f"Held-Suarez {cfg.ni}x{cfg.nj}x{cfg.nk}, dt={cfg.dt}s, AB3, nu4=0.5 max",
+                           "ni": cfg.ni, "nj": cfg.nj, "nk": cfg.nk, "dt": cfg.dt, "precision": "fp64"},
+                "cpu_baseline": {"value": val, "unit": "cell-steps/s", "cores": procs, "kind": "port",
+                                 "sample": f"{procs} independent single-threaded replicas x {steps} steps of the "
+                                           f"oracle's restatement (bit-identical to the reference build)"},
+                "e2e": {"value": val, "unit": "cell-steps/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+        print(json.dumps(line))
+        return
+
+    out = run_gpu(args)
+    if rank == 0 and out is not None:
+        if ws == 1 and not args.no_cpu_baseline:
+            val, wall = cpu_reference(args.workload, args.cpu_steps, 0, 1)
+            out["cpu_baseline"] = {"value": val, "unit": "cell-steps/s", "cores": 1, "kind": "port",
+                                   "sample": f"{args.cpu_steps} steps of {WORKLOADS[args.workload][:3]} on one core "
+                                             f"({wall:.1f} s) with the oracle's restatement of the reference step"}
+        print(json.dumps(out))
+
+
+if __name__ == "__main__":
+    main()

@@ -52,6 +52,8 @@ def load_library(path: str | None = None) -> C.CDLL:
     lib.epic_model_step_host.argtypes = [C.c_void_p, C.POINTER(EpicFields), C.c_int32, C.c_int32]
     lib.epic_model_stream.argtypes = [C.c_void_p]
     lib.epic_model_stream.restype = C.c_void_p
+    lib.epic_model_kernels_per_step.argtypes = [C.c_void_p]
+    lib.epic_model_kernels_per_step.restype = C.c_int32
     lib.epic_model_device_bytes.argtypes = [C.c_void_p]
     lib.epic_model_device_bytes.restype = C.c_int64
     lib.epic_hs_grid_build.argtypes = [C.POINTER(EpicHsParams), C.POINTER(EpicGrid), C.POINTER(C.c_double),
@@ -131,6 +133,10 @@ class Model:
     @property
     def stream(self) -> int:
         return self.lib.epic_model_stream(self._h) or 0
+
+    @property
+    def kernels_per_step(self) -> int:
+        return int(self.lib.epic_model_kernels_per_step(self._h))
 
     @property
     def device_bytes(self) -> int:

@@ -138,21 +138,28 @@ class GridArrays:
         return out
 
 
+def _pinned_zeros(shape):
+    """Page-locked host array (what cudaMemcpyAsync needs to overlap and run at full rate)."""
+    import torch
+    return torch.zeros(shape, dtype=torch.float64, pin_memory=True).numpy()
+
+
 class Fields:
     """Owns numpy storage for every EpicFields pointer, in the reference layout."""
 
-    def __init__(self, ni: int, nj: int, nk: int, uv_scheme: int):
+    def __init__(self, ni: int, nj: int, nk: int, uv_scheme: int, pinned: bool = False):
         self.layout = Layout(ni, nj, nk)
         self.uv_scheme = uv_scheme
         nvp, ntp = (1, 3) if uv_scheme == EPIC_UV_AB3 else (2, 1)
         s3 = self.layout.shape3
+        zeros = _pinned_zeros if pinned else np.zeros
         self.arrays = {
-            "u": np.zeros((nvp,) + s3), "v": np.zeros((nvp,) + s3),
-            "dudt": np.zeros((ntp,) + s3), "dvdt": np.zeros((ntp,) + s3),
+            "u": zeros((nvp,) + s3), "v": zeros((nvp,) + s3),
+            "dudt": zeros((ntp,) + s3), "dvdt": zeros((ntp,) + s3),
         }
         for n in FIELD_NAMES_3D:
-            self.arrays[n] = np.zeros(s3)
-        self.arrays["gz_surface"] = np.zeros(self.layout.shape2)
+            self.arrays[n] = zeros(s3)
+        self.arrays["gz_surface"] = zeros(self.layout.shape2)
         self.struct = EpicFields()
         for k, a in self.arrays.items():
             setattr(self.struct, k, _ptr(a))
@@ -164,13 +171,17 @@ class Fields:
             return arrays[name]
         raise AttributeError(name)
 
-    def copy(self) -> "Fields":
-        out = Fields(self.layout.ni, self.layout.nj, self.layout.nk, self.uv_scheme)
+    def copy(self, pinned: bool = False) -> "Fields":
+        out = Fields(self.layout.ni, self.layout.nj, self.layout.nk, self.uv_scheme, pinned=pinned)
         for k, a in self.arrays.items():
             out.arrays[k][...] = a
         for name in ("it_zero", "it_minus1", "it_minus2", "itime", "model_time"):
             setattr(out.struct, name, getattr(self.struct, name))
         return out
+
+    @property
+    def nbytes(self) -> int:
+        return int(sum(a.nbytes for a in self.arrays.values()))
 
     def wind(self, name: str) -> np.ndarray:
         """Current value plane of u or v (grid.it_uv: plane 0 for AB3, IT_ZERO for leapfrog)."""

@@ -29,8 +29,9 @@ def _nvcc() -> str:
 
 
 def _flags() -> list[str]:
+    extra = os.environ.get("EPIC_NVCC_EXTRA", "").split()
     return ["-O3", "-std=c++17", ARCH, "-lineinfo", "-Xcompiler", "-fPIC,-ffp-contract=off",
-            "-I" + os.path.join(ROOT, "include"), "-I" + SRC, "--expt-relaxed-constexpr"]
+            "-I" + os.path.join(ROOT, "include"), "-I" + SRC, "--expt-relaxed-constexpr", *extra]
 
 
 def _compile(src: str) -> str:
@@ -48,6 +49,14 @@ def _compile(src: str) -> str:
 
 def build(verbose: bool = False) -> str:
     os.makedirs(OUT, exist_ok=True)
+    stamp = os.path.join(OUT, "build_flags.txt")
+    flags = " ".join(_flags())
+    if not os.path.exists(stamp) or open(stamp).read() != flags:
+        for f in os.listdir(OUT):
+            if f.endswith(".o") or f.endswith(".so"):
+                os.remove(os.path.join(OUT, f))
+        with open(stamp, "w") as fh:
+            fh.write(flags)
     with cf.ThreadPoolExecutor(max_workers=len(SOURCES)) as ex:
         objs = list(ex.map(_compile, SOURCES))
     if not os.path.exists(LIB) or any(os.path.getmtime(o) > os.path.getmtime(LIB) for o in objs):

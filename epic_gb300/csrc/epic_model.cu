@@ -24,6 +24,7 @@ struct epic_model {
   bool uploaded = false;
   cudaGraphExec_t run_graph = nullptr;
   bool graph_failed = false;
+  int kernels_per_step = -1;
 };
 
 namespace {
@@ -416,6 +417,17 @@ extern "C" int epic_model_run(epic_model *m, int32_t nsteps) {
       if (!rc) rc = epic::launch_itime_advance(m->d, m->stream);
       cudaError_t e = cudaStreamEndCapture(m->stream, &graph);
       if (rc == EPIC_OK && e == cudaSuccess && graph) {
+        size_t nn = 0;
+        if (cudaGraphGetNodes(graph, nullptr, &nn) == cudaSuccess && nn > 0) {
+          std::vector<cudaGraphNode_t> nodes(nn);
+          cudaGraphGetNodes(graph, nodes.data(), &nn);
+          int nk = 0;
+          for (auto nd : nodes) {
+            cudaGraphNodeType t;
+            if (cudaGraphNodeGetType(nd, &t) == cudaSuccess && t == cudaGraphNodeTypeKernel) nk++;
+          }
+          m->kernels_per_step = nk;
+        }
         if (cudaGraphInstantiate(&m->run_graph, graph, 0) != cudaSuccess) m->run_graph = nullptr;
       }
       if (graph) cudaGraphDestroy(graph);
@@ -481,5 +493,7 @@ extern "C" int epic_model_step_host(epic_model *m, epic_fields *f, int32_t prime
 }
 
 extern "C" void *epic_model_stream(epic_model *m) { return m ? (void *)m->stream : nullptr; }
+
+extern "C" int32_t epic_model_kernels_per_step(const epic_model *m) { return m ? m->kernels_per_step : -1; }
 
 extern "C" int64_t epic_model_device_bytes(const epic_model *m) { return m ? (int64_t)m->pool_bytes : 0; }

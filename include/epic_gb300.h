@@ -159,6 +159,10 @@ int  epic_model_step_host(epic_model *m, epic_fields *f, int32_t prime, int32_t 
 /* Device stream the model runs on (a cudaStream_t), for callers that interleave work. */
 void *epic_model_stream(epic_model *m);
 
+/* Kernel launches in one step of epic_model_run (its captured graph), the step counter
+ * included; -1 before the first epic_model_run.  No counterpart in the reference. */
+int32_t epic_model_kernels_per_step(const epic_model *m);
+
 /* Bytes of device memory the model holds. */
 int64_t epic_model_device_bytes(const epic_model *m);
 
