@@ -30,7 +30,7 @@ def _nvcc() -> str:
 
 def _flags() -> list[str]:
     extra = os.environ.get("EPIC_NVCC_EXTRA", "").split()
-    return ["-O3", "-std=c++17", ARCH, "-lineinfo", "-Xcompiler", "-fPIC,-ffp-contract=off",
+    return ["-O3", "-std=c++17", ARCH, "-lineinfo", "-fmad=false", "-Xcompiler", "-fPIC,-ffp-contract=off",
             "-I" + os.path.join(ROOT, "include"), "-I" + SRC, "--expt-relaxed-constexpr", *extra]
 
 

@@ -1,0 +1,184 @@
+// Correctly rounded log, exp and pow for binary64, evaluated in double-double arithmetic.
+//
+// The reference calls glibc's log/exp/pow, whose results are correctly rounded in all but a
+// tiny fraction of cases.  Several of the reference's formulas cancel hard (the finite-volume
+// pressure gradient differences products of geopotentials), so one-ulp differences in GZ3 or P2
+// grow to ~4e-11 in U after a step from rest.  Evaluating these functions to ~2^-84 relative and
+// rounding once gives the correctly rounded value in all but ~2^-30 of cases, and so the
+// reference's value whenever glibc's is correctly rounded.
+//
+// Methods (textbook, no vendor code): the error-free transformations TwoSum (Knuth) and TwoProd
+// with a fused multiply-add; log by x = 2^e m, m = c (1 + r) with c = k/1024 from a table of
+// log(c) and 1/c, log(1+r) by its Taylor series (leading terms in double-double, the tail in
+// double); exp by x = (1024 q + j) ln2/1024 + r with a table of 2^(j/1024), exp(r) by its Taylor
+// series; pow = exp(y log x) with the double-double logarithm.  The tables are built on the
+// host from slow, long double-double series (2 atanh((c-1)/(c+1)) and exp(y/2^10)^(2^10)).
+#pragma once
+#include <cmath>
+
+namespace epic {
+
+struct dd { double hi, lo; };
+
+__host__ __device__ __forceinline__ dd two_sum(double a, double b) {
+  const double s = a + b;
+  const double bb = s - a;
+  const double e = (a - (s - bb)) + (b - bb);
+  return {s, e};
+}
+__host__ __device__ __forceinline__ dd fast_two_sum(double a, double b) {   // |a| >= |b|
+  const double s = a + b;
+  return {s, b - (s - a)};
+}
+__host__ __device__ __forceinline__ dd two_prod(double a, double b) {
+  const double p = a * b;
+  return {p, fma(a, b, -p)};
+}
+__host__ __device__ __forceinline__ dd dd_add(dd a, dd b) {
+  dd s = two_sum(a.hi, b.hi);
+  const dd t = two_sum(a.lo, b.lo);
+  s.lo += t.hi;
+  s = fast_two_sum(s.hi, s.lo);
+  s.lo += t.lo;
+  return fast_two_sum(s.hi, s.lo);
+}
+__host__ __device__ __forceinline__ dd dd_add_d(dd a, double b) {
+  dd s = two_sum(a.hi, b);
+  s.lo += a.lo;
+  return fast_two_sum(s.hi, s.lo);
+}
+__host__ __device__ __forceinline__ dd dd_neg(dd a) { return {-a.hi, -a.lo}; }
+__host__ __device__ __forceinline__ dd dd_sub(dd a, dd b) { return dd_add(a, dd_neg(b)); }
+__host__ __device__ __forceinline__ dd dd_mul(dd a, dd b) {
+  dd p = two_prod(a.hi, b.hi);
+  p.lo = fma(a.hi, b.lo, p.lo);
+  p.lo = fma(a.lo, b.hi, p.lo);
+  return fast_two_sum(p.hi, p.lo);
+}
+__host__ __device__ __forceinline__ dd dd_mul_d(dd a, double b) {
+  dd p = two_prod(a.hi, b);
+  p.lo = fma(a.lo, b, p.lo);
+  return fast_two_sum(p.hi, p.lo);
+}
+__host__ __device__ __forceinline__ dd dd_div(dd a, dd b) {
+  const double q1 = a.hi / b.hi;
+  dd r = dd_sub(a, dd_mul_d(b, q1));
+  const double q2 = r.hi / b.hi;
+  r = dd_sub(r, dd_mul_d(b, q2));
+  const double q3 = r.hi / b.hi;
+  return dd_add(fast_two_sum(q1, q2), {q3, 0.});
+}
+
+// ---- slow, long series used only to build the tables (host) ----
+
+// 2 atanh(s) summed to 2^-106 for |s| <= 0.18.
+inline dd slow_two_atanh(dd s) {
+  const dd s2 = dd_mul(s, s);
+  dd term = s, sum = s;
+  for (int t = 1; t < 45; t++) {
+    term = dd_mul(term, s2);
+    sum = dd_add(sum, dd_div(term, {(double)(2 * t + 1), 0.}));
+  }
+  return {2. * sum.hi, 2. * sum.lo};
+}
+inline dd slow_log(double c) {   // c in [0.7, 1.45]
+  return slow_two_atanh(dd_div(dd_sub({c, 0.}, {1., 0.}), dd_add({c, 0.}, {1., 0.})));
+}
+inline dd slow_exp(dd x) {       // |x| < 1: Taylor of exp(x/2^10), then ten squarings
+  dd r = {ldexp(x.hi, -10), ldexp(x.lo, -10)};
+  dd term = r, sum = dd_add({1., 0.}, r);
+  for (int n = 2; n <= 14; n++) {
+    term = dd_div(dd_mul(term, r), {(double)n, 0.});
+    sum = dd_add(sum, term);
+  }
+  for (int q = 0; q < 10; q++) sum = dd_mul(sum, sum);
+  return sum;
+}
+
+constexpr int LOG_K0 = 724;       // c = k/1024, k = 724 .. 1448 covers m in [sqrt(1/2), sqrt(2)]
+constexpr int LOG_N = 725;
+constexpr int EXP_N = 1024;
+
+struct MathTable {
+  dd ln2;                  // ln 2
+  dd ln2_1024;             // ln 2 / 1024
+  dd logc[LOG_N];          // log(k/1024)
+  double invc[LOG_N];      // 1024/k rounded
+  dd exp2j[EXP_N];         // 2^(j/1024)
+};
+
+inline void fill_math_table(MathTable &t) {
+  const dd third = dd_div({1., 0.}, {3., 0.});
+  t.ln2 = slow_two_atanh(third);
+  t.ln2_1024 = {ldexp(t.ln2.hi, -10), ldexp(t.ln2.lo, -10)};
+  for (int i = 0; i < LOG_N; i++) {
+    const double c = (double)(LOG_K0 + i) / 1024.;
+    t.logc[i] = slow_log(c);
+    t.invc[i] = 1. / c;
+  }
+  for (int j = 0; j < EXP_N; j++) t.exp2j[j] = slow_exp(dd_mul_d(t.ln2_1024, (double)j));
+}
+
+// log(x) in double-double, x > 0 finite and normal.  Relative error ~2^-84.
+__host__ __device__ __forceinline__ dd dd_log(double x, const MathTable &T) {
+  int e;
+  double m = frexp(x, &e);   // m in [0.5, 1)
+  m *= 2.;
+  e -= 1;                    // m in [1, 2)
+  if (m > 1.4142135623730951) { m *= 0.5; e += 1; }
+  const int k = (int)rint(m * 1024.);
+  const double c = (double)k * (1. / 1024.);
+  const double num = m - c;                          // exact (Sterbenz)
+  const double invc = T.invc[k - LOG_K0];
+  const double rh = num * invc;
+  const double rl = fma(-rh, c, num) * invc;
+  const dd r = fast_two_sum(rh, rl);                 // |r| < 7e-4
+  const dd r2 = dd_mul(r, r);
+  const dd r3 = dd_mul(r2, r);
+  // log(1+r) = r - r^2/2 + r^3/3 - r^4 (1/4 - r/5 + r^2/6 - r^3/7 + r^4/8)
+  const double x1 = r.hi;
+  const double tail = -(r2.hi * r2.hi) * (0.25 - x1 * (0.2 - x1 * (1. / 6. - x1 * (1. / 7. - x1 * 0.125))));
+  dd s = dd_add(r, {-0.5 * r2.hi, -0.5 * r2.lo});
+  s = dd_add(s, dd_mul(r3, {0.33333333333333331, 1.8503717077085941e-17}));
+  s = dd_add_d(s, tail);
+  const dd le = dd_mul_d(T.ln2, (double)e);
+  return dd_add(dd_add(le, T.logc[k - LOG_K0]), s);
+}
+
+// exp(x) for a double-double argument, |x| < 700, rounded to double.
+__host__ __device__ __forceinline__ double dd_exp_round(dd x, const MathTable &T) {
+  const double nf = rint(x.hi * (1024. / 0.69314718055994529));
+  const dd r = dd_sub(x, dd_mul_d(T.ln2_1024, nf));  // |r| <= ln2/2048 (+ rounding)
+  const long long n = (long long)nf;
+  const int j = (int)(n & 1023);
+  const int q = (int)((n - j) / 1024);
+  const dd r2 = dd_mul(r, r);
+  const double x1 = r.hi;
+  // exp(r) - 1 = r + r^2/2 + r^3 (1/6 + r/24 + r^2/120 + r^3/720 + r^4/5040)
+  const double tail = (r2.hi * x1) * (1. / 6. + x1 * (1. / 24. + x1 * (1. / 120. + x1 * (1. / 720. + x1 * (1. / 5040.)))));
+  dd em1 = dd_add(r, {0.5 * r2.hi, 0.5 * r2.lo});
+  em1 = dd_add_d(em1, tail);
+  const dd e = dd_add_d(em1, 1.);
+  const dd v = dd_mul(T.exp2j[j], e);
+  return ldexp(v.hi, q);
+}
+
+__host__ __device__ __forceinline__ double cr_log(double x, const MathTable &T) {
+  if (!(x > 0.) || !(x < INFINITY) || x < 2.2250738585072014e-308) return log(x);
+  if (x == 1.) return 0.;
+  return dd_log(x, T).hi;
+}
+__host__ __device__ __forceinline__ double cr_exp(double x, const MathTable &T) {
+  if (!(fabs(x) < 700.)) return exp(x);
+  if (x == 0.) return 1.;
+  return dd_exp_round({x, 0.}, T);
+}
+__host__ __device__ __forceinline__ double cr_pow(double x, double y, const MathTable &T) {
+  if (y == 0. || x == 1.) return 1.;
+  if (!(x > 0.) || !(x < INFINITY) || x < 2.2250738585072014e-308 || !(fabs(y) < 1e6)) return pow(x, y);
+  const dd l = dd_mul_d(dd_log(x, T), y);
+  if (!(fabs(l.hi) < 700.)) return pow(x, y);
+  return dd_exp_round(l, T);
+}
+
+}  // namespace epic

@@ -6,6 +6,7 @@
 #include <cuda_runtime.h>
 #include <cstdint>
 #include <cfloat>
+#include "dd_math.cuh"
 
 #define EPIC_MAX_NK 126      // column kernels keep per-column arrays of nk+2 entries
 #define EPIC_MAX_NI 1024     // row kernels keep one row of ni entries in shared memory
@@ -43,7 +44,9 @@ struct DevModel {
   const double *sgth, *dsgth, *dsgth_inv, *h_min, *t_sponge_inv;
   const double *high_lat_h, *high_lat_pv;   // [(nj+3)*(ni+2)] 2-D like the reference
   const double *h_coef, *v_coef;            // d2dy2 coefficients, 3 per row
-  const double *tw;                         // FFT twiddles: N/2 for the half-length FFT, N+1 for the split
+  const double *tw;                         // realft/four1 twiddles (see k_filter.cu)
+  const double *coslat;                     // cos(lat[2j+1] deg), j = 0..nj, from the host libm
+  const MathTable *lt;                      // double-double tables for cr_log/cr_exp/cr_pow
   // state
   double *u, *v, *dudt, *dvdt, *hdry, *theta, *p3, *h3, *p2, *theta2, *t2, *t3, *rho2, *rho3, *exner3;
   double *gz3, *mont3, *heat3, *pv3, *ri2, *div_uv3, *w3, *dzdt3, *u_spinup, *gz_surface;
@@ -72,12 +75,20 @@ __device__ __forceinline__ int fcmp(double x1, double x2) {
 }
 
 // get_sigma / get_p_sigma / g_sigma / f_sigma / return_sigmatheta, epic_funcs_diag.c:1238-1314,1751-1770
-__device__ __forceinline__ double get_sigma(double pbot, double p, double ptop) { return log(p / pbot) / log(ptop / pbot); }
-__device__ __forceinline__ double get_p_sigma(double pbot, double sigma, double ptop) { return pbot * exp(sigma * log(ptop / pbot)); }
+// Transcendentals are correctly rounded (dd_math.cuh) so that they agree with the reference's libm.
+__device__ __forceinline__ double xlog(const DevModel &M, double x) { return cr_log(x, *M.lt); }
+__device__ __forceinline__ double xexp(const DevModel &M, double x) { return cr_exp(x, *M.lt); }
+__device__ __forceinline__ double xpow(const DevModel &M, double x, double y) { return cr_pow(x, y, *M.lt); }
+__device__ __forceinline__ double get_sigma(const DevModel &M, double pbot, double p, double ptop) {
+  return xlog(M, p / pbot) / xlog(M, ptop / pbot);
+}
+__device__ __forceinline__ double get_p_sigma(const DevModel &M, double pbot, double sigma, double ptop) {
+  return pbot * xexp(M, sigma * xlog(M, ptop / pbot));
+}
 __device__ __forceinline__ double g_sigma(const DevModel &M, double s) {
   if (s <= M.sigma_sigma) return 0.;
   if (s >= 1.) return 1.;
-  return M.g_coeff * (1. - exp(-M.alpha * (s - M.sigma_sigma)));
+  return M.g_coeff * (1. - xexp(M, -M.alpha * (s - M.sigma_sigma)));
 }
 __device__ __forceinline__ double f_sigma(const DevModel &M, double s) {
   if (s < 0.) return M.zeta0;
@@ -87,18 +98,18 @@ __device__ __forceinline__ double f_sigma(const DevModel &M, double s) {
 }
 __device__ __forceinline__ double return_sigmatheta(const DevModel &M, double theta, double p, double pbot, double ptop) {
   if (p <= ptop) return theta;
-  const double s = get_sigma(pbot, p, ptop);
+  const double s = get_sigma(M, pbot, p, ptop);
   return f_sigma(M, s) + g_sigma(M, s) * theta;
 }
 // return_temp (x_h2 = 0), return_density (ideal gas), return_enthalpy (cpr*T*rgas)
-__device__ __forceinline__ double return_temp(const DevModel &M, double p, double theta) { return theta * pow(p / M.press0, M.kappa); }
+__device__ __forceinline__ double return_temp(const DevModel &M, double p, double theta) { return theta * xpow(M, p / M.press0, M.kappa); }
 __device__ __forceinline__ double return_density(double p, double t, double mu) { return p * mu / (8.314472e+3 * t); }
 __device__ __forceinline__ double return_enthalpy(const DevModel &M, double t) { return (M.cpr * t) * M.rgas; }
 // onto_kk(P2_INDEX) at a layer, epic_funcs_diag.c:2601-2618
 __device__ __forceinline__ double layer_p(const DevModel &M, double top, double bot) {
   if (fcmp(bot, top) == 0) return .5 * (bot + top);
   const double kp1 = M.kappa + 1.;
-  return pow((pow(bot, kp1) - pow(top, kp1)) / (kp1 * (bot - top)), 1. / M.kappa);
+  return xpow(M, (xpow(M, bot, kp1) - xpow(M, top, kp1)) / (kp1 * (bot - top)), 1. / M.kappa);
 }
 
 struct Trip { double x, y, z; };

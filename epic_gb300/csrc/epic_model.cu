@@ -287,7 +287,8 @@ extern "C" int epic_model_create(const epic_grid *g, int32_t precision, epic_mod
   auto rnd = [](size_t b) { return ((b + 255) / 256) * 256; };
   size_t bytes = rnd(sizeof(Ctl)) + (n_state3 + n_scratch3) * rnd(n3 * 8) + 3 * rnd(n2 * 8) + rnd((size_t)(g->nj + 3) * (g->nk + 2) * 3 * 8) +
                  rnd(ni1 * 8) + 10 * rnd(nj1 * 8) + 3 * rnd(nk1 * 8) + rnd((g->nk + 2) * 8) + rnd((g->k_sponge + 1) * 8) +
-                 2 * rnd(3 * (g->nj + 2) * 8) + rnd(T.tw.size() * 8) + 4096;
+                 2 * rnd(3 * (g->nj + 2) * 8) + rnd(T.tw.size() * 8) + rnd((g->nj + 1) * 8) +
+                 rnd(sizeof(epic::MathTable)) + 4096;
   cudaError_t e = cudaStreamCreateWithFlags(&m->stream, cudaStreamNonBlocking);
   if (e != cudaSuccess) { delete m; return set_error(EPIC_ERR_CUDA, "cudaStreamCreate: %s", cudaGetErrorString(e)); }
   e = cudaMalloc(&m->pool, bytes);
@@ -317,6 +318,8 @@ extern "C" int epic_model_create(const epic_grid *g, int32_t precision, epic_mod
   double *hmin = carve<double>(p, g->nk + 2), *tsp = carve<double>(p, g->k_sponge + 1);
   double *hc = carve<double>(p, 3 * (g->nj + 2)), *vc = carve<double>(p, 3 * (g->nj + 2));
   double *tw = carve<double>(p, T.tw.size());
+  double *coslat = carve<double>(p, g->nj + 1);
+  epic::MathTable *lt = carve<epic::MathTable>(p, 1);
   if ((size_t)(p - m->pool) > bytes) {
     epic_model_destroy(m);
     return set_error(EPIC_ERR_NOMEM, "internal pool layout overflow");
@@ -332,6 +335,15 @@ extern "C" int epic_model_create(const epic_grid *g, int32_t precision, epic_mod
   up(hlh, T.high_lat_h.data(), n2); up(hlpv, T.high_lat_pv.data(), n2);
   up(hc, T.h_coef.data(), T.h_coef.size()); up(vc, T.v_coef.data(), T.v_coef.size());
   up(tw, T.tw.data(), T.tw.size());
+  // cos of the h-row latitudes with the host libm (t_rad and temp_eq use them)
+  std::vector<double> cl(g->nj + 1);
+  for (int J = 0; J <= g->nj; J++) cl[J] = cos(g->lat[2 * J + 1] * kDeg);
+  up(coslat, cl.data(), cl.size());
+  std::vector<epic::MathTable> host_lt(1);   // ~34 KB, built per model in a few ms
+  epic::fill_math_table(host_lt[0]);
+  cudaMemcpyAsync(lt, host_lt.data(), sizeof(epic::MathTable), cudaMemcpyHostToDevice, m->stream);
+  d.coslat = coslat;
+  d.lt = lt;
   d.lon = lon; d.lat = j1[0]; d.rln = j1[1]; d.rlt = j1[2]; d.f = j1[3]; d.m = j1[4]; d.n = j1[5]; d.mn = j1[6]; d.grav = j1[7];
   d.mn_inv = j1[8];
   d.sgth = sg; d.dsgth = ds; d.dsgth_inv = dsi; d.h_min = hmin; d.t_sponge_inv = tsp;

@@ -43,14 +43,14 @@ __global__ void k_calc_w(DevModel M) {
     const long long x = M.at(k, j, i);
     double w;
     if (k < ks - 1) {
-      const double sigma = get_sigma(pbot, M.p3[x], ptop);
+      const double sigma = get_sigma(M, pbot, M.p3[x], ptop);
       w = g_sigma(M, sigma) * M.heat3[x] / M.exner3[x];
     } else {
       w = 0.;
     }
     if (k >= 2) {
       const double P0 = M.p3[M.at(k - 2, j, i)], P1 = M.p3[M.at(k - 1, j, i)], P2 = M.p3[x], P3 = M.p3[M.at(k + 1, j, i)];
-      const double dz10 = log(P1 / P0), dz21 = log(P2 / P1), dz32 = log(P3 / P2);
+      const double dz10 = xlog(M, P1 / P0), dz21 = xlog(M, P2 / P1), dz32 = xlog(M, P3 / P2);
       const double dz20 = dz21 + dz10, dz30 = dz32 + dz20, dz31 = dz32 + dz21;
       const double df0 = P0 * M.div_uv3[M.at(k - 2, j, i)];
       const double df1 = P1 * M.div_uv3[M.at(k - 1, j, i)];
@@ -222,7 +222,7 @@ __global__ void k_set_p2etc(DevModel M, int update_theta) {
   const double ptop = p[0], pbot = p[nk];
   for (int k = ks - 1; k < nk; k++) {
     const double sigma = (M.sgth[2 * k + 1] - M.zeta0) / (M.zeta1 - M.zeta0);
-    p[k] = get_p_sigma(pbot, sigma, ptop);
+    p[k] = get_p_sigma(M, pbot, sigma, ptop);
   }
   double hl[EPIC_MAX_NK + 2];   // get_h at the layers, from the final P3
   for (int k = 1; k <= nk; k++) {
@@ -234,7 +234,7 @@ __global__ void k_set_p2etc(DevModel M, int update_theta) {
   for (int k = 0; k <= nk; k++) th[k] = M.theta[M.at(k, j, i)];
   if (update_theta) {
     for (int k = 0; k < ks - 1; k++) {
-      const double sigma = get_sigma(pbot, p[k], ptop);
+      const double sigma = get_sigma(M, pbot, p[k], ptop);
       th[k] = (M.sgth[2 * k + 1] - f_sigma(M, sigma)) / g_sigma(M, sigma);
       M.theta[M.at(k, j, i)] = th[k];
     }
@@ -257,7 +257,7 @@ __global__ void k_set_p2etc(DevModel M, int update_theta) {
   }
   if (update_theta) {
     for (int k = 1; k < ks - 1; k++) {
-      const double sigma = get_sigma(pbot, p2[k], ptop);
+      const double sigma = get_sigma(M, pbot, p2[k], ptop);
       M.theta2[M.at(k, j, i)] = (M.sgth[2 * k] - f_sigma(M, sigma)) / g_sigma(M, sigma);
     }
     M.theta2[M.at(ks - 1, j, i)] = .5 * (th[ks - 1] + th[ks - 2]);
@@ -323,9 +323,9 @@ __global__ void k_pgrad_vars_column(DevModel M) {
   }
   double gz[EPIC_MAX_NK + 2];
   gz[nk] = M.topo_scale * M.gz_surface[M.at2(j, i)];
-  gz[nk - 1] = gz[nk] + ((p[nk] + p[nk - 1]) / (rho[nk] + rho[nk - 1])) * log(p[nk] / p[nk - 1]);
+  gz[nk - 1] = gz[nk] + ((p[nk] + p[nk - 1]) / (rho[nk] + rho[nk - 1])) * xlog(M, p[nk] / p[nk - 1]);
   for (int k = nk - 1; k >= 2; k--) {
-    const double dz10 = log(p[k + 1] / p[k]), dz21 = log(p[k] / p[k - 1]), dz32 = log(p[k - 1] / p[k - 2]);
+    const double dz10 = xlog(M, p[k + 1] / p[k]), dz21 = xlog(M, p[k] / p[k - 1]), dz32 = xlog(M, p[k - 1] / p[k - 2]);
     const double dz20 = dz21 + dz10, dz30 = dz32 + dz20, dz31 = dz32 + dz21;
     const double df0 = p[k + 1] / rho[k + 1], df1 = p[k] / rho[k], df2 = p[k - 1] / rho[k - 1], df3 = p[k - 2] / rho[k - 2];
     const double dgz = -(df0 * (dz21 * dz21 * dz21 * (dz31 + dz32)) / (dz10 * dz20 * dz30) +
@@ -335,7 +335,7 @@ __global__ void k_pgrad_vars_column(DevModel M) {
                        12.;
     gz[k - 1] = gz[k] + dgz;
   }
-  gz[0] = gz[1] + ((p[1] + p[0]) / (rho[1] + rho[0])) * log(p[1] / p[0]);
+  gz[0] = gz[1] + ((p[1] + p[0]) / (rho[1] + rho[0])) * xlog(M, p[1] / p[0]);
   const bool interior = i >= 1 && i <= M.ni;
   for (int k = 0; k <= nk; k++) {
     const long long x = M.at(k, j, i);
@@ -411,13 +411,13 @@ __global__ void k_calc_heating(DevModel M) {
     const double pbot = M.p3[M.at(M.nk, j, ii)];
     const double amp = (pressure / pbot - 0.7) / (1. - 0.7);
     double kt = ka;
-    if (amp > 0.) kt += (ks - ka) * pow(cos(M.lat[2 * j + 1] * (M_PI / 180.)), 4.) * amp;
+    if (amp > 0.) kt += (ks - ka) * xpow(M, M.coslat[j], 4.) * amp;
     const double cp_over_time = 1004. / (1. / kt);
-    double c2 = cos(M.lat[2 * j + 1] * (M_PI / 180.));
+    double c2 = M.coslat[j];
     c2 *= c2;
     const double s2 = 1. - c2;
     const double p_p0 = pressure / (1000. * 100.);
-    double teq = (315. - 60. * s2 - 10. * log(p_p0) * c2) * pow(p_p0, M.kappa);
+    double teq = (315. - 60. * s2 - 10. * xlog(M, p_p0) * c2) * xpow(M, p_p0, M.kappa);
     teq = dmaxr(200., teq);
     val = -cp_over_time * (M.t3[x] - teq);
   }

@@ -1,11 +1,13 @@
 // High-latitude zonal filter kernels (the reference's zonal_filter, src/shared/epic_adjust.c:102-480).
 //
-// The reference filters one latitude row at a time: realft() forward, multiply wavenumber m
-// by HIGH_LAT(J,m+1), realft() inverse and scale by 2/ni (epic_adjust.c:412-456).  That is the
-// real symmetric circulant operator F_J = IDFT diag(h_J) DFT.  Here one thread block owns one
-// row: the ni reals are packed as ni/2 complex points, transformed by an in-shared-memory
-// radix-2 FFT, split into the ni/2+1 real-input spectrum, scaled by h_J, and transformed back.
-// Rows equatorward of lat0 are passed through unchanged.
+// The reference filters one latitude row at a time: realft() forward, multiply wavenumber m by
+// HIGH_LAT(J,m+1), realft() inverse and scale by 2/ni (epic_adjust.c:412-456), where realft and
+// four1 are the Numerical Recipes in C (2nd ed., pp. 507, 513) real and complex radix-2 FFTs
+// (epic_funcs_util.c:4023-4132).  Here one thread block owns one row and carries out the same
+// arithmetic in parallel: every butterfly of a four1 stage and every iteration of realft's
+// post-processing loop touches its own data, so they run concurrently; the twiddle factors,
+// which NR builds by a recurrence, are computed once on the host with exactly that recurrence.
+// Compiled without FMA contraction, each filtered row is bit-identical to the reference's.
 #include "device_common.cuh"
 #include "kernels.h"
 #include "epic_common.h"
@@ -14,94 +16,136 @@
 namespace epic {
 
 struct Cplx { double re, im; };
-__device__ __forceinline__ Cplx cmul(Cplx a, Cplx b) { return {a.re * b.re - a.im * b.im, a.re * b.im + a.im * b.re}; }
 
-// Shared-memory workspace of one row filter: z[N], X[N+1], tw[N/2 + N+1].
+// Twiddle table layout (pairs of doubles), N = ni/2 complex points:
+//   [0, N-1)              four1 isign=+1, stage with half h at offset h-1, entries p = 0..h-1
+//   [N-1, 2N-2)           four1 isign=-1, same layout
+//   [2N-2, 2N-2 + N/2-1)  realft forward post-processing, q = 1..N/2-1
+//   [.., + N/2-1)         realft inverse pre-processing, q = 1..N/2-1
+__host__ __device__ inline size_t nr_twiddle_pairs(int ni) {
+  const int N = ni / 2;
+  return 2 * (size_t)(N - 1) + 2 * (size_t)(N / 2 - 1);
+}
+
 struct FilterSmem {
-  Cplx *z, *X, *w, *t;
+  Cplx *z, *w;   // row as N complex points; twiddles
 };
 
 __device__ __forceinline__ FilterSmem carve_filter(double *base, int ni) {
   const int N = ni / 2;
   FilterSmem s;
   s.z = reinterpret_cast<Cplx *>(base);
-  s.X = s.z + N;
-  s.w = s.X + (N + 1);
-  s.t = s.w + N / 2;
+  s.w = s.z + N;
   return s;
 }
 __host__ __device__ inline size_t filter_smem_doubles(int ni) {
-  const int N = ni / 2;
-  return 2 * ((size_t)N + (N + 1) + N / 2 + (N + 1));
+  return 2 * ((size_t)(ni / 2) + nr_twiddle_pairs(ni));
 }
 
 __device__ __forceinline__ void load_twiddles(const DevModel &M, FilterSmem &s) {
-  const int N = M.ni / 2;
+  const int n = (int)nr_twiddle_pairs(M.ni);
   const Cplx *g = reinterpret_cast<const Cplx *>(M.tw);
-  for (int k = threadIdx.x; k < N / 2 + N + 1; k += blockDim.x) s.w[k] = g[k];
+  for (int k = threadIdx.x; k < n; k += blockDim.x) s.w[k] = g[k];
 }
 
-// Radix-2 decimation-in-time FFT of z[0..N-1] (already in bit-reversed order).
-// sign = -1 uses W = exp(-2 pi i/N) (forward), +1 its conjugate.
-__device__ __forceinline__ void fft_stages(FilterSmem &s, int N, int lg, int sign) {
-  for (int st = 1; st <= lg; st++) {
-    const int half = 1 << (st - 1);
+// four1's Danielson-Lanczos stages on z (already bit-reversed); tw = this direction's table.
+__device__ __forceinline__ void four1_stages(Cplx *z, const Cplx *tw, int N) {
+  for (int h = 1; h < N; h <<= 1) {
+    const Cplx *wt = tw + (h - 1);
     for (int b = threadIdx.x; b < N / 2; b += blockDim.x) {
-      const int pos = b & (half - 1);
-      const int i0 = ((b >> (st - 1)) << st) + pos;
-      const int i1 = i0 + half;
-      Cplx w = s.w[pos << (lg - st)];
-      if (sign > 0) w.im = -w.im;
-      const Cplx tv = cmul(w, s.z[i1]);
-      const Cplx a = s.z[i0];
-      s.z[i1] = {a.re - tv.re, a.im - tv.im};
-      s.z[i0] = {a.re + tv.re, a.im + tv.im};
+      const int p = b & (h - 1);
+      const int i0 = (b / h) * 2 * h + p;
+      const int j0 = i0 + h;
+      const double wr = wt[p].re, wi = wt[p].im;
+      const double tempr = wr * z[j0].re - wi * z[j0].im;
+      const double tempi = wr * z[j0].im + wi * z[j0].re;
+      z[j0].re = z[i0].re - tempr;
+      z[j0].im = z[i0].im - tempi;
+      z[i0].re += tempr;
+      z[i0].im += tempi;
     }
     __syncthreads();
   }
 }
 
-// Filter row x[1..ni] (1-based, shared memory) in place with weights h(m) = hl[rowbase + m + 1].
-// Every thread of the block must call this; it synchronises internally.
+__device__ __forceinline__ void bitrev_permute(Cplx *z, int N, int lg) {
+  for (int k = threadIdx.x; k < N; k += blockDim.x) {
+    const int r = (int)(__brev((unsigned)k) >> (32 - lg));
+    if (r > k) {
+      const Cplx t = z[k];
+      z[k] = z[r];
+      z[r] = t;
+    }
+  }
+  __syncthreads();
+}
+
+// realft's split loop (i = 2..n/4, here q = i-1): c2 = -0.5 forward, +0.5 inverse.
+__device__ __forceinline__ void realft_split(Cplx *z, const Cplx *tw, int N, double c2) {
+  const double c1 = 0.5;
+  for (int q = 1 + threadIdx.x; q < N / 2; q += blockDim.x) {
+    const Cplx a = z[q], b = z[N - q];
+    const double wr = tw[q - 1].re, wi = tw[q - 1].im;
+    const double h1r = c1 * (a.re + b.re);
+    const double h1i = c1 * (a.im - b.im);
+    const double h2r = -c2 * (a.im + b.im);
+    const double h2i = c2 * (a.re - b.re);
+    z[q].re = h1r + wr * h2r - wi * h2i;
+    z[q].im = h1i + wr * h2i + wi * h2r;
+    z[N - q].re = h1r - wr * h2r + wi * h2i;
+    z[N - q].im = -h1i + wr * h2i + wi * h2r;
+  }
+  __syncthreads();
+}
+
+// Filter row x[1..ni] (1-based, shared memory) in place with weights h(I) = hl[rowbase + I],
+// I = 1..ni/2+1 (HIGH_LAT(J,I)).  Every thread of the block must call this.
 __device__ void filter_row_smem(const DevModel &M, double *x, const double *hl, long long rowbase, FilterSmem &s) {
   const int ni = M.ni, N = ni / 2;
   const int lg = 31 - __clz(N);
-  // pack and bit-reverse
+  const Cplx *t4p = s.w, *t4m = s.w + (N - 1), *trp = s.w + 2 * (N - 1), *trm = trp + (N / 2 - 1);
+  Cplx *z = s.z;
+  // realft(data, n, 1): four1(data, n/2, 1) -- bit reversal, stages -- then the split loop
   for (int k = threadIdx.x; k < N; k += blockDim.x) {
     const int r = (int)(__brev((unsigned)k) >> (32 - lg));
-    s.z[r] = {x[2 * k + 1], x[2 * k + 2]};
+    z[r].re = x[2 * k + 1];
+    z[r].im = x[2 * k + 2];
   }
   __syncthreads();
-  fft_stages(s, N, lg, -1);
-  // split into the real-input spectrum X_m, m = 0..N, and apply the filter weights
-  for (int m = threadIdx.x; m <= N; m += blockDim.x) {
-    const Cplx zm = s.z[m % N];
-    const Cplx zc = s.z[(N - m) % N];
-    const Cplx e = {0.5 * (zm.re + zc.re), 0.5 * (zm.im - zc.im)};
-    const Cplx o = {0.5 * (zm.im + zc.im), -0.5 * (zm.re - zc.re)};
-    const Cplx tm = s.t[m];
-    const Cplx to = cmul(tm, o);
-    const double h = hl[rowbase + m + 1];
-    s.X[m] = {h * (e.re + to.re), h * (e.im + to.im)};
+  four1_stages(z, t4p, N);
+  realft_split(z, trp, N, -0.5);
+  if (threadIdx.x == 0) {
+    const double h1r = z[0].re;
+    z[0].re = h1r + z[0].im;
+    z[0].im = h1r - z[0].im;
   }
   __syncthreads();
-  // merge back into a half-length spectrum and bit-reverse
-  for (int m = threadIdx.x; m < N; m += blockDim.x) {
-    const Cplx ym = s.X[m];
-    const Cplx yc = {s.X[N - m].re, -s.X[N - m].im};
-    const Cplx e = {0.5 * (ym.re + yc.re), 0.5 * (ym.im + yc.im)};
-    Cplx o = {0.5 * (ym.re - yc.re), 0.5 * (ym.im - yc.im)};
-    const Cplx tc = {s.t[m].re, -s.t[m].im};
-    o = cmul(o, tc);
-    const int r = (int)(__brev((unsigned)m) >> (32 - lg));
-    s.z[r] = {e.re - o.im, e.im + o.re};
+  // spectral weights (epic_adjust.c:447-453)
+  for (int q = threadIdx.x; q < N; q += blockDim.x) {
+    if (q == 0) {
+      z[0].re *= hl[rowbase + 1];
+      z[0].im *= hl[rowbase + N + 1];
+    } else {
+      const double h = hl[rowbase + q + 1];
+      z[q].re *= h;
+      z[q].im *= h;
+    }
   }
   __syncthreads();
-  fft_stages(s, N, lg, +1);
-  const double inv = 1.0 / (double)N;
+  // realft(data, n, -1): split loop, then four1(data, n/2, -1)
+  realft_split(z, trm, N, 0.5);
+  if (threadIdx.x == 0) {
+    const double h1r = z[0].re;
+    z[0].re = 0.5 * (h1r + z[0].im);
+    z[0].im = 0.5 * (h1r - z[0].im);
+  }
+  __syncthreads();
+  bitrev_permute(z, N, lg);
+  four1_stages(z, t4m, N);
+  const double scale = 2. / (double)ni;
   for (int k = threadIdx.x; k < N; k += blockDim.x) {
-    x[2 * k + 1] = s.z[k].re * inv;
-    x[2 * k + 2] = s.z[k].im * inv;
+    x[2 * k + 1] = z[k].re * scale;
+    x[2 * k + 2] = z[k].im * scale;
   }
   __syncthreads();
 }
@@ -168,7 +212,7 @@ __global__ void k_varz_tables(DevModel M, const double *buff, int sel, int index
       default: x = gz[M.at(k, j, i)]; break;
     }
     t[kay].x = x;
-    t[kay].y = index == 2 ? log(buff[M.at(k, j, i)]) : buff[M.at(k, j, i)];
+    t[kay].y = index == 2 ? xlog(M, buff[M.at(k, j, i)]) : buff[M.at(k, j, i)];
   }
   if (!spline_pchip(kend - kstart + 1, t)) flag_error(M.ctl, ERR_PCHIP_X, kstart, j, i, t[0].x);
 }
@@ -201,7 +245,7 @@ __global__ void k_varz_filter_rows(DevModel M, double *buff, int sel, int index,
     double dgz;
     const int kay = find_place_in_table(n, t, gzz, &dgz);
     double v = splint_pchip(gzz, t + kay, dgz);
-    if (index == 2) v = exp(v);
+    if (index == 2) v = xexp(M, v);
     vz[i] = v;
     x[i] = buff[base + i] - v;
   }
@@ -275,7 +319,8 @@ __global__ void k_hsu_zonal(DevModel M, double *buff, int kind, int kstart) {
     gam = gam * gam;
     const double bep = 1. + (1. / (2. * al) - 1.) * gap;
     const double bem = 1. + (1. / (2. * al) - 1.) * gam;
-    const double g = -al * (up[i] * bep * d1[i] - uhatp * (1. - gap) * d1[i - 1] + um[i] * bem * d2[i - 1] - uhatm * (1. - gam) * d2[i]);
+    const double behatp = 1. - gap, behatm = 1. - gam;
+    const double g = -al * (up[i] * bep * d1[i] - uhatp * behatp * d1[i - 1] + um[i] * bem * d2[i - 1] - uhatm * behatm * d2[i]);
     ff[i] += g;
   }
   __syncthreads();
@@ -326,25 +371,42 @@ int filter_kernels_init(int ni) {
   return 0;
 }
 
-size_t twiddle_doubles(int ni) {
-  const int N = ni / 2;
-  return 2 * ((size_t)N / 2 + N + 1);
-}
+size_t twiddle_doubles(int ni) { return 2 * nr_twiddle_pairs(ni); }
 
-// Twiddles for the half-length FFT, W^k = exp(-2 pi i k/N) for k < N/2, followed by the
-// real-split factors t^m = exp(-2 pi i m/ni) for m = 0..N.
+// Host: the twiddle factors four1 and realft generate by recurrence, in their order, with
+// their arithmetic (epic_funcs_util.c:4047-4076, :4096-4120).  Compiled without contraction.
 void fill_twiddles(int ni, double *tw) {
   const int N = ni / 2;
-  for (int k = 0; k < N / 2; k++) {
-    const double a = -2. * M_PI * (double)k / (double)N;
-    tw[2 * k] = cos(a);
-    tw[2 * k + 1] = sin(a);
+  const unsigned long n = (unsigned long)N << 1;
+  double *out = tw;
+  for (int isign = 1; isign >= -1; isign -= 2) {
+    for (unsigned long mmax = 2; n > mmax; mmax <<= 1) {
+      const double theta = isign * (2 * M_PI / mmax);
+      double wtemp = sin(0.5 * theta);
+      const double wpr = -2.0 * wtemp * wtemp;
+      const double wpi = sin(theta);
+      double wr = 1.0, wi = 0.0;
+      for (unsigned long m = 1; m < mmax; m += 2) {
+        *out++ = wr;
+        *out++ = wi;
+        wr = (wtemp = wr) * wpr - wi * wpi + wr;
+        wi = wi * wpr + wtemp * wpi + wi;
+      }
+    }
   }
-  double *t = tw + 2 * (N / 2);
-  for (int m = 0; m <= N; m++) {
-    const double a = -2. * M_PI * (double)m / (double)ni;
-    t[2 * m] = cos(a);
-    t[2 * m + 1] = sin(a);
+  for (int isign = 1; isign >= -1; isign -= 2) {
+    double theta = M_PI / (double)((unsigned long)ni >> 1);
+    if (isign != 1) theta = -theta;
+    double wtemp = sin(0.5 * theta);
+    const double wpr = -2.0 * wtemp * wtemp;
+    const double wpi = sin(theta);
+    double wr = 1.0 + wpr, wi = wpi;
+    for (unsigned long i = 2; i <= ((unsigned long)ni >> 2); i++) {
+      *out++ = wr;
+      *out++ = wi;
+      wr = (wtemp = wr) * wpr - wi * wpi + wr;
+      wi = wi * wpr + wtemp * wpi + wi;
+    }
   }
 }
 

@@ -1,9 +1,11 @@
 """Parity of the CUDA step (through the C ABI) with the oracle's CPU restatement.
 
-Tolerances: the plain FP64 path must match the reference CPU build to relative L2 <= 1e-11
-per prognostic after 1 step and <= 1e-8 after 100 steps.  Kernel by kernel the GPU and the
-restatement differ only by FMA contraction, summation order and libm ulps, so single stages
-are held to 1e-12.
+Tolerances: the FP64 form must match the reference CPU build to relative L2 <= 1e-11 per
+prognostic after 1 step and <= 1e-8 after 100 steps.  Kernel by kernel, the GPU evaluates the
+reference's expressions in the reference's order without FMA contraction, with correctly rounded
+log/exp/pow and a bit-exact restatement of realft, so stages without transcendentals must be
+bit-identical; stages with them differ only where glibc itself misrounds (a few cells) and are
+held to 1e-12, except DZDT3, a difference of successive geopotentials (1e-10).
 """
 import numpy as np
 import pytest
@@ -15,6 +17,9 @@ from oracle_lib import Port
 pytestmark = pytest.mark.gpu
 
 STEP_STAGES = [0, 1, 2, 3, 4, 5, 6, 7, 8, 9, 10, 11, 7, 12, 13, 14, 15, 16, 17]
+# stages whose kernels evaluate no log/exp/pow: the GPU must reproduce the restatement bit for bit
+BITWISE_STAGES = {0, 1, 3, 4, 5, 8, 9, 12, 13, 14, 15, 16}
+FIELD_TOL = {"dzdt3": 1e-10}
 STAGE_NAMES = {0: "zero_tend", 1: "source_sink", 2: "calc_w", 3: "uv_core", 4: "uv_drag", 5: "scalar_hypervisc",
                6: "advection", 7: "store_pgrad_vars", 8: "gz_filter", 9: "filter_tend_3d", 10: "filter_mass_3d",
                11: "set_p2etc", 12: "uv_pgrad", 13: "div_damp", 14: "uv_update", 15: "uv_hypervisc",
@@ -56,10 +61,14 @@ def test_stage_by_stage(gpu, scheme):
         model.sync()
         a, b = model.download(), port.download()
         errs = field_errors(a, b)
-        name, e = worst(errs)
-        if e > 1e-12:
-            failures.append(f"stage {st} {STAGE_NAMES[st]}: worst {name} rel L2 {e:.3e}")
-            # continue from the oracle's state so later stages are tested on their own
+        bad = {k: v[0] for k, v in errs.items() if v[0] > FIELD_TOL.get(k, 1e-12)}
+        ndiff = sum(int((a.arrays[k] != b.arrays[k]).sum()) for k in a.arrays)
+        if bad:
+            failures.append(f"stage {st} {STAGE_NAMES[st]}: {bad}")
+        if st in BITWISE_STAGES and ndiff:
+            failures.append(f"stage {st} {STAGE_NAMES[st]}: {ndiff} cells differ, expected bit-identical")
+        if bad or ndiff:
+            # continue from the oracle's state so that later stages are tested on their own
             model.upload(b)
     assert not failures, "\n".join(failures)
 
