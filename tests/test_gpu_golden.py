@@ -1,0 +1,34 @@
+"""The CUDA step, from the inputs stored in tests/golden/*.npz, against the reference build's
+outputs stored there (made by tests/golden/make_golden.py from the reference sources)."""
+import glob
+import os
+
+import numpy as np
+import pytest
+
+from epic_gb300 import EPIC_SYNC_DIAGS_ONLY, Model
+from test_oracle import compare_snapshot, grid_from_fixture, inputs_from_fixture, snapshots
+
+pytestmark = pytest.mark.gpu
+GOLDEN = sorted(glob.glob(os.path.join(os.path.dirname(__file__), "golden", "*.npz")))
+
+
+@pytest.mark.parametrize("path", GOLDEN, ids=[os.path.basename(p) for p in GOLDEN])
+def test_golden_gpu(gpu, path):
+    """Relative L2 per field <= 1e-11 after the synchronising call and after each step."""
+    z = np.load(path)
+    ga = grid_from_fixture(z)
+    f = inputs_from_fixture(z, ga)
+    m = Model(ga)
+    m.upload(f)
+    done = 0
+    for tag in snapshots(z):
+        if tag == "sync":
+            m.timestep(EPIC_SYNC_DIAGS_ONLY)
+        else:
+            n = int(tag[4:])
+            m.run(n - done)
+            done = n
+        m.sync()
+        bad = compare_snapshot(m.download(), z, tag, 1e-11)
+        assert not bad, (tag, bad)

@@ -1,0 +1,129 @@
+"""The oracle: its CPU restatement against the reference build and the golden fixtures.
+
+* test_restatement_matches_reference: the restatement (oracle/epic_port.c) reproduces the
+  reference's own step (oracle/_ref, compiled from the reference sources) bit for bit.  Runs
+  only where the reference tree is present.
+* test_golden_*: the restatement, from the inputs stored in tests/golden/*.npz, against the
+  reference outputs stored there.  Runs everywhere (the fixtures were made by
+  tests/golden/make_golden.py from the reference build).
+"""
+import glob
+import os
+
+import numpy as np
+import pytest
+
+from compare import PROGNOSTIC, field_errors
+from epic_gb300 import EPIC_SYNC_DIAGS_ONLY, EPIC_UV_AB3, EPIC_UV_LEAPFROG, Fields, GridArrays, HSConfig, hs_setup
+from oracle_lib import Port, dict_to_fields, fields_to_dict, reference_available, run_reference
+
+GOLDEN = sorted(glob.glob(os.path.join(os.path.dirname(__file__), "golden", "*.npz")))
+
+
+def grid_from_fixture(z) -> GridArrays:
+    ni, nj, nk = int(z["scalar_ni"]), int(z["scalar_nj"]), int(z["scalar_nk"])
+    ga = GridArrays(ni, nj, nk)
+    for k in ga.arrays:
+        ga.arrays[k][...] = z["grid_" + k]
+    for name in z.files:
+        if name.startswith("scalar_"):
+            key = name[len("scalar_"):]
+            v = z[name]
+            if key == "nu":
+                for i in range(9):
+                    ga.struct.nu[i] = float(v[i])
+            else:
+                setattr(ga.struct, key, v.item())
+    return ga
+
+
+def inputs_from_fixture(z, ga) -> Fields:
+    f = Fields(ga.layout.ni, ga.layout.nj, ga.layout.nk, int(z["scalar_uv_scheme"]))
+    for k in ("u", "v", "dudt", "dvdt", "hdry", "theta", "p3", "gz_surface", "u_spinup"):
+        f.arrays[k][...] = z["in_" + k]
+    for n in ("it_zero", "it_minus1", "it_minus2", "itime", "model_time"):
+        setattr(f.struct, n, int(z["in_" + n]))
+    return f
+
+
+def snapshots(z):
+    tags = sorted({n.split("_")[0] for n in z.files if n.startswith(("sync_", "step"))},
+                  key=lambda t: -1 if t == "sync" else int(t[4:]))
+    return tags
+
+
+def compare_snapshot(f: Fields, z, tag, tol):
+    bad = {}
+    for k in ("u", "v", "hdry", "theta", "p3", "gz3", "pv3", "w3", "heat3", "div_uv3"):
+        want = z[f"{tag}_{k}"]
+        got = f.arrays[k]
+        big = np.abs(want) > 1e300
+        assert np.array_equal(np.abs(got) > 1e300, big), (tag, k)
+        w, g = np.where(big, 0., want), np.where(big, 0., got)
+        den = np.linalg.norm(w)
+        rel = np.linalg.norm(g - w) / den if den > 0 else np.linalg.norm(g - w)
+        if rel > tol:
+            bad[k] = rel
+    for n in ("it_zero", "it_minus1", "it_minus2", "model_time"):
+        assert int(getattr(f.struct, n)) == int(z[f"{tag}_{n}"]), (tag, n)
+    return bad
+
+
+@pytest.mark.parametrize("path", GOLDEN, ids=[os.path.basename(p) for p in GOLDEN])
+def test_golden_restatement(path):
+    """Restatement vs the reference's outputs stored in the fixture (1e-13: identical bits on
+    x86-64; aarch64 glibc may round a few log/exp/pow results differently)."""
+    z = np.load(path)
+    ga = grid_from_fixture(z)
+    f = inputs_from_fixture(z, ga)
+    port = Port(ga)
+    port.upload(f)
+    done = 0
+    for tag in snapshots(z):
+        if tag == "sync":
+            port.timestep(EPIC_SYNC_DIAGS_ONLY)
+        else:
+            n = int(tag[4:])
+            port.run(n - done)
+            done = n
+        bad = compare_snapshot(port.download(), z, tag, 1e-13)
+        assert not bad, (tag, bad)
+
+
+def test_golden_inputs_match_generator():
+    """The committed inputs equal what epic_hs_grid_build/epic_hs_initial_state produce now."""
+    z = np.load(os.path.join(os.path.dirname(__file__), "golden", "hs32x16x10_ab3.npz"))   # seed 11
+    ga0 = grid_from_fixture(z)
+    s = ga0.struct
+    cfg = HSConfig(ni=s.ni, nj=s.nj, nk=s.nk, dt=s.dt, uv_scheme=s.uv_scheme, seed=11)
+    ga, f = hs_setup(cfg)
+    for k in ga.arrays:
+        np.testing.assert_allclose(ga.arrays[k], ga0.arrays[k], rtol=1e-14, atol=0, err_msg=k)
+    np.testing.assert_allclose(f.arrays["p3"], z["in_p3"], rtol=1e-13, atol=0)
+    np.testing.assert_allclose(f.arrays["theta"], z["in_theta"], rtol=1e-13, atol=0)
+
+
+@pytest.mark.reference
+@pytest.mark.parametrize("scheme,shape,steps", [(EPIC_UV_AB3, (64, 32, 10), 12), (EPIC_UV_LEAPFROG, (32, 16, 10), 6),
+                                                 (EPIC_UV_AB3, (32, 16, 20), 4)])
+def test_restatement_matches_reference(scheme, shape, steps):
+    if not reference_available():
+        pytest.skip("reference source tree not present on this host")
+    ni, nj, nk = shape
+    cfg = HSConfig(ni=ni, nj=nj, nk=nk, dt=300, uv_scheme=scheme, seed=5)
+    ga, f = hs_setup(cfg)
+    sched = [("sync", 0)] + [("step", 1)] * steps
+    geo, snaps = run_reference(ga, f, sched)
+    assert max(geo) == 0.0, "grid geometry differs from the reference's set_lonlat/set_fmn/set_gravity/set_dsgth"
+    port = Port(ga)
+    port.upload(f)
+    for i, (what, n) in enumerate(sched):
+        if what == "sync":
+            port.timestep(EPIC_SYNC_DIAGS_ONLY)
+        else:
+            port.run(n)
+        got = port.download()
+        want = dict_to_fields(snaps[i], ni, nj, nk, scheme)
+        for k in got.arrays:
+            assert np.array_equal(got.arrays[k], want.arrays[k]), f"snapshot {i}: field {k} differs"
+        assert fields_to_dict(got)["it_zero"] == snaps[i]["it_zero"]
