@@ -56,6 +56,7 @@ def load_library(path: str | None = None) -> C.CDLL:
     lib.epic_model_kernels_per_step.restype = C.c_int32
     lib.epic_model_device_bytes.argtypes = [C.c_void_p]
     lib.epic_model_device_bytes.restype = C.c_int64
+    lib.epic_model_filter_mass_noalloc.argtypes = [C.c_void_p]
     lib.epic_hs_grid_build.argtypes = [C.POINTER(EpicHsParams), C.POINTER(EpicGrid), C.POINTER(C.c_double),
                                        C.POINTER(C.c_double)]
     lib.epic_hs_initial_state.argtypes = [C.POINTER(EpicGrid), C.POINTER(EpicHsParams), C.c_uint64, C.c_double,
@@ -126,6 +127,10 @@ class Model:
 
     def sync(self) -> None:
         _check(self.lib.epic_model_sync(self._h), "epic_model_sync")
+
+    def filter_mass_noalloc(self) -> None:
+        """run_stage(10) with the filter's profile tables in the library's fixed device array."""
+        _check(self.lib.epic_model_filter_mass_noalloc(self._h), "epic_model_filter_mass_noalloc")
 
     def step_host(self, f: Fields, nsteps: int, prime: bool = False) -> None:
         _check(self.lib.epic_model_step_host(self._h, C.byref(f.struct), int(prime), nsteps), "epic_model_step_host")

@@ -4,6 +4,7 @@
 #include <cstdio>
 #include <cstdlib>
 #include <cstring>
+#include <mutex>
 #include <vector>
 #include "device_common.cuh"
 #include "kernels.h"
@@ -509,3 +510,63 @@ extern "C" void *epic_model_stream(epic_model *m) { return m ? (void *)m->stream
 extern "C" int32_t epic_model_kernels_per_step(const epic_model *m) { return m ? m->kernels_per_step : -1; }
 
 extern "C" int64_t epic_model_device_bytes(const epic_model *m) { return m ? (int64_t)m->pool_bytes : 0; }
+
+// ---- the 3-D mass filter with a fixed scratch table (epic_model_filter_mass_noalloc) ----
+//
+// Some callers cannot allocate device memory at the point where they want the filter: a
+// serving loop that has already handed every byte of its HBM budget to admitted runs, or code
+// running beside other streams' work, where a cudaMalloc/cudaFree could stall on that work.
+// For them the PCHIP profile tables, (nj+3)*(nk+2) entries of (x, y, slope), live in one array
+// compiled into the library, sized for grids up to EPIC_NOALLOC_TABLE_ENTRIES entries
+// (384 KiB).  Everything else the filter reads is the model's own, allocated once in
+// epic_model_create.
+
+static __device__ __align__(256) double g_noalloc_ptable[3 * EPIC_NOALLOC_TABLE_ENTRIES];
+
+namespace {
+
+constexpr int kNoallocMaxDevices = 64;
+std::mutex g_noalloc_mu;
+double *g_noalloc_addr[kNoallocMaxDevices] = {nullptr};
+
+// Address of g_noalloc_ptable on device `dev`, which must be current.  Resolved once per device.
+int noalloc_table(int dev, double **out) {
+  if (dev < 0 || dev >= kNoallocMaxDevices) return set_error(EPIC_ERR_ARG, "device %d out of range", dev);
+  std::lock_guard<std::mutex> lock(g_noalloc_mu);
+  if (!g_noalloc_addr[dev]) {
+    void *p = nullptr;
+    const cudaError_t e = cudaGetSymbolAddress(&p, g_noalloc_ptable);
+    if (e != cudaSuccess || !p) return set_error(EPIC_ERR_CUDA, "cudaGetSymbolAddress: %s", cudaGetErrorString(e));
+    g_noalloc_addr[dev] = static_cast<double *>(p);
+  }
+  *out = g_noalloc_addr[dev];
+  return EPIC_OK;
+}
+
+}  // namespace
+
+extern "C" int epic_model_filter_mass_noalloc(epic_model *m) {
+  if (!m) return set_error(EPIC_ERR_ARG, "epic_model_filter_mass_noalloc: NULL model");
+  const long long entries = (long long)(m->d.nj + 3) * (m->d.nk + 2);
+  if (entries > EPIC_NOALLOC_TABLE_ENTRIES)
+    return set_error(EPIC_ERR_ARG, "epic_model_filter_mass_noalloc: (nj+3)*(nk+2) = %lld exceeds %d", entries,
+                     EPIC_NOALLOC_TABLE_ENTRIES);
+  if (!m->uploaded) return set_error(EPIC_ERR_STATE, "filter before upload");
+  int dev = -1, cur = -1;
+  EPIC_CUDA_CHECK(cudaStreamGetDevice(m->stream, &dev));
+  EPIC_CUDA_CHECK(cudaGetDevice(&cur));
+  if (dev != cur) EPIC_CUDA_CHECK(cudaSetDevice(dev));
+  double *table = nullptr;
+  int rc = noalloc_table(dev, &table);
+  if (rc == EPIC_OK) {
+    DevModel M = m->d;   // the model's description with only the table pointer replaced
+    M.ptable = table;
+    cudaStream_t s = m->stream;
+    epic::launch_varz_filter(M, M.hdry, epic::PL_NONE, 2, 1, M.nk, s);
+    epic::launch_restore_mass(M, s);
+    epic::launch_varz_filter(M, M.theta, epic::PL_NONE, 3, M.k_sigma - 1, M.nk, s);
+    rc = check_launch("epic_model_filter_mass_noalloc");
+  }
+  if (dev != cur) cudaSetDevice(cur);
+  return rc;
+}

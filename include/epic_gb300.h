@@ -166,6 +166,23 @@ int32_t epic_model_kernels_per_step(const epic_model *m);
 /* Bytes of device memory the model holds. */
 int64_t epic_model_device_bytes(const epic_model *m);
 
+/*
+ * The 3-D zonal filter of the mass variables (stage 10 above: zonal_filter(HDRY_INDEX, ...,
+ * THREEDIM), restore_mass, zonal_filter(THETA_INDEX, ..., THREEDIM); epic_timestep.c:207-222),
+ * with its per-row PCHIP profile tables held in a fixed device array of the library instead of
+ * the model's own scratch.  It allocates nothing: no cudaMalloc/cudaFree and no library call
+ * that allocates.  No counterpart in the reference.
+ *
+ * Limit: (nj+3)*(nk+2) <= EPIC_NOALLOC_TABLE_ENTRIES; larger grids return EPIC_ERR_ARG.
+ * The first call on a device resolves the array's address (cudaGetSymbolAddress with the
+ * model's device current); make that first call before any stream capture begins.  Nothing in
+ * the array needs to start at zero: every table entry is written before it is read in the same
+ * call.  The array is shared by every model on the device, so calls must not overlap: issue
+ * them on one stream, or synchronise between them.  Results equal epic_model_run_stage(m, 10).
+ */
+#define EPIC_NOALLOC_TABLE_ENTRIES 16384
+int  epic_model_filter_mass_noalloc(epic_model *m);
+
 /* Text of the last error on this thread. */
 const char *epic_last_error(void);
 
