@@ -13,8 +13,15 @@
 // double); exp by x = (1024 q + j) ln2/1024 + r with a table of 2^(j/1024), exp(r) by its Taylor
 // series; pow = exp(y log x) with the double-double logarithm.  The tables are built on the
 // host from slow, long double-double series (2 atanh((c-1)/(c+1)) and exp(y/2^10)^(2^10)).
+//
+// Each function first takes a fast path (Ziv's strategy): the same reductions with a shorter
+// evaluation whose error is bounded well below 2^-69 of the result, then a rounding test that
+// returns the result only if both ends of the error interval round to the same double.  About
+// one call in 2^16 fails the test and goes on to the double-double evaluation above.
 #pragma once
 #include <cmath>
+#include <cstdint>
+#include <cstring>
 
 namespace epic {
 
@@ -163,22 +170,118 @@ __host__ __device__ __forceinline__ double dd_exp_round(dd x, const MathTable &T
   return ldexp(v.hi, q);
 }
 
+// ---- fast paths ----
+
+__host__ __device__ __forceinline__ uint64_t dbits(double x) {
+#ifdef __CUDA_ARCH__
+  return (uint64_t)__double_as_longlong(x);
+#else
+  uint64_t u;
+  memcpy(&u, &x, 8);
+  return u;
+#endif
+}
+__host__ __device__ __forceinline__ double dfrom(uint64_t u) {
+#ifdef __CUDA_ARCH__
+  return __longlong_as_double((long long)u);
+#else
+  double x;
+  memcpy(&x, &u, 8);
+  return x;
+#endif
+}
+// 2^q for -1022 <= q <= 1023
+__host__ __device__ __forceinline__ double pow2i(int q) { return dfrom((uint64_t)(q + 1023) << 52); }
+
+// log(x) as an unevaluated sum hi + lo, x > 0 finite and normal, x != 1.  |error| < 2^-72 |log x|:
+// x = 2^e m, m = c (1 + r) as in dd_log; log(1+r) = r - r^2/2 + r^3 (1/3 - r/4 + ... - r^5/8), with
+// r^2 split exactly by TwoProd and |r| < 6.9e-4 (the r^9 truncation is < 2^-90 |r|).
+__host__ __device__ __forceinline__ dd fast_log(double x, const MathTable &T) {
+  const uint64_t u = dbits(x);
+  int e = (int)(u >> 52) - 1023;
+  double m = dfrom((u & 0x000FFFFFFFFFFFFFull) | 0x3FF0000000000000ull);   // [1, 2)
+  if (m > 1.4142135623730951) { m *= 0.5; e += 1; }
+  const int k = (int)rint(m * 1024.);
+  const double c = (double)k * (1. / 1024.);
+  const double num = m - c;                          // exact (Sterbenz)
+  const double invc = T.invc[k - LOG_K0];
+  const double rh = num * invc;
+  const double rl = fma(-rh, c, num) * invc;
+  const dd r2 = two_prod(rh, rh);
+  const double tail = (rh * r2.hi) *
+                      (1. / 3. - rh * (0.25 - rh * (0.2 - rh * (1. / 6. - rh * (1. / 7. - rh * 0.125)))));
+  const dd lc = T.logc[k - LOG_K0];
+  const double ed = (double)e;
+  const dd a = two_prod(ed, T.ln2.hi);
+  const dd s1 = two_sum(a.hi, lc.hi);
+  const dd s2 = two_sum(s1.hi, rh);
+  const dd s3 = two_sum(s2.hi, -0.5 * r2.hi);
+  const double lo = (((a.lo + s1.lo) + (s2.lo + s3.lo)) + (ed * T.ln2.lo + lc.lo)) + ((rl - rh * rl) - 0.5 * r2.lo + tail);
+  return fast_two_sum(s3.hi, lo);
+}
+
+// exp(x) for x = xh + xl (|xh| < 700, |xl| <= ulp(xh)) as 2^q (hi + lo).  |error| < 2^-72 of the
+// result: x = (1024 q + j) ln2/1024 + r, |r| <= ln2/2048 (+ rounding), exp(r) - 1 =
+// r + r^2/2 + r^3 (1/6 + r/24 + r^2/120) with r^2 split exactly (the r^6 truncation is < 2^-78).
+__host__ __device__ __forceinline__ dd fast_exp(double xh, double xl, const MathTable &T, int &q) {
+  const double nf = rint(xh * (1024. / 0.69314718055994529));
+  const dd p = two_prod(nf, T.ln2_1024.hi);
+  const double rh = xh - p.hi;                       // exact: xh and p.hi are within a factor 2
+  const double rl = (xl - p.lo) - nf * T.ln2_1024.lo;
+  const long long n = (long long)nf;
+  const int j = (int)(n & 1023);
+  q = (int)((n - j) / 1024);
+  const dd r2 = two_prod(rh, rh);
+  const double tail = (rh * r2.hi) * (1. / 6. + rh * (1. / 24. + rh * (1. / 120.)));
+  const double qlo = rl + rh * rl + 0.5 * r2.lo + tail;   // exp(r) - 1 = rh + r2.hi/2 + qlo
+  const dd t = T.exp2j[j];
+  const dd a = two_prod(t.hi, rh);
+  const dd b = two_prod(t.hi, 0.5 * r2.hi);
+  const dd s1 = fast_two_sum(t.hi, a.hi);
+  const dd s2 = fast_two_sum(s1.hi, b.hi);
+  const double lo = ((s1.lo + s2.lo) + (a.lo + b.lo)) + (t.hi * qlo + (t.lo + t.lo * (rh + 0.5 * r2.hi)));
+  return fast_two_sum(s2.hi, lo);
+}
+
+// Round hi + lo if every value within err of it rounds the same way; else report failure.
+__host__ __device__ __forceinline__ bool round_test(dd v, double err, double &out) {
+  const double a = v.hi + (v.lo - err), b = v.hi + (v.lo + err);
+  out = a;
+  return a == b;
+}
+
 __host__ __device__ __forceinline__ double cr_log(double x, const MathTable &T) {
   if (!(x > 0.) || !(x < INFINITY) || x < 2.2250738585072014e-308) return log(x);
   if (x == 1.) return 0.;
+  const dd v = fast_log(x, T);
+  double r;
+  if (round_test(v, fabs(v.hi) * 0x1p-69, r)) return r;
   return dd_log(x, T).hi;
 }
 __host__ __device__ __forceinline__ double cr_exp(double x, const MathTable &T) {
   if (!(fabs(x) < 700.)) return exp(x);
   if (x == 0.) return 1.;
+  int q;
+  const dd v = fast_exp(x, 0., T, q);
+  double r;
+  if (round_test(v, fabs(v.hi) * 0x1p-69, r)) return r * pow2i(q);
   return dd_exp_round({x, 0.}, T);
 }
 __host__ __device__ __forceinline__ double cr_pow(double x, double y, const MathTable &T) {
   if (y == 0. || x == 1.) return 1.;
   if (!(x > 0.) || !(x < INFINITY) || x < 2.2250738585072014e-308 || !(fabs(y) < 1e6)) return pow(x, y);
-  const dd l = dd_mul_d(dd_log(x, T), y);
-  if (!(fabs(l.hi) < 700.)) return pow(x, y);
-  return dd_exp_round(l, T);
+  const dd l = fast_log(x, T);
+  dd yl = two_prod(y, l.hi);
+  yl.lo += y * l.lo;
+  if (!(fabs(yl.hi) < 700.)) return pow(x, y);
+  yl = fast_two_sum(yl.hi, yl.lo);
+  int q;
+  const dd v = fast_exp(yl.hi, yl.lo, T, q);
+  double r;
+  // the logarithm's relative error 2^-72 becomes an absolute error in y log x
+  if (round_test(v, fabs(v.hi) * (0x1p-69 + fabs(yl.hi) * 0x1p-68), r)) return r * pow2i(q);
+  const dd ls = dd_mul_d(dd_log(x, T), y);
+  return dd_exp_round(ls, T);
 }
 
 }  // namespace epic

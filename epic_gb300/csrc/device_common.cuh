@@ -96,6 +96,14 @@ __device__ __forceinline__ double f_sigma(const DevModel &M, double s) {
   if (s < 1.) return (1. - g_sigma(M, s)) * (M.zeta0 + s * (M.zeta1 - M.zeta0));
   return 0.;
 }
+// f_sigma(s), with g_sigma(s) returned in g: one exponential serves both.
+__device__ __forceinline__ double f_and_g_sigma(const DevModel &M, double s, double &g) {
+  g = g_sigma(M, s);
+  if (s < 0.) return M.zeta0;
+  if (s <= M.sigma_sigma) return M.zeta0 + s * (M.zeta1 - M.zeta0);
+  if (s < 1.) return (1. - g) * (M.zeta0 + s * (M.zeta1 - M.zeta0));
+  return 0.;
+}
 __device__ __forceinline__ double return_sigmatheta(const DevModel &M, double theta, double p, double pbot, double ptop) {
   if (p <= ptop) return theta;
   const double s = get_sigma(M, pbot, p, ptop);

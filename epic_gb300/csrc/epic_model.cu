@@ -350,6 +350,7 @@ extern "C" int epic_model_create(const epic_grid *g, int32_t precision, epic_mod
   d.sgth = sg; d.dsgth = ds; d.dsgth_inv = dsi; d.h_min = hmin; d.t_sponge_inv = tsp;
   d.high_lat_h = hlh; d.high_lat_pv = hlpv; d.h_coef = hc; d.v_coef = vc; d.tw = tw;
   epic::filter_kernels_init(g->ni);
+  epic::column_kernels_init(g->nk);
   e = cudaStreamSynchronize(m->stream);
   if (e != cudaSuccess) {
     epic_model_destroy(m);

@@ -27,52 +27,110 @@ __global__ void k_source_sink(DevModel M) {
   }
 }
 
+// ---- column tiles ----
+//
+// The transcendental work of calc_w, set_p2etc and store_pgrad_vars is pointwise once a
+// column's pressures are known; only their running sums are sequential.  A block takes 32
+// neighbouring columns (one per lane; neighbouring columns are neighbouring addresses, so every
+// level is one coalesced 256-byte access) and stages their levels in shared memory as
+// [k][lane].  Pointwise phases spread the levels over CT_WARPS warps; warp 0 alone runs each
+// running sum, in the reference's order, so the results are those of one thread per column.
+constexpr int CT_WARPS = 8;
+constexpr int CT_THREADS = 32 * CT_WARPS;
+
+struct ColTile {
+  int lane, warp, j, i;
+  bool valid;
+  long long base;   // M.at(0, j, i)
+};
+__device__ __forceinline__ ColTile col_tile(const DevModel &M) {
+  ColTile c;
+  c.lane = (int)(threadIdx.x & 31);
+  c.warp = (int)(threadIdx.x >> 5);
+  const int t = (int)blockIdx.x * 32 + c.lane;
+  c.valid = t < (M.nj + 1) * M.iadim;
+  c.j = c.valid ? t / M.iadim : 0;
+  c.i = c.valid ? t - c.j * M.iadim : 0;
+  c.base = M.at(0, c.j, c.i);
+  return c;
+}
+// level k of a [k][lane] shared array
+#define CT(a, k) (a)[(k) * 32 + c.lane]
+
+// return_sigmatheta (epic_funcs_diag.c:1238-1250) with log(ptop/pbot) supplied
+__device__ __forceinline__ double sigmatheta_lp(const DevModel &M, double theta, double p, double pbot, double ptop, double lp) {
+  if (p <= ptop) return theta;
+  const double s = xlog(M, p / pbot) / lp;
+  double g;
+  const double f = f_and_g_sigma(M, s, g);
+  return f + g * theta;
+}
+
 // calc_w, epic_flux.c:123-335.  The Leslie-Purser summed divergence keeps SUM_DIV = 0 at
 // k = 1 and k = nk in every real column (the reference assigns those entries outside its
 // column loops, epic_flux.c:224-226, :259-261), so the dF/dpbot term vanishes.
-__global__ void k_calc_w(DevModel M) {
-  int j, i;
-  if (!col_index(M, j, i)) return;
-  const int nk = M.nk, ks = M.k_sigma;
-  const double ptop = M.p3[M.at(0, j, i)], pbot = M.p3[M.at(nk, j, i)];
-  const double psigma = M.p3[M.at(ks - 1, j, i)];
-  M.w3[M.at(0, j, i)] = 0.;
-  M.w3[M.at(nk, j, i)] = 0.;
-  double sum_div = 0.;   // SUM_DIV(k) for the current k
-  for (int k = 1; k < nk; k++) {
-    const long long x = M.at(k, j, i);
-    double w;
-    if (k < ks - 1) {
-      const double sigma = get_sigma(M, pbot, M.p3[x], ptop);
-      w = g_sigma(M, sigma) * M.heat3[x] / M.exner3[x];
-    } else {
-      w = 0.;
+// Shared arrays: P (pressure), LG (log of successive pressure ratios), DS (SUM_DIV increments),
+// W (heating term), DF (dF/dp).
+__global__ void __launch_bounds__(CT_THREADS) k_calc_w(DevModel M) {
+  extern __shared__ double sm[];
+  __shared__ double s_lp[32];
+  const ColTile c = col_tile(M);
+  const int nk = M.nk, ks = M.k_sigma, L = nk + 1;
+  const long long n2 = M.n2;
+  double *P = sm, *LG = P + 32 * L, *DS = LG + 32 * L, *W = DS + 32 * L, *DF = W + 32 * L;
+  if (c.valid)
+    for (int k = c.warp; k <= nk; k += CT_WARPS) CT(P, k) = M.p3[c.base + k * n2];
+  __syncthreads();
+  const double ptop = CT(P, 0), pbot = CT(P, nk), psigma = CT(P, ks - 1);
+  if (c.valid) {
+    for (int k = c.warp; k < nk; k += CT_WARPS) CT(LG, k) = xlog(M, CT(P, k + 1) / CT(P, k));
+    if (c.warp == CT_WARPS - 1) s_lp[c.lane] = xlog(M, ptop / pbot);
+  }
+  __syncthreads();
+  const double lp = s_lp[c.lane];
+  if (c.valid)
+    for (int k = 1 + c.warp; k < nk; k += CT_WARPS) {
+      const long long x = c.base + k * n2;
+      const double p3 = CT(P, k);
+      double w = 0.;
+      if (k < ks - 1) {
+        const double sigma = xlog(M, p3 / pbot) / lp;
+        w = g_sigma(M, sigma) * M.heat3[x] / M.exner3[x];
+      }
+      if (k >= 2) {
+        const double P0 = CT(P, k - 2), P1 = CT(P, k - 1), P2 = p3, P3 = CT(P, k + 1);
+        const double dz10 = CT(LG, k - 2), dz21 = CT(LG, k - 1), dz32 = CT(LG, k);
+        const double dz20 = dz21 + dz10, dz30 = dz32 + dz20, dz31 = dz32 + dz21;
+        const double df0 = P0 * M.div_uv3[x - 2 * n2];
+        const double df1 = P1 * M.div_uv3[x - n2];
+        const double df2 = P2 * M.div_uv3[x];
+        const double df3 = P3 * M.div_uv3[x + n2];
+        CT(DS, k) = -(df0 * (dz21 * dz21 * dz21 * (dz31 + dz32)) / (dz10 * dz20 * dz30) +
+                      df1 * (dz21 * (dz21 * (dz21 + 2. * (dz10 - dz31)) - 6. * dz10 * dz31)) / (dz10 * dz31) +
+                      df2 * (dz21 * (dz21 * (dz21 + 2. * (dz32 - dz20)) - 6. * dz20 * dz32)) / (dz20 * dz32) +
+                      df3 * (dz21 * dz21 * dz21 * (dz10 + dz20)) / (dz30 * dz31 * dz32)) /
+                    12.;
+      }
+      // dF/dp by a centred difference of return_sigmatheta at fixed theta and pbot
+      const double theta3 = M.theta[x];
+      const double dp = p3 * M.eps13;
+      double p2 = dmaxr(p3 - dp * .5, ptop);
+      const double p4 = dminr(p3 + dp * .5, pbot);
+      if (p2 < psigma && p4 >= psigma) p2 = p3;
+      if (!(p2 < p4)) flag_error(M.ctl, ERR_CALC_W_P, k, c.j, c.i, p2);
+      CT(DF, k) = (sigmatheta_lp(M, theta3, p2, pbot, ptop, lp) - sigmatheta_lp(M, theta3, p4, pbot, ptop, lp)) / (p2 - p4);
+      CT(W, k) = w;
     }
-    if (k >= 2) {
-      const double P0 = M.p3[M.at(k - 2, j, i)], P1 = M.p3[M.at(k - 1, j, i)], P2 = M.p3[x], P3 = M.p3[M.at(k + 1, j, i)];
-      const double dz10 = xlog(M, P1 / P0), dz21 = xlog(M, P2 / P1), dz32 = xlog(M, P3 / P2);
-      const double dz20 = dz21 + dz10, dz30 = dz32 + dz20, dz31 = dz32 + dz21;
-      const double df0 = P0 * M.div_uv3[M.at(k - 2, j, i)];
-      const double df1 = P1 * M.div_uv3[M.at(k - 1, j, i)];
-      const double df2 = P2 * M.div_uv3[x];
-      const double df3 = P3 * M.div_uv3[M.at(k + 1, j, i)];
-      const double dsumdiv = -(df0 * (dz21 * dz21 * dz21 * (dz31 + dz32)) / (dz10 * dz20 * dz30) +
-                               df1 * (dz21 * (dz21 * (dz21 + 2. * (dz10 - dz31)) - 6. * dz10 * dz31)) / (dz10 * dz31) +
-                               df2 * (dz21 * (dz21 * (dz21 + 2. * (dz32 - dz20)) - 6. * dz20 * dz32)) / (dz20 * dz32) +
-                               df3 * (dz21 * dz21 * dz21 * (dz10 + dz20)) / (dz30 * dz31 * dz32)) /
-                             12.;
-      sum_div = sum_div + dsumdiv;
+  __syncthreads();
+  if (c.warp == 0 && c.valid) {
+    M.w3[c.base] = 0.;
+    M.w3[c.base + nk * n2] = 0.;
+    double sum_div = 0.;
+    for (int k = 1; k < nk; k++) {
+      if (k >= 2) sum_div = sum_div + CT(DS, k);
+      // SUM_DIV(nk) = 0, so the dF/dpbot term contributes nothing.
+      M.w3[c.base + k * n2] = CT(W, k) - (sum_div * CT(DF, k) + 0.);
     }
-    // dF/dp by a centred difference of return_sigmatheta at fixed theta and pbot
-    const double theta3 = M.theta[x], p3 = M.p3[x];
-    const double dp = p3 * M.eps13;
-    double p2 = dmaxr(p3 - dp * .5, ptop);
-    const double p4 = dminr(p3 + dp * .5, pbot);
-    if (p2 < psigma && p4 >= psigma) p2 = p3;
-    if (!(p2 < p4)) flag_error(M.ctl, ERR_CALC_W_P, k, j, i, p2);
-    const double dFdp = (return_sigmatheta(M, theta3, p2, pbot, ptop) - return_sigmatheta(M, theta3, p4, pbot, ptop)) / (p2 - p4);
-    // SUM_DIV(nk) = 0, so the dF/dpbot term contributes nothing.
-    M.w3[x] = w - (sum_div * dFdp + 0.);
   }
 }
 
@@ -210,64 +268,93 @@ __global__ void k_restore_mass(DevModel M) {
   }
 }
 
-// set_p2etc, epic_funcs_diag.c:3352-3569 (nq = 0: H2 is HDRY, PDRY3 is P3, HDRY3 is H3)
-__global__ void k_set_p2etc(DevModel M, int update_theta) {
-  int j, i;
-  if (!col_index(M, j, i)) return;
-  const int nk = M.nk, ks = M.k_sigma;
-  const double g = M.grav[2 * j + 1];
-  double p[EPIC_MAX_NK + 2];
-  p[0] = M.p3[M.at(0, j, i)];
-  for (int k = 1; k <= nk; k++) p[k] = p[k - 1] + M.dsgth[2 * k] * g * M.hdry[M.at(k, j, i)];
-  const double ptop = p[0], pbot = p[nk];
-  for (int k = ks - 1; k < nk; k++) {
-    const double sigma = (M.sgth[2 * k + 1] - M.zeta0) / (M.zeta1 - M.zeta0);
-    p[k] = get_p_sigma(M, pbot, sigma, ptop);
-  }
-  double hl[EPIC_MAX_NK + 2];   // get_h at the layers, from the final P3
-  for (int k = 1; k <= nk; k++) {
-    M.p3[M.at(k, j, i)] = p[k];
-    hl[k] = (p[k] - p[k - 1]) / (g * M.dsgth[2 * k]);
-    M.hdry[M.at(k, j, i)] = dmaxr(M.h_min[k], hl[k]);
-  }
-  double th[EPIC_MAX_NK + 2];
-  for (int k = 0; k <= nk; k++) th[k] = M.theta[M.at(k, j, i)];
-  if (update_theta) {
-    for (int k = 0; k < ks - 1; k++) {
-      const double sigma = get_sigma(M, pbot, p[k], ptop);
-      th[k] = (M.sgth[2 * k + 1] - f_sigma(M, sigma)) / g_sigma(M, sigma);
-      M.theta[M.at(k, j, i)] = th[k];
+// set_p2etc, epic_funcs_diag.c:3352-3569 (nq = 0: H2 is HDRY, PDRY3 is P3, HDRY3 is H3).
+// Shared arrays: P (interface pressure), HL (get_h at the layers), TH (THETA), PP (P^(kappa+1),
+// each interface's power computed once for the two layers that share it).
+__global__ void __launch_bounds__(CT_THREADS) k_set_p2etc(DevModel M, int update_theta) {
+  extern __shared__ double sm[];
+  __shared__ double s_lp[32];
+  const ColTile c = col_tile(M);
+  const int nk = M.nk, ks = M.k_sigma, L = nk + 1;
+  const long long n2 = M.n2;
+  double *P = sm, *HL = P + 32 * L, *TH = HL + 32 * L, *PP = TH + 32 * L;
+  const double g = M.grav[2 * c.j + 1];
+  if (c.warp == 0) {
+    if (c.valid) {   // P3 top-down: P3(K) = P3(K-1) + dsgth*g*H2
+      double p = M.p3[c.base];
+      CT(P, 0) = p;
+      for (int k = 1; k <= nk; k++) {
+        p = p + M.dsgth[2 * k] * g * M.hdry[c.base + k * n2];
+        CT(P, k) = p;
+      }
+      s_lp[c.lane] = xlog(M, CT(P, 0) / p);   // log(ptop/pbot)
     }
+  } else if (c.valid) {
+    for (int k = c.warp - 1; k <= nk; k += CT_WARPS - 1) CT(TH, k) = M.theta[c.base + k * n2];
   }
-  double p2[EPIC_MAX_NK + 2];
-  for (int k = 1; k <= nk; k++) {
-    p2[k] = layer_p(M, p[k - 1], p[k]);
-    M.p2[M.at(k, j, i)] = p2[k];
-  }
-  M.p2[M.at(0, j, i)] = p[0] * p[0] / p2[1];
-  for (int k = 1; k <= nk; k++) {
+  __syncthreads();
+  const double ptop = CT(P, 0), pbot = CT(P, nk), lp = s_lp[c.lane];
+  if (c.valid)   // pure-sigma interfaces: get_p_sigma
+    for (int k = ks - 1 + c.warp; k < nk; k += CT_WARPS) {
+      const double sigma = (M.sgth[2 * k + 1] - M.zeta0) / (M.zeta1 - M.zeta0);
+      CT(P, k) = pbot * xexp(M, sigma * lp);
+    }
+  __syncthreads();
+  const double kp1 = M.kappa + 1.;
+  if (c.valid)
+    for (int k = c.warp; k <= nk; k += CT_WARPS) {
+      const double pk = CT(P, k);
+      if (k >= 1) {
+        const long long x = c.base + k * n2;
+        M.p3[x] = pk;
+        const double hl = (pk - CT(P, k - 1)) / (g * M.dsgth[2 * k]);
+        CT(HL, k) = hl;
+        M.hdry[x] = dmaxr(M.h_min[k], hl);
+      }
+      CT(PP, k) = xpow(M, pk, kp1);
+      if (update_theta && k < ks - 1) {   // the diagnostic THETA above k_sigma-1
+        const double sigma = xlog(M, pk / pbot) / lp;
+        double gs;
+        const double fs = f_and_g_sigma(M, sigma, gs);
+        const double th = (M.sgth[2 * k + 1] - fs) / gs;
+        CT(TH, k) = th;
+        M.theta[c.base + k * n2] = th;
+      }
+    }
+  __syncthreads();
+  if (!c.valid) return;
+  for (int k = 1 + c.warp; k <= nk; k += CT_WARPS) {
+    const long long x = c.base + k * n2;
+    const double top = CT(P, k - 1), bot = CT(P, k);
+    double p2;   // onto_kk(P2_INDEX) at the layer, epic_funcs_diag.c:2601-2618
+    if (fcmp(bot, top) == 0) p2 = .5 * (bot + top);
+    else p2 = xpow(M, (CT(PP, k) - CT(PP, k - 1)) / (kp1 * (bot - top)), 1. / M.kappa);
+    M.p2[x] = p2;
+    if (k == 1) M.p2[c.base] = top * top / p2;
     double h;
-    if (k == nk) h = hl[nk];
+    if (k == nk) h = CT(HL, nk);
     else {
       const double topwt = M.dsgth[2 * k], botwt = M.dsgth[2 * k + 2];
-      h = (topwt * hl[k] + botwt * hl[k + 1]) / (topwt + botwt);
+      h = (topwt * CT(HL, k) + botwt * CT(HL, k + 1)) / (topwt + botwt);
     }
-    M.h3[M.at(k, j, i)] = h;
-    if (k == 1) M.h3[M.at(0, j, i)] = h;
-  }
-  if (update_theta) {
-    for (int k = 1; k < ks - 1; k++) {
-      const double sigma = get_sigma(M, pbot, p2[k], ptop);
-      M.theta2[M.at(k, j, i)] = (M.sgth[2 * k] - f_sigma(M, sigma)) / g_sigma(M, sigma);
-    }
-    M.theta2[M.at(ks - 1, j, i)] = .5 * (th[ks - 1] + th[ks - 2]);
-    // linint on the table (sigmatheta[2K+1], THETA(K)), K = nk down to k_sigma-1
-    const int nkay = nk - (ks - 1) + 1;
-    for (int k = ks; k <= nk; k++) {
-      const double sg = M.sgth[2 * k];
+    M.h3[x] = h;
+    if (k == 1) M.h3[c.base] = h;
+    if (!update_theta) continue;
+    double t2;
+    if (k < ks - 1) {
+      const double sigma = xlog(M, p2 / pbot) / lp;
+      double gs;
+      const double fs = f_and_g_sigma(M, sigma, gs);
+      t2 = (M.sgth[2 * k] - fs) / gs;
+    } else if (k == ks - 1) {
+      t2 = .5 * (CT(TH, ks - 1) + CT(TH, ks - 2));
+    } else {
+      // linint on the table (sigmatheta[2K+1], THETA(K)), K = nk down to k_sigma-1;
       // find_place_in_table on ascending x = sigmatheta[2(nk-kay)+1]
+      const int nkay = nk - (ks - 1) + 1;
+      const double sg = M.sgth[2 * k];
       auto X = [&](int kay) { return M.sgth[2 * (nk - kay) + 1]; };
-      auto Y = [&](int kay) { return th[nk - kay]; };
+      auto Y = [&](int kay) { return CT(TH, nk - kay); };
       int kay;
       if (fcmp(sg, X(0)) <= 0) kay = 0;
       else if (fcmp(sg, X(nkay - 1)) >= 0) kay = nkay - 2;
@@ -280,78 +367,99 @@ __global__ void k_set_p2etc(DevModel M, int update_theta) {
         kay = il;
       }
       const double dx = X(kay + 1) - X(kay);
-      M.theta2[M.at(k, j, i)] = Y(kay) + (Y(kay + 1) - Y(kay)) * (sg - X(kay)) / dx;
+      t2 = Y(kay) + (Y(kay + 1) - Y(kay)) * (sg - X(kay)) / dx;
     }
+    M.theta2[x] = t2;
   }
 }
 
 // store_pgrad_vars, column part (epic_funcs_diag.c:3595-3895): T3, EXNER3, RHO3, T2, RHO2,
 // the k = 0 extrapolations, GZ3 and MONT3 from the surface up, the monotone-GZ check, and
-// the first DZDT3 terms.
-__global__ void k_pgrad_vars_column(DevModel M) {
-  int j, i;
-  if (!col_index(M, j, i)) return;
-  const int nk = M.nk;
+// the first DZDT3 terms.  Shared arrays: P, R (RHO3), T3, LG (log of successive pressure
+// ratios), GZ (the Leslie-Purser increments, then the running sum in place).
+__global__ void __launch_bounds__(CT_THREADS) k_pgrad_vars_column(DevModel M) {
+  extern __shared__ double sm[];
+  __shared__ double s_rho2_1[32];
+  const ColTile c = col_tile(M);
+  const int nk = M.nk, L = nk + 1;
+  const long long n2 = M.n2;
   const double mu = M.mu_dry;
+  double *P = sm, *R = P + 32 * L, *T3 = R + 32 * L, *LG = T3 + 32 * L, *GZ = LG + 32 * L;
+  if (c.valid)
+    for (int k = c.warp; k <= nk; k += CT_WARPS) {
+      const long long x = c.base + k * n2;
+      const double theta = M.theta[x], p = M.p3[x];
+      const double t3 = return_temp(M, p, theta);
+      M.t3[x] = t3;
+      M.exner3[x] = M.cp * t3 / theta;
+      const double rho = return_density(p, t3, mu);
+      M.rho3[x] = rho;
+      CT(P, k) = p;
+      CT(R, k) = rho;
+      CT(T3, k) = t3;
+      if (k >= 1) {
+        const double pr = M.p2[x];
+        const double t2 = return_temp(M, pr, M.theta2[x]);
+        M.t2[x] = t2;
+        const double r2 = return_density(pr, t2, mu);
+        M.rho2[x] = r2;
+        if (k == 1) s_rho2_1[c.lane] = r2;
+      }
+    }
+  __syncthreads();
+  if (c.valid) {
+    for (int k = c.warp; k < nk; k += CT_WARPS) CT(LG, k) = xlog(M, CT(P, k + 1) / CT(P, k));
+    if (c.warp == CT_WARPS - 1) {
+      M.rho2[c.base] = CT(R, 0) * CT(R, 0) / s_rho2_1[c.lane];
+      M.theta2[c.base] = M.sgth[0];
+      M.t2[c.base] = CT(T3, 0);
+    }
+  }
+  __syncthreads();
+  if (c.valid)
+    for (int k = 2 + c.warp; k <= nk - 1; k += CT_WARPS) {
+      const double dz10 = CT(LG, k), dz21 = CT(LG, k - 1), dz32 = CT(LG, k - 2);
+      const double dz20 = dz21 + dz10, dz30 = dz32 + dz20, dz31 = dz32 + dz21;
+      const double df0 = CT(P, k + 1) / CT(R, k + 1), df1 = CT(P, k) / CT(R, k), df2 = CT(P, k - 1) / CT(R, k - 1),
+                   df3 = CT(P, k - 2) / CT(R, k - 2);
+      CT(GZ, k - 1) = -(df0 * (dz21 * dz21 * dz21 * (dz31 + dz32)) / (dz10 * dz20 * dz30) +
+                        df1 * (dz21 * (dz21 * (dz21 + 2. * (dz10 - dz31)) - 6. * dz10 * dz31)) / (dz10 * dz31) +
+                        df2 * (dz21 * (dz21 * (dz21 + 2. * (dz32 - dz20)) - 6. * dz20 * dz32)) / (dz20 * dz32) +
+                        df3 * (dz21 * dz21 * dz21 * (dz10 + dz20)) / (dz30 * dz31 * dz32)) /
+                      12.;
+    }
+  __syncthreads();
+  if (c.warp == 0 && c.valid) {   // GZ3 from the surface up
+    double gz = M.topo_scale * M.gz_surface[M.at2(c.j, c.i)];
+    CT(GZ, nk) = gz;
+    gz = gz + ((CT(P, nk) + CT(P, nk - 1)) / (CT(R, nk) + CT(R, nk - 1))) * CT(LG, nk - 1);
+    CT(GZ, nk - 1) = gz;
+    for (int k = nk - 1; k >= 2; k--) {
+      gz = gz + CT(GZ, k - 1);
+      CT(GZ, k - 1) = gz;
+    }
+    CT(GZ, 0) = gz + ((CT(P, 1) + CT(P, 0)) / (CT(R, 1) + CT(R, 0))) * CT(LG, 0);
+  }
+  __syncthreads();
+  if (!c.valid) return;
+  const bool interior = c.i >= 1 && c.i <= M.ni;
   const long long itime = M.ctl->itime;
-  double p[EPIC_MAX_NK + 2], rho[EPIC_MAX_NK + 2], t3[EPIC_MAX_NK + 2];
-  for (int k = 0; k <= nk; k++) {
-    const long long x = M.at(k, j, i);
-    const double theta = M.theta[x];
-    p[k] = M.p3[x];
-    t3[k] = return_temp(M, p[k], theta);
-    M.t3[x] = t3[k];
-    M.exner3[x] = M.cp * t3[k] / theta;
-    rho[k] = return_density(p[k], t3[k], mu);
-    M.rho3[x] = rho[k];
-  }
-  double rho2_1 = 0.;
-  for (int k = 1; k <= nk; k++) {
-    const long long x = M.at(k, j, i);
-    const double pr = M.p2[x];
-    const double t2 = return_temp(M, pr, M.theta2[x]);
-    M.t2[x] = t2;
-    const double r2 = return_density(pr, t2, mu);
-    M.rho2[x] = r2;
-    if (k == 1) rho2_1 = r2;
-  }
-  {
-    const long long x = M.at(0, j, i);
-    M.rho2[x] = rho[0] * rho[0] / rho2_1;
-    M.theta2[x] = M.sgth[0];
-    M.t2[x] = t3[0];
-  }
-  double gz[EPIC_MAX_NK + 2];
-  gz[nk] = M.topo_scale * M.gz_surface[M.at2(j, i)];
-  gz[nk - 1] = gz[nk] + ((p[nk] + p[nk - 1]) / (rho[nk] + rho[nk - 1])) * xlog(M, p[nk] / p[nk - 1]);
-  for (int k = nk - 1; k >= 2; k--) {
-    const double dz10 = xlog(M, p[k + 1] / p[k]), dz21 = xlog(M, p[k] / p[k - 1]), dz32 = xlog(M, p[k - 1] / p[k - 2]);
-    const double dz20 = dz21 + dz10, dz30 = dz32 + dz20, dz31 = dz32 + dz21;
-    const double df0 = p[k + 1] / rho[k + 1], df1 = p[k] / rho[k], df2 = p[k - 1] / rho[k - 1], df3 = p[k - 2] / rho[k - 2];
-    const double dgz = -(df0 * (dz21 * dz21 * dz21 * (dz31 + dz32)) / (dz10 * dz20 * dz30) +
-                         df1 * (dz21 * (dz21 * (dz21 + 2. * (dz10 - dz31)) - 6. * dz10 * dz31)) / (dz10 * dz31) +
-                         df2 * (dz21 * (dz21 * (dz21 + 2. * (dz32 - dz20)) - 6. * dz20 * dz32)) / (dz20 * dz32) +
-                         df3 * (dz21 * dz21 * dz21 * (dz10 + dz20)) / (dz30 * dz31 * dz32)) /
-                       12.;
-    gz[k - 1] = gz[k] + dgz;
-  }
-  gz[0] = gz[1] + ((p[1] + p[0]) / (rho[1] + rho[0])) * xlog(M, p[1] / p[0]);
-  const bool interior = i >= 1 && i <= M.ni;
-  for (int k = 0; k <= nk; k++) {
-    const long long x = M.at(k, j, i);
+  for (int k = c.warp; k <= nk; k += CT_WARPS) {
+    const long long x = c.base + k * n2;
+    const double gzk = CT(GZ, k);
     const double old = M.gz3[x];
-    M.gz3[x] = gz[k];
-    M.mont3[x] = gz[k] + return_enthalpy(M, t3[k]);
+    M.gz3[x] = gzk;
+    M.mont3[x] = gzk + return_enthalpy(M, CT(T3, k));
     if (interior && k >= 1) {
       // DZDT3 = -(GZ3_new - GZ3_old)/(dt*g) from the third step on, 0 before (:3679-3693, :3897-3909)
       double dz = 0.;
       if (itime > 1) {
-        const double dtg_inv = -1. / (M.dt * M.grav[2 * j + 1]);
-        dz = (old - gz[k]) * dtg_inv;
+        const double dtg_inv = -1. / (M.dt * M.grav[2 * c.j + 1]);
+        dz = (old - gzk) * dtg_inv;
       }
-      dz += M.w3[x] * M.h3[x] / M.rho3[x];
+      dz += M.w3[x] * M.h3[x] / CT(R, k);
       M.dzdt3[x] = dz;
-      if (gz[k] >= gz[k - 1]) flag_error(M.ctl, ERR_GZ_MONOTONE, k, j, i, gz[k]);
+      if (gzk >= CT(GZ, k - 1)) flag_error(M.ctl, ERR_GZ_MONOTONE, k, c.j, c.i, gzk);
     }
   }
 }
@@ -445,7 +553,12 @@ __global__ void k_advection_prep(DevModel M, int phase) {
 static inline unsigned ncol_blocks(const DevModel &M, int th) { return epic_blocks((long long)(M.nj + 1) * (M.ni + 2), th); }
 
 int launch_source_sink(const DevModel &M, cudaStream_t s) { k_source_sink<<<ncol_blocks(M, 128), 128, 0, s>>>(M); return 0; }
-int launch_calc_w(const DevModel &M, cudaStream_t s) { k_calc_w<<<ncol_blocks(M, 128), 128, 0, s>>>(M); return 0; }
+static inline unsigned ntile_blocks(const DevModel &M) { return epic_blocks((long long)(M.nj + 1) * (M.ni + 2), 32); }
+static inline size_t tile_smem(const DevModel &M, int arrays) { return (size_t)arrays * 32 * (M.nk + 1) * sizeof(double); }
+int launch_calc_w(const DevModel &M, cudaStream_t s) {
+  k_calc_w<<<ntile_blocks(M), CT_THREADS, tile_smem(M, 5), s>>>(M);
+  return 0;
+}
 int launch_uv_drag(const DevModel &M, cudaStream_t s) {
   const long long n = (long long)(M.nj + 1) * M.ni + (long long)M.nj * M.ni;
   k_uv_drag<<<epic_blocks(n, 128), 128, 0, s>>>(M);
@@ -457,11 +570,11 @@ int launch_hsu_vertical(const DevModel &M, double *buff, int kind, cudaStream_t 
 }
 int launch_restore_mass(const DevModel &M, cudaStream_t s) { k_restore_mass<<<ncol_blocks(M, 128), 128, 0, s>>>(M); return 0; }
 int launch_set_p2etc(const DevModel &M, int update_theta, cudaStream_t s) {
-  k_set_p2etc<<<ncol_blocks(M, 64), 64, 0, s>>>(M, update_theta);
+  k_set_p2etc<<<ntile_blocks(M), CT_THREADS, tile_smem(M, 4), s>>>(M, update_theta);
   return 0;
 }
 int launch_store_pgrad_vars(const DevModel &M, cudaStream_t s) {
-  k_pgrad_vars_column<<<ncol_blocks(M, 64), 64, 0, s>>>(M);
+  k_pgrad_vars_column<<<ntile_blocks(M), CT_THREADS, tile_smem(M, 5), s>>>(M);
   k_pgrad_dzdt<<<epic_blocks((long long)M.nk * (M.nj + 1) * M.ni, 128), 128, 0, s>>>(M);
   return 0;
 }
@@ -469,6 +582,18 @@ int launch_gz_monotone(const DevModel &M, cudaStream_t s) { k_gz_monotone<<<ncol
 int launch_calc_heating(const DevModel &M, cudaStream_t s) { k_calc_heating<<<epic_blocks(M.n3, 128), 128, 0, s>>>(M); return 0; }
 int launch_advection_prep(const DevModel &M, int phase, cudaStream_t s) {
   k_advection_prep<<<epic_blocks((long long)(M.nj + 1) * M.iadim * (M.nk + 2), 128), 128, 0, s>>>(M, phase);
+  return 0;
+}
+
+// The tile kernels take (arrays x 32 x (nk+1)) doubles of dynamic shared memory: up to 162 KB
+// at nk = 126, above the 48 KB default.
+int column_kernels_init(int nk) {
+  const int big = (int)(5 * 32 * (nk + 1) * sizeof(double));
+  if (big <= 48 * 1024) return 0;
+  if (cudaFuncSetAttribute(k_calc_w, cudaFuncAttributeMaxDynamicSharedMemorySize, big) != cudaSuccess ||
+      cudaFuncSetAttribute(k_set_p2etc, cudaFuncAttributeMaxDynamicSharedMemorySize, big) != cudaSuccess ||
+      cudaFuncSetAttribute(k_pgrad_vars_column, cudaFuncAttributeMaxDynamicSharedMemorySize, big) != cudaSuccess)
+    return -1;
   return 0;
 }
 

@@ -38,6 +38,7 @@ int launch_store_pgrad_vars(const DevModel &M, cudaStream_t s);
 int launch_gz_monotone(const DevModel &M, cudaStream_t s);
 int launch_calc_heating(const DevModel &M, cudaStream_t s);
 int launch_advection_prep(const DevModel &M, int phase, cudaStream_t s);
+int column_kernels_init(int nk);
 
 // k_stencil.cu -- horizontal stencils and the time update
 int launch_zero_tend(const DevModel &M, cudaStream_t s);

@@ -3,6 +3,9 @@
 Two oracles live under oracle/:
   libepicport.so  the CPU restatement of the reference step (oracle/epic_port.c), built from
                   committed sources anywhere (also on the GPU host);
+  libepicport_cr.so  the same restatement with log/exp/pow correctly rounded, the rounding
+                  the CUDA kernels use; glibc's pow is not correctly rounded in ~0.1% of calls,
+                  so this variant is what the kernels must match bit for bit;
   libepicref.so   the reference's own step compiled from its sources (oracle/Makefile `ref`),
                   only where the reference tree is present.  It keeps static state, so each
                   model runs in a fresh spawned process.
@@ -21,10 +24,11 @@ from epic_gb300.abi import EPIC_STEP_PROGS_AND_SYNC_DIAGS, EPIC_SYNC_DIAGS_ONLY,
 ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
 ORACLE = os.path.join(ROOT, "oracle")
 PORT_LIB = os.path.join(ORACLE, "_build", "libepicport.so")
+PORT_CR_LIB = os.path.join(ORACLE, "_build", "libepicport_cr.so")
 REF_LIB = os.path.join(ORACLE, "_ref", "libepicref.so")
 REFERENCE_DIR = os.environ.get("EPIC_REFERENCE_DIR", "/root/reference")
 
-_port = None
+_port = {}
 
 
 def build_port() -> str:
@@ -41,11 +45,10 @@ def reference_available() -> bool:
     return r.returncode == 0 and os.path.exists(REF_LIB)
 
 
-def port_lib() -> C.CDLL:
-    global _port
-    if _port is None:
+def port_lib(cr_libm: bool = False) -> C.CDLL:
+    if cr_libm not in _port:
         build_port()
-        lib = C.CDLL(PORT_LIB)
+        lib = C.CDLL(PORT_CR_LIB if cr_libm else PORT_LIB)
         lib.ep_create.restype = C.c_void_p
         lib.ep_create.argtypes = [C.POINTER(EpicGrid)]
         lib.ep_destroy.argtypes = [C.c_void_p]
@@ -57,15 +60,15 @@ def port_lib() -> C.CDLL:
         lib.ep_error.restype = C.c_char_p
         lib.ep_error.argtypes = [C.c_void_p]
         lib.ep_create_error.restype = C.c_char_p
-        _port = lib
-    return _port
+        _port[cr_libm] = lib
+    return _port[cr_libm]
 
 
 class Port:
-    """The CPU restatement of the step on one grid."""
+    """The CPU restatement of the step on one grid (cr_libm: with correctly rounded log/exp/pow)."""
 
-    def __init__(self, grid: GridArrays):
-        self.lib = port_lib()
+    def __init__(self, grid: GridArrays, cr_libm: bool = False):
+        self.lib = port_lib(cr_libm)
         self.layout = grid.layout
         self.uv_scheme = grid.struct.uv_scheme
         h = self.lib.ep_create(C.byref(grid.struct))

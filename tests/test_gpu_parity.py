@@ -1,11 +1,12 @@
 """Parity of the CUDA step (through the C ABI) with the oracle's CPU restatement.
 
 Tolerances: the FP64 form must match the reference CPU build to relative L2 <= 1e-11 per
-prognostic after 1 step and <= 1e-8 after 100 steps.  Kernel by kernel, the GPU evaluates the
-reference's expressions in the reference's order without FMA contraction, with correctly rounded
-log/exp/pow and a bit-exact restatement of realft, so stages without transcendentals must be
-bit-identical; stages with them differ only where glibc itself misrounds (a few cells) and are
-held to 1e-12, except DZDT3, a difference of successive geopotentials (1e-10).
+prognostic after 1 step and <= 1e-8 after 100 steps (test_full_step, against the restatement
+with the host glibc, which reproduces the reference build bit for bit).  Kernel by kernel the
+GPU evaluates the reference's expressions in the reference's order without FMA contraction,
+with correctly rounded log/exp/pow and a bit-exact restatement of realft, so every stage and
+every step must equal the restatement compiled with the same correctly rounded functions
+(oracle libepicport_cr.so) bit for bit.
 """
 import numpy as np
 import pytest
@@ -17,18 +18,15 @@ from oracle_lib import Port
 pytestmark = pytest.mark.gpu
 
 STEP_STAGES = [0, 1, 2, 3, 4, 5, 6, 7, 8, 9, 10, 11, 7, 12, 13, 14, 15, 16, 17]
-# stages whose kernels evaluate no log/exp/pow: the GPU must reproduce the restatement bit for bit
-BITWISE_STAGES = {0, 1, 3, 4, 5, 8, 9, 12, 13, 14, 15, 16}
-FIELD_TOL = {"dzdt3": 1e-10}
 STAGE_NAMES = {0: "zero_tend", 1: "source_sink", 2: "calc_w", 3: "uv_core", 4: "uv_drag", 5: "scalar_hypervisc",
                6: "advection", 7: "store_pgrad_vars", 8: "gz_filter", 9: "filter_tend_3d", 10: "filter_mass_3d",
                11: "set_p2etc", 12: "uv_pgrad", 13: "div_damp", 14: "uv_update", 15: "uv_hypervisc",
                16: "store_diag", 17: "calc_heating", 18: "set_p2etc_noupdate"}
 
 
-def _pair(cfg):
+def _pair(cfg, cr_libm=False):
     ga, f = hs_setup(cfg)
-    port = Port(ga)
+    port = Port(ga, cr_libm)
     port.upload(f)
     model = Model(ga)
     model.upload(f)
@@ -45,12 +43,17 @@ def _spin_up(cfg, nsteps):
     return ga, port.download()
 
 
+def _differing(a, b):
+    return {k: int((a.arrays[k] != b.arrays[k]).sum()) for k in a.arrays if not np.array_equal(a.arrays[k], b.arrays[k])}
+
+
 @pytest.mark.parametrize("scheme", [EPIC_UV_AB3, EPIC_UV_LEAPFROG])
 def test_stage_by_stage(gpu, scheme):
-    """Each reference function on the path, GPU vs restatement, from the same spun-up state."""
+    """Each reference function on the path, GPU vs the correctly rounded restatement, bit for
+    bit, from the same spun-up state."""
     cfg = HSConfig(ni=32, nj=16, nk=10, dt=300, uv_scheme=scheme, seed=3)
     ga, f = _spin_up(cfg, 4)
-    port = Port(ga)
+    port = Port(ga, cr_libm=True)
     port.upload(f)
     model = Model(ga)
     model.upload(f)
@@ -60,17 +63,26 @@ def test_stage_by_stage(gpu, scheme):
         model.run_stage(st)
         model.sync()
         a, b = model.download(), port.download()
-        errs = field_errors(a, b)
-        bad = {k: v[0] for k, v in errs.items() if v[0] > FIELD_TOL.get(k, 1e-12)}
-        ndiff = sum(int((a.arrays[k] != b.arrays[k]).sum()) for k in a.arrays)
-        if bad:
-            failures.append(f"stage {st} {STAGE_NAMES[st]}: {bad}")
-        if st in BITWISE_STAGES and ndiff:
-            failures.append(f"stage {st} {STAGE_NAMES[st]}: {ndiff} cells differ, expected bit-identical")
-        if bad or ndiff:
+        diff = _differing(a, b)
+        if diff:
+            failures.append(f"stage {st} {STAGE_NAMES[st]}: cells differing per field {diff}")
             # continue from the oracle's state so that later stages are tested on their own
             model.upload(b)
     assert not failures, "\n".join(failures)
+
+
+@pytest.mark.parametrize("scheme", [EPIC_UV_AB3, EPIC_UV_LEAPFROG])
+def test_steps_bitwise(gpu, scheme):
+    """Ten graph-replayed steps at 64x32x20 equal the correctly rounded restatement bit for bit."""
+    cfg = HSConfig(ni=64, nj=32, nk=20, dt=300, uv_scheme=scheme, seed=9)
+    ga, f, port, model = _pair(cfg, cr_libm=True)
+    port.timestep(EPIC_SYNC_DIAGS_ONLY)
+    port.run(10)
+    model.timestep(EPIC_SYNC_DIAGS_ONLY)
+    model.run(10)
+    model.sync()
+    diff = _differing(model.download(), port.download())
+    assert not diff, diff
 
 
 def test_sync_diags(gpu):
