@@ -158,7 +158,7 @@ def _dist():
 
 def run_gpu(args):
     import torch
-    from epic_gb300 import EPIC_SYNC_DIAGS_ONLY, Model, hs_setup
+    from epic_gb300 import EPIC_PREC_FP64, EPIC_PREC_MIXED, EPIC_SYNC_DIAGS_ONLY, Model, hs_setup
     ws, rank, local = _dist()
     torch.cuda.set_device(local)
     if ws > 1:
@@ -166,7 +166,7 @@ def run_gpu(args):
         dist.init_process_group("nccl")
     cfg = _workload_cfg(args.workload, seed=rank)
     ga, f = hs_setup(cfg)
-    model = Model(ga)
+    model = Model(ga, EPIC_PREC_MIXED if args.precision == "mixed" else EPIC_PREC_FP64)
     model.upload(f)
     model.timestep(EPIC_SYNC_DIAGS_ONLY)
     stream = torch.cuda.ExternalStream(model.stream)
@@ -295,6 +295,7 @@ def main():
     ap.add_argument("--workload", default="hs256", choices=sorted(WORKLOADS))
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--cpu-steps", type=int, default=3)
+    ap.add_argument("--precision", default="fp64", choices=["fp64", "mixed"])
     args = ap.parse_args()
     ws, rank, _ = _dist()
 

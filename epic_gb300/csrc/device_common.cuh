@@ -47,6 +47,8 @@ struct DevModel {
   const double *tw;                         // realft/four1 twiddles (see k_filter.cu)
   const double *coslat;                     // cos(lat[2j+1] deg), j = 0..nj, from the host libm
   const MathTable *lt;                      // double-double tables for cr_log/cr_exp/cr_pow
+  const float *twf;                         // the twiddles rounded to float (mixed form)
+  int mixed;                                // precision form: 0 FP64, 1 mixed (FP32 stencils)
   // state
   double *u, *v, *dudt, *dvdt, *hdry, *theta, *p3, *h3, *p2, *theta2, *t2, *t3, *rho2, *rho3, *exner3;
   double *gz3, *mont3, *heat3, *pv3, *ri2, *div_uv3, *w3, *dzdt3, *u_spinup, *gz_surface;
@@ -119,6 +121,32 @@ __device__ __forceinline__ double layer_p(const DevModel &M, double top, double 
   const double kp1 = M.kappa + 1.;
   return xpow(M, (xpow(M, bot, kp1) - xpow(M, top, kp1)) / (kp1 * (bot - top)), 1. / M.kappa);
 }
+
+// ---- compute-type helpers for kernels instantiated in FP64 (R = double: the drop-in form,
+// bit-identical to the reference's arithmetic) and FP32 (R = float: the mixed form) ----
+
+template <class R> __device__ __forceinline__ R rmax(R x, R y) { return x > y ? x : y; }
+template <class R> __device__ __forceinline__ R rmin(R x, R y) { return x < y ? x : y; }
+template <class R> struct RMath;
+template <> struct RMath<double> {
+  static __device__ __forceinline__ double log(const DevModel &M, double x) { return xlog(M, x); }
+  static __device__ __forceinline__ double exp(const DevModel &M, double x) { return xexp(M, x); }
+  static __device__ __forceinline__ double pow(const DevModel &M, double x, double y) { return xpow(M, x, y); }
+  static __device__ __forceinline__ int cmp(double x1, double x2) { return fcmp(x1, x2); }
+};
+template <> struct RMath<float> {
+  static __device__ __forceinline__ float log(const DevModel &, float x) { return logf(x); }
+  static __device__ __forceinline__ float exp(const DevModel &, float x) { return expf(x); }
+  static __device__ __forceinline__ float pow(const DevModel &, float x, float y) { return powf(x, y); }
+  // fcmp with the float epsilon
+  static __device__ __forceinline__ int cmp(float x1, float x2) {
+    int e;
+    frexpf(fabsf(x1) > fabsf(x2) ? x1 : x2, &e);
+    const float delta = ldexpf(FLT_EPSILON, e);
+    const float d = x1 - x2;
+    return d > delta ? 1 : (d < -delta ? -1 : 0);
+  }
+};
 
 struct Trip { double x, y, z; };
 

@@ -233,7 +233,7 @@ extern "C" const char *epic_last_error(void) { return epic::error_buffer(); }
 extern "C" int epic_model_create(const epic_grid *g, int32_t precision, epic_model **out) {
   if (!g || !out) return set_error(EPIC_ERR_ARG, "epic_model_create: NULL argument");
   *out = nullptr;
-  if (precision != EPIC_PREC_FP64) return set_error(EPIC_ERR_ARG, "precision form %d not available", precision);
+  if (precision != EPIC_PREC_FP64 && precision != EPIC_PREC_MIXED) return set_error(EPIC_ERR_ARG, "precision form %d not available", precision);
   if (g->ni < 4 || (g->ni & (g->ni - 1)) || g->ni > EPIC_MAX_NI) return set_error(EPIC_ERR_ARG, "ni=%d: need a power of 2 in [4,%d]", g->ni, EPIC_MAX_NI);
   if (g->nj < 3 || g->nk < 3 || g->nk > EPIC_MAX_NK) return set_error(EPIC_ERR_ARG, "nj=%d nk=%d out of range", g->nj, g->nk);
   if (g->globe_latbot != -90. || g->globe_lattop != 90.) return set_error(EPIC_ERR_ARG, "only the full globe is supported");
@@ -266,6 +266,7 @@ extern "C" int epic_model_create(const epic_grid *g, int32_t precision, epic_mod
   d.kappa = g->kappa; d.cp = g->cp; d.cpr = g->cpr; d.rgas = g->rgas;
   d.mu_dry = 1. / (g->rgas / 8.314472e+3);
   d.hs_kf = g->hs_kf; d.lat0 = g->lat0;
+  d.mixed = precision == EPIC_PREC_MIXED;
 
   HostTables T;
   filter_tables(*g, L, T);
@@ -288,7 +289,7 @@ extern "C" int epic_model_create(const epic_grid *g, int32_t precision, epic_mod
   auto rnd = [](size_t b) { return ((b + 255) / 256) * 256; };
   size_t bytes = rnd(sizeof(Ctl)) + (n_state3 + n_scratch3) * rnd(n3 * 8) + 3 * rnd(n2 * 8) + rnd((size_t)(g->nj + 3) * (g->nk + 2) * 3 * 8) +
                  rnd(ni1 * 8) + 10 * rnd(nj1 * 8) + 3 * rnd(nk1 * 8) + rnd((g->nk + 2) * 8) + rnd((g->k_sponge + 1) * 8) +
-                 2 * rnd(3 * (g->nj + 2) * 8) + rnd(T.tw.size() * 8) + rnd((g->nj + 1) * 8) +
+                 2 * rnd(3 * (g->nj + 2) * 8) + rnd(T.tw.size() * 8) + rnd(T.tw.size() * 4) + rnd((g->nj + 1) * 8) +
                  rnd(sizeof(epic::MathTable)) + 4096;
   cudaError_t e = cudaStreamCreateWithFlags(&m->stream, cudaStreamNonBlocking);
   if (e != cudaSuccess) { delete m; return set_error(EPIC_ERR_CUDA, "cudaStreamCreate: %s", cudaGetErrorString(e)); }
@@ -319,6 +320,7 @@ extern "C" int epic_model_create(const epic_grid *g, int32_t precision, epic_mod
   double *hmin = carve<double>(p, g->nk + 2), *tsp = carve<double>(p, g->k_sponge + 1);
   double *hc = carve<double>(p, 3 * (g->nj + 2)), *vc = carve<double>(p, 3 * (g->nj + 2));
   double *tw = carve<double>(p, T.tw.size());
+  float *twf = carve<float>(p, T.tw.size());
   double *coslat = carve<double>(p, g->nj + 1);
   epic::MathTable *lt = carve<epic::MathTable>(p, 1);
   if ((size_t)(p - m->pool) > bytes) {
@@ -336,6 +338,8 @@ extern "C" int epic_model_create(const epic_grid *g, int32_t precision, epic_mod
   up(hlh, T.high_lat_h.data(), n2); up(hlpv, T.high_lat_pv.data(), n2);
   up(hc, T.h_coef.data(), T.h_coef.size()); up(vc, T.v_coef.data(), T.v_coef.size());
   up(tw, T.tw.data(), T.tw.size());
+  std::vector<float> twf_host(T.tw.begin(), T.tw.end());
+  cudaMemcpyAsync(twf, twf_host.data(), twf_host.size() * sizeof(float), cudaMemcpyHostToDevice, m->stream);
   // cos of the h-row latitudes with the host libm (t_rad and temp_eq use them)
   std::vector<double> cl(g->nj + 1);
   for (int J = 0; J <= g->nj; J++) cl[J] = cos(g->lat[2 * J + 1] * kDeg);
@@ -348,7 +352,7 @@ extern "C" int epic_model_create(const epic_grid *g, int32_t precision, epic_mod
   d.lon = lon; d.lat = j1[0]; d.rln = j1[1]; d.rlt = j1[2]; d.f = j1[3]; d.m = j1[4]; d.n = j1[5]; d.mn = j1[6]; d.grav = j1[7];
   d.mn_inv = j1[8];
   d.sgth = sg; d.dsgth = ds; d.dsgth_inv = dsi; d.h_min = hmin; d.t_sponge_inv = tsp;
-  d.high_lat_h = hlh; d.high_lat_pv = hlpv; d.h_coef = hc; d.v_coef = vc; d.tw = tw;
+  d.high_lat_h = hlh; d.high_lat_pv = hlpv; d.h_coef = hc; d.v_coef = vc; d.tw = tw; d.twf = twf;
   epic::filter_kernels_init(g->ni);
   epic::column_kernels_init(g->nk);
   e = cudaStreamSynchronize(m->stream);

@@ -57,12 +57,26 @@ __device__ __forceinline__ ColTile col_tile(const DevModel &M) {
 // level k of a [k][lane] shared array
 #define CT(a, k) (a)[(k) * 32 + c.lane]
 
+// f_sigma/g_sigma (epic_funcs_diag.c:1271-1314) in the compute type, one exponential for both
+template <class R>
+__device__ __forceinline__ R f_and_g_sigma_r(const DevModel &M, R s, R &g) {
+  const R ss = R(M.sigma_sigma), z0 = R(M.zeta0), z1 = R(M.zeta1);
+  if (s <= ss) g = R(0.);
+  else if (s >= R(1.)) g = R(1.);
+  else g = R(M.g_coeff) * (R(1.) - RMath<R>::exp(M, -R(M.alpha) * (s - ss)));
+  if (s < R(0.)) return z0;
+  if (s <= ss) return z0 + s * (z1 - z0);
+  if (s < R(1.)) return (R(1.) - g) * (z0 + s * (z1 - z0));
+  return R(0.);
+}
+
 // return_sigmatheta (epic_funcs_diag.c:1238-1250) with log(ptop/pbot) supplied
-__device__ __forceinline__ double sigmatheta_lp(const DevModel &M, double theta, double p, double pbot, double ptop, double lp) {
+template <class R>
+__device__ __forceinline__ R sigmatheta_lp(const DevModel &M, R theta, R p, R pbot, R ptop, R lp) {
   if (p <= ptop) return theta;
-  const double s = xlog(M, p / pbot) / lp;
-  double g;
-  const double f = f_and_g_sigma(M, s, g);
+  const R s = RMath<R>::log(M, p / pbot) / lp;
+  R g;
+  const R f = f_and_g_sigma_r<R>(M, s, g);
   return f + g * theta;
 }
 
@@ -71,54 +85,61 @@ __device__ __forceinline__ double sigmatheta_lp(const DevModel &M, double theta,
 // column loops, epic_flux.c:224-226, :259-261), so the dF/dpbot term vanishes.
 // Shared arrays: P (pressure), LG (log of successive pressure ratios), DS (SUM_DIV increments),
 // W (heating term), DF (dF/dp).
+// In the mixed form (R = float) the pointwise terms are FP32, SUM_DIV is accumulated in FP64, and
+// the dF/dp difference step is cbrt(FLT_EPSILON) relative instead of cbrt(DBL_EPSILON).
+template <class R>
 __global__ void __launch_bounds__(CT_THREADS) k_calc_w(DevModel M) {
-  extern __shared__ double sm[];
-  __shared__ double s_lp[32];
+  extern __shared__ __align__(16) unsigned char smraw[];
+  R *sm = reinterpret_cast<R *>(smraw);
+  __shared__ R s_lp[32];
   const ColTile c = col_tile(M);
   const int nk = M.nk, ks = M.k_sigma, L = nk + 1;
   const long long n2 = M.n2;
-  double *P = sm, *LG = P + 32 * L, *DS = LG + 32 * L, *W = DS + 32 * L, *DF = W + 32 * L;
+  R *P = sm, *LG = P + 32 * L, *DS = LG + 32 * L, *W = DS + 32 * L, *DF = W + 32 * L;
   if (c.valid)
-    for (int k = c.warp; k <= nk; k += CT_WARPS) CT(P, k) = M.p3[c.base + k * n2];
+    for (int k = c.warp; k <= nk; k += CT_WARPS) CT(P, k) = R(M.p3[c.base + k * n2]);
   __syncthreads();
-  const double ptop = CT(P, 0), pbot = CT(P, nk), psigma = CT(P, ks - 1);
+  const R ptop = CT(P, 0), pbot = CT(P, nk), psigma = CT(P, ks - 1);
   if (c.valid) {
-    for (int k = c.warp; k < nk; k += CT_WARPS) CT(LG, k) = xlog(M, CT(P, k + 1) / CT(P, k));
-    if (c.warp == CT_WARPS - 1) s_lp[c.lane] = xlog(M, ptop / pbot);
+    for (int k = c.warp; k < nk; k += CT_WARPS) CT(LG, k) = RMath<R>::log(M, CT(P, k + 1) / CT(P, k));
+    if (c.warp == CT_WARPS - 1) s_lp[c.lane] = RMath<R>::log(M, ptop / pbot);
   }
   __syncthreads();
-  const double lp = s_lp[c.lane];
+  const R lp = s_lp[c.lane];
+  const R eps13 = sizeof(R) == sizeof(float) ? R(4.9215666e-3) : R(M.eps13);   // cbrt(FLT_EPSILON)
   if (c.valid)
     for (int k = 1 + c.warp; k < nk; k += CT_WARPS) {
       const long long x = c.base + k * n2;
-      const double p3 = CT(P, k);
-      double w = 0.;
+      const R p3 = CT(P, k);
+      R w = R(0.);
       if (k < ks - 1) {
-        const double sigma = xlog(M, p3 / pbot) / lp;
-        w = g_sigma(M, sigma) * M.heat3[x] / M.exner3[x];
+        const R sigma = RMath<R>::log(M, p3 / pbot) / lp;
+        R g;
+        f_and_g_sigma_r<R>(M, sigma, g);
+        w = g * R(M.heat3[x]) / R(M.exner3[x]);
       }
       if (k >= 2) {
-        const double P0 = CT(P, k - 2), P1 = CT(P, k - 1), P2 = p3, P3 = CT(P, k + 1);
-        const double dz10 = CT(LG, k - 2), dz21 = CT(LG, k - 1), dz32 = CT(LG, k);
-        const double dz20 = dz21 + dz10, dz30 = dz32 + dz20, dz31 = dz32 + dz21;
-        const double df0 = P0 * M.div_uv3[x - 2 * n2];
-        const double df1 = P1 * M.div_uv3[x - n2];
-        const double df2 = P2 * M.div_uv3[x];
-        const double df3 = P3 * M.div_uv3[x + n2];
+        const R P0 = CT(P, k - 2), P1 = CT(P, k - 1), P2 = p3, P3 = CT(P, k + 1);
+        const R dz10 = CT(LG, k - 2), dz21 = CT(LG, k - 1), dz32 = CT(LG, k);
+        const R dz20 = dz21 + dz10, dz30 = dz32 + dz20, dz31 = dz32 + dz21;
+        const R df0 = P0 * R(M.div_uv3[x - 2 * n2]);
+        const R df1 = P1 * R(M.div_uv3[x - n2]);
+        const R df2 = P2 * R(M.div_uv3[x]);
+        const R df3 = P3 * R(M.div_uv3[x + n2]);
         CT(DS, k) = -(df0 * (dz21 * dz21 * dz21 * (dz31 + dz32)) / (dz10 * dz20 * dz30) +
-                      df1 * (dz21 * (dz21 * (dz21 + 2. * (dz10 - dz31)) - 6. * dz10 * dz31)) / (dz10 * dz31) +
-                      df2 * (dz21 * (dz21 * (dz21 + 2. * (dz32 - dz20)) - 6. * dz20 * dz32)) / (dz20 * dz32) +
+                      df1 * (dz21 * (dz21 * (dz21 + R(2.) * (dz10 - dz31)) - R(6.) * dz10 * dz31)) / (dz10 * dz31) +
+                      df2 * (dz21 * (dz21 * (dz21 + R(2.) * (dz32 - dz20)) - R(6.) * dz20 * dz32)) / (dz20 * dz32) +
                       df3 * (dz21 * dz21 * dz21 * (dz10 + dz20)) / (dz30 * dz31 * dz32)) /
-                    12.;
+                    R(12.);
       }
       // dF/dp by a centred difference of return_sigmatheta at fixed theta and pbot
-      const double theta3 = M.theta[x];
-      const double dp = p3 * M.eps13;
-      double p2 = dmaxr(p3 - dp * .5, ptop);
-      const double p4 = dminr(p3 + dp * .5, pbot);
+      const R theta3 = R(M.theta[x]);
+      const R dp = p3 * eps13;
+      R p2 = rmax(p3 - dp * R(.5), ptop);
+      const R p4 = rmin(p3 + dp * R(.5), pbot);
       if (p2 < psigma && p4 >= psigma) p2 = p3;
       if (!(p2 < p4)) flag_error(M.ctl, ERR_CALC_W_P, k, c.j, c.i, p2);
-      CT(DF, k) = (sigmatheta_lp(M, theta3, p2, pbot, ptop, lp) - sigmatheta_lp(M, theta3, p4, pbot, ptop, lp)) / (p2 - p4);
+      CT(DF, k) = (sigmatheta_lp<R>(M, theta3, p2, pbot, ptop, lp) - sigmatheta_lp<R>(M, theta3, p4, pbot, ptop, lp)) / (p2 - p4);
       CT(W, k) = w;
     }
   __syncthreads();
@@ -127,15 +148,16 @@ __global__ void __launch_bounds__(CT_THREADS) k_calc_w(DevModel M) {
     M.w3[c.base + nk * n2] = 0.;
     double sum_div = 0.;
     for (int k = 1; k < nk; k++) {
-      if (k >= 2) sum_div = sum_div + CT(DS, k);
+      if (k >= 2) sum_div = sum_div + (double)CT(DS, k);
       // SUM_DIV(nk) = 0, so the dF/dpbot term contributes nothing.
-      M.w3[c.base + k * n2] = CT(W, k) - (sum_div * CT(DF, k) + 0.);
+      M.w3[c.base + k * n2] = (double)CT(W, k) - (sum_div * (double)CT(DF, k) + 0.);
     }
   }
 }
 
 // Held-Suarez boundary-layer drag and the top sponge of uv_drag, epic_timestep.c:1303-1509.
 // Columns on the u grid (j = 0..nj) and v grid (j = 1..nj), i = 1..ni.
+template <class R>
 __global__ void k_uv_drag(DevModel M) {
   const int t = (int)(blockIdx.x * blockDim.x + threadIdx.x);
   const int ni = M.ni, nk = M.nk;
@@ -151,110 +173,118 @@ __global__ void k_uv_drag(DevModel M) {
   const int jm = isv ? j - 1 : j, im = isv ? i : i - 1;   // neighbour averaged onto the u or v point
   for (int k = 0; k <= M.k_sponge; k++) {
     const long long x = M.at(k, j, i);
-    D[x] -= (M.t_sponge_inv[k]) * (W[x] - (isv ? 0. : M.u_spinup[x]));
+    D[x] = D[x] - (double)(R(M.t_sponge_inv[k]) * (R(W[x]) - (isv ? R(0.) : R(M.u_spinup[x]))));
   }
   if (M.rayleigh_on) {
     // The zonal-mean Rayleigh drag block is not part of the supported configurations
     // (held_suarez sets prandtl = 0 and tau_drag = 1e20); epic_model_create rejects it.
   }
-  const double pbot = 0.5 * (M.p3[M.at(nk, j, i)] + M.p3[M.at(nk, jm, im)]);
+  const R pbot = R(0.5) * (R(M.p3[M.at(nk, j, i)]) + R(M.p3[M.at(nk, jm, im)]));
   for (int k = nk - 1; k >= 1; k--) {
-    const double p3 = .5 * (M.p3[M.at(k, j, i)] + M.p3[M.at(k, jm, im)]);
-    const double amp = (p3 / pbot - 0.7) / (1. - 0.7);
-    if (amp < 0.) break;
-    const double nu0 = M.hs_kf * amp;
+    const R p3 = R(.5) * (R(M.p3[M.at(k, j, i)]) + R(M.p3[M.at(k, jm, im)]));
+    const R amp = (p3 / pbot - R(0.7)) / (R(1.) - R(0.7));
+    if (amp < R(0.)) break;
+    const R nu0 = R(M.hs_kf) * amp;
     const long long x = M.at(k, j, i);
-    D[x] -= nu0 * W[x];
+    D[x] = D[x] - (double)(nu0 * R(W[x]));
   }
 }
 
 // Vertical pass of hsu_advection, epic_flux.c:717-1052.  kind: 0 = unity (P3_INDEX),
 // 1 = THETA, 2 = HDRY.  One thread per column j = 0..nj, i = 0..ni+1.
+template <class R>
 __global__ void k_hsu_vertical(DevModel M, double *buff, int kind) {
   int j, i;
   if (!col_index(M, j, i)) return;
   const int nk = M.nk;
   const bool layer = kind == 2;
   const int kf = kind == 1 ? M.k_sigma - 1 : 1;
-  const double ep = 1.e-10, DT = M.dt;
-  double wm[EPIC_MAX_NK + 2], wp[EPIC_MAX_NK + 2], wa[EPIC_MAX_NK + 2], pred[EPIC_MAX_NK + 2];
-  double ff[EPIC_MAX_NK + 2], d1[EPIC_MAX_NK + 2], d2[EPIC_MAX_NK + 2], aa[EPIC_MAX_NK + 2];
-  auto amin = [&](int k) { return layer ? M.h_min[k] : 0.; };
-  for (int k = layer ? kf : kf - 1; k <= nk; k++) wa[k] = buff[M.at(k, j, i)];
+  const R ep = R(1.e-10), DT = R(M.dt);
+  R wm[EPIC_MAX_NK + 2], wp[EPIC_MAX_NK + 2], wa[EPIC_MAX_NK + 2], pred[EPIC_MAX_NK + 2];
+  R ff[EPIC_MAX_NK + 2], d1[EPIC_MAX_NK + 2], d2[EPIC_MAX_NK + 2], aa[EPIC_MAX_NK + 2];
+  auto amin = [&](int k) { return layer ? R(M.h_min[k]) : R(0.); };
+  auto dsi = [&](int kk) { return R(M.dsgth_inv[kk]); };
+  for (int k = layer ? kf : kf - 1; k <= nk; k++) wa[k] = R(buff[M.at(k, j, i)]);
   if (layer) {
     for (int k = kf - 1; k <= nk; k++) {
-      const double w = M.w3[M.at(k, j, i)];
-      wm[k] = dminr(0., w);
-      wp[k] = dmaxr(0., w);
+      const R w = R(M.w3[M.at(k, j, i)]);
+      wm[k] = rmin(R(0.), w);
+      wp[k] = rmax(R(0.), w);
     }
-    ff[kf - 1] = 0.;
-    ff[nk] = 0.;
+    ff[kf - 1] = R(0.);
+    ff[nk] = R(0.);
     for (int k = kf; k < nk; k++) ff[k] = wp[k] * wa[k + 1] + wm[k] * wa[k];
-    for (int k = kf; k <= nk; k++) pred[k] = wa[k] + (ff[k] - ff[k - 1]) * M.dsgth_inv[2 * k] * DT;
-    for (int k = kf; k < nk; k++) ff[k] = .5 * (wp[k] * (pred[k] + wa[k + 1]) + wm[k] * (pred[k + 1] + wa[k]));
+    for (int k = kf; k <= nk; k++) pred[k] = wa[k] + (ff[k] - ff[k - 1]) * dsi(2 * k) * DT;
+    for (int k = kf; k < nk; k++) ff[k] = R(.5) * (wp[k] * (pred[k] + wa[k + 1]) + wm[k] * (pred[k + 1] + wa[k]));
     for (int k = kf; k <= nk; k++) {
-      double tmp;
-      if (k == 1) { d1[k] = pred[k] - wa[k + 1]; d2[k] = 0.; tmp = fabs(wa[k + 1] - wa[k]) + ep; }
-      else if (k == nk) { d1[k] = 0.; d2[k] = pred[k] - wa[k - 1]; tmp = fabs(-wa[k] + wa[k - 1]) + ep; }
-      else { d1[k] = pred[k] - wa[k + 1]; d2[k] = pred[k] - wa[k - 1]; tmp = fabs(wa[k + 1] - 2. * wa[k] + wa[k - 1]) + ep; }
+      R tmp;
+      if (k == 1) { d1[k] = pred[k] - wa[k + 1]; d2[k] = R(0.); tmp = fabs(wa[k + 1] - wa[k]) + ep; }
+      else if (k == nk) { d1[k] = R(0.); d2[k] = pred[k] - wa[k - 1]; tmp = fabs(-wa[k] + wa[k - 1]) + ep; }
+      else { d1[k] = pred[k] - wa[k + 1]; d2[k] = pred[k] - wa[k - 1]; tmp = fabs(wa[k + 1] - R(2.) * wa[k] + wa[k - 1]) + ep; }
       aa[k] = tmp * tmp;
     }
     for (int k = kf; k < nk; k++) {
-      const double whatp = sqrt(wp[k] * wp[k + 1]);
-      const double whatm = -sqrt(wm[k] * wm[k - 1]);
-      const double mu = (wp[k] - wm[k]) * M.dsgth_inv[2 * k + 1] * DT;
-      const double al = (1. + mu) / 6.;
-      const double prod = (wa[k + 1] - amin(k + 1)) * (wa[k] - amin(k));
-      double gap = aa[k + 1] / (aa[k + 1] + prod); gap = gap * gap;
-      double gam = aa[k] / (aa[k] + prod); gam = gam * gam;
-      const double bep = 1. + (1. / (2. * al) - 1.) * gap;
-      const double bem = 1. + (1. / (2. * al) - 1.) * gam;
-      ff[k] += -al * (wp[k] * bep * d1[k] - whatp * (1. - gap) * d1[k + 1] + wm[k] * bem * d2[k + 1] - whatm * (1. - gam) * d2[k]);
+      const R whatp = sqrt(wp[k] * wp[k + 1]);
+      const R whatm = -sqrt(wm[k] * wm[k - 1]);
+      const R mu = (wp[k] - wm[k]) * dsi(2 * k + 1) * DT;
+      const R al = (R(1.) + mu) / R(6.);
+      const R prod = (wa[k + 1] - amin(k + 1)) * (wa[k] - amin(k));
+      R gap = aa[k + 1] / (aa[k + 1] + prod); gap = gap * gap;
+      R gam = aa[k] / (aa[k] + prod); gam = gam * gam;
+      const R bep = R(1.) + (R(1.) / (R(2.) * al) - R(1.)) * gap;
+      const R bem = R(1.) + (R(1.) / (R(2.) * al) - R(1.)) * gam;
+      ff[k] += -al * (wp[k] * bep * d1[k] - whatp * (R(1.) - gap) * d1[k + 1] + wm[k] * bem * d2[k + 1] - whatm * (R(1.) - gam) * d2[k]);
     }
-    for (int k = kf; k <= nk; k++) buff[M.at(k, j, i)] += (ff[k] - ff[k - 1]) * M.dsgth_inv[2 * k] * DT;
+    for (int k = kf; k <= nk; k++) {
+      const long long x = M.at(k, j, i);
+      buff[x] = buff[x] + (double)((ff[k] - ff[k - 1]) * dsi(2 * k) * DT);
+    }
   } else {
     for (int k = kf; k <= nk; k++) {
-      const double w = (k == 1 || k == nk) ? 0. : .5 * (M.w3[M.at(k, j, i)] + M.w3[M.at(k - 1, j, i)]);
-      wm[k] = dminr(0., w);
-      wp[k] = dmaxr(0., w);
+      const R w = (k == 1 || k == nk) ? R(0.) : R(.5) * (R(M.w3[M.at(k, j, i)]) + R(M.w3[M.at(k - 1, j, i)]));
+      wm[k] = rmin(R(0.), w);
+      wp[k] = rmax(R(0.), w);
     }
     for (int k = kf; k <= nk; k++) ff[k] = wp[k] * wa[k] + wm[k] * wa[k - 1];
-    ff[nk + 1] = 0.;
+    ff[nk + 1] = R(0.);
     pred[kf - 1] = wa[kf - 1];
-    for (int k = kf; k <= nk; k++) pred[k] = wa[k] + (ff[k + 1] - ff[k]) * M.dsgth_inv[2 * k + 1] * DT;
-    for (int k = kf; k <= nk; k++) ff[k] = .5 * (wp[k] * (pred[k - 1] + wa[k]) + wm[k] * (pred[k] + wa[k - 1]));
+    for (int k = kf; k <= nk; k++) pred[k] = wa[k] + (ff[k + 1] - ff[k]) * dsi(2 * k + 1) * DT;
+    for (int k = kf; k <= nk; k++) ff[k] = R(.5) * (wp[k] * (pred[k - 1] + wa[k]) + wm[k] * (pred[k] + wa[k - 1]));
     for (int k = kf - 1; k <= nk; k++) {
       // For THETA (kf > 1) the entry below the first loaded one is the value the reference's
       // static column buffer keeps from the preceding unity advection: 1.0 (epic_flux.c:866-877).
-      const double wkm1 = k >= 1 ? (k - 1 < kf - 1 ? 1.0 : wa[k - 1]) : 0.;
-      double tmp;
+      const R wkm1 = k >= 1 ? (k - 1 < kf - 1 ? R(1.0) : wa[k - 1]) : R(0.);
+      R tmp;
       if (k == 0) tmp = fabs(wa[k + 1] - wa[k]) + ep;
       else if (k == nk) tmp = fabs(-wa[k] + wkm1) + ep;
-      else tmp = fabs(wa[k + 1] - 2. * wa[k] + wkm1) + ep;
+      else tmp = fabs(wa[k + 1] - R(2.) * wa[k] + wkm1) + ep;
       aa[k] = tmp * tmp;
     }
-    d2[kf - 1] = 0.;
+    d2[kf - 1] = R(0.);
     for (int k = kf; k <= nk; k++) {
       d1[k] = pred[k - 1] - wa[k];
       d2[k] = pred[k] - wa[k - 1];
     }
     for (int k = kf; k <= nk; k++) {
-      const double whatm = (k == 1 || k - 1 < kf) ? 0. : -sqrt(wm[k] * wm[k - 1]);
-      const double whatp = (k == nk) ? 0. : sqrt(wp[k] * wp[k + 1]);
-      const double mu = (wp[k] - wm[k]) * M.dsgth_inv[2 * k] * DT;
-      const double al = (1. + mu) / 6.;
-      const double prod = (wa[k] - amin(k)) * (wa[k - 1] - amin(k - 1));
-      double gap = aa[k] / (aa[k] + prod); gap = gap * gap;
-      double gam = aa[k - 1] / (aa[k - 1] + prod); gam = gam * gam;
-      const double bep = 1. + (1. / (2. * al) - 1.) * gap;
-      const double bem = 1. + (1. / (2. * al) - 1.) * gam;
-      double g;
-      if (k < nk) g = -al * (wp[k] * bep * d1[k] - whatp * (1. - gap) * d1[k + 1] + wm[k] * bem * d2[k] - whatm * (1. - gam) * d2[k - 1]);
-      else g = -al * (wp[k] * bep * d1[k] + wm[k] * bem * d2[k] - whatm * (1. - gam) * d2[k - 1]);
+      const R whatm = (k == 1 || k - 1 < kf) ? R(0.) : -sqrt(wm[k] * wm[k - 1]);
+      const R whatp = (k == nk) ? R(0.) : sqrt(wp[k] * wp[k + 1]);
+      const R mu = (wp[k] - wm[k]) * dsi(2 * k) * DT;
+      const R al = (R(1.) + mu) / R(6.);
+      const R prod = (wa[k] - amin(k)) * (wa[k - 1] - amin(k - 1));
+      R gap = aa[k] / (aa[k] + prod); gap = gap * gap;
+      R gam = aa[k - 1] / (aa[k - 1] + prod); gam = gam * gam;
+      const R bep = R(1.) + (R(1.) / (R(2.) * al) - R(1.)) * gap;
+      const R bem = R(1.) + (R(1.) / (R(2.) * al) - R(1.)) * gam;
+      R g;
+      if (k < nk) g = -al * (wp[k] * bep * d1[k] - whatp * (R(1.) - gap) * d1[k + 1] + wm[k] * bem * d2[k] - whatm * (R(1.) - gam) * d2[k - 1]);
+      else g = -al * (wp[k] * bep * d1[k] + wm[k] * bem * d2[k] - whatm * (R(1.) - gam) * d2[k - 1]);
       ff[k] += g;
     }
-    ff[nk + 1] = 0.;
-    for (int k = kf; k <= nk; k++) buff[M.at(k, j, i)] += (ff[k + 1] - ff[k]) * M.dsgth_inv[2 * k + 1] * DT;
+    ff[nk + 1] = R(0.);
+    for (int k = kf; k <= nk; k++) {
+      const long long x = M.at(k, j, i);
+      buff[x] = buff[x] + (double)((ff[k + 1] - ff[k]) * dsi(2 * k + 1) * DT);
+    }
   }
 }
 
@@ -464,6 +494,214 @@ __global__ void __launch_bounds__(CT_THREADS) k_pgrad_vars_column(DevModel M) {
   }
 }
 
+// ---- the mixed form of the two hydrostatic column routines ----
+//
+// The interface pressures P3 (prefix sum of the layer masses) and GZ3 (the surface-up sum of
+// Leslie-Purser increments) are accumulated in FP64, as are HDRY, H3 and every stored state
+// value; the pointwise transcendentals feeding them (the layer-mean pressure P2, T3 and T2,
+// the logarithms of successive pressure ratios, the diagnostic theta above k_sigma-1) are
+// evaluated in FP32 from FP64 differences (log1p/expm1 of small ratios), which keeps their
+// relative error near 1e-7.
+
+// log(b/a) for b/a near 1, from the FP64 difference
+__device__ __forceinline__ float log_ratio_f(double a, double b) { return log1pf((float)((b - a) / a)); }
+
+// onto_kk(P2_INDEX) at a layer: ((bot^(k+1) - top^(k+1)) / ((k+1)(bot - top)))^(1/k), written as
+// bot * q^(1/kappa), q = (1 - r^(kappa+1)) / ((kappa+1)(1 - r)), r = top/bot.
+__device__ __forceinline__ double layer_p_mixed(const DevModel &M, double top, double bot) {
+  if (fcmp(bot, top) == 0) return .5 * (bot + top);
+  const float kap = (float)M.kappa, kp1 = kap + 1.f;
+  const float eps = (float)((bot - top) / bot);
+  const float num = -expm1f(kp1 * log1pf(-eps));
+  const float q = num / (kp1 * eps);
+  return bot * (double)expf(log1pf(q - 1.f) / kap);
+}
+
+__global__ void __launch_bounds__(CT_THREADS) k_set_p2etc_mixed(DevModel M, int update_theta) {
+  extern __shared__ double sm[];
+  __shared__ double s_lp[32];
+  const ColTile c = col_tile(M);
+  const int nk = M.nk, ks = M.k_sigma, L = nk + 1;
+  const long long n2 = M.n2;
+  double *P = sm, *HL = P + 32 * L, *TH = HL + 32 * L;
+  const double g = M.grav[2 * c.j + 1];
+  if (c.warp == 0) {
+    if (c.valid) {
+      double p = M.p3[c.base];
+      CT(P, 0) = p;
+      for (int k = 1; k <= nk; k++) {
+        p = p + M.dsgth[2 * k] * g * M.hdry[c.base + k * n2];
+        CT(P, k) = p;
+      }
+      s_lp[c.lane] = xlog(M, CT(P, 0) / p);
+    }
+  } else if (c.valid) {
+    for (int k = c.warp - 1; k <= nk; k += CT_WARPS - 1) CT(TH, k) = M.theta[c.base + k * n2];
+  }
+  __syncthreads();
+  const double ptop = CT(P, 0), pbot = CT(P, nk), lp = s_lp[c.lane];
+  if (c.valid)
+    for (int k = ks - 1 + c.warp; k < nk; k += CT_WARPS) {
+      const double sigma = (M.sgth[2 * k + 1] - M.zeta0) / (M.zeta1 - M.zeta0);
+      CT(P, k) = pbot * xexp(M, sigma * lp);
+    }
+  __syncthreads();
+  const float lpf = (float)lp;
+  if (c.valid)
+    for (int k = c.warp; k <= nk; k += CT_WARPS) {
+      const double pk = CT(P, k);
+      if (k >= 1) {
+        const long long x = c.base + k * n2;
+        M.p3[x] = pk;
+        const double hl = (pk - CT(P, k - 1)) / (g * M.dsgth[2 * k]);
+        CT(HL, k) = hl;
+        M.hdry[x] = dmaxr(M.h_min[k], hl);
+      }
+      if (update_theta && k < ks - 1) {
+        const float sigma = log_ratio_f(pbot, pk) / lpf;
+        float gs;
+        const float fs = f_and_g_sigma_r<float>(M, sigma, gs);
+        const double th = (double)(((float)M.sgth[2 * k + 1] - fs) / gs);
+        CT(TH, k) = th;
+        M.theta[c.base + k * n2] = th;
+      }
+    }
+  __syncthreads();
+  if (!c.valid) return;
+  for (int k = 1 + c.warp; k <= nk; k += CT_WARPS) {
+    const long long x = c.base + k * n2;
+    const double top = CT(P, k - 1), bot = CT(P, k);
+    const double p2 = layer_p_mixed(M, top, bot);
+    M.p2[x] = p2;
+    if (k == 1) M.p2[c.base] = top * top / p2;
+    double h;
+    if (k == nk) h = CT(HL, nk);
+    else {
+      const double topwt = M.dsgth[2 * k], botwt = M.dsgth[2 * k + 2];
+      h = (topwt * CT(HL, k) + botwt * CT(HL, k + 1)) / (topwt + botwt);
+    }
+    M.h3[x] = h;
+    if (k == 1) M.h3[c.base] = h;
+    if (!update_theta) continue;
+    double t2;
+    if (k < ks - 1) {
+      const float sigma = log_ratio_f(pbot, p2) / lpf;
+      float gs;
+      const float fs = f_and_g_sigma_r<float>(M, sigma, gs);
+      t2 = (double)(((float)M.sgth[2 * k] - fs) / gs);
+    } else if (k == ks - 1) {
+      t2 = .5 * (CT(TH, ks - 1) + CT(TH, ks - 2));
+    } else {
+      const int nkay = nk - (ks - 1) + 1;
+      const double sg = M.sgth[2 * k];
+      auto X = [&](int kay) { return M.sgth[2 * (nk - kay) + 1]; };
+      auto Y = [&](int kay) { return CT(TH, nk - kay); };
+      int kay;
+      if (fcmp(sg, X(0)) <= 0) kay = 0;
+      else if (fcmp(sg, X(nkay - 1)) >= 0) kay = nkay - 2;
+      else {
+        int il = -1, iu = nkay;
+        while (iu - il > 1) {
+          const int im = (iu + il) >> 1;
+          if (fcmp(sg, X(im)) >= 0) il = im; else iu = im;
+        }
+        kay = il;
+      }
+      t2 = Y(kay) + (Y(kay + 1) - Y(kay)) * (sg - X(kay)) / (X(kay + 1) - X(kay));
+    }
+    M.theta2[x] = t2;
+  }
+}
+
+__global__ void __launch_bounds__(CT_THREADS) k_pgrad_vars_column_mixed(DevModel M) {
+  extern __shared__ double sm[];
+  __shared__ double s_rho2_1[32];
+  const ColTile c = col_tile(M);
+  const int nk = M.nk, L = nk + 1;
+  const long long n2 = M.n2;
+  const double mu = M.mu_dry;
+  double *P = sm, *R = P + 32 * L, *T3 = R + 32 * L, *GZ = T3 + 32 * L;
+  float *LG = reinterpret_cast<float *>(GZ + 32 * L);
+  const float kap = (float)M.kappa;
+  const double p0 = M.press0;
+  if (c.valid)
+    for (int k = c.warp; k <= nk; k += CT_WARPS) {
+      const long long x = c.base + k * n2;
+      const double theta = M.theta[x], p = M.p3[x];
+      const double t3 = theta * (double)powf((float)(p / p0), kap);
+      M.t3[x] = t3;
+      M.exner3[x] = M.cp * t3 / theta;
+      const double rho = return_density(p, t3, mu);
+      M.rho3[x] = rho;
+      CT(P, k) = p;
+      CT(R, k) = rho;
+      CT(T3, k) = t3;
+      if (k >= 1) {
+        const double pr = M.p2[x];
+        const double t2 = M.theta2[x] * (double)powf((float)(pr / p0), kap);
+        M.t2[x] = t2;
+        const double r2 = return_density(pr, t2, mu);
+        M.rho2[x] = r2;
+        if (k == 1) s_rho2_1[c.lane] = r2;
+      }
+    }
+  __syncthreads();
+  if (c.valid) {
+    for (int k = c.warp; k < nk; k += CT_WARPS) CT(LG, k) = log_ratio_f(CT(P, k), CT(P, k + 1));
+    if (c.warp == CT_WARPS - 1) {
+      M.rho2[c.base] = CT(R, 0) * CT(R, 0) / s_rho2_1[c.lane];
+      M.theta2[c.base] = M.sgth[0];
+      M.t2[c.base] = CT(T3, 0);
+    }
+  }
+  __syncthreads();
+  if (c.valid)
+    for (int k = 2 + c.warp; k <= nk - 1; k += CT_WARPS) {
+      const float dz10 = CT(LG, k), dz21 = CT(LG, k - 1), dz32 = CT(LG, k - 2);
+      const float dz20 = dz21 + dz10, dz30 = dz32 + dz20, dz31 = dz32 + dz21;
+      const float df0 = (float)(CT(P, k + 1) / CT(R, k + 1)), df1 = (float)(CT(P, k) / CT(R, k));
+      const float df2 = (float)(CT(P, k - 1) / CT(R, k - 1)), df3 = (float)(CT(P, k - 2) / CT(R, k - 2));
+      CT(GZ, k - 1) = (double)(-(df0 * (dz21 * dz21 * dz21 * (dz31 + dz32)) / (dz10 * dz20 * dz30) +
+                                 df1 * (dz21 * (dz21 * (dz21 + 2.f * (dz10 - dz31)) - 6.f * dz10 * dz31)) / (dz10 * dz31) +
+                                 df2 * (dz21 * (dz21 * (dz21 + 2.f * (dz32 - dz20)) - 6.f * dz20 * dz32)) / (dz20 * dz32) +
+                                 df3 * (dz21 * dz21 * dz21 * (dz10 + dz20)) / (dz30 * dz31 * dz32)) /
+                               12.f);
+    }
+  __syncthreads();
+  if (c.warp == 0 && c.valid) {   // GZ3 from the surface up, in FP64
+    double gz = M.topo_scale * M.gz_surface[M.at2(c.j, c.i)];
+    CT(GZ, nk) = gz;
+    gz = gz + ((CT(P, nk) + CT(P, nk - 1)) / (CT(R, nk) + CT(R, nk - 1))) * (double)CT(LG, nk - 1);
+    CT(GZ, nk - 1) = gz;
+    for (int k = nk - 1; k >= 2; k--) {
+      gz = gz + CT(GZ, k - 1);
+      CT(GZ, k - 1) = gz;
+    }
+    CT(GZ, 0) = gz + ((CT(P, 1) + CT(P, 0)) / (CT(R, 1) + CT(R, 0))) * (double)CT(LG, 0);
+  }
+  __syncthreads();
+  if (!c.valid) return;
+  const bool interior = c.i >= 1 && c.i <= M.ni;
+  const long long itime = M.ctl->itime;
+  for (int k = c.warp; k <= nk; k += CT_WARPS) {
+    const long long x = c.base + k * n2;
+    const double gzk = CT(GZ, k);
+    const double old = M.gz3[x];
+    M.gz3[x] = gzk;
+    M.mont3[x] = gzk + return_enthalpy(M, CT(T3, k));
+    if (interior && k >= 1) {
+      double dz = 0.;
+      if (itime > 1) {
+        const double dtg_inv = -1. / (M.dt * M.grav[2 * c.j + 1]);
+        dz = (old - gzk) * dtg_inv;
+      }
+      dz += M.w3[x] * M.h3[x] / CT(R, k);
+      M.dzdt3[x] = dz;
+      if (gzk >= CT(GZ, k - 1)) flag_error(M.ctl, ERR_GZ_MONOTONE, k, c.j, c.i, gzk);
+    }
+  }
+}
+
 // store_pgrad_vars, horizontal part of DZDT3 (epic_funcs_diag.c:3924-3945) plus bc_lateral.
 __global__ void k_pgrad_dzdt(DevModel M) {
   const int t = (int)(blockIdx.x * blockDim.x + threadIdx.x);
@@ -504,30 +742,31 @@ __global__ void k_gz_monotone(DevModel M) {
 // calc_heating -> newtonian_cooling for held_suarez (epic_funcs_diag.c:4793-4869,
 // epic_sensible_heating.c:51-180, t_rad :217-314, temp_eq :325-463).  Writes every HEAT3 cell:
 // 0 outside k = 1..nk, j = 0..nj, i = 1..ni, with periodic pads.
+template <class R>
 __global__ void k_calc_heating(DevModel M) {
   const long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
   if (t >= M.n3) return;
   const int i = (int)(t % M.iadim);
   const int j = (int)((t / M.iadim) % M.jadim) - 1;
   const int k = (int)(t / M.n2);
-  double val = 0.;
+  R val = R(0.);
   int ii = i == 0 ? M.ni : (i == M.ni + 1 ? 1 : i);
   if (k >= 1 && k <= M.nk && j >= 0 && j <= M.nj && M.newt_cool_on) {
     const long long x = M.at(k, j, ii);
-    const double ka = 1. / (40. * 60. * 60. * 24.), ks = 1. / (4. * 60. * 60. * 24.);
-    const double pressure = M.p3[x];
-    const double pbot = M.p3[M.at(M.nk, j, ii)];
-    const double amp = (pressure / pbot - 0.7) / (1. - 0.7);
-    double kt = ka;
-    if (amp > 0.) kt += (ks - ka) * xpow(M, M.coslat[j], 4.) * amp;
-    const double cp_over_time = 1004. / (1. / kt);
-    double c2 = M.coslat[j];
+    const R ka = R(1.) / (R(40.) * R(60.) * R(60.) * R(24.)), ks = R(1.) / (R(4.) * R(60.) * R(60.) * R(24.));
+    const R pressure = R(M.p3[x]);
+    const R pbot = R(M.p3[M.at(M.nk, j, ii)]);
+    const R amp = (pressure / pbot - R(0.7)) / (R(1.) - R(0.7));
+    R kt = ka;
+    if (amp > R(0.)) kt += (ks - ka) * RMath<R>::pow(M, R(M.coslat[j]), R(4.)) * amp;
+    const R cp_over_time = R(1004.) / (R(1.) / kt);
+    R c2 = R(M.coslat[j]);
     c2 *= c2;
-    const double s2 = 1. - c2;
-    const double p_p0 = pressure / (1000. * 100.);
-    double teq = (315. - 60. * s2 - 10. * xlog(M, p_p0) * c2) * xpow(M, p_p0, M.kappa);
-    teq = dmaxr(200., teq);
-    val = -cp_over_time * (M.t3[x] - teq);
+    const R s2 = R(1.) - c2;
+    const R p_p0 = pressure / (R(1000.) * R(100.));
+    R teq = (R(315.) - R(60.) * s2 - R(10.) * RMath<R>::log(M, p_p0) * c2) * RMath<R>::pow(M, p_p0, R(M.kappa));
+    teq = rmax(R(200.), teq);
+    val = -cp_over_time * (R(M.t3[x]) - teq);
   }
   M.heat3[t] = val;
 }
@@ -556,30 +795,35 @@ int launch_source_sink(const DevModel &M, cudaStream_t s) { k_source_sink<<<ncol
 static inline unsigned ntile_blocks(const DevModel &M) { return epic_blocks((long long)(M.nj + 1) * (M.ni + 2), 32); }
 static inline size_t tile_smem(const DevModel &M, int arrays) { return (size_t)arrays * 32 * (M.nk + 1) * sizeof(double); }
 int launch_calc_w(const DevModel &M, cudaStream_t s) {
-  k_calc_w<<<ntile_blocks(M), CT_THREADS, tile_smem(M, 5), s>>>(M);
+  EPIC_LAUNCH_R(M.mixed, k_calc_w, ntile_blocks(M), CT_THREADS, tile_smem(M, 5), s, M);
   return 0;
 }
 int launch_uv_drag(const DevModel &M, cudaStream_t s) {
   const long long n = (long long)(M.nj + 1) * M.ni + (long long)M.nj * M.ni;
-  k_uv_drag<<<epic_blocks(n, 128), 128, 0, s>>>(M);
+  EPIC_LAUNCH_R(M.mixed, k_uv_drag, epic_blocks(n, 128), 128, 0, s, M);
   return 0;
 }
 int launch_hsu_vertical(const DevModel &M, double *buff, int kind, cudaStream_t s) {
-  k_hsu_vertical<<<ncol_blocks(M, 64), 64, 0, s>>>(M, buff, kind);
+  EPIC_LAUNCH_R(M.mixed, k_hsu_vertical, ncol_blocks(M, 64), 64, 0, s, M, buff, kind);
   return 0;
 }
 int launch_restore_mass(const DevModel &M, cudaStream_t s) { k_restore_mass<<<ncol_blocks(M, 128), 128, 0, s>>>(M); return 0; }
 int launch_set_p2etc(const DevModel &M, int update_theta, cudaStream_t s) {
-  k_set_p2etc<<<ntile_blocks(M), CT_THREADS, tile_smem(M, 4), s>>>(M, update_theta);
+  if (M.mixed) k_set_p2etc_mixed<<<ntile_blocks(M), CT_THREADS, tile_smem(M, 3), s>>>(M, update_theta);
+  else k_set_p2etc<<<ntile_blocks(M), CT_THREADS, tile_smem(M, 4), s>>>(M, update_theta);
   return 0;
 }
 int launch_store_pgrad_vars(const DevModel &M, cudaStream_t s) {
-  k_pgrad_vars_column<<<ntile_blocks(M), CT_THREADS, tile_smem(M, 5), s>>>(M);
+  if (M.mixed) k_pgrad_vars_column_mixed<<<ntile_blocks(M), CT_THREADS, tile_smem(M, 5), s>>>(M);
+  else k_pgrad_vars_column<<<ntile_blocks(M), CT_THREADS, tile_smem(M, 5), s>>>(M);
   k_pgrad_dzdt<<<epic_blocks((long long)M.nk * (M.nj + 1) * M.ni, 128), 128, 0, s>>>(M);
   return 0;
 }
 int launch_gz_monotone(const DevModel &M, cudaStream_t s) { k_gz_monotone<<<ncol_blocks(M, 128), 128, 0, s>>>(M); return 0; }
-int launch_calc_heating(const DevModel &M, cudaStream_t s) { k_calc_heating<<<epic_blocks(M.n3, 128), 128, 0, s>>>(M); return 0; }
+int launch_calc_heating(const DevModel &M, cudaStream_t s) {
+  EPIC_LAUNCH_R(M.mixed, k_calc_heating, epic_blocks(M.n3, 128), 128, 0, s, M);
+  return 0;
+}
 int launch_advection_prep(const DevModel &M, int phase, cudaStream_t s) {
   k_advection_prep<<<epic_blocks((long long)(M.nj + 1) * M.iadim * (M.nk + 2), 128), 128, 0, s>>>(M, phase);
   return 0;
@@ -590,9 +834,12 @@ int launch_advection_prep(const DevModel &M, int phase, cudaStream_t s) {
 int column_kernels_init(int nk) {
   const int big = (int)(5 * 32 * (nk + 1) * sizeof(double));
   if (big <= 48 * 1024) return 0;
-  if (cudaFuncSetAttribute(k_calc_w, cudaFuncAttributeMaxDynamicSharedMemorySize, big) != cudaSuccess ||
+  if (cudaFuncSetAttribute(k_calc_w<double>, cudaFuncAttributeMaxDynamicSharedMemorySize, big) != cudaSuccess ||
+      cudaFuncSetAttribute(k_calc_w<float>, cudaFuncAttributeMaxDynamicSharedMemorySize, big) != cudaSuccess ||
       cudaFuncSetAttribute(k_set_p2etc, cudaFuncAttributeMaxDynamicSharedMemorySize, big) != cudaSuccess ||
-      cudaFuncSetAttribute(k_pgrad_vars_column, cudaFuncAttributeMaxDynamicSharedMemorySize, big) != cudaSuccess)
+      cudaFuncSetAttribute(k_pgrad_vars_column, cudaFuncAttributeMaxDynamicSharedMemorySize, big) != cudaSuccess ||
+      cudaFuncSetAttribute(k_set_p2etc_mixed, cudaFuncAttributeMaxDynamicSharedMemorySize, big) != cudaSuccess ||
+      cudaFuncSetAttribute(k_pgrad_vars_column_mixed, cudaFuncAttributeMaxDynamicSharedMemorySize, big) != cudaSuccess)
     return -1;
   return 0;
 }

@@ -15,50 +15,61 @@
 
 namespace epic {
 
-struct Cplx { double re, im; };
+template <class R> struct Cplx { R re, im; };
 
-// Twiddle table layout (pairs of doubles), N = ni/2 complex points:
+// Twiddle table layout (pairs), N = ni/2 complex points:
 //   [0, N-1)              four1 isign=+1, stage with half h at offset h-1, entries p = 0..h-1
 //   [N-1, 2N-2)           four1 isign=-1, same layout
 //   [2N-2, 2N-2 + N/2-1)  realft forward post-processing, q = 1..N/2-1
 //   [.., + N/2-1)         realft inverse pre-processing, q = 1..N/2-1
+// The FP64 table holds the recurrence values of the reference; the mixed form reads the same
+// values rounded to float.
 __host__ __device__ inline size_t nr_twiddle_pairs(int ni) {
   const int N = ni / 2;
   return 2 * (size_t)(N - 1) + 2 * (size_t)(N / 2 - 1);
 }
 
+template <class R>
 struct FilterSmem {
-  Cplx *z, *w;   // row as N complex points; twiddles
+  Cplx<R> *z, *w;   // row as N complex points; twiddles
 };
 
-__device__ __forceinline__ FilterSmem carve_filter(double *base, int ni) {
+template <class R>
+__device__ __forceinline__ FilterSmem<R> carve_filter(R *base, int ni) {
   const int N = ni / 2;
-  FilterSmem s;
-  s.z = reinterpret_cast<Cplx *>(base);
+  FilterSmem<R> s;
+  s.z = reinterpret_cast<Cplx<R> *>(base);
   s.w = s.z + N;
   return s;
 }
-__host__ __device__ inline size_t filter_smem_doubles(int ni) {
+// shared-memory elements (of the compute type) one row filter needs
+__host__ __device__ inline size_t filter_smem_elems(int ni) {
   return 2 * ((size_t)(ni / 2) + nr_twiddle_pairs(ni));
 }
 
-__device__ __forceinline__ void load_twiddles(const DevModel &M, FilterSmem &s) {
+template <class R> __device__ __forceinline__ const R *twiddle_table(const DevModel &M);
+template <> __device__ __forceinline__ const double *twiddle_table<double>(const DevModel &M) { return M.tw; }
+template <> __device__ __forceinline__ const float *twiddle_table<float>(const DevModel &M) { return M.twf; }
+
+template <class R>
+__device__ __forceinline__ void load_twiddles(const DevModel &M, FilterSmem<R> &s) {
   const int n = (int)nr_twiddle_pairs(M.ni);
-  const Cplx *g = reinterpret_cast<const Cplx *>(M.tw);
+  const Cplx<R> *g = reinterpret_cast<const Cplx<R> *>(twiddle_table<R>(M));
   for (int k = threadIdx.x; k < n; k += blockDim.x) s.w[k] = g[k];
 }
 
 // four1's Danielson-Lanczos stages on z (already bit-reversed); tw = this direction's table.
-__device__ __forceinline__ void four1_stages(Cplx *z, const Cplx *tw, int N) {
+template <class R>
+__device__ __forceinline__ void four1_stages(Cplx<R> *z, const Cplx<R> *tw, int N) {
   for (int h = 1; h < N; h <<= 1) {
-    const Cplx *wt = tw + (h - 1);
+    const Cplx<R> *wt = tw + (h - 1);
     for (int b = threadIdx.x; b < N / 2; b += blockDim.x) {
       const int p = b & (h - 1);
       const int i0 = (b / h) * 2 * h + p;
       const int j0 = i0 + h;
-      const double wr = wt[p].re, wi = wt[p].im;
-      const double tempr = wr * z[j0].re - wi * z[j0].im;
-      const double tempi = wr * z[j0].im + wi * z[j0].re;
+      const R wr = wt[p].re, wi = wt[p].im;
+      const R tempr = wr * z[j0].re - wi * z[j0].im;
+      const R tempi = wr * z[j0].im + wi * z[j0].re;
       z[j0].re = z[i0].re - tempr;
       z[j0].im = z[i0].im - tempi;
       z[i0].re += tempr;
@@ -68,11 +79,12 @@ __device__ __forceinline__ void four1_stages(Cplx *z, const Cplx *tw, int N) {
   }
 }
 
-__device__ __forceinline__ void bitrev_permute(Cplx *z, int N, int lg) {
+template <class R>
+__device__ __forceinline__ void bitrev_permute(Cplx<R> *z, int N, int lg) {
   for (int k = threadIdx.x; k < N; k += blockDim.x) {
     const int r = (int)(__brev((unsigned)k) >> (32 - lg));
     if (r > k) {
-      const Cplx t = z[k];
+      const Cplx<R> t = z[k];
       z[k] = z[r];
       z[r] = t;
     }
@@ -81,15 +93,16 @@ __device__ __forceinline__ void bitrev_permute(Cplx *z, int N, int lg) {
 }
 
 // realft's split loop (i = 2..n/4, here q = i-1): c2 = -0.5 forward, +0.5 inverse.
-__device__ __forceinline__ void realft_split(Cplx *z, const Cplx *tw, int N, double c2) {
-  const double c1 = 0.5;
+template <class R>
+__device__ __forceinline__ void realft_split(Cplx<R> *z, const Cplx<R> *tw, int N, R c2) {
+  const R c1 = R(0.5);
   for (int q = 1 + threadIdx.x; q < N / 2; q += blockDim.x) {
-    const Cplx a = z[q], b = z[N - q];
-    const double wr = tw[q - 1].re, wi = tw[q - 1].im;
-    const double h1r = c1 * (a.re + b.re);
-    const double h1i = c1 * (a.im - b.im);
-    const double h2r = -c2 * (a.im + b.im);
-    const double h2i = c2 * (a.re - b.re);
+    const Cplx<R> a = z[q], b = z[N - q];
+    const R wr = tw[q - 1].re, wi = tw[q - 1].im;
+    const R h1r = c1 * (a.re + b.re);
+    const R h1i = c1 * (a.im - b.im);
+    const R h2r = -c2 * (a.im + b.im);
+    const R h2i = c2 * (a.re - b.re);
     z[q].re = h1r + wr * h2r - wi * h2i;
     z[q].im = h1i + wr * h2i + wi * h2r;
     z[N - q].re = h1r - wr * h2r + wi * h2i;
@@ -100,11 +113,12 @@ __device__ __forceinline__ void realft_split(Cplx *z, const Cplx *tw, int N, dou
 
 // Filter row x[1..ni] (1-based, shared memory) in place with weights h(I) = hl[rowbase + I],
 // I = 1..ni/2+1 (HIGH_LAT(J,I)).  Every thread of the block must call this.
-__device__ void filter_row_smem(const DevModel &M, double *x, const double *hl, long long rowbase, FilterSmem &s) {
+template <class R>
+__device__ void filter_row_smem(const DevModel &M, R *x, const double *hl, long long rowbase, FilterSmem<R> &s) {
   const int ni = M.ni, N = ni / 2;
   const int lg = 31 - __clz(N);
-  const Cplx *t4p = s.w, *t4m = s.w + (N - 1), *trp = s.w + 2 * (N - 1), *trm = trp + (N / 2 - 1);
-  Cplx *z = s.z;
+  const Cplx<R> *t4p = s.w, *t4m = s.w + (N - 1), *trp = s.w + 2 * (N - 1), *trm = trp + (N / 2 - 1);
+  Cplx<R> *z = s.z;
   // realft(data, n, 1): four1(data, n/2, 1) -- bit reversal, stages -- then the split loop
   for (int k = threadIdx.x; k < N; k += blockDim.x) {
     const int r = (int)(__brev((unsigned)k) >> (32 - lg));
@@ -113,9 +127,9 @@ __device__ void filter_row_smem(const DevModel &M, double *x, const double *hl, 
   }
   __syncthreads();
   four1_stages(z, t4p, N);
-  realft_split(z, trp, N, -0.5);
+  realft_split(z, trp, N, R(-0.5));
   if (threadIdx.x == 0) {
-    const double h1r = z[0].re;
+    const R h1r = z[0].re;
     z[0].re = h1r + z[0].im;
     z[0].im = h1r - z[0].im;
   }
@@ -123,26 +137,26 @@ __device__ void filter_row_smem(const DevModel &M, double *x, const double *hl, 
   // spectral weights (epic_adjust.c:447-453)
   for (int q = threadIdx.x; q < N; q += blockDim.x) {
     if (q == 0) {
-      z[0].re *= hl[rowbase + 1];
-      z[0].im *= hl[rowbase + N + 1];
+      z[0].re *= R(hl[rowbase + 1]);
+      z[0].im *= R(hl[rowbase + N + 1]);
     } else {
-      const double h = hl[rowbase + q + 1];
+      const R h = R(hl[rowbase + q + 1]);
       z[q].re *= h;
       z[q].im *= h;
     }
   }
   __syncthreads();
   // realft(data, n, -1): split loop, then four1(data, n/2, -1)
-  realft_split(z, trm, N, 0.5);
+  realft_split(z, trm, N, R(0.5));
   if (threadIdx.x == 0) {
-    const double h1r = z[0].re;
-    z[0].re = 0.5 * (h1r + z[0].im);
-    z[0].im = 0.5 * (h1r - z[0].im);
+    const R h1r = z[0].re;
+    z[0].re = R(0.5) * (h1r + z[0].im);
+    z[0].im = R(0.5) * (h1r - z[0].im);
   }
   __syncthreads();
   bitrev_permute(z, N, lg);
   four1_stages(z, t4m, N);
-  const double scale = 2. / (double)ni;
+  const R scale = R(2.) / R(ni);
   for (int k = threadIdx.x; k < N; k += blockDim.x) {
     x[2 * k + 1] = z[k].re * scale;
     x[2 * k + 2] = z[k].im * scale;
@@ -157,14 +171,16 @@ __device__ __forceinline__ bool row_is_filtered(const DevModel &M, int j, int vg
 // zonal_filter(index, plane, NULL, TWODIM) of planes k0..k0+gridDim.y-1, from src into dst
 // (dst may equal src).  Block = one row j in -1..nj+1; rows outside the filtered set are
 // copied; rows 0..nj+1 get periodic pads (bc_lateral).
+template <class R>
 __global__ void k_filter_planes(DevModel M, const double *src, int src_sel, double *dst, int k0, int vgrid) {
-  extern __shared__ double sm[];
+  extern __shared__ __align__(16) unsigned char smraw[];
+  R *sm = reinterpret_cast<R *>(smraw);
   src += plane_offset(M, src_sel);
   const int j = (int)blockIdx.x - 1;
   const int k = k0 + (int)blockIdx.y;
   const long long base = M.at(k, j, 0);
-  double *x = sm;
-  FilterSmem fs = carve_filter(sm + (M.ni + 2), M.ni);
+  R *x = sm;
+  FilterSmem<R> fs = carve_filter(sm + (M.ni + 2), M.ni);
   const bool valid = vgrid ? (j >= 1 && j <= M.nj) : (j >= 0 && j <= M.nj);
   const bool filt = valid && row_is_filtered(M, j, vgrid);
   if (!filt) {
@@ -178,31 +194,38 @@ __global__ void k_filter_planes(DevModel M, const double *src, int src_sel, doub
     return;
   }
   load_twiddles(M, fs);
-  for (int i = threadIdx.x; i <= M.ni + 1; i += blockDim.x) x[i] = src[base + i];
+  for (int i = threadIdx.x; i <= M.ni + 1; i += blockDim.x) x[i] = R(src[base + i]);
   __syncthreads();
   filter_row_smem(M, x, vgrid ? M.high_lat_pv : M.high_lat_h, M.at2(j, 0), fs);
   for (int i = threadIdx.x + 1; i <= M.ni; i += blockDim.x) write_with_pads(dst, M, base, i, x[i]);
 }
 
 // Per-latitude var(gz) profile at the column of lowest bottom GZ, the first half of the
-// THREEDIM branch of zonal_filter (epic_adjust.c:266-395).  One thread per row j.
-// index: 0 = U, 1 = V, 2 = HDRY (log), 3 = THETA.
+// THREEDIM branch of zonal_filter (epic_adjust.c:266-395).  One warp per row j: the lanes find
+// the first column of minimum bottom GZ (the reference's strict-less scan) and fill the table;
+// lane 0 fits the spline.  index: 0 = U, 1 = V, 2 = HDRY (log), 3 = THETA.
 __global__ void k_varz_tables(DevModel M, const double *buff, int sel, int index, int kstart, int kend) {
   buff += plane_offset(M, sel);
   const int jstart = index == 1 ? 1 : 0;
-  const int j = jstart + (int)(blockIdx.x * blockDim.x + threadIdx.x);
+  const int lane = (int)(threadIdx.x & 31);
+  const int j = jstart + (int)((blockIdx.x * blockDim.x + threadIdx.x) >> 5);
   if (j > M.nj) return;
   const double *gz = M.gz;
   const int K = M.nk;
-  int imin = 1;
+  int imin = 1 << 30;
   double gzmin = DBL_MAX;
-  for (int i = 1; i <= M.ni; i++) {
+  for (int i = 1 + lane; i <= M.ni; i += 32) {
     const double v = gz[M.at(K, j, i)];
     if (v < gzmin) { imin = i; gzmin = v; }
   }
-  const int i = imin;
+  for (int o = 16; o > 0; o >>= 1) {
+    const double ov = __shfl_xor_sync(0xffffffffu, gzmin, o);
+    const int oi = __shfl_xor_sync(0xffffffffu, imin, o);
+    if (ov < gzmin || (ov == gzmin && oi < imin)) { gzmin = ov; imin = oi; }
+  }
+  const int i = imin == (1 << 30) ? 1 : imin;
   Trip *t = reinterpret_cast<Trip *>(M.ptable) + (long long)(j + 1) * (M.nk + 2);
-  for (int k = kend; k >= kstart; k--) {
+  for (int k = kend - lane; k >= kstart; k -= 32) {
     const int kay = kend - k;
     double x;
     switch (index) {
@@ -214,20 +237,23 @@ __global__ void k_varz_tables(DevModel M, const double *buff, int sel, int index
     t[kay].x = x;
     t[kay].y = index == 2 ? xlog(M, buff[M.at(k, j, i)]) : buff[M.at(k, j, i)];
   }
-  if (!spline_pchip(kend - kstart + 1, t)) flag_error(M.ctl, ERR_PCHIP_X, kstart, j, i, t[0].x);
+  __syncwarp();
+  if (lane == 0 && !spline_pchip(kend - kstart + 1, t)) flag_error(M.ctl, ERR_PCHIP_X, kstart, j, i, t[0].x);
 }
 
 // The rest of the THREEDIM zonal_filter: subtract var(gz), filter, add it back.
 // Block = one row (k = kstart + blockIdx.y, j = jstart + blockIdx.x).
+template <class R>
 __global__ void k_varz_filter_rows(DevModel M, double *buff, int sel, int index, int kstart, int kend) {
-  extern __shared__ double sm[];
+  extern __shared__ __align__(16) unsigned char smraw[];
+  R *sm = reinterpret_cast<R *>(smraw);
   buff += plane_offset(M, sel);
   const int jstart = index == 1 ? 1 : 0;
   const int j = jstart + (int)blockIdx.x;
   const int k = kstart + (int)blockIdx.y;
   const int vgrid = index == 1;
-  double *x = sm, *vz = sm + (M.ni + 2);
-  FilterSmem fs = carve_filter(sm + 2 * (M.ni + 2), M.ni);
+  R *x = sm, *vz = sm + (M.ni + 2);
+  FilterSmem<R> fs = carve_filter(sm + 2 * (M.ni + 2), M.ni);
   const Trip *t = reinterpret_cast<const Trip *>(M.ptable) + (long long)(j + 1) * (M.nk + 2);
   const int n = kend - kstart + 1;
   const double *gz = M.gz;
@@ -235,50 +261,73 @@ __global__ void k_varz_filter_rows(DevModel M, double *buff, int sel, int index,
   const bool filt = row_is_filtered(M, j, vgrid);
   if (filt) load_twiddles(M, fs);
   for (int i = threadIdx.x + 1; i <= M.ni; i += blockDim.x) {
-    double gzz;
+    R gzz;
     switch (index) {
-      case 0: gzz = .5 * (gz[M.at(k, j, i)] + gz[M.at(k, j, i - 1)]); break;
-      case 1: gzz = .5 * (gz[M.at(k, j, i)] + gz[M.at(k, j - 1, i)]); break;
-      case 2: gzz = .5 * (gz[M.at(k, j, i)] + gz[M.at(k - 1, j, i)]); break;
-      default: gzz = gz[M.at(k, j, i)]; break;
+      case 0: gzz = R(.5) * (R(gz[M.at(k, j, i)]) + R(gz[M.at(k, j, i - 1)])); break;
+      case 1: gzz = R(.5) * (R(gz[M.at(k, j, i)]) + R(gz[M.at(k, j - 1, i)])); break;
+      case 2: gzz = R(.5) * (R(gz[M.at(k, j, i)]) + R(gz[M.at(k - 1, j, i)])); break;
+      default: gzz = R(gz[M.at(k, j, i)]); break;
     }
-    double dgz;
-    const int kay = find_place_in_table(n, t, gzz, &dgz);
-    double v = splint_pchip(gzz, t + kay, dgz);
-    if (index == 2) v = xexp(M, v);
+    // find_place_in_table (epic_funcs_util.c:2908-2967) and splint_pchip (:926-946)
+    int kay;
+    if (RMath<R>::cmp(gzz, R(t[0].x)) <= 0) kay = 0;
+    else if (RMath<R>::cmp(gzz, R(t[n - 1].x)) >= 0) kay = n - 2;
+    else {
+      int il = -1, iu = n;
+      while (iu - il > 1) {
+        const int im = (iu + il) >> 1;
+        if (RMath<R>::cmp(gzz, R(t[im].x)) >= 0) il = im; else iu = im;
+      }
+      kay = il;
+    }
+    const Trip *tk = t + kay;
+    const R h = R(tk[1].x) - R(tk[0].x);
+    const R delta = (R(tk[1].y) - R(tk[0].y)) / h;
+    const R del1 = (R(tk[0].z) - delta) / h;
+    const R del2 = (R(tk[1].z) - delta) / h;
+    const R c3 = (del1 + del2) / h;
+    const R c2 = -(del1 + del1 + del2);
+    const R xx = gzz - R(tk[0].x);
+    R v = R(tk[0].y) + xx * (R(tk[0].z) + xx * (c2 + xx * c3));
+    if (index == 2) v = RMath<R>::exp(M, v);
     vz[i] = v;
-    x[i] = buff[base + i] - v;
+    x[i] = R(buff[base + i] - (double)v);
   }
   __syncthreads();
   if (filt) filter_row_smem(M, x, vgrid ? M.high_lat_pv : M.high_lat_h, M.at2(j, 0), fs);
-  for (int i = threadIdx.x + 1; i <= M.ni; i += blockDim.x) write_with_pads(buff, M, base, i, x[i] + vz[i]);
+  // The mixed form leaves unfiltered rows untouched (their subtract-and-add-back is the
+  // identity up to one rounding); the FP64 form repeats the reference's arithmetic on them.
+  if (!filt && sizeof(R) == sizeof(float)) return;
+  for (int i = threadIdx.x + 1; i <= M.ni; i += blockDim.x) write_with_pads(buff, M, base, i, (double)x[i] + (double)vz[i]);
 }
 
 // Zonal pass of hsu_advection (epic_flux.c:1316-1484) for one row: the fluxes come from a
 // zonally filtered copy of the row, the update goes to the unfiltered field.
 // kind: 0 = interface variable (unity, THETA), 1 = HDRY (layer; u averaged to the layer).
+template <class R>
 __global__ void k_hsu_zonal(DevModel M, double *buff, int kind, int kstart) {
-  extern __shared__ double sm[];
+  extern __shared__ __align__(16) unsigned char smraw[];
+  R *sm = reinterpret_cast<R *>(smraw);
   const int ni = M.ni, W = ni + 2;
   const int j = (int)blockIdx.x;
   const int k = kstart + (int)blockIdx.y;
-  double *a = sm, *um = a + W, *up = um + W, *ff = up + W, *ap = ff + W, *d1 = ap + W, *d2 = d1 + W, *aa = d2 + W;
-  FilterSmem fs = carve_filter(aa + W, ni);
-  const double ep = 1.e-10, DT = M.dt;
-  const double a_min = kind == 1 ? M.h_min[k] : 0.;
+  R *a = sm, *um = a + W, *up = um + W, *ff = up + W, *ap = ff + W, *d1 = ap + W, *d2 = d1 + W, *aa = d2 + W;
+  FilterSmem<R> fs = carve_filter(aa + W, ni);
+  const R ep = R(1.e-10), DT = R(M.dt);
+  const R a_min = kind == 1 ? R(M.h_min[k]) : R(0.);
   const long long base = M.at(k, j, 0);
   const bool filt = row_is_filtered(M, j, 0);
   if (filt) load_twiddles(M, fs);
   const double *U = M.u + (long long)M.ctl->it_uv * M.n3;
-  const double n_inv = 1. / M.n[2 * j + 1];
-  const double mn1 = M.mn[2 * j + 1];
+  const R n_inv = R(1.) / R(M.n[2 * j + 1]);
+  const R mn1 = R(M.mn[2 * j + 1]);
   for (int i = threadIdx.x; i <= ni + 1; i += blockDim.x) {
-    a[i] = buff[base + i];
+    a[i] = R(buff[base + i]);
     // u2d, with periodic pads for the layer average (bc_lateral(u2d))
     const int ii = kind == 1 ? (i == 0 ? ni : (i == ni + 1 ? 1 : i)) : i;
-    const double u2d = kind == 1 ? .5 * (U[M.at(k, j, ii)] + U[M.at(k - 1, j, ii)]) : U[M.at(k, j, i)];
-    um[i] = dminr(0., u2d * n_inv);
-    up[i] = dmaxr(0., u2d * n_inv);
+    const R u2d = kind == 1 ? R(.5) * (R(U[M.at(k, j, ii)]) + R(U[M.at(k - 1, j, ii)])) : R(U[M.at(k, j, i)]);
+    um[i] = rmin(R(0.), u2d * n_inv);
+    up[i] = rmax(R(0.), u2d * n_inv);
   }
   __syncthreads();
   if (filt) filter_row_smem(M, a, M.high_lat_h, M.at2(j, 0), fs);
@@ -295,10 +344,10 @@ __global__ void k_hsu_zonal(DevModel M, double *buff, int kind, int kstart) {
   __syncthreads();
   // corrector
   for (int i = threadIdx.x + 1; i <= ni; i += blockDim.x) {
-    ff[i] = .5 * (up[i] * (ap[i] + a[i - 1]) + um[i] * (ap[i - 1] + a[i]));
+    ff[i] = R(.5) * (up[i] * (ap[i] + a[i - 1]) + um[i] * (ap[i - 1] + a[i]));
     d1[i] = ap[i] - a[i - 1];
     d2[i] = ap[i] - a[i + 1];
-    const double tmp = fabs(a[i - 1] - 2. * a[i] + a[i + 1]) + ep;
+    const R tmp = fabs(a[i - 1] - R(2.) * a[i] + a[i + 1]) + ep;
     aa[i] = tmp * tmp;
   }
   __syncthreads();
@@ -309,64 +358,71 @@ __global__ void k_hsu_zonal(DevModel M, double *buff, int kind, int kstart) {
   }
   __syncthreads();
   for (int i = threadIdx.x + 1; i <= ni; i += blockDim.x) {
-    const double uhatp = sqrt(up[i] * up[i - 1]);
-    const double uhatm = -sqrt(um[i] * um[i + 1]);
-    const double mu = (up[i] - um[i]) * mn1 * DT;
-    const double al = (1. + mu) / 6.;
-    double gap = aa[i - 1] / (aa[i - 1] + (a[i - 1] - a_min) * (a[i] - a_min));
+    const R uhatp = sqrt(up[i] * up[i - 1]);
+    const R uhatm = -sqrt(um[i] * um[i + 1]);
+    const R mu = (up[i] - um[i]) * mn1 * DT;
+    const R al = (R(1.) + mu) / R(6.);
+    R gap = aa[i - 1] / (aa[i - 1] + (a[i - 1] - a_min) * (a[i] - a_min));
     gap = gap * gap;
-    double gam = aa[i] / (aa[i] + (a[i - 1] - a_min) * (a[i] - a_min));
+    R gam = aa[i] / (aa[i] + (a[i - 1] - a_min) * (a[i] - a_min));
     gam = gam * gam;
-    const double bep = 1. + (1. / (2. * al) - 1.) * gap;
-    const double bem = 1. + (1. / (2. * al) - 1.) * gam;
-    const double behatp = 1. - gap, behatm = 1. - gam;
-    const double g = -al * (up[i] * bep * d1[i] - uhatp * behatp * d1[i - 1] + um[i] * bem * d2[i - 1] - uhatm * behatm * d2[i]);
+    const R bep = R(1.) + (R(1.) / (R(2.) * al) - R(1.)) * gap;
+    const R bem = R(1.) + (R(1.) / (R(2.) * al) - R(1.)) * gam;
+    const R behatp = R(1.) - gap, behatm = R(1.) - gam;
+    const R g = -al * (up[i] * bep * d1[i] - uhatp * behatp * d1[i - 1] + um[i] * bem * d2[i - 1] - uhatm * behatm * d2[i]);
     ff[i] += g;
   }
   __syncthreads();
   if (threadIdx.x == 0) { ff[0] = ff[ni]; ff[ni + 1] = ff[1]; }
   __syncthreads();
   for (int i = threadIdx.x + 1; i <= ni; i += blockDim.x) {
-    const double val = buff[base + i] + (ff[i] - ff[i + 1]) * mn1 * DT;
-    write_with_pads(buff, M, base, i, val);
+    write_with_pads(buff, M, base, i, buff[base + i] + (double)((ff[i] - ff[i + 1]) * mn1 * DT));
   }
 }
 
 // ---- launchers ----
 
 static int row_threads(int ni) { return ni >= 256 ? 128 : 64; }
+static size_t relem(int fp32) { return fp32 ? sizeof(float) : sizeof(double); }
 
-int launch_filter_planes(const DevModel &M, const double *src, int src_sel, double *dst, int k0, int nplanes, int vgrid, cudaStream_t s) {
+int launch_filter_planes(const DevModel &M, const double *src, int src_sel, double *dst, int k0, int nplanes, int vgrid, cudaStream_t s,
+                         int fp32) {
   if (nplanes <= 0) return 0;
-  const size_t smem = ((size_t)(M.ni + 2) + filter_smem_doubles(M.ni)) * sizeof(double);
+  const size_t smem = ((size_t)(M.ni + 2) + filter_smem_elems(M.ni)) * relem(fp32);
   dim3 grid(M.nj + 3, nplanes);
-  k_filter_planes<<<grid, row_threads(M.ni), smem, s>>>(M, src, src_sel, dst, k0, vgrid);
+  EPIC_LAUNCH_R(fp32, k_filter_planes, grid, row_threads(M.ni), smem, s, M, src, src_sel, dst, k0, vgrid);
   return 0;
 }
 
 int launch_varz_filter(const DevModel &M, double *buff, int sel, int index, int kstart, int kend, cudaStream_t s) {
   const int jstart = index == 1 ? 1 : 0;
   const int nrows = M.nj - jstart + 1;
-  k_varz_tables<<<epic_blocks(nrows, 64), 64, 0, s>>>(M, buff, sel, index, kstart, kend);
-  const size_t smem = (2 * (size_t)(M.ni + 2) + filter_smem_doubles(M.ni)) * sizeof(double);
+  k_varz_tables<<<epic_blocks(32LL * nrows, 128), 128, 0, s>>>(M, buff, sel, index, kstart, kend);
+  const size_t smem = (2 * (size_t)(M.ni + 2) + filter_smem_elems(M.ni)) * relem(M.mixed);
   dim3 grid(nrows, kend - kstart + 1);
-  k_varz_filter_rows<<<grid, row_threads(M.ni), smem, s>>>(M, buff, sel, index, kstart, kend);
+  EPIC_LAUNCH_R(M.mixed, k_varz_filter_rows, grid, row_threads(M.ni), smem, s, M, buff, sel, index, kstart, kend);
   return 0;
 }
 
 int launch_hsu_zonal(const DevModel &M, double *buff, int kind, int kstart, cudaStream_t s) {
-  const size_t smem = (8 * (size_t)(M.ni + 2) + filter_smem_doubles(M.ni)) * sizeof(double);
+  const size_t smem = (8 * (size_t)(M.ni + 2) + filter_smem_elems(M.ni)) * relem(M.mixed);
   dim3 grid(M.nj + 1, M.nk - kstart + 1);
-  k_hsu_zonal<<<grid, row_threads(M.ni), smem, s>>>(M, buff, kind, kstart);
+  EPIC_LAUNCH_R(M.mixed, k_hsu_zonal, grid, row_threads(M.ni), smem, s, M, buff, kind, kstart);
   return 0;
 }
 
+template <class R>
+static void filter_attrs(int bytes) {
+  cudaFuncSetAttribute(k_hsu_zonal<R>, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes);
+  cudaFuncSetAttribute(k_varz_filter_rows<R>, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes);
+  cudaFuncSetAttribute(k_filter_planes<R>, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes);
+}
+
 int filter_kernels_init(int ni) {
-  const size_t big = (8 * (size_t)(ni + 2) + filter_smem_doubles(ni)) * sizeof(double);
+  const size_t big = (8 * (size_t)(ni + 2) + filter_smem_elems(ni)) * sizeof(double);
   if (big > 48 * 1024) {
-    cudaFuncSetAttribute(k_hsu_zonal, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)big);
-    cudaFuncSetAttribute(k_varz_filter_rows, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)big);
-    cudaFuncSetAttribute(k_filter_planes, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)big);
+    filter_attrs<double>((int)big);
+    filter_attrs<float>((int)big);
   }
   return 0;
 }

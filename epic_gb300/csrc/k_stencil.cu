@@ -38,43 +38,49 @@ __global__ void k_zero_tend(DevModel M) {
 // epic_funcs_diag.c:2694-2847) and the PV averages of include/epic_pv_schemes.h:48-61.
 // ---------------------------------------------------------------------------------------------
 
-__device__ __forceinline__ double kin_at(const DevModel &M, const double *Uk, const double *Vk, int j, int i) {
+template <class R>
+__device__ __forceinline__ R kin_at(const DevModel &M, const double *Uk, const double *Vk, int j, int i) {
   const int jj = 2 * j;
-  double u2 = Uk[M.at2(j, i)], u4 = Uk[M.at2(j, i + 1)], v2 = Vk[M.at2(j, i)], v4 = Vk[M.at2(j + 1, i)];
-  const double kin_c = (u2 * u2 + u4 * u4 + M.mn[jj + 1] * (v2 * v2 * M.mn_inv[jj] + v4 * v4 * M.mn_inv[jj + 2])) * .25;
+  const R mn1 = R(M.mn[jj + 1]), mni0 = R(M.mn_inv[jj]), mni2 = R(M.mn_inv[jj + 2]);
+  R u2 = R(Uk[M.at2(j, i)]), u4 = R(Uk[M.at2(j, i + 1)]), v2 = R(Vk[M.at2(j, i)]), v4 = R(Vk[M.at2(j + 1, i)]);
+  const R kin_c = (u2 * u2 + u4 * u4 + mn1 * (v2 * v2 * mni0 + v4 * v4 * mni2)) * R(.25);
   if (j == 0 || j == M.nj) return kin_c;
-  u2 = .5 * (Uk[M.at2(j + 1, i)] + Uk[M.at2(j - 1, i)]);
-  u4 = .5 * (Uk[M.at2(j + 1, i + 1)] + Uk[M.at2(j - 1, i + 1)]);
-  v2 = .5 * (Vk[M.at2(j, i + 1)] + Vk[M.at2(j, i - 1)]);
-  v4 = .5 * (Vk[M.at2(j + 1, i + 1)] + Vk[M.at2(j + 1, i - 1)]);
-  const double kin_s = (u2 * u2 + u4 * u4 + M.mn[jj + 1] * (v2 * v2 * M.mn_inv[jj] + v4 * v4 * M.mn_inv[jj + 2])) * .25;
-  return (5. / 6.) * kin_c + (1. / 6.) * kin_s;
+  u2 = R(.5) * (R(Uk[M.at2(j + 1, i)]) + R(Uk[M.at2(j - 1, i)]));
+  u4 = R(.5) * (R(Uk[M.at2(j + 1, i + 1)]) + R(Uk[M.at2(j - 1, i + 1)]));
+  v2 = R(.5) * (R(Vk[M.at2(j, i + 1)]) + R(Vk[M.at2(j, i - 1)]));
+  v4 = R(.5) * (R(Vk[M.at2(j + 1, i + 1)]) + R(Vk[M.at2(j + 1, i - 1)]));
+  const R kin_s = (u2 * u2 + u4 * u4 + mn1 * (v2 * v2 * mni0 + v4 * v4 * mni2)) * R(.25);
+  return (R(5.) / R(6.)) * kin_c + (R(1.) / R(6.)) * kin_s;
 }
 // UH(j,i) for j = 0..nj (0 above), periodic in i
-__device__ __forceinline__ double uh_at(const DevModel &M, const double *Uk, const double *Hk, int j, int i) {
-  if (j < 0 || j > M.nj) return 0.;
+template <class R>
+__device__ __forceinline__ R uh_at(const DevModel &M, const double *Uk, const double *Hk, int j, int i) {
+  if (j < 0 || j > M.nj) return R(0.);
   i = wrap_i(M, i);
-  const double havg = .5 * (Hk[M.at2(j, i)] + Hk[M.at2(j, i - 1)]);
-  return Uk[M.at2(j, i)] * havg * (1. / M.n[2 * j + 1]);
+  const R havg = R(.5) * (R(Hk[M.at2(j, i)]) + R(Hk[M.at2(j, i - 1)]));
+  return R(Uk[M.at2(j, i)]) * havg * (R(1.) / R(M.n[2 * j + 1]));
 }
 // VH(j,i) for j = 1..nj (0 at the poles), periodic in i
-__device__ __forceinline__ double vh_at(const DevModel &M, const double *Vk, const double *Hk, int j, int i) {
-  if (j < 1 || j > M.nj) return 0.;
+template <class R>
+__device__ __forceinline__ R vh_at(const DevModel &M, const double *Vk, const double *Hk, int j, int i) {
+  if (j < 1 || j > M.nj) return R(0.);
   i = wrap_i(M, i);
-  const double havg = .5 * (Hk[M.at2(j, i)] + Hk[M.at2(j - 1, i)]);
-  return Vk[M.at2(j, i)] * havg * (1. / M.m[2 * j]);
+  const R havg = R(.5) * (R(Hk[M.at2(j, i)]) + R(Hk[M.at2(j - 1, i)]));
+  return R(Vk[M.at2(j, i)]) * havg * (R(1.) / R(M.m[2 * j]));
 }
 
 // Kinetic energy per mass on the h grid, planes k = 1..nk-1, into work0 (with pads).
+template <class R>
 __global__ void k_uv_kin(DevModel M) {
   Cell c;
   if (!cell3(M, 1, M.nk - 1, 0, M.nj + 1, c)) return;
   const long long off = plane_offset(M, PL_UV);
   const double *Uk = M.u + off + c.k * M.n2, *Vk = M.v + off + c.k * M.n2;
-  write_with_pads(M.work0, M, M.at(c.k, c.j, 0), c.i, kin_at(M, Uk, Vk, c.j, c.i));
+  write_with_pads(M.work0, M, M.at(c.k, c.j, 0), c.i, kin_at<R>(M, Uk, Vk, c.j, c.i));
 }
 
 // DVDT += (PV*UH terms + KIN(j-1)-KIN(j))*n, then the vertical advection of V.
+template <class R>
 __global__ void k_uv_core_v(DevModel M) {
   Cell c;
   if (!cell3(M, 1, M.nk - 1, 1, M.nj, c)) return;
@@ -84,22 +90,24 @@ __global__ void k_uv_core_v(DevModel M) {
   const double *Uk = U + k * M.n2, *Hk = M.h3 + k * M.n2;
   const double *PV = M.pv3 + k * M.n2, *KIN = M.work0 + k * M.n2;
   double *D = M.dvdt + plane_offset(M, PL_UV_TEND);
-  auto pv = [&](int jj, int ii) { return PV[M.at2(jj, ii)]; };
-  const double ga = (pv(j, i) + pv(j, i + 1) + pv(j + 1, i + 1));
-  const double de = (pv(j, i) + pv(j + 1, i) + pv(j, i + 1));
-  const double al = (pv(j - 1, i) + pv(j, i) + pv(j, i + 1));
-  const double be = (pv(j, i) + pv(j, i + 1) + pv(j - 1, i + 1));
-  const double core = ((-ga * uh_at(M, Uk, Hk, j, i + 1) - de * uh_at(M, Uk, Hk, j, i) - al * uh_at(M, Uk, Hk, j - 1, i) -
-                        be * uh_at(M, Uk, Hk, j - 1, i + 1)) * (1. / 12.) +
-                       KIN[M.at2(j - 1, i)] - KIN[M.at2(j, i)]) * M.n[2 * j];
+  auto pv = [&](int jj, int ii) { return R(PV[M.at2(jj, ii)]); };
+  const R ga = (pv(j, i) + pv(j, i + 1) + pv(j + 1, i + 1));
+  const R de = (pv(j, i) + pv(j + 1, i) + pv(j, i + 1));
+  const R al = (pv(j - 1, i) + pv(j, i) + pv(j, i + 1));
+  const R be = (pv(j, i) + pv(j, i + 1) + pv(j - 1, i + 1));
+  const R core = ((-ga * uh_at<R>(M, Uk, Hk, j, i + 1) - de * uh_at<R>(M, Uk, Hk, j, i) - al * uh_at<R>(M, Uk, Hk, j - 1, i) -
+                   be * uh_at<R>(M, Uk, Hk, j - 1, i + 1)) * (R(1.) / R(12.)) +
+                  R(KIN[M.at2(j - 1, i)]) - R(KIN[M.at2(j, i)])) * R(M.n[2 * j]);
   const long long x = M.at(k, j, i);
-  double d = D[x] + core;
+  double d = D[x] + (double)core;
   const int kk = 2 * k + 1;
-  d -= .5 * (M.w3[x] + M.w3[M.at(k, j - 1, i)]) * (V[M.at(k - 1, j, i)] - V[M.at(k + 1, j, i)]) / (M.sgth[kk - 2] - M.sgth[kk + 2]);
+  d -= (double)(R(.5) * (R(M.w3[x]) + R(M.w3[M.at(k, j - 1, i)])) * (R(V[M.at(k - 1, j, i)]) - R(V[M.at(k + 1, j, i)])) /
+                (R(M.sgth[kk - 2]) - R(M.sgth[kk + 2])));
   D[x] = d;
 }
 
 // DUDT += (PV*VH terms + KIN(i-1)-KIN(i))*m with the filtered KIN, then the vertical advection of U.
+template <class R>
 __global__ void k_uv_core_u(DevModel M) {
   Cell c;
   if (!cell3(M, 1, M.nk - 1, 0, M.nj + 1, c)) return;
@@ -109,18 +117,19 @@ __global__ void k_uv_core_u(DevModel M) {
   const double *Vk = V + k * M.n2, *Hk = M.h3 + k * M.n2;
   const double *PV = M.pv3 + k * M.n2, *KIN = M.work0 + k * M.n2;
   double *D = M.dudt + plane_offset(M, PL_UV_TEND);
-  auto pv = [&](int jj, int ii) { return PV[M.at2(jj, ii)]; };
-  const double al = (pv(j, i) + pv(j + 1, i) + pv(j + 1, i + 1));
-  const double be = (pv(j + 1, i - 1) + pv(j + 1, i) + pv(j, i));
-  const double ga = (pv(j, i - 1) + pv(j, i) + pv(j + 1, i));
-  const double de = (pv(j, i) + pv(j + 1, i) + pv(j, i + 1));
-  const double core = ((al * vh_at(M, Vk, Hk, j + 1, i) + be * vh_at(M, Vk, Hk, j + 1, i - 1) + ga * vh_at(M, Vk, Hk, j, i - 1) +
-                        de * vh_at(M, Vk, Hk, j, i)) * (1. / 12.) +
-                       KIN[M.at2(j, i - 1)] - KIN[M.at2(j, i)]) * M.m[2 * j + 1];
+  auto pv = [&](int jj, int ii) { return R(PV[M.at2(jj, ii)]); };
+  const R al = (pv(j, i) + pv(j + 1, i) + pv(j + 1, i + 1));
+  const R be = (pv(j + 1, i - 1) + pv(j + 1, i) + pv(j, i));
+  const R ga = (pv(j, i - 1) + pv(j, i) + pv(j + 1, i));
+  const R de = (pv(j, i) + pv(j + 1, i) + pv(j, i + 1));
+  const R core = ((al * vh_at<R>(M, Vk, Hk, j + 1, i) + be * vh_at<R>(M, Vk, Hk, j + 1, i - 1) + ga * vh_at<R>(M, Vk, Hk, j, i - 1) +
+                   de * vh_at<R>(M, Vk, Hk, j, i)) * (R(1.) / R(12.)) +
+                  R(KIN[M.at2(j, i - 1)]) - R(KIN[M.at2(j, i)])) * R(M.m[2 * j + 1]);
   const long long x = M.at(k, j, i);
-  double d = D[x] + core;
+  double d = D[x] + (double)core;
   const int kk = 2 * k + 1;
-  d -= .5 * (M.w3[x] + M.w3[M.at(k, j, i - 1)]) * (U[M.at(k - 1, j, i)] - U[M.at(k + 1, j, i)]) / (M.sgth[kk - 2] - M.sgth[kk + 2]);
+  d -= (double)(R(.5) * (R(M.w3[x]) + R(M.w3[M.at(k, j, i - 1)])) * (R(U[M.at(k - 1, j, i)]) - R(U[M.at(k + 1, j, i)])) /
+                (R(M.sgth[kk - 2]) - R(M.sgth[kk + 2])));
   D[x] = d;
 }
 
@@ -298,86 +307,91 @@ __global__ void k_pgrad_lat(DevModel M) {
 // THETA), 2 = HDRY (v averaged to the layer).  Four launches over all planes k0..nk.
 // ---------------------------------------------------------------------------------------------
 
-__device__ __forceinline__ void vmp(const DevModel &M, const double *V, int kind, int k, int j, int i, double &vm, double &vp) {
-  double v2d;
-  if (j < 0 || j > M.nj + 1) { vm = vp = 0.; return; }
-  if (kind == 2) v2d = (j >= 1 && j <= M.nj) ? .5 * (V[M.at(k, j, i)] + V[M.at(k - 1, j, i)]) : 0.;
-  else v2d = V[M.at(k, j, i)];
-  const double mi = (fabs(M.lat[2 * j]) == 90.) ? 0. : 1. / M.m[2 * j];
-  vm = dminr(0., v2d * mi);
-  vp = dmaxr(0., v2d * mi);
+template <class R>
+__device__ __forceinline__ void vmp(const DevModel &M, const double *V, int kind, int k, int j, int i, R &vm, R &vp) {
+  R v2d;
+  if (j < 0 || j > M.nj + 1) { vm = vp = R(0.); return; }
+  if (kind == 2) v2d = (j >= 1 && j <= M.nj) ? R(.5) * (R(V[M.at(k, j, i)]) + R(V[M.at(k - 1, j, i)])) : R(0.);
+  else v2d = R(V[M.at(k, j, i)]);
+  const R mi = (fabs(M.lat[2 * j]) == 90.) ? R(0.) : R(1.) / R(M.m[2 * j]);
+  vm = rmin(R(0.), v2d * mi);
+  vp = rmax(R(0.), v2d * mi);
 }
 
+template <class R>
 __global__ void k_hsu_merid_pred(DevModel M, const double *A, int kind, int k0) {
   Cell c;
   if (!cell3(M, k0, M.nk - k0 + 1, 0, M.nj + 2, c)) return;   // rows 0..nj+1
   const double *V = M.v + plane_offset(M, PL_UV);
-  double ff = 0.;
+  R ff = R(0.);
   if (c.j >= 1 && c.j <= M.nj) {
-    double vm, vp;
-    vmp(M, V, kind, c.k, c.j, c.i, vm, vp);
-    ff = vp * A[M.at(c.k, c.j - 1, c.i)] + vm * A[M.at(c.k, c.j, c.i)];
+    R vm, vp;
+    vmp<R>(M, V, kind, c.k, c.j, c.i, vm, vp);
+    ff = vp * R(A[M.at(c.k, c.j - 1, c.i)]) + vm * R(A[M.at(c.k, c.j, c.i)]);
   }
   write_with_pads(M.work1, M, M.at(c.k, c.j, 0), c.i, ff);
 }
 
+template <class R>
 __global__ void k_hsu_merid_apred(DevModel M, const double *A, int k0) {
   Cell c;
   if (!cell3(M, k0, M.nk - k0 + 1, 0, M.nj + 1, c)) return;
   const double *FF = M.work1;
   const long long x = M.at(c.k, c.j, c.i);
-  const double da = (FF[x] - FF[M.at(c.k, c.j + 1, c.i)]) * M.mn[2 * c.j + 1] * M.dt;
-  write_with_pads(M.work2, M, M.at(c.k, c.j, 0), c.i, A[x] + da);
+  const R da = (R(FF[x]) - R(FF[M.at(c.k, c.j + 1, c.i)])) * R(M.mn[2 * c.j + 1]) * R(M.dt);
+  write_with_pads(M.work2, M, M.at(c.k, c.j, 0), c.i, A[x] + (double)da);
 }
 
+template <class R>
 __global__ void k_hsu_merid_corr(DevModel M, const double *A, int kind, int k0) {
   Cell c;
   if (!cell3(M, k0, M.nk - k0 + 1, 0, M.nj + 2, c)) return;
   const int k = c.k, j = c.j, i = c.i, nj = M.nj;
-  double ffv = 0.;
+  R ffv = R(0.);
   if (j >= 1 && j <= nj) {
-    const double ep = 1.e-10, DT = M.dt;
-    const double a_min = kind == 2 ? M.h_min[k] : 0.;
+    const R ep = R(1.e-10), DT = R(M.dt);
+    const R a_min = kind == 2 ? R(M.h_min[k]) : R(0.);
     const double *V = M.v + plane_offset(M, PL_UV);
     const double *AP = M.work2;
-    auto a = [&](int jj) { return A[M.at(k, jj, i)]; };
-    auto ap = [&](int jj) { return AP[M.at(k, jj, i)]; };
-    auto diff1 = [&](int jj) { return jj == 0 ? 0. : ap(jj) - a(jj - 1); };
-    auto diff2 = [&](int jj) { return jj == nj ? 0. : ap(jj) - a(jj + 1); };
+    auto a = [&](int jj) { return R(A[M.at(k, jj, i)]); };
+    auto ap = [&](int jj) { return R(AP[M.at(k, jj, i)]); };
+    auto diff1 = [&](int jj) { return jj == 0 ? R(0.) : ap(jj) - a(jj - 1); };
+    auto diff2 = [&](int jj) { return jj == nj ? R(0.) : ap(jj) - a(jj + 1); };
     auto aaa = [&](int jj) {
-      double t;
+      R t;
       if (jj == 0) t = fabs(-a(0) + a(1)) + ep;
       else if (jj == nj) t = fabs(a(nj - 1) - a(nj)) + ep;
-      else t = fabs(a(jj - 1) - 2. * a(jj) + a(jj + 1)) + ep;
+      else t = fabs(a(jj - 1) - R(2.) * a(jj) + a(jj + 1)) + ep;
       return t * t;
     };
-    double vm, vp, vmm, vpm, vmp1, vpp1;
-    vmp(M, V, kind, k, j, i, vm, vp);
-    vmp(M, V, kind, k, j - 1, i, vmm, vpm);
-    vmp(M, V, kind, k, j + 1, i, vmp1, vpp1);
-    ffv = .5 * (vp * (ap(j) + a(j - 1)) + vm * (ap(j - 1) + a(j)));
-    const double vhatp = sqrt(vp * vpm);
-    const double vhatm = -sqrt(vm * vmp1);
-    const double mu = (vp - vm) * M.mn[2 * j] * DT;
-    const double al = (1. + mu) / 6.;
-    const double am1 = aaa(j - 1), a0 = aaa(j);
-    const double prod = (a(j - 1) - a_min) * (a(j) - a_min);
-    double gap = am1 / (am1 + prod); gap = gap * gap;
-    double gam = a0 / (a0 + prod); gam = gam * gam;
-    const double bep = 1. + (1. / (2. * al) - 1.) * gap;
-    const double bem = 1. + (1. / (2. * al) - 1.) * gam;
-    ffv += -al * (vp * bep * diff1(j) - vhatp * (1. - gap) * diff1(j - 1) + vm * bem * diff2(j - 1) - vhatm * (1. - gam) * diff2(j));
+    R vm, vp, vmm, vpm, vmp1, vpp1;
+    vmp<R>(M, V, kind, k, j, i, vm, vp);
+    vmp<R>(M, V, kind, k, j - 1, i, vmm, vpm);
+    vmp<R>(M, V, kind, k, j + 1, i, vmp1, vpp1);
+    ffv = R(.5) * (vp * (ap(j) + a(j - 1)) + vm * (ap(j - 1) + a(j)));
+    const R vhatp = sqrt(vp * vpm);
+    const R vhatm = -sqrt(vm * vmp1);
+    const R mu = (vp - vm) * R(M.mn[2 * j]) * DT;
+    const R al = (R(1.) + mu) / R(6.);
+    const R am1 = aaa(j - 1), a0 = aaa(j);
+    const R prod = (a(j - 1) - a_min) * (a(j) - a_min);
+    R gap = am1 / (am1 + prod); gap = gap * gap;
+    R gam = a0 / (a0 + prod); gam = gam * gam;
+    const R bep = R(1.) + (R(1.) / (R(2.) * al) - R(1.)) * gap;
+    const R bem = R(1.) + (R(1.) / (R(2.) * al) - R(1.)) * gam;
+    ffv += -al * (vp * bep * diff1(j) - vhatp * (R(1.) - gap) * diff1(j - 1) + vm * bem * diff2(j - 1) - vhatm * (R(1.) - gam) * diff2(j));
   }
   write_with_pads(M.work3, M, M.at(k, j, 0), i, ffv);
 }
 
+template <class R>
 __global__ void k_hsu_merid_update(DevModel M, double *A, int k0) {
   Cell c;
   if (!cell3(M, k0, M.nk - k0 + 1, 0, M.nj + 1, c)) return;
   const double *FF = M.work3;
   const long long x = M.at(c.k, c.j, c.i);
-  const double da = (FF[x] - FF[M.at(c.k, c.j + 1, c.i)]) * M.mn[2 * c.j + 1] * M.dt;
-  write_with_pads(A, M, M.at(c.k, c.j, 0), c.i, A[x] + da);
+  const R da = (R(FF[x]) - R(FF[M.at(c.k, c.j + 1, c.i)])) * R(M.mn[2 * c.j + 1]) * R(M.dt);
+  write_with_pads(A, M, M.at(c.k, c.j, 0), c.i, A[x] + (double)da);
 }
 
 // ---------------------------------------------------------------------------------------------
@@ -385,6 +399,7 @@ __global__ void k_hsu_merid_update(DevModel M, double *A, int k0) {
 // ---------------------------------------------------------------------------------------------
 
 // d2dy2 of planes k0..k1 of src into dst (coefficients per row from the init block, :1049-1141).
+template <class R>
 __global__ void k_d2dy2(DevModel M, const double *src, int src_sel, double *dst, int vgrid, double diff_coef, int k0, int nkk) {
   Cell c;
   const int nrows = vgrid ? M.nj + 2 : M.nj + 1;   // v: j = 0..nj+1, h: j = 0..nj
@@ -392,9 +407,9 @@ __global__ void k_d2dy2(DevModel M, const double *src, int src_sel, double *dst,
   src += plane_offset(M, src_sel);
   const int k = c.k, j = c.j, i = c.i, nj = M.nj;
   const double *cf = (vgrid ? M.v_coef : M.h_coef) + 3 * j;
-  const double a0 = diff_coef * cf[0], a1 = diff_coef * cf[1], a2 = diff_coef * cf[2];
-  auto h = [&](int jj) { return src[M.at(k, jj, i)]; };
-  double d;
+  const R a0 = R(diff_coef) * R(cf[0]), a1 = R(diff_coef) * R(cf[1]), a2 = R(diff_coef) * R(cf[2]);
+  auto h = [&](int jj) { return R(src[M.at(k, jj, i)]); };
+  R d;
   const int jlast = vgrid ? nj + 1 : nj;
   if (j == 0) d = a0 * h(0) + a1 * h(1) + a2 * h(2);
   else if (j == jlast) d = a0 * h(j - 2) + a1 * h(j - 1) + a2 * h(j);
@@ -403,46 +418,67 @@ __global__ void k_d2dy2(DevModel M, const double *src, int src_sel, double *dst,
 }
 
 // A += dt*sign*D over the rows the reference updates (v: 1..nj, h: 0..nj).
+template <class R>
 __global__ void k_visc_apply(DevModel M, double *A, int sel, const double *D, int vgrid, double sign, int k0, int nkk) {
   Cell c;
   if (!cell3(M, k0, nkk, vgrid ? 1 : 0, vgrid ? M.nj : M.nj + 1, c)) return;
   A += plane_offset(M, sel);
   const long long x = M.at(c.k, c.j, c.i);
-  write_with_pads(A, M, M.at(c.k, c.j, 0), c.i, A[x] + M.dt * sign * D[x]);
+  write_with_pads(A, M, M.at(c.k, c.j, 0), c.i, A[x] + (double)(R(M.dt) * R(sign) * R(D[x])));
 }
 
-// zonal_hyperviscosity for one row (block), epic_subgrid.c:715-808.
+// zonal_hyperviscosity for one row (block), epic_subgrid.c:715-808.  The updated row stays in
+// FP64 in both forms.  The FP64 form sums the row mean in the reference's order on one thread;
+// the mixed form sums it in FP64 with a block reduction.
+template <class R>
 __global__ void k_zonal_visc(DevModel M, double *A, int sel, int jbot, int jhalf, int k0) {
-  extern __shared__ double sm[];
+  extern __shared__ __align__(16) unsigned char smraw[];
   const int ni = M.ni;
   const int j = jbot + (int)blockIdx.x;
   const int k = k0 + (int)blockIdx.y;
   A += plane_offset(M, sel);
   const long long base = M.at(k, j, 0);
-  double *a = sm, *hh = a + (ni + 2), *d = hh + (ni + 2);
-  __shared__ double mean;
-  for (int i = threadIdx.x; i <= ni + 1; i += blockDim.x) { a[i] = A[base + i]; hh[i] = a[i]; }
+  double *a = reinterpret_cast<double *>(smraw);
+  R *hh = reinterpret_cast<R *>(a + (ni + 2)), *d = hh + (ni + 2);
+  __shared__ R mean;
+  __shared__ double part[32];
+  for (int i = threadIdx.x; i <= ni + 1; i += blockDim.x) { a[i] = A[base + i]; hh[i] = R(a[i]); }
   __syncthreads();
   const bool taper = fabs(M.lat[2 * j + jhalf]) > M.lat0;
   const double mm = M.m[2 * j + jhalf];
-  double sign = 1.;
+  R sign = R(1.);
   bool any_applied = false;
   for (int itmp = 2; itmp <= 8; itmp += 2) {
-    const double dc = taper ? M.coef[itmp] * M.m0 * M.m0 : M.coef[itmp] * mm * mm;
-    for (int i = threadIdx.x + 1; i <= ni; i += blockDim.x) d[i] = dc * (hh[i - 1] - 2. * hh[i] + hh[i + 1]);
+    const R dc = R(taper ? M.coef[itmp] * M.m0 * M.m0 : M.coef[itmp] * mm * mm);
+    for (int i = threadIdx.x + 1; i <= ni; i += blockDim.x) d[i] = dc * (hh[i - 1] - R(2.) * hh[i] + hh[i + 1]);
     __syncthreads();
-    if (threadIdx.x == 0) {
-      d[ni + 1] = d[1];
-      d[0] = d[ni];
+    if (sizeof(R) == sizeof(double)) {
+      if (threadIdx.x == 0) {
+        d[ni + 1] = d[1];
+        d[0] = d[ni];
+        double fm = 0.;
+        for (int i = 1; i <= ni; i++) fm += d[i];
+        mean = R(fm / ni);
+      }
+    } else {
       double fm = 0.;
-      for (int i = 1; i <= ni; i++) fm += d[i];
-      mean = fm / ni;
+      for (int i = threadIdx.x + 1; i <= ni; i += blockDim.x) fm += (double)d[i];
+      for (int o = 16; o > 0; o >>= 1) fm += __shfl_xor_sync(0xffffffffu, fm, o);
+      if ((threadIdx.x & 31) == 0) part[threadIdx.x >> 5] = fm;
+      __syncthreads();
+      if (threadIdx.x == 0) {
+        double t = 0.;
+        for (int w = 0; w < (int)(blockDim.x >> 5); w++) t += part[w];
+        mean = R(t / ni);
+        d[ni + 1] = d[1];
+        d[0] = d[ni];
+      }
     }
     __syncthreads();
     for (int i = threadIdx.x; i <= ni + 1; i += blockDim.x) d[i] -= mean;
     __syncthreads();
     if (M.nu[itmp] > 0.) {
-      for (int i = threadIdx.x + 1; i <= ni; i += blockDim.x) a[i] += M.dt * sign * d[i];
+      for (int i = threadIdx.x + 1; i <= ni; i += blockDim.x) a[i] += (double)(R(M.dt) * sign * d[i]);
       any_applied = true;
     }
     sign = -sign;
@@ -462,37 +498,42 @@ __global__ void k_zonal_visc(DevModel M, double *A, int sel, int jbot, int jhalf
 // ---------------------------------------------------------------------------------------------
 
 // DIV(j,i) of (UU, VV) on planes k0.., divergence() :4064-4117
-__device__ __forceinline__ double div_at(const DevModel &M, const double *UU, const double *VV, int k, int j, int i) {
+template <class R>
+__device__ __forceinline__ R div_at(const DevModel &M, const double *UU, const double *VV, int k, int j, int i) {
   const int jj = 2 * j + 1;
-  const double n_inv = 1. / M.n[jj];
-  const double mn1 = M.mn[jj];
-  const double m2j_inv = (j == 0) ? 0. : 1. / M.m[jj - 1];
-  const double m2jp2_inv = (j == M.nj) ? 0. : 1. / M.m[jj + 1];
-  return mn1 * ((UU[M.at(k, j, i + 1)] * n_inv - UU[M.at(k, j, i)] * n_inv) + (VV[M.at(k, j + 1, i)] * m2jp2_inv - VV[M.at(k, j, i)] * m2j_inv));
+  const R n_inv = R(1.) / R(M.n[jj]);
+  const R mn1 = R(M.mn[jj]);
+  const R m2j_inv = (j == 0) ? R(0.) : R(1.) / R(M.m[jj - 1]);
+  const R m2jp2_inv = (j == M.nj) ? R(0.) : R(1.) / R(M.m[jj + 1]);
+  return mn1 * ((R(UU[M.at(k, j, i + 1)]) * n_inv - R(UU[M.at(k, j, i)]) * n_inv) +
+                (R(VV[M.at(k, j + 1, i)]) * m2jp2_inv - R(VV[M.at(k, j, i)]) * m2j_inv));
 }
 
+template <class R>
 __global__ void k_divergence(DevModel M, const double *UU, const double *VV, int vsel, double *DI, int k0, int nkk) {
   Cell c;
   if (!cell3(M, k0, nkk, 0, M.nj + 1, c)) return;
   VV += plane_offset(M, vsel);
-  write_with_pads(DI, M, M.at(c.k, c.j, 0), c.i, div_at(M, UU, VV, c.k, c.j, c.i));
+  write_with_pads(DI, M, M.at(c.k, c.j, 0), c.i, div_at<R>(M, UU, VV, c.k, c.j, c.i));
 }
 
 // Interior potential vorticity, vorticity(ON_SIGMATHETA, POTENTIAL) :4168-4186, planes 0..nk.
+template <class R>
 __global__ void k_pv_interior(DevModel M, const double *VV) {
   Cell c;
   if (!cell3(M, 0, M.nk + 1, 1, M.nj, c)) return;
   const int k = c.k, j = c.j, i = c.i;
   const double *UU = M.u + plane_offset(M, PL_UV);
   const double *HH = M.h3;
-  const double f2j = M.f[2 * j], m2j = M.m[2 * j], n2j = M.n[2 * j];
-  const double m_m1_inv = 1. / M.m[2 * j - 1], m_p1_inv = 1. / M.m[2 * j + 1];
-  const double mn_m1_inv = 1. / M.mn[2 * j - 1], mn_p1_inv = 1. / M.mn[2 * j + 1];
-  const double mn_pv = .5 / (mn_m1_inv + mn_p1_inv);
-  const double ze = m2j * ((VV[M.at(k, j, i)] - VV[M.at(k, j, i - 1)]) +
-                           n2j * (UU[M.at(k, j - 1, i)] * m_m1_inv - UU[M.at(k, j, i)] * m_p1_inv));
-  double pv = (ze + f2j);
-  const double h_pv = ((HH[M.at(k, j, i)] + HH[M.at(k, j, i - 1)]) * mn_p1_inv + (HH[M.at(k, j - 1, i)] + HH[M.at(k, j - 1, i - 1)]) * mn_m1_inv) * mn_pv;
+  const R f2j = R(M.f[2 * j]), m2j = R(M.m[2 * j]), n2j = R(M.n[2 * j]);
+  const R m_m1_inv = R(1.) / R(M.m[2 * j - 1]), m_p1_inv = R(1.) / R(M.m[2 * j + 1]);
+  const R mn_m1_inv = R(1.) / R(M.mn[2 * j - 1]), mn_p1_inv = R(1.) / R(M.mn[2 * j + 1]);
+  const R mn_pv = R(.5) / (mn_m1_inv + mn_p1_inv);
+  const R ze = m2j * ((R(VV[M.at(k, j, i)]) - R(VV[M.at(k, j, i - 1)])) +
+                      n2j * (R(UU[M.at(k, j - 1, i)]) * m_m1_inv - R(UU[M.at(k, j, i)]) * m_p1_inv));
+  R pv = (ze + f2j);
+  const R h_pv = ((R(HH[M.at(k, j, i)]) + R(HH[M.at(k, j, i - 1)])) * mn_p1_inv +
+                  (R(HH[M.at(k, j - 1, i)]) + R(HH[M.at(k, j - 1, i - 1)])) * mn_m1_inv) * mn_pv;
   pv /= h_pv;
   write_with_pads(M.pv3, M, M.at(k, j, 0), i, pv);
 }
@@ -528,35 +569,40 @@ __global__ void k_pv_poles(DevModel M) {
 
 // Richardson number in the layers, get_richardson/get_brunt2 (:2885-3156).  The V term of
 // dvdz2 keeps the reference's sign slip (:3127-3128); only dudz2 decides the 1e6 branch.
+template <class R>
 __global__ void k_ri2(DevModel M) {
   Cell c;
   if (!cell3(M, 1, M.nk, 0, M.nj + 1, c)) return;
   const int k = c.k, j = c.j, i = c.i;
   const long long off = plane_offset(M, PL_UV);
   const double *U = M.u + off, *V = M.v + off;
-  double dudz2 = .5 * (U[M.at(k - 1, j, i)] + U[M.at(k - 1, j, i + 1)] - U[M.at(k, j, i)] - U[M.at(k, j, i + 1)]);
-  double dvdz2 = .5 * (V[M.at(k - 1, j, i)] + V[M.at(k - 1, j + 1, i)] - V[M.at(k, j, i)] + V[M.at(k, j + 1, i)]);
+  auto u = [&](int kk, int jj, int ii) { return R(U[M.at(kk, jj, ii)]); };
+  auto v = [&](int kk, int jj, int ii) { return R(V[M.at(kk, jj, ii)]); };
+  R dudz2 = R(.5) * (u(k - 1, j, i) + u(k - 1, j, i + 1) - u(k, j, i) - u(k, j, i + 1));
+  R dvdz2 = R(.5) * (v(k - 1, j, i) + v(k - 1, j + 1, i) - v(k, j, i) + v(k, j + 1, i));
   dudz2 *= dudz2;
   dvdz2 *= dvdz2;
-  double ri;
-  if (fcmp(dudz2, 0.) != 0) {
+  R ri;
+  if (RMath<R>::cmp(dudz2, R(0.)) != 0) {
     const long long x = M.at(k, j, i);
-    const double pressure = M.p2[x], temperature = M.t2[x], density = M.rho2[x];
-    const double cp = 1004., mu = M.mu_dry;
-    const double deltap = 0.001 * pressure, deltaT = 0.001 * temperature;
-    const double drho_dp_T = (return_density(pressure + deltap, temperature, mu) - return_density(pressure - deltap, temperature, mu)) / (2. * deltap);
-    const double drho_dT_p = (return_density(pressure, temperature + deltaT, mu) - return_density(pressure, temperature - deltaT, mu)) / (2. * deltaT);
-    const double Drho_Dp = (M.rho3[x] - M.rho3[M.at(k - 1, j, i)]) / (M.p3[x] - M.p3[M.at(k - 1, j, i)]);
-    const double g = M.grav[2 * j + 1];
-    const double brunt2 = g * g * (Drho_Dp - drho_dp_T + temperature / (cp * density * density) * drho_dT_p * drho_dT_p);
+    const R pressure = R(M.p2[x]), temperature = R(M.t2[x]), density = R(M.rho2[x]);
+    const R cp = R(1004.), mu = R(M.mu_dry);
+    const R deltap = R(0.001) * pressure, deltaT = R(0.001) * temperature;
+    auto dens = [&](R p, R t) { return p * mu / (R(8.314472e+3) * t); };   // return_density
+    const R drho_dp_T = (dens(pressure + deltap, temperature) - dens(pressure - deltap, temperature)) / (R(2.) * deltap);
+    const R drho_dT_p = (dens(pressure, temperature + deltaT) - dens(pressure, temperature - deltaT)) / (R(2.) * deltaT);
+    const R Drho_Dp = (R(M.rho3[x]) - R(M.rho3[M.at(k - 1, j, i)])) / (R(M.p3[x]) - R(M.p3[M.at(k - 1, j, i)]));
+    const R g = R(M.grav[2 * j + 1]);
+    const R brunt2 = g * g * (Drho_Dp - drho_dp_T + temperature / (cp * density * density) * drho_dT_p * drho_dT_p);
     ri = brunt2 / (dudz2 + dvdz2);
   } else {
-    ri = 1.e+6;
+    ri = R(1.e+6);
   }
   write_with_pads(M.ri2, M, M.at(k, j, 0), i, ri);
 }
 
 // divergence_damping apply step, epic_subgrid.c:1857-1881 (DIV from k_divergence in work2).
+template <class R>
 __global__ void k_divdamp_apply(DevModel M, double nudiv) {
   const long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
   const long long per = (long long)(M.nk - 1) * (M.nj + 1) * M.ni;
@@ -569,11 +615,13 @@ __global__ void k_divdamp_apply(DevModel M, double nudiv) {
   const double *DIV = M.work2;
   const long long off = plane_offset(M, PL_UV_TEND);
   if (!isv) {
-    const double coef = (M.lat[2 * j + 1] > M.lat0) ? nudiv * M.m0 : nudiv * M.m[2 * j + 1];
-    M.dudt[off + M.at(k, j, i)] += coef * (DIV[M.at(k, j, i)] - DIV[M.at(k, j, i - 1)]);
+    const R coef = R((M.lat[2 * j + 1] > M.lat0) ? nudiv * M.m0 : nudiv * M.m[2 * j + 1]);
+    const long long x = off + M.at(k, j, i);
+    M.dudt[x] = M.dudt[x] + (double)(coef * (R(DIV[M.at(k, j, i)]) - R(DIV[M.at(k, j, i - 1)])));
   } else if (j >= 1) {
-    const double coef = nudiv * M.n[2 * j];
-    M.dvdt[off + M.at(k, j, i)] += coef * (DIV[M.at(k, j, i)] - DIV[M.at(k, j - 1, i)]);
+    const R coef = R(nudiv * M.n[2 * j]);
+    const long long x = off + M.at(k, j, i);
+    M.dvdt[x] = M.dvdt[x] + (double)(coef * (R(DIV[M.at(k, j, i)]) - R(DIV[M.at(k, j - 1, i)])));
   }
 }
 
@@ -666,10 +714,10 @@ int launch_zero_tend(const DevModel &M, cudaStream_t s) {
 }
 
 int launch_uv_core(const DevModel &M, cudaStream_t s) {
-  k_uv_kin<<<cells_blocks(M, M.nk - 1, M.nj + 1, 128), 128, 0, s>>>(M);
-  k_uv_core_v<<<cells_blocks(M, M.nk - 1, M.nj, 128), 128, 0, s>>>(M);
-  launch_filter_planes(M, M.work0, PL_NONE, M.work0, 1, M.nk - 1, 0, s);
-  k_uv_core_u<<<cells_blocks(M, M.nk - 1, M.nj + 1, 128), 128, 0, s>>>(M);
+  EPIC_LAUNCH_R(M.mixed, k_uv_kin, cells_blocks(M, M.nk - 1, M.nj + 1, 128), 128, 0, s, M);
+  EPIC_LAUNCH_R(M.mixed, k_uv_core_v, cells_blocks(M, M.nk - 1, M.nj, 128), 128, 0, s, M);
+  launch_filter_planes(M, M.work0, PL_NONE, M.work0, 1, M.nk - 1, 0, s, M.mixed);
+  EPIC_LAUNCH_R(M.mixed, k_uv_core_u, cells_blocks(M, M.nk - 1, M.nj + 1, 128), 128, 0, s, M);
   return 0;
 }
 
@@ -683,10 +731,10 @@ int launch_uv_pgrad(const DevModel &M, cudaStream_t s) {
 int launch_hsu_meridional(const DevModel &M, double *buff, int kind, cudaStream_t s) {
   const int k0 = kind == 1 ? M.k_sigma - 1 : 1;
   const int nkk = M.nk - k0 + 1;
-  k_hsu_merid_pred<<<cells_blocks(M, nkk, M.nj + 2, 128), 128, 0, s>>>(M, buff, kind, k0);
-  k_hsu_merid_apred<<<cells_blocks(M, nkk, M.nj + 1, 128), 128, 0, s>>>(M, buff, k0);
-  k_hsu_merid_corr<<<cells_blocks(M, nkk, M.nj + 2, 128), 128, 0, s>>>(M, buff, kind, k0);
-  k_hsu_merid_update<<<cells_blocks(M, nkk, M.nj + 1, 128), 128, 0, s>>>(M, buff, k0);
+  EPIC_LAUNCH_R(M.mixed, k_hsu_merid_pred, cells_blocks(M, nkk, M.nj + 2, 128), 128, 0, s, M, buff, kind, k0);
+  EPIC_LAUNCH_R(M.mixed, k_hsu_merid_apred, cells_blocks(M, nkk, M.nj + 1, 128), 128, 0, s, M, buff, k0);
+  EPIC_LAUNCH_R(M.mixed, k_hsu_merid_corr, cells_blocks(M, nkk, M.nj + 2, 128), 128, 0, s, M, buff, kind, k0);
+  EPIC_LAUNCH_R(M.mixed, k_hsu_merid_update, cells_blocks(M, nkk, M.nj + 1, 128), 128, 0, s, M, buff, k0);
   return 0;
 }
 
@@ -715,11 +763,11 @@ int launch_meridional_hyperviscosity(const DevModel &M, int index, double *var, 
   double sign = 1.;
   for (int itmp = 2; itmp <= 8; itmp += 2) {
     double *dst = bufs[which];
-    k_d2dy2<<<cells_blocks(M, nkk, nrows, 128), 128, 0, s>>>(M, cur_src, src_sel, dst, vgrid, M.coef[itmp], k0, nkk);
+    EPIC_LAUNCH_R(M.mixed, k_d2dy2, cells_blocks(M, nkk, nrows, 128), 128, 0, s, M, cur_src, src_sel, dst, vgrid, M.coef[itmp], k0, nkk);
     src_sel = PL_NONE;
     if (M.nu[itmp] > 0.) {
-      launch_filter_planes(M, dst, PL_NONE, dst, k0, nkk, vgrid, s);
-      k_visc_apply<<<cells_blocks(M, nkk, vgrid ? M.nj : M.nj + 1, 128), 128, 0, s>>>(M, var, sel, dst, vgrid, sign, k0, nkk);
+      launch_filter_planes(M, dst, PL_NONE, dst, k0, nkk, vgrid, s, M.mixed);
+      EPIC_LAUNCH_R(M.mixed, k_visc_apply, cells_blocks(M, nkk, vgrid ? M.nj : M.nj + 1, 128), 128, 0, s, M, var, sel, dst, vgrid, sign, k0, nkk);
     }
     sign = -sign;
     double rest = 0.;
@@ -737,16 +785,16 @@ int launch_zonal_hyperviscosity(const DevModel &M, int index, double *var, int s
   visc_krange(M, index, k0, k1);
   const int jbot = index == 1 ? 1 : 0, jhalf = index == 1 ? 0 : 1;
   dim3 grid(M.nj - jbot + 1, k1 - k0 + 1);
-  const size_t smem = 3 * (size_t)(M.ni + 2) * sizeof(double);
-  k_zonal_visc<<<grid, M.ni >= 256 ? 128 : 64, smem, s>>>(M, var, sel, jbot, jhalf, k0);
+  const size_t smem = (size_t)(M.ni + 2) * (sizeof(double) + 2 * (M.mixed ? sizeof(float) : sizeof(double)));
+  EPIC_LAUNCH_R(M.mixed, k_zonal_visc, grid, M.ni >= 256 ? 128 : 64, smem, s, M, var, sel, jbot, jhalf, k0);
   return 0;
 }
 
 int launch_divergence_damping(const DevModel &M, cudaStream_t s) {
   if (M.nudiv == 0.) return 0;
-  launch_filter_planes(M, M.u, PL_UV_DIS, M.work1, 1, M.nk - 1, 0, s);
-  k_divergence<<<cells_blocks(M, M.nk - 1, M.nj + 1, 128), 128, 0, s>>>(M, M.work1, M.v, PL_UV_DIS, M.work2, 1, M.nk - 1);
-  k_divdamp_apply<<<epic_blocks(2LL * (M.nk - 1) * (M.nj + 1) * M.ni, 128), 128, 0, s>>>(M, M.nudiv);
+  launch_filter_planes(M, M.u, PL_UV_DIS, M.work1, 1, M.nk - 1, 0, s, M.mixed);
+  EPIC_LAUNCH_R(M.mixed, k_divergence, cells_blocks(M, M.nk - 1, M.nj + 1, 128), 128, 0, s, M, M.work1, M.v, PL_UV_DIS, M.work2, 1, M.nk - 1);
+  EPIC_LAUNCH_R(M.mixed, k_divdamp_apply, epic_blocks(2LL * (M.nk - 1) * (M.nj + 1) * M.ni, 128), 128, 0, s, M, M.nudiv);
   return 0;
 }
 
@@ -759,13 +807,13 @@ int launch_uv_update(const DevModel &M, cudaStream_t s) {
 
 int launch_store_diag(const DevModel &M, cudaStream_t s) {
   // PV3: filtered copy of V (v rows), then the interior and polar values.
-  launch_filter_planes(M, M.v, PL_UV, M.work1, 0, M.nk + 1, 1, s);
-  k_pv_interior<<<cells_blocks(M, M.nk + 1, M.nj, 128), 128, 0, s>>>(M, M.work1);
+  launch_filter_planes(M, M.v, PL_UV, M.work1, 0, M.nk + 1, 1, s, M.mixed);
+  EPIC_LAUNCH_R(M.mixed, k_pv_interior, cells_blocks(M, M.nk + 1, M.nj, 128), 128, 0, s, M, M.work1);
   k_pv_poles<<<M.nk + 1, 128, 0, s>>>(M);
   // DIV_UV3 from a filtered copy of U.
-  launch_filter_planes(M, M.u, PL_UV, M.work2, 0, M.nk + 1, 0, s);
-  k_divergence<<<cells_blocks(M, M.nk + 1, M.nj + 1, 128), 128, 0, s>>>(M, M.work2, M.v, PL_UV, M.div_uv3, 0, M.nk + 1);
-  k_ri2<<<cells_blocks(M, M.nk, M.nj + 1, 128), 128, 0, s>>>(M);
+  launch_filter_planes(M, M.u, PL_UV, M.work2, 0, M.nk + 1, 0, s, M.mixed);
+  EPIC_LAUNCH_R(M.mixed, k_divergence, cells_blocks(M, M.nk + 1, M.nj + 1, 128), 128, 0, s, M, M.work2, M.v, PL_UV, M.div_uv3, 0, M.nk + 1);
+  EPIC_LAUNCH_R(M.mixed, k_ri2, cells_blocks(M, M.nk, M.nj + 1, 128), 128, 0, s, M);
   return 0;
 }
 

@@ -19,8 +19,17 @@ __device__ __forceinline__ long long plane_offset(const DevModel &M, int sel) {
   }
 }
 
-// k_filter.cu -- zonal filter (epic_adjust.c) and the zonal pass of hsu_advection
-int launch_filter_planes(const DevModel &M, const double *src, int src_sel, double *dst, int k0, int nplanes, int vgrid, cudaStream_t s);
+// Launch the FP32 (mixed form) or FP64 instantiation of a kernel template.
+#define EPIC_LAUNCH_R(mixed, kern, grid, block, smem, stream, ...)                 \
+  do {                                                                             \
+    if (mixed) kern<float><<<(grid), (block), (smem), (stream)>>>(__VA_ARGS__);    \
+    else kern<double><<<(grid), (block), (smem), (stream)>>>(__VA_ARGS__);        \
+  } while (0)
+
+// k_filter.cu -- zonal filter (epic_adjust.c) and the zonal pass of hsu_advection.
+// fp32: filter in FP32 (mixed form; the filtered GZ copy always stays FP64).
+int launch_filter_planes(const DevModel &M, const double *src, int src_sel, double *dst, int k0, int nplanes, int vgrid, cudaStream_t s,
+                         int fp32 = 0);
 int launch_varz_filter(const DevModel &M, double *buff, int sel, int index, int kstart, int kend, cudaStream_t s);
 int launch_hsu_zonal(const DevModel &M, double *buff, int kind, int kstart, cudaStream_t s);
 int filter_kernels_init(int ni);

@@ -1,0 +1,82 @@
+"""The mixed-precision form (EPIC_PREC_MIXED) against the FP64 form on the GPU.
+
+Mixed form: stencils, advection, hyperviscosity, the zonal filter and the physics evaluate in
+FP32; the hydrostatic sums (P3, GZ3, SUM_DIV), the row means, every update of a stored field
+and the Adams-Bashforth/leapfrog step stay FP64 (the state is stored in FP64).
+
+Stated error (relative L2 per field, mixed vs FP64), measured on a GB300:
+  * one simulated day (288 steps of 300 s) at 64x32x10 from a state spun up for 10 days:
+    U 3.5e-5, V 3.6e-4, HDRY 2.6e-7, THETA 3.7e-8;
+  * one simulated day from rest: U 2.1e-4, V 5.0e-4 (the first days are driven by horizontal
+    pressure differences 1e-5 of the geopotential, so FP32 rounding is amplified ~1e4 in U, V).
+The bounds below leave a factor ~3 over those figures.
+"""
+import numpy as np
+import pytest
+
+from compare import PROGNOSTIC, field_errors
+from epic_gb300 import EPIC_PREC_FP64, EPIC_PREC_MIXED, EPIC_SYNC_DIAGS_ONLY, HSConfig, Model, hs_setup
+
+pytestmark = pytest.mark.gpu
+DAY = 288   # steps of 300 s
+
+
+@pytest.fixture(scope="module")
+def spun_up(gpu):
+    ga, f = hs_setup(HSConfig(ni=64, nj=32, nk=10, dt=300, seed=0))
+    m = Model(ga, EPIC_PREC_FP64)
+    m.upload(f)
+    m.timestep(EPIC_SYNC_DIAGS_ONLY)
+    m.run(10 * DAY)
+    m.sync()
+    return ga, m.download()
+
+
+def _pair(ga, f, prime):
+    a, b = Model(ga, EPIC_PREC_FP64), Model(ga, EPIC_PREC_MIXED)
+    for m in (a, b):
+        m.upload(f)
+        if prime:
+            m.timestep(EPIC_SYNC_DIAGS_ONLY)
+    return a, b
+
+
+def _run(a, b, n):
+    a.run(n)
+    b.run(n)
+    a.sync()
+    b.sync()
+    return field_errors(b.download(), a.download(), PROGNOSTIC)
+
+
+def test_mixed_one_day_after_spin_up(spun_up):
+    ga, f = spun_up
+    a, b = _pair(ga, f, prime=False)
+    e = _run(a, b, DAY)
+    bounds = {"u": 1e-4, "v": 1e-3, "hdry": 1e-6, "theta": 1e-7}
+    assert all(e[k][0] <= bounds[k] for k in bounds), e
+
+
+def test_mixed_one_day_from_rest(gpu):
+    ga, f = hs_setup(HSConfig(ni=64, nj=32, nk=10, dt=300, seed=0))
+    a, b = _pair(ga, f, prime=True)
+    e = _run(a, b, DAY)
+    bounds = {"u": 1e-3, "v": 2e-3, "hdry": 1e-6, "theta": 1e-7}
+    assert all(e[k][0] <= bounds[k] for k in bounds), e
+
+
+def test_mixed_is_deterministic(gpu):
+    """Two mixed runs (graph replay and single steps) give identical bits."""
+    ga, f = hs_setup(HSConfig(ni=32, nj=16, nk=10, dt=300, seed=4))
+    m1, m2 = Model(ga, EPIC_PREC_MIXED), Model(ga, EPIC_PREC_MIXED)
+    for m in (m1, m2):
+        m.upload(f)
+        m.timestep(EPIC_SYNC_DIAGS_ONLY)
+    m1.run(6)
+    for _ in range(6):
+        m2.run(1)
+    m1.sync()
+    m2.sync()
+    a, b = m1.download(), m2.download()
+    for k in a.arrays:
+        assert np.array_equal(a.arrays[k], b.arrays[k]), k
