@@ -57,6 +57,16 @@ def load_library(path: str | None = None) -> C.CDLL:
     lib.epic_model_device_bytes.argtypes = [C.c_void_p]
     lib.epic_model_device_bytes.restype = C.c_int64
     lib.epic_model_filter_mass_noalloc.argtypes = [C.c_void_p]
+    lib.epic_batch_create.argtypes = [C.POINTER(C.c_void_p), C.c_int32, C.POINTER(C.c_void_p)]
+    lib.epic_batch_destroy.argtypes = [C.c_void_p]
+    lib.epic_batch_destroy.restype = None
+    for name in ("epic_batch_timestep", "epic_batch_run"):
+        getattr(lib, name).argtypes = [C.c_void_p, C.c_int32]
+    lib.epic_batch_sync.argtypes = [C.c_void_p]
+    lib.epic_batch_stream.argtypes = [C.c_void_p]
+    lib.epic_batch_stream.restype = C.c_void_p
+    lib.epic_batch_kernels_per_step.argtypes = [C.c_void_p]
+    lib.epic_batch_kernels_per_step.restype = C.c_int32
     lib.epic_hs_grid_build.argtypes = [C.POINTER(EpicHsParams), C.POINTER(EpicGrid), C.POINTER(C.c_double),
                                        C.POINTER(C.c_double)]
     lib.epic_hs_initial_state.argtypes = [C.POINTER(EpicGrid), C.POINTER(EpicHsParams), C.c_uint64, C.c_double,
@@ -148,6 +158,47 @@ class Model:
         return int(self.lib.epic_model_device_bytes(self._h))
 
 
-__all__ = ["Model", "hs_setup", "load_library", "EpicError", "HSConfig", "Fields", "GridArrays", "Layout",
+class Batch:
+    """Several Models of one shape class stepped together: each kernel of the step is launched
+    once for all members (epic_batch_* in include/epic_gb300.h).  Upload to and download from
+    the member Models; call sync() first."""
+
+    def __init__(self, models: list[Model]):
+        self.lib = load_library()
+        self.models = list(models)
+        arr = (C.c_void_p * len(self.models))(*[m._h.value for m in self.models])
+        self._h = C.c_void_p()
+        _check(self.lib.epic_batch_create(arr, len(self.models), C.byref(self._h)), "epic_batch_create")
+
+    def close(self) -> None:
+        if self._h:
+            self.lib.epic_batch_destroy(self._h)
+            self._h = C.c_void_p()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def timestep(self, action: int = EPIC_STEP_PROGS_AND_SYNC_DIAGS) -> None:
+        _check(self.lib.epic_batch_timestep(self._h, action), "epic_batch_timestep")
+
+    def run(self, nsteps: int) -> None:
+        _check(self.lib.epic_batch_run(self._h, nsteps), "epic_batch_run")
+
+    def sync(self) -> None:
+        _check(self.lib.epic_batch_sync(self._h), "epic_batch_sync")
+
+    @property
+    def stream(self) -> int:
+        return self.lib.epic_batch_stream(self._h) or 0
+
+    @property
+    def kernels_per_step(self) -> int:
+        return int(self.lib.epic_batch_kernels_per_step(self._h))
+
+
+__all__ = ["Model", "Batch", "hs_setup", "load_library", "EpicError", "HSConfig", "Fields", "GridArrays", "Layout",
            "EPIC_PREC_FP64", "EPIC_PREC_MIXED", "EPIC_STEP_PROGS_AND_SYNC_DIAGS", "EPIC_SYNC_DIAGS_ONLY",
            "EPIC_UV_AB3", "EPIC_UV_LEAPFROG", "LIB_PATH", "np"]

@@ -55,12 +55,29 @@ struct DevModel {
   // scratch
   double *gz, *unity, *old, *work0, *work1, *work2, *work3, *ptable;
   Ctl *ctl;
+  // batch: the members' descriptions on the device (nullptr for a single model); kernels
+  // launched over a batch take member blockIdx.z's description on entry (EPIC_MEMBER)
+  const DevModel *batch;
+  int nbatch;
+  char *pool_base;   // start of the model's device pool (state, scratch and tables)
 
   __host__ __device__ __forceinline__ long long at(int k, int j, int i) const {
     return (long long)i + (long long)(j + 1) * iadim + (long long)k * n2;
   }
   __host__ __device__ __forceinline__ long long at2(int j, int i) const { return (long long)i + (long long)(j + 1) * iadim; }
 };
+
+// Entry of every kernel: in a batch launch, take member blockIdx.z's description and move the
+// state pointers passed as arguments (addresses in the launch description's pool) to the same
+// offsets in the member's pool (members of a batch share the pool layout).
+template <class... P>
+__device__ __forceinline__ void epic_member(DevModel &M, P *&...ptrs) {
+  if (!M.batch) return;
+  const char *from = M.pool_base;
+  M = M.batch[blockIdx.z];
+  const char *to = M.pool_base;
+  ((ptrs = ptrs ? (P *)(to + ((const char *)ptrs - from)) : ptrs), ...);
+}
 
 // ---- pointwise helpers: restatements of the reference routines named beside each ----
 

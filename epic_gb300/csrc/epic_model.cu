@@ -5,6 +5,7 @@
 #include <cstdlib>
 #include <cstring>
 #include <mutex>
+#include <string>
 #include <vector>
 #include "device_common.cuh"
 #include "kernels.h"
@@ -127,10 +128,9 @@ int check_launch(const char *what) {
   return EPIC_OK;
 }
 
-// One reference-function stage of the step, in the reference's call order.
-int run_stage(epic_model *m, int stage) {
-  DevModel &M = m->d;
-  cudaStream_t s = m->stream;
+// One reference-function stage of the step, in the reference's call order, for a model or
+// (M.batch set) for every member of a batch.
+int run_stage_on(const DevModel &M, cudaStream_t s, int stage) {
   using namespace epic;
   switch (stage) {
     case 0: launch_zero_tend(M, s); break;
@@ -163,7 +163,7 @@ int run_stage(epic_model *m, int stage) {
       break;
     case 7: launch_store_pgrad_vars(M, s); break;
     case 8:
-      cudaMemcpyAsync(M.gz, M.gz3, M.n3 * sizeof(double), cudaMemcpyDeviceToDevice, s);
+      launch_copy_gz(M, s);
       launch_filter_planes(M, M.gz, PL_NONE, M.gz, 0, M.nk, 0, s);
       launch_gz_monotone(M, s);
       break;
@@ -194,22 +194,56 @@ int run_stage(epic_model *m, int stage) {
   return check_launch("stage launch");
 }
 
-int enqueue_step(epic_model *m) {
+int run_stage(epic_model *m, int stage) { return run_stage_on(m->d, m->stream, stage); }
+
+int enqueue_step_on(const DevModel &M, cudaStream_t s) {
   static const int step[] = {0, 1, 2, 3, 4, 5, 6, 7, 8, 9, 10, 11, 7, 12, 13, 14, 15, 16, 17};
   for (int st : step) {
-    int rc = run_stage(m, st);
+    int rc = run_stage_on(M, s, st);
     if (rc) return rc;
   }
   return EPIC_OK;
 }
 
-int enqueue_sync(epic_model *m) {
+int enqueue_sync_on(const DevModel &M, cudaStream_t s) {
   static const int sync[] = {11, 7, 16, 17, 2};
   for (int st : sync) {
-    int rc = run_stage(m, st);
+    int rc = run_stage_on(M, s, st);
     if (rc) return rc;
   }
   return EPIC_OK;
+}
+
+int enqueue_step(epic_model *m) { return enqueue_step_on(m->d, m->stream); }
+int enqueue_sync(epic_model *m) { return enqueue_sync_on(m->d, m->stream); }
+
+// Capture one step (and the step counter) on stream s into an executable graph; counts its
+// kernel nodes.  Returns nullptr if capture is not possible.
+cudaGraphExec_t capture_step(const DevModel &M, cudaStream_t s, int *kernels) {
+  cudaGraph_t graph = nullptr;
+  cudaGraphExec_t exec = nullptr;
+  if (cudaStreamBeginCapture(s, cudaStreamCaptureModeThreadLocal) == cudaSuccess) {
+    int rc = enqueue_step_on(M, s);
+    if (!rc) rc = epic::launch_itime_advance(M, s);
+    cudaError_t e = cudaStreamEndCapture(s, &graph);
+    if (rc == EPIC_OK && e == cudaSuccess && graph) {
+      size_t nn = 0;
+      if (cudaGraphGetNodes(graph, nullptr, &nn) == cudaSuccess && nn > 0) {
+        std::vector<cudaGraphNode_t> nodes(nn);
+        cudaGraphGetNodes(graph, nodes.data(), &nn);
+        int nk = 0;
+        for (auto nd : nodes) {
+          cudaGraphNodeType t;
+          if (cudaGraphNodeGetType(nd, &t) == cudaSuccess && t == cudaGraphNodeTypeKernel) nk++;
+        }
+        *kernels = nk;
+      }
+      if (cudaGraphInstantiate(&exec, graph, 0) != cudaSuccess) exec = nullptr;
+    }
+    if (graph) cudaGraphDestroy(graph);
+  }
+  cudaGetLastError();
+  return exec;
 }
 
 int read_ctl(epic_model *m, Ctl &c) {
@@ -302,6 +336,7 @@ extern "C" int epic_model_create(const epic_grid *g, int32_t precision, epic_mod
   m->pool_bytes = bytes;
   cudaMemsetAsync(m->pool, 0, bytes, m->stream);
   char *p = m->pool;
+  d.pool_base = m->pool;
   d.ctl = carve<Ctl>(p, 1);
   d.u = carve<double>(p, d.nvp * n3); d.v = carve<double>(p, d.nvp * n3);
   d.dudt = carve<double>(p, d.ntp * n3); d.dvdt = carve<double>(p, d.ntp * n3);
@@ -429,28 +464,7 @@ extern "C" int epic_model_run(epic_model *m, int32_t nsteps) {
   if (!m->uploaded) return set_error(EPIC_ERR_STATE, "run before upload");
   if (nsteps <= 0) return EPIC_OK;
   if (!m->run_graph && !m->graph_failed) {
-    cudaGraph_t graph = nullptr;
-    if (cudaStreamBeginCapture(m->stream, cudaStreamCaptureModeThreadLocal) == cudaSuccess) {
-      int rc = enqueue_step(m);
-      if (!rc) rc = epic::launch_itime_advance(m->d, m->stream);
-      cudaError_t e = cudaStreamEndCapture(m->stream, &graph);
-      if (rc == EPIC_OK && e == cudaSuccess && graph) {
-        size_t nn = 0;
-        if (cudaGraphGetNodes(graph, nullptr, &nn) == cudaSuccess && nn > 0) {
-          std::vector<cudaGraphNode_t> nodes(nn);
-          cudaGraphGetNodes(graph, nodes.data(), &nn);
-          int nk = 0;
-          for (auto nd : nodes) {
-            cudaGraphNodeType t;
-            if (cudaGraphNodeGetType(nd, &t) == cudaSuccess && t == cudaGraphNodeTypeKernel) nk++;
-          }
-          m->kernels_per_step = nk;
-        }
-        if (cudaGraphInstantiate(&m->run_graph, graph, 0) != cudaSuccess) m->run_graph = nullptr;
-      }
-      if (graph) cudaGraphDestroy(graph);
-    }
-    cudaGetLastError();
+    m->run_graph = capture_step(m->d, m->stream, &m->kernels_per_step);
     if (!m->run_graph) m->graph_failed = true;
   }
   for (int s = 0; s < nsteps; s++) {
@@ -575,3 +589,138 @@ extern "C" int epic_model_filter_mass_noalloc(epic_model *m) {
   if (dev != cur) cudaSetDevice(cur);
   return rc;
 }
+
+// ---- batches: one launch per kernel for every member of a shape class ----
+//
+// A batch is a view over models created by epic_model_create that share every launch-shaping
+// parameter (sizes, scheme, precision form, k_sigma, dt, viscosities); members may differ in
+// their state and in the Held-Suarez drag rate k_f.  The members' descriptions live in one
+// device array; each kernel of the step is launched once with gridDim.z = members and takes
+// member blockIdx.z's description on entry, so a 64-member ensemble costs the launches of one
+// model.  Member state stays in each member's own device memory: upload and download go
+// through the member models, after epic_batch_sync.
+
+struct epic_batch {
+  std::vector<epic_model *> members;
+  DevModel d;                       // launch description: member 0's, with batch/nbatch set
+  DevModel *dev_members = nullptr;
+  cudaStream_t stream = nullptr;
+  cudaGraphExec_t run_graph = nullptr;
+  bool graph_failed = false;
+  int kernels_per_step = -1;
+};
+
+namespace {
+
+bool same_launch_shape(const DevModel &a, const DevModel &b) {
+  if (a.ni != b.ni || a.nj != b.nj || a.nk != b.nk || a.uv_scheme != b.uv_scheme || a.mixed != b.mixed ||
+      a.k_sigma != b.k_sigma || a.k_sponge != b.k_sponge || a.newt_cool_on != b.newt_cool_on || a.dt != b.dt ||
+      a.nudiv != b.nudiv || a.lat0 != b.lat0)
+    return false;
+  for (int i = 0; i < 9; i++)
+    if (a.coef[i] != b.coef[i] || a.nu[i] != b.nu[i]) return false;
+  return true;
+}
+
+}  // namespace
+
+extern "C" int epic_batch_create(epic_model *const *members, int32_t n, epic_batch **out) {
+  if (!members || !out || n < 1) return set_error(EPIC_ERR_ARG, "epic_batch_create: bad arguments");
+  *out = nullptr;
+  for (int i = 0; i < n; i++) {
+    if (!members[i]) return set_error(EPIC_ERR_ARG, "epic_batch_create: member %d is NULL", i);
+    if (!same_launch_shape(members[0]->d, members[i]->d))
+      return set_error(EPIC_ERR_ARG, "epic_batch_create: member %d differs from member 0 in size, scheme, precision or viscosity", i);
+    for (int q = 0; q < i; q++)
+      if (members[q] == members[i]) return set_error(EPIC_ERR_ARG, "epic_batch_create: member %d repeats member %d", i, q);
+  }
+  epic_batch *b = new epic_batch();
+  b->members.assign(members, members + n);
+  cudaError_t e = cudaStreamCreateWithFlags(&b->stream, cudaStreamNonBlocking);
+  if (e == cudaSuccess) e = cudaMalloc(&b->dev_members, sizeof(DevModel) * (size_t)n);
+  if (e != cudaSuccess) {
+    epic_batch_destroy(b);
+    return set_error(EPIC_ERR_NOMEM, "epic_batch_create: %s", cudaGetErrorString(e));
+  }
+  std::vector<DevModel> host(n);
+  for (int i = 0; i < n; i++) host[i] = members[i]->d;
+  e = cudaMemcpy(b->dev_members, host.data(), sizeof(DevModel) * (size_t)n, cudaMemcpyHostToDevice);
+  if (e != cudaSuccess) {
+    epic_batch_destroy(b);
+    return set_error(EPIC_ERR_CUDA, "epic_batch_create: %s", cudaGetErrorString(e));
+  }
+  b->d = members[0]->d;
+  b->d.batch = b->dev_members;
+  b->d.nbatch = n;
+  *out = b;
+  return EPIC_OK;
+}
+
+extern "C" void epic_batch_destroy(epic_batch *b) {
+  if (!b) return;
+  if (b->run_graph) cudaGraphExecDestroy(b->run_graph);
+  if (b->stream) cudaStreamSynchronize(b->stream);
+  if (b->dev_members) cudaFree(b->dev_members);
+  if (b->stream) cudaStreamDestroy(b->stream);
+  delete b;
+}
+
+static int batch_ready(epic_batch *b, const char *what) {
+  if (!b) return set_error(EPIC_ERR_ARG, "%s: NULL batch", what);
+  for (size_t i = 0; i < b->members.size(); i++)
+    if (!b->members[i]->uploaded) return set_error(EPIC_ERR_STATE, "%s: member %zu has no state", what, i);
+  // members' own streams may hold uploads; the batch runs after them
+  for (auto *m : b->members) EPIC_CUDA_CHECK(cudaStreamSynchronize(m->stream));
+  return EPIC_OK;
+}
+
+extern "C" int epic_batch_timestep(epic_batch *b, int32_t action) {
+  int rc = batch_ready(b, "epic_batch_timestep");
+  if (rc) return rc;
+  if (action == EPIC_STEP_PROGS_AND_SYNC_DIAGS) rc = enqueue_step_on(b->d, b->stream);
+  else if (action == EPIC_SYNC_DIAGS_ONLY) rc = enqueue_sync_on(b->d, b->stream);
+  else return set_error(EPIC_ERR_ARG, "unrecognized action=%d", action);
+  if (rc) return rc;
+  return check_launch("epic_batch_timestep");
+}
+
+extern "C" int epic_batch_run(epic_batch *b, int32_t nsteps) {
+  int rc = batch_ready(b, "epic_batch_run");
+  if (rc) return rc;
+  if (nsteps <= 0) return EPIC_OK;
+  if (!b->run_graph && !b->graph_failed) {
+    b->run_graph = capture_step(b->d, b->stream, &b->kernels_per_step);
+    if (!b->run_graph) b->graph_failed = true;
+  }
+  for (int s = 0; s < nsteps; s++) {
+    if (b->run_graph) {
+      EPIC_CUDA_CHECK(cudaGraphLaunch(b->run_graph, b->stream));
+    } else {
+      rc = enqueue_step_on(b->d, b->stream);
+      if (rc) return rc;
+      epic::launch_itime_advance(b->d, b->stream);
+    }
+  }
+  return check_launch("epic_batch_run");
+}
+
+extern "C" int epic_batch_sync(epic_batch *b) {
+  if (!b) return set_error(EPIC_ERR_ARG, "epic_batch_sync: NULL batch");
+  EPIC_CUDA_CHECK(cudaStreamSynchronize(b->stream));
+  for (size_t i = 0; i < b->members.size(); i++) {
+    Ctl c;
+    int rc = read_ctl(b->members[i], c);
+    if (rc) return rc;
+    rc = model_error(c);
+    if (rc) {
+      const std::string msg = epic::error_buffer();
+      return set_error(EPIC_ERR_MODEL, "member %zu: %s", i, msg.c_str());
+    }
+  }
+  return EPIC_OK;
+}
+
+extern "C" void *epic_batch_stream(epic_batch *b) { return b ? (void *)b->stream : nullptr; }
+
+extern "C" int32_t epic_batch_kernels_per_step(const epic_batch *b) { return b ? b->kernels_per_step : -1; }
+

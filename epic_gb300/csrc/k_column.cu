@@ -19,6 +19,7 @@ __device__ __forceinline__ bool col_index(const DevModel &M, int &j, int &i) {
 
 // source_sink: THETA += dt*HEAT3/EXNER3 for k >= k_sigma-1, epic_funcs_diag.c:4768-4778
 __global__ void k_source_sink(DevModel M) {
+  epic_member(M);
   int j, i;
   if (!col_index(M, j, i)) return;
   for (int k = M.k_sigma - 1; k <= M.nk; k++) {
@@ -89,6 +90,7 @@ __device__ __forceinline__ R sigmatheta_lp(const DevModel &M, R theta, R p, R pb
 // the dF/dp difference step is cbrt(FLT_EPSILON) relative instead of cbrt(DBL_EPSILON).
 template <class R>
 __global__ void __launch_bounds__(CT_THREADS) k_calc_w(DevModel M) {
+  epic_member(M);
   extern __shared__ __align__(16) unsigned char smraw[];
   R *sm = reinterpret_cast<R *>(smraw);
   __shared__ R s_lp[32];
@@ -159,6 +161,7 @@ __global__ void __launch_bounds__(CT_THREADS) k_calc_w(DevModel M) {
 // Columns on the u grid (j = 0..nj) and v grid (j = 1..nj), i = 1..ni.
 template <class R>
 __global__ void k_uv_drag(DevModel M) {
+  epic_member(M);
   const int t = (int)(blockIdx.x * blockDim.x + threadIdx.x);
   const int ni = M.ni, nk = M.nk;
   const int nu = (M.nj + 1) * ni;
@@ -194,6 +197,7 @@ __global__ void k_uv_drag(DevModel M) {
 // 1 = THETA, 2 = HDRY.  One thread per column j = 0..nj, i = 0..ni+1.
 template <class R>
 __global__ void k_hsu_vertical(DevModel M, double *buff, int kind) {
+  epic_member(M, buff);
   int j, i;
   if (!col_index(M, j, i)) return;
   const int nk = M.nk;
@@ -290,6 +294,7 @@ __global__ void k_hsu_vertical(DevModel M, double *buff, int kind) {
 
 // restore_mass(HDRY_INDEX), epic_adjust.c:45-96
 __global__ void k_restore_mass(DevModel M) {
+  epic_member(M);
   int j, i;
   if (!col_index(M, j, i)) return;
   for (int k = 1; k <= M.nk; k++) {
@@ -302,6 +307,7 @@ __global__ void k_restore_mass(DevModel M) {
 // Shared arrays: P (interface pressure), HL (get_h at the layers), TH (THETA), PP (P^(kappa+1),
 // each interface's power computed once for the two layers that share it).
 __global__ void __launch_bounds__(CT_THREADS) k_set_p2etc(DevModel M, int update_theta) {
+  epic_member(M);
   extern __shared__ double sm[];
   __shared__ double s_lp[32];
   const ColTile c = col_tile(M);
@@ -408,6 +414,7 @@ __global__ void __launch_bounds__(CT_THREADS) k_set_p2etc(DevModel M, int update
 // the first DZDT3 terms.  Shared arrays: P, R (RHO3), T3, LG (log of successive pressure
 // ratios), GZ (the Leslie-Purser increments, then the running sum in place).
 __global__ void __launch_bounds__(CT_THREADS) k_pgrad_vars_column(DevModel M) {
+  epic_member(M);
   extern __shared__ double sm[];
   __shared__ double s_rho2_1[32];
   const ColTile c = col_tile(M);
@@ -518,6 +525,7 @@ __device__ __forceinline__ double layer_p_mixed(const DevModel &M, double top, d
 }
 
 __global__ void __launch_bounds__(CT_THREADS) k_set_p2etc_mixed(DevModel M, int update_theta) {
+  epic_member(M);
   extern __shared__ double sm[];
   __shared__ double s_lp[32];
   const ColTile c = col_tile(M);
@@ -614,6 +622,7 @@ __global__ void __launch_bounds__(CT_THREADS) k_set_p2etc_mixed(DevModel M, int 
 }
 
 __global__ void __launch_bounds__(CT_THREADS) k_pgrad_vars_column_mixed(DevModel M) {
+  epic_member(M);
   extern __shared__ double sm[];
   __shared__ double s_rho2_1[32];
   const ColTile c = col_tile(M);
@@ -704,6 +713,7 @@ __global__ void __launch_bounds__(CT_THREADS) k_pgrad_vars_column_mixed(DevModel
 
 // store_pgrad_vars, horizontal part of DZDT3 (epic_funcs_diag.c:3924-3945) plus bc_lateral.
 __global__ void k_pgrad_dzdt(DevModel M) {
+  epic_member(M);
   const int t = (int)(blockIdx.x * blockDim.x + threadIdx.x);
   const int ni = M.ni, nk = M.nk;
   if (t >= nk * (M.nj + 1) * ni) return;
@@ -726,6 +736,7 @@ __global__ void k_pgrad_dzdt(DevModel M) {
 // Monotone fix of the filtered GZ copy, epic_timestep.c:182-195 (the zonal filter of planes
 // 0..nk-1 has already run; each plane's fix only needs the finished plane below it).
 __global__ void k_gz_monotone(DevModel M) {
+  epic_member(M);
   int j, i;
   if (!col_index(M, j, i)) return;
   double below = M.gz[M.at(M.nk, j, i)];
@@ -744,6 +755,7 @@ __global__ void k_gz_monotone(DevModel M) {
 // 0 outside k = 1..nk, j = 0..nj, i = 1..ni, with periodic pads.
 template <class R>
 __global__ void k_calc_heating(DevModel M) {
+  epic_member(M);
   const long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
   if (t >= M.n3) return;
   const int i = (int)(t % M.iadim);
@@ -775,6 +787,7 @@ __global__ void k_calc_heating(DevModel M) {
 // phase 0: UNITY = 1 over k = 0..nk+1, j = 0..nj, all i;  phase 1: OLD = THETA for k >= k_sigma-1;
 // phase 2: THETA -= OLD*(UNITY-1) for k >= k_sigma-1.
 __global__ void k_advection_prep(DevModel M, int phase) {
+  epic_member(M);
   const long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
   const long long w = (long long)(M.nj + 1) * M.iadim;
   if (t >= w * (M.nk + 2)) return;
@@ -791,7 +804,7 @@ __global__ void k_advection_prep(DevModel M, int phase) {
 
 static inline unsigned ncol_blocks(const DevModel &M, int th) { return epic_blocks((long long)(M.nj + 1) * (M.ni + 2), th); }
 
-int launch_source_sink(const DevModel &M, cudaStream_t s) { k_source_sink<<<ncol_blocks(M, 128), 128, 0, s>>>(M); return 0; }
+int launch_source_sink(const DevModel &M, cudaStream_t s) { k_source_sink<<<zg(ncol_blocks(M, 128), M), 128, 0, s>>>(M); return 0; }
 static inline unsigned ntile_blocks(const DevModel &M) { return epic_blocks((long long)(M.nj + 1) * (M.ni + 2), 32); }
 static inline size_t tile_smem(const DevModel &M, int arrays) { return (size_t)arrays * 32 * (M.nk + 1) * sizeof(double); }
 int launch_calc_w(const DevModel &M, cudaStream_t s) {
@@ -807,25 +820,25 @@ int launch_hsu_vertical(const DevModel &M, double *buff, int kind, cudaStream_t 
   EPIC_LAUNCH_R(M.mixed, k_hsu_vertical, ncol_blocks(M, 64), 64, 0, s, M, buff, kind);
   return 0;
 }
-int launch_restore_mass(const DevModel &M, cudaStream_t s) { k_restore_mass<<<ncol_blocks(M, 128), 128, 0, s>>>(M); return 0; }
+int launch_restore_mass(const DevModel &M, cudaStream_t s) { k_restore_mass<<<zg(ncol_blocks(M, 128), M), 128, 0, s>>>(M); return 0; }
 int launch_set_p2etc(const DevModel &M, int update_theta, cudaStream_t s) {
-  if (M.mixed) k_set_p2etc_mixed<<<ntile_blocks(M), CT_THREADS, tile_smem(M, 3), s>>>(M, update_theta);
-  else k_set_p2etc<<<ntile_blocks(M), CT_THREADS, tile_smem(M, 4), s>>>(M, update_theta);
+  if (M.mixed) k_set_p2etc_mixed<<<zg(ntile_blocks(M), M), CT_THREADS, tile_smem(M, 3), s>>>(M, update_theta);
+  else k_set_p2etc<<<zg(ntile_blocks(M), M), CT_THREADS, tile_smem(M, 4), s>>>(M, update_theta);
   return 0;
 }
 int launch_store_pgrad_vars(const DevModel &M, cudaStream_t s) {
-  if (M.mixed) k_pgrad_vars_column_mixed<<<ntile_blocks(M), CT_THREADS, tile_smem(M, 5), s>>>(M);
-  else k_pgrad_vars_column<<<ntile_blocks(M), CT_THREADS, tile_smem(M, 5), s>>>(M);
-  k_pgrad_dzdt<<<epic_blocks((long long)M.nk * (M.nj + 1) * M.ni, 128), 128, 0, s>>>(M);
+  if (M.mixed) k_pgrad_vars_column_mixed<<<zg(ntile_blocks(M), M), CT_THREADS, tile_smem(M, 5), s>>>(M);
+  else k_pgrad_vars_column<<<zg(ntile_blocks(M), M), CT_THREADS, tile_smem(M, 5), s>>>(M);
+  k_pgrad_dzdt<<<zg(epic_blocks((long long)M.nk * (M.nj + 1) * M.ni, 128), M), 128, 0, s>>>(M);
   return 0;
 }
-int launch_gz_monotone(const DevModel &M, cudaStream_t s) { k_gz_monotone<<<ncol_blocks(M, 128), 128, 0, s>>>(M); return 0; }
+int launch_gz_monotone(const DevModel &M, cudaStream_t s) { k_gz_monotone<<<zg(ncol_blocks(M, 128), M), 128, 0, s>>>(M); return 0; }
 int launch_calc_heating(const DevModel &M, cudaStream_t s) {
   EPIC_LAUNCH_R(M.mixed, k_calc_heating, epic_blocks(M.n3, 128), 128, 0, s, M);
   return 0;
 }
 int launch_advection_prep(const DevModel &M, int phase, cudaStream_t s) {
-  k_advection_prep<<<epic_blocks((long long)(M.nj + 1) * M.iadim * (M.nk + 2), 128), 128, 0, s>>>(M, phase);
+  k_advection_prep<<<zg(epic_blocks((long long)(M.nj + 1) * M.iadim * (M.nk + 2), 128), M), 128, 0, s>>>(M, phase);
   return 0;
 }
 

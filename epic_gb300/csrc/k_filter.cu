@@ -173,6 +173,7 @@ __device__ __forceinline__ bool row_is_filtered(const DevModel &M, int j, int vg
 // copied; rows 0..nj+1 get periodic pads (bc_lateral).
 template <class R>
 __global__ void k_filter_planes(DevModel M, const double *src, int src_sel, double *dst, int k0, int vgrid) {
+  epic_member(M, src, dst);
   extern __shared__ __align__(16) unsigned char smraw[];
   R *sm = reinterpret_cast<R *>(smraw);
   src += plane_offset(M, src_sel);
@@ -205,6 +206,7 @@ __global__ void k_filter_planes(DevModel M, const double *src, int src_sel, doub
 // the first column of minimum bottom GZ (the reference's strict-less scan) and fill the table;
 // lane 0 fits the spline.  index: 0 = U, 1 = V, 2 = HDRY (log), 3 = THETA.
 __global__ void k_varz_tables(DevModel M, const double *buff, int sel, int index, int kstart, int kend) {
+  epic_member(M, buff);
   buff += plane_offset(M, sel);
   const int jstart = index == 1 ? 1 : 0;
   const int lane = (int)(threadIdx.x & 31);
@@ -245,6 +247,7 @@ __global__ void k_varz_tables(DevModel M, const double *buff, int sel, int index
 // Block = one row (k = kstart + blockIdx.y, j = jstart + blockIdx.x).
 template <class R>
 __global__ void k_varz_filter_rows(DevModel M, double *buff, int sel, int index, int kstart, int kend) {
+  epic_member(M, buff);
   extern __shared__ __align__(16) unsigned char smraw[];
   R *sm = reinterpret_cast<R *>(smraw);
   buff += plane_offset(M, sel);
@@ -306,6 +309,7 @@ __global__ void k_varz_filter_rows(DevModel M, double *buff, int sel, int index,
 // kind: 0 = interface variable (unity, THETA), 1 = HDRY (layer; u averaged to the layer).
 template <class R>
 __global__ void k_hsu_zonal(DevModel M, double *buff, int kind, int kstart) {
+  epic_member(M, buff);
   extern __shared__ __align__(16) unsigned char smraw[];
   R *sm = reinterpret_cast<R *>(smraw);
   const int ni = M.ni, W = ni + 2;
@@ -397,7 +401,7 @@ int launch_filter_planes(const DevModel &M, const double *src, int src_sel, doub
 int launch_varz_filter(const DevModel &M, double *buff, int sel, int index, int kstart, int kend, cudaStream_t s) {
   const int jstart = index == 1 ? 1 : 0;
   const int nrows = M.nj - jstart + 1;
-  k_varz_tables<<<epic_blocks(32LL * nrows, 128), 128, 0, s>>>(M, buff, sel, index, kstart, kend);
+  k_varz_tables<<<zg(epic_blocks(32LL * nrows, 128), M), 128, 0, s>>>(M, buff, sel, index, kstart, kend);
   const size_t smem = (2 * (size_t)(M.ni + 2) + filter_smem_elems(M.ni)) * relem(M.mixed);
   dim3 grid(nrows, kend - kstart + 1);
   EPIC_LAUNCH_R(M.mixed, k_varz_filter_rows, grid, row_threads(M.ni), smem, s, M, buff, sel, index, kstart, kend);

@@ -24,8 +24,16 @@ static inline unsigned cells_blocks(const DevModel &M, int nkk, int njj, int th)
 }
 __device__ __forceinline__ int wrap_i(const DevModel &M, int i) { return i == 0 ? M.ni : (i == M.ni + 1 ? 1 : i); }
 
+// The copy of GZ3 that the filtered geopotential starts from, epic_timestep.c:176-181.
+__global__ void k_copy_gz(DevModel M) {
+  epic_member(M);
+  const long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (t < M.n3) M.gz[t] = M.gz3[t];
+}
+
 // memset of DUDT, DVDT(it_uv_tend), epic_timestep.c:107-108
 __global__ void k_zero_tend(DevModel M) {
+  epic_member(M);
   const long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
   if (t >= M.n3) return;
   const long long off = plane_offset(M, PL_UV_TEND);
@@ -72,6 +80,7 @@ __device__ __forceinline__ R vh_at(const DevModel &M, const double *Vk, const do
 // Kinetic energy per mass on the h grid, planes k = 1..nk-1, into work0 (with pads).
 template <class R>
 __global__ void k_uv_kin(DevModel M) {
+  epic_member(M);
   Cell c;
   if (!cell3(M, 1, M.nk - 1, 0, M.nj + 1, c)) return;
   const long long off = plane_offset(M, PL_UV);
@@ -82,6 +91,7 @@ __global__ void k_uv_kin(DevModel M) {
 // DVDT += (PV*UH terms + KIN(j-1)-KIN(j))*n, then the vertical advection of V.
 template <class R>
 __global__ void k_uv_core_v(DevModel M) {
+  epic_member(M);
   Cell c;
   if (!cell3(M, 1, M.nk - 1, 1, M.nj, c)) return;
   const int k = c.k, j = c.j, i = c.i;
@@ -109,6 +119,7 @@ __global__ void k_uv_core_v(DevModel M) {
 // DUDT += (PV*VH terms + KIN(i-1)-KIN(i))*m with the filtered KIN, then the vertical advection of U.
 template <class R>
 __global__ void k_uv_core_u(DevModel M) {
+  epic_member(M);
   Cell c;
   if (!cell3(M, 1, M.nk - 1, 0, M.nj + 1, c)) return;
   const int k = c.k, j = c.j, i = c.i;
@@ -140,6 +151,7 @@ __global__ void k_uv_core_u(DevModel M) {
 // Pole boundary rows of GZ3 (zonal means of the adjacent row), epic_timestep.c:930-998.
 // One block per k; thread 0 sums in the reference order.
 __global__ void k_gz_pole_rows(DevModel M) {
+  epic_member(M);
   const int k = blockIdx.x;
   __shared__ double avg[2];
   if (threadIdx.x < 2) {
@@ -180,6 +192,7 @@ __device__ __forceinline__ LonFace lon_face(const DevModel &M, int k, int j, int
 }
 
 __global__ void k_pgrad_lon(DevModel M) {
+  epic_member(M);
   Cell c;
   if (!cell3(M, 1, M.nk - 1, 0, M.nj + 1, c)) return;
   const int k = c.k, j = c.j, i = c.i;
@@ -238,6 +251,7 @@ __device__ __forceinline__ LatFace lat_face(const DevModel &M, int k, int j, int
 }
 
 __global__ void k_pgrad_lat(DevModel M) {
+  epic_member(M);
   Cell c;
   if (!cell3(M, 1, M.nk - 1, 1, M.nj, c)) return;
   const int k = c.k, j = c.j, i = c.i;
@@ -320,6 +334,7 @@ __device__ __forceinline__ void vmp(const DevModel &M, const double *V, int kind
 
 template <class R>
 __global__ void k_hsu_merid_pred(DevModel M, const double *A, int kind, int k0) {
+  epic_member(M, A);
   Cell c;
   if (!cell3(M, k0, M.nk - k0 + 1, 0, M.nj + 2, c)) return;   // rows 0..nj+1
   const double *V = M.v + plane_offset(M, PL_UV);
@@ -334,6 +349,7 @@ __global__ void k_hsu_merid_pred(DevModel M, const double *A, int kind, int k0) 
 
 template <class R>
 __global__ void k_hsu_merid_apred(DevModel M, const double *A, int k0) {
+  epic_member(M, A);
   Cell c;
   if (!cell3(M, k0, M.nk - k0 + 1, 0, M.nj + 1, c)) return;
   const double *FF = M.work1;
@@ -344,6 +360,7 @@ __global__ void k_hsu_merid_apred(DevModel M, const double *A, int k0) {
 
 template <class R>
 __global__ void k_hsu_merid_corr(DevModel M, const double *A, int kind, int k0) {
+  epic_member(M, A);
   Cell c;
   if (!cell3(M, k0, M.nk - k0 + 1, 0, M.nj + 2, c)) return;
   const int k = c.k, j = c.j, i = c.i, nj = M.nj;
@@ -386,6 +403,7 @@ __global__ void k_hsu_merid_corr(DevModel M, const double *A, int kind, int k0) 
 
 template <class R>
 __global__ void k_hsu_merid_update(DevModel M, double *A, int k0) {
+  epic_member(M, A);
   Cell c;
   if (!cell3(M, k0, M.nk - k0 + 1, 0, M.nj + 1, c)) return;
   const double *FF = M.work3;
@@ -401,6 +419,7 @@ __global__ void k_hsu_merid_update(DevModel M, double *A, int k0) {
 // d2dy2 of planes k0..k1 of src into dst (coefficients per row from the init block, :1049-1141).
 template <class R>
 __global__ void k_d2dy2(DevModel M, const double *src, int src_sel, double *dst, int vgrid, double diff_coef, int k0, int nkk) {
+  epic_member(M, src, dst);
   Cell c;
   const int nrows = vgrid ? M.nj + 2 : M.nj + 1;   // v: j = 0..nj+1, h: j = 0..nj
   if (!cell3(M, k0, nkk, 0, nrows, c)) return;
@@ -420,6 +439,7 @@ __global__ void k_d2dy2(DevModel M, const double *src, int src_sel, double *dst,
 // A += dt*sign*D over the rows the reference updates (v: 1..nj, h: 0..nj).
 template <class R>
 __global__ void k_visc_apply(DevModel M, double *A, int sel, const double *D, int vgrid, double sign, int k0, int nkk) {
+  epic_member(M, A, D);
   Cell c;
   if (!cell3(M, k0, nkk, vgrid ? 1 : 0, vgrid ? M.nj : M.nj + 1, c)) return;
   A += plane_offset(M, sel);
@@ -432,6 +452,7 @@ __global__ void k_visc_apply(DevModel M, double *A, int sel, const double *D, in
 // the mixed form sums it in FP64 with a block reduction.
 template <class R>
 __global__ void k_zonal_visc(DevModel M, double *A, int sel, int jbot, int jhalf, int k0) {
+  epic_member(M, A);
   extern __shared__ __align__(16) unsigned char smraw[];
   const int ni = M.ni;
   const int j = jbot + (int)blockIdx.x;
@@ -511,6 +532,7 @@ __device__ __forceinline__ R div_at(const DevModel &M, const double *UU, const d
 
 template <class R>
 __global__ void k_divergence(DevModel M, const double *UU, const double *VV, int vsel, double *DI, int k0, int nkk) {
+  epic_member(M, UU, VV, DI);
   Cell c;
   if (!cell3(M, k0, nkk, 0, M.nj + 1, c)) return;
   VV += plane_offset(M, vsel);
@@ -520,6 +542,7 @@ __global__ void k_divergence(DevModel M, const double *UU, const double *VV, int
 // Interior potential vorticity, vorticity(ON_SIGMATHETA, POTENTIAL) :4168-4186, planes 0..nk.
 template <class R>
 __global__ void k_pv_interior(DevModel M, const double *VV) {
+  epic_member(M, VV);
   Cell c;
   if (!cell3(M, 0, M.nk + 1, 1, M.nj, c)) return;
   const int k = c.k, j = c.j, i = c.i;
@@ -541,6 +564,7 @@ __global__ void k_pv_interior(DevModel M, const double *VV) {
 // Polar potential vorticity from the circulation of the adjacent u row, :4279-4341.
 // One block per plane; thread 0 forms the sums in the reference order.
 __global__ void k_pv_poles(DevModel M) {
+  epic_member(M);
   const int k = blockIdx.x;
   const double *UU = M.u + plane_offset(M, PL_UV);
   const double *HH = M.h3;
@@ -571,6 +595,7 @@ __global__ void k_pv_poles(DevModel M) {
 // dvdz2 keeps the reference's sign slip (:3127-3128); only dudz2 decides the 1e6 branch.
 template <class R>
 __global__ void k_ri2(DevModel M) {
+  epic_member(M);
   Cell c;
   if (!cell3(M, 1, M.nk, 0, M.nj + 1, c)) return;
   const int k = c.k, j = c.j, i = c.i;
@@ -604,6 +629,7 @@ __global__ void k_ri2(DevModel M) {
 // divergence_damping apply step, epic_subgrid.c:1857-1881 (DIV from k_divergence in work2).
 template <class R>
 __global__ void k_divdamp_apply(DevModel M, double nudiv) {
+  epic_member(M);
   const long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
   const long long per = (long long)(M.nk - 1) * (M.nj + 1) * M.ni;
   if (t >= 2 * per) return;
@@ -631,6 +657,7 @@ __global__ void k_divdamp_apply(DevModel M, double nudiv) {
 // ---------------------------------------------------------------------------------------------
 
 __global__ void k_uv_decide(DevModel M) {
+  epic_member(M);
   Ctl *c = M.ctl;
   for (int w = 0; w < 2; w++) {
     const double *val = w == 0 ? M.u : M.v, *ten = w == 0 ? M.dudt : M.dvdt;
@@ -649,6 +676,7 @@ __global__ void k_uv_decide(DevModel M) {
 }
 
 __global__ void k_uv_update(DevModel M) {
+  epic_member(M);
   const long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
   const long long per = (long long)(M.nk - 1) * (M.nj + 1) * M.ni;
   if (t >= 2 * per) return;
@@ -684,6 +712,7 @@ __global__ void k_uv_update(DevModel M) {
 }
 
 __global__ void k_uv_rotate(DevModel M) {
+  epic_member(M);
   Ctl *c = M.ctl;
   if (M.uv_scheme == EPIC_UV_AB3) {
     const int itmp = c->it_minus2;
@@ -704,12 +733,18 @@ __global__ void k_uv_rotate(DevModel M) {
   c->model_time += (long long)M.dt;
 }
 
-__global__ void k_itime_advance(DevModel M) { M.ctl->itime += 1; }
+__global__ void k_itime_advance(DevModel M) {
+  epic_member(M); M.ctl->itime += 1; }
 
 // ---- launchers ----
 
+int launch_copy_gz(const DevModel &M, cudaStream_t s) {
+  k_copy_gz<<<zg(epic_blocks(M.n3, 256), M), 256, 0, s>>>(M);
+  return 0;
+}
+
 int launch_zero_tend(const DevModel &M, cudaStream_t s) {
-  k_zero_tend<<<epic_blocks(M.n3, 256), 256, 0, s>>>(M);
+  k_zero_tend<<<zg(epic_blocks(M.n3, 256), M), 256, 0, s>>>(M);
   return 0;
 }
 
@@ -722,9 +757,9 @@ int launch_uv_core(const DevModel &M, cudaStream_t s) {
 }
 
 int launch_uv_pgrad(const DevModel &M, cudaStream_t s) {
-  k_gz_pole_rows<<<M.nk + 1, 128, 0, s>>>(M);
-  k_pgrad_lon<<<cells_blocks(M, M.nk - 1, M.nj + 1, 128), 128, 0, s>>>(M);
-  k_pgrad_lat<<<cells_blocks(M, M.nk - 1, M.nj, 128), 128, 0, s>>>(M);
+  k_gz_pole_rows<<<zg(M.nk + 1, M), 128, 0, s>>>(M);
+  k_pgrad_lon<<<zg(cells_blocks(M, M.nk - 1, M.nj + 1, 128), M), 128, 0, s>>>(M);
+  k_pgrad_lat<<<zg(cells_blocks(M, M.nk - 1, M.nj, 128), M), 128, 0, s>>>(M);
   return 0;
 }
 
@@ -799,9 +834,9 @@ int launch_divergence_damping(const DevModel &M, cudaStream_t s) {
 }
 
 int launch_uv_update(const DevModel &M, cudaStream_t s) {
-  k_uv_decide<<<1, 1, 0, s>>>(M);
-  k_uv_update<<<epic_blocks(2LL * (M.nk - 1) * (M.nj + 1) * M.ni, 128), 128, 0, s>>>(M);
-  k_uv_rotate<<<1, 1, 0, s>>>(M);
+  k_uv_decide<<<zg(1, M), 1, 0, s>>>(M);
+  k_uv_update<<<zg(epic_blocks(2LL * (M.nk - 1) * (M.nj + 1) * M.ni, 128), M), 128, 0, s>>>(M);
+  k_uv_rotate<<<zg(1, M), 1, 0, s>>>(M);
   return 0;
 }
 
@@ -809,7 +844,7 @@ int launch_store_diag(const DevModel &M, cudaStream_t s) {
   // PV3: filtered copy of V (v rows), then the interior and polar values.
   launch_filter_planes(M, M.v, PL_UV, M.work1, 0, M.nk + 1, 1, s, M.mixed);
   EPIC_LAUNCH_R(M.mixed, k_pv_interior, cells_blocks(M, M.nk + 1, M.nj, 128), 128, 0, s, M, M.work1);
-  k_pv_poles<<<M.nk + 1, 128, 0, s>>>(M);
+  k_pv_poles<<<zg(M.nk + 1, M), 128, 0, s>>>(M);
   // DIV_UV3 from a filtered copy of U.
   launch_filter_planes(M, M.u, PL_UV, M.work2, 0, M.nk + 1, 0, s, M.mixed);
   EPIC_LAUNCH_R(M.mixed, k_divergence, cells_blocks(M, M.nk + 1, M.nj + 1, 128), 128, 0, s, M, M.work2, M.v, PL_UV, M.div_uv3, 0, M.nk + 1);
@@ -818,7 +853,7 @@ int launch_store_diag(const DevModel &M, cudaStream_t s) {
 }
 
 int launch_itime_advance(const DevModel &M, cudaStream_t s) {
-  k_itime_advance<<<1, 1, 0, s>>>(M);
+  k_itime_advance<<<zg(1, M), 1, 0, s>>>(M);
   return 0;
 }
 

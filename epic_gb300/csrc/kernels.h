@@ -19,11 +19,19 @@ __device__ __forceinline__ long long plane_offset(const DevModel &M, int sel) {
   }
 }
 
-// Launch the FP32 (mixed form) or FP64 instantiation of a kernel template.
-#define EPIC_LAUNCH_R(mixed, kern, grid, block, smem, stream, ...)                 \
-  do {                                                                             \
-    if (mixed) kern<float><<<(grid), (block), (smem), (stream)>>>(__VA_ARGS__);    \
-    else kern<double><<<(grid), (block), (smem), (stream)>>>(__VA_ARGS__);        \
+// Grid of a launch over every member of a batch: blockIdx.z selects the member (one member
+// when the model is not a batch).
+inline dim3 zg(dim3 g, const DevModel &M) {
+  g.z = M.nbatch > 1 ? (unsigned)M.nbatch : 1u;
+  return g;
+}
+
+// Launch the FP32 (mixed form) or FP64 instantiation of a kernel template over every member
+// (the launcher's `M` sets the batch).
+#define EPIC_LAUNCH_R(mixed, kern, grid, block, smem, stream, ...)                              \
+  do {                                                                                          \
+    if (mixed) kern<float><<<zg((grid), M), (block), (smem), (stream)>>>(__VA_ARGS__);          \
+    else kern<double><<<zg((grid), M), (block), (smem), (stream)>>>(__VA_ARGS__);              \
   } while (0)
 
 // k_filter.cu -- zonal filter (epic_adjust.c) and the zonal pass of hsu_advection.
@@ -50,6 +58,7 @@ int launch_advection_prep(const DevModel &M, int phase, cudaStream_t s);
 int column_kernels_init(int nk);
 
 // k_stencil.cu -- horizontal stencils and the time update
+int launch_copy_gz(const DevModel &M, cudaStream_t s);
 int launch_zero_tend(const DevModel &M, cudaStream_t s);
 int launch_uv_core(const DevModel &M, cudaStream_t s);
 int launch_uv_pgrad(const DevModel &M, cudaStream_t s);

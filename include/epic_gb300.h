@@ -183,6 +183,22 @@ int64_t epic_model_device_bytes(const epic_model *m);
 #define EPIC_NOALLOC_TABLE_ENTRIES 16384
 int  epic_model_filter_mass_noalloc(epic_model *m);
 
+/*
+ * Batches (no counterpart in the reference, which runs one model per process).  A batch is a
+ * view over n models from epic_model_create that share sizes, scheme, precision form,
+ * k_sigma, dt and viscosities (members may differ in state and in the drag rate hs_kf); every
+ * kernel of a step is launched once for all members.  Member state stays in the member models:
+ * upload and download through them (after epic_batch_sync).  The batch does not own them.
+ */
+typedef struct epic_batch epic_batch;
+int  epic_batch_create(epic_model *const *members, int32_t n, epic_batch **out);
+void epic_batch_destroy(epic_batch *b);
+int  epic_batch_timestep(epic_batch *b, int32_t action);   /* every member, as epic_model_timestep */
+int  epic_batch_run(epic_batch *b, int32_t nsteps);        /* every member, as epic_model_run */
+int  epic_batch_sync(epic_batch *b);                       /* wait; first member error, if any */
+void *epic_batch_stream(epic_batch *b);
+int32_t epic_batch_kernels_per_step(const epic_batch *b);
+
 /* Text of the last error on this thread. */
 const char *epic_last_error(void);
 

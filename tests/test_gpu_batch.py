@@ -1,0 +1,48 @@
+"""Batches (epic_batch_*): every kernel launched once for all members must give each member
+exactly the bits it gets when stepped alone, in both precision forms."""
+import numpy as np
+import pytest
+
+from epic_gb300 import EPIC_PREC_FP64, EPIC_PREC_MIXED, EPIC_SYNC_DIAGS_ONLY, Batch, EpicError, HSConfig, Model, hs_setup
+
+pytestmark = pytest.mark.gpu
+
+
+def _member(seed, kf_scale, precision, shape=(32, 16, 10)):
+    ni, nj, nk = shape
+    ga, f = hs_setup(HSConfig(ni=ni, nj=nj, nk=nk, dt=300, seed=seed))
+    ga.struct.hs_kf *= kf_scale
+    m = Model(ga, precision)
+    m.upload(f)
+    return ga, f, m
+
+
+@pytest.mark.parametrize("precision", [EPIC_PREC_FP64, EPIC_PREC_MIXED])
+def test_batch_equals_members_alone(gpu, precision):
+    scales = [1.0, 0.93, 1.07, 1.1, 0.9]
+    members = [_member(10 + q, s, precision) for q, s in enumerate(scales)]
+    batch = Batch([m for _, _, m in members])
+    batch.timestep(EPIC_SYNC_DIAGS_ONLY)
+    batch.run(7)
+    batch.sync()
+    for ga, f, m in members:
+        alone = Model(ga, precision)
+        alone.upload(f)
+        alone.timestep(EPIC_SYNC_DIAGS_ONLY)
+        alone.run(7)
+        alone.sync()
+        a, b = m.download(), alone.download()
+        for k in a.arrays:
+            assert np.array_equal(a.arrays[k], b.arrays[k]), k
+        assert (a.struct.itime, a.struct.it_zero) == (b.struct.itime, b.struct.it_zero)
+    assert batch.kernels_per_step > 0
+
+
+def test_batch_rejects_mixed_shapes(gpu):
+    _, _, a = _member(1, 1.0, EPIC_PREC_FP64)
+    _, _, b = _member(2, 1.0, EPIC_PREC_FP64, shape=(64, 32, 10))
+    _, _, c = _member(3, 1.0, EPIC_PREC_MIXED)
+    with pytest.raises(EpicError, match="differs"):
+        Batch([a, b])
+    with pytest.raises(EpicError, match="differs"):
+        Batch([a, c])
