@@ -1,15 +1,23 @@
-"""Throughput of the GB300 EPIC timestep() on a synthetic Held-Suarez state.
+"""Throughput of the GB300 EPIC timestep() on synthetic Held-Suarez states.
 
     python bench.py [--gpus N] [--steps K] [--warmup W] [--impl gb300|reference]
-                    [--workload hs256|hs512|hs128|hs64] [--no-cpu-baseline]
+                    [--workload ens64|hs64|hs128|hs256|hs512] [--precision mixed|fp64]
+                    [--no-cpu-baseline] [--no-extras]
 
-A step is one timestep(STEP_PROGS_AND_SYNC_DIAGS) of the whole grid.  The default workload
-is 256 x 128 x 32 at dt = 60 s (the shape of the plain-FP64 256x128x32 run); its state
-(~37 FP64 3-D arrays, 0.35 GB) is larger than the 129 MB L2, so no flush is needed between
-steps.  value = cell-steps/s (cells = ni*nj*nk) with the state resident in HBM, timed with
-CUDA events on the model's stream; e2e = the same metric through the C ABI with the state
-in pinned host memory, uploaded and downloaded every step (what a reference-side
-timestep() wrapper over host-owned `var` costs).
+A step is one timestep(STEP_PROGS_AND_SYNC_DIAGS) of every grid in the workload.  metric =
+cell-steps/s (cells = ni*nj*nk per grid).
+
+Default workload ens64: an ensemble of 64 Held-Suarez members at 128 x 64 x 20, dt = 300 s,
+each with its own noise seed and a +/-10% seeded drag rate k_f, advanced as one batch (every
+kernel launched once for all members, one captured graph per step) in the mixed-precision
+form.  The ensemble's state (64 x 54 MB) is far larger than the 129 MB L2, so no flush is
+needed between steps.  Beside `value` the line reports the plain FP64 step of one member
+shape and the mixed/FP64 ratio, the mixed form's error against FP64 after one simulated day,
+and the serving loop's p50/p99 run latency on a seeded Poisson request stream.
+
+value = cell-steps/s with the state resident in HBM, timed with CUDA events on the stream the
+work runs on; e2e = the same metric through the C ABI with every member's state in pinned
+host memory, uploaded and downloaded every step.
 
 --impl reference times the reference's CPU implementation of the step (the oracle's
 restatement, bit-identical to the reference build) on every host core as independent
@@ -35,8 +43,14 @@ WORKLOADS = {
     "hs64": (64, 32, 10, 300),
     "hs128": (128, 64, 20, 300),
     "hs256": (256, 128, 32, 60),
-    "hs512": (512, 256, 40, 75),
+    "hs512": (512, 256, 40, 60),
+    "ens64": (128, 64, 20, 300),   # per member; 64 members
 }
+ENSEMBLE = {"ens64": 64}
+# Serving stream: shapes and the time step each runs stably with (dt from runs of the FP64
+# form that kept GZ3 monotonic for at least half a simulated day at that shape).
+SERVE_SHAPES = {(64, 32, 10): 300, (64, 32, 20): 300, (128, 64, 20): 300, (128, 64, 10): 150, (256, 128, 10): 120,
+                (256, 128, 20): 150, (512, 256, 10): 60, (512, 256, 20): 60}
 METRIC = "cell-steps/s"
 
 
@@ -246,6 +260,221 @@ def run_gpu(args):
     return out
 
 
+def _members(cfg, n, precision, torch_seed=7):
+    """n ensemble members of one shape: member q has noise seed q and k_f scaled by 1 +/- 10%."""
+    import numpy as np
+    from epic_gb300 import HSConfig, Model, hs_setup
+    rng = np.random.default_rng(torch_seed)
+    out = []
+    for q in range(n):
+        ga, f = hs_setup(HSConfig(ni=cfg.ni, nj=cfg.nj, nk=cfg.nk, dt=cfg.dt, seed=q))
+        ga.struct.hs_kf *= 1.0 + float(rng.uniform(-0.1, 0.1))
+        m = Model(ga, precision)
+        m.upload(f)
+        out.append(m)
+    return out
+
+
+def single_rate(cfg, precision, steps, torch):
+    """cell-steps/s of one model stepped alone (graph replay), timed with events on its stream."""
+    from epic_gb300 import EPIC_SYNC_DIAGS_ONLY, Model, hs_setup
+    ga, f = hs_setup(cfg)
+    m = Model(ga, precision)
+    m.upload(f)
+    m.timestep(EPIC_SYNC_DIAGS_ONLY)
+    m.run(3)
+    m.sync()
+    st = torch.cuda.ExternalStream(m.stream)
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record(st)
+    m.run(steps)
+    e1.record(st)
+    e1.synchronize()
+    m.sync()
+    ms = e0.elapsed_time(e1) / steps
+    m.close()
+    return {"value": cfg.cells / (ms / 1e3), "ms_per_step": ms}
+
+
+def mixed_error(torch):
+    """Per-prognostic relative L2 of the mixed form against FP64 after one simulated day
+    (288 steps of 300 s) at 64x32x10, from a state spun up for 10 days in FP64, and from rest."""
+    sys.path.insert(0, os.path.join(ROOT, "tests"))
+    from compare import PROGNOSTIC, field_errors
+    from epic_gb300 import EPIC_PREC_FP64, EPIC_PREC_MIXED, EPIC_SYNC_DIAGS_ONLY, HSConfig, Model, hs_setup
+    ga, f = hs_setup(HSConfig(ni=64, nj=32, nk=10, dt=300, seed=0))
+    out = {}
+    for label, spin in (("after_10_day_spin_up", 2880), ("from_rest", 0)):
+        start = f
+        if spin:
+            m = Model(ga, EPIC_PREC_FP64)
+            m.upload(f)
+            m.timestep(EPIC_SYNC_DIAGS_ONLY)
+            m.run(spin)
+            m.sync()
+            start = m.download()
+            m.close()
+        res = []
+        for prec in (EPIC_PREC_FP64, EPIC_PREC_MIXED):
+            m = Model(ga, prec)
+            m.upload(start)
+            if not spin:
+                m.timestep(EPIC_SYNC_DIAGS_ONLY)
+            m.run(288)
+            m.sync()
+            res.append(m.download())
+            m.close()
+        e = field_errors(res[1], res[0], PROGNOSTIC)
+        out[label] = {k: v[0] for k, v in e.items()}
+    out["case"] = "64x32x10, dt=300 s, 1 simulated day (288 steps), relative L2 per prognostic vs the FP64 form"
+    return out
+
+
+def serving_summary(precision, seed=3):
+    """The serving loop on a seeded Poisson stream (20 requests/s, 40 requests)."""
+    from epic_gb300.serving import RunServer, latency_summary, poisson_requests
+    reqs = poisson_requests(40, 20.0, seed, sorted(SERVE_SHAPES), (36, 144), lambda s: SERVE_SHAPES[s])
+    res = RunServer(hbm_budget=40 << 30, precision=precision, round_steps=16).serve(reqs)
+    out = latency_summary(res)
+    out.update({"arrivals": "Poisson, 20 requests/s, seed 3", "shapes": [list(k) + [v] for k, v in sorted(SERVE_SHAPES.items())],
+                "steps_per_request": "uniform 36..144", "hbm_budget_gb": 40,
+                "note": "durations are steps, not the 0.25-2 simulated days of the stream description, to bound the run"})
+    return out
+
+
+def run_gpu_ensemble(args):
+    import torch
+    from epic_gb300 import EPIC_PREC_FP64, EPIC_PREC_MIXED, EPIC_SYNC_DIAGS_ONLY, Batch
+    ws, rank, local = _dist()
+    torch.cuda.set_device(local)
+    if ws > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl")
+    precision = EPIC_PREC_MIXED if args.precision == "mixed" else EPIC_PREC_FP64
+    cfg = _workload_cfg(args.workload)
+    nmem = ENSEMBLE[args.workload]
+    members = _members(cfg, nmem, precision, torch_seed=7 + rank)
+    batch = Batch(members)
+    batch.timestep(EPIC_SYNC_DIAGS_ONLY)
+    for _ in range(args.warmup):
+        batch.run(1)
+    batch.sync()
+    stream = torch.cuda.ExternalStream(batch.stream)
+
+    def barrier():
+        torch.cuda.synchronize()
+        if ws > 1:
+            import torch.distributed as dist
+            dist.barrier()
+
+    ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    barrier()
+    with ClockSampler(local) as clk:
+        ev0.record(stream)
+        for _ in range(args.steps):
+            batch.run(1)
+        ev1.record(stream)
+        ev1.synchronize()
+    batch.sync()
+    barrier()
+    ms = ev0.elapsed_time(ev1)
+    if ws > 1:
+        import torch.distributed as dist
+        t = torch.tensor([ms], device="cuda")
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        ms = float(t.item())
+    ms_step = ms / args.steps
+    cells = nmem * cfg.cells
+    value = ws * cells * args.steps / (ms / 1e3)
+    clocks = clk.summary()
+    launches = batch.kernels_per_step * args.steps
+
+    roof = batch_roofline(batch, cfg, nmem, stream, torch)
+
+    # end to end: every member's state uploaded from pinned host memory and downloaded, each step
+    hosts = [m.download().copy(pinned=True) for m in members]
+    e2e_steps = max(1, min(args.steps, 3))
+    barrier()
+    t0 = time.perf_counter()
+    for _ in range(e2e_steps):
+        for m, h in zip(members, hosts):
+            m.upload(h)
+        batch.run(1)
+        batch.sync()
+        for m, h in zip(members, hosts):
+            m.download(h)
+    torch.cuda.synchronize()
+    e2e_s = (time.perf_counter() - t0) / e2e_steps
+    e2e_val = ws * cells / e2e_s
+    host_bytes = sum(h.nbytes for h in hosts)
+    state_gb = sum(m.device_bytes for m in members) / 1e9
+    batch.close()
+    for m in members:
+        m.close()
+
+    out = None
+    if rank == 0:
+        peaks = _peaks()
+        out = {
+            "metric": METRIC, "value": value, "unit": "cell-steps/s", "n_gpus": ws, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": ms_step, "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "f32+f64" if precision == EPIC_PREC_MIXED else "f64", "data": "synthetic",
+            "config": {"workload": f"ensemble of {nmem} Held-Suarez members {cfg.ni}x{cfg.nj}x{cfg.nk}, dt={cfg.dt}s, AB3, "
+                                   f"seeded 0.1 K noise and +/-10% k_f per member, {args.precision} form, one launch per "
+                                   f"kernel for all members", "ni": cfg.ni, "nj": cfg.nj, "nk": cfg.nk, "dt": cfg.dt,
+                       "members": nmem, "precision": args.precision, "parallelism": f"replicas{ws}",
+                       "l2": f"ensemble state {state_gb:.1f} GB > 129 MB L2; no flush needed",
+                       "state": "horizontally uniform HS equilibrium column at rest + seeded 0.1 K theta noise"},
+            "clocks": clocks,
+            "e2e": {"value": e2e_val, "unit": "cell-steps/s", "h2d_bytes_per_step": host_bytes, "d2h_bytes_per_step": host_bytes},
+            "gpu_launches": launches,
+            "roofline": roof,
+            "step_roofline": {"bound": "hbm", "algorithmic_bytes_per_step": nmem * algorithmic_bytes_per_step(cfg),
+                              "achieved_gbs": nmem * algorithmic_bytes_per_step(cfg) / (ms_step / 1e3) / 1e9,
+                              "peak_gbs": peaks.get("hbm_gbs")},
+        }
+        if peaks.get("hbm_gbs"):
+            out["step_roofline"]["frac"] = out["step_roofline"]["achieved_gbs"] / peaks["hbm_gbs"]
+        if not args.no_extras:
+            fp64 = single_rate(cfg, EPIC_PREC_FP64, args.steps, torch)
+            mixed = single_rate(cfg, EPIC_PREC_MIXED, args.steps, torch)
+            out["fp64_single"] = dict(fp64, note=f"plain FP64 timestep of one {cfg.ni}x{cfg.nj}x{cfg.nk} grid")
+            out["mixed_single"] = dict(mixed, note=f"mixed form, one {cfg.ni}x{cfg.nj}x{cfg.nk} grid")
+            out["batched_over_fp64_single"] = value / ws / fp64["value"]
+            out["mixed_error"] = mixed_error(torch)
+            out["serving"] = serving_summary(precision)
+    if ws > 1:
+        import torch.distributed as dist
+        dist.barrier()
+        dist.destroy_process_group()
+    return out
+
+
+def batch_roofline(batch, cfg, nmem, stream, torch):
+    """The finite-volume pressure gradient (stage 12: k_pgrad_lon + k_pgrad_lat, FP64 in both
+    forms, the largest share of the mixed step) over all members, timed with events on the
+    batch stream.  Algorithmic bytes per launch: GZ3, P2 and RHO3 read once and DUDT, DVDT read
+    and written once, 7 FP64 3-D fields of ni*(nj+1)*nk cells per member."""
+    peaks = _peaks()
+    n = 5
+    batch.run_stage(12)
+    batch.sync()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record(stream)
+    for _ in range(n):
+        batch.run_stage(12)
+    e1.record(stream)
+    e1.synchronize()
+    dur = e0.elapsed_time(e1) / n / 1e3
+    alg = 7 * 8 * cfg.ni * (cfg.nj + 1) * cfg.nk * nmem
+    ach = alg / dur / 1e9
+    return {"kernel": "uv_pgrad_finite_volume (k_pgrad_lon + k_pgrad_lat, FP64) over all members", "bound": "hbm",
+            "achieved": ach, "peak": peaks["hbm_gbs"], "unit": "GB/s", "frac": ach / peaks["hbm_gbs"],
+            "peak_source": peaks["source"] + " (burst copy)", "algorithmic_bytes": alg, "launch_ms": dur * 1e3,
+            "traffic": None,
+            "note": "FP64-pipe bound on GB300 (about 240 FP64 operations per cell); the HBM fraction is low by design"}
+
+
 def _peaks():
     p = os.path.join(ROOT, "MEASURED_PEAKS.json")
     if os.path.exists(p):
@@ -292,11 +521,14 @@ def main():
     ap.add_argument("--steps", type=int, default=20)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
-    ap.add_argument("--workload", default="hs256", choices=sorted(WORKLOADS))
+    ap.add_argument("--workload", default="ens64", choices=sorted(WORKLOADS))
+    ap.add_argument("--no-extras", action="store_true", help="skip the FP64/mixed single-grid, error and serving figures")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--cpu-steps", type=int, default=3)
-    ap.add_argument("--precision", default="fp64", choices=["fp64", "mixed"])
+    ap.add_argument("--precision", default=None, choices=["fp64", "mixed"])
     args = ap.parse_args()
+    if args.precision is None:
+        args.precision = "mixed" if args.workload in ENSEMBLE else "fp64"
     ws, rank, _ = _dist()
 
     if args.impl == "reference":
@@ -309,7 +541,9 @@ def main():
         line = {"impl": "reference", "metric": METRIC, "value": val, "unit": "cell-steps/s", "n_gpus": args.gpus,
                 "steps": steps, "warmup": args.warmup, "ms_per_step": wall / steps * 1e3, "higher_is_better": True,
                 "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
-                "config": {"workload": f"Held-Suarez {cfg.ni}x{cfg.nj}x{cfg.nk}, dt={cfg.dt}s, AB3, nu4=0.5 max",
+                "config": {"workload": (f"ensemble of {ENSEMBLE[args.workload]} Held-Suarez members " if args.workload in ENSEMBLE
+                                        else "Held-Suarez ") + f"{cfg.ni}x{cfg.nj}x{cfg.nk}, dt={cfg.dt}s, AB3, nu4=0.5 max; "
+                                        f"reference CPU step (FP64) as {procs} concurrent single-threaded grids",
                            "ni": cfg.ni, "nj": cfg.nj, "nk": cfg.nk, "dt": cfg.dt, "precision": "fp64"},
                 "cpu_baseline": {"value": val, "unit": "cell-steps/s", "cores": procs, "kind": "port",
                                  "sample": f"{procs} independent single-threaded replicas x {steps} steps of the "
@@ -318,7 +552,7 @@ def main():
         print(json.dumps(line))
         return
 
-    out = run_gpu(args)
+    out = run_gpu_ensemble(args) if args.workload in ENSEMBLE else run_gpu(args)
     if rank == 0 and out is not None:
         if ws == 1 and not args.no_cpu_baseline:
             val, wall = cpu_reference(args.workload, args.cpu_steps, 0, 1)

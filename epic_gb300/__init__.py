@@ -56,11 +56,13 @@ def load_library(path: str | None = None) -> C.CDLL:
     lib.epic_model_kernels_per_step.restype = C.c_int32
     lib.epic_model_device_bytes.argtypes = [C.c_void_p]
     lib.epic_model_device_bytes.restype = C.c_int64
+    lib.epic_model_bytes.argtypes = [C.POINTER(EpicGrid), C.c_int32]
+    lib.epic_model_bytes.restype = C.c_int64
     lib.epic_model_filter_mass_noalloc.argtypes = [C.c_void_p]
     lib.epic_batch_create.argtypes = [C.POINTER(C.c_void_p), C.c_int32, C.POINTER(C.c_void_p)]
     lib.epic_batch_destroy.argtypes = [C.c_void_p]
     lib.epic_batch_destroy.restype = None
-    for name in ("epic_batch_timestep", "epic_batch_run"):
+    for name in ("epic_batch_timestep", "epic_batch_run", "epic_batch_run_stage"):
         getattr(lib, name).argtypes = [C.c_void_p, C.c_int32]
     lib.epic_batch_sync.argtypes = [C.c_void_p]
     lib.epic_batch_stream.argtypes = [C.c_void_p]
@@ -93,6 +95,11 @@ def hs_setup(cfg: HSConfig) -> tuple[GridArrays, Fields]:
     _check(lib.epic_hs_initial_state(C.byref(ga.struct), C.byref(p), C.c_uint64(cfg.seed), C.c_double(cfg.noise_k),
                                      C.byref(f.struct)), "epic_hs_initial_state")
     return ga, f
+
+
+def model_bytes(grid: GridArrays, precision: int = EPIC_PREC_FP64) -> int:
+    """Device bytes a Model of this grid takes (for admission by memory budget)."""
+    return int(load_library().epic_model_bytes(C.byref(grid.struct), precision))
 
 
 class Model:
@@ -187,6 +194,9 @@ class Batch:
     def run(self, nsteps: int) -> None:
         _check(self.lib.epic_batch_run(self._h, nsteps), "epic_batch_run")
 
+    def run_stage(self, stage: int) -> None:
+        _check(self.lib.epic_batch_run_stage(self._h, stage), "epic_batch_run_stage")
+
     def sync(self) -> None:
         _check(self.lib.epic_batch_sync(self._h), "epic_batch_sync")
 
@@ -199,6 +209,6 @@ class Batch:
         return int(self.lib.epic_batch_kernels_per_step(self._h))
 
 
-__all__ = ["Model", "Batch", "hs_setup", "load_library", "EpicError", "HSConfig", "Fields", "GridArrays", "Layout",
+__all__ = ["Model", "Batch", "model_bytes", "hs_setup", "load_library", "EpicError", "HSConfig", "Fields", "GridArrays", "Layout",
            "EPIC_PREC_FP64", "EPIC_PREC_MIXED", "EPIC_STEP_PROGS_AND_SYNC_DIAGS", "EPIC_SYNC_DIAGS_ONLY",
            "EPIC_UV_AB3", "EPIC_UV_LEAPFROG", "LIB_PATH", "np"]

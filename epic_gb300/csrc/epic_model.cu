@@ -260,7 +260,28 @@ int model_error(const Ctl &c) {
                    c.err_k, c.err_j, c.err_i, c.err_val);
 }
 
+// Device bytes of a model's pool: state, scratch and tables, carved in 256-byte units.
+size_t model_pool_bytes(const epic_grid &g) {
+  const epic::Layout L(g.ni, g.nj, g.nk);
+  const size_t n3 = (size_t)L.n3, n2 = (size_t)L.n2;
+  const size_t nvp = g.uv_scheme == EPIC_UV_AB3 ? 1 : 2, ntp = g.uv_scheme == EPIC_UV_AB3 ? 3 : 1;
+  const size_t n_state3 = 2 * nvp + 2 * ntp + 20;   // u,v planes + tendencies + 20 single fields
+  const size_t n_scratch3 = 7;                      // gz, unity, old, work0..3
+  const size_t nj1 = 2 * (g.nj + 1) + 1, ni1 = 2 * (g.ni + 1) + 1, nk1 = 2 * (g.nk + 1) + 1;
+  const size_t ntw = epic::twiddle_doubles(g.ni);
+  auto rnd = [](size_t b) { return ((b + 255) / 256) * 256; };
+  return rnd(sizeof(Ctl)) + (n_state3 + n_scratch3) * rnd(n3 * 8) + 3 * rnd(n2 * 8) + rnd((size_t)(g.nj + 3) * (g.nk + 2) * 3 * 8) +
+         rnd(ni1 * 8) + 10 * rnd(nj1 * 8) + 3 * rnd(nk1 * 8) + rnd((g.nk + 2) * 8) + rnd((g.k_sponge + 1) * 8) +
+         2 * rnd(3 * (g.nj + 2) * 8) + rnd(ntw * 8) + rnd(ntw * 4) + rnd((g.nj + 1) * 8) + rnd(sizeof(epic::MathTable)) + 4096;
+}
+
 }  // namespace
+
+extern "C" int64_t epic_model_bytes(const epic_grid *g, int32_t precision) {
+  (void)precision;   // both forms store the state in binary64
+  if (!g || g->ni < 4 || g->nj < 3 || g->nk < 3) return -1;
+  return (int64_t)model_pool_bytes(*g);
+}
 
 extern "C" const char *epic_last_error(void) { return epic::error_buffer(); }
 
@@ -318,13 +339,7 @@ extern "C" int epic_model_create(const epic_grid *g, int32_t precision, epic_mod
 
   // One pool for everything: state, scratch, tables.
   const size_t n3 = (size_t)L.n3, n2 = (size_t)L.n2;
-  const size_t n_state3 = 2 * d.nvp + 2 * d.ntp + 20;   // u,v planes + tendencies + 20 single fields
-  const size_t n_scratch3 = 7;                          // gz, unity, old, work0..3
-  auto rnd = [](size_t b) { return ((b + 255) / 256) * 256; };
-  size_t bytes = rnd(sizeof(Ctl)) + (n_state3 + n_scratch3) * rnd(n3 * 8) + 3 * rnd(n2 * 8) + rnd((size_t)(g->nj + 3) * (g->nk + 2) * 3 * 8) +
-                 rnd(ni1 * 8) + 10 * rnd(nj1 * 8) + 3 * rnd(nk1 * 8) + rnd((g->nk + 2) * 8) + rnd((g->k_sponge + 1) * 8) +
-                 2 * rnd(3 * (g->nj + 2) * 8) + rnd(T.tw.size() * 8) + rnd(T.tw.size() * 4) + rnd((g->nj + 1) * 8) +
-                 rnd(sizeof(epic::MathTable)) + 4096;
+  const size_t bytes = model_pool_bytes(*g);
   cudaError_t e = cudaStreamCreateWithFlags(&m->stream, cudaStreamNonBlocking);
   if (e != cudaSuccess) { delete m; return set_error(EPIC_ERR_CUDA, "cudaStreamCreate: %s", cudaGetErrorString(e)); }
   e = cudaMalloc(&m->pool, bytes);
@@ -702,6 +717,12 @@ extern "C" int epic_batch_run(epic_batch *b, int32_t nsteps) {
     }
   }
   return check_launch("epic_batch_run");
+}
+
+extern "C" int epic_batch_run_stage(epic_batch *b, int32_t stage) {
+  int rc = batch_ready(b, "epic_batch_run_stage");
+  if (rc) return rc;
+  return run_stage_on(b->d, b->stream, stage);
 }
 
 extern "C" int epic_batch_sync(epic_batch *b) {

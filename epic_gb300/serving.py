@@ -1,0 +1,198 @@
+"""Serving: a request loop that keeps many runs of different shapes on one GPU.
+
+The reference runs one model per process and has no serving layer; this module is new.  A
+request is one synthetic Held-Suarez run (shape, time step, seed, drag-rate scale, number of
+steps).  The server
+
+  * admits waiting requests, in arrival order with backfill, while the device bytes of the
+    admitted runs (epic_model_bytes) stay within its HBM budget;
+  * keeps every admitted run's state on the device from admission to completion;
+  * groups the active runs by shape class (sizes, scheme, precision form and time step) and
+    advances each class as one Batch: every kernel of a step is launched once for all of the
+    class's runs, and the classes' batches run on their own streams, so their work overlaps
+    on the device;
+  * re-forms a class's batch whenever a run joins or leaves it (continuous batching: runs that
+    arrive while others are on the GPU join at the next scheduling round);
+  * retires a run when its steps are done: its state is copied to the host and its device
+    memory returns to the budget.
+
+Each run's result is the same bits it gets when run alone (a batch gives every member the bits
+of its own step, and the number of steps per round does not change the arithmetic).
+"""
+from __future__ import annotations
+
+import time
+from dataclasses import dataclass, field
+
+import numpy as np
+
+from . import Batch, EPIC_PREC_MIXED, EPIC_SYNC_DIAGS_ONLY, Fields, HSConfig, Model, hs_setup, model_bytes
+
+
+@dataclass
+class RunRequest:
+    rid: int
+    cfg: HSConfig
+    steps: int
+    arrival: float = 0.0          # seconds after the server starts
+    kf_scale: float = 1.0         # Held-Suarez drag rate k_f multiplier
+
+
+@dataclass
+class RunResult:
+    rid: int
+    shape: tuple
+    steps: int
+    arrival: float
+    admitted: float
+    finished: float
+    fields: Fields | None = None
+    checksum: float = 0.0
+
+    @property
+    def latency(self) -> float:
+        return self.finished - self.arrival
+
+
+@dataclass
+class _Active:
+    req: RunRequest
+    model: Model
+    bytes: int
+    remaining: int
+    admitted: float
+
+
+def _shape_class(cfg: HSConfig, precision: int) -> tuple:
+    return (cfg.ni, cfg.nj, cfg.nk, cfg.dt, cfg.uv_scheme, precision, cfg.nu4, cfg.nu6, cfg.nu8, cfg.nudiv, cfg.lat0)
+
+
+def state_checksum(f: Fields) -> float:
+    """Sum of |U| + |V| + |HDRY| + |THETA| over the current planes (a compact result summary)."""
+    tot = 0.0
+    for k in ("u", "v", "hdry", "theta"):
+        a = f.arrays[k]
+        tot += float(np.abs(np.where(np.abs(a) > 1e300, 0., a)).sum())
+    return tot
+
+
+@dataclass
+class RunServer:
+    hbm_budget: int                      # bytes of device memory the admitted runs may hold
+    precision: int = EPIC_PREC_MIXED
+    round_steps: int = 16                # most steps a class advances per scheduling round
+    keep_fields: bool = False            # keep each result's full state (else a checksum)
+    waiting: list = field(default_factory=list)
+    active: dict = field(default_factory=dict)      # shape class -> list[_Active]
+    batches: dict = field(default_factory=dict)     # shape class -> (Batch, member ids)
+    results: list = field(default_factory=list)
+    used: int = 0
+    t0: float = 0.0
+
+    def now(self) -> float:
+        return time.perf_counter() - self.t0
+
+    def submit(self, req: RunRequest) -> None:
+        self.waiting.append(req)
+
+    # -- admission -------------------------------------------------------------------------
+    def admit(self) -> None:
+        keep = []
+        for req in self.waiting:
+            ga, f = hs_setup(req.cfg)
+            need = model_bytes(ga, self.precision)
+            if need > self.hbm_budget:
+                raise ValueError(f"request {req.rid} needs {need} bytes, more than the whole budget")
+            if self.used + need > self.hbm_budget:
+                keep.append(req)
+                continue
+            ga.struct.hs_kf *= req.kf_scale
+            m = Model(ga, self.precision)
+            m.upload(f)
+            m.timestep(EPIC_SYNC_DIAGS_ONLY)
+            self.used += need
+            cls = _shape_class(req.cfg, self.precision)
+            self.active.setdefault(cls, []).append(_Active(req, m, need, req.steps, self.now()))
+        self.waiting = keep
+
+    # -- one scheduling round ---------------------------------------------------------------
+    def round(self) -> None:
+        launched = []
+        for cls, runs in self.active.items():
+            if not runs:
+                continue
+            ids = tuple(r.req.rid for r in runs)
+            b = self.batches.get(cls)
+            if b is None or b[1] != ids:
+                if b is not None:
+                    b[0].close()
+                b = (Batch([r.model for r in runs]), ids)
+                self.batches[cls] = b
+            n = min(self.round_steps, min(r.remaining for r in runs))
+            b[0].run(n)
+            launched.append((cls, n))
+        for cls, n in launched:
+            self.batches[cls][0].sync()
+            done = []
+            for r in self.active[cls]:
+                r.remaining -= n
+                if r.remaining == 0:
+                    done.append(r)
+            for r in done:
+                self._retire(cls, r)
+
+    def _retire(self, cls, r: _Active) -> None:
+        f = r.model.download()
+        res = RunResult(r.req.rid, (r.req.cfg.ni, r.req.cfg.nj, r.req.cfg.nk), r.req.steps, r.req.arrival, r.admitted,
+                        self.now(), f if self.keep_fields else None, state_checksum(f))
+        self.results.append(res)
+        self.active[cls].remove(r)
+        b = self.batches.pop(cls, None)
+        if b is not None:
+            b[0].close()
+        r.model.close()
+        self.used -= r.bytes
+
+    # -- the loop ---------------------------------------------------------------------------
+    def serve(self, requests: list[RunRequest]) -> list[RunResult]:
+        """Serve requests that arrive at their `arrival` times (seconds from now)."""
+        pending = sorted(requests, key=lambda q: q.arrival)
+        self.t0 = time.perf_counter()
+        while pending or self.waiting or any(self.active.values()):
+            t = self.now()
+            while pending and pending[0].arrival <= t:
+                self.submit(pending.pop(0))
+            if self.waiting:
+                self.admit()
+            if any(self.active.values()):
+                self.round()
+            elif pending:
+                time.sleep(max(0.0, min(0.01, pending[0].arrival - self.now())))
+        for b, _ in self.batches.values():
+            b.close()
+        self.batches.clear()
+        return sorted(self.results, key=lambda r: r.rid)
+
+
+def poisson_requests(n: int, rate: float, seed: int, shapes: list[tuple], steps_range: tuple[int, int],
+                     dt_of=lambda shape: 300) -> list[RunRequest]:
+    """n requests with seeded Poisson arrivals (mean `rate` per second), shapes drawn from
+    `shapes` (ni, nj, nk), step counts uniform in steps_range and k_f scaled by 1 +/- 10%."""
+    rng = np.random.default_rng(seed)
+    t = 0.0
+    out = []
+    for q in range(n):
+        t += float(rng.exponential(1.0 / rate))
+        ni, nj, nk = shapes[int(rng.integers(len(shapes)))]
+        steps = int(rng.integers(steps_range[0], steps_range[1] + 1))
+        cfg = HSConfig(ni=ni, nj=nj, nk=nk, dt=dt_of((ni, nj, nk)), seed=1000 + q)
+        out.append(RunRequest(q, cfg, steps, t, 1.0 + float(rng.uniform(-0.1, 0.1))))
+    return out
+
+
+def latency_summary(results: list[RunResult]) -> dict:
+    lat = np.array([r.latency for r in results])
+    makespan = max(r.finished for r in results) - min(r.arrival for r in results)
+    cells = sum(r.shape[0] * r.shape[1] * r.shape[2] * r.steps for r in results)
+    return {"requests": len(results), "p50_s": float(np.percentile(lat, 50)), "p99_s": float(np.percentile(lat, 99)),
+            "makespan_s": makespan, "aggregate_cell_steps_per_s": cells / makespan}

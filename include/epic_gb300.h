@@ -166,6 +166,10 @@ int32_t epic_model_kernels_per_step(const epic_model *m);
 /* Bytes of device memory the model holds. */
 int64_t epic_model_device_bytes(const epic_model *m);
 
+/* Bytes of device memory epic_model_create would take for this grid (-1 for a bad grid); for
+ * admission by memory budget.  No counterpart in the reference. */
+int64_t epic_model_bytes(const epic_grid *grid, int32_t precision);
+
 /*
  * The 3-D zonal filter of the mass variables (stage 10 above: zonal_filter(HDRY_INDEX, ...,
  * THREEDIM), restore_mass, zonal_filter(THETA_INDEX, ..., THREEDIM); epic_timestep.c:207-222),
@@ -195,6 +199,7 @@ int  epic_batch_create(epic_model *const *members, int32_t n, epic_batch **out);
 void epic_batch_destroy(epic_batch *b);
 int  epic_batch_timestep(epic_batch *b, int32_t action);   /* every member, as epic_model_timestep */
 int  epic_batch_run(epic_batch *b, int32_t nsteps);        /* every member, as epic_model_run */
+int  epic_batch_run_stage(epic_batch *b, int32_t stage);   /* test/timing hook, as epic_model_run_stage */
 int  epic_batch_sync(epic_batch *b);                       /* wait; first member error, if any */
 void *epic_batch_stream(epic_batch *b);
 int32_t epic_batch_kernels_per_step(const epic_batch *b);
