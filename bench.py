@@ -352,7 +352,7 @@ def run_gpu_ensemble(args):
         dist.init_process_group("nccl")
     precision = EPIC_PREC_MIXED if args.precision == "mixed" else EPIC_PREC_FP64
     cfg = _workload_cfg(args.workload)
-    nmem = ENSEMBLE[args.workload]
+    nmem = args.members or ENSEMBLE[args.workload]
     members = _members(cfg, nmem, precision, torch_seed=7 + rank)
     batch = Batch(members)
     batch.timestep(EPIC_SYNC_DIAGS_ONLY)
@@ -523,6 +523,7 @@ def main():
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     ap.add_argument("--workload", default="ens64", choices=sorted(WORKLOADS))
     ap.add_argument("--no-extras", action="store_true", help="skip the FP64/mixed single-grid, error and serving figures")
+    ap.add_argument("--members", type=int, default=None, help="ensemble size (profiling runs use a smaller ensemble)")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--cpu-steps", type=int, default=3)
     ap.add_argument("--precision", default=None, choices=["fp64", "mixed"])

@@ -511,14 +511,14 @@ __global__ void __launch_bounds__(CT_THREADS) k_pgrad_vars_column(DevModel M) {
 // relative error near 1e-7.
 
 // log(b/a) for b/a near 1, from the FP64 difference
-__device__ __forceinline__ float log_ratio_f(double a, double b) { return log1pf((float)((b - a) / a)); }
+__device__ __forceinline__ float log_ratio_f(double a, double b) { return log1pf((float)(b - a) / (float)a); }
 
 // onto_kk(P2_INDEX) at a layer: ((bot^(k+1) - top^(k+1)) / ((k+1)(bot - top)))^(1/k), written as
 // bot * q^(1/kappa), q = (1 - r^(kappa+1)) / ((kappa+1)(1 - r)), r = top/bot.
 __device__ __forceinline__ double layer_p_mixed(const DevModel &M, double top, double bot) {
   if (fcmp(bot, top) == 0) return .5 * (bot + top);
   const float kap = (float)M.kappa, kp1 = kap + 1.f;
-  const float eps = (float)((bot - top) / bot);
+  const float eps = (float)(bot - top) / (float)bot;
   const float num = -expm1f(kp1 * log1pf(-eps));
   const float q = num / (kp1 * eps);
   return bot * (double)expf(log1pf(q - 1.f) / kap);
@@ -585,8 +585,8 @@ __global__ void __launch_bounds__(CT_THREADS) k_set_p2etc_mixed(DevModel M, int 
     double h;
     if (k == nk) h = CT(HL, nk);
     else {
-      const double topwt = M.dsgth[2 * k], botwt = M.dsgth[2 * k + 2];
-      h = (topwt * CT(HL, k) + botwt * CT(HL, k + 1)) / (topwt + botwt);
+      const float topwt = (float)M.dsgth[2 * k], botwt = (float)M.dsgth[2 * k + 2];
+      h = (double)((topwt * (float)CT(HL, k) + botwt * (float)CT(HL, k + 1)) / (topwt + botwt));
     }
     M.h3[x] = h;
     if (k == 1) M.h3[c.base] = h;
@@ -632,24 +632,26 @@ __global__ void __launch_bounds__(CT_THREADS) k_pgrad_vars_column_mixed(DevModel
   double *P = sm, *R = P + 32 * L, *T3 = R + 32 * L, *GZ = T3 + 32 * L;
   float *LG = reinterpret_cast<float *>(GZ + 32 * L);
   const float kap = (float)M.kappa;
-  const double p0 = M.press0;
+  const float p0_inv = (float)(1. / M.press0);
+  const float mu_over_r = (float)(mu / 8.314472e+3);   // return_density: p mu / (R T)
   if (c.valid)
     for (int k = c.warp; k <= nk; k += CT_WARPS) {
       const long long x = c.base + k * n2;
       const double theta = M.theta[x], p = M.p3[x];
-      const double t3 = theta * (double)powf((float)(p / p0), kap);
+      const float pf = powf((float)p * p0_inv, kap);
+      const double t3 = theta * (double)pf;
       M.t3[x] = t3;
-      M.exner3[x] = M.cp * t3 / theta;
-      const double rho = return_density(p, t3, mu);
+      M.exner3[x] = M.cp * (double)pf;
+      const double rho = (double)((float)p * mu_over_r / (float)t3);
       M.rho3[x] = rho;
       CT(P, k) = p;
       CT(R, k) = rho;
       CT(T3, k) = t3;
       if (k >= 1) {
         const double pr = M.p2[x];
-        const double t2 = M.theta2[x] * (double)powf((float)(pr / p0), kap);
+        const double t2 = M.theta2[x] * (double)powf((float)pr * p0_inv, kap);
         M.t2[x] = t2;
-        const double r2 = return_density(pr, t2, mu);
+        const double r2 = (double)((float)pr * mu_over_r / (float)t2);
         M.rho2[x] = r2;
         if (k == 1) s_rho2_1[c.lane] = r2;
       }
@@ -668,8 +670,10 @@ __global__ void __launch_bounds__(CT_THREADS) k_pgrad_vars_column_mixed(DevModel
     for (int k = 2 + c.warp; k <= nk - 1; k += CT_WARPS) {
       const float dz10 = CT(LG, k), dz21 = CT(LG, k - 1), dz32 = CT(LG, k - 2);
       const float dz20 = dz21 + dz10, dz30 = dz32 + dz20, dz31 = dz32 + dz21;
-      const float df0 = (float)(CT(P, k + 1) / CT(R, k + 1)), df1 = (float)(CT(P, k) / CT(R, k));
-      const float df2 = (float)(CT(P, k - 1) / CT(R, k - 1)), df3 = (float)(CT(P, k - 2) / CT(R, k - 2));
+      // p/rho = R T / mu
+      const float r_over_mu = 1.f / mu_over_r;
+      const float df0 = r_over_mu * (float)CT(T3, k + 1), df1 = r_over_mu * (float)CT(T3, k);
+      const float df2 = r_over_mu * (float)CT(T3, k - 1), df3 = r_over_mu * (float)CT(T3, k - 2);
       CT(GZ, k - 1) = (double)(-(df0 * (dz21 * dz21 * dz21 * (dz31 + dz32)) / (dz10 * dz20 * dz30) +
                                  df1 * (dz21 * (dz21 * (dz21 + 2.f * (dz10 - dz31)) - 6.f * dz10 * dz31)) / (dz10 * dz31) +
                                  df2 * (dz21 * (dz21 * (dz21 + 2.f * (dz32 - dz20)) - 6.f * dz20 * dz32)) / (dz20 * dz32) +
@@ -704,7 +708,7 @@ __global__ void __launch_bounds__(CT_THREADS) k_pgrad_vars_column_mixed(DevModel
         const double dtg_inv = -1. / (M.dt * M.grav[2 * c.j + 1]);
         dz = (old - gzk) * dtg_inv;
       }
-      dz += M.w3[x] * M.h3[x] / CT(R, k);
+      dz += (double)((float)M.w3[x] * (float)M.h3[x] / (float)CT(R, k));
       M.dzdt3[x] = dz;
       if (gzk >= CT(GZ, k - 1)) flag_error(M.ctl, ERR_GZ_MONOTONE, k, c.j, c.i, gzk);
     }

@@ -167,153 +167,176 @@ __global__ void k_gz_pole_rows(DevModel M) {
   }
 }
 
-struct LonFace { double zbse, zbne, ztse, ztne, zbe, zte, pbe, pte, east, ln; };
+// The finite-volume force is a sum of face integrals that is unchanged when every GZ3 (or every
+// P2) of the stencil moves by one constant; the mixed form evaluates it in FP32 on
+// GZ3 - GZ3(k,j,i) and P2 - P2(k,j,i) (formed in FP64), which keeps the FP32 products near the
+// size of the differences the force is made of.  The FP64 form uses the values as they are.
+template <class R>
+struct PgradRef {
+  double z, p;
+  __device__ __forceinline__ PgradRef(const DevModel &M, int k, int j, int i) {
+    if (sizeof(R) == sizeof(double)) { z = 0.; p = 0.; }
+    else { z = M.gz3[M.at(k, j, i)]; p = M.p2[M.at(k, j, i)]; }
+  }
+};
+
+template <class R>
+struct LonFace { R zbse, zbne, ztse, ztne, zbe, zte, pbe, pte, east, ln; };
 
 // East face of the u control volume at column i (the quantities the reference carries
 // from one i to the next).
-__device__ __forceinline__ LonFace lon_face(const DevModel &M, int k, int j, int i) {
+template <class R>
+__device__ __forceinline__ LonFace<R> lon_face(const DevModel &M, const PgradRef<R> &ref, int k, int j, int i) {
   const double *G = M.gz3, *P = M.p2;
-  auto gz = [&](int kk, int jj, int ii) { return G[M.at(kk, jj, ii)]; };
-  LonFace f;
-  f.ln = M.lon[2 * i + 1] * (M_PI / 180.);
-  f.zbse = .25 * (gz(k, j, i) + gz(k, j - 1, i) + gz(k + 1, j, i) + gz(k + 1, j - 1, i));
-  f.zbne = .25 * (gz(k, j, i) + gz(k, j + 1, i) + gz(k + 1, j, i) + gz(k + 1, j + 1, i));
-  f.ztse = .25 * (gz(k, j, i) + gz(k, j - 1, i) + gz(k - 1, j, i) + gz(k - 1, j - 1, i));
-  f.ztne = .25 * (gz(k, j, i) + gz(k, j + 1, i) + gz(k - 1, j, i) + gz(k - 1, j + 1, i));
-  f.zbe = .5 * (gz(k, j, i) + gz(k + 1, j, i));
-  f.zte = .5 * (gz(k, j, i) + gz(k - 1, j, i));
-  f.pbe = P[M.at(k + 1, j, i)];
-  f.pte = P[M.at(k, j, i)];
-  const double a1 = f.ztne + f.ztse, b1 = f.ztne * f.ztse, a2 = f.zbne + f.zbse, b2 = f.zbne * f.zbse;
-  const double terms1 = a1 * a1 - b1 - (a2 * a2 - b2);
-  const double terms2 = 3. * (a1 - a2);
+  auto gz = [&](int kk, int jj, int ii) { return R(G[M.at(kk, jj, ii)] - ref.z); };
+  LonFace<R> f;
+  f.ln = R(M.lon[2 * i + 1] * (M_PI / 180.));
+  f.zbse = R(.25) * (gz(k, j, i) + gz(k, j - 1, i) + gz(k + 1, j, i) + gz(k + 1, j - 1, i));
+  f.zbne = R(.25) * (gz(k, j, i) + gz(k, j + 1, i) + gz(k + 1, j, i) + gz(k + 1, j + 1, i));
+  f.ztse = R(.25) * (gz(k, j, i) + gz(k, j - 1, i) + gz(k - 1, j, i) + gz(k - 1, j - 1, i));
+  f.ztne = R(.25) * (gz(k, j, i) + gz(k, j + 1, i) + gz(k - 1, j, i) + gz(k - 1, j + 1, i));
+  f.zbe = R(.5) * (gz(k, j, i) + gz(k + 1, j, i));
+  f.zte = R(.5) * (gz(k, j, i) + gz(k - 1, j, i));
+  f.pbe = R(P[M.at(k + 1, j, i)] - ref.p);
+  f.pte = R(P[M.at(k, j, i)] - ref.p);
+  const R a1 = f.ztne + f.ztse, b1 = f.ztne * f.ztse, a2 = f.zbne + f.zbse, b2 = f.zbne * f.zbse;
+  const R terms1 = a1 * a1 - b1 - (a2 * a2 - b2);
+  const R terms2 = R(3.) * (a1 - a2);
   f.east = (-terms1 * (f.pbe - f.pte) + terms2 * (f.zte * f.pbe - f.zbe * f.pte)) / (f.zte - f.zbe);
   return f;
 }
 
+template <class R>
 __global__ void k_pgrad_lon(DevModel M) {
   epic_member(M);
   Cell c;
   if (!cell3(M, 1, M.nk - 1, 0, M.nj + 1, c)) return;
   const int k = c.k, j = c.j, i = c.i;
-  const double DLOGZ_TOL = 1.e-2;
-  const LonFace w = lon_face(M, k, j, i - 1), e = lon_face(M, k, j, i);
-  const double rho = .5 * (M.rho3[M.at(k, j, i)] + M.rho3[M.at(k, j, i - 1)]);
-  const double rlns = M.rln[2 * j], rlnn = M.rln[2 * j + 2];
-  double a1 = e.ztne + e.ztse, a2 = w.ztne + w.ztse;
-  double terms2 = 3. * (a1 - a2), top, bottom;
-  if (fabs(2. * (e.zte - w.zte) / (e.zte + w.zte - e.zbe - w.zbe)) > DLOGZ_TOL) {
-    const double b1 = e.ztne * e.ztse, b2 = w.ztne * w.ztse;
-    const double terms1 = a1 * a1 - b1 - (a2 * a2 - b2);
+  const R DLOGZ_TOL = R(1.e-2);
+  const PgradRef<R> ref(M, k, j, i);
+  const LonFace<R> w = lon_face<R>(M, ref, k, j, i - 1), e = lon_face<R>(M, ref, k, j, i);
+  const R rho = R(.5) * (R(M.rho3[M.at(k, j, i)]) + R(M.rho3[M.at(k, j, i - 1)]));
+  const R rlns = R(M.rln[2 * j]), rlnn = R(M.rln[2 * j + 2]);
+  R a1 = e.ztne + e.ztse, a2 = w.ztne + w.ztse;
+  R terms2 = R(3.) * (a1 - a2), top, bottom;
+  if (fabs(R(2.) * (e.zte - w.zte) / (e.zte + w.zte - e.zbe - w.zbe)) > DLOGZ_TOL) {
+    const R b1 = e.ztne * e.ztse, b2 = w.ztne * w.ztse;
+    const R terms1 = a1 * a1 - b1 - (a2 * a2 - b2);
     top = (-terms1 * (w.pte - e.pte) + terms2 * (e.zte * w.pte - w.zte * e.pte)) / (e.zte - w.zte);
   } else {
-    top = .5 * (w.pte + e.pte) * terms2;
+    top = R(.5) * (w.pte + e.pte) * terms2;
   }
   a1 = e.zbne + e.zbse;
   a2 = w.zbne + w.zbse;
-  terms2 = 3. * (a1 - a2);
-  if (fabs(2. * (e.zbe - w.zbe) / (e.zte + w.zte - e.zbe - w.zbe)) > DLOGZ_TOL) {
-    const double b1 = e.zbne * e.zbse, b2 = w.zbne * w.zbse;
-    const double terms1 = a1 * a1 - b1 - (a2 * a2 - b2);
+  terms2 = R(3.) * (a1 - a2);
+  if (fabs(R(2.) * (e.zbe - w.zbe) / (e.zte + w.zte - e.zbe - w.zbe)) > DLOGZ_TOL) {
+    const R b1 = e.zbne * e.zbse, b2 = w.zbne * w.zbse;
+    const R terms1 = a1 * a1 - b1 - (a2 * a2 - b2);
     bottom = (-terms1 * (w.pbe - e.pbe) + terms2 * (e.zbe * w.pbe - w.zbe * e.pbe)) / (e.zbe - w.zbe);
   } else {
-    bottom = .5 * (w.pbe + e.pbe) * terms2;
+    bottom = R(.5) * (w.pbe + e.pbe) * terms2;
   }
-  double pgflon = top - bottom + 0. - 0. + w.east - e.east;
-  const double dzn = e.ztne - e.zbne + w.ztne - w.zbne;
-  const double dzs = e.ztse - e.zbse + w.ztse - w.zbse;
-  pgflon /= (e.ln - w.ln) * rho * (rlns * (dzs + .5 * dzn) + rlnn * (dzn + .5 * dzs));
-  M.dudt[plane_offset(M, PL_UV_TEND) + M.at(k, j, i)] += pgflon;
+  R pgflon = top - bottom + R(0.) - R(0.) + w.east - e.east;
+  const R dzn = e.ztne - e.zbne + w.ztne - w.zbne;
+  const R dzs = e.ztse - e.zbse + w.ztse - w.zbse;
+  pgflon /= (e.ln - w.ln) * rho * (rlns * (dzs + R(.5) * dzn) + rlnn * (dzn + R(.5) * dzs));
+  const long long x = plane_offset(M, PL_UV_TEND) + M.at(k, j, i);
+  M.dudt[x] = M.dudt[x] + (double)pgflon;
 }
 
-struct LatFace { double zbnw, zbne, ztnw, ztne, zbn, ztn, pbn, ptn, north, rln, lt; };
+template <class R>
+struct LatFace { R zbnw, zbne, ztnw, ztne, zbn, ztn, pbn, ptn, north, rln, lt; };
 
 // North face of the v control volume at row j.
-__device__ __forceinline__ LatFace lat_face(const DevModel &M, int k, int j, int i) {
+template <class R>
+__device__ __forceinline__ LatFace<R> lat_face(const DevModel &M, const PgradRef<R> &ref, int k, int j, int i) {
   const double *G = M.gz3, *P = M.p2;
-  auto gz = [&](int kk, int jj, int ii) { return G[M.at(kk, jj, ii)]; };
-  LatFace f;
-  f.rln = M.rln[2 * j + 1];
-  f.lt = M.lat[2 * j + 1] * (M_PI / 180.);
-  f.zbnw = .25 * (gz(k, j, i) + gz(k, j, i - 1) + gz(k + 1, j, i) + gz(k + 1, j, i - 1));
-  f.zbne = .25 * (gz(k, j, i) + gz(k, j, i + 1) + gz(k + 1, j, i) + gz(k + 1, j, i + 1));
-  f.ztnw = .25 * (gz(k, j, i) + gz(k, j, i - 1) + gz(k - 1, j, i) + gz(k - 1, j, i - 1));
-  f.ztne = .25 * (gz(k, j, i) + gz(k, j, i + 1) + gz(k - 1, j, i) + gz(k - 1, j, i + 1));
-  f.zbn = .5 * (gz(k, j, i) + gz(k + 1, j, i));
-  f.ztn = .5 * (gz(k, j, i) + gz(k - 1, j, i));
-  f.pbn = P[M.at(k + 1, j, i)];
-  f.ptn = P[M.at(k, j, i)];
-  const double a1 = f.ztne + f.ztnw, b1 = f.ztne * f.ztnw, a2 = f.zbne + f.zbnw, b2 = f.zbne * f.zbnw;
-  const double terms1 = a1 * a1 - b1 - (a2 * a2 - b2);
-  const double terms2 = 3. * (a1 - a2);
+  auto gz = [&](int kk, int jj, int ii) { return R(G[M.at(kk, jj, ii)] - ref.z); };
+  LatFace<R> f;
+  f.rln = R(M.rln[2 * j + 1]);
+  f.lt = R(M.lat[2 * j + 1] * (M_PI / 180.));
+  f.zbnw = R(.25) * (gz(k, j, i) + gz(k, j, i - 1) + gz(k + 1, j, i) + gz(k + 1, j, i - 1));
+  f.zbne = R(.25) * (gz(k, j, i) + gz(k, j, i + 1) + gz(k + 1, j, i) + gz(k + 1, j, i + 1));
+  f.ztnw = R(.25) * (gz(k, j, i) + gz(k, j, i - 1) + gz(k - 1, j, i) + gz(k - 1, j, i - 1));
+  f.ztne = R(.25) * (gz(k, j, i) + gz(k, j, i + 1) + gz(k - 1, j, i) + gz(k - 1, j, i + 1));
+  f.zbn = R(.5) * (gz(k, j, i) + gz(k + 1, j, i));
+  f.ztn = R(.5) * (gz(k, j, i) + gz(k - 1, j, i));
+  f.pbn = R(P[M.at(k + 1, j, i)] - ref.p);
+  f.ptn = R(P[M.at(k, j, i)] - ref.p);
+  const R a1 = f.ztne + f.ztnw, b1 = f.ztne * f.ztnw, a2 = f.zbne + f.zbnw, b2 = f.zbne * f.zbnw;
+  const R terms1 = a1 * a1 - b1 - (a2 * a2 - b2);
+  const R terms2 = R(3.) * (a1 - a2);
   f.north = f.rln * (-terms1 * (f.pbn - f.ptn) + terms2 * (f.ztn * f.pbn - f.zbn * f.ptn)) / (f.ztn - f.zbn);
   return f;
 }
 
+template <class R>
 __global__ void k_pgrad_lat(DevModel M) {
   epic_member(M);
   Cell c;
   if (!cell3(M, 1, M.nk - 1, 1, M.nj, c)) return;
   const int k = c.k, j = c.j, i = c.i;
-  const double DLOGZ_TOL = 1.e-2;
-  const LatFace s = lat_face(M, k, j - 1, i), n = lat_face(M, k, j, i);
+  const R DLOGZ_TOL = R(1.e-2);
+  const PgradRef<R> ref(M, k, j, i);
+  const LatFace<R> s = lat_face<R>(M, ref, k, j - 1, i), n = lat_face<R>(M, ref, k, j, i);
   const double *G = M.gz3, *P = M.p2;
-  auto gz = [&](int kk, int jj, int ii) { return G[M.at(kk, jj, ii)]; };
-  auto pp = [&](int kk, int jj, int ii) { return P[M.at(kk, jj, ii)]; };
-  const double rho = .5 * (M.rho3[M.at(k, j, i)] + M.rho3[M.at(k, j - 1, i)]);
-  const double rlt = M.rlt[2 * j];
-  const double rlns = s.rln, rlnn = n.rln;
-  const double south = s.north, north = n.north;
+  auto gz = [&](int kk, int jj, int ii) { return R(G[M.at(kk, jj, ii)] - ref.z); };
+  auto pp = [&](int kk, int jj, int ii) { return R(P[M.at(kk, jj, ii)] - ref.p); };
+  const R rho = R(.5) * (R(M.rho3[M.at(k, j, i)]) + R(M.rho3[M.at(k, j - 1, i)]));
+  const R rlt = R(M.rlt[2 * j]);
+  const R rlns = s.rln, rlnn = n.rln;
+  const R south = s.north, north = n.north;
   // s-face values carried over from row j-1: zbsw = zbnw(j-1), zbse = zbne(j-1), ...
-  const double zbsw = s.zbnw, zbse = s.zbne, ztsw = s.ztnw, ztse = s.ztne;
-  const double zbs = s.zbn, zts = s.ztn, pbs = s.pbn, pts = s.ptn;
-  double a1, a2, b1, b2, b3, terms1, terms2;
-  const double zbe = .125 * (gz(k, j, i) + gz(k, j, i + 1) + gz(k, j - 1, i) + gz(k, j - 1, i + 1) + gz(k + 1, j, i) +
-                             gz(k + 1, j, i + 1) + gz(k + 1, j - 1, i) + gz(k + 1, j - 1, i + 1));
-  const double zte = .125 * (gz(k - 1, j, i) + gz(k - 1, j, i + 1) + gz(k - 1, j - 1, i) + gz(k - 1, j - 1, i + 1) + gz(k, j, i) +
-                             gz(k, j, i + 1) + gz(k, j - 1, i) + gz(k, j - 1, i + 1));
-  const double pbe = .25 * (pp(k + 1, j, i) + pp(k + 1, j, i + 1) + pp(k + 1, j - 1, i) + pp(k + 1, j - 1, i + 1));
-  const double pte = .25 * (pp(k, j, i) + pp(k, j, i + 1) + pp(k, j - 1, i) + pp(k, j - 1, i + 1));
+  const R zbsw = s.zbnw, zbse = s.zbne, ztsw = s.ztnw, ztse = s.ztne;
+  const R zbs = s.zbn, zts = s.ztn, pbs = s.pbn, pts = s.ptn;
+  R a1, a2, b1, b2, b3, terms1, terms2;
+  const R zbe = R(.125) * (gz(k, j, i) + gz(k, j, i + 1) + gz(k, j - 1, i) + gz(k, j - 1, i + 1) + gz(k + 1, j, i) +
+                           gz(k + 1, j, i + 1) + gz(k + 1, j - 1, i) + gz(k + 1, j - 1, i + 1));
+  const R zte = R(.125) * (gz(k - 1, j, i) + gz(k - 1, j, i + 1) + gz(k - 1, j - 1, i) + gz(k - 1, j - 1, i + 1) + gz(k, j, i) +
+                           gz(k, j, i + 1) + gz(k, j - 1, i) + gz(k, j - 1, i + 1));
+  const R pbe = R(.25) * (pp(k + 1, j, i) + pp(k + 1, j, i + 1) + pp(k + 1, j - 1, i) + pp(k + 1, j - 1, i + 1));
+  const R pte = R(.25) * (pp(k, j, i) + pp(k, j, i + 1) + pp(k, j - 1, i) + pp(k, j - 1, i + 1));
   a1 = n.ztne + ztse; b1 = n.ztne * ztse; a2 = n.zbne + zbse; b2 = n.zbne * zbse;
   terms1 = a1 * a1 - b1 - (a2 * a2 - b2);
-  terms2 = 3. * (a1 - a2);
-  const double east = .5 * (rlns - rlnn) * (-terms1 * (pbe - pte) + terms2 * (zte * pbe - zbe * pte)) / (zte - zbe);
-  const double zbw = .125 * (gz(k, j, i) + gz(k, j, i - 1) + gz(k, j - 1, i) + gz(k, j - 1, i - 1) + gz(k + 1, j, i) +
-                             gz(k + 1, j, i - 1) + gz(k + 1, j - 1, i) + gz(k + 1, j - 1, i - 1));
-  const double ztw = .125 * (gz(k - 1, j, i) + gz(k - 1, j, i - 1) + gz(k - 1, j - 1, i) + gz(k - 1, j - 1, i - 1) + gz(k, j, i) +
-                             gz(k, j, i - 1) + gz(k, j - 1, i) + gz(k, j - 1, i - 1));
-  const double pbw = .25 * (pp(k + 1, j, i) + pp(k + 1, j, i - 1) + pp(k + 1, j - 1, i) + pp(k + 1, j - 1, i - 1));
-  const double ptw = .25 * (pp(k, j, i) + pp(k, j, i - 1) + pp(k, j - 1, i) + pp(k, j - 1, i - 1));
+  terms2 = R(3.) * (a1 - a2);
+  const R east = R(.5) * (rlns - rlnn) * (-terms1 * (pbe - pte) + terms2 * (zte * pbe - zbe * pte)) / (zte - zbe);
+  const R zbw = R(.125) * (gz(k, j, i) + gz(k, j, i - 1) + gz(k, j - 1, i) + gz(k, j - 1, i - 1) + gz(k + 1, j, i) +
+                           gz(k + 1, j, i - 1) + gz(k + 1, j - 1, i) + gz(k + 1, j - 1, i - 1));
+  const R ztw = R(.125) * (gz(k - 1, j, i) + gz(k - 1, j, i - 1) + gz(k - 1, j - 1, i) + gz(k - 1, j - 1, i - 1) + gz(k, j, i) +
+                           gz(k, j, i - 1) + gz(k, j - 1, i) + gz(k, j - 1, i - 1));
+  const R pbw = R(.25) * (pp(k + 1, j, i) + pp(k + 1, j, i - 1) + pp(k + 1, j - 1, i) + pp(k + 1, j - 1, i - 1));
+  const R ptw = R(.25) * (pp(k, j, i) + pp(k, j, i - 1) + pp(k, j - 1, i) + pp(k, j - 1, i - 1));
   a1 = n.ztnw + ztsw; b1 = n.ztnw * ztsw; a2 = n.zbnw + zbsw; b2 = n.zbnw * zbsw;
   terms1 = a1 * a1 - b1 - (a2 * a2 - b2);
-  terms2 = 3. * (a1 - a2);
-  const double west = .5 * (rlns - rlnn) * (-terms1 * (pbw - ptw) + terms2 * (ztw * pbw - zbw * ptw)) / (ztw - zbw);
-  double top, bottom;
+  terms2 = R(3.) * (a1 - a2);
+  const R west = R(.5) * (rlns - rlnn) * (-terms1 * (pbw - ptw) + terms2 * (ztw * pbw - zbw * ptw)) / (ztw - zbw);
+  R top, bottom;
   a1 = n.ztne + n.ztnw; a2 = ztse + ztsw;
-  terms2 = 3. * (a1 - a2);
-  if (fabs(2. * (n.ztn - zts) / (n.ztn + zts - n.zbn - zbs)) > DLOGZ_TOL) {
+  terms2 = R(3.) * (a1 - a2);
+  if (fabs(R(2.) * (n.ztn - zts) / (n.ztn + zts - n.zbn - zbs)) > DLOGZ_TOL) {
     b1 = n.ztne * n.ztnw; b2 = ztse * ztsw; b3 = n.ztne * ztse + n.ztnw * ztsw;
     terms1 = a1 * a1 - b1 - (a2 * a2 - b2);
-    top = .5 * ((n.ptn - pts) * ((rlnn + rlns) * terms1 + (rlnn - rlns) * (b1 + b2 - b3)) + (rlnn + rlns) * terms2 * (n.ztn * pts - zts * n.ptn)) /
+    top = R(.5) * ((n.ptn - pts) * ((rlnn + rlns) * terms1 + (rlnn - rlns) * (b1 + b2 - b3)) + (rlnn + rlns) * terms2 * (n.ztn * pts - zts * n.ptn)) /
           (n.ztn - zts);
   } else {
-    top = .25 * (rlnn + rlns) * (pts + n.ptn) * terms2;
+    top = R(.25) * (rlnn + rlns) * (pts + n.ptn) * terms2;
   }
   a1 = n.zbne + n.zbnw; a2 = zbse + zbsw;
-  terms2 = 3. * (a1 - a2);
-  if (fabs(2. * (n.zbn - zbs) / (n.ztn + zts - n.zbn - zbs)) > DLOGZ_TOL) {
+  terms2 = R(3.) * (a1 - a2);
+  if (fabs(R(2.) * (n.zbn - zbs) / (n.ztn + zts - n.zbn - zbs)) > DLOGZ_TOL) {
     b1 = n.zbne * n.zbnw; b2 = zbse * zbsw; b3 = n.zbne * zbse + n.zbnw * zbsw;
     terms1 = a1 * a1 - b1 - (a2 * a2 - b2);
-    bottom = .5 * ((n.pbn - pbs) * ((rlnn + rlns) * terms1 + (rlnn - rlns) * (b1 + b2 - b3)) + (rlnn + rlns) * terms2 * (n.zbn * pbs - zbs * n.pbn)) /
+    bottom = R(.5) * ((n.pbn - pbs) * ((rlnn + rlns) * terms1 + (rlnn - rlns) * (b1 + b2 - b3)) + (rlnn + rlns) * terms2 * (n.zbn * pbs - zbs * n.pbn)) /
              (n.zbn - zbs);
   } else {
-    bottom = .25 * (rlnn + rlns) * (pbs + n.pbn) * terms2;
+    bottom = R(.25) * (rlnn + rlns) * (pbs + n.pbn) * terms2;
   }
-  double pgflat = top - bottom + south - (north + west + east);
-  const double dzn = n.ztne - n.zbne + n.ztnw - n.zbnw;
-  const double dzs = ztse - zbse + ztsw - zbsw;
-  pgflat /= (n.lt - s.lt) * rho * rlt * (rlns * (dzs + .5 * dzn) + rlnn * (dzn + .5 * dzs));
-  M.dvdt[plane_offset(M, PL_UV_TEND) + M.at(k, j, i)] += pgflat;
+  R pgflat = top - bottom + south - (north + west + east);
+  const R dzn = n.ztne - n.zbne + n.ztnw - n.zbnw;
+  const R dzs = ztse - zbse + ztsw - zbsw;
+  pgflat /= (n.lt - s.lt) * rho * rlt * (rlns * (dzs + R(.5) * dzn) + rlnn * (dzn + R(.5) * dzs));
+  const long long x = plane_offset(M, PL_UV_TEND) + M.at(k, j, i);
+  M.dvdt[x] = M.dvdt[x] + (double)pgflat;
 }
 
 // ---------------------------------------------------------------------------------------------
@@ -447,71 +470,71 @@ __global__ void k_visc_apply(DevModel M, double *A, int sel, const double *D, in
   write_with_pads(A, M, M.at(c.k, c.j, 0), c.i, A[x] + (double)(R(M.dt) * R(sign) * R(D[x])));
 }
 
-// zonal_hyperviscosity for one row (block), epic_subgrid.c:715-808.  The updated row stays in
-// FP64 in both forms.  The FP64 form sums the row mean in the reference's order on one thread;
-// the mixed form sums it in FP64 with a block reduction.
+// zonal_hyperviscosity, epic_subgrid.c:715-808: one warp per row (j, k), rows_per_block rows
+// per block.  The updated row stays in FP64 in both forms.  The FP64 form sums the row mean in
+// the reference's order on lane 0; the mixed form sums it in FP64 with a warp reduction.
 template <class R>
 __global__ void k_zonal_visc(DevModel M, double *A, int sel, int jbot, int jhalf, int k0) {
   epic_member(M, A);
   extern __shared__ __align__(16) unsigned char smraw[];
-  const int ni = M.ni;
-  const int j = jbot + (int)blockIdx.x;
+  const int ni = M.ni, lane = (int)(threadIdx.x & 31), w = (int)(threadIdx.x >> 5), nw = (int)(blockDim.x >> 5);
+  const int j = jbot + (int)blockIdx.x * nw + w;
   const int k = k0 + (int)blockIdx.y;
+  if (j > M.nj) return;
   A += plane_offset(M, sel);
   const long long base = M.at(k, j, 0);
-  double *a = reinterpret_cast<double *>(smraw);
+  const size_t row_bytes = (size_t)(ni + 2) * (sizeof(double) + 2 * sizeof(R));
+  double *a = reinterpret_cast<double *>(smraw + w * row_bytes);
   R *hh = reinterpret_cast<R *>(a + (ni + 2)), *d = hh + (ni + 2);
-  __shared__ R mean;
-  __shared__ double part[32];
-  for (int i = threadIdx.x; i <= ni + 1; i += blockDim.x) { a[i] = A[base + i]; hh[i] = R(a[i]); }
-  __syncthreads();
+  const unsigned full = 0xffffffffu;
+  for (int i = lane; i <= ni + 1; i += 32) { a[i] = A[base + i]; hh[i] = R(a[i]); }
+  __syncwarp();
   const bool taper = fabs(M.lat[2 * j + jhalf]) > M.lat0;
   const double mm = M.m[2 * j + jhalf];
   R sign = R(1.);
   bool any_applied = false;
   for (int itmp = 2; itmp <= 8; itmp += 2) {
     const R dc = R(taper ? M.coef[itmp] * M.m0 * M.m0 : M.coef[itmp] * mm * mm);
-    for (int i = threadIdx.x + 1; i <= ni; i += blockDim.x) d[i] = dc * (hh[i - 1] - R(2.) * hh[i] + hh[i + 1]);
-    __syncthreads();
+    for (int i = lane + 1; i <= ni; i += 32) d[i] = dc * (hh[i - 1] - R(2.) * hh[i] + hh[i + 1]);
+    __syncwarp();
+    R mean;
     if (sizeof(R) == sizeof(double)) {
-      if (threadIdx.x == 0) {
+      double mv = 0.;
+      if (lane == 0) {
         d[ni + 1] = d[1];
         d[0] = d[ni];
         double fm = 0.;
         for (int i = 1; i <= ni; i++) fm += d[i];
-        mean = R(fm / ni);
+        mv = fm / ni;
       }
+      mean = R(__shfl_sync(full, mv, 0));
     } else {
       double fm = 0.;
-      for (int i = threadIdx.x + 1; i <= ni; i += blockDim.x) fm += (double)d[i];
-      for (int o = 16; o > 0; o >>= 1) fm += __shfl_xor_sync(0xffffffffu, fm, o);
-      if ((threadIdx.x & 31) == 0) part[threadIdx.x >> 5] = fm;
-      __syncthreads();
-      if (threadIdx.x == 0) {
-        double t = 0.;
-        for (int w = 0; w < (int)(blockDim.x >> 5); w++) t += part[w];
-        mean = R(t / ni);
+      for (int i = lane + 1; i <= ni; i += 32) fm += (double)d[i];
+      for (int o = 16; o > 0; o >>= 1) fm += __shfl_xor_sync(full, fm, o);
+      mean = R(fm / ni);
+      if (lane == 0) {
         d[ni + 1] = d[1];
         d[0] = d[ni];
       }
     }
-    __syncthreads();
-    for (int i = threadIdx.x; i <= ni + 1; i += blockDim.x) d[i] -= mean;
-    __syncthreads();
+    __syncwarp();
+    for (int i = lane; i <= ni + 1; i += 32) d[i] -= mean;
+    __syncwarp();
     if (M.nu[itmp] > 0.) {
-      for (int i = threadIdx.x + 1; i <= ni; i += blockDim.x) a[i] += (double)(R(M.dt) * sign * d[i]);
+      for (int i = lane + 1; i <= ni; i += 32) a[i] += (double)(R(M.dt) * sign * d[i]);
       any_applied = true;
     }
     sign = -sign;
     double rest = 0.;
     for (int q = itmp + 2; q <= 8; q += 2) rest += M.nu[q];
     if (!(rest > 0.)) break;
-    for (int i = threadIdx.x; i <= ni + 1; i += blockDim.x) hh[i] = d[i];   // swap roles
-    __syncthreads();
+    for (int i = lane; i <= ni + 1; i += 32) hh[i] = d[i];   // swap roles
+    __syncwarp();
   }
-  __syncthreads();
+  __syncwarp();
   if (any_applied)
-    for (int i = threadIdx.x + 1; i <= ni; i += blockDim.x) write_with_pads(A, M, base, i, a[i]);
+    for (int i = lane + 1; i <= ni; i += 32) write_with_pads(A, M, base, i, a[i]);
 }
 
 // ---------------------------------------------------------------------------------------------
@@ -758,8 +781,8 @@ int launch_uv_core(const DevModel &M, cudaStream_t s) {
 
 int launch_uv_pgrad(const DevModel &M, cudaStream_t s) {
   k_gz_pole_rows<<<zg(M.nk + 1, M), 128, 0, s>>>(M);
-  k_pgrad_lon<<<zg(cells_blocks(M, M.nk - 1, M.nj + 1, 128), M), 128, 0, s>>>(M);
-  k_pgrad_lat<<<zg(cells_blocks(M, M.nk - 1, M.nj, 128), M), 128, 0, s>>>(M);
+  EPIC_LAUNCH_R(M.mixed, k_pgrad_lon, cells_blocks(M, M.nk - 1, M.nj + 1, 128), 128, 0, s, M);
+  EPIC_LAUNCH_R(M.mixed, k_pgrad_lat, cells_blocks(M, M.nk - 1, M.nj, 128), 128, 0, s, M);
   return 0;
 }
 
@@ -819,9 +842,12 @@ int launch_zonal_hyperviscosity(const DevModel &M, int index, double *var, int s
   int k0, k1;
   visc_krange(M, index, k0, k1);
   const int jbot = index == 1 ? 1 : 0, jhalf = index == 1 ? 0 : 1;
-  dim3 grid(M.nj - jbot + 1, k1 - k0 + 1);
-  const size_t smem = (size_t)(M.ni + 2) * (sizeof(double) + 2 * (M.mixed ? sizeof(float) : sizeof(double)));
-  EPIC_LAUNCH_R(M.mixed, k_zonal_visc, grid, M.ni >= 256 ? 128 : 64, smem, s, M, var, sel, jbot, jhalf, k0);
+  const size_t row_bytes = (size_t)(M.ni + 2) * (sizeof(double) + 2 * (M.mixed ? sizeof(float) : sizeof(double)));
+  int rows = (int)((40 * 1024) / row_bytes);
+  rows = rows < 1 ? 1 : (rows > 4 ? 4 : rows);
+  const int nrows = M.nj - jbot + 1;
+  dim3 grid((nrows + rows - 1) / rows, k1 - k0 + 1);
+  EPIC_LAUNCH_R(M.mixed, k_zonal_visc, grid, 32 * rows, rows * row_bytes, s, M, var, sel, jbot, jhalf, k0);
   return 0;
 }
 
