@@ -354,7 +354,12 @@ def run_gpu_ensemble(args):
     cfg = _workload_cfg(args.workload)
     nmem = args.members or ENSEMBLE[args.workload]
     members = _members(cfg, nmem, precision, torch_seed=7 + rank)
+    starts = [m.download() for m in members]
     batch = Batch(members)
+    # launch shapes: autotuned on this batch, then every member goes back to its initial state
+    tuning = batch.autotune(trial_steps=2)
+    for m, f in zip(members, starts):
+        m.upload(f)
     batch.timestep(EPIC_SYNC_DIAGS_ONLY)
     for _ in range(args.warmup):
         batch.run(1)
@@ -423,6 +428,9 @@ def run_gpu_ensemble(args):
                                    f"seeded 0.1 K noise and +/-10% k_f per member, {args.precision} form, one launch per "
                                    f"kernel for all members", "ni": cfg.ni, "nj": cfg.nj, "nk": cfg.nk, "dt": cfg.dt,
                        "members": nmem, "precision": args.precision, "parallelism": f"replicas{ws}",
+                       "launch_shapes": {"autotuned_block_sizes": tuning,
+                                         "groups": ["uv_core", "pgrad", "hsu_meridional", "hyperviscosity", "diagnostics",
+                                                    "update", "column", "pointwise", "row_filter"]},
                        "l2": f"ensemble state {state_gb:.1f} GB > 129 MB L2; no flush needed",
                        "state": "horizontally uniform HS equilibrium column at rest + seeded 0.1 K theta noise"},
             "clocks": clocks,

@@ -21,6 +21,7 @@ from .abi import (EPIC_PREC_FP64, EPIC_PREC_MIXED, EPIC_STEP_PROGS_AND_SYNC_DIAG
                   EPIC_UV_AB3, EPIC_UV_LEAPFROG, EpicFields, EpicGrid, EpicHsParams, Fields, GridArrays,
                   HSConfig, Layout)
 
+TUNE_GROUPS = 9   # EPIC_TUNE_GROUPS
 _HERE = os.path.dirname(os.path.abspath(__file__))
 LIB_PATH = os.path.join(_HERE, "_lib", "libepic_gb300.so")
 _lib = None
@@ -69,6 +70,9 @@ def load_library(path: str | None = None) -> C.CDLL:
     lib.epic_batch_stream.restype = C.c_void_p
     lib.epic_batch_kernels_per_step.argtypes = [C.c_void_p]
     lib.epic_batch_kernels_per_step.restype = C.c_int32
+    lib.epic_batch_autotune.argtypes = [C.c_void_p, C.c_int32, C.POINTER(C.c_int32)]
+    for name in ("epic_batch_set_tuning", "epic_model_set_tuning"):
+        getattr(lib, name).argtypes = [C.c_void_p, C.POINTER(C.c_int32)]
     lib.epic_hs_grid_build.argtypes = [C.POINTER(EpicHsParams), C.POINTER(EpicGrid), C.POINTER(C.c_double),
                                        C.POINTER(C.c_double)]
     lib.epic_hs_initial_state.argtypes = [C.POINTER(EpicGrid), C.POINTER(EpicHsParams), C.c_uint64, C.c_double,
@@ -149,6 +153,11 @@ class Model:
         """run_stage(10) with the filter's profile tables in the library's fixed device array."""
         _check(self.lib.epic_model_filter_mass_noalloc(self._h), "epic_model_filter_mass_noalloc")
 
+    def set_tuning(self, table: list[int]) -> None:
+        """Launch shapes from Batch.autotune (block size per kernel group; 0 = built-in)."""
+        arr = (C.c_int32 * TUNE_GROUPS)(*table)
+        _check(self.lib.epic_model_set_tuning(self._h, arr), "epic_model_set_tuning")
+
     def step_host(self, f: Fields, nsteps: int, prime: bool = False) -> None:
         _check(self.lib.epic_model_step_host(self._h, C.byref(f.struct), int(prime), nsteps), "epic_model_step_host")
 
@@ -196,6 +205,16 @@ class Batch:
 
     def run_stage(self, stage: int) -> None:
         _check(self.lib.epic_batch_run_stage(self._h, stage), "epic_batch_run_stage")
+
+    def autotune(self, trial_steps: int = 3) -> list[int]:
+        """Pick the block size of each kernel group by timing whole steps (advances the state)."""
+        arr = (C.c_int32 * TUNE_GROUPS)()
+        _check(self.lib.epic_batch_autotune(self._h, trial_steps, arr), "epic_batch_autotune")
+        return list(arr)
+
+    def set_tuning(self, table: list[int]) -> None:
+        arr = (C.c_int32 * TUNE_GROUPS)(*table)
+        _check(self.lib.epic_batch_set_tuning(self._h, arr), "epic_batch_set_tuning")
 
     def sync(self) -> None:
         _check(self.lib.epic_batch_sync(self._h), "epic_batch_sync")

@@ -8,6 +8,10 @@
 #include <cfloat>
 #include "dd_math.cuh"
 
+// kernel groups whose block size the autotuner picks (DevModel::tb)
+enum TuneGroup { TB_UV_CORE = 0, TB_PGRAD, TB_HSU, TB_VISC, TB_DIAG, TB_UPDATE, TB_COLUMN, TB_POINT, TB_ROW, TB_COUNT };
+#define TB(M, g) ((M).tb[g] > 0 ? (M).tb[g] : 128)
+
 #define EPIC_MAX_NK 126      // column kernels keep per-column arrays of nk+2 entries
 #define EPIC_MAX_NI 1024     // row kernels keep one row of ni entries in shared memory
 
@@ -60,6 +64,9 @@ struct DevModel {
   const DevModel *batch;
   int nbatch;
   char *pool_base;   // start of the model's device pool (state, scratch and tables)
+  // launch shapes (host side only): threads per block of each kernel group, set by the
+  // autotuner; they change no result (every tuned kernel is pointwise or per row)
+  int tb[9];
 
   __host__ __device__ __forceinline__ long long at(int k, int j, int i) const {
     return (long long)i + (long long)(j + 1) * iadim + (long long)k * n2;

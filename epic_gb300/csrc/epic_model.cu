@@ -745,3 +745,68 @@ extern "C" void *epic_batch_stream(epic_batch *b) { return b ? (void *)b->stream
 
 extern "C" int32_t epic_batch_kernels_per_step(const epic_batch *b) { return b ? b->kernels_per_step : -1; }
 
+// ---- autotuning of launch shapes ----
+//
+// For each kernel group (DevModel::tb) in turn, time whole steps of the batch with each candidate
+// block size, the other groups at their best so far, and keep the fastest.  Every tuned kernel
+// is pointwise or per row, so the choice changes no result.  The trial steps advance the
+// members' state: tune before uploading the state a run starts from, or on scratch members.
+
+extern "C" int epic_batch_autotune(epic_batch *b, int32_t trial_steps, int32_t *table_out) {
+  int rc = batch_ready(b, "epic_batch_autotune");
+  if (rc) return rc;
+  if (trial_steps < 1) trial_steps = 1;
+  cudaEvent_t e0 = nullptr, e1 = nullptr;
+  EPIC_CUDA_CHECK(cudaEventCreate(&e0));
+  EPIC_CUDA_CHECK(cudaEventCreate(&e1));
+  auto time_steps = [&](float *ms) -> int {
+    int r = enqueue_step_on(b->d, b->stream);   // warm-up step for this shape
+    if (r) return r;
+    cudaEventRecord(e0, b->stream);
+    for (int q = 0; q < trial_steps && !r; q++) r = enqueue_step_on(b->d, b->stream);
+    cudaEventRecord(e1, b->stream);
+    if (r) return r;
+    EPIC_CUDA_CHECK(cudaEventSynchronize(e1));
+    EPIC_CUDA_CHECK(cudaEventElapsedTime(ms, e0, e1));
+    return check_launch("epic_batch_autotune");
+  };
+  static const int cell_cand[] = {64, 128, 256, 512};
+  static const int row_cand[] = {32, 64, 128, 256};
+  for (int g = 0; g < TB_COUNT && rc == EPIC_OK; g++) {
+    const int *cand = g == TB_ROW ? row_cand : cell_cand;
+    int best = b->d.tb[g];
+    float best_ms = 3.4e38f;
+    for (int c = 0; c < 4 && rc == EPIC_OK; c++) {
+      if (g == TB_ROW && c > 0 && cand[c] > b->d.ni / 2) continue;   // more threads than butterflies
+      b->d.tb[g] = cand[c];
+      float ms = 0.f;
+      rc = time_steps(&ms);
+      if (rc == EPIC_OK && ms < best_ms) { best_ms = ms; best = cand[c]; }
+    }
+    b->d.tb[g] = best;
+  }
+  cudaEventDestroy(e0);
+  cudaEventDestroy(e1);
+  if (b->run_graph) { cudaGraphExecDestroy(b->run_graph); b->run_graph = nullptr; }
+  b->graph_failed = false;
+  if (table_out)
+    for (int g = 0; g < TB_COUNT; g++) table_out[g] = b->d.tb[g];
+  return rc;
+}
+
+extern "C" int epic_batch_set_tuning(epic_batch *b, const int32_t *table) {
+  if (!b || !table) return set_error(EPIC_ERR_ARG, "epic_batch_set_tuning: NULL argument");
+  for (int g = 0; g < TB_COUNT; g++) b->d.tb[g] = table[g];
+  if (b->run_graph) { cudaGraphExecDestroy(b->run_graph); b->run_graph = nullptr; }
+  b->graph_failed = false;
+  return EPIC_OK;
+}
+
+extern "C" int epic_model_set_tuning(epic_model *m, const int32_t *table) {
+  if (!m || !table) return set_error(EPIC_ERR_ARG, "epic_model_set_tuning: NULL argument");
+  for (int g = 0; g < TB_COUNT; g++) m->d.tb[g] = table[g];
+  if (m->run_graph) { cudaGraphExecDestroy(m->run_graph); m->run_graph = nullptr; }
+  m->graph_failed = false;
+  return EPIC_OK;
+}
+

@@ -808,7 +808,7 @@ __global__ void k_advection_prep(DevModel M, int phase) {
 
 static inline unsigned ncol_blocks(const DevModel &M, int th) { return epic_blocks((long long)(M.nj + 1) * (M.ni + 2), th); }
 
-int launch_source_sink(const DevModel &M, cudaStream_t s) { k_source_sink<<<zg(ncol_blocks(M, 128), M), 128, 0, s>>>(M); return 0; }
+int launch_source_sink(const DevModel &M, cudaStream_t s) { k_source_sink<<<zg(ncol_blocks(M, TB(M, TB_COLUMN)), M), TB(M, TB_COLUMN), 0, s>>>(M); return 0; }
 static inline unsigned ntile_blocks(const DevModel &M) { return epic_blocks((long long)(M.nj + 1) * (M.ni + 2), 32); }
 static inline size_t tile_smem(const DevModel &M, int arrays) { return (size_t)arrays * 32 * (M.nk + 1) * sizeof(double); }
 int launch_calc_w(const DevModel &M, cudaStream_t s) {
@@ -817,14 +817,14 @@ int launch_calc_w(const DevModel &M, cudaStream_t s) {
 }
 int launch_uv_drag(const DevModel &M, cudaStream_t s) {
   const long long n = (long long)(M.nj + 1) * M.ni + (long long)M.nj * M.ni;
-  EPIC_LAUNCH_R(M.mixed, k_uv_drag, epic_blocks(n, 128), 128, 0, s, M);
+  EPIC_LAUNCH_R(M.mixed, k_uv_drag, epic_blocks(n, TB(M, TB_COLUMN)), TB(M, TB_COLUMN), 0, s, M);
   return 0;
 }
 int launch_hsu_vertical(const DevModel &M, double *buff, int kind, cudaStream_t s) {
-  EPIC_LAUNCH_R(M.mixed, k_hsu_vertical, ncol_blocks(M, 64), 64, 0, s, M, buff, kind);
+  EPIC_LAUNCH_R(M.mixed, k_hsu_vertical, ncol_blocks(M, TB(M, TB_COLUMN)), TB(M, TB_COLUMN), 0, s, M, buff, kind);
   return 0;
 }
-int launch_restore_mass(const DevModel &M, cudaStream_t s) { k_restore_mass<<<zg(ncol_blocks(M, 128), M), 128, 0, s>>>(M); return 0; }
+int launch_restore_mass(const DevModel &M, cudaStream_t s) { k_restore_mass<<<zg(ncol_blocks(M, TB(M, TB_COLUMN)), M), TB(M, TB_COLUMN), 0, s>>>(M); return 0; }
 int launch_set_p2etc(const DevModel &M, int update_theta, cudaStream_t s) {
   if (M.mixed) k_set_p2etc_mixed<<<zg(ntile_blocks(M), M), CT_THREADS, tile_smem(M, 3), s>>>(M, update_theta);
   else k_set_p2etc<<<zg(ntile_blocks(M), M), CT_THREADS, tile_smem(M, 4), s>>>(M, update_theta);
@@ -833,16 +833,16 @@ int launch_set_p2etc(const DevModel &M, int update_theta, cudaStream_t s) {
 int launch_store_pgrad_vars(const DevModel &M, cudaStream_t s) {
   if (M.mixed) k_pgrad_vars_column_mixed<<<zg(ntile_blocks(M), M), CT_THREADS, tile_smem(M, 5), s>>>(M);
   else k_pgrad_vars_column<<<zg(ntile_blocks(M), M), CT_THREADS, tile_smem(M, 5), s>>>(M);
-  k_pgrad_dzdt<<<zg(epic_blocks((long long)M.nk * (M.nj + 1) * M.ni, 128), M), 128, 0, s>>>(M);
+  k_pgrad_dzdt<<<zg(epic_blocks((long long)M.nk * (M.nj + 1) * M.ni, TB(M, TB_UPDATE)), M), TB(M, TB_UPDATE), 0, s>>>(M);
   return 0;
 }
-int launch_gz_monotone(const DevModel &M, cudaStream_t s) { k_gz_monotone<<<zg(ncol_blocks(M, 128), M), 128, 0, s>>>(M); return 0; }
+int launch_gz_monotone(const DevModel &M, cudaStream_t s) { k_gz_monotone<<<zg(ncol_blocks(M, TB(M, TB_COLUMN)), M), TB(M, TB_COLUMN), 0, s>>>(M); return 0; }
 int launch_calc_heating(const DevModel &M, cudaStream_t s) {
-  EPIC_LAUNCH_R(M.mixed, k_calc_heating, epic_blocks(M.n3, 128), 128, 0, s, M);
+  EPIC_LAUNCH_R(M.mixed, k_calc_heating, epic_blocks(M.n3, TB(M, TB_POINT)), TB(M, TB_POINT), 0, s, M);
   return 0;
 }
 int launch_advection_prep(const DevModel &M, int phase, cudaStream_t s) {
-  k_advection_prep<<<zg(epic_blocks((long long)(M.nj + 1) * M.iadim * (M.nk + 2), 128), M), 128, 0, s>>>(M, phase);
+  k_advection_prep<<<zg(epic_blocks((long long)(M.nj + 1) * M.iadim * (M.nk + 2), TB(M, TB_POINT)), M), TB(M, TB_POINT), 0, s>>>(M, phase);
   return 0;
 }
 

@@ -386,7 +386,7 @@ __global__ void k_hsu_zonal(DevModel M, double *buff, int kind, int kstart) {
 
 // ---- launchers ----
 
-static int row_threads(int ni) { return ni >= 256 ? 128 : 64; }
+static int row_threads(const DevModel &M) { return M.tb[TB_ROW] > 0 ? M.tb[TB_ROW] : (M.ni >= 256 ? 128 : 64); }
 static size_t relem(int fp32) { return fp32 ? sizeof(float) : sizeof(double); }
 
 int launch_filter_planes(const DevModel &M, const double *src, int src_sel, double *dst, int k0, int nplanes, int vgrid, cudaStream_t s,
@@ -394,7 +394,7 @@ int launch_filter_planes(const DevModel &M, const double *src, int src_sel, doub
   if (nplanes <= 0) return 0;
   const size_t smem = ((size_t)(M.ni + 2) + filter_smem_elems(M.ni)) * relem(fp32);
   dim3 grid(M.nj + 3, nplanes);
-  EPIC_LAUNCH_R(fp32, k_filter_planes, grid, row_threads(M.ni), smem, s, M, src, src_sel, dst, k0, vgrid);
+  EPIC_LAUNCH_R(fp32, k_filter_planes, grid, row_threads(M), smem, s, M, src, src_sel, dst, k0, vgrid);
   return 0;
 }
 
@@ -404,14 +404,14 @@ int launch_varz_filter(const DevModel &M, double *buff, int sel, int index, int 
   k_varz_tables<<<zg(epic_blocks(32LL * nrows, 128), M), 128, 0, s>>>(M, buff, sel, index, kstart, kend);
   const size_t smem = (2 * (size_t)(M.ni + 2) + filter_smem_elems(M.ni)) * relem(M.mixed);
   dim3 grid(nrows, kend - kstart + 1);
-  EPIC_LAUNCH_R(M.mixed, k_varz_filter_rows, grid, row_threads(M.ni), smem, s, M, buff, sel, index, kstart, kend);
+  EPIC_LAUNCH_R(M.mixed, k_varz_filter_rows, grid, row_threads(M), smem, s, M, buff, sel, index, kstart, kend);
   return 0;
 }
 
 int launch_hsu_zonal(const DevModel &M, double *buff, int kind, int kstart, cudaStream_t s) {
   const size_t smem = (8 * (size_t)(M.ni + 2) + filter_smem_elems(M.ni)) * relem(M.mixed);
   dim3 grid(M.nj + 1, M.nk - kstart + 1);
-  EPIC_LAUNCH_R(M.mixed, k_hsu_zonal, grid, row_threads(M.ni), smem, s, M, buff, kind, kstart);
+  EPIC_LAUNCH_R(M.mixed, k_hsu_zonal, grid, row_threads(M), smem, s, M, buff, kind, kstart);
   return 0;
 }
 

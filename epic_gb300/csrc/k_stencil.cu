@@ -762,37 +762,37 @@ __global__ void k_itime_advance(DevModel M) {
 // ---- launchers ----
 
 int launch_copy_gz(const DevModel &M, cudaStream_t s) {
-  k_copy_gz<<<zg(epic_blocks(M.n3, 256), M), 256, 0, s>>>(M);
+  k_copy_gz<<<zg(epic_blocks(M.n3, TB(M, TB_POINT)), M), TB(M, TB_POINT), 0, s>>>(M);
   return 0;
 }
 
 int launch_zero_tend(const DevModel &M, cudaStream_t s) {
-  k_zero_tend<<<zg(epic_blocks(M.n3, 256), M), 256, 0, s>>>(M);
+  k_zero_tend<<<zg(epic_blocks(M.n3, TB(M, TB_POINT)), M), TB(M, TB_POINT), 0, s>>>(M);
   return 0;
 }
 
 int launch_uv_core(const DevModel &M, cudaStream_t s) {
-  EPIC_LAUNCH_R(M.mixed, k_uv_kin, cells_blocks(M, M.nk - 1, M.nj + 1, 128), 128, 0, s, M);
-  EPIC_LAUNCH_R(M.mixed, k_uv_core_v, cells_blocks(M, M.nk - 1, M.nj, 128), 128, 0, s, M);
+  EPIC_LAUNCH_R(M.mixed, k_uv_kin, cells_blocks(M, M.nk - 1, M.nj + 1, TB(M, TB_UV_CORE)), TB(M, TB_UV_CORE), 0, s, M);
+  EPIC_LAUNCH_R(M.mixed, k_uv_core_v, cells_blocks(M, M.nk - 1, M.nj, TB(M, TB_UV_CORE)), TB(M, TB_UV_CORE), 0, s, M);
   launch_filter_planes(M, M.work0, PL_NONE, M.work0, 1, M.nk - 1, 0, s, M.mixed);
-  EPIC_LAUNCH_R(M.mixed, k_uv_core_u, cells_blocks(M, M.nk - 1, M.nj + 1, 128), 128, 0, s, M);
+  EPIC_LAUNCH_R(M.mixed, k_uv_core_u, cells_blocks(M, M.nk - 1, M.nj + 1, TB(M, TB_UV_CORE)), TB(M, TB_UV_CORE), 0, s, M);
   return 0;
 }
 
 int launch_uv_pgrad(const DevModel &M, cudaStream_t s) {
   k_gz_pole_rows<<<zg(M.nk + 1, M), 128, 0, s>>>(M);
-  EPIC_LAUNCH_R(M.mixed, k_pgrad_lon, cells_blocks(M, M.nk - 1, M.nj + 1, 128), 128, 0, s, M);
-  EPIC_LAUNCH_R(M.mixed, k_pgrad_lat, cells_blocks(M, M.nk - 1, M.nj, 128), 128, 0, s, M);
+  EPIC_LAUNCH_R(M.mixed, k_pgrad_lon, cells_blocks(M, M.nk - 1, M.nj + 1, TB(M, TB_PGRAD)), TB(M, TB_PGRAD), 0, s, M);
+  EPIC_LAUNCH_R(M.mixed, k_pgrad_lat, cells_blocks(M, M.nk - 1, M.nj, TB(M, TB_PGRAD)), TB(M, TB_PGRAD), 0, s, M);
   return 0;
 }
 
 int launch_hsu_meridional(const DevModel &M, double *buff, int kind, cudaStream_t s) {
   const int k0 = kind == 1 ? M.k_sigma - 1 : 1;
   const int nkk = M.nk - k0 + 1;
-  EPIC_LAUNCH_R(M.mixed, k_hsu_merid_pred, cells_blocks(M, nkk, M.nj + 2, 128), 128, 0, s, M, buff, kind, k0);
-  EPIC_LAUNCH_R(M.mixed, k_hsu_merid_apred, cells_blocks(M, nkk, M.nj + 1, 128), 128, 0, s, M, buff, k0);
-  EPIC_LAUNCH_R(M.mixed, k_hsu_merid_corr, cells_blocks(M, nkk, M.nj + 2, 128), 128, 0, s, M, buff, kind, k0);
-  EPIC_LAUNCH_R(M.mixed, k_hsu_merid_update, cells_blocks(M, nkk, M.nj + 1, 128), 128, 0, s, M, buff, k0);
+  EPIC_LAUNCH_R(M.mixed, k_hsu_merid_pred, cells_blocks(M, nkk, M.nj + 2, TB(M, TB_HSU)), TB(M, TB_HSU), 0, s, M, buff, kind, k0);
+  EPIC_LAUNCH_R(M.mixed, k_hsu_merid_apred, cells_blocks(M, nkk, M.nj + 1, TB(M, TB_HSU)), TB(M, TB_HSU), 0, s, M, buff, k0);
+  EPIC_LAUNCH_R(M.mixed, k_hsu_merid_corr, cells_blocks(M, nkk, M.nj + 2, TB(M, TB_HSU)), TB(M, TB_HSU), 0, s, M, buff, kind, k0);
+  EPIC_LAUNCH_R(M.mixed, k_hsu_merid_update, cells_blocks(M, nkk, M.nj + 1, TB(M, TB_HSU)), TB(M, TB_HSU), 0, s, M, buff, k0);
   return 0;
 }
 
@@ -821,11 +821,11 @@ int launch_meridional_hyperviscosity(const DevModel &M, int index, double *var, 
   double sign = 1.;
   for (int itmp = 2; itmp <= 8; itmp += 2) {
     double *dst = bufs[which];
-    EPIC_LAUNCH_R(M.mixed, k_d2dy2, cells_blocks(M, nkk, nrows, 128), 128, 0, s, M, cur_src, src_sel, dst, vgrid, M.coef[itmp], k0, nkk);
+    EPIC_LAUNCH_R(M.mixed, k_d2dy2, cells_blocks(M, nkk, nrows, TB(M, TB_VISC)), TB(M, TB_VISC), 0, s, M, cur_src, src_sel, dst, vgrid, M.coef[itmp], k0, nkk);
     src_sel = PL_NONE;
     if (M.nu[itmp] > 0.) {
       launch_filter_planes(M, dst, PL_NONE, dst, k0, nkk, vgrid, s, M.mixed);
-      EPIC_LAUNCH_R(M.mixed, k_visc_apply, cells_blocks(M, nkk, vgrid ? M.nj : M.nj + 1, 128), 128, 0, s, M, var, sel, dst, vgrid, sign, k0, nkk);
+      EPIC_LAUNCH_R(M.mixed, k_visc_apply, cells_blocks(M, nkk, vgrid ? M.nj : M.nj + 1, TB(M, TB_VISC)), TB(M, TB_VISC), 0, s, M, var, sel, dst, vgrid, sign, k0, nkk);
     }
     sign = -sign;
     double rest = 0.;
@@ -854,14 +854,14 @@ int launch_zonal_hyperviscosity(const DevModel &M, int index, double *var, int s
 int launch_divergence_damping(const DevModel &M, cudaStream_t s) {
   if (M.nudiv == 0.) return 0;
   launch_filter_planes(M, M.u, PL_UV_DIS, M.work1, 1, M.nk - 1, 0, s, M.mixed);
-  EPIC_LAUNCH_R(M.mixed, k_divergence, cells_blocks(M, M.nk - 1, M.nj + 1, 128), 128, 0, s, M, M.work1, M.v, PL_UV_DIS, M.work2, 1, M.nk - 1);
-  EPIC_LAUNCH_R(M.mixed, k_divdamp_apply, epic_blocks(2LL * (M.nk - 1) * (M.nj + 1) * M.ni, 128), 128, 0, s, M, M.nudiv);
+  EPIC_LAUNCH_R(M.mixed, k_divergence, cells_blocks(M, M.nk - 1, M.nj + 1, TB(M, TB_DIAG)), TB(M, TB_DIAG), 0, s, M, M.work1, M.v, PL_UV_DIS, M.work2, 1, M.nk - 1);
+  EPIC_LAUNCH_R(M.mixed, k_divdamp_apply, epic_blocks(2LL * (M.nk - 1) * (M.nj + 1) * M.ni, TB(M, TB_UPDATE)), TB(M, TB_UPDATE), 0, s, M, M.nudiv);
   return 0;
 }
 
 int launch_uv_update(const DevModel &M, cudaStream_t s) {
   k_uv_decide<<<zg(1, M), 1, 0, s>>>(M);
-  k_uv_update<<<zg(epic_blocks(2LL * (M.nk - 1) * (M.nj + 1) * M.ni, 128), M), 128, 0, s>>>(M);
+  k_uv_update<<<zg(epic_blocks(2LL * (M.nk - 1) * (M.nj + 1) * M.ni, TB(M, TB_UPDATE)), M), TB(M, TB_UPDATE), 0, s>>>(M);
   k_uv_rotate<<<zg(1, M), 1, 0, s>>>(M);
   return 0;
 }
@@ -869,12 +869,12 @@ int launch_uv_update(const DevModel &M, cudaStream_t s) {
 int launch_store_diag(const DevModel &M, cudaStream_t s) {
   // PV3: filtered copy of V (v rows), then the interior and polar values.
   launch_filter_planes(M, M.v, PL_UV, M.work1, 0, M.nk + 1, 1, s, M.mixed);
-  EPIC_LAUNCH_R(M.mixed, k_pv_interior, cells_blocks(M, M.nk + 1, M.nj, 128), 128, 0, s, M, M.work1);
+  EPIC_LAUNCH_R(M.mixed, k_pv_interior, cells_blocks(M, M.nk + 1, M.nj, TB(M, TB_DIAG)), TB(M, TB_DIAG), 0, s, M, M.work1);
   k_pv_poles<<<zg(M.nk + 1, M), 128, 0, s>>>(M);
   // DIV_UV3 from a filtered copy of U.
   launch_filter_planes(M, M.u, PL_UV, M.work2, 0, M.nk + 1, 0, s, M.mixed);
-  EPIC_LAUNCH_R(M.mixed, k_divergence, cells_blocks(M, M.nk + 1, M.nj + 1, 128), 128, 0, s, M, M.work2, M.v, PL_UV, M.div_uv3, 0, M.nk + 1);
-  EPIC_LAUNCH_R(M.mixed, k_ri2, cells_blocks(M, M.nk, M.nj + 1, 128), 128, 0, s, M);
+  EPIC_LAUNCH_R(M.mixed, k_divergence, cells_blocks(M, M.nk + 1, M.nj + 1, TB(M, TB_DIAG)), TB(M, TB_DIAG), 0, s, M, M.work2, M.v, PL_UV, M.div_uv3, 0, M.nk + 1);
+  EPIC_LAUNCH_R(M.mixed, k_ri2, cells_blocks(M, M.nk, M.nj + 1, TB(M, TB_DIAG)), TB(M, TB_DIAG), 0, s, M);
   return 0;
 }
 

@@ -204,6 +204,18 @@ int  epic_batch_sync(epic_batch *b);                       /* wait; first member
 void *epic_batch_stream(epic_batch *b);
 int32_t epic_batch_kernels_per_step(const epic_batch *b);
 
+/*
+ * Launch-shape autotuning (no counterpart in the reference).  A tuning table holds
+ * EPIC_TUNE_GROUPS block sizes, one per kernel group; 0 keeps the built-in choice.  Tuned kernels
+ * are pointwise or per row, so a table changes no result.  epic_batch_autotune times whole steps
+ * of the batch for each candidate (trial_steps timed steps each) and keeps the fastest; those
+ * steps advance the members' state, so tune before uploading the state a run starts from.
+ */
+#define EPIC_TUNE_GROUPS 9
+int  epic_batch_autotune(epic_batch *b, int32_t trial_steps, int32_t *table_out);
+int  epic_batch_set_tuning(epic_batch *b, const int32_t *table);
+int  epic_model_set_tuning(epic_model *m, const int32_t *table);
+
 /* Text of the last error on this thread. */
 const char *epic_last_error(void);
 

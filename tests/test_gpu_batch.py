@@ -46,3 +46,24 @@ def test_batch_rejects_mixed_shapes(gpu):
         Batch([a, b])
     with pytest.raises(EpicError, match="differs"):
         Batch([a, c])
+
+
+def test_autotuned_shapes_change_no_result(gpu):
+    """Tuning picks block sizes only; a tuned batch gives the bits of the untuned one."""
+    members = [_member(20 + q, 1.0, EPIC_PREC_MIXED) for q in range(3)]
+    scratch = Batch([m for _, _, m in members])
+    table = scratch.autotune(trial_steps=1)
+    scratch.close()
+    assert len(table) == 9 and all(t > 0 for t in table)
+    tuned = [_member(30 + q, 1.0, EPIC_PREC_MIXED) for q in range(3)]
+    plain = [_member(30 + q, 1.0, EPIC_PREC_MIXED) for q in range(3)]
+    bt, bp = Batch([m for _, _, m in tuned]), Batch([m for _, _, m in plain])
+    bt.set_tuning([64, 256, 512, 64, 256, 512, 64, 512, 32])
+    for b in (bt, bp):
+        b.timestep(EPIC_SYNC_DIAGS_ONLY)
+        b.run(4)
+        b.sync()
+    for (_, _, a), (_, _, c) in zip(tuned, plain):
+        x, y = a.download(), c.download()
+        for k in x.arrays:
+            assert np.array_equal(x.arrays[k], y.arrays[k]), k
