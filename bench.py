@@ -356,10 +356,15 @@ def run_gpu_ensemble(args):
     members = _members(cfg, nmem, precision, torch_seed=7 + rank)
     starts = [m.download() for m in members]
     batch = Batch(members)
-    # launch shapes: autotuned on this batch, then every member goes back to its initial state
-    tuning = batch.autotune(trial_steps=2)
-    for m, f in zip(members, starts):
-        m.upload(f)
+    tuning = None
+    if not args.no_tune:
+        # launch shapes: autotuned on this batch (primed), then every member goes back to its
+        # initial state
+        batch.timestep(EPIC_SYNC_DIAGS_ONLY)
+        tuning = batch.autotune(trial_steps=2)
+        batch.sync()
+        for m, f in zip(members, starts):
+            m.upload(f)
     batch.timestep(EPIC_SYNC_DIAGS_ONLY)
     for _ in range(args.warmup):
         batch.run(1)
@@ -532,6 +537,7 @@ def main():
     ap.add_argument("--workload", default="ens64", choices=sorted(WORKLOADS))
     ap.add_argument("--no-extras", action="store_true", help="skip the FP64/mixed single-grid, error and serving figures")
     ap.add_argument("--members", type=int, default=None, help="ensemble size (profiling runs use a smaller ensemble)")
+    ap.add_argument("--no-tune", action="store_true", help="keep the built-in launch shapes (profiling runs)")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--cpu-steps", type=int, default=3)
     ap.add_argument("--precision", default=None, choices=["fp64", "mixed"])

@@ -716,6 +716,7 @@ __global__ void __launch_bounds__(CT_THREADS) k_pgrad_vars_column_mixed(DevModel
 }
 
 // store_pgrad_vars, horizontal part of DZDT3 (epic_funcs_diag.c:3924-3945) plus bc_lateral.
+template <class R>
 __global__ void k_pgrad_dzdt(DevModel M) {
   epic_member(M);
   const int t = (int)(blockIdx.x * blockDim.x + threadIdx.x);
@@ -727,14 +728,15 @@ __global__ void k_pgrad_dzdt(DevModel M) {
   const int jj = 2 * j;
   const Ctl *c = M.ctl;
   const double *U = M.u + (long long)c->it_uv * M.n3, *V = M.v + (long long)c->it_uv * M.n3;
-  const double gdx_inv3 = .5 * M.m[jj + 1] / M.grav[jj + 1];
-  const double gdy_inv2 = .5 * M.n[jj] / M.grav[jj];
-  const double gdy_inv4 = .5 * M.n[jj + 2] / M.grav[jj + 2];
+  const R gdx_inv3 = R(.5) * R(M.m[jj + 1]) / R(M.grav[jj + 1]);
+  const R gdy_inv2 = R(.5) * R(M.n[jj]) / R(M.grav[jj]);
+  const R gdy_inv4 = R(.5) * R(M.n[jj + 2]) / R(M.grav[jj + 2]);
   const double *G = M.gz3;
   const long long x = M.at(k, j, i);
-  const double add = V[x] * (G[x] - G[M.at(k, j - 1, i)]) * gdy_inv2 + V[M.at(k, j + 1, i)] * (G[M.at(k, j + 1, i)] - G[x]) * gdy_inv4 +
-                     U[x] * (G[x] - G[M.at(k, j, i - 1)]) * gdx_inv3 + U[M.at(k, j, i + 1)] * (G[M.at(k, j, i + 1)] - G[x]) * gdx_inv3;
-  write_with_pads(M.dzdt3, M, M.at(k, j, 0), i, M.dzdt3[x] + add);
+  // geopotential differences are formed in FP64 in both forms
+  const R add = R(V[x]) * R(G[x] - G[M.at(k, j - 1, i)]) * gdy_inv2 + R(V[M.at(k, j + 1, i)]) * R(G[M.at(k, j + 1, i)] - G[x]) * gdy_inv4 +
+                R(U[x]) * R(G[x] - G[M.at(k, j, i - 1)]) * gdx_inv3 + R(U[M.at(k, j, i + 1)]) * R(G[M.at(k, j, i + 1)] - G[x]) * gdx_inv3;
+  write_with_pads(M.dzdt3, M, M.at(k, j, 0), i, M.dzdt3[x] + (double)add);
 }
 
 // Monotone fix of the filtered GZ copy, epic_timestep.c:182-195 (the zonal filter of planes
@@ -833,7 +835,7 @@ int launch_set_p2etc(const DevModel &M, int update_theta, cudaStream_t s) {
 int launch_store_pgrad_vars(const DevModel &M, cudaStream_t s) {
   if (M.mixed) k_pgrad_vars_column_mixed<<<zg(ntile_blocks(M), M), CT_THREADS, tile_smem(M, 5), s>>>(M);
   else k_pgrad_vars_column<<<zg(ntile_blocks(M), M), CT_THREADS, tile_smem(M, 5), s>>>(M);
-  k_pgrad_dzdt<<<zg(epic_blocks((long long)M.nk * (M.nj + 1) * M.ni, TB(M, TB_UPDATE)), M), TB(M, TB_UPDATE), 0, s>>>(M);
+  EPIC_LAUNCH_R(M.mixed, k_pgrad_dzdt, epic_blocks((long long)M.nk * (M.nj + 1) * M.ni, TB(M, TB_UPDATE)), TB(M, TB_UPDATE), 0, s, M);
   return 0;
 }
 int launch_gz_monotone(const DevModel &M, cudaStream_t s) { k_gz_monotone<<<zg(ncol_blocks(M, TB(M, TB_COLUMN)), M), TB(M, TB_COLUMN), 0, s>>>(M); return 0; }

@@ -183,22 +183,22 @@ struct PgradRef {
 template <class R>
 struct LonFace { R zbse, zbne, ztse, ztne, zbe, zte, pbe, pte, east, ln; };
 
-// East face of the u control volume at column i (the quantities the reference carries
-// from one i to the next).
+// East face of the u control volume at column i+c-1 (the quantities the reference carries
+// from one i to the next).  z[a][b][c]: GZ3 at level k+a-1, row j+b-1, column i+c-1;
+// p[a][c]: P2 at level k+a, row j, column i+c-1 (shifted by the reference values, §PgradRef).
 template <class R>
-__device__ __forceinline__ LonFace<R> lon_face(const DevModel &M, const PgradRef<R> &ref, int k, int j, int i) {
-  const double *G = M.gz3, *P = M.p2;
-  auto gz = [&](int kk, int jj, int ii) { return R(G[M.at(kk, jj, ii)] - ref.z); };
+__device__ __forceinline__ LonFace<R> lon_face(const DevModel &M, const R (&z)[3][3][2], const R (&p)[2][2], int c, int i) {
+  auto gz = [&](int a, int b) { return z[a][b][c]; };
   LonFace<R> f;
   f.ln = R(M.lon[2 * i + 1] * (M_PI / 180.));
-  f.zbse = R(.25) * (gz(k, j, i) + gz(k, j - 1, i) + gz(k + 1, j, i) + gz(k + 1, j - 1, i));
-  f.zbne = R(.25) * (gz(k, j, i) + gz(k, j + 1, i) + gz(k + 1, j, i) + gz(k + 1, j + 1, i));
-  f.ztse = R(.25) * (gz(k, j, i) + gz(k, j - 1, i) + gz(k - 1, j, i) + gz(k - 1, j - 1, i));
-  f.ztne = R(.25) * (gz(k, j, i) + gz(k, j + 1, i) + gz(k - 1, j, i) + gz(k - 1, j + 1, i));
-  f.zbe = R(.5) * (gz(k, j, i) + gz(k + 1, j, i));
-  f.zte = R(.5) * (gz(k, j, i) + gz(k - 1, j, i));
-  f.pbe = R(P[M.at(k + 1, j, i)] - ref.p);
-  f.pte = R(P[M.at(k, j, i)] - ref.p);
+  f.zbse = R(.25) * (gz(1, 1) + gz(1, 0) + gz(2, 1) + gz(2, 0));
+  f.zbne = R(.25) * (gz(1, 1) + gz(1, 2) + gz(2, 1) + gz(2, 2));
+  f.ztse = R(.25) * (gz(1, 1) + gz(1, 0) + gz(0, 1) + gz(0, 0));
+  f.ztne = R(.25) * (gz(1, 1) + gz(1, 2) + gz(0, 1) + gz(0, 2));
+  f.zbe = R(.5) * (gz(1, 1) + gz(2, 1));
+  f.zte = R(.5) * (gz(1, 1) + gz(0, 1));
+  f.pbe = p[1][c];
+  f.pte = p[0][c];
   const R a1 = f.ztne + f.ztse, b1 = f.ztne * f.ztse, a2 = f.zbne + f.zbse, b2 = f.zbne * f.zbse;
   const R terms1 = a1 * a1 - b1 - (a2 * a2 - b2);
   const R terms2 = R(3.) * (a1 - a2);
@@ -214,7 +214,18 @@ __global__ void k_pgrad_lon(DevModel M) {
   const int k = c.k, j = c.j, i = c.i;
   const R DLOGZ_TOL = R(1.e-2);
   const PgradRef<R> ref(M, k, j, i);
-  const LonFace<R> w = lon_face<R>(M, ref, k, j, i - 1), e = lon_face<R>(M, ref, k, j, i);
+  R z[3][3][2], p[2][2];
+#pragma unroll
+  for (int a = 0; a < 3; a++)
+#pragma unroll
+    for (int b = 0; b < 3; b++)
+#pragma unroll
+      for (int q = 0; q < 2; q++) z[a][b][q] = R(M.gz3[M.at(k + a - 1, j + b - 1, i + q - 1)] - ref.z);
+#pragma unroll
+  for (int a = 0; a < 2; a++)
+#pragma unroll
+    for (int q = 0; q < 2; q++) p[a][q] = R(M.p2[M.at(k + a, j, i + q - 1)] - ref.p);
+  const LonFace<R> w = lon_face<R>(M, z, p, 0, i - 1), e = lon_face<R>(M, z, p, 1, i);
   const R rho = R(.5) * (R(M.rho3[M.at(k, j, i)]) + R(M.rho3[M.at(k, j, i - 1)]));
   const R rlns = R(M.rln[2 * j]), rlnn = R(M.rln[2 * j + 2]);
   R a1 = e.ztne + e.ztse, a2 = w.ztne + w.ztse;
@@ -247,22 +258,23 @@ __global__ void k_pgrad_lon(DevModel M) {
 template <class R>
 struct LatFace { R zbnw, zbne, ztnw, ztne, zbn, ztn, pbn, ptn, north, rln, lt; };
 
-// North face of the v control volume at row j.
+// North face of the v control volume at row j+b-1.  z[a][b][c]: GZ3 at level k+a-1, row j+b-1,
+// column i+c-1; p[a][b][c]: P2 at level k+a, row j+b-1, column i+c-1 (shifted by the reference
+// values).
 template <class R>
-__device__ __forceinline__ LatFace<R> lat_face(const DevModel &M, const PgradRef<R> &ref, int k, int j, int i) {
-  const double *G = M.gz3, *P = M.p2;
-  auto gz = [&](int kk, int jj, int ii) { return R(G[M.at(kk, jj, ii)] - ref.z); };
+__device__ __forceinline__ LatFace<R> lat_face(const DevModel &M, const R (&z)[3][2][3], const R (&p)[2][2][3], int b, int jrow) {
+  auto gz = [&](int a, int c) { return z[a][b][c]; };
   LatFace<R> f;
-  f.rln = R(M.rln[2 * j + 1]);
-  f.lt = R(M.lat[2 * j + 1] * (M_PI / 180.));
-  f.zbnw = R(.25) * (gz(k, j, i) + gz(k, j, i - 1) + gz(k + 1, j, i) + gz(k + 1, j, i - 1));
-  f.zbne = R(.25) * (gz(k, j, i) + gz(k, j, i + 1) + gz(k + 1, j, i) + gz(k + 1, j, i + 1));
-  f.ztnw = R(.25) * (gz(k, j, i) + gz(k, j, i - 1) + gz(k - 1, j, i) + gz(k - 1, j, i - 1));
-  f.ztne = R(.25) * (gz(k, j, i) + gz(k, j, i + 1) + gz(k - 1, j, i) + gz(k - 1, j, i + 1));
-  f.zbn = R(.5) * (gz(k, j, i) + gz(k + 1, j, i));
-  f.ztn = R(.5) * (gz(k, j, i) + gz(k - 1, j, i));
-  f.pbn = R(P[M.at(k + 1, j, i)] - ref.p);
-  f.ptn = R(P[M.at(k, j, i)] - ref.p);
+  f.rln = R(M.rln[2 * jrow + 1]);
+  f.lt = R(M.lat[2 * jrow + 1] * (M_PI / 180.));
+  f.zbnw = R(.25) * (gz(1, 1) + gz(1, 0) + gz(2, 1) + gz(2, 0));
+  f.zbne = R(.25) * (gz(1, 1) + gz(1, 2) + gz(2, 1) + gz(2, 2));
+  f.ztnw = R(.25) * (gz(1, 1) + gz(1, 0) + gz(0, 1) + gz(0, 0));
+  f.ztne = R(.25) * (gz(1, 1) + gz(1, 2) + gz(0, 1) + gz(0, 2));
+  f.zbn = R(.5) * (gz(1, 1) + gz(2, 1));
+  f.ztn = R(.5) * (gz(1, 1) + gz(0, 1));
+  f.pbn = p[1][b][1];
+  f.ptn = p[0][b][1];
   const R a1 = f.ztne + f.ztnw, b1 = f.ztne * f.ztnw, a2 = f.zbne + f.zbnw, b2 = f.zbne * f.zbnw;
   const R terms1 = a1 * a1 - b1 - (a2 * a2 - b2);
   const R terms2 = R(3.) * (a1 - a2);
@@ -278,10 +290,23 @@ __global__ void k_pgrad_lat(DevModel M) {
   const int k = c.k, j = c.j, i = c.i;
   const R DLOGZ_TOL = R(1.e-2);
   const PgradRef<R> ref(M, k, j, i);
-  const LatFace<R> s = lat_face<R>(M, ref, k, j - 1, i), n = lat_face<R>(M, ref, k, j, i);
-  const double *G = M.gz3, *P = M.p2;
-  auto gz = [&](int kk, int jj, int ii) { return R(G[M.at(kk, jj, ii)] - ref.z); };
-  auto pp = [&](int kk, int jj, int ii) { return R(P[M.at(kk, jj, ii)] - ref.p); };
+  R z[3][2][3], p[2][2][3];
+#pragma unroll
+  for (int a = 0; a < 3; a++)
+#pragma unroll
+    for (int b = 0; b < 2; b++)
+#pragma unroll
+      for (int q = 0; q < 3; q++) z[a][b][q] = R(M.gz3[M.at(k + a - 1, j + b - 1, i + q - 1)] - ref.z);
+#pragma unroll
+  for (int a = 0; a < 2; a++)
+#pragma unroll
+    for (int b = 0; b < 2; b++)
+#pragma unroll
+      for (int q = 0; q < 3; q++) p[a][b][q] = R(M.p2[M.at(k + a, j + b - 1, i + q - 1)] - ref.p);
+  // z(level k+a-1, row j+b-1, column i+q-1), pp(level k+a, row j+b-1, column i+q-1)
+  auto gz = [&](int a, int b, int q) { return z[a][b][q]; };
+  auto pp = [&](int a, int b, int q) { return p[a][b][q]; };
+  const LatFace<R> s = lat_face<R>(M, z, p, 0, j - 1), n = lat_face<R>(M, z, p, 1, j);
   const R rho = R(.5) * (R(M.rho3[M.at(k, j, i)]) + R(M.rho3[M.at(k, j - 1, i)]));
   const R rlt = R(M.rlt[2 * j]);
   const R rlns = s.rln, rlnn = n.rln;
@@ -290,22 +315,23 @@ __global__ void k_pgrad_lat(DevModel M) {
   const R zbsw = s.zbnw, zbse = s.zbne, ztsw = s.ztnw, ztse = s.ztne;
   const R zbs = s.zbn, zts = s.ztn, pbs = s.pbn, pts = s.ptn;
   R a1, a2, b1, b2, b3, terms1, terms2;
-  const R zbe = R(.125) * (gz(k, j, i) + gz(k, j, i + 1) + gz(k, j - 1, i) + gz(k, j - 1, i + 1) + gz(k + 1, j, i) +
-                           gz(k + 1, j, i + 1) + gz(k + 1, j - 1, i) + gz(k + 1, j - 1, i + 1));
-  const R zte = R(.125) * (gz(k - 1, j, i) + gz(k - 1, j, i + 1) + gz(k - 1, j - 1, i) + gz(k - 1, j - 1, i + 1) + gz(k, j, i) +
-                           gz(k, j, i + 1) + gz(k, j - 1, i) + gz(k, j - 1, i + 1));
-  const R pbe = R(.25) * (pp(k + 1, j, i) + pp(k + 1, j, i + 1) + pp(k + 1, j - 1, i) + pp(k + 1, j - 1, i + 1));
-  const R pte = R(.25) * (pp(k, j, i) + pp(k, j, i + 1) + pp(k, j - 1, i) + pp(k, j - 1, i + 1));
+  // levels: a = 0 (k-1), 1 (k), 2 (k+1); rows: b = 0 (j-1), 1 (j); columns: q = 0 (i-1), 1 (i), 2 (i+1)
+  const R zbe = R(.125) * (gz(1, 1, 1) + gz(1, 1, 2) + gz(1, 0, 1) + gz(1, 0, 2) + gz(2, 1, 1) +
+                           gz(2, 1, 2) + gz(2, 0, 1) + gz(2, 0, 2));
+  const R zte = R(.125) * (gz(0, 1, 1) + gz(0, 1, 2) + gz(0, 0, 1) + gz(0, 0, 2) + gz(1, 1, 1) +
+                           gz(1, 1, 2) + gz(1, 0, 1) + gz(1, 0, 2));
+  const R pbe = R(.25) * (pp(1, 1, 1) + pp(1, 1, 2) + pp(1, 0, 1) + pp(1, 0, 2));
+  const R pte = R(.25) * (pp(0, 1, 1) + pp(0, 1, 2) + pp(0, 0, 1) + pp(0, 0, 2));
   a1 = n.ztne + ztse; b1 = n.ztne * ztse; a2 = n.zbne + zbse; b2 = n.zbne * zbse;
   terms1 = a1 * a1 - b1 - (a2 * a2 - b2);
   terms2 = R(3.) * (a1 - a2);
   const R east = R(.5) * (rlns - rlnn) * (-terms1 * (pbe - pte) + terms2 * (zte * pbe - zbe * pte)) / (zte - zbe);
-  const R zbw = R(.125) * (gz(k, j, i) + gz(k, j, i - 1) + gz(k, j - 1, i) + gz(k, j - 1, i - 1) + gz(k + 1, j, i) +
-                           gz(k + 1, j, i - 1) + gz(k + 1, j - 1, i) + gz(k + 1, j - 1, i - 1));
-  const R ztw = R(.125) * (gz(k - 1, j, i) + gz(k - 1, j, i - 1) + gz(k - 1, j - 1, i) + gz(k - 1, j - 1, i - 1) + gz(k, j, i) +
-                           gz(k, j, i - 1) + gz(k, j - 1, i) + gz(k, j - 1, i - 1));
-  const R pbw = R(.25) * (pp(k + 1, j, i) + pp(k + 1, j, i - 1) + pp(k + 1, j - 1, i) + pp(k + 1, j - 1, i - 1));
-  const R ptw = R(.25) * (pp(k, j, i) + pp(k, j, i - 1) + pp(k, j - 1, i) + pp(k, j - 1, i - 1));
+  const R zbw = R(.125) * (gz(1, 1, 1) + gz(1, 1, 0) + gz(1, 0, 1) + gz(1, 0, 0) + gz(2, 1, 1) +
+                           gz(2, 1, 0) + gz(2, 0, 1) + gz(2, 0, 0));
+  const R ztw = R(.125) * (gz(0, 1, 1) + gz(0, 1, 0) + gz(0, 0, 1) + gz(0, 0, 0) + gz(1, 1, 1) +
+                           gz(1, 1, 0) + gz(1, 0, 1) + gz(1, 0, 0));
+  const R pbw = R(.25) * (pp(1, 1, 1) + pp(1, 1, 0) + pp(1, 0, 1) + pp(1, 0, 0));
+  const R ptw = R(.25) * (pp(0, 1, 1) + pp(0, 1, 0) + pp(0, 0, 1) + pp(0, 0, 0));
   a1 = n.ztnw + ztsw; b1 = n.ztnw * ztsw; a2 = n.zbnw + zbsw; b2 = n.zbnw * zbsw;
   terms1 = a1 * a1 - b1 - (a2 * a2 - b2);
   terms2 = R(3.) * (a1 - a2);
@@ -493,6 +519,8 @@ __global__ void k_zonal_visc(DevModel M, double *A, int sel, int jbot, int jhalf
   const double mm = M.m[2 * j + jhalf];
   R sign = R(1.);
   bool any_applied = false;
+  // fully unrolled so that M.coef[], M.nu[] are indexed by constants (M stays in registers)
+#pragma unroll
   for (int itmp = 2; itmp <= 8; itmp += 2) {
     const R dc = R(taper ? M.coef[itmp] * M.m0 * M.m0 : M.coef[itmp] * mm * mm);
     for (int i = lane + 1; i <= ni; i += 32) d[i] = dc * (hh[i - 1] - R(2.) * hh[i] + hh[i + 1]);
@@ -527,6 +555,7 @@ __global__ void k_zonal_visc(DevModel M, double *A, int sel, int jbot, int jhalf
     }
     sign = -sign;
     double rest = 0.;
+#pragma unroll
     for (int q = itmp + 2; q <= 8; q += 2) rest += M.nu[q];
     if (!(rest > 0.)) break;
     for (int i = lane; i <= ni + 1; i += 32) hh[i] = d[i];   // swap roles

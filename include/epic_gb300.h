@@ -208,8 +208,9 @@ int32_t epic_batch_kernels_per_step(const epic_batch *b);
  * Launch-shape autotuning (no counterpart in the reference).  A tuning table holds
  * EPIC_TUNE_GROUPS block sizes, one per kernel group; 0 keeps the built-in choice.  Tuned kernels
  * are pointwise or per row, so a table changes no result.  epic_batch_autotune times whole steps
- * of the batch for each candidate (trial_steps timed steps each) and keeps the fastest; those
- * steps advance the members' state, so tune before uploading the state a run starts from.
+ * of the batch for each candidate (trial_steps timed steps each) and keeps the fastest; the
+ * members must hold a primed state (after epic_batch_timestep(b, EPIC_SYNC_DIAGS_ONLY)), and the
+ * trial steps advance it, so tune before uploading the state a run starts from.
  */
 #define EPIC_TUNE_GROUPS 9
 int  epic_batch_autotune(epic_batch *b, int32_t trial_steps, int32_t *table_out);

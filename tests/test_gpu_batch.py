@@ -52,6 +52,7 @@ def test_autotuned_shapes_change_no_result(gpu):
     """Tuning picks block sizes only; a tuned batch gives the bits of the untuned one."""
     members = [_member(20 + q, 1.0, EPIC_PREC_MIXED) for q in range(3)]
     scratch = Batch([m for _, _, m in members])
+    scratch.timestep(EPIC_SYNC_DIAGS_ONLY)
     table = scratch.autotune(trial_steps=1)
     scratch.close()
     assert len(table) == 9 and all(t > 0 for t in table)
