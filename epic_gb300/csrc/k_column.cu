@@ -315,18 +315,20 @@ __global__ void __launch_bounds__(CT_THREADS) k_set_p2etc(DevModel M, int update
   const long long n2 = M.n2;
   double *P = sm, *HL = P + 32 * L, *TH = HL + 32 * L, *PP = TH + 32 * L;
   const double g = M.grav[2 * c.j + 1];
-  if (c.warp == 0) {
-    if (c.valid) {   // P3 top-down: P3(K) = P3(K-1) + dsgth*g*H2
-      double p = M.p3[c.base];
-      CT(P, 0) = p;
-      for (int k = 1; k <= nk; k++) {
-        p = p + M.dsgth[2 * k] * g * M.hdry[c.base + k * n2];
-        CT(P, k) = p;
-      }
-      s_lp[c.lane] = xlog(M, CT(P, 0) / p);   // log(ptop/pbot)
+  if (c.valid)   // stage H2 (in HL until the prefix sum is done) and THETA
+    for (int k = c.warp; k <= nk; k += CT_WARPS) {
+      CT(TH, k) = M.theta[c.base + k * n2];
+      if (k >= 1) CT(HL, k) = M.hdry[c.base + k * n2];
     }
-  } else if (c.valid) {
-    for (int k = c.warp - 1; k <= nk; k += CT_WARPS - 1) CT(TH, k) = M.theta[c.base + k * n2];
+  __syncthreads();
+  if (c.warp == 0 && c.valid) {   // P3 top-down: P3(K) = P3(K-1) + dsgth*g*H2
+    double p = M.p3[c.base];
+    CT(P, 0) = p;
+    for (int k = 1; k <= nk; k++) {
+      p = p + M.dsgth[2 * k] * g * CT(HL, k);
+      CT(P, k) = p;
+    }
+    s_lp[c.lane] = xlog(M, CT(P, 0) / p);   // log(ptop/pbot)
   }
   __syncthreads();
   const double ptop = CT(P, 0), pbot = CT(P, nk), lp = s_lp[c.lane];
@@ -533,18 +535,20 @@ __global__ void __launch_bounds__(CT_THREADS) k_set_p2etc_mixed(DevModel M, int 
   const long long n2 = M.n2;
   double *P = sm, *HL = P + 32 * L, *TH = HL + 32 * L;
   const double g = M.grav[2 * c.j + 1];
-  if (c.warp == 0) {
-    if (c.valid) {
-      double p = M.p3[c.base];
-      CT(P, 0) = p;
-      for (int k = 1; k <= nk; k++) {
-        p = p + M.dsgth[2 * k] * g * M.hdry[c.base + k * n2];
-        CT(P, k) = p;
-      }
-      s_lp[c.lane] = xlog(M, CT(P, 0) / p);
+  if (c.valid)
+    for (int k = c.warp; k <= nk; k += CT_WARPS) {
+      CT(TH, k) = M.theta[c.base + k * n2];
+      if (k >= 1) CT(HL, k) = M.hdry[c.base + k * n2];
     }
-  } else if (c.valid) {
-    for (int k = c.warp - 1; k <= nk; k += CT_WARPS - 1) CT(TH, k) = M.theta[c.base + k * n2];
+  __syncthreads();
+  if (c.warp == 0 && c.valid) {
+    double p = M.p3[c.base];
+    CT(P, 0) = p;
+    for (int k = 1; k <= nk; k++) {
+      p = p + M.dsgth[2 * k] * g * CT(HL, k);
+      CT(P, k) = p;
+    }
+    s_lp[c.lane] = xlog(M, CT(P, 0) / p);
   }
   __syncthreads();
   const double ptop = CT(P, 0), pbot = CT(P, nk), lp = s_lp[c.lane];

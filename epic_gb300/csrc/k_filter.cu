@@ -240,7 +240,57 @@ __global__ void k_varz_tables(DevModel M, const double *buff, int sel, int index
     t[kay].y = index == 2 ? xlog(M, buff[M.at(k, j, i)]) : buff[M.at(k, j, i)];
   }
   __syncwarp();
-  if (lane == 0 && !spline_pchip(kend - kstart + 1, t)) flag_error(M.ctl, ERR_PCHIP_X, kstart, j, i, t[0].x);
+  // spline_pchip (epic_funcs_util.c:721-845): every slope uses only its two neighbouring
+  // intervals, so the lanes compute them in parallel with the reference's expressions.
+  const int n = kend - kstart + 1;
+  bool bad = false;
+  for (int q = 1 + lane; q < n; q += 32) bad |= t[q].x <= t[q - 1].x;
+  if (__any_sync(0xffffffffu, bad)) {
+    if (lane == 0) flag_error(M.ctl, ERR_PCHIP_X, kstart, j, i, t[0].x);
+    return;
+  }
+  if (n == 2) {
+    if (lane == 0) {
+      const double del1 = (t[1].y - t[0].y) / (t[1].x - t[0].x);
+      t[0].z = del1;
+      t[1].z = del1;
+    }
+    return;
+  }
+  for (int q = lane; q < n; q += 32) {
+    // the two intervals around point q (the first two for q = 0, the last two for q = n-1)
+    const int m = q == 0 ? 1 : (q == n - 1 ? n - 2 : q);
+    const double h1 = t[m].x - t[m - 1].x, h2 = t[m + 1].x - t[m].x;
+    const double del1 = (t[m].y - t[m - 1].y) / h1, del2 = (t[m + 1].y - t[m].y) / h2;
+    const double hsum = h1 + h2;
+    double z;
+    if (q == 0) {
+      const double w1 = (h1 + hsum) / hsum, w2 = -h1 / hsum;
+      z = w1 * del1 + w2 * del2;
+      if (pchst(z, del1) <= 0.0) z = 0.0;
+      else if (pchst(del1, del2) < 0.0) {
+        const double dmx = 3.0 * del1;
+        if (fabs(dmx) < fabs(z)) z = dmx;
+      }
+    } else if (q == n - 1) {
+      const double w1 = -h2 / hsum, w2 = (h2 + hsum) / hsum;
+      z = w1 * del1 + w2 * del2;
+      if (pchst(z, del2) <= 0.0) z = 0.0;
+      else if (pchst(del1, del2) < 0.0) {
+        const double dmx = 3.0 * del2;
+        if (fabs(dmx) < fabs(z)) z = dmx;
+      }
+    } else {
+      z = 0.0;
+      if (pchst(del1, del2) > 0.0) {
+        const double hsumt3 = 3.0 * hsum;
+        const double w1 = (hsum + h1) / hsumt3, w2 = (hsum + h2) / hsumt3;
+        const double dmx = dmaxr(fabs(del1), fabs(del2)), dmn = dminr(fabs(del1), fabs(del2));
+        z = dmn / (w1 * (del1 / dmx) + w2 * (del2 / dmx));
+      }
+    }
+    t[q].z = z;
+  }
 }
 
 // The rest of the THREEDIM zonal_filter: subtract var(gz), filter, add it back.
