@@ -30,7 +30,7 @@ struct Ctl {
   int lf_first[2];                     // leapfrog: forward (Euler) first step for u, v
 };
 
-enum ErrCode { ERR_NONE = 0, ERR_GZ_MONOTONE = 1, ERR_CALC_W_P = 2, ERR_PCHIP_X = 3, ERR_NONFINITE = 4 };
+enum ErrCode { ERR_NONE = 0, ERR_GZ_MONOTONE = 1, ERR_CALC_W_P = 2, ERR_PCHIP_X = 3, ERR_NONFINITE = 4, ERR_TIMEOUT = 5 };
 
 struct DevModel {
   // sizes
@@ -52,6 +52,7 @@ struct DevModel {
   const double *coslat;                     // cos(lat[2j+1] deg), j = 0..nj, from the host libm
   const MathTable *lt;                      // double-double tables for cr_log/cr_exp/cr_pow
   const float *twf;                         // the twiddles rounded to float (mixed form)
+  const float *fkern_h, *fkern_v;           // circulant filter kernels per row (mixed form, tensor-core filter)
   int mixed;                                // precision form: 0 FP64, 1 mixed (FP32 stencils)
   // state
   double *u, *v, *dudt, *dvdt, *hdry, *theta, *p3, *h3, *p2, *theta2, *t2, *t3, *rho2, *rho3, *exner3;

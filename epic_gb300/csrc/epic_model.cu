@@ -255,8 +255,9 @@ int read_ctl(epic_model *m, Ctl &c) {
 int model_error(const Ctl &c) {
   if (c.err_code == 0) return EPIC_OK;
   static const char *what[] = {"", "store_pgrad_vars: GZ3 not monotonic", "calc_w: p2 >= p4",
-                               "zonal_filter: spline_pchip x not increasing", "non-finite value"};
-  return set_error(EPIC_ERR_MODEL, "%s at (k=%d, j=%d, i=%d), value %g", c.err_code < 5 ? what[c.err_code] : "model error",
+                               "zonal_filter: spline_pchip x not increasing", "non-finite value",
+                               "tensor-core filter: product completion not signalled in time"};
+  return set_error(EPIC_ERR_MODEL, "%s at (k=%d, j=%d, i=%d), value %g", c.err_code < 6 ? what[c.err_code] : "model error",
                    c.err_k, c.err_j, c.err_i, c.err_val);
 }
 
@@ -272,7 +273,8 @@ size_t model_pool_bytes(const epic_grid &g) {
   auto rnd = [](size_t b) { return ((b + 255) / 256) * 256; };
   return rnd(sizeof(Ctl)) + (n_state3 + n_scratch3) * rnd(n3 * 8) + 3 * rnd(n2 * 8) + rnd((size_t)(g.nj + 3) * (g.nk + 2) * 3 * 8) +
          rnd(ni1 * 8) + 10 * rnd(nj1 * 8) + 3 * rnd(nk1 * 8) + rnd((g.nk + 2) * 8) + rnd((g.k_sponge + 1) * 8) +
-         2 * rnd(3 * (g.nj + 2) * 8) + rnd(ntw * 8) + rnd(ntw * 4) + rnd((g.nj + 1) * 8) + rnd(sizeof(epic::MathTable)) + 4096;
+         2 * rnd(3 * (g.nj + 2) * 8) + rnd(ntw * 8) + rnd(ntw * 4) + rnd((g.nj + 1) * 8) + rnd(sizeof(epic::MathTable)) +
+         2 * rnd((size_t)(g.nj + 3) * g.ni * 4) + 4096;
 }
 
 }  // namespace
@@ -371,6 +373,7 @@ extern "C" int epic_model_create(const epic_grid *g, int32_t precision, epic_mod
   double *hc = carve<double>(p, 3 * (g->nj + 2)), *vc = carve<double>(p, 3 * (g->nj + 2));
   double *tw = carve<double>(p, T.tw.size());
   float *twf = carve<float>(p, T.tw.size());
+  float *fkh = carve<float>(p, (size_t)(g->nj + 3) * g->ni), *fkv = carve<float>(p, (size_t)(g->nj + 3) * g->ni);
   double *coslat = carve<double>(p, g->nj + 1);
   epic::MathTable *lt = carve<epic::MathTable>(p, 1);
   if ((size_t)(p - m->pool) > bytes) {
@@ -390,6 +393,15 @@ extern "C" int epic_model_create(const epic_grid *g, int32_t precision, epic_mod
   up(tw, T.tw.data(), T.tw.size());
   std::vector<float> twf_host(T.tw.begin(), T.tw.end());
   cudaMemcpyAsync(twf, twf_host.data(), twf_host.size() * sizeof(float), cudaMemcpyHostToDevice, m->stream);
+  std::vector<float> fk_host;
+  if (precision == EPIC_PREC_MIXED) {   // circulant kernels of the tensor-core filter
+    fk_host.assign(2 * (size_t)(g->nj + 3) * g->ni, 0.f);
+    epic::fill_filter_kernels(g->ni, g->nj, T.high_lat_h.data(), T.high_lat_pv.data(), L.iadim, fk_host.data(),
+                              fk_host.data() + (size_t)(g->nj + 3) * g->ni);
+    const size_t half = (size_t)(g->nj + 3) * g->ni;
+    cudaMemcpyAsync(fkh, fk_host.data(), half * sizeof(float), cudaMemcpyHostToDevice, m->stream);
+    cudaMemcpyAsync(fkv, fk_host.data() + half, half * sizeof(float), cudaMemcpyHostToDevice, m->stream);
+  }
   // cos of the h-row latitudes with the host libm (t_rad and temp_eq use them)
   std::vector<double> cl(g->nj + 1);
   for (int J = 0; J <= g->nj; J++) cl[J] = cos(g->lat[2 * J + 1] * kDeg);
@@ -403,8 +415,11 @@ extern "C" int epic_model_create(const epic_grid *g, int32_t precision, epic_mod
   d.mn_inv = j1[8];
   d.sgth = sg; d.dsgth = ds; d.dsgth_inv = dsi; d.h_min = hmin; d.t_sponge_inv = tsp;
   d.high_lat_h = hlh; d.high_lat_pv = hlpv; d.h_coef = hc; d.v_coef = vc; d.tw = tw; d.twf = twf;
+  d.fkern_h = precision == EPIC_PREC_MIXED ? fkh : nullptr;
+  d.fkern_v = precision == EPIC_PREC_MIXED ? fkv : nullptr;
   epic::filter_kernels_init(g->ni);
   epic::column_kernels_init(g->nk);
+  epic::filter_gemm_init(g->ni);
   e = cudaStreamSynchronize(m->stream);
   if (e != cudaSuccess) {
     epic_model_destroy(m);

@@ -853,10 +853,10 @@ int launch_advection_prep(const DevModel &M, int phase, cudaStream_t s) {
 }
 
 // The tile kernels take (arrays x 32 x (nk+1)) doubles of dynamic shared memory: up to 162 KB
-// at nk = 126, above the 48 KB default.
-int column_kernels_init(int nk) {
-  const int big = (int)(5 * 32 * (nk + 1) * sizeof(double));
-  if (big <= 48 * 1024) return 0;
+// at nk = EPIC_MAX_NK, above the 48 KB default.  The limit is raised once to that maximum, so
+// models of different sizes in one process never lower it for one another.
+int column_kernels_init(int) {
+  const int big = (int)(5 * 32 * (EPIC_MAX_NK + 1) * sizeof(double));
   if (cudaFuncSetAttribute(k_calc_w<double>, cudaFuncAttributeMaxDynamicSharedMemorySize, big) != cudaSuccess ||
       cudaFuncSetAttribute(k_calc_w<float>, cudaFuncAttributeMaxDynamicSharedMemorySize, big) != cudaSuccess ||
       cudaFuncSetAttribute(k_set_p2etc, cudaFuncAttributeMaxDynamicSharedMemorySize, big) != cudaSuccess ||

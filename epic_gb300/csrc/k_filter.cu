@@ -172,7 +172,7 @@ __device__ __forceinline__ bool row_is_filtered(const DevModel &M, int j, int vg
 // (dst may equal src).  Block = one row j in -1..nj+1; rows outside the filtered set are
 // copied; rows 0..nj+1 get periodic pads (bc_lateral).
 template <class R>
-__global__ void k_filter_planes(DevModel M, const double *src, int src_sel, double *dst, int k0, int vgrid) {
+__global__ void k_filter_planes(DevModel M, const double *src, int src_sel, double *dst, int k0, int vgrid, int copy_only) {
   epic_member(M, src, dst);
   extern __shared__ __align__(16) unsigned char smraw[];
   R *sm = reinterpret_cast<R *>(smraw);
@@ -184,6 +184,7 @@ __global__ void k_filter_planes(DevModel M, const double *src, int src_sel, doub
   FilterSmem<R> fs = carve_filter(sm + (M.ni + 2), M.ni);
   const bool valid = vgrid ? (j >= 1 && j <= M.nj) : (j >= 0 && j <= M.nj);
   const bool filt = valid && row_is_filtered(M, j, vgrid);
+  if (filt && copy_only) return;   // the tensor-core filter writes this row
   if (!filt) {
     if (src != dst)
       for (int i = threadIdx.x; i <= M.ni + 1; i += blockDim.x) dst[base + i] = src[base + i];
@@ -444,7 +445,9 @@ int launch_filter_planes(const DevModel &M, const double *src, int src_sel, doub
   if (nplanes <= 0) return 0;
   const size_t smem = ((size_t)(M.ni + 2) + filter_smem_elems(M.ni)) * relem(fp32);
   dim3 grid(M.nj + 3, nplanes);
-  EPIC_LAUNCH_R(fp32, k_filter_planes, grid, row_threads(M), smem, s, M, src, src_sel, dst, k0, vgrid);
+  const int gemm = fp32 && filter_gemm_usable(M);
+  EPIC_LAUNCH_R(fp32, k_filter_planes, grid, row_threads(M), smem, s, M, src, src_sel, dst, k0, vgrid, gemm);
+  if (gemm) launch_filter_planes_gemm(M, src, src_sel, dst, k0, nplanes, vgrid, s);
   return 0;
 }
 
@@ -472,12 +475,12 @@ static void filter_attrs(int bytes) {
   cudaFuncSetAttribute(k_filter_planes<R>, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes);
 }
 
-int filter_kernels_init(int ni) {
-  const size_t big = (8 * (size_t)(ni + 2) + filter_smem_elems(ni)) * sizeof(double);
-  if (big > 48 * 1024) {
-    filter_attrs<double>((int)big);
-    filter_attrs<float>((int)big);
-  }
+// Raised once to the largest row (ni = EPIC_MAX_NI), so models of different sizes in one process
+// never lower the limit for one another.
+int filter_kernels_init(int) {
+  const size_t big = (8 * (size_t)(EPIC_MAX_NI + 2) + filter_smem_elems(EPIC_MAX_NI)) * sizeof(double);
+  filter_attrs<double>((int)big);
+  filter_attrs<float>((int)big);
   return 0;
 }
 

@@ -41,6 +41,11 @@ int launch_filter_planes(const DevModel &M, const double *src, int src_sel, doub
 int launch_varz_filter(const DevModel &M, double *buff, int sel, int index, int kstart, int kend, cudaStream_t s);
 int launch_hsu_zonal(const DevModel &M, double *buff, int kind, int kstart, cudaStream_t s);
 int filter_kernels_init(int ni);
+// k_filter_gemm.cu -- the plane filter as a tcgen05 (3xTF32) operator product, mixed form
+bool filter_gemm_usable(const DevModel &M);
+int launch_filter_planes_gemm(const DevModel &M, const double *src, int src_sel, double *dst, int k0, int nplanes, int vgrid, cudaStream_t s);
+int filter_gemm_init(int ni);
+void fill_filter_kernels(int ni, int nj, const double *hl_h, const double *hl_pv, long long iadim, float *fh, float *fv);
 size_t twiddle_doubles(int ni);
 void fill_twiddles(int ni, double *tw);
 

@@ -80,3 +80,18 @@ def test_mixed_is_deterministic(gpu):
     a, b = m1.download(), m2.download()
     for k in a.arrays:
         assert np.array_equal(a.arrays[k], b.arrays[k]), k
+
+
+def test_models_of_different_sizes_coexist(gpu):
+    """Creating a smaller model after a larger one must not shrink any launch limit the larger
+    one needs (shared-memory sizes depend on ni and nk)."""
+    big_ga, big_f = hs_setup(HSConfig(ni=256, nj=128, nk=20, dt=150))
+    big = Model(big_ga, EPIC_PREC_MIXED)
+    big64 = Model(big_ga, EPIC_PREC_FP64)
+    small_ga, small_f = hs_setup(HSConfig(ni=32, nj=16, nk=10, dt=300))
+    small, small64 = Model(small_ga, EPIC_PREC_MIXED), Model(small_ga, EPIC_PREC_FP64)
+    for m, f in ((big, big_f), (big64, big_f), (small, small_f), (small64, small_f)):
+        m.upload(f)
+        m.timestep(EPIC_SYNC_DIAGS_ONLY)
+        m.run(2)
+        m.sync()
