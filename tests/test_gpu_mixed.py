@@ -1,13 +1,14 @@
 """The mixed-precision form (EPIC_PREC_MIXED) against the FP64 form on the GPU.
 
-Mixed form: stencils, advection, hyperviscosity, the zonal filter and the physics evaluate in
-FP32; the hydrostatic sums (P3, GZ3, SUM_DIV), the row means, every update of a stored field
-and the Adams-Bashforth/leapfrog step stay FP64 (the state is stored in FP64).
+Mixed form: stencils, advection, hyperviscosity, the pressure gradient, the zonal filter (on the
+tensor cores for ni a multiple of 128) and the physics evaluate in FP32; the hydrostatic sums
+(P3, GZ3, SUM_DIV), the row means, every update of a stored field and the Adams-Bashforth/
+leapfrog step stay FP64 (the state is stored in FP64).
 
 Stated error (relative L2 per field, mixed vs FP64), measured on a GB300:
   * one simulated day (288 steps of 300 s) at 64x32x10 from a state spun up for 10 days:
-    U 3.5e-5, V 3.6e-4, HDRY 2.6e-7, THETA 3.7e-8;
-  * one simulated day from rest: U 2.1e-4, V 5.0e-4 (the first days are driven by horizontal
+    U 3.5e-5, V 3.9e-4, HDRY 2.6e-7, THETA 3.7e-8;
+  * one simulated day from rest: U 2.2e-4, V 5.9e-4 (the first days are driven by horizontal
     pressure differences 1e-5 of the geopotential, so FP32 rounding is amplified ~1e4 in U, V).
 The bounds below leave a factor ~3 over those figures.
 """
