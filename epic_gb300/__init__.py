@@ -60,6 +60,8 @@ def load_library(path: str | None = None) -> C.CDLL:
     lib.epic_model_bytes.argtypes = [C.POINTER(EpicGrid), C.c_int32]
     lib.epic_model_bytes.restype = C.c_int64
     lib.epic_model_filter_mass_noalloc.argtypes = [C.c_void_p]
+    lib.epic_model_snapshot_begin.argtypes = [C.c_void_p, C.POINTER(EpicFields)]
+    lib.epic_model_snapshot_wait.argtypes = [C.c_void_p]
     lib.epic_batch_create.argtypes = [C.POINTER(C.c_void_p), C.c_int32, C.POINTER(C.c_void_p)]
     lib.epic_batch_destroy.argtypes = [C.c_void_p]
     lib.epic_batch_destroy.restype = None
@@ -152,6 +154,16 @@ class Model:
     def filter_mass_noalloc(self) -> None:
         """run_stage(10) with the filter's profile tables in the library's fixed device array."""
         _check(self.lib.epic_model_filter_mass_noalloc(self._h), "epic_model_filter_mass_noalloc")
+
+    def snapshot_begin(self, f: Fields) -> None:
+        """Start copying the current state into f (pinned) while later steps run; keep f alive."""
+        self._snap = f
+        _check(self.lib.epic_model_snapshot_begin(self._h, C.byref(f.struct)), "epic_model_snapshot_begin")
+
+    def snapshot_wait(self) -> Fields | None:
+        _check(self.lib.epic_model_snapshot_wait(self._h), "epic_model_snapshot_wait")
+        f, self._snap = getattr(self, "_snap", None), None
+        return f
 
     def set_tuning(self, table: list[int]) -> None:
         """Launch shapes from Batch.autotune (block size per kernel group; 0 = built-in)."""

@@ -27,6 +27,12 @@ struct epic_model {
   cudaGraphExec_t run_graph = nullptr;
   bool graph_failed = false;
   int kernels_per_step = -1;
+  // asynchronous snapshots (epic_model_snapshot_begin/_wait)
+  char *snap = nullptr;              // device copy of the state region, gz_surface and Ctl
+  cudaStream_t copy_stream = nullptr;
+  cudaEvent_t snap_taken = nullptr, snap_done = nullptr;
+  Ctl *snap_ctl = nullptr;           // pinned host copy of the snapshot's Ctl
+  epic_fields *snap_dst = nullptr;   // the pending snapshot's destination, or nullptr
 };
 
 namespace {
@@ -432,6 +438,14 @@ extern "C" int epic_model_create(const epic_grid *g, int32_t precision, epic_mod
 extern "C" void epic_model_destroy(epic_model *m) {
   if (!m) return;
   if (m->run_graph) cudaGraphExecDestroy(m->run_graph);
+  if (m->copy_stream) {
+    cudaStreamSynchronize(m->copy_stream);
+    cudaStreamDestroy(m->copy_stream);
+  }
+  if (m->snap_taken) cudaEventDestroy(m->snap_taken);
+  if (m->snap_done) cudaEventDestroy(m->snap_done);
+  if (m->snap) cudaFree(m->snap);
+  if (m->snap_ctl) cudaFreeHost(m->snap_ctl);
   if (m->stream) cudaStreamSynchronize(m->stream);
   if (m->pool) cudaFree(m->pool);
   if (m->stream) cudaStreamDestroy(m->stream);
@@ -823,5 +837,84 @@ extern "C" int epic_model_set_tuning(epic_model *m, const int32_t *table) {
   if (m->run_graph) { cudaGraphExecDestroy(m->run_graph); m->run_graph = nullptr; }
   m->graph_failed = false;
   return EPIC_OK;
+}
+
+// ---- asynchronous snapshots: the state copied out while the model keeps stepping ----
+//
+// The reference writes epic.nc/extract.nc from host `var` every itsave/itextract steps
+// (src/shared/epic_main.c:338-411), which here would mean stopping the device for a full
+// device-to-host copy.  A snapshot instead copies the state region device-to-device in stream
+// order (between two steps; a few hundred microseconds even for a large grid) and then copies
+// that copy to the host on a second stream while the following steps run.  The host-side
+// writer (the reference's var_write) runs once epic_model_snapshot_wait returns.
+
+namespace {
+
+// [u, end of u_spinup): the state arrays, carved contiguously from the pool
+size_t state_region_bytes(const DevModel &d) {
+  return (size_t)((const char *)(d.u_spinup + d.n3) - (const char *)d.u);
+}
+
+int finish_snapshot(epic_model *m) {
+  if (!m->snap_dst) return EPIC_OK;
+  EPIC_CUDA_CHECK(cudaEventSynchronize(m->snap_done));
+  epic_fields *f = m->snap_dst;
+  m->snap_dst = nullptr;
+  const Ctl &c = *m->snap_ctl;
+  f->it_zero = c.it_zero; f->it_minus1 = c.it_minus1; f->it_minus2 = c.it_minus2;
+  f->itime = c.itime; f->model_time = c.model_time;
+  return model_error(c);
+}
+
+}  // namespace
+
+extern "C" int epic_model_snapshot_begin(epic_model *m, epic_fields *f) {
+  if (!m || !f) return set_error(EPIC_ERR_ARG, "epic_model_snapshot_begin: NULL argument");
+  if (!m->uploaded) return set_error(EPIC_ERR_STATE, "snapshot before upload");
+  int rc = finish_snapshot(m);   // one snapshot in flight per model
+  if (rc) return rc;
+  const DevModel &d = m->d;
+  const size_t sb = state_region_bytes(d), gb = (size_t)d.n2 * sizeof(double);
+  if (!m->snap) {
+    EPIC_CUDA_CHECK(cudaStreamCreateWithFlags(&m->copy_stream, cudaStreamNonBlocking));
+    EPIC_CUDA_CHECK(cudaEventCreateWithFlags(&m->snap_taken, cudaEventDisableTiming));
+    EPIC_CUDA_CHECK(cudaEventCreateWithFlags(&m->snap_done, cudaEventDisableTiming));
+    EPIC_CUDA_CHECK(cudaMallocHost(&m->snap_ctl, sizeof(Ctl)));
+    cudaError_t e = cudaMalloc(&m->snap, sb + gb + sizeof(Ctl));
+    if (e != cudaSuccess) {
+      m->snap = nullptr;
+      return set_error(EPIC_ERR_NOMEM, "snapshot buffer: %s", cudaGetErrorString(e));
+    }
+  }
+  char *s_state = m->snap, *s_gzs = m->snap + sb, *s_ctl = s_gzs + gb;
+  // in stream order, between the steps already enqueued and the ones that follow
+  EPIC_CUDA_CHECK(cudaMemcpyAsync(s_state, d.u, sb, cudaMemcpyDeviceToDevice, m->stream));
+  EPIC_CUDA_CHECK(cudaMemcpyAsync(s_gzs, d.gz_surface, gb, cudaMemcpyDeviceToDevice, m->stream));
+  EPIC_CUDA_CHECK(cudaMemcpyAsync(s_ctl, d.ctl, sizeof(Ctl), cudaMemcpyDeviceToDevice, m->stream));
+  EPIC_CUDA_CHECK(cudaEventRecord(m->snap_taken, m->stream));
+  EPIC_CUDA_CHECK(cudaStreamWaitEvent(m->copy_stream, m->snap_taken, 0));
+  auto at = [&](const double *dev) { return s_state + ((const char *)dev - (const char *)d.u); };
+  const size_t b3 = (size_t)d.n3 * sizeof(double);
+  cudaStream_t cs = m->copy_stream;
+  if (f->u) EPIC_CUDA_CHECK(cudaMemcpyAsync(f->u, at(d.u), d.nvp * b3, cudaMemcpyDeviceToHost, cs));
+  if (f->v) EPIC_CUDA_CHECK(cudaMemcpyAsync(f->v, at(d.v), d.nvp * b3, cudaMemcpyDeviceToHost, cs));
+  if (f->dudt) EPIC_CUDA_CHECK(cudaMemcpyAsync(f->dudt, at(d.dudt), d.ntp * b3, cudaMemcpyDeviceToHost, cs));
+  if (f->dvdt) EPIC_CUDA_CHECK(cudaMemcpyAsync(f->dvdt, at(d.dvdt), d.ntp * b3, cudaMemcpyDeviceToHost, cs));
+  double *dst[] = {f->hdry, f->theta, f->p3, f->h3, f->p2, f->theta2, f->t2, f->t3, f->rho2, f->rho3, f->exner3, f->gz3,
+                   f->mont3, f->heat3, f->pv3, f->ri2, f->div_uv3, f->w3, f->dzdt3, f->u_spinup};
+  const double *src[] = {d.hdry, d.theta, d.p3, d.h3, d.p2, d.theta2, d.t2, d.t3, d.rho2, d.rho3, d.exner3, d.gz3,
+                         d.mont3, d.heat3, d.pv3, d.ri2, d.div_uv3, d.w3, d.dzdt3, d.u_spinup};
+  for (int i = 0; i < 20; i++)
+    if (dst[i]) EPIC_CUDA_CHECK(cudaMemcpyAsync(dst[i], at(src[i]), b3, cudaMemcpyDeviceToHost, cs));
+  if (f->gz_surface) EPIC_CUDA_CHECK(cudaMemcpyAsync(f->gz_surface, s_gzs, gb, cudaMemcpyDeviceToHost, cs));
+  EPIC_CUDA_CHECK(cudaMemcpyAsync(m->snap_ctl, s_ctl, sizeof(Ctl), cudaMemcpyDeviceToHost, cs));
+  EPIC_CUDA_CHECK(cudaEventRecord(m->snap_done, cs));
+  m->snap_dst = f;
+  return EPIC_OK;
+}
+
+extern "C" int epic_model_snapshot_wait(epic_model *m) {
+  if (!m) return set_error(EPIC_ERR_ARG, "epic_model_snapshot_wait: NULL model");
+  return finish_snapshot(m);
 }
 

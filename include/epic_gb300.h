@@ -151,6 +151,18 @@ int  epic_model_sync(epic_model *m);
 int  epic_model_download(epic_model *m, epic_fields *f);
 
 /*
+ * Asynchronous form of the download for the epic.nc/extract.nc saves of the driver loop
+ * (src/shared/epic_main.c:338-411): the state as it stands after the work already enqueued is
+ * copied on the device, in stream order, and then to f's host arrays on a second stream while
+ * later epic_model_run/timestep calls proceed.  f must stay valid (and should be pinned host
+ * memory for the copy to overlap) until epic_model_snapshot_wait returns; one snapshot is in
+ * flight per model (a second begin first completes the first).  The first call allocates a
+ * device buffer of the state's size.  No counterpart in the reference.
+ */
+int  epic_model_snapshot_begin(epic_model *m, epic_fields *f);
+int  epic_model_snapshot_wait(epic_model *m);
+
+/*
  * End-to-end form of the drop-in: upload f, run nsteps (after a SYNC_DIAGS_ONLY call when
  * prime != 0), download into f.  This is what a reference-side timestep() wrapper does.
  */
