@@ -73,6 +73,9 @@ def load_library(path: str | None = None) -> C.CDLL:
     lib.epic_batch_kernels_per_step.argtypes = [C.c_void_p]
     lib.epic_batch_kernels_per_step.restype = C.c_int32
     lib.epic_batch_autotune.argtypes = [C.c_void_p, C.c_int32, C.POINTER(C.c_int32)]
+    for name in ("epic_batch_upload", "epic_batch_download"):
+        getattr(lib, name).argtypes = [C.c_void_p, C.POINTER(C.POINTER(EpicFields))]
+    lib.epic_batch_step_host.argtypes = [C.c_void_p, C.POINTER(C.POINTER(EpicFields)), C.c_int32, C.c_int32]
     for name in ("epic_batch_set_tuning", "epic_model_set_tuning"):
         getattr(lib, name).argtypes = [C.c_void_p, C.POINTER(C.c_int32)]
     lib.epic_hs_grid_build.argtypes = [C.POINTER(EpicHsParams), C.POINTER(EpicGrid), C.POINTER(C.c_double),
@@ -217,6 +220,24 @@ class Batch:
 
     def run_stage(self, stage: int) -> None:
         _check(self.lib.epic_batch_run_stage(self._h, stage), "epic_batch_run_stage")
+
+    def _ptrs(self, fields: list[Fields]):
+        if len(fields) != len(self.models):
+            raise ValueError("one Fields per member")
+        return (C.POINTER(EpicFields) * len(fields))(*[C.pointer(f.struct) for f in fields])
+
+    def upload(self, fields: list[Fields]) -> None:
+        """Every member's state from host arrays (pinned for full speed), one synchronisation."""
+        _check(self.lib.epic_batch_upload(self._h, self._ptrs(fields)), "epic_batch_upload")
+
+    def download(self, fields: list[Fields]) -> list[Fields]:
+        _check(self.lib.epic_batch_download(self._h, self._ptrs(fields)), "epic_batch_download")
+        return fields
+
+    def step_host(self, fields: list[Fields], nsteps: int = 1, groups: int = 4) -> list[Fields]:
+        """End-to-end steps with host-resident (pinned) state, copies overlapped with kernels."""
+        _check(self.lib.epic_batch_step_host(self._h, self._ptrs(fields), groups, nsteps), "epic_batch_step_host")
+        return fields
 
     def autotune(self, trial_steps: int = 3) -> list[int]:
         """Pick the block size of each kernel group by timing whole steps (advances the state)."""

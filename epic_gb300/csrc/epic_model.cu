@@ -452,13 +452,15 @@ extern "C" void epic_model_destroy(epic_model *m) {
   delete m;
 }
 
-extern "C" int epic_model_upload(epic_model *m, const epic_fields *f) {
-  if (!m || !f) return set_error(EPIC_ERR_ARG, "epic_model_upload: NULL argument");
+namespace {
+
+// The copies of epic_model_upload, enqueued on stream s; *c receives the control block and must
+// stay valid until s has run them.
+int enqueue_upload(epic_model *m, const epic_fields *f, cudaStream_t s, Ctl *c) {
   if (!f->u || !f->v || !f->dudt || !f->dvdt || !f->hdry || !f->theta || !f->p3 || !f->gz_surface || !f->u_spinup)
     return set_error(EPIC_ERR_ARG, "epic_model_upload: a required field pointer is NULL");
   DevModel &d = m->d;
   const size_t b3 = (size_t)d.n3 * sizeof(double);
-  cudaStream_t s = m->stream;
   EPIC_CUDA_CHECK(cudaMemcpyAsync(d.u, f->u, d.nvp * b3, cudaMemcpyHostToDevice, s));
   EPIC_CUDA_CHECK(cudaMemcpyAsync(d.v, f->v, d.nvp * b3, cudaMemcpyHostToDevice, s));
   EPIC_CUDA_CHECK(cudaMemcpyAsync(d.dudt, f->dudt, d.ntp * b3, cudaMemcpyHostToDevice, s));
@@ -470,21 +472,54 @@ extern "C" int epic_model_upload(epic_model *m, const epic_fields *f) {
   for (int i = 0; i < 20; i++)
     if (src[i]) EPIC_CUDA_CHECK(cudaMemcpyAsync(dst[i], src[i], b3, cudaMemcpyHostToDevice, s));
   EPIC_CUDA_CHECK(cudaMemcpyAsync(d.gz_surface, f->gz_surface, (size_t)d.n2 * sizeof(double), cudaMemcpyHostToDevice, s));
-  Ctl c;
-  memset(&c, 0, sizeof(c));
-  c.it_zero = f->it_zero; c.it_minus1 = f->it_minus1; c.it_minus2 = f->it_minus2;
-  c.itime = f->itime; c.model_time = f->model_time;
+  memset(c, 0, sizeof(*c));
+  c->it_zero = f->it_zero; c->it_minus1 = f->it_minus1; c->it_minus2 = f->it_minus2;
+  c->itime = f->itime; c->model_time = f->model_time;
   // timeplane_bookkeeping, epic_funcs_diag.c:7086-7124
   if (d.uv_scheme == EPIC_UV_AB3) {
-    c.it_uv = 0; c.it_uv_dis = 0; c.it_uv_tend = c.it_zero;
+    c->it_uv = 0; c->it_uv_dis = 0; c->it_uv_tend = c->it_zero;
   } else {
-    c.it_uv = c.it_zero;
-    const double flag = f->u[(size_t)c.it_minus1 * d.n3 + d.at(1, 0, 1)];
-    c.it_uv_dis = flag == DBL_MAX ? c.it_zero : c.it_minus1;
-    c.it_uv_tend = 0;
+    c->it_uv = c->it_zero;
+    const double flag = f->u[(size_t)c->it_minus1 * d.n3 + d.at(1, 0, 1)];
+    c->it_uv_dis = flag == DBL_MAX ? c->it_zero : c->it_minus1;
+    c->it_uv_tend = 0;
   }
-  EPIC_CUDA_CHECK(cudaMemcpyAsync(d.ctl, &c, sizeof(Ctl), cudaMemcpyHostToDevice, s));
-  EPIC_CUDA_CHECK(cudaStreamSynchronize(s));
+  EPIC_CUDA_CHECK(cudaMemcpyAsync(d.ctl, c, sizeof(Ctl), cudaMemcpyHostToDevice, s));
+  return EPIC_OK;
+}
+
+// The copies of epic_model_download, enqueued on stream s; *c receives the control block.
+int enqueue_download(epic_model *m, epic_fields *f, cudaStream_t s, Ctl *c) {
+  DevModel &d = m->d;
+  const size_t b3 = (size_t)d.n3 * sizeof(double);
+  if (f->u) EPIC_CUDA_CHECK(cudaMemcpyAsync(f->u, d.u, d.nvp * b3, cudaMemcpyDeviceToHost, s));
+  if (f->v) EPIC_CUDA_CHECK(cudaMemcpyAsync(f->v, d.v, d.nvp * b3, cudaMemcpyDeviceToHost, s));
+  if (f->dudt) EPIC_CUDA_CHECK(cudaMemcpyAsync(f->dudt, d.dudt, d.ntp * b3, cudaMemcpyDeviceToHost, s));
+  if (f->dvdt) EPIC_CUDA_CHECK(cudaMemcpyAsync(f->dvdt, d.dvdt, d.ntp * b3, cudaMemcpyDeviceToHost, s));
+  double *dst[] = {f->hdry, f->theta, f->p3, f->h3, f->p2, f->theta2, f->t2, f->t3, f->rho2, f->rho3, f->exner3, f->gz3,
+                   f->mont3, f->heat3, f->pv3, f->ri2, f->div_uv3, f->w3, f->dzdt3, f->u_spinup};
+  const double *src[] = {d.hdry, d.theta, d.p3, d.h3, d.p2, d.theta2, d.t2, d.t3, d.rho2, d.rho3, d.exner3, d.gz3,
+                         d.mont3, d.heat3, d.pv3, d.ri2, d.div_uv3, d.w3, d.dzdt3, d.u_spinup};
+  for (int i = 0; i < 20; i++)
+    if (dst[i]) EPIC_CUDA_CHECK(cudaMemcpyAsync(dst[i], src[i], b3, cudaMemcpyDeviceToHost, s));
+  if (f->gz_surface) EPIC_CUDA_CHECK(cudaMemcpyAsync(f->gz_surface, d.gz_surface, (size_t)d.n2 * sizeof(double), cudaMemcpyDeviceToHost, s));
+  EPIC_CUDA_CHECK(cudaMemcpyAsync(c, d.ctl, sizeof(Ctl), cudaMemcpyDeviceToHost, s));
+  return EPIC_OK;
+}
+
+void fields_from_ctl(epic_fields *f, const Ctl &c) {
+  f->it_zero = c.it_zero; f->it_minus1 = c.it_minus1; f->it_minus2 = c.it_minus2;
+  f->itime = c.itime; f->model_time = c.model_time;
+}
+
+}  // namespace
+
+extern "C" int epic_model_upload(epic_model *m, const epic_fields *f) {
+  if (!m || !f) return set_error(EPIC_ERR_ARG, "epic_model_upload: NULL argument");
+  Ctl c;
+  int rc = enqueue_upload(m, f, m->stream, &c);
+  EPIC_CUDA_CHECK(cudaStreamSynchronize(m->stream));
+  if (rc) return rc;
   m->uploaded = true;
   return EPIC_OK;
 }
@@ -534,25 +569,11 @@ extern "C" int epic_model_sync(epic_model *m) {
 
 extern "C" int epic_model_download(epic_model *m, epic_fields *f) {
   if (!m || !f) return set_error(EPIC_ERR_ARG, "epic_model_download: NULL argument");
-  DevModel &d = m->d;
-  const size_t b3 = (size_t)d.n3 * sizeof(double);
-  cudaStream_t s = m->stream;
-  if (f->u) EPIC_CUDA_CHECK(cudaMemcpyAsync(f->u, d.u, d.nvp * b3, cudaMemcpyDeviceToHost, s));
-  if (f->v) EPIC_CUDA_CHECK(cudaMemcpyAsync(f->v, d.v, d.nvp * b3, cudaMemcpyDeviceToHost, s));
-  if (f->dudt) EPIC_CUDA_CHECK(cudaMemcpyAsync(f->dudt, d.dudt, d.ntp * b3, cudaMemcpyDeviceToHost, s));
-  if (f->dvdt) EPIC_CUDA_CHECK(cudaMemcpyAsync(f->dvdt, d.dvdt, d.ntp * b3, cudaMemcpyDeviceToHost, s));
-  double *dst[] = {f->hdry, f->theta, f->p3, f->h3, f->p2, f->theta2, f->t2, f->t3, f->rho2, f->rho3, f->exner3, f->gz3,
-                   f->mont3, f->heat3, f->pv3, f->ri2, f->div_uv3, f->w3, f->dzdt3, f->u_spinup};
-  const double *src[] = {d.hdry, d.theta, d.p3, d.h3, d.p2, d.theta2, d.t2, d.t3, d.rho2, d.rho3, d.exner3, d.gz3,
-                         d.mont3, d.heat3, d.pv3, d.ri2, d.div_uv3, d.w3, d.dzdt3, d.u_spinup};
-  for (int i = 0; i < 20; i++)
-    if (dst[i]) EPIC_CUDA_CHECK(cudaMemcpyAsync(dst[i], src[i], b3, cudaMemcpyDeviceToHost, s));
-  if (f->gz_surface) EPIC_CUDA_CHECK(cudaMemcpyAsync(f->gz_surface, d.gz_surface, (size_t)d.n2 * sizeof(double), cudaMemcpyDeviceToHost, s));
   Ctl c;
-  int rc = read_ctl(m, c);
+  int rc = enqueue_download(m, f, m->stream, &c);
+  EPIC_CUDA_CHECK(cudaStreamSynchronize(m->stream));
   if (rc) return rc;
-  f->it_zero = c.it_zero; f->it_minus1 = c.it_minus1; f->it_minus2 = c.it_minus2;
-  f->itime = c.itime; f->model_time = c.model_time;
+  fields_from_ctl(f, c);
   return model_error(c);
 }
 
@@ -652,6 +673,8 @@ struct epic_batch {
   cudaGraphExec_t run_graph = nullptr;
   bool graph_failed = false;
   int kernels_per_step = -1;
+  std::vector<epic_batch *> groups;  // sub-batches of epic_batch_step_host's pipeline
+  Ctl *host_ctl = nullptr;           // pinned control blocks for the pipeline's copies
 };
 
 namespace {
@@ -702,6 +725,8 @@ extern "C" int epic_batch_create(epic_model *const *members, int32_t n, epic_bat
 
 extern "C" void epic_batch_destroy(epic_batch *b) {
   if (!b) return;
+  for (auto *g : b->groups) epic_batch_destroy(g);
+  if (b->host_ctl) cudaFreeHost(b->host_ctl);
   if (b->run_graph) cudaGraphExecDestroy(b->run_graph);
   if (b->stream) cudaStreamSynchronize(b->stream);
   if (b->dev_members) cudaFree(b->dev_members);
@@ -752,6 +777,45 @@ extern "C" int epic_batch_run_stage(epic_batch *b, int32_t stage) {
   int rc = batch_ready(b, "epic_batch_run_stage");
   if (rc) return rc;
   return run_stage_on(b->d, b->stream, stage);
+}
+
+// Every member's state to / from host arrays with all copies on the batch stream and one
+// synchronisation (instead of one per member).
+extern "C" int epic_batch_upload(epic_batch *b, const epic_fields *const *f) {
+  if (!b || !f) return set_error(EPIC_ERR_ARG, "epic_batch_upload: NULL argument");
+  for (auto *m : b->members) EPIC_CUDA_CHECK(cudaStreamSynchronize(m->stream));
+  EPIC_CUDA_CHECK(cudaStreamSynchronize(b->stream));
+  std::vector<Ctl> ctl(b->members.size());
+  int rc = EPIC_OK;
+  for (size_t i = 0; i < b->members.size() && rc == EPIC_OK; i++) {
+    if (!f[i]) rc = set_error(EPIC_ERR_ARG, "epic_batch_upload: member %zu has no fields", i);
+    else rc = enqueue_upload(b->members[i], f[i], b->stream, &ctl[i]);
+  }
+  EPIC_CUDA_CHECK(cudaStreamSynchronize(b->stream));
+  if (rc) return rc;
+  for (auto *m : b->members) m->uploaded = true;
+  return EPIC_OK;
+}
+
+extern "C" int epic_batch_download(epic_batch *b, epic_fields *const *f) {
+  if (!b || !f) return set_error(EPIC_ERR_ARG, "epic_batch_download: NULL argument");
+  std::vector<Ctl> ctl(b->members.size());
+  int rc = EPIC_OK;
+  for (size_t i = 0; i < b->members.size() && rc == EPIC_OK; i++) {
+    if (!f[i]) rc = set_error(EPIC_ERR_ARG, "epic_batch_download: member %zu has no fields", i);
+    else rc = enqueue_download(b->members[i], f[i], b->stream, &ctl[i]);
+  }
+  EPIC_CUDA_CHECK(cudaStreamSynchronize(b->stream));
+  if (rc) return rc;
+  for (size_t i = 0; i < b->members.size(); i++) {
+    fields_from_ctl(f[i], ctl[i]);
+    rc = model_error(ctl[i]);
+    if (rc) {
+      const std::string msg = epic::error_buffer();
+      return set_error(EPIC_ERR_MODEL, "member %zu: %s", i, msg.c_str());
+    }
+  }
+  return EPIC_OK;
 }
 
 extern "C" int epic_batch_sync(epic_batch *b) {
@@ -916,5 +980,69 @@ extern "C" int epic_model_snapshot_begin(epic_model *m, epic_fields *f) {
 extern "C" int epic_model_snapshot_wait(epic_model *m) {
   if (!m) return set_error(EPIC_ERR_ARG, "epic_model_snapshot_wait: NULL model");
   return finish_snapshot(m);
+}
+
+// ---- the end-to-end step of a batch with host-resident state, pipelined ----
+//
+// Each step copies every member's state in from host arrays, steps it and copies it back (the
+// drop-in's contract when `var` lives on the host).  The members are split into `groups`
+// sub-batches, each with its own stream and captured graph, so one group's copies overlap the
+// others' kernels and the two copy directions overlap each other.
+
+extern "C" int epic_batch_step_host(epic_batch *b, epic_fields *const *f, int32_t groups, int32_t nsteps) {
+  if (!b || !f) return set_error(EPIC_ERR_ARG, "epic_batch_step_host: NULL argument");
+  const int n = (int)b->members.size();
+  if (groups < 1) groups = 1;
+  if (groups > n) groups = n;
+  if ((int)b->groups.size() != groups) {
+    for (auto *g : b->groups) epic_batch_destroy(g);
+    b->groups.clear();
+    for (int q = 0; q < groups; q++) {
+      const int lo = (int)((long long)n * q / groups), hi = (int)((long long)n * (q + 1) / groups);
+      epic_batch *g = nullptr;
+      int rc = epic_batch_create(b->members.data() + lo, hi - lo, &g);
+      if (rc) return rc;
+      for (int t = 0; t < TB_COUNT; t++) g->d.tb[t] = b->d.tb[t];
+      b->groups.push_back(g);
+    }
+  }
+  if (!b->host_ctl) EPIC_CUDA_CHECK(cudaMallocHost(&b->host_ctl, sizeof(Ctl) * 2 * (size_t)n));
+  for (auto *m : b->members) EPIC_CUDA_CHECK(cudaStreamSynchronize(m->stream));
+  for (int step = 0; step < nsteps; step++) {
+    int idx = 0;
+    for (auto *g : b->groups) {
+      const int lo = idx;
+      for (auto *m : g->members) {
+        int rc = enqueue_upload(m, f[idx], g->stream, &b->host_ctl[2 * idx]);
+        if (rc) return rc;
+        m->uploaded = true;
+        idx++;
+      }
+      if (!g->run_graph && !g->graph_failed) {
+        g->run_graph = capture_step(g->d, g->stream, &g->kernels_per_step);
+        if (!g->run_graph) g->graph_failed = true;
+      }
+      if (g->run_graph) EPIC_CUDA_CHECK(cudaGraphLaunch(g->run_graph, g->stream));
+      else {
+        int rc = enqueue_step_on(g->d, g->stream);
+        if (!rc) rc = epic::launch_itime_advance(g->d, g->stream);
+        if (rc) return rc;
+      }
+      for (int q = lo; q < idx; q++) {
+        int rc = enqueue_download(b->members[q], f[q], g->stream, &b->host_ctl[2 * q + 1]);
+        if (rc) return rc;
+      }
+    }
+    for (auto *g : b->groups) EPIC_CUDA_CHECK(cudaStreamSynchronize(g->stream));
+    for (int q = 0; q < n; q++) {
+      fields_from_ctl(f[q], b->host_ctl[2 * q + 1]);
+      int rc = model_error(b->host_ctl[2 * q + 1]);
+      if (rc) {
+        const std::string msg = epic::error_buffer();
+        return set_error(EPIC_ERR_MODEL, "member %d: %s", q, msg.c_str());
+      }
+    }
+  }
+  return check_launch("epic_batch_step_host");
 }
 

@@ -212,6 +212,16 @@ void epic_batch_destroy(epic_batch *b);
 int  epic_batch_timestep(epic_batch *b, int32_t action);   /* every member, as epic_model_timestep */
 int  epic_batch_run(epic_batch *b, int32_t nsteps);        /* every member, as epic_model_run */
 int  epic_batch_run_stage(epic_batch *b, int32_t stage);   /* test/timing hook, as epic_model_run_stage */
+/* every member's upload / download (f[i] for member i) with one synchronisation */
+int  epic_batch_upload(epic_batch *b, const epic_fields *const *f);
+int  epic_batch_download(epic_batch *b, epic_fields *const *f);
+/*
+ * nsteps end-to-end steps with host-resident state: each step uploads every member from f[i],
+ * steps it and downloads it into f[i] (as epic_model_step_host does for one model).  The members
+ * are split into `groups` sub-batches on their own streams so that copies overlap kernels; f
+ * should be pinned host memory.
+ */
+int  epic_batch_step_host(epic_batch *b, epic_fields *const *f, int32_t groups, int32_t nsteps);
 int  epic_batch_sync(epic_batch *b);                       /* wait; first member error, if any */
 void *epic_batch_stream(epic_batch *b);
 int32_t epic_batch_kernels_per_step(const epic_batch *b);

@@ -68,3 +68,46 @@ def test_autotuned_shapes_change_no_result(gpu):
         x, y = a.download(), c.download()
         for k in x.arrays:
             assert np.array_equal(x.arrays[k], y.arrays[k]), k
+
+
+def test_batch_upload_download_match_members(gpu):
+    """epic_batch_upload/download move every member's state like the per-member calls."""
+    members = [_member(40 + q, 1.0 + 0.05 * q, EPIC_PREC_FP64) for q in range(3)]
+    b = Batch([m for _, _, m in members])
+    b.upload([f for _, f, _ in members])
+    b.timestep(EPIC_SYNC_DIAGS_ONLY)
+    b.run(3)
+    b.sync()
+    got = b.download([m.download().copy() for _, _, m in members])
+    for (ga, f, m), g in zip(members, got):
+        alone = Model(ga, EPIC_PREC_FP64)
+        alone.upload(f)
+        alone.timestep(EPIC_SYNC_DIAGS_ONLY)
+        alone.run(3)
+        alone.sync()
+        w = alone.download()
+        for k in w.arrays:
+            assert np.array_equal(g.arrays[k], w.arrays[k]), k
+        assert g.struct.itime == w.struct.itime
+
+
+@pytest.mark.parametrize("groups", [1, 2, 3])
+def test_batch_step_host_pipeline(gpu, groups):
+    """The pipelined end-to-end step (host-resident state, sub-batches on their own streams)
+    gives every member the bits it gets stepped alone."""
+    members = [_member(60 + q, 1.0 - 0.04 * q, EPIC_PREC_MIXED) for q in range(3)]
+    b = Batch([m for _, _, m in members])
+    b.timestep(EPIC_SYNC_DIAGS_ONLY)
+    b.sync()
+    hosts = [m.download().copy(pinned=True) for _, _, m in members]
+    b.step_host(hosts, 4, groups=groups)
+    for (ga, f, _), h in zip(members, hosts):
+        alone = Model(ga, EPIC_PREC_MIXED)
+        alone.upload(f)
+        alone.timestep(EPIC_SYNC_DIAGS_ONLY)
+        alone.run(4)
+        alone.sync()
+        w = alone.download()
+        for k in w.arrays:
+            assert np.array_equal(h.arrays[k], w.arrays[k]), (groups, k)
+        assert h.struct.itime == w.struct.itime
