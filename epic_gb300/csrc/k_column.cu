@@ -194,101 +194,131 @@ __global__ void k_uv_drag(DevModel M) {
 }
 
 // Vertical pass of hsu_advection, epic_flux.c:717-1052.  kind: 0 = unity (P3_INDEX),
-// 1 = THETA, 2 = HDRY.  One thread per column j = 0..nj, i = 0..ni+1.
+// 1 = THETA, 2 = HDRY.  A column tile (32 columns j = 0..nj, i = 0..ni+1 per block): every pass
+// of the predictor-corrector is pointwise in k given the previous pass, so the levels are
+// spread over the warps with a barrier between passes; d1, d2 and the smoothness weights are
+// recomputed where used (the same expressions, so the same values).  Shared arrays [k][lane]:
+// WA (the field), WM, WP (the split vertical velocity), PR (the predictor), FF (the fluxes).
 template <class R>
-__global__ void k_hsu_vertical(DevModel M, double *buff, int kind) {
+__global__ void __launch_bounds__(CT_THREADS) k_hsu_vertical(DevModel M, double *buff, int kind) {
   epic_member(M, buff);
-  int j, i;
-  if (!col_index(M, j, i)) return;
-  const int nk = M.nk;
+  extern __shared__ __align__(16) unsigned char smraw[];
+  R *sm = reinterpret_cast<R *>(smraw);
+  const ColTile c = col_tile(M);
+  const int nk = M.nk, L = nk + 2;
+  const long long n2 = M.n2;
   const bool layer = kind == 2;
   const int kf = kind == 1 ? M.k_sigma - 1 : 1;
   const R ep = R(1.e-10), DT = R(M.dt);
-  R wm[EPIC_MAX_NK + 2], wp[EPIC_MAX_NK + 2], wa[EPIC_MAX_NK + 2], pred[EPIC_MAX_NK + 2];
-  R ff[EPIC_MAX_NK + 2], d1[EPIC_MAX_NK + 2], d2[EPIC_MAX_NK + 2], aa[EPIC_MAX_NK + 2];
+  R *WA = sm, *WM = WA + 32 * L, *WP = WM + 32 * L, *PR = WP + 32 * L, *FF = PR + 32 * L;
   auto amin = [&](int k) { return layer ? R(M.h_min[k]) : R(0.); };
   auto dsi = [&](int kk) { return R(M.dsgth_inv[kk]); };
-  for (int k = layer ? kf : kf - 1; k <= nk; k++) wa[k] = R(buff[M.at(k, j, i)]);
+  auto wa = [&](int k) { return CT(WA, k); };
+  if (c.valid)
+    for (int k = (layer ? kf : kf - 1) + c.warp; k <= nk; k += CT_WARPS) CT(WA, k) = R(buff[c.base + k * n2]);
   if (layer) {
-    for (int k = kf - 1; k <= nk; k++) {
-      const R w = R(M.w3[M.at(k, j, i)]);
-      wm[k] = rmin(R(0.), w);
-      wp[k] = rmax(R(0.), w);
-    }
-    ff[kf - 1] = R(0.);
-    ff[nk] = R(0.);
-    for (int k = kf; k < nk; k++) ff[k] = wp[k] * wa[k + 1] + wm[k] * wa[k];
-    for (int k = kf; k <= nk; k++) pred[k] = wa[k] + (ff[k] - ff[k - 1]) * dsi(2 * k) * DT;
-    for (int k = kf; k < nk; k++) ff[k] = R(.5) * (wp[k] * (pred[k] + wa[k + 1]) + wm[k] * (pred[k + 1] + wa[k]));
-    for (int k = kf; k <= nk; k++) {
+    if (c.valid)
+      for (int k = kf - 1 + c.warp; k <= nk; k += CT_WARPS) {
+        const R w = R(M.w3[c.base + k * n2]);
+        CT(WM, k) = rmin(R(0.), w);
+        CT(WP, k) = rmax(R(0.), w);
+      }
+    __syncthreads();
+    if (c.valid)
+      for (int k = kf - 1 + c.warp; k <= nk; k += CT_WARPS)
+        CT(FF, k) = (k == kf - 1 || k == nk) ? R(0.) : CT(WP, k) * wa(k + 1) + CT(WM, k) * wa(k);
+    __syncthreads();
+    if (c.valid)
+      for (int k = kf + c.warp; k <= nk; k += CT_WARPS) CT(PR, k) = wa(k) + (CT(FF, k) - CT(FF, k - 1)) * dsi(2 * k) * DT;
+    __syncthreads();
+    // d1, d2 and the smoothness weight aa of level k (epic_flux.c's first corrector loop)
+    auto d1 = [&](int k) { return k == nk ? R(0.) : CT(PR, k) - wa(k + 1); };
+    auto d2 = [&](int k) { return k == 1 ? R(0.) : CT(PR, k) - wa(k - 1); };
+    auto aa = [&](int k) {
       R tmp;
-      if (k == 1) { d1[k] = pred[k] - wa[k + 1]; d2[k] = R(0.); tmp = fabs(wa[k + 1] - wa[k]) + ep; }
-      else if (k == nk) { d1[k] = R(0.); d2[k] = pred[k] - wa[k - 1]; tmp = fabs(-wa[k] + wa[k - 1]) + ep; }
-      else { d1[k] = pred[k] - wa[k + 1]; d2[k] = pred[k] - wa[k - 1]; tmp = fabs(wa[k + 1] - R(2.) * wa[k] + wa[k - 1]) + ep; }
-      aa[k] = tmp * tmp;
-    }
-    for (int k = kf; k < nk; k++) {
-      const R whatp = sqrt(wp[k] * wp[k + 1]);
-      const R whatm = -sqrt(wm[k] * wm[k - 1]);
-      const R mu = (wp[k] - wm[k]) * dsi(2 * k + 1) * DT;
-      const R al = (R(1.) + mu) / R(6.);
-      const R prod = (wa[k + 1] - amin(k + 1)) * (wa[k] - amin(k));
-      R gap = aa[k + 1] / (aa[k + 1] + prod); gap = gap * gap;
-      R gam = aa[k] / (aa[k] + prod); gam = gam * gam;
-      const R bep = R(1.) + (R(1.) / (R(2.) * al) - R(1.)) * gap;
-      const R bem = R(1.) + (R(1.) / (R(2.) * al) - R(1.)) * gam;
-      ff[k] += -al * (wp[k] * bep * d1[k] - whatp * (R(1.) - gap) * d1[k + 1] + wm[k] * bem * d2[k + 1] - whatm * (R(1.) - gam) * d2[k]);
-    }
-    for (int k = kf; k <= nk; k++) {
-      const long long x = M.at(k, j, i);
-      buff[x] = buff[x] + (double)((ff[k] - ff[k - 1]) * dsi(2 * k) * DT);
-    }
+      if (k == 1) tmp = fabs(wa(k + 1) - wa(k)) + ep;
+      else if (k == nk) tmp = fabs(-wa(k) + wa(k - 1)) + ep;
+      else tmp = fabs(wa(k + 1) - R(2.) * wa(k) + wa(k - 1)) + ep;
+      return tmp * tmp;
+    };
+    // the corrector reads PR, WA, WM and WP only, so it rewrites FF in place
+    if (c.valid)
+      for (int k = kf + c.warp; k < nk; k += CT_WARPS) {
+        const R wpk = CT(WP, k), wmk = CT(WM, k);
+        R f = R(.5) * (wpk * (CT(PR, k) + wa(k + 1)) + wmk * (CT(PR, k + 1) + wa(k)));
+        const R whatp = sqrt(wpk * CT(WP, k + 1));
+        const R whatm = -sqrt(wmk * CT(WM, k - 1));
+        const R mu = (wpk - wmk) * dsi(2 * k + 1) * DT;
+        const R al = (R(1.) + mu) / R(6.);
+        const R prod = (wa(k + 1) - amin(k + 1)) * (wa(k) - amin(k));
+        const R aap = aa(k + 1), aak = aa(k);
+        R gap = aap / (aap + prod); gap = gap * gap;
+        R gam = aak / (aak + prod); gam = gam * gam;
+        const R bep = R(1.) + (R(1.) / (R(2.) * al) - R(1.)) * gap;
+        const R bem = R(1.) + (R(1.) / (R(2.) * al) - R(1.)) * gam;
+        f += -al * (wpk * bep * d1(k) - whatp * (R(1.) - gap) * d1(k + 1) + wmk * bem * d2(k + 1) - whatm * (R(1.) - gam) * d2(k));
+        CT(FF, k) = f;
+      }
+    __syncthreads();
+    if (c.valid)
+      for (int k = kf + c.warp; k <= nk; k += CT_WARPS) {
+        const long long x = c.base + k * n2;
+        buff[x] = buff[x] + (double)((CT(FF, k) - CT(FF, k - 1)) * dsi(2 * k) * DT);
+      }
   } else {
-    for (int k = kf; k <= nk; k++) {
-      const R w = (k == 1 || k == nk) ? R(0.) : R(.5) * (R(M.w3[M.at(k, j, i)]) + R(M.w3[M.at(k - 1, j, i)]));
-      wm[k] = rmin(R(0.), w);
-      wp[k] = rmax(R(0.), w);
-    }
-    for (int k = kf; k <= nk; k++) ff[k] = wp[k] * wa[k] + wm[k] * wa[k - 1];
-    ff[nk + 1] = R(0.);
-    pred[kf - 1] = wa[kf - 1];
-    for (int k = kf; k <= nk; k++) pred[k] = wa[k] + (ff[k + 1] - ff[k]) * dsi(2 * k + 1) * DT;
-    for (int k = kf; k <= nk; k++) ff[k] = R(.5) * (wp[k] * (pred[k - 1] + wa[k]) + wm[k] * (pred[k] + wa[k - 1]));
-    for (int k = kf - 1; k <= nk; k++) {
-      // For THETA (kf > 1) the entry below the first loaded one is the value the reference's
-      // static column buffer keeps from the preceding unity advection: 1.0 (epic_flux.c:866-877).
-      const R wkm1 = k >= 1 ? (k - 1 < kf - 1 ? R(1.0) : wa[k - 1]) : R(0.);
+    if (c.valid)
+      for (int k = kf + c.warp; k <= nk; k += CT_WARPS) {
+        const R w = (k == 1 || k == nk) ? R(0.) : R(.5) * (R(M.w3[c.base + k * n2]) + R(M.w3[c.base + (k - 1) * n2]));
+        CT(WM, k) = rmin(R(0.), w);
+        CT(WP, k) = rmax(R(0.), w);
+      }
+    __syncthreads();
+    if (c.valid)
+      for (int k = kf + c.warp; k <= nk + 1; k += CT_WARPS)
+        CT(FF, k) = k == nk + 1 ? R(0.) : CT(WP, k) * wa(k) + CT(WM, k) * wa(k - 1);
+    __syncthreads();
+    if (c.valid)
+      for (int k = kf - 1 + c.warp; k <= nk; k += CT_WARPS)
+        CT(PR, k) = k == kf - 1 ? wa(kf - 1) : wa(k) + (CT(FF, k + 1) - CT(FF, k)) * dsi(2 * k + 1) * DT;
+    __syncthreads();
+    // For THETA (kf > 1) the entry below the first loaded one is the value the reference's
+    // static column buffer keeps from the preceding unity advection: 1.0 (epic_flux.c:866-877).
+    auto aa = [&](int k) {
+      const R wkm1 = k >= 1 ? (k - 1 < kf - 1 ? R(1.0) : wa(k - 1)) : R(0.);
       R tmp;
-      if (k == 0) tmp = fabs(wa[k + 1] - wa[k]) + ep;
-      else if (k == nk) tmp = fabs(-wa[k] + wkm1) + ep;
-      else tmp = fabs(wa[k + 1] - R(2.) * wa[k] + wkm1) + ep;
-      aa[k] = tmp * tmp;
-    }
-    d2[kf - 1] = R(0.);
-    for (int k = kf; k <= nk; k++) {
-      d1[k] = pred[k - 1] - wa[k];
-      d2[k] = pred[k] - wa[k - 1];
-    }
-    for (int k = kf; k <= nk; k++) {
-      const R whatm = (k == 1 || k - 1 < kf) ? R(0.) : -sqrt(wm[k] * wm[k - 1]);
-      const R whatp = (k == nk) ? R(0.) : sqrt(wp[k] * wp[k + 1]);
-      const R mu = (wp[k] - wm[k]) * dsi(2 * k) * DT;
-      const R al = (R(1.) + mu) / R(6.);
-      const R prod = (wa[k] - amin(k)) * (wa[k - 1] - amin(k - 1));
-      R gap = aa[k] / (aa[k] + prod); gap = gap * gap;
-      R gam = aa[k - 1] / (aa[k - 1] + prod); gam = gam * gam;
-      const R bep = R(1.) + (R(1.) / (R(2.) * al) - R(1.)) * gap;
-      const R bem = R(1.) + (R(1.) / (R(2.) * al) - R(1.)) * gam;
-      R g;
-      if (k < nk) g = -al * (wp[k] * bep * d1[k] - whatp * (R(1.) - gap) * d1[k + 1] + wm[k] * bem * d2[k] - whatm * (R(1.) - gam) * d2[k - 1]);
-      else g = -al * (wp[k] * bep * d1[k] + wm[k] * bem * d2[k] - whatm * (R(1.) - gam) * d2[k - 1]);
-      ff[k] += g;
-    }
-    ff[nk + 1] = R(0.);
-    for (int k = kf; k <= nk; k++) {
-      const long long x = M.at(k, j, i);
-      buff[x] = buff[x] + (double)((ff[k + 1] - ff[k]) * dsi(2 * k + 1) * DT);
-    }
+      if (k == 0) tmp = fabs(wa(k + 1) - wa(k)) + ep;
+      else if (k == nk) tmp = fabs(-wa(k) + wkm1) + ep;
+      else tmp = fabs(wa(k + 1) - R(2.) * wa(k) + wkm1) + ep;
+      return tmp * tmp;
+    };
+    auto d1 = [&](int k) { return CT(PR, k - 1) - wa(k); };
+    auto d2 = [&](int k) { return k == kf - 1 ? R(0.) : CT(PR, k) - wa(k - 1); };
+    if (c.valid)
+      for (int k = kf + c.warp; k <= nk; k += CT_WARPS) {
+        const R wpk = CT(WP, k), wmk = CT(WM, k);
+        R f = R(.5) * (wpk * (CT(PR, k - 1) + wa(k)) + wmk * (CT(PR, k) + wa(k - 1)));
+        const R whatm = (k == 1 || k - 1 < kf) ? R(0.) : -sqrt(wmk * CT(WM, k - 1));
+        const R whatp = (k == nk) ? R(0.) : sqrt(wpk * CT(WP, k + 1));
+        const R mu = (wpk - wmk) * dsi(2 * k) * DT;
+        const R al = (R(1.) + mu) / R(6.);
+        const R prod = (wa(k) - amin(k)) * (wa(k - 1) - amin(k - 1));
+        const R aak = aa(k), aam = aa(k - 1);
+        R gap = aak / (aak + prod); gap = gap * gap;
+        R gam = aam / (aam + prod); gam = gam * gam;
+        const R bep = R(1.) + (R(1.) / (R(2.) * al) - R(1.)) * gap;
+        const R bem = R(1.) + (R(1.) / (R(2.) * al) - R(1.)) * gam;
+        R g;
+        if (k < nk) g = -al * (wpk * bep * d1(k) - whatp * (R(1.) - gap) * d1(k + 1) + wmk * bem * d2(k) - whatm * (R(1.) - gam) * d2(k - 1));
+        else g = -al * (wpk * bep * d1(k) + wmk * bem * d2(k) - whatm * (R(1.) - gam) * d2(k - 1));
+        CT(FF, k) = f + g;
+      }
+    __syncthreads();
+    if (c.valid)
+      for (int k = kf + c.warp; k <= nk; k += CT_WARPS) {
+        const long long x = c.base + k * n2;
+        const R ffk1 = k == nk ? R(0.) : CT(FF, k + 1);
+        buff[x] = buff[x] + (double)((ffk1 - CT(FF, k)) * dsi(2 * k + 1) * DT);
+      }
   }
 }
 
@@ -827,7 +857,8 @@ int launch_uv_drag(const DevModel &M, cudaStream_t s) {
   return 0;
 }
 int launch_hsu_vertical(const DevModel &M, double *buff, int kind, cudaStream_t s) {
-  EPIC_LAUNCH_R(M.mixed, k_hsu_vertical, ncol_blocks(M, TB(M, TB_COLUMN)), TB(M, TB_COLUMN), 0, s, M, buff, kind);
+  EPIC_LAUNCH_R(M.mixed, k_hsu_vertical, ntile_blocks(M), CT_THREADS,
+                (size_t)5 * 32 * (M.nk + 2) * (M.mixed ? sizeof(float) : sizeof(double)), s, M, buff, kind);
   return 0;
 }
 int launch_restore_mass(const DevModel &M, cudaStream_t s) { k_restore_mass<<<zg(ncol_blocks(M, TB(M, TB_COLUMN)), M), TB(M, TB_COLUMN), 0, s>>>(M); return 0; }
@@ -857,12 +888,15 @@ int launch_advection_prep(const DevModel &M, int phase, cudaStream_t s) {
 // models of different sizes in one process never lower it for one another.
 int column_kernels_init(int) {
   const int big = (int)(5 * 32 * (EPIC_MAX_NK + 1) * sizeof(double));
+  const int hv = (int)(5 * 32 * (EPIC_MAX_NK + 2) * sizeof(double));
   if (cudaFuncSetAttribute(k_calc_w<double>, cudaFuncAttributeMaxDynamicSharedMemorySize, big) != cudaSuccess ||
       cudaFuncSetAttribute(k_calc_w<float>, cudaFuncAttributeMaxDynamicSharedMemorySize, big) != cudaSuccess ||
       cudaFuncSetAttribute(k_set_p2etc, cudaFuncAttributeMaxDynamicSharedMemorySize, big) != cudaSuccess ||
       cudaFuncSetAttribute(k_pgrad_vars_column, cudaFuncAttributeMaxDynamicSharedMemorySize, big) != cudaSuccess ||
       cudaFuncSetAttribute(k_set_p2etc_mixed, cudaFuncAttributeMaxDynamicSharedMemorySize, big) != cudaSuccess ||
-      cudaFuncSetAttribute(k_pgrad_vars_column_mixed, cudaFuncAttributeMaxDynamicSharedMemorySize, big) != cudaSuccess)
+      cudaFuncSetAttribute(k_pgrad_vars_column_mixed, cudaFuncAttributeMaxDynamicSharedMemorySize, big) != cudaSuccess ||
+      cudaFuncSetAttribute(k_hsu_vertical<double>, cudaFuncAttributeMaxDynamicSharedMemorySize, hv) != cudaSuccess ||
+      cudaFuncSetAttribute(k_hsu_vertical<float>, cudaFuncAttributeMaxDynamicSharedMemorySize, hv) != cudaSuccess)
     return -1;
   return 0;
 }
