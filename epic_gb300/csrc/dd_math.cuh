@@ -267,6 +267,28 @@ __host__ __device__ __forceinline__ double cr_exp(double x, const MathTable &T) 
   if (round_test(v, fabs(v.hi) * 0x1p-69, r)) return r * pow2i(q);
   return dd_exp_round({x, 0.}, T);
 }
+// pow(x, y) and log(x) of one argument, sharing the fast logarithm; each result equals the
+// separate cr_pow / cr_log call.
+__host__ __device__ __forceinline__ double cr_pow(double x, double y, const MathTable &T);
+__host__ __device__ __forceinline__ double cr_log_pow(double x, double y, const MathTable &T, double &lg) {
+  if (!(x > 0.) || !(x < INFINITY) || x < 2.2250738585072014e-308 || x == 1. || y == 0. || !(fabs(y) < 1e6)) {
+    lg = cr_log(x, T);
+    return cr_pow(x, y, T);
+  }
+  const dd l = fast_log(x, T);
+  double r;
+  lg = round_test(l, fabs(l.hi) * 0x1p-69, r) ? r : dd_log(x, T).hi;
+  dd yl = two_prod(y, l.hi);
+  yl.lo += y * l.lo;
+  if (!(fabs(yl.hi) < 700.)) return pow(x, y);
+  yl = fast_two_sum(yl.hi, yl.lo);
+  int q;
+  const dd v = fast_exp(yl.hi, yl.lo, T, q);
+  if (round_test(v, fabs(v.hi) * (0x1p-69 + fabs(yl.hi) * 0x1p-68), r)) return r * pow2i(q);
+  const dd ls = dd_mul_d(dd_log(x, T), y);
+  return dd_exp_round(ls, T);
+}
+
 __host__ __device__ __forceinline__ double cr_pow(double x, double y, const MathTable &T) {
   if (y == 0. || x == 1.) return 1.;
   if (!(x > 0.) || !(x < INFINITY) || x < 2.2250738585072014e-308 || !(fabs(y) < 1e6)) return pow(x, y);

@@ -50,6 +50,7 @@ struct DevModel {
   const double *h_coef, *v_coef;            // d2dy2 coefficients, 3 per row
   const double *tw;                         // realft/four1 twiddles (see k_filter.cu)
   const double *coslat;                     // cos(lat[2j+1] deg), j = 0..nj, from the host libm
+  const double *coslat4;                    // pow(coslat[j], 4.) correctly rounded (t_rad's cos^4)
   const MathTable *lt;                      // double-double tables for cr_log/cr_exp/cr_pow
   const float *twf;                         // the twiddles rounded to float (mixed form)
   const float *fkern_h, *fkern_v;           // circulant filter kernels per row (mixed form, tensor-core filter)
@@ -158,11 +159,20 @@ template <> struct RMath<double> {
   static __device__ __forceinline__ double exp(const DevModel &M, double x) { return xexp(M, x); }
   static __device__ __forceinline__ double pow(const DevModel &M, double x, double y) { return xpow(M, x, y); }
   static __device__ __forceinline__ int cmp(double x1, double x2) { return fcmp(x1, x2); }
+  static __device__ __forceinline__ double log_pow(const DevModel &M, double x, double y, double &lg) {
+    return cr_log_pow(x, y, *M.lt, lg);
+  }
+  static __device__ __forceinline__ double cos4(const DevModel &M, int j) { return M.coslat4[j]; }
 };
 template <> struct RMath<float> {
   static __device__ __forceinline__ float log(const DevModel &, float x) { return logf(x); }
   static __device__ __forceinline__ float exp(const DevModel &, float x) { return expf(x); }
   static __device__ __forceinline__ float pow(const DevModel &, float x, float y) { return powf(x, y); }
+  static __device__ __forceinline__ float log_pow(const DevModel &, float x, float y, float &lg) {
+    lg = logf(x);
+    return powf(x, y);
+  }
+  static __device__ __forceinline__ float cos4(const DevModel &M, int j) { return (float)M.coslat4[j]; }
   // fcmp with the float epsilon
   static __device__ __forceinline__ int cmp(float x1, float x2) {
     int e;

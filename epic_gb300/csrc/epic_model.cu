@@ -279,7 +279,7 @@ size_t model_pool_bytes(const epic_grid &g) {
   auto rnd = [](size_t b) { return ((b + 255) / 256) * 256; };
   return rnd(sizeof(Ctl)) + (n_state3 + n_scratch3) * rnd(n3 * 8) + 3 * rnd(n2 * 8) + rnd((size_t)(g.nj + 3) * (g.nk + 2) * 3 * 8) +
          rnd(ni1 * 8) + 10 * rnd(nj1 * 8) + 3 * rnd(nk1 * 8) + rnd((g.nk + 2) * 8) + rnd((g.k_sponge + 1) * 8) +
-         2 * rnd(3 * (g.nj + 2) * 8) + rnd(ntw * 8) + rnd(ntw * 4) + rnd((g.nj + 1) * 8) + rnd(sizeof(epic::MathTable)) +
+         2 * rnd(3 * (g.nj + 2) * 8) + rnd(ntw * 8) + rnd(ntw * 4) + 2 * rnd((g.nj + 1) * 8) + rnd(sizeof(epic::MathTable)) +
          2 * rnd((size_t)(g.nj + 3) * g.ni * 4) + 4096;
 }
 
@@ -381,6 +381,7 @@ extern "C" int epic_model_create(const epic_grid *g, int32_t precision, epic_mod
   float *twf = carve<float>(p, T.tw.size());
   float *fkh = carve<float>(p, (size_t)(g->nj + 3) * g->ni), *fkv = carve<float>(p, (size_t)(g->nj + 3) * g->ni);
   double *coslat = carve<double>(p, g->nj + 1);
+  double *coslat4 = carve<double>(p, g->nj + 1);
   epic::MathTable *lt = carve<epic::MathTable>(p, 1);
   if ((size_t)(p - m->pool) > bytes) {
     epic_model_destroy(m);
@@ -414,8 +415,13 @@ extern "C" int epic_model_create(const epic_grid *g, int32_t precision, epic_mod
   up(coslat, cl.data(), cl.size());
   std::vector<epic::MathTable> host_lt(1);   // ~34 KB, built per model in a few ms
   epic::fill_math_table(host_lt[0]);
+  // t_rad's pow(cos(lat), 4.) once per row, with the device's correctly rounded pow (host-compiled)
+  std::vector<double> cl4(g->nj + 1);
+  for (int J = 0; J <= g->nj; J++) cl4[J] = epic::cr_pow(cl[J], 4., host_lt[0]);
+  up(coslat4, cl4.data(), cl4.size());
   cudaMemcpyAsync(lt, host_lt.data(), sizeof(epic::MathTable), cudaMemcpyHostToDevice, m->stream);
   d.coslat = coslat;
+  d.coslat4 = coslat4;
   d.lt = lt;
   d.lon = lon; d.lat = j1[0]; d.rln = j1[1]; d.rlt = j1[2]; d.f = j1[3]; d.m = j1[4]; d.n = j1[5]; d.mn = j1[6]; d.grav = j1[7];
   d.mn_inv = j1[8];

@@ -810,13 +810,15 @@ __global__ void k_calc_heating(DevModel M) {
     const R pbot = R(M.p3[M.at(M.nk, j, ii)]);
     const R amp = (pressure / pbot - R(0.7)) / (R(1.) - R(0.7));
     R kt = ka;
-    if (amp > R(0.)) kt += (ks - ka) * RMath<R>::pow(M, R(M.coslat[j]), R(4.)) * amp;
+    if (amp > R(0.)) kt += (ks - ka) * RMath<R>::cos4(M, j) * amp;   // pow(cos(lat), 4.), per row
     const R cp_over_time = R(1004.) / (R(1.) / kt);
     R c2 = R(M.coslat[j]);
     c2 *= c2;
     const R s2 = R(1.) - c2;
     const R p_p0 = pressure / (R(1000.) * R(100.));
-    R teq = (R(315.) - R(60.) * s2 - R(10.) * RMath<R>::log(M, p_p0) * c2) * RMath<R>::pow(M, p_p0, R(M.kappa));
+    R lg;
+    const R pw = RMath<R>::log_pow(M, p_p0, R(M.kappa), lg);
+    R teq = (R(315.) - R(60.) * s2 - R(10.) * lg * c2) * pw;
     teq = rmax(R(200.), teq);
     val = -cp_over_time * (R(M.t3[x]) - teq);
   }
