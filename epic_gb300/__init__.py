@@ -68,6 +68,7 @@ def load_library(path: str | None = None) -> C.CDLL:
     for name in ("epic_batch_timestep", "epic_batch_run", "epic_batch_run_stage"):
         getattr(lib, name).argtypes = [C.c_void_p, C.c_int32]
     lib.epic_batch_sync.argtypes = [C.c_void_p]
+    lib.epic_batch_query.argtypes = [C.c_void_p]
     lib.epic_batch_stream.argtypes = [C.c_void_p]
     lib.epic_batch_stream.restype = C.c_void_p
     lib.epic_batch_kernels_per_step.argtypes = [C.c_void_p]
@@ -251,6 +252,14 @@ class Batch:
 
     def sync(self) -> None:
         _check(self.lib.epic_batch_sync(self._h), "epic_batch_sync")
+
+    def done(self) -> bool:
+        """True once the work queued on the batch has finished (does not wait; errors of the
+        members surface on sync())."""
+        rc = self.lib.epic_batch_query(self._h)
+        if rc < 0:
+            _check(rc, "epic_batch_query")
+        return rc == 1
 
     @property
     def stream(self) -> int:

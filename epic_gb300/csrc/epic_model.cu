@@ -840,6 +840,14 @@ extern "C" int epic_batch_sync(epic_batch *b) {
   return EPIC_OK;
 }
 
+extern "C" int epic_batch_query(epic_batch *b) {
+  if (!b) return set_error(EPIC_ERR_ARG, "epic_batch_query: NULL batch");
+  const cudaError_t e = cudaStreamQuery(b->stream);
+  if (e == cudaSuccess) return 1;
+  if (e == cudaErrorNotReady) return 0;
+  return set_error(EPIC_ERR_CUDA, "epic_batch_query: %s", cudaGetErrorString(e));
+}
+
 extern "C" void *epic_batch_stream(epic_batch *b) { return b ? (void *)b->stream : nullptr; }
 
 extern "C" int32_t epic_batch_kernels_per_step(const epic_batch *b) { return b ? b->kernels_per_step : -1; }

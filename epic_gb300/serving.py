@@ -11,8 +11,10 @@ steps).  The server
     advances each class as one Batch: every kernel of a step is launched once for all of the
     class's runs, and the classes' batches run on their own streams, so their work overlaps
     on the device;
+  * never waits on one class while another could be launched: each pass polls every class's
+    batch (epic_batch_query), settles the ones that finished and relaunches them at once;
   * re-forms a class's batch whenever a run joins or leaves it (continuous batching: runs that
-    arrive while others are on the GPU join at the next scheduling round);
+    arrive while others are on the GPU join when their class's batch in flight finishes);
   * retires a run when its steps are done: its state is copied to the host and its device
     memory returns to the budget.
 
@@ -76,17 +78,40 @@ def state_checksum(f: Fields) -> float:
     return tot
 
 
+class DeviceBackend:
+    """What the server needs from the library (the CPU tests of the scheduling logic replace it)."""
+
+    def setup(self, cfg: HSConfig):
+        return hs_setup(cfg)
+
+    def bytes(self, grid, precision: int) -> int:
+        return model_bytes(grid, precision)
+
+    def model(self, grid, fields, precision: int):
+        m = Model(grid, precision)
+        m.upload(fields)
+        m.timestep(EPIC_SYNC_DIAGS_ONLY)
+        return m
+
+    def batch(self, models):
+        return Batch(models)
+
+
 @dataclass
 class RunServer:
     hbm_budget: int                      # bytes of device memory the admitted runs may hold
     precision: int = EPIC_PREC_MIXED
-    round_steps: int = 16                # most steps a class advances per scheduling round
+    round_steps: int = 16                # most steps a class advances per scheduling pass
     keep_fields: bool = False            # keep each result's full state (else a checksum)
+    backend: object = field(default_factory=DeviceBackend)
     waiting: list = field(default_factory=list)
+    prepared: dict = field(default_factory=dict)    # rid -> (grid, initial fields, device bytes)
     active: dict = field(default_factory=dict)      # shape class -> list[_Active]
     batches: dict = field(default_factory=dict)     # shape class -> (Batch, member ids)
+    inflight: dict = field(default_factory=dict)    # shape class -> (Batch, steps, members) running
     results: list = field(default_factory=list)
     used: int = 0
+    peak_used: int = 0
     t0: float = 0.0
 
     def now(self) -> float:
@@ -99,47 +124,59 @@ class RunServer:
     def admit(self) -> None:
         keep = []
         for req in self.waiting:
-            ga, f = hs_setup(req.cfg)
-            need = model_bytes(ga, self.precision)
-            if need > self.hbm_budget:
-                raise ValueError(f"request {req.rid} needs {need} bytes, more than the whole budget")
+            if req.rid not in self.prepared:   # the host-side set-up is done once per request
+                ga, f = self.backend.setup(req.cfg)
+                ga.struct.hs_kf *= req.kf_scale
+                need = self.backend.bytes(ga, self.precision)
+                if need > self.hbm_budget:
+                    raise ValueError(f"request {req.rid} needs {need} bytes, more than the whole budget")
+                self.prepared[req.rid] = (ga, f, need)
+            ga, f, need = self.prepared[req.rid]
             if self.used + need > self.hbm_budget:
                 keep.append(req)
                 continue
-            ga.struct.hs_kf *= req.kf_scale
-            m = Model(ga, self.precision)
-            m.upload(f)
-            m.timestep(EPIC_SYNC_DIAGS_ONLY)
+            m = self.backend.model(ga, f, self.precision)
+            del self.prepared[req.rid]
             self.used += need
+            self.peak_used = max(self.peak_used, self.used)
             cls = _shape_class(req.cfg, self.precision)
             self.active.setdefault(cls, []).append(_Active(req, m, need, req.steps, self.now()))
         self.waiting = keep
 
-    # -- one scheduling round ---------------------------------------------------------------
-    def round(self) -> None:
-        launched = []
-        for cls, runs in self.active.items():
+    # -- one scheduling pass ----------------------------------------------------------------
+    def round(self) -> bool:
+        """Advance every shape class that is idle; a class whose batch is still running is left
+        alone, so classes of different sizes never wait for one another.  Returns whether any
+        class was handled."""
+        progressed = False
+        for cls in list(self.active):
+            runs = self.active[cls]
+            fl = self.inflight.get(cls)
+            if fl is not None:
+                b, n, members = fl
+                if not b.done():
+                    continue
+                b.sync()                          # reports a model error of any member
+                del self.inflight[cls]
+                progressed = True
+                for r in members:                 # runs admitted meanwhile were not in this batch
+                    r.remaining -= n
+                    if r.remaining <= 0:
+                        self._retire(cls, r)
             if not runs:
                 continue
             ids = tuple(r.req.rid for r in runs)
             b = self.batches.get(cls)
-            if b is None or b[1] != ids:
+            if b is None or b[1] != ids:          # a run joined or left: re-form the batch
                 if b is not None:
                     b[0].close()
-                b = (Batch([r.model for r in runs]), ids)
+                b = (self.backend.batch([r.model for r in runs]), ids)
                 self.batches[cls] = b
             n = min(self.round_steps, min(r.remaining for r in runs))
             b[0].run(n)
-            launched.append((cls, n))
-        for cls, n in launched:
-            self.batches[cls][0].sync()
-            done = []
-            for r in self.active[cls]:
-                r.remaining -= n
-                if r.remaining == 0:
-                    done.append(r)
-            for r in done:
-                self._retire(cls, r)
+            self.inflight[cls] = (b[0], n, list(runs))
+            progressed = True
+        return progressed
 
     def _retire(self, cls, r: _Active) -> None:
         f = r.model.download()
@@ -165,7 +202,8 @@ class RunServer:
             if self.waiting:
                 self.admit()
             if any(self.active.values()):
-                self.round()
+                if not self.round():
+                    time.sleep(0.0002)
             elif pending:
                 time.sleep(max(0.0, min(0.01, pending[0].arrival - self.now())))
         for b, _ in self.batches.values():

@@ -223,6 +223,7 @@ int  epic_batch_download(epic_batch *b, epic_fields *const *f);
  */
 int  epic_batch_step_host(epic_batch *b, epic_fields *const *f, int32_t groups, int32_t nsteps);
 int  epic_batch_sync(epic_batch *b);                       /* wait; first member error, if any */
+int  epic_batch_query(epic_batch *b);   /* 1: work queued on the batch finished, 0: still running */
 void *epic_batch_stream(epic_batch *b);
 int32_t epic_batch_kernels_per_step(const epic_batch *b);
 
