@@ -148,8 +148,43 @@ __device__ __forceinline__ double layer_p(const DevModel &M, double top, double 
   return xpow(M, (xpow(M, bot, kp1) - xpow(M, top, kp1)) / (kp1 * (bot - top)), 1. / M.kappa);
 }
 
+// ---- binary64 <-> binary32 conversions on the integer pipe ----
+//
+// GB300 executes FP64 arithmetic and the F64<->F32 conversion instructions on the same narrow
+// FP64 unit, about 1.7 operations per clock per SM against ~114 for FP32 adds (measured).  The
+// mixed form reads its binary64 state in every kernel, so it converts with a few integer
+// operations and selects instead (no branch).  For every normal binary32 result, zero,
+// infinity and overflow the bits are those of the hardware's round-to-nearest-even conversion;
+// a NaN stays a NaN; binary32 subnormals (magnitudes below 1.2e-38, which the model's fields
+// never hold except as exact zeros) are flushed to signed zero in both directions.
+__device__ __forceinline__ float d2f(double x) {
+  const unsigned hi = (unsigned)__double2hiint(x), lo = (unsigned)__double2loint(x);
+  const unsigned e = (hi >> 20) & 0x7ffu;
+  unsigned u = __funnelshift_l(lo, hi, 3) - (896u << 23);   // 8-bit exponent, 23 leading mantissa bits
+  const unsigned rest = lo & 0x1fffffffu;                    // the 29 bits dropped
+  u += (rest > 0x10000000u) | ((rest == 0x10000000u) & u);  // to nearest, ties to even
+  u = e < 897u ? 0u : u;
+  u = e > 1150u ? (((hi & 0xfffffu) | lo) && e == 2047u ? 0x7fc00000u : 0x7f800000u) : u;
+  return __uint_as_float(u | (hi & 0x80000000u));
+}
+__device__ __forceinline__ double f2d(float f) {
+  const unsigned w = __float_as_uint(f), a = w & 0x7fffffffu;
+  unsigned hi = (a >> 3) + (896u << 20), lo = a << 29;
+  hi = a >= 0x7f800000u ? hi + (896u << 20) : hi;            // infinity, NaN: exponent 2047
+  hi = a < 0x00800000u ? 0u : hi;
+  lo = a < 0x00800000u ? 0u : lo;
+  return __hiloint2double((int)(hi | (w & 0x80000000u)), (int)lo);
+}
+
 // ---- compute-type helpers for kernels instantiated in FP64 (R = double: the drop-in form,
 // bit-identical to the reference's arithmetic) and FP32 (R = float: the mixed form) ----
+
+// a binary64 value in the compute type, and a compute-type value back in binary64
+template <class R> __device__ __forceinline__ R cv(double x);
+template <> __device__ __forceinline__ double cv<double>(double x) { return x; }
+template <> __device__ __forceinline__ float cv<float>(double x) { return d2f(x); }
+__device__ __forceinline__ double to_d(double x) { return x; }
+__device__ __forceinline__ double to_d(float x) { return f2d(x); }
 
 template <class R> __device__ __forceinline__ R rmax(R x, R y) { return x > y ? x : y; }
 template <class R> __device__ __forceinline__ R rmin(R x, R y) { return x < y ? x : y; }

@@ -38,6 +38,8 @@ __global__ void k_source_sink(DevModel M) {
 // running sum, in the reference's order, so the results are those of one thread per column.
 constexpr int CT_WARPS = 8;
 constexpr int CT_THREADS = 32 * CT_WARPS;
+// levels per warp whose loads a column kernel issues together before using them
+constexpr int TILE_SLOTS = 4;
 
 struct ColTile {
   int lane, warp, j, i;
@@ -61,10 +63,10 @@ __device__ __forceinline__ ColTile col_tile(const DevModel &M) {
 // f_sigma/g_sigma (epic_funcs_diag.c:1271-1314) in the compute type, one exponential for both
 template <class R>
 __device__ __forceinline__ R f_and_g_sigma_r(const DevModel &M, R s, R &g) {
-  const R ss = R(M.sigma_sigma), z0 = R(M.zeta0), z1 = R(M.zeta1);
+  const R ss = cv<R>(M.sigma_sigma), z0 = cv<R>(M.zeta0), z1 = cv<R>(M.zeta1);
   if (s <= ss) g = R(0.);
   else if (s >= R(1.)) g = R(1.);
-  else g = R(M.g_coeff) * (R(1.) - RMath<R>::exp(M, -R(M.alpha) * (s - ss)));
+  else g = cv<R>(M.g_coeff) * (R(1.) - RMath<R>::exp(M, -cv<R>(M.alpha) * (s - ss)));
   if (s < R(0.)) return z0;
   if (s <= ss) return z0 + s * (z1 - z0);
   if (s < R(1.)) return (R(1.) - g) * (z0 + s * (z1 - z0));
@@ -97,9 +99,29 @@ __global__ void __launch_bounds__(CT_THREADS) k_calc_w(DevModel M) {
   const ColTile c = col_tile(M);
   const int nk = M.nk, ks = M.k_sigma, L = nk + 1;
   const long long n2 = M.n2;
-  R *P = sm, *LG = P + 32 * L, *DS = LG + 32 * L, *W = DS + 32 * L, *DF = W + 32 * L;
-  if (c.valid)
-    for (int k = c.warp; k <= nk; k += CT_WARPS) CT(P, k) = R(M.p3[c.base + k * n2]);
+  R *P = sm, *LG = P + 32 * L, *DS = LG + 32 * L, *W = DS + 32 * L, *DF = W + 32 * L, *DV = DF + 32 * L;
+  // Stage P3 and DIV_UV3 of every level, and THETA, HEAT3 and EXNER3 in the DS, W and DF rows
+  // that the pointwise pass reads before it overwrites them.  The loads of the first
+  // TILE_SLOTS levels of each warp are issued together so that their latencies overlap.
+  auto stage = [&](int k, double p3, double dv, double th, double ht, double ex) {
+    CT(P, k) = cv<R>(p3); CT(DV, k) = cv<R>(dv); CT(DS, k) = cv<R>(th); CT(W, k) = cv<R>(ht); CT(DF, k) = cv<R>(ex);
+  };
+  if (c.valid) {
+    double v[TILE_SLOTS][5];
+#pragma unroll
+    for (int r = 0; r < TILE_SLOTS; r++) {
+      const long long x = c.base + min(c.warp + r * CT_WARPS, nk) * n2;
+      v[r][0] = __ldg(M.p3 + x); v[r][1] = __ldg(M.div_uv3 + x); v[r][2] = __ldg(M.theta + x);
+      v[r][3] = __ldg(M.heat3 + x); v[r][4] = __ldg(M.exner3 + x);
+    }
+#pragma unroll
+    for (int r = 0; r < TILE_SLOTS; r++)
+      if (c.warp + r * CT_WARPS <= nk) stage(c.warp + r * CT_WARPS, v[r][0], v[r][1], v[r][2], v[r][3], v[r][4]);
+    for (int k = c.warp + TILE_SLOTS * CT_WARPS; k <= nk; k += CT_WARPS) {
+      const long long x = c.base + k * n2;
+      stage(k, M.p3[x], M.div_uv3[x], M.theta[x], M.heat3[x], M.exner3[x]);
+    }
+  }
   __syncthreads();
   const R ptop = CT(P, 0), pbot = CT(P, nk), psigma = CT(P, ks - 1);
   if (c.valid) {
@@ -108,26 +130,26 @@ __global__ void __launch_bounds__(CT_THREADS) k_calc_w(DevModel M) {
   }
   __syncthreads();
   const R lp = s_lp[c.lane];
-  const R eps13 = sizeof(R) == sizeof(float) ? R(4.9215666e-3) : R(M.eps13);   // cbrt(FLT_EPSILON)
+  const R eps13 = sizeof(R) == sizeof(float) ? R(4.9215666e-3) : cv<R>(M.eps13);   // cbrt(FLT_EPSILON)
   if (c.valid)
     for (int k = 1 + c.warp; k < nk; k += CT_WARPS) {
-      const long long x = c.base + k * n2;
       const R p3 = CT(P, k);
+      const R theta3 = CT(DS, k), heat = CT(W, k), exner = CT(DF, k);
       R w = R(0.);
       if (k < ks - 1) {
         const R sigma = RMath<R>::log(M, p3 / pbot) / lp;
         R g;
         f_and_g_sigma_r<R>(M, sigma, g);
-        w = g * R(M.heat3[x]) / R(M.exner3[x]);
+        w = g * heat / exner;
       }
       if (k >= 2) {
         const R P0 = CT(P, k - 2), P1 = CT(P, k - 1), P2 = p3, P3 = CT(P, k + 1);
         const R dz10 = CT(LG, k - 2), dz21 = CT(LG, k - 1), dz32 = CT(LG, k);
         const R dz20 = dz21 + dz10, dz30 = dz32 + dz20, dz31 = dz32 + dz21;
-        const R df0 = P0 * R(M.div_uv3[x - 2 * n2]);
-        const R df1 = P1 * R(M.div_uv3[x - n2]);
-        const R df2 = P2 * R(M.div_uv3[x]);
-        const R df3 = P3 * R(M.div_uv3[x + n2]);
+        const R df0 = P0 * CT(DV, k - 2);
+        const R df1 = P1 * CT(DV, k - 1);
+        const R df2 = P2 * CT(DV, k);
+        const R df3 = P3 * CT(DV, k + 1);
         CT(DS, k) = -(df0 * (dz21 * dz21 * dz21 * (dz31 + dz32)) / (dz10 * dz20 * dz30) +
                       df1 * (dz21 * (dz21 * (dz21 + R(2.) * (dz10 - dz31)) - R(6.) * dz10 * dz31)) / (dz10 * dz31) +
                       df2 * (dz21 * (dz21 * (dz21 + R(2.) * (dz32 - dz20)) - R(6.) * dz20 * dz32)) / (dz20 * dz32) +
@@ -135,7 +157,6 @@ __global__ void __launch_bounds__(CT_THREADS) k_calc_w(DevModel M) {
                     R(12.);
       }
       // dF/dp by a centred difference of return_sigmatheta at fixed theta and pbot
-      const R theta3 = R(M.theta[x]);
       const R dp = p3 * eps13;
       R p2 = rmax(p3 - dp * R(.5), ptop);
       const R p4 = rmin(p3 + dp * R(.5), pbot);
@@ -150,9 +171,9 @@ __global__ void __launch_bounds__(CT_THREADS) k_calc_w(DevModel M) {
     M.w3[c.base + nk * n2] = 0.;
     double sum_div = 0.;
     for (int k = 1; k < nk; k++) {
-      if (k >= 2) sum_div = sum_div + (double)CT(DS, k);
+      if (k >= 2) sum_div = sum_div + to_d(CT(DS, k));
       // SUM_DIV(nk) = 0, so the dF/dpbot term contributes nothing.
-      M.w3[c.base + k * n2] = (double)CT(W, k) - (sum_div * (double)CT(DF, k) + 0.);
+      M.w3[c.base + k * n2] = to_d(CT(W, k)) - (sum_div * to_d(CT(DF, k)) + 0.);
     }
   }
 }
@@ -176,20 +197,20 @@ __global__ void k_uv_drag(DevModel M) {
   const int jm = isv ? j - 1 : j, im = isv ? i : i - 1;   // neighbour averaged onto the u or v point
   for (int k = 0; k <= M.k_sponge; k++) {
     const long long x = M.at(k, j, i);
-    D[x] = D[x] - (double)(R(M.t_sponge_inv[k]) * (R(W[x]) - (isv ? R(0.) : R(M.u_spinup[x]))));
+    D[x] = D[x] - to_d(cv<R>(M.t_sponge_inv[k]) * (cv<R>(W[x]) - (isv ? R(0.) : cv<R>(M.u_spinup[x]))));
   }
   if (M.rayleigh_on) {
     // The zonal-mean Rayleigh drag block is not part of the supported configurations
     // (held_suarez sets prandtl = 0 and tau_drag = 1e20); epic_model_create rejects it.
   }
-  const R pbot = R(0.5) * (R(M.p3[M.at(nk, j, i)]) + R(M.p3[M.at(nk, jm, im)]));
+  const R pbot = R(0.5) * (cv<R>(M.p3[M.at(nk, j, i)]) + cv<R>(M.p3[M.at(nk, jm, im)]));
   for (int k = nk - 1; k >= 1; k--) {
-    const R p3 = R(.5) * (R(M.p3[M.at(k, j, i)]) + R(M.p3[M.at(k, jm, im)]));
+    const R p3 = R(.5) * (cv<R>(M.p3[M.at(k, j, i)]) + cv<R>(M.p3[M.at(k, jm, im)]));
     const R amp = (p3 / pbot - R(0.7)) / (R(1.) - R(0.7));
     if (amp < R(0.)) break;
-    const R nu0 = R(M.hs_kf) * amp;
+    const R nu0 = cv<R>(M.hs_kf) * amp;
     const long long x = M.at(k, j, i);
-    D[x] = D[x] - (double)(nu0 * R(W[x]));
+    D[x] = D[x] - to_d(nu0 * cv<R>(W[x]));
   }
 }
 
@@ -209,17 +230,17 @@ __global__ void __launch_bounds__(CT_THREADS) k_hsu_vertical(DevModel M, double 
   const long long n2 = M.n2;
   const bool layer = kind == 2;
   const int kf = kind == 1 ? M.k_sigma - 1 : 1;
-  const R ep = R(1.e-10), DT = R(M.dt);
+  const R ep = R(1.e-10), DT = cv<R>(M.dt);
   R *WA = sm, *WM = WA + 32 * L, *WP = WM + 32 * L, *PR = WP + 32 * L, *FF = PR + 32 * L;
-  auto amin = [&](int k) { return layer ? R(M.h_min[k]) : R(0.); };
-  auto dsi = [&](int kk) { return R(M.dsgth_inv[kk]); };
+  auto amin = [&](int k) { return layer ? cv<R>(M.h_min[k]) : R(0.); };
+  auto dsi = [&](int kk) { return cv<R>(M.dsgth_inv[kk]); };
   auto wa = [&](int k) { return CT(WA, k); };
   if (c.valid)
-    for (int k = (layer ? kf : kf - 1) + c.warp; k <= nk; k += CT_WARPS) CT(WA, k) = R(buff[c.base + k * n2]);
+    for (int k = (layer ? kf : kf - 1) + c.warp; k <= nk; k += CT_WARPS) CT(WA, k) = cv<R>(buff[c.base + k * n2]);
   if (layer) {
     if (c.valid)
       for (int k = kf - 1 + c.warp; k <= nk; k += CT_WARPS) {
-        const R w = R(M.w3[c.base + k * n2]);
+        const R w = cv<R>(M.w3[c.base + k * n2]);
         CT(WM, k) = rmin(R(0.), w);
         CT(WP, k) = rmax(R(0.), w);
       }
@@ -263,12 +284,12 @@ __global__ void __launch_bounds__(CT_THREADS) k_hsu_vertical(DevModel M, double 
     if (c.valid)
       for (int k = kf + c.warp; k <= nk; k += CT_WARPS) {
         const long long x = c.base + k * n2;
-        buff[x] = buff[x] + (double)((CT(FF, k) - CT(FF, k - 1)) * dsi(2 * k) * DT);
+        buff[x] = buff[x] + to_d((CT(FF, k) - CT(FF, k - 1)) * dsi(2 * k) * DT);
       }
   } else {
     if (c.valid)
       for (int k = kf + c.warp; k <= nk; k += CT_WARPS) {
-        const R w = (k == 1 || k == nk) ? R(0.) : R(.5) * (R(M.w3[c.base + k * n2]) + R(M.w3[c.base + (k - 1) * n2]));
+        const R w = (k == 1 || k == nk) ? R(0.) : R(.5) * (cv<R>(M.w3[c.base + k * n2]) + cv<R>(M.w3[c.base + (k - 1) * n2]));
         CT(WM, k) = rmin(R(0.), w);
         CT(WP, k) = rmax(R(0.), w);
       }
@@ -317,7 +338,7 @@ __global__ void __launch_bounds__(CT_THREADS) k_hsu_vertical(DevModel M, double 
       for (int k = kf + c.warp; k <= nk; k += CT_WARPS) {
         const long long x = c.base + k * n2;
         const R ffk1 = k == nk ? R(0.) : CT(FF, k + 1);
-        buff[x] = buff[x] + (double)((ffk1 - CT(FF, k)) * dsi(2 * k + 1) * DT);
+        buff[x] = buff[x] + to_d((ffk1 - CT(FF, k)) * dsi(2 * k + 1) * DT);
       }
   }
 }
@@ -543,17 +564,17 @@ __global__ void __launch_bounds__(CT_THREADS) k_pgrad_vars_column(DevModel M) {
 // relative error near 1e-7.
 
 // log(b/a) for b/a near 1, from the FP64 difference
-__device__ __forceinline__ float log_ratio_f(double a, double b) { return log1pf((float)(b - a) / (float)a); }
+__device__ __forceinline__ float log_ratio_f(double a, double b) { return log1pf(d2f(b - a) / d2f(a)); }
 
 // onto_kk(P2_INDEX) at a layer: ((bot^(k+1) - top^(k+1)) / ((k+1)(bot - top)))^(1/k), written as
 // bot * q^(1/kappa), q = (1 - r^(kappa+1)) / ((kappa+1)(1 - r)), r = top/bot.
 __device__ __forceinline__ double layer_p_mixed(const DevModel &M, double top, double bot) {
   if (fcmp(bot, top) == 0) return .5 * (bot + top);
-  const float kap = (float)M.kappa, kp1 = kap + 1.f;
-  const float eps = (float)(bot - top) / (float)bot;
+  const float kap = d2f(M.kappa), kp1 = kap + 1.f;
+  const float eps = d2f(bot - top) / d2f(bot);
   const float num = -expm1f(kp1 * log1pf(-eps));
   const float q = num / (kp1 * eps);
-  return bot * (double)expf(log1pf(q - 1.f) / kap);
+  return bot * f2d(expf(log1pf(q - 1.f) / kap));
 }
 
 __global__ void __launch_bounds__(CT_THREADS) k_set_p2etc_mixed(DevModel M, int update_theta) {
@@ -565,11 +586,23 @@ __global__ void __launch_bounds__(CT_THREADS) k_set_p2etc_mixed(DevModel M, int 
   const long long n2 = M.n2;
   double *P = sm, *HL = P + 32 * L, *TH = HL + 32 * L;
   const double g = M.grav[2 * c.j + 1];
-  if (c.valid)
-    for (int k = c.warp; k <= nk; k += CT_WARPS) {
-      CT(TH, k) = M.theta[c.base + k * n2];
-      if (k >= 1) CT(HL, k) = M.hdry[c.base + k * n2];
+  if (c.valid) {
+    double v[TILE_SLOTS][2];
+#pragma unroll
+    for (int r = 0; r < TILE_SLOTS; r++) {
+      const long long x = c.base + min(c.warp + r * CT_WARPS, nk) * n2;
+      v[r][0] = __ldg(M.theta + x); v[r][1] = __ldg(M.hdry + x);
     }
+#pragma unroll
+    for (int r = 0; r < TILE_SLOTS; r++) {
+      const int k = c.warp + r * CT_WARPS;
+      if (k <= nk) { CT(TH, k) = v[r][0]; CT(HL, k) = v[r][1]; }
+    }
+    for (int k = c.warp + TILE_SLOTS * CT_WARPS; k <= nk; k += CT_WARPS) {
+      CT(TH, k) = M.theta[c.base + k * n2];
+      CT(HL, k) = M.hdry[c.base + k * n2];
+    }
+  }
   __syncthreads();
   if (c.warp == 0 && c.valid) {
     double p = M.p3[c.base];
@@ -588,7 +621,7 @@ __global__ void __launch_bounds__(CT_THREADS) k_set_p2etc_mixed(DevModel M, int 
       CT(P, k) = pbot * xexp(M, sigma * lp);
     }
   __syncthreads();
-  const float lpf = (float)lp;
+  const float lpf = d2f(lp);
   if (c.valid)
     for (int k = c.warp; k <= nk; k += CT_WARPS) {
       const double pk = CT(P, k);
@@ -603,7 +636,7 @@ __global__ void __launch_bounds__(CT_THREADS) k_set_p2etc_mixed(DevModel M, int 
         const float sigma = log_ratio_f(pbot, pk) / lpf;
         float gs;
         const float fs = f_and_g_sigma_r<float>(M, sigma, gs);
-        const double th = (double)(((float)M.sgth[2 * k + 1] - fs) / gs);
+        const double th = f2d((d2f(M.sgth[2 * k + 1]) - fs) / gs);
         CT(TH, k) = th;
         M.theta[c.base + k * n2] = th;
       }
@@ -619,8 +652,8 @@ __global__ void __launch_bounds__(CT_THREADS) k_set_p2etc_mixed(DevModel M, int 
     double h;
     if (k == nk) h = CT(HL, nk);
     else {
-      const float topwt = (float)M.dsgth[2 * k], botwt = (float)M.dsgth[2 * k + 2];
-      h = (double)((topwt * (float)CT(HL, k) + botwt * (float)CT(HL, k + 1)) / (topwt + botwt));
+      const float topwt = d2f(M.dsgth[2 * k]), botwt = d2f(M.dsgth[2 * k + 2]);
+      h = f2d((topwt * d2f(CT(HL, k)) + botwt * d2f(CT(HL, k + 1))) / (topwt + botwt));
     }
     M.h3[x] = h;
     if (k == 1) M.h3[c.base] = h;
@@ -630,7 +663,7 @@ __global__ void __launch_bounds__(CT_THREADS) k_set_p2etc_mixed(DevModel M, int 
       const float sigma = log_ratio_f(pbot, p2) / lpf;
       float gs;
       const float fs = f_and_g_sigma_r<float>(M, sigma, gs);
-      t2 = (double)(((float)M.sgth[2 * k] - fs) / gs);
+      t2 = f2d((d2f(M.sgth[2 * k]) - fs) / gs);
     } else if (k == ks - 1) {
       t2 = .5 * (CT(TH, ks - 1) + CT(TH, ks - 2));
     } else {
@@ -655,7 +688,7 @@ __global__ void __launch_bounds__(CT_THREADS) k_set_p2etc_mixed(DevModel M, int 
   }
 }
 
-__global__ void __launch_bounds__(CT_THREADS) k_pgrad_vars_column_mixed(DevModel M) {
+__global__ void __launch_bounds__(CT_THREADS, 3) k_pgrad_vars_column_mixed(DevModel M) {
   epic_member(M);
   extern __shared__ double sm[];
   __shared__ double s_rho2_1[32];
@@ -665,31 +698,45 @@ __global__ void __launch_bounds__(CT_THREADS) k_pgrad_vars_column_mixed(DevModel
   const double mu = M.mu_dry;
   double *P = sm, *R = P + 32 * L, *T3 = R + 32 * L, *GZ = T3 + 32 * L;
   float *LG = reinterpret_cast<float *>(GZ + 32 * L);
-  const float kap = (float)M.kappa;
-  const float p0_inv = (float)(1. / M.press0);
-  const float mu_over_r = (float)(mu / 8.314472e+3);   // return_density: p mu / (R T)
-  if (c.valid)
-    for (int k = c.warp; k <= nk; k += CT_WARPS) {
+  const float kap = d2f(M.kappa);
+  const float p0_inv = d2f(1. / M.press0);
+  const float mu_over_r = d2f(mu / 8.314472e+3);   // return_density: p mu / (R T)
+  auto level = [&](int k, double theta, double p, double pr, double th2) {
       const long long x = c.base + k * n2;
-      const double theta = M.theta[x], p = M.p3[x];
-      const float pf = powf((float)p * p0_inv, kap);
-      const double t3 = theta * (double)pf;
+      const float pf = powf(d2f(p) * p0_inv, kap);
+      const double t3 = theta * f2d(pf);
       M.t3[x] = t3;
-      M.exner3[x] = M.cp * (double)pf;
-      const double rho = (double)((float)p * mu_over_r / (float)t3);
+      M.exner3[x] = M.cp * f2d(pf);
+      const double rho = f2d(d2f(p) * mu_over_r / d2f(t3));
       M.rho3[x] = rho;
       CT(P, k) = p;
       CT(R, k) = rho;
       CT(T3, k) = t3;
       if (k >= 1) {
-        const double pr = M.p2[x];
-        const double t2 = M.theta2[x] * (double)powf((float)pr * p0_inv, kap);
+        const double t2 = th2 * f2d(powf(d2f(pr) * p0_inv, kap));
         M.t2[x] = t2;
-        const double r2 = (double)((float)pr * mu_over_r / (float)t2);
+        const double r2 = f2d(d2f(pr) * mu_over_r / d2f(t2));
         M.rho2[x] = r2;
         if (k == 1) s_rho2_1[c.lane] = r2;
       }
+  };
+  if (c.valid) {
+    // the loads of the first TILE_SLOTS levels of this warp are issued together (their
+    // latencies overlap); level 0's P2 and THETA2 are loaded but not used
+    double v[TILE_SLOTS][4];
+#pragma unroll
+    for (int r = 0; r < TILE_SLOTS; r++) {
+      const long long x = c.base + min(c.warp + r * CT_WARPS, nk) * n2;
+      v[r][0] = __ldg(M.theta + x); v[r][1] = __ldg(M.p3 + x); v[r][2] = __ldg(M.p2 + x); v[r][3] = __ldg(M.theta2 + x);
     }
+#pragma unroll
+    for (int r = 0; r < TILE_SLOTS; r++)
+      if (c.warp + r * CT_WARPS <= nk) level(c.warp + r * CT_WARPS, v[r][0], v[r][1], v[r][2], v[r][3]);
+    for (int k = c.warp + TILE_SLOTS * CT_WARPS; k <= nk; k += CT_WARPS) {
+      const long long x = c.base + k * n2;
+      level(k, M.theta[x], M.p3[x], M.p2[x], M.theta2[x]);
+    }
+  }
   __syncthreads();
   if (c.valid) {
     for (int k = c.warp; k < nk; k += CT_WARPS) CT(LG, k) = log_ratio_f(CT(P, k), CT(P, k + 1));
@@ -706,9 +753,9 @@ __global__ void __launch_bounds__(CT_THREADS) k_pgrad_vars_column_mixed(DevModel
       const float dz20 = dz21 + dz10, dz30 = dz32 + dz20, dz31 = dz32 + dz21;
       // p/rho = R T / mu
       const float r_over_mu = 1.f / mu_over_r;
-      const float df0 = r_over_mu * (float)CT(T3, k + 1), df1 = r_over_mu * (float)CT(T3, k);
-      const float df2 = r_over_mu * (float)CT(T3, k - 1), df3 = r_over_mu * (float)CT(T3, k - 2);
-      CT(GZ, k - 1) = (double)(-(df0 * (dz21 * dz21 * dz21 * (dz31 + dz32)) / (dz10 * dz20 * dz30) +
+      const float df0 = r_over_mu * d2f(CT(T3, k + 1)), df1 = r_over_mu * d2f(CT(T3, k));
+      const float df2 = r_over_mu * d2f(CT(T3, k - 1)), df3 = r_over_mu * d2f(CT(T3, k - 2));
+      CT(GZ, k - 1) = f2d(-(df0 * (dz21 * dz21 * dz21 * (dz31 + dz32)) / (dz10 * dz20 * dz30) +
                                  df1 * (dz21 * (dz21 * (dz21 + 2.f * (dz10 - dz31)) - 6.f * dz10 * dz31)) / (dz10 * dz31) +
                                  df2 * (dz21 * (dz21 * (dz21 + 2.f * (dz32 - dz20)) - 6.f * dz20 * dz32)) / (dz20 * dz32) +
                                  df3 * (dz21 * dz21 * dz21 * (dz10 + dz20)) / (dz30 * dz31 * dz32)) /
@@ -718,34 +765,44 @@ __global__ void __launch_bounds__(CT_THREADS) k_pgrad_vars_column_mixed(DevModel
   if (c.warp == 0 && c.valid) {   // GZ3 from the surface up, in FP64
     double gz = M.topo_scale * M.gz_surface[M.at2(c.j, c.i)];
     CT(GZ, nk) = gz;
-    gz = gz + ((CT(P, nk) + CT(P, nk - 1)) / (CT(R, nk) + CT(R, nk - 1))) * (double)CT(LG, nk - 1);
+    gz = gz + ((CT(P, nk) + CT(P, nk - 1)) / (CT(R, nk) + CT(R, nk - 1))) * f2d(CT(LG, nk - 1));
     CT(GZ, nk - 1) = gz;
     for (int k = nk - 1; k >= 2; k--) {
       gz = gz + CT(GZ, k - 1);
       CT(GZ, k - 1) = gz;
     }
-    CT(GZ, 0) = gz + ((CT(P, 1) + CT(P, 0)) / (CT(R, 1) + CT(R, 0))) * (double)CT(LG, 0);
+    CT(GZ, 0) = gz + ((CT(P, 1) + CT(P, 0)) / (CT(R, 1) + CT(R, 0))) * f2d(CT(LG, 0));
   }
   __syncthreads();
   if (!c.valid) return;
   const bool interior = c.i >= 1 && c.i <= M.ni;
   const long long itime = M.ctl->itime;
-  for (int k = c.warp; k <= nk; k += CT_WARPS) {
+  const double dtg_inv = -1. / (M.dt * M.grav[2 * c.j + 1]);
+  auto level_out = [&](int k, double old, double w, double h) {
     const long long x = c.base + k * n2;
     const double gzk = CT(GZ, k);
-    const double old = M.gz3[x];
     M.gz3[x] = gzk;
     M.mont3[x] = gzk + return_enthalpy(M, CT(T3, k));
     if (interior && k >= 1) {
       double dz = 0.;
-      if (itime > 1) {
-        const double dtg_inv = -1. / (M.dt * M.grav[2 * c.j + 1]);
-        dz = (old - gzk) * dtg_inv;
-      }
-      dz += (double)((float)M.w3[x] * (float)M.h3[x] / (float)CT(R, k));
+      if (itime > 1) dz = (old - gzk) * dtg_inv;
+      dz += f2d(d2f(w) * d2f(h) / d2f(CT(R, k)));
       M.dzdt3[x] = dz;
       if (gzk >= CT(GZ, k - 1)) flag_error(M.ctl, ERR_GZ_MONOTONE, k, c.j, c.i, gzk);
     }
+  };
+  double v[TILE_SLOTS][3];
+#pragma unroll
+  for (int r = 0; r < TILE_SLOTS; r++) {
+    const long long x = c.base + min(c.warp + r * CT_WARPS, nk) * n2;
+    v[r][0] = M.gz3[x]; v[r][1] = __ldg(M.w3 + x); v[r][2] = __ldg(M.h3 + x);
+  }
+#pragma unroll
+  for (int r = 0; r < TILE_SLOTS; r++)
+    if (c.warp + r * CT_WARPS <= nk) level_out(c.warp + r * CT_WARPS, v[r][0], v[r][1], v[r][2]);
+  for (int k = c.warp + TILE_SLOTS * CT_WARPS; k <= nk; k += CT_WARPS) {
+    const long long x = c.base + k * n2;
+    level_out(k, M.gz3[x], M.w3[x], M.h3[x]);
   }
 }
 
@@ -762,15 +819,15 @@ __global__ void k_pgrad_dzdt(DevModel M) {
   const int jj = 2 * j;
   const Ctl *c = M.ctl;
   const double *U = M.u + (long long)c->it_uv * M.n3, *V = M.v + (long long)c->it_uv * M.n3;
-  const R gdx_inv3 = R(.5) * R(M.m[jj + 1]) / R(M.grav[jj + 1]);
-  const R gdy_inv2 = R(.5) * R(M.n[jj]) / R(M.grav[jj]);
-  const R gdy_inv4 = R(.5) * R(M.n[jj + 2]) / R(M.grav[jj + 2]);
+  const R gdx_inv3 = R(.5) * cv<R>(M.m[jj + 1]) / cv<R>(M.grav[jj + 1]);
+  const R gdy_inv2 = R(.5) * cv<R>(M.n[jj]) / cv<R>(M.grav[jj]);
+  const R gdy_inv4 = R(.5) * cv<R>(M.n[jj + 2]) / cv<R>(M.grav[jj + 2]);
   const double *G = M.gz3;
   const long long x = M.at(k, j, i);
   // geopotential differences are formed in FP64 in both forms
-  const R add = R(V[x]) * R(G[x] - G[M.at(k, j - 1, i)]) * gdy_inv2 + R(V[M.at(k, j + 1, i)]) * R(G[M.at(k, j + 1, i)] - G[x]) * gdy_inv4 +
-                R(U[x]) * R(G[x] - G[M.at(k, j, i - 1)]) * gdx_inv3 + R(U[M.at(k, j, i + 1)]) * R(G[M.at(k, j, i + 1)] - G[x]) * gdx_inv3;
-  write_with_pads(M.dzdt3, M, M.at(k, j, 0), i, M.dzdt3[x] + (double)add);
+  const R add = cv<R>(V[x]) * cv<R>(G[x] - G[M.at(k, j - 1, i)]) * gdy_inv2 + cv<R>(V[M.at(k, j + 1, i)]) * cv<R>(G[M.at(k, j + 1, i)] - G[x]) * gdy_inv4 +
+                cv<R>(U[x]) * cv<R>(G[x] - G[M.at(k, j, i - 1)]) * gdx_inv3 + cv<R>(U[M.at(k, j, i + 1)]) * cv<R>(G[M.at(k, j, i + 1)] - G[x]) * gdx_inv3;
+  write_with_pads(M.dzdt3, M, M.at(k, j, 0), i, M.dzdt3[x] + to_d(add));
 }
 
 // Monotone fix of the filtered GZ copy, epic_timestep.c:182-195 (the zonal filter of planes
@@ -806,21 +863,21 @@ __global__ void k_calc_heating(DevModel M) {
   if (k >= 1 && k <= M.nk && j >= 0 && j <= M.nj && M.newt_cool_on) {
     const long long x = M.at(k, j, ii);
     const R ka = R(1.) / (R(40.) * R(60.) * R(60.) * R(24.)), ks = R(1.) / (R(4.) * R(60.) * R(60.) * R(24.));
-    const R pressure = R(M.p3[x]);
-    const R pbot = R(M.p3[M.at(M.nk, j, ii)]);
+    const R pressure = cv<R>(M.p3[x]);
+    const R pbot = cv<R>(M.p3[M.at(M.nk, j, ii)]);
     const R amp = (pressure / pbot - R(0.7)) / (R(1.) - R(0.7));
     R kt = ka;
     if (amp > R(0.)) kt += (ks - ka) * RMath<R>::cos4(M, j) * amp;   // pow(cos(lat), 4.), per row
     const R cp_over_time = R(1004.) / (R(1.) / kt);
-    R c2 = R(M.coslat[j]);
+    R c2 = cv<R>(M.coslat[j]);
     c2 *= c2;
     const R s2 = R(1.) - c2;
     const R p_p0 = pressure / (R(1000.) * R(100.));
     R lg;
-    const R pw = RMath<R>::log_pow(M, p_p0, R(M.kappa), lg);
+    const R pw = RMath<R>::log_pow(M, p_p0, cv<R>(M.kappa), lg);
     R teq = (R(315.) - R(60.) * s2 - R(10.) * lg * c2) * pw;
     teq = rmax(R(200.), teq);
-    val = -cp_over_time * (R(M.t3[x]) - teq);
+    val = -cp_over_time * (cv<R>(M.t3[x]) - teq);
   }
   M.heat3[t] = val;
 }
@@ -850,7 +907,7 @@ int launch_source_sink(const DevModel &M, cudaStream_t s) { k_source_sink<<<zg(n
 static inline unsigned ntile_blocks(const DevModel &M) { return epic_blocks((long long)(M.nj + 1) * (M.ni + 2), 32); }
 static inline size_t tile_smem(const DevModel &M, int arrays) { return (size_t)arrays * 32 * (M.nk + 1) * sizeof(double); }
 int launch_calc_w(const DevModel &M, cudaStream_t s) {
-  EPIC_LAUNCH_R(M.mixed, k_calc_w, ntile_blocks(M), CT_THREADS, tile_smem(M, 5), s, M);
+  EPIC_LAUNCH_R(M.mixed, k_calc_w, ntile_blocks(M), CT_THREADS, tile_smem(M, 6), s, M);
   return 0;
 }
 int launch_uv_drag(const DevModel &M, cudaStream_t s) {
@@ -889,7 +946,7 @@ int launch_advection_prep(const DevModel &M, int phase, cudaStream_t s) {
 // at nk = EPIC_MAX_NK, above the 48 KB default.  The limit is raised once to that maximum, so
 // models of different sizes in one process never lower it for one another.
 int column_kernels_init(int) {
-  const int big = (int)(5 * 32 * (EPIC_MAX_NK + 1) * sizeof(double));
+  const int big = (int)(6 * 32 * (EPIC_MAX_NK + 1) * sizeof(double));
   const int hv = (int)(5 * 32 * (EPIC_MAX_NK + 2) * sizeof(double));
   if (cudaFuncSetAttribute(k_calc_w<double>, cudaFuncAttributeMaxDynamicSharedMemorySize, big) != cudaSuccess ||
       cudaFuncSetAttribute(k_calc_w<float>, cudaFuncAttributeMaxDynamicSharedMemorySize, big) != cudaSuccess ||

@@ -137,10 +137,10 @@ __device__ void filter_row_smem(const DevModel &M, R *x, const double *hl, long 
   // spectral weights (epic_adjust.c:447-453)
   for (int q = threadIdx.x; q < N; q += blockDim.x) {
     if (q == 0) {
-      z[0].re *= R(hl[rowbase + 1]);
-      z[0].im *= R(hl[rowbase + N + 1]);
+      z[0].re *= cv<R>(hl[rowbase + 1]);
+      z[0].im *= cv<R>(hl[rowbase + N + 1]);
     } else {
-      const R h = R(hl[rowbase + q + 1]);
+      const R h = cv<R>(hl[rowbase + q + 1]);
       z[q].re *= h;
       z[q].im *= h;
     }
@@ -196,7 +196,7 @@ __global__ void k_filter_planes(DevModel M, const double *src, int src_sel, doub
     return;
   }
   load_twiddles(M, fs);
-  for (int i = threadIdx.x; i <= M.ni + 1; i += blockDim.x) x[i] = R(src[base + i]);
+  for (int i = threadIdx.x; i <= M.ni + 1; i += blockDim.x) x[i] = cv<R>(src[base + i]);
   __syncthreads();
   filter_row_smem(M, x, vgrid ? M.high_lat_pv : M.high_lat_h, M.at2(j, 0), fs);
   for (int i = threadIdx.x + 1; i <= M.ni; i += blockDim.x) write_with_pads(dst, M, base, i, x[i]);
@@ -317,42 +317,42 @@ __global__ void k_varz_filter_rows(DevModel M, double *buff, int sel, int index,
   for (int i = threadIdx.x + 1; i <= M.ni; i += blockDim.x) {
     R gzz;
     switch (index) {
-      case 0: gzz = R(.5) * (R(gz[M.at(k, j, i)]) + R(gz[M.at(k, j, i - 1)])); break;
-      case 1: gzz = R(.5) * (R(gz[M.at(k, j, i)]) + R(gz[M.at(k, j - 1, i)])); break;
-      case 2: gzz = R(.5) * (R(gz[M.at(k, j, i)]) + R(gz[M.at(k - 1, j, i)])); break;
-      default: gzz = R(gz[M.at(k, j, i)]); break;
+      case 0: gzz = R(.5) * (cv<R>(gz[M.at(k, j, i)]) + cv<R>(gz[M.at(k, j, i - 1)])); break;
+      case 1: gzz = R(.5) * (cv<R>(gz[M.at(k, j, i)]) + cv<R>(gz[M.at(k, j - 1, i)])); break;
+      case 2: gzz = R(.5) * (cv<R>(gz[M.at(k, j, i)]) + cv<R>(gz[M.at(k - 1, j, i)])); break;
+      default: gzz = cv<R>(gz[M.at(k, j, i)]); break;
     }
     // find_place_in_table (epic_funcs_util.c:2908-2967) and splint_pchip (:926-946)
     int kay;
-    if (RMath<R>::cmp(gzz, R(t[0].x)) <= 0) kay = 0;
-    else if (RMath<R>::cmp(gzz, R(t[n - 1].x)) >= 0) kay = n - 2;
+    if (RMath<R>::cmp(gzz, cv<R>(t[0].x)) <= 0) kay = 0;
+    else if (RMath<R>::cmp(gzz, cv<R>(t[n - 1].x)) >= 0) kay = n - 2;
     else {
       int il = -1, iu = n;
       while (iu - il > 1) {
         const int im = (iu + il) >> 1;
-        if (RMath<R>::cmp(gzz, R(t[im].x)) >= 0) il = im; else iu = im;
+        if (RMath<R>::cmp(gzz, cv<R>(t[im].x)) >= 0) il = im; else iu = im;
       }
       kay = il;
     }
     const Trip *tk = t + kay;
-    const R h = R(tk[1].x) - R(tk[0].x);
-    const R delta = (R(tk[1].y) - R(tk[0].y)) / h;
-    const R del1 = (R(tk[0].z) - delta) / h;
-    const R del2 = (R(tk[1].z) - delta) / h;
+    const R h = cv<R>(tk[1].x) - cv<R>(tk[0].x);
+    const R delta = (cv<R>(tk[1].y) - cv<R>(tk[0].y)) / h;
+    const R del1 = (cv<R>(tk[0].z) - delta) / h;
+    const R del2 = (cv<R>(tk[1].z) - delta) / h;
     const R c3 = (del1 + del2) / h;
     const R c2 = -(del1 + del1 + del2);
-    const R xx = gzz - R(tk[0].x);
-    R v = R(tk[0].y) + xx * (R(tk[0].z) + xx * (c2 + xx * c3));
+    const R xx = gzz - cv<R>(tk[0].x);
+    R v = cv<R>(tk[0].y) + xx * (cv<R>(tk[0].z) + xx * (c2 + xx * c3));
     if (index == 2) v = RMath<R>::exp(M, v);
     vz[i] = v;
-    x[i] = R(buff[base + i] - (double)v);
+    x[i] = cv<R>(buff[base + i] - to_d(v));
   }
   __syncthreads();
   if (filt) filter_row_smem(M, x, vgrid ? M.high_lat_pv : M.high_lat_h, M.at2(j, 0), fs);
   // The mixed form leaves unfiltered rows untouched (their subtract-and-add-back is the
   // identity up to one rounding); the FP64 form repeats the reference's arithmetic on them.
   if (!filt && sizeof(R) == sizeof(float)) return;
-  for (int i = threadIdx.x + 1; i <= M.ni; i += blockDim.x) write_with_pads(buff, M, base, i, (double)x[i] + (double)vz[i]);
+  for (int i = threadIdx.x + 1; i <= M.ni; i += blockDim.x) write_with_pads(buff, M, base, i, to_d(x[i]) + to_d(vz[i]));
 }
 
 // Zonal pass of hsu_advection (epic_flux.c:1316-1484) for one row: the fluxes come from a
@@ -368,19 +368,19 @@ __global__ void k_hsu_zonal(DevModel M, double *buff, int kind, int kstart) {
   const int k = kstart + (int)blockIdx.y;
   R *a = sm, *um = a + W, *up = um + W, *ff = up + W, *ap = ff + W, *d1 = ap + W, *d2 = d1 + W, *aa = d2 + W;
   FilterSmem<R> fs = carve_filter(aa + W, ni);
-  const R ep = R(1.e-10), DT = R(M.dt);
-  const R a_min = kind == 1 ? R(M.h_min[k]) : R(0.);
+  const R ep = R(1.e-10), DT = cv<R>(M.dt);
+  const R a_min = kind == 1 ? cv<R>(M.h_min[k]) : R(0.);
   const long long base = M.at(k, j, 0);
   const bool filt = row_is_filtered(M, j, 0);
   if (filt) load_twiddles(M, fs);
   const double *U = M.u + (long long)M.ctl->it_uv * M.n3;
-  const R n_inv = R(1.) / R(M.n[2 * j + 1]);
-  const R mn1 = R(M.mn[2 * j + 1]);
+  const R n_inv = R(1.) / cv<R>(M.n[2 * j + 1]);
+  const R mn1 = cv<R>(M.mn[2 * j + 1]);
   for (int i = threadIdx.x; i <= ni + 1; i += blockDim.x) {
-    a[i] = R(buff[base + i]);
+    a[i] = cv<R>(buff[base + i]);
     // u2d, with periodic pads for the layer average (bc_lateral(u2d))
     const int ii = kind == 1 ? (i == 0 ? ni : (i == ni + 1 ? 1 : i)) : i;
-    const R u2d = kind == 1 ? R(.5) * (R(U[M.at(k, j, ii)]) + R(U[M.at(k - 1, j, ii)])) : R(U[M.at(k, j, i)]);
+    const R u2d = kind == 1 ? R(.5) * (cv<R>(U[M.at(k, j, ii)]) + cv<R>(U[M.at(k - 1, j, ii)])) : cv<R>(U[M.at(k, j, i)]);
     um[i] = rmin(R(0.), u2d * n_inv);
     up[i] = rmax(R(0.), u2d * n_inv);
   }
@@ -431,7 +431,7 @@ __global__ void k_hsu_zonal(DevModel M, double *buff, int kind, int kstart) {
   if (threadIdx.x == 0) { ff[0] = ff[ni]; ff[ni + 1] = ff[1]; }
   __syncthreads();
   for (int i = threadIdx.x + 1; i <= ni; i += blockDim.x) {
-    write_with_pads(buff, M, base, i, buff[base + i] + (double)((ff[i] - ff[i + 1]) * mn1 * DT));
+    write_with_pads(buff, M, base, i, buff[base + i] + to_d((ff[i] - ff[i + 1]) * mn1 * DT));
   }
 }
 

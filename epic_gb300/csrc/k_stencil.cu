@@ -49,14 +49,14 @@ __global__ void k_zero_tend(DevModel M) {
 template <class R>
 __device__ __forceinline__ R kin_at(const DevModel &M, const double *Uk, const double *Vk, int j, int i) {
   const int jj = 2 * j;
-  const R mn1 = R(M.mn[jj + 1]), mni0 = R(M.mn_inv[jj]), mni2 = R(M.mn_inv[jj + 2]);
-  R u2 = R(Uk[M.at2(j, i)]), u4 = R(Uk[M.at2(j, i + 1)]), v2 = R(Vk[M.at2(j, i)]), v4 = R(Vk[M.at2(j + 1, i)]);
+  const R mn1 = cv<R>(M.mn[jj + 1]), mni0 = cv<R>(M.mn_inv[jj]), mni2 = cv<R>(M.mn_inv[jj + 2]);
+  R u2 = cv<R>(Uk[M.at2(j, i)]), u4 = cv<R>(Uk[M.at2(j, i + 1)]), v2 = cv<R>(Vk[M.at2(j, i)]), v4 = cv<R>(Vk[M.at2(j + 1, i)]);
   const R kin_c = (u2 * u2 + u4 * u4 + mn1 * (v2 * v2 * mni0 + v4 * v4 * mni2)) * R(.25);
   if (j == 0 || j == M.nj) return kin_c;
-  u2 = R(.5) * (R(Uk[M.at2(j + 1, i)]) + R(Uk[M.at2(j - 1, i)]));
-  u4 = R(.5) * (R(Uk[M.at2(j + 1, i + 1)]) + R(Uk[M.at2(j - 1, i + 1)]));
-  v2 = R(.5) * (R(Vk[M.at2(j, i + 1)]) + R(Vk[M.at2(j, i - 1)]));
-  v4 = R(.5) * (R(Vk[M.at2(j + 1, i + 1)]) + R(Vk[M.at2(j + 1, i - 1)]));
+  u2 = R(.5) * (cv<R>(Uk[M.at2(j + 1, i)]) + cv<R>(Uk[M.at2(j - 1, i)]));
+  u4 = R(.5) * (cv<R>(Uk[M.at2(j + 1, i + 1)]) + cv<R>(Uk[M.at2(j - 1, i + 1)]));
+  v2 = R(.5) * (cv<R>(Vk[M.at2(j, i + 1)]) + cv<R>(Vk[M.at2(j, i - 1)]));
+  v4 = R(.5) * (cv<R>(Vk[M.at2(j + 1, i + 1)]) + cv<R>(Vk[M.at2(j + 1, i - 1)]));
   const R kin_s = (u2 * u2 + u4 * u4 + mn1 * (v2 * v2 * mni0 + v4 * v4 * mni2)) * R(.25);
   return (R(5.) / R(6.)) * kin_c + (R(1.) / R(6.)) * kin_s;
 }
@@ -65,16 +65,16 @@ template <class R>
 __device__ __forceinline__ R uh_at(const DevModel &M, const double *Uk, const double *Hk, int j, int i) {
   if (j < 0 || j > M.nj) return R(0.);
   i = wrap_i(M, i);
-  const R havg = R(.5) * (R(Hk[M.at2(j, i)]) + R(Hk[M.at2(j, i - 1)]));
-  return R(Uk[M.at2(j, i)]) * havg * (R(1.) / R(M.n[2 * j + 1]));
+  const R havg = R(.5) * (cv<R>(Hk[M.at2(j, i)]) + cv<R>(Hk[M.at2(j, i - 1)]));
+  return cv<R>(Uk[M.at2(j, i)]) * havg * (R(1.) / cv<R>(M.n[2 * j + 1]));
 }
 // VH(j,i) for j = 1..nj (0 at the poles), periodic in i
 template <class R>
 __device__ __forceinline__ R vh_at(const DevModel &M, const double *Vk, const double *Hk, int j, int i) {
   if (j < 1 || j > M.nj) return R(0.);
   i = wrap_i(M, i);
-  const R havg = R(.5) * (R(Hk[M.at2(j, i)]) + R(Hk[M.at2(j - 1, i)]));
-  return R(Vk[M.at2(j, i)]) * havg * (R(1.) / R(M.m[2 * j]));
+  const R havg = R(.5) * (cv<R>(Hk[M.at2(j, i)]) + cv<R>(Hk[M.at2(j - 1, i)]));
+  return cv<R>(Vk[M.at2(j, i)]) * havg * (R(1.) / cv<R>(M.m[2 * j]));
 }
 
 // Kinetic energy per mass on the h grid, planes k = 1..nk-1, into work0 (with pads).
@@ -100,19 +100,19 @@ __global__ void k_uv_core_v(DevModel M) {
   const double *Uk = U + k * M.n2, *Hk = M.h3 + k * M.n2;
   const double *PV = M.pv3 + k * M.n2, *KIN = M.work0 + k * M.n2;
   double *D = M.dvdt + plane_offset(M, PL_UV_TEND);
-  auto pv = [&](int jj, int ii) { return R(PV[M.at2(jj, ii)]); };
+  auto pv = [&](int jj, int ii) { return cv<R>(PV[M.at2(jj, ii)]); };
   const R ga = (pv(j, i) + pv(j, i + 1) + pv(j + 1, i + 1));
   const R de = (pv(j, i) + pv(j + 1, i) + pv(j, i + 1));
   const R al = (pv(j - 1, i) + pv(j, i) + pv(j, i + 1));
   const R be = (pv(j, i) + pv(j, i + 1) + pv(j - 1, i + 1));
   const R core = ((-ga * uh_at<R>(M, Uk, Hk, j, i + 1) - de * uh_at<R>(M, Uk, Hk, j, i) - al * uh_at<R>(M, Uk, Hk, j - 1, i) -
                    be * uh_at<R>(M, Uk, Hk, j - 1, i + 1)) * (R(1.) / R(12.)) +
-                  R(KIN[M.at2(j - 1, i)]) - R(KIN[M.at2(j, i)])) * R(M.n[2 * j]);
+                  cv<R>(KIN[M.at2(j - 1, i)]) - cv<R>(KIN[M.at2(j, i)])) * cv<R>(M.n[2 * j]);
   const long long x = M.at(k, j, i);
-  double d = D[x] + (double)core;
+  double d = D[x] + to_d(core);
   const int kk = 2 * k + 1;
-  d -= (double)(R(.5) * (R(M.w3[x]) + R(M.w3[M.at(k, j - 1, i)])) * (R(V[M.at(k - 1, j, i)]) - R(V[M.at(k + 1, j, i)])) /
-                (R(M.sgth[kk - 2]) - R(M.sgth[kk + 2])));
+  d -= to_d(R(.5) * (cv<R>(M.w3[x]) + cv<R>(M.w3[M.at(k, j - 1, i)])) * (cv<R>(V[M.at(k - 1, j, i)]) - cv<R>(V[M.at(k + 1, j, i)])) /
+                (cv<R>(M.sgth[kk - 2]) - cv<R>(M.sgth[kk + 2])));
   D[x] = d;
 }
 
@@ -128,19 +128,19 @@ __global__ void k_uv_core_u(DevModel M) {
   const double *Vk = V + k * M.n2, *Hk = M.h3 + k * M.n2;
   const double *PV = M.pv3 + k * M.n2, *KIN = M.work0 + k * M.n2;
   double *D = M.dudt + plane_offset(M, PL_UV_TEND);
-  auto pv = [&](int jj, int ii) { return R(PV[M.at2(jj, ii)]); };
+  auto pv = [&](int jj, int ii) { return cv<R>(PV[M.at2(jj, ii)]); };
   const R al = (pv(j, i) + pv(j + 1, i) + pv(j + 1, i + 1));
   const R be = (pv(j + 1, i - 1) + pv(j + 1, i) + pv(j, i));
   const R ga = (pv(j, i - 1) + pv(j, i) + pv(j + 1, i));
   const R de = (pv(j, i) + pv(j + 1, i) + pv(j, i + 1));
   const R core = ((al * vh_at<R>(M, Vk, Hk, j + 1, i) + be * vh_at<R>(M, Vk, Hk, j + 1, i - 1) + ga * vh_at<R>(M, Vk, Hk, j, i - 1) +
                    de * vh_at<R>(M, Vk, Hk, j, i)) * (R(1.) / R(12.)) +
-                  R(KIN[M.at2(j, i - 1)]) - R(KIN[M.at2(j, i)])) * R(M.m[2 * j + 1]);
+                  cv<R>(KIN[M.at2(j, i - 1)]) - cv<R>(KIN[M.at2(j, i)])) * cv<R>(M.m[2 * j + 1]);
   const long long x = M.at(k, j, i);
-  double d = D[x] + (double)core;
+  double d = D[x] + to_d(core);
   const int kk = 2 * k + 1;
-  d -= (double)(R(.5) * (R(M.w3[x]) + R(M.w3[M.at(k, j, i - 1)])) * (R(U[M.at(k - 1, j, i)]) - R(U[M.at(k + 1, j, i)])) /
-                (R(M.sgth[kk - 2]) - R(M.sgth[kk + 2])));
+  d -= to_d(R(.5) * (cv<R>(M.w3[x]) + cv<R>(M.w3[M.at(k, j, i - 1)])) * (cv<R>(U[M.at(k - 1, j, i)]) - cv<R>(U[M.at(k + 1, j, i)])) /
+                (cv<R>(M.sgth[kk - 2]) - cv<R>(M.sgth[kk + 2])));
   D[x] = d;
 }
 
@@ -169,19 +169,51 @@ __global__ void k_gz_pole_rows(DevModel M) {
 
 // The finite-volume force is a sum of face integrals that is unchanged when every GZ3 (or every
 // P2) of the stencil moves by one constant; the mixed form evaluates it in FP32 on
-// GZ3 - GZ3(k,j,i) and P2 - P2(k,j,i) (formed in FP64), which keeps the FP32 products near the
-// size of the differences the force is made of.  The FP64 form uses the values as they are.
+// GZ3 - GZ3(k,j,i) and P2 - P2(k,j,i), which keeps the FP32 products near the size of the
+// differences the force is made of.  The differences are formed in FP32 from (hi, lo) splits of
+// GZ3 and P2 (hi = float(x), lo = float(x - hi); k_pgrad_split, in scratch work1 and work2) as
+// (hi_x - hi_ref) + (lo_x - lo_ref): within a rounding or two of the FP64 difference, with no
+// FP64 operation per stencil point.  The FP64 form uses the values as they are.
+__global__ void k_pgrad_split(DevModel M) {
+  epic_member(M);
+  const long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= M.n3) return;
+  const double z = M.gz3[t], p = M.p2[t];
+  const float zh = d2f(z), ph = d2f(p);
+  reinterpret_cast<float2 *>(M.work1)[t] = make_float2(zh, d2f(z - f2d(zh)));
+  reinterpret_cast<float2 *>(M.work2)[t] = make_float2(ph, d2f(p - f2d(ph)));
+}
 template <class R>
 struct PgradRef {
-  double z, p;
-  __device__ __forceinline__ PgradRef(const DevModel &M, int k, int j, int i) {
-    if (sizeof(R) == sizeof(double)) { z = 0.; p = 0.; }
-    else { z = M.gz3[M.at(k, j, i)]; p = M.p2[M.at(k, j, i)]; }
+  const DevModel &M;
+  float2 zr, pr;
+  __device__ __forceinline__ PgradRef(const DevModel &M_, int k, int j, int i) : M(M_) {
+    if constexpr (sizeof(R) == sizeof(float)) {
+      zr = reinterpret_cast<const float2 *>(M.work1)[M.at(k, j, i)];
+      pr = reinterpret_cast<const float2 *>(M.work2)[M.at(k, j, i)];
+    }
+  }
+  __device__ __forceinline__ R z(long long x) const {
+    if constexpr (sizeof(R) == sizeof(double)) return M.gz3[x];
+    else { const float2 v = reinterpret_cast<const float2 *>(M.work1)[x]; return (v.x - zr.x) + (v.y - zr.y); }
+  }
+  __device__ __forceinline__ R p(long long x) const {
+    if constexpr (sizeof(R) == sizeof(double)) return M.p2[x];
+    else { const float2 v = reinterpret_cast<const float2 *>(M.work2)[x]; return (v.x - pr.x) + (v.y - pr.y); }
   }
 };
+// Width of a u (v) control volume in longitude (latitude), radians, between the faces at
+// half-levels ii-1 and ii+1: the FP64 form subtracts the two face coordinates in the compute
+// type as the reference does; the mixed form subtracts in FP64 first (FP32 face coordinates
+// of up to 2 pi would lose five digits to cancellation).
+template <class R>
+__device__ __forceinline__ R face_width(const double *deg, int iw, int ie) {
+  if constexpr (sizeof(R) == sizeof(double)) return deg[ie] * (M_PI / 180.) - deg[iw] * (M_PI / 180.);
+  else return d2f((deg[ie] - deg[iw]) * (M_PI / 180.));
+}
 
 template <class R>
-struct LonFace { R zbse, zbne, ztse, ztne, zbe, zte, pbe, pte, east, ln; };
+struct LonFace { R zbse, zbne, ztse, ztne, zbe, zte, pbe, pte, east; };
 
 // East face of the u control volume at column i+c-1 (the quantities the reference carries
 // from one i to the next).  z[a][b][c]: GZ3 at level k+a-1, row j+b-1, column i+c-1;
@@ -190,7 +222,6 @@ template <class R>
 __device__ __forceinline__ LonFace<R> lon_face(const DevModel &M, const R (&z)[3][3][2], const R (&p)[2][2], int c, int i) {
   auto gz = [&](int a, int b) { return z[a][b][c]; };
   LonFace<R> f;
-  f.ln = R(M.lon[2 * i + 1] * (M_PI / 180.));
   f.zbse = R(.25) * (gz(1, 1) + gz(1, 0) + gz(2, 1) + gz(2, 0));
   f.zbne = R(.25) * (gz(1, 1) + gz(1, 2) + gz(2, 1) + gz(2, 2));
   f.ztse = R(.25) * (gz(1, 1) + gz(1, 0) + gz(0, 1) + gz(0, 0));
@@ -220,14 +251,14 @@ __global__ void k_pgrad_lon(DevModel M) {
 #pragma unroll
     for (int b = 0; b < 3; b++)
 #pragma unroll
-      for (int q = 0; q < 2; q++) z[a][b][q] = R(M.gz3[M.at(k + a - 1, j + b - 1, i + q - 1)] - ref.z);
+      for (int q = 0; q < 2; q++) z[a][b][q] = ref.z(M.at(k + a - 1, j + b - 1, i + q - 1));
 #pragma unroll
   for (int a = 0; a < 2; a++)
 #pragma unroll
-    for (int q = 0; q < 2; q++) p[a][q] = R(M.p2[M.at(k + a, j, i + q - 1)] - ref.p);
+    for (int q = 0; q < 2; q++) p[a][q] = ref.p(M.at(k + a, j, i + q - 1));
   const LonFace<R> w = lon_face<R>(M, z, p, 0, i - 1), e = lon_face<R>(M, z, p, 1, i);
-  const R rho = R(.5) * (R(M.rho3[M.at(k, j, i)]) + R(M.rho3[M.at(k, j, i - 1)]));
-  const R rlns = R(M.rln[2 * j]), rlnn = R(M.rln[2 * j + 2]);
+  const R rho = R(.5) * (cv<R>(M.rho3[M.at(k, j, i)]) + cv<R>(M.rho3[M.at(k, j, i - 1)]));
+  const R rlns = cv<R>(M.rln[2 * j]), rlnn = cv<R>(M.rln[2 * j + 2]);
   R a1 = e.ztne + e.ztse, a2 = w.ztne + w.ztse;
   R terms2 = R(3.) * (a1 - a2), top, bottom;
   if (fabs(R(2.) * (e.zte - w.zte) / (e.zte + w.zte - e.zbe - w.zbe)) > DLOGZ_TOL) {
@@ -250,13 +281,13 @@ __global__ void k_pgrad_lon(DevModel M) {
   R pgflon = top - bottom + R(0.) - R(0.) + w.east - e.east;
   const R dzn = e.ztne - e.zbne + w.ztne - w.zbne;
   const R dzs = e.ztse - e.zbse + w.ztse - w.zbse;
-  pgflon /= (e.ln - w.ln) * rho * (rlns * (dzs + R(.5) * dzn) + rlnn * (dzn + R(.5) * dzs));
+  pgflon /= face_width<R>(M.lon, 2 * i - 1, 2 * i + 1) * rho * (rlns * (dzs + R(.5) * dzn) + rlnn * (dzn + R(.5) * dzs));
   const long long x = plane_offset(M, PL_UV_TEND) + M.at(k, j, i);
-  M.dudt[x] = M.dudt[x] + (double)pgflon;
+  M.dudt[x] = M.dudt[x] + to_d(pgflon);
 }
 
 template <class R>
-struct LatFace { R zbnw, zbne, ztnw, ztne, zbn, ztn, pbn, ptn, north, rln, lt; };
+struct LatFace { R zbnw, zbne, ztnw, ztne, zbn, ztn, pbn, ptn, north, rln; };
 
 // North face of the v control volume at row j+b-1.  z[a][b][c]: GZ3 at level k+a-1, row j+b-1,
 // column i+c-1; p[a][b][c]: P2 at level k+a, row j+b-1, column i+c-1 (shifted by the reference
@@ -265,8 +296,7 @@ template <class R>
 __device__ __forceinline__ LatFace<R> lat_face(const DevModel &M, const R (&z)[3][2][3], const R (&p)[2][2][3], int b, int jrow) {
   auto gz = [&](int a, int c) { return z[a][b][c]; };
   LatFace<R> f;
-  f.rln = R(M.rln[2 * jrow + 1]);
-  f.lt = R(M.lat[2 * jrow + 1] * (M_PI / 180.));
+  f.rln = cv<R>(M.rln[2 * jrow + 1]);
   f.zbnw = R(.25) * (gz(1, 1) + gz(1, 0) + gz(2, 1) + gz(2, 0));
   f.zbne = R(.25) * (gz(1, 1) + gz(1, 2) + gz(2, 1) + gz(2, 2));
   f.ztnw = R(.25) * (gz(1, 1) + gz(1, 0) + gz(0, 1) + gz(0, 0));
@@ -296,19 +326,19 @@ __global__ void k_pgrad_lat(DevModel M) {
 #pragma unroll
     for (int b = 0; b < 2; b++)
 #pragma unroll
-      for (int q = 0; q < 3; q++) z[a][b][q] = R(M.gz3[M.at(k + a - 1, j + b - 1, i + q - 1)] - ref.z);
+      for (int q = 0; q < 3; q++) z[a][b][q] = ref.z(M.at(k + a - 1, j + b - 1, i + q - 1));
 #pragma unroll
   for (int a = 0; a < 2; a++)
 #pragma unroll
     for (int b = 0; b < 2; b++)
 #pragma unroll
-      for (int q = 0; q < 3; q++) p[a][b][q] = R(M.p2[M.at(k + a, j + b - 1, i + q - 1)] - ref.p);
+      for (int q = 0; q < 3; q++) p[a][b][q] = ref.p(M.at(k + a, j + b - 1, i + q - 1));
   // z(level k+a-1, row j+b-1, column i+q-1), pp(level k+a, row j+b-1, column i+q-1)
   auto gz = [&](int a, int b, int q) { return z[a][b][q]; };
   auto pp = [&](int a, int b, int q) { return p[a][b][q]; };
   const LatFace<R> s = lat_face<R>(M, z, p, 0, j - 1), n = lat_face<R>(M, z, p, 1, j);
-  const R rho = R(.5) * (R(M.rho3[M.at(k, j, i)]) + R(M.rho3[M.at(k, j - 1, i)]));
-  const R rlt = R(M.rlt[2 * j]);
+  const R rho = R(.5) * (cv<R>(M.rho3[M.at(k, j, i)]) + cv<R>(M.rho3[M.at(k, j - 1, i)]));
+  const R rlt = cv<R>(M.rlt[2 * j]);
   const R rlns = s.rln, rlnn = n.rln;
   const R south = s.north, north = n.north;
   // s-face values carried over from row j-1: zbsw = zbnw(j-1), zbse = zbne(j-1), ...
@@ -360,9 +390,9 @@ __global__ void k_pgrad_lat(DevModel M) {
   R pgflat = top - bottom + south - (north + west + east);
   const R dzn = n.ztne - n.zbne + n.ztnw - n.zbnw;
   const R dzs = ztse - zbse + ztsw - zbsw;
-  pgflat /= (n.lt - s.lt) * rho * rlt * (rlns * (dzs + R(.5) * dzn) + rlnn * (dzn + R(.5) * dzs));
+  pgflat /= face_width<R>(M.lat, 2 * j - 1, 2 * j + 1) * rho * rlt * (rlns * (dzs + R(.5) * dzn) + rlnn * (dzn + R(.5) * dzs));
   const long long x = plane_offset(M, PL_UV_TEND) + M.at(k, j, i);
-  M.dvdt[x] = M.dvdt[x] + (double)pgflat;
+  M.dvdt[x] = M.dvdt[x] + to_d(pgflat);
 }
 
 // ---------------------------------------------------------------------------------------------
@@ -374,9 +404,9 @@ template <class R>
 __device__ __forceinline__ void vmp(const DevModel &M, const double *V, int kind, int k, int j, int i, R &vm, R &vp) {
   R v2d;
   if (j < 0 || j > M.nj + 1) { vm = vp = R(0.); return; }
-  if (kind == 2) v2d = (j >= 1 && j <= M.nj) ? R(.5) * (R(V[M.at(k, j, i)]) + R(V[M.at(k - 1, j, i)])) : R(0.);
-  else v2d = R(V[M.at(k, j, i)]);
-  const R mi = (fabs(M.lat[2 * j]) == 90.) ? R(0.) : R(1.) / R(M.m[2 * j]);
+  if (kind == 2) v2d = (j >= 1 && j <= M.nj) ? R(.5) * (cv<R>(V[M.at(k, j, i)]) + cv<R>(V[M.at(k - 1, j, i)])) : R(0.);
+  else v2d = cv<R>(V[M.at(k, j, i)]);
+  const R mi = (fabs(M.lat[2 * j]) == 90.) ? R(0.) : R(1.) / cv<R>(M.m[2 * j]);
   vm = rmin(R(0.), v2d * mi);
   vp = rmax(R(0.), v2d * mi);
 }
@@ -391,7 +421,7 @@ __global__ void k_hsu_merid_pred(DevModel M, const double *A, int kind, int k0) 
   if (c.j >= 1 && c.j <= M.nj) {
     R vm, vp;
     vmp<R>(M, V, kind, c.k, c.j, c.i, vm, vp);
-    ff = vp * R(A[M.at(c.k, c.j - 1, c.i)]) + vm * R(A[M.at(c.k, c.j, c.i)]);
+    ff = vp * cv<R>(A[M.at(c.k, c.j - 1, c.i)]) + vm * cv<R>(A[M.at(c.k, c.j, c.i)]);
   }
   write_with_pads(M.work1, M, M.at(c.k, c.j, 0), c.i, ff);
 }
@@ -403,8 +433,8 @@ __global__ void k_hsu_merid_apred(DevModel M, const double *A, int k0) {
   if (!cell3(M, k0, M.nk - k0 + 1, 0, M.nj + 1, c)) return;
   const double *FF = M.work1;
   const long long x = M.at(c.k, c.j, c.i);
-  const R da = (R(FF[x]) - R(FF[M.at(c.k, c.j + 1, c.i)])) * R(M.mn[2 * c.j + 1]) * R(M.dt);
-  write_with_pads(M.work2, M, M.at(c.k, c.j, 0), c.i, A[x] + (double)da);
+  const R da = (cv<R>(FF[x]) - cv<R>(FF[M.at(c.k, c.j + 1, c.i)])) * cv<R>(M.mn[2 * c.j + 1]) * cv<R>(M.dt);
+  write_with_pads(M.work2, M, M.at(c.k, c.j, 0), c.i, A[x] + to_d(da));
 }
 
 template <class R>
@@ -415,12 +445,12 @@ __global__ void k_hsu_merid_corr(DevModel M, const double *A, int kind, int k0) 
   const int k = c.k, j = c.j, i = c.i, nj = M.nj;
   R ffv = R(0.);
   if (j >= 1 && j <= nj) {
-    const R ep = R(1.e-10), DT = R(M.dt);
-    const R a_min = kind == 2 ? R(M.h_min[k]) : R(0.);
+    const R ep = R(1.e-10), DT = cv<R>(M.dt);
+    const R a_min = kind == 2 ? cv<R>(M.h_min[k]) : R(0.);
     const double *V = M.v + plane_offset(M, PL_UV);
     const double *AP = M.work2;
-    auto a = [&](int jj) { return R(A[M.at(k, jj, i)]); };
-    auto ap = [&](int jj) { return R(AP[M.at(k, jj, i)]); };
+    auto a = [&](int jj) { return cv<R>(A[M.at(k, jj, i)]); };
+    auto ap = [&](int jj) { return cv<R>(AP[M.at(k, jj, i)]); };
     auto diff1 = [&](int jj) { return jj == 0 ? R(0.) : ap(jj) - a(jj - 1); };
     auto diff2 = [&](int jj) { return jj == nj ? R(0.) : ap(jj) - a(jj + 1); };
     auto aaa = [&](int jj) {
@@ -437,7 +467,7 @@ __global__ void k_hsu_merid_corr(DevModel M, const double *A, int kind, int k0) 
     ffv = R(.5) * (vp * (ap(j) + a(j - 1)) + vm * (ap(j - 1) + a(j)));
     const R vhatp = sqrt(vp * vpm);
     const R vhatm = -sqrt(vm * vmp1);
-    const R mu = (vp - vm) * R(M.mn[2 * j]) * DT;
+    const R mu = (vp - vm) * cv<R>(M.mn[2 * j]) * DT;
     const R al = (R(1.) + mu) / R(6.);
     const R am1 = aaa(j - 1), a0 = aaa(j);
     const R prod = (a(j - 1) - a_min) * (a(j) - a_min);
@@ -457,8 +487,8 @@ __global__ void k_hsu_merid_update(DevModel M, double *A, int k0) {
   if (!cell3(M, k0, M.nk - k0 + 1, 0, M.nj + 1, c)) return;
   const double *FF = M.work3;
   const long long x = M.at(c.k, c.j, c.i);
-  const R da = (R(FF[x]) - R(FF[M.at(c.k, c.j + 1, c.i)])) * R(M.mn[2 * c.j + 1]) * R(M.dt);
-  write_with_pads(A, M, M.at(c.k, c.j, 0), c.i, A[x] + (double)da);
+  const R da = (cv<R>(FF[x]) - cv<R>(FF[M.at(c.k, c.j + 1, c.i)])) * cv<R>(M.mn[2 * c.j + 1]) * cv<R>(M.dt);
+  write_with_pads(A, M, M.at(c.k, c.j, 0), c.i, A[x] + to_d(da));
 }
 
 // ---------------------------------------------------------------------------------------------
@@ -475,8 +505,8 @@ __global__ void k_d2dy2(DevModel M, const double *src, int src_sel, double *dst,
   src += plane_offset(M, src_sel);
   const int k = c.k, j = c.j, i = c.i, nj = M.nj;
   const double *cf = (vgrid ? M.v_coef : M.h_coef) + 3 * j;
-  const R a0 = R(diff_coef) * R(cf[0]), a1 = R(diff_coef) * R(cf[1]), a2 = R(diff_coef) * R(cf[2]);
-  auto h = [&](int jj) { return R(src[M.at(k, jj, i)]); };
+  const R a0 = cv<R>(diff_coef) * cv<R>(cf[0]), a1 = cv<R>(diff_coef) * cv<R>(cf[1]), a2 = cv<R>(diff_coef) * cv<R>(cf[2]);
+  auto h = [&](int jj) { return cv<R>(src[M.at(k, jj, i)]); };
   R d;
   const int jlast = vgrid ? nj + 1 : nj;
   if (j == 0) d = a0 * h(0) + a1 * h(1) + a2 * h(2);
@@ -493,7 +523,7 @@ __global__ void k_visc_apply(DevModel M, double *A, int sel, const double *D, in
   if (!cell3(M, k0, nkk, vgrid ? 1 : 0, vgrid ? M.nj : M.nj + 1, c)) return;
   A += plane_offset(M, sel);
   const long long x = M.at(c.k, c.j, c.i);
-  write_with_pads(A, M, M.at(c.k, c.j, 0), c.i, A[x] + (double)(R(M.dt) * R(sign) * R(D[x])));
+  write_with_pads(A, M, M.at(c.k, c.j, 0), c.i, A[x] + to_d(cv<R>(M.dt) * cv<R>(sign) * cv<R>(D[x])));
 }
 
 // zonal_hyperviscosity, epic_subgrid.c:715-808: one warp per row (j, k), rows_per_block rows
@@ -513,7 +543,7 @@ __global__ void k_zonal_visc(DevModel M, double *A, int sel, int jbot, int jhalf
   double *a = reinterpret_cast<double *>(smraw + w * row_bytes);
   R *hh = reinterpret_cast<R *>(a + (ni + 2)), *d = hh + (ni + 2);
   const unsigned full = 0xffffffffu;
-  for (int i = lane; i <= ni + 1; i += 32) { a[i] = A[base + i]; hh[i] = R(a[i]); }
+  for (int i = lane; i <= ni + 1; i += 32) { a[i] = A[base + i]; hh[i] = cv<R>(a[i]); }
   __syncwarp();
   const bool taper = fabs(M.lat[2 * j + jhalf]) > M.lat0;
   const double mm = M.m[2 * j + jhalf];
@@ -522,7 +552,7 @@ __global__ void k_zonal_visc(DevModel M, double *A, int sel, int jbot, int jhalf
   // fully unrolled so that M.coef[], M.nu[] are indexed by constants (M stays in registers)
 #pragma unroll
   for (int itmp = 2; itmp <= 8; itmp += 2) {
-    const R dc = R(taper ? M.coef[itmp] * M.m0 * M.m0 : M.coef[itmp] * mm * mm);
+    const R dc = cv<R>(taper ? M.coef[itmp] * M.m0 * M.m0 : M.coef[itmp] * mm * mm);
     for (int i = lane + 1; i <= ni; i += 32) d[i] = dc * (hh[i - 1] - R(2.) * hh[i] + hh[i + 1]);
     __syncwarp();
     R mean;
@@ -535,12 +565,12 @@ __global__ void k_zonal_visc(DevModel M, double *A, int sel, int jbot, int jhalf
         for (int i = 1; i <= ni; i++) fm += d[i];
         mv = fm / ni;
       }
-      mean = R(__shfl_sync(full, mv, 0));
+      mean = cv<R>(__shfl_sync(full, mv, 0));
     } else {
       double fm = 0.;
-      for (int i = lane + 1; i <= ni; i += 32) fm += (double)d[i];
+      for (int i = lane + 1; i <= ni; i += 32) fm += to_d(d[i]);
       for (int o = 16; o > 0; o >>= 1) fm += __shfl_xor_sync(full, fm, o);
-      mean = R(fm / ni);
+      mean = cv<R>(fm / ni);
       if (lane == 0) {
         d[ni + 1] = d[1];
         d[0] = d[ni];
@@ -550,7 +580,7 @@ __global__ void k_zonal_visc(DevModel M, double *A, int sel, int jbot, int jhalf
     for (int i = lane; i <= ni + 1; i += 32) d[i] -= mean;
     __syncwarp();
     if (M.nu[itmp] > 0.) {
-      for (int i = lane + 1; i <= ni; i += 32) a[i] += (double)(R(M.dt) * sign * d[i]);
+      for (int i = lane + 1; i <= ni; i += 32) a[i] += to_d(cv<R>(M.dt) * sign * d[i]);
       any_applied = true;
     }
     sign = -sign;
@@ -574,12 +604,12 @@ __global__ void k_zonal_visc(DevModel M, double *A, int sel, int jbot, int jhalf
 template <class R>
 __device__ __forceinline__ R div_at(const DevModel &M, const double *UU, const double *VV, int k, int j, int i) {
   const int jj = 2 * j + 1;
-  const R n_inv = R(1.) / R(M.n[jj]);
-  const R mn1 = R(M.mn[jj]);
-  const R m2j_inv = (j == 0) ? R(0.) : R(1.) / R(M.m[jj - 1]);
-  const R m2jp2_inv = (j == M.nj) ? R(0.) : R(1.) / R(M.m[jj + 1]);
-  return mn1 * ((R(UU[M.at(k, j, i + 1)]) * n_inv - R(UU[M.at(k, j, i)]) * n_inv) +
-                (R(VV[M.at(k, j + 1, i)]) * m2jp2_inv - R(VV[M.at(k, j, i)]) * m2j_inv));
+  const R n_inv = R(1.) / cv<R>(M.n[jj]);
+  const R mn1 = cv<R>(M.mn[jj]);
+  const R m2j_inv = (j == 0) ? R(0.) : R(1.) / cv<R>(M.m[jj - 1]);
+  const R m2jp2_inv = (j == M.nj) ? R(0.) : R(1.) / cv<R>(M.m[jj + 1]);
+  return mn1 * ((cv<R>(UU[M.at(k, j, i + 1)]) * n_inv - cv<R>(UU[M.at(k, j, i)]) * n_inv) +
+                (cv<R>(VV[M.at(k, j + 1, i)]) * m2jp2_inv - cv<R>(VV[M.at(k, j, i)]) * m2j_inv));
 }
 
 template <class R>
@@ -600,15 +630,15 @@ __global__ void k_pv_interior(DevModel M, const double *VV) {
   const int k = c.k, j = c.j, i = c.i;
   const double *UU = M.u + plane_offset(M, PL_UV);
   const double *HH = M.h3;
-  const R f2j = R(M.f[2 * j]), m2j = R(M.m[2 * j]), n2j = R(M.n[2 * j]);
-  const R m_m1_inv = R(1.) / R(M.m[2 * j - 1]), m_p1_inv = R(1.) / R(M.m[2 * j + 1]);
-  const R mn_m1_inv = R(1.) / R(M.mn[2 * j - 1]), mn_p1_inv = R(1.) / R(M.mn[2 * j + 1]);
+  const R f2j = cv<R>(M.f[2 * j]), m2j = cv<R>(M.m[2 * j]), n2j = cv<R>(M.n[2 * j]);
+  const R m_m1_inv = R(1.) / cv<R>(M.m[2 * j - 1]), m_p1_inv = R(1.) / cv<R>(M.m[2 * j + 1]);
+  const R mn_m1_inv = R(1.) / cv<R>(M.mn[2 * j - 1]), mn_p1_inv = R(1.) / cv<R>(M.mn[2 * j + 1]);
   const R mn_pv = R(.5) / (mn_m1_inv + mn_p1_inv);
-  const R ze = m2j * ((R(VV[M.at(k, j, i)]) - R(VV[M.at(k, j, i - 1)])) +
-                      n2j * (R(UU[M.at(k, j - 1, i)]) * m_m1_inv - R(UU[M.at(k, j, i)]) * m_p1_inv));
+  const R ze = m2j * ((cv<R>(VV[M.at(k, j, i)]) - cv<R>(VV[M.at(k, j, i - 1)])) +
+                      n2j * (cv<R>(UU[M.at(k, j - 1, i)]) * m_m1_inv - cv<R>(UU[M.at(k, j, i)]) * m_p1_inv));
   R pv = (ze + f2j);
-  const R h_pv = ((R(HH[M.at(k, j, i)]) + R(HH[M.at(k, j, i - 1)])) * mn_p1_inv +
-                  (R(HH[M.at(k, j - 1, i)]) + R(HH[M.at(k, j - 1, i - 1)])) * mn_m1_inv) * mn_pv;
+  const R h_pv = ((cv<R>(HH[M.at(k, j, i)]) + cv<R>(HH[M.at(k, j, i - 1)])) * mn_p1_inv +
+                  (cv<R>(HH[M.at(k, j - 1, i)]) + cv<R>(HH[M.at(k, j - 1, i - 1)])) * mn_m1_inv) * mn_pv;
   pv /= h_pv;
   write_with_pads(M.pv3, M, M.at(k, j, 0), i, pv);
 }
@@ -653,8 +683,8 @@ __global__ void k_ri2(DevModel M) {
   const int k = c.k, j = c.j, i = c.i;
   const long long off = plane_offset(M, PL_UV);
   const double *U = M.u + off, *V = M.v + off;
-  auto u = [&](int kk, int jj, int ii) { return R(U[M.at(kk, jj, ii)]); };
-  auto v = [&](int kk, int jj, int ii) { return R(V[M.at(kk, jj, ii)]); };
+  auto u = [&](int kk, int jj, int ii) { return cv<R>(U[M.at(kk, jj, ii)]); };
+  auto v = [&](int kk, int jj, int ii) { return cv<R>(V[M.at(kk, jj, ii)]); };
   R dudz2 = R(.5) * (u(k - 1, j, i) + u(k - 1, j, i + 1) - u(k, j, i) - u(k, j, i + 1));
   R dvdz2 = R(.5) * (v(k - 1, j, i) + v(k - 1, j + 1, i) - v(k, j, i) + v(k, j + 1, i));
   dudz2 *= dudz2;
@@ -662,14 +692,14 @@ __global__ void k_ri2(DevModel M) {
   R ri;
   if (RMath<R>::cmp(dudz2, R(0.)) != 0) {
     const long long x = M.at(k, j, i);
-    const R pressure = R(M.p2[x]), temperature = R(M.t2[x]), density = R(M.rho2[x]);
-    const R cp = R(1004.), mu = R(M.mu_dry);
+    const R pressure = cv<R>(M.p2[x]), temperature = cv<R>(M.t2[x]), density = cv<R>(M.rho2[x]);
+    const R cp = R(1004.), mu = cv<R>(M.mu_dry);
     const R deltap = R(0.001) * pressure, deltaT = R(0.001) * temperature;
     auto dens = [&](R p, R t) { return p * mu / (R(8.314472e+3) * t); };   // return_density
     const R drho_dp_T = (dens(pressure + deltap, temperature) - dens(pressure - deltap, temperature)) / (R(2.) * deltap);
     const R drho_dT_p = (dens(pressure, temperature + deltaT) - dens(pressure, temperature - deltaT)) / (R(2.) * deltaT);
-    const R Drho_Dp = (R(M.rho3[x]) - R(M.rho3[M.at(k - 1, j, i)])) / (R(M.p3[x]) - R(M.p3[M.at(k - 1, j, i)]));
-    const R g = R(M.grav[2 * j + 1]);
+    const R Drho_Dp = (cv<R>(M.rho3[x]) - cv<R>(M.rho3[M.at(k - 1, j, i)])) / (cv<R>(M.p3[x]) - cv<R>(M.p3[M.at(k - 1, j, i)]));
+    const R g = cv<R>(M.grav[2 * j + 1]);
     const R brunt2 = g * g * (Drho_Dp - drho_dp_T + temperature / (cp * density * density) * drho_dT_p * drho_dT_p);
     ri = brunt2 / (dudz2 + dvdz2);
   } else {
@@ -693,13 +723,13 @@ __global__ void k_divdamp_apply(DevModel M, double nudiv) {
   const double *DIV = M.work2;
   const long long off = plane_offset(M, PL_UV_TEND);
   if (!isv) {
-    const R coef = R((M.lat[2 * j + 1] > M.lat0) ? nudiv * M.m0 : nudiv * M.m[2 * j + 1]);
+    const R coef = cv<R>((M.lat[2 * j + 1] > M.lat0) ? nudiv * M.m0 : nudiv * M.m[2 * j + 1]);
     const long long x = off + M.at(k, j, i);
-    M.dudt[x] = M.dudt[x] + (double)(coef * (R(DIV[M.at(k, j, i)]) - R(DIV[M.at(k, j, i - 1)])));
+    M.dudt[x] = M.dudt[x] + to_d(coef * (cv<R>(DIV[M.at(k, j, i)]) - cv<R>(DIV[M.at(k, j, i - 1)])));
   } else if (j >= 1) {
-    const R coef = R(nudiv * M.n[2 * j]);
+    const R coef = cv<R>(nudiv * M.n[2 * j]);
     const long long x = off + M.at(k, j, i);
-    M.dvdt[x] = M.dvdt[x] + (double)(coef * (R(DIV[M.at(k, j, i)]) - R(DIV[M.at(k, j - 1, i)])));
+    M.dvdt[x] = M.dvdt[x] + to_d(coef * (cv<R>(DIV[M.at(k, j, i)]) - cv<R>(DIV[M.at(k, j - 1, i)])));
   }
 }
 
@@ -810,6 +840,7 @@ int launch_uv_core(const DevModel &M, cudaStream_t s) {
 
 int launch_uv_pgrad(const DevModel &M, cudaStream_t s) {
   k_gz_pole_rows<<<zg(M.nk + 1, M), 128, 0, s>>>(M);
+  if (M.mixed) k_pgrad_split<<<zg(epic_blocks(M.n3, TB(M, TB_POINT)), M), TB(M, TB_POINT), 0, s>>>(M);
   EPIC_LAUNCH_R(M.mixed, k_pgrad_lon, cells_blocks(M, M.nk - 1, M.nj + 1, TB(M, TB_PGRAD)), TB(M, TB_PGRAD), 0, s, M);
   EPIC_LAUNCH_R(M.mixed, k_pgrad_lat, cells_blocks(M, M.nk - 1, M.nj, TB(M, TB_PGRAD)), TB(M, TB_PGRAD), 0, s, M);
   return 0;
