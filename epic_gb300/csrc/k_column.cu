@@ -567,11 +567,13 @@ __global__ void __launch_bounds__(CT_THREADS) k_pgrad_vars_column(DevModel M) {
 __device__ __forceinline__ float log_ratio_f(double a, double b) { return log1pf(d2f(b - a) / d2f(a)); }
 
 // onto_kk(P2_INDEX) at a layer: ((bot^(k+1) - top^(k+1)) / ((k+1)(bot - top)))^(1/k), written as
-// bot * q^(1/kappa), q = (1 - r^(kappa+1)) / ((kappa+1)(1 - r)), r = top/bot.
+// bot * q^(1/kappa), q = (1 - r^(kappa+1)) / ((kappa+1)(1 - r)), r = top/bot.  The FP32
+// expression stays accurate as eps = 1 - r goes to zero (log1p/expm1), so only eps = 0 needs
+// the reference's equal-pressure branch.
 __device__ __forceinline__ double layer_p_mixed(const DevModel &M, double top, double bot) {
-  if (fcmp(bot, top) == 0) return .5 * (bot + top);
   const float kap = d2f(M.kappa), kp1 = kap + 1.f;
   const float eps = d2f(bot - top) / d2f(bot);
+  if (eps == 0.f) return .5 * (bot + top);
   const float num = -expm1f(kp1 * log1pf(-eps));
   const float q = num / (kp1 * eps);
   return bot * f2d(expf(log1pf(q - 1.f) / kap));
@@ -611,24 +613,24 @@ __global__ void __launch_bounds__(CT_THREADS) k_set_p2etc_mixed(DevModel M, int 
       p = p + M.dsgth[2 * k] * g * CT(HL, k);
       CT(P, k) = p;
     }
-    s_lp[c.lane] = xlog(M, CT(P, 0) / p);
+    s_lp[c.lane] = log(CT(P, 0) / p);   // binary64 libdevice log: the mixed form needs no correct rounding
   }
   __syncthreads();
   const double ptop = CT(P, 0), pbot = CT(P, nk), lp = s_lp[c.lane];
-  if (c.valid)
-    for (int k = ks - 1 + c.warp; k < nk; k += CT_WARPS) {
-      const double sigma = (M.sgth[2 * k + 1] - M.zeta0) / (M.zeta1 - M.zeta0);
-      CT(P, k) = pbot * xexp(M, sigma * lp);
-    }
+  if (c.valid && ks - 1 < nk) {
+    const double dz_inv = 1. / (M.zeta1 - M.zeta0);
+    for (int k = ks - 1 + c.warp; k < nk; k += CT_WARPS) CT(P, k) = pbot * exp((M.sgth[2 * k + 1] - M.zeta0) * dz_inv * lp);
+  }
   __syncthreads();
   const float lpf = d2f(lp);
+  const double ginv = 1. / g;
   if (c.valid)
     for (int k = c.warp; k <= nk; k += CT_WARPS) {
       const double pk = CT(P, k);
       if (k >= 1) {
         const long long x = c.base + k * n2;
         M.p3[x] = pk;
-        const double hl = (pk - CT(P, k - 1)) / (g * M.dsgth[2 * k]);
+        const double hl = (pk - CT(P, k - 1)) * (ginv * M.dsgth_inv[2 * k]);
         CT(HL, k) = hl;
         M.hdry[x] = dmaxr(M.h_min[k], hl);
       }

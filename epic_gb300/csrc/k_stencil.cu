@@ -567,10 +567,11 @@ __global__ void k_zonal_visc(DevModel M, double *A, int sel, int jbot, int jhalf
       }
       mean = cv<R>(__shfl_sync(full, mv, 0));
     } else {
-      double fm = 0.;
-      for (int i = lane + 1; i <= ni; i += 32) fm += to_d(d[i]);
+      // the row sum of a periodic second difference vanishes but for rounding: FP32 suffices
+      float fm = 0.f;
+      for (int i = lane + 1; i <= ni; i += 32) fm += d[i];
       for (int o = 16; o > 0; o >>= 1) fm += __shfl_xor_sync(full, fm, o);
-      mean = cv<R>(fm / ni);
+      mean = fm / (float)ni;
       if (lane == 0) {
         d[ni + 1] = d[1];
         d[0] = d[ni];
