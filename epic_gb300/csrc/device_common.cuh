@@ -70,10 +70,10 @@ struct DevModel {
   // autotuner; they change no result (every tuned kernel is pointwise or per row)
   int tb[9];
 
-  __host__ __device__ __forceinline__ long long at(int k, int j, int i) const {
-    return (long long)i + (long long)(j + 1) * iadim + (long long)k * n2;
-  }
-  __host__ __device__ __forceinline__ long long at2(int j, int i) const { return (long long)i + (long long)(j + 1) * iadim; }
+  // Offsets within one 3-D field of one model: 32-bit arithmetic (epic_model_create rejects
+  // grids whose wind arrays, up to three time planes, reach 2^31 elements).
+  __host__ __device__ __forceinline__ int at(int k, int j, int i) const { return i + (j + 1) * iadim + k * (int)n2; }
+  __host__ __device__ __forceinline__ int at2(int j, int i) const { return i + (j + 1) * iadim; }
 };
 
 // Entry of every kernel: in a batch launch, take member blockIdx.z's description and move the
@@ -159,13 +159,14 @@ __device__ __forceinline__ double layer_p(const DevModel &M, double top, double 
 // never hold except as exact zeros) are flushed to signed zero in both directions.
 __device__ __forceinline__ float d2f(double x) {
   const unsigned hi = (unsigned)__double2hiint(x), lo = (unsigned)__double2loint(x);
-  const unsigned e = (hi >> 20) & 0x7ffu;
-  unsigned u = __funnelshift_l(lo, hi, 3) - (896u << 23);   // 8-bit exponent, 23 leading mantissa bits
-  const unsigned rest = lo & 0x1fffffffu;                    // the 29 bits dropped
-  u += (rest > 0x10000000u) | ((rest == 0x10000000u) & u);  // to nearest, ties to even
-  u = e < 897u ? 0u : u;
-  u = e > 1150u ? (((hi & 0xfffffu) | lo) && e == 2047u ? 0x7fc00000u : 0x7f800000u) : u;
-  return __uint_as_float(u | (hi & 0x80000000u));
+  const unsigned a = hi & 0x7fffffffu;
+  // round the 64-bit pattern to nearest-even at bit 29 (a carry may bump the exponent), then
+  // take the 8 low exponent bits and the 23 leading mantissa bits and rebias the exponent
+  const unsigned long long v = (((unsigned long long)hi << 32) | lo) + (0x0fffffffull + ((lo >> 29) & 1u));
+  unsigned u = (__funnelshift_l((unsigned)v, (unsigned)(v >> 32), 3) - (896u << 23)) | (hi & 0x80000000u);
+  if (a - 0x38100000u >= 0x0fe00000u)   // |x| < FLT_MIN (to signed zero), or beyond FLT_MAX, inf, NaN
+    u = (hi & 0x80000000u) | (a < 0x38100000u ? 0u : ((a | (lo != 0u)) > 0x7ff00000u ? 0x7fc00000u : 0x7f800000u));
+  return __uint_as_float(u);
 }
 __device__ __forceinline__ double f2d(float f) {
   const unsigned w = __float_as_uint(f), a = w & 0x7fffffffu;

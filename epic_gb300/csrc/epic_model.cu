@@ -299,6 +299,8 @@ extern "C" int epic_model_create(const epic_grid *g, int32_t precision, epic_mod
   if (precision != EPIC_PREC_FP64 && precision != EPIC_PREC_MIXED) return set_error(EPIC_ERR_ARG, "precision form %d not available", precision);
   if (g->ni < 4 || (g->ni & (g->ni - 1)) || g->ni > EPIC_MAX_NI) return set_error(EPIC_ERR_ARG, "ni=%d: need a power of 2 in [4,%d]", g->ni, EPIC_MAX_NI);
   if (g->nj < 3 || g->nk < 3 || g->nk > EPIC_MAX_NK) return set_error(EPIC_ERR_ARG, "nj=%d nk=%d out of range", g->nj, g->nk);
+  if (3. * (g->ni + 2) * (g->nj + 3) * (g->nk + 2) >= 2147483648.)
+    return set_error(EPIC_ERR_ARG, "grid %dx%dx%d too large: a field's offsets must fit in 32 bits", g->ni, g->nj, g->nk);
   if (g->globe_latbot != -90. || g->globe_lattop != 90.) return set_error(EPIC_ERR_ARG, "only the full globe is supported");
   if (g->k_sigma < 2 || g->k_sigma > g->nk) return set_error(EPIC_ERR_ARG, "k_sigma=%d out of range", g->k_sigma);
   if (g->k_sponge != 0 || g->newt_cool_adjust) return set_error(EPIC_ERR_ARG, "k_sponge > 0 and newt_cool_adjust are not supported");

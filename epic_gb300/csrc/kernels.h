@@ -9,12 +9,12 @@ namespace epic {
 // one captured graph serves every step.
 enum PlaneSel { PL_NONE = 0, PL_UV = 1, PL_UV_DIS = 2, PL_UV_TEND = 3 };
 
-__device__ __forceinline__ long long plane_offset(const DevModel &M, int sel) {
+__device__ __forceinline__ int plane_offset(const DevModel &M, int sel) {
   const Ctl *c = M.ctl;
   switch (sel) {
-    case PL_UV: return (long long)c->it_uv * M.n3;
-    case PL_UV_DIS: return (long long)c->it_uv_dis * M.n3;
-    case PL_UV_TEND: return (long long)c->it_uv_tend * M.n3;
+    case PL_UV: return c->it_uv * (int)M.n3;
+    case PL_UV_DIS: return c->it_uv_dis * (int)M.n3;
+    case PL_UV_TEND: return c->it_uv_tend * (int)M.n3;
     default: return 0;
   }
 }
