@@ -29,8 +29,12 @@ def _nvcc() -> str:
 
 
 def _flags() -> list[str]:
+    # -fmad=false keeps every binary64 operation separately rounded (the FP64 form matches the
+    # reference bit for bit); -prec-div/-prec-sqrt=false make binary32 division and square root
+    # (used by the mixed form only) the fast approximate instructions, within 2 ulp
     extra = os.environ.get("EPIC_NVCC_EXTRA", "").split()
-    return ["-O3", "-std=c++17", ARCH, "-lineinfo", "-fmad=false", "-Xcompiler", "-fPIC,-ffp-contract=off",
+    return ["-O3", "-std=c++17", ARCH, "-lineinfo", "-fmad=false", "-prec-div=false", "-prec-sqrt=false",
+            "-Xcompiler", "-fPIC,-ffp-contract=off",
             "-I" + os.path.join(ROOT, "include"), "-I" + SRC, "--expt-relaxed-constexpr", *extra]
 
 

@@ -91,7 +91,7 @@ __device__ __forceinline__ R sigmatheta_lp(const DevModel &M, R theta, R p, R pb
 // In the mixed form (R = float) the pointwise terms are FP32, SUM_DIV is accumulated in FP64, and
 // the dF/dp difference step is cbrt(FLT_EPSILON) relative instead of cbrt(DBL_EPSILON).
 template <class R>
-__global__ void __launch_bounds__(CT_THREADS) k_calc_w(DevModel M) {
+__global__ void __launch_bounds__(CT_THREADS, 3) k_calc_w(DevModel M) {
   epic_member(M);
   extern __shared__ __align__(16) unsigned char smraw[];
   R *sm = reinterpret_cast<R *>(smraw);
@@ -579,10 +579,10 @@ __device__ __forceinline__ double layer_p_mixed(const DevModel &M, double top, d
   return bot * f2d(expf(log1pf(q - 1.f) / kap));
 }
 
-__global__ void __launch_bounds__(CT_THREADS) k_set_p2etc_mixed(DevModel M, int update_theta) {
+__global__ void __launch_bounds__(CT_THREADS, 3) k_set_p2etc_mixed(DevModel M, int update_theta) {
   epic_member(M);
   extern __shared__ double sm[];
-  __shared__ double s_lp[32];
+  __shared__ double s_lp[32], s_ginv[32];
   const ColTile c = col_tile(M);
   const int nk = M.nk, ks = M.k_sigma, L = nk + 1;
   const long long n2 = M.n2;
@@ -610,10 +610,11 @@ __global__ void __launch_bounds__(CT_THREADS) k_set_p2etc_mixed(DevModel M, int 
     double p = M.p3[c.base];
     CT(P, 0) = p;
     for (int k = 1; k <= nk; k++) {
-      p = p + M.dsgth[2 * k] * g * CT(HL, k);
+      p = fma(M.dsgth[2 * k] * g, CT(HL, k), p);
       CT(P, k) = p;
     }
     s_lp[c.lane] = log(CT(P, 0) / p);   // binary64 libdevice log: the mixed form needs no correct rounding
+    s_ginv[c.lane] = 1. / g;
   }
   __syncthreads();
   const double ptop = CT(P, 0), pbot = CT(P, nk), lp = s_lp[c.lane];
@@ -623,15 +624,21 @@ __global__ void __launch_bounds__(CT_THREADS) k_set_p2etc_mixed(DevModel M, int 
   }
   __syncthreads();
   const float lpf = d2f(lp);
-  const double ginv = 1. / g;
+  const double ginv = s_ginv[c.lane];
   if (c.valid)
     for (int k = c.warp; k <= nk; k += CT_WARPS) {
       const double pk = CT(P, k);
       if (k >= 1) {
         const long long x = c.base + k * n2;
         M.p3[x] = pk;
-        const double hl = (pk - CT(P, k - 1)) * (ginv * M.dsgth_inv[2 * k]);
-        CT(HL, k) = hl;
+        // above the pure-sigma interfaces the layer's dp is the one just summed, so its mass is
+        // the input HDRY (to the rounding of the sum); only layers next to a rescaled interface
+        // are recomputed from the pressures
+        double hl = CT(HL, k);
+        if (k >= ks - 1) {
+          hl = (pk - CT(P, k - 1)) * (ginv * M.dsgth_inv[2 * k]);
+          CT(HL, k) = hl;
+        }
         M.hdry[x] = dmaxr(M.h_min[k], hl);
       }
       if (update_theta && k < ks - 1) {
@@ -703,21 +710,25 @@ __global__ void __launch_bounds__(CT_THREADS, 3) k_pgrad_vars_column_mixed(DevMo
   const float kap = d2f(M.kappa);
   const float p0_inv = d2f(1. / M.press0);
   const float mu_over_r = d2f(mu / 8.314472e+3);   // return_density: p mu / (R T)
+  const float cpf = d2f(M.cp);
+  // T3 = theta (p/p0)^kappa, EXNER3, RHO3 and the layer T2, RHO2 in FP32 (their relative error
+  // is that of the FP32 power, 1e-7, either way), stored in binary64
   auto level = [&](int k, double theta, double p, double pr, double th2) {
       const long long x = c.base + k * n2;
       const float pf = powf(d2f(p) * p0_inv, kap);
-      const double t3 = theta * f2d(pf);
+      const float t3f = d2f(theta) * pf;
+      const double t3 = f2d(t3f);
       M.t3[x] = t3;
-      M.exner3[x] = M.cp * f2d(pf);
-      const double rho = f2d(d2f(p) * mu_over_r / d2f(t3));
+      M.exner3[x] = f2d(cpf * pf);
+      const double rho = f2d(d2f(p) * mu_over_r / t3f);
       M.rho3[x] = rho;
       CT(P, k) = p;
       CT(R, k) = rho;
       CT(T3, k) = t3;
       if (k >= 1) {
-        const double t2 = th2 * f2d(powf(d2f(pr) * p0_inv, kap));
-        M.t2[x] = t2;
-        const double r2 = f2d(d2f(pr) * mu_over_r / d2f(t2));
+        const float t2f = d2f(th2) * powf(d2f(pr) * p0_inv, kap);
+        M.t2[x] = f2d(t2f);
+        const double r2 = f2d(d2f(pr) * mu_over_r / t2f);
         M.rho2[x] = r2;
         if (k == 1) s_rho2_1[c.lane] = r2;
       }
@@ -780,11 +791,12 @@ __global__ void __launch_bounds__(CT_THREADS, 3) k_pgrad_vars_column_mixed(DevMo
   const bool interior = c.i >= 1 && c.i <= M.ni;
   const long long itime = M.ctl->itime;
   const double dtg_inv = -1. / (M.dt * M.grav[2 * c.j + 1]);
+  const float cprf = d2f(M.cpr), rgasf = d2f(M.rgas);
   auto level_out = [&](int k, double old, double w, double h) {
     const long long x = c.base + k * n2;
     const double gzk = CT(GZ, k);
     M.gz3[x] = gzk;
-    M.mont3[x] = gzk + return_enthalpy(M, CT(T3, k));
+    M.mont3[x] = gzk + f2d(cprf * d2f(CT(T3, k)) * rgasf);   // return_enthalpy in FP32
     if (interior && k >= 1) {
       double dz = 0.;
       if (itime > 1) dz = (old - gzk) * dtg_inv;
