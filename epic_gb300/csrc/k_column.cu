@@ -344,14 +344,15 @@ __global__ void __launch_bounds__(CT_THREADS) k_hsu_vertical(DevModel M, double 
 }
 
 // restore_mass(HDRY_INDEX), epic_adjust.c:45-96
+// Pointwise: one thread per cell of layers 1..nk, rows 0..nj, all columns.
 __global__ void k_restore_mass(DevModel M) {
   epic_member(M);
-  int j, i;
-  if (!col_index(M, j, i)) return;
-  for (int k = 1; k <= M.nk; k++) {
-    const long long x = M.at(k, j, i);
-    M.hdry[x] = dmaxr(M.h_min[k], M.hdry[x]);
-  }
+  const int t = (int)(blockIdx.x * blockDim.x + threadIdx.x);
+  const int per_k = (M.nj + 1) * (M.ni + 2);
+  if (t >= M.nk * per_k) return;
+  const int k = 1 + t / per_k;
+  const int x = M.at(k, 0, 0) + (t - (k - 1) * per_k);
+  M.hdry[x] = dmaxr(M.h_min[k], M.hdry[x]);
 }
 
 // set_p2etc, epic_funcs_diag.c:3352-3569 (nq = 0: H2 is HDRY, PDRY3 is P3, HDRY3 is H3).
@@ -934,7 +935,10 @@ int launch_hsu_vertical(const DevModel &M, double *buff, int kind, cudaStream_t 
                 (size_t)5 * 32 * (M.nk + 2) * (M.mixed ? sizeof(float) : sizeof(double)), s, M, buff, kind);
   return 0;
 }
-int launch_restore_mass(const DevModel &M, cudaStream_t s) { k_restore_mass<<<zg(ncol_blocks(M, TB(M, TB_COLUMN)), M), TB(M, TB_COLUMN), 0, s>>>(M); return 0; }
+int launch_restore_mass(const DevModel &M, cudaStream_t s) {
+  k_restore_mass<<<zg(epic_blocks((long long)M.nk * (M.nj + 1) * (M.ni + 2), TB(M, TB_POINT)), M), TB(M, TB_POINT), 0, s>>>(M);
+  return 0;
+}
 int launch_set_p2etc(const DevModel &M, int update_theta, cudaStream_t s) {
   if (M.mixed) k_set_p2etc_mixed<<<zg(ntile_blocks(M), M), CT_THREADS, tile_smem(M, 3), s>>>(M, update_theta);
   else k_set_p2etc<<<zg(ntile_blocks(M), M), CT_THREADS, tile_smem(M, 4), s>>>(M, update_theta);

@@ -652,18 +652,27 @@ __global__ void k_pv_poles(DevModel M) {
   const double *UU = M.u + plane_offset(M, PL_UV);
   const double *HH = M.h3;
   __shared__ double pole[2];
+  // the four rows are staged by every thread, then summed by one thread in the reference's order
+  extern __shared__ double rows[];   // [4][ni]: U(j=0), H(j=0), U(j=nj), H(j=nj)
+  const int ni = M.ni, J = M.nj;
+  for (int i = threadIdx.x; i < ni; i += blockDim.x) {
+    rows[i] = UU[M.at(k, 0, i + 1)];
+    rows[ni + i] = HH[M.at(k, 0, i + 1)];
+    rows[2 * ni + i] = UU[M.at(k, J, i + 1)];
+    rows[3 * ni + i] = HH[M.at(k, J, i + 1)];
+  }
+  __syncthreads();
   if (threadIdx.x == 0) {
     double ze = 0., h = 0.;
-    for (int i = 1; i <= M.ni; i++) ze -= UU[M.at(k, 0, i)];
+    for (int i = 0; i < ni; i++) ze -= rows[i];
     ze *= M.mn[0] / ((M.m[1]) * (double)(M.ni));
-    for (int i = 1; i <= M.ni; i++) h += HH[M.at(k, 0, i)];
+    for (int i = 0; i < ni; i++) h += rows[ni + i];
     h /= (double)(M.ni);
     pole[0] = (ze + M.f[0]) / h;
-    const int J = M.nj;
     ze = 0.; h = 0.;
-    for (int i = 1; i <= M.ni; i++) ze += UU[M.at(k, J, i)];
+    for (int i = 0; i < ni; i++) ze += rows[2 * ni + i];
     ze *= M.mn[2 * (J + 1)] / (M.m[2 * J + 1] * (double)(M.ni));
-    for (int i = 1; i <= M.ni; i++) h += HH[M.at(k, J, i)];
+    for (int i = 0; i < ni; i++) h += rows[3 * ni + i];
     h /= (double)(M.ni);
     pole[1] = (ze + M.f[2 * (J + 1)]) / h;
   }
@@ -931,7 +940,7 @@ int launch_store_diag(const DevModel &M, cudaStream_t s) {
   // PV3: filtered copy of V (v rows), then the interior and polar values.
   launch_filter_planes(M, M.v, PL_UV, M.work1, 0, M.nk + 1, 1, s, M.mixed);
   EPIC_LAUNCH_R(M.mixed, k_pv_interior, cells_blocks(M, M.nk + 1, M.nj, TB(M, TB_DIAG)), TB(M, TB_DIAG), 0, s, M, M.work1);
-  k_pv_poles<<<zg(M.nk + 1, M), 128, 0, s>>>(M);
+  k_pv_poles<<<zg(M.nk + 1, M), 128, 4 * M.ni * sizeof(double), s>>>(M);
   // DIV_UV3 from a filtered copy of U.
   launch_filter_planes(M, M.u, PL_UV, M.work2, 0, M.nk + 1, 0, s, M.mixed);
   EPIC_LAUNCH_R(M.mixed, k_divergence, cells_blocks(M, M.nk + 1, M.nj + 1, TB(M, TB_DIAG)), TB(M, TB_DIAG), 0, s, M, M.work2, M.v, PL_UV, M.div_uv3, 0, M.nk + 1);
