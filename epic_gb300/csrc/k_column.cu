@@ -791,18 +791,20 @@ __global__ void __launch_bounds__(CT_THREADS, 3) k_pgrad_vars_column_mixed(DevMo
   if (!c.valid) return;
   const bool interior = c.i >= 1 && c.i <= M.ni;
   const long long itime = M.ctl->itime;
-  const double dtg_inv = -1. / (M.dt * M.grav[2 * c.j + 1]);
+  // MONT3 and DZDT3 are diagnostics that no later kernel of the step reads: FP32 arithmetic on
+  // the FP64 change of GZ3 (the difference itself stays FP64: it cancels)
+  const float dtg_inv = -1.f / (d2f(M.dt) * d2f(M.grav[2 * c.j + 1]));
   const float cprf = d2f(M.cpr), rgasf = d2f(M.rgas);
   auto level_out = [&](int k, double old, double w, double h) {
     const long long x = c.base + k * n2;
     const double gzk = CT(GZ, k);
     M.gz3[x] = gzk;
-    M.mont3[x] = gzk + f2d(cprf * d2f(CT(T3, k)) * rgasf);   // return_enthalpy in FP32
+    M.mont3[x] = f2d(d2f(gzk) + cprf * d2f(CT(T3, k)) * rgasf);   // GZ3 + return_enthalpy
     if (interior && k >= 1) {
-      double dz = 0.;
-      if (itime > 1) dz = (old - gzk) * dtg_inv;
-      dz += f2d(d2f(w) * d2f(h) / d2f(CT(R, k)));
-      M.dzdt3[x] = dz;
+      float dz = 0.f;
+      if (itime > 1) dz = d2f(old - gzk) * dtg_inv;
+      dz += d2f(w) * d2f(h) / d2f(CT(R, k));
+      M.dzdt3[x] = f2d(dz);
       if (gzk >= CT(GZ, k - 1)) flag_error(M.ctl, ERR_GZ_MONOTONE, k, c.j, c.i, gzk);
     }
   };

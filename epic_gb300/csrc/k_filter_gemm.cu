@@ -18,7 +18,7 @@
 // a_hi = tf32(a), the sum a_hi b_hi + a_hi b_lo + a_lo b_hi misses only the a_lo b_lo term.
 //
 // Every wait is bounded: a CTA whose MMA completion does not arrive within the limit records
-// ERR_TIMEOUT, frees its tensor memory and returns.
+// ERR_TIMEOUT, waits (bounded) for its last commit, frees its tensor memory and returns.
 #include <cmath>
 #include <vector>
 #include "device_common.cuh"
@@ -87,33 +87,41 @@ __device__ __forceinline__ bool mbar_wait(unsigned mbar, unsigned phase) {
 
 // Block = one row j in -1..nj+1 (x), a chunk of 32 planes (y), the member (z).  Rows outside
 // the filtered set return at once (the copy path of k_filter_planes handles them).
+//
+// The product runs as a two-stage pipeline over steps t = (K chunk kc, output tile mt): the A
+// (operator) and B (input) tiles are double-buffered in shared memory; while the tensor cores
+// multiply step t, the threads stage step t+1 and the next K chunk's inputs are already on their
+// way from global memory into registers.  Each step's products are committed to the mbarrier of
+// its buffer; a buffer is restaged only after the commit of the step that last read it (commits
+// complete in issue order).
 __global__ void __launch_bounds__(FG_THREADS) k_filter_planes_gemm(DevModel M, const double *src, int src_sel, double *dst, int k0,
                                                                      int nplanes, int vgrid) {
   epic_member(M, src, dst);
   extern __shared__ __align__(16) unsigned char fg_raw[];
-  __shared__ __align__(8) uint64_t mbar;
+  __shared__ __align__(8) uint64_t mbar[2];
   __shared__ uint32_t tmem_base;
   __shared__ int fail;
-  const int ni = M.ni, mtiles = ni / FG_M;
+  const int ni = M.ni, mtiles = ni / FG_M, nchunks = ni / FG_KC, nsteps = nchunks * mtiles;
   const int j = (int)blockIdx.x - 1;
   const bool valid = vgrid ? (j >= 1 && j <= M.nj) : (j >= 0 && j <= M.nj);
   if (!valid || fabs(M.lat[vgrid ? 2 * j : 2 * j + 1]) < M.lat0) return;
   src += plane_offset(M, src_sel);
   const int n0 = (int)blockIdx.y * FG_N;
-  const int tid = (int)threadIdx.x, warp = tid >> 5, lane = tid & 31;
+  const int tid = (int)threadIdx.x, warp = tid >> 5;
   const uint32_t tcols = (uint32_t)(mtiles * FG_N);   // 32, 64, 128 or 256: a power of 2
 
-  // A_hi, A_lo (128 x 32 FP32 each), B_hi, B_lo (32 x 32 each), then the row's kernel f; the
-  // swizzle atoms need a 1024-byte aligned base
+  // two buffers of A_hi, A_lo (128 x 32 FP32 each) and B_hi, B_lo (32 x 32 each), then the
+  // row's kernel f; the swizzle atoms need a 1024-byte aligned base
+  constexpr unsigned A_BYTES = FG_M * FG_KC * 4, B_BYTES = FG_N * FG_KC * 4, BUF_BYTES = 2 * A_BYTES + 2 * B_BYTES;
   unsigned char *fg_smem = fg_raw + ((1024u - ((unsigned)__cvta_generic_to_shared(fg_raw) & 1023u)) & 1023u);
-  unsigned char *a_hi = fg_smem, *a_lo = a_hi + FG_M * FG_KC * 4, *b_hi = a_lo + FG_M * FG_KC * 4, *b_lo = b_hi + FG_N * FG_KC * 4;
-  float *fk = reinterpret_cast<float *>(b_lo + FG_N * FG_KC * 4);
+  float *fk = reinterpret_cast<float *>(fg_smem + 2 * BUF_BYTES);
   const float *fsrc = (vgrid ? M.fkern_v : M.fkern_h) + (long long)(j + 1) * ni;
   for (int d = tid; d < ni; d += FG_THREADS) fk[d] = fsrc[d];
-  const unsigned mbar_s = (unsigned)__cvta_generic_to_shared(&mbar);
+  const unsigned mbar_s = (unsigned)__cvta_generic_to_shared(&mbar[0]);
   if (tid == 0) {
     fail = 0;
     asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(mbar_s));
+    asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(mbar_s + 8));
     asm volatile("fence.mbarrier_init.release.cluster;");
   }
   if (warp == 0) {
@@ -125,62 +133,84 @@ __global__ void __launch_bounds__(FG_THREADS) k_filter_planes_gemm(DevModel M, c
   __syncthreads();
   asm volatile("tcgen05.fence::after_thread_sync;");
   const uint32_t dtmem = tmem_base;
-  const unsigned a_hi_s = (unsigned)__cvta_generic_to_shared(a_hi), a_lo_s = (unsigned)__cvta_generic_to_shared(a_lo);
-  const unsigned b_hi_s = (unsigned)__cvta_generic_to_shared(b_hi), b_lo_s = (unsigned)__cvta_generic_to_shared(b_lo);
+  const unsigned smem_s = (unsigned)__cvta_generic_to_shared(fg_smem);
 
-  unsigned phase = 0;
-  for (int kc = 0; kc < ni && !fail; kc += FG_KC) {
-    // B[n][e] = x_{n0+n}(kc + e + 1), zero beyond the last plane; one 16-byte chunk (4 values)
-    // per thread and iteration
-    for (int q = tid; q < FG_N * FG_KC / 4; q += FG_THREADS) {
-      const int n = q / (FG_KC / 4), e0 = 4 * (q % (FG_KC / 4));
-      float4 hv = make_float4(0.f, 0.f, 0.f, 0.f), lv = hv;
+  // B[n][e] = x_{n0+n}(kc + e + 1), zero beyond the last plane: two 16-byte chunks (4 values
+  // each) per thread and K chunk, loaded into registers one chunk ahead
+  constexpr int BQ = FG_N * FG_KC / 4 / FG_THREADS;   // 2
+  double bnext[BQ][4];
+  auto load_b = [&](int kc) {
+#pragma unroll
+    for (int u = 0; u < BQ; u++) {
+      const int q = tid + u * FG_THREADS, n = q / (FG_KC / 4), e0 = 4 * (q % (FG_KC / 4));
       if (n0 + n < nplanes) {
         const double *row = src + M.at(k0 + n0 + n, j, kc + e0 + 1);
-        float b[4] = {(float)row[0], (float)row[1], (float)row[2], (float)row[3]};
-        hv = make_float4(tf32_hi(b[0]), tf32_hi(b[1]), tf32_hi(b[2]), tf32_hi(b[3]));
-        lv = make_float4(b[0] - hv.x, b[1] - hv.y, b[2] - hv.z, b[3] - hv.w);
+#pragma unroll
+        for (int v = 0; v < 4; v++) bnext[u][v] = row[v];
+      } else {
+#pragma unroll
+        for (int v = 0; v < 4; v++) bnext[u][v] = 0.;
       }
+    }
+  };
+  load_b(0);
+  int t = 0;
+  for (; t < nsteps; t++) {
+    const int c = t / mtiles, mt = t - c * mtiles, kc = c * FG_KC, buf = t & 1;
+    // the buffer was last read by the products of step t-2
+    if (t >= 2 && !mbar_wait(mbar_s + 8 * buf, (unsigned)(((t - 2) >> 1) & 1))) atomicExch(&fail, 1);
+    __syncthreads();
+    if (fail) break;
+    unsigned char *a_hi = fg_smem + buf * BUF_BYTES, *a_lo = a_hi + A_BYTES, *b_hi = a_lo + A_BYTES, *b_lo = b_hi + B_BYTES;
+    // B of this K chunk (every output tile of the chunk restages it into its own buffer)
+#pragma unroll
+    for (int u = 0; u < BQ; u++) {
+      const int q = tid + u * FG_THREADS, n = q / (FG_KC / 4), e0 = 4 * (q % (FG_KC / 4));
+      const float b0 = d2f(bnext[u][0]), b1 = d2f(bnext[u][1]), b2 = d2f(bnext[u][2]), b3 = d2f(bnext[u][3]);
+      const float4 hv = make_float4(tf32_hi(b0), tf32_hi(b1), tf32_hi(b2), tf32_hi(b3));
+      const float4 lv = make_float4(b0 - hv.x, b1 - hv.y, b2 - hv.z, b3 - hv.w);
       const unsigned off = sw128(n, e0);
       *reinterpret_cast<float4 *>(b_hi + off) = hv;
       *reinterpret_cast<float4 *>(b_lo + off) = lv;
     }
-    for (int mt = 0; mt < mtiles && !fail; mt++) {
-      // A[m][e] = f((128 mt + m - (kc + e)) mod ni), ni a power of 2
-      for (int q = tid; q < FG_M * FG_KC / 4; q += FG_THREADS) {
-        const int m = q / (FG_KC / 4), e0 = 4 * (q % (FG_KC / 4));
-        const int d0 = mt * FG_M + m - (kc + e0) + ni;
-        float a[4];
+    // A[m][e] = f((128 mt + m - (kc + e)) mod ni), ni a power of 2
+    for (int q = tid; q < FG_M * FG_KC / 4; q += FG_THREADS) {
+      const int m = q / (FG_KC / 4), e0 = 4 * (q % (FG_KC / 4));
+      const int d0 = mt * FG_M + m - (kc + e0) + ni;
+      float a[4];
 #pragma unroll
-        for (int u = 0; u < 4; u++) a[u] = fk[(d0 - u) & (ni - 1)];
-        const float4 hv = make_float4(tf32_hi(a[0]), tf32_hi(a[1]), tf32_hi(a[2]), tf32_hi(a[3]));
-        const float4 lv = make_float4(a[0] - hv.x, a[1] - hv.y, a[2] - hv.z, a[3] - hv.w);
-        const unsigned off = sw128(m, e0);
-        *reinterpret_cast<float4 *>(a_hi + off) = hv;
-        *reinterpret_cast<float4 *>(a_lo + off) = lv;
-      }
-      asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
-      __syncthreads();
-      if (tid == 0) {
-        asm volatile("tcgen05.fence::after_thread_sync;");
-        const uint32_t d_mt = dtmem + (uint32_t)(mt * FG_N);
-        for (int ks = 0; ks < FG_KC / 8; ks++) {   // K = 8 TF32 (32 bytes) per instruction
-          const unsigned koff = (unsigned)ks * 32;
-          const uint32_t acc = (kc > 0 || ks > 0) ? 1u : 0u;
-          mma_tf32(d_mt, smem_desc(a_hi_s + koff), smem_desc(b_hi_s + koff), acc);
-          mma_tf32(d_mt, smem_desc(a_hi_s + koff), smem_desc(b_lo_s + koff), 1u);
-          mma_tf32(d_mt, smem_desc(a_lo_s + koff), smem_desc(b_hi_s + koff), 1u);
-        }
-        asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(mbar_s) : "memory");
-      }
-      // the products read the staged tiles: every thread waits before anything is restaged
-      if (!mbar_wait(mbar_s, phase)) atomicExch(&fail, 1);
-      phase ^= 1u;
-      __syncthreads();
+      for (int u = 0; u < 4; u++) a[u] = fk[(d0 - u) & (ni - 1)];
+      const float4 hv = make_float4(tf32_hi(a[0]), tf32_hi(a[1]), tf32_hi(a[2]), tf32_hi(a[3]));
+      const float4 lv = make_float4(a[0] - hv.x, a[1] - hv.y, a[2] - hv.z, a[3] - hv.w);
+      const unsigned off = sw128(m, e0);
+      *reinterpret_cast<float4 *>(a_hi + off) = hv;
+      *reinterpret_cast<float4 *>(a_lo + off) = lv;
     }
+    asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+    __syncthreads();
+    if (tid == 0) {
+      asm volatile("tcgen05.fence::after_thread_sync;");
+      const unsigned a_hi_s = smem_s + buf * BUF_BYTES, a_lo_s = a_hi_s + A_BYTES, b_hi_s = a_lo_s + A_BYTES, b_lo_s = b_hi_s + B_BYTES;
+      const uint32_t d_mt = dtmem + (uint32_t)(mt * FG_N);
+      for (int ks = 0; ks < FG_KC / 8; ks++) {   // K = 8 TF32 (32 bytes) per instruction
+        const unsigned koff = (unsigned)ks * 32;
+        const uint32_t acc = (kc > 0 || ks > 0) ? 1u : 0u;
+        mma_tf32(d_mt, smem_desc(a_hi_s + koff), smem_desc(b_hi_s + koff), acc);
+        mma_tf32(d_mt, smem_desc(a_hi_s + koff), smem_desc(b_lo_s + koff), 1u);
+        mma_tf32(d_mt, smem_desc(a_lo_s + koff), smem_desc(b_hi_s + koff), 1u);
+      }
+      asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(mbar_s + 8 * buf) : "memory");
+    }
+    // the next K chunk's inputs travel while the products run
+    if (mt == mtiles - 1 && c + 1 < nchunks) load_b(kc + FG_KC);
   }
+  // all products done: the last commit covers every earlier one (bounded also after a failure,
+  // so that no product is in flight when the tensor memory is freed)
+  if (t > 0 && !mbar_wait(mbar_s + 8 * ((t - 1) & 1), (unsigned)(((t - 1) >> 1) & 1))) atomicExch(&fail, 1);
+  __syncthreads();
   asm volatile("tcgen05.fence::after_thread_sync;");
   if (!fail) {
+    const int lane = tid & 31;
     for (int mt = 0; mt < mtiles; mt++) {
       // warp w reads tensor-memory lanes 32w..32w+31: output point 128 mt + 32w + lane, 32 planes
       uint32_t r[FG_N];
@@ -197,7 +227,7 @@ __global__ void __launch_bounds__(FG_THREADS) k_filter_planes_gemm(DevModel M, c
       const int i = mt * FG_M + warp * 32 + lane + 1;
 #pragma unroll
       for (int n = 0; n < FG_N; n++)
-        if (n0 + n < nplanes) write_with_pads(dst, M, M.at(k0 + n0 + n, j, 0), i, (double)__uint_as_float(r[n]));
+        if (n0 + n < nplanes) write_with_pads(dst, M, M.at(k0 + n0 + n, j, 0), i, f2d(__uint_as_float(r[n])));
     }
   } else if (tid == 0) {
     flag_error(M.ctl, ERR_TIMEOUT, k0 + n0, j, 0, 0.);
@@ -207,7 +237,9 @@ __global__ void __launch_bounds__(FG_THREADS) k_filter_planes_gemm(DevModel M, c
   if (warp == 0) asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(dtmem), "r"(tcols));
 }
 
-size_t filter_gemm_smem_bytes(int ni) { return 1024 + (size_t)2 * FG_M * FG_KC * 4 + (size_t)2 * FG_N * FG_KC * 4 + (size_t)ni * 4; }
+size_t filter_gemm_smem_bytes(int ni) {
+  return 1024 + (size_t)2 * (2 * FG_M * FG_KC * 4 + 2 * FG_N * FG_KC * 4) + (size_t)ni * 4;
+}
 
 bool filter_gemm_usable(const DevModel &M) { return M.fkern_h && M.ni % FG_M == 0 && M.ni <= 8 * FG_M; }
 
@@ -217,8 +249,11 @@ int launch_filter_planes_gemm(const DevModel &M, const double *src, int src_sel,
   return 0;
 }
 
-// At most 46 KB (ni = 1024), under the 48 KB default: nothing to raise.
-int filter_gemm_init(int) { return 0; }
+// 86 KB at ni = 1024: the shared-memory limit is raised once to that maximum.
+int filter_gemm_init(int) {
+  return cudaFuncSetAttribute(k_filter_planes_gemm, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                              (int)filter_gemm_smem_bytes(8 * FG_M)) == cudaSuccess ? 0 : -1;
+}
 
 // Host: the circulant kernel f_J(d) of every row (h rows from HIGH_LAT_H, v rows from
 // HIGH_LAT_PV), rows indexed J+1 = 0..nj+2, rounded to FP32.
