@@ -1,7 +1,7 @@
 """Throughput of the GB300 EPIC timestep() on synthetic Held-Suarez states.
 
     python bench.py [--gpus N] [--steps K] [--warmup W] [--impl gb300|reference]
-                    [--workload ens64|hs64|hs128|hs256|hs512] [--precision mixed|fp64]
+                    [--workload ens64|hs64|hs128|hs256|hs512] [--precision mixed|fast|fp64]
                     [--no-cpu-baseline] [--no-extras]
 
 A step is one timestep(STEP_PROGS_AND_SYNC_DIAGS) of every grid in the workload.  metric =
@@ -181,7 +181,7 @@ def run_gpu(args):
         dist.init_process_group("nccl")
     cfg = _workload_cfg(args.workload, seed=rank)
     ga, f = hs_setup(cfg)
-    model = Model(ga, EPIC_PREC_MIXED if args.precision == "mixed" else EPIC_PREC_FP64)
+    model = Model(ga, _prec(args.precision))
     model.upload(f)
     model.timestep(EPIC_SYNC_DIAGS_ONLY)
     stream = torch.cuda.ExternalStream(model.stream)
@@ -297,12 +297,17 @@ def single_rate(cfg, precision, steps, torch):
     return {"value": cfg.cells / (ms / 1e3), "ms_per_step": ms}
 
 
-def mixed_error(torch):
-    """Per-prognostic relative L2 of the mixed form against FP64 after one simulated day
+def _prec(name):
+    from epic_gb300 import EPIC_PREC_FP64, EPIC_PREC_MIXED, EPIC_PREC_MIXED_FAST
+    return {"fp64": EPIC_PREC_FP64, "mixed": EPIC_PREC_MIXED, "fast": EPIC_PREC_MIXED_FAST}[name]
+
+
+def mixed_error(torch, precision):
+    """Per-prognostic relative L2 of a mixed form against FP64 after one simulated day
     (288 steps of 300 s) at 64x32x10, from a state spun up for 10 days in FP64, and from rest."""
     sys.path.insert(0, os.path.join(ROOT, "tests"))
     from compare import PROGNOSTIC, field_errors
-    from epic_gb300 import EPIC_PREC_FP64, EPIC_PREC_MIXED, EPIC_SYNC_DIAGS_ONLY, HSConfig, Model, hs_setup
+    from epic_gb300 import EPIC_PREC_FP64, EPIC_SYNC_DIAGS_ONLY, HSConfig, Model, hs_setup
     ga, f = hs_setup(HSConfig(ni=64, nj=32, nk=10, dt=300, seed=0))
     out = {}
     for label, spin in (("after_10_day_spin_up", 2880), ("from_rest", 0)):
@@ -316,7 +321,7 @@ def mixed_error(torch):
             start = m.download()
             m.close()
         res = []
-        for prec in (EPIC_PREC_FP64, EPIC_PREC_MIXED):
+        for prec in (EPIC_PREC_FP64, precision):
             m = Model(ga, prec)
             m.upload(start)
             if not spin:
@@ -343,6 +348,37 @@ def serving_summary(precision, seed=3):
     return out
 
 
+def ensemble_rate(cfg, nmem, precision, args, torch, rank):
+    """Cell-steps/s of one ensemble in a given form (tuned, primed, timed like the headline)."""
+    from epic_gb300 import EPIC_SYNC_DIAGS_ONLY, Batch
+    members = _members(cfg, nmem, precision, torch_seed=7 + rank)
+    starts = [m.download() for m in members]
+    batch = Batch(members)
+    if not args.no_tune:
+        batch.timestep(EPIC_SYNC_DIAGS_ONLY)
+        batch.autotune(trial_steps=2)
+        batch.sync()
+        for m, f in zip(members, starts):
+            m.upload(f)
+    batch.timestep(EPIC_SYNC_DIAGS_ONLY)
+    for _ in range(args.warmup):
+        batch.run(1)
+    batch.sync()
+    stream = torch.cuda.ExternalStream(batch.stream)
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record(stream)
+    for _ in range(args.steps):
+        batch.run(1)
+    e1.record(stream)
+    e1.synchronize()
+    batch.sync()
+    ms = e0.elapsed_time(e1)
+    batch.close()
+    for m in members:
+        m.close()
+    return {"value": nmem * cfg.cells * args.steps / (ms / 1e3), "ms_per_step": ms / args.steps}
+
+
 def run_gpu_ensemble(args):
     import torch
     from epic_gb300 import EPIC_PREC_FP64, EPIC_PREC_MIXED, EPIC_SYNC_DIAGS_ONLY, Batch
@@ -351,7 +387,7 @@ def run_gpu_ensemble(args):
     if ws > 1:
         import torch.distributed as dist
         dist.init_process_group("nccl")
-    precision = EPIC_PREC_MIXED if args.precision == "mixed" else EPIC_PREC_FP64
+    precision = _prec(args.precision)
     cfg = _workload_cfg(args.workload)
     nmem = args.members or ENSEMBLE[args.workload]
     members = _members(cfg, nmem, precision, torch_seed=7 + rank)
@@ -400,7 +436,8 @@ def run_gpu_ensemble(args):
     clocks = clk.summary()
     launches = batch.kernels_per_step * args.steps
 
-    roof = batch_roofline(batch, cfg, nmem, stream, torch)
+    roof = batch_roofline(batch, cfg, nmem, stream, torch, stage=7)
+    roof_pgrad = batch_roofline(batch, cfg, nmem, stream, torch, stage=12)
 
     # end to end: every member's state uploaded from pinned host memory and downloaded, each step
     hosts = [m.download().copy(pinned=True) for m in members]
@@ -424,7 +461,7 @@ def run_gpu_ensemble(args):
         out = {
             "metric": METRIC, "value": value, "unit": "cell-steps/s", "n_gpus": ws, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": ms_step, "higher_is_better": True, "scaling": "weak",
-            "vs_baseline": None, "dtype": "f32+f64" if precision == EPIC_PREC_MIXED else "f64", "data": "synthetic",
+            "vs_baseline": None, "dtype": "f64" if precision == EPIC_PREC_FP64 else "f32+f64", "data": "synthetic",
             "config": {"workload": f"ensemble of {nmem} Held-Suarez members {cfg.ni}x{cfg.nj}x{cfg.nk}, dt={cfg.dt}s, AB3, "
                                    f"seeded 0.1 K noise and +/-10% k_f per member, {args.precision} form, one launch per "
                                    f"kernel for all members", "ni": cfg.ni, "nj": cfg.nj, "nk": cfg.nk, "dt": cfg.dt,
@@ -438,6 +475,7 @@ def run_gpu_ensemble(args):
             "e2e": {"value": e2e_val, "unit": "cell-steps/s", "h2d_bytes_per_step": host_bytes, "d2h_bytes_per_step": host_bytes},
             "gpu_launches": launches,
             "roofline": roof,
+            "roofline_pgrad": roof_pgrad,
             "step_roofline": {"bound": "hbm", "algorithmic_bytes_per_step": nmem * algorithmic_bytes_per_step(cfg),
                               "achieved_gbs": nmem * algorithmic_bytes_per_step(cfg) / (ms_step / 1e3) / 1e9,
                               "peak_gbs": peaks.get("hbm_gbs")},
@@ -446,11 +484,17 @@ def run_gpu_ensemble(args):
             out["step_roofline"]["frac"] = out["step_roofline"]["achieved_gbs"] / peaks["hbm_gbs"]
         if not args.no_extras:
             fp64 = single_rate(cfg, EPIC_PREC_FP64, args.steps, torch)
-            mixed = single_rate(cfg, EPIC_PREC_MIXED, args.steps, torch)
+            mixed = single_rate(cfg, precision, args.steps, torch)
             out["fp64_single"] = dict(fp64, note=f"plain FP64 timestep of one {cfg.ni}x{cfg.nj}x{cfg.nk} grid")
-            out["mixed_single"] = dict(mixed, note=f"mixed form, one {cfg.ni}x{cfg.nj}x{cfg.nk} grid")
+            out["mixed_single"] = dict(mixed, note=f"{args.precision} form, one {cfg.ni}x{cfg.nj}x{cfg.nk} grid")
             out["batched_over_fp64_single"] = value / ws / fp64["value"]
-            out["mixed_error"] = mixed_error(torch)
+            if precision != EPIC_PREC_FP64:
+                out["mixed_error"] = mixed_error(torch, precision)
+            if args.precision == "mixed":
+                # the faster form that keeps the vertical integration and pressure gradient in FP32
+                fast = ensemble_rate(cfg, nmem, _prec("fast"), args, torch, rank)
+                out["mixed_fast"] = dict(fast, error=mixed_error(torch, _prec("fast")),
+                                         note="EPIC_PREC_MIXED_FAST ensemble, same workload and timing")
             out["serving"] = serving_summary(precision)
     if ws > 1:
         import torch.distributed as dist
@@ -459,30 +503,41 @@ def run_gpu_ensemble(args):
     return out
 
 
-def batch_roofline(batch, cfg, nmem, stream, torch):
-    """The finite-volume pressure gradient (stage 12: k_gz_pole_rows, k_pgrad_split and
-    k_pgrad_lon + k_pgrad_lat, FP32 on (hi, lo) splits of GZ3 and P2 in the mixed form) over all
-    members, timed with events on the batch stream.  Algorithmic bytes per launch: GZ3, P2 and
-    RHO3 read once and DUDT, DVDT read and written once, 7 FP64 3-D fields of ni*(nj+1)*nk cells
-    per member."""
+# Stages timed for the roofline: (stage, kernels, algorithmic 8-byte field passes per cell, note)
+ROOF_STAGES = {
+    7: ("store_pgrad_vars (k_pgrad_vars_column_mixed + k_pgrad_dzdt) over all members", 20,
+        "THETA, P3, P2, THETA2, GZ3, W3, H3 read and T3, EXNER3, RHO3, T2, RHO2, GZ3, MONT3, DZDT3 written by the "
+        "column tile; U, V, GZ3, DZDT3 read and DZDT3 written by the horizontal part; bound by load latency and "
+        "the FP64 hydrostatic sum, not by HBM"),
+    12: ("uv_pgrad_finite_volume (k_gz_pole_rows + k_pgrad_split + k_pgrad_lon + k_pgrad_lat) over all members", 7,
+         "GZ3, P2, RHO3 read and DUDT, DVDT read and written; stencils of 18-24 loads per cell from L1/L2 plus ~300 "
+         "FP32/integer operations: issue- and latency-bound, not HBM-bound"),
+}
+
+
+def batch_roofline(batch, cfg, nmem, stream, torch, stage=7):
+    """One stage of the step over all members, timed with CUDA events on the batch stream after
+    a warm-up call.  Algorithmic bytes per launch: the stage's field passes (ROOF_STAGES) of
+    8-byte values over ni*(nj+1)*nk cells per member.  Stage 7 (store_pgrad_vars) holds the
+    largest kernel of the mixed step (k_pgrad_vars_column_mixed, 12% of the launch list)."""
     peaks = _peaks()
+    label, passes, note = ROOF_STAGES[stage]
     n = 5
-    batch.run_stage(12)
+    batch.run_stage(stage)
     batch.sync()
     e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
     e0.record(stream)
     for _ in range(n):
-        batch.run_stage(12)
+        batch.run_stage(stage)
     e1.record(stream)
     e1.synchronize()
+    batch.sync()
     dur = e0.elapsed_time(e1) / n / 1e3
-    alg = 7 * 8 * cfg.ni * (cfg.nj + 1) * cfg.nk * nmem
+    alg = passes * 8 * cfg.ni * (cfg.nj + 1) * cfg.nk * nmem
     ach = alg / dur / 1e9
-    return {"kernel": "uv_pgrad_finite_volume (k_pgrad_split + k_pgrad_lon + k_pgrad_lat) over all members", "bound": "hbm",
-            "achieved": ach, "peak": peaks["hbm_gbs"], "unit": "GB/s", "frac": ach / peaks["hbm_gbs"],
-            "peak_source": peaks["source"] + " (burst copy)", "algorithmic_bytes": alg, "launch_ms": dur * 1e3,
-            "traffic": None,
-            "note": "stencil of 18-24 loads per cell from L1/L2 plus ~300 FP32/integer operations; issue- and latency-bound, not HBM-bound"}
+    return {"kernel": label, "bound": "hbm", "achieved": ach, "peak": peaks["hbm_gbs"], "unit": "GB/s",
+            "frac": ach / peaks["hbm_gbs"], "peak_source": peaks["source"] + " (burst copy)", "algorithmic_bytes": alg,
+            "launch_ms": dur * 1e3, "traffic": None, "note": note}
 
 
 def _peaks():
@@ -537,7 +592,7 @@ def main():
     ap.add_argument("--no-tune", action="store_true", help="keep the built-in launch shapes (profiling runs)")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--cpu-steps", type=int, default=3)
-    ap.add_argument("--precision", default=None, choices=["fp64", "mixed"])
+    ap.add_argument("--precision", default=None, choices=["fp64", "mixed", "fast"])
     args = ap.parse_args()
     if args.precision is None:
         args.precision = "mixed" if args.workload in ENSEMBLE else "fp64"

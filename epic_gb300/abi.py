@@ -17,6 +17,7 @@ EPIC_UV_AB3 = 0
 EPIC_UV_LEAPFROG = 1
 EPIC_PREC_FP64 = 0
 EPIC_PREC_MIXED = 1
+EPIC_PREC_MIXED_FAST = 2
 
 _dp = C.POINTER(C.c_double)
 

@@ -54,7 +54,11 @@ struct DevModel {
   const MathTable *lt;                      // double-double tables for cr_log/cr_exp/cr_pow
   const float *twf;                         // the twiddles rounded to float (mixed form)
   const float *fkern_h, *fkern_v;           // circulant filter kernels per row (mixed form, tensor-core filter)
-  int mixed;                                // precision form: 0 FP64, 1 mixed (FP32 stencils)
+  int mixed;                                // FP32 stencils, advection, hyperviscosity, filter, physics
+  int col64;                                // mixed, with the vertical pressure/geopotential integration
+                                            // (set_p2etc, store_pgrad_vars) and the pressure gradient in FP64
+  int cr;                                   // binary64 log/exp/pow correctly rounded (the drop-in form);
+                                            // else the libdevice functions
   // state
   double *u, *v, *dudt, *dvdt, *hdry, *theta, *p3, *h3, *p2, *theta2, *t2, *t3, *rho2, *rho3, *exner3;
   double *gz3, *mont3, *heat3, *pv3, *ri2, *div_uv3, *w3, *dzdt3, *u_spinup, *gz_surface;
@@ -103,10 +107,11 @@ __device__ __forceinline__ int fcmp(double x1, double x2) {
 }
 
 // get_sigma / get_p_sigma / g_sigma / f_sigma / return_sigmatheta, epic_funcs_diag.c:1238-1314,1751-1770
-// Transcendentals are correctly rounded (dd_math.cuh) so that they agree with the reference's libm.
-__device__ __forceinline__ double xlog(const DevModel &M, double x) { return cr_log(x, *M.lt); }
-__device__ __forceinline__ double xexp(const DevModel &M, double x) { return cr_exp(x, *M.lt); }
-__device__ __forceinline__ double xpow(const DevModel &M, double x, double y) { return cr_pow(x, y, *M.lt); }
+// In the drop-in form the transcendentals are correctly rounded (dd_math.cuh) so that they agree
+// with the reference's libm; the mixed form's binary64 kernels take the libdevice functions.
+__device__ __forceinline__ double xlog(const DevModel &M, double x) { return M.cr ? cr_log(x, *M.lt) : ::log(x); }
+__device__ __forceinline__ double xexp(const DevModel &M, double x) { return M.cr ? cr_exp(x, *M.lt) : ::exp(x); }
+__device__ __forceinline__ double xpow(const DevModel &M, double x, double y) { return M.cr ? cr_pow(x, y, *M.lt) : ::pow(x, y); }
 __device__ __forceinline__ double get_sigma(const DevModel &M, double pbot, double p, double ptop) {
   return xlog(M, p / pbot) / xlog(M, ptop / pbot);
 }
@@ -196,6 +201,7 @@ template <> struct RMath<double> {
   static __device__ __forceinline__ double pow(const DevModel &M, double x, double y) { return xpow(M, x, y); }
   static __device__ __forceinline__ int cmp(double x1, double x2) { return fcmp(x1, x2); }
   static __device__ __forceinline__ double log_pow(const DevModel &M, double x, double y, double &lg) {
+    if (!M.cr) { lg = ::log(x); return ::pow(x, y); }
     return cr_log_pow(x, y, *M.lt, lg);
   }
   static __device__ __forceinline__ double cos4(const DevModel &M, int j) { return M.coslat4[j]; }

@@ -296,7 +296,8 @@ extern "C" const char *epic_last_error(void) { return epic::error_buffer(); }
 extern "C" int epic_model_create(const epic_grid *g, int32_t precision, epic_model **out) {
   if (!g || !out) return set_error(EPIC_ERR_ARG, "epic_model_create: NULL argument");
   *out = nullptr;
-  if (precision != EPIC_PREC_FP64 && precision != EPIC_PREC_MIXED) return set_error(EPIC_ERR_ARG, "precision form %d not available", precision);
+  if (precision != EPIC_PREC_FP64 && precision != EPIC_PREC_MIXED && precision != EPIC_PREC_MIXED_FAST)
+    return set_error(EPIC_ERR_ARG, "precision form %d not available", precision);
   if (g->ni < 4 || (g->ni & (g->ni - 1)) || g->ni > EPIC_MAX_NI) return set_error(EPIC_ERR_ARG, "ni=%d: need a power of 2 in [4,%d]", g->ni, EPIC_MAX_NI);
   if (g->nj < 3 || g->nk < 3 || g->nk > EPIC_MAX_NK) return set_error(EPIC_ERR_ARG, "nj=%d nk=%d out of range", g->nj, g->nk);
   if (3. * (g->ni + 2) * (g->nj + 3) * (g->nk + 2) >= 2147483648.)
@@ -331,7 +332,9 @@ extern "C" int epic_model_create(const epic_grid *g, int32_t precision, epic_mod
   d.kappa = g->kappa; d.cp = g->cp; d.cpr = g->cpr; d.rgas = g->rgas;
   d.mu_dry = 1. / (g->rgas / 8.314472e+3);
   d.hs_kf = g->hs_kf; d.lat0 = g->lat0;
-  d.mixed = precision == EPIC_PREC_MIXED;
+  d.mixed = precision != EPIC_PREC_FP64;
+  d.col64 = precision == EPIC_PREC_MIXED;
+  d.cr = precision == EPIC_PREC_FP64;
 
   HostTables T;
   filter_tables(*g, L, T);
@@ -403,7 +406,7 @@ extern "C" int epic_model_create(const epic_grid *g, int32_t precision, epic_mod
   std::vector<float> twf_host(T.tw.begin(), T.tw.end());
   cudaMemcpyAsync(twf, twf_host.data(), twf_host.size() * sizeof(float), cudaMemcpyHostToDevice, m->stream);
   std::vector<float> fk_host;
-  if (precision == EPIC_PREC_MIXED) {   // circulant kernels of the tensor-core filter
+  if (precision != EPIC_PREC_FP64) {   // circulant kernels of the tensor-core filter
     fk_host.assign(2 * (size_t)(g->nj + 3) * g->ni, 0.f);
     epic::fill_filter_kernels(g->ni, g->nj, T.high_lat_h.data(), T.high_lat_pv.data(), L.iadim, fk_host.data(),
                               fk_host.data() + (size_t)(g->nj + 3) * g->ni);
@@ -429,8 +432,8 @@ extern "C" int epic_model_create(const epic_grid *g, int32_t precision, epic_mod
   d.mn_inv = j1[8];
   d.sgth = sg; d.dsgth = ds; d.dsgth_inv = dsi; d.h_min = hmin; d.t_sponge_inv = tsp;
   d.high_lat_h = hlh; d.high_lat_pv = hlpv; d.h_coef = hc; d.v_coef = vc; d.tw = tw; d.twf = twf;
-  d.fkern_h = precision == EPIC_PREC_MIXED ? fkh : nullptr;
-  d.fkern_v = precision == EPIC_PREC_MIXED ? fkv : nullptr;
+  d.fkern_h = precision != EPIC_PREC_FP64 ? fkh : nullptr;
+  d.fkern_v = precision != EPIC_PREC_FP64 ? fkv : nullptr;
   epic::filter_kernels_init(g->ni);
   epic::column_kernels_init(g->nk);
   epic::filter_gemm_init(g->ni);
@@ -688,7 +691,7 @@ struct epic_batch {
 namespace {
 
 bool same_launch_shape(const DevModel &a, const DevModel &b) {
-  if (a.ni != b.ni || a.nj != b.nj || a.nk != b.nk || a.uv_scheme != b.uv_scheme || a.mixed != b.mixed ||
+  if (a.ni != b.ni || a.nj != b.nj || a.nk != b.nk || a.uv_scheme != b.uv_scheme || a.mixed != b.mixed || a.col64 != b.col64 ||
       a.k_sigma != b.k_sigma || a.k_sponge != b.k_sponge || a.newt_cool_on != b.newt_cool_on || a.dt != b.dt ||
       a.nudiv != b.nudiv || a.lat0 != b.lat0)
     return false;
@@ -890,6 +893,12 @@ extern "C" int epic_batch_autotune(epic_batch *b, int32_t trial_steps, int32_t *
       b->d.tb[g] = cand[c];
       float ms = 0.f;
       rc = time_steps(&ms);
+      if (rc == EPIC_ERR_CUDA && c > 0 && cudaStreamSynchronize(b->stream) == cudaSuccess) {
+        // a block size some kernel of the group cannot launch with (its registers per block):
+        // the launch failed before running, nothing is in flight; skip the candidate
+        rc = EPIC_OK;
+        continue;
+      }
       if (rc == EPIC_OK && ms < best_ms) { best_ms = ms; best = cand[c]; }
     }
     b->d.tb[g] = best;

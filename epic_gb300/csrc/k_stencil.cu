@@ -491,6 +491,101 @@ __global__ void k_hsu_merid_update(DevModel M, double *A, int k0) {
   write_with_pads(A, M, M.at(c.k, c.j, 0), c.i, A[x] + to_d(da));
 }
 
+// The four meridional passes fused: one thread per (k, i) marches j = 0..nj and keeps, in a
+// sliding register window, the original field A at rows j-2..j+2 (A is updated in place behind
+// the march), the split velocity at rows j-1..j+2, the predictor fluxes FF at j+1, j+2, the
+// predicted field AP at j-1..j+1 and the corrector flux FFV at j.  Every value is the same
+// expression on the same operands as in the four passes (k_hsu_merid_pred/apred/corr/update),
+// so the results are identical bit for bit, with no scratch traffic.  Row j+3's loads are issued
+// at the top of iteration j, ahead of the arithmetic that does not need them.
+template <class R>
+__global__ void k_hsu_meridional(DevModel M, double *A, int kind, int k0) {
+  epic_member(M, A);
+  const int i = 1 + (int)(blockIdx.x * blockDim.x + threadIdx.x);
+  const int k = k0 + (int)blockIdx.y;
+  if (i > M.ni) return;
+  const int nj = M.nj;
+  const double *V = M.v + plane_offset(M, PL_UV);
+  const R ep = R(1.e-10), DT = cv<R>(M.dt);
+  const R a_min = kind == 2 ? cv<R>(M.h_min[k]) : R(0.);
+  auto ld = [&](int jj) { return A[M.at(k, jj, i)]; };
+  auto ff_of = [&](int jj, R vm, R vp, R am1, R a0) { return (jj >= 1 && jj <= nj) ? vp * am1 + vm * a0 : R(0.); };
+  auto ap_of = [&](int jj, double ad, R ff0, R ff1) { return cv<R>(ad + to_d((ff0 - ff1) * cv<R>(M.mn[2 * jj + 1]) * DT)); };
+  // window at the top of iteration j
+  R a_m2 = R(0.), a_m1 = R(0.), a_0, a_1, a_2;   // A(j-2..j+2)
+  double ad_0, ad_1, ad_2;                       // A(j..j+2) in binary64
+  R vm_m1 = R(0.), vp_m1 = R(0.), vm_0, vp_0, vm_1, vp_1, vm_2, vp_2;   // split velocity at j-1..j+2
+  R ff_1, ff_2;                                  // FF(j+1), FF(j+2)
+  R ap_m1 = R(0.), ap_0, ap_1;                   // AP(j-1..j+1)
+  R ffv_0 = R(0.);                               // FFV(j); FFV(0) = 0
+  ad_0 = ld(0); ad_1 = ld(1); ad_2 = ld(2);
+  a_0 = cv<R>(ad_0); a_1 = cv<R>(ad_1); a_2 = cv<R>(ad_2);
+  vmp<R>(M, V, kind, k, 0, i, vm_0, vp_0);
+  vmp<R>(M, V, kind, k, 1, i, vm_1, vp_1);
+  vmp<R>(M, V, kind, k, 2, i, vm_2, vp_2);
+  {
+    const R ff_0 = R(0.);   // FF(0): row 0 is outside 1..nj
+    ff_1 = ff_of(1, vm_1, vp_1, a_0, a_1);
+    ff_2 = ff_of(2, vm_2, vp_2, a_1, a_2);
+    ap_0 = ap_of(0, ad_0, ff_0, ff_1);
+    ap_1 = ap_of(1, ad_1, ff_1, ff_2);
+  }
+  // aaa(jj) of the reference from a(jj-1), a(jj), a(jj+1)
+  auto aaa = [&](int jj, R am, R a0v, R ap1) {
+    R t;
+    if (jj == 0) t = fabs(-a0v + ap1) + ep;
+    else if (jj == nj) t = fabs(am - a0v) + ep;
+    else t = fabs(am - R(2.) * a0v + ap1) + ep;
+    return t * t;
+  };
+  for (int j = 0; j <= nj; j++) {
+    // row j+3's inputs (rows beyond nj+1 do not exist and are not used)
+    const int j3 = j + 3;
+    double ad_3 = 0.;
+    R vm_3 = R(0.), vp_3 = R(0.);
+    if (j3 <= nj + 1) {
+      ad_3 = ld(j3);
+      vmp<R>(M, V, kind, k, j3, i, vm_3, vp_3);
+    }
+    // FFV(j+1): the corrector flux of row jj = j+1 (k_hsu_merid_corr)
+    R ffv_1 = R(0.);
+    const int jj = j + 1;
+    if (jj >= 1 && jj <= nj) {
+      const R diff1_jj = ap_1 - a_0;                              // diff1(jj), jj >= 1
+      const R diff1_jm = (jj - 1 == 0) ? R(0.) : ap_0 - a_m1;     // diff1(jj-1)
+      const R diff2_jm = (jj - 1 == nj) ? R(0.) : ap_0 - a_1;     // diff2(jj-1)
+      const R diff2_jj = (jj == nj) ? R(0.) : ap_1 - a_2;         // diff2(jj)
+      R f = R(.5) * (vp_1 * (ap_1 + a_0) + vm_1 * (ap_0 + a_1));
+      const R vhatp = sqrt(vp_1 * vp_0);
+      const R vhatm = -sqrt(vm_1 * vm_2);
+      const R mu = (vp_1 - vm_1) * cv<R>(M.mn[2 * jj]) * DT;
+      const R al = (R(1.) + mu) / R(6.);
+      const R am1 = aaa(jj - 1, a_m1, a_0, a_1), a0 = aaa(jj, a_0, a_1, a_2);
+      const R prod = (a_0 - a_min) * (a_1 - a_min);
+      R gap = am1 / (am1 + prod); gap = gap * gap;
+      R gam = a0 / (a0 + prod); gam = gam * gam;
+      const R bep = R(1.) + (R(1.) / (R(2.) * al) - R(1.)) * gap;
+      const R bem = R(1.) + (R(1.) / (R(2.) * al) - R(1.)) * gam;
+      f += -al * (vp_1 * bep * diff1_jj - vhatp * (R(1.) - gap) * diff1_jm + vm_1 * bem * diff2_jm - vhatm * (R(1.) - gam) * diff2_jj);
+      ffv_1 = f;
+    }
+    // the update of row j (k_hsu_merid_update)
+    const R da = (ffv_0 - ffv_1) * cv<R>(M.mn[2 * j + 1]) * cv<R>(M.dt);
+    write_with_pads(A, M, M.at(k, j, 0), i, ad_0 + to_d(da));
+    // advance the window to j+1: FF(j+3), AP(j+2)
+    const R a_3 = cv<R>(ad_3);
+    const R ff_3 = ff_of(j3, vm_3, vp_3, a_2, a_3);
+    const R ap_2 = (j + 2 <= nj) ? ap_of(j + 2, ad_2, ff_2, ff_3) : R(0.);
+    a_m2 = a_m1; a_m1 = a_0; a_0 = a_1; a_1 = a_2; a_2 = a_3;
+    ad_0 = ad_1; ad_1 = ad_2; ad_2 = ad_3;
+    vm_m1 = vm_0; vp_m1 = vp_0; vm_0 = vm_1; vp_0 = vp_1; vm_1 = vm_2; vp_1 = vp_2; vm_2 = vm_3; vp_2 = vp_3;
+    ff_1 = ff_2; ff_2 = ff_3;
+    ap_m1 = ap_0; ap_0 = ap_1; ap_1 = ap_2;
+    ffv_0 = ffv_1;
+  }
+  (void)a_m2; (void)vm_m1; (void)vp_m1; (void)ap_m1;
+}
+
 // ---------------------------------------------------------------------------------------------
 // Hyperviscosity, epic_subgrid.c:590-1232
 // ---------------------------------------------------------------------------------------------
@@ -850,19 +945,30 @@ int launch_uv_core(const DevModel &M, cudaStream_t s) {
 
 int launch_uv_pgrad(const DevModel &M, cudaStream_t s) {
   k_gz_pole_rows<<<zg(M.nk + 1, M), 128, 0, s>>>(M);
-  if (M.mixed) k_pgrad_split<<<zg(epic_blocks(M.n3, TB(M, TB_POINT)), M), TB(M, TB_POINT), 0, s>>>(M);
-  EPIC_LAUNCH_R(M.mixed, k_pgrad_lon, cells_blocks(M, M.nk - 1, M.nj + 1, TB(M, TB_PGRAD)), TB(M, TB_PGRAD), 0, s, M);
-  EPIC_LAUNCH_R(M.mixed, k_pgrad_lat, cells_blocks(M, M.nk - 1, M.nj, TB(M, TB_PGRAD)), TB(M, TB_PGRAD), 0, s, M);
+  const int f32 = M.mixed && !M.col64;
+  if (f32) k_pgrad_split<<<zg(epic_blocks(M.n3, TB(M, TB_POINT)), M), TB(M, TB_POINT), 0, s>>>(M);
+  EPIC_LAUNCH_R(f32, k_pgrad_lon, cells_blocks(M, M.nk - 1, M.nj + 1, TB(M, TB_PGRAD)), TB(M, TB_PGRAD), 0, s, M);
+  EPIC_LAUNCH_R(f32, k_pgrad_lat, cells_blocks(M, M.nk - 1, M.nj, TB(M, TB_PGRAD)), TB(M, TB_PGRAD), 0, s, M);
   return 0;
 }
+
+// The fused march (k_hsu_meridional) has one thread per (k, i, member) walking nj+1 rows; it
+// wins once those threads fill the GPU (large batches).  Smaller launches take the four passes,
+// whose threads cover every cell.  Both give the same bits.
+constexpr long long HSU_FUSED_MIN_THREADS = 65536;
 
 int launch_hsu_meridional(const DevModel &M, double *buff, int kind, cudaStream_t s) {
   const int k0 = kind == 1 ? M.k_sigma - 1 : 1;
   const int nkk = M.nk - k0 + 1;
-  EPIC_LAUNCH_R(M.mixed, k_hsu_merid_pred, cells_blocks(M, nkk, M.nj + 2, TB(M, TB_HSU)), TB(M, TB_HSU), 0, s, M, buff, kind, k0);
-  EPIC_LAUNCH_R(M.mixed, k_hsu_merid_apred, cells_blocks(M, nkk, M.nj + 1, TB(M, TB_HSU)), TB(M, TB_HSU), 0, s, M, buff, k0);
-  EPIC_LAUNCH_R(M.mixed, k_hsu_merid_corr, cells_blocks(M, nkk, M.nj + 2, TB(M, TB_HSU)), TB(M, TB_HSU), 0, s, M, buff, kind, k0);
-  EPIC_LAUNCH_R(M.mixed, k_hsu_merid_update, cells_blocks(M, nkk, M.nj + 1, TB(M, TB_HSU)), TB(M, TB_HSU), 0, s, M, buff, k0);
+  const int th = TB(M, TB_HSU);
+  if ((long long)M.ni * nkk * (M.nbatch > 1 ? M.nbatch : 1) >= HSU_FUSED_MIN_THREADS) {
+    EPIC_LAUNCH_R(M.mixed, k_hsu_meridional, dim3(epic_blocks(M.ni, th), nkk), th, 0, s, M, buff, kind, k0);
+    return 0;
+  }
+  EPIC_LAUNCH_R(M.mixed, k_hsu_merid_pred, cells_blocks(M, nkk, M.nj + 2, th), th, 0, s, M, buff, kind, k0);
+  EPIC_LAUNCH_R(M.mixed, k_hsu_merid_apred, cells_blocks(M, nkk, M.nj + 1, th), th, 0, s, M, buff, k0);
+  EPIC_LAUNCH_R(M.mixed, k_hsu_merid_corr, cells_blocks(M, nkk, M.nj + 2, th), th, 0, s, M, buff, kind, k0);
+  EPIC_LAUNCH_R(M.mixed, k_hsu_merid_update, cells_blocks(M, nkk, M.nj + 1, th), th, 0, s, M, buff, k0);
   return 0;
 }
 

@@ -40,8 +40,13 @@ extern "C" {
 
 /* Precision forms accepted by epic_model_create(). */
 #define EPIC_PREC_FP64  0    /* every kernel in binary64 (the drop-in form)                    */
-#define EPIC_PREC_MIXED 1    /* stencils/advection/hyperviscosity in binary32, vertical sums,
-                                updates and global sums in binary64                           */
+#define EPIC_PREC_MIXED 1    /* stencils/advection/hyperviscosity/filter/physics in binary32;
+                                the vertical pressure and geopotential integration (set_p2etc,
+                                store_pgrad_vars), the pressure gradient, the updates and the
+                                global sums in binary64 (libdevice log/exp/pow)                */
+#define EPIC_PREC_MIXED_FAST 2   /* as EPIC_PREC_MIXED, with the vertical integration and the
+                                pressure gradient in binary32 too (binary64 running sums and
+                                updates kept): faster, larger error in the meridional wind     */
 
 /* Error codes. */
 #define EPIC_OK               0

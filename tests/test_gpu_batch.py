@@ -3,7 +3,7 @@ exactly the bits it gets when stepped alone, in both precision forms."""
 import numpy as np
 import pytest
 
-from epic_gb300 import (EPIC_PREC_FP64, EPIC_PREC_MIXED, EPIC_SYNC_DIAGS_ONLY, EPIC_UV_AB3, EPIC_UV_LEAPFROG, Batch,
+from epic_gb300 import (EPIC_PREC_FP64, EPIC_PREC_MIXED, EPIC_PREC_MIXED_FAST, EPIC_SYNC_DIAGS_ONLY, EPIC_UV_AB3, EPIC_UV_LEAPFROG, Batch,
                         EpicError, HSConfig, Model, hs_setup)
 
 pytestmark = pytest.mark.gpu
@@ -19,7 +19,8 @@ def _member(seed, kf_scale, precision, shape=(32, 16, 10), scheme=EPIC_UV_AB3):
 
 
 @pytest.mark.parametrize("precision,scheme", [(EPIC_PREC_FP64, EPIC_UV_AB3), (EPIC_PREC_MIXED, EPIC_UV_AB3),
-                                              (EPIC_PREC_FP64, EPIC_UV_LEAPFROG), (EPIC_PREC_MIXED, EPIC_UV_LEAPFROG)])
+                                              (EPIC_PREC_MIXED_FAST, EPIC_UV_AB3), (EPIC_PREC_FP64, EPIC_UV_LEAPFROG),
+                                              (EPIC_PREC_MIXED, EPIC_UV_LEAPFROG), (EPIC_PREC_MIXED_FAST, EPIC_UV_LEAPFROG)])
 def test_batch_equals_members_alone(gpu, precision, scheme):
     scales = [1.0, 0.93, 1.07, 1.1, 0.9]
     members = [_member(10 + q, s, precision, scheme=scheme) for q, s in enumerate(scales)]
@@ -44,10 +45,13 @@ def test_batch_rejects_mixed_shapes(gpu):
     _, _, a = _member(1, 1.0, EPIC_PREC_FP64)
     _, _, b = _member(2, 1.0, EPIC_PREC_FP64, shape=(64, 32, 10))
     _, _, c = _member(3, 1.0, EPIC_PREC_MIXED)
+    _, _, d = _member(4, 1.0, EPIC_PREC_MIXED_FAST)
     with pytest.raises(EpicError, match="differs"):
         Batch([a, b])
     with pytest.raises(EpicError, match="differs"):
         Batch([a, c])
+    with pytest.raises(EpicError, match="differs"):
+        Batch([c, d])
 
 
 def test_autotuned_shapes_change_no_result(gpu):

@@ -1,25 +1,48 @@
-"""The mixed-precision form (EPIC_PREC_MIXED) against the FP64 form on the GPU.
+"""The two mixed-precision forms against the FP64 form on the GPU.
 
-Mixed form: stencils, advection, hyperviscosity, the pressure gradient, the zonal filter (on the
-tensor cores for ni a multiple of 128) and the physics evaluate in FP32; the hydrostatic sums
-(P3, GZ3, SUM_DIV), the row means, every update of a stored field and the Adams-Bashforth/
-leapfrog step stay FP64 (the state is stored in FP64).
+EPIC_PREC_MIXED: stencils, advection, hyperviscosity, the zonal filter (on the tensor cores for
+ni a multiple of 128), calc_w and the physics evaluate in FP32; the vertical pressure and
+geopotential integration (set_p2etc, store_pgrad_vars), the pressure gradient, the running sums,
+every update of a stored field and the Adams-Bashforth/leapfrog step stay FP64 (the state is
+stored in FP64).
+EPIC_PREC_MIXED_FAST: the same with set_p2etc, store_pgrad_vars and the pressure gradient in FP32
+too (their running sums and the updates stay FP64).
 
-Stated error (relative L2 per field, mixed vs FP64), measured on a GB300:
-  * one simulated day (288 steps of 300 s) at 64x32x10 from a state spun up for 10 days:
-    U 3.5e-5, V 3.9e-4, HDRY 2.6e-7, THETA 3.7e-8;
-  * one simulated day from rest: U 2.2e-4, V 5.9e-4 (the first days are driven by horizontal
-    pressure differences 1e-5 of the geopotential, so FP32 rounding is amplified ~1e4 in U, V).
-The bounds below leave a factor ~3 over those figures.
+Stated error (relative L2 per field vs FP64, 64x32x10, dt 300 s), measured on a GB300:
+
+  form   case                              U        V        HDRY     THETA
+  mixed  1 day after a 10-day spin-up      9.6e-6   4.2e-5   6.1e-8   3.3e-9
+  mixed  1 day from rest                   6.4e-5   8.0e-5   5.7e-8   3.2e-9
+  mixed  12 h from rest, leapfrog          8.4e-4   2.1e-4   6.5e-8   2.9e-9
+  fast   1 day after a 10-day spin-up      3.8e-5   6.1e-4   3.9e-7   3.7e-8
+  fast   1 day from rest                   2.5e-4   8.3e-4   2.1e-7   3.7e-8
+  fast   12 h from rest, leapfrog          1.9e-3   7.2e-4   1.9e-7   3.7e-8
+
+The first hours from rest are driven by horizontal pressure differences 1e-5 of the geopotential,
+so rounding is amplified there (the leapfrog case ends at 12 h: the FP64 leapfrog run of this
+configuration itself stops with non-monotonic GZ3 in its second day).  The fast form's V error
+comes from FP32 rounding of P2, THETA and GZ3 recomputed every step (the pressure-gradient
+chain); the mixed form keeps that chain in FP64 and stays within 1e-4 after one day.  The bounds
+below leave a factor ~3 over the figures.
 """
 import numpy as np
 import pytest
 
 from compare import PROGNOSTIC, field_errors
-from epic_gb300 import EPIC_PREC_FP64, EPIC_PREC_MIXED, EPIC_SYNC_DIAGS_ONLY, EPIC_UV_LEAPFROG, HSConfig, Model, hs_setup
+from epic_gb300 import (EPIC_PREC_FP64, EPIC_PREC_MIXED, EPIC_PREC_MIXED_FAST, EPIC_SYNC_DIAGS_ONLY, EPIC_UV_LEAPFROG,
+                        HSConfig, Model, hs_setup)
 
 pytestmark = pytest.mark.gpu
 DAY = 288   # steps of 300 s
+FORMS = {"mixed": EPIC_PREC_MIXED, "fast": EPIC_PREC_MIXED_FAST}
+BOUNDS = {
+    ("mixed", "spun_up"): {"u": 3e-5, "v": 1e-4, "hdry": 2e-7, "theta": 1e-8},
+    ("mixed", "rest"): {"u": 2e-4, "v": 2.5e-4, "hdry": 2e-7, "theta": 1e-8},
+    ("mixed", "leapfrog"): {"u": 3e-3, "v": 1e-3, "hdry": 2e-7, "theta": 1e-8},
+    ("fast", "spun_up"): {"u": 1e-4, "v": 2e-3, "hdry": 1e-6, "theta": 1e-7},
+    ("fast", "rest"): {"u": 1e-3, "v": 3e-3, "hdry": 1e-6, "theta": 1e-7},
+    ("fast", "leapfrog"): {"u": 6e-3, "v": 3e-3, "hdry": 1e-6, "theta": 1e-7},
+}
 
 
 @pytest.fixture(scope="module")
@@ -33,8 +56,8 @@ def spun_up(gpu):
     return ga, m.download()
 
 
-def _pair(ga, f, prime):
-    a, b = Model(ga, EPIC_PREC_FP64), Model(ga, EPIC_PREC_MIXED)
+def _pair(ga, f, prime, precision):
+    a, b = Model(ga, EPIC_PREC_FP64), Model(ga, precision)
     for m in (a, b):
         m.upload(f)
         if prime:
@@ -50,42 +73,40 @@ def _run(a, b, n):
     return field_errors(b.download(), a.download(), PROGNOSTIC)
 
 
-def test_mixed_one_day_after_spin_up(spun_up):
+def _check(e, bounds):
+    assert all(e[k][0] <= bounds[k] for k in bounds), e
+
+
+@pytest.mark.parametrize("form", FORMS)
+def test_one_day_after_spin_up(spun_up, form):
     ga, f = spun_up
-    a, b = _pair(ga, f, prime=False)
-    e = _run(a, b, DAY)
-    bounds = {"u": 1e-4, "v": 1e-3, "hdry": 1e-6, "theta": 1e-7}
-    assert all(e[k][0] <= bounds[k] for k in bounds), e
+    a, b = _pair(ga, f, False, FORMS[form])
+    _check(_run(a, b, DAY), BOUNDS[(form, "spun_up")])
 
 
-def test_mixed_one_day_from_rest(gpu):
+@pytest.mark.parametrize("form", FORMS)
+def test_one_day_from_rest(gpu, form):
     ga, f = hs_setup(HSConfig(ni=64, nj=32, nk=10, dt=300, seed=0))
-    a, b = _pair(ga, f, prime=True)
-    e = _run(a, b, DAY)
-    bounds = {"u": 1e-3, "v": 2e-3, "hdry": 1e-6, "theta": 1e-7}
-    assert all(e[k][0] <= bounds[k] for k in bounds), e
+    a, b = _pair(ga, f, True, FORMS[form])
+    _check(_run(a, b, DAY), BOUNDS[(form, "rest")])
 
 
-def test_mixed_leapfrog_follows_fp64(gpu):
-    """The leapfrog (Asselin-filtered) wind step in the mixed form, 12 simulated hours from rest
-    (measured on a GB300: U 1.6e-3, V 5.0e-4, HDRY 1.5e-7, THETA 3.7e-8; the U, V errors are
-    those of the AB3 form at the same time, where the winds are still weak).  The FP64 leapfrog
-    run of this configuration itself stops with non-monotonic GZ3 between the first and second
-    day, so the comparison ends before.  The time-plane bookkeeping (IT_ZERO, itime) must be the
-    FP64 form's."""
+@pytest.mark.parametrize("form", FORMS)
+def test_leapfrog_follows_fp64(gpu, form):
+    """The leapfrog (Asselin-filtered) wind step, 12 simulated hours from rest; the time-plane
+    bookkeeping (IT_ZERO, itime) must be the FP64 form's."""
     ga, f = hs_setup(HSConfig(ni=64, nj=32, nk=10, dt=300, seed=0, uv_scheme=EPIC_UV_LEAPFROG))
-    a, b = _pair(ga, f, prime=True)
-    e = _run(a, b, DAY // 2)
-    bounds = {"u": 5e-3, "v": 2e-3, "hdry": 1e-6, "theta": 1e-7}
-    assert all(e[k][0] <= bounds[k] for k in bounds), e
+    a, b = _pair(ga, f, True, FORMS[form])
+    _check(_run(a, b, DAY // 2), BOUNDS[(form, "leapfrog")])
     fa, fb = a.download(), b.download()
     assert (fa.struct.it_zero, fa.struct.itime) == (fb.struct.it_zero, fb.struct.itime)
 
 
-def test_mixed_is_deterministic(gpu):
-    """Two mixed runs (graph replay and single steps) give identical bits."""
+@pytest.mark.parametrize("form", FORMS)
+def test_is_deterministic(gpu, form):
+    """Two runs (graph replay and single steps) give identical bits."""
     ga, f = hs_setup(HSConfig(ni=32, nj=16, nk=10, dt=300, seed=4))
-    m1, m2 = Model(ga, EPIC_PREC_MIXED), Model(ga, EPIC_PREC_MIXED)
+    m1, m2 = Model(ga, FORMS[form]), Model(ga, FORMS[form])
     for m in (m1, m2):
         m.upload(f)
         m.timestep(EPIC_SYNC_DIAGS_ONLY)
@@ -103,11 +124,13 @@ def test_models_of_different_sizes_coexist(gpu):
     """Creating a smaller model after a larger one must not shrink any launch limit the larger
     one needs (shared-memory sizes depend on ni and nk)."""
     big_ga, big_f = hs_setup(HSConfig(ni=256, nj=128, nk=20, dt=150))
-    big = Model(big_ga, EPIC_PREC_MIXED)
-    big64 = Model(big_ga, EPIC_PREC_FP64)
     small_ga, small_f = hs_setup(HSConfig(ni=32, nj=16, nk=10, dt=300))
-    small, small64 = Model(small_ga, EPIC_PREC_MIXED), Model(small_ga, EPIC_PREC_FP64)
-    for m, f in ((big, big_f), (big64, big_f), (small, small_f), (small64, small_f)):
+    models = []
+    for prec in (EPIC_PREC_MIXED, EPIC_PREC_MIXED_FAST, EPIC_PREC_FP64):
+        models.append((Model(big_ga, prec), big_f))
+    for prec in (EPIC_PREC_MIXED, EPIC_PREC_MIXED_FAST, EPIC_PREC_FP64):
+        models.append((Model(small_ga, prec), small_f))
+    for m, f in models:
         m.upload(f)
         m.timestep(EPIC_SYNC_DIAGS_ONLY)
         m.run(2)
