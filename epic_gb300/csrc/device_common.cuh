@@ -6,7 +6,9 @@
 #include <cuda_runtime.h>
 #include <cstdint>
 #include <cfloat>
+#include <type_traits>
 #include "dd_math.cuh"
+#include "df.cuh"
 
 // kernel groups whose block size the autotuner picks (DevModel::tb)
 enum TuneGroup { TB_UV_CORE = 0, TB_PGRAD, TB_HSU, TB_VISC, TB_DIAG, TB_UPDATE, TB_COLUMN, TB_POINT, TB_ROW, TB_COUNT };
@@ -54,6 +56,7 @@ struct DevModel {
   const MathTable *lt;                      // double-double tables for cr_log/cr_exp/cr_pow
   const float *twf;                         // the twiddles rounded to float (mixed form)
   const float *fkern_h, *fkern_v;           // circulant filter kernels per row (mixed form, tensor-core filter)
+  const float2 *exp2tab;                    // 2^(j/32), j = 0..31, as double-floats (exp_df)
   int mixed;                                // FP32 stencils, advection, hyperviscosity, filter, physics
   int col64;                                // mixed, with the vertical pressure/geopotential integration
                                             // (set_p2etc, store_pgrad_vars) and the pressure gradient in FP64
@@ -189,8 +192,13 @@ __device__ __forceinline__ double f2d(float f) {
 template <class R> __device__ __forceinline__ R cv(double x);
 template <> __device__ __forceinline__ double cv<double>(double x) { return x; }
 template <> __device__ __forceinline__ float cv<float>(double x) { return d2f(x); }
+template <> __device__ __forceinline__ dfl cv<dfl>(double x) {
+  const float h = d2f(x);
+  return dfl(h, d2f(x - f2d(h)));
+}
 __device__ __forceinline__ double to_d(double x) { return x; }
 __device__ __forceinline__ double to_d(float x) { return f2d(x); }
+__device__ __forceinline__ double to_d(dfl x) { return f2d(x.hi) + f2d(x.lo); }
 
 template <class R> __device__ __forceinline__ R rmax(R x, R y) { return x > y ? x : y; }
 template <class R> __device__ __forceinline__ R rmin(R x, R y) { return x < y ? x : y; }
@@ -205,6 +213,11 @@ template <> struct RMath<double> {
     return cr_log_pow(x, y, *M.lt, lg);
   }
   static __device__ __forceinline__ double cos4(const DevModel &M, int j) { return M.coslat4[j]; }
+};
+template <> struct RMath<dfl> {
+  static __device__ __forceinline__ dfl log(const DevModel &M, dfl x) { return log_df(x, M.exp2tab); }
+  static __device__ __forceinline__ dfl exp(const DevModel &M, dfl x) { return exp_df(x, M.exp2tab); }
+  static __device__ __forceinline__ dfl pow(const DevModel &M, dfl x, dfl y) { return exp_df(y * log_df(x, M.exp2tab), M.exp2tab); }
 };
 template <> struct RMath<float> {
   static __device__ __forceinline__ float log(const DevModel &, float x) { return logf(x); }

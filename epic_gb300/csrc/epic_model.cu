@@ -280,7 +280,7 @@ size_t model_pool_bytes(const epic_grid &g) {
   return rnd(sizeof(Ctl)) + (n_state3 + n_scratch3) * rnd(n3 * 8) + 3 * rnd(n2 * 8) + rnd((size_t)(g.nj + 3) * (g.nk + 2) * 3 * 8) +
          rnd(ni1 * 8) + 10 * rnd(nj1 * 8) + 3 * rnd(nk1 * 8) + rnd((g.nk + 2) * 8) + rnd((g.k_sponge + 1) * 8) +
          2 * rnd(3 * (g.nj + 2) * 8) + rnd(ntw * 8) + rnd(ntw * 4) + 2 * rnd((g.nj + 1) * 8) + rnd(sizeof(epic::MathTable)) +
-         2 * rnd((size_t)(g.nj + 3) * g.ni * 4) + 4096;
+         2 * rnd((size_t)(g.nj + 3) * g.ni * 4) + rnd(32 * sizeof(float2)) + 4096;
 }
 
 }  // namespace
@@ -388,6 +388,7 @@ extern "C" int epic_model_create(const epic_grid *g, int32_t precision, epic_mod
   double *coslat = carve<double>(p, g->nj + 1);
   double *coslat4 = carve<double>(p, g->nj + 1);
   epic::MathTable *lt = carve<epic::MathTable>(p, 1);
+  float2 *exp2tab = carve<float2>(p, 32);
   if ((size_t)(p - m->pool) > bytes) {
     epic_model_destroy(m);
     return set_error(EPIC_ERR_NOMEM, "internal pool layout overflow");
@@ -425,9 +426,18 @@ extern "C" int epic_model_create(const epic_grid *g, int32_t precision, epic_mod
   for (int J = 0; J <= g->nj; J++) cl4[J] = epic::cr_pow(cl[J], 4., host_lt[0]);
   up(coslat4, cl4.data(), cl4.size());
   cudaMemcpyAsync(lt, host_lt.data(), sizeof(epic::MathTable), cudaMemcpyHostToDevice, m->stream);
+  // 2^(j/32) as double-floats for the double-float exponential of the mixed form
+  std::vector<float2> e2(32);
+  for (int q = 0; q < 32; q++) {
+    const double v = std::exp2(q / 32.);
+    e2[q].x = (float)v;
+    e2[q].y = (float)(v - (double)e2[q].x);
+  }
+  cudaMemcpyAsync(exp2tab, e2.data(), e2.size() * sizeof(float2), cudaMemcpyHostToDevice, m->stream);
   d.coslat = coslat;
   d.coslat4 = coslat4;
   d.lt = lt;
+  d.exp2tab = exp2tab;
   d.lon = lon; d.lat = j1[0]; d.rln = j1[1]; d.rlt = j1[2]; d.f = j1[3]; d.m = j1[4]; d.n = j1[5]; d.mn = j1[6]; d.grav = j1[7];
   d.mn_inv = j1[8];
   d.sgth = sg; d.dsgth = ds; d.dsgth_inv = dsi; d.h_min = hmin; d.t_sponge_inv = tsp;
@@ -436,6 +446,7 @@ extern "C" int epic_model_create(const epic_grid *g, int32_t precision, epic_mod
   d.fkern_v = precision != EPIC_PREC_FP64 ? fkv : nullptr;
   epic::filter_kernels_init(g->ni);
   epic::column_kernels_init(g->nk);
+  epic::column_acc_kernels_init();
   epic::filter_gemm_init(g->ni);
   e = cudaStreamSynchronize(m->stream);
   if (e != cudaSuccess) {

@@ -1,6 +1,7 @@
 // Column (vertical) kernels: one thread per (j,i) column, marching in k.
 // Each kernel restates the reference routine named in its comment.
 #include "device_common.cuh"
+#include "column_tile.cuh"
 #include "kernels.h"
 #include "epic_common.h"
 #include "epic_gb300.h"
@@ -26,61 +27,6 @@ __global__ void k_source_sink(DevModel M) {
     const long long x = M.at(k, j, i);
     M.theta[x] += M.dt * M.heat3[x] / M.exner3[x];
   }
-}
-
-// ---- column tiles ----
-//
-// The transcendental work of calc_w, set_p2etc and store_pgrad_vars is pointwise once a
-// column's pressures are known; only their running sums are sequential.  A block takes 32
-// neighbouring columns (one per lane; neighbouring columns are neighbouring addresses, so every
-// level is one coalesced 256-byte access) and stages their levels in shared memory as
-// [k][lane].  Pointwise phases spread the levels over CT_WARPS warps; warp 0 alone runs each
-// running sum, in the reference's order, so the results are those of one thread per column.
-constexpr int CT_WARPS = 8;
-constexpr int CT_THREADS = 32 * CT_WARPS;
-// levels per warp whose loads a column kernel issues together before using them
-constexpr int TILE_SLOTS = 4;
-
-struct ColTile {
-  int lane, warp, j, i;
-  bool valid;
-  long long base;   // M.at(0, j, i)
-};
-__device__ __forceinline__ ColTile col_tile(const DevModel &M) {
-  ColTile c;
-  c.lane = (int)(threadIdx.x & 31);
-  c.warp = (int)(threadIdx.x >> 5);
-  const int t = (int)blockIdx.x * 32 + c.lane;
-  c.valid = t < (M.nj + 1) * M.iadim;
-  c.j = c.valid ? t / M.iadim : 0;
-  c.i = c.valid ? t - c.j * M.iadim : 0;
-  c.base = M.at(0, c.j, c.i);
-  return c;
-}
-// level k of a [k][lane] shared array
-#define CT(a, k) (a)[(k) * 32 + c.lane]
-
-// f_sigma/g_sigma (epic_funcs_diag.c:1271-1314) in the compute type, one exponential for both
-template <class R>
-__device__ __forceinline__ R f_and_g_sigma_r(const DevModel &M, R s, R &g) {
-  const R ss = cv<R>(M.sigma_sigma), z0 = cv<R>(M.zeta0), z1 = cv<R>(M.zeta1);
-  if (s <= ss) g = R(0.);
-  else if (s >= R(1.)) g = R(1.);
-  else g = cv<R>(M.g_coeff) * (R(1.) - RMath<R>::exp(M, -cv<R>(M.alpha) * (s - ss)));
-  if (s < R(0.)) return z0;
-  if (s <= ss) return z0 + s * (z1 - z0);
-  if (s < R(1.)) return (R(1.) - g) * (z0 + s * (z1 - z0));
-  return R(0.);
-}
-
-// return_sigmatheta (epic_funcs_diag.c:1238-1250) with log(ptop/pbot) supplied
-template <class R>
-__device__ __forceinline__ R sigmatheta_lp(const DevModel &M, R theta, R p, R pbot, R ptop, R lp) {
-  if (p <= ptop) return theta;
-  const R s = RMath<R>::log(M, p / pbot) / lp;
-  R g;
-  const R f = f_and_g_sigma_r<R>(M, s, g);
-  return f + g * theta;
 }
 
 // calc_w, epic_flux.c:123-335.  The Leslie-Purser summed divergence keeps SUM_DIV = 0 at
@@ -942,12 +888,14 @@ int launch_restore_mass(const DevModel &M, cudaStream_t s) {
   return 0;
 }
 int launch_set_p2etc(const DevModel &M, int update_theta, cudaStream_t s) {
-  if (M.mixed && !M.col64) k_set_p2etc_mixed<<<zg(ntile_blocks(M), M), CT_THREADS, tile_smem(M, 3), s>>>(M, update_theta);
+  if (M.col64) k_set_p2etc_acc<<<zg(ntile_blocks(M), M), CT_THREADS, tile_smem(M, 3), s>>>(M, update_theta);
+  else if (M.mixed) k_set_p2etc_mixed<<<zg(ntile_blocks(M), M), CT_THREADS, tile_smem(M, 3), s>>>(M, update_theta);
   else k_set_p2etc<<<zg(ntile_blocks(M), M), CT_THREADS, tile_smem(M, 4), s>>>(M, update_theta);
   return 0;
 }
 int launch_store_pgrad_vars(const DevModel &M, cudaStream_t s) {
-  if (M.mixed && !M.col64) k_pgrad_vars_column_mixed<<<zg(ntile_blocks(M), M), CT_THREADS, tile_smem(M, 5), s>>>(M);
+  if (M.col64) k_pgrad_vars_column_acc<<<zg(ntile_blocks(M), M), CT_THREADS, tile_smem(M, 5), s>>>(M);
+  else if (M.mixed) k_pgrad_vars_column_mixed<<<zg(ntile_blocks(M), M), CT_THREADS, tile_smem(M, 5), s>>>(M);
   else k_pgrad_vars_column<<<zg(ntile_blocks(M), M), CT_THREADS, tile_smem(M, 5), s>>>(M);
   EPIC_LAUNCH_R(M.mixed, k_pgrad_dzdt, epic_blocks((long long)M.nk * (M.nj + 1) * M.ni, TB(M, TB_UPDATE)), TB(M, TB_UPDATE), 0, s, M);
   return 0;

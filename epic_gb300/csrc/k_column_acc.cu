@@ -1,0 +1,279 @@
+// The vertical pressure and geopotential integration of the mixed form (EPIC_PREC_MIXED):
+// set_p2etc and the column part of store_pgrad_vars, with the quantities that feed the pressure
+// gradient -- the layer pressure P2, the diagnosed THETA and THETA2, T3, RHO3 and the
+// geopotential increments -- evaluated in double-float (df.cuh: ~1e-13 relative, on the FP32
+// pipe) instead of binary32, and the running sums in binary64.  Rounding these to binary32 every
+// step is what makes the meridional wind of the all-FP32 form (EPIC_PREC_MIXED_FAST) drift from
+// FP64 by 6e-4 in a day; with them in double-float the mixed form stays within 1e-4.  Diagnostics
+// that nothing in the step reads back (EXNER3's use in the heating, H3, MONT3, DZDT3) stay FP32.
+//
+// Structure, phases and the restated reference lines are those of k_set_p2etc_mixed and
+// k_pgrad_vars_column_mixed (k_column.cu): set_p2etc, epic_funcs_diag.c:3352-3569;
+// store_pgrad_vars, epic_funcs_diag.c:3595-3895.
+#include "device_common.cuh"
+#include "column_tile.cuh"
+#include "kernels.h"
+#include "epic_common.h"
+#include "epic_gb300.h"
+
+namespace epic {
+
+namespace {
+
+__device__ __forceinline__ dfl one_df() { return dfl(1.f, 0.f); }
+
+// onto_kk(P2_INDEX) at a layer: bot * q^(1/kappa), q = (1 - r^(kappa+1)) / ((kappa+1)(1 - r)),
+// r = top/bot.  Layers thinner than 1e-7 relative take the reference's equal-pressure branch
+// (the mean differs from the formula by O(eps^2) there).
+__device__ __forceinline__ double layer_p_acc(const DevModel &M, double top, double bot) {
+  const dfl B = cv<dfl>(bot), T = cv<dfl>(top);
+  const dfl eps = cv<dfl>(bot - top) / B;
+  if (!(eps.hi >= 1e-7f)) return .5 * (bot + top);
+  const dfl a = cv<dfl>(M.kappa + 1.);
+  const dfl lr = log_df(T / B, M.exp2tab);                     // log r < 0
+  const dfl q = (one_df() - exp_df(a * lr, M.exp2tab)) / (a * eps);
+  return to_d(B * exp_df(log_df(q, M.exp2tab) / cv<dfl>(M.kappa), M.exp2tab));
+}
+
+// theta on the hybrid surface sigmatheta = sg at pressure p (the inversion of
+// return_sigmatheta), sigma = log(p/pbot) / log(ptop/pbot)
+__device__ __forceinline__ double theta_acc(const DevModel &M, double sg, double p, dfl pbot, dfl lp) {
+  const dfl sigma = log_df(cv<dfl>(p) / pbot, M.exp2tab) / lp;
+  dfl gs;
+  const dfl fs = f_and_g_sigma_r<dfl>(M, sigma, gs);
+  return to_d((cv<dfl>(sg) - fs) / gs);
+}
+
+}  // namespace
+
+__global__ void __launch_bounds__(CT_THREADS, 2) k_set_p2etc_acc(DevModel M, int update_theta) {
+  epic_member(M);
+  extern __shared__ double sm[];
+  __shared__ double s_lp[32], s_ginv[32];
+  const ColTile c = col_tile(M);
+  const int nk = M.nk, ks = M.k_sigma, L = nk + 1;
+  const long long n2 = M.n2;
+  double *P = sm, *HL = P + 32 * L, *TH = HL + 32 * L;
+  const double g = M.grav[2 * c.j + 1];
+  if (c.valid) {
+    double v[TILE_SLOTS][2];
+#pragma unroll
+    for (int r = 0; r < TILE_SLOTS; r++) {
+      const long long x = c.base + min(c.warp + r * CT_WARPS, nk) * n2;
+      v[r][0] = __ldg(M.theta + x); v[r][1] = __ldg(M.hdry + x);
+    }
+#pragma unroll
+    for (int r = 0; r < TILE_SLOTS; r++) {
+      const int k = c.warp + r * CT_WARPS;
+      if (k <= nk) { CT(TH, k) = v[r][0]; CT(HL, k) = v[r][1]; }
+    }
+    for (int k = c.warp + TILE_SLOTS * CT_WARPS; k <= nk; k += CT_WARPS) {
+      CT(TH, k) = M.theta[c.base + k * n2];
+      CT(HL, k) = M.hdry[c.base + k * n2];
+    }
+  }
+  __syncthreads();
+  if (c.warp == 0 && c.valid) {   // P3 from the top down, in FP64
+    double p = M.p3[c.base];
+    CT(P, 0) = p;
+    for (int k = 1; k <= nk; k++) {
+      p = fma(M.dsgth[2 * k] * g, CT(HL, k), p);
+      CT(P, k) = p;
+    }
+    s_lp[c.lane] = log(CT(P, 0) / p);
+    s_ginv[c.lane] = 1. / g;
+  }
+  __syncthreads();
+  const double ptop = CT(P, 0), pbot = CT(P, nk), lp = s_lp[c.lane];
+  if (c.valid && ks - 1 < nk) {   // the pure-sigma interfaces
+    const double dz_inv = 1. / (M.zeta1 - M.zeta0);
+    for (int k = ks - 1 + c.warp; k < nk; k += CT_WARPS) CT(P, k) = pbot * exp((M.sgth[2 * k + 1] - M.zeta0) * dz_inv * lp);
+  }
+  __syncthreads();
+  if (!c.valid) return;
+  const double ginv = s_ginv[c.lane];
+  const dfl PB = cv<dfl>(pbot);
+  const dfl LP = log_df(cv<dfl>(ptop) / PB, M.exp2tab);
+  for (int k = c.warp; k <= nk; k += CT_WARPS) {
+    const double pk = CT(P, k);
+    if (k >= 1) {
+      const long long x = c.base + k * n2;
+      M.p3[x] = pk;
+      double hl = CT(HL, k);   // recomputed only next to a rescaled interface (k_set_p2etc_mixed)
+      if (k >= ks - 1) {
+        hl = (pk - CT(P, k - 1)) * (ginv * M.dsgth_inv[2 * k]);
+        CT(HL, k) = hl;
+      }
+      M.hdry[x] = dmaxr(M.h_min[k], hl);
+    }
+    if (update_theta && k < ks - 1) {
+      const double th = theta_acc(M, M.sgth[2 * k + 1], pk, PB, LP);
+      CT(TH, k) = th;
+      M.theta[c.base + k * n2] = th;
+    }
+  }
+  __syncthreads();
+  for (int k = 1 + c.warp; k <= nk; k += CT_WARPS) {
+    const long long x = c.base + k * n2;
+    const double top = CT(P, k - 1), bot = CT(P, k);
+    const double p2 = layer_p_acc(M, top, bot);
+    M.p2[x] = p2;
+    if (k == 1) M.p2[c.base] = top * top / p2;
+    double h;
+    if (k == nk) h = CT(HL, nk);
+    else {
+      const float topwt = d2f(M.dsgth[2 * k]), botwt = d2f(M.dsgth[2 * k + 2]);
+      h = f2d((topwt * d2f(CT(HL, k)) + botwt * d2f(CT(HL, k + 1))) / (topwt + botwt));
+    }
+    M.h3[x] = h;
+    if (k == 1) M.h3[c.base] = h;
+    if (!update_theta) continue;
+    double t2;
+    if (k < ks - 1) {
+      t2 = theta_acc(M, M.sgth[2 * k], p2, PB, LP);
+    } else if (k == ks - 1) {
+      t2 = .5 * (CT(TH, ks - 1) + CT(TH, ks - 2));
+    } else {
+      const int nkay = nk - (ks - 1) + 1;
+      const double sg = M.sgth[2 * k];
+      auto X = [&](int kay) { return M.sgth[2 * (nk - kay) + 1]; };
+      auto Y = [&](int kay) { return CT(TH, nk - kay); };
+      int kay;
+      if (fcmp(sg, X(0)) <= 0) kay = 0;
+      else if (fcmp(sg, X(nkay - 1)) >= 0) kay = nkay - 2;
+      else {
+        int il = -1, iu = nkay;
+        while (iu - il > 1) {
+          const int im = (iu + il) >> 1;
+          if (fcmp(sg, X(im)) >= 0) il = im; else iu = im;
+        }
+        kay = il;
+      }
+      t2 = Y(kay) + (Y(kay + 1) - Y(kay)) * (sg - X(kay)) / (X(kay + 1) - X(kay));
+    }
+    M.theta2[x] = t2;
+  }
+}
+
+__global__ void __launch_bounds__(CT_THREADS, 2) k_pgrad_vars_column_acc(DevModel M) {
+  epic_member(M);
+  extern __shared__ double sm[];
+  __shared__ double s_rho2_1[32];
+  const ColTile c = col_tile(M);
+  const int nk = M.nk, L = nk + 1;
+  const long long n2 = M.n2;
+  double *P = sm, *R = P + 32 * L, *T3 = R + 32 * L, *GZ = T3 + 32 * L;
+  float2 *LG = reinterpret_cast<float2 *>(GZ + 32 * L);   // log of successive pressure ratios, double-float
+  const float2 *tab = M.exp2tab;
+  const dfl kap = cv<dfl>(M.kappa), p0_inv = cv<dfl>(1. / M.press0);
+  const dfl mu_over_r = cv<dfl>(M.mu_dry / 8.314472e+3);   // return_density: p mu / (R T)
+  const float cpf = d2f(M.cp);
+  auto level = [&](int k, double theta, double p, double pr, double th2) {
+    const long long x = c.base + k * n2;
+    const dfl Pk = cv<dfl>(p);
+    const dfl pi = exp_df(kap * log_df(Pk * p0_inv, tab), tab);   // (p/p0)^kappa
+    const dfl t3 = cv<dfl>(theta) * pi;
+    const double t3d = to_d(t3);
+    M.t3[x] = t3d;
+    M.exner3[x] = f2d(cpf * pi.hi);
+    const double rho = to_d(Pk * mu_over_r / t3);
+    M.rho3[x] = rho;
+    CT(P, k) = p;
+    CT(R, k) = rho;
+    CT(T3, k) = t3d;
+    if (k >= 1) {
+      const dfl Pr = cv<dfl>(pr);
+      const dfl t2 = cv<dfl>(th2) * exp_df(kap * log_df(Pr * p0_inv, tab), tab);
+      M.t2[x] = to_d(t2);
+      const double r2 = to_d(Pr * mu_over_r / t2);
+      M.rho2[x] = r2;
+      if (k == 1) s_rho2_1[c.lane] = r2;
+    }
+  };
+  if (c.valid) {
+    double v[TILE_SLOTS][4];
+#pragma unroll
+    for (int r = 0; r < TILE_SLOTS; r++) {
+      const long long x = c.base + min(c.warp + r * CT_WARPS, nk) * n2;
+      v[r][0] = __ldg(M.theta + x); v[r][1] = __ldg(M.p3 + x); v[r][2] = __ldg(M.p2 + x); v[r][3] = __ldg(M.theta2 + x);
+    }
+#pragma unroll
+    for (int r = 0; r < TILE_SLOTS; r++)
+      if (c.warp + r * CT_WARPS <= nk) level(c.warp + r * CT_WARPS, v[r][0], v[r][1], v[r][2], v[r][3]);
+    for (int k = c.warp + TILE_SLOTS * CT_WARPS; k <= nk; k += CT_WARPS) {
+      const long long x = c.base + k * n2;
+      level(k, M.theta[x], M.p3[x], M.p2[x], M.theta2[x]);
+    }
+  }
+  __syncthreads();
+  if (c.valid) {
+    for (int k = c.warp; k < nk; k += CT_WARPS) {
+      const dfl lg = log_df(cv<dfl>(CT(P, k + 1)) / cv<dfl>(CT(P, k)), tab);
+      CT(LG, k) = make_float2(lg.hi, lg.lo);
+    }
+    if (c.warp == CT_WARPS - 1) {
+      M.rho2[c.base] = CT(R, 0) * CT(R, 0) / s_rho2_1[c.lane];
+      M.theta2[c.base] = M.sgth[0];
+      M.t2[c.base] = CT(T3, 0);
+    }
+  }
+  __syncthreads();
+  auto lgd = [&](int k) { const float2 v = CT(LG, k); return dfl(v.x, v.y); };
+  if (c.valid)
+    for (int k = 2 + c.warp; k <= nk - 1; k += CT_WARPS) {   // Leslie-Purser increments
+      const dfl dz10 = lgd(k), dz21 = lgd(k - 1), dz32 = lgd(k - 2);
+      const dfl dz20 = dz21 + dz10, dz30 = dz32 + dz20, dz31 = dz32 + dz21;
+      const dfl r_over_mu = one_df() / mu_over_r;   // p/rho = R T / mu
+      const dfl df0 = r_over_mu * cv<dfl>(CT(T3, k + 1)), df1 = r_over_mu * cv<dfl>(CT(T3, k));
+      const dfl df2 = r_over_mu * cv<dfl>(CT(T3, k - 1)), df3 = r_over_mu * cv<dfl>(CT(T3, k - 2));
+      const dfl two(2.), six(6.);
+      const dfl s = df0 * (dz21 * dz21 * dz21 * (dz31 + dz32)) / (dz10 * dz20 * dz30) +
+                    df1 * (dz21 * (dz21 * (dz21 + two * (dz10 - dz31)) - six * dz10 * dz31)) / (dz10 * dz31) +
+                    df2 * (dz21 * (dz21 * (dz21 + two * (dz32 - dz20)) - six * dz20 * dz32)) / (dz20 * dz32) +
+                    df3 * (dz21 * dz21 * dz21 * (dz10 + dz20)) / (dz30 * dz31 * dz32);
+      CT(GZ, k - 1) = -to_d(s / dfl(12.));
+    }
+  __syncthreads();
+  if (c.warp == 0 && c.valid) {   // GZ3 from the surface up, in FP64
+    double gz = M.topo_scale * M.gz_surface[M.at2(c.j, c.i)];
+    CT(GZ, nk) = gz;
+    gz = gz + ((CT(P, nk) + CT(P, nk - 1)) / (CT(R, nk) + CT(R, nk - 1))) * to_d(lgd(nk - 1));
+    CT(GZ, nk - 1) = gz;
+    for (int k = nk - 1; k >= 2; k--) {
+      gz = gz + CT(GZ, k - 1);
+      CT(GZ, k - 1) = gz;
+    }
+    CT(GZ, 0) = gz + ((CT(P, 1) + CT(P, 0)) / (CT(R, 1) + CT(R, 0))) * to_d(lgd(0));
+  }
+  __syncthreads();
+  if (!c.valid) return;
+  const bool interior = c.i >= 1 && c.i <= M.ni;
+  const long long itime = M.ctl->itime;
+  // MONT3 and DZDT3: diagnostics no later kernel of the step reads (k_pgrad_vars_column_mixed)
+  const float dtg_inv = -1.f / (d2f(M.dt) * d2f(M.grav[2 * c.j + 1]));
+  const float cprf = d2f(M.cpr), rgasf = d2f(M.rgas);
+  for (int k = c.warp; k <= nk; k += CT_WARPS) {
+    const long long x = c.base + k * n2;
+    const double gzk = CT(GZ, k);
+    const double old = M.gz3[x];
+    M.gz3[x] = gzk;
+    M.mont3[x] = f2d(d2f(gzk) + cprf * d2f(CT(T3, k)) * rgasf);
+    if (interior && k >= 1) {
+      float dz = 0.f;
+      if (itime > 1) dz = d2f(old - gzk) * dtg_inv;
+      dz += d2f(M.w3[x]) * d2f(M.h3[x]) / d2f(CT(R, k));
+      M.dzdt3[x] = f2d(dz);
+      if (gzk >= CT(GZ, k - 1)) flag_error(M.ctl, ERR_GZ_MONOTONE, k, c.j, c.i, gzk);
+    }
+  }
+}
+
+int column_acc_kernels_init() {
+  const int big = (int)(5 * 32 * (EPIC_MAX_NK + 1) * sizeof(double));
+  if (cudaFuncSetAttribute(k_set_p2etc_acc, cudaFuncAttributeMaxDynamicSharedMemorySize, big) != cudaSuccess ||
+      cudaFuncSetAttribute(k_pgrad_vars_column_acc, cudaFuncAttributeMaxDynamicSharedMemorySize, big) != cudaSuccess)
+    return -1;
+  return 0;
+}
+
+}  // namespace epic

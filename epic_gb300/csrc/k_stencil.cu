@@ -183,23 +183,30 @@ __global__ void k_pgrad_split(DevModel M) {
   reinterpret_cast<float2 *>(M.work1)[t] = make_float2(zh, d2f(z - f2d(zh)));
   reinterpret_cast<float2 *>(M.work2)[t] = make_float2(ph, d2f(p - f2d(ph)));
 }
+// Double-float (dfl, the accurate mixed form) takes the same splits and forms the differences in
+// double-float: the stencil's values then carry ~48 bits, and the face integrals' cancellation
+// costs no accuracy that matters.
 template <class R>
 struct PgradRef {
   const DevModel &M;
   float2 zr, pr;
   __device__ __forceinline__ PgradRef(const DevModel &M_, int k, int j, int i) : M(M_) {
-    if constexpr (sizeof(R) == sizeof(float)) {
+    if constexpr (!std::is_same_v<R, double>) {
       zr = reinterpret_cast<const float2 *>(M.work1)[M.at(k, j, i)];
       pr = reinterpret_cast<const float2 *>(M.work2)[M.at(k, j, i)];
     }
   }
+  static __device__ __forceinline__ R diff(float2 v, float2 r) {
+    if constexpr (std::is_same_v<R, float>) return (v.x - r.x) + (v.y - r.y);
+    else return dfl(v.x, v.y) - dfl(r.x, r.y);
+  }
   __device__ __forceinline__ R z(long long x) const {
-    if constexpr (sizeof(R) == sizeof(double)) return M.gz3[x];
-    else { const float2 v = reinterpret_cast<const float2 *>(M.work1)[x]; return (v.x - zr.x) + (v.y - zr.y); }
+    if constexpr (std::is_same_v<R, double>) return M.gz3[x];
+    else return diff(reinterpret_cast<const float2 *>(M.work1)[x], zr);
   }
   __device__ __forceinline__ R p(long long x) const {
-    if constexpr (sizeof(R) == sizeof(double)) return M.p2[x];
-    else { const float2 v = reinterpret_cast<const float2 *>(M.work2)[x]; return (v.x - pr.x) + (v.y - pr.y); }
+    if constexpr (std::is_same_v<R, double>) return M.p2[x];
+    else return diff(reinterpret_cast<const float2 *>(M.work2)[x], pr);
   }
 };
 // Width of a u (v) control volume in longitude (latitude), radians, between the faces at
@@ -208,8 +215,8 @@ struct PgradRef {
 // of up to 2 pi would lose five digits to cancellation).
 template <class R>
 __device__ __forceinline__ R face_width(const double *deg, int iw, int ie) {
-  if constexpr (sizeof(R) == sizeof(double)) return deg[ie] * (M_PI / 180.) - deg[iw] * (M_PI / 180.);
-  else return d2f((deg[ie] - deg[iw]) * (M_PI / 180.));
+  if constexpr (std::is_same_v<R, double>) return deg[ie] * (M_PI / 180.) - deg[iw] * (M_PI / 180.);
+  else return cv<R>((deg[ie] - deg[iw]) * (M_PI / 180.));
 }
 
 template <class R>
@@ -945,10 +952,21 @@ int launch_uv_core(const DevModel &M, cudaStream_t s) {
 
 int launch_uv_pgrad(const DevModel &M, cudaStream_t s) {
   k_gz_pole_rows<<<zg(M.nk + 1, M), 128, 0, s>>>(M);
-  const int f32 = M.mixed && !M.col64;
-  if (f32) k_pgrad_split<<<zg(epic_blocks(M.n3, TB(M, TB_POINT)), M), TB(M, TB_POINT), 0, s>>>(M);
-  EPIC_LAUNCH_R(f32, k_pgrad_lon, cells_blocks(M, M.nk - 1, M.nj + 1, TB(M, TB_PGRAD)), TB(M, TB_PGRAD), 0, s, M);
-  EPIC_LAUNCH_R(f32, k_pgrad_lat, cells_blocks(M, M.nk - 1, M.nj, TB(M, TB_PGRAD)), TB(M, TB_PGRAD), 0, s, M);
+  // FP64 form: binary64; mixed: double-float on the splits; fast mixed: binary32 on the splits
+  const dim3 glon = zg(cells_blocks(M, M.nk - 1, M.nj + 1, TB(M, TB_PGRAD)), M), glat = zg(cells_blocks(M, M.nk - 1, M.nj, TB(M, TB_PGRAD)), M);
+  if (!M.mixed) {
+    k_pgrad_lon<double><<<glon, TB(M, TB_PGRAD), 0, s>>>(M);
+    k_pgrad_lat<double><<<glat, TB(M, TB_PGRAD), 0, s>>>(M);
+    return 0;
+  }
+  k_pgrad_split<<<zg(epic_blocks(M.n3, TB(M, TB_POINT)), M), TB(M, TB_POINT), 0, s>>>(M);
+  if (M.col64) {
+    k_pgrad_lon<dfl><<<glon, TB(M, TB_PGRAD), 0, s>>>(M);
+    k_pgrad_lat<dfl><<<glat, TB(M, TB_PGRAD), 0, s>>>(M);
+  } else {
+    k_pgrad_lon<float><<<glon, TB(M, TB_PGRAD), 0, s>>>(M);
+    k_pgrad_lat<float><<<glat, TB(M, TB_PGRAD), 0, s>>>(M);
+  }
   return 0;
 }
 

@@ -45,6 +45,12 @@ int filter_kernels_init(int ni);
 bool filter_gemm_usable(const DevModel &M);
 int launch_filter_planes_gemm(const DevModel &M, const double *src, int src_sel, double *dst, int k0, int nplanes, int vgrid, cudaStream_t s);
 int filter_gemm_init(int ni);
+
+// k_column_acc.cu -- set_p2etc and store_pgrad_vars (column part) of the mixed form, with the
+// quantities feeding the pressure gradient in double-float.
+__global__ void k_set_p2etc_acc(DevModel M, int update_theta);
+__global__ void k_pgrad_vars_column_acc(DevModel M);
+int column_acc_kernels_init();
 void fill_filter_kernels(int ni, int nj, const double *hl_h, const double *hl_pv, long long iadim, float *fh, float *fv);
 size_t twiddle_doubles(int ni);
 void fill_twiddles(int ni, double *tw);
