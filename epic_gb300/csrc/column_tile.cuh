@@ -50,6 +50,9 @@ __device__ __forceinline__ R f_and_g_sigma_r(const DevModel &M, R s, R &g) {
   return R(0.);
 }
 
+// log(b/a) for b/a near 1, from the FP64 difference
+__device__ __forceinline__ float log_ratio_f(double a, double b) { return log1pf(d2f(b - a) / d2f(a)); }
+
 // return_sigmatheta (epic_funcs_diag.c:1238-1250) with log(ptop/pbot) supplied
 template <class R>
 __device__ __forceinline__ R sigmatheta_lp(const DevModel &M, R theta, R p, R pbot, R ptop, R lp) {

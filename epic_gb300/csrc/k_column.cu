@@ -510,8 +510,6 @@ __global__ void __launch_bounds__(CT_THREADS) k_pgrad_vars_column(DevModel M) {
 // evaluated in FP32 from FP64 differences (log1p/expm1 of small ratios), which keeps their
 // relative error near 1e-7.
 
-// log(b/a) for b/a near 1, from the FP64 difference
-__device__ __forceinline__ float log_ratio_f(double a, double b) { return log1pf(d2f(b - a) / d2f(a)); }
 
 // onto_kk(P2_INDEX) at a layer: ((bot^(k+1) - top^(k+1)) / ((k+1)(bot - top)))^(1/k), written as
 // bot * q^(1/kappa), q = (1 - r^(kappa+1)) / ((kappa+1)(1 - r)), r = top/bot.  The FP32

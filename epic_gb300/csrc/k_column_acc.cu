@@ -1,11 +1,12 @@
 // The vertical pressure and geopotential integration of the mixed form (EPIC_PREC_MIXED):
 // set_p2etc and the column part of store_pgrad_vars, with the quantities that feed the pressure
-// gradient -- the layer pressure P2, the diagnosed THETA and THETA2, T3, RHO3 and the
+// gradient -- the layer pressure P2, the diagnosed THETA, T3, RHO3 and the
 // geopotential increments -- evaluated in double-float (df.cuh: ~1e-13 relative, on the FP32
 // pipe) instead of binary32, and the running sums in binary64.  Rounding these to binary32 every
 // step is what makes the meridional wind of the all-FP32 form (EPIC_PREC_MIXED_FAST) drift from
-// FP64 by 6e-4 in a day; with them in double-float the mixed form stays within 1e-4.  Diagnostics
-// that nothing in the step reads back (EXNER3's use in the heating, H3, MONT3, DZDT3) stay FP32.
+// FP64 by 6e-4 in a day; with them in double-float the mixed form stays within 1e-4.  Quantities
+// that only diagnostics read (THETA2, T2 and RHO2 feed the Richardson number alone; H3, EXNER3,
+// MONT3, DZDT3) stay FP32, as in the fast form.
 //
 // Structure, phases and the restated reference lines are those of k_set_p2etc_mixed and
 // k_pgrad_vars_column_mixed (k_column.cu): set_p2etc, epic_funcs_diag.c:3352-3569;
@@ -92,6 +93,7 @@ __global__ void __launch_bounds__(CT_THREADS, 2) k_set_p2etc_acc(DevModel M, int
   __syncthreads();
   if (!c.valid) return;
   const double ginv = s_ginv[c.lane];
+  const float lpf = d2f(lp);
   const dfl PB = cv<dfl>(pbot);
   const dfl LP = log_df(cv<dfl>(ptop) / PB, M.exp2tab);
   for (int k = c.warp; k <= nk; k += CT_WARPS) {
@@ -130,7 +132,10 @@ __global__ void __launch_bounds__(CT_THREADS, 2) k_set_p2etc_acc(DevModel M, int
     if (!update_theta) continue;
     double t2;
     if (k < ks - 1) {
-      t2 = theta_acc(M, M.sgth[2 * k], p2, PB, LP);
+      const float sigma = log_ratio_f(pbot, p2) / lpf;
+      float gs;
+      const float fs = f_and_g_sigma_r<float>(M, sigma, gs);
+      t2 = f2d((d2f(M.sgth[2 * k]) - fs) / gs);
     } else if (k == ks - 1) {
       t2 = .5 * (CT(TH, ks - 1) + CT(TH, ks - 2));
     } else {
@@ -162,8 +167,9 @@ __global__ void __launch_bounds__(CT_THREADS, 2) k_pgrad_vars_column_acc(DevMode
   const ColTile c = col_tile(M);
   const int nk = M.nk, L = nk + 1;
   const long long n2 = M.n2;
-  double *P = sm, *R = P + 32 * L, *T3 = R + 32 * L, *GZ = T3 + 32 * L;
-  float2 *LG = reinterpret_cast<float2 *>(GZ + 32 * L);   // log of successive pressure ratios, double-float
+  double *P = sm, *R = P + 32 * L, *GZ = R + 32 * L;
+  float2 *T3 = reinterpret_cast<float2 *>(GZ + 32 * L);   // T3, double-float
+  float2 *LG = T3 + 32 * L;                               // log of successive pressure ratios, double-float
   const float2 *tab = M.exp2tab;
   const dfl kap = cv<dfl>(M.kappa), p0_inv = cv<dfl>(1. / M.press0);
   const dfl mu_over_r = cv<dfl>(M.mu_dry / 8.314472e+3);   // return_density: p mu / (R T)
@@ -180,12 +186,11 @@ __global__ void __launch_bounds__(CT_THREADS, 2) k_pgrad_vars_column_acc(DevMode
     M.rho3[x] = rho;
     CT(P, k) = p;
     CT(R, k) = rho;
-    CT(T3, k) = t3d;
-    if (k >= 1) {
-      const dfl Pr = cv<dfl>(pr);
-      const dfl t2 = cv<dfl>(th2) * exp_df(kap * log_df(Pr * p0_inv, tab), tab);
-      M.t2[x] = to_d(t2);
-      const double r2 = to_d(Pr * mu_over_r / t2);
+    CT(T3, k) = make_float2(t3.hi, t3.lo);
+    if (k >= 1) {   // the layer's T2, RHO2: read by the Richardson number only
+      const float t2f = d2f(th2) * powf(d2f(pr) * p0_inv.hi, kap.hi);
+      M.t2[x] = f2d(t2f);
+      const double r2 = f2d(d2f(pr) * mu_over_r.hi / t2f);
       M.rho2[x] = r2;
       if (k == 1) s_rho2_1[c.lane] = r2;
     }
@@ -214,18 +219,19 @@ __global__ void __launch_bounds__(CT_THREADS, 2) k_pgrad_vars_column_acc(DevMode
     if (c.warp == CT_WARPS - 1) {
       M.rho2[c.base] = CT(R, 0) * CT(R, 0) / s_rho2_1[c.lane];
       M.theta2[c.base] = M.sgth[0];
-      M.t2[c.base] = CT(T3, 0);
+      M.t2[c.base] = f2d(CT(T3, 0).x) + f2d(CT(T3, 0).y);
     }
   }
   __syncthreads();
   auto lgd = [&](int k) { const float2 v = CT(LG, k); return dfl(v.x, v.y); };
+  auto t3df = [&](int k) { const float2 v = CT(T3, k); return dfl(v.x, v.y); };
+  const dfl r_over_mu = one_df() / mu_over_r;   // p/rho = R T / mu
   if (c.valid)
     for (int k = 2 + c.warp; k <= nk - 1; k += CT_WARPS) {   // Leslie-Purser increments
       const dfl dz10 = lgd(k), dz21 = lgd(k - 1), dz32 = lgd(k - 2);
       const dfl dz20 = dz21 + dz10, dz30 = dz32 + dz20, dz31 = dz32 + dz21;
-      const dfl r_over_mu = one_df() / mu_over_r;   // p/rho = R T / mu
-      const dfl df0 = r_over_mu * cv<dfl>(CT(T3, k + 1)), df1 = r_over_mu * cv<dfl>(CT(T3, k));
-      const dfl df2 = r_over_mu * cv<dfl>(CT(T3, k - 1)), df3 = r_over_mu * cv<dfl>(CT(T3, k - 2));
+      const dfl df0 = r_over_mu * t3df(k + 1), df1 = r_over_mu * t3df(k);
+      const dfl df2 = r_over_mu * t3df(k - 1), df3 = r_over_mu * t3df(k - 2);
       const dfl two(2.), six(6.);
       const dfl s = df0 * (dz21 * dz21 * dz21 * (dz31 + dz32)) / (dz10 * dz20 * dz30) +
                     df1 * (dz21 * (dz21 * (dz21 + two * (dz10 - dz31)) - six * dz10 * dz31)) / (dz10 * dz31) +
@@ -257,7 +263,7 @@ __global__ void __launch_bounds__(CT_THREADS, 2) k_pgrad_vars_column_acc(DevMode
     const double gzk = CT(GZ, k);
     const double old = M.gz3[x];
     M.gz3[x] = gzk;
-    M.mont3[x] = f2d(d2f(gzk) + cprf * d2f(CT(T3, k)) * rgasf);
+    M.mont3[x] = f2d(d2f(gzk) + cprf * CT(T3, k).x * rgasf);
     if (interior && k >= 1) {
       float dz = 0.f;
       if (itime > 1) dz = d2f(old - gzk) * dtg_inv;
