@@ -258,19 +258,31 @@ __global__ void __launch_bounds__(CT_THREADS, 2) k_pgrad_vars_column_acc(DevMode
   // MONT3 and DZDT3: diagnostics no later kernel of the step reads (k_pgrad_vars_column_mixed)
   const float dtg_inv = -1.f / (d2f(M.dt) * d2f(M.grav[2 * c.j + 1]));
   const float cprf = d2f(M.cpr), rgasf = d2f(M.rgas);
-  for (int k = c.warp; k <= nk; k += CT_WARPS) {
+  auto level_out = [&](int k, double old, double w, double h) {
     const long long x = c.base + k * n2;
     const double gzk = CT(GZ, k);
-    const double old = M.gz3[x];
     M.gz3[x] = gzk;
     M.mont3[x] = f2d(d2f(gzk) + cprf * CT(T3, k).x * rgasf);
     if (interior && k >= 1) {
       float dz = 0.f;
       if (itime > 1) dz = d2f(old - gzk) * dtg_inv;
-      dz += d2f(M.w3[x]) * d2f(M.h3[x]) / d2f(CT(R, k));
+      dz += d2f(w) * d2f(h) / d2f(CT(R, k));
       M.dzdt3[x] = f2d(dz);
       if (gzk >= CT(GZ, k - 1)) flag_error(M.ctl, ERR_GZ_MONOTONE, k, c.j, c.i, gzk);
     }
+  };
+  double v[TILE_SLOTS][3];   // the loads of this warp's first levels issued together
+#pragma unroll
+  for (int r = 0; r < TILE_SLOTS; r++) {
+    const long long x = c.base + min(c.warp + r * CT_WARPS, nk) * n2;
+    v[r][0] = M.gz3[x]; v[r][1] = __ldg(M.w3 + x); v[r][2] = __ldg(M.h3 + x);
+  }
+#pragma unroll
+  for (int r = 0; r < TILE_SLOTS; r++)
+    if (c.warp + r * CT_WARPS <= nk) level_out(c.warp + r * CT_WARPS, v[r][0], v[r][1], v[r][2]);
+  for (int k = c.warp + TILE_SLOTS * CT_WARPS; k <= nk; k += CT_WARPS) {
+    const long long x = c.base + k * n2;
+    level_out(k, M.gz3[x], M.w3[x], M.h3[x]);
   }
 }
 
