@@ -436,7 +436,7 @@ def run_gpu_ensemble(args):
     clocks = clk.summary()
     launches = batch.kernels_per_step * args.steps
 
-    roof = batch_roofline(batch, cfg, nmem, stream, torch, stage=7)
+    roof = batch_roofline(batch, cfg, nmem, stream, torch, stage=19)
     roof_pgrad = batch_roofline(batch, cfg, nmem, stream, torch, stage=12)
 
     # end to end: every member's state uploaded from pinned host memory and downloaded, each step
@@ -505,7 +505,7 @@ def run_gpu_ensemble(args):
 
 # Stages timed for the roofline: (stage, kernels, algorithmic 8-byte field passes per cell, note)
 ROOF_STAGES = {
-    7: ("store_pgrad_vars (the column tile of the form + k_pgrad_dzdt) over all members", 20,
+    19: ("store_pgrad_vars before the pressure gradient (the column tile of the form + k_pgrad_dzdt) over all members", 20,
         "THETA, P3, P2, THETA2, GZ3, W3, H3 read and T3, EXNER3, RHO3, T2, RHO2, GZ3, MONT3, DZDT3 written by the "
         "column tile; U, V, GZ3, DZDT3 read and DZDT3 written by the horizontal part; bound by load latency and "
         "the FP64 hydrostatic sum, not by HBM"),
@@ -515,12 +515,11 @@ ROOF_STAGES = {
 }
 
 
-def batch_roofline(batch, cfg, nmem, stream, torch, stage=7):
+def batch_roofline(batch, cfg, nmem, stream, torch, stage=19):
     """One stage of the step over all members, timed with CUDA events on the batch stream after
     a warm-up call.  Algorithmic bytes per launch: the stage's field passes (ROOF_STAGES) of
-    8-byte values over ni*(nj+1)*nk cells per member.  Stage 7 (store_pgrad_vars) holds the
-    largest kernel of the mixed step (k_pgrad_vars_column_acc, run twice per step, with
-    k_pgrad_dzdt 18% of the step's launch list)."""
+    8-byte values over ni*(nj+1)*nk cells per member.  Stage 19 (store_pgrad_vars feeding the
+    pressure gradient) holds the largest kernel of the mixed step, k_pgrad_vars_column_acc."""
     peaks = _peaks()
     label, passes, note = ROOF_STAGES[stage]
     n = 5

@@ -165,9 +165,9 @@ int run_stage_on(const DevModel &M, cudaStream_t s, int stage) {
       launch_hsu_meridional(M, M.hdry, 2, s);
       launch_hsu_zonal(M, M.hdry, 1, 1, s);
       launch_restore_mass(M, s);
-      launch_set_p2etc(M, 0, s);
+      launch_set_p2etc(M, 0, s, false);   // its P2 is recomputed (stage 11) before the pressure gradient
       break;
-    case 7: launch_store_pgrad_vars(M, s); break;
+    case 7: launch_store_pgrad_vars(M, s, false); break;   // GZ3 for the filtered copy (stage 8)
     case 8:
       launch_copy_gz(M, s);
       launch_filter_planes(M, M.gz, PL_NONE, M.gz, 0, M.nk, 0, s);
@@ -195,6 +195,7 @@ int run_stage_on(const DevModel &M, cudaStream_t s, int stage) {
     case 16: launch_store_diag(M, s); break;
     case 17: launch_calc_heating(M, s); break;
     case 18: launch_set_p2etc(M, 0, s); break;
+    case 19: launch_store_pgrad_vars(M, s, true); break;   // after stage 11: what the pressure gradient reads
     default: return set_error(EPIC_ERR_ARG, "unknown stage %d", stage);
   }
   return check_launch("stage launch");
@@ -203,7 +204,7 @@ int run_stage_on(const DevModel &M, cudaStream_t s, int stage) {
 int run_stage(epic_model *m, int stage) { return run_stage_on(m->d, m->stream, stage); }
 
 int enqueue_step_on(const DevModel &M, cudaStream_t s) {
-  static const int step[] = {0, 1, 2, 3, 4, 5, 6, 7, 8, 9, 10, 11, 7, 12, 13, 14, 15, 16, 17};
+  static const int step[] = {0, 1, 2, 3, 4, 5, 6, 7, 8, 9, 10, 11, 19, 12, 13, 14, 15, 16, 17};
   for (int st : step) {
     int rc = run_stage_on(M, s, st);
     if (rc) return rc;
@@ -212,7 +213,7 @@ int enqueue_step_on(const DevModel &M, cudaStream_t s) {
 }
 
 int enqueue_sync_on(const DevModel &M, cudaStream_t s) {
-  static const int sync[] = {11, 7, 16, 17, 2};
+  static const int sync[] = {11, 19, 16, 17, 2};
   for (int st : sync) {
     int rc = run_stage_on(M, s, st);
     if (rc) return rc;

@@ -61,8 +61,11 @@ int launch_calc_w(const DevModel &M, cudaStream_t s);
 int launch_uv_drag(const DevModel &M, cudaStream_t s);
 int launch_hsu_vertical(const DevModel &M, double *buff, int kind, cudaStream_t s);
 int launch_restore_mass(const DevModel &M, cudaStream_t s);
-int launch_set_p2etc(const DevModel &M, int update_theta, cudaStream_t s);
-int launch_store_pgrad_vars(const DevModel &M, cudaStream_t s);
+// feeds_pgrad: the call whose P2, THETA, GZ3 and RHO3 the pressure gradient reads (the mixed
+// form takes its double-float kernels there; elsewhere the FP32 ones, whose outputs are
+// recomputed before the pressure gradient reads them)
+int launch_set_p2etc(const DevModel &M, int update_theta, cudaStream_t s, bool feeds_pgrad = true);
+int launch_store_pgrad_vars(const DevModel &M, cudaStream_t s, bool feeds_pgrad = true);
 int launch_gz_monotone(const DevModel &M, cudaStream_t s);
 int launch_calc_heating(const DevModel &M, cudaStream_t s);
 int launch_advection_prep(const DevModel &M, int phase, cudaStream_t s);
