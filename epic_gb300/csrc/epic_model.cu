@@ -170,6 +170,8 @@ int run_stage_on(const DevModel &M, cudaStream_t s, int stage) {
     case 7: launch_store_pgrad_vars(M, s, false); break;   // GZ3 for the filtered copy (stage 8)
     case 8:
       launch_copy_gz(M, s);
+      // binary64 in every form: the 3-D filter's profiles interpolate in the filtered GZ, and in
+      // FP32 the mixed form's V error after a day grows from 4e-5 to 7e-5 (leapfrog: 1.7e-4 -> 1.6e-3)
       launch_filter_planes(M, M.gz, PL_NONE, M.gz, 0, M.nk, 0, s);
       launch_gz_monotone(M, s);
       break;

@@ -213,6 +213,8 @@ __global__ void k_varz_tables(DevModel M, const double *buff, int sel, int index
   const int lane = (int)(threadIdx.x & 31);
   const int j = jstart + (int)((blockIdx.x * blockDim.x + threadIdx.x) >> 5);
   if (j > M.nj) return;
+  // the mixed forms filter (and so tabulate) only the filtered rows
+  if (M.mixed && !row_is_filtered(M, j, index == 1)) return;
   const double *gz = M.gz;
   const int K = M.nk;
   int imin = 1 << 30;
@@ -313,6 +315,9 @@ __global__ void k_varz_filter_rows(DevModel M, double *buff, int sel, int index,
   const double *gz = M.gz;
   const long long base = M.at(k, j, 0);
   const bool filt = row_is_filtered(M, j, vgrid);
+  // The mixed forms leave unfiltered rows untouched (their subtract-and-add-back is the identity
+  // up to one rounding); the FP64 form repeats the reference's arithmetic on them.
+  if (!filt && !std::is_same_v<R, double>) return;
   if (filt) load_twiddles(M, fs);
   for (int i = threadIdx.x + 1; i <= M.ni; i += blockDim.x) {
     R gzz;
@@ -349,9 +354,6 @@ __global__ void k_varz_filter_rows(DevModel M, double *buff, int sel, int index,
   }
   __syncthreads();
   if (filt) filter_row_smem(M, x, vgrid ? M.high_lat_pv : M.high_lat_h, M.at2(j, 0), fs);
-  // The mixed form leaves unfiltered rows untouched (their subtract-and-add-back is the
-  // identity up to one rounding); the FP64 form repeats the reference's arithmetic on them.
-  if (!filt && sizeof(R) == sizeof(float)) return;
   for (int i = threadIdx.x + 1; i <= M.ni; i += blockDim.x) write_with_pads(buff, M, base, i, to_d(x[i]) + to_d(vz[i]));
 }
 

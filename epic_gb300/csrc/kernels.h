@@ -35,7 +35,8 @@ inline dim3 zg(dim3 g, const DevModel &M) {
   } while (0)
 
 // k_filter.cu -- zonal filter (epic_adjust.c) and the zonal pass of hsu_advection.
-// fp32: filter in FP32 (mixed form; the filtered GZ copy always stays FP64).
+// fp32: filter in FP32 (the mixed forms, except the filtered GZ copy; on the tensor cores for ni a
+// multiple of 128).
 int launch_filter_planes(const DevModel &M, const double *src, int src_sel, double *dst, int k0, int nplanes, int vgrid, cudaStream_t s,
                          int fp32 = 0);
 int launch_varz_filter(const DevModel &M, double *buff, int sel, int index, int kstart, int kend, cudaStream_t s);
