@@ -47,7 +47,7 @@ WORKLOADS = {
     "ens64": (128, 64, 20, 300),   # per member; 64 members
 }
 ENSEMBLE = {"ens64": 64}
-E2E_GROUPS = 4   # sub-batches of the end-to-end pipeline (copies of one overlap kernels of others)
+E2E_GROUPS = 8   # sub-batches of the end-to-end pipeline (copies of one overlap kernels of others)
 # Serving stream: shapes and the time step each runs stably with (dt from runs of the FP64
 # form that kept GZ3 monotonic for at least half a simulated day at that shape).
 SERVE_SHAPES = {(64, 32, 10): 300, (64, 32, 20): 300, (128, 64, 20): 300, (128, 64, 10): 150, (256, 128, 10): 120,
@@ -441,7 +441,7 @@ def run_gpu_ensemble(args):
 
     # end to end: every member's state uploaded from pinned host memory and downloaded, each step
     hosts = [m.download().copy(pinned=True) for m in members]
-    e2e_steps = max(1, min(args.steps, 3))
+    e2e_steps = max(1, min(args.steps, 6))
     batch.step_host(hosts, 1, groups=E2E_GROUPS)   # first call builds the sub-batch graphs
     barrier()
     t0 = time.perf_counter()

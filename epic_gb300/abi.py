@@ -146,20 +146,27 @@ def _pinned_zeros(shape):
 
 
 class Fields:
-    """Owns numpy storage for every EpicFields pointer, in the reference layout."""
+    """Owns numpy storage for every EpicFields pointer, in the reference layout.  The 3-D arrays
+    are views of one block, back to back in the library's order (u, v, dudt, dvdt, then
+    FIELD_NAMES_3D), so that the library moves a whole state with one copy."""
 
     def __init__(self, ni: int, nj: int, nk: int, uv_scheme: int, pinned: bool = False):
         self.layout = Layout(ni, nj, nk)
         self.uv_scheme = uv_scheme
         nvp, ntp = (1, 3) if uv_scheme == EPIC_UV_AB3 else (2, 1)
         s3 = self.layout.shape3
+        n3 = int(np.prod(s3))
         zeros = _pinned_zeros if pinned else np.zeros
-        self.arrays = {
-            "u": zeros((nvp,) + s3), "v": zeros((nvp,) + s3),
-            "dudt": zeros((ntp,) + s3), "dvdt": zeros((ntp,) + s3),
-        }
-        for n in FIELD_NAMES_3D:
-            self.arrays[n] = zeros(s3)
+        planes = [("u", nvp), ("v", nvp), ("dudt", ntp), ("dvdt", ntp)] + [(n, 0) for n in FIELD_NAMES_3D]
+        block = zeros((sum(max(q, 1) for _, q in planes) * n3,))
+        self.arrays = {}
+        off = 0
+        for name, q in planes:
+            cnt = max(q, 1) * n3
+            view = block[off:off + cnt]
+            self.arrays[name] = view.reshape(((q,) if q else ()) + s3)
+            off += cnt
+        self._block = block
         self.arrays["gz_surface"] = zeros(self.layout.shape2)
         self.struct = EpicFields()
         for k, a in self.arrays.items():

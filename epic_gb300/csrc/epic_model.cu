@@ -127,6 +127,14 @@ T *carve(char *&p, size_t count) {
   p += ((count * sizeof(T) + 255) / 256) * 256;
   return r;
 }
+// the state arrays are packed back to back (no padding), so that a caller whose host arrays are
+// laid out the same way moves a whole state with one copy (enqueue_upload / enqueue_download)
+template <typename T>
+T *carve_packed(char *&p, size_t count) {
+  T *r = reinterpret_cast<T *>(p);
+  p += count * sizeof(T);
+  return r;
+}
 
 int check_launch(const char *what) {
   cudaError_t e = cudaGetLastError();
@@ -369,11 +377,12 @@ extern "C" int epic_model_create(const epic_grid *g, int32_t precision, epic_mod
   char *p = m->pool;
   d.pool_base = m->pool;
   d.ctl = carve<Ctl>(p, 1);
-  d.u = carve<double>(p, d.nvp * n3); d.v = carve<double>(p, d.nvp * n3);
-  d.dudt = carve<double>(p, d.ntp * n3); d.dvdt = carve<double>(p, d.ntp * n3);
+  d.u = carve_packed<double>(p, d.nvp * n3); d.v = carve_packed<double>(p, d.nvp * n3);
+  d.dudt = carve_packed<double>(p, d.ntp * n3); d.dvdt = carve_packed<double>(p, d.ntp * n3);
   double **f3[] = {&d.hdry, &d.theta, &d.p3, &d.h3, &d.p2, &d.theta2, &d.t2, &d.t3, &d.rho2, &d.rho3, &d.exner3, &d.gz3, &d.mont3,
                    &d.heat3, &d.pv3, &d.ri2, &d.div_uv3, &d.w3, &d.dzdt3, &d.u_spinup};
-  for (double **q : f3) *q = carve<double>(p, n3);
+  for (double **q : f3) *q = carve_packed<double>(p, n3);
+  p += (256 - ((size_t)(p - m->pool) & 255)) & 255;   // the scratch and tables start 256-aligned
   double **s3[] = {&d.gz, &d.unity, &d.old, &d.work0, &d.work1, &d.work2, &d.work3};
   for (double **q : s3) *q = carve<double>(p, n3);
   d.gz_surface = carve<double>(p, n2);
@@ -481,22 +490,36 @@ namespace {
 
 // The copies of epic_model_upload, enqueued on stream s; *c receives the control block and must
 // stay valid until s has run them.
-int enqueue_upload(epic_model *m, const epic_fields *f, cudaStream_t s, Ctl *c) {
+// Whether the host's state arrays sit back to back in the device's order (u, v, dudt, dvdt, then
+// the 20 single fields), as the device's do: then a state moves with one copy.
+bool host_state_packed(const DevModel &d, const double *const *fld) {
+  const size_t n3 = (size_t)d.n3;
+  const double *base = fld[0];
+  size_t off = 0;
+  for (int i = 0; i < 24; i++) {
+    if (fld[i] != base + off) return false;
+    off += (i < 2 ? d.nvp : (i < 4 ? d.ntp : 1)) * n3;
+  }
+  return true;
+}
+
+int enqueue_upload(epic_model *m, const epic_fields *f, cudaStream_t s, Ctl *c, bool with_ctl = true) {
   if (!f->u || !f->v || !f->dudt || !f->dvdt || !f->hdry || !f->theta || !f->p3 || !f->gz_surface || !f->u_spinup)
     return set_error(EPIC_ERR_ARG, "epic_model_upload: a required field pointer is NULL");
   DevModel &d = m->d;
   const size_t b3 = (size_t)d.n3 * sizeof(double);
-  EPIC_CUDA_CHECK(cudaMemcpyAsync(d.u, f->u, d.nvp * b3, cudaMemcpyHostToDevice, s));
-  EPIC_CUDA_CHECK(cudaMemcpyAsync(d.v, f->v, d.nvp * b3, cudaMemcpyHostToDevice, s));
-  EPIC_CUDA_CHECK(cudaMemcpyAsync(d.dudt, f->dudt, d.ntp * b3, cudaMemcpyHostToDevice, s));
-  EPIC_CUDA_CHECK(cudaMemcpyAsync(d.dvdt, f->dvdt, d.ntp * b3, cudaMemcpyHostToDevice, s));
-  const double *src[] = {f->hdry, f->theta, f->p3, f->h3, f->p2, f->theta2, f->t2, f->t3, f->rho2, f->rho3, f->exner3, f->gz3,
-                         f->mont3, f->heat3, f->pv3, f->ri2, f->div_uv3, f->w3, f->dzdt3, f->u_spinup};
-  double *dst[] = {d.hdry, d.theta, d.p3, d.h3, d.p2, d.theta2, d.t2, d.t3, d.rho2, d.rho3, d.exner3, d.gz3,
-                   d.mont3, d.heat3, d.pv3, d.ri2, d.div_uv3, d.w3, d.dzdt3, d.u_spinup};
-  for (int i = 0; i < 20; i++)
-    if (src[i]) EPIC_CUDA_CHECK(cudaMemcpyAsync(dst[i], src[i], b3, cudaMemcpyHostToDevice, s));
+  const double *src[] = {f->u, f->v, f->dudt, f->dvdt, f->hdry, f->theta, f->p3, f->h3, f->p2, f->theta2, f->t2, f->t3, f->rho2,
+                         f->rho3, f->exner3, f->gz3, f->mont3, f->heat3, f->pv3, f->ri2, f->div_uv3, f->w3, f->dzdt3, f->u_spinup};
+  double *dst[] = {d.u, d.v, d.dudt, d.dvdt, d.hdry, d.theta, d.p3, d.h3, d.p2, d.theta2, d.t2, d.t3, d.rho2,
+                   d.rho3, d.exner3, d.gz3, d.mont3, d.heat3, d.pv3, d.ri2, d.div_uv3, d.w3, d.dzdt3, d.u_spinup};
+  if (host_state_packed(d, src)) {
+    EPIC_CUDA_CHECK(cudaMemcpyAsync(d.u, f->u, (size_t)(2 * d.nvp + 2 * d.ntp + 20) * b3, cudaMemcpyHostToDevice, s));
+  } else {
+    for (int i = 0; i < 24; i++)
+      if (src[i]) EPIC_CUDA_CHECK(cudaMemcpyAsync(dst[i], src[i], (i < 2 ? d.nvp : (i < 4 ? d.ntp : 1)) * b3, cudaMemcpyHostToDevice, s));
+  }
   EPIC_CUDA_CHECK(cudaMemcpyAsync(d.gz_surface, f->gz_surface, (size_t)d.n2 * sizeof(double), cudaMemcpyHostToDevice, s));
+  if (!with_ctl) return EPIC_OK;
   memset(c, 0, sizeof(*c));
   c->it_zero = f->it_zero; c->it_minus1 = f->it_minus1; c->it_minus2 = f->it_minus2;
   c->itime = f->itime; c->model_time = f->model_time;
@@ -517,16 +540,16 @@ int enqueue_upload(epic_model *m, const epic_fields *f, cudaStream_t s, Ctl *c) 
 int enqueue_download(epic_model *m, epic_fields *f, cudaStream_t s, Ctl *c) {
   DevModel &d = m->d;
   const size_t b3 = (size_t)d.n3 * sizeof(double);
-  if (f->u) EPIC_CUDA_CHECK(cudaMemcpyAsync(f->u, d.u, d.nvp * b3, cudaMemcpyDeviceToHost, s));
-  if (f->v) EPIC_CUDA_CHECK(cudaMemcpyAsync(f->v, d.v, d.nvp * b3, cudaMemcpyDeviceToHost, s));
-  if (f->dudt) EPIC_CUDA_CHECK(cudaMemcpyAsync(f->dudt, d.dudt, d.ntp * b3, cudaMemcpyDeviceToHost, s));
-  if (f->dvdt) EPIC_CUDA_CHECK(cudaMemcpyAsync(f->dvdt, d.dvdt, d.ntp * b3, cudaMemcpyDeviceToHost, s));
-  double *dst[] = {f->hdry, f->theta, f->p3, f->h3, f->p2, f->theta2, f->t2, f->t3, f->rho2, f->rho3, f->exner3, f->gz3,
-                   f->mont3, f->heat3, f->pv3, f->ri2, f->div_uv3, f->w3, f->dzdt3, f->u_spinup};
-  const double *src[] = {d.hdry, d.theta, d.p3, d.h3, d.p2, d.theta2, d.t2, d.t3, d.rho2, d.rho3, d.exner3, d.gz3,
-                         d.mont3, d.heat3, d.pv3, d.ri2, d.div_uv3, d.w3, d.dzdt3, d.u_spinup};
-  for (int i = 0; i < 20; i++)
-    if (dst[i]) EPIC_CUDA_CHECK(cudaMemcpyAsync(dst[i], src[i], b3, cudaMemcpyDeviceToHost, s));
+  double *dst[] = {f->u, f->v, f->dudt, f->dvdt, f->hdry, f->theta, f->p3, f->h3, f->p2, f->theta2, f->t2, f->t3, f->rho2,
+                   f->rho3, f->exner3, f->gz3, f->mont3, f->heat3, f->pv3, f->ri2, f->div_uv3, f->w3, f->dzdt3, f->u_spinup};
+  const double *src[] = {d.u, d.v, d.dudt, d.dvdt, d.hdry, d.theta, d.p3, d.h3, d.p2, d.theta2, d.t2, d.t3, d.rho2,
+                         d.rho3, d.exner3, d.gz3, d.mont3, d.heat3, d.pv3, d.ri2, d.div_uv3, d.w3, d.dzdt3, d.u_spinup};
+  if (host_state_packed(d, dst)) {
+    EPIC_CUDA_CHECK(cudaMemcpyAsync(f->u, d.u, (size_t)(2 * d.nvp + 2 * d.ntp + 20) * b3, cudaMemcpyDeviceToHost, s));
+  } else {
+    for (int i = 0; i < 24; i++)
+      if (dst[i]) EPIC_CUDA_CHECK(cudaMemcpyAsync(dst[i], src[i], (i < 2 ? d.nvp : (i < 4 ? d.ntp : 1)) * b3, cudaMemcpyDeviceToHost, s));
+  }
   if (f->gz_surface) EPIC_CUDA_CHECK(cudaMemcpyAsync(f->gz_surface, d.gz_surface, (size_t)d.n2 * sizeof(double), cudaMemcpyDeviceToHost, s));
   EPIC_CUDA_CHECK(cudaMemcpyAsync(c, d.ctl, sizeof(Ctl), cudaMemcpyDeviceToHost, s));
   return EPIC_OK;
@@ -700,6 +723,7 @@ struct epic_batch {
   int kernels_per_step = -1;
   std::vector<epic_batch *> groups;  // sub-batches of epic_batch_step_host's pipeline
   Ctl *host_ctl = nullptr;           // pinned control blocks for the pipeline's copies
+  size_t host_ctl_count = 0;
 };
 
 namespace {
@@ -1045,14 +1069,26 @@ extern "C" int epic_batch_step_host(epic_batch *b, epic_fields *const *f, int32_
       b->groups.push_back(g);
     }
   }
-  if (!b->host_ctl) EPIC_CUDA_CHECK(cudaMallocHost(&b->host_ctl, sizeof(Ctl) * 2 * (size_t)n));
+  // one upload and one download control block per member and step: the steps are not drained
+  // one by one, each group's next upload follows its last download in stream order
+  const size_t nctl = 2 * (size_t)n * (size_t)(nsteps > 0 ? nsteps : 1);
+  if (b->host_ctl_count < nctl) {
+    if (b->host_ctl) cudaFreeHost(b->host_ctl);
+    b->host_ctl = nullptr;
+    b->host_ctl_count = 0;
+    EPIC_CUDA_CHECK(cudaMallocHost(&b->host_ctl, sizeof(Ctl) * nctl));
+    b->host_ctl_count = nctl;
+  }
   for (auto *m : b->members) EPIC_CUDA_CHECK(cudaStreamSynchronize(m->stream));
   for (int step = 0; step < nsteps; step++) {
+    Ctl *ctl = b->host_ctl + 2 * (size_t)n * step;
     int idx = 0;
     for (auto *g : b->groups) {
       const int lo = idx;
       for (auto *m : g->members) {
-        int rc = enqueue_upload(m, f[idx], g->stream, &b->host_ctl[2 * idx]);
+        // after the first step the host arrays hold exactly what the device state was, and the
+        // device's control block (time-plane indices, itime) is already the one they belong to
+        int rc = enqueue_upload(m, f[idx], g->stream, &ctl[2 * idx], step == 0);
         if (rc) return rc;
         m->uploaded = true;
         idx++;
@@ -1068,20 +1104,22 @@ extern "C" int epic_batch_step_host(epic_batch *b, epic_fields *const *f, int32_
         if (rc) return rc;
       }
       for (int q = lo; q < idx; q++) {
-        int rc = enqueue_download(b->members[q], f[q], g->stream, &b->host_ctl[2 * q + 1]);
+        int rc = enqueue_download(b->members[q], f[q], g->stream, &ctl[2 * q + 1]);
         if (rc) return rc;
       }
     }
-    for (auto *g : b->groups) EPIC_CUDA_CHECK(cudaStreamSynchronize(g->stream));
+  }
+  for (auto *g : b->groups) EPIC_CUDA_CHECK(cudaStreamSynchronize(g->stream));
+  for (int step = 0; step < nsteps; step++)
     for (int q = 0; q < n; q++) {
-      fields_from_ctl(f[q], b->host_ctl[2 * q + 1]);
-      int rc = model_error(b->host_ctl[2 * q + 1]);
+      const Ctl &c = b->host_ctl[2 * ((size_t)n * step + q) + 1];
+      if (step == nsteps - 1) fields_from_ctl(f[q], c);
+      int rc = model_error(c);
       if (rc) {
         const std::string msg = epic::error_buffer();
-        return set_error(EPIC_ERR_MODEL, "member %d: %s", q, msg.c_str());
+        return set_error(EPIC_ERR_MODEL, "step %d, member %d: %s", step, q, msg.c_str());
       }
     }
-  }
   return check_launch("epic_batch_step_host");
 }
 

@@ -226,8 +226,12 @@ int  epic_batch_download(epic_batch *b, epic_fields *const *f);
 /*
  * nsteps end-to-end steps with host-resident state: each step uploads every member from f[i],
  * steps it and downloads it into f[i] (as epic_model_step_host does for one model).  The members
- * are split into `groups` sub-batches on their own streams so that copies overlap kernels; f
- * should be pinned host memory.
+ * are split into `groups` sub-batches on their own streams so that copies overlap kernels, and a
+ * group's next step starts as soon as its own download is done (no drain between steps; the
+ * host's time-plane indices and itime in f[i] are updated once, after the last step).  f should
+ * be pinned host memory; when a member's 3-D arrays sit back to back in the order u, v, dudt,
+ * dvdt, hdry, theta, p3, h3, p2, theta2, t2, t3, rho2, rho3, exner3, gz3, mont3, heat3, pv3, ri2,
+ * div_uv3, w3, dzdt3, u_spinup, its state moves with one copy each way (any layout works).
  */
 int  epic_batch_step_host(epic_batch *b, epic_fields *const *f, int32_t groups, int32_t nsteps);
 int  epic_batch_sync(epic_batch *b);                       /* wait; first member error, if any */
