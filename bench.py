@@ -55,10 +55,14 @@ SERVE_SHAPES = {(64, 32, 10): 300, (64, 32, 20): 300, (128, 64, 20): 300, (128, 
 METRIC = "cell-steps/s"
 
 
-def _workload_cfg(name, seed=0):
+ADVECTION = {"hsu": 0, "akima": 1}   # EPIC_ADV_HSU, EPIC_ADV_AKIMA
+ADVECTION_NAME = {"hsu": "Hsu-Konor-Arakawa advection", "akima": "Akima advection"}
+
+
+def _workload_cfg(name, seed=0, advection="hsu"):
     from epic_gb300 import HSConfig
     ni, nj, nk, dt = WORKLOADS[name]
-    return HSConfig(ni=ni, nj=nj, nk=nk, dt=dt, seed=seed)
+    return HSConfig(ni=ni, nj=nj, nk=nk, dt=dt, seed=seed, advection_scheme=ADVECTION[advection])
 
 
 def algorithmic_bytes_per_step(cfg, word=8):
@@ -128,11 +132,11 @@ class ClockSampler:
 # CPU side: the oracle's restatement of the reference step
 # ---------------------------------------------------------------------------------------------
 
-def _cpu_replica(name, seed, nsteps, warm, q):
+def _cpu_replica(name, seed, nsteps, warm, advection, q):
     sys.path.insert(0, os.path.join(ROOT, "tests"))
     from oracle_lib import Port
     from epic_gb300 import EPIC_SYNC_DIAGS_ONLY, hs_setup
-    cfg = _workload_cfg(name, seed)
+    cfg = _workload_cfg(name, seed, advection)
     ga, f = hs_setup(cfg)
     p = Port(ga)
     p.upload(f)
@@ -143,14 +147,14 @@ def _cpu_replica(name, seed, nsteps, warm, q):
     q.put(time.perf_counter() - t0)
 
 
-def cpu_reference(name, nsteps, warm, procs):
+def cpu_reference(name, nsteps, warm, procs, advection="hsu"):
     """Aggregate cell-steps/s of `procs` independent single-threaded replicas of the reference step."""
     sys.path.insert(0, os.path.join(ROOT, "tests"))
     from oracle_lib import build_port
     build_port()
     ctx = mp.get_context("spawn")
     q = ctx.Queue()
-    ps = [ctx.Process(target=_cpu_replica, args=(name, s, nsteps, warm, q)) for s in range(procs)]
+    ps = [ctx.Process(target=_cpu_replica, args=(name, s, nsteps, warm, advection, q)) for s in range(procs)]
     for p in ps:
         p.start()
     times = [q.get(timeout=3600) for _ in ps]
@@ -179,7 +183,7 @@ def run_gpu(args):
     if ws > 1:
         import torch.distributed as dist
         dist.init_process_group("nccl")
-    cfg = _workload_cfg(args.workload, seed=rank)
+    cfg = _workload_cfg(args.workload, seed=rank, advection=args.advection)
     ga, f = hs_setup(cfg)
     model = Model(ga, _prec(args.precision))
     model.upload(f)
@@ -237,10 +241,12 @@ def run_gpu(args):
         out = {
             "metric": METRIC, "value": value, "unit": "cell-steps/s", "n_gpus": ws, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": ms_step, "higher_is_better": True, "scaling": "weak",
-            "vs_baseline": None, "dtype": "f64", "data": "synthetic",
-            "config": {"workload": f"Held-Suarez {cfg.ni}x{cfg.nj}x{cfg.nk}, dt={cfg.dt}s, AB3, nu4=0.5 max, "
-                                   f"FP64 drop-in form", "ni": cfg.ni, "nj": cfg.nj, "nk": cfg.nk, "dt": cfg.dt,
-                       "precision": "fp64", "parallelism": f"replicas{ws}",
+            "vs_baseline": None, "dtype": "f64" if args.precision == "fp64" else "f32+f64", "data": "synthetic",
+            "config": {"workload": f"Held-Suarez {cfg.ni}x{cfg.nj}x{cfg.nk}, dt={cfg.dt}s, AB3, "
+                                   f"{ADVECTION_NAME[args.advection]}, nu4=0.5 max, "
+                                   + ("FP64 drop-in form" if args.precision == "fp64" else f"{args.precision} form"),
+                       "ni": cfg.ni, "nj": cfg.nj, "nk": cfg.nk, "dt": cfg.dt,
+                       "precision": args.precision, "advection": args.advection, "parallelism": f"replicas{ws}",
                        "l2": f"state {model.device_bytes / 1e9:.2f} GB > 129 MB L2; no flush needed",
                        "state": "horizontally uniform HS equilibrium column at rest + seeded 0.1 K theta noise"},
             "clocks": clocks,
@@ -268,7 +274,7 @@ def _members(cfg, n, precision, torch_seed=7):
     rng = np.random.default_rng(torch_seed)
     out = []
     for q in range(n):
-        ga, f = hs_setup(HSConfig(ni=cfg.ni, nj=cfg.nj, nk=cfg.nk, dt=cfg.dt, seed=q))
+        ga, f = hs_setup(HSConfig(ni=cfg.ni, nj=cfg.nj, nk=cfg.nk, dt=cfg.dt, seed=q, advection_scheme=cfg.advection_scheme))
         ga.struct.hs_kf *= 1.0 + float(rng.uniform(-0.1, 0.1))
         m = Model(ga, precision)
         m.upload(f)
@@ -302,13 +308,14 @@ def _prec(name):
     return {"fp64": EPIC_PREC_FP64, "mixed": EPIC_PREC_MIXED, "fast": EPIC_PREC_MIXED_FAST}[name]
 
 
-def mixed_error(torch, precision):
+def mixed_error(torch, precision, advection="hsu"):
     """Per-prognostic relative L2 of a mixed form against FP64 after one simulated day
-    (288 steps of 300 s) at 64x32x10, from a state spun up for 10 days in FP64, and from rest."""
+    (288 steps of 300 s) at 64x32x10, from a state spun up for 10 days in FP64, and from rest
+    (both the spin-up and the day use the given advection scheme)."""
     sys.path.insert(0, os.path.join(ROOT, "tests"))
     from compare import PROGNOSTIC, field_errors
     from epic_gb300 import EPIC_PREC_FP64, EPIC_SYNC_DIAGS_ONLY, HSConfig, Model, hs_setup
-    ga, f = hs_setup(HSConfig(ni=64, nj=32, nk=10, dt=300, seed=0))
+    ga, f = hs_setup(HSConfig(ni=64, nj=32, nk=10, dt=300, seed=0, advection_scheme=ADVECTION[advection]))
     out = {}
     for label, spin in (("after_10_day_spin_up", 2880), ("from_rest", 0)):
         start = f
@@ -332,7 +339,8 @@ def mixed_error(torch, precision):
             m.close()
         e = field_errors(res[1], res[0], PROGNOSTIC)
         out[label] = {k: v[0] for k, v in e.items()}
-    out["case"] = "64x32x10, dt=300 s, 1 simulated day (288 steps), relative L2 per prognostic vs the FP64 form"
+    out["case"] = (f"64x32x10, dt=300 s, {ADVECTION_NAME[advection]}, 1 simulated day (288 steps), relative L2 per "
+                   f"prognostic vs the FP64 form")
     return out
 
 
@@ -388,7 +396,7 @@ def run_gpu_ensemble(args):
         import torch.distributed as dist
         dist.init_process_group("nccl")
     precision = _prec(args.precision)
-    cfg = _workload_cfg(args.workload)
+    cfg = _workload_cfg(args.workload, advection=args.advection)
     nmem = args.members or ENSEMBLE[args.workload]
     members = _members(cfg, nmem, precision, torch_seed=7 + rank)
     starts = [m.download() for m in members]
@@ -463,9 +471,10 @@ def run_gpu_ensemble(args):
             "warmup": args.warmup, "ms_per_step": ms_step, "higher_is_better": True, "scaling": "weak",
             "vs_baseline": None, "dtype": "f64" if precision == EPIC_PREC_FP64 else "f32+f64", "data": "synthetic",
             "config": {"workload": f"ensemble of {nmem} Held-Suarez members {cfg.ni}x{cfg.nj}x{cfg.nk}, dt={cfg.dt}s, AB3, "
-                                   f"seeded 0.1 K noise and +/-10% k_f per member, {args.precision} form, one launch per "
+                                   f"{ADVECTION_NAME[args.advection]}, seeded 0.1 K noise and +/-10% k_f per member, {args.precision} form, one launch per "
                                    f"kernel for all members", "ni": cfg.ni, "nj": cfg.nj, "nk": cfg.nk, "dt": cfg.dt,
-                       "members": nmem, "precision": args.precision, "parallelism": f"replicas{ws}",
+                       "members": nmem, "precision": args.precision, "advection": args.advection,
+                       "parallelism": f"replicas{ws}",
                        "launch_shapes": {"autotuned_block_sizes": tuning,
                                          "groups": ["uv_core", "pgrad", "hsu_meridional", "hyperviscosity", "diagnostics",
                                                     "update", "column", "pointwise", "row_filter"]},
@@ -489,11 +498,11 @@ def run_gpu_ensemble(args):
             out["mixed_single"] = dict(mixed, note=f"{args.precision} form, one {cfg.ni}x{cfg.nj}x{cfg.nk} grid")
             out["batched_over_fp64_single"] = value / ws / fp64["value"]
             if precision != EPIC_PREC_FP64:
-                out["mixed_error"] = mixed_error(torch, precision)
+                out["mixed_error"] = mixed_error(torch, precision, args.advection)
             if args.precision == "mixed":
                 # the faster form that keeps the vertical integration and pressure gradient in FP32
                 fast = ensemble_rate(cfg, nmem, _prec("fast"), args, torch, rank)
-                out["mixed_fast"] = dict(fast, error=mixed_error(torch, _prec("fast")),
+                out["mixed_fast"] = dict(fast, error=mixed_error(torch, _prec("fast"), args.advection),
                                          note="EPIC_PREC_MIXED_FAST ensemble, same workload and timing")
             out["serving"] = serving_summary(precision)
     if ws > 1:
@@ -550,7 +559,7 @@ def _peaks():
 
 
 def kernel_roofline(model, cfg, stream, torch):
-    """Stage 6 (advection: the three Hsu predictor-corrector advections) timed alone.
+    """Stage 6 (advection: three passes of the grid's scheme, Hsu or Akima) timed alone.
 
     Algorithmic bytes per launch: each advected field (unity, THETA, HDRY) is read and written
     once, plus U, V, W3 read once: 6 reads + 3 writes of one FP64 3-D field
@@ -574,7 +583,8 @@ def kernel_roofline(model, cfg, stream, torch):
     cells = cfg.ni * (cfg.nj + 1) * cfg.nk
     alg = 9 * 8 * cells
     ach = alg / dur / 1e9
-    return {"kernel": "advection (hsu_advection of unity, THETA, HDRY)", "bound": "hbm", "achieved": ach,
+    scheme = "akima_advection" if cfg.advection_scheme == ADVECTION["akima"] else "hsu_advection"
+    return {"kernel": f"advection ({scheme} of unity, THETA, HDRY)", "bound": "hbm", "achieved": ach,
             "peak": peaks["hbm_gbs"], "unit": "GB/s", "frac": ach / peaks["hbm_gbs"],
             "peak_source": peaks["source"] + " (burst copy)", "algorithmic_bytes": alg, "launch_ms": dur * 1e3,
             "traffic": None}
@@ -593,6 +603,8 @@ def main():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--cpu-steps", type=int, default=3)
     ap.add_argument("--precision", default=None, choices=["fp64", "mixed", "fast"])
+    ap.add_argument("--advection", default="hsu", choices=sorted(ADVECTION),
+                    help="THETA/HDRY advection scheme (the Held-Suarez default is hsu)")
     args = ap.parse_args()
     if args.precision is None:
         args.precision = "mixed" if args.workload in ENSEMBLE else "fp64"
@@ -603,15 +615,17 @@ def main():
             return
         procs = os.cpu_count() or 1
         steps = max(1, min(args.steps, 3))
-        val, wall = cpu_reference(args.workload, steps, 0, procs)
-        cfg = _workload_cfg(args.workload)
+        val, wall = cpu_reference(args.workload, steps, 0, procs, args.advection)
+        cfg = _workload_cfg(args.workload, advection=args.advection)
         line = {"impl": "reference", "metric": METRIC, "value": val, "unit": "cell-steps/s", "n_gpus": args.gpus,
                 "steps": steps, "warmup": args.warmup, "ms_per_step": wall / steps * 1e3, "higher_is_better": True,
                 "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
                 "config": {"workload": (f"ensemble of {ENSEMBLE[args.workload]} Held-Suarez members " if args.workload in ENSEMBLE
-                                        else "Held-Suarez ") + f"{cfg.ni}x{cfg.nj}x{cfg.nk}, dt={cfg.dt}s, AB3, nu4=0.5 max; "
+                                        else "Held-Suarez ") + f"{cfg.ni}x{cfg.nj}x{cfg.nk}, dt={cfg.dt}s, AB3, "
+                                        f"{ADVECTION_NAME[args.advection]}, nu4=0.5 max; "
                                         f"reference CPU step (FP64) as {procs} concurrent single-threaded grids",
-                           "ni": cfg.ni, "nj": cfg.nj, "nk": cfg.nk, "dt": cfg.dt, "precision": "fp64"},
+                           "ni": cfg.ni, "nj": cfg.nj, "nk": cfg.nk, "dt": cfg.dt, "precision": "fp64",
+                           "advection": args.advection},
                 "cpu_baseline": {"value": val, "unit": "cell-steps/s", "cores": procs, "kind": "port",
                                  "sample": f"{procs} independent single-threaded replicas x {steps} steps of the "
                                            f"oracle's restatement (bit-identical to the reference build)"},
@@ -622,7 +636,7 @@ def main():
     out = run_gpu_ensemble(args) if args.workload in ENSEMBLE else run_gpu(args)
     if rank == 0 and out is not None:
         if ws == 1 and not args.no_cpu_baseline:
-            val, wall = cpu_reference(args.workload, args.cpu_steps, 0, 1)
+            val, wall = cpu_reference(args.workload, args.cpu_steps, 0, 1, args.advection)
             out["cpu_baseline"] = {"value": val, "unit": "cell-steps/s", "cores": 1, "kind": "port",
                                    "sample": f"{args.cpu_steps} steps of {WORKLOADS[args.workload][:3]} on one core "
                                              f"({wall:.1f} s) with the oracle's restatement of the reference step"}

@@ -17,7 +17,7 @@ import os
 
 import numpy as np
 
-from .abi import (EPIC_PREC_FP64, EPIC_PREC_MIXED, EPIC_PREC_MIXED_FAST, EPIC_STEP_PROGS_AND_SYNC_DIAGS, EPIC_SYNC_DIAGS_ONLY,
+from .abi import (EPIC_ADV_AKIMA, EPIC_ADV_HSU, EPIC_PREC_FP64, EPIC_PREC_MIXED, EPIC_PREC_MIXED_FAST, EPIC_STEP_PROGS_AND_SYNC_DIAGS, EPIC_SYNC_DIAGS_ONLY,
                   EPIC_UV_AB3, EPIC_UV_LEAPFROG, EpicFields, EpicGrid, EpicHsParams, Fields, GridArrays,
                   HSConfig, Layout)
 
@@ -271,5 +271,5 @@ class Batch:
 
 
 __all__ = ["Model", "Batch", "model_bytes", "hs_setup", "load_library", "EpicError", "HSConfig", "Fields", "GridArrays", "Layout",
-           "EPIC_PREC_FP64", "EPIC_PREC_MIXED", "EPIC_PREC_MIXED_FAST", "EPIC_STEP_PROGS_AND_SYNC_DIAGS", "EPIC_SYNC_DIAGS_ONLY",
+           "EPIC_ADV_AKIMA", "EPIC_ADV_HSU", "EPIC_PREC_FP64", "EPIC_PREC_MIXED", "EPIC_PREC_MIXED_FAST", "EPIC_STEP_PROGS_AND_SYNC_DIAGS", "EPIC_SYNC_DIAGS_ONLY",
            "EPIC_UV_AB3", "EPIC_UV_LEAPFROG", "LIB_PATH", "np"]

@@ -18,6 +18,8 @@ EPIC_UV_LEAPFROG = 1
 EPIC_PREC_FP64 = 0
 EPIC_PREC_MIXED = 1
 EPIC_PREC_MIXED_FAST = 2
+EPIC_ADV_HSU = 0
+EPIC_ADV_AKIMA = 1
 
 _dp = C.POINTER(C.c_double)
 
@@ -27,7 +29,7 @@ class EpicGrid(C.Structure):
         ("ni", C.c_int32), ("nj", C.c_int32), ("nk", C.c_int32), ("dt", C.c_int32),
         ("uv_scheme", C.c_int32), ("k_sigma", C.c_int32), ("k_sponge", C.c_int32),
         ("newt_cool_on", C.c_int32), ("newt_cool_adjust", C.c_int32), ("drag_v", C.c_int32),
-        ("drag_zonal_avg", C.c_int32), ("jtp", C.c_int32),
+        ("drag_zonal_avg", C.c_int32), ("jtp", C.c_int32), ("advection_scheme", C.c_int32), ("pad1", C.c_int32),
         ("dln", C.c_double), ("dlt", C.c_double), ("dy0", C.c_double),
         ("globe_latbot", C.c_double), ("globe_lattop", C.c_double), ("press0", C.c_double),
         ("topo_scale", C.c_double), ("prandtl", C.c_double), ("tau_drag", C.c_double),
@@ -58,7 +60,7 @@ class EpicFields(C.Structure):
 
 class EpicHsParams(C.Structure):
     _fields_ = [("ni", C.c_int32), ("nj", C.c_int32), ("nk", C.c_int32), ("dt", C.c_int32),
-                ("uv_scheme", C.c_int32), ("pad0", C.c_int32),
+                ("uv_scheme", C.c_int32), ("advection_scheme", C.c_int32),
                 ("ptop", C.c_double), ("pbot", C.c_double), ("p_sigma", C.c_double),
                 ("nu_nondim", C.c_double * 9), ("nudiv_nondim", C.c_double), ("lat0", C.c_double)]
 
@@ -212,6 +214,7 @@ class HSConfig:
     nk: int = 10
     dt: int = 300
     uv_scheme: int = EPIC_UV_AB3
+    advection_scheme: int = EPIC_ADV_HSU
     nu4: float = 0.5
     nu6: float = 0.0
     nu8: float = 0.0
@@ -227,6 +230,7 @@ class HSConfig:
     def params(self) -> EpicHsParams:
         p = EpicHsParams()
         p.ni, p.nj, p.nk, p.dt, p.uv_scheme = self.ni, self.nj, self.nk, self.dt, self.uv_scheme
+        p.advection_scheme = self.advection_scheme
         p.ptop, p.pbot, p.p_sigma = self.ptop, self.pbot, self.p_sigma
         for i in range(9):
             p.nu_nondim[i] = 0.0

@@ -41,6 +41,7 @@ struct DevModel {
   int nvp, ntp;
   // scalars
   int uv_scheme, k_sigma, k_sponge, newt_cool_on, drag_v, drag_zonal_avg, rayleigh_on;
+  int akima;   // advection scheme: 0 Hsu-Konor-Arakawa predictor-corrector, 1 Akima
   double dt, press0, topo_scale, prandtl, tau_drag, nudiv;
   double zeta0, zeta1, alpha, sigma_sigma, g_coeff;   // g_coeff = 1/(1-exp(-alpha*(1-sigma_sigma)))
   double kappa, cp, cpr, rgas, mu_dry, hs_kf, lat0, m0, eps13;

@@ -159,22 +159,27 @@ int run_stage_on(const DevModel &M, cudaStream_t s, int stage) {
       launch_meridional_hyperviscosity(M, 3, M.theta, PL_NONE, s);
       launch_zonal_hyperviscosity(M, 3, M.theta, PL_NONE, s);
       break;
-    case 6:
+    case 6: {
+      // advection(), epic_flux.c:346-637: UNITY, THETA and HDRY with the grid's scheme
+      auto vertical = M.akima ? launch_akima_vertical : launch_hsu_vertical;
+      auto meridional = M.akima ? launch_akima_meridional : launch_hsu_meridional;
+      auto zonal = M.akima ? launch_akima_zonal : launch_hsu_zonal;
       launch_advection_prep(M, 0, s);
-      launch_hsu_vertical(M, M.unity, 0, s);
-      launch_hsu_meridional(M, M.unity, 0, s);
-      launch_hsu_zonal(M, M.unity, 0, 1, s);
+      vertical(M, M.unity, 0, s);
+      meridional(M, M.unity, 0, s);
+      zonal(M, M.unity, 0, 1, s);
       launch_advection_prep(M, 1, s);
-      launch_hsu_vertical(M, M.theta, 1, s);
-      launch_hsu_meridional(M, M.theta, 1, s);
-      launch_hsu_zonal(M, M.theta, 0, M.k_sigma - 1, s);
+      vertical(M, M.theta, 1, s);
+      meridional(M, M.theta, 1, s);
+      zonal(M, M.theta, 0, M.k_sigma - 1, s);
       launch_advection_prep(M, 2, s);
-      launch_hsu_vertical(M, M.hdry, 2, s);
-      launch_hsu_meridional(M, M.hdry, 2, s);
-      launch_hsu_zonal(M, M.hdry, 1, 1, s);
+      vertical(M, M.hdry, 2, s);
+      meridional(M, M.hdry, 2, s);
+      zonal(M, M.hdry, 1, 1, s);
       launch_restore_mass(M, s);
       launch_set_p2etc(M, 0, s, false);   // its P2 is recomputed (stage 11) before the pressure gradient
       break;
+    }
     case 7: launch_store_pgrad_vars(M, s, false); break;   // GZ3 for the filtered copy (stage 8)
     case 8:
       launch_copy_gz(M, s);
@@ -319,6 +324,8 @@ extern "C" int epic_model_create(const epic_grid *g, int32_t precision, epic_mod
   if ((g->newt_cool_on && g->prandtl > 0.) || (g->tau_drag > 0. && g->tau_drag < 1.e+20))
     return set_error(EPIC_ERR_ARG, "zonal Rayleigh drag (prandtl/tau_drag) is not supported");
   if (g->uv_scheme != EPIC_UV_AB3 && g->uv_scheme != EPIC_UV_LEAPFROG) return set_error(EPIC_ERR_ARG, "uv_scheme=%d", g->uv_scheme);
+  if (g->advection_scheme != EPIC_ADV_HSU && g->advection_scheme != EPIC_ADV_AKIMA)
+    return set_error(EPIC_ERR_ARG, "advection_scheme=%d", g->advection_scheme);
   const char *ptrs[] = {(const char *)g->lon, (const char *)g->lat, (const char *)g->rln, (const char *)g->rlt, (const char *)g->f,
                         (const char *)g->m, (const char *)g->n, (const char *)g->mn, (const char *)g->g, (const char *)g->sigmatheta,
                         (const char *)g->dsgth, (const char *)g->dsgth_inv, (const char *)g->h_min, (const char *)g->t_sponge_inv};
@@ -335,7 +342,7 @@ extern "C" int epic_model_create(const epic_grid *g, int32_t precision, epic_mod
   d.n2 = L.n2; d.n3 = L.n3;
   d.nvp = g->uv_scheme == EPIC_UV_AB3 ? 1 : 2;
   d.ntp = g->uv_scheme == EPIC_UV_AB3 ? 3 : 1;
-  d.uv_scheme = g->uv_scheme; d.k_sigma = g->k_sigma; d.k_sponge = g->k_sponge; d.newt_cool_on = g->newt_cool_on;
+  d.uv_scheme = g->uv_scheme; d.akima = g->advection_scheme == EPIC_ADV_AKIMA; d.k_sigma = g->k_sigma; d.k_sponge = g->k_sponge; d.newt_cool_on = g->newt_cool_on;
   d.drag_v = g->drag_v; d.drag_zonal_avg = g->drag_zonal_avg; d.rayleigh_on = 0;
   d.dt = (double)g->dt; d.press0 = g->press0; d.topo_scale = g->topo_scale; d.prandtl = g->prandtl; d.tau_drag = g->tau_drag;
   d.zeta0 = g->zeta0; d.zeta1 = g->zeta1; d.alpha = g->hybrid_alpha; d.sigma_sigma = g->sigma_sigma;
@@ -729,7 +736,7 @@ struct epic_batch {
 namespace {
 
 bool same_launch_shape(const DevModel &a, const DevModel &b) {
-  if (a.ni != b.ni || a.nj != b.nj || a.nk != b.nk || a.uv_scheme != b.uv_scheme || a.mixed != b.mixed || a.col64 != b.col64 ||
+  if (a.ni != b.ni || a.nj != b.nj || a.nk != b.nk || a.uv_scheme != b.uv_scheme || a.akima != b.akima || a.mixed != b.mixed || a.col64 != b.col64 ||
       a.k_sigma != b.k_sigma || a.k_sponge != b.k_sponge || a.newt_cool_on != b.newt_cool_on || a.dt != b.dt ||
       a.nudiv != b.nudiv || a.lat0 != b.lat0)
     return false;

@@ -119,6 +119,8 @@ extern "C" int epic_hs_grid_build(const epic_hs_params *p, epic_grid *g, double 
   if (nj < 3 || nk < 3) return set_error(EPIC_ERR_ARG, "nj=%d, nk=%d too small", nj, nk);
   if (p->dt <= 0) return set_error(EPIC_ERR_ARG, "dt=%d", p->dt);
   if (p->uv_scheme != EPIC_UV_AB3 && p->uv_scheme != EPIC_UV_LEAPFROG) return set_error(EPIC_ERR_ARG, "uv_scheme=%d", p->uv_scheme);
+  if (p->advection_scheme != EPIC_ADV_HSU && p->advection_scheme != EPIC_ADV_AKIMA)
+    return set_error(EPIC_ERR_ARG, "advection_scheme=%d", p->advection_scheme);
   double *lon = const_cast<double *>(g->lon), *lat = const_cast<double *>(g->lat);
   double *rln = const_cast<double *>(g->rln), *rlt = const_cast<double *>(g->rlt);
   double *fc = const_cast<double *>(g->f), *m = const_cast<double *>(g->m), *n = const_cast<double *>(g->n);
@@ -130,6 +132,7 @@ extern "C" int epic_hs_grid_build(const epic_hs_params *p, epic_grid *g, double 
     return set_error(EPIC_ERR_ARG, "epic_hs_grid_build: grid array pointer is NULL");
 
   g->ni = ni; g->nj = nj; g->nk = nk; g->dt = p->dt; g->uv_scheme = p->uv_scheme;
+  g->advection_scheme = p->advection_scheme;
   g->k_sponge = 0;               // held_suarez forces k_sponge = 0, epic_initial.c:1252-1254
   g->newt_cool_on = 1;           // epic_initial.c:473-475
   g->newt_cool_adjust = 0; g->prandtl = 0.;     // :488-490

@@ -289,6 +289,80 @@ __global__ void __launch_bounds__(CT_THREADS) k_hsu_vertical(DevModel M, double 
   }
 }
 
+// Akima's harmonic mean of like-signed differences (akima_advection's dela)
+template <class R>
+__device__ __forceinline__ R akima_dela(R d0, R d1) {
+  const R tmp = d0 * d1;
+  return (tmp > R(0.)) ? R(2.) * tmp / (d0 + d1) : R(0.);
+}
+
+// Vertical pass of akima_advection, epic_flux.c:1549-1744 (mass fluxes through the model top
+// and bottom are 0 for Held-Suarez, :47-115).  kind: 0 = unity (P3_INDEX), 1 = THETA,
+// 2 = HDRY.  A column tile (32 columns j = 0..nj, i = 0..ni+1 per block), the levels spread over
+// the warps; shared arrays [k][lane]: WA (the field), W (the vertical velocity at the flux
+// points), DL (dela), FF (the fluxes).
+template <class R>
+__global__ void __launch_bounds__(CT_THREADS) k_akima_vertical(DevModel M, double *buff, int kind) {
+  epic_member(M, buff);
+  extern __shared__ __align__(16) unsigned char smraw[];
+  R *sm = reinterpret_cast<R *>(smraw);
+  const ColTile c = col_tile(M);
+  const int nk = M.nk, L = nk + 2;
+  const long long n2 = M.n2;
+  const bool layer = kind == 2;
+  const int kf = kind == 1 ? M.k_sigma - 1 : 1;
+  const R DT = cv<R>(M.dt);
+  R *WA = sm, *W = WA + 32 * L, *DL = W + 32 * L, *FF = DL + 32 * L;
+  auto wa = [&](int k) { return CT(WA, k); };
+  if (c.valid) {
+    for (int k = (layer ? kf : kf - 1) + c.warp; k <= nk; k += CT_WARPS) CT(WA, k) = cv<R>(buff[c.base + k * n2]);
+    if (layer)
+      for (int k = kf - 1 + c.warp; k <= nk; k += CT_WARPS) CT(W, k) = cv<R>(M.w3[c.base + k * n2]);
+    else
+      for (int k = kf + c.warp; k <= nk; k += CT_WARPS)
+        CT(W, k) = (k == 1 || k == nk) ? R(0.) : R(.5) * (cv<R>(M.w3[c.base + k * n2]) + cv<R>(M.w3[c.base + (k - 1) * n2]));
+  }
+  __syncthreads();
+  if (layer) {
+    // deltaa(k) = a(k) - a(k+1) for kf <= k < nk, 0 at kf-1 and nk
+    auto deltaa = [&](int k) { return (k < kf || k >= nk) ? R(0.) : wa(k) - wa(k + 1); };
+    if (c.valid)
+      for (int k = kf + c.warp; k <= nk; k += CT_WARPS) CT(DL, k) = akima_dela<R>(deltaa(k), deltaa(k - 1));
+    __syncthreads();
+    if (c.valid)
+      for (int k = kf - 1 + c.warp; k <= nk; k += CT_WARPS) {
+        if (k == kf - 1 || k == nk) { CT(FF, k) = R(0.); continue; }   // mass_flux_top, mass_flux_bot
+        const R aval = R(.5) * (wa(k) + wa(k + 1)) - (CT(DL, k) - CT(DL, k + 1)) / R(6.);
+        CT(FF, k) = CT(W, k) * aval;
+      }
+    __syncthreads();
+    if (c.valid)
+      for (int k = kf + c.warp; k <= nk; k += CT_WARPS) {
+        const long long x = c.base + k * n2;
+        buff[x] = buff[x] + to_d((CT(FF, k) - CT(FF, k - 1)) * cv<R>(M.dsgth_inv[2 * k]) * DT);
+      }
+  } else {
+    // deltaa(k) = a(k-1) - a(k) for kf <= k <= nk
+    auto deltaa = [&](int k) { return wa(k - 1) - wa(k); };
+    if (c.valid)
+      for (int k = kf - 1 + c.warp; k <= nk; k += CT_WARPS)
+        CT(DL, k) = (k == kf - 1 || k == nk) ? R(0.) : akima_dela<R>(deltaa(k), deltaa(k + 1));
+    __syncthreads();
+    if (c.valid)
+      for (int k = kf + c.warp; k <= nk + 1; k += CT_WARPS) {
+        if (k == nk + 1) { CT(FF, k) = R(0.); continue; }
+        const R aval = R(.5) * (wa(k - 1) + wa(k)) - (CT(DL, k - 1) - CT(DL, k)) / R(6.);
+        CT(FF, k) = CT(W, k) * aval;
+      }
+    __syncthreads();
+    if (c.valid)
+      for (int k = kf + c.warp; k <= nk; k += CT_WARPS) {
+        const long long x = c.base + k * n2;
+        buff[x] = buff[x] + to_d((CT(FF, k + 1) - CT(FF, k)) * cv<R>(M.dsgth_inv[2 * k + 1]) * DT);
+      }
+  }
+}
+
 // restore_mass(HDRY_INDEX), epic_adjust.c:45-96
 // Pointwise: one thread per cell of layers 1..nk, rows 0..nj, all columns.
 __global__ void k_restore_mass(DevModel M) {
@@ -881,6 +955,11 @@ int launch_hsu_vertical(const DevModel &M, double *buff, int kind, cudaStream_t 
                 (size_t)5 * 32 * (M.nk + 2) * (M.mixed ? sizeof(float) : sizeof(double)), s, M, buff, kind);
   return 0;
 }
+int launch_akima_vertical(const DevModel &M, double *buff, int kind, cudaStream_t s) {
+  EPIC_LAUNCH_R(M.mixed, k_akima_vertical, ntile_blocks(M), CT_THREADS,
+                (size_t)4 * 32 * (M.nk + 2) * (M.mixed ? sizeof(float) : sizeof(double)), s, M, buff, kind);
+  return 0;
+}
 int launch_restore_mass(const DevModel &M, cudaStream_t s) {
   k_restore_mass<<<zg(epic_blocks((long long)M.nk * (M.nj + 1) * (M.ni + 2), TB(M, TB_POINT)), M), TB(M, TB_POINT), 0, s>>>(M);
   return 0;
@@ -921,7 +1000,9 @@ int column_kernels_init(int) {
       cudaFuncSetAttribute(k_set_p2etc_mixed, cudaFuncAttributeMaxDynamicSharedMemorySize, big) != cudaSuccess ||
       cudaFuncSetAttribute(k_pgrad_vars_column_mixed, cudaFuncAttributeMaxDynamicSharedMemorySize, big) != cudaSuccess ||
       cudaFuncSetAttribute(k_hsu_vertical<double>, cudaFuncAttributeMaxDynamicSharedMemorySize, hv) != cudaSuccess ||
-      cudaFuncSetAttribute(k_hsu_vertical<float>, cudaFuncAttributeMaxDynamicSharedMemorySize, hv) != cudaSuccess)
+      cudaFuncSetAttribute(k_hsu_vertical<float>, cudaFuncAttributeMaxDynamicSharedMemorySize, hv) != cudaSuccess ||
+      cudaFuncSetAttribute(k_akima_vertical<double>, cudaFuncAttributeMaxDynamicSharedMemorySize, hv) != cudaSuccess ||
+      cudaFuncSetAttribute(k_akima_vertical<float>, cudaFuncAttributeMaxDynamicSharedMemorySize, hv) != cudaSuccess)
     return -1;
   return 0;
 }

@@ -437,6 +437,58 @@ __global__ void k_hsu_zonal(DevModel M, double *buff, int kind, int kstart) {
   }
 }
 
+// Zonal pass of akima_advection (epic_flux.c:1826-1932) for one row: the fluxes come from a
+// zonally filtered copy of the row, the update goes to the unfiltered field.
+// kind: 0 = interface variable (unity, THETA), 1 = HDRY (layer; u averaged to the layer).
+template <class R>
+__global__ void k_akima_zonal(DevModel M, double *buff, int kind, int kstart) {
+  epic_member(M, buff);
+  extern __shared__ __align__(16) unsigned char smraw[];
+  R *sm = reinterpret_cast<R *>(smraw);
+  const int ni = M.ni, W = ni + 2;
+  const int j = (int)blockIdx.x;
+  const int k = kstart + (int)blockIdx.y;
+  R *a = sm, *u2d = a + W, *da = u2d + W, *dl = da + W, *ff = dl + W;
+  FilterSmem<R> fs = carve_filter(ff + W, ni);
+  const R DT = cv<R>(M.dt);
+  const long long base = M.at(k, j, 0);
+  const bool filt = row_is_filtered(M, j, 0);
+  if (filt) load_twiddles(M, fs);
+  const double *U = M.u + (long long)M.ctl->it_uv * M.n3;
+  const R n_inv = R(1.) / cv<R>(M.n[2 * j + 1]);
+  const R mn1 = cv<R>(M.mn[2 * j + 1]);
+  for (int i = threadIdx.x; i <= ni + 1; i += blockDim.x) {
+    a[i] = cv<R>(buff[base + i]);
+    // u2d, with periodic pads for the layer average (bc_lateral(u2d))
+    const int ii = kind == 1 ? (i == 0 ? ni : (i == ni + 1 ? 1 : i)) : i;
+    u2d[i] = kind == 1 ? R(.5) * (cv<R>(U[M.at(k, j, ii)]) + cv<R>(U[M.at(k - 1, j, ii)])) : cv<R>(U[M.at(k, j, i)]);
+  }
+  __syncthreads();
+  if (filt) filter_row_smem(M, a, M.high_lat_h, M.at2(j, 0), fs);
+  if (threadIdx.x == 0) { a[0] = a[ni]; a[ni + 1] = a[1]; }
+  __syncthreads();
+  for (int i = threadIdx.x + 1; i <= ni; i += blockDim.x) da[i] = a[i] - a[i - 1];
+  __syncthreads();
+  if (threadIdx.x == 0) { da[0] = da[ni]; da[ni + 1] = da[1]; }
+  __syncthreads();
+  for (int i = threadIdx.x + 1; i <= ni; i += blockDim.x) {
+    const R tmp = da[i] * da[i + 1];
+    dl[i] = (tmp > R(0.)) ? R(2.) * tmp / (da[i] + da[i + 1]) : R(0.);
+  }
+  __syncthreads();
+  if (threadIdx.x == 0) { dl[0] = dl[ni]; dl[ni + 1] = dl[1]; }
+  __syncthreads();
+  for (int i = threadIdx.x + 1; i <= ni; i += blockDim.x) {
+    const R aval = R(.5) * (a[i] + a[i - 1]) - (dl[i] - dl[i - 1]) / R(6.);
+    ff[i] = u2d[i] * aval * n_inv;
+  }
+  __syncthreads();
+  if (threadIdx.x == 0) { ff[0] = ff[ni]; ff[ni + 1] = ff[1]; }
+  __syncthreads();
+  for (int i = threadIdx.x + 1; i <= ni; i += blockDim.x)
+    write_with_pads(buff, M, base, i, buff[base + i] + to_d((ff[i] - ff[i + 1]) * mn1 * DT));
+}
+
 // ---- launchers ----
 
 static int row_threads(const DevModel &M) { return M.tb[TB_ROW] > 0 ? M.tb[TB_ROW] : (M.ni >= 256 ? 128 : 64); }
@@ -463,6 +515,13 @@ int launch_varz_filter(const DevModel &M, double *buff, int sel, int index, int 
   return 0;
 }
 
+int launch_akima_zonal(const DevModel &M, double *buff, int kind, int kstart, cudaStream_t s) {
+  const size_t smem = (5 * (size_t)(M.ni + 2) + filter_smem_elems(M.ni)) * relem(M.mixed);
+  dim3 grid(M.nj + 1, M.nk - kstart + 1);
+  EPIC_LAUNCH_R(M.mixed, k_akima_zonal, grid, row_threads(M), smem, s, M, buff, kind, kstart);
+  return 0;
+}
+
 int launch_hsu_zonal(const DevModel &M, double *buff, int kind, int kstart, cudaStream_t s) {
   const size_t smem = (8 * (size_t)(M.ni + 2) + filter_smem_elems(M.ni)) * relem(M.mixed);
   dim3 grid(M.nj + 1, M.nk - kstart + 1);
@@ -473,6 +532,7 @@ int launch_hsu_zonal(const DevModel &M, double *buff, int kind, int kstart, cuda
 template <class R>
 static void filter_attrs(int bytes) {
   cudaFuncSetAttribute(k_hsu_zonal<R>, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes);
+  cudaFuncSetAttribute(k_akima_zonal<R>, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes);
   cudaFuncSetAttribute(k_varz_filter_rows<R>, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes);
   cudaFuncSetAttribute(k_filter_planes<R>, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes);
 }

@@ -594,6 +594,49 @@ __global__ void k_hsu_meridional(DevModel M, double *A, int kind, int k0) {
 }
 
 // ---------------------------------------------------------------------------------------------
+// Meridional pass of akima_advection, epic_flux.c:1752-1820.  kind: 0/1 interface (unity,
+// THETA; V of the interface), 2 = HDRY (V averaged to the layer).  Two launches over planes
+// k0..nk: the fluxes FF (v rows 1..nj, into work3), then the update of rows 0..nj.
+// ---------------------------------------------------------------------------------------------
+
+template <class R>
+__device__ __forceinline__ R akima_mean(R d0, R d1) {   // the dela of akima_advection
+  const R tmp = d0 * d1;
+  return (tmp > R(0.)) ? R(2.) * tmp / (d0 + d1) : R(0.);
+}
+
+template <class R>
+__global__ void k_akima_merid_flux(DevModel M, const double *A, int kind, int k0) {
+  epic_member(M, A);
+  Cell c;
+  if (!cell3(M, k0, M.nk - k0 + 1, 1, M.nj, c)) return;   // v rows 1..nj
+  const int k = c.k, j = c.j, i = c.i, nj = M.nj;
+  auto a = [&](int jj) { return cv<R>(A[M.at(k, jj, i)]); };
+  // deltaa(jj) = A(jj) - A(jj-1) on rows 1..nj, 0 elsewhere
+  auto deltaa = [&](int jj) { return (jj < 1 || jj > nj) ? R(0.) : a(jj) - a(jj - 1); };
+  const R dl_j = akima_mean<R>(deltaa(j), deltaa(j + 1));
+  const R dl_jm = akima_mean<R>(deltaa(j - 1), deltaa(j));
+  const double *V = M.v + plane_offset(M, PL_UV);
+  const R v2d = kind == 2 ? R(.5) * (cv<R>(V[M.at(k, j, i)]) + cv<R>(V[M.at(k - 1, j, i)])) : cv<R>(V[M.at(k, j, i)]);
+  const R m_2j_inv = (fabs(M.lat[2 * j]) == 90.) ? R(0.) : R(1.) / cv<R>(M.m[2 * j]);
+  const R aval = R(.5) * (a(j) + a(j - 1)) - (dl_j - dl_jm) / R(6.);
+  write_with_pads(M.work3, M, M.at(k, j, 0), i, to_d(v2d * aval * m_2j_inv));
+}
+
+template <class R>
+__global__ void k_akima_merid_update(DevModel M, double *A, int k0) {
+  epic_member(M, A);
+  Cell c;
+  if (!cell3(M, k0, M.nk - k0 + 1, 0, M.nj + 1, c)) return;   // rows 0..nj
+  const int k = c.k, j = c.j, nj = M.nj;
+  const double *FF = M.work3;
+  auto ff = [&](int jj) { return (jj < 1 || jj > nj) ? R(0.) : cv<R>(FF[M.at(k, jj, c.i)]); };
+  const long long x = M.at(k, j, c.i);
+  const R da = (ff(j) - ff(j + 1)) * cv<R>(M.mn[2 * j + 1]) * cv<R>(M.dt);
+  write_with_pads(A, M, M.at(k, j, 0), c.i, A[x] + to_d(da));
+}
+
+// ---------------------------------------------------------------------------------------------
 // Hyperviscosity, epic_subgrid.c:590-1232
 // ---------------------------------------------------------------------------------------------
 
@@ -974,6 +1017,15 @@ int launch_uv_pgrad(const DevModel &M, cudaStream_t s) {
 // wins once those threads fill the GPU (large batches).  Smaller launches take the four passes,
 // whose threads cover every cell.  Both give the same bits.
 constexpr long long HSU_FUSED_MIN_THREADS = 65536;
+
+int launch_akima_meridional(const DevModel &M, double *buff, int kind, cudaStream_t s) {
+  const int k0 = kind == 1 ? M.k_sigma - 1 : 1;
+  const int nkk = M.nk - k0 + 1;
+  const int th = TB(M, TB_HSU);
+  EPIC_LAUNCH_R(M.mixed, k_akima_merid_flux, cells_blocks(M, nkk, M.nj, th), th, 0, s, M, buff, kind, k0);
+  EPIC_LAUNCH_R(M.mixed, k_akima_merid_update, cells_blocks(M, nkk, M.nj + 1, th), th, 0, s, M, buff, k0);
+  return 0;
+}
 
 int launch_hsu_meridional(const DevModel &M, double *buff, int kind, cudaStream_t s) {
   const int k0 = kind == 1 ? M.k_sigma - 1 : 1;

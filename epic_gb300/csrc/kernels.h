@@ -78,6 +78,11 @@ int launch_zero_tend(const DevModel &M, cudaStream_t s);
 int launch_uv_core(const DevModel &M, cudaStream_t s);
 int launch_uv_pgrad(const DevModel &M, cudaStream_t s);
 int launch_hsu_meridional(const DevModel &M, double *buff, int kind, cudaStream_t s);
+// akima_advection (epic_flux.c:1502-1940), the other advection scheme: vertical (k_column.cu),
+// meridional (k_stencil.cu) and zonal (k_filter.cu) passes, arguments as their Hsu counterparts
+int launch_akima_vertical(const DevModel &M, double *buff, int kind, cudaStream_t s);
+int launch_akima_meridional(const DevModel &M, double *buff, int kind, cudaStream_t s);
+int launch_akima_zonal(const DevModel &M, double *buff, int kind, int kstart, cudaStream_t s);
 int launch_meridional_hyperviscosity(const DevModel &M, int index, double *var, int sel, cudaStream_t s);
 int launch_zonal_hyperviscosity(const DevModel &M, int index, double *var, int sel, cudaStream_t s);
 int launch_divergence_damping(const DevModel &M, cudaStream_t s);

@@ -66,7 +66,8 @@ class _Active:
 
 
 def _shape_class(cfg: HSConfig, precision: int) -> tuple:
-    return (cfg.ni, cfg.nj, cfg.nk, cfg.dt, cfg.uv_scheme, precision, cfg.nu4, cfg.nu6, cfg.nu8, cfg.nudiv, cfg.lat0)
+    return (cfg.ni, cfg.nj, cfg.nk, cfg.dt, cfg.uv_scheme, cfg.advection_scheme, precision, cfg.nu4, cfg.nu6, cfg.nu8,
+            cfg.nudiv, cfg.lat0)
 
 
 def state_checksum(f: Fields) -> float:

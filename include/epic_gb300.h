@@ -38,6 +38,10 @@ extern "C" {
 #define EPIC_UV_AB3      0   /* "3rd-order Adams-Bashforth"   */
 #define EPIC_UV_LEAPFROG 1   /* "Leapfrog (Asselin filtered)" */
 
+/* var.theta/hdry.advection_scheme (src/shared/epic_flux.c:346-637) */
+#define EPIC_ADV_HSU   0   /* "Predictor-corrector (Hsu, Konor, and Arakawa)" */
+#define EPIC_ADV_AKIMA 1   /* "Monotonized, 4th-order centered (Akima)"       */
+
 /* Precision forms accepted by epic_model_create(). */
 #define EPIC_PREC_FP64  0    /* every kernel in binary64 (the drop-in form)                    */
 #define EPIC_PREC_MIXED 1    /* stencils/advection/hyperviscosity/filter/physics in binary32;
@@ -74,6 +78,8 @@ typedef struct epic_grid {
   int32_t drag_v;              /* grid.drag_v                                                   */
   int32_t drag_zonal_avg;      /* grid.drag_zonal_avg                                           */
   int32_t jtp;                 /* grid.jtp                                                      */
+  int32_t advection_scheme;    /* EPIC_ADV_HSU or EPIC_ADV_AKIMA, for THETA and HDRY alike      */
+  int32_t pad1;
   double  dln, dlt, dy0;       /* grid.dln, grid.dlt [deg], grid.dy0 [m]                        */
   double  globe_latbot, globe_lattop;
   double  press0;              /* grid.press0 [Pa]                                              */
@@ -269,7 +275,7 @@ const char *epic_last_error(void);
 typedef struct epic_hs_params {
   int32_t ni, nj, nk, dt;
   int32_t uv_scheme;
-  int32_t pad0;
+  int32_t advection_scheme;    /* EPIC_ADV_HSU (the Held-Suarez default) or EPIC_ADV_AKIMA */
   double  ptop, pbot, p_sigma; /* [Pa]; reference HS defaults 10, 1e5, 9e4 */
   double  nu_nondim[9];        /* grid.nu_nondim; HS runs use nu[4] = 0.5, the rest 0 */
   double  nudiv_nondim;

@@ -1605,21 +1605,153 @@ static void hsu_advection(ep_model *M, int kind, double *buff) {
   bc3(M, buff);
 }
 
-/* advection, epic_flux.c:346-637 (theta and hdry, Hsu scheme) */
+/* akima_advection(is, buff3d, HORIZONTAL_AND_VERTICAL), epic_flux.c:1502-1940: the monotonized
+ * fourth-order centred divergence-form scheme (Shchepetkin and McWilliams 2003, (4.9)-(4.12)).
+ * kind: IDX_OTHER = P3_INDEX (unity), IDX_THETA, IDX_HDRY.  mass_flux_top/bot are 0 for
+ * Held-Suarez (epic_flux.c:47-115). */
+static double akima_dela(double d0, double d1) {   /* harmonic mean of like-signed differences */
+  const double tmp = d0 * d1;
+  return (tmp > 0.) ? 2. * tmp / (d0 + d1) : 0.;
+}
+static void akima_advection(ep_model *M, int kind, double *buff) {
+  const int layer = (kind == IDX_HDRY);
+  const int k_first = (kind == IDX_THETA) ? M->g.k_sigma - 1 : 1;
+  int K, J, I;
+  double *w = M->wm, *w_a = M->w_a, *w_deltaa = M->w_a_diff1, *w_dela = M->w_a_diff2, *w_ff = M->w_ff;
+  double aval;
+  const double *U = M->u + (long)M->it_uv * M->n3, *V = M->v + (long)M->it_uv * M->n3;
+
+  /* Vertical advection, column by column (:1549-1744). */
+  for (J = 0; J <= NJ; J++)
+    for (I = 0; I <= NI + 1; I++) {
+      for (K = layer ? k_first : k_first - 1; K <= KHI; K++) w_a[K] = A3(buff, K, J, I);
+      if (layer) {
+        for (K = k_first - 1; K <= KHI; K++) w[K] = A3(M->w3, K, J, I);
+        w_deltaa[k_first - 1] = 0.;
+        for (K = k_first; K < KHI; K++) w_deltaa[K] = w_a[K] - w_a[K + 1];
+        w_deltaa[KHI] = 0.;
+        for (K = k_first; K <= KHI; K++) w_dela[K] = akima_dela(w_deltaa[K], w_deltaa[K - 1]);
+        w_ff[k_first - 1] = 0.;   /* mass_flux_top for k_first = 1, else 0 */
+        for (K = k_first; K < KHI; K++) {
+          aval = .5 * (w_a[K] + w_a[K + 1]) - (w_dela[K] - w_dela[K + 1]) / 6.;
+          w_ff[K] = w[K] * aval;
+        }
+        w_ff[KHI] = 0.;           /* mass_flux_bot */
+        for (K = k_first; K <= KHI; K++) A3(buff, K, J, I) += (w_ff[K] - w_ff[K - 1]) * M->dsgth_inv[2 * K] * DT;
+      } else {
+        for (K = k_first; K <= KHI; K++)
+          w[K] = (K == 1 || K == KHI) ? 0. : .5 * (A3(M->w3, K, J, I) + A3(M->w3, K - 1, J, I));
+        for (K = k_first; K <= KHI; K++) w_deltaa[K] = w_a[K - 1] - w_a[K];
+        w_dela[k_first - 1] = 0.;
+        for (K = k_first; K < KHI; K++) w_dela[K] = akima_dela(w_deltaa[K], w_deltaa[K + 1]);
+        w_dela[KHI] = 0.;
+        for (K = k_first; K <= KHI; K++) {
+          aval = .5 * (w_a[K - 1] + w_a[K]) - (w_dela[K - 1] - w_dela[K]) / 6.;
+          w_ff[K] = w[K] * aval;
+        }
+        w_ff[KHI + 1] = 0.;
+        for (K = k_first; K <= KHI; K++) A3(buff, K, J, I) += (w_ff[K + 1] - w_ff[K]) * M->dsgth_inv[2 * K + 1] * DT;
+      }
+    }
+
+  /* Meridional advection, plane by plane (:1752-1820). */
+  for (K = 1; K <= KHI; K++) {
+    double *a = buff + K * M->n2, *v2d = M->b2d[0], *deltaa = M->b2d[1], *dela = M->b2d[2], *ff = M->b2d[3];
+    double m_2j_inv, mn_2jp1;
+    if (kind == IDX_THETA && K <= M->g.k_sigma - 2) continue;
+    memset(v2d, 0, M->n2 * sizeof(double));
+    memset(deltaa, 0, M->n2 * sizeof(double));
+    memset(dela, 0, M->n2 * sizeof(double));
+    memset(ff, 0, M->n2 * sizeof(double));
+    if (layer) {
+      for (J = 1; J <= NJ; J++)
+        for (I = 1; I <= NI; I++) A2(v2d, J, I) = .5 * (A3(V, K, J, I) + A3(V, K - 1, J, I));   /* get_var at kk = 2K */
+      bc2(M, v2d);
+    } else {
+      for (J = 0; J <= NJ + 1; J++)
+        for (I = 0; I <= NI + 1; I++) A2(v2d, J, I) = A3(V, K, J, I);
+    }
+    for (J = 1; J <= NJ; J++)
+      for (I = 1; I <= NI; I++) A2(deltaa, J, I) = A2(a, J, I) - A2(a, J - 1, I);
+    bc2(M, deltaa);
+    for (J = 0; J <= NJ; J++)
+      for (I = 1; I <= NI; I++) A2(dela, J, I) = akima_dela(A2(deltaa, J, I), A2(deltaa, J + 1, I));
+    bc2(M, dela);
+    for (J = 1; J <= NJ; J++) {
+      m_2j_inv = (fabs(M->lat[2 * J]) == 90.) ? 0. : 1. / M->m[2 * J];
+      for (I = 1; I <= NI; I++) {
+        aval = .5 * (A2(a, J, I) + A2(a, J - 1, I)) - (A2(dela, J, I) - A2(dela, J - 1, I)) / 6.;
+        A2(ff, J, I) = A2(v2d, J, I) * aval * m_2j_inv;
+      }
+    }
+    bc2(M, ff);
+    for (J = 0; J <= NJ; J++) {
+      mn_2jp1 = M->mn[2 * J + 1];
+      for (I = 1; I <= NI; I++) A2(a, J, I) += (A2(ff, J, I) - A2(ff, J + 1, I)) * mn_2jp1 * DT;
+    }
+    bc2(M, a);
+  }
+
+  /* Zonal advection, plane by plane, fluxes from a filtered copy (:1826-1932). */
+  for (K = 1; K <= KHI; K++) {
+    double *a = M->b2d[6], *u2d = M->b2d[0], *deltaa = M->b2d[1], *dela = M->b2d[2], *ff = M->b2d[3];
+    double n_2jp1_inv, mn_2jp1;
+    if (kind == IDX_THETA && K <= M->g.k_sigma - 2) continue;
+    memcpy(a, buff + K * M->n2, M->n2 * sizeof(double));
+    zonal_filter_2d(M, IDX_OTHER, a);
+    memset(u2d, 0, M->n2 * sizeof(double));
+    memset(deltaa, 0, M->n2 * sizeof(double));
+    memset(dela, 0, M->n2 * sizeof(double));
+    memset(ff, 0, M->n2 * sizeof(double));
+    if (layer) {
+      for (J = 0; J <= NJ; J++)
+        for (I = 1; I <= NI; I++) A2(u2d, J, I) = .5 * (A3(U, K, J, I) + A3(U, K - 1, J, I));   /* get_var at kk = 2K */
+      bc2(M, u2d);
+    } else {
+      for (J = 0; J <= NJ; J++)
+        for (I = 0; I <= NI + 1; I++) A2(u2d, J, I) = A3(U, K, J, I);
+    }
+    for (J = 0; J <= NJ; J++)
+      for (I = 1; I <= NI; I++) A2(deltaa, J, I) = A2(a, J, I) - A2(a, J, I - 1);
+    bc2(M, deltaa);
+    for (J = 0; J <= NJ; J++)
+      for (I = 1; I <= NI; I++) A2(dela, J, I) = akima_dela(A2(deltaa, J, I), A2(deltaa, J, I + 1));
+    bc2(M, dela);
+    for (J = 0; J <= NJ; J++) {
+      n_2jp1_inv = 1. / M->n[2 * J + 1];
+      for (I = 1; I <= NI; I++) {
+        aval = .5 * (A2(a, J, I) + A2(a, J, I - 1)) - (A2(dela, J, I) - A2(dela, J, I - 1)) / 6.;
+        A2(ff, J, I) = A2(u2d, J, I) * aval * n_2jp1_inv;
+      }
+    }
+    bc2(M, ff);
+    for (J = 0; J <= NJ; J++) {
+      mn_2jp1 = M->mn[2 * J + 1];
+      for (I = 1; I <= NI; I++) A3(buff, K, J, I) += (A2(ff, J, I) - A2(ff, J, I + 1)) * mn_2jp1 * DT;
+    }
+  }
+  bc3(M, buff);
+}
+
+/* advection, epic_flux.c:346-637 (theta and hdry, one scheme for both) */
+static void advect(ep_model *M, int kind, double *buff) {
+  if (M->g.advection_scheme == EPIC_ADV_AKIMA) akima_advection(M, kind, buff);
+  else hsu_advection(M, kind, buff);
+}
 static void advection(ep_model *M) {
   int K, J, I;
   for (K = 0; K <= KHI + 1; K++)
     for (J = 0; J <= NJ; J++)
       for (I = 0; I <= NI + 1; I++) A3(M->unity, K, J, I) = 1.;
-  hsu_advection(M, IDX_OTHER, M->unity);
+  advect(M, IDX_OTHER, M->unity);
   for (K = M->g.k_sigma - 1; K <= KHI + 1; K++)
     for (J = 0; J <= NJ; J++)
       for (I = 0; I <= NI + 1; I++) A3(M->old, K, J, I) = A3(M->theta, K, J, I);
-  hsu_advection(M, IDX_THETA, M->theta);
+  advect(M, IDX_THETA, M->theta);
   for (K = M->g.k_sigma - 1; K <= KHI + 1; K++)
     for (J = 0; J <= NJ; J++)
       for (I = 0; I <= NI + 1; I++) A3(M->theta, K, J, I) -= A3(M->old, K, J, I) * (A3(M->unity, K, J, I) - 1.);
-  hsu_advection(M, IDX_HDRY, M->hdry);
+  advect(M, IDX_HDRY, M->hdry);
   restore_mass(M);
   set_p2etc(M, 0);
 }

@@ -53,7 +53,8 @@ int ref_init(const epic_grid *g, const epic_fields *f) {
   strcpy(grid.uv_timestep_scheme, g->uv_scheme == EPIC_UV_AB3 ? "3rd-order Adams-Bashforth" : "Leapfrog (Asselin filtered)");
   strcpy(grid.turbulence_scheme, "off");
   strcpy(grid.eos, "ideal");
-  strcpy(grid.advection_scheme, "Predictor-corrector (Hsu, Konor, and Arakawa)");
+  strcpy(grid.advection_scheme, g->advection_scheme == EPIC_ADV_AKIMA ? "Monotonized, 4th-order centered (Akima)"
+                                                                      : "Predictor-corrector (Hsu, Konor, and Arakawa)");
   strcpy(var.theta.advection_scheme, grid.advection_scheme);
   strcpy(var.hdry.advection_scheme, grid.advection_scheme);
   grid.nk = g->nk; grid.nj = g->nj; grid.ni = g->ni; grid.dt = g->dt;

@@ -5,7 +5,7 @@ Each fixture holds the inputs (grid scalars and arrays, the initial state) and t
 state after timestep(SYNC_DIAGS_ONLY) and after a number of timestep(STEP_PROGS_AND_SYNC_DIAGS)
 calls, computed by oracle/_ref/libepicref.so (the reference's own sources, driven in-process).
 
-    python tests/golden/make_golden.py
+    python tests/golden/make_golden.py [case ...]     (all cases when none is named)
 """
 import os
 import sys
@@ -16,7 +16,7 @@ HERE = os.path.dirname(os.path.abspath(__file__))
 sys.path.insert(0, os.path.dirname(HERE))
 sys.path.insert(0, os.path.dirname(os.path.dirname(HERE)))
 
-from epic_gb300 import EPIC_UV_AB3, EPIC_UV_LEAPFROG, HSConfig, hs_setup  # noqa: E402
+from epic_gb300 import EPIC_ADV_AKIMA, EPIC_UV_AB3, EPIC_UV_LEAPFROG, HSConfig, hs_setup  # noqa: E402
 from oracle_lib import reference_available, run_reference, fields_to_dict  # noqa: E402
 
 SAVED = ("u", "v", "hdry", "theta", "p3", "gz3", "pv3", "w3", "heat3", "div_uv3")
@@ -24,6 +24,8 @@ CASES = {
     "hs32x16x10_ab3": (HSConfig(ni=32, nj=16, nk=10, dt=300, uv_scheme=EPIC_UV_AB3, seed=11), [("sync", 0), ("step", 1), ("step", 4)]),
     "hs32x16x10_leapfrog": (HSConfig(ni=32, nj=16, nk=10, dt=300, uv_scheme=EPIC_UV_LEAPFROG, seed=12), [("sync", 0), ("step", 1), ("step", 2)]),
     "hs16x8x12_ab3": (HSConfig(ni=16, nj=8, nk=12, dt=600, uv_scheme=EPIC_UV_AB3, seed=13), [("sync", 0), ("step", 3)]),
+    "hs32x16x10_ab3_akima": (HSConfig(ni=32, nj=16, nk=10, dt=300, uv_scheme=EPIC_UV_AB3, seed=14, advection_scheme=EPIC_ADV_AKIMA),
+                             [("sync", 0), ("step", 1), ("step", 4)]),
 }
 
 
@@ -57,5 +59,5 @@ def make(name, cfg, schedule):
 if __name__ == "__main__":
     if not reference_available():
         sys.exit("the reference source tree is needed to generate the fixtures")
-    for name, (cfg, sched) in CASES.items():
-        make(name, cfg, sched)
+    for name in sys.argv[1:] or CASES:
+        make(name, *CASES[name])

@@ -3,15 +3,15 @@ exactly the bits it gets when stepped alone, in both precision forms."""
 import numpy as np
 import pytest
 
-from epic_gb300 import (EPIC_PREC_FP64, EPIC_PREC_MIXED, EPIC_PREC_MIXED_FAST, EPIC_SYNC_DIAGS_ONLY, EPIC_UV_AB3, EPIC_UV_LEAPFROG, Batch,
+from epic_gb300 import (EPIC_ADV_AKIMA, EPIC_PREC_FP64, EPIC_PREC_MIXED, EPIC_PREC_MIXED_FAST, EPIC_SYNC_DIAGS_ONLY, EPIC_UV_AB3, EPIC_UV_LEAPFROG, Batch,
                         EpicError, HSConfig, Model, hs_setup)
 
 pytestmark = pytest.mark.gpu
 
 
-def _member(seed, kf_scale, precision, shape=(32, 16, 10), scheme=EPIC_UV_AB3):
+def _member(seed, kf_scale, precision, shape=(32, 16, 10), scheme=EPIC_UV_AB3, adv=0):
     ni, nj, nk = shape
-    ga, f = hs_setup(HSConfig(ni=ni, nj=nj, nk=nk, dt=300, seed=seed, uv_scheme=scheme))
+    ga, f = hs_setup(HSConfig(ni=ni, nj=nj, nk=nk, dt=300, seed=seed, uv_scheme=scheme, advection_scheme=adv))
     ga.struct.hs_kf *= kf_scale
     m = Model(ga, precision)
     m.upload(f)
@@ -21,9 +21,10 @@ def _member(seed, kf_scale, precision, shape=(32, 16, 10), scheme=EPIC_UV_AB3):
 @pytest.mark.parametrize("precision,scheme", [(EPIC_PREC_FP64, EPIC_UV_AB3), (EPIC_PREC_MIXED, EPIC_UV_AB3),
                                               (EPIC_PREC_MIXED_FAST, EPIC_UV_AB3), (EPIC_PREC_FP64, EPIC_UV_LEAPFROG),
                                               (EPIC_PREC_MIXED, EPIC_UV_LEAPFROG), (EPIC_PREC_MIXED_FAST, EPIC_UV_LEAPFROG)])
-def test_batch_equals_members_alone(gpu, precision, scheme):
+@pytest.mark.parametrize("adv", [0, EPIC_ADV_AKIMA])
+def test_batch_equals_members_alone(gpu, precision, scheme, adv):
     scales = [1.0, 0.93, 1.07, 1.1, 0.9]
-    members = [_member(10 + q, s, precision, scheme=scheme) for q, s in enumerate(scales)]
+    members = [_member(10 + q, s, precision, scheme=scheme, adv=adv) for q, s in enumerate(scales)]
     batch = Batch([m for _, _, m in members])
     batch.timestep(EPIC_SYNC_DIAGS_ONLY)
     batch.run(7)

@@ -29,8 +29,8 @@ import numpy as np
 import pytest
 
 from compare import PROGNOSTIC, field_errors
-from epic_gb300 import (EPIC_PREC_FP64, EPIC_PREC_MIXED, EPIC_PREC_MIXED_FAST, EPIC_SYNC_DIAGS_ONLY, EPIC_UV_LEAPFROG,
-                        HSConfig, Model, hs_setup)
+from epic_gb300 import (EPIC_ADV_AKIMA, EPIC_ADV_HSU, EPIC_PREC_FP64, EPIC_PREC_MIXED, EPIC_PREC_MIXED_FAST,
+                        EPIC_SYNC_DIAGS_ONLY, EPIC_UV_LEAPFROG, HSConfig, Model, hs_setup)
 
 pytestmark = pytest.mark.gpu
 DAY = 288   # steps of 300 s
@@ -135,3 +135,16 @@ def test_models_of_different_sizes_coexist(gpu):
         m.timestep(EPIC_SYNC_DIAGS_ONLY)
         m.run(2)
         m.sync()
+
+
+@pytest.mark.parametrize("form", FORMS)
+def test_akima_one_day_after_spin_up(spun_up, form):
+    """The Akima advection scheme, one day from the spun-up state (the state's winds and mass
+    come from the Hsu-scheme spin-up; the day is stepped with Akima in both forms)."""
+    ga, f = spun_up
+    ga.struct.advection_scheme = EPIC_ADV_AKIMA
+    try:
+        a, b = _pair(ga, f, False, FORMS[form])
+    finally:
+        ga.struct.advection_scheme = EPIC_ADV_HSU
+    _check(_run(a, b, DAY), BOUNDS[(form, "spun_up")])

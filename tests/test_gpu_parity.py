@@ -6,13 +6,15 @@ with the host glibc, which reproduces the reference build bit for bit).  Kernel 
 GPU evaluates the reference's expressions in the reference's order without FMA contraction,
 with correctly rounded log/exp/pow and a bit-exact restatement of realft, so every stage and
 every step must equal the restatement compiled with the same correctly rounded functions
-(oracle libepicport_cr.so) bit for bit.
+(oracle libepicport_cr.so) bit for bit.  Both advection schemes (Hsu-Konor-Arakawa, Akima) are
+covered.
 """
 import numpy as np
 import pytest
 
 from compare import DIAGNOSTIC, PROGNOSTIC, field_errors, worst
-from epic_gb300 import EPIC_SYNC_DIAGS_ONLY, EPIC_UV_AB3, EPIC_UV_LEAPFROG, HSConfig, Model, hs_setup
+from epic_gb300 import (EPIC_ADV_AKIMA, EPIC_ADV_HSU, EPIC_SYNC_DIAGS_ONLY, EPIC_UV_AB3, EPIC_UV_LEAPFROG, HSConfig, Model,
+                        hs_setup)
 from oracle_lib import Port
 
 pytestmark = pytest.mark.gpu
@@ -47,11 +49,12 @@ def _differing(a, b):
     return {k: int((a.arrays[k] != b.arrays[k]).sum()) for k in a.arrays if not np.array_equal(a.arrays[k], b.arrays[k])}
 
 
+@pytest.mark.parametrize("adv", [EPIC_ADV_HSU, EPIC_ADV_AKIMA])
 @pytest.mark.parametrize("scheme", [EPIC_UV_AB3, EPIC_UV_LEAPFROG])
-def test_stage_by_stage(gpu, scheme):
+def test_stage_by_stage(gpu, scheme, adv):
     """Each reference function on the path, GPU vs the correctly rounded restatement, bit for
     bit, from the same spun-up state."""
-    cfg = HSConfig(ni=32, nj=16, nk=10, dt=300, uv_scheme=scheme, seed=3)
+    cfg = HSConfig(ni=32, nj=16, nk=10, dt=300, uv_scheme=scheme, seed=3, advection_scheme=adv)
     ga, f = _spin_up(cfg, 4)
     port = Port(ga, cr_libm=True)
     port.upload(f)
@@ -71,10 +74,11 @@ def test_stage_by_stage(gpu, scheme):
     assert not failures, "\n".join(failures)
 
 
+@pytest.mark.parametrize("adv", [EPIC_ADV_HSU, EPIC_ADV_AKIMA])
 @pytest.mark.parametrize("scheme", [EPIC_UV_AB3, EPIC_UV_LEAPFROG])
-def test_steps_bitwise(gpu, scheme):
+def test_steps_bitwise(gpu, scheme, adv):
     """Ten graph-replayed steps at 64x32x20 equal the correctly rounded restatement bit for bit."""
-    cfg = HSConfig(ni=64, nj=32, nk=20, dt=300, uv_scheme=scheme, seed=9)
+    cfg = HSConfig(ni=64, nj=32, nk=20, dt=300, uv_scheme=scheme, seed=9, advection_scheme=adv)
     ga, f, port, model = _pair(cfg, cr_libm=True)
     port.timestep(EPIC_SYNC_DIAGS_ONLY)
     port.run(10)
@@ -96,11 +100,12 @@ def test_sync_diags(gpu):
     assert not bad, bad
 
 
-@pytest.mark.parametrize("scheme,nsteps,tol", [(EPIC_UV_AB3, 1, 1e-11), (EPIC_UV_LEAPFROG, 1, 1e-11),
-                                                (EPIC_UV_AB3, 100, 1e-8)])
-def test_full_step(gpu, scheme, nsteps, tol):
+@pytest.mark.parametrize("scheme,nsteps,tol,adv", [(EPIC_UV_AB3, 1, 1e-11, EPIC_ADV_HSU), (EPIC_UV_LEAPFROG, 1, 1e-11, EPIC_ADV_HSU),
+                                                    (EPIC_UV_AB3, 100, 1e-8, EPIC_ADV_HSU), (EPIC_UV_AB3, 1, 1e-11, EPIC_ADV_AKIMA),
+                                                    (EPIC_UV_AB3, 100, 1e-8, EPIC_ADV_AKIMA)])
+def test_full_step(gpu, scheme, nsteps, tol, adv):
     """The 64x32x10 Held-Suarez configuration: per-prognostic relative L2 after nsteps."""
-    cfg = HSConfig(ni=64, nj=32, nk=10, dt=300, uv_scheme=scheme)
+    cfg = HSConfig(ni=64, nj=32, nk=10, dt=300, uv_scheme=scheme, advection_scheme=adv)
     ga, f, port, model = _pair(cfg)
     port.timestep(EPIC_SYNC_DIAGS_ONLY)
     port.run(nsteps)

@@ -14,7 +14,8 @@ import numpy as np
 import pytest
 
 from compare import PROGNOSTIC, field_errors
-from epic_gb300 import EPIC_SYNC_DIAGS_ONLY, EPIC_UV_AB3, EPIC_UV_LEAPFROG, Fields, GridArrays, HSConfig, hs_setup
+from epic_gb300 import (EPIC_ADV_AKIMA, EPIC_ADV_HSU, EPIC_SYNC_DIAGS_ONLY, EPIC_UV_AB3, EPIC_UV_LEAPFROG, Fields, GridArrays,
+                        HSConfig, hs_setup)
 from oracle_lib import Port, dict_to_fields, fields_to_dict, reference_available, run_reference
 
 GOLDEN = sorted(glob.glob(os.path.join(os.path.dirname(__file__), "golden", "*.npz")))
@@ -104,13 +105,16 @@ def test_golden_inputs_match_generator():
 
 
 @pytest.mark.reference
-@pytest.mark.parametrize("scheme,shape,steps", [(EPIC_UV_AB3, (64, 32, 10), 12), (EPIC_UV_LEAPFROG, (32, 16, 10), 6),
-                                                 (EPIC_UV_AB3, (32, 16, 20), 4)])
-def test_restatement_matches_reference(scheme, shape, steps):
+@pytest.mark.parametrize("scheme,shape,steps,adv", [(EPIC_UV_AB3, (64, 32, 10), 12, EPIC_ADV_HSU),
+                                                     (EPIC_UV_LEAPFROG, (32, 16, 10), 6, EPIC_ADV_HSU),
+                                                     (EPIC_UV_AB3, (32, 16, 20), 4, EPIC_ADV_HSU),
+                                                     (EPIC_UV_AB3, (64, 32, 10), 12, EPIC_ADV_AKIMA),
+                                                     (EPIC_UV_LEAPFROG, (32, 16, 10), 6, EPIC_ADV_AKIMA)])
+def test_restatement_matches_reference(scheme, shape, steps, adv):
     if not reference_available():
         pytest.skip("reference source tree not present on this host")
     ni, nj, nk = shape
-    cfg = HSConfig(ni=ni, nj=nj, nk=nk, dt=300, uv_scheme=scheme, seed=5)
+    cfg = HSConfig(ni=ni, nj=nj, nk=nk, dt=300, uv_scheme=scheme, seed=5, advection_scheme=adv)
     ga, f = hs_setup(cfg)
     sched = [("sync", 0)] + [("step", 1)] * steps
     geo, snaps = run_reference(ga, f, sched)
@@ -145,3 +149,19 @@ def test_libm_rounding_floor_at_64x32x10(seed):
         out.append(p.download())
     errs = field_errors(out[1], out[0], PROGNOSTIC)
     assert all(v[0] <= 1e-11 for v in errs.values()), errs
+
+
+def test_akima_fixture_differs_from_hsu():
+    """The Akima fixture's first step is not what the Hsu scheme gives from the same inputs, so
+    the fixture (and every parity test that sets advection_scheme) exercises the Akima path."""
+    z = np.load(os.path.join(os.path.dirname(__file__), "golden", "hs32x16x10_ab3_akima.npz"))
+    ga = grid_from_fixture(z)
+    assert ga.struct.advection_scheme == EPIC_ADV_AKIMA
+    ga.struct.advection_scheme = EPIC_ADV_HSU
+    port = Port(ga)
+    port.upload(inputs_from_fixture(z, ga))
+    port.timestep(EPIC_SYNC_DIAGS_ONLY)
+    port.run(1)
+    got = port.download()
+    for k in ("hdry", "theta"):
+        assert not np.array_equal(got.arrays[k], z["step1_" + k]), k
