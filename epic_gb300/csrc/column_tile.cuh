@@ -40,10 +40,11 @@ __device__ __forceinline__ ColTile col_tile(const DevModel &M) {
 // f_sigma/g_sigma (epic_funcs_diag.c:1271-1314) in the compute type, one exponential for both
 template <class R>
 __device__ __forceinline__ R f_and_g_sigma_r(const DevModel &M, R s, R &g) {
-  const R ss = cv<R>(M.sigma_sigma), z0 = cv<R>(M.zeta0), z1 = cv<R>(M.zeta1);
+  const R ss = mconst<R>(M, DFC_SIGMA_SIGMA, M.sigma_sigma), z0 = mconst<R>(M, DFC_ZETA0, M.zeta0),
+          z1 = mconst<R>(M, DFC_ZETA1, M.zeta1);
   if (s <= ss) g = R(0.);
   else if (s >= R(1.)) g = R(1.);
-  else g = cv<R>(M.g_coeff) * (R(1.) - RMath<R>::exp(M, -cv<R>(M.alpha) * (s - ss)));
+  else g = mconst<R>(M, DFC_G_COEFF, M.g_coeff) * (R(1.) - RMath<R>::exp(M, -mconst<R>(M, DFC_ALPHA, M.alpha) * (s - ss)));
   if (s < R(0.)) return z0;
   if (s <= ss) return z0 + s * (z1 - z0);
   if (s < R(1.)) return (R(1.) - g) * (z0 + s * (z1 - z0));

@@ -34,6 +34,10 @@ struct Ctl {
 
 enum ErrCode { ERR_NONE = 0, ERR_GZ_MONOTONE = 1, ERR_CALC_W_P = 2, ERR_PCHIP_X = 3, ERR_NONFINITE = 4, ERR_TIMEOUT = 5 };
 
+// double-float constants of the mixed form (DevModel::dfc), split on the host
+enum { DFC_KAPPA, DFC_KAPPA_INV, DFC_KAPPA1, DFC_SIGMA_SIGMA, DFC_ZETA0, DFC_ZETA1, DFC_G_COEFF, DFC_ALPHA, DFC_LOG_P0,
+       DFC_COUNT };
+
 struct DevModel {
   // sizes
   int ni, nj, nk, iadim, jadim, kadim;
@@ -58,6 +62,8 @@ struct DevModel {
   const float *twf;                         // the twiddles rounded to float (mixed form)
   const float *fkern_h, *fkern_v;           // circulant filter kernels per row (mixed form, tensor-core filter)
   const float2 *exp2tab;                    // 2^(j/32), j = 0..31, as double-floats (exp_df)
+  float2 dfc[DFC_COUNT];                    // kappa, 1/kappa, kappa+1, the hybrid-coordinate constants
+                                            // and log(press0) as double-floats (hi, lo)
   int mixed;                                // FP32 stencils, advection, hyperviscosity, filter, physics
   int col64;                                // mixed, with the vertical pressure/geopotential integration
                                             // (set_p2etc, store_pgrad_vars) and the pressure gradient in FP64
@@ -68,6 +74,9 @@ struct DevModel {
   double *gz3, *mont3, *heat3, *pv3, *ri2, *div_uv3, *w3, *dzdt3, *u_spinup, *gz_surface;
   // scratch
   double *gz, *unity, *old, *work0, *work1, *work2, *work3, *ptable;
+  float2 *lp3;   // log P3 at every interface as a double-float: written by set_p2etc of the mixed
+                 // form (stage 11), read by its store_pgrad_vars (stage 19); P3 does not change
+                 // between the two
   Ctl *ctl;
   // batch: the members' descriptions on the device (nullptr for a single model); kernels
   // launched over a batch take member blockIdx.z's description on entry (EPIC_MEMBER)
@@ -197,6 +206,10 @@ template <> __device__ __forceinline__ dfl cv<dfl>(double x) {
   const float h = d2f(x);
   return dfl(h, d2f(x - f2d(h)));
 }
+// a model constant in the compute type: the double-float ones come split from the host (the
+// same bits as cv<dfl> of the binary64 value), the others by cv
+template <class R> __device__ __forceinline__ R mconst(const DevModel &, int, double v) { return cv<R>(v); }
+template <> __device__ __forceinline__ dfl mconst<dfl>(const DevModel &M, int q, double) { return dfl(M.dfc[q].x, M.dfc[q].y); }
 __device__ __forceinline__ double to_d(double x) { return x; }
 __device__ __forceinline__ double to_d(float x) { return f2d(x); }
 __device__ __forceinline__ double to_d(dfl x) { return f2d(x.hi) + f2d(x.lo); }

@@ -289,7 +289,7 @@ size_t model_pool_bytes(const epic_grid &g) {
   const size_t n3 = (size_t)L.n3, n2 = (size_t)L.n2;
   const size_t nvp = g.uv_scheme == EPIC_UV_AB3 ? 1 : 2, ntp = g.uv_scheme == EPIC_UV_AB3 ? 3 : 1;
   const size_t n_state3 = 2 * nvp + 2 * ntp + 20;   // u,v planes + tendencies + 20 single fields
-  const size_t n_scratch3 = 7;                      // gz, unity, old, work0..3
+  const size_t n_scratch3 = 8;                      // gz, unity, old, work0..3, lp3 (float2)
   const size_t nj1 = 2 * (g.nj + 1) + 1, ni1 = 2 * (g.ni + 1) + 1, nk1 = 2 * (g.nk + 1) + 1;
   const size_t ntw = epic::twiddle_doubles(g.ni);
   auto rnd = [](size_t b) { return ((b + 255) / 256) * 256; };
@@ -353,6 +353,18 @@ extern "C" int epic_model_create(const epic_grid *g, int32_t precision, epic_mod
   d.mixed = precision != EPIC_PREC_FP64;
   d.col64 = precision == EPIC_PREC_MIXED;
   d.cr = precision == EPIC_PREC_FP64;
+  {
+    auto split = [](double v) { return make_float2((float)v, (float)(v - (double)(float)v)); };
+    d.dfc[epic::DFC_KAPPA] = split(d.kappa);
+    d.dfc[epic::DFC_KAPPA_INV] = split(1. / d.kappa);
+    d.dfc[epic::DFC_KAPPA1] = split(d.kappa + 1.);
+    d.dfc[epic::DFC_SIGMA_SIGMA] = split(d.sigma_sigma);
+    d.dfc[epic::DFC_ZETA0] = split(d.zeta0);
+    d.dfc[epic::DFC_ZETA1] = split(d.zeta1);
+    d.dfc[epic::DFC_G_COEFF] = split(d.g_coeff);
+    d.dfc[epic::DFC_ALPHA] = split(d.alpha);
+    d.dfc[epic::DFC_LOG_P0] = split(std::log(d.press0));
+  }
 
   HostTables T;
   filter_tables(*g, L, T);
@@ -392,6 +404,7 @@ extern "C" int epic_model_create(const epic_grid *g, int32_t precision, epic_mod
   p += (256 - ((size_t)(p - m->pool) & 255)) & 255;   // the scratch and tables start 256-aligned
   double **s3[] = {&d.gz, &d.unity, &d.old, &d.work0, &d.work1, &d.work2, &d.work3};
   for (double **q : s3) *q = carve<double>(p, n3);
+  d.lp3 = carve<float2>(p, n3);
   d.gz_surface = carve<double>(p, n2);
   double *hlh = carve<double>(p, n2), *hlpv = carve<double>(p, n2);
   d.ptable = carve<double>(p, (size_t)(g->nj + 3) * (g->nk + 2) * 3);

@@ -598,7 +598,9 @@ __device__ __forceinline__ double layer_p_mixed(const DevModel &M, double top, d
   return bot * f2d(expf(log1pf(q - 1.f) / kap));
 }
 
-__global__ void __launch_bounds__(CT_THREADS, 3) k_set_p2etc_mixed(DevModel M, int update_theta) {
+// layers = 0: P3 and HDRY only (the call inside advection, whose P2 and H3 stage 11 rewrites
+// before anything reads them)
+__global__ void __launch_bounds__(CT_THREADS, 3) k_set_p2etc_mixed(DevModel M, int update_theta, int layers) {
   epic_member(M);
   extern __shared__ double sm[];
   __shared__ double s_lp[32], s_ginv[32];
@@ -670,7 +672,7 @@ __global__ void __launch_bounds__(CT_THREADS, 3) k_set_p2etc_mixed(DevModel M, i
       }
     }
   __syncthreads();
-  if (!c.valid) return;
+  if (!c.valid || !layers) return;
   for (int k = 1 + c.warp; k <= nk; k += CT_WARPS) {
     const long long x = c.base + k * n2;
     const double top = CT(P, k - 1), bot = CT(P, k);
@@ -716,6 +718,10 @@ __global__ void __launch_bounds__(CT_THREADS, 3) k_set_p2etc_mixed(DevModel M, i
   }
 }
 
+// FULL = false: GZ3 alone (and its monotonicity check), for the call before the filtered-GZ
+// copy; that call's T3, EXNER3, RHO3, T2, RHO2, MONT3 and DZDT3 are rewritten by the call after
+// set_p2etc (stage 19) before anything reads them, and that call reads this GZ3 as the old one.
+template <bool FULL>
 __global__ void __launch_bounds__(CT_THREADS, 3) k_pgrad_vars_column_mixed(DevModel M) {
   epic_member(M);
   extern __shared__ double sm[];
@@ -737,13 +743,14 @@ __global__ void __launch_bounds__(CT_THREADS, 3) k_pgrad_vars_column_mixed(DevMo
       const float pf = powf(d2f(p) * p0_inv, kap);
       const float t3f = d2f(theta) * pf;
       const double t3 = f2d(t3f);
-      M.t3[x] = t3;
-      M.exner3[x] = f2d(cpf * pf);
       const double rho = f2d(d2f(p) * mu_over_r / t3f);
-      M.rho3[x] = rho;
       CT(P, k) = p;
       CT(R, k) = rho;
       CT(T3, k) = t3;
+      if (!FULL) return;
+      M.t3[x] = t3;
+      M.exner3[x] = f2d(cpf * pf);
+      M.rho3[x] = rho;
       if (k >= 1) {
         const float t2f = d2f(th2) * powf(d2f(pr) * p0_inv, kap);
         M.t2[x] = f2d(t2f);
@@ -759,20 +766,22 @@ __global__ void __launch_bounds__(CT_THREADS, 3) k_pgrad_vars_column_mixed(DevMo
 #pragma unroll
     for (int r = 0; r < TILE_SLOTS; r++) {
       const long long x = c.base + min(c.warp + r * CT_WARPS, nk) * n2;
-      v[r][0] = __ldg(M.theta + x); v[r][1] = __ldg(M.p3 + x); v[r][2] = __ldg(M.p2 + x); v[r][3] = __ldg(M.theta2 + x);
+      v[r][0] = __ldg(M.theta + x); v[r][1] = __ldg(M.p3 + x);
+      if (FULL) { v[r][2] = __ldg(M.p2 + x); v[r][3] = __ldg(M.theta2 + x); }
+      else v[r][2] = v[r][3] = 0.;
     }
 #pragma unroll
     for (int r = 0; r < TILE_SLOTS; r++)
       if (c.warp + r * CT_WARPS <= nk) level(c.warp + r * CT_WARPS, v[r][0], v[r][1], v[r][2], v[r][3]);
     for (int k = c.warp + TILE_SLOTS * CT_WARPS; k <= nk; k += CT_WARPS) {
       const long long x = c.base + k * n2;
-      level(k, M.theta[x], M.p3[x], M.p2[x], M.theta2[x]);
+      level(k, M.theta[x], M.p3[x], FULL ? M.p2[x] : 0., FULL ? M.theta2[x] : 0.);
     }
   }
   __syncthreads();
   if (c.valid) {
     for (int k = c.warp; k < nk; k += CT_WARPS) CT(LG, k) = log_ratio_f(CT(P, k), CT(P, k + 1));
-    if (c.warp == CT_WARPS - 1) {
+    if (FULL && c.warp == CT_WARPS - 1) {
       M.rho2[c.base] = CT(R, 0) * CT(R, 0) / s_rho2_1[c.lane];
       M.theta2[c.base] = M.sgth[0];
       M.t2[c.base] = CT(T3, 0);
@@ -813,6 +822,14 @@ __global__ void __launch_bounds__(CT_THREADS, 3) k_pgrad_vars_column_mixed(DevMo
   // the FP64 change of GZ3 (the difference itself stays FP64: it cancels)
   const float dtg_inv = -1.f / (d2f(M.dt) * d2f(M.grav[2 * c.j + 1]));
   const float cprf = d2f(M.cpr), rgasf = d2f(M.rgas);
+  if (!FULL) {
+    for (int k = c.warp; k <= nk; k += CT_WARPS) {
+      const double gzk = CT(GZ, k);
+      M.gz3[c.base + k * n2] = gzk;
+      if (interior && k >= 1 && gzk >= CT(GZ, k - 1)) flag_error(M.ctl, ERR_GZ_MONOTONE, k, c.j, c.i, gzk);
+    }
+    return;
+  }
   auto level_out = [&](int k, double old, double w, double h) {
     const long long x = c.base + k * n2;
     const double gzk = CT(GZ, k);
@@ -965,14 +982,18 @@ int launch_restore_mass(const DevModel &M, cudaStream_t s) {
   return 0;
 }
 int launch_set_p2etc(const DevModel &M, int update_theta, cudaStream_t s, bool feeds_pgrad) {
-  if (M.col64 && feeds_pgrad) k_set_p2etc_acc<<<zg(ntile_blocks(M), M), CT_THREADS, tile_smem(M, 3), s>>>(M, update_theta);
-  else if (M.mixed) k_set_p2etc_mixed<<<zg(ntile_blocks(M), M), CT_THREADS, tile_smem(M, 3), s>>>(M, update_theta);
+  if (M.col64 && feeds_pgrad) k_set_p2etc_acc<<<zg(ntile_blocks(M), M), CT_THREADS, tile_smem(M, 4), s>>>(M, update_theta);
+  else if (M.mixed) k_set_p2etc_mixed<<<zg(ntile_blocks(M), M), CT_THREADS, tile_smem(M, 3), s>>>(M, update_theta, feeds_pgrad);
   else k_set_p2etc<<<zg(ntile_blocks(M), M), CT_THREADS, tile_smem(M, 4), s>>>(M, update_theta);
   return 0;
 }
 int launch_store_pgrad_vars(const DevModel &M, cudaStream_t s, bool feeds_pgrad) {
-  if (M.col64 && feeds_pgrad) k_pgrad_vars_column_acc<<<zg(ntile_blocks(M), M), CT_THREADS, tile_smem(M, 5), s>>>(M);
-  else if (M.mixed) k_pgrad_vars_column_mixed<<<zg(ntile_blocks(M), M), CT_THREADS, tile_smem(M, 5), s>>>(M);
+  if (M.mixed && !feeds_pgrad) {   // GZ3 alone: no DZDT3, so no horizontal part either
+    k_pgrad_vars_column_mixed<false><<<zg(ntile_blocks(M), M), CT_THREADS, tile_smem(M, 5), s>>>(M);
+    return 0;
+  }
+  if (M.col64) k_pgrad_vars_column_acc<<<zg(ntile_blocks(M), M), CT_THREADS, tile_smem(M, 5), s>>>(M);
+  else if (M.mixed) k_pgrad_vars_column_mixed<true><<<zg(ntile_blocks(M), M), CT_THREADS, tile_smem(M, 5), s>>>(M);
   else k_pgrad_vars_column<<<zg(ntile_blocks(M), M), CT_THREADS, tile_smem(M, 5), s>>>(M);
   EPIC_LAUNCH_R(M.mixed, k_pgrad_dzdt, epic_blocks((long long)M.nk * (M.nj + 1) * M.ni, TB(M, TB_UPDATE)), TB(M, TB_UPDATE), 0, s, M);
   return 0;
@@ -998,7 +1019,8 @@ int column_kernels_init(int) {
       cudaFuncSetAttribute(k_set_p2etc, cudaFuncAttributeMaxDynamicSharedMemorySize, big) != cudaSuccess ||
       cudaFuncSetAttribute(k_pgrad_vars_column, cudaFuncAttributeMaxDynamicSharedMemorySize, big) != cudaSuccess ||
       cudaFuncSetAttribute(k_set_p2etc_mixed, cudaFuncAttributeMaxDynamicSharedMemorySize, big) != cudaSuccess ||
-      cudaFuncSetAttribute(k_pgrad_vars_column_mixed, cudaFuncAttributeMaxDynamicSharedMemorySize, big) != cudaSuccess ||
+      cudaFuncSetAttribute(k_pgrad_vars_column_mixed<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, big) != cudaSuccess ||
+      cudaFuncSetAttribute(k_pgrad_vars_column_mixed<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, big) != cudaSuccess ||
       cudaFuncSetAttribute(k_hsu_vertical<double>, cudaFuncAttributeMaxDynamicSharedMemorySize, hv) != cudaSuccess ||
       cudaFuncSetAttribute(k_hsu_vertical<float>, cudaFuncAttributeMaxDynamicSharedMemorySize, hv) != cudaSuccess ||
       cudaFuncSetAttribute(k_akima_vertical<double>, cudaFuncAttributeMaxDynamicSharedMemorySize, hv) != cudaSuccess ||

@@ -24,22 +24,22 @@ namespace {
 __device__ __forceinline__ dfl one_df() { return dfl(1.f, 0.f); }
 
 // onto_kk(P2_INDEX) at a layer: bot * q^(1/kappa), q = (1 - r^(kappa+1)) / ((kappa+1)(1 - r)),
-// r = top/bot.  Layers thinner than 1e-7 relative take the reference's equal-pressure branch
-// (the mean differs from the formula by O(eps^2) there).
-__device__ __forceinline__ double layer_p_acc(const DevModel &M, double top, double bot) {
-  const dfl B = cv<dfl>(bot), T = cv<dfl>(top);
+// r = top/bot, with lr = log r given as the difference of the interfaces' logarithms (absolute
+// error ~1e-12, so P2 keeps ~1e-10 relative accuracy down to layers 1% thick -- 500 times
+// better than binary32).  Layers thinner than 1e-7 relative take the reference's
+// equal-pressure branch (the mean differs from the formula by O(eps^2) there).
+__device__ __forceinline__ double layer_p_acc(const DevModel &M, double top, double bot, dfl lr) {
+  const dfl B = cv<dfl>(bot);
   const dfl eps = cv<dfl>(bot - top) / B;
   if (!(eps.hi >= 1e-7f)) return .5 * (bot + top);
-  const dfl a = cv<dfl>(M.kappa + 1.);
-  const dfl lr = log_df(T / B, M.exp2tab);                     // log r < 0
+  const dfl a = mconst<dfl>(M, DFC_KAPPA1, 0.);
   const dfl q = (one_df() - exp_df(a * lr, M.exp2tab)) / (a * eps);
-  return to_d(B * exp_df(log_df(q, M.exp2tab) / cv<dfl>(M.kappa), M.exp2tab));
+  return to_d(B * exp_df(log_df(q, M.exp2tab) * mconst<dfl>(M, DFC_KAPPA_INV, 0.), M.exp2tab));
 }
 
-// theta on the hybrid surface sigmatheta = sg at pressure p (the inversion of
-// return_sigmatheta), sigma = log(p/pbot) / log(ptop/pbot)
-__device__ __forceinline__ double theta_acc(const DevModel &M, double sg, double p, dfl pbot, dfl lp) {
-  const dfl sigma = log_df(cv<dfl>(p) / pbot, M.exp2tab) / lp;
+// theta on the hybrid surface sigmatheta = sg at sigma = log(p/pbot) / log(ptop/pbot) (the
+// inversion of return_sigmatheta)
+__device__ __forceinline__ double theta_acc(const DevModel &M, double sg, dfl sigma) {
   dfl gs;
   const dfl fs = f_and_g_sigma_r<dfl>(M, sigma, gs);
   return to_d((cv<dfl>(sg) - fs) / gs);
@@ -47,7 +47,7 @@ __device__ __forceinline__ double theta_acc(const DevModel &M, double sg, double
 
 }  // namespace
 
-__global__ void __launch_bounds__(CT_THREADS, 2) k_set_p2etc_acc(DevModel M, int update_theta) {
+__global__ void __launch_bounds__(CT_THREADS, 3) k_set_p2etc_acc(DevModel M, int update_theta) {
   epic_member(M);
   extern __shared__ double sm[];
   __shared__ double s_lp[32], s_ginv[32];
@@ -55,6 +55,7 @@ __global__ void __launch_bounds__(CT_THREADS, 2) k_set_p2etc_acc(DevModel M, int
   const int nk = M.nk, ks = M.k_sigma, L = nk + 1;
   const long long n2 = M.n2;
   double *P = sm, *HL = P + 32 * L, *TH = HL + 32 * L;
+  float2 *LPS = reinterpret_cast<float2 *>(TH + 32 * L);   // log P3 per interface, double-float
   const double g = M.grav[2 * c.j + 1];
   if (c.valid) {
     double v[TILE_SLOTS][2];
@@ -94,10 +95,16 @@ __global__ void __launch_bounds__(CT_THREADS, 2) k_set_p2etc_acc(DevModel M, int
   if (!c.valid) return;
   const double ginv = s_ginv[c.lane];
   const float lpf = d2f(lp);
-  const dfl PB = cv<dfl>(pbot);
-  const dfl LP = log_df(cv<dfl>(ptop) / PB, M.exp2tab);
+  // the logarithms of the interface pressures, once per interface: the layer-mean pressure, the
+  // diagnosed theta here and T3 and the geopotential increments of store_pgrad_vars (lp3) take
+  // theirs from these
+  const dfl LPB = log_df(cv<dfl>(pbot), M.exp2tab);
+  const dfl LP = log_df(cv<dfl>(ptop), M.exp2tab) - LPB;   // log(ptop/pbot)
   for (int k = c.warp; k <= nk; k += CT_WARPS) {
     const double pk = CT(P, k);
+    const dfl lpk = k == nk ? LPB : log_df(cv<dfl>(pk), M.exp2tab);
+    CT(LPS, k) = make_float2(lpk.hi, lpk.lo);
+    M.lp3[c.base + k * n2] = make_float2(lpk.hi, lpk.lo);
     if (k >= 1) {
       const long long x = c.base + k * n2;
       M.p3[x] = pk;
@@ -109,7 +116,7 @@ __global__ void __launch_bounds__(CT_THREADS, 2) k_set_p2etc_acc(DevModel M, int
       M.hdry[x] = dmaxr(M.h_min[k], hl);
     }
     if (update_theta && k < ks - 1) {
-      const double th = theta_acc(M, M.sgth[2 * k + 1], pk, PB, LP);
+      const double th = theta_acc(M, M.sgth[2 * k + 1], (lpk - LPB) / LP);
       CT(TH, k) = th;
       M.theta[c.base + k * n2] = th;
     }
@@ -118,7 +125,8 @@ __global__ void __launch_bounds__(CT_THREADS, 2) k_set_p2etc_acc(DevModel M, int
   for (int k = 1 + c.warp; k <= nk; k += CT_WARPS) {
     const long long x = c.base + k * n2;
     const double top = CT(P, k - 1), bot = CT(P, k);
-    const double p2 = layer_p_acc(M, top, bot);
+    const float2 lt = CT(LPS, k - 1), lb = CT(LPS, k);
+    const double p2 = layer_p_acc(M, top, bot, dfl(lt.x, lt.y) - dfl(lb.x, lb.y));
     M.p2[x] = p2;
     if (k == 1) M.p2[c.base] = top * top / p2;
     double h;
@@ -160,7 +168,7 @@ __global__ void __launch_bounds__(CT_THREADS, 2) k_set_p2etc_acc(DevModel M, int
   }
 }
 
-__global__ void __launch_bounds__(CT_THREADS, 2) k_pgrad_vars_column_acc(DevModel M) {
+__global__ void __launch_bounds__(CT_THREADS, 3) k_pgrad_vars_column_acc(DevModel M) {
   epic_member(M);
   extern __shared__ double sm[];
   __shared__ double s_rho2_1[32];
@@ -169,15 +177,16 @@ __global__ void __launch_bounds__(CT_THREADS, 2) k_pgrad_vars_column_acc(DevMode
   const long long n2 = M.n2;
   double *P = sm, *R = P + 32 * L, *GZ = R + 32 * L;
   float2 *T3 = reinterpret_cast<float2 *>(GZ + 32 * L);   // T3, double-float
-  float2 *LG = T3 + 32 * L;                               // log of successive pressure ratios, double-float
+  float2 *LP = T3 + 32 * L;                               // log P3, double-float (set_p2etc's)
   const float2 *tab = M.exp2tab;
-  const dfl kap = cv<dfl>(M.kappa), p0_inv = cv<dfl>(1. / M.press0);
+  const dfl kap = mconst<dfl>(M, DFC_KAPPA, 0.), lp0 = mconst<dfl>(M, DFC_LOG_P0, 0.), p0_inv = cv<dfl>(1. / M.press0);
   const dfl mu_over_r = cv<dfl>(M.mu_dry / 8.314472e+3);   // return_density: p mu / (R T)
   const float cpf = d2f(M.cp);
-  auto level = [&](int k, double theta, double p, double pr, double th2) {
+  auto level = [&](int k, double theta, double p, double pr, double th2, float2 lpk) {
     const long long x = c.base + k * n2;
     const dfl Pk = cv<dfl>(p);
-    const dfl pi = exp_df(kap * log_df(Pk * p0_inv, tab), tab);   // (p/p0)^kappa
+    const dfl pi = exp_df(kap * (dfl(lpk.x, lpk.y) - lp0), tab);   // (p/p0)^kappa
+    CT(LP, k) = lpk;
     const dfl t3 = cv<dfl>(theta) * pi;
     const double t3d = to_d(t3);
     M.t3[x] = t3d;
@@ -197,33 +206,29 @@ __global__ void __launch_bounds__(CT_THREADS, 2) k_pgrad_vars_column_acc(DevMode
   };
   if (c.valid) {
     double v[TILE_SLOTS][4];
+    float2 vl[TILE_SLOTS];
 #pragma unroll
     for (int r = 0; r < TILE_SLOTS; r++) {
       const long long x = c.base + min(c.warp + r * CT_WARPS, nk) * n2;
       v[r][0] = __ldg(M.theta + x); v[r][1] = __ldg(M.p3 + x); v[r][2] = __ldg(M.p2 + x); v[r][3] = __ldg(M.theta2 + x);
+      vl[r] = M.lp3[x];
     }
 #pragma unroll
     for (int r = 0; r < TILE_SLOTS; r++)
-      if (c.warp + r * CT_WARPS <= nk) level(c.warp + r * CT_WARPS, v[r][0], v[r][1], v[r][2], v[r][3]);
+      if (c.warp + r * CT_WARPS <= nk) level(c.warp + r * CT_WARPS, v[r][0], v[r][1], v[r][2], v[r][3], vl[r]);
     for (int k = c.warp + TILE_SLOTS * CT_WARPS; k <= nk; k += CT_WARPS) {
       const long long x = c.base + k * n2;
-      level(k, M.theta[x], M.p3[x], M.p2[x], M.theta2[x]);
+      level(k, M.theta[x], M.p3[x], M.p2[x], M.theta2[x], M.lp3[x]);
     }
   }
   __syncthreads();
-  if (c.valid) {
-    for (int k = c.warp; k < nk; k += CT_WARPS) {
-      const dfl lg = log_df(cv<dfl>(CT(P, k + 1)) / cv<dfl>(CT(P, k)), tab);
-      CT(LG, k) = make_float2(lg.hi, lg.lo);
-    }
-    if (c.warp == CT_WARPS - 1) {
-      M.rho2[c.base] = CT(R, 0) * CT(R, 0) / s_rho2_1[c.lane];
-      M.theta2[c.base] = M.sgth[0];
-      M.t2[c.base] = f2d(CT(T3, 0).x) + f2d(CT(T3, 0).y);
-    }
+  if (c.valid && c.warp == CT_WARPS - 1) {
+    M.rho2[c.base] = CT(R, 0) * CT(R, 0) / s_rho2_1[c.lane];
+    M.theta2[c.base] = M.sgth[0];
+    M.t2[c.base] = f2d(CT(T3, 0).x) + f2d(CT(T3, 0).y);
   }
-  __syncthreads();
-  auto lgd = [&](int k) { const float2 v = CT(LG, k); return dfl(v.x, v.y); };
+  // log(P3(k+1)/P3(k)) as the difference of the interfaces' logarithms
+  auto lgd = [&](int k) { const float2 a = CT(LP, k + 1), b = CT(LP, k); return dfl(a.x, a.y) - dfl(b.x, b.y); };
   auto t3df = [&](int k) { const float2 v = CT(T3, k); return dfl(v.x, v.y); };
   const dfl r_over_mu = one_df() / mu_over_r;   // p/rho = R T / mu
   if (c.valid)

@@ -63,8 +63,10 @@ int launch_uv_drag(const DevModel &M, cudaStream_t s);
 int launch_hsu_vertical(const DevModel &M, double *buff, int kind, cudaStream_t s);
 int launch_restore_mass(const DevModel &M, cudaStream_t s);
 // feeds_pgrad: the call whose P2, THETA, GZ3 and RHO3 the pressure gradient reads (the mixed
-// form takes its double-float kernels there; elsewhere the FP32 ones, whose outputs are
-// recomputed before the pressure gradient reads them)
+// form takes its double-float kernels there).  feeds_pgrad = false marks the calls inside
+// advection (set_p2etc) and before the filtered-GZ copy (store_pgrad_vars): the mixed forms
+// write only what is read before stages 11 and 19 recompute the rest -- P3 and HDRY, and GZ3
+// (with its monotonicity check); the FP64 form writes everything, as the reference does.
 int launch_set_p2etc(const DevModel &M, int update_theta, cudaStream_t s, bool feeds_pgrad = true);
 int launch_store_pgrad_vars(const DevModel &M, cudaStream_t s, bool feeds_pgrad = true);
 int launch_gz_monotone(const DevModel &M, cudaStream_t s);
