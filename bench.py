@@ -344,6 +344,42 @@ def mixed_error(torch, precision, advection="hsu"):
     return out
 
 
+def ensemble_error(torch, precision, cfg, nmem=8, steps=288):
+    """The ensemble error at the member shape (where the tensor-core filter paths run): nmem
+    members (ensemble_rate's seeds and k_f perturbations) stepped one simulated day from rest as
+    a batch in the given form and in FP64.  Reported per prognostic: relative L2 of the ensemble
+    mean and of the ensemble spread (standard deviation over members) against FP64's, and the
+    largest per-member relative L2."""
+    import numpy as np
+    sys.path.insert(0, os.path.join(ROOT, "tests"))
+    from compare import PROGNOSTIC, field_errors
+    from epic_gb300 import EPIC_PREC_FP64, EPIC_SYNC_DIAGS_ONLY, Batch
+    runs = []
+    for prec in (EPIC_PREC_FP64, precision):
+        members = _members(cfg, nmem, prec, torch_seed=7)
+        b = Batch(members)
+        b.timestep(EPIC_SYNC_DIAGS_ONLY)
+        b.run(steps)
+        b.sync()
+        runs.append([m.download() for m in members])
+        b.close()
+        for m in members:
+            m.close()
+    ref, got = runs
+    out = {"mean": {}, "spread": {}, "member_max": {}}
+    for k in PROGNOSTIC:
+        a = np.stack([f.arrays[k] for f in got])
+        r = np.stack([f.arrays[k] for f in ref])
+        big = np.abs(r) > 1e300
+        a, r = np.where(big, 0., a), np.where(big, 0., r)
+        out["mean"][k] = float(np.linalg.norm(a.mean(0) - r.mean(0)) / np.linalg.norm(r.mean(0)))
+        out["spread"][k] = float(np.linalg.norm(a.std(0) - r.std(0)) / np.linalg.norm(r.std(0)))
+        out["member_max"][k] = max(field_errors(g, f, (k,))[k][0] for g, f in zip(got, ref))
+    out["case"] = (f"{nmem} members {cfg.ni}x{cfg.nj}x{cfg.nk}, dt={cfg.dt} s, {steps} steps from rest, batched, "
+                   f"relative L2 vs the FP64 members")
+    return out
+
+
 def serving_summary(precision, seed=3):
     """The serving loop on a seeded Poisson stream (20 requests/s, 40 requests)."""
     from epic_gb300.serving import RunServer, latency_summary, poisson_requests
@@ -499,10 +535,12 @@ def run_gpu_ensemble(args):
             out["batched_over_fp64_single"] = value / ws / fp64["value"]
             if precision != EPIC_PREC_FP64:
                 out["mixed_error"] = mixed_error(torch, precision, args.advection)
+                out["ensemble_error"] = ensemble_error(torch, precision, cfg)
             if args.precision == "mixed":
                 # the faster form that keeps the vertical integration and pressure gradient in FP32
                 fast = ensemble_rate(cfg, nmem, _prec("fast"), args, torch, rank)
                 out["mixed_fast"] = dict(fast, error=mixed_error(torch, _prec("fast"), args.advection),
+                                         ensemble_error=ensemble_error(torch, _prec("fast"), cfg),
                                          note="EPIC_PREC_MIXED_FAST ensemble, same workload and timing")
             out["serving"] = serving_summary(precision)
     if ws > 1:

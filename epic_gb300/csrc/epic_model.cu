@@ -183,9 +183,13 @@ int run_stage_on(const DevModel &M, cudaStream_t s, int stage) {
     case 7: launch_store_pgrad_vars(M, s, false); break;   // GZ3 for the filtered copy (stage 8)
     case 8:
       launch_copy_gz(M, s);
-      // binary64 in every form: the 3-D filter's profiles interpolate in the filtered GZ, and in
-      // FP32 the mixed form's V error after a day grows from 4e-5 to 7e-5 (leapfrog: 1.7e-4 -> 1.6e-3)
-      launch_filter_planes(M, M.gz, PL_NONE, M.gz, 0, M.nk, 0, s);
+      // The 3-D filter's profiles interpolate in the filtered GZ: filtering GZ itself in FP32
+      // makes the mixed form's V error after a day grow from 4e-5 to 7e-5 (leapfrog: 1.7e-4 ->
+      // 1.6e-3).  The mixed forms filter it on the tensor cores as GZ - GZ(i=1) per row (FP32
+      // rounding of the zonal variations only) where the operator product applies, the FP64 form
+      // in binary64.
+      if (M.mixed && filter_gemm_usable(M)) launch_filter_planes(M, M.gz, PL_NONE, M.gz, 0, M.nk, 0, s, 1, 1);
+      else launch_filter_planes(M, M.gz, PL_NONE, M.gz, 0, M.nk, 0, s);
       launch_gz_monotone(M, s);
       break;
     case 9:

@@ -296,20 +296,47 @@ __global__ void k_varz_tables(DevModel M, const double *buff, int sel, int index
   }
 }
 
+// The mixed forms' profile: var(gz) to binary64 accuracy as the knot value (binary64) plus the
+// cubic's increment from the knot (FP32 on the FP64 distance gz - x_knot), and the filtered
+// deviation added back to it in binary64 -- the field itself is never rounded to FP32 (a
+// rounding of THETA or HDRY on the filtered rows every step feeds the pressure gradient,
+// which amplifies it).  HDRY is interpolated in log space: knot value exp(y) (once per knot and
+// row) times 1 + expm1(increment).
+__device__ __forceinline__ double varz_profile_mixed(const DevModel &M, const Trip *t, const double *knot, int n, int index,
+                                                     double gzd) {
+  int kay;
+  if (gzd <= t[0].x) kay = 0;
+  else if (gzd >= t[n - 1].x) kay = n - 2;
+  else {
+    int il = -1, iu = n;
+    while (iu - il > 1) {
+      const int im = (iu + il) >> 1;
+      if (gzd >= t[im].x) il = im; else iu = im;
+    }
+    kay = il;
+  }
+  const Trip *tk = t + kay;
+  const float h = d2f(tk[1].x - tk[0].x);
+  const float delta = d2f(tk[1].y - tk[0].y) / h;
+  const float z0 = d2f(tk[0].z);
+  const float del1 = (z0 - delta) / h, del2 = (d2f(tk[1].z) - delta) / h;
+  const float c3 = (del1 + del2) / h, c2 = -(del1 + del1 + del2);
+  const float xx = d2f(gzd - tk[0].x);
+  const float inc = xx * (z0 + xx * (c2 + xx * c3));
+  return index == 2 ? knot[kay] + knot[kay] * f2d(expm1f(inc)) : tk[0].y + f2d(inc);
+}
+
 // The rest of the THREEDIM zonal_filter: subtract var(gz), filter, add it back.
 // Block = one row (k = kstart + blockIdx.y, j = jstart + blockIdx.x).
 template <class R>
 __global__ void k_varz_filter_rows(DevModel M, double *buff, int sel, int index, int kstart, int kend) {
   epic_member(M, buff);
   extern __shared__ __align__(16) unsigned char smraw[];
-  R *sm = reinterpret_cast<R *>(smraw);
   buff += plane_offset(M, sel);
   const int jstart = index == 1 ? 1 : 0;
   const int j = jstart + (int)blockIdx.x;
   const int k = kstart + (int)blockIdx.y;
   const int vgrid = index == 1;
-  R *x = sm, *vz = sm + (M.ni + 2);
-  FilterSmem<R> fs = carve_filter(sm + 2 * (M.ni + 2), M.ni);
   const Trip *t = reinterpret_cast<const Trip *>(M.ptable) + (long long)(j + 1) * (M.nk + 2);
   const int n = kend - kstart + 1;
   const double *gz = M.gz;
@@ -318,6 +345,34 @@ __global__ void k_varz_filter_rows(DevModel M, double *buff, int sel, int index,
   // The mixed forms leave unfiltered rows untouched (their subtract-and-add-back is the identity
   // up to one rounding); the FP64 form repeats the reference's arithmetic on them.
   if (!filt && !std::is_same_v<R, double>) return;
+  if constexpr (!std::is_same_v<R, double>) {
+    double *vzd = reinterpret_cast<double *>(smraw), *knot = vzd + (M.ni + 2);
+    R *x = reinterpret_cast<R *>(knot + (M.nk + 2));
+    FilterSmem<R> fs = carve_filter(x + (M.ni + 2), M.ni);
+    load_twiddles(M, fs);
+    if (index == 2)
+      for (int q = threadIdx.x; q < n; q += blockDim.x) knot[q] = ::exp(t[q].y);
+    __syncthreads();
+    for (int i = threadIdx.x + 1; i <= M.ni; i += blockDim.x) {
+      double gzd;
+      switch (index) {
+        case 0: gzd = .5 * (gz[M.at(k, j, i)] + gz[M.at(k, j, i - 1)]); break;
+        case 1: gzd = .5 * (gz[M.at(k, j, i)] + gz[M.at(k, j - 1, i)]); break;
+        case 2: gzd = .5 * (gz[M.at(k, j, i)] + gz[M.at(k - 1, j, i)]); break;
+        default: gzd = gz[M.at(k, j, i)]; break;
+      }
+      const double v = varz_profile_mixed(M, t, knot, n, index, gzd);
+      vzd[i] = v;
+      x[i] = d2f(buff[base + i] - v);
+    }
+    __syncthreads();
+    filter_row_smem(M, x, vgrid ? M.high_lat_pv : M.high_lat_h, M.at2(j, 0), fs);
+    for (int i = threadIdx.x + 1; i <= M.ni; i += blockDim.x) write_with_pads(buff, M, base, i, f2d(x[i]) + vzd[i]);
+    return;
+  }
+  R *sm = reinterpret_cast<R *>(smraw);
+  R *x = sm, *vz = sm + (M.ni + 2);
+  FilterSmem<R> fs = carve_filter(sm + 2 * (M.ni + 2), M.ni);
   if (filt) load_twiddles(M, fs);
   for (int i = threadIdx.x + 1; i <= M.ni; i += blockDim.x) {
     R gzz;
@@ -495,13 +550,13 @@ static int row_threads(const DevModel &M) { return M.tb[TB_ROW] > 0 ? M.tb[TB_RO
 static size_t relem(int fp32) { return fp32 ? sizeof(float) : sizeof(double); }
 
 int launch_filter_planes(const DevModel &M, const double *src, int src_sel, double *dst, int k0, int nplanes, int vgrid, cudaStream_t s,
-                         int fp32) {
+                         int fp32, int shift) {
   if (nplanes <= 0) return 0;
   const size_t smem = ((size_t)(M.ni + 2) + filter_smem_elems(M.ni)) * relem(fp32);
   dim3 grid(M.nj + 3, nplanes);
   const int gemm = fp32 && filter_gemm_usable(M);
   EPIC_LAUNCH_R(fp32, k_filter_planes, grid, row_threads(M), smem, s, M, src, src_sel, dst, k0, vgrid, gemm);
-  if (gemm) launch_filter_planes_gemm(M, src, src_sel, dst, k0, nplanes, vgrid, s);
+  if (gemm) launch_filter_planes_gemm(M, src, src_sel, dst, k0, nplanes, vgrid, s, shift);
   return 0;
 }
 
@@ -509,7 +564,8 @@ int launch_varz_filter(const DevModel &M, double *buff, int sel, int index, int 
   const int jstart = index == 1 ? 1 : 0;
   const int nrows = M.nj - jstart + 1;
   k_varz_tables<<<zg(epic_blocks(32LL * nrows, 128), M), 128, 0, s>>>(M, buff, sel, index, kstart, kend);
-  const size_t smem = (2 * (size_t)(M.ni + 2) + filter_smem_elems(M.ni)) * relem(M.mixed);
+  const size_t smem = M.mixed ? ((size_t)(M.ni + 2) + (M.nk + 2)) * sizeof(double) + ((size_t)(M.ni + 2) + filter_smem_elems(M.ni)) * sizeof(float)
+                             : (2 * (size_t)(M.ni + 2) + filter_smem_elems(M.ni)) * sizeof(double);
   dim3 grid(nrows, kend - kstart + 1);
   EPIC_LAUNCH_R(M.mixed, k_varz_filter_rows, grid, row_threads(M), smem, s, M, buff, sel, index, kstart, kend);
   return 0;

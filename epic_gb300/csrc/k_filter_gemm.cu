@@ -17,6 +17,11 @@
 // Three products per K step give FP32 accuracy from TF32 inputs ("3xTF32"): with a = a_hi + a_lo,
 // a_hi = tf32(a), the sum a_hi b_hi + a_hi b_lo + a_lo b_hi misses only the a_lo b_lo term.
 //
+// With shift set, each row of each plane is filtered as x - x(1), and x(1) is added back to the
+// output in binary64: the operator passes a constant unchanged (its wavenumber-0 weight is 1), so
+// the result is the same while the FP32 rounding acts on the zonal variations only -- for the
+// geopotential, ~1e-5 of its value.
+//
 // Every wait is bounded: a CTA whose MMA completion does not arrive within the limit records
 // ERR_TIMEOUT, waits (bounded) for its last commit, frees its tensor memory and returns.
 #include <cmath>
@@ -95,12 +100,13 @@ __device__ __forceinline__ bool mbar_wait(unsigned mbar, unsigned phase) {
 // its buffer; a buffer is restaged only after the commit of the step that last read it (commits
 // complete in issue order).
 __global__ void __launch_bounds__(FG_THREADS) k_filter_planes_gemm(DevModel M, const double *src, int src_sel, double *dst, int k0,
-                                                                     int nplanes, int vgrid) {
+                                                                     int nplanes, int vgrid, int shift) {
   epic_member(M, src, dst);
   extern __shared__ __align__(16) unsigned char fg_raw[];
   __shared__ __align__(8) uint64_t mbar[2];
   __shared__ uint32_t tmem_base;
   __shared__ int fail;
+  __shared__ double x1[FG_N];   // the subtracted value of each plane's row (shift), else 0
   const int ni = M.ni, mtiles = ni / FG_M, nchunks = ni / FG_KC, nsteps = nchunks * mtiles;
   const int j = (int)blockIdx.x - 1;
   const bool valid = vgrid ? (j >= 1 && j <= M.nj) : (j >= 0 && j <= M.nj);
@@ -117,6 +123,7 @@ __global__ void __launch_bounds__(FG_THREADS) k_filter_planes_gemm(DevModel M, c
   float *fk = reinterpret_cast<float *>(fg_smem + 2 * BUF_BYTES);
   const float *fsrc = (vgrid ? M.fkern_v : M.fkern_h) + (long long)(j + 1) * ni;
   for (int d = tid; d < ni; d += FG_THREADS) fk[d] = fsrc[d];
+  if (tid < FG_N) x1[tid] = shift && n0 + tid < nplanes ? src[M.at(k0 + n0 + tid, j, 1)] : 0.;
   const unsigned mbar_s = (unsigned)__cvta_generic_to_shared(&mbar[0]);
   if (tid == 0) {
     fail = 0;
@@ -145,8 +152,9 @@ __global__ void __launch_bounds__(FG_THREADS) k_filter_planes_gemm(DevModel M, c
       const int q = tid + u * FG_THREADS, n = q / (FG_KC / 4), e0 = 4 * (q % (FG_KC / 4));
       if (n0 + n < nplanes) {
         const double *row = src + M.at(k0 + n0 + n, j, kc + e0 + 1);
+        const double c = x1[n];
 #pragma unroll
-        for (int v = 0; v < 4; v++) bnext[u][v] = row[v];
+        for (int v = 0; v < 4; v++) bnext[u][v] = row[v] - c;
       } else {
 #pragma unroll
         for (int v = 0; v < 4; v++) bnext[u][v] = 0.;
@@ -227,7 +235,7 @@ __global__ void __launch_bounds__(FG_THREADS) k_filter_planes_gemm(DevModel M, c
       const int i = mt * FG_M + warp * 32 + lane + 1;
 #pragma unroll
       for (int n = 0; n < FG_N; n++)
-        if (n0 + n < nplanes) write_with_pads(dst, M, M.at(k0 + n0 + n, j, 0), i, f2d(__uint_as_float(r[n])));
+        if (n0 + n < nplanes) write_with_pads(dst, M, M.at(k0 + n0 + n, j, 0), i, f2d(__uint_as_float(r[n])) + x1[n]);
     }
   } else if (tid == 0) {
     flag_error(M.ctl, ERR_TIMEOUT, k0 + n0, j, 0, 0.);
@@ -243,9 +251,10 @@ size_t filter_gemm_smem_bytes(int ni) {
 
 bool filter_gemm_usable(const DevModel &M) { return M.fkern_h && M.ni % FG_M == 0 && M.ni <= 8 * FG_M; }
 
-int launch_filter_planes_gemm(const DevModel &M, const double *src, int src_sel, double *dst, int k0, int nplanes, int vgrid, cudaStream_t s) {
+int launch_filter_planes_gemm(const DevModel &M, const double *src, int src_sel, double *dst, int k0, int nplanes, int vgrid, cudaStream_t s,
+                              int shift) {
   dim3 grid(M.nj + 3, (nplanes + FG_N - 1) / FG_N);
-  k_filter_planes_gemm<<<zg(grid, M), FG_THREADS, filter_gemm_smem_bytes(M.ni), s>>>(M, src, src_sel, dst, k0, nplanes, vgrid);
+  k_filter_planes_gemm<<<zg(grid, M), FG_THREADS, filter_gemm_smem_bytes(M.ni), s>>>(M, src, src_sel, dst, k0, nplanes, vgrid, shift);
   return 0;
 }
 

@@ -35,16 +35,18 @@ inline dim3 zg(dim3 g, const DevModel &M) {
   } while (0)
 
 // k_filter.cu -- zonal filter (epic_adjust.c) and the zonal pass of hsu_advection.
-// fp32: filter in FP32 (the mixed forms, except the filtered GZ copy; on the tensor cores for ni a
-// multiple of 128).
+// fp32: filter in FP32 (the mixed forms; on the tensor cores for ni a multiple of 128).
+// shift (tensor-core path only): filter x - x(i=1) of each row and add x(i=1) back in binary64,
+// for fields whose zonal variations are small beside their value (the geopotential).
 int launch_filter_planes(const DevModel &M, const double *src, int src_sel, double *dst, int k0, int nplanes, int vgrid, cudaStream_t s,
-                         int fp32 = 0);
+                         int fp32 = 0, int shift = 0);
 int launch_varz_filter(const DevModel &M, double *buff, int sel, int index, int kstart, int kend, cudaStream_t s);
 int launch_hsu_zonal(const DevModel &M, double *buff, int kind, int kstart, cudaStream_t s);
 int filter_kernels_init(int ni);
 // k_filter_gemm.cu -- the plane filter as a tcgen05 (3xTF32) operator product, mixed form
 bool filter_gemm_usable(const DevModel &M);
-int launch_filter_planes_gemm(const DevModel &M, const double *src, int src_sel, double *dst, int k0, int nplanes, int vgrid, cudaStream_t s);
+int launch_filter_planes_gemm(const DevModel &M, const double *src, int src_sel, double *dst, int k0, int nplanes, int vgrid, cudaStream_t s,
+                              int shift = 0);
 int filter_gemm_init(int ni);
 
 // k_column_acc.cu -- set_p2etc and store_pgrad_vars (column part) of the mixed form, with the
