@@ -51,6 +51,31 @@ __device__ __forceinline__ R f_and_g_sigma_r(const DevModel &M, R s, R &g) {
   return R(0.);
 }
 
+// d(return_sigmatheta)/dp at fixed theta and pbot, from f_sigma/g_sigma's derivatives:
+// sigma = log(p/pbot)/lp, dsigma/dp = 1/(p lp); sigma_side takes the pure-sigma branch (f linear,
+// g = 0) whatever sigma's rounding says.
+template <class R>
+__device__ __forceinline__ R dsigmatheta_dp(const DevModel &M, R theta, R p, R pbot, R lp, bool sigma_side) {
+  const R ss = mconst<R>(M, DFC_SIGMA_SIGMA, M.sigma_sigma), z0 = mconst<R>(M, DFC_ZETA0, M.zeta0),
+          z1 = mconst<R>(M, DFC_ZETA1, M.zeta1);
+  const R s = RMath<R>::log(M, p / pbot) / lp;
+  R dfs, dgs;
+  if (sigma_side || (s <= ss && s >= R(0.))) {
+    dfs = z1 - z0;
+    dgs = R(0.);
+  } else if (s > ss && s < R(1.)) {
+    const R a = mconst<R>(M, DFC_ALPHA, M.alpha), gc = mconst<R>(M, DFC_G_COEFF, M.g_coeff);
+    const R e = RMath<R>::exp(M, -a * (s - ss));
+    const R g = gc * (R(1.) - e);
+    dgs = gc * a * e;
+    dfs = -dgs * (z0 + s * (z1 - z0)) + (R(1.) - g) * (z1 - z0);
+  } else {
+    dfs = R(0.);
+    dgs = R(0.);
+  }
+  return (dfs + dgs * theta) / (p * lp);
+}
+
 // log(b/a) for b/a near 1, from the FP64 difference
 __device__ __forceinline__ float log_ratio_f(double a, double b) { return log1pf(d2f(b - a) / d2f(a)); }
 

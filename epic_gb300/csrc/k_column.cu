@@ -76,7 +76,6 @@ __global__ void __launch_bounds__(CT_THREADS, 3) k_calc_w(DevModel M) {
   }
   __syncthreads();
   const R lp = s_lp[c.lane];
-  const R eps13 = sizeof(R) == sizeof(float) ? R(4.9215666e-3) : cv<R>(M.eps13);   // cbrt(FLT_EPSILON)
   if (c.valid)
     for (int k = 1 + c.warp; k < nk; k += CT_WARPS) {
       const R p3 = CT(P, k);
@@ -102,13 +101,23 @@ __global__ void __launch_bounds__(CT_THREADS, 3) k_calc_w(DevModel M) {
                       df3 * (dz21 * dz21 * dz21 * (dz10 + dz20)) / (dz30 * dz31 * dz32)) /
                     R(12.);
       }
-      // dF/dp by a centred difference of return_sigmatheta at fixed theta and pbot
-      const R dp = p3 * eps13;
-      R p2 = rmax(p3 - dp * R(.5), ptop);
-      const R p4 = rmin(p3 + dp * R(.5), pbot);
-      if (p2 < psigma && p4 >= psigma) p2 = p3;
-      if (!(p2 < p4)) flag_error(M.ctl, ERR_CALC_W_P, k, c.j, c.i, p2);
-      CT(DF, k) = (sigmatheta_lp<R>(M, theta3, p2, pbot, ptop, lp) - sigmatheta_lp<R>(M, theta3, p4, pbot, ptop, lp)) / (p2 - p4);
+      if constexpr (std::is_same_v<R, double>) {
+        // dF/dp by a centred difference of return_sigmatheta at fixed theta and pbot
+        const R dp = p3 * M.eps13;
+        R p2 = rmax(p3 - dp * R(.5), ptop);
+        const R p4 = rmin(p3 + dp * R(.5), pbot);
+        if (p2 < psigma && p4 >= psigma) p2 = p3;
+        if (!(p2 < p4)) flag_error(M.ctl, ERR_CALC_W_P, k, c.j, c.i, p2);
+        CT(DF, k) = (sigmatheta_lp<R>(M, theta3, p2, pbot, ptop, lp) - sigmatheta_lp<R>(M, theta3, p4, pbot, ptop, lp)) / (p2 - p4);
+      } else {
+        // The mixed forms differentiate return_sigmatheta analytically: in binary32 the centred
+        // difference loses ~1e-5 of the derivative to rounding and truncation, and W3's error
+        // then dominates the mixed form's error after a day (0.5e-3 in V at 128x64x20; the
+        // difference quotient in binary64 agrees with the derivative to ~1e-11).  At the
+        // interface where the hybrid coordinate turns to pure sigma, the reference's difference
+        // is one-sided into the sigma region, so the sigma-side derivative is taken there.
+        CT(DF, k) = dsigmatheta_dp<R>(M, theta3, p3, pbot, lp, k == ks - 1);
+      }
       CT(W, k) = w;
     }
   __syncthreads();
