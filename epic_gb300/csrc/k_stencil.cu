@@ -642,7 +642,8 @@ __global__ void k_akima_merid_update(DevModel M, double *A, int k0) {
 
 // d2dy2 of planes k0..k1 of src into dst (coefficients per row from the init block, :1049-1141).
 template <class R>
-__global__ void k_d2dy2(DevModel M, const double *src, int src_sel, double *dst, int vgrid, double diff_coef, int k0, int nkk) {
+__global__ void k_d2dy2(DevModel M, const double *src, int src_sel, double *dst, int vgrid, double diff_coef, int k0, int nkk,
+                        int of_state) {
   epic_member(M, src, dst);
   Cell c;
   const int nrows = vgrid ? M.nj + 2 : M.nj + 1;   // v: j = 0..nj+1, h: j = 0..nj
@@ -654,7 +655,15 @@ __global__ void k_d2dy2(DevModel M, const double *src, int src_sel, double *dst,
   auto h = [&](int jj) { return cv<R>(src[M.at(k, jj, i)]); };
   R d;
   const int jlast = vgrid ? nj + 1 : nj;
-  if (j == 0) d = a0 * h(0) + a1 * h(1) + a2 * h(2);
+  if (!std::is_same_v<R, double> && of_state) {
+    // The mixed forms' second difference of a state field: the three coefficients sum to zero
+    // (to ~1e-14 of the largest), so the stencil is a0 (h0 - h1) + a2 (h2 - h1) with the
+    // differences taken in binary64 -- in binary32 the field's own rounding (1e-7 of its value,
+    // 1e-4 of a neighbour difference) would enter the hyperviscous increment every step.
+    const int m = j == 0 ? 1 : (j == jlast ? j - 1 : j);
+    const double hm = src[M.at(k, m, i)];
+    d = a0 * cv<R>(src[M.at(k, m - 1, i)] - hm) + a2 * cv<R>(src[M.at(k, m + 1, i)] - hm);
+  } else if (j == 0) d = a0 * h(0) + a1 * h(1) + a2 * h(2);
   else if (j == jlast) d = a0 * h(j - 2) + a1 * h(j - 1) + a2 * h(j);
   else d = a0 * h(j - 1) + a1 * h(j) + a2 * h(j + 1);
   write_with_pads(dst, M, M.at(k, j, 0), i, d);
@@ -698,7 +707,10 @@ __global__ void k_zonal_visc(DevModel M, double *A, int sel, int jbot, int jhalf
 #pragma unroll
   for (int itmp = 2; itmp <= 8; itmp += 2) {
     const R dc = cv<R>(taper ? M.coef[itmp] * M.m0 * M.m0 : M.coef[itmp] * mm * mm);
-    for (int i = lane + 1; i <= ni; i += 32) d[i] = dc * (hh[i - 1] - R(2.) * hh[i] + hh[i + 1]);
+    if (!std::is_same_v<R, double> && itmp == 2)   // of the field itself: neighbour differences in binary64 (k_d2dy2)
+      for (int i = lane + 1; i <= ni; i += 32) d[i] = dc * (cv<R>(a[i - 1] - a[i]) + cv<R>(a[i + 1] - a[i]));
+    else
+      for (int i = lane + 1; i <= ni; i += 32) d[i] = dc * (hh[i - 1] - R(2.) * hh[i] + hh[i + 1]);
     __syncwarp();
     R mean;
     if (sizeof(R) == sizeof(double)) {
@@ -1067,7 +1079,8 @@ int launch_meridional_hyperviscosity(const DevModel &M, int index, double *var, 
   double sign = 1.;
   for (int itmp = 2; itmp <= 8; itmp += 2) {
     double *dst = bufs[which];
-    EPIC_LAUNCH_R(M.mixed, k_d2dy2, cells_blocks(M, nkk, nrows, TB(M, TB_VISC)), TB(M, TB_VISC), 0, s, M, cur_src, src_sel, dst, vgrid, M.coef[itmp], k0, nkk);
+    EPIC_LAUNCH_R(M.mixed, k_d2dy2, cells_blocks(M, nkk, nrows, TB(M, TB_VISC)), TB(M, TB_VISC), 0, s, M, cur_src, src_sel, dst, vgrid, M.coef[itmp], k0, nkk,
+                  cur_src == var);
     src_sel = PL_NONE;
     if (M.nu[itmp] > 0.) {
       launch_filter_planes(M, dst, PL_NONE, dst, k0, nkk, vgrid, s, M.mixed);
