@@ -480,8 +480,10 @@ def run_gpu_ensemble(args):
     clocks = clk.summary()
     launches = batch.kernels_per_step * args.steps
 
-    roof = batch_roofline(batch, cfg, nmem, stream, torch, stage=19)
-    roof_pgrad = batch_roofline(batch, cfg, nmem, stream, torch, stage=12)
+    # the dominant stage of the step (the pressure gradient, whose k_pgrad_lat is the top kernel
+    # of the launch list) and the vertical integration feeding it
+    roof = batch_roofline(batch, cfg, nmem, stream, torch, stage=12)
+    roof_column = batch_roofline(batch, cfg, nmem, stream, torch, stage=19)
 
     # end to end: every member's state uploaded from pinned host memory and downloaded, each step
     hosts = [m.download().copy(pinned=True) for m in members]
@@ -520,7 +522,7 @@ def run_gpu_ensemble(args):
             "e2e": {"value": e2e_val, "unit": "cell-steps/s", "h2d_bytes_per_step": host_bytes, "d2h_bytes_per_step": host_bytes},
             "gpu_launches": launches,
             "roofline": roof,
-            "roofline_pgrad": roof_pgrad,
+            "roofline_store_pgrad_vars": roof_column,
             "step_roofline": {"bound": "hbm", "algorithmic_bytes_per_step": nmem * algorithmic_bytes_per_step(cfg),
                               "achieved_gbs": nmem * algorithmic_bytes_per_step(cfg) / (ms_step / 1e3) / 1e9,
                               "peak_gbs": peaks.get("hbm_gbs")},
@@ -562,6 +564,14 @@ ROOF_STAGES = {
 }
 
 
+# DRAM traffic per member of each roofline stage: dram__bytes_read.sum + dram__bytes_write.sum of
+# the stage's kernels from one ncu capture of an 8-member launch at 128x64x20 (cold L2; writes
+# still resident in L2 when a kernel ends are not counted), divided by 8
+# (profiles/traffic_stages_mixed_ensemble8_128x64x20.md).  Scaled by the members of the launch.
+ROOF_TRAFFIC_PER_MEMBER = {19: 176.4e6 / 8, 12: 111.0e6 / 8}
+ROOF_TRAFFIC_SHAPE = (128, 64, 20)
+
+
 def batch_roofline(batch, cfg, nmem, stream, torch, stage=19):
     """One stage of the step over all members, timed with CUDA events on the batch stream after
     a warm-up call.  Algorithmic bytes per launch: the stage's field passes (ROOF_STAGES) of
@@ -582,9 +592,14 @@ def batch_roofline(batch, cfg, nmem, stream, torch, stage=19):
     dur = e0.elapsed_time(e1) / n / 1e3
     alg = passes * 8 * cfg.ni * (cfg.nj + 1) * cfg.nk * nmem
     ach = alg / dur / 1e9
+    traffic = None
+    if (cfg.ni, cfg.nj, cfg.nk) == ROOF_TRAFFIC_SHAPE and stage in ROOF_TRAFFIC_PER_MEMBER:
+        traffic = ROOF_TRAFFIC_PER_MEMBER[stage] * nmem
     return {"kernel": label, "bound": "hbm", "achieved": ach, "peak": peaks["hbm_gbs"], "unit": "GB/s",
             "frac": ach / peaks["hbm_gbs"], "peak_source": peaks["source"] + " (burst copy)", "algorithmic_bytes": alg,
-            "launch_ms": dur * 1e3, "traffic": None, "note": note}
+            "launch_ms": dur * 1e3, "traffic": traffic,
+            "traffic_source": "ncu dram__bytes_read.sum + dram__bytes_write.sum of the stage's kernels, one 8-member launch "
+                              "at 128x64x20 scaled by members" if traffic else None, "note": note}
 
 
 def _peaks():
@@ -639,7 +654,7 @@ def main():
     ap.add_argument("--members", type=int, default=None, help="ensemble size (profiling runs use a smaller ensemble)")
     ap.add_argument("--no-tune", action="store_true", help="keep the built-in launch shapes (profiling runs)")
     ap.add_argument("--no-cpu-baseline", action="store_true")
-    ap.add_argument("--cpu-steps", type=int, default=3)
+    ap.add_argument("--cpu-steps", type=int, default=100)
     ap.add_argument("--precision", default=None, choices=["fp64", "mixed", "fast"])
     ap.add_argument("--advection", default="hsu", choices=sorted(ADVECTION),
                     help="THETA/HDRY advection scheme (the Held-Suarez default is hsu)")
