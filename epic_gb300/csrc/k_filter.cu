@@ -172,7 +172,7 @@ __device__ __forceinline__ bool row_is_filtered(const DevModel &M, int j, int vg
 // (dst may equal src).  Block = one row j in -1..nj+1; rows outside the filtered set are
 // copied; rows 0..nj+1 get periodic pads (bc_lateral).
 template <class R>
-__global__ void k_filter_planes(DevModel M, const double *src, int src_sel, double *dst, int k0, int vgrid, int copy_only) {
+__global__ void k_filter_planes(DevModel M, const double *src, int src_sel, double *dst, int k0, int vgrid) {
   epic_member(M, src, dst);
   extern __shared__ __align__(16) unsigned char smraw[];
   R *sm = reinterpret_cast<R *>(smraw);
@@ -184,7 +184,6 @@ __global__ void k_filter_planes(DevModel M, const double *src, int src_sel, doub
   FilterSmem<R> fs = carve_filter(sm + (M.ni + 2), M.ni);
   const bool valid = vgrid ? (j >= 1 && j <= M.nj) : (j >= 0 && j <= M.nj);
   const bool filt = valid && row_is_filtered(M, j, vgrid);
-  if (filt && copy_only) return;   // the tensor-core filter writes this row
   if (!filt) {
     if (src != dst)
       for (int i = threadIdx.x; i <= M.ni + 1; i += blockDim.x) dst[base + i] = src[base + i];
@@ -200,6 +199,28 @@ __global__ void k_filter_planes(DevModel M, const double *src, int src_sel, doub
   __syncthreads();
   filter_row_smem(M, x, vgrid ? M.high_lat_pv : M.high_lat_h, M.at2(j, 0), fs);
   for (int i = threadIdx.x + 1; i <= M.ni; i += blockDim.x) write_with_pads(dst, M, base, i, x[i]);
+}
+
+// The rows the tensor-core filter leaves alone (k_filter_planes_gemm filters the others): copied
+// when dst is not src, periodic pads on rows 0..nj+1.  One warp per (row, plane).
+__global__ void k_filter_rows_unfiltered(DevModel M, const double *src, int src_sel, double *dst, int k0, int nplanes, int vgrid) {
+  epic_member(M, src, dst);
+  src += plane_offset(M, src_sel);
+  const int lane = (int)(threadIdx.x & 31);
+  const int w = (int)((blockIdx.x * blockDim.x + threadIdx.x) >> 5);
+  const int rows = M.nj + 3;
+  if (w >= rows * nplanes) return;
+  const int j = w % rows - 1, k = k0 + w / rows;
+  const bool valid = vgrid ? (j >= 1 && j <= M.nj) : (j >= 0 && j <= M.nj);
+  if (valid && row_is_filtered(M, j, vgrid)) return;
+  const int base = M.at(k, j, 0);
+  if (src != dst)
+    for (int i = lane; i <= M.ni + 1; i += 32) dst[base + i] = src[base + i];
+  __syncwarp();
+  if (j >= 0 && lane == 0) {
+    dst[base] = dst[base + M.ni];
+    dst[base + M.ni + 1] = dst[base + 1];
+  }
 }
 
 // Per-latitude var(gz) profile at the column of lowest bottom GZ, the first half of the
@@ -554,9 +575,12 @@ int launch_filter_planes(const DevModel &M, const double *src, int src_sel, doub
   if (nplanes <= 0) return 0;
   const size_t smem = ((size_t)(M.ni + 2) + filter_smem_elems(M.ni)) * relem(fp32);
   dim3 grid(M.nj + 3, nplanes);
-  const int gemm = fp32 && filter_gemm_usable(M);
-  EPIC_LAUNCH_R(fp32, k_filter_planes, grid, row_threads(M), smem, s, M, src, src_sel, dst, k0, vgrid, gemm);
-  if (gemm) launch_filter_planes_gemm(M, src, src_sel, dst, k0, nplanes, vgrid, s, shift);
+  if (fp32 && filter_gemm_usable(M)) {
+    const long long warps = (long long)(M.nj + 3) * nplanes;
+    k_filter_rows_unfiltered<<<zg(epic_blocks(32 * warps, 128), M), 128, 0, s>>>(M, src, src_sel, dst, k0, nplanes, vgrid);
+    return launch_filter_planes_gemm(M, src, src_sel, dst, k0, nplanes, vgrid, s, shift);
+  }
+  EPIC_LAUNCH_R(fp32, k_filter_planes, grid, row_threads(M), smem, s, M, src, src_sel, dst, k0, vgrid);
   return 0;
 }
 
