@@ -612,7 +612,6 @@ __device__ __forceinline__ double layer_p_mixed(const DevModel &M, double top, d
 __global__ void __launch_bounds__(CT_THREADS, 3) k_set_p2etc_mixed(DevModel M, int update_theta, int layers) {
   epic_member(M);
   extern __shared__ double sm[];
-  __shared__ double s_lp[32], s_ginv[32];
   const ColTile c = col_tile(M);
   const int nk = M.nk, ks = M.k_sigma, L = nk + 1;
   const long long n2 = M.n2;
@@ -636,25 +635,29 @@ __global__ void __launch_bounds__(CT_THREADS, 3) k_set_p2etc_mixed(DevModel M, i
     }
   }
   __syncthreads();
-  if (c.warp == 0 && c.valid) {
+  if (c.warp == 0 && c.valid) {   // P3 from the top down, in FP64
     double p = M.p3[c.base];
     CT(P, 0) = p;
     for (int k = 1; k <= nk; k++) {
       p = fma(M.dsgth[2 * k] * g, CT(HL, k), p);
       CT(P, k) = p;
     }
-    s_lp[c.lane] = log(CT(P, 0) / p);   // binary64 libdevice log: the mixed form needs no correct rounding
-    s_ginv[c.lane] = 1. / g;
   }
   __syncthreads();
-  const double ptop = CT(P, 0), pbot = CT(P, nk), lp = s_lp[c.lane];
+  const double ptop = CT(P, 0), pbot = CT(P, nk);
+  // log(ptop/pbot) and the pure-sigma interfaces pbot (ptop/pbot)^sigma in double-float, by every
+  // warp (binary64 log/exp by warp 0 alone kept the other warps waiting at the barrier)
+  const dfl LPB = c.valid ? log_df(cv<dfl>(pbot), M.exp2tab) : dfl(0.f, 0.f);
+  const dfl LP = c.valid ? log_df(cv<dfl>(ptop), M.exp2tab) - LPB : dfl(1.f, 0.f);   // log(ptop/pbot)
   if (c.valid && ks - 1 < nk) {
-    const double dz_inv = 1. / (M.zeta1 - M.zeta0);
-    for (int k = ks - 1 + c.warp; k < nk; k += CT_WARPS) CT(P, k) = pbot * exp((M.sgth[2 * k + 1] - M.zeta0) * dz_inv * lp);
+    const dfl Z0 = mconst<dfl>(M, DFC_ZETA0, 0.), DZ = mconst<dfl>(M, DFC_ZETA1, 0.) - Z0, PB = cv<dfl>(pbot);
+    for (int k = ks - 1 + c.warp; k < nk; k += CT_WARPS)
+      CT(P, k) = to_d(PB * exp_df((cv<dfl>(M.sgth[2 * k + 1]) - Z0) / DZ * LP, M.exp2tab));
   }
   __syncthreads();
-  const float lpf = d2f(lp);
-  const double ginv = s_ginv[c.lane];
+  if (!c.valid) return;
+  const double ginv = to_d(dfl(1.f, 0.f) / cv<dfl>(g));
+  const float lpf = LP.hi;
   if (c.valid)
     for (int k = c.warp; k <= nk; k += CT_WARPS) {
       const double pk = CT(P, k);

@@ -50,7 +50,6 @@ __device__ __forceinline__ double theta_acc(const DevModel &M, double sg, dfl si
 __global__ void __launch_bounds__(CT_THREADS, 3) k_set_p2etc_acc(DevModel M, int update_theta) {
   epic_member(M);
   extern __shared__ double sm[];
-  __shared__ double s_lp[32], s_ginv[32];
   const ColTile c = col_tile(M);
   const int nk = M.nk, ks = M.k_sigma, L = nk + 1;
   const long long n2 = M.n2;
@@ -82,24 +81,25 @@ __global__ void __launch_bounds__(CT_THREADS, 3) k_set_p2etc_acc(DevModel M, int
       p = fma(M.dsgth[2 * k] * g, CT(HL, k), p);
       CT(P, k) = p;
     }
-    s_lp[c.lane] = log(CT(P, 0) / p);
-    s_ginv[c.lane] = 1. / g;
   }
   __syncthreads();
-  const double ptop = CT(P, 0), pbot = CT(P, nk), lp = s_lp[c.lane];
-  if (c.valid && ks - 1 < nk) {   // the pure-sigma interfaces
-    const double dz_inv = 1. / (M.zeta1 - M.zeta0);
-    for (int k = ks - 1 + c.warp; k < nk; k += CT_WARPS) CT(P, k) = pbot * exp((M.sgth[2 * k + 1] - M.zeta0) * dz_inv * lp);
+  const double ptop = CT(P, 0), pbot = CT(P, nk);
+  // log(ptop/pbot) and the pure-sigma interfaces pbot (ptop/pbot)^sigma in double-float, by every
+  // warp (binary64 log/exp by warp 0 alone kept the other warps waiting at the barrier)
+  const dfl LPB = c.valid ? log_df(cv<dfl>(pbot), M.exp2tab) : dfl(0.f, 0.f);
+  const dfl LP = c.valid ? log_df(cv<dfl>(ptop), M.exp2tab) - LPB : dfl(1.f, 0.f);   // log(ptop/pbot)
+  if (c.valid && ks - 1 < nk) {
+    const dfl Z0 = mconst<dfl>(M, DFC_ZETA0, 0.), DZ = mconst<dfl>(M, DFC_ZETA1, 0.) - Z0, PB = cv<dfl>(pbot);
+    for (int k = ks - 1 + c.warp; k < nk; k += CT_WARPS)
+      CT(P, k) = to_d(PB * exp_df((cv<dfl>(M.sgth[2 * k + 1]) - Z0) / DZ * LP, M.exp2tab));
   }
   __syncthreads();
   if (!c.valid) return;
-  const double ginv = s_ginv[c.lane];
-  const float lpf = d2f(lp);
+  const double ginv = to_d(dfl(1.f, 0.f) / cv<dfl>(g));
+  const float lpf = LP.hi;
   // the logarithms of the interface pressures, once per interface: the layer-mean pressure, the
   // diagnosed theta here and T3 and the geopotential increments of store_pgrad_vars (lp3) take
   // theirs from these
-  const dfl LPB = log_df(cv<dfl>(pbot), M.exp2tab);
-  const dfl LP = log_df(cv<dfl>(ptop), M.exp2tab) - LPB;   // log(ptop/pbot)
   for (int k = c.warp; k <= nk; k += CT_WARPS) {
     const double pk = CT(P, k);
     const dfl lpk = k == nk ? LPB : log_df(cv<dfl>(pk), M.exp2tab);

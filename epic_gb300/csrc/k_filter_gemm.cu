@@ -152,9 +152,14 @@ __global__ void __launch_bounds__(FG_THREADS) k_filter_planes_gemm(DevModel M, c
       const int q = tid + u * FG_THREADS, n = q / (FG_KC / 4), e0 = 4 * (q % (FG_KC / 4));
       if (n0 + n < nplanes) {
         const double *row = src + M.at(k0 + n0 + n, j, kc + e0 + 1);
-        const double c = x1[n];
+        if (shift) {
+          const double c = x1[n];
 #pragma unroll
-        for (int v = 0; v < 4; v++) bnext[u][v] = row[v] - c;
+          for (int v = 0; v < 4; v++) bnext[u][v] = row[v] - c;
+        } else {
+#pragma unroll
+          for (int v = 0; v < 4; v++) bnext[u][v] = row[v];
+        }
       } else {
 #pragma unroll
         for (int v = 0; v < 4; v++) bnext[u][v] = 0.;
@@ -235,7 +240,10 @@ __global__ void __launch_bounds__(FG_THREADS) k_filter_planes_gemm(DevModel M, c
       const int i = mt * FG_M + warp * 32 + lane + 1;
 #pragma unroll
       for (int n = 0; n < FG_N; n++)
-        if (n0 + n < nplanes) write_with_pads(dst, M, M.at(k0 + n0 + n, j, 0), i, f2d(__uint_as_float(r[n])) + x1[n]);
+        if (n0 + n < nplanes) {
+          const double y = f2d(__uint_as_float(r[n]));
+          write_with_pads(dst, M, M.at(k0 + n0 + n, j, 0), i, shift ? y + x1[n] : y);
+        }
     }
   } else if (tid == 0) {
     flag_error(M.ctl, ERR_TIMEOUT, k0 + n0, j, 0, 0.);
