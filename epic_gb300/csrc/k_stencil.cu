@@ -219,6 +219,35 @@ __device__ __forceinline__ R face_width(const double *deg, int iw, int ie) {
   else return cv<R>((deg[ie] - deg[iw]) * (M_PI / 180.));
 }
 
+// Multiplication by a power of two, exact in every compute type: a double-float scales its two
+// parts (two multiplications, where the general product takes seven operations).
+struct Pow2 { float c; };
+template <class R>
+__device__ __forceinline__ R operator*(Pow2 s, R x) { return R(s.c) * x; }
+__device__ __forceinline__ dfl operator*(Pow2 s, dfl x) { return dfl(s.c * x.hi, s.c * x.lo); }
+
+// The four quarter sums and two half sums of a face (lon_face, lat_face): in the FP64 form in
+// the reference's order; the mixed forms share the pair each two of them have in common.
+template <class R, class G>
+__device__ __forceinline__ void face_sums(G gz, R &zb0, R &zb2, R &zt0, R &zt2, R &zb, R &zt) {
+  if constexpr (std::is_same_v<R, double>) {
+    zb0 = R(.25) * (gz(1, 1) + gz(1, 0) + gz(2, 1) + gz(2, 0));
+    zb2 = R(.25) * (gz(1, 1) + gz(1, 2) + gz(2, 1) + gz(2, 2));
+    zt0 = R(.25) * (gz(1, 1) + gz(1, 0) + gz(0, 1) + gz(0, 0));
+    zt2 = R(.25) * (gz(1, 1) + gz(1, 2) + gz(0, 1) + gz(0, 2));
+    zb = R(.5) * (gz(1, 1) + gz(2, 1));
+    zt = R(.5) * (gz(1, 1) + gz(0, 1));
+  } else {
+    const R sb = gz(1, 1) + gz(2, 1), st = gz(1, 1) + gz(0, 1);
+    zb0 = Pow2{.25f} * (sb + gz(1, 0) + gz(2, 0));
+    zb2 = Pow2{.25f} * (sb + gz(1, 2) + gz(2, 2));
+    zt0 = Pow2{.25f} * (st + gz(1, 0) + gz(0, 0));
+    zt2 = Pow2{.25f} * (st + gz(1, 2) + gz(0, 2));
+    zb = Pow2{.5f} * sb;
+    zt = Pow2{.5f} * st;
+  }
+}
+
 template <class R>
 struct LonFace { R zbse, zbne, ztse, ztne, zbe, zte, pbe, pte, east; };
 
@@ -229,12 +258,7 @@ template <class R>
 __device__ __forceinline__ LonFace<R> lon_face(const DevModel &M, const R (&z)[3][3][2], const R (&p)[2][2], int c, int i) {
   auto gz = [&](int a, int b) { return z[a][b][c]; };
   LonFace<R> f;
-  f.zbse = R(.25) * (gz(1, 1) + gz(1, 0) + gz(2, 1) + gz(2, 0));
-  f.zbne = R(.25) * (gz(1, 1) + gz(1, 2) + gz(2, 1) + gz(2, 2));
-  f.ztse = R(.25) * (gz(1, 1) + gz(1, 0) + gz(0, 1) + gz(0, 0));
-  f.ztne = R(.25) * (gz(1, 1) + gz(1, 2) + gz(0, 1) + gz(0, 2));
-  f.zbe = R(.5) * (gz(1, 1) + gz(2, 1));
-  f.zte = R(.5) * (gz(1, 1) + gz(0, 1));
+  face_sums<R>(gz, f.zbse, f.zbne, f.ztse, f.ztne, f.zbe, f.zte);
   f.pbe = p[1][c];
   f.pte = p[0][c];
   const R a1 = f.ztne + f.ztse, b1 = f.ztne * f.ztse, a2 = f.zbne + f.zbse, b2 = f.zbne * f.zbse;
@@ -264,7 +288,7 @@ __global__ void k_pgrad_lon(DevModel M) {
 #pragma unroll
     for (int q = 0; q < 2; q++) p[a][q] = ref.p(M.at(k + a, j, i + q - 1));
   const LonFace<R> w = lon_face<R>(M, z, p, 0, i - 1), e = lon_face<R>(M, z, p, 1, i);
-  const R rho = R(.5) * (cv<R>(M.rho3[M.at(k, j, i)]) + cv<R>(M.rho3[M.at(k, j, i - 1)]));
+  const R rho = Pow2{.5f} * (cv<R>(M.rho3[M.at(k, j, i)]) + cv<R>(M.rho3[M.at(k, j, i - 1)]));
   const R rlns = cv<R>(M.rln[2 * j]), rlnn = cv<R>(M.rln[2 * j + 2]);
   R a1 = e.ztne + e.ztse, a2 = w.ztne + w.ztse;
   R terms2 = R(3.) * (a1 - a2), top, bottom;
@@ -273,7 +297,7 @@ __global__ void k_pgrad_lon(DevModel M) {
     const R terms1 = a1 * a1 - b1 - (a2 * a2 - b2);
     top = (-terms1 * (w.pte - e.pte) + terms2 * (e.zte * w.pte - w.zte * e.pte)) / (e.zte - w.zte);
   } else {
-    top = R(.5) * (w.pte + e.pte) * terms2;
+    top = Pow2{.5f} * (w.pte + e.pte) * terms2;
   }
   a1 = e.zbne + e.zbse;
   a2 = w.zbne + w.zbse;
@@ -283,12 +307,12 @@ __global__ void k_pgrad_lon(DevModel M) {
     const R terms1 = a1 * a1 - b1 - (a2 * a2 - b2);
     bottom = (-terms1 * (w.pbe - e.pbe) + terms2 * (e.zbe * w.pbe - w.zbe * e.pbe)) / (e.zbe - w.zbe);
   } else {
-    bottom = R(.5) * (w.pbe + e.pbe) * terms2;
+    bottom = Pow2{.5f} * (w.pbe + e.pbe) * terms2;
   }
   R pgflon = top - bottom + R(0.) - R(0.) + w.east - e.east;
   const R dzn = e.ztne - e.zbne + w.ztne - w.zbne;
   const R dzs = e.ztse - e.zbse + w.ztse - w.zbse;
-  pgflon /= face_width<R>(M.lon, 2 * i - 1, 2 * i + 1) * rho * (rlns * (dzs + R(.5) * dzn) + rlnn * (dzn + R(.5) * dzs));
+  pgflon /= face_width<R>(M.lon, 2 * i - 1, 2 * i + 1) * rho * (rlns * (dzs + Pow2{.5f} * dzn) + rlnn * (dzn + Pow2{.5f} * dzs));
   const long long x = plane_offset(M, PL_UV_TEND) + M.at(k, j, i);
   M.dudt[x] = M.dudt[x] + to_d(pgflon);
 }
@@ -304,12 +328,7 @@ __device__ __forceinline__ LatFace<R> lat_face(const DevModel &M, const R (&z)[3
   auto gz = [&](int a, int c) { return z[a][b][c]; };
   LatFace<R> f;
   f.rln = cv<R>(M.rln[2 * jrow + 1]);
-  f.zbnw = R(.25) * (gz(1, 1) + gz(1, 0) + gz(2, 1) + gz(2, 0));
-  f.zbne = R(.25) * (gz(1, 1) + gz(1, 2) + gz(2, 1) + gz(2, 2));
-  f.ztnw = R(.25) * (gz(1, 1) + gz(1, 0) + gz(0, 1) + gz(0, 0));
-  f.ztne = R(.25) * (gz(1, 1) + gz(1, 2) + gz(0, 1) + gz(0, 2));
-  f.zbn = R(.5) * (gz(1, 1) + gz(2, 1));
-  f.ztn = R(.5) * (gz(1, 1) + gz(0, 1));
+  face_sums<R>(gz, f.zbnw, f.zbne, f.ztnw, f.ztne, f.zbn, f.ztn);
   f.pbn = p[1][b][1];
   f.ptn = p[0][b][1];
   const R a1 = f.ztne + f.ztnw, b1 = f.ztne * f.ztnw, a2 = f.zbne + f.zbnw, b2 = f.zbne * f.zbnw;
@@ -344,7 +363,7 @@ __global__ void k_pgrad_lat(DevModel M) {
   auto gz = [&](int a, int b, int q) { return z[a][b][q]; };
   auto pp = [&](int a, int b, int q) { return p[a][b][q]; };
   const LatFace<R> s = lat_face<R>(M, z, p, 0, j - 1), n = lat_face<R>(M, z, p, 1, j);
-  const R rho = R(.5) * (cv<R>(M.rho3[M.at(k, j, i)]) + cv<R>(M.rho3[M.at(k, j - 1, i)]));
+  const R rho = Pow2{.5f} * (cv<R>(M.rho3[M.at(k, j, i)]) + cv<R>(M.rho3[M.at(k, j - 1, i)]));
   const R rlt = cv<R>(M.rlt[2 * j]);
   const R rlns = s.rln, rlnn = n.rln;
   const R south = s.north, north = n.north;
@@ -353,51 +372,62 @@ __global__ void k_pgrad_lat(DevModel M) {
   const R zbs = s.zbn, zts = s.ztn, pbs = s.pbn, pts = s.ptn;
   R a1, a2, b1, b2, b3, terms1, terms2;
   // levels: a = 0 (k-1), 1 (k), 2 (k+1); rows: b = 0 (j-1), 1 (j); columns: q = 0 (i-1), 1 (i), 2 (i+1)
-  const R zbe = R(.125) * (gz(1, 1, 1) + gz(1, 1, 2) + gz(1, 0, 1) + gz(1, 0, 2) + gz(2, 1, 1) +
-                           gz(2, 1, 2) + gz(2, 0, 1) + gz(2, 0, 2));
-  const R zte = R(.125) * (gz(0, 1, 1) + gz(0, 1, 2) + gz(0, 0, 1) + gz(0, 0, 2) + gz(1, 1, 1) +
-                           gz(1, 1, 2) + gz(1, 0, 1) + gz(1, 0, 2));
-  const R pbe = R(.25) * (pp(1, 1, 1) + pp(1, 1, 2) + pp(1, 0, 1) + pp(1, 0, 2));
-  const R pte = R(.25) * (pp(0, 1, 1) + pp(0, 1, 2) + pp(0, 0, 1) + pp(0, 0, 2));
+  // the 8-point means are the means of the faces' quarter sums and the 4-point P means share their
+  // centre-column pair (mixed forms; the FP64 form sums in the reference's order)
+  R zbe, zte, pbe, pte, zbw, ztw, pbw, ptw;
+  if constexpr (std::is_same_v<R, double>) {
+    zbe = R(.125) * (gz(1, 1, 1) + gz(1, 1, 2) + gz(1, 0, 1) + gz(1, 0, 2) + gz(2, 1, 1) + gz(2, 1, 2) + gz(2, 0, 1) + gz(2, 0, 2));
+    zte = R(.125) * (gz(0, 1, 1) + gz(0, 1, 2) + gz(0, 0, 1) + gz(0, 0, 2) + gz(1, 1, 1) + gz(1, 1, 2) + gz(1, 0, 1) + gz(1, 0, 2));
+    pbe = R(.25) * (pp(1, 1, 1) + pp(1, 1, 2) + pp(1, 0, 1) + pp(1, 0, 2));
+    pte = R(.25) * (pp(0, 1, 1) + pp(0, 1, 2) + pp(0, 0, 1) + pp(0, 0, 2));
+    zbw = R(.125) * (gz(1, 1, 1) + gz(1, 1, 0) + gz(1, 0, 1) + gz(1, 0, 0) + gz(2, 1, 1) + gz(2, 1, 0) + gz(2, 0, 1) + gz(2, 0, 0));
+    ztw = R(.125) * (gz(0, 1, 1) + gz(0, 1, 0) + gz(0, 0, 1) + gz(0, 0, 0) + gz(1, 1, 1) + gz(1, 1, 0) + gz(1, 0, 1) + gz(1, 0, 0));
+    pbw = R(.25) * (pp(1, 1, 1) + pp(1, 1, 0) + pp(1, 0, 1) + pp(1, 0, 0));
+    ptw = R(.25) * (pp(0, 1, 1) + pp(0, 1, 0) + pp(0, 0, 1) + pp(0, 0, 0));
+  } else {
+    zbe = Pow2{.5f} * (n.zbne + s.zbne);
+    zte = Pow2{.5f} * (n.ztne + s.ztne);
+    zbw = Pow2{.5f} * (n.zbnw + s.zbnw);
+    ztw = Pow2{.5f} * (n.ztnw + s.ztnw);
+    const R cb = pp(1, 1, 1) + pp(1, 0, 1), ct = pp(0, 1, 1) + pp(0, 0, 1);
+    pbe = Pow2{.25f} * (cb + pp(1, 1, 2) + pp(1, 0, 2));
+    pte = Pow2{.25f} * (ct + pp(0, 1, 2) + pp(0, 0, 2));
+    pbw = Pow2{.25f} * (cb + pp(1, 1, 0) + pp(1, 0, 0));
+    ptw = Pow2{.25f} * (ct + pp(0, 1, 0) + pp(0, 0, 0));
+  }
   a1 = n.ztne + ztse; b1 = n.ztne * ztse; a2 = n.zbne + zbse; b2 = n.zbne * zbse;
   terms1 = a1 * a1 - b1 - (a2 * a2 - b2);
   terms2 = R(3.) * (a1 - a2);
-  const R east = R(.5) * (rlns - rlnn) * (-terms1 * (pbe - pte) + terms2 * (zte * pbe - zbe * pte)) / (zte - zbe);
-  const R zbw = R(.125) * (gz(1, 1, 1) + gz(1, 1, 0) + gz(1, 0, 1) + gz(1, 0, 0) + gz(2, 1, 1) +
-                           gz(2, 1, 0) + gz(2, 0, 1) + gz(2, 0, 0));
-  const R ztw = R(.125) * (gz(0, 1, 1) + gz(0, 1, 0) + gz(0, 0, 1) + gz(0, 0, 0) + gz(1, 1, 1) +
-                           gz(1, 1, 0) + gz(1, 0, 1) + gz(1, 0, 0));
-  const R pbw = R(.25) * (pp(1, 1, 1) + pp(1, 1, 0) + pp(1, 0, 1) + pp(1, 0, 0));
-  const R ptw = R(.25) * (pp(0, 1, 1) + pp(0, 1, 0) + pp(0, 0, 1) + pp(0, 0, 0));
+  const R east = Pow2{.5f} * (rlns - rlnn) * (-terms1 * (pbe - pte) + terms2 * (zte * pbe - zbe * pte)) / (zte - zbe);
   a1 = n.ztnw + ztsw; b1 = n.ztnw * ztsw; a2 = n.zbnw + zbsw; b2 = n.zbnw * zbsw;
   terms1 = a1 * a1 - b1 - (a2 * a2 - b2);
   terms2 = R(3.) * (a1 - a2);
-  const R west = R(.5) * (rlns - rlnn) * (-terms1 * (pbw - ptw) + terms2 * (ztw * pbw - zbw * ptw)) / (ztw - zbw);
+  const R west = Pow2{.5f} * (rlns - rlnn) * (-terms1 * (pbw - ptw) + terms2 * (ztw * pbw - zbw * ptw)) / (ztw - zbw);
   R top, bottom;
   a1 = n.ztne + n.ztnw; a2 = ztse + ztsw;
   terms2 = R(3.) * (a1 - a2);
   if (fabs(R(2.) * (n.ztn - zts) / (n.ztn + zts - n.zbn - zbs)) > DLOGZ_TOL) {
     b1 = n.ztne * n.ztnw; b2 = ztse * ztsw; b3 = n.ztne * ztse + n.ztnw * ztsw;
     terms1 = a1 * a1 - b1 - (a2 * a2 - b2);
-    top = R(.5) * ((n.ptn - pts) * ((rlnn + rlns) * terms1 + (rlnn - rlns) * (b1 + b2 - b3)) + (rlnn + rlns) * terms2 * (n.ztn * pts - zts * n.ptn)) /
+    top = Pow2{.5f} * ((n.ptn - pts) * ((rlnn + rlns) * terms1 + (rlnn - rlns) * (b1 + b2 - b3)) + (rlnn + rlns) * terms2 * (n.ztn * pts - zts * n.ptn)) /
           (n.ztn - zts);
   } else {
-    top = R(.25) * (rlnn + rlns) * (pts + n.ptn) * terms2;
+    top = Pow2{.25f} * (rlnn + rlns) * (pts + n.ptn) * terms2;
   }
   a1 = n.zbne + n.zbnw; a2 = zbse + zbsw;
   terms2 = R(3.) * (a1 - a2);
   if (fabs(R(2.) * (n.zbn - zbs) / (n.ztn + zts - n.zbn - zbs)) > DLOGZ_TOL) {
     b1 = n.zbne * n.zbnw; b2 = zbse * zbsw; b3 = n.zbne * zbse + n.zbnw * zbsw;
     terms1 = a1 * a1 - b1 - (a2 * a2 - b2);
-    bottom = R(.5) * ((n.pbn - pbs) * ((rlnn + rlns) * terms1 + (rlnn - rlns) * (b1 + b2 - b3)) + (rlnn + rlns) * terms2 * (n.zbn * pbs - zbs * n.pbn)) /
+    bottom = Pow2{.5f} * ((n.pbn - pbs) * ((rlnn + rlns) * terms1 + (rlnn - rlns) * (b1 + b2 - b3)) + (rlnn + rlns) * terms2 * (n.zbn * pbs - zbs * n.pbn)) /
              (n.zbn - zbs);
   } else {
-    bottom = R(.25) * (rlnn + rlns) * (pbs + n.pbn) * terms2;
+    bottom = Pow2{.25f} * (rlnn + rlns) * (pbs + n.pbn) * terms2;
   }
   R pgflat = top - bottom + south - (north + west + east);
   const R dzn = n.ztne - n.zbne + n.ztnw - n.zbnw;
   const R dzs = ztse - zbse + ztsw - zbsw;
-  pgflat /= face_width<R>(M.lat, 2 * j - 1, 2 * j + 1) * rho * rlt * (rlns * (dzs + R(.5) * dzn) + rlnn * (dzn + R(.5) * dzs));
+  pgflat /= face_width<R>(M.lat, 2 * j - 1, 2 * j + 1) * rho * rlt * (rlns * (dzs + Pow2{.5f} * dzn) + rlnn * (dzn + Pow2{.5f} * dzs));
   const long long x = plane_offset(M, PL_UV_TEND) + M.at(k, j, i);
   M.dvdt[x] = M.dvdt[x] + to_d(pgflat);
 }
