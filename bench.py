@@ -44,6 +44,7 @@ WORKLOADS = {
     "hs128": (128, 64, 20, 300),
     "hs256": (256, 128, 32, 60),
     "hs512": (512, 256, 40, 60),
+    "jet256": (256, 128, 32, 60),  # balanced zonal jets on the constant-N^2 sounding
     "ens64": (128, 64, 20, 300),   # per member; 64 members
 }
 ENSEMBLE = {"ens64": 64}
@@ -60,8 +61,11 @@ ADVECTION_NAME = {"hsu": "Hsu-Konor-Arakawa advection", "akima": "Akima advectio
 
 
 def _workload_cfg(name, seed=0, advection="hsu"):
-    from epic_gb300 import HSConfig
+    from epic_gb300 import EPIC_PROFILE_N2, HSConfig
     ni, nj, nk, dt = WORKLOADS[name]
+    if name.startswith("jet"):
+        return HSConfig(ni=ni, nj=nj, nk=nk, dt=dt, seed=seed, advection_scheme=ADVECTION[advection], profile=EPIC_PROFILE_N2,
+                        state="jet")
     return HSConfig(ni=ni, nj=nj, nk=nk, dt=dt, seed=seed, advection_scheme=ADVECTION[advection])
 
 
@@ -242,13 +246,17 @@ def run_gpu(args):
             "metric": METRIC, "value": value, "unit": "cell-steps/s", "n_gpus": ws, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": ms_step, "higher_is_better": True, "scaling": "weak",
             "vs_baseline": None, "dtype": "f64" if args.precision == "fp64" else "f32+f64", "data": "synthetic",
-            "config": {"workload": f"Held-Suarez {cfg.ni}x{cfg.nj}x{cfg.nk}, dt={cfg.dt}s, AB3, "
+            "config": {"workload": ("Zonal jets on the Held-Suarez planet " if cfg.state == "jet" else "Held-Suarez ") +
+                                   f"{cfg.ni}x{cfg.nj}x{cfg.nk}, dt={cfg.dt}s, AB3, "
                                    f"{ADVECTION_NAME[args.advection]}, nu4=0.5 max, "
                                    + ("FP64 drop-in form" if args.precision == "fp64" else f"{args.precision} form"),
                        "ni": cfg.ni, "nj": cfg.nj, "nk": cfg.nk, "dt": cfg.dt,
                        "precision": args.precision, "advection": args.advection, "parallelism": f"replicas{ws}",
                        "l2": f"state {model.device_bytes / 1e9:.2f} GB > 129 MB L2; no flush needed",
-                       "state": "horizontally uniform HS equilibrium column at rest + seeded 0.1 K theta noise"},
+                       "state": ("6 seeded Gaussian zonal jets (50-150 m/s, centres -70..70 deg, widths 3-8 deg) in "
+                                 "gradient-wind balance on a constant N^2 = 1e-4 s^-2 sounding (isothermal at 200 K above), "
+                                 "1% seeded vorticity perturbation" if cfg.state == "jet" else
+                                 "horizontally uniform HS equilibrium column at rest + seeded 0.1 K theta noise")},
             "clocks": clocks,
             "e2e": {"value": e2e_val, "unit": "cell-steps/s", "h2d_bytes_per_step": host.nbytes,
                     "d2h_bytes_per_step": host.nbytes},
@@ -386,7 +394,8 @@ def serving_summary(precision, seed=3):
     reqs = poisson_requests(40, 20.0, seed, sorted(SERVE_SHAPES), (36, 144), lambda s: SERVE_SHAPES[s])
     res = RunServer(hbm_budget=40 << 30, precision=precision, round_steps=16).serve(reqs)
     out = latency_summary(res)
-    out.update({"arrivals": "Poisson, 20 requests/s, seed 3", "shapes": [list(k) + [v] for k, v in sorted(SERVE_SHAPES.items())],
+    out.update({"arrivals": "Poisson, 20 requests/s, seed 3", "states": "Held-Suarez column at rest with seeded theta noise",
+                "shapes": [list(k) + [v] for k, v in sorted(SERVE_SHAPES.items())],
                 "steps_per_request": "uniform 36..144", "hbm_budget_gb": 40,
                 "note": "durations are steps, not the 0.25-2 simulated days of the stream description, to bound the run"})
     return out
@@ -674,7 +683,8 @@ def main():
                 "steps": steps, "warmup": args.warmup, "ms_per_step": wall / steps * 1e3, "higher_is_better": True,
                 "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
                 "config": {"workload": (f"ensemble of {ENSEMBLE[args.workload]} Held-Suarez members " if args.workload in ENSEMBLE
-                                        else "Held-Suarez ") + f"{cfg.ni}x{cfg.nj}x{cfg.nk}, dt={cfg.dt}s, AB3, "
+                                        else "Zonal jets on the Held-Suarez planet " if cfg.state == "jet" else "Held-Suarez ")
+                                       + f"{cfg.ni}x{cfg.nj}x{cfg.nk}, dt={cfg.dt}s, AB3, "
                                         f"{ADVECTION_NAME[args.advection]}, nu4=0.5 max; "
                                         f"reference CPU step (FP64) as {procs} concurrent single-threaded grids",
                            "ni": cfg.ni, "nj": cfg.nj, "nk": cfg.nk, "dt": cfg.dt, "precision": "fp64",

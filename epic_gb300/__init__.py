@@ -17,9 +17,9 @@ import os
 
 import numpy as np
 
-from .abi import (EPIC_ADV_AKIMA, EPIC_ADV_HSU, EPIC_PREC_FP64, EPIC_PREC_MIXED, EPIC_PREC_MIXED_FAST, EPIC_STEP_PROGS_AND_SYNC_DIAGS, EPIC_SYNC_DIAGS_ONLY,
-                  EPIC_UV_AB3, EPIC_UV_LEAPFROG, EpicFields, EpicGrid, EpicHsParams, Fields, GridArrays,
-                  HSConfig, Layout)
+from .abi import (EPIC_ADV_AKIMA, EPIC_ADV_HSU, EPIC_PREC_FP64, EPIC_PREC_MIXED, EPIC_PREC_MIXED_FAST, EPIC_PROFILE_HS_EQ,
+                  EPIC_PROFILE_N2, EPIC_STEP_PROGS_AND_SYNC_DIAGS, EPIC_SYNC_DIAGS_ONLY, EPIC_UV_AB3, EPIC_UV_LEAPFROG,
+                  EpicFields, EpicGrid, EpicHsParams, EpicJetParams, Fields, GridArrays, HSConfig, JetConfig, Layout)
 
 TUNE_GROUPS = 9   # EPIC_TUNE_GROUPS
 _HERE = os.path.dirname(os.path.abspath(__file__))
@@ -83,6 +83,8 @@ def load_library(path: str | None = None) -> C.CDLL:
                                        C.POINTER(C.c_double)]
     lib.epic_hs_initial_state.argtypes = [C.POINTER(EpicGrid), C.POINTER(EpicHsParams), C.c_uint64, C.c_double,
                                           C.POINTER(EpicFields)]
+    lib.epic_jet_initial_state.argtypes = [C.POINTER(EpicGrid), C.POINTER(EpicHsParams), C.POINTER(EpicJetParams),
+                                           C.c_uint64, C.POINTER(EpicFields)]
     _lib = lib
     return lib
 
@@ -94,7 +96,8 @@ def _check(rc: int, what: str) -> None:
 
 
 def hs_setup(cfg: HSConfig) -> tuple[GridArrays, Fields]:
-    """Synthetic Held-Suarez grid and initial state (host only; no GPU needed)."""
+    """Synthetic grid and initial state on the Held-Suarez planet (host only; no GPU needed):
+    the sounding's column at rest (cfg.state "hs") or the balanced zonal jets ("jet")."""
     lib = load_library()
     ga = GridArrays(cfg.ni, cfg.nj, cfg.nk)
     p = cfg.params()
@@ -102,8 +105,15 @@ def hs_setup(cfg: HSConfig) -> tuple[GridArrays, Fields]:
     _check(lib.epic_hs_grid_build(C.byref(p), C.byref(ga.struct), ga.p_ref.ctypes.data_as(dp),
                                   ga.theta_ref.ctypes.data_as(dp)), "epic_hs_grid_build")
     f = Fields(cfg.ni, cfg.nj, cfg.nk, cfg.uv_scheme)
-    _check(lib.epic_hs_initial_state(C.byref(ga.struct), C.byref(p), C.c_uint64(cfg.seed), C.c_double(cfg.noise_k),
-                                     C.byref(f.struct)), "epic_hs_initial_state")
+    if cfg.state == "jet":
+        jp = cfg.jet.params()
+        _check(lib.epic_jet_initial_state(C.byref(ga.struct), C.byref(p), C.byref(jp), C.c_uint64(cfg.seed),
+                                          C.byref(f.struct)), "epic_jet_initial_state")
+    elif cfg.state == "hs":
+        _check(lib.epic_hs_initial_state(C.byref(ga.struct), C.byref(p), C.c_uint64(cfg.seed), C.c_double(cfg.noise_k),
+                                         C.byref(f.struct)), "epic_hs_initial_state")
+    else:
+        raise ValueError(f"unknown initial state {cfg.state!r}")
     return ga, f
 
 

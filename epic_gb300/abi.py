@@ -20,6 +20,8 @@ EPIC_PREC_MIXED = 1
 EPIC_PREC_MIXED_FAST = 2
 EPIC_ADV_HSU = 0
 EPIC_ADV_AKIMA = 1
+EPIC_PROFILE_HS_EQ = 0
+EPIC_PROFILE_N2 = 1
 
 _dp = C.POINTER(C.c_double)
 
@@ -62,7 +64,15 @@ class EpicHsParams(C.Structure):
     _fields_ = [("ni", C.c_int32), ("nj", C.c_int32), ("nk", C.c_int32), ("dt", C.c_int32),
                 ("uv_scheme", C.c_int32), ("advection_scheme", C.c_int32),
                 ("ptop", C.c_double), ("pbot", C.c_double), ("p_sigma", C.c_double),
-                ("nu_nondim", C.c_double * 9), ("nudiv_nondim", C.c_double), ("lat0", C.c_double)]
+                ("nu_nondim", C.c_double * 9), ("nudiv_nondim", C.c_double), ("lat0", C.c_double),
+                ("profile", C.c_int32), ("pad1", C.c_int32), ("n2", C.c_double), ("theta_surface", C.c_double),
+                ("t_iso", C.c_double)]
+
+
+class EpicJetParams(C.Structure):
+    _fields_ = [("njets", C.c_int32), ("pad0", C.c_int32), ("amp_min", C.c_double), ("amp_max", C.c_double),
+                ("lat_min", C.c_double), ("lat_max", C.c_double), ("width_min", C.c_double), ("width_max", C.c_double),
+                ("vort_frac", C.c_double)]
 
 
 def _ptr(a: np.ndarray):
@@ -207,8 +217,31 @@ class Fields:
 
 
 @dataclass
+class JetConfig:
+    """Seeded zonal jets (epic_jet_initial_state): njets Gaussian jets u(lat), constant with
+    height, amplitudes, centres and widths uniform in the ranges; a non-divergent perturbation
+    with vort_frac of the jets' rms vorticity."""
+    njets: int = 6
+    amp: tuple = (50.0, 150.0)
+    lat: tuple = (-70.0, 70.0)
+    width: tuple = (3.0, 8.0)
+    vort_frac: float = 0.01
+
+    def params(self) -> EpicJetParams:
+        j = EpicJetParams()
+        j.njets = self.njets
+        j.amp_min, j.amp_max = self.amp
+        j.lat_min, j.lat_max = self.lat
+        j.width_min, j.width_max = self.width
+        j.vort_frac = self.vort_frac
+        return j
+
+
+@dataclass
 class HSConfig:
-    """A synthetic Held-Suarez run: grid shape, time step, scheme and dissipation."""
+    """A synthetic run on the Held-Suarez planet: grid shape, time step, schemes, dissipation,
+    sounding and initial state (state "hs": the sounding's column at rest with theta noise;
+    state "jet": the balanced zonal jets of `jet` on the sounding)."""
     ni: int = 64
     nj: int = 32
     nk: int = 10
@@ -225,6 +258,12 @@ class HSConfig:
     lat0: float = 45.0
     seed: int = 0
     noise_k: float = 0.1
+    profile: int = EPIC_PROFILE_HS_EQ
+    n2: float = 1.0e-4
+    theta_surface: float = 300.0
+    t_iso: float = 200.0
+    state: str = "hs"
+    jet: JetConfig = field(default_factory=JetConfig)
     extra: dict = field(default_factory=dict)
 
     def params(self) -> EpicHsParams:
@@ -237,6 +276,8 @@ class HSConfig:
         p.nu_nondim[4], p.nu_nondim[6], p.nu_nondim[8] = self.nu4, self.nu6, self.nu8
         p.nudiv_nondim = self.nudiv
         p.lat0 = self.lat0
+        p.profile = self.profile
+        p.n2, p.theta_surface, p.t_iso = self.n2, self.theta_surface, self.t_iso
         return p
 
     @property

@@ -9,7 +9,8 @@
 //   AB3/leapfrog start flags                             src/shared/epic_initial.c:1301-1330
 //   HDRY from P3    get_h                                src/shared/epic_main.c:290-297
 // The temperature sounding t_vs_p.held_suarez is replaced by the analytic Held-Suarez
-// equilibrium profile at 45 degrees (temp_eq, src/shared/epic_sensible_heating.c:394-406).
+// equilibrium profile at 45 degrees (temp_eq, src/shared/epic_sensible_heating.c:394-406), or
+// by a constant-N^2 sounding for the zonal-jet state (epic_jet_initial_state).
 // Compiled with -ffp-contract=off so the same bits come out on x86-64 and aarch64 hosts.
 #include <cmath>
 #include <cstdint>
@@ -33,6 +34,7 @@ constexpr double kHsJ2 = 1082.636e-6;
 constexpr double kHsKinvisc = 14.60e-6;
 constexpr double kAlphaBoundary = 0.5;   // ALPHA_BOUNDARY, epic_initial.c:110
 constexpr double kPress0 = 1.e+5;        // grid.press0, epic_initial.c:242
+constexpr double kSoundingGrav = 9.8;    // gravity of the constant-N^2 sounding's definition
 
 struct Coord {  // the hybrid-coordinate constants get_sigma ... return_sigmatheta read
   double zeta0, zeta1, alpha, sigma_sigma;
@@ -91,6 +93,20 @@ inline double hs_theta_eq(double lat_deg, double p, double kappa) {
   return hs_temp_eq(lat_deg, p, kappa) * pow(kPress0 / p, kappa);
 }
 
+// The sounding (theta at pressure pres) the vertical grid and the initial columns follow.
+// EPIC_PROFILE_N2: theta(z) = theta_s exp(N^2 z / g) in hydrostatic balance from pbot up, i.e.
+// 1/theta(p) = 1/theta_s + N^2 R / (g^2 kappa) ((p/p0)^kappa - (pbot/p0)^kappa), with the
+// temperature held at t_iso above the level where it falls to t_iso.
+inline double sounding_theta(const epic_hs_params *p, double pres) {
+  if (p->profile != EPIC_PROFILE_N2) return hs_theta_eq(45., pres, kHsKappa);
+  const double pbot = p->pbot > 0. ? p->pbot : 1.e+5;
+  const double c = p->n2 * kHsRgas / (kSoundingGrav * kSoundingGrav * kHsKappa);
+  const double pk = pow(pres / kPress0, kHsKappa);
+  const double th = 1. / (1. / p->theta_surface + c * (pk - pow(pbot / kPress0, kHsKappa)));
+  const double t = th * pk;
+  return t > p->t_iso ? th : p->t_iso / pk;
+}
+
 // SplitMix64, one independent stream value per (seed, counter).
 inline uint64_t splitmix64(uint64_t x) {
   x += 0x9E3779B97F4A7C15ull;
@@ -121,6 +137,14 @@ extern "C" int epic_hs_grid_build(const epic_hs_params *p, epic_grid *g, double 
   if (p->uv_scheme != EPIC_UV_AB3 && p->uv_scheme != EPIC_UV_LEAPFROG) return set_error(EPIC_ERR_ARG, "uv_scheme=%d", p->uv_scheme);
   if (p->advection_scheme != EPIC_ADV_HSU && p->advection_scheme != EPIC_ADV_AKIMA)
     return set_error(EPIC_ERR_ARG, "advection_scheme=%d", p->advection_scheme);
+  if (p->profile != EPIC_PROFILE_HS_EQ && p->profile != EPIC_PROFILE_N2) return set_error(EPIC_ERR_ARG, "profile=%d", p->profile);
+  if (p->profile == EPIC_PROFILE_N2) {
+    const double pbot_chk = p->pbot > 0. ? p->pbot : 1.e+5;
+    const double c = p->n2 * kHsRgas / (kSoundingGrav * kSoundingGrav * kHsKappa);
+    if (!(p->n2 > 0.) || !(p->theta_surface > 0.) || !(p->t_iso > 0.) ||
+        !(1. / p->theta_surface - c * pow(pbot_chk / kPress0, kHsKappa) > 0.))
+      return set_error(EPIC_ERR_ARG, "N^2 sounding: n2=%g theta_surface=%g t_iso=%g", p->n2, p->theta_surface, p->t_iso);
+  }
   double *lon = const_cast<double *>(g->lon), *lat = const_cast<double *>(g->lat);
   double *rln = const_cast<double *>(g->rln), *rlt = const_cast<double *>(g->rlt);
   double *fc = const_cast<double *>(g->f), *m = const_cast<double *>(g->m), *n = const_cast<double *>(g->n);
@@ -228,13 +252,12 @@ extern "C" int epic_hs_grid_build(const epic_hs_params *p, epic_grid *g, double 
   const double ptop = p->ptop > 0. ? p->ptop : 10.;
   const double pbot = p->pbot > 0. ? p->pbot : 1.e+5;
   const double p_sigma = p->p_sigma > 0. ? p->p_sigma : 900. * 100.;
-  const double lat_ref = 45.;
   for (int kk = 0; kk <= 2 * (nk + 1); kk++) { p_ref[kk] = 0.; theta_ref[kk] = 0.; sgth[kk] = 0.; }
   Coord c{g->zeta0, g->zeta1, g->hybrid_alpha, 0.};
   p_ref[1] = ptop;
   p_ref[2 * KHI + 1] = pbot;
-  theta_ref[1] = hs_theta_eq(lat_ref, ptop, kHsKappa);
-  theta_ref[2 * KHI + 1] = hs_theta_eq(lat_ref, pbot, kHsKappa);
+  theta_ref[1] = sounding_theta(p, ptop);
+  theta_ref[2 * KHI + 1] = sounding_theta(p, pbot);
   const double sgth_top = theta_ref[1];
   const double sgth_bot = return_sigmatheta(c, theta_ref[2 * KHI + 1], pbot, pbot, ptop);
   sgth[0] = sgth[1] = sgth_top;
@@ -266,7 +289,7 @@ extern "C" int epic_hs_grid_build(const epic_hs_params *p, epic_grid *g, double 
     g->k_sigma = k_sigma;
   }
   c.sigma_sigma = get_sigma(p_ref[2 * KHI + 1], p_ref[2 * (g->k_sigma - 1) + 1], p_ref[1]);
-  for (int kk = 2; kk < 2 * KHI + 1; kk++) theta_ref[kk] = hs_theta_eq(lat_ref, p_ref[kk], kHsKappa);
+  for (int kk = 2; kk < 2 * KHI + 1; kk++) theta_ref[kk] = sounding_theta(p, p_ref[kk]);
   for (int kk = 2; kk < 2 * KHI + 1; kk++) sgth[kk] = return_sigmatheta(c, theta_ref[kk], p_ref[kk], pbot, ptop);
   g->sigma_sigma = (sgth[2 * g->k_sigma - 1] - g->zeta0) / (g->zeta1 - g->zeta0);
 
@@ -308,31 +331,16 @@ extern "C" int epic_hs_grid_build(const epic_hs_params *p, epic_grid *g, double 
   return EPIC_OK;
 }
 
-extern "C" int epic_hs_initial_state(const epic_grid *g, const epic_hs_params *p, uint64_t seed, double noise_k,
-                                     epic_fields *f) {
-  using epic::set_error;
-  if (!g || !p || !f) return set_error(EPIC_ERR_ARG, "epic_hs_initial_state: NULL argument");
-  if (!f->u || !f->v || !f->dudt || !f->dvdt || !f->hdry || !f->theta || !f->p3 || !f->gz_surface || !f->u_spinup)
-    return set_error(EPIC_ERR_ARG, "epic_hs_initial_state: required field pointer is NULL");
-  const epic::Layout L(g->ni, g->nj, g->nk);
-  const int ni = g->ni, nj = g->nj, nk = g->nk, KHI = nk;
-  Coord c{g->zeta0, g->zeta1, g->hybrid_alpha, g->sigma_sigma};
+namespace {
+
+// P3 at the interfaces of a column with bottom pressure p_bot that follows the sounding, as
+// init_with_u does from a sounding (src/shared/epic_funcs_init.c:1514-1662): get_p_sigma() in the
+// pure-sigma region, bisection of return_sigmatheta(theta(p), p) = sigmatheta[2K+1] above it.
+void sounding_column(const epic_grid *g, const epic_hs_params *p, double p_top, double p_bot, std::vector<double> &pcol) {
+  const int KHI = g->nk, ksig = g->k_sigma;
+  const Coord c{g->zeta0, g->zeta1, g->hybrid_alpha, g->sigma_sigma};
   const double *sgth = g->sigmatheta;
-  const double p_top = p->ptop > 0. ? p->ptop : 10.;
-  const double p_bot = p->pbot > 0. ? p->pbot : 1.e+5;
-
-  f->it_zero = 0; f->it_minus1 = 1; f->it_minus2 = 2;
-  f->itime = 0; f->model_time = 0;
-
-  // Horizontally uniform column at rest, as the reference's own Held-Suarez runs start from a
-  // single sounding (init_with_u with u_scale = 0, src/shared/epic_funcs_init.c:1514-1662):
-  // P3 on the sigmatheta interfaces of the 45-degree equilibrium profile, found by bisection
-  // of return_sigmatheta(theta_eq(p), p) = sigmatheta[2K+1] above the pure-sigma region and
-  // from get_p_sigma() inside it; THETA = theta_eq(P3).  Seeded N(0, noise_k^2) noise is then
-  // added to THETA where it is prognostic (K >= k_sigma-1).
-  const int ksig = g->k_sigma;
-  const double la = 45.;
-  std::vector<double> pcol(KHI + 1), thcol(KHI + 1);
+  pcol.assign(KHI + 1, 0.);
   pcol[0] = p_top;
   pcol[KHI] = p_bot;
   for (int K = ksig - 1; K < KHI; K++) {
@@ -345,13 +353,73 @@ extern "C" int epic_hs_initial_state(const epic_grid *g, const epic_hs_params *p
     for (int it = 0; it < 200; it++) {
       const double mid = .5 * (lo + hi);
       const double pm = exp(mid);
-      const double v = return_sigmatheta(c, hs_theta_eq(la, pm, g->kappa), pm, p_bot, p_top) - target;
+      const double v = return_sigmatheta(c, sounding_theta(p, pm), pm, p_bot, p_top) - target;
       if (v > 0.) lo = mid; else hi = mid;   // sigmatheta decreases downward
       if (hi - lo < 1.e-15) break;
     }
     pcol[K] = exp(.5 * (lo + hi));
   }
-  for (int K = 0; K <= KHI; K++) thcol[K] = hs_theta_eq(la, pcol[K], g->kappa);
+}
+
+// HDRY = get_h(P3) in the layers, epic_main.c:290-297 with get_h, epic_funcs_diag.c:1780-1853.
+void hdry_from_p3(const epic_grid *g, const epic::Layout &L, epic_fields *f) {
+  for (int K = 1; K <= g->nk; K++)
+    for (int J = 0; J <= g->nj; J++)
+      for (int I = 1; I <= g->ni; I++)
+        f->hdry[L.at(K, J, I)] = (f->p3[L.at(K, J, I)] - f->p3[L.at(K - 1, J, I)]) / (g->g[2 * J + 1] * g->dsgth[2 * K]);
+}
+
+// Time-plane indices and the first-step flags of the time scheme (epic_initial.c:1301-1330).
+void start_flags(const epic_grid *g, const epic::Layout &L, epic_fields *f) {
+  f->it_zero = 0; f->it_minus1 = 1; f->it_minus2 = 2;
+  f->itime = 0; f->model_time = 0;
+  const int64_t n3 = L.n3;
+  if (g->uv_scheme == EPIC_UV_AB3) {
+    for (int K = 1; K <= g->nk; K++)
+      for (int J = 0; J <= g->nj; J++)
+        for (int I = 1; I <= g->ni; I++) {
+          f->dudt[2 * n3 + L.at(K, J, I)] = DBL_MAX;   // IT_MINUS2
+          f->dudt[1 * n3 + L.at(K, J, I)] = DBL_MAX;   // IT_MINUS1
+          f->dvdt[2 * n3 + L.at(K, J, I)] = DBL_MAX;
+          f->dvdt[1 * n3 + L.at(K, J, I)] = DBL_MAX;
+        }
+  } else {
+    // Leapfrog: the reference flags the whole IT_MINUS1 plane (epic_initial.c:1316-1325), which
+    // leaves DBL_MAX in V's polar row after the first step.  Only the two cells that
+    // leapfrog_step and timeplane_bookkeeping test are flagged here
+    // (U at (KLO,JLO,ILO), V at (KLO,JFIRST,ILO)); the rest of IT_MINUS1 copies IT_ZERO.
+    f->u[n3 + L.at(1, 0, 1)] = DBL_MAX;
+    f->v[n3 + L.at(1, 1, 1)] = DBL_MAX;
+  }
+}
+
+inline double uniform(uint64_t seed, uint64_t counter, double lo, double hi) {
+  const uint64_t base = splitmix64(seed * 0x9E6C63D0676A9A99ull + 0x2545F4914F6CDD1Dull);
+  return lo + (hi - lo) * (unit_open(splitmix64(base ^ counter)) - 0.5 / 9007199254740992.0);
+}
+
+}  // namespace
+
+extern "C" int epic_hs_initial_state(const epic_grid *g, const epic_hs_params *p, uint64_t seed, double noise_k,
+                                     epic_fields *f) {
+  using epic::set_error;
+  if (!g || !p || !f) return set_error(EPIC_ERR_ARG, "epic_hs_initial_state: NULL argument");
+  if (!f->u || !f->v || !f->dudt || !f->dvdt || !f->hdry || !f->theta || !f->p3 || !f->gz_surface || !f->u_spinup)
+    return set_error(EPIC_ERR_ARG, "epic_hs_initial_state: required field pointer is NULL");
+  const epic::Layout L(g->ni, g->nj, g->nk);
+  const int ni = g->ni, nj = g->nj, KHI = g->nk;
+  const double p_top = p->ptop > 0. ? p->ptop : 10.;
+  const double p_bot = p->pbot > 0. ? p->pbot : 1.e+5;
+  start_flags(g, L, f);
+
+  // Horizontally uniform column at rest, as the reference's own Held-Suarez runs start from a
+  // single sounding (init_with_u with u_scale = 0, src/shared/epic_funcs_init.c:1514-1662):
+  // P3 on the sigmatheta interfaces of the sounding, THETA = theta(P3).  Seeded N(0, noise_k^2)
+  // noise is then added to THETA where it is prognostic (K >= k_sigma-1).
+  const int ksig = g->k_sigma;
+  std::vector<double> pcol, thcol(KHI + 1);
+  sounding_column(g, p, p_top, p_bot, pcol);
+  for (int K = 0; K <= KHI; K++) thcol[K] = sounding_theta(p, pcol[K]);
   for (int J = 0; J <= nj; J++) {
     for (int I = 1; I <= ni; I++) {
       for (int K = 0; K <= KHI; K++) {
@@ -365,32 +433,148 @@ extern "C" int epic_hs_initial_state(const epic_grid *g, const epic_hs_params *p
       }
     }
   }
-  // HDRY = get_h(P3) in the layers, epic_main.c:290-297 with get_h, epic_funcs_diag.c:1780-1853.
-  for (int K = 1; K <= KHI; K++)
-    for (int J = 0; J <= nj; J++)
-      for (int I = 1; I <= ni; I++)
-        f->hdry[L.at(K, J, I)] = (f->p3[L.at(K, J, I)] - f->p3[L.at(K - 1, J, I)]) / (g->g[2 * J + 1] * g->dsgth[2 * K]);
+  hdry_from_p3(g, L, f);
   // Zonal periodicity of everything that was filled (bc_lateral, src/single/s_epic_functions.c:39-87).
   double *fields3[] = {f->p3, f->theta, f->hdry};
   for (double *a : fields3) L.periodic3(a);
-  // Rest state; time-scheme start flags.
+  return EPIC_OK;
+}
+
+extern "C" int epic_jet_initial_state(const epic_grid *g, const epic_hs_params *p, const epic_jet_params *jet, uint64_t seed,
+                                      epic_fields *f) {
+  using epic::set_error;
+  if (!g || !p || !jet || !f) return set_error(EPIC_ERR_ARG, "epic_jet_initial_state: NULL argument");
+  if (!f->u || !f->v || !f->dudt || !f->dvdt || !f->hdry || !f->theta || !f->p3 || !f->gz_surface || !f->u_spinup)
+    return set_error(EPIC_ERR_ARG, "epic_jet_initial_state: required field pointer is NULL");
+  if (jet->njets < 0 || jet->njets > 64 || !(jet->amp_min <= jet->amp_max) || !(jet->lat_min <= jet->lat_max) ||
+      !(jet->width_min > 0.) || !(jet->width_min <= jet->width_max) || !(jet->vort_frac >= 0.))
+    return set_error(EPIC_ERR_ARG, "epic_jet_initial_state: bad jet parameters");
+  const epic::Layout L(g->ni, g->nj, g->nk);
+  const int ni = g->ni, nj = g->nj, KHI = g->nk;
+  const double p_top = p->ptop > 0. ? p->ptop : 10.;
+  const double p_bot = p->pbot > 0. ? p->pbot : 1.e+5;
+  const double a = g->re;
+  start_flags(g, L, f);
+
+  // the jets, u at the h rows
+  std::vector<double> amp(jet->njets), cen(jet->njets), wid(jet->njets), uh(nj + 1, 0.);
+  for (int q = 0; q < jet->njets; q++) {
+    amp[q] = uniform(seed, 3 * (uint64_t)q, jet->amp_min, jet->amp_max);
+    cen[q] = uniform(seed, 3 * (uint64_t)q + 1, jet->lat_min, jet->lat_max);
+    wid[q] = uniform(seed, 3 * (uint64_t)q + 2, jet->width_min, jet->width_max);
+  }
+  for (int J = 0; J <= nj; J++) {
+    const double la = g->lat[2 * J + 1];
+    for (int q = 0; q < jet->njets; q++) {
+      const double x = (la - cen[q]) / wid[q];
+      uh[J] += amp[q] * exp(-x * x);
+    }
+  }
+  // geopotential on pressure surfaces, relative to row 0, from gradient-wind balance at the v rows
+  std::vector<double> phi(nj + 1, 0.);
+  for (int J = 1; J <= nj; J++) {
+    const double uv = .5 * (uh[J - 1] + uh[J]);
+    const double dy = (g->lat[2 * J + 1] - g->lat[2 * J - 1]) * kDeg * a;
+    phi[J] = phi[J - 1] - dy * (g->f[2 * J] + uv * tan(g->lat[2 * J] * kDeg) / a) * uv;
+  }
+  // the sounding's geopotential above p_bot, phiref(p) = int_p^p_bot R T dlnp, tabulated in ln p
+  const int NT = 4096;
+  const double l0 = log(p_top), l1 = log(1.5 * p_bot), dl = (l1 - l0) / (NT - 1);
+  std::vector<double> tab(NT);
+  auto temp = [&](double lp) { const double pr = exp(lp); return sounding_theta(p, pr) * pow(pr / kPress0, kHsKappa); };
+  const int ib = (int)((log(p_bot) - l0) / dl);
+  tab[0] = 0.;
+  for (int q = 1; q < NT; q++) tab[q] = tab[q - 1] - .5 * kHsRgas * (temp(l0 + (q - 1) * dl) + temp(l0 + q * dl)) * dl;
+  const double at_pbot = tab[ib] + (tab[ib + 1] - tab[ib]) * ((log(p_bot) - (l0 + ib * dl)) / dl);
+  for (double &v : tab) v -= at_pbot;   // phiref(p_bot) = 0; phiref falls with p
+  auto p_of_phi = [&](double target) {   // phiref^-1, linear in ln p between table points
+    if (target >= tab[0]) return p_top;
+    if (target <= tab[NT - 1]) return exp(l1);
+    int lo = 0, hi = NT - 1;
+    while (hi - lo > 1) {
+      const int mid = (lo + hi) / 2;
+      if (tab[mid] >= target) lo = mid; else hi = mid;
+    }
+    return exp(l0 + dl * (lo + (target - tab[lo]) / (tab[hi] - tab[lo])));
+  };
+  // each row's bottom pressure: the surface (GZ_SURFACE = 0) is where phiref + phi - C = 0, with C
+  // fixed by bisection so that the cos(lat)-weighted mean bottom pressure is p_bot
+  std::vector<double> pb(nj + 1);
+  auto mean_pb = [&](double C) {
+    double sw = 0., s = 0.;
+    for (int J = 0; J <= nj; J++) {
+      pb[J] = p_of_phi(C - phi[J]);
+      const double w = cos(g->lat[2 * J + 1] * kDeg);
+      sw += w;
+      s += w * pb[J];
+    }
+    return s / sw;
+  };
+  double clo = -1.e6, chi = 1.e6;   // mean_pb falls as C grows
+  for (int it = 0; it < 200; it++) {
+    const double mid = .5 * (clo + chi);
+    if (mean_pb(mid) > p_bot) clo = mid; else chi = mid;
+  }
+  mean_pb(.5 * (clo + chi));
+  for (int J = 0; J <= nj; J++)
+    if (!(pb[J] > 2. * p_top && pb[J] < 1.4 * p_bot))
+      return set_error(EPIC_ERR_ARG, "epic_jet_initial_state: row %d bottom pressure %g out of range", J, pb[J]);
+  // P3 and THETA of each row's column
+  std::vector<double> pcol;
+  for (int J = 0; J <= nj; J++) {
+    sounding_column(g, p, p_top, pb[J], pcol);
+    for (int I = 1; I <= ni; I++)
+      for (int K = 0; K <= KHI; K++) {
+        f->p3[L.at(K, J, I)] = pcol[K];
+        f->theta[L.at(K, J, I)] = sounding_theta(p, pcol[K]);
+      }
+  }
+  hdry_from_p3(g, L, f);
+  // the non-divergent perturbation: streamfunction psi at the vorticity points (v rows J,
+  // u columns I), zero on the polar rows; u' = -dpsi/dy at the u points, v' = dpsi/dx at the v points
+  std::vector<double> psi((size_t)(nj + 2) * (ni + 2), 0.), up((size_t)(nj + 1) * (ni + 2), 0.), vp((size_t)(nj + 2) * (ni + 2), 0.);
+  auto PS = [&](int J, int I) -> double & { return psi[(size_t)J * (ni + 2) + I]; };
+  for (int J = 1; J <= nj; J++) {
+    for (int I = 1; I <= ni; I++) PS(J, I) = gauss(seed ^ 0x5DEECE66Dull, (uint64_t)J * ni + (I - 1));
+    PS(J, ni + 1) = PS(J, 1);
+    PS(J, 0) = PS(J, ni);
+  }
+  for (int J = 0; J <= nj; J++)
+    for (int I = 1; I <= ni; I++) up[(size_t)J * (ni + 2) + I] = -(PS(J + 1, I) - PS(J, I)) * g->n[2 * J + 1];
+  for (int J = 1; J <= nj; J++)
+    for (int I = 1; I <= ni; I++) vp[(size_t)J * (ni + 2) + I] = (PS(J, I + 1) - PS(J, I)) * g->m[2 * J];
+  // rms relative vorticity at the interior vorticity points, of the jets and of the perturbation
+  double zj = 0., zp = 0.;
+  for (int J = 1; J <= nj; J++)
+    for (int I = 1; I <= ni; I++) {
+      const double du = (up[(size_t)J * (ni + 2) + I] - up[(size_t)(J - 1) * (ni + 2) + I]) * g->n[2 * J];
+      const int Im = I == 1 ? ni : I - 1;
+      const double dv = (vp[(size_t)J * (ni + 2) + I] - vp[(size_t)J * (ni + 2) + Im]) * g->m[2 * J];
+      zp += (dv - du) * (dv - du);
+      const double zjet = -(uh[J] - uh[J - 1]) * g->n[2 * J];
+      zj += zjet * zjet;
+    }
+  const double scale = zp > 0. ? jet->vort_frac * sqrt(zj / zp) : 0.;
   const int64_t n3 = L.n3;
-  if (g->uv_scheme == EPIC_UV_AB3) {
-    for (int K = 1; K <= KHI; K++)
+  const int nplanes = g->uv_scheme == EPIC_UV_AB3 ? 1 : 2;
+  for (int t = 0; t < nplanes; t++)
+    for (int K = 1; K <= KHI; K++) {
       for (int J = 0; J <= nj; J++)
         for (int I = 1; I <= ni; I++) {
-          f->dudt[2 * n3 + L.at(K, J, I)] = DBL_MAX;   // IT_MINUS2
-          f->dudt[1 * n3 + L.at(K, J, I)] = DBL_MAX;   // IT_MINUS1
-          f->dvdt[2 * n3 + L.at(K, J, I)] = DBL_MAX;
-          f->dvdt[1 * n3 + L.at(K, J, I)] = DBL_MAX;
+          double &u = f->u[t * n3 + L.at(K, J, I)];
+          if (u != DBL_MAX) u = uh[J] + scale * up[(size_t)J * (ni + 2) + I];
         }
-  } else {
-    // Leapfrog: the reference flags the whole IT_MINUS1 plane (epic_initial.c:1316-1325), which
-    // leaves DBL_MAX in V's polar row after the first step.  Only the two cells that
-    // leapfrog_step and timeplane_bookkeeping test are flagged here
-    // (U at (KLO,JLO,ILO), V at (KLO,JFIRST,ILO)); the rest of IT_MINUS1 copies IT_ZERO.
-    f->u[n3 + L.at(1, 0, 1)] = DBL_MAX;
-    f->v[n3 + L.at(1, 1, 1)] = DBL_MAX;
+      for (int J = 1; J <= nj; J++)
+        for (int I = 1; I <= ni; I++) {
+          double &v = f->v[t * n3 + L.at(K, J, I)];
+          if (v != DBL_MAX) v = scale * vp[(size_t)J * (ni + 2) + I];
+        }
+    }
+  double *fields3[] = {f->p3, f->theta, f->hdry};
+  for (double *x : fields3) L.periodic3(x);
+  for (int t = 0; t < nplanes; t++) {
+    L.periodic3(f->u + t * n3);
+    L.periodic3(f->v + t * n3);
   }
   return EPIC_OK;
 }

@@ -28,7 +28,7 @@ from dataclasses import dataclass, field
 
 import numpy as np
 
-from . import Batch, EPIC_PREC_MIXED, EPIC_SYNC_DIAGS_ONLY, Fields, HSConfig, Model, hs_setup, model_bytes
+from . import Batch, EPIC_PREC_MIXED, EPIC_PROFILE_N2, EPIC_SYNC_DIAGS_ONLY, Fields, HSConfig, Model, hs_setup, model_bytes
 
 
 @dataclass
@@ -66,8 +66,9 @@ class _Active:
 
 
 def _shape_class(cfg: HSConfig, precision: int) -> tuple:
+    # the sounding fixes the vertical grid (sigmatheta), so it is part of the class
     return (cfg.ni, cfg.nj, cfg.nk, cfg.dt, cfg.uv_scheme, cfg.advection_scheme, precision, cfg.nu4, cfg.nu6, cfg.nu8,
-            cfg.nudiv, cfg.lat0)
+            cfg.nudiv, cfg.lat0, cfg.profile, cfg.n2, cfg.theta_surface, cfg.t_iso)
 
 
 def state_checksum(f: Fields) -> float:
@@ -214,9 +215,11 @@ class RunServer:
 
 
 def poisson_requests(n: int, rate: float, seed: int, shapes: list[tuple], steps_range: tuple[int, int],
-                     dt_of=lambda shape: 300) -> list[RunRequest]:
+                     dt_of=lambda shape: 300, jet_frac: float = 0.0, jet_dt: int = 60) -> list[RunRequest]:
     """n requests with seeded Poisson arrivals (mean `rate` per second), shapes drawn from
-    `shapes` (ni, nj, nk), step counts uniform in steps_range and k_f scaled by 1 +/- 10%."""
+    `shapes` (ni, nj, nk), step counts uniform in steps_range and k_f scaled by 1 +/- 10%; a
+    fraction jet_frac of them (seeded) start from the balanced zonal jets on the constant-N^2
+    sounding with time step jet_dt, the others from the Held-Suarez column with dt_of(shape)."""
     rng = np.random.default_rng(seed)
     t = 0.0
     out = []
@@ -224,8 +227,12 @@ def poisson_requests(n: int, rate: float, seed: int, shapes: list[tuple], steps_
         t += float(rng.exponential(1.0 / rate))
         ni, nj, nk = shapes[int(rng.integers(len(shapes)))]
         steps = int(rng.integers(steps_range[0], steps_range[1] + 1))
-        cfg = HSConfig(ni=ni, nj=nj, nk=nk, dt=dt_of((ni, nj, nk)), seed=1000 + q)
-        out.append(RunRequest(q, cfg, steps, t, 1.0 + float(rng.uniform(-0.1, 0.1))))
+        kf = 1.0 + float(rng.uniform(-0.1, 0.1))
+        if jet_frac > 0.0 and float(rng.uniform()) < jet_frac:
+            cfg = HSConfig(ni=ni, nj=nj, nk=nk, dt=jet_dt, seed=1000 + q, profile=EPIC_PROFILE_N2, state="jet")
+        else:
+            cfg = HSConfig(ni=ni, nj=nj, nk=nk, dt=dt_of((ni, nj, nk)), seed=1000 + q)
+        out.append(RunRequest(q, cfg, steps, t, kf))
     return out
 
 

@@ -280,19 +280,58 @@ typedef struct epic_hs_params {
   double  nu_nondim[9];        /* grid.nu_nondim; HS runs use nu[4] = 0.5, the rest 0 */
   double  nudiv_nondim;
   double  lat0;                /* 45 reproduces the reference's LAT0 */
+  /* the sounding the vertical grid (sigmatheta) and the initial column follow */
+  int32_t profile;             /* EPIC_PROFILE_HS_EQ or EPIC_PROFILE_N2 */
+  int32_t pad1;
+  double  n2;                  /* EPIC_PROFILE_N2: buoyancy frequency squared [s^-2] below the ... */
+  double  theta_surface;       /* ... isothermal layer: theta = theta_surface at pbot [K] ... */
+  double  t_iso;               /* ... and T = max(t_iso, T_N2(p)) [K] */
 } epic_hs_params;
+
+/* Soundings: the Held-Suarez equilibrium column at 45 degrees (temp_eq), or a column of
+ * constant buoyancy frequency N^2 from theta_surface at pbot, isothermal at t_iso above the
+ * level where it reaches that temperature (the stable jet sounding). */
+#define EPIC_PROFILE_HS_EQ 0
+#define EPIC_PROFILE_N2    1
 
 int epic_hs_grid_build(const epic_hs_params *p, epic_grid *grid, double *p_ref, double *theta_ref);
 
 /*
- * Seeded initial state: rest (U = V = 0), P3 on the sigmatheta interfaces from the
- * Held-Suarez equilibrium temperature of each latitude row, theta noise N(0, noise_k^2)
- * in the pure-sigma region (k >= k_sigma-1), HDRY = get_h(P3), GZ_SURFACE = 0,
- * U_SPINUP = 0, and the first-step flags of the chosen time scheme
- * (src/shared/epic_initial.c:1301-1330).  Fields f must point at zeroed storage.
+ * Seeded initial state: rest (U = V = 0), P3 on the sigmatheta interfaces of the sounding
+ * (p->profile), horizontally uniform, theta noise N(0, noise_k^2) in the pure-sigma region
+ * (k >= k_sigma-1), HDRY = get_h(P3), GZ_SURFACE = 0, U_SPINUP = 0, and the first-step flags of
+ * the chosen time scheme (src/shared/epic_initial.c:1301-1330).  Fields f must point at zeroed
+ * storage.
  */
 int epic_hs_initial_state(const epic_grid *grid, const epic_hs_params *p, uint64_t seed, double noise_k,
                           epic_fields *f);
+
+/* Zonal jets: u(lat) = sum over njets of amp_i exp(-((lat - lat_i)/width_i)^2), the amplitudes,
+ * centres and widths drawn uniformly from the ranges below (seeded), constant with height. */
+typedef struct epic_jet_params {
+  int32_t njets;
+  int32_t pad0;
+  double  amp_min, amp_max;       /* [m/s] */
+  double  lat_min, lat_max;       /* jet centres [deg] */
+  double  width_min, width_max;   /* [deg] */
+  double  vort_frac;              /* rms relative vorticity of the seeded perturbation, as a
+                                     fraction of the jets' */
+} epic_jet_params;
+
+/*
+ * Seeded jet state, no counterpart in the reference (its jet runs start from `initial`'s
+ * gradient-balance integration, src/shared/epic_funcs_init.c:1294-1342): the zonal jets of
+ * *jet on every layer, theta horizontally uniform on pressure surfaces (the sounding of
+ * p->profile), and each row's bottom pressure set so that the geopotential on pressure
+ * surfaces balances the jets, d(phi)/dy = -(f + u tan(lat)/a) u, integrated from the south
+ * row with the row-mean bottom pressure p->pbot; P3 on the sigmatheta interfaces of each row's
+ * column, HDRY = get_h(P3); plus a seeded non-divergent wind perturbation (white streamfunction
+ * noise at the vorticity points, the same on every layer) with vort_frac of the jets' rms
+ * vorticity.  Grid built by epic_hs_grid_build with the same p.  Fields f must point at zeroed
+ * storage.
+ */
+int epic_jet_initial_state(const epic_grid *grid, const epic_hs_params *p, const epic_jet_params *jet, uint64_t seed,
+                           epic_fields *f);
 
 #ifdef __cplusplus
 }

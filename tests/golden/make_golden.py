@@ -16,7 +16,7 @@ HERE = os.path.dirname(os.path.abspath(__file__))
 sys.path.insert(0, os.path.dirname(HERE))
 sys.path.insert(0, os.path.dirname(os.path.dirname(HERE)))
 
-from epic_gb300 import EPIC_ADV_AKIMA, EPIC_UV_AB3, EPIC_UV_LEAPFROG, HSConfig, hs_setup  # noqa: E402
+from epic_gb300 import EPIC_ADV_AKIMA, EPIC_PROFILE_N2, EPIC_UV_AB3, EPIC_UV_LEAPFROG, HSConfig, hs_setup  # noqa: E402
 from oracle_lib import reference_available, run_reference, fields_to_dict  # noqa: E402
 
 SAVED = ("u", "v", "hdry", "theta", "p3", "gz3", "pv3", "w3", "heat3", "div_uv3")
@@ -26,6 +26,8 @@ CASES = {
     "hs16x8x12_ab3": (HSConfig(ni=16, nj=8, nk=12, dt=600, uv_scheme=EPIC_UV_AB3, seed=13), [("sync", 0), ("step", 3)]),
     "hs32x16x10_ab3_akima": (HSConfig(ni=32, nj=16, nk=10, dt=300, uv_scheme=EPIC_UV_AB3, seed=14, advection_scheme=EPIC_ADV_AKIMA),
                              [("sync", 0), ("step", 1), ("step", 4)]),
+    "jet32x16x10_ab3": (HSConfig(ni=32, nj=16, nk=10, dt=300, uv_scheme=EPIC_UV_AB3, seed=15, profile=EPIC_PROFILE_N2, state="jet"),
+                        [("sync", 0), ("step", 1), ("step", 4)]),
 }
 
 

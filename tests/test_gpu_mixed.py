@@ -21,6 +21,8 @@ Stated error (relative L2 per field vs FP64, dt 300 s), measured on a GB300:
   fast   64x32x10   12 h from rest, leapfrog          1.8e-3   6.4e-4   1.6e-7   3.7e-8
   fast   128x64x20  1 day after a 1-day spin-up       3.4e-4   9.7e-4   1.1e-5   7.0e-8
   fast   128x64x20  1 day from rest                   9.5e-4   1.7e-3   2.0e-5   1.2e-7
+  mixed  64x32x10   zonal jets, 1 day                 3.4e-7   8.9e-7   1.7e-8   3.4e-9
+  fast   64x32x10   zonal jets, 1 day                 3.6e-6   1.8e-5   1.4e-7   3.8e-8
 
 (128x64x20 is the ensemble member shape: ni = 128 takes the tensor-core filter; its FP64 run
 stays stable for about two days, so its spin-up is one day.)
@@ -42,7 +44,7 @@ import pytest
 
 from compare import PROGNOSTIC, field_errors
 from epic_gb300 import (EPIC_ADV_AKIMA, EPIC_ADV_HSU, EPIC_PREC_FP64, EPIC_PREC_MIXED, EPIC_PREC_MIXED_FAST,
-                        EPIC_SYNC_DIAGS_ONLY, EPIC_UV_LEAPFROG, HSConfig, Model, hs_setup)
+                        EPIC_PROFILE_N2, EPIC_SYNC_DIAGS_ONLY, EPIC_UV_LEAPFROG, HSConfig, Model, hs_setup)
 
 pytestmark = pytest.mark.gpu
 DAY = 288   # steps of 300 s
@@ -55,6 +57,8 @@ BOUNDS = {
     ("mixed", "member_rest"): {"u": 3e-4, "v": 3.5e-4, "hdry": 4e-6, "theta": 2.5e-8},
     ("fast", "member_spun_up"): {"u": 1e-3, "v": 3e-3, "hdry": 3.5e-5, "theta": 2e-7},
     ("fast", "member_rest"): {"u": 3e-3, "v": 5e-3, "hdry": 6e-5, "theta": 4e-7},
+    ("mixed", "jet"): {"u": 1.2e-6, "v": 3e-6, "hdry": 6e-8, "theta": 1e-8},
+    ("fast", "jet"): {"u": 1.2e-5, "v": 6e-5, "hdry": 5e-7, "theta": 1.2e-7},
     ("fast", "spun_up"): {"u": 1e-4, "v": 2e-3, "hdry": 1e-6, "theta": 1e-7},
     ("fast", "rest"): {"u": 1e-3, "v": 3e-3, "hdry": 1e-6, "theta": 1e-7},
     ("fast", "leapfrog"): {"u": 6e-3, "v": 3e-3, "hdry": 1e-6, "theta": 1e-7},
@@ -182,3 +186,11 @@ def test_one_day_at_member_shape(gpu, form, case):
         f = m.download()
     a, b = _pair(ga, f, prime, FORMS[form])
     _check(_run(a, b, DAY), BOUNDS[(form, case)])
+
+
+@pytest.mark.parametrize("form", FORMS)
+def test_jets_one_day(gpu, form):
+    """The balanced zonal-jet state on the constant-N^2 sounding, one day."""
+    ga, f = hs_setup(HSConfig(ni=64, nj=32, nk=10, dt=300, seed=0, profile=EPIC_PROFILE_N2, state="jet"))
+    a, b = _pair(ga, f, True, FORMS[form])
+    _check(_run(a, b, DAY), BOUNDS[(form, "jet")])

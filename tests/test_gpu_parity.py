@@ -6,15 +6,16 @@ with the host glibc, which reproduces the reference build bit for bit).  Kernel 
 GPU evaluates the reference's expressions in the reference's order without FMA contraction,
 with correctly rounded log/exp/pow and a bit-exact restatement of realft, so every stage and
 every step must equal the restatement compiled with the same correctly rounded functions
-(oracle libepicport_cr.so) bit for bit.  Both advection schemes (Hsu-Konor-Arakawa, Akima) are
-covered.
+(oracle libepicport_cr.so) bit for bit.  Both advection schemes (Hsu-Konor-Arakawa, Akima) and
+both initial states (the Held-Suarez column at rest, the balanced zonal jets on the constant-N^2
+sounding) are covered.
 """
 import numpy as np
 import pytest
 
 from compare import DIAGNOSTIC, PROGNOSTIC, field_errors, worst
-from epic_gb300 import (EPIC_ADV_AKIMA, EPIC_ADV_HSU, EPIC_SYNC_DIAGS_ONLY, EPIC_UV_AB3, EPIC_UV_LEAPFROG, HSConfig, Model,
-                        hs_setup)
+from epic_gb300 import (EPIC_ADV_AKIMA, EPIC_ADV_HSU, EPIC_PROFILE_N2, EPIC_SYNC_DIAGS_ONLY, EPIC_UV_AB3, EPIC_UV_LEAPFROG,
+                        HSConfig, Model, hs_setup)
 from oracle_lib import Port
 
 pytestmark = pytest.mark.gpu
@@ -49,12 +50,16 @@ def _differing(a, b):
     return {k: int((a.arrays[k] != b.arrays[k]).sum()) for k in a.arrays if not np.array_equal(a.arrays[k], b.arrays[k])}
 
 
-@pytest.mark.parametrize("adv", [EPIC_ADV_HSU, EPIC_ADV_AKIMA])
+def _state(state):
+    return {"state": state, "profile": EPIC_PROFILE_N2 if state == "jet" else 0}
+
+
+@pytest.mark.parametrize("adv,state", [(EPIC_ADV_HSU, "hs"), (EPIC_ADV_AKIMA, "hs"), (EPIC_ADV_HSU, "jet")])
 @pytest.mark.parametrize("scheme", [EPIC_UV_AB3, EPIC_UV_LEAPFROG])
-def test_stage_by_stage(gpu, scheme, adv):
+def test_stage_by_stage(gpu, scheme, adv, state):
     """Each reference function on the path, GPU vs the correctly rounded restatement, bit for
     bit, from the same spun-up state."""
-    cfg = HSConfig(ni=32, nj=16, nk=10, dt=300, uv_scheme=scheme, seed=3, advection_scheme=adv)
+    cfg = HSConfig(ni=32, nj=16, nk=10, dt=300, uv_scheme=scheme, seed=3, advection_scheme=adv, **_state(state))
     ga, f = _spin_up(cfg, 4)
     port = Port(ga, cr_libm=True)
     port.upload(f)
@@ -74,11 +79,11 @@ def test_stage_by_stage(gpu, scheme, adv):
     assert not failures, "\n".join(failures)
 
 
-@pytest.mark.parametrize("adv", [EPIC_ADV_HSU, EPIC_ADV_AKIMA])
+@pytest.mark.parametrize("adv,state", [(EPIC_ADV_HSU, "hs"), (EPIC_ADV_AKIMA, "hs"), (EPIC_ADV_HSU, "jet")])
 @pytest.mark.parametrize("scheme", [EPIC_UV_AB3, EPIC_UV_LEAPFROG])
-def test_steps_bitwise(gpu, scheme, adv):
+def test_steps_bitwise(gpu, scheme, adv, state):
     """Ten graph-replayed steps at 64x32x20 equal the correctly rounded restatement bit for bit."""
-    cfg = HSConfig(ni=64, nj=32, nk=20, dt=300, uv_scheme=scheme, seed=9, advection_scheme=adv)
+    cfg = HSConfig(ni=64, nj=32, nk=20, dt=300, uv_scheme=scheme, seed=9, advection_scheme=adv, **_state(state))
     ga, f, port, model = _pair(cfg, cr_libm=True)
     port.timestep(EPIC_SYNC_DIAGS_ONLY)
     port.run(10)
@@ -100,12 +105,17 @@ def test_sync_diags(gpu):
     assert not bad, bad
 
 
-@pytest.mark.parametrize("scheme,nsteps,tol,adv", [(EPIC_UV_AB3, 1, 1e-11, EPIC_ADV_HSU), (EPIC_UV_LEAPFROG, 1, 1e-11, EPIC_ADV_HSU),
-                                                    (EPIC_UV_AB3, 100, 1e-8, EPIC_ADV_HSU), (EPIC_UV_AB3, 1, 1e-11, EPIC_ADV_AKIMA),
-                                                    (EPIC_UV_AB3, 100, 1e-8, EPIC_ADV_AKIMA)])
-def test_full_step(gpu, scheme, nsteps, tol, adv):
-    """The 64x32x10 Held-Suarez configuration: per-prognostic relative L2 after nsteps."""
-    cfg = HSConfig(ni=64, nj=32, nk=10, dt=300, uv_scheme=scheme, advection_scheme=adv)
+@pytest.mark.parametrize("scheme,nsteps,tol,adv,state", [(EPIC_UV_AB3, 1, 1e-11, EPIC_ADV_HSU, "hs"),
+                                                          (EPIC_UV_LEAPFROG, 1, 1e-11, EPIC_ADV_HSU, "hs"),
+                                                          (EPIC_UV_AB3, 100, 1e-8, EPIC_ADV_HSU, "hs"),
+                                                          (EPIC_UV_AB3, 1, 1e-11, EPIC_ADV_AKIMA, "hs"),
+                                                          (EPIC_UV_AB3, 100, 1e-8, EPIC_ADV_AKIMA, "hs"),
+                                                          (EPIC_UV_AB3, 1, 1e-11, EPIC_ADV_HSU, "jet"),
+                                                          (EPIC_UV_AB3, 100, 1e-8, EPIC_ADV_HSU, "jet")])
+def test_full_step(gpu, scheme, nsteps, tol, adv, state):
+    """The 64x32x10 configuration (Held-Suarez column or zonal jets): per-prognostic relative L2
+    after nsteps."""
+    cfg = HSConfig(ni=64, nj=32, nk=10, dt=300, uv_scheme=scheme, advection_scheme=adv, **_state(state))
     ga, f, port, model = _pair(cfg)
     port.timestep(EPIC_SYNC_DIAGS_ONLY)
     port.run(nsteps)

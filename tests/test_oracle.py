@@ -14,8 +14,8 @@ import numpy as np
 import pytest
 
 from compare import PROGNOSTIC, field_errors
-from epic_gb300 import (EPIC_ADV_AKIMA, EPIC_ADV_HSU, EPIC_SYNC_DIAGS_ONLY, EPIC_UV_AB3, EPIC_UV_LEAPFROG, Fields, GridArrays,
-                        HSConfig, hs_setup)
+from epic_gb300 import (EPIC_ADV_AKIMA, EPIC_ADV_HSU, EPIC_PROFILE_N2, EPIC_SYNC_DIAGS_ONLY, EPIC_UV_AB3, EPIC_UV_LEAPFROG,
+                        Fields, GridArrays, HSConfig, hs_setup)
 from oracle_lib import Port, dict_to_fields, fields_to_dict, reference_available, run_reference
 
 GOLDEN = sorted(glob.glob(os.path.join(os.path.dirname(__file__), "golden", "*.npz")))
@@ -105,16 +105,19 @@ def test_golden_inputs_match_generator():
 
 
 @pytest.mark.reference
-@pytest.mark.parametrize("scheme,shape,steps,adv", [(EPIC_UV_AB3, (64, 32, 10), 12, EPIC_ADV_HSU),
-                                                     (EPIC_UV_LEAPFROG, (32, 16, 10), 6, EPIC_ADV_HSU),
-                                                     (EPIC_UV_AB3, (32, 16, 20), 4, EPIC_ADV_HSU),
-                                                     (EPIC_UV_AB3, (64, 32, 10), 12, EPIC_ADV_AKIMA),
-                                                     (EPIC_UV_LEAPFROG, (32, 16, 10), 6, EPIC_ADV_AKIMA)])
-def test_restatement_matches_reference(scheme, shape, steps, adv):
+@pytest.mark.parametrize("scheme,shape,steps,adv,state", [(EPIC_UV_AB3, (64, 32, 10), 12, EPIC_ADV_HSU, "hs"),
+                                                           (EPIC_UV_LEAPFROG, (32, 16, 10), 6, EPIC_ADV_HSU, "hs"),
+                                                           (EPIC_UV_AB3, (32, 16, 20), 4, EPIC_ADV_HSU, "hs"),
+                                                           (EPIC_UV_AB3, (64, 32, 10), 12, EPIC_ADV_AKIMA, "hs"),
+                                                           (EPIC_UV_LEAPFROG, (32, 16, 10), 6, EPIC_ADV_AKIMA, "hs"),
+                                                           (EPIC_UV_AB3, (64, 32, 10), 12, EPIC_ADV_HSU, "jet"),
+                                                           (EPIC_UV_LEAPFROG, (32, 16, 10), 6, EPIC_ADV_HSU, "jet")])
+def test_restatement_matches_reference(scheme, shape, steps, adv, state):
     if not reference_available():
         pytest.skip("reference source tree not present on this host")
     ni, nj, nk = shape
-    cfg = HSConfig(ni=ni, nj=nj, nk=nk, dt=300, uv_scheme=scheme, seed=5, advection_scheme=adv)
+    cfg = HSConfig(ni=ni, nj=nj, nk=nk, dt=300, uv_scheme=scheme, seed=5, advection_scheme=adv, state=state,
+                   profile=EPIC_PROFILE_N2 if state == "jet" else 0)
     ga, f = hs_setup(cfg)
     sched = [("sync", 0)] + [("step", 1)] * steps
     geo, snaps = run_reference(ga, f, sched)
@@ -165,3 +168,20 @@ def test_akima_fixture_differs_from_hsu():
     got = port.download()
     for k in ("hdry", "theta"):
         assert not np.array_equal(got.arrays[k], z["step1_" + k]), k
+
+
+def test_jet_fixture_inputs_match_generator():
+    """The jet fixture's inputs (constant-N^2 sounding grid, balanced jets, perturbation) equal
+    what epic_hs_grid_build/epic_jet_initial_state produce now, and the state is a jet state:
+    bottom pressure varying with latitude, zonal winds of tens of m/s."""
+    z = np.load(os.path.join(os.path.dirname(__file__), "golden", "jet32x16x10_ab3.npz"))   # seed 15
+    cfg = HSConfig(ni=32, nj=16, nk=10, dt=300, seed=15, profile=EPIC_PROFILE_N2, state="jet")
+    ga, f = hs_setup(cfg)
+    ga0 = grid_from_fixture(z)
+    for k in ga.arrays:
+        np.testing.assert_allclose(ga.arrays[k], ga0.arrays[k], rtol=1e-14, atol=0, err_msg=k)
+    for k in ("p3", "theta", "hdry", "u", "v"):
+        np.testing.assert_allclose(f.arrays[k], z["in_" + k], rtol=1e-12, atol=1e-12, err_msg=k)
+    pbot = f.arrays["p3"][10, 1:18, 5]
+    assert pbot.max() - pbot.min() > 5e3
+    assert np.abs(f.arrays["u"][0][1:11]).max() > 50.
