@@ -105,6 +105,7 @@ class RunServer:
     precision: int = EPIC_PREC_MIXED
     round_steps: int = 16                # most steps a class advances per scheduling pass
     keep_fields: bool = False            # keep each result's full state (else a checksum)
+    allow_jets: bool = False             # serve jet-state requests (see submit)
     backend: object = field(default_factory=DeviceBackend)
     waiting: list = field(default_factory=list)
     prepared: dict = field(default_factory=dict)    # rid -> (grid, initial fields, device bytes)
@@ -120,6 +121,11 @@ class RunServer:
         return time.perf_counter() - self.t0
 
     def submit(self, req: RunRequest) -> None:
+        # Serving a stream with jet-state requests mixed in raised an illegal device memory access
+        # once, whose cause has not been found; until it is, such requests are refused here (a
+        # jet state runs through Model on its own).
+        if req.cfg.state != "hs" and not self.allow_jets:
+            raise ValueError(f"request {req.rid}: only Held-Suarez-state requests are served")
         self.waiting.append(req)
 
     # -- admission -------------------------------------------------------------------------
