@@ -37,6 +37,48 @@ __device__ __forceinline__ ColTile col_tile(const DevModel &M) {
 // level k of a [k][lane] shared array
 #define CT(a, k) (a)[(k) * 32 + c.lane]
 
+// Running sum over the levels of every column of a tile, by all CT_WARPS warps: on entry
+// A[k] (k = 1..n) holds the increments and A[0] the starting value, on exit
+// A[k] = A[0] + A[1] + ... + A[k].  Each warp sums a contiguous chunk of levels, then adds the
+// totals of the chunks above it -- binary64 throughout, in an order other than the sequential
+// one (the mixed forms; the FP64 form keeps warp 0's sum in the reference's order).  Every
+// thread of the block must call it (it holds two barriers).
+__device__ __forceinline__ void ct_running_sum(double *A, int n, int lane, int warp) {
+  __shared__ double s_part[CT_WARPS * 32];
+  const int chunk = (n + CT_WARPS - 1) / CT_WARPS;
+  const int k0 = 1 + warp * chunk, k1 = min(n, k0 + chunk - 1);
+  double run = 0.;
+  for (int k = k0; k <= k1; k++) {
+    run += A[k * 32 + lane];
+    A[k * 32 + lane] = run;
+  }
+  s_part[warp * 32 + lane] = run;
+  __syncthreads();
+  double off = A[lane];
+  for (int w = 0; w < warp; w++) off += s_part[w * 32 + lane];
+  for (int k = k0; k <= k1; k++) A[k * 32 + lane] += off;
+  __syncthreads();
+}
+
+// The same from the bottom up: on entry A[n] holds the starting value and A[k] (k = 0..n-1) the
+// increments, on exit A[k] = A[n] + A[n-1] + ... + A[k].
+__device__ __forceinline__ void ct_running_sum_up(double *A, int n, int lane, int warp) {
+  __shared__ double s_part[CT_WARPS * 32];
+  const int chunk = (n + CT_WARPS - 1) / CT_WARPS;
+  const int k1 = n - 1 - warp * chunk, k0 = max(0, k1 - chunk + 1);
+  double run = 0.;
+  for (int k = k1; k >= k0; k--) {
+    run += A[k * 32 + lane];
+    A[k * 32 + lane] = run;
+  }
+  s_part[warp * 32 + lane] = run;
+  __syncthreads();
+  double off = A[n * 32 + lane];
+  for (int w = 0; w < warp; w++) off += s_part[w * 32 + lane];
+  for (int k = k1; k >= k0; k--) A[k * 32 + lane] += off;
+  __syncthreads();
+}
+
 // f_sigma/g_sigma (epic_funcs_diag.c:1271-1314) in the compute type, one exponential for both
 template <class R>
 __device__ __forceinline__ R f_and_g_sigma_r(const DevModel &M, R s, R &g) {

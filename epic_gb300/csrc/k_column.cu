@@ -635,15 +635,14 @@ __global__ void __launch_bounds__(CT_THREADS, 3) k_set_p2etc_mixed(DevModel M, i
     }
   }
   __syncthreads();
-  if (c.warp == 0 && c.valid) {   // P3 from the top down, in FP64
-    double p = M.p3[c.base];
-    CT(P, 0) = p;
-    for (int k = 1; k <= nk; k++) {
-      p = fma(M.dsgth[2 * k] * g, CT(HL, k), p);
-      CT(P, k) = p;
-    }
+  // P3 from the top down, in FP64: the layer pressure thicknesses dsgth g HDRY in parallel, then
+  // their running sum by every warp
+  if (c.valid) {
+    if (c.warp == 0) CT(P, 0) = M.p3[c.base];
+    for (int k = 1 + c.warp; k <= nk; k += CT_WARPS) CT(P, k) = M.dsgth[2 * k] * g * CT(HL, k);
   }
   __syncthreads();
+  ct_running_sum(P, nk, c.lane, c.warp);
   const double ptop = CT(P, 0), pbot = CT(P, nk);
   // log(ptop/pbot) and the pure-sigma interfaces pbot (ptop/pbot)^sigma in double-float, by every
   // warp (binary64 log/exp by warp 0 alone kept the other warps waiting at the barrier)
@@ -800,7 +799,14 @@ __global__ void __launch_bounds__(CT_THREADS, 3) k_pgrad_vars_column_mixed(DevMo
     }
   }
   __syncthreads();
-  if (c.valid)
+  // the geopotential increments of every layer (Leslie-Purser inside, short centred at the two
+  // ends; the differences of P and RHO in FP64), then GZ3 from the surface up by every warp
+  if (c.valid) {
+    if (c.warp == 0) CT(GZ, nk) = M.topo_scale * M.gz_surface[M.at2(c.j, c.i)];
+    if (c.warp == CT_WARPS - 1) {
+      CT(GZ, nk - 1) = ((CT(P, nk) + CT(P, nk - 1)) / (CT(R, nk) + CT(R, nk - 1))) * f2d(CT(LG, nk - 1));
+      CT(GZ, 0) = ((CT(P, 1) + CT(P, 0)) / (CT(R, 1) + CT(R, 0))) * f2d(CT(LG, 0));
+    }
     for (int k = 2 + c.warp; k <= nk - 1; k += CT_WARPS) {
       const float dz10 = CT(LG, k), dz21 = CT(LG, k - 1), dz32 = CT(LG, k - 2);
       const float dz20 = dz21 + dz10, dz30 = dz32 + dz20, dz31 = dz32 + dz21;
@@ -814,19 +820,9 @@ __global__ void __launch_bounds__(CT_THREADS, 3) k_pgrad_vars_column_mixed(DevMo
                                  df3 * (dz21 * dz21 * dz21 * (dz10 + dz20)) / (dz30 * dz31 * dz32)) /
                                12.f);
     }
-  __syncthreads();
-  if (c.warp == 0 && c.valid) {   // GZ3 from the surface up, in FP64
-    double gz = M.topo_scale * M.gz_surface[M.at2(c.j, c.i)];
-    CT(GZ, nk) = gz;
-    gz = gz + ((CT(P, nk) + CT(P, nk - 1)) / (CT(R, nk) + CT(R, nk - 1))) * f2d(CT(LG, nk - 1));
-    CT(GZ, nk - 1) = gz;
-    for (int k = nk - 1; k >= 2; k--) {
-      gz = gz + CT(GZ, k - 1);
-      CT(GZ, k - 1) = gz;
-    }
-    CT(GZ, 0) = gz + ((CT(P, 1) + CT(P, 0)) / (CT(R, 1) + CT(R, 0))) * f2d(CT(LG, 0));
   }
   __syncthreads();
+  ct_running_sum_up(GZ, nk, c.lane, c.warp);
   if (!c.valid) return;
   const bool interior = c.i >= 1 && c.i <= M.ni;
   const long long itime = M.ctl->itime;
