@@ -489,8 +489,9 @@ def run_gpu_ensemble(args):
     clocks = clk.summary()
     launches = batch.kernels_per_step * args.steps
 
-    # the dominant stage of the step (the pressure gradient, whose k_pgrad_lat is the top kernel
-    # of the launch list) and the vertical integration feeding it
+    # the largest stage of the step (the pressure gradient, 13-15% of it; k_pgrad_lat and
+    # k_pgrad_lon are among the top kernels of the launch list) and the vertical integration
+    # feeding it
     roof = batch_roofline(batch, cfg, nmem, stream, torch, stage=12)
     roof_column = batch_roofline(batch, cfg, nmem, stream, torch, stage=19)
 
