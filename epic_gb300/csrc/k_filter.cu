@@ -321,30 +321,46 @@ __global__ void k_varz_tables(DevModel M, const double *buff, int sel, int index
 // cubic's increment from the knot (FP32 on the FP64 distance gz - x_knot), and the filtered
 // deviation added back to it in binary64 -- the field itself is never rounded to FP32 (a
 // rounding of THETA or HDRY on the filtered rows every step feeds the pressure gradient,
-// which amplifies it).  HDRY is interpolated in log space: knot value exp(y) (once per knot and
-// row) times 1 + expm1(increment).
-__device__ __forceinline__ double varz_profile_mixed(const DevModel &M, const Trip *t, const double *knot, int n, int index,
+// which amplifies it).  HDRY is interpolated in log space: knot value exp(y) times
+// 1 + expm1(increment).  The knot values and the cubics' FP32 coefficients are tabulated once per
+// row (varz_intervals_mixed); the interval is found in FP32 (next to a knot either neighbouring
+// cubic gives the same value to the cubic's accuracy), the distance from its knot in binary64.
+struct VarzInterval { float x, z0, c2, c3; };
+__device__ __forceinline__ void varz_intervals_mixed(const Trip *t, int n, int index, double *knot, VarzInterval *iv) {
+  for (int q = threadIdx.x; q < n; q += blockDim.x) {
+    knot[q] = index == 2 ? ::exp(t[q].y) : t[q].y;
+    VarzInterval v;
+    v.x = d2f(t[q].x);
+    v.z0 = d2f(t[q].z);
+    v.c2 = v.c3 = 0.f;
+    if (q + 1 < n) {
+      const float h = d2f(t[q + 1].x - t[q].x);
+      const float delta = d2f(t[q + 1].y - t[q].y) / h;
+      const float del1 = (v.z0 - delta) / h, del2 = (d2f(t[q + 1].z) - delta) / h;
+      v.c3 = (del1 + del2) / h;
+      v.c2 = -(del1 + del1 + del2);
+    }
+    iv[q] = v;
+  }
+}
+__device__ __forceinline__ double varz_profile_mixed(const Trip *t, const double *knot, const VarzInterval *iv, int n, int index,
                                                      double gzd) {
+  const float g = d2f(gzd);
   int kay;
-  if (gzd <= t[0].x) kay = 0;
-  else if (gzd >= t[n - 1].x) kay = n - 2;
+  if (g <= iv[0].x) kay = 0;
+  else if (g >= iv[n - 1].x) kay = n - 2;
   else {
     int il = -1, iu = n;
     while (iu - il > 1) {
       const int im = (iu + il) >> 1;
-      if (gzd >= t[im].x) il = im; else iu = im;
+      if (g >= iv[im].x) il = im; else iu = im;
     }
     kay = il;
   }
-  const Trip *tk = t + kay;
-  const float h = d2f(tk[1].x - tk[0].x);
-  const float delta = d2f(tk[1].y - tk[0].y) / h;
-  const float z0 = d2f(tk[0].z);
-  const float del1 = (z0 - delta) / h, del2 = (d2f(tk[1].z) - delta) / h;
-  const float c3 = (del1 + del2) / h, c2 = -(del1 + del1 + del2);
-  const float xx = d2f(gzd - tk[0].x);
-  const float inc = xx * (z0 + xx * (c2 + xx * c3));
-  return index == 2 ? knot[kay] + knot[kay] * f2d(expm1f(inc)) : tk[0].y + f2d(inc);
+  const VarzInterval v = iv[kay];
+  const float xx = d2f(gzd - t[kay].x);
+  const float inc = xx * (v.z0 + xx * (v.c2 + xx * v.c3));
+  return index == 2 ? knot[kay] + knot[kay] * f2d(expm1f(inc)) : knot[kay] + f2d(inc);
 }
 
 // The rest of the THREEDIM zonal_filter: subtract var(gz), filter, add it back.
@@ -368,11 +384,11 @@ __global__ void k_varz_filter_rows(DevModel M, double *buff, int sel, int index,
   if (!filt && !std::is_same_v<R, double>) return;
   if constexpr (!std::is_same_v<R, double>) {
     double *vzd = reinterpret_cast<double *>(smraw), *knot = vzd + (M.ni + 2);
-    R *x = reinterpret_cast<R *>(knot + (M.nk + 2));
+    VarzInterval *iv = reinterpret_cast<VarzInterval *>(knot + (M.nk + 2));
+    R *x = reinterpret_cast<R *>(iv + (M.nk + 2));
     FilterSmem<R> fs = carve_filter(x + (M.ni + 2), M.ni);
     load_twiddles(M, fs);
-    if (index == 2)
-      for (int q = threadIdx.x; q < n; q += blockDim.x) knot[q] = ::exp(t[q].y);
+    varz_intervals_mixed(t, n, index, knot, iv);
     __syncthreads();
     for (int i = threadIdx.x + 1; i <= M.ni; i += blockDim.x) {
       double gzd;
@@ -382,7 +398,7 @@ __global__ void k_varz_filter_rows(DevModel M, double *buff, int sel, int index,
         case 2: gzd = .5 * (gz[M.at(k, j, i)] + gz[M.at(k - 1, j, i)]); break;
         default: gzd = gz[M.at(k, j, i)]; break;
       }
-      const double v = varz_profile_mixed(M, t, knot, n, index, gzd);
+      const double v = varz_profile_mixed(t, knot, iv, n, index, gzd);
       vzd[i] = v;
       x[i] = d2f(buff[base + i] - v);
     }
@@ -588,7 +604,8 @@ int launch_varz_filter(const DevModel &M, double *buff, int sel, int index, int 
   const int jstart = index == 1 ? 1 : 0;
   const int nrows = M.nj - jstart + 1;
   k_varz_tables<<<zg(epic_blocks(32LL * nrows, 128), M), 128, 0, s>>>(M, buff, sel, index, kstart, kend);
-  const size_t smem = M.mixed ? ((size_t)(M.ni + 2) + (M.nk + 2)) * sizeof(double) + ((size_t)(M.ni + 2) + filter_smem_elems(M.ni)) * sizeof(float)
+  const size_t smem = M.mixed ? ((size_t)(M.ni + 2) + (M.nk + 2)) * sizeof(double) + (size_t)(M.nk + 2) * sizeof(VarzInterval) +
+                                    ((size_t)(M.ni + 2) + filter_smem_elems(M.ni)) * sizeof(float)
                              : (2 * (size_t)(M.ni + 2) + filter_smem_elems(M.ni)) * sizeof(double);
   dim3 grid(nrows, kend - kstart + 1);
   EPIC_LAUNCH_R(M.mixed, k_varz_filter_rows, grid, row_threads(M), smem, s, M, buff, sel, index, kstart, kend);

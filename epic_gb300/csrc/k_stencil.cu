@@ -729,6 +729,12 @@ __global__ void k_zonal_visc(DevModel M, double *A, int sel, int jbot, int jhalf
   const unsigned full = 0xffffffffu;
   for (int i = lane; i <= ni + 1; i += 32) { a[i] = A[base + i]; hh[i] = cv<R>(a[i]); }
   __syncwarp();
+  if (!std::is_same_v<R, double>) {
+    // the mixed forms' first second difference is of the field itself: its neighbour
+    // differences a(i+1) - a(i) in binary64, one per point (k_d2dy2)
+    for (int i = lane; i <= ni; i += 32) hh[i] = cv<R>(a[i + 1] - a[i]);
+    __syncwarp();
+  }
   const bool taper = fabs(M.lat[2 * j + jhalf]) > M.lat0;
   const double mm = M.m[2 * j + jhalf];
   R sign = R(1.);
@@ -737,8 +743,8 @@ __global__ void k_zonal_visc(DevModel M, double *A, int sel, int jbot, int jhalf
 #pragma unroll
   for (int itmp = 2; itmp <= 8; itmp += 2) {
     const R dc = cv<R>(taper ? M.coef[itmp] * M.m0 * M.m0 : M.coef[itmp] * mm * mm);
-    if (!std::is_same_v<R, double> && itmp == 2)   // of the field itself: neighbour differences in binary64 (k_d2dy2)
-      for (int i = lane + 1; i <= ni; i += 32) d[i] = dc * (cv<R>(a[i - 1] - a[i]) + cv<R>(a[i + 1] - a[i]));
+    if (!std::is_same_v<R, double> && itmp == 2)   // differences of the neighbour differences
+      for (int i = lane + 1; i <= ni; i += 32) d[i] = dc * (hh[i] - hh[i - 1]);
     else
       for (int i = lane + 1; i <= ni; i += 32) d[i] = dc * (hh[i - 1] - R(2.) * hh[i] + hh[i + 1]);
     __syncwarp();
