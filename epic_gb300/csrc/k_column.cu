@@ -900,7 +900,10 @@ __global__ void k_gz_monotone(DevModel M) {
   for (int k = M.nk - 1; k >= 0; k--) {
     const long long x = M.at(k, j, i);
     double g;
-    if (fcmp(below, 0.) == 0) g = 1.e-3;
+    // fcmp(below, 0.) == 0 holds exactly when below is +-0 or NaN (for any other value the
+    // tolerance, DBL_EPSILON times 2^exponent, is below |below|): tested without frexp/ldexp,
+    // which cost ten FP64 instructions a level
+    if (below == 0. || below != below) g = 1.e-3;
     else g = dmaxr(M.gz[x], below + fabs(below) * 1.e-5);
     M.gz[x] = g;
     below = g;
