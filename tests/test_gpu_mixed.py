@@ -11,11 +11,11 @@ too (their running sums and the updates stay FP64).
 Stated error (relative L2 per field vs FP64, dt 300 s), measured on a GB300:
 
   form   shape      case                              U        V        HDRY     THETA
-  mixed  64x32x10   1 day after a 10-day spin-up      7.1e-6   2.3e-5   3.2e-8   3.1e-10
-  mixed  64x32x10   1 day from rest                   4.3e-5   2.3e-5   2.5e-8   2.0e-10
+  mixed  64x32x10   1 day after a 10-day spin-up      6.1e-6   2.1e-5   3.1e-8   3.1e-10
+  mixed  64x32x10   1 day from rest                   3.9e-5   2.5e-5   2.4e-8   2.0e-10
   mixed  64x32x10   12 h from rest, leapfrog          5.8e-4   1.4e-4   3.7e-8   9.5e-11
-  mixed  128x64x20  1 day after a 1-day spin-up       3.8e-5   2.4e-5   1.7e-7   8.4e-10
-  mixed  128x64x20  1 day from rest                   1.0e-4   1.4e-4   1.7e-6   9.1e-9
+  mixed  128x64x20  1 day after a 1-day spin-up       3.8e-5   2.3e-5   1.7e-7   8.4e-10
+  mixed  128x64x20  1 day from rest                   1.0e-4   1.3e-4   1.6e-6   8.3e-9
   fast   64x32x10   1 day after a 10-day spin-up      3.7e-5   6.0e-4   3.8e-7   3.7e-8
   fast   64x32x10   1 day from rest                   2.5e-4   8.7e-4   2.1e-7   3.7e-8
   fast   64x32x10   12 h from rest, leapfrog          1.8e-3   6.4e-4   1.6e-7   3.7e-8
