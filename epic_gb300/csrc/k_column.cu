@@ -916,11 +916,12 @@ __global__ void k_gz_monotone(DevModel M) {
 template <class R>
 __global__ void k_calc_heating(DevModel M) {
   epic_member(M);
-  const long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
-  if (t >= M.n3) return;
-  const int i = (int)(t % M.iadim);
-  const int j = (int)((t / M.iadim) % M.jadim) - 1;
-  const int k = (int)(t / M.n2);
+  const unsigned t = blockIdx.x * blockDim.x + threadIdx.x;   // n3 < 2^31
+  if (t >= (unsigned)M.n3) return;
+  const unsigned r = t / (unsigned)M.iadim, q = r / (unsigned)M.jadim;
+  const int i = (int)(t - r * (unsigned)M.iadim);
+  const int j = (int)(r - q * (unsigned)M.jadim) - 1;
+  const int k = (int)q;
   R val = R(0.);
   int ii = i == 0 ? M.ni : (i == M.ni + 1 ? 1 : i);
   if (k >= 1 && k <= M.nk && j >= 0 && j <= M.nj && M.newt_cool_on) {
@@ -950,11 +951,12 @@ __global__ void k_calc_heating(DevModel M) {
 // phase 2: THETA -= OLD*(UNITY-1) for k >= k_sigma-1.
 __global__ void k_advection_prep(DevModel M, int phase) {
   epic_member(M);
-  const long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
-  const long long w = (long long)(M.nj + 1) * M.iadim;
-  if (t >= w * (M.nk + 2)) return;
-  const int k = (int)(t / w);
-  const long long x = M.at(k, 0, 0) + t % w;
+  const unsigned t = blockIdx.x * blockDim.x + threadIdx.x;   // fewer than n3 < 2^31 cells
+  const unsigned w = (unsigned)(M.nj + 1) * (unsigned)M.iadim;
+  if (t >= w * (unsigned)(M.nk + 2)) return;
+  const unsigned q = t / w;
+  const int k = (int)q;
+  const long long x = M.at(k, 0, 0) + (t - q * w);
   if (phase == 0) M.unity[x] = 1.;
   else if (k >= M.k_sigma - 1) {
     if (phase == 1) M.old[x] = M.theta[x];

@@ -9,15 +9,26 @@ namespace epic {
 
 // Cell index helpers for 3-D launches over k in [k0, k0+nk), j in [j0, j0+nj), i in 1..ni.
 struct Cell { int k, j, i; };
+// The index arithmetic is 32-bit unsigned (two divisions, remainders by multiply-subtract): a
+// launch covers fewer than 2^31 cells of a member (epic_model_create bounds a field below 2^31
+// elements), and 64-bit divisions cost as many instructions as the stencil's own loads.
 __device__ __forceinline__ bool cell3(const DevModel &M, int k0, int nkk, int j0, int njj, Cell &c) {
-  const long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
-  const long long tot = (long long)nkk * njj * M.ni;
-  if (t >= tot) return false;
-  c.i = 1 + (int)(t % M.ni);
-  const long long r = t / M.ni;
-  c.j = j0 + (int)(r % njj);
-  c.k = k0 + (int)(r / njj);
+  const unsigned t = blockIdx.x * blockDim.x + threadIdx.x;
+  const unsigned ni = (unsigned)M.ni, nr = (unsigned)njj;
+  if (t >= (unsigned)nkk * nr * ni) return false;
+  const unsigned r = t / ni, q = r / nr;
+  c.i = 1 + (int)(t - r * ni);
+  c.j = j0 + (int)(r - q * nr);
+  c.k = k0 + (int)q;
   return true;
+}
+// (k, j, i) of cell t of the interior layers k = 1..nk-1, rows j = 0..nj (the wind updates)
+__device__ __forceinline__ void cell_kji(const DevModel &M, unsigned t, int &k, int &j, int &i) {
+  const unsigned ni = (unsigned)M.ni, nr = (unsigned)(M.nj + 1);
+  const unsigned r = t / ni, q = r / nr;
+  i = 1 + (int)(t - r * ni);
+  j = (int)(r - q * nr);
+  k = 1 + (int)q;
 }
 static inline unsigned cells_blocks(const DevModel &M, int nkk, int njj, int th) {
   return epic_blocks((long long)nkk * njj * M.ni, th);
@@ -915,14 +926,12 @@ __global__ void k_ri2(DevModel M) {
 template <class R>
 __global__ void k_divdamp_apply(DevModel M, double nudiv) {
   epic_member(M);
-  const long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
-  const long long per = (long long)(M.nk - 1) * (M.nj + 1) * M.ni;
+  const unsigned t = blockIdx.x * blockDim.x + threadIdx.x;
+  const unsigned per = (unsigned)(M.nk - 1) * (unsigned)(M.nj + 1) * (unsigned)M.ni;
   if (t >= 2 * per) return;
   const int isv = t >= per;
-  const long long r = isv ? t - per : t;
-  const int i = 1 + (int)(r % M.ni);
-  const int j = (int)((r / M.ni) % (M.nj + 1));
-  const int k = 1 + (int)(r / ((long long)M.ni * (M.nj + 1)));
+  int i, j, k;
+  cell_kji(M, isv ? t - per : t, k, j, i);
   const double *DIV = M.work2;
   const long long off = plane_offset(M, PL_UV_TEND);
   if (!isv) {
@@ -962,14 +971,12 @@ __global__ void k_uv_decide(DevModel M) {
 
 __global__ void k_uv_update(DevModel M) {
   epic_member(M);
-  const long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
-  const long long per = (long long)(M.nk - 1) * (M.nj + 1) * M.ni;
+  const unsigned t = blockIdx.x * blockDim.x + threadIdx.x;
+  const unsigned per = (unsigned)(M.nk - 1) * (unsigned)(M.nj + 1) * (unsigned)M.ni;
   if (t >= 2 * per) return;
   const int w = t >= per;
-  const long long r = w ? t - per : t;
-  const int i = 1 + (int)(r % M.ni);
-  const int j = (int)((r / M.ni) % (M.nj + 1));
-  const int k = 1 + (int)(r / ((long long)M.ni * (M.nj + 1)));
+  int i, j, k;
+  cell_kji(M, w ? t - per : t, k, j, i);
   if (w == 1 && j == 0) return;   // v is updated for j = 1..nj
   const Ctl *c = M.ctl;
   double *val = w == 0 ? M.u : M.v;
