@@ -710,6 +710,45 @@ __global__ void k_d2dy2(DevModel M, const double *src, int src_sel, double *dst,
   write_with_pads(dst, M, M.at(k, j, 0), i, d);
 }
 
+// The mixed forms' first two d2dy2 passes of meridional_hyperviscosity in one kernel: the first
+// (of the state field, binary64 differences as in k_d2dy2) into shared memory, the second from
+// there into dst.  Block = 32 columns of one layer k0 + blockIdx.y, every row; the values are
+// those of two k_d2dy2<float> launches (the intermediate is a float either way), without the
+// intermediate volume's write and read.
+__global__ void k_d2dy2_pair_mixed(DevModel M, const double *src, int src_sel, double *dst, int vgrid, double coef1, double coef2,
+                                   int k0) {
+  epic_member(M, src, dst);
+  extern __shared__ __align__(16) unsigned char smraw[];
+  float *d1 = reinterpret_cast<float *>(smraw);   // [row][lane]
+  src += plane_offset(M, src_sel);
+  const int lane = (int)(threadIdx.x & 31), w = (int)(threadIdx.x >> 5), nw = (int)(blockDim.x >> 5);
+  const int i = (int)blockIdx.x * 32 + lane + 1;
+  const int k = k0 + (int)blockIdx.y;
+  const int nj = M.nj, jlast = vgrid ? nj + 1 : nj;
+  const double *cfa = vgrid ? M.v_coef : M.h_coef;
+  const bool live = i <= M.ni;
+  for (int j = w; j <= jlast; j += nw) {
+    float d = 0.f;
+    if (live) {
+      const double *cf = cfa + 3 * j;
+      const float a0 = d2f(coef1) * d2f(cf[0]), a2 = d2f(coef1) * d2f(cf[2]);
+      const int m = j == 0 ? 1 : (j == jlast ? j - 1 : j);
+      const double hm = src[M.at(k, m, i)];
+      d = a0 * d2f(src[M.at(k, m - 1, i)] - hm) + a2 * d2f(src[M.at(k, m + 1, i)] - hm);
+    }
+    d1[j * 32 + lane] = d;
+  }
+  __syncthreads();
+  if (!live) return;
+  for (int j = w; j <= jlast; j += nw) {
+    const double *cf = cfa + 3 * j;
+    const float a0 = d2f(coef2) * d2f(cf[0]), a1 = d2f(coef2) * d2f(cf[1]), a2 = d2f(coef2) * d2f(cf[2]);
+    const int m = j == 0 ? 1 : (j == jlast ? j - 1 : j);
+    const float d = a0 * d1[(m - 1) * 32 + lane] + a1 * d1[m * 32 + lane] + a2 * d1[(m + 1) * 32 + lane];
+    write_with_pads(dst, M, M.at(k, j, 0), i, f2d(d));
+  }
+}
+
 // A += dt*sign*D over the rows the reference updates (v: 1..nj, h: 0..nj).
 template <class R>
 __global__ void k_visc_apply(DevModel M, double *A, int sel, const double *D, int vgrid, double sign, int k0, int nkk) {
@@ -1120,10 +1159,23 @@ int launch_meridional_hyperviscosity(const DevModel &M, int index, double *var, 
   double *bufs[2] = {M.work1, M.work2};
   int which = 0;
   double sign = 1.;
+  // the mixed forms fuse the first two passes when nothing is applied between them
+  const size_t pair_smem = (size_t)nrows * 32 * sizeof(float);
+  const bool pair = M.mixed && !(M.nu[2] > 0.) && M.nu[4] + M.nu[6] + M.nu[8] > 0. && pair_smem <= 48 * 1024;
   for (int itmp = 2; itmp <= 8; itmp += 2) {
     double *dst = bufs[which];
-    EPIC_LAUNCH_R(M.mixed, k_d2dy2, cells_blocks(M, nkk, nrows, TB(M, TB_VISC)), TB(M, TB_VISC), 0, s, M, cur_src, src_sel, dst, vgrid, M.coef[itmp], k0, nkk,
-                  cur_src == var);
+    if (pair && itmp == 2) {
+      // the second pass's output goes where the unfused loop leaves it
+      dst = bufs[1];
+      k_d2dy2_pair_mixed<<<zg(dim3((unsigned)((M.ni + 31) / 32), (unsigned)nkk), M), 256, pair_smem, s>>>(M, var, sel, dst, vgrid, M.coef[2],
+                                                                                                        M.coef[4], k0);
+      itmp = 4;
+      which = 1;
+      sign = -sign;
+    } else {
+      EPIC_LAUNCH_R(M.mixed, k_d2dy2, cells_blocks(M, nkk, nrows, TB(M, TB_VISC)), TB(M, TB_VISC), 0, s, M, cur_src, src_sel, dst, vgrid, M.coef[itmp], k0,
+                    nkk, cur_src == var);
+    }
     src_sel = PL_NONE;
     if (M.nu[itmp] > 0.) {
       launch_filter_planes(M, dst, PL_NONE, dst, k0, nkk, vgrid, s, M.mixed);
