@@ -587,13 +587,15 @@ static int row_threads(const DevModel &M) { return M.tb[TB_ROW] > 0 ? M.tb[TB_RO
 static size_t relem(int fp32) { return fp32 ? sizeof(float) : sizeof(double); }
 
 int launch_filter_planes(const DevModel &M, const double *src, int src_sel, double *dst, int k0, int nplanes, int vgrid, cudaStream_t s,
-                         int fp32, int shift) {
+                         int fp32, int shift, int pads_set) {
   if (nplanes <= 0) return 0;
   const size_t smem = ((size_t)(M.ni + 2) + filter_smem_elems(M.ni)) * relem(fp32);
   dim3 grid(M.nj + 3, nplanes);
   if (fp32 && filter_gemm_usable(M)) {
     const long long warps = (long long)(M.nj + 3) * nplanes;
-    k_filter_rows_unfiltered<<<zg(epic_blocks(32 * warps, 128), M), 128, 0, s>>>(M, src, src_sel, dst, k0, nplanes, vgrid);
+    // in place with the pads already set, the rows left unfiltered need nothing
+    if (!(pads_set && src == dst && src_sel == PL_NONE))
+      k_filter_rows_unfiltered<<<zg(epic_blocks(32 * warps, 128), M), 128, 0, s>>>(M, src, src_sel, dst, k0, nplanes, vgrid);
     return launch_filter_planes_gemm(M, src, src_sel, dst, k0, nplanes, vgrid, s, shift);
   }
   EPIC_LAUNCH_R(fp32, k_filter_planes, grid, row_threads(M), smem, s, M, src, src_sel, dst, k0, vgrid);

@@ -1178,7 +1178,8 @@ int launch_meridional_hyperviscosity(const DevModel &M, int index, double *var, 
     }
     src_sel = PL_NONE;
     if (M.nu[itmp] > 0.) {
-      launch_filter_planes(M, dst, PL_NONE, dst, k0, nkk, vgrid, s, M.mixed);
+      // k_d2dy2 / k_d2dy2_pair_mixed wrote every row of dst with its pads
+      launch_filter_planes(M, dst, PL_NONE, dst, k0, nkk, vgrid, s, M.mixed, 0, 1);
       EPIC_LAUNCH_R(M.mixed, k_visc_apply, cells_blocks(M, nkk, vgrid ? M.nj : M.nj + 1, TB(M, TB_VISC)), TB(M, TB_VISC), 0, s, M, var, sel, dst, vgrid, sign, k0, nkk);
     }
     sign = -sign;

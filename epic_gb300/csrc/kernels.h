@@ -38,8 +38,10 @@ inline dim3 zg(dim3 g, const DevModel &M) {
 // fp32: filter in FP32 (the mixed forms; on the tensor cores for ni a multiple of 128).
 // shift (tensor-core path only): filter x - x(i=1) of each row and add x(i=1) back in binary64,
 // for fields whose zonal variations are small beside their value (the geopotential).
+// pads_set: an in-place call whose rows 0..nj(+1) already carry their periodic pads (the
+// tensor-core path then touches the filtered rows only).
 int launch_filter_planes(const DevModel &M, const double *src, int src_sel, double *dst, int k0, int nplanes, int vgrid, cudaStream_t s,
-                         int fp32 = 0, int shift = 0);
+                         int fp32 = 0, int shift = 0, int pads_set = 0);
 int launch_varz_filter(const DevModel &M, double *buff, int sel, int index, int kstart, int kend, cudaStream_t s);
 int launch_hsu_zonal(const DevModel &M, double *buff, int kind, int kstart, cudaStream_t s);
 int filter_kernels_init(int ni);
