@@ -1082,7 +1082,8 @@ int launch_zero_tend(const DevModel &M, cudaStream_t s) {
 int launch_uv_core(const DevModel &M, cudaStream_t s) {
   EPIC_LAUNCH_R(M.mixed, k_uv_kin, cells_blocks(M, M.nk - 1, M.nj + 1, TB(M, TB_UV_CORE)), TB(M, TB_UV_CORE), 0, s, M);
   EPIC_LAUNCH_R(M.mixed, k_uv_core_v, cells_blocks(M, M.nk - 1, M.nj, TB(M, TB_UV_CORE)), TB(M, TB_UV_CORE), 0, s, M);
-  launch_filter_planes(M, M.work0, PL_NONE, M.work0, 1, M.nk - 1, 0, s, M.mixed);
+  // k_uv_kin wrote KIN on rows 0..nj with their pads
+  launch_filter_planes(M, M.work0, PL_NONE, M.work0, 1, M.nk - 1, 0, s, M.mixed, 0, 1);
   EPIC_LAUNCH_R(M.mixed, k_uv_core_u, cells_blocks(M, M.nk - 1, M.nj + 1, TB(M, TB_UV_CORE)), TB(M, TB_UV_CORE), 0, s, M);
   return 0;
 }
