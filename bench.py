@@ -136,36 +136,78 @@ class ClockSampler:
 # CPU side: the oracle's restatement of the reference step
 # ---------------------------------------------------------------------------------------------
 
-def _cpu_replica(name, seed, nsteps, warm, advection, q):
+def kf_scales(n, seed=7):
+    """The ensemble's drag-rate factors: member q runs with k_f * (1 + U[-0.1, 0.1]), drawn in order."""
+    import numpy as np
+    rng = np.random.default_rng(seed)
+    return [1.0 + float(rng.uniform(-0.1, 0.1)) for _ in range(n)]
+
+
+def _cpu_worker(name, jobs, nsteps, warm, advection, q):
+    """Step each (seed, k_f factor) grid of `jobs` in turn on this core: set-up, priming and
+    `warm` steps untimed, then `nsteps` timed steps; reports the summed timed seconds."""
     sys.path.insert(0, os.path.join(ROOT, "tests"))
     from oracle_lib import Port
     from epic_gb300 import EPIC_SYNC_DIAGS_ONLY, hs_setup
-    cfg = _workload_cfg(name, seed, advection)
-    ga, f = hs_setup(cfg)
-    p = Port(ga)
-    p.upload(f)
-    p.timestep(EPIC_SYNC_DIAGS_ONLY)
-    p.run(warm)
-    t0 = time.perf_counter()
-    p.run(nsteps)
-    q.put(time.perf_counter() - t0)
+    total = 0.
+    for seed, scale in jobs:
+        cfg = _workload_cfg(name, seed, advection)
+        ga, f = hs_setup(cfg)
+        ga.struct.hs_kf *= scale
+        p = Port(ga)
+        p.upload(f)
+        p.timestep(EPIC_SYNC_DIAGS_ONLY)
+        p.run(warm)
+        t0 = time.perf_counter()
+        p.run(nsteps)
+        total += time.perf_counter() - t0
+    q.put(total)
 
 
-def cpu_reference(name, nsteps, warm, procs, advection="hsu"):
-    """Aggregate cell-steps/s of `procs` independent single-threaded replicas of the reference step."""
+def cpu_reference(name, nsteps, warm, procs, advection="hsu", grids=1, scales=None):
+    """Aggregate cell-steps/s of the reference step (the oracle's restatement, single-threaded
+    like the reference) over `grids` grids spread round-robin over `procs` worker processes, one
+    per host core: grid g has noise seed g and k_f factor scales[g].  The rate is the cells of
+    every grid times nsteps over the slowest worker's timed seconds."""
     sys.path.insert(0, os.path.join(ROOT, "tests"))
     from oracle_lib import build_port
     build_port()
+    scales = scales or [1.0] * grids
+    nw = max(1, min(procs, grids))
+    jobs = [[] for _ in range(nw)]
+    for g in range(grids):
+        jobs[g % nw].append((g, scales[g]))
     ctx = mp.get_context("spawn")
     q = ctx.Queue()
-    ps = [ctx.Process(target=_cpu_replica, args=(name, s, nsteps, warm, advection, q)) for s in range(procs)]
+    ps = [ctx.Process(target=_cpu_worker, args=(name, j, nsteps, warm, advection, q)) for j in jobs]
     for p in ps:
         p.start()
     times = [q.get(timeout=3600) for _ in ps]
     for p in ps:
         p.join()
     cfg = _workload_cfg(name)
-    return sum(cfg.cells * nsteps / t for t in times), max(times)
+    wall = max(times)
+    return grids * cfg.cells * nsteps / wall, wall
+
+
+def workload_config(args, cfg, nmem, ws):
+    """The `config` object of both arms' lines: the workload only (shape, members, time step,
+    schemes, state), so that the GPU arm and the reference arm name the same one."""
+    state = ("6 seeded Gaussian zonal jets (50-150 m/s, centres -70..70 deg, widths 3-8 deg) in gradient-wind balance "
+             "on a constant N^2 = 1e-4 s^-2 sounding (isothermal at 200 K above), 1% seeded vorticity perturbation"
+             if cfg.state == "jet" else "horizontally uniform HS equilibrium column at rest + seeded 0.1 K theta noise")
+    # u, v (AB3: one plane each), three tendency planes each, 20 single fields
+    state_gb = nmem * 28 * 8 * (cfg.ni + 2) * (cfg.nj + 3) * (cfg.nk + 2) / 1e9
+    if nmem > 1:
+        what = (f"ensemble of {nmem} Held-Suarez members {cfg.ni}x{cfg.nj}x{cfg.nk}, dt={cfg.dt}s, AB3, "
+                f"{ADVECTION_NAME[args.advection]}, nu4=0.5 max, seeded 0.1 K noise and +/-10% k_f per member")
+    else:
+        what = (("Zonal jets on the Held-Suarez planet " if cfg.state == "jet" else "Held-Suarez ") +
+                f"{cfg.ni}x{cfg.nj}x{cfg.nk}, dt={cfg.dt}s, AB3, {ADVECTION_NAME[args.advection]}, nu4=0.5 max")
+    return {"workload": what, "ni": cfg.ni, "nj": cfg.nj, "nk": cfg.nk, "dt": cfg.dt, "members": nmem,
+            "advection": args.advection, "parallelism": f"replicas{ws}", "state": state,
+            "l2": f"every step reads and writes the whole state, {state_gb:.2f} GB of binary64 arrays "
+                  + ("> 129 MB L2; no flush needed" if state_gb > 0.129 else "(fits in the 129 MB L2; no flush)")}
 
 
 # ---------------------------------------------------------------------------------------------
@@ -246,17 +288,8 @@ def run_gpu(args):
             "metric": METRIC, "value": value, "unit": "cell-steps/s", "n_gpus": ws, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": ms_step, "higher_is_better": True, "scaling": "weak",
             "vs_baseline": None, "dtype": "f64" if args.precision == "fp64" else "f32+f64", "data": "synthetic",
-            "config": {"workload": ("Zonal jets on the Held-Suarez planet " if cfg.state == "jet" else "Held-Suarez ") +
-                                   f"{cfg.ni}x{cfg.nj}x{cfg.nk}, dt={cfg.dt}s, AB3, "
-                                   f"{ADVECTION_NAME[args.advection]}, nu4=0.5 max, "
-                                   + ("FP64 drop-in form" if args.precision == "fp64" else f"{args.precision} form"),
-                       "ni": cfg.ni, "nj": cfg.nj, "nk": cfg.nk, "dt": cfg.dt,
-                       "precision": args.precision, "advection": args.advection, "parallelism": f"replicas{ws}",
-                       "l2": f"state {model.device_bytes / 1e9:.2f} GB > 129 MB L2; no flush needed",
-                       "state": ("6 seeded Gaussian zonal jets (50-150 m/s, centres -70..70 deg, widths 3-8 deg) in "
-                                 "gradient-wind balance on a constant N^2 = 1e-4 s^-2 sounding (isothermal at 200 K above), "
-                                 "1% seeded vorticity perturbation" if cfg.state == "jet" else
-                                 "horizontally uniform HS equilibrium column at rest + seeded 0.1 K theta noise")},
+            "config": workload_config(args, cfg, 1, ws),
+            "form": args.precision,
             "clocks": clocks,
             "e2e": {"value": e2e_val, "unit": "cell-steps/s", "h2d_bytes_per_step": host.nbytes,
                     "d2h_bytes_per_step": host.nbytes},
@@ -277,13 +310,11 @@ def run_gpu(args):
 
 def _members(cfg, n, precision, torch_seed=7):
     """n ensemble members of one shape: member q has noise seed q and k_f scaled by 1 +/- 10%."""
-    import numpy as np
     from epic_gb300 import HSConfig, Model, hs_setup
-    rng = np.random.default_rng(torch_seed)
     out = []
-    for q in range(n):
+    for q, scale in enumerate(kf_scales(n, torch_seed)):
         ga, f = hs_setup(HSConfig(ni=cfg.ni, nj=cfg.nj, nk=cfg.nk, dt=cfg.dt, seed=q, advection_scheme=cfg.advection_scheme))
-        ga.struct.hs_kf *= 1.0 + float(rng.uniform(-0.1, 0.1))
+        ga.struct.hs_kf *= scale
         m = Model(ga, precision)
         m.upload(f)
         out.append(m)
@@ -352,39 +383,60 @@ def mixed_error(torch, precision, advection="hsu"):
     return out
 
 
-def ensemble_error(torch, precision, cfg, nmem=8, steps=288):
-    """The ensemble error at the member shape (where the tensor-core filter paths run): nmem
-    members (ensemble_rate's seeds and k_f perturbations) stepped one simulated day from rest as
-    a batch in the given form and in FP64.  Reported per prognostic: relative L2 of the ensemble
-    mean and of the ensemble spread (standard deviation over members) against FP64's, and the
-    largest per-member relative L2."""
+_ENSEMBLE_RUNS = {}
+
+
+def _ensemble_day(cfg, nmem, precision, steps):
+    """Prognostic fields of every member after `steps` steps from rest, stepped as one batch
+    (the launch shapes of the timed ensemble: with 64 members of 128x64x20 the meridional Hsu
+    passes of UNITY and HDRY take the fused march).  Cached per form: the FP64 run serves every
+    form's comparison."""
     import numpy as np
-    sys.path.insert(0, os.path.join(ROOT, "tests"))
-    from compare import PROGNOSTIC, field_errors
-    from epic_gb300 import EPIC_PREC_FP64, EPIC_SYNC_DIAGS_ONLY, Batch
-    runs = []
-    for prec in (EPIC_PREC_FP64, precision):
-        members = _members(cfg, nmem, prec, torch_seed=7)
+    from epic_gb300 import EPIC_SYNC_DIAGS_ONLY, Batch
+    key = (cfg.ni, cfg.nj, cfg.nk, cfg.dt, cfg.advection_scheme, nmem, precision, steps)
+    if key not in _ENSEMBLE_RUNS:
+        members = _members(cfg, nmem, precision, torch_seed=7)
         b = Batch(members)
         b.timestep(EPIC_SYNC_DIAGS_ONLY)
         b.run(steps)
         b.sync()
-        runs.append([m.download() for m in members])
+        out = []
+        for m in members:
+            f = m.download()
+            out.append({k: np.array(f.arrays[k], copy=True) for k in ("u", "v", "hdry", "theta")})
         b.close()
         for m in members:
             m.close()
-    ref, got = runs
-    out = {"mean": {}, "spread": {}, "member_max": {}}
-    for k in PROGNOSTIC:
-        a = np.stack([f.arrays[k] for f in got])
-        r = np.stack([f.arrays[k] for f in ref])
-        big = np.abs(r) > 1e300
-        a, r = np.where(big, 0., a), np.where(big, 0., r)
+        _ENSEMBLE_RUNS[key] = out
+    return _ENSEMBLE_RUNS[key]
+
+
+def ensemble_error(torch, precision, cfg, nmem=64, steps=288):
+    """The ensemble error at the member shape, on the timed ensemble itself: nmem members
+    (ensemble_rate's seeds and k_f perturbations) stepped one simulated day from rest as a batch
+    in the given form and in FP64.  Reported per prognostic: relative L2 of the ensemble mean and
+    of the ensemble spread (standard deviation over members) against FP64's, and the largest and
+    the median per-member relative L2 (relative L2 over each member's interior cells)."""
+    import numpy as np
+    from epic_gb300 import EPIC_PREC_FP64
+    from epic_gb300.abi import Layout
+    ref = _ensemble_day(cfg, nmem, EPIC_PREC_FP64, steps)
+    got = _ensemble_day(cfg, nmem, precision, steps)
+    L = Layout(cfg.ni, cfg.nj, cfg.nk)
+    kinds = {"u": "uv", "v": "vv", "hdry": "h", "theta": "h"}
+    out = {"mean": {}, "spread": {}, "member_max": {}, "member_median": {}, "max_abs_over_max": {}}
+    for k in ("u", "v", "hdry", "theta"):
+        plane = (lambda a: a[0]) if k in ("u", "v") else (lambda a: a)
+        a = np.stack([L.interior(plane(g[k]), kinds[k]) for g in got])
+        r = np.stack([L.interior(plane(f[k]), kinds[k]) for f in ref])
         out["mean"][k] = float(np.linalg.norm(a.mean(0) - r.mean(0)) / np.linalg.norm(r.mean(0)))
         out["spread"][k] = float(np.linalg.norm(a.std(0) - r.std(0)) / np.linalg.norm(r.std(0)))
-        out["member_max"][k] = max(field_errors(g, f, (k,))[k][0] for g, f in zip(got, ref))
-    out["case"] = (f"{nmem} members {cfg.ni}x{cfg.nj}x{cfg.nk}, dt={cfg.dt} s, {steps} steps from rest, batched, "
-                   f"relative L2 vs the FP64 members")
+        per = [float(np.linalg.norm(x - y) / np.linalg.norm(y)) for x, y in zip(a, r)]
+        out["member_max"][k] = max(per)
+        out["member_median"][k] = float(np.median(per))
+        out["max_abs_over_max"][k] = float(np.abs(a - r).max() / np.abs(r).max())
+    out["case"] = (f"{nmem} members {cfg.ni}x{cfg.nj}x{cfg.nk}, dt={cfg.dt} s, {steps} steps (1 simulated day) from rest, "
+                   f"batched as in the timed run, relative L2 over interior cells vs the FP64 members")
     return out
 
 
@@ -443,7 +495,7 @@ def run_gpu_ensemble(args):
     precision = _prec(args.precision)
     cfg = _workload_cfg(args.workload, advection=args.advection)
     nmem = args.members or ENSEMBLE[args.workload]
-    members = _members(cfg, nmem, precision, torch_seed=7 + rank)
+    members = _members(cfg, nmem, precision, torch_seed=7)
     starts = [m.download() for m in members]
     batch = Batch(members)
     tuning = None
@@ -518,16 +570,12 @@ def run_gpu_ensemble(args):
             "metric": METRIC, "value": value, "unit": "cell-steps/s", "n_gpus": ws, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": ms_step, "higher_is_better": True, "scaling": "weak",
             "vs_baseline": None, "dtype": "f64" if precision == EPIC_PREC_FP64 else "f32+f64", "data": "synthetic",
-            "config": {"workload": f"ensemble of {nmem} Held-Suarez members {cfg.ni}x{cfg.nj}x{cfg.nk}, dt={cfg.dt}s, AB3, "
-                                   f"{ADVECTION_NAME[args.advection]}, seeded 0.1 K noise and +/-10% k_f per member, {args.precision} form, one launch per "
-                                   f"kernel for all members", "ni": cfg.ni, "nj": cfg.nj, "nk": cfg.nk, "dt": cfg.dt,
-                       "members": nmem, "precision": args.precision, "advection": args.advection,
-                       "parallelism": f"replicas{ws}",
-                       "launch_shapes": {"autotuned_block_sizes": tuning,
-                                         "groups": ["uv_core", "pgrad", "hsu_meridional", "hyperviscosity", "diagnostics",
-                                                    "update", "column", "pointwise", "row_filter"]},
-                       "l2": f"ensemble state {state_gb:.1f} GB > 129 MB L2; no flush needed",
-                       "state": "horizontally uniform HS equilibrium column at rest + seeded 0.1 K theta noise"},
+            "config": workload_config(args, cfg, nmem, ws),
+            "form": f"{args.precision} precision form, one launch per kernel for all members under a captured CUDA graph",
+            "launch_shapes": {"autotuned": tuning,
+                              "groups": ["uv_core", "pgrad", "hsu_meridional", "hyperviscosity", "diagnostics",
+                                         "update", "column", "pointwise", "row_filter",
+                                         "hsu_meridional_form (1 fused march, 2 four passes)"]},
             "clocks": clocks,
             "e2e": {"value": e2e_val, "unit": "cell-steps/s", "h2d_bytes_per_step": host_bytes, "d2h_bytes_per_step": host_bytes},
             "gpu_launches": launches,
@@ -547,12 +595,12 @@ def run_gpu_ensemble(args):
             out["batched_over_fp64_single"] = value / ws / fp64["value"]
             if precision != EPIC_PREC_FP64:
                 out["mixed_error"] = mixed_error(torch, precision, args.advection)
-                out["ensemble_error"] = ensemble_error(torch, precision, cfg)
+                out["ensemble_error"] = ensemble_error(torch, precision, cfg, nmem)
             if args.precision == "mixed":
                 # the faster form that keeps the vertical integration and pressure gradient in FP32
                 fast = ensemble_rate(cfg, nmem, _prec("fast"), args, torch, rank)
                 out["mixed_fast"] = dict(fast, error=mixed_error(torch, _prec("fast"), args.advection),
-                                         ensemble_error=ensemble_error(torch, _prec("fast"), cfg),
+                                         ensemble_error=ensemble_error(torch, _prec("fast"), cfg, nmem),
                                          note="EPIC_PREC_MIXED_FAST ensemble, same workload and timing")
             out["serving"] = serving_summary(precision)
     if ws > 1:
@@ -677,22 +725,24 @@ def main():
         if rank != 0:
             return
         procs = os.cpu_count() or 1
-        steps = max(1, min(args.steps, 3))
-        val, wall = cpu_reference(args.workload, steps, 0, procs, args.advection)
         cfg = _workload_cfg(args.workload, advection=args.advection)
+        nmem = (args.members or ENSEMBLE[args.workload]) if args.workload in ENSEMBLE else 1
+        # the ensemble: the GPU arm's members (seeds, k_f factors) over every host core; a single
+        # grid: one replica per host core (the reference is single-threaded)
+        grids = nmem if nmem > 1 else procs
+        val, wall = cpu_reference(args.workload, args.steps, args.warmup, procs, args.advection, grids=grids,
+                                  scales=kf_scales(nmem) if nmem > 1 else None)
         line = {"impl": "reference", "metric": METRIC, "value": val, "unit": "cell-steps/s", "n_gpus": args.gpus,
-                "steps": steps, "warmup": args.warmup, "ms_per_step": wall / steps * 1e3, "higher_is_better": True,
+                "steps": args.steps, "warmup": args.warmup, "ms_per_step": wall / args.steps * 1e3, "higher_is_better": True,
                 "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
-                "config": {"workload": (f"ensemble of {ENSEMBLE[args.workload]} Held-Suarez members " if args.workload in ENSEMBLE
-                                        else "Zonal jets on the Held-Suarez planet " if cfg.state == "jet" else "Held-Suarez ")
-                                       + f"{cfg.ni}x{cfg.nj}x{cfg.nk}, dt={cfg.dt}s, AB3, "
-                                        f"{ADVECTION_NAME[args.advection]}, nu4=0.5 max; "
-                                        f"reference CPU step (FP64) as {procs} concurrent single-threaded grids",
-                           "ni": cfg.ni, "nj": cfg.nj, "nk": cfg.nk, "dt": cfg.dt, "precision": "fp64",
-                           "advection": args.advection},
-                "cpu_baseline": {"value": val, "unit": "cell-steps/s", "cores": procs, "kind": "port",
-                                 "sample": f"{procs} independent single-threaded replicas x {steps} steps of the "
-                                           f"oracle's restatement (bit-identical to the reference build)"},
+                "config": workload_config(args, cfg, nmem, args.gpus),
+                "form": "reference CPU step (FP64, single-threaded) on the host cores",
+                "cpu_baseline": {"value": val, "unit": "cell-steps/s", "cores": min(procs, grids), "kind": "port",
+                                 "sample": f"{grids} grids of the workload round-robin over {min(procs, grids)} worker "
+                                           f"processes (one per host core), {args.warmup} untimed + {args.steps} timed steps "
+                                           f"each, with the oracle's restatement of the step (bit-identical to the "
+                                           f"reference build, which needs the reference tree to compile); rate = cells of "
+                                           f"every grid x steps / slowest worker's timed seconds"},
                 "e2e": {"value": val, "unit": "cell-steps/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
         print(json.dumps(line))
         return
@@ -700,7 +750,7 @@ def main():
     out = run_gpu_ensemble(args) if args.workload in ENSEMBLE else run_gpu(args)
     if rank == 0 and out is not None:
         if ws == 1 and not args.no_cpu_baseline:
-            val, wall = cpu_reference(args.workload, args.cpu_steps, 0, 1, args.advection)
+            val, wall = cpu_reference(args.workload, args.cpu_steps, 0, 1, args.advection, grids=1)
             out["cpu_baseline"] = {"value": val, "unit": "cell-steps/s", "cores": 1, "kind": "port",
                                    "sample": f"{args.cpu_steps} steps of {WORKLOADS[args.workload][:3]} on one core "
                                              f"({wall:.1f} s) with the oracle's restatement of the reference step"}

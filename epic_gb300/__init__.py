@@ -21,7 +21,8 @@ from .abi import (EPIC_ADV_AKIMA, EPIC_ADV_HSU, EPIC_PREC_FP64, EPIC_PREC_MIXED,
                   EPIC_PROFILE_N2, EPIC_STEP_PROGS_AND_SYNC_DIAGS, EPIC_SYNC_DIAGS_ONLY, EPIC_UV_AB3, EPIC_UV_LEAPFROG,
                   EpicFields, EpicGrid, EpicHsParams, EpicJetParams, Fields, GridArrays, HSConfig, JetConfig, Layout)
 
-TUNE_GROUPS = 9   # EPIC_TUNE_GROUPS
+TUNE_GROUPS = 10   # EPIC_TUNE_GROUPS
+TUNE_HSU_MERID_VARIANT = 9   # table entry: 0 automatic, 1 fused march, 2 four passes
 _HERE = os.path.dirname(os.path.abspath(__file__))
 LIB_PATH = os.path.join(_HERE, "_lib", "libepic_gb300.so")
 _lib = None
@@ -57,6 +58,8 @@ def load_library(path: str | None = None) -> C.CDLL:
     lib.epic_model_kernels_per_step.restype = C.c_int32
     lib.epic_model_device_bytes.argtypes = [C.c_void_p]
     lib.epic_model_device_bytes.restype = C.c_int64
+    lib.epic_model_device.argtypes = [C.c_void_p]
+    lib.epic_model_device.restype = C.c_int32
     lib.epic_model_bytes.argtypes = [C.POINTER(EpicGrid), C.c_int32]
     lib.epic_model_bytes.restype = C.c_int64
     lib.epic_model_filter_mass_noalloc.argtypes = [C.c_void_p]
@@ -87,6 +90,13 @@ def load_library(path: str | None = None) -> C.CDLL:
                                            C.c_uint64, C.POINTER(EpicFields)]
     _lib = lib
     return lib
+
+
+def _tuning_table(table: list[int]) -> list[int]:
+    table = [int(t) for t in table]
+    if len(table) > TUNE_GROUPS:
+        raise ValueError(f"a tuning table has at most {TUNE_GROUPS} entries")
+    return table + [0] * (TUNE_GROUPS - len(table))
 
 
 def _check(rc: int, what: str) -> None:
@@ -180,8 +190,9 @@ class Model:
         return f
 
     def set_tuning(self, table: list[int]) -> None:
-        """Launch shapes from Batch.autotune (block size per kernel group; 0 = built-in)."""
-        arr = (C.c_int32 * TUNE_GROUPS)(*table)
+        """Launch shapes from Batch.autotune (one entry per kernel group, 0 = built-in; missing
+        trailing entries are 0)."""
+        arr = (C.c_int32 * TUNE_GROUPS)(*_tuning_table(table))
         _check(self.lib.epic_model_set_tuning(self._h, arr), "epic_model_set_tuning")
 
     def step_host(self, f: Fields, nsteps: int, prime: bool = False) -> None:
@@ -198,6 +209,11 @@ class Model:
     @property
     def device_bytes(self) -> int:
         return int(self.lib.epic_model_device_bytes(self._h))
+
+    @property
+    def device(self) -> int:
+        """The CUDA device the model was created on."""
+        return int(self.lib.epic_model_device(self._h))
 
 
 class Batch:
@@ -257,7 +273,7 @@ class Batch:
         return list(arr)
 
     def set_tuning(self, table: list[int]) -> None:
-        arr = (C.c_int32 * TUNE_GROUPS)(*table)
+        arr = (C.c_int32 * TUNE_GROUPS)(*_tuning_table(table))
         _check(self.lib.epic_batch_set_tuning(self._h, arr), "epic_batch_set_tuning")
 
     def sync(self) -> None:
@@ -282,4 +298,4 @@ class Batch:
 
 __all__ = ["Model", "Batch", "model_bytes", "hs_setup", "load_library", "EpicError", "HSConfig", "Fields", "GridArrays", "Layout",
            "EPIC_ADV_AKIMA", "EPIC_ADV_HSU", "EPIC_PREC_FP64", "EPIC_PREC_MIXED", "EPIC_PREC_MIXED_FAST", "EPIC_STEP_PROGS_AND_SYNC_DIAGS", "EPIC_SYNC_DIAGS_ONLY",
-           "EPIC_UV_AB3", "EPIC_UV_LEAPFROG", "LIB_PATH", "np"]
+           "EPIC_UV_AB3", "EPIC_UV_LEAPFROG", "LIB_PATH", "TUNE_GROUPS", "TUNE_HSU_MERID_VARIANT", "np"]

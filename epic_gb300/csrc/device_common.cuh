@@ -11,7 +11,9 @@
 #include "df.cuh"
 
 // kernel groups whose block size the autotuner picks (DevModel::tb)
-enum TuneGroup { TB_UV_CORE = 0, TB_PGRAD, TB_HSU, TB_VISC, TB_DIAG, TB_UPDATE, TB_COLUMN, TB_POINT, TB_ROW, TB_COUNT };
+enum TuneGroup { TB_UV_CORE = 0, TB_PGRAD, TB_HSU, TB_VISC, TB_DIAG, TB_UPDATE, TB_COLUMN, TB_POINT, TB_ROW,
+                 TB_HSU_MERID_VARIANT,   // not a block size: 0 automatic, 1 fused march, 2 four passes
+                 TB_COUNT };
 #define TB(M, g) ((M).tb[g] > 0 ? (M).tb[g] : 128)
 
 #define EPIC_MAX_NK 126      // column kernels keep per-column arrays of nk+2 entries
@@ -30,6 +32,9 @@ struct Ctl {
   double err_val;
   double ab[2][3];                     // Adams-Bashforth coefficients chosen for u, v this step
   int lf_first[2];                     // leapfrog: forward (Euler) first step for u, v
+  int halted;                          // set between steps once err_code is set: every kernel of the
+                                       // model then returns at entry (the reference stops the run at
+                                       // its first epic_error); cleared by an upload
 };
 
 enum ErrCode { ERR_NONE = 0, ERR_GZ_MONOTONE = 1, ERR_CALC_W_P = 2, ERR_PCHIP_X = 3, ERR_NONFINITE = 4, ERR_TIMEOUT = 5 };
@@ -85,7 +90,7 @@ struct DevModel {
   char *pool_base;   // start of the model's device pool (state, scratch and tables)
   // launch shapes (host side only): threads per block of each kernel group, set by the
   // autotuner; they change no result (every tuned kernel is pointwise or per row)
-  int tb[9];
+  int tb[TB_COUNT];
 
   // Offsets within one 3-D field of one model: 32-bit arithmetic (epic_model_create rejects
   // grids whose wind arrays, up to three time planes, reach 2^31 elements).
@@ -95,14 +100,18 @@ struct DevModel {
 
 // Entry of every kernel: in a batch launch, take member blockIdx.z's description and move the
 // state pointers passed as arguments (addresses in the launch description's pool) to the same
-// offsets in the member's pool (members of a batch share the pool layout).
+// offsets in the member's pool (members of a batch share the pool layout).  Returns true when
+// the model is halted (a step found a fatal error): the kernel then returns at once.  Ctl::halted
+// changes only in k_itime_advance, between steps, so every thread of a launch reads the same value.
 template <class... P>
-__device__ __forceinline__ void epic_member(DevModel &M, P *&...ptrs) {
-  if (!M.batch) return;
-  const char *from = M.pool_base;
-  M = M.batch[blockIdx.z];
-  const char *to = M.pool_base;
-  ((ptrs = ptrs ? (P *)(to + ((const char *)ptrs - from)) : ptrs), ...);
+__device__ __forceinline__ bool epic_member(DevModel &M, P *&...ptrs) {
+  if (M.batch) {
+    const char *from = M.pool_base;
+    M = M.batch[blockIdx.z];
+    const char *to = M.pool_base;
+    ((ptrs = ptrs ? (P *)(to + ((const char *)ptrs - from)) : ptrs), ...);
+  }
+  return M.ctl->halted != 0;
 }
 
 // ---- pointwise helpers: restatements of the reference routines named beside each ----

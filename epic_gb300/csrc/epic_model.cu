@@ -20,6 +20,7 @@ struct epic_model {
   epic_grid g;
   DevModel d;
   int precision;
+  int device = -1;                   // the CUDA device that holds the pool and runs the stream
   cudaStream_t stream = nullptr;
   char *pool = nullptr;
   size_t pool_bytes = 0;
@@ -336,9 +337,12 @@ extern "C" int epic_model_create(const epic_grid *g, int32_t precision, epic_mod
   for (const char *p : ptrs)
     if (!p) return set_error(EPIC_ERR_ARG, "epic_model_create: grid array pointer is NULL");
 
+  int device = -1;
+  if (cudaGetDevice(&device) != cudaSuccess) return set_error(EPIC_ERR_CUDA, "epic_model_create: no CUDA device");
   epic_model *m = new epic_model();
   m->g = *g;
   m->precision = precision;
+  m->device = device;
   const epic::Layout L(g->ni, g->nj, g->nk);
   DevModel &d = m->d;
   d.ni = g->ni; d.nj = g->nj; d.nk = g->nk;
@@ -667,6 +671,8 @@ extern "C" int32_t epic_model_kernels_per_step(const epic_model *m) { return m ?
 
 extern "C" int64_t epic_model_device_bytes(const epic_model *m) { return m ? (int64_t)m->pool_bytes : 0; }
 
+extern "C" int32_t epic_model_device(const epic_model *m) { return m ? m->device : -1; }
+
 // ---- the 3-D mass filter with a fixed scratch table (epic_model_filter_mass_noalloc) ----
 //
 // Some callers cannot allocate device memory at the point where they want the filter: a
@@ -773,18 +779,27 @@ extern "C" int epic_batch_create(epic_model *const *members, int32_t n, epic_bat
       return set_error(EPIC_ERR_ARG, "epic_batch_create: member %d differs from member 0 in size, scheme, precision or viscosity", i);
     for (int q = 0; q < i; q++)
       if (members[q] == members[i]) return set_error(EPIC_ERR_ARG, "epic_batch_create: member %d repeats member %d", i, q);
+    // every kernel of the batch reads and writes each member's pool: all on one device
+    if (members[i]->device != members[0]->device)
+      return set_error(EPIC_ERR_ARG, "epic_batch_create: member %d lives on device %d, member 0 on device %d", i,
+                       members[i]->device, members[0]->device);
   }
+  int cur = -1;
+  EPIC_CUDA_CHECK(cudaGetDevice(&cur));
+  if (cur != members[0]->device) EPIC_CUDA_CHECK(cudaSetDevice(members[0]->device));
   epic_batch *b = new epic_batch();
   b->members.assign(members, members + n);
   cudaError_t e = cudaStreamCreateWithFlags(&b->stream, cudaStreamNonBlocking);
   if (e == cudaSuccess) e = cudaMalloc(&b->dev_members, sizeof(DevModel) * (size_t)n);
   if (e != cudaSuccess) {
     epic_batch_destroy(b);
+    if (cur != members[0]->device) cudaSetDevice(cur);
     return set_error(EPIC_ERR_NOMEM, "epic_batch_create: %s", cudaGetErrorString(e));
   }
   std::vector<DevModel> host(n);
   for (int i = 0; i < n; i++) host[i] = members[i]->d;
   e = cudaMemcpy(b->dev_members, host.data(), sizeof(DevModel) * (size_t)n, cudaMemcpyHostToDevice);
+  if (cur != members[0]->device) cudaSetDevice(cur);
   if (e != cudaSuccess) {
     epic_batch_destroy(b);
     return set_error(EPIC_ERR_CUDA, "epic_batch_create: %s", cudaGetErrorString(e));
@@ -946,11 +961,13 @@ extern "C" int epic_batch_autotune(epic_batch *b, int32_t trial_steps, int32_t *
   };
   static const int cell_cand[] = {64, 128, 256, 512};
   static const int row_cand[] = {32, 64, 128, 256};
+  static const int variant_cand[] = {1, 2};   // meridional Hsu pass: fused march, four passes
   for (int g = 0; g < TB_COUNT && rc == EPIC_OK; g++) {
-    const int *cand = g == TB_ROW ? row_cand : cell_cand;
+    const int *cand = g == TB_ROW ? row_cand : (g == TB_HSU_MERID_VARIANT ? variant_cand : cell_cand);
+    const int ncand = g == TB_HSU_MERID_VARIANT ? 2 : 4;
     int best = b->d.tb[g];
     float best_ms = 3.4e38f;
-    for (int c = 0; c < 4 && rc == EPIC_OK; c++) {
+    for (int c = 0; c < ncand && rc == EPIC_OK; c++) {
       if (g == TB_ROW && c > 0 && cand[c] > b->d.ni / 2) continue;   // more threads than butterflies
       b->d.tb[g] = cand[c];
       float ms = 0.f;

@@ -20,7 +20,7 @@ __device__ __forceinline__ bool col_index(const DevModel &M, int &j, int &i) {
 
 // source_sink: THETA += dt*HEAT3/EXNER3 for k >= k_sigma-1, epic_funcs_diag.c:4768-4778
 __global__ void k_source_sink(DevModel M) {
-  epic_member(M);
+  if (epic_member(M)) return;
   int j, i;
   if (!col_index(M, j, i)) return;
   for (int k = M.k_sigma - 1; k <= M.nk; k++) {
@@ -38,7 +38,7 @@ __global__ void k_source_sink(DevModel M) {
 // the dF/dp difference step is cbrt(FLT_EPSILON) relative instead of cbrt(DBL_EPSILON).
 template <class R>
 __global__ void __launch_bounds__(CT_THREADS, 3) k_calc_w(DevModel M) {
-  epic_member(M);
+  if (epic_member(M)) return;
   extern __shared__ __align__(16) unsigned char smraw[];
   R *sm = reinterpret_cast<R *>(smraw);
   __shared__ R s_lp[32];
@@ -137,7 +137,7 @@ __global__ void __launch_bounds__(CT_THREADS, 3) k_calc_w(DevModel M) {
 // Columns on the u grid (j = 0..nj) and v grid (j = 1..nj), i = 1..ni.
 template <class R>
 __global__ void k_uv_drag(DevModel M) {
-  epic_member(M);
+  if (epic_member(M)) return;
   const int t = (int)(blockIdx.x * blockDim.x + threadIdx.x);
   const int ni = M.ni, nk = M.nk;
   const int nu = (M.nj + 1) * ni;
@@ -177,7 +177,7 @@ __global__ void k_uv_drag(DevModel M) {
 // WA (the field), WM, WP (the split vertical velocity), PR (the predictor), FF (the fluxes).
 template <class R>
 __global__ void __launch_bounds__(CT_THREADS) k_hsu_vertical(DevModel M, double *buff, int kind) {
-  epic_member(M, buff);
+  if (epic_member(M, buff)) return;
   extern __shared__ __align__(16) unsigned char smraw[];
   R *sm = reinterpret_cast<R *>(smraw);
   const ColTile c = col_tile(M);
@@ -312,7 +312,7 @@ __device__ __forceinline__ R akima_dela(R d0, R d1) {
 // points), DL (dela), FF (the fluxes).
 template <class R>
 __global__ void __launch_bounds__(CT_THREADS) k_akima_vertical(DevModel M, double *buff, int kind) {
-  epic_member(M, buff);
+  if (epic_member(M, buff)) return;
   extern __shared__ __align__(16) unsigned char smraw[];
   R *sm = reinterpret_cast<R *>(smraw);
   const ColTile c = col_tile(M);
@@ -375,7 +375,7 @@ __global__ void __launch_bounds__(CT_THREADS) k_akima_vertical(DevModel M, doubl
 // restore_mass(HDRY_INDEX), epic_adjust.c:45-96
 // Pointwise: one thread per cell of layers 1..nk, rows 0..nj, all columns.
 __global__ void k_restore_mass(DevModel M) {
-  epic_member(M);
+  if (epic_member(M)) return;
   const int t = (int)(blockIdx.x * blockDim.x + threadIdx.x);
   const int per_k = (M.nj + 1) * (M.ni + 2);
   if (t >= M.nk * per_k) return;
@@ -388,7 +388,7 @@ __global__ void k_restore_mass(DevModel M) {
 // Shared arrays: P (interface pressure), HL (get_h at the layers), TH (THETA), PP (P^(kappa+1),
 // each interface's power computed once for the two layers that share it).
 __global__ void __launch_bounds__(CT_THREADS) k_set_p2etc(DevModel M, int update_theta) {
-  epic_member(M);
+  if (epic_member(M)) return;
   extern __shared__ double sm[];
   __shared__ double s_lp[32];
   const ColTile c = col_tile(M);
@@ -497,7 +497,7 @@ __global__ void __launch_bounds__(CT_THREADS) k_set_p2etc(DevModel M, int update
 // the first DZDT3 terms.  Shared arrays: P, R (RHO3), T3, LG (log of successive pressure
 // ratios), GZ (the Leslie-Purser increments, then the running sum in place).
 __global__ void __launch_bounds__(CT_THREADS) k_pgrad_vars_column(DevModel M) {
-  epic_member(M);
+  if (epic_member(M)) return;
   extern __shared__ double sm[];
   __shared__ double s_rho2_1[32];
   const ColTile c = col_tile(M);
@@ -610,7 +610,7 @@ __device__ __forceinline__ double layer_p_mixed(const DevModel &M, double top, d
 // layers = 0: P3 and HDRY only (the call inside advection, whose P2 and H3 stage 11 rewrites
 // before anything reads them)
 __global__ void __launch_bounds__(CT_THREADS, 3) k_set_p2etc_mixed(DevModel M, int update_theta, int layers) {
-  epic_member(M);
+  if (epic_member(M)) return;
   extern __shared__ double sm[];
   const ColTile c = col_tile(M);
   const int nk = M.nk, ks = M.k_sigma, L = nk + 1;
@@ -734,7 +734,7 @@ __global__ void __launch_bounds__(CT_THREADS, 3) k_set_p2etc_mixed(DevModel M, i
 // set_p2etc (stage 19) before anything reads them, and that call reads this GZ3 as the old one.
 template <bool FULL>
 __global__ void __launch_bounds__(CT_THREADS, 3) k_pgrad_vars_column_mixed(DevModel M) {
-  epic_member(M);
+  if (epic_member(M)) return;
   extern __shared__ double sm[];
   __shared__ double s_rho2_1[32];
   const ColTile c = col_tile(M);
@@ -869,7 +869,7 @@ __global__ void __launch_bounds__(CT_THREADS, 3) k_pgrad_vars_column_mixed(DevMo
 // store_pgrad_vars, horizontal part of DZDT3 (epic_funcs_diag.c:3924-3945) plus bc_lateral.
 template <class R>
 __global__ void k_pgrad_dzdt(DevModel M) {
-  epic_member(M);
+  if (epic_member(M)) return;
   const int t = (int)(blockIdx.x * blockDim.x + threadIdx.x);
   const int ni = M.ni, nk = M.nk;
   if (t >= nk * (M.nj + 1) * ni) return;
@@ -893,7 +893,7 @@ __global__ void k_pgrad_dzdt(DevModel M) {
 // Monotone fix of the filtered GZ copy, epic_timestep.c:182-195 (the zonal filter of planes
 // 0..nk-1 has already run; each plane's fix only needs the finished plane below it).
 __global__ void k_gz_monotone(DevModel M) {
-  epic_member(M);
+  if (epic_member(M)) return;
   int j, i;
   if (!col_index(M, j, i)) return;
   double below = M.gz[M.at(M.nk, j, i)];
@@ -915,7 +915,7 @@ __global__ void k_gz_monotone(DevModel M) {
 // 0 outside k = 1..nk, j = 0..nj, i = 1..ni, with periodic pads.
 template <class R>
 __global__ void k_calc_heating(DevModel M) {
-  epic_member(M);
+  if (epic_member(M)) return;
   const unsigned t = blockIdx.x * blockDim.x + threadIdx.x;   // n3 < 2^31
   if (t >= (unsigned)M.n3) return;
   const unsigned r = t / (unsigned)M.iadim, q = r / (unsigned)M.jadim;
@@ -950,7 +950,7 @@ __global__ void k_calc_heating(DevModel M) {
 // phase 0: UNITY = 1 over k = 0..nk+1, j = 0..nj, all i;  phase 1: OLD = THETA for k >= k_sigma-1;
 // phase 2: THETA -= OLD*(UNITY-1) for k >= k_sigma-1.
 __global__ void k_advection_prep(DevModel M, int phase) {
-  epic_member(M);
+  if (epic_member(M)) return;
   const unsigned t = blockIdx.x * blockDim.x + threadIdx.x;   // fewer than n3 < 2^31 cells
   const unsigned w = (unsigned)(M.nj + 1) * (unsigned)M.iadim;
   if (t >= w * (unsigned)(M.nk + 2)) return;

@@ -48,7 +48,7 @@ __device__ __forceinline__ double theta_acc(const DevModel &M, double sg, dfl si
 }  // namespace
 
 __global__ void __launch_bounds__(CT_THREADS, 3) k_set_p2etc_acc(DevModel M, int update_theta) {
-  epic_member(M);
+  if (epic_member(M)) return;
   extern __shared__ double sm[];
   const ColTile c = col_tile(M);
   const int nk = M.nk, ks = M.k_sigma, L = nk + 1;
@@ -168,7 +168,7 @@ __global__ void __launch_bounds__(CT_THREADS, 3) k_set_p2etc_acc(DevModel M, int
 }
 
 __global__ void __launch_bounds__(CT_THREADS, 3) k_pgrad_vars_column_acc(DevModel M) {
-  epic_member(M);
+  if (epic_member(M)) return;
   extern __shared__ double sm[];
   __shared__ double s_rho2_1[32];
   const ColTile c = col_tile(M);

@@ -173,7 +173,7 @@ __device__ __forceinline__ bool row_is_filtered(const DevModel &M, int j, int vg
 // copied; rows 0..nj+1 get periodic pads (bc_lateral).
 template <class R>
 __global__ void k_filter_planes(DevModel M, const double *src, int src_sel, double *dst, int k0, int vgrid) {
-  epic_member(M, src, dst);
+  if (epic_member(M, src, dst)) return;
   extern __shared__ __align__(16) unsigned char smraw[];
   R *sm = reinterpret_cast<R *>(smraw);
   src += plane_offset(M, src_sel);
@@ -204,7 +204,7 @@ __global__ void k_filter_planes(DevModel M, const double *src, int src_sel, doub
 // The rows the tensor-core filter leaves alone (k_filter_planes_gemm filters the others): copied
 // when dst is not src, periodic pads on rows 0..nj+1.  One warp per (row, plane).
 __global__ void k_filter_rows_unfiltered(DevModel M, const double *src, int src_sel, double *dst, int k0, int nplanes, int vgrid) {
-  epic_member(M, src, dst);
+  if (epic_member(M, src, dst)) return;
   src += plane_offset(M, src_sel);
   const int lane = (int)(threadIdx.x & 31);
   const int w = (int)((blockIdx.x * blockDim.x + threadIdx.x) >> 5);
@@ -228,7 +228,7 @@ __global__ void k_filter_rows_unfiltered(DevModel M, const double *src, int src_
 // the first column of minimum bottom GZ (the reference's strict-less scan) and fill the table;
 // lane 0 fits the spline.  index: 0 = U, 1 = V, 2 = HDRY (log), 3 = THETA.
 __global__ void k_varz_tables(DevModel M, const double *buff, int sel, int index, int kstart, int kend) {
-  epic_member(M, buff);
+  if (epic_member(M, buff)) return;
   buff += plane_offset(M, sel);
   const int jstart = index == 1 ? 1 : 0;
   const int lane = (int)(threadIdx.x & 31);
@@ -357,6 +357,8 @@ __device__ __forceinline__ double varz_profile_mixed(const Trip *t, const double
     }
     kay = il;
   }
+  // a NaN argument fails every comparison: keep the interval index inside the table
+  kay = kay < 0 ? 0 : (kay > n - 2 ? n - 2 : kay);
   const VarzInterval v = iv[kay];
   const float xx = d2f(gzd - t[kay].x);
   const float inc = xx * (v.z0 + xx * (v.c2 + xx * v.c3));
@@ -367,7 +369,7 @@ __device__ __forceinline__ double varz_profile_mixed(const Trip *t, const double
 // Block = one row (k = kstart + blockIdx.y, j = jstart + blockIdx.x).
 template <class R>
 __global__ void k_varz_filter_rows(DevModel M, double *buff, int sel, int index, int kstart, int kend) {
-  epic_member(M, buff);
+  if (epic_member(M, buff)) return;
   extern __shared__ __align__(16) unsigned char smraw[];
   buff += plane_offset(M, sel);
   const int jstart = index == 1 ? 1 : 0;
@@ -429,7 +431,7 @@ __global__ void k_varz_filter_rows(DevModel M, double *buff, int sel, int index,
         const int im = (iu + il) >> 1;
         if (RMath<R>::cmp(gzz, cv<R>(t[im].x)) >= 0) il = im; else iu = im;
       }
-      kay = il;
+      kay = il < 0 ? 0 : il;
     }
     const Trip *tk = t + kay;
     const R h = cv<R>(tk[1].x) - cv<R>(tk[0].x);
@@ -454,7 +456,7 @@ __global__ void k_varz_filter_rows(DevModel M, double *buff, int sel, int index,
 // kind: 0 = interface variable (unity, THETA), 1 = HDRY (layer; u averaged to the layer).
 template <class R>
 __global__ void k_hsu_zonal(DevModel M, double *buff, int kind, int kstart) {
-  epic_member(M, buff);
+  if (epic_member(M, buff)) return;
   extern __shared__ __align__(16) unsigned char smraw[];
   R *sm = reinterpret_cast<R *>(smraw);
   const int ni = M.ni, W = ni + 2;
@@ -534,7 +536,7 @@ __global__ void k_hsu_zonal(DevModel M, double *buff, int kind, int kstart) {
 // kind: 0 = interface variable (unity, THETA), 1 = HDRY (layer; u averaged to the layer).
 template <class R>
 __global__ void k_akima_zonal(DevModel M, double *buff, int kind, int kstart) {
-  epic_member(M, buff);
+  if (epic_member(M, buff)) return;
   extern __shared__ __align__(16) unsigned char smraw[];
   R *sm = reinterpret_cast<R *>(smraw);
   const int ni = M.ni, W = ni + 2;

@@ -101,7 +101,7 @@ __device__ __forceinline__ bool mbar_wait(unsigned mbar, unsigned phase) {
 // complete in issue order).
 __global__ void __launch_bounds__(FG_THREADS) k_filter_planes_gemm(DevModel M, const double *src, int src_sel, double *dst, int k0,
                                                                      int nplanes, int vgrid, int shift) {
-  epic_member(M, src, dst);
+  if (epic_member(M, src, dst)) return;
   extern __shared__ __align__(16) unsigned char fg_raw[];
   __shared__ __align__(8) uint64_t mbar[2];
   __shared__ uint32_t tmem_base;

@@ -37,14 +37,14 @@ __device__ __forceinline__ int wrap_i(const DevModel &M, int i) { return i == 0 
 
 // The copy of GZ3 that the filtered geopotential starts from, epic_timestep.c:176-181.
 __global__ void k_copy_gz(DevModel M) {
-  epic_member(M);
+  if (epic_member(M)) return;
   const long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
   if (t < M.n3) M.gz[t] = M.gz3[t];
 }
 
 // memset of DUDT, DVDT(it_uv_tend), epic_timestep.c:107-108
 __global__ void k_zero_tend(DevModel M) {
-  epic_member(M);
+  if (epic_member(M)) return;
   const long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
   if (t >= M.n3) return;
   const long long off = plane_offset(M, PL_UV_TEND);
@@ -91,7 +91,7 @@ __device__ __forceinline__ R vh_at(const DevModel &M, const double *Vk, const do
 // Kinetic energy per mass on the h grid, planes k = 1..nk-1, into work0 (with pads).
 template <class R>
 __global__ void k_uv_kin(DevModel M) {
-  epic_member(M);
+  if (epic_member(M)) return;
   Cell c;
   if (!cell3(M, 1, M.nk - 1, 0, M.nj + 1, c)) return;
   const long long off = plane_offset(M, PL_UV);
@@ -102,7 +102,7 @@ __global__ void k_uv_kin(DevModel M) {
 // DVDT += (PV*UH terms + KIN(j-1)-KIN(j))*n, then the vertical advection of V.
 template <class R>
 __global__ void k_uv_core_v(DevModel M) {
-  epic_member(M);
+  if (epic_member(M)) return;
   Cell c;
   if (!cell3(M, 1, M.nk - 1, 1, M.nj, c)) return;
   const int k = c.k, j = c.j, i = c.i;
@@ -130,7 +130,7 @@ __global__ void k_uv_core_v(DevModel M) {
 // DUDT += (PV*VH terms + KIN(i-1)-KIN(i))*m with the filtered KIN, then the vertical advection of U.
 template <class R>
 __global__ void k_uv_core_u(DevModel M) {
-  epic_member(M);
+  if (epic_member(M)) return;
   Cell c;
   if (!cell3(M, 1, M.nk - 1, 0, M.nj + 1, c)) return;
   const int k = c.k, j = c.j, i = c.i;
@@ -162,7 +162,7 @@ __global__ void k_uv_core_u(DevModel M) {
 // Pole boundary rows of GZ3 (zonal means of the adjacent row), epic_timestep.c:930-998.
 // One block per k; thread 0 sums in the reference order.
 __global__ void k_gz_pole_rows(DevModel M) {
-  epic_member(M);
+  if (epic_member(M)) return;
   const int k = blockIdx.x;
   __shared__ double avg[2];
   if (threadIdx.x < 2) {
@@ -186,7 +186,7 @@ __global__ void k_gz_pole_rows(DevModel M) {
 // (hi_x - hi_ref) + (lo_x - lo_ref): within a rounding or two of the FP64 difference, with no
 // FP64 operation per stencil point.  The FP64 form uses the values as they are.
 __global__ void k_pgrad_split(DevModel M) {
-  epic_member(M);
+  if (epic_member(M)) return;
   const long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
   if (t >= M.n3) return;
   const double z = M.gz3[t], p = M.p2[t];
@@ -281,7 +281,7 @@ __device__ __forceinline__ LonFace<R> lon_face(const DevModel &M, const R (&z)[3
 
 template <class R>
 __global__ void k_pgrad_lon(DevModel M) {
-  epic_member(M);
+  if (epic_member(M)) return;
   Cell c;
   if (!cell3(M, 1, M.nk - 1, 0, M.nj + 1, c)) return;
   const int k = c.k, j = c.j, i = c.i;
@@ -351,7 +351,7 @@ __device__ __forceinline__ LatFace<R> lat_face(const DevModel &M, const R (&z)[3
 
 template <class R>
 __global__ void k_pgrad_lat(DevModel M) {
-  epic_member(M);
+  if (epic_member(M)) return;
   Cell c;
   if (!cell3(M, 1, M.nk - 1, 1, M.nj, c)) return;
   const int k = c.k, j = c.j, i = c.i;
@@ -461,7 +461,7 @@ __device__ __forceinline__ void vmp(const DevModel &M, const double *V, int kind
 
 template <class R>
 __global__ void k_hsu_merid_pred(DevModel M, const double *A, int kind, int k0) {
-  epic_member(M, A);
+  if (epic_member(M, A)) return;
   Cell c;
   if (!cell3(M, k0, M.nk - k0 + 1, 0, M.nj + 2, c)) return;   // rows 0..nj+1
   const double *V = M.v + plane_offset(M, PL_UV);
@@ -476,7 +476,7 @@ __global__ void k_hsu_merid_pred(DevModel M, const double *A, int kind, int k0) 
 
 template <class R>
 __global__ void k_hsu_merid_apred(DevModel M, const double *A, int k0) {
-  epic_member(M, A);
+  if (epic_member(M, A)) return;
   Cell c;
   if (!cell3(M, k0, M.nk - k0 + 1, 0, M.nj + 1, c)) return;
   const double *FF = M.work1;
@@ -487,7 +487,7 @@ __global__ void k_hsu_merid_apred(DevModel M, const double *A, int k0) {
 
 template <class R>
 __global__ void k_hsu_merid_corr(DevModel M, const double *A, int kind, int k0) {
-  epic_member(M, A);
+  if (epic_member(M, A)) return;
   Cell c;
   if (!cell3(M, k0, M.nk - k0 + 1, 0, M.nj + 2, c)) return;
   const int k = c.k, j = c.j, i = c.i, nj = M.nj;
@@ -530,7 +530,7 @@ __global__ void k_hsu_merid_corr(DevModel M, const double *A, int kind, int k0) 
 
 template <class R>
 __global__ void k_hsu_merid_update(DevModel M, double *A, int k0) {
-  epic_member(M, A);
+  if (epic_member(M, A)) return;
   Cell c;
   if (!cell3(M, k0, M.nk - k0 + 1, 0, M.nj + 1, c)) return;
   const double *FF = M.work3;
@@ -548,7 +548,7 @@ __global__ void k_hsu_merid_update(DevModel M, double *A, int k0) {
 // at the top of iteration j, ahead of the arithmetic that does not need them.
 template <class R>
 __global__ void k_hsu_meridional(DevModel M, double *A, int kind, int k0) {
-  epic_member(M, A);
+  if (epic_member(M, A)) return;
   const int i = 1 + (int)(blockIdx.x * blockDim.x + threadIdx.x);
   const int k = k0 + (int)blockIdx.y;
   if (i > M.ni) return;
@@ -648,7 +648,7 @@ __device__ __forceinline__ R akima_mean(R d0, R d1) {   // the dela of akima_adv
 
 template <class R>
 __global__ void k_akima_merid_flux(DevModel M, const double *A, int kind, int k0) {
-  epic_member(M, A);
+  if (epic_member(M, A)) return;
   Cell c;
   if (!cell3(M, k0, M.nk - k0 + 1, 1, M.nj, c)) return;   // v rows 1..nj
   const int k = c.k, j = c.j, i = c.i, nj = M.nj;
@@ -666,7 +666,7 @@ __global__ void k_akima_merid_flux(DevModel M, const double *A, int kind, int k0
 
 template <class R>
 __global__ void k_akima_merid_update(DevModel M, double *A, int k0) {
-  epic_member(M, A);
+  if (epic_member(M, A)) return;
   Cell c;
   if (!cell3(M, k0, M.nk - k0 + 1, 0, M.nj + 1, c)) return;   // rows 0..nj
   const int k = c.k, j = c.j, nj = M.nj;
@@ -685,7 +685,7 @@ __global__ void k_akima_merid_update(DevModel M, double *A, int k0) {
 template <class R>
 __global__ void k_d2dy2(DevModel M, const double *src, int src_sel, double *dst, int vgrid, double diff_coef, int k0, int nkk,
                         int of_state) {
-  epic_member(M, src, dst);
+  if (epic_member(M, src, dst)) return;
   Cell c;
   const int nrows = vgrid ? M.nj + 2 : M.nj + 1;   // v: j = 0..nj+1, h: j = 0..nj
   if (!cell3(M, k0, nkk, 0, nrows, c)) return;
@@ -717,7 +717,7 @@ __global__ void k_d2dy2(DevModel M, const double *src, int src_sel, double *dst,
 // intermediate volume's write and read.
 __global__ void k_d2dy2_pair_mixed(DevModel M, const double *src, int src_sel, double *dst, int vgrid, double coef1, double coef2,
                                    int k0) {
-  epic_member(M, src, dst);
+  if (epic_member(M, src, dst)) return;
   extern __shared__ __align__(16) unsigned char smraw[];
   float *d1 = reinterpret_cast<float *>(smraw);   // [row][lane]
   src += plane_offset(M, src_sel);
@@ -752,7 +752,7 @@ __global__ void k_d2dy2_pair_mixed(DevModel M, const double *src, int src_sel, d
 // A += dt*sign*D over the rows the reference updates (v: 1..nj, h: 0..nj).
 template <class R>
 __global__ void k_visc_apply(DevModel M, double *A, int sel, const double *D, int vgrid, double sign, int k0, int nkk) {
-  epic_member(M, A, D);
+  if (epic_member(M, A, D)) return;
   Cell c;
   if (!cell3(M, k0, nkk, vgrid ? 1 : 0, vgrid ? M.nj : M.nj + 1, c)) return;
   A += plane_offset(M, sel);
@@ -765,7 +765,7 @@ __global__ void k_visc_apply(DevModel M, double *A, int sel, const double *D, in
 // the reference's order on lane 0; the mixed form sums it in FP64 with a warp reduction.
 template <class R>
 __global__ void k_zonal_visc(DevModel M, double *A, int sel, int jbot, int jhalf, int k0) {
-  epic_member(M, A);
+  if (epic_member(M, A)) return;
   extern __shared__ __align__(16) unsigned char smraw[];
   const int ni = M.ni, lane = (int)(threadIdx.x & 31), w = (int)(threadIdx.x >> 5), nw = (int)(blockDim.x >> 5);
   const int j = jbot + (int)blockIdx.x * nw + w;
@@ -858,7 +858,7 @@ __device__ __forceinline__ R div_at(const DevModel &M, const double *UU, const d
 
 template <class R>
 __global__ void k_divergence(DevModel M, const double *UU, const double *VV, int vsel, double *DI, int k0, int nkk) {
-  epic_member(M, UU, VV, DI);
+  if (epic_member(M, UU, VV, DI)) return;
   Cell c;
   if (!cell3(M, k0, nkk, 0, M.nj + 1, c)) return;
   VV += plane_offset(M, vsel);
@@ -868,7 +868,7 @@ __global__ void k_divergence(DevModel M, const double *UU, const double *VV, int
 // Interior potential vorticity, vorticity(ON_SIGMATHETA, POTENTIAL) :4168-4186, planes 0..nk.
 template <class R>
 __global__ void k_pv_interior(DevModel M, const double *VV) {
-  epic_member(M, VV);
+  if (epic_member(M, VV)) return;
   Cell c;
   if (!cell3(M, 0, M.nk + 1, 1, M.nj, c)) return;
   const int k = c.k, j = c.j, i = c.i;
@@ -890,7 +890,7 @@ __global__ void k_pv_interior(DevModel M, const double *VV) {
 // Polar potential vorticity from the circulation of the adjacent u row, :4279-4341.
 // One block per plane; thread 0 forms the sums in the reference order.
 __global__ void k_pv_poles(DevModel M) {
-  epic_member(M);
+  if (epic_member(M)) return;
   const int k = blockIdx.x;
   const double *UU = M.u + plane_offset(M, PL_UV);
   const double *HH = M.h3;
@@ -930,7 +930,7 @@ __global__ void k_pv_poles(DevModel M) {
 // dvdz2 keeps the reference's sign slip (:3127-3128); only dudz2 decides the 1e6 branch.
 template <class R>
 __global__ void k_ri2(DevModel M) {
-  epic_member(M);
+  if (epic_member(M)) return;
   Cell c;
   if (!cell3(M, 1, M.nk, 0, M.nj + 1, c)) return;
   const int k = c.k, j = c.j, i = c.i;
@@ -964,7 +964,7 @@ __global__ void k_ri2(DevModel M) {
 // divergence_damping apply step, epic_subgrid.c:1857-1881 (DIV from k_divergence in work2).
 template <class R>
 __global__ void k_divdamp_apply(DevModel M, double nudiv) {
-  epic_member(M);
+  if (epic_member(M)) return;
   const unsigned t = blockIdx.x * blockDim.x + threadIdx.x;
   const unsigned per = (unsigned)(M.nk - 1) * (unsigned)(M.nj + 1) * (unsigned)M.ni;
   if (t >= 2 * per) return;
@@ -990,7 +990,7 @@ __global__ void k_divdamp_apply(DevModel M, double nudiv) {
 // ---------------------------------------------------------------------------------------------
 
 __global__ void k_uv_decide(DevModel M) {
-  epic_member(M);
+  if (epic_member(M)) return;
   Ctl *c = M.ctl;
   for (int w = 0; w < 2; w++) {
     const double *val = w == 0 ? M.u : M.v, *ten = w == 0 ? M.dudt : M.dvdt;
@@ -1009,7 +1009,7 @@ __global__ void k_uv_decide(DevModel M) {
 }
 
 __global__ void k_uv_update(DevModel M) {
-  epic_member(M);
+  if (epic_member(M)) return;
   const unsigned t = blockIdx.x * blockDim.x + threadIdx.x;
   const unsigned per = (unsigned)(M.nk - 1) * (unsigned)(M.nj + 1) * (unsigned)M.ni;
   if (t >= 2 * per) return;
@@ -1043,7 +1043,7 @@ __global__ void k_uv_update(DevModel M) {
 }
 
 __global__ void k_uv_rotate(DevModel M) {
-  epic_member(M);
+  if (epic_member(M)) return;
   Ctl *c = M.ctl;
   if (M.uv_scheme == EPIC_UV_AB3) {
     const int itmp = c->it_minus2;
@@ -1064,8 +1064,13 @@ __global__ void k_uv_rotate(DevModel M) {
   c->model_time += (long long)M.dt;
 }
 
+// End of a step: grid.itime += 1 (the driver loop, epic_main.c:424); a step that recorded a fatal
+// error instead halts the model, as the reference's epic_error() ends the run in that step.
 __global__ void k_itime_advance(DevModel M) {
-  epic_member(M); M.ctl->itime += 1; }
+  if (epic_member(M)) return;
+  if (M.ctl->err_code != 0) M.ctl->halted = 1;
+  else M.ctl->itime += 1;
+}
 
 // ---- launchers ----
 
@@ -1110,7 +1115,8 @@ int launch_uv_pgrad(const DevModel &M, cudaStream_t s) {
 
 // The fused march (k_hsu_meridional) has one thread per (k, i, member) walking nj+1 rows; it
 // wins once those threads fill the GPU (large batches).  Smaller launches take the four passes,
-// whose threads cover every cell.  Both give the same bits.
+// whose threads cover every cell.  Both give the same bits.  The tuning table's
+// TB_HSU_MERID_VARIANT entry overrides the choice (1 fused, 2 four passes).
 constexpr long long HSU_FUSED_MIN_THREADS = 65536;
 
 int launch_akima_meridional(const DevModel &M, double *buff, int kind, cudaStream_t s) {
@@ -1126,7 +1132,10 @@ int launch_hsu_meridional(const DevModel &M, double *buff, int kind, cudaStream_
   const int k0 = kind == 1 ? M.k_sigma - 1 : 1;
   const int nkk = M.nk - k0 + 1;
   const int th = TB(M, TB_HSU);
-  if ((long long)M.ni * nkk * (M.nbatch > 1 ? M.nbatch : 1) >= HSU_FUSED_MIN_THREADS) {
+  const int variant = M.tb[TB_HSU_MERID_VARIANT];
+  const bool fused = variant == 1 ||
+                     (variant == 0 && (long long)M.ni * nkk * (M.nbatch > 1 ? M.nbatch : 1) >= HSU_FUSED_MIN_THREADS);
+  if (fused) {
     EPIC_LAUNCH_R(M.mixed, k_hsu_meridional, dim3(epic_blocks(M.ni, th), nkk), th, 0, s, M, buff, kind, k0);
     return 0;
   }

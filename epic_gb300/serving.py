@@ -16,7 +16,10 @@ steps).  The server
   * re-forms a class's batch whenever a run joins or leaves it (continuous batching: runs that
     arrive while others are on the GPU join when their class's batch in flight finishes);
   * retires a run when its steps are done: its state is copied to the host and its device
-    memory returns to the budget.
+    memory returns to the budget;
+  * retires a run whose step recorded a fatal model error (where the reference's epic_error()
+    would end the run) with that error: the model halts on the device, its memory returns to the
+    budget, and the other runs of its class go on.
 
 Each run's result is the same bits it gets when run alone (a batch gives every member the bits
 of its own step, and the number of steps per round does not change the arithmetic).
@@ -28,7 +31,8 @@ from dataclasses import dataclass, field
 
 import numpy as np
 
-from . import Batch, EPIC_PREC_MIXED, EPIC_PROFILE_N2, EPIC_SYNC_DIAGS_ONLY, Fields, HSConfig, Model, hs_setup, model_bytes
+from . import (Batch, EPIC_PREC_MIXED, EPIC_PROFILE_N2, EPIC_SYNC_DIAGS_ONLY, EpicError, Fields, HSConfig, Model, hs_setup,
+               model_bytes)
 
 
 @dataclass
@@ -50,6 +54,7 @@ class RunResult:
     finished: float
     fields: Fields | None = None
     checksum: float = 0.0
+    error: str | None = None      # the model error that ended the run early, if any
 
     @property
     def latency(self) -> float:
@@ -98,6 +103,16 @@ class DeviceBackend:
     def batch(self, models):
         return Batch(models)
 
+    def failures(self, models) -> dict:
+        """Index -> message of every model whose device-side error record is set."""
+        out = {}
+        for q, m in enumerate(models):
+            try:
+                m.sync()
+            except EpicError as e:
+                out[q] = str(e)
+        return out
+
 
 @dataclass
 class RunServer:
@@ -121,11 +136,8 @@ class RunServer:
         return time.perf_counter() - self.t0
 
     def submit(self, req: RunRequest) -> None:
-        # Serving a stream with jet-state requests mixed in raised an illegal device memory access
-        # once, whose cause has not been found; until it is, such requests are refused here (a
-        # jet state runs through Model on its own).
         if req.cfg.state != "hs" and not self.allow_jets:
-            raise ValueError(f"request {req.rid}: only Held-Suarez-state requests are served")
+            raise ValueError(f"request {req.rid}: jet-state requests need allow_jets")
         self.waiting.append(req)
 
     # -- admission -------------------------------------------------------------------------
@@ -164,10 +176,17 @@ class RunServer:
                 b, n, members = fl
                 if not b.done():
                     continue
-                b.sync()                          # reports a model error of any member
+                failed = {}
+                try:
+                    b.sync()
+                except EpicError:
+                    failed = self.backend.failures([r.model for r in members])
                 del self.inflight[cls]
                 progressed = True
-                for r in members:                 # runs admitted meanwhile were not in this batch
+                for q, r in enumerate(members):   # runs admitted meanwhile were not in this batch
+                    if q in failed:
+                        self._retire(cls, r, error=failed[q])
+                        continue
                     r.remaining -= n
                     if r.remaining <= 0:
                         self._retire(cls, r)
@@ -186,10 +205,14 @@ class RunServer:
             progressed = True
         return progressed
 
-    def _retire(self, cls, r: _Active) -> None:
-        f = r.model.download()
-        res = RunResult(r.req.rid, (r.req.cfg.ni, r.req.cfg.nj, r.req.cfg.nk), r.req.steps, r.req.arrival, r.admitted,
-                        self.now(), f if self.keep_fields else None, state_checksum(f))
+    def _retire(self, cls, r: _Active, error: str | None = None) -> None:
+        if error is None:
+            f = r.model.download()
+            res = RunResult(r.req.rid, (r.req.cfg.ni, r.req.cfg.nj, r.req.cfg.nk), r.req.steps, r.req.arrival, r.admitted,
+                            self.now(), f if self.keep_fields else None, state_checksum(f))
+        else:
+            res = RunResult(r.req.rid, (r.req.cfg.ni, r.req.cfg.nj, r.req.cfg.nk), r.req.steps, r.req.arrival, r.admitted,
+                            self.now(), None, float("nan"), error)
         self.results.append(res)
         self.active[cls].remove(r)
         b = self.batches.pop(cls, None)
@@ -220,31 +243,41 @@ class RunServer:
         return sorted(self.results, key=lambda r: r.rid)
 
 
-def poisson_requests(n: int, rate: float, seed: int, shapes: list[tuple], steps_range: tuple[int, int],
-                     dt_of=lambda shape: 300, jet_frac: float = 0.0, jet_dt: int = 60) -> list[RunRequest]:
+def poisson_requests(n: int, rate: float, seed: int, shapes: list[tuple], steps_range: tuple[int, int] | None = None,
+                     dt_of=lambda shape: 300, jet_frac: float = 0.0, jet_dt_of=lambda shape: 60,
+                     days_range: tuple[float, float] | None = None) -> list[RunRequest]:
     """n requests with seeded Poisson arrivals (mean `rate` per second), shapes drawn from
-    `shapes` (ni, nj, nk), step counts uniform in steps_range and k_f scaled by 1 +/- 10%; a
-    fraction jet_frac of them (seeded) start from the balanced zonal jets on the constant-N^2
-    sounding with time step jet_dt, the others from the Held-Suarez column with dt_of(shape)."""
+    `shapes` (ni, nj, nk), k_f scaled by 1 +/- 10%, and a duration either in steps (uniform in
+    steps_range) or in simulated days (uniform in days_range, converted to steps of the request's
+    time step); a fraction jet_frac of them (seeded) start from the balanced zonal jets on the
+    constant-N^2 sounding with time step jet_dt_of(shape), the others from the Held-Suarez column
+    with dt_of(shape)."""
+    if (steps_range is None) == (days_range is None):
+        raise ValueError("give one of steps_range and days_range")
     rng = np.random.default_rng(seed)
     t = 0.0
     out = []
     for q in range(n):
         t += float(rng.exponential(1.0 / rate))
         ni, nj, nk = shapes[int(rng.integers(len(shapes)))]
-        steps = int(rng.integers(steps_range[0], steps_range[1] + 1))
+        dur = int(rng.integers(steps_range[0], steps_range[1] + 1)) if steps_range else float(rng.uniform(*days_range))
         kf = 1.0 + float(rng.uniform(-0.1, 0.1))
         if jet_frac > 0.0 and float(rng.uniform()) < jet_frac:
-            cfg = HSConfig(ni=ni, nj=nj, nk=nk, dt=jet_dt, seed=1000 + q, profile=EPIC_PROFILE_N2, state="jet")
+            cfg = HSConfig(ni=ni, nj=nj, nk=nk, dt=jet_dt_of((ni, nj, nk)), seed=1000 + q, profile=EPIC_PROFILE_N2, state="jet")
         else:
             cfg = HSConfig(ni=ni, nj=nj, nk=nk, dt=dt_of((ni, nj, nk)), seed=1000 + q)
+        steps = dur if steps_range else max(1, int(round(dur * 86400.0 / cfg.dt)))
         out.append(RunRequest(q, cfg, steps, t, kf))
     return out
 
 
 def latency_summary(results: list[RunResult]) -> dict:
-    lat = np.array([r.latency for r in results])
+    """p50/p99 time from arrival to completion over the runs that completed, and aggregate
+    cell-steps/s over the makespan (runs ended by a model error count only up to their error)."""
+    done = [r for r in results if r.error is None]
+    lat = np.array([r.latency for r in done]) if done else np.array([np.nan])
     makespan = max(r.finished for r in results) - min(r.arrival for r in results)
-    cells = sum(r.shape[0] * r.shape[1] * r.shape[2] * r.steps for r in results)
-    return {"requests": len(results), "p50_s": float(np.percentile(lat, 50)), "p99_s": float(np.percentile(lat, 99)),
+    cells = sum(r.shape[0] * r.shape[1] * r.shape[2] * r.steps for r in done)
+    return {"requests": len(results), "completed": len(done), "ended_by_model_error": len(results) - len(done),
+            "p50_s": float(np.percentile(lat, 50)), "p99_s": float(np.percentile(lat, 99)),
             "makespan_s": makespan, "aggregate_cell_steps_per_s": cells / makespan}

@@ -192,6 +192,10 @@ int32_t epic_model_kernels_per_step(const epic_model *m);
 /* Bytes of device memory the model holds. */
 int64_t epic_model_device_bytes(const epic_model *m);
 
+/* The CUDA device the model was created on (current at epic_model_create); -1 for NULL.  Its
+ * state, stream and kernels stay there.  No counterpart in the reference. */
+int32_t epic_model_device(const epic_model *m);
+
 /* Bytes of device memory epic_model_create would take for this grid (-1 for a bad grid); for
  * admission by memory budget.  No counterpart in the reference. */
 int64_t epic_model_bytes(const epic_grid *grid, int32_t precision);
@@ -219,6 +223,7 @@ int  epic_model_filter_mass_noalloc(epic_model *m);
  * k_sigma, dt and viscosities (members may differ in state and in the drag rate hs_kf); every
  * kernel of a step is launched once for all members.  Member state stays in the member models:
  * upload and download through them (after epic_batch_sync).  The batch does not own them.
+ * Members must live on one device (epic_model_device); the batch's stream is created there.
  */
 typedef struct epic_batch epic_batch;
 int  epic_batch_create(epic_model *const *members, int32_t n, epic_batch **out);
@@ -246,14 +251,17 @@ void *epic_batch_stream(epic_batch *b);
 int32_t epic_batch_kernels_per_step(const epic_batch *b);
 
 /*
- * Launch-shape autotuning (no counterpart in the reference).  A tuning table holds
- * EPIC_TUNE_GROUPS block sizes, one per kernel group; 0 keeps the built-in choice.  Tuned kernels
- * are pointwise or per row, so a table changes no result.  epic_batch_autotune times whole steps
+ * Launch-shape autotuning (no counterpart in the reference).  A tuning table holds one entry per
+ * kernel group, 0 keeping the built-in choice: entries 0-8 are block sizes (uv_core, pgrad, Hsu
+ * meridional, hyperviscosity, diagnostics, update, column, pointwise, row filter), entry 9 the
+ * form of the meridional Hsu pass (1 one fused march per column of cells, 2 four passes over every
+ * cell; by default the fused march once its threads fill the GPU).  Tuned kernels are pointwise,
+ * per row or per column, and the two Hsu forms give the same bits, so a table changes no result.  epic_batch_autotune times whole steps
  * of the batch for each candidate (trial_steps timed steps each) and keeps the fastest; the
  * members must hold a primed state (after epic_batch_timestep(b, EPIC_SYNC_DIAGS_ONLY)), and the
  * trial steps advance it, so tune before uploading the state a run starts from.
  */
-#define EPIC_TUNE_GROUPS 9
+#define EPIC_TUNE_GROUPS 10
 int  epic_batch_autotune(epic_batch *b, int32_t trial_steps, int32_t *table_out);
 int  epic_batch_set_tuning(epic_batch *b, const int32_t *table);
 int  epic_model_set_tuning(epic_model *m, const int32_t *table);

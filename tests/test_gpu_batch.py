@@ -62,11 +62,11 @@ def test_autotuned_shapes_change_no_result(gpu):
     scratch.timestep(EPIC_SYNC_DIAGS_ONLY)
     table = scratch.autotune(trial_steps=1)
     scratch.close()
-    assert len(table) == 9 and all(t > 0 for t in table)
+    assert len(table) == 10 and all(t > 0 for t in table)
     tuned = [_member(30 + q, 1.0, EPIC_PREC_MIXED) for q in range(3)]
     plain = [_member(30 + q, 1.0, EPIC_PREC_MIXED) for q in range(3)]
     bt, bp = Batch([m for _, _, m in tuned]), Batch([m for _, _, m in plain])
-    bt.set_tuning([64, 256, 512, 64, 256, 512, 64, 512, 32])
+    bt.set_tuning([64, 256, 512, 64, 256, 512, 64, 512, 32, 1])
     for b in (bt, bp):
         b.timestep(EPIC_SYNC_DIAGS_ONLY)
         b.run(4)
@@ -118,3 +118,114 @@ def test_batch_step_host_pipeline(gpu, groups):
         for k in w.arrays:
             assert np.array_equal(h.arrays[k], w.arrays[k]), (groups, k)
         assert h.struct.itime == w.struct.itime
+
+
+# 26 members of 128x64x20: the UNITY and HDRY passes of the meridional Hsu advection cover
+# 128 * 20 * 26 = 66,560 (k, i, member) columns, past the 65,536 at which the batch launch takes
+# the fused march (k_hsu_meridional), as the 64-member ensemble of the benchmark does; THETA's
+# pass (k >= k_sigma - 1, two layers) stays on the four passes, as it does there.  A model stepped
+# alone takes the four passes for all three.
+FUSED_MEMBERS = 26
+
+
+@pytest.mark.parametrize("precision", [EPIC_PREC_FP64, EPIC_PREC_MIXED, EPIC_PREC_MIXED_FAST])
+def test_fused_meridional_march_batch_equals_members_alone(gpu, precision):
+    from oracle_lib import Port
+    shape = (128, 64, 20)
+    assert shape[0] * shape[2] * FUSED_MEMBERS >= 65536
+    members = [_member(100 + q, 1.0 + 0.1 * ((q * 7) % 11 - 5) / 5, precision, shape=shape) for q in range(FUSED_MEMBERS)]
+    batch = Batch([m for _, _, m in members])
+    batch.timestep(EPIC_SYNC_DIAGS_ONLY)
+    batch.run(3)
+    batch.sync()
+    for q, (ga, f, m) in enumerate(members):
+        alone = Model(ga, precision)
+        alone.upload(f)
+        alone.timestep(EPIC_SYNC_DIAGS_ONLY)
+        alone.run(3)
+        alone.sync()
+        a, b = m.download(), alone.download()
+        for k in a.arrays:
+            assert np.array_equal(a.arrays[k], b.arrays[k]), (q, k)
+        alone.close()
+    if precision == EPIC_PREC_FP64:
+        # and the batch's first member is the oracle's grid bit for bit
+        ga, f, m = members[0]
+        port = Port(ga, cr_libm=True)
+        port.upload(f)
+        port.timestep(EPIC_SYNC_DIAGS_ONLY)
+        port.run(3)
+        a, b = m.download(), port.download()
+        for k in a.arrays:
+            assert np.array_equal(a.arrays[k], b.arrays[k]), k
+    batch.close()
+    for _, _, m in members:
+        m.close()
+
+
+def test_divergence_damping_batch_equals_members_alone(gpu):
+    """nudiv > 0 (divergence_damping runs in every step) in a mixed batch of three members."""
+    members = []
+    for q in range(3):
+        ga, f = hs_setup(HSConfig(ni=32, nj=16, nk=10, dt=300, seed=70 + q, nudiv=0.5))
+        m = Model(ga, EPIC_PREC_MIXED)
+        m.upload(f)
+        members.append((ga, f, m))
+    b = Batch([m for _, _, m in members])
+    b.timestep(EPIC_SYNC_DIAGS_ONLY)
+    b.run(5)
+    b.sync()
+    for ga, f, m in members:
+        alone = Model(ga, EPIC_PREC_MIXED)
+        alone.upload(f)
+        alone.timestep(EPIC_SYNC_DIAGS_ONLY)
+        alone.run(5)
+        alone.sync()
+        x, y = m.download(), alone.download()
+        for k in x.arrays:
+            assert np.array_equal(x.arrays[k], y.arrays[k]), k
+
+
+def test_batch_members_on_one_device(gpu):
+    """Models record the device they were created on; a batch of them is created on it.  (A batch
+    mixing devices is refused with EPIC_ERR_ARG; one GPU cannot show that case.)"""
+    import torch
+    members = [_member(80 + q, 1.0, EPIC_PREC_FP64) for q in range(2)]
+    assert all(m.device == torch.cuda.current_device() for _, _, m in members)
+    b = Batch([m for _, _, m in members])
+    b.timestep(EPIC_SYNC_DIAGS_ONLY)
+    b.sync()
+
+
+def test_halted_member_stops_and_reports(gpu):
+    """A member whose state makes the reference stop (a negative potential temperature in one cell:
+    GZ3 not monotonic in store_pgrad_vars, found by the priming call) halts after the step in which
+    the error is seen: its state and itime stop changing and every sync reports it, while the other
+    member of the batch keeps stepping."""
+    from epic_gb300 import Fields
+    members = [_member(90 + q, 1.0, EPIC_PREC_MIXED) for q in range(2)]
+    ga, f, bad = members[1]
+    broken = f.copy()
+    broken.theta[10, 5, 5] = -1.0
+    bad.upload(broken)
+    b = Batch([m for _, _, m in members])
+    b.timestep(EPIC_SYNC_DIAGS_ONLY)
+    b.run(3)
+    with pytest.raises(EpicError, match="member 1: store_pgrad_vars: GZ3 not monotonic"):
+        b.sync()
+    good = members[0][2]
+    g0 = good.download()
+    h0 = Fields(32, 16, 10, f.uv_scheme)
+    with pytest.raises(EpicError, match="GZ3 not monotonic"):
+        bad.download(h0)
+    b.run(2)
+    with pytest.raises(EpicError, match="member 1"):
+        b.sync()
+    g1 = good.download()
+    h1 = Fields(32, 16, 10, f.uv_scheme)
+    with pytest.raises(EpicError):
+        bad.download(h1)
+    assert g1.struct.itime == g0.struct.itime + 2
+    assert h1.struct.itime == h0.struct.itime
+    for k in h0.arrays:
+        assert np.array_equal(h0.arrays[k], h1.arrays[k], equal_nan=True), k

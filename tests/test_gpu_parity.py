@@ -54,12 +54,7 @@ def _state(state):
     return {"state": state, "profile": EPIC_PROFILE_N2 if state == "jet" else 0}
 
 
-@pytest.mark.parametrize("adv,state", [(EPIC_ADV_HSU, "hs"), (EPIC_ADV_AKIMA, "hs"), (EPIC_ADV_HSU, "jet")])
-@pytest.mark.parametrize("scheme", [EPIC_UV_AB3, EPIC_UV_LEAPFROG])
-def test_stage_by_stage(gpu, scheme, adv, state):
-    """Each reference function on the path, GPU vs the correctly rounded restatement, bit for
-    bit, from the same spun-up state."""
-    cfg = HSConfig(ni=32, nj=16, nk=10, dt=300, uv_scheme=scheme, seed=3, advection_scheme=adv, **_state(state))
+def _stage_by_stage(cfg):
     ga, f = _spin_up(cfg, 4)
     port = Port(ga, cr_libm=True)
     port.upload(f)
@@ -77,6 +72,21 @@ def test_stage_by_stage(gpu, scheme, adv, state):
             # continue from the oracle's state so that later stages are tested on their own
             model.upload(b)
     assert not failures, "\n".join(failures)
+
+
+@pytest.mark.parametrize("adv,state", [(EPIC_ADV_HSU, "hs"), (EPIC_ADV_AKIMA, "hs"), (EPIC_ADV_HSU, "jet")])
+@pytest.mark.parametrize("scheme", [EPIC_UV_AB3, EPIC_UV_LEAPFROG])
+def test_stage_by_stage(gpu, scheme, adv, state):
+    """Each reference function on the path, GPU vs the correctly rounded restatement, bit for
+    bit, from the same spun-up state."""
+    _stage_by_stage(HSConfig(ni=32, nj=16, nk=10, dt=300, uv_scheme=scheme, seed=3, advection_scheme=adv, **_state(state)))
+
+
+@pytest.mark.parametrize("scheme", [EPIC_UV_AB3, EPIC_UV_LEAPFROG])
+def test_stage_by_stage_divergence_damping(gpu, scheme):
+    """As above with nudiv_nondim = 0.5, so that divergence_damping (epic_subgrid.c:1792-1885,
+    stage 13) acts."""
+    _stage_by_stage(HSConfig(ni=32, nj=16, nk=10, dt=300, uv_scheme=scheme, seed=5, nudiv=0.5))
 
 
 @pytest.mark.parametrize("adv,state", [(EPIC_ADV_HSU, "hs"), (EPIC_ADV_AKIMA, "hs"), (EPIC_ADV_HSU, "jet")])
@@ -111,11 +121,17 @@ def test_sync_diags(gpu):
                                                           (EPIC_UV_AB3, 1, 1e-11, EPIC_ADV_AKIMA, "hs"),
                                                           (EPIC_UV_AB3, 100, 1e-8, EPIC_ADV_AKIMA, "hs"),
                                                           (EPIC_UV_AB3, 1, 1e-11, EPIC_ADV_HSU, "jet"),
-                                                          (EPIC_UV_AB3, 100, 1e-8, EPIC_ADV_HSU, "jet")])
+                                                          (EPIC_UV_AB3, 100, 1e-8, EPIC_ADV_HSU, "jet"),
+                                                          (EPIC_UV_AB3, 200, 1e-8, EPIC_ADV_HSU, "hs"),
+                                                          (EPIC_UV_AB3, 100, 1e-8, EPIC_ADV_HSU, "hs-nudiv")])
 def test_full_step(gpu, scheme, nsteps, tol, adv, state):
-    """The 64x32x10 configuration (Held-Suarez column or zonal jets): per-prognostic relative L2
-    after nsteps."""
-    cfg = HSConfig(ni=64, nj=32, nk=10, dt=300, uv_scheme=scheme, advection_scheme=adv, **_state(state))
+    """The 64x32x10 configuration (Held-Suarez column or zonal jets; "hs-nudiv": the column with
+    divergence damping, nudiv_nondim = 0.5): per-prognostic relative L2 after nsteps.  200
+    steps is the configuration's own run length."""
+    extra = {}
+    if state == "hs-nudiv":
+        state, extra = "hs", {"nudiv": 0.5}
+    cfg = HSConfig(ni=64, nj=32, nk=10, dt=300, uv_scheme=scheme, advection_scheme=adv, **_state(state), **extra)
     ga, f, port, model = _pair(cfg)
     port.timestep(EPIC_SYNC_DIAGS_ONLY)
     port.run(nsteps)
@@ -146,3 +162,58 @@ def test_graph_replay_matches_eager(gpu):
     for k in PROGNOSTIC:
         x, y = a.arrays[k], b.arrays[k]
         assert np.array_equal(x, y), k
+
+
+@pytest.mark.parametrize("state", ["hs", "jet"])
+@pytest.mark.parametrize("scheme", [EPIC_UV_AB3, EPIC_UV_LEAPFROG])
+def test_fused_meridional_march_bitwise(gpu, scheme, state):
+    """The fused meridional Hsu march (k_hsu_meridional, which batches of many members take)
+    forced on one 64x32x20 model for every advected field (UNITY, THETA, HDRY): ten steps equal
+    the correctly rounded restatement bit for bit."""
+    from epic_gb300 import TUNE_HSU_MERID_VARIANT
+    cfg = HSConfig(ni=64, nj=32, nk=20, dt=300, uv_scheme=scheme, seed=11, **_state(state))
+    ga, f, port, model = _pair(cfg, cr_libm=True)
+    table = [0] * (TUNE_HSU_MERID_VARIANT + 1)
+    table[TUNE_HSU_MERID_VARIANT] = 1
+    model.set_tuning(table)
+    port.timestep(EPIC_SYNC_DIAGS_ONLY)
+    port.run(10)
+    model.timestep(EPIC_SYNC_DIAGS_ONLY)
+    model.run(10)
+    model.sync()
+    diff = _differing(model.download(), port.download())
+    assert not diff, diff
+
+
+# The shapes of the configurations themselves: the 128x64x20 ensemble member (Held-Suarez column,
+# dt 300 s) and the 256x128x32 zonal-jet run (dt 60 s).  Launch shapes there differ from the small
+# grids above (row threads of the filters, block counts, the autotuner's defaults).
+NAMED_SHAPES = [("hs", 128, 64, 20, 300), ("jet", 256, 128, 32, 60)]
+
+
+@pytest.mark.parametrize("state,ni,nj,nk,dt", NAMED_SHAPES)
+def test_named_shapes(gpu, state, ni, nj, nk, dt):
+    """FP64 form at the configurations' shapes: ten steps equal the correctly rounded
+    restatement bit for bit; against the glibc restatement (the reference build's arithmetic)
+    relative L2 per prognostic <= 1e-11 after one step and <= 1e-8 after ten."""
+    cfg = HSConfig(ni=ni, nj=nj, nk=nk, dt=dt, seed=1, **_state(state))
+    ga, f = hs_setup(cfg)
+    model = Model(ga)
+    model.upload(f)
+    model.timestep(EPIC_SYNC_DIAGS_ONLY)
+    glibc = Port(ga)
+    glibc.upload(f)
+    glibc.timestep(EPIC_SYNC_DIAGS_ONLY)
+    for nsteps, tol in ((1, 1e-11), (9, 1e-8)):
+        model.run(nsteps)
+        model.sync()
+        glibc.run(nsteps)
+        errs = field_errors(model.download(), glibc.download(), PROGNOSTIC)
+        for k in PROGNOSTIC:
+            assert errs[k][0] <= tol, (nsteps, k, errs[k])
+    cr = Port(ga, cr_libm=True)
+    cr.upload(f)
+    cr.timestep(EPIC_SYNC_DIAGS_ONLY)
+    cr.run(10)
+    diff = _differing(model.download(), cr.download())
+    assert not diff, diff

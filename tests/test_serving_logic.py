@@ -12,8 +12,12 @@ from epic_gb300.serving import RunRequest, RunServer, latency_summary
 
 
 class FakeModel:
-    def __init__(self, cfg):
-        self.cfg, self.steps, self.closed = cfg, 0, False
+    def __init__(self, cfg, fail_at=None):
+        self.cfg, self.steps, self.closed, self.fail_at = cfg, 0, False, fail_at
+
+    @property
+    def failed(self):
+        return self.fail_at is not None and self.steps >= self.fail_at
 
     def download(self):
         a = np.full((2, 2), float(self.steps))
@@ -41,7 +45,9 @@ class FakeBatch:
         return self.polls > self.lag
 
     def sync(self):
-        pass
+        from epic_gb300 import EpicError
+        if any(m.failed for m in self.models):
+            raise EpicError("member failed")
 
     def close(self):
         pass
@@ -50,8 +56,9 @@ class FakeBatch:
 class FakeBackend:
     """Device bytes = cells (so that the budget is easy to reason about)."""
 
-    def __init__(self, lag=0):
+    def __init__(self, lag=0, fail_at=None):
         self.models, self.log, self.lag = [], [], lag
+        self.fail_at = fail_at or {}   # request seed -> step count at which its model errs
 
     def setup(self, cfg):
         return SimpleNamespace(struct=SimpleNamespace(hs_kf=1.0), cfg=cfg), None
@@ -61,17 +68,20 @@ class FakeBackend:
         return c.ni * c.nj * c.nk
 
     def model(self, grid, fields, precision):
-        m = FakeModel(grid.cfg)
+        m = FakeModel(grid.cfg, self.fail_at.get(grid.cfg.seed))
         self.models.append(m)
         return m
 
     def batch(self, models):
         return FakeBatch(self.log, models, self.lag)
 
+    def failures(self, models):
+        return {q: "model error" for q, m in enumerate(models) if m.failed}
+
 
 def _req(rid, shape, steps, arrival=0.0):
     ni, nj, nk = shape
-    return RunRequest(rid, HSConfig(ni=ni, nj=nj, nk=nk), steps, arrival=arrival)
+    return RunRequest(rid, HSConfig(ni=ni, nj=nj, nk=nk, seed=rid), steps, arrival=arrival)
 
 
 @pytest.mark.parametrize("lag", [0, 3])
@@ -110,3 +120,30 @@ def test_run_joining_a_busy_class_steps_exactly_its_count():
 def test_oversized_request_is_rejected():
     with pytest.raises(ValueError, match="budget"):
         RunServer(hbm_budget=100, backend=FakeBackend()).serve([_req(0, (64, 32, 10), 2)])
+
+
+def test_run_ended_by_a_model_error_is_retired_and_the_rest_go_on():
+    """A run whose model reports an error (the device halts it) is retired with that error and its
+    memory returns to the budget; the other run of its class and a later one still complete."""
+    be = FakeBackend(fail_at={1: 5})
+    shape = (32, 16, 10)
+    reqs = [_req(0, shape, 12), _req(1, shape, 12), _req(2, shape, 8, arrival=0.003)]
+    server = RunServer(hbm_budget=2 * 32 * 16 * 10, round_steps=4, backend=be)
+    res = server.serve(reqs)
+    assert [r.rid for r in res] == [0, 1, 2]
+    assert res[1].error == "model error" and res[0].error is None and res[2].error is None
+    assert [m.steps for m in be.models] == [12, 8, 8]
+    assert server.used == 0 and all(m.closed for m in be.models)
+    s = latency_summary(res)
+    assert s["completed"] == 2 and s["ended_by_model_error"] == 1
+
+
+def test_durations_in_simulated_days():
+    from epic_gb300.serving import poisson_requests
+    reqs = poisson_requests(30, 20.0, 5, [(64, 32, 10), (128, 64, 20)], dt_of=lambda s: 300, jet_frac=0.5,
+                            jet_dt_of=lambda s: 60, days_range=(0.25, 2.0))
+    assert any(r.cfg.state == "jet" for r in reqs) and any(r.cfg.state == "hs" for r in reqs)
+    for r in reqs:
+        days = r.steps * r.cfg.dt / 86400.0
+        assert 0.25 - 1e-3 <= days <= 2.0 + 1e-3
+    assert all(np.diff([r.arrival for r in reqs]) > 0)

@@ -5,7 +5,7 @@ after every other GPU test in the same process."""
 import numpy as np
 import pytest
 
-from epic_gb300 import EPIC_SYNC_DIAGS_ONLY, EpicError, HSConfig, Model, hs_setup
+from epic_gb300 import EPIC_PREC_FP64, EPIC_PREC_MIXED, EPIC_SYNC_DIAGS_ONLY, EpicError, HSConfig, Model, hs_setup
 from oracle_lib import Port
 
 pytestmark = pytest.mark.gpu
@@ -22,11 +22,15 @@ def _spun_up(cfg, nsteps):
     return ga, port.download()
 
 
-@pytest.mark.parametrize("shape", [(32, 16, 10), (64, 32, 20)])
-def test_noalloc_filter_matches_stage(gpu, shape):
+@pytest.mark.parametrize("shape,precision", [((32, 16, 10), EPIC_PREC_FP64), ((64, 32, 20), EPIC_PREC_FP64),
+                                              ((32, 16, 10), EPIC_PREC_MIXED), ((128, 64, 20), EPIC_PREC_MIXED)])
+def test_noalloc_filter_matches_stage(gpu, shape, precision):
+    """Both precision forms: the mixed form's filter has its own shared-memory layout (profile
+    intervals, FP32 row) and filters only the filtered rows; at ni = 128 its filtered GZ copy
+    (stage 8) runs on the tensor cores."""
     ni, nj, nk = shape
     ga, f = _spun_up(HSConfig(ni=ni, nj=nj, nk=nk, dt=300, seed=7), 3)
-    ref, fixed = Model(ga), Model(ga)
+    ref, fixed = Model(ga, precision), Model(ga, precision)
     for m in (ref, fixed):
         m.upload(f)
         m.run_stage(8)   # the filtered GZ copy whose bottom row and profiles the 3-D filter reads
