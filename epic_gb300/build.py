@@ -17,7 +17,8 @@ ROOT = os.path.dirname(HERE)
 SRC = os.path.join(HERE, "csrc")
 OUT = os.path.join(HERE, "_lib")
 LIB = os.path.join(OUT, "libepic_gb300.so")
-SOURCES = ["epic_model.cu", "k_filter.cu", "k_filter_gemm.cu", "k_column.cu", "k_column_acc.cu", "k_stencil.cu", "epic_setup.cpp"]
+SOURCES = ["epic_model.cu", "k_filter.cu", "k_filter_gemm.cu", "k_column.cu", "k_column_acc.cu", "k_stencil.cu", "epic_setup.cpp",
+           "epic_dropin.cpp"]
 ARCH = "-gencode=arch=compute_103a,code=sm_103a"
 
 
@@ -73,16 +74,6 @@ def build(verbose: bool = False) -> str:
     return LIB
 
 
-def build_oracle(with_reference: bool = True) -> None:
-    """Compile the oracle's CPU restatement, and the reference harness where its sources exist."""
-    oracle = os.path.join(ROOT, "oracle")
-    subprocess.run(["make", "-s", "-C", oracle, "port"], check=True)
-    ref = os.environ.get("EPIC_REFERENCE_DIR", "/root/reference")
-    if with_reference and os.path.isdir(os.path.join(ref, "src", "shared")):
-        subprocess.run(["make", "-s", "-j8", "-C", oracle, "ref", f"REF={ref}"], check=True)
-
-
 if __name__ == "__main__":
     build(verbose=True)
-    build_oracle()
     sys.exit(0)

@@ -608,6 +608,13 @@ extern "C" int epic_model_timestep(epic_model *m, int32_t action) {
   return set_error(EPIC_ERR_ARG, "unrecognized action=%d", action);
 }
 
+extern "C" int epic_model_set_itime(epic_model *m, int64_t itime) {
+  if (!m) return set_error(EPIC_ERR_ARG, "epic_model_set_itime: NULL model");
+  if (!m->uploaded) return set_error(EPIC_ERR_STATE, "set_itime before upload");
+  epic::launch_set_itime(m->d, (long long)itime, m->stream);
+  return check_launch("epic_model_set_itime");
+}
+
 extern "C" int epic_model_run_stage(epic_model *m, int32_t stage) {
   if (!m) return set_error(EPIC_ERR_ARG, "epic_model_run_stage: NULL model");
   if (!m->uploaded) return set_error(EPIC_ERR_STATE, "stage before upload");

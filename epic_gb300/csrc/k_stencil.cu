@@ -1072,6 +1072,13 @@ __global__ void k_itime_advance(DevModel M) {
   else M.ctl->itime += 1;
 }
 
+// grid.itime as the caller's driver loop holds it (the drop-in: the driver advances it after each
+// timestep() call, epic_main.c:424).  Runs on a halted model too.
+__global__ void k_set_itime(DevModel M, long long itime) {
+  epic_member(M);
+  M.ctl->itime = itime;
+}
+
 // ---- launchers ----
 
 int launch_copy_gz(const DevModel &M, cudaStream_t s) {
@@ -1245,6 +1252,11 @@ int launch_store_diag(const DevModel &M, cudaStream_t s) {
 
 int launch_itime_advance(const DevModel &M, cudaStream_t s) {
   k_itime_advance<<<zg(1, M), 1, 0, s>>>(M);
+  return 0;
+}
+
+int launch_set_itime(const DevModel &M, long long itime, cudaStream_t s) {
+  k_set_itime<<<zg(1, M), 1, 0, s>>>(M, itime);
   return 0;
 }
 

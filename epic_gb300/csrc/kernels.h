@@ -95,5 +95,6 @@ int launch_divergence_damping(const DevModel &M, cudaStream_t s);
 int launch_uv_update(const DevModel &M, cudaStream_t s);
 int launch_store_diag(const DevModel &M, cudaStream_t s);
 int launch_itime_advance(const DevModel &M, cudaStream_t s);
+int launch_set_itime(const DevModel &M, long long itime, cudaStream_t s);
 
 }  // namespace epic

@@ -158,6 +158,14 @@ int  epic_model_run(epic_model *m, int32_t nsteps);
  */
 int  epic_model_run_stage(epic_model *m, int32_t stage);
 
+/*
+ * Set grid.itime on the device, in stream order, to the value a driver that owns it holds (the
+ * reference's loop advances grid.itime after each timestep() call, src/shared/epic_main.c:424;
+ * store_pgrad_vars reads it, epic_funcs_diag.c:3666,3901).  epic_model_run advances it by one
+ * per step; epic_model_timestep leaves it unchanged.
+ */
+int  epic_model_set_itime(epic_model *m, int64_t itime);
+
 /* Wait for queued work and report any device-side model error. */
 int  epic_model_sync(epic_model *m);
 
@@ -209,7 +217,9 @@ int64_t epic_model_bytes(const epic_grid *grid, int32_t precision);
  *
  * Limit: (nj+3)*(nk+2) <= EPIC_NOALLOC_TABLE_ENTRIES; larger grids return EPIC_ERR_ARG.
  * The first call on a device resolves the array's address (cudaGetSymbolAddress with the
- * model's device current); make that first call before any stream capture begins.  Nothing in
+ * model's device current) and keeps it for the life of the process; make that first call before
+ * any stream capture begins, and do not reset the device (cudaDeviceReset) while the library is
+ * in use, which could move the array.  Nothing in
  * the array needs to start at zero: every table entry is written before it is read in the same
  * call.  The array is shared by every model on the device, so calls must not overlap: issue
  * them on one stream, or synchronise between them.  Results equal epic_model_run_stage(m, 10).
@@ -268,6 +278,36 @@ int  epic_model_set_tuning(epic_model *m, const int32_t *table);
 
 /* Text of the last error on this thread. */
 const char *epic_last_error(void);
+
+/*
+ * The drop-in step, with the calling convention of the reference's
+ *     void timestep(planetspec *planet, int action, EPIC_FLOAT **Buff2D)
+ * (include/epic.h:654-656, src/shared/epic_timestep.c:62): one model per process, created by the
+ * first call, as the reference's first call allocates and its callees keep static state.  A
+ * timestep() wrapper compiled with the reference's headers (epic_gb300/dropin/epic_timestep_gb300.c)
+ * fills *grid and *f from the globals `grid`, `planet` and `var` and calls these.
+ *
+ * epic_dropin_timestep: the first call creates the model from *grid on the current device
+ * (precision form as for epic_model_create) and uploads *f.  Every call sets the device's itime
+ * to `itime` (the driver's grid.itime, which the driver advances after the call) and runs
+ * timestep(action): one step, or the synchronising call.  Mode EPIC_DROPIN_MIRROR (fixed by the
+ * first call) then copies the state back into *f, time-plane indices, itime and model_time
+ * included, so that the host arrays are current after every call and an unchanged driver works;
+ * EPIC_DROPIN_RESIDENT leaves the host arrays stale until epic_dropin_sync_to_host (the driver
+ * calls it before var_write).  The first error is kept: later calls return it without stepping
+ * (the reference's epic_error() ends the run, src/shared/epic_funcs_io.c:4872).
+ *
+ * epic_dropin_status: EPIC_OK, or the code of the first error, after waiting for queued work
+ * (the reference's epic_error text is epic_dropin_message()).  epic_dropin_release frees the
+ * model; the next epic_dropin_timestep starts over.
+ */
+#define EPIC_DROPIN_MIRROR   0
+#define EPIC_DROPIN_RESIDENT 1
+int  epic_dropin_timestep(const epic_grid *grid, epic_fields *f, int32_t precision, int32_t mode, int32_t action, int64_t itime);
+int  epic_dropin_sync_to_host(epic_fields *f);
+int  epic_dropin_status(void);
+const char *epic_dropin_message(void);
+void epic_dropin_release(void);
 
 /*
  * Host-side synthetic Held-Suarez set-up (no GPU needed).  These restate the grid

@@ -26,7 +26,8 @@ ORACLE = os.path.join(ROOT, "oracle")
 PORT_LIB = os.path.join(ORACLE, "_build", "libepicport.so")
 PORT_CR_LIB = os.path.join(ORACLE, "_build", "libepicport_cr.so")
 REF_LIB = os.path.join(ORACLE, "_ref", "libepicref.so")
-REFERENCE_DIR = os.environ.get("EPIC_REFERENCE_DIR", "/root/reference")
+# where the reference's sources are: oracle/Makefile's REF unless EPIC_REFERENCE_DIR says otherwise
+REF_ARGS = [f"REF={os.environ['EPIC_REFERENCE_DIR']}"] if os.environ.get("EPIC_REFERENCE_DIR") else []
 
 _port = {}
 
@@ -37,11 +38,10 @@ def build_port() -> str:
 
 
 def reference_available() -> bool:
-    if os.path.exists(REF_LIB):
-        return True
-    if not os.path.isdir(os.path.join(REFERENCE_DIR, "src", "shared")):
+    """Whether the reference's sources are present (and its step is built)."""
+    if subprocess.run(["make", "-s", "-C", ORACLE, "have-ref", *REF_ARGS], capture_output=True).returncode != 0:
         return False
-    r = subprocess.run(["make", "-s", "-j8", "-C", ORACLE, "ref", f"REF={REFERENCE_DIR}"], capture_output=True)
+    r = subprocess.run(["make", "-s", "-j8", "-C", ORACLE, "ref", *REF_ARGS], capture_output=True)
     return r.returncode == 0 and os.path.exists(REF_LIB)
 
 

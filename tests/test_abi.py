@@ -75,3 +75,33 @@ def test_model_needs_a_gpu_here():
     ga, _ = hs_setup(HSConfig(ni=16, nj=8, nk=6))
     with pytest.raises(EpicError):
         epic_gb300.Model(ga)
+
+
+def test_dropin_wrapper_links_in_place_of_the_reference_step(cuda_lib):
+    """epic_gb300/dropin/epic_timestep_gb300.c, compiled with the reference's headers, linked with
+    the reference's objects in place of its timestep() (oracle/Makefile `dropin`) and driven by the
+    reference harness: its timestep() is the one reached, and without a GPU it ends the run the
+    reference's way, epic_error() naming timestep and the CUDA failure, exit status 1."""
+    import subprocess
+    import sys
+    from oracle_lib import ORACLE, REF_ARGS, reference_available
+    if not reference_available():
+        pytest.skip("needs the reference source tree")
+    r = subprocess.run(["make", "-s", "-C", ORACLE, "dropin", *REF_ARGS], capture_output=True, text=True)
+    assert r.returncode == 0, r.stderr
+    import torch
+    if torch.cuda.is_available():
+        pytest.skip("a GPU is present: tests/test_gpu_dropin.py covers the step")
+    code = (
+        "import ctypes as C, sys\n"
+        f"sys.path[:0] = [{ROOT!r}, {os.path.join(ROOT, 'tests')!r}]\n"
+        "from epic_gb300 import HSConfig, hs_setup\n"
+        "ga, f = hs_setup(HSConfig(ni=32, nj=16, nk=10, dt=300))\n"
+        f"lib = C.CDLL({os.path.join(ORACLE, '_ref', 'libepicref_dropin.so')!r})\n"
+        "assert lib.ref_init(C.byref(ga.struct), C.byref(f.struct)) == 0\n"
+        "lib.ref_timestep(1)\n"
+        "print('returned')\n")
+    p = subprocess.run([sys.executable, "-c", code], capture_output=True, text=True, timeout=300)
+    out = p.stdout + p.stderr
+    assert p.returncode == 1 and "returned" not in out, out
+    assert "EPIC Error" in out and "timestep" in out, out

@@ -193,27 +193,37 @@ NAMED_SHAPES = [("hs", 128, 64, 20, 300), ("jet", 256, 128, 32, 60)]
 
 @pytest.mark.parametrize("state,ni,nj,nk,dt", NAMED_SHAPES)
 def test_named_shapes(gpu, state, ni, nj, nk, dt):
-    """FP64 form at the configurations' shapes: ten steps equal the correctly rounded
-    restatement bit for bit; against the glibc restatement (the reference build's arithmetic)
-    relative L2 per prognostic <= 1e-11 after one step and <= 1e-8 after ten."""
+    """FP64 form at the configurations' shapes: after one and after ten steps the GPU state equals
+    the correctly rounded restatement bit for bit, and stays within relative L2 1e-11 (one step)
+    and 1e-8 (ten steps) per prognostic of the glibc restatement (the reference build's
+    arithmetic) -- or, where the two restatements are farther apart than that (glibc's pow is
+    not correctly rounded in ~0.1% of calls; from rest U is small after one step, so one-ulp
+    differences in P2/T3 show at ~1e-11), exactly their distance, which the GPU then inherits."""
     cfg = HSConfig(ni=ni, nj=nj, nk=nk, dt=dt, seed=1, **_state(state))
     ga, f = hs_setup(cfg)
     model = Model(ga)
     model.upload(f)
     model.timestep(EPIC_SYNC_DIAGS_ONLY)
-    glibc = Port(ga)
-    glibc.upload(f)
-    glibc.timestep(EPIC_SYNC_DIAGS_ONLY)
+    ports = {}
+    for cr in (True, False):
+        ports[cr] = Port(ga, cr_libm=cr)
+        ports[cr].upload(f)
+        ports[cr].timestep(EPIC_SYNC_DIAGS_ONLY)
+    floors = {}
     for nsteps, tol in ((1, 1e-11), (9, 1e-8)):
         model.run(nsteps)
         model.sync()
-        glibc.run(nsteps)
-        errs = field_errors(model.download(), glibc.download(), PROGNOSTIC)
+        got = model.download()
+        for p in ports.values():
+            p.run(nsteps)
+        want_cr, want_glibc = ports[True].download(), ports[False].download()
+        diff = _differing(got, want_cr)
+        assert not diff, (nsteps, diff)
+        errs = field_errors(got, want_glibc, PROGNOSTIC)
+        floor = field_errors(want_cr, want_glibc, PROGNOSTIC)
         for k in PROGNOSTIC:
-            assert errs[k][0] <= tol, (nsteps, k, errs[k])
-    cr = Port(ga, cr_libm=True)
-    cr.upload(f)
-    cr.timestep(EPIC_SYNC_DIAGS_ONLY)
-    cr.run(10)
-    diff = _differing(model.download(), cr.download())
-    assert not diff, diff
+            assert errs[k][0] <= max(tol, floor[k][0]), (nsteps, k, errs[k], floor[k])
+            # the restatements differ by libm rounding only: far below the 100-step bar
+            assert floor[k][0] <= 1e-9, (nsteps, k, floor[k])
+        floors[nsteps] = {k: v[0] for k, v in floor.items()}
+    print(f"{state} {ni}x{nj}x{nk}: glibc-vs-correctly-rounded restatement distance {floors}")
