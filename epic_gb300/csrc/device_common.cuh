@@ -87,6 +87,10 @@ struct DevModel {
   // launched over a batch take member blockIdx.z's description on entry (EPIC_MEMBER)
   const DevModel *batch;
   int nbatch;
+  int hetero;          // batch launch over members of different ni / nj (epic_member relocates
+                       // pointer arguments field by field); the launch description then carries
+                       // the largest sizes of its members, and member 0's arrays
+  long long reloc_n3;  // a launch description's field size of member 0 (whose arrays it carries)
   char *pool_base;   // start of the model's device pool (state, scratch and tables)
   // launch shapes (host side only): threads per block of each kernel group, set by the
   // autotuner; they change no result (every tuned kernel is pointwise or per row)
@@ -98,18 +102,47 @@ struct DevModel {
   __host__ __device__ __forceinline__ int at2(int j, int i) const { return i + (j + 1) * iadim; }
 };
 
+// The 3-D arrays a kernel argument can point into, with their plane counts.
+#define EPIC_FIELD_LIST(X)                                                                         \
+  X(u, from.nvp) X(v, from.nvp) X(dudt, from.ntp) X(dvdt, from.ntp) X(hdry, 1) X(theta, 1) X(p3, 1)  \
+  X(h3, 1) X(p2, 1) X(theta2, 1) X(t2, 1) X(t3, 1) X(rho2, 1) X(rho3, 1) X(exner3, 1) X(gz3, 1)      \
+  X(mont3, 1) X(heat3, 1) X(pv3, 1) X(ri2, 1) X(div_uv3, 1) X(w3, 1) X(dzdt3, 1) X(u_spinup, 1)      \
+  X(gz, 1) X(unity, 1) X(old, 1) X(work0, 1) X(work1, 1) X(work2, 1) X(work3, 1)
+
+// A pointer into one of member 0's arrays (plane q, offset o within the plane), moved to the
+// same plane of the same array of member `to`.  Members of different sizes have different pool
+// layouts, so the array is found by address; a pointer outside every array is returned as is.
+template <class P>
+__device__ __forceinline__ P *relocate_field(const DevModel &from, const DevModel &to, P *p) {
+  const double *d = reinterpret_cast<const double *>(p);
+  const long long n3 = from.reloc_n3;
+#define EPIC_RELOCATE(f, planes)                                              \
+  if (d >= from.f && d < from.f + (long long)(planes) * n3) {                 \
+    const long long o = d - from.f, q = o / n3;                               \
+    return reinterpret_cast<P *>(to.f + q * to.n3 + (o - q * n3));            \
+  }
+  EPIC_FIELD_LIST(EPIC_RELOCATE)
+#undef EPIC_RELOCATE
+  return p;
+}
+
 // Entry of every kernel: in a batch launch, take member blockIdx.z's description and move the
-// state pointers passed as arguments (addresses in the launch description's pool) to the same
-// offsets in the member's pool (members of a batch share the pool layout).  Returns true when
-// the model is halted (a step found a fatal error): the kernel then returns at once.  Ctl::halted
-// changes only in k_itime_advance, between steps, so every thread of a launch reads the same value.
+// state pointers passed as arguments (addresses in the launch description's arrays) to the same
+// places in the member's arrays: by offset when the members share the pool layout (same sizes),
+// array by array when they do not.  Returns true when the model is halted (a step found a fatal
+// error): the kernel then returns at once.  Ctl::halted changes only in k_itime_advance, between
+// steps, so every thread of a launch reads the same value.
 template <class... P>
 __device__ __forceinline__ bool epic_member(DevModel &M, P *&...ptrs) {
   if (M.batch) {
-    const char *from = M.pool_base;
-    M = M.batch[blockIdx.z];
-    const char *to = M.pool_base;
-    ((ptrs = ptrs ? (P *)(to + ((const char *)ptrs - from)) : ptrs), ...);
+    const DevModel &mem = M.batch[blockIdx.z];
+    if (M.hetero) {
+      ((ptrs = ptrs ? relocate_field(M, mem, ptrs) : ptrs), ...);
+    } else {
+      const char *from = M.pool_base, *to = mem.pool_base;
+      ((ptrs = ptrs ? (P *)(to + ((const char *)ptrs - from)) : ptrs), ...);
+    }
+    M = mem;
   }
   return M.ctl->halted != 0;
 }

@@ -1,5 +1,6 @@
 // Host side of the GB300 timestep(): device state, the step sequence, CUDA-graph replay and
 // the C ABI of include/epic_gb300.h.
+#include <algorithm>
 #include <cmath>
 #include <cstdio>
 #include <cstdlib>
@@ -178,10 +179,16 @@ int run_stage_on(const DevModel &M, cudaStream_t s, int stage) {
       meridional(M, M.hdry, 2, s);
       zonal(M, M.hdry, 1, 1, s);
       launch_restore_mass(M, s);
-      launch_set_p2etc(M, 0, s, false);   // its P2 is recomputed (stage 11) before the pressure gradient
+      // Its P2 is recomputed (stage 11) before the pressure gradient.  EPIC_PREC_MIXED runs the
+      // double-float kernel here too: it writes the interfaces' logarithms that stage 7 reads.
+      launch_set_p2etc(M, 0, s, M.col64);
       break;
     }
-    case 7: launch_store_pgrad_vars(M, s, false); break;   // GZ3 for the filtered copy (stage 8)
+    // GZ3 for the filtered copy (stage 8).  The copy places the 3-D filter's profiles (stages 9
+    // and 10), which pass column-to-column rounding noise of GZ3 into the filtered fields, so
+    // EPIC_PREC_MIXED computes it with the double-float kernel of stage 19 (its FP32 one made
+    // the wind error after a day ~2x larger); EPIC_PREC_MIXED_FAST keeps the FP32 kernel.
+    case 7: launch_store_pgrad_vars(M, s, M.col64); break;
     case 8:
       launch_copy_gz(M, s);
       // The 3-D filter's profiles interpolate in the filtered GZ: filtering GZ itself in FP32
@@ -740,19 +747,23 @@ extern "C" int epic_model_filter_mass_noalloc(epic_model *m) {
   return rc;
 }
 
-// ---- batches: one launch per kernel for every member of a shape class ----
+// ---- batches: one launch per kernel for every member ----
 //
-// A batch is a view over models created by epic_model_create that share every launch-shaping
-// parameter (sizes, scheme, precision form, k_sigma, dt, viscosities); members may differ in
-// their state and in the Held-Suarez drag rate k_f.  The members' descriptions live in one
-// device array; each kernel of the step is launched once with gridDim.z = members and takes
-// member blockIdx.z's description on entry, so a 64-member ensemble costs the launches of one
-// model.  Member state stays in each member's own device memory: upload and download go
-// through the member models, after epic_batch_sync.
+// A batch is a view over models created by epic_model_create that share what shapes the step's
+// sequence of launches: the layers (nk, k_sigma), the schemes, the precision form, which
+// viscosity orders and whether divergence damping act, the filter latitude, and (in the mixed
+// forms) whether the zonal filter runs on the tensor cores (ni a multiple of 128).  Members may
+// differ in ni, nj, dt, their state and the Held-Suarez drag rate k_f.  The members' descriptions
+// live in one device array; each kernel of the step is launched once with gridDim.z = members
+// and a grid sized for the largest member, and takes member blockIdx.z's description on entry
+// (epic_member): its own sizes bound its threads, its own coefficients and arrays are used.  So
+// a 64-member ensemble, or runs of several grid sizes, cost the launches of one model.  Member
+// state stays in each member's own device memory: upload and download go through the member
+// models, after epic_batch_sync.
 
 struct epic_batch {
   std::vector<epic_model *> members;
-  DevModel d;                       // launch description: member 0's, with batch/nbatch set
+  DevModel d;                       // launch description: member 0's arrays, the largest sizes
   DevModel *dev_members = nullptr;
   cudaStream_t stream = nullptr;
   cudaGraphExec_t run_graph = nullptr;
@@ -765,14 +776,23 @@ struct epic_batch {
 
 namespace {
 
-bool same_launch_shape(const DevModel &a, const DevModel &b) {
-  if (a.ni != b.ni || a.nj != b.nj || a.nk != b.nk || a.uv_scheme != b.uv_scheme || a.akima != b.akima || a.mixed != b.mixed || a.col64 != b.col64 ||
-      a.k_sigma != b.k_sigma || a.k_sponge != b.k_sponge || a.newt_cool_on != b.newt_cool_on || a.dt != b.dt ||
-      a.nudiv != b.nudiv || a.lat0 != b.lat0)
-    return false;
-  for (int i = 0; i < 9; i++)
-    if (a.coef[i] != b.coef[i] || a.nu[i] != b.nu[i]) return false;
-  return true;
+bool tensor_filter(const DevModel &a) { return a.mixed && a.ni % 128 == 0 && a.ni <= 1024; }
+
+// Whether two models can share every launch of a step (see above); *why names the difference.
+bool batch_compatible(const DevModel &a, const DevModel &b, const char **why) {
+  *why = nullptr;
+  if (a.nk != b.nk || a.k_sigma != b.k_sigma) *why = "layers (nk, k_sigma)";
+  else if (a.uv_scheme != b.uv_scheme || a.akima != b.akima) *why = "time or advection scheme";
+  else if (a.mixed != b.mixed || a.col64 != b.col64) *why = "precision form";
+  else if (a.k_sponge != b.k_sponge || a.newt_cool_on != b.newt_cool_on || a.drag_v != b.drag_v ||
+           a.drag_zonal_avg != b.drag_zonal_avg || a.lat0 != b.lat0)
+    *why = "physics options";
+  else if ((a.nudiv == 0.) != (b.nudiv == 0.)) *why = "divergence damping on/off";
+  else if (tensor_filter(a) != tensor_filter(b)) *why = "zonal filter path (ni a multiple of 128 or not)";
+  else
+    for (int i = 0; i < 9; i++)
+      if ((a.nu[i] > 0.) != (b.nu[i] > 0.)) *why = "hyperviscosity orders";
+  return *why == nullptr;
 }
 
 }  // namespace
@@ -782,8 +802,9 @@ extern "C" int epic_batch_create(epic_model *const *members, int32_t n, epic_bat
   *out = nullptr;
   for (int i = 0; i < n; i++) {
     if (!members[i]) return set_error(EPIC_ERR_ARG, "epic_batch_create: member %d is NULL", i);
-    if (!same_launch_shape(members[0]->d, members[i]->d))
-      return set_error(EPIC_ERR_ARG, "epic_batch_create: member %d differs from member 0 in size, scheme, precision or viscosity", i);
+    const char *why = nullptr;
+    if (!batch_compatible(members[0]->d, members[i]->d, &why))
+      return set_error(EPIC_ERR_ARG, "epic_batch_create: member %d differs from member 0 in %s", i, why);
     for (int q = 0; q < i; q++)
       if (members[q] == members[i]) return set_error(EPIC_ERR_ARG, "epic_batch_create: member %d repeats member %d", i, q);
     // every kernel of the batch reads and writes each member's pool: all on one device
@@ -811,9 +832,24 @@ extern "C" int epic_batch_create(epic_model *const *members, int32_t n, epic_bat
     epic_batch_destroy(b);
     return set_error(EPIC_ERR_CUDA, "epic_batch_create: %s", cudaGetErrorString(e));
   }
-  b->d = members[0]->d;
-  b->d.batch = b->dev_members;
-  b->d.nbatch = n;
+  // the launch description: member 0's arrays (the kernels move pointer arguments to each
+  // member's) with the largest sizes, which every grid, shared-memory size and loop bound of a
+  // launch is computed from
+  DevModel &d = b->d;
+  d = members[0]->d;
+  d.reloc_n3 = d.n3;
+  for (int i = 1; i < n; i++) {
+    const DevModel &m = members[i]->d;
+    if (m.ni != members[0]->d.ni || m.nj != members[0]->d.nj) d.hetero = 1;
+    d.ni = std::max(d.ni, m.ni);
+    d.nj = std::max(d.nj, m.nj);
+    d.iadim = std::max(d.iadim, m.iadim);
+    d.jadim = std::max(d.jadim, m.jadim);
+    d.n2 = std::max(d.n2, m.n2);
+    d.n3 = std::max(d.n3, m.n3);
+  }
+  d.batch = b->dev_members;
+  d.nbatch = n;
   *out = b;
   return EPIC_OK;
 }

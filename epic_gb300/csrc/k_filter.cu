@@ -178,6 +178,7 @@ __global__ void k_filter_planes(DevModel M, const double *src, int src_sel, doub
   R *sm = reinterpret_cast<R *>(smraw);
   src += plane_offset(M, src_sel);
   const int j = (int)blockIdx.x - 1;
+  if (j > M.nj + 1) return;   // a member with fewer rows than the launch (batches of mixed sizes)
   const int k = k0 + (int)blockIdx.y;
   const long long base = M.at(k, j, 0);
   R *x = sm;
@@ -318,33 +319,46 @@ __global__ void k_varz_tables(DevModel M, const double *buff, int sel, int index
 }
 
 // The mixed forms' profile: var(gz) to binary64 accuracy as the knot value (binary64) plus the
-// cubic's increment from the knot (FP32 on the FP64 distance gz - x_knot), and the filtered
-// deviation added back to it in binary64 -- the field itself is never rounded to FP32 (a
-// rounding of THETA or HDRY on the filtered rows every step feeds the pressure gradient,
-// which amplifies it).  HDRY is interpolated in log space: knot value exp(y) times
-// 1 + expm1(increment).  The knot values and the cubics' FP32 coefficients are tabulated once per
-// row (varz_intervals_mixed); the interval is found in FP32 (next to a knot either neighbouring
-// cubic gives the same value to the cubic's accuracy), the distance from its knot in binary64.
-struct VarzInterval { float x, z0, c2, c3; };
+// cubic's increment from the knot, evaluated in double-float on the binary64 distance gz - x_knot
+// with the cubic's coefficients computed in binary64 and split into double-floats, and the
+// filtered deviation added back to it in binary64 -- the field itself is never rounded to FP32.
+// The profile has to be this accurate: out = var + F(buff - var) = buff - (I - F)(buff - var), so a
+// rounding error of the profile that varies from column to column (an FP32 increment's does)
+// passes the filter's high-wavenumber part (I - F) straight into THETA and HDRY on every filtered
+// row, every step; with FP32 increments that was the largest single source of the mixed form's
+// wind error after a simulated day (it halved the median member's U error to remove it).  HDRY is
+// interpolated in log space: knot value exp(y) times exp(increment).  The knot values and the
+// coefficients are tabulated once per row (varz_intervals_mixed); the interval is found in FP32
+// (next to a knot either neighbouring cubic gives the same value, the pieces joining with their
+// first derivative), the distance from its knot in binary64.
+struct VarzInterval {
+  float x, pad;
+  float2 z0, c2, c3;   // double-float coefficients of the cubic in the distance from the knot
+};
+__device__ __forceinline__ float2 split_df(double v) {
+  const float hi = d2f(v);
+  return make_float2(hi, d2f(v - f2d(hi)));
+}
 __device__ __forceinline__ void varz_intervals_mixed(const Trip *t, int n, int index, double *knot, VarzInterval *iv) {
   for (int q = threadIdx.x; q < n; q += blockDim.x) {
     knot[q] = index == 2 ? ::exp(t[q].y) : t[q].y;
     VarzInterval v;
     v.x = d2f(t[q].x);
-    v.z0 = d2f(t[q].z);
-    v.c2 = v.c3 = 0.f;
-    if (q + 1 < n) {
-      const float h = d2f(t[q + 1].x - t[q].x);
-      const float delta = d2f(t[q + 1].y - t[q].y) / h;
-      const float del1 = (v.z0 - delta) / h, del2 = (d2f(t[q + 1].z) - delta) / h;
-      v.c3 = (del1 + del2) / h;
-      v.c2 = -(del1 + del1 + del2);
+    v.pad = 0.f;
+    v.z0 = split_df(t[q].z);
+    v.c2 = v.c3 = make_float2(0.f, 0.f);
+    if (q + 1 < n) {   // splint_pchip's cubic, epic_funcs_util.c:926-946
+      const double h = t[q + 1].x - t[q].x;
+      const double delta = (t[q + 1].y - t[q].y) / h;
+      const double del1 = (t[q].z - delta) / h, del2 = (t[q + 1].z - delta) / h;
+      v.c3 = split_df((del1 + del2) / h);
+      v.c2 = split_df(-(del1 + del1 + del2));
     }
     iv[q] = v;
   }
 }
 __device__ __forceinline__ double varz_profile_mixed(const Trip *t, const double *knot, const VarzInterval *iv, int n, int index,
-                                                     double gzd) {
+                                                     double gzd, const float2 *exp2tab) {
   const float g = d2f(gzd);
   int kay;
   if (g <= iv[0].x) kay = 0;
@@ -360,9 +374,10 @@ __device__ __forceinline__ double varz_profile_mixed(const Trip *t, const double
   // a NaN argument fails every comparison: keep the interval index inside the table
   kay = kay < 0 ? 0 : (kay > n - 2 ? n - 2 : kay);
   const VarzInterval v = iv[kay];
-  const float xx = d2f(gzd - t[kay].x);
-  const float inc = xx * (v.z0 + xx * (v.c2 + xx * v.c3));
-  return index == 2 ? knot[kay] + knot[kay] * f2d(expm1f(inc)) : knot[kay] + f2d(inc);
+  const float2 xs = split_df(gzd - t[kay].x);
+  const dfl xx(xs.x, xs.y);
+  const dfl inc = xx * (dfl(v.z0.x, v.z0.y) + xx * (dfl(v.c2.x, v.c2.y) + xx * dfl(v.c3.x, v.c3.y)));
+  return index == 2 ? knot[kay] * to_d(exp_df(inc, exp2tab)) : knot[kay] + to_d(inc);
 }
 
 // The rest of the THREEDIM zonal_filter: subtract var(gz), filter, add it back.
@@ -374,6 +389,7 @@ __global__ void k_varz_filter_rows(DevModel M, double *buff, int sel, int index,
   buff += plane_offset(M, sel);
   const int jstart = index == 1 ? 1 : 0;
   const int j = jstart + (int)blockIdx.x;
+  if (j > M.nj) return;   // a member with fewer rows than the launch (batches of mixed sizes)
   const int k = kstart + (int)blockIdx.y;
   const int vgrid = index == 1;
   const Trip *t = reinterpret_cast<const Trip *>(M.ptable) + (long long)(j + 1) * (M.nk + 2);
@@ -400,7 +416,7 @@ __global__ void k_varz_filter_rows(DevModel M, double *buff, int sel, int index,
         case 2: gzd = .5 * (gz[M.at(k, j, i)] + gz[M.at(k - 1, j, i)]); break;
         default: gzd = gz[M.at(k, j, i)]; break;
       }
-      const double v = varz_profile_mixed(t, knot, iv, n, index, gzd);
+      const double v = varz_profile_mixed(t, knot, iv, n, index, gzd, M.exp2tab);
       vzd[i] = v;
       x[i] = d2f(buff[base + i] - v);
     }
@@ -461,6 +477,7 @@ __global__ void k_hsu_zonal(DevModel M, double *buff, int kind, int kstart) {
   R *sm = reinterpret_cast<R *>(smraw);
   const int ni = M.ni, W = ni + 2;
   const int j = (int)blockIdx.x;
+  if (j > M.nj) return;   // a member with fewer rows than the launch (batches of mixed sizes)
   const int k = kstart + (int)blockIdx.y;
   R *a = sm, *um = a + W, *up = um + W, *ff = up + W, *ap = ff + W, *d1 = ap + W, *d2 = d1 + W, *aa = d2 + W;
   FilterSmem<R> fs = carve_filter(aa + W, ni);
@@ -541,6 +558,7 @@ __global__ void k_akima_zonal(DevModel M, double *buff, int kind, int kstart) {
   R *sm = reinterpret_cast<R *>(smraw);
   const int ni = M.ni, W = ni + 2;
   const int j = (int)blockIdx.x;
+  if (j > M.nj) return;   // a member with fewer rows than the launch (batches of mixed sizes)
   const int k = kstart + (int)blockIdx.y;
   R *a = sm, *u2d = a + W, *da = u2d + W, *dl = da + W, *ff = dl + W;
   FilterSmem<R> fs = carve_filter(ff + W, ni);

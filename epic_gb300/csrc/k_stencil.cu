@@ -683,9 +683,11 @@ __global__ void k_akima_merid_update(DevModel M, double *A, int k0) {
 
 // d2dy2 of planes k0..k1 of src into dst (coefficients per row from the init block, :1049-1141).
 template <class R>
-__global__ void k_d2dy2(DevModel M, const double *src, int src_sel, double *dst, int vgrid, double diff_coef, int k0, int nkk,
+__global__ void k_d2dy2(DevModel M, const double *src, int src_sel, double *dst, int vgrid, int order, int k0, int nkk,
                         int of_state) {
   if (epic_member(M, src, dst)) return;
+  // the member's own coefficient (it depends on dt and dy0): order 2, 4, 6 or 8, constant indices
+  const double diff_coef = order == 2 ? M.coef[2] : (order == 4 ? M.coef[4] : (order == 6 ? M.coef[6] : M.coef[8]));
   Cell c;
   const int nrows = vgrid ? M.nj + 2 : M.nj + 1;   // v: j = 0..nj+1, h: j = 0..nj
   if (!cell3(M, k0, nkk, 0, nrows, c)) return;
@@ -715,9 +717,9 @@ __global__ void k_d2dy2(DevModel M, const double *src, int src_sel, double *dst,
 // there into dst.  Block = 32 columns of one layer k0 + blockIdx.y, every row; the values are
 // those of two k_d2dy2<float> launches (the intermediate is a float either way), without the
 // intermediate volume's write and read.
-__global__ void k_d2dy2_pair_mixed(DevModel M, const double *src, int src_sel, double *dst, int vgrid, double coef1, double coef2,
-                                   int k0) {
+__global__ void k_d2dy2_pair_mixed(DevModel M, const double *src, int src_sel, double *dst, int vgrid, int k0) {
   if (epic_member(M, src, dst)) return;
+  const double coef1 = M.coef[2], coef2 = M.coef[4];
   extern __shared__ __align__(16) unsigned char smraw[];
   float *d1 = reinterpret_cast<float *>(smraw);   // [row][lane]
   src += plane_offset(M, src_sel);
@@ -963,8 +965,9 @@ __global__ void k_ri2(DevModel M) {
 
 // divergence_damping apply step, epic_subgrid.c:1857-1881 (DIV from k_divergence in work2).
 template <class R>
-__global__ void k_divdamp_apply(DevModel M, double nudiv) {
+__global__ void k_divdamp_apply(DevModel M) {
   if (epic_member(M)) return;
+  const double nudiv = M.nudiv;
   const unsigned t = blockIdx.x * blockDim.x + threadIdx.x;
   const unsigned per = (unsigned)(M.nk - 1) * (unsigned)(M.nj + 1) * (unsigned)M.ni;
   if (t >= 2 * per) return;
@@ -1184,13 +1187,12 @@ int launch_meridional_hyperviscosity(const DevModel &M, int index, double *var, 
     if (pair && itmp == 2) {
       // the second pass's output goes where the unfused loop leaves it
       dst = bufs[1];
-      k_d2dy2_pair_mixed<<<zg(dim3((unsigned)((M.ni + 31) / 32), (unsigned)nkk), M), 256, pair_smem, s>>>(M, var, sel, dst, vgrid, M.coef[2],
-                                                                                                        M.coef[4], k0);
+      k_d2dy2_pair_mixed<<<zg(dim3((unsigned)((M.ni + 31) / 32), (unsigned)nkk), M), 256, pair_smem, s>>>(M, var, sel, dst, vgrid, k0);
       itmp = 4;
       which = 1;
       sign = -sign;
     } else {
-      EPIC_LAUNCH_R(M.mixed, k_d2dy2, cells_blocks(M, nkk, nrows, TB(M, TB_VISC)), TB(M, TB_VISC), 0, s, M, cur_src, src_sel, dst, vgrid, M.coef[itmp], k0,
+      EPIC_LAUNCH_R(M.mixed, k_d2dy2, cells_blocks(M, nkk, nrows, TB(M, TB_VISC)), TB(M, TB_VISC), 0, s, M, cur_src, src_sel, dst, vgrid, itmp, k0,
                     nkk, cur_src == var);
     }
     src_sel = PL_NONE;
@@ -1227,7 +1229,7 @@ int launch_divergence_damping(const DevModel &M, cudaStream_t s) {
   if (M.nudiv == 0.) return 0;
   launch_filter_planes(M, M.u, PL_UV_DIS, M.work1, 1, M.nk - 1, 0, s, M.mixed);
   EPIC_LAUNCH_R(M.mixed, k_divergence, cells_blocks(M, M.nk - 1, M.nj + 1, TB(M, TB_DIAG)), TB(M, TB_DIAG), 0, s, M, M.work1, M.v, PL_UV_DIS, M.work2, 1, M.nk - 1);
-  EPIC_LAUNCH_R(M.mixed, k_divdamp_apply, epic_blocks(2LL * (M.nk - 1) * (M.nj + 1) * M.ni, TB(M, TB_UPDATE)), TB(M, TB_UPDATE), 0, s, M, M.nudiv);
+  EPIC_LAUNCH_R(M.mixed, k_divdamp_apply, epic_blocks(2LL * (M.nk - 1) * (M.nj + 1) * M.ni, TB(M, TB_UPDATE)), TB(M, TB_UPDATE), 0, s, M);
   return 0;
 }
 

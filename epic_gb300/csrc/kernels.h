@@ -66,13 +66,15 @@ int launch_calc_w(const DevModel &M, cudaStream_t s);
 int launch_uv_drag(const DevModel &M, cudaStream_t s);
 int launch_hsu_vertical(const DevModel &M, double *buff, int kind, cudaStream_t s);
 int launch_restore_mass(const DevModel &M, cudaStream_t s);
-// feeds_pgrad: the call whose P2, THETA, GZ3 and RHO3 the pressure gradient reads (the mixed
-// form takes its double-float kernels there).  feeds_pgrad = false marks the calls inside
-// advection (set_p2etc) and before the filtered-GZ copy (store_pgrad_vars): the mixed forms
-// write only what is read before stages 11 and 19 recompute the rest -- P3 and HDRY, and GZ3
-// (with its monotonicity check); the FP64 form writes everything, as the reference does.
-int launch_set_p2etc(const DevModel &M, int update_theta, cudaStream_t s, bool feeds_pgrad = true);
-int launch_store_pgrad_vars(const DevModel &M, cudaStream_t s, bool feeds_pgrad = true);
+// accurate: EPIC_PREC_MIXED takes its double-float kernels (every call of its step does: the
+// calls before the pressure gradient, and those inside advection and before the filtered-GZ
+// copy, whose GZ3 places the 3-D filter's profiles).  accurate = false in a mixed form runs the
+// FP32 kernels, which write only what is read before stages 11 and 19 recompute the rest -- P3
+// and HDRY, and GZ3 (with its monotonicity check); EPIC_PREC_MIXED_FAST takes them inside
+// advection and before the filtered-GZ copy.  The FP64 form writes everything, as the reference
+// does.
+int launch_set_p2etc(const DevModel &M, int update_theta, cudaStream_t s, bool accurate = true);
+int launch_store_pgrad_vars(const DevModel &M, cudaStream_t s, bool accurate = true);
 int launch_gz_monotone(const DevModel &M, cudaStream_t s);
 int launch_calc_heating(const DevModel &M, cudaStream_t s);
 int launch_advection_prep(const DevModel &M, int phase, cudaStream_t s);

@@ -7,10 +7,11 @@ steps).  The server
   * admits waiting requests, in arrival order with backfill, while the device bytes of the
     admitted runs (epic_model_bytes) stay within its HBM budget;
   * keeps every admitted run's state on the device from admission to completion;
-  * groups the active runs by shape class (sizes, scheme, precision form and time step) and
-    advances each class as one Batch: every kernel of a step is launched once for all of the
-    class's runs, and the classes' batches run on their own streams, so their work overlaps
-    on the device;
+  * groups the active runs by launch class -- what the runs of one Batch must share: layers,
+    schemes, precision form, viscosity orders, and in the mixed forms the zonal filter's path;
+    grid sizes and time steps may differ -- and advances each class as one Batch: every kernel
+    of a step is launched once for all of the class's runs, uneven sizes included, and the
+    classes' batches run on their own streams, so their work overlaps on the device;
   * never waits on one class while another could be launched: each pass polls every class's
     batch (epic_batch_query), settles the ones that finished and relaunches them at once;
   * re-forms a class's batch whenever a run joins or leaves it (continuous batching: runs that
@@ -31,7 +32,7 @@ from dataclasses import dataclass, field
 
 import numpy as np
 
-from . import (Batch, EPIC_PREC_MIXED, EPIC_PROFILE_N2, EPIC_SYNC_DIAGS_ONLY, EpicError, Fields, HSConfig, Model, hs_setup,
+from . import (Batch, EPIC_PREC_FP64, EPIC_PREC_MIXED, EPIC_PROFILE_N2, EPIC_SYNC_DIAGS_ONLY, EpicError, Fields, HSConfig, Model, hs_setup,
                model_bytes)
 
 
@@ -70,10 +71,13 @@ class _Active:
     admitted: float
 
 
-def _shape_class(cfg: HSConfig, precision: int) -> tuple:
-    # the sounding fixes the vertical grid (sigmatheta), so it is part of the class
-    return (cfg.ni, cfg.nj, cfg.nk, cfg.dt, cfg.uv_scheme, cfg.advection_scheme, precision, cfg.nu4, cfg.nu6, cfg.nu8,
-            cfg.nudiv, cfg.lat0, cfg.profile, cfg.n2, cfg.theta_surface, cfg.t_iso)
+def launch_class(cfg: HSConfig, k_sigma: int, precision: int) -> tuple:
+    """What the members of one Batch must share (epic_batch_create): layers and the pure-sigma
+    split, schemes, precision form, which viscosity orders and whether divergence damping act,
+    the filter latitude, and in the mixed forms whether ni takes the tensor-core filter."""
+    tensor_filter = precision != EPIC_PREC_FP64 and cfg.ni % 128 == 0 and cfg.ni <= 1024
+    return (cfg.nk, k_sigma, cfg.uv_scheme, cfg.advection_scheme, precision, tensor_filter, cfg.nu4 > 0, cfg.nu6 > 0,
+            cfg.nu8 > 0, cfg.nudiv != 0, cfg.lat0)
 
 
 def state_checksum(f: Fields) -> float:
@@ -124,9 +128,9 @@ class RunServer:
     backend: object = field(default_factory=DeviceBackend)
     waiting: list = field(default_factory=list)
     prepared: dict = field(default_factory=dict)    # rid -> (grid, initial fields, device bytes)
-    active: dict = field(default_factory=dict)      # shape class -> list[_Active]
-    batches: dict = field(default_factory=dict)     # shape class -> (Batch, member ids)
-    inflight: dict = field(default_factory=dict)    # shape class -> (Batch, steps, members) running
+    active: dict = field(default_factory=dict)      # launch class -> list[_Active]
+    batches: dict = field(default_factory=dict)     # launch class -> (Batch, member ids)
+    inflight: dict = field(default_factory=dict)    # launch class -> (Batch, steps, members) running
     results: list = field(default_factory=list)
     used: int = 0
     peak_used: int = 0
@@ -159,13 +163,13 @@ class RunServer:
             del self.prepared[req.rid]
             self.used += need
             self.peak_used = max(self.peak_used, self.used)
-            cls = _shape_class(req.cfg, self.precision)
+            cls = launch_class(req.cfg, getattr(ga.struct, "k_sigma", req.cfg.nk), self.precision)
             self.active.setdefault(cls, []).append(_Active(req, m, need, req.steps, self.now()))
         self.waiting = keep
 
     # -- one scheduling pass ----------------------------------------------------------------
     def round(self) -> bool:
-        """Advance every shape class that is idle; a class whose batch is still running is left
+        """Advance every launch class that is idle; a class whose batch is still running is left
         alone, so classes of different sizes never wait for one another.  Returns whether any
         class was handled."""
         progressed = False

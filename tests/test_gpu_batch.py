@@ -42,17 +42,90 @@ def test_batch_equals_members_alone(gpu, precision, scheme, adv):
     assert batch.kernels_per_step > 0
 
 
-def test_batch_rejects_mixed_shapes(gpu):
+def test_batch_rejects_incompatible_members(gpu):
+    """Members must share the layers, the precision form and, in the mixed forms, the zonal
+    filter's path (tensor cores for ni a multiple of 128); ni, nj and dt may differ."""
     _, _, a = _member(1, 1.0, EPIC_PREC_FP64)
-    _, _, b = _member(2, 1.0, EPIC_PREC_FP64, shape=(64, 32, 10))
+    _, _, b = _member(2, 1.0, EPIC_PREC_FP64, shape=(32, 16, 20))
     _, _, c = _member(3, 1.0, EPIC_PREC_MIXED)
     _, _, d = _member(4, 1.0, EPIC_PREC_MIXED_FAST)
-    with pytest.raises(EpicError, match="differs"):
+    _, _, e = _member(5, 1.0, EPIC_PREC_MIXED, shape=(128, 64, 10))
+    _, _, f = _member(6, 1.0, EPIC_PREC_FP64, shape=(64, 32, 10))
+    with pytest.raises(EpicError, match="layers"):
         Batch([a, b])
-    with pytest.raises(EpicError, match="differs"):
+    with pytest.raises(EpicError, match="precision"):
         Batch([a, c])
-    with pytest.raises(EpicError, match="differs"):
+    with pytest.raises(EpicError, match="precision"):
         Batch([c, d])
+    with pytest.raises(EpicError, match="filter path"):
+        Batch([c, e])
+    Batch([a, f]).close()   # sizes alone may differ
+
+
+# Batches whose members differ in ni, nj and dt: one launch per kernel for all of them, each
+# member's threads bounded by its own sizes, its pointers moved array by array.
+UNEVEN = {
+    "fp64": (EPIC_PREC_FP64, [(32, 16, 10, 300), (64, 32, 10, 300), (64, 48, 10, 150), (128, 64, 10, 150)]),
+    "mixed_fft": (EPIC_PREC_MIXED, [(32, 16, 10, 300), (64, 32, 10, 300), (64, 40, 10, 150)]),
+    "mixed_tensor": (EPIC_PREC_MIXED, [(128, 64, 20, 300), (256, 128, 20, 150), (128, 96, 20, 150)]),
+    "fast_tensor": (EPIC_PREC_MIXED_FAST, [(128, 64, 20, 300), (256, 128, 20, 150)]),
+}
+
+
+def _uneven_member(q, shape, precision, scheme=EPIC_UV_AB3):
+    ni, nj, nk, dt = shape
+    ga, f = hs_setup(HSConfig(ni=ni, nj=nj, nk=nk, dt=dt, seed=200 + q, uv_scheme=scheme))
+    ga.struct.hs_kf *= 1.0 + 0.03 * q
+    m = Model(ga, precision)
+    m.upload(f)
+    return ga, f, m
+
+
+@pytest.mark.parametrize("fused", [False, True], ids=["auto", "fused_march"])
+@pytest.mark.parametrize("case", sorted(UNEVEN))
+def test_uneven_batch_equals_members_alone(gpu, case, fused):
+    from epic_gb300 import TUNE_HSU_MERID_VARIANT
+    precision, shapes = UNEVEN[case]
+    members = [_uneven_member(q, sh, precision) for q, sh in enumerate(shapes)]
+    batch = Batch([m for _, _, m in members])
+    if fused:
+        table = [0] * (TUNE_HSU_MERID_VARIANT + 1)
+        table[TUNE_HSU_MERID_VARIANT] = 1
+        batch.set_tuning(table)
+    batch.timestep(EPIC_SYNC_DIAGS_ONLY)
+    batch.run(5)
+    batch.sync()
+    for q, (ga, f, m) in enumerate(members):
+        alone = Model(ga, precision)
+        alone.upload(f)
+        alone.timestep(EPIC_SYNC_DIAGS_ONLY)
+        alone.run(5)
+        alone.sync()
+        a, b = m.download(), alone.download()
+        for k in a.arrays:
+            assert np.array_equal(a.arrays[k], b.arrays[k]), (shapes[q], k)
+        assert (a.struct.itime, a.struct.it_zero, a.struct.model_time) == (b.struct.itime, b.struct.it_zero, b.struct.model_time)
+
+
+def test_uneven_batch_leapfrog_and_pipeline(gpu):
+    """Leapfrog members of three sizes through the pipelined end-to-end step (sub-batches of
+    uneven members on their own streams)."""
+    shapes = [(32, 16, 10, 300), (64, 32, 10, 300), (64, 24, 10, 150)]
+    members = [_uneven_member(q, sh, EPIC_PREC_MIXED, EPIC_UV_LEAPFROG) for q, sh in enumerate(shapes)]
+    b = Batch([m for _, _, m in members])
+    b.timestep(EPIC_SYNC_DIAGS_ONLY)
+    b.sync()
+    hosts = [m.download().copy(pinned=True) for _, _, m in members]
+    b.step_host(hosts, 3, groups=2)
+    for (ga, f, _), h in zip(members, hosts):
+        alone = Model(ga, EPIC_PREC_MIXED)
+        alone.upload(f)
+        alone.timestep(EPIC_SYNC_DIAGS_ONLY)
+        alone.run(3)
+        alone.sync()
+        w = alone.download()
+        for k in w.arrays:
+            assert np.array_equal(h.arrays[k], w.arrays[k]), k
 
 
 def test_autotuned_shapes_change_no_result(gpu):

@@ -96,9 +96,10 @@ def test_budget_backfill_classes_and_step_counts(lag):
     # every run stepped exactly its count, and its model was released
     assert sorted(m.steps for m in be.models) == sorted(q.steps for q in reqs)
     assert all(m.closed for m in be.models)
-    # a batch never mixes shapes; the two small runs were admitted beside the first big one
-    assert all(len(shapes) == 1 for _, shapes, _ in be.log)
-    assert any(n == 2 and shapes == {small} for n, shapes, _ in be.log)
+    # a batch never mixes layer counts (a launch class); the two small runs were admitted beside
+    # the first big one and share its class, so they are batched with it
+    assert all(len({nk for _, _, nk in shapes}) == 1 for _, shapes, _ in be.log)
+    assert any(n == 3 and shapes == {small, big} for n, shapes, _ in be.log)
     assert all(n <= 4 for _, _, n in be.log)
     s = latency_summary(res)
     assert s["requests"] == 5 and s["p99_s"] >= s["p50_s"]
