@@ -102,27 +102,29 @@ struct DevModel {
   __host__ __device__ __forceinline__ int at2(int j, int i) const { return i + (j + 1) * iadim; }
 };
 
-// The 3-D arrays a kernel argument can point into, with their plane counts.
-#define EPIC_FIELD_LIST(X)                                                                         \
-  X(u, from.nvp) X(v, from.nvp) X(dudt, from.ntp) X(dvdt, from.ntp) X(hdry, 1) X(theta, 1) X(p3, 1)  \
-  X(h3, 1) X(p2, 1) X(theta2, 1) X(t2, 1) X(t3, 1) X(rho2, 1) X(rho3, 1) X(exner3, 1) X(gz3, 1)      \
-  X(mont3, 1) X(heat3, 1) X(pv3, 1) X(ri2, 1) X(div_uv3, 1) X(w3, 1) X(dzdt3, 1) X(u_spinup, 1)      \
-  X(gz, 1) X(unity, 1) X(old, 1) X(work0, 1) X(work1, 1) X(work2, 1) X(work3, 1)
-
-// A pointer into one of member 0's arrays (plane q, offset o within the plane), moved to the
-// same plane of the same array of member `to`.  Members of different sizes have different pool
-// layouts, so the array is found by address; a pointer outside every array is returned as is.
+// A pointer into member 0's arrays, moved to the same place in member `to`'s arrays.  The pool of
+// a model (epic_model_create) packs the state arrays back to back as planes of n3 values (u and v
+// value planes, the tendency planes, then the single fields), and carves the scratch volumes gz,
+// unity, old, work0..3 one after another, each rounded up to 256 bytes; so the plane (or volume)
+// index and the offset inside it follow from the address by integer arithmetic, and map to the
+// member's pool with its own n3.  A pointer outside both regions (a table) is returned as is.
+__host__ __device__ __forceinline__ long long scratch_stride(long long n3) { return ((n3 * 8 + 255) / 256) * 256; }
 template <class P>
 __device__ __forceinline__ P *relocate_field(const DevModel &from, const DevModel &to, P *p) {
-  const double *d = reinterpret_cast<const double *>(p);
+  const char *c = reinterpret_cast<const char *>(p);
   const long long n3 = from.reloc_n3;
-#define EPIC_RELOCATE(f, planes)                                              \
-  if (d >= from.f && d < from.f + (long long)(planes) * n3) {                 \
-    const long long o = d - from.f, q = o / n3;                               \
-    return reinterpret_cast<P *>(to.f + q * to.n3 + (o - q * n3));            \
+  const char *s0 = reinterpret_cast<const char *>(from.gz);
+  const long long st0 = scratch_stride(n3);
+  if (c >= s0 && c < s0 + 7 * st0) {
+    const long long o = c - s0, q = o / st0;
+    return reinterpret_cast<P *>(reinterpret_cast<char *>(to.gz) + q * scratch_stride(to.n3) + (o - q * st0));
   }
-  EPIC_FIELD_LIST(EPIC_RELOCATE)
-#undef EPIC_RELOCATE
+  const char *b0 = reinterpret_cast<const char *>(from.u);
+  const long long planes = 2LL * from.nvp + 2LL * from.ntp + 20;
+  if (c >= b0 && c < b0 + planes * n3 * 8) {
+    const long long o = (c - b0) / 8, q = o / n3;
+    return reinterpret_cast<P *>(to.u + q * to.n3 + (o - q * n3));
+  }
   return p;
 }
 

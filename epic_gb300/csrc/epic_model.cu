@@ -181,14 +181,14 @@ int run_stage_on(const DevModel &M, cudaStream_t s, int stage) {
       launch_restore_mass(M, s);
       // Its P2 is recomputed (stage 11) before the pressure gradient.  EPIC_PREC_MIXED runs the
       // double-float kernel here too: it writes the interfaces' logarithms that stage 7 reads.
-      launch_set_p2etc(M, 0, s, M.col64);
+      launch_set_p2etc(M, 0, s, true);
       break;
     }
     // GZ3 for the filtered copy (stage 8).  The copy places the 3-D filter's profiles (stages 9
     // and 10), which pass column-to-column rounding noise of GZ3 into the filtered fields, so
-    // EPIC_PREC_MIXED computes it with the double-float kernel of stage 19 (its FP32 one made
-    // the wind error after a day ~2x larger); EPIC_PREC_MIXED_FAST keeps the FP32 kernel.
-    case 7: launch_store_pgrad_vars(M, s, M.col64); break;
+    // EPIC_PREC_MIXED computes it in double-float like stage 19 (the FP32 kernel made the wind
+    // error after a day ~2x larger); EPIC_PREC_MIXED_FAST keeps the FP32 kernel.
+    case 7: launch_store_pgrad_vars(M, s, true); break;
     case 8:
       launch_copy_gz(M, s);
       // The 3-D filter's profiles interpolate in the filtered GZ: filtering GZ itself in FP32
@@ -222,7 +222,7 @@ int run_stage_on(const DevModel &M, cudaStream_t s, int stage) {
     case 16: launch_store_diag(M, s); break;
     case 17: launch_calc_heating(M, s); break;
     case 18: launch_set_p2etc(M, 0, s); break;
-    case 19: launch_store_pgrad_vars(M, s, true); break;   // after stage 11: what the pressure gradient reads
+    case 19: launch_store_pgrad_vars(M, s); break;   // after stage 11: what the pressure gradient reads
     default: return set_error(EPIC_ERR_ARG, "unknown stage %d", stage);
   }
   return check_launch("stage launch");
@@ -439,6 +439,13 @@ extern "C" int epic_model_create(const epic_grid *g, int32_t precision, epic_mod
   if ((size_t)(p - m->pool) > bytes) {
     epic_model_destroy(m);
     return set_error(EPIC_ERR_NOMEM, "internal pool layout overflow");
+  }
+  // the layout relocate_field (batches of mixed sizes) relies on: packed state planes, then the
+  // seven scratch volumes at one stride
+  if ((const char *)d.u_spinup - (const char *)d.u != (long long)(2 * d.nvp + 2 * d.ntp + 19) * d.n3 * 8 ||
+      (const char *)d.work3 - (const char *)d.gz != 6 * epic::scratch_stride(d.n3)) {
+    epic_model_destroy(m);
+    return set_error(EPIC_ERR_STATE, "internal pool layout differs from the batch relocation's");
   }
   auto up = [&](double *dst, const double *src, size_t n) {
     return cudaMemcpyAsync(dst, src, n * sizeof(double), cudaMemcpyHostToDevice, m->stream);

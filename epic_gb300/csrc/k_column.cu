@@ -994,15 +994,16 @@ int launch_restore_mass(const DevModel &M, cudaStream_t s) {
   k_restore_mass<<<zg(epic_blocks((long long)M.nk * (M.nj + 1) * (M.ni + 2), TB(M, TB_POINT)), M), TB(M, TB_POINT), 0, s>>>(M);
   return 0;
 }
-int launch_set_p2etc(const DevModel &M, int update_theta, cudaStream_t s, bool accurate) {
-  if (M.col64 && accurate) k_set_p2etc_acc<<<zg(ntile_blocks(M), M), CT_THREADS, tile_smem(M, 4), s>>>(M, update_theta);
-  else if (M.mixed) k_set_p2etc_mixed<<<zg(ntile_blocks(M), M), CT_THREADS, tile_smem(M, 3), s>>>(M, update_theta, accurate);
+int launch_set_p2etc(const DevModel &M, int update_theta, cudaStream_t s, bool early) {
+  if (M.col64) k_set_p2etc_acc<<<zg(ntile_blocks(M), M), CT_THREADS, tile_smem(M, 4), s>>>(M, update_theta, !early);
+  else if (M.mixed) k_set_p2etc_mixed<<<zg(ntile_blocks(M), M), CT_THREADS, tile_smem(M, 3), s>>>(M, update_theta, !early);
   else k_set_p2etc<<<zg(ntile_blocks(M), M), CT_THREADS, tile_smem(M, 4), s>>>(M, update_theta);
   return 0;
 }
-int launch_store_pgrad_vars(const DevModel &M, cudaStream_t s, bool accurate) {
-  if (M.mixed && !accurate) {   // GZ3 alone: no DZDT3, so no horizontal part either
-    k_pgrad_vars_column_mixed<false><<<zg(ntile_blocks(M), M), CT_THREADS, tile_smem(M, 5), s>>>(M);
+int launch_store_pgrad_vars(const DevModel &M, cudaStream_t s, bool early) {
+  if (M.mixed && early) {   // GZ3 alone: no DZDT3, so no horizontal part either
+    if (M.col64) k_gz3_column_acc<<<zg(ntile_blocks(M), M), CT_THREADS, tile_smem(M, 5), s>>>(M);
+    else k_pgrad_vars_column_mixed<false><<<zg(ntile_blocks(M), M), CT_THREADS, tile_smem(M, 5), s>>>(M);
     return 0;
   }
   if (M.col64) k_pgrad_vars_column_acc<<<zg(ntile_blocks(M), M), CT_THREADS, tile_smem(M, 5), s>>>(M);

@@ -47,7 +47,9 @@ __device__ __forceinline__ double theta_acc(const DevModel &M, double sg, dfl si
 
 }  // namespace
 
-__global__ void __launch_bounds__(CT_THREADS, 3) k_set_p2etc_acc(DevModel M, int update_theta) {
+// layers = 0: only P3, HDRY and the interfaces' logarithms (lp3) -- the call inside advection,
+// whose P2, H3 and THETA2 stage 11 recomputes before anything reads them.
+__global__ void __launch_bounds__(CT_THREADS, 3) k_set_p2etc_acc(DevModel M, int update_theta, int layers) {
   if (epic_member(M)) return;
   extern __shared__ double sm[];
   const ColTile c = col_tile(M);
@@ -121,6 +123,7 @@ __global__ void __launch_bounds__(CT_THREADS, 3) k_set_p2etc_acc(DevModel M, int
     }
   }
   __syncthreads();
+  if (!layers) return;
   for (int k = 1 + c.warp; k <= nk; k += CT_WARPS) {
     const long long x = c.base + k * n2;
     const double top = CT(P, k - 1), bot = CT(P, k);
@@ -167,8 +170,10 @@ __global__ void __launch_bounds__(CT_THREADS, 3) k_set_p2etc_acc(DevModel M, int
   }
 }
 
-__global__ void __launch_bounds__(CT_THREADS, 3) k_pgrad_vars_column_acc(DevModel M) {
-  if (epic_member(M)) return;
+// FULL = false: GZ3 alone (with its monotonicity check) -- the call before the filtered-GZ
+// copy, whose other outputs the call after stage 11 rewrites before anything reads them.
+template <bool FULL>
+__device__ __forceinline__ void pgrad_vars_column_acc(DevModel &M) {
   extern __shared__ double sm[];
   __shared__ double s_rho2_1[32];
   const ColTile c = col_tile(M);
@@ -187,15 +192,16 @@ __global__ void __launch_bounds__(CT_THREADS, 3) k_pgrad_vars_column_acc(DevMode
     const dfl pi = exp_df(kap * (dfl(lpk.x, lpk.y) - lp0), tab);   // (p/p0)^kappa
     CT(LP, k) = lpk;
     const dfl t3 = cv<dfl>(theta) * pi;
-    const double t3d = to_d(t3);
-    M.t3[x] = t3d;
-    M.exner3[x] = f2d(cpf * pi.hi);
     const double rho = to_d(Pk * mu_over_r / t3);
-    M.rho3[x] = rho;
+    if (FULL) {
+      M.t3[x] = to_d(t3);
+      M.exner3[x] = f2d(cpf * pi.hi);
+      M.rho3[x] = rho;
+    }
     CT(P, k) = p;
     CT(R, k) = rho;
     CT(T3, k) = make_float2(t3.hi, t3.lo);
-    if (k >= 1) {   // the layer's T2, RHO2: read by the Richardson number only
+    if (FULL && k >= 1) {   // the layer's T2, RHO2: read by the Richardson number only
       const float t2f = d2f(th2) * powf(d2f(pr) * p0_inv.hi, kap.hi);
       M.t2[x] = f2d(t2f);
       const double r2 = f2d(d2f(pr) * mu_over_r.hi / t2f);
@@ -209,7 +215,9 @@ __global__ void __launch_bounds__(CT_THREADS, 3) k_pgrad_vars_column_acc(DevMode
 #pragma unroll
     for (int r = 0; r < TILE_SLOTS; r++) {
       const long long x = c.base + min(c.warp + r * CT_WARPS, nk) * n2;
-      v[r][0] = __ldg(M.theta + x); v[r][1] = __ldg(M.p3 + x); v[r][2] = __ldg(M.p2 + x); v[r][3] = __ldg(M.theta2 + x);
+      v[r][0] = __ldg(M.theta + x); v[r][1] = __ldg(M.p3 + x);
+      v[r][2] = FULL ? __ldg(M.p2 + x) : 0.;
+      v[r][3] = FULL ? __ldg(M.theta2 + x) : 0.;
       vl[r] = M.lp3[x];
     }
 #pragma unroll
@@ -217,11 +225,11 @@ __global__ void __launch_bounds__(CT_THREADS, 3) k_pgrad_vars_column_acc(DevMode
       if (c.warp + r * CT_WARPS <= nk) level(c.warp + r * CT_WARPS, v[r][0], v[r][1], v[r][2], v[r][3], vl[r]);
     for (int k = c.warp + TILE_SLOTS * CT_WARPS; k <= nk; k += CT_WARPS) {
       const long long x = c.base + k * n2;
-      level(k, M.theta[x], M.p3[x], M.p2[x], M.theta2[x], M.lp3[x]);
+      level(k, M.theta[x], M.p3[x], FULL ? M.p2[x] : 0., FULL ? M.theta2[x] : 0., M.lp3[x]);
     }
   }
   __syncthreads();
-  if (c.valid && c.warp == CT_WARPS - 1) {
+  if (FULL && c.valid && c.warp == CT_WARPS - 1) {
     M.rho2[c.base] = CT(R, 0) * CT(R, 0) / s_rho2_1[c.lane];
     M.theta2[c.base] = M.sgth[0];
     M.t2[c.base] = f2d(CT(T3, 0).x) + f2d(CT(T3, 0).y);
@@ -263,15 +271,21 @@ __global__ void __launch_bounds__(CT_THREADS, 3) k_pgrad_vars_column_acc(DevMode
     const long long x = c.base + k * n2;
     const double gzk = CT(GZ, k);
     M.gz3[x] = gzk;
-    M.mont3[x] = f2d(d2f(gzk) + cprf * CT(T3, k).x * rgasf);
+    if (FULL) M.mont3[x] = f2d(d2f(gzk) + cprf * CT(T3, k).x * rgasf);
     if (interior && k >= 1) {
-      float dz = 0.f;
-      if (itime > 1) dz = d2f(old - gzk) * dtg_inv;
-      dz += d2f(w) * d2f(h) / d2f(CT(R, k));
-      M.dzdt3[x] = f2d(dz);
+      if (FULL) {
+        float dz = 0.f;
+        if (itime > 1) dz = d2f(old - gzk) * dtg_inv;
+        dz += d2f(w) * d2f(h) / d2f(CT(R, k));
+        M.dzdt3[x] = f2d(dz);
+      }
       if (gzk >= CT(GZ, k - 1)) flag_error(M.ctl, ERR_GZ_MONOTONE, k, c.j, c.i, gzk);
     }
   };
+  if (!FULL) {
+    for (int k = c.warp; k <= nk; k += CT_WARPS) level_out(k, 0., 0., 0.);
+    return;
+  }
   double v[TILE_SLOTS][3];   // the loads of this warp's first levels issued together
 #pragma unroll
   for (int r = 0; r < TILE_SLOTS; r++) {
@@ -287,10 +301,20 @@ __global__ void __launch_bounds__(CT_THREADS, 3) k_pgrad_vars_column_acc(DevMode
   }
 }
 
+__global__ void __launch_bounds__(CT_THREADS, 3) k_pgrad_vars_column_acc(DevModel M) {
+  if (epic_member(M)) return;
+  pgrad_vars_column_acc<true>(M);
+}
+__global__ void __launch_bounds__(CT_THREADS, 3) k_gz3_column_acc(DevModel M) {
+  if (epic_member(M)) return;
+  pgrad_vars_column_acc<false>(M);
+}
+
 int column_acc_kernels_init() {
   const int big = (int)(5 * 32 * (EPIC_MAX_NK + 1) * sizeof(double));
   if (cudaFuncSetAttribute(k_set_p2etc_acc, cudaFuncAttributeMaxDynamicSharedMemorySize, big) != cudaSuccess ||
-      cudaFuncSetAttribute(k_pgrad_vars_column_acc, cudaFuncAttributeMaxDynamicSharedMemorySize, big) != cudaSuccess)
+      cudaFuncSetAttribute(k_pgrad_vars_column_acc, cudaFuncAttributeMaxDynamicSharedMemorySize, big) != cudaSuccess ||
+      cudaFuncSetAttribute(k_gz3_column_acc, cudaFuncAttributeMaxDynamicSharedMemorySize, big) != cudaSuccess)
     return -1;
   return 0;
 }

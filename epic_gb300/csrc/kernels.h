@@ -53,8 +53,9 @@ int filter_gemm_init(int ni);
 
 // k_column_acc.cu -- set_p2etc and store_pgrad_vars (column part) of the mixed form, with the
 // quantities feeding the pressure gradient in double-float.
-__global__ void k_set_p2etc_acc(DevModel M, int update_theta);
+__global__ void k_set_p2etc_acc(DevModel M, int update_theta, int layers);
 __global__ void k_pgrad_vars_column_acc(DevModel M);
+__global__ void k_gz3_column_acc(DevModel M);   // GZ3 alone (the call before the filtered-GZ copy)
 int column_acc_kernels_init();
 void fill_filter_kernels(int ni, int nj, const double *hl_h, const double *hl_pv, long long iadim, float *fh, float *fv);
 size_t twiddle_doubles(int ni);
@@ -66,15 +67,14 @@ int launch_calc_w(const DevModel &M, cudaStream_t s);
 int launch_uv_drag(const DevModel &M, cudaStream_t s);
 int launch_hsu_vertical(const DevModel &M, double *buff, int kind, cudaStream_t s);
 int launch_restore_mass(const DevModel &M, cudaStream_t s);
-// accurate: EPIC_PREC_MIXED takes its double-float kernels (every call of its step does: the
-// calls before the pressure gradient, and those inside advection and before the filtered-GZ
-// copy, whose GZ3 places the 3-D filter's profiles).  accurate = false in a mixed form runs the
-// FP32 kernels, which write only what is read before stages 11 and 19 recompute the rest -- P3
-// and HDRY, and GZ3 (with its monotonicity check); EPIC_PREC_MIXED_FAST takes them inside
-// advection and before the filtered-GZ copy.  The FP64 form writes everything, as the reference
-// does.
-int launch_set_p2etc(const DevModel &M, int update_theta, cudaStream_t s, bool accurate = true);
-int launch_store_pgrad_vars(const DevModel &M, cudaStream_t s, bool accurate = true);
+// early: the calls inside advection (set_p2etc) and before the filtered-GZ copy
+// (store_pgrad_vars), whose outputs but P3, HDRY and GZ3 stage 11 and stage 19 rewrite before
+// anything reads them.  The mixed forms compute only those there (EPIC_PREC_MIXED with its
+// double-float kernels, which also leave the interfaces' logarithms for store_pgrad_vars:
+// GZ3 places the 3-D filter's profiles, so it needs their accuracy; EPIC_PREC_MIXED_FAST with
+// its FP32 ones).  The FP64 form writes everything in every call, as the reference does.
+int launch_set_p2etc(const DevModel &M, int update_theta, cudaStream_t s, bool early = false);
+int launch_store_pgrad_vars(const DevModel &M, cudaStream_t s, bool early = false);
 int launch_gz_monotone(const DevModel &M, cudaStream_t s);
 int launch_calc_heating(const DevModel &M, cudaStream_t s);
 int launch_advection_prep(const DevModel &M, int phase, cudaStream_t s);
