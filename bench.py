@@ -618,7 +618,7 @@ ROOF_STAGES = {
         "THETA, P3, P2, THETA2, GZ3, W3, H3 read and T3, EXNER3, RHO3, T2, RHO2, GZ3, MONT3, DZDT3 written by the "
         "column tile; U, V, GZ3, DZDT3 read and DZDT3 written by the horizontal part; bound by load latency and "
         "the FP64 hydrostatic sum, not by HBM"),
-    12: ("uv_pgrad_finite_volume (k_gz_pole_rows + k_pgrad_split + k_pgrad_lon + k_pgrad_lat) over all members", 7,
+    12: ("uv_pgrad_finite_volume (k_gz_pole_rows + k_pgrad_lon + k_pgrad_lat) over all members", 7,
          "GZ3, P2, RHO3 read and DUDT, DVDT read and written; stencils of 18-24 loads per cell from L1/L2 plus ~300 "
          "FP32/integer operations: issue- and latency-bound, not HBM-bound"),
 }

@@ -377,6 +377,15 @@ __device__ __forceinline__ void flag_error(Ctl *c, int code, int k, int j, int i
   }
 }
 
+// The mixed forms' pressure gradient reads GZ3 and P2 as (hi, lo) binary32 splits, hi = float(x),
+// lo = float(x - hi), kept in the scratch volumes work1 (GZ3) and work2 (P2) from the kernels that
+// write the two fields before it (store_pgrad_vars and set_p2etc of stages 19 and 11, and the
+// polar rows of GZ3 in uv_pgrad itself) to the pressure gradient.
+__device__ __forceinline__ void put_split(double *work, long long x, double v) {
+  const float hi = d2f(v);
+  reinterpret_cast<float2 *>(work)[x] = make_float2(hi, d2f(v - f2d(hi)));
+}
+
 // Zonal periodicity of one row: pads i = 0 and i = ni+1 (bc_lateral, src/single/s_epic_functions.c:55-59).
 // Called by the thread that owns interior cell i after it wrote the final value.
 __device__ __forceinline__ void write_with_pads(double *a, const DevModel &M, long long rowbase, int i, double val) {

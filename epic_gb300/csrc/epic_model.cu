@@ -156,8 +156,7 @@ int run_stage_on(const DevModel &M, cudaStream_t s, int stage) {
     case 4: launch_uv_drag(M, s); break;
     case 5:
       launch_meridional_hyperviscosity(M, 2, M.hdry, PL_NONE, s);
-      launch_zonal_hyperviscosity(M, 2, M.hdry, PL_NONE, s);
-      launch_restore_mass(M, s);
+      launch_zonal_hyperviscosity(M, 2, M.hdry, PL_NONE, s);   // then restore_mass, in the same kernel
       launch_meridional_hyperviscosity(M, 3, M.theta, PL_NONE, s);
       launch_zonal_hyperviscosity(M, 3, M.theta, PL_NONE, s);
       break;
@@ -177,8 +176,7 @@ int run_stage_on(const DevModel &M, cudaStream_t s, int stage) {
       launch_advection_prep(M, 2, s);
       vertical(M, M.hdry, 2, s);
       meridional(M, M.hdry, 2, s);
-      zonal(M, M.hdry, 1, 1, s);
-      launch_restore_mass(M, s);
+      zonal(M, M.hdry, 1, 1, s);   // then restore_mass, in the same kernel
       // Its P2 is recomputed (stage 11) before the pressure gradient.  EPIC_PREC_MIXED runs the
       // double-float kernel here too: it writes the interfaces' logarithms that stage 7 reads.
       launch_set_p2etc(M, 0, s, true);
@@ -205,8 +203,7 @@ int run_stage_on(const DevModel &M, cudaStream_t s, int stage) {
       launch_varz_filter(M, M.dvdt, PL_UV_TEND, 1, 1, M.nk, s);
       break;
     case 10:
-      launch_varz_filter(M, M.hdry, PL_NONE, 2, 1, M.nk, s);
-      launch_restore_mass(M, s);
+      launch_varz_filter(M, M.hdry, PL_NONE, 2, 1, M.nk, s);   // then restore_mass, in the same kernel
       launch_varz_filter(M, M.theta, PL_NONE, 3, M.k_sigma - 1, M.nk, s);
       break;
     case 11: launch_set_p2etc(M, 1, s); break;
@@ -222,6 +219,7 @@ int run_stage_on(const DevModel &M, cudaStream_t s, int stage) {
     case 16: launch_store_diag(M, s); break;
     case 17: launch_calc_heating(M, s); break;
     case 18: launch_set_p2etc(M, 0, s); break;
+    case 20: launch_calc_w(M, s, true); break;   // stages 1 and 2 in one pass over the columns
     case 19: launch_store_pgrad_vars(M, s); break;   // after stage 11: what the pressure gradient reads
     default: return set_error(EPIC_ERR_ARG, "unknown stage %d", stage);
   }
@@ -231,7 +229,7 @@ int run_stage_on(const DevModel &M, cudaStream_t s, int stage) {
 int run_stage(epic_model *m, int stage) { return run_stage_on(m->d, m->stream, stage); }
 
 int enqueue_step_on(const DevModel &M, cudaStream_t s) {
-  static const int step[] = {0, 1, 2, 3, 4, 5, 6, 7, 8, 9, 10, 11, 19, 12, 13, 14, 15, 16, 17};
+  static const int step[] = {0, 20, 3, 4, 5, 6, 7, 8, 9, 10, 11, 19, 12, 13, 14, 15, 16, 17};
   for (int st : step) {
     int rc = run_stage_on(M, s, st);
     if (rc) return rc;
@@ -745,8 +743,7 @@ extern "C" int epic_model_filter_mass_noalloc(epic_model *m) {
     DevModel M = m->d;   // the model's description with only the table pointer replaced
     M.ptable = table;
     cudaStream_t s = m->stream;
-    epic::launch_varz_filter(M, M.hdry, epic::PL_NONE, 2, 1, M.nk, s);
-    epic::launch_restore_mass(M, s);
+    epic::launch_varz_filter(M, M.hdry, epic::PL_NONE, 2, 1, M.nk, s);   // with restore_mass
     epic::launch_varz_filter(M, M.theta, epic::PL_NONE, 3, M.k_sigma - 1, M.nk, s);
     rc = check_launch("epic_model_filter_mass_noalloc");
   }

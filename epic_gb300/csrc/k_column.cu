@@ -36,8 +36,10 @@ __global__ void k_source_sink(DevModel M) {
 // W (heating term), DF (dF/dp).
 // In the mixed form (R = float) the pointwise terms are FP32, SUM_DIV is accumulated in FP64, and
 // the dF/dp difference step is cbrt(FLT_EPSILON) relative instead of cbrt(DBL_EPSILON).
+// source_sink = 1: the step's source_sink (k_source_sink) first, in the same pass over the
+// columns: THETA(k >= k_sigma-1) += dt*HEAT3/EXNER3 in binary64, written back and then used.
 template <class R>
-__global__ void __launch_bounds__(CT_THREADS, 3) k_calc_w(DevModel M) {
+__global__ void __launch_bounds__(CT_THREADS, 3) k_calc_w(DevModel M, int source_sink) {
   if (epic_member(M)) return;
   extern __shared__ __align__(16) unsigned char smraw[];
   R *sm = reinterpret_cast<R *>(smraw);
@@ -50,6 +52,10 @@ __global__ void __launch_bounds__(CT_THREADS, 3) k_calc_w(DevModel M) {
   // that the pointwise pass reads before it overwrites them.  The loads of the first
   // TILE_SLOTS levels of each warp are issued together so that their latencies overlap.
   auto stage = [&](int k, double p3, double dv, double th, double ht, double ex) {
+    if (source_sink && k >= ks - 1) {   // epic_funcs_diag.c:4768-4778
+      th += M.dt * ht / ex;
+      M.theta[c.base + k * n2] = th;
+    }
     CT(P, k) = cv<R>(p3); CT(DV, k) = cv<R>(dv); CT(DS, k) = cv<R>(th); CT(W, k) = cv<R>(ht); CT(DF, k) = cv<R>(ex);
   };
   if (c.valid) {
@@ -689,7 +695,11 @@ __global__ void __launch_bounds__(CT_THREADS, 3) k_set_p2etc_mixed(DevModel M, i
     const double top = CT(P, k - 1), bot = CT(P, k);
     const double p2 = layer_p_mixed(M, top, bot);
     M.p2[x] = p2;
-    if (k == 1) M.p2[c.base] = top * top / p2;
+    put_split(M.work2, x, p2);
+    if (k == 1) {
+      M.p2[c.base] = top * top / p2;
+      put_split(M.work2, c.base, top * top / p2);
+    }
     double h;
     if (k == nk) h = CT(HL, nk);
     else {
@@ -842,6 +852,7 @@ __global__ void __launch_bounds__(CT_THREADS, 3) k_pgrad_vars_column_mixed(DevMo
     const long long x = c.base + k * n2;
     const double gzk = CT(GZ, k);
     M.gz3[x] = gzk;
+    put_split(M.work1, x, gzk);
     M.mont3[x] = f2d(d2f(gzk) + cprf * d2f(CT(T3, k)) * rgasf);   // GZ3 + return_enthalpy
     if (interior && k >= 1) {
       float dz = 0.f;
@@ -971,8 +982,8 @@ static inline unsigned ncol_blocks(const DevModel &M, int th) { return epic_bloc
 int launch_source_sink(const DevModel &M, cudaStream_t s) { k_source_sink<<<zg(ncol_blocks(M, TB(M, TB_COLUMN)), M), TB(M, TB_COLUMN), 0, s>>>(M); return 0; }
 static inline unsigned ntile_blocks(const DevModel &M) { return epic_blocks((long long)(M.nj + 1) * (M.ni + 2), 32); }
 static inline size_t tile_smem(const DevModel &M, int arrays) { return (size_t)arrays * 32 * (M.nk + 1) * sizeof(double); }
-int launch_calc_w(const DevModel &M, cudaStream_t s) {
-  EPIC_LAUNCH_R(M.mixed, k_calc_w, ntile_blocks(M), CT_THREADS, tile_smem(M, 6), s, M);
+int launch_calc_w(const DevModel &M, cudaStream_t s, bool with_source_sink) {
+  EPIC_LAUNCH_R(M.mixed, k_calc_w, ntile_blocks(M), CT_THREADS, tile_smem(M, 6), s, M, (int)with_source_sink);
   return 0;
 }
 int launch_uv_drag(const DevModel &M, cudaStream_t s) {

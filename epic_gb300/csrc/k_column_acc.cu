@@ -130,7 +130,11 @@ __global__ void __launch_bounds__(CT_THREADS, 3) k_set_p2etc_acc(DevModel M, int
     const float2 lt = CT(LPS, k - 1), lb = CT(LPS, k);
     const double p2 = layer_p_acc(M, top, bot, dfl(lt.x, lt.y) - dfl(lb.x, lb.y));
     M.p2[x] = p2;
-    if (k == 1) M.p2[c.base] = top * top / p2;
+    put_split(M.work2, x, p2);
+    if (k == 1) {
+      M.p2[c.base] = top * top / p2;
+      put_split(M.work2, c.base, top * top / p2);
+    }
     double h;
     if (k == nk) h = CT(HL, nk);
     else {
@@ -271,7 +275,10 @@ __device__ __forceinline__ void pgrad_vars_column_acc(DevModel &M) {
     const long long x = c.base + k * n2;
     const double gzk = CT(GZ, k);
     M.gz3[x] = gzk;
-    if (FULL) M.mont3[x] = f2d(d2f(gzk) + cprf * CT(T3, k).x * rgasf);
+    if (FULL) {
+      put_split(M.work1, x, gzk);
+      M.mont3[x] = f2d(d2f(gzk) + cprf * CT(T3, k).x * rgasf);
+    }
     if (interior && k >= 1) {
       if (FULL) {
         float dz = 0.f;

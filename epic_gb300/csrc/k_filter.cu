@@ -202,27 +202,6 @@ __global__ void k_filter_planes(DevModel M, const double *src, int src_sel, doub
   for (int i = threadIdx.x + 1; i <= M.ni; i += blockDim.x) write_with_pads(dst, M, base, i, x[i]);
 }
 
-// The rows the tensor-core filter leaves alone (k_filter_planes_gemm filters the others): copied
-// when dst is not src, periodic pads on rows 0..nj+1.  One warp per (row, plane).
-__global__ void k_filter_rows_unfiltered(DevModel M, const double *src, int src_sel, double *dst, int k0, int nplanes, int vgrid) {
-  if (epic_member(M, src, dst)) return;
-  src += plane_offset(M, src_sel);
-  const int lane = (int)(threadIdx.x & 31);
-  const int w = (int)((blockIdx.x * blockDim.x + threadIdx.x) >> 5);
-  const int rows = M.nj + 3;
-  if (w >= rows * nplanes) return;
-  const int j = w % rows - 1, k = k0 + w / rows;
-  const bool valid = vgrid ? (j >= 1 && j <= M.nj) : (j >= 0 && j <= M.nj);
-  if (valid && row_is_filtered(M, j, vgrid)) return;
-  const int base = M.at(k, j, 0);
-  if (src != dst)
-    for (int i = lane; i <= M.ni + 1; i += 32) dst[base + i] = src[base + i];
-  __syncwarp();
-  if (j >= 0 && lane == 0) {
-    dst[base] = dst[base + M.ni];
-    dst[base + M.ni + 1] = dst[base + 1];
-  }
-}
 
 // Per-latitude var(gz) profile at the column of lowest bottom GZ, the first half of the
 // THREEDIM branch of zonal_filter (epic_adjust.c:266-395).  One warp per row j: the lanes find
@@ -422,7 +401,12 @@ __global__ void k_varz_filter_rows(DevModel M, double *buff, int sel, int index,
     }
     __syncthreads();
     filter_row_smem(M, x, vgrid ? M.high_lat_pv : M.high_lat_h, M.at2(j, 0), fs);
-    for (int i = threadIdx.x + 1; i <= M.ni; i += blockDim.x) write_with_pads(buff, M, base, i, f2d(x[i]) + vzd[i]);
+    // HDRY (index 2): restore_mass, which timestep() calls next (epic_timestep.c:212), on the
+    // filtered value; unfiltered rows are untouched here and already restored
+    for (int i = threadIdx.x + 1; i <= M.ni; i += blockDim.x) {
+      const double v = f2d(x[i]) + vzd[i];
+      write_with_pads(buff, M, base, i, index == 2 ? dmaxr(M.h_min[k], v) : v);
+    }
     return;
   }
   R *sm = reinterpret_cast<R *>(smraw);
@@ -464,7 +448,10 @@ __global__ void k_varz_filter_rows(DevModel M, double *buff, int sel, int index,
   }
   __syncthreads();
   if (filt) filter_row_smem(M, x, vgrid ? M.high_lat_pv : M.high_lat_h, M.at2(j, 0), fs);
-  for (int i = threadIdx.x + 1; i <= M.ni; i += blockDim.x) write_with_pads(buff, M, base, i, to_d(x[i]) + to_d(vz[i]));
+  for (int i = threadIdx.x + 1; i <= M.ni; i += blockDim.x) {   // HDRY (index 2): restore_mass too
+    const double v = to_d(x[i]) + to_d(vz[i]);
+    write_with_pads(buff, M, base, i, index == 2 ? dmaxr(M.h_min[k], v) : v);
+  }
 }
 
 // Zonal pass of hsu_advection (epic_flux.c:1316-1484) for one row: the fluxes come from a
@@ -543,8 +530,11 @@ __global__ void k_hsu_zonal(DevModel M, double *buff, int kind, int kstart) {
   __syncthreads();
   if (threadIdx.x == 0) { ff[0] = ff[ni]; ff[ni + 1] = ff[1]; }
   __syncthreads();
+  // HDRY (kind 1): restore_mass (epic_adjust.c:45-96), which advection() calls next
+  // (epic_flux.c:623), on the new value -- the same max per cell, one pass fewer
   for (int i = threadIdx.x + 1; i <= ni; i += blockDim.x) {
-    write_with_pads(buff, M, base, i, buff[base + i] + to_d((ff[i] - ff[i + 1]) * mn1 * DT));
+    const double v = buff[base + i] + to_d((ff[i] - ff[i + 1]) * mn1 * DT);
+    write_with_pads(buff, M, base, i, kind == 1 ? dmaxr(M.h_min[k], v) : v);
   }
 }
 
@@ -597,8 +587,10 @@ __global__ void k_akima_zonal(DevModel M, double *buff, int kind, int kstart) {
   __syncthreads();
   if (threadIdx.x == 0) { ff[0] = ff[ni]; ff[ni + 1] = ff[1]; }
   __syncthreads();
-  for (int i = threadIdx.x + 1; i <= ni; i += blockDim.x)
-    write_with_pads(buff, M, base, i, buff[base + i] + to_d((ff[i] - ff[i + 1]) * mn1 * DT));
+  for (int i = threadIdx.x + 1; i <= ni; i += blockDim.x) {   // HDRY (kind 1): restore_mass too
+    const double v = buff[base + i] + to_d((ff[i] - ff[i + 1]) * mn1 * DT);
+    write_with_pads(buff, M, base, i, kind == 1 ? dmaxr(M.h_min[k], v) : v);
+  }
 }
 
 // ---- launchers ----
@@ -612,11 +604,9 @@ int launch_filter_planes(const DevModel &M, const double *src, int src_sel, doub
   const size_t smem = ((size_t)(M.ni + 2) + filter_smem_elems(M.ni)) * relem(fp32);
   dim3 grid(M.nj + 3, nplanes);
   if (fp32 && filter_gemm_usable(M)) {
-    const long long warps = (long long)(M.nj + 3) * nplanes;
-    // in place with the pads already set, the rows left unfiltered need nothing
-    if (!(pads_set && src == dst && src_sel == PL_NONE))
-      k_filter_rows_unfiltered<<<zg(epic_blocks(32 * warps, 128), M), 128, 0, s>>>(M, src, src_sel, dst, k0, nplanes, vgrid);
-    return launch_filter_planes_gemm(M, src, src_sel, dst, k0, nplanes, vgrid, s, shift);
+    // the same launch copies the rows the operator leaves alone and sets their pads, except in
+    // place with the pads already set, where they need nothing
+    return launch_filter_planes_gemm(M, src, src_sel, dst, k0, nplanes, vgrid, s, shift, !(pads_set && src == dst && src_sel == PL_NONE));
   }
   EPIC_LAUNCH_R(fp32, k_filter_planes, grid, row_threads(M), smem, s, M, src, src_sel, dst, k0, vgrid);
   return 0;

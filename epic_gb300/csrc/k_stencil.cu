@@ -175,6 +175,10 @@ __global__ void k_gz_pole_rows(DevModel M) {
   for (int i = threadIdx.x; i <= M.ni + 1; i += blockDim.x) {
     M.gz3[M.at(k, -1, i)] = avg[0];
     M.gz3[M.at(k, M.nj + 1, i)] = avg[1];
+    if (M.mixed) {
+      put_split(M.work1, M.at(k, -1, i), avg[0]);
+      put_split(M.work1, M.at(k, M.nj + 1, i), avg[1]);
+    }
   }
 }
 
@@ -182,18 +186,10 @@ __global__ void k_gz_pole_rows(DevModel M) {
 // P2) of the stencil moves by one constant; the mixed form evaluates it in FP32 on
 // GZ3 - GZ3(k,j,i) and P2 - P2(k,j,i), which keeps the FP32 products near the size of the
 // differences the force is made of.  The differences are formed in FP32 from (hi, lo) splits of
-// GZ3 and P2 (hi = float(x), lo = float(x - hi); k_pgrad_split, in scratch work1 and work2) as
-// (hi_x - hi_ref) + (lo_x - lo_ref): within a rounding or two of the FP64 difference, with no
-// FP64 operation per stencil point.  The FP64 form uses the values as they are.
-__global__ void k_pgrad_split(DevModel M) {
-  if (epic_member(M)) return;
-  const long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
-  if (t >= M.n3) return;
-  const double z = M.gz3[t], p = M.p2[t];
-  const float zh = d2f(z), ph = d2f(p);
-  reinterpret_cast<float2 *>(M.work1)[t] = make_float2(zh, d2f(z - f2d(zh)));
-  reinterpret_cast<float2 *>(M.work2)[t] = make_float2(ph, d2f(p - f2d(ph)));
-}
+// GZ3 and P2 (put_split: hi = float(x), lo = float(x - hi), in scratch work1 and work2, written by
+// the kernels that computed the two fields) as (hi_x - hi_ref) + (lo_x - lo_ref): within a
+// rounding or two of the FP64 difference, with no FP64 operation per stencil point.  The FP64
+// form uses the values as they are.
 // Double-float (dfl, the accurate mixed form) takes the same splits and forms the differences in
 // double-float: the stencil's values then carry ~48 bits, and the face integrals' cancellation
 // costs no accuracy that matters.
@@ -766,7 +762,7 @@ __global__ void k_visc_apply(DevModel M, double *A, int sel, const double *D, in
 // per block.  The updated row stays in FP64 in both forms.  The FP64 form sums the row mean in
 // the reference's order on lane 0; the mixed form sums it in FP64 with a warp reduction.
 template <class R>
-__global__ void k_zonal_visc(DevModel M, double *A, int sel, int jbot, int jhalf, int k0) {
+__global__ void k_zonal_visc(DevModel M, double *A, int sel, int jbot, int jhalf, int k0, int restore) {
   if (epic_member(M, A)) return;
   extern __shared__ __align__(16) unsigned char smraw[];
   const int ni = M.ni, lane = (int)(threadIdx.x & 31), w = (int)(threadIdx.x >> 5), nw = (int)(blockDim.x >> 5);
@@ -838,8 +834,10 @@ __global__ void k_zonal_visc(DevModel M, double *A, int sel, int jbot, int jhalf
     __syncwarp();
   }
   __syncwarp();
-  if (any_applied)
-    for (int i = lane + 1; i <= ni; i += 32) write_with_pads(A, M, base, i, a[i]);
+  // restore (HDRY): restore_mass, which the hyperviscosity step calls next (epic_subgrid.c:240),
+  // on the new row -- the same max per cell, one pass fewer
+  if (any_applied || restore)
+    for (int i = lane + 1; i <= ni; i += 32) write_with_pads(A, M, base, i, restore ? dmaxr(M.h_min[k], a[i]) : a[i]);
 }
 
 // ---------------------------------------------------------------------------------------------
@@ -1112,7 +1110,6 @@ int launch_uv_pgrad(const DevModel &M, cudaStream_t s) {
     k_pgrad_lat<double><<<glat, TB(M, TB_PGRAD), 0, s>>>(M);
     return 0;
   }
-  k_pgrad_split<<<zg(epic_blocks(M.n3, TB(M, TB_POINT)), M), TB(M, TB_POINT), 0, s>>>(M);
   if (M.col64) {
     k_pgrad_lon<dfl><<<glon, TB(M, TB_PGRAD), 0, s>>>(M);
     k_pgrad_lat<dfl><<<glat, TB(M, TB_PGRAD), 0, s>>>(M);
@@ -1211,8 +1208,9 @@ int launch_meridional_hyperviscosity(const DevModel &M, int index, double *var, 
   return 0;
 }
 
+// index 2 (HDRY) applies restore_mass as well (in the kernel, or alone without hyperviscosity)
 int launch_zonal_hyperviscosity(const DevModel &M, int index, double *var, int sel, cudaStream_t s) {
-  if (M.ni < 2 || !(M.nu[4] + M.nu[6] + M.nu[8] > 0.)) return 0;
+  if (M.ni < 2 || !(M.nu[4] + M.nu[6] + M.nu[8] > 0.)) return index == 2 ? launch_restore_mass(M, s) : 0;
   int k0, k1;
   visc_krange(M, index, k0, k1);
   const int jbot = index == 1 ? 1 : 0, jhalf = index == 1 ? 0 : 1;
@@ -1221,7 +1219,7 @@ int launch_zonal_hyperviscosity(const DevModel &M, int index, double *var, int s
   rows = rows < 1 ? 1 : (rows > 4 ? 4 : rows);
   const int nrows = M.nj - jbot + 1;
   dim3 grid((nrows + rows - 1) / rows, k1 - k0 + 1);
-  EPIC_LAUNCH_R(M.mixed, k_zonal_visc, grid, 32 * rows, rows * row_bytes, s, M, var, sel, jbot, jhalf, k0);
+  EPIC_LAUNCH_R(M.mixed, k_zonal_visc, grid, 32 * rows, rows * row_bytes, s, M, var, sel, jbot, jhalf, k0, index == 2);
   return 0;
 }
 

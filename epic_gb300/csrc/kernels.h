@@ -47,8 +47,9 @@ int launch_hsu_zonal(const DevModel &M, double *buff, int kind, int kstart, cuda
 int filter_kernels_init(int ni);
 // k_filter_gemm.cu -- the plane filter as a tcgen05 (3xTF32) operator product, mixed form
 bool filter_gemm_usable(const DevModel &M);
+// copy_rows: also copy the rows the operator leaves alone (and set their pads)
 int launch_filter_planes_gemm(const DevModel &M, const double *src, int src_sel, double *dst, int k0, int nplanes, int vgrid, cudaStream_t s,
-                              int shift = 0);
+                              int shift, int copy_rows);
 int filter_gemm_init(int ni);
 
 // k_column_acc.cu -- set_p2etc and store_pgrad_vars (column part) of the mixed form, with the
@@ -63,7 +64,8 @@ void fill_twiddles(int ni, double *tw);
 
 // k_column.cu -- vertical (column) work
 int launch_source_sink(const DevModel &M, cudaStream_t s);
-int launch_calc_w(const DevModel &M, cudaStream_t s);
+// with_source_sink: source_sink first, in the same kernel (the step calls the two in a row)
+int launch_calc_w(const DevModel &M, cudaStream_t s, bool with_source_sink = false);
 int launch_uv_drag(const DevModel &M, cudaStream_t s);
 int launch_hsu_vertical(const DevModel &M, double *buff, int kind, cudaStream_t s);
 int launch_restore_mass(const DevModel &M, cudaStream_t s);

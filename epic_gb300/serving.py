@@ -9,9 +9,11 @@ steps).  The server
   * keeps every admitted run's state on the device from admission to completion;
   * groups the active runs by launch class -- what the runs of one Batch must share: layers,
     schemes, precision form, viscosity orders, and in the mixed forms the zonal filter's path;
-    grid sizes and time steps may differ -- and advances each class as one Batch: every kernel
-    of a step is launched once for all of the class's runs, uneven sizes included, and the
-    classes' batches run on their own streams, so their work overlaps on the device;
+    grid sizes and time steps may differ, within a size bucket (a power of 16 in cells by
+    default, since a batch steps at its largest member's pace) -- and advances each class as one
+    Batch: every kernel of a step is launched once for all of the class's runs, uneven sizes
+    included, and the classes' batches run on their own streams, so their work overlaps on the
+    device;
   * never waits on one class while another could be launched: each pass polls every class's
     batch (epic_batch_query), settles the ones that finished and relaunches them at once;
   * re-forms a class's batch whenever a run joins or leaves it (continuous batching: runs that
@@ -27,6 +29,7 @@ of its own step, and the number of steps per round does not change the arithmeti
 """
 from __future__ import annotations
 
+import math
 import time
 from dataclasses import dataclass, field
 
@@ -71,13 +74,17 @@ class _Active:
     admitted: float
 
 
-def launch_class(cfg: HSConfig, k_sigma: int, precision: int) -> tuple:
+def launch_class(cfg: HSConfig, k_sigma: int, precision: int, size_ratio: int = 16) -> tuple:
     """What the members of one Batch must share (epic_batch_create): layers and the pure-sigma
     split, schemes, precision form, which viscosity orders and whether divergence damping act,
-    the filter latitude, and in the mixed forms whether ni takes the tensor-core filter."""
+    the filter latitude, and in the mixed forms whether ni takes the tensor-core filter -- plus a
+    size bucket: a batch's step takes as long as its largest member's, so runs are batched only
+    with runs whose cell count lies in the same power of size_ratio (0 batches every size of a
+    class together)."""
     tensor_filter = precision != EPIC_PREC_FP64 and cfg.ni % 128 == 0 and cfg.ni <= 1024
+    bucket = int(math.log(cfg.ni * cfg.nj * cfg.nk, size_ratio)) if size_ratio > 1 else 0
     return (cfg.nk, k_sigma, cfg.uv_scheme, cfg.advection_scheme, precision, tensor_filter, cfg.nu4 > 0, cfg.nu6 > 0,
-            cfg.nu8 > 0, cfg.nudiv != 0, cfg.lat0)
+            cfg.nu8 > 0, cfg.nudiv != 0, cfg.lat0, bucket)
 
 
 def state_checksum(f: Fields) -> float:
@@ -124,6 +131,7 @@ class RunServer:
     precision: int = EPIC_PREC_MIXED
     round_steps: int = 16                # most steps a class advances per scheduling pass
     keep_fields: bool = False            # keep each result's full state (else a checksum)
+    size_ratio: int = 16                 # runs share a batch only in one power of this in cells (0: any)
     allow_jets: bool = False             # serve jet-state requests (see submit)
     backend: object = field(default_factory=DeviceBackend)
     waiting: list = field(default_factory=list)
@@ -163,7 +171,7 @@ class RunServer:
             del self.prepared[req.rid]
             self.used += need
             self.peak_used = max(self.peak_used, self.used)
-            cls = launch_class(req.cfg, getattr(ga.struct, "k_sigma", req.cfg.nk), self.precision)
+            cls = launch_class(req.cfg, getattr(ga.struct, "k_sigma", req.cfg.nk), self.precision, self.size_ratio)
             self.active.setdefault(cls, []).append(_Active(req, m, need, req.steps, self.now()))
         self.waiting = keep
 

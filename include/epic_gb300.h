@@ -152,8 +152,9 @@ int  epic_model_run(epic_model *m, int32_t nsteps);
  * HDRY/THETA, 11 set_p2etc(UPDATE_THETA), 12 uv_pgrad, 13 divergence damping, 14 u/v time
  * update, 15 u/v hyperviscosity, 16 store_diag, 17 calc_heating, 18 set_p2etc(DONT_UPDATE),
  * 19 store_pgrad_vars after stage 11 -- the call whose output the pressure gradient reads: the
- * same kernels as 7 in the FP64 form; in EPIC_PREC_MIXED the double-float ones, while 6 and 7,
- * whose P2 and GZ3 are recomputed before the pressure gradient, run the FP32 ones).
+ * same kernels as 7 in the FP64 form; in the mixed forms the full ones, while 6 and 7 compute
+ * only what is read before stages 11 and 19 recompute the rest), 20 stages 1 and 2 in one kernel
+ * (the step's form of them).
  * It has no counterpart in the reference, which only exposes the whole step.
  */
 int  epic_model_run_stage(epic_model *m, int32_t stage);

@@ -89,7 +89,7 @@ def test_budget_backfill_classes_and_step_counts(lag):
     be = FakeBackend(lag)
     big, small = (64, 32, 10), (16, 8, 10)          # 20480 and 1280 "bytes"
     reqs = [_req(0, big, 7), _req(1, big, 5), _req(2, small, 9), _req(3, small, 4), _req(4, big, 3)]
-    server = RunServer(hbm_budget=20480 + 2 * 1280, round_steps=4, backend=be)
+    server = RunServer(hbm_budget=20480 + 2 * 1280, round_steps=4, backend=be, size_ratio=0)
     res = server.serve(reqs)
     assert [r.rid for r in res] == [0, 1, 2, 3, 4]
     assert server.peak_used <= server.hbm_budget and server.used == 0
@@ -148,3 +148,17 @@ def test_durations_in_simulated_days():
         days = r.steps * r.cfg.dt / 86400.0
         assert 0.25 - 1e-3 <= days <= 2.0 + 1e-3
     assert all(np.diff([r.arrival for r in reqs]) > 0)
+
+
+def test_size_buckets_keep_small_runs_out_of_large_batches():
+    """With size buckets (the default: powers of 16 in cells) a small run is not batched with a run
+    64 times its size, but is with one 4 times its size; with size_ratio=0 all three share one."""
+    from epic_gb300.serving import launch_class
+    small, mid, big = HSConfig(ni=32, nj=16, nk=10), HSConfig(ni=64, nj=32, nk=10), HSConfig(ni=128, nj=64, nk=10)
+    assert launch_class(small, 10, 0) != launch_class(big, 10, 0)      # FP64: one filter path
+    assert launch_class(small, 10, 0) == launch_class(mid, 10, 0)
+    assert launch_class(small, 10, 0, 0) == launch_class(big, 10, 0, 0)
+    be = FakeBackend()
+    reqs = [_req(0, (32, 16, 10), 6), _req(1, (256, 128, 10), 6), _req(2, (64, 32, 10), 6)]
+    RunServer(hbm_budget=10 ** 9, round_steps=3, backend=be).serve(reqs)
+    assert all(len(shapes) == 1 or shapes == {(32, 16, 10), (64, 32, 10)} for _, shapes, _ in be.log)
