@@ -440,6 +440,35 @@ def ensemble_error(torch, precision, cfg, nmem=64, steps=288):
     return out
 
 
+def cfg2_error(precision, steps=240):
+    """The mixed-precision configuration's own shape, 512x256x40 (the 512x512 tensor-core filter
+    operator), from rest at dt = 60 s for `steps` steps -- the FP64 run of this state stops with
+    non-monotonic GZ3 after ~288 steps at dt 60 and within the first steps at dt 150 -- against the
+    FP64 form: relative L2 over interior cells and max |error| / max |FP64| per prognostic."""
+    import numpy as np
+    from epic_gb300 import EPIC_PREC_FP64, EPIC_SYNC_DIAGS_ONLY, HSConfig, Model, hs_setup
+    from epic_gb300.abi import Layout
+    ga, f = hs_setup(HSConfig(ni=512, nj=256, nk=40, dt=60, seed=0))
+    res = []
+    for prec in (EPIC_PREC_FP64, precision):
+        m = Model(ga, prec)
+        m.upload(f)
+        m.timestep(EPIC_SYNC_DIAGS_ONLY)
+        m.run(steps)
+        m.sync()
+        res.append(m.download())
+        m.close()
+    L = Layout(512, 256, 40)
+    out = {"rel_l2": {}, "max_abs_over_max": {}}
+    for k, kind in (("u", "uv"), ("v", "vv"), ("hdry", "h"), ("theta", "h")):
+        pick = (lambda x: x.wind(k)) if k in ("u", "v") else (lambda x: x.arrays[k])
+        a, r = L.interior(pick(res[1]), kind), L.interior(pick(res[0]), kind)
+        out["rel_l2"][k] = float(np.linalg.norm(a - r) / np.linalg.norm(r))
+        out["max_abs_over_max"][k] = float(np.abs(a - r).max() / np.abs(r).max())
+    out["case"] = f"512x256x40, dt=60 s, {steps} steps ({steps * 60 / 3600:.0f} h) from rest, vs the FP64 form"
+    return out
+
+
 def serving_summary(precision, seed=3, nreq=24):
     """The serving loop on a seeded Poisson stream (20 requests/s) of Held-Suarez runs of the shapes
     of SERVE_SHAPES, each lasting U[0.25, 2] simulated days."""
@@ -597,6 +626,7 @@ def run_gpu_ensemble(args):
             out["batched_over_fp64_single"] = value / ws / fp64["value"]
             if precision != EPIC_PREC_FP64:
                 out["mixed_error"] = mixed_error(torch, precision, args.advection)
+                out["cfg2_error"] = cfg2_error(precision)
                 out["ensemble_error"] = ensemble_error(torch, precision, cfg, nmem)
             if args.precision == "mixed":
                 # the faster form that keeps the vertical integration and pressure gradient in FP32

@@ -18,7 +18,7 @@ import os
 import numpy as np
 
 from .abi import (EPIC_ADV_AKIMA, EPIC_ADV_HSU, EPIC_PREC_FP64, EPIC_PREC_MIXED, EPIC_PREC_MIXED_FAST, EPIC_PROFILE_HS_EQ,
-                  EPIC_PROFILE_N2, EPIC_STEP_PROGS_AND_SYNC_DIAGS, EPIC_SYNC_DIAGS_ONLY, EPIC_UV_AB3, EPIC_UV_LEAPFROG,
+                  EPIC_PROFILE_N2, EPIC_PROFILE_TABLE, EPIC_STEP_PROGS_AND_SYNC_DIAGS, EPIC_SYNC_DIAGS_ONLY, EPIC_UV_AB3, EPIC_UV_LEAPFROG,
                   EpicFields, EpicGrid, EpicHsParams, EpicJetParams, Fields, GridArrays, HSConfig, JetConfig, Layout)
 
 TUNE_GROUPS = 10   # EPIC_TUNE_GROUPS

@@ -22,6 +22,7 @@ EPIC_ADV_HSU = 0
 EPIC_ADV_AKIMA = 1
 EPIC_PROFILE_HS_EQ = 0
 EPIC_PROFILE_N2 = 1
+EPIC_PROFILE_TABLE = 2
 
 _dp = C.POINTER(C.c_double)
 
@@ -66,7 +67,7 @@ class EpicHsParams(C.Structure):
                 ("ptop", C.c_double), ("pbot", C.c_double), ("p_sigma", C.c_double),
                 ("nu_nondim", C.c_double * 9), ("nudiv_nondim", C.c_double), ("lat0", C.c_double),
                 ("profile", C.c_int32), ("pad1", C.c_int32), ("n2", C.c_double), ("theta_surface", C.c_double),
-                ("t_iso", C.c_double)]
+                ("t_iso", C.c_double), ("table_p", _dp), ("table_t", _dp), ("table_n", C.c_int32), ("pad2", C.c_int32)]
 
 
 class EpicJetParams(C.Structure):
@@ -264,6 +265,9 @@ class HSConfig:
     t_iso: float = 200.0
     state: str = "hs"
     jet: JetConfig = field(default_factory=JetConfig)
+    # EPIC_PROFILE_TABLE: the sounding as (pressures [Pa], temperatures [K]), e.g. the reference's
+    # t_vs_p.held_suarez (tests/golden/t_vs_p_held_suarez.npz)
+    table: tuple | None = None
     extra: dict = field(default_factory=dict)
 
     def params(self) -> EpicHsParams:
@@ -278,6 +282,13 @@ class HSConfig:
         p.lat0 = self.lat0
         p.profile = self.profile
         p.n2, p.theta_surface, p.t_iso = self.n2, self.theta_surface, self.t_iso
+        if self.table is not None:
+            # the struct points at these arrays: they live as long as this config
+            self._table_arrays = tuple(np.ascontiguousarray(a, dtype=np.float64) for a in self.table)
+            tp, tt = self._table_arrays
+            if tp.shape != tt.shape:
+                raise ValueError("sounding table: pressures and temperatures differ in length")
+            p.table_p, p.table_t, p.table_n = _ptr(tp), _ptr(tt), int(tp.size)
         return p
 
     @property

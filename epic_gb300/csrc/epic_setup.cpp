@@ -12,6 +12,7 @@
 // equilibrium profile at 45 degrees (temp_eq, src/shared/epic_sensible_heating.c:394-406), or
 // by a constant-N^2 sounding for the zonal-jet state (epic_jet_initial_state).
 // Compiled with -ffp-contract=off so the same bits come out on x86-64 and aarch64 hosts.
+#include <algorithm>
 #include <cmath>
 #include <cstdint>
 #include <cstring>
@@ -93,11 +94,111 @@ inline double hs_theta_eq(double lat_deg, double p, double kappa) {
   return hs_temp_eq(lat_deg, p, kappa) * pow(kPress0 / p, kappa);
 }
 
+// A tabulated sounding, as get_sounding (epic_funcs_diag.c:3160-3290) prepares it from
+// t_vs_p.<planet>: levels ordered by x = -ln p ascending (the reference stores them bottom first,
+// epic_funcs_io.c:4074-4088), theta = T (p0/p)^kappa at each level (return_theta with x_h2 = 0,
+// epic_funcs_diag.c:6408-6430), Fritsch-Carlson monotone slopes with three-point end conditions
+// (spline_pchip, epic_funcs_util.c:715-846) taken before theta is ironed from the top down (a
+// level warmer than the one above it takes that level's theta, the slopes stay), and the cubic
+// Hermite piece of the interval holding x (splint_pchip, :926-946); below the table's lowest level
+// its bottom value.
+struct TableSounding {
+  const double *src_p = nullptr, *src_t = nullptr;
+  int n = 0;
+  std::vector<double> x, y, z;
+};
+
+inline double sign_product(double a, double b) {   // pchst: the sign of a*b, 0 when either is 0
+  return (a == 0. || b == 0.) ? 0. : ((a > 0.) == (b > 0.) ? 1. : -1.);
+}
+
+void pchip_slopes(const std::vector<double> &x, const std::vector<double> &y, std::vector<double> &z) {
+  const int n = (int)x.size();
+  z.assign(n, 0.);
+  std::vector<double> h(n - 1), d(n - 1);
+  for (int q = 0; q + 1 < n; q++) {
+    h[q] = x[q + 1] - x[q];
+    d[q] = (y[q + 1] - y[q]) / h[q];
+  }
+  if (n == 2) { z[0] = z[1] = d[0]; return; }
+  // end points: three-point slopes, zeroed when against the end interval's slope, limited to three
+  // times it when the first two intervals change direction
+  {
+    const double hs = h[0] + h[1];
+    double t = ((h[0] + hs) / hs) * d[0] + (-h[0] / hs) * d[1];
+    if (sign_product(t, d[0]) <= 0.) t = 0.;
+    else if (sign_product(d[0], d[1]) < 0. && fabs(3. * d[0]) < fabs(t)) t = 3. * d[0];
+    z[0] = t;
+  }
+  {
+    const double h1 = h[n - 3], h2 = h[n - 2], d1 = d[n - 3], d2 = d[n - 2], hs = h1 + h2;
+    double t = (-h2 / hs) * d1 + ((h2 + hs) / hs) * d2;
+    if (sign_product(t, d2) <= 0.) t = 0.;
+    else if (sign_product(d1, d2) < 0. && fabs(3. * d2) < fabs(t)) t = 3. * d2;
+    z[n - 1] = t;
+  }
+  // interior: the weighted harmonic mean of the neighbouring slopes where they agree in sign, else 0
+  for (int q = 1; q + 1 < n; q++) {
+    const double h1 = h[q - 1], h2 = h[q], d1 = d[q - 1], d2 = d[q];
+    if (sign_product(d1, d2) > 0.) {
+      const double hs = h1 + h2, hs3 = 3. * hs;
+      const double w1 = (hs + h1) / hs3, w2 = (hs + h2) / hs3;
+      const double dmax = std::max(fabs(d1), fabs(d2)), dmin = std::min(fabs(d1), fabs(d2));
+      z[q] = dmin / (w1 * (d1 / dmax) + w2 * (d2 / dmax));
+    }
+  }
+}
+
+const TableSounding &table_sounding(const epic_hs_params *p) {
+  thread_local TableSounding s;
+  if (s.src_p == p->table_p && s.src_t == p->table_t && s.n == p->table_n && !s.x.empty()) return s;
+  const int n = p->table_n;
+  std::vector<int> order(n);
+  for (int q = 0; q < n; q++) order[q] = q;
+  std::sort(order.begin(), order.end(), [&](int a, int b) { return p->table_p[a] > p->table_p[b]; });
+  s.x.resize(n);
+  s.y.resize(n);
+  for (int q = 0; q < n; q++) {
+    const double pq = p->table_p[order[q]], tq = p->table_t[order[q]];
+    s.x[q] = -log(pq);
+    s.y[q] = tq * pow(kPress0 / pq, kHsKappa);
+  }
+  pchip_slopes(s.x, s.y, s.z);
+  for (int q = n - 2; q >= 0; q--)
+    if (s.y[q] > s.y[q + 1]) s.y[q] = s.y[q + 1];
+  s.src_p = p->table_p;
+  s.src_t = p->table_t;
+  s.n = n;
+  return s;
+}
+
+double table_theta(const epic_hs_params *p, double pres) {
+  const TableSounding &s = table_sounding(p);
+  const double x = -log(pres);
+  const int n = (int)s.x.size();
+  if (x < s.x[0]) return s.y[0];
+  int q = 0;
+  if (x >= s.x[n - 1]) q = n - 2;
+  else {
+    int lo = 0, hi = n - 1;
+    while (hi - lo > 1) {
+      const int m = (lo + hi) / 2;
+      if (x >= s.x[m]) lo = m; else hi = m;
+    }
+    q = lo;
+  }
+  const double h = s.x[q + 1] - s.x[q], delta = (s.y[q + 1] - s.y[q]) / h;
+  const double del1 = (s.z[q] - delta) / h, del2 = (s.z[q + 1] - delta) / h;
+  const double c3 = (del1 + del2) / h, c2 = -(del1 + del1 + del2), t = x - s.x[q];
+  return s.y[q] + t * (s.z[q] + t * (c2 + t * c3));
+}
+
 // The sounding (theta at pressure pres) the vertical grid and the initial columns follow.
 // EPIC_PROFILE_N2: theta(z) = theta_s exp(N^2 z / g) in hydrostatic balance from pbot up, i.e.
 // 1/theta(p) = 1/theta_s + N^2 R / (g^2 kappa) ((p/p0)^kappa - (pbot/p0)^kappa), with the
 // temperature held at t_iso above the level where it falls to t_iso.
 inline double sounding_theta(const epic_hs_params *p, double pres) {
+  if (p->profile == EPIC_PROFILE_TABLE) return table_theta(p, pres);
   if (p->profile != EPIC_PROFILE_N2) return hs_theta_eq(45., pres, kHsKappa);
   const double pbot = p->pbot > 0. ? p->pbot : 1.e+5;
   const double c = p->n2 * kHsRgas / (kSoundingGrav * kSoundingGrav * kHsKappa);
@@ -137,7 +238,17 @@ extern "C" int epic_hs_grid_build(const epic_hs_params *p, epic_grid *g, double 
   if (p->uv_scheme != EPIC_UV_AB3 && p->uv_scheme != EPIC_UV_LEAPFROG) return set_error(EPIC_ERR_ARG, "uv_scheme=%d", p->uv_scheme);
   if (p->advection_scheme != EPIC_ADV_HSU && p->advection_scheme != EPIC_ADV_AKIMA)
     return set_error(EPIC_ERR_ARG, "advection_scheme=%d", p->advection_scheme);
-  if (p->profile != EPIC_PROFILE_HS_EQ && p->profile != EPIC_PROFILE_N2) return set_error(EPIC_ERR_ARG, "profile=%d", p->profile);
+  if (p->profile != EPIC_PROFILE_HS_EQ && p->profile != EPIC_PROFILE_N2 && p->profile != EPIC_PROFILE_TABLE)
+    return set_error(EPIC_ERR_ARG, "profile=%d", p->profile);
+  if (p->profile == EPIC_PROFILE_TABLE) {
+    if (!p->table_p || !p->table_t || p->table_n < 3) return set_error(EPIC_ERR_ARG, "sounding table: need 3 or more levels");
+    for (int q = 0; q < p->table_n; q++) {
+      if (!(p->table_p[q] > 0.) || !(p->table_t[q] > 0.))
+        return set_error(EPIC_ERR_ARG, "sounding table level %d: p=%g T=%g", q, p->table_p[q], p->table_t[q]);
+      for (int r = 0; r < q; r++)
+        if (p->table_p[r] == p->table_p[q]) return set_error(EPIC_ERR_ARG, "sounding table: pressure %g repeats", p->table_p[q]);
+    }
+  }
   if (p->profile == EPIC_PROFILE_N2) {
     const double pbot_chk = p->pbot > 0. ? p->pbot : 1.e+5;
     const double c = p->n2 * kHsRgas / (kSoundingGrav * kSoundingGrav * kHsKappa);

@@ -335,13 +335,22 @@ typedef struct epic_hs_params {
   double  n2;                  /* EPIC_PROFILE_N2: buoyancy frequency squared [s^-2] below the ... */
   double  theta_surface;       /* ... isothermal layer: theta = theta_surface at pbot [K] ... */
   double  t_iso;               /* ... and T = max(t_iso, T_N2(p)) [K] */
+  /* EPIC_PROFILE_TABLE: a temperature sounding as the reference reads it from t_vs_p.<planet>
+   * (read_t_vs_p, src/shared/epic_funcs_io.c:4027-4088): table_n levels of pressure [Pa] and
+   * temperature [K], in either order of pressure; the arrays are read during the call only */
+  const double *table_p, *table_t;
+  int32_t table_n, pad2;
 } epic_hs_params;
 
-/* Soundings: the Held-Suarez equilibrium column at 45 degrees (temp_eq), or a column of
- * constant buoyancy frequency N^2 from theta_surface at pbot, isothermal at t_iso above the
- * level where it reaches that temperature (the stable jet sounding). */
+/* Soundings: the Held-Suarez equilibrium column at 45 degrees (temp_eq); a column of constant
+ * buoyancy frequency N^2 from theta_surface at pbot, isothermal at t_iso above the level where
+ * it reaches that temperature (the stable jet sounding); or a table, interpolated as the
+ * reference's get_sounding (src/shared/epic_funcs_diag.c:3160-3290) does: theta of the table's
+ * levels, ironed from the top down so that it never decreases upward, by monotone cubic Hermite
+ * interpolation (PCHIP) in -ln p, the table's bottom value below its lowest level. */
 #define EPIC_PROFILE_HS_EQ 0
 #define EPIC_PROFILE_N2    1
+#define EPIC_PROFILE_TABLE 2
 
 int epic_hs_grid_build(const epic_hs_params *p, epic_grid *grid, double *p_ref, double *theta_ref);
 

@@ -183,6 +183,29 @@ int ref_get(epic_fields *f) {
   return 0;
 }
 
+/*
+ * The reference's get_sounding(planet, p, "theta", &theta) (src/shared/epic_funcs_diag.c:3160-3290)
+ * on a t_vs_p table -- ntp levels, pressures [Pa] and temperatures [K] bottom level first, as
+ * read_t_vs_p stores them (src/shared/epic_funcs_io.c:4074-4088) -- at n pressures, for the
+ * Held-Suarez planet with grid.press0 = press0.  get_sounding keeps its table in static storage,
+ * so one table per process.
+ */
+int ref_sounding_theta(int ntp, const double *pdat, const double *tdat, double press0, int n, const double *pres, double *out) {
+  int q;
+  if (!planet) {
+    planet = (planetspec *)malloc(sizeof(planetspec));
+    *planet = held_suarez;
+  }
+  grid.press0 = press0;
+  var.ntp = ntp;
+  var.pdat = fvector(0, ntp - 1, "ref_harness");
+  var.tdat = fvector(0, ntp - 1, "ref_harness");
+  var.dtdat = fvector(0, ntp - 1, "ref_harness");
+  for (q = 0; q < ntp; q++) { var.pdat[q] = pdat[q]; var.tdat[q] = tdat[q]; var.dtdat[q] = 0.; }
+  for (q = 0; q < n; q++) get_sounding(planet, pres[q], "theta", out + q);
+  return 0;
+}
+
 /* netCDF entry points referenced by src/shared/epic_funcs_io.c; the step never calls them. */
 int nc_close(int a) { (void)a; return -1; }
 int nc_create(const char *p, int m, int *id) { (void)p; (void)m; (void)id; return -1; }

@@ -175,3 +175,30 @@ def rel_l2(a: np.ndarray, b: np.ndarray) -> float:
     den = np.linalg.norm(b.ravel())
     num = np.linalg.norm((a - b).ravel())
     return float(num / den) if den > 0 else float(num)
+
+
+def _sounding_worker(pdat, tdat, press0, pres, q):
+    try:
+        lib = C.CDLL(REF_LIB)
+        dp = C.POINTER(C.c_double)
+        pdat, tdat, pres = (np.ascontiguousarray(a, dtype=np.float64) for a in (pdat, tdat, pres))
+        out = np.zeros(pres.size)
+        lib.ref_sounding_theta(C.c_int(pdat.size), pdat.ctypes.data_as(dp), tdat.ctypes.data_as(dp), C.c_double(press0),
+                               C.c_int(pres.size), pres.ctypes.data_as(dp), out.ctypes.data_as(dp))
+        q.put(("ok", out))
+    except Exception as e:  # pragma: no cover - reported to the parent
+        q.put(("err", repr(e)))
+
+
+def reference_sounding_theta(pdat, tdat, press0, pres) -> np.ndarray:
+    """theta at `pres` from the reference's own get_sounding on the table (pdat bottom first),
+    computed in a spawned process (the reference keeps the table in static storage)."""
+    ctx = mp.get_context("spawn")
+    q = ctx.Queue()
+    p = ctx.Process(target=_sounding_worker, args=(np.asarray(pdat), np.asarray(tdat), press0, np.asarray(pres), q))
+    p.start()
+    status, out = q.get(timeout=600)
+    p.join(60)
+    if status != "ok":
+        raise RuntimeError(out)
+    return out

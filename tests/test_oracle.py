@@ -185,3 +185,40 @@ def test_jet_fixture_inputs_match_generator():
     pbot = f.arrays["p3"][10, 1:18, 5]
     assert pbot.max() - pbot.min() > 5e3
     assert np.abs(f.arrays["u"][0][1:11]).max() > 50.
+
+
+SOUNDING = os.path.join(os.path.dirname(__file__), "golden", "t_vs_p_held_suarez.npz")
+
+
+@pytest.mark.parametrize("shape", [(64, 32, 10), (512, 256, 40)])
+def test_table_sounding_matches_reference_get_sounding(shape):
+    """The grid build's theta profile from the reference's own Held-Suarez sounding (profile
+    EPIC_PROFILE_TABLE) against the reference's get_sounding on the same table, at the grid's
+    reference pressures: bit for bit."""
+    from epic_gb300 import EPIC_PROFILE_TABLE
+    from oracle_lib import reference_sounding_theta
+    if not reference_available():
+        pytest.skip("needs the reference source tree")
+    z = np.load(SOUNDING)
+    ni, nj, nk = shape
+    ga, _ = hs_setup(HSConfig(ni=ni, nj=nj, nk=nk, dt=150, profile=EPIC_PROFILE_TABLE, table=(z["p"], z["t"])))
+    kk = np.arange(2, 2 * nk + 1)
+    want = reference_sounding_theta(z["p"], z["t"], ga.struct.press0, ga.p_ref[kk])
+    got = ga.theta_ref[kk]
+    assert np.array_equal(got, want), np.max(np.abs(got - want) / want)
+
+
+def test_table_sounding_state():
+    """The Held-Suarez state on the reference's sounding: sigmatheta decreasing downward, P3
+    increasing downward in every column, theta of the pure-sigma layers near the table's."""
+    from epic_gb300 import EPIC_PROFILE_TABLE
+    z = np.load(SOUNDING)
+    ga, f = hs_setup(HSConfig(ni=64, nj=32, nk=10, dt=300, profile=EPIC_PROFILE_TABLE, table=(z["p"], z["t"])))
+    s = ga.struct
+    sg = ga.sigmatheta[1:2 * s.nk + 2]
+    assert np.all(np.diff(sg) < 0)
+    p3 = f.p3[:s.nk + 1, 1:s.nj + 2, 1:s.ni + 1]
+    assert np.all(np.diff(p3, axis=0) > 0)
+    # the surface layer's theta follows the table's 1000 hPa temperature (288.15 K at 1013 hPa)
+    th = f.theta[s.nk, 1:s.nj + 2, 1:s.ni + 1]
+    assert 280. < th.mean() < 295.
