@@ -266,7 +266,7 @@ class HSConfig:
     state: str = "hs"
     jet: JetConfig = field(default_factory=JetConfig)
     # EPIC_PROFILE_TABLE: the sounding as (pressures [Pa], temperatures [K]), e.g. the reference's
-    # t_vs_p.held_suarez (tests/golden/t_vs_p_held_suarez.npz)
+    # t_vs_p.held_suarez (tests/golden/sounding/t_vs_p_held_suarez.npz)
     table: tuple | None = None
     extra: dict = field(default_factory=dict)
 

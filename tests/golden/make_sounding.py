@@ -1,5 +1,5 @@
 """Write the reference's Held-Suarez temperature sounding (data/held_suarez/t_vs_p.held_suarez)
-as tests/golden/t_vs_p_held_suarez.npz: pressures [Pa] and temperatures [K] bottom level first,
+as tests/golden/sounding/t_vs_p_held_suarez.npz: pressures [Pa] and temperatures [K] bottom level first,
 the order in which read_t_vs_p stores them (src/shared/epic_funcs_io.c:4027-4088).  Run where the
 reference tree is present; the fixture travels, the reference does not.
 
@@ -27,6 +27,6 @@ def read_t_vs_p(path):
 if __name__ == "__main__":
     ref = sys.argv[1] if len(sys.argv) > 1 else "/root/reference"
     p, t = read_t_vs_p(os.path.join(ref, "data", "held_suarez", "t_vs_p.held_suarez"))
-    out = os.path.join(HERE, "t_vs_p_held_suarez.npz")
+    out = os.path.join(HERE, "sounding", "t_vs_p_held_suarez.npz")
     np.savez_compressed(out, p=p, t=t)
     print(out, p.size, "levels", p[0], "..", p[-1], "Pa")

@@ -187,7 +187,7 @@ def test_jet_fixture_inputs_match_generator():
     assert np.abs(f.arrays["u"][0][1:11]).max() > 50.
 
 
-SOUNDING = os.path.join(os.path.dirname(__file__), "golden", "t_vs_p_held_suarez.npz")
+SOUNDING = os.path.join(os.path.dirname(__file__), "golden", "sounding", "t_vs_p_held_suarez.npz")
 
 
 @pytest.mark.parametrize("shape", [(64, 32, 10), (512, 256, 40)])
