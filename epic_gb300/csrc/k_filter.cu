@@ -593,6 +593,28 @@ __global__ void k_akima_zonal(DevModel M, double *buff, int kind, int kstart) {
   }
 }
 
+// The rows the tensor-core filter leaves alone (k_filter_planes_gemm filters the others): copied
+// when dst is not src, periodic pads on rows 0..nj+1.  One warp per (row, plane).
+__global__ void k_filter_rows_unfiltered(DevModel M, const double *src, int src_sel, double *dst, int k0, int nplanes, int vgrid) {
+  if (epic_member(M, src, dst)) return;
+  src += plane_offset(M, src_sel);
+  const int lane = (int)(threadIdx.x & 31);
+  const int w = (int)((blockIdx.x * blockDim.x + threadIdx.x) >> 5);
+  const int rows = M.nj + 3;
+  if (w >= rows * nplanes) return;
+  const int j = w % rows - 1, k = k0 + w / rows;
+  const bool valid = vgrid ? (j >= 1 && j <= M.nj) : (j >= 0 && j <= M.nj);
+  if (valid && row_is_filtered(M, j, vgrid)) return;
+  const int base = M.at(k, j, 0);
+  if (src != dst)
+    for (int i = lane; i <= M.ni + 1; i += 32) dst[base + i] = src[base + i];
+  __syncwarp();
+  if (j >= 0 && lane == 0) {
+    dst[base] = dst[base + M.ni];
+    dst[base + M.ni + 1] = dst[base + 1];
+  }
+}
+
 // ---- launchers ----
 
 static int row_threads(const DevModel &M) { return M.tb[TB_ROW] > 0 ? M.tb[TB_ROW] : (M.ni >= 256 ? 128 : 64); }
@@ -604,9 +626,14 @@ int launch_filter_planes(const DevModel &M, const double *src, int src_sel, doub
   const size_t smem = ((size_t)(M.ni + 2) + filter_smem_elems(M.ni)) * relem(fp32);
   dim3 grid(M.nj + 3, nplanes);
   if (fp32 && filter_gemm_usable(M)) {
-    // the same launch copies the rows the operator leaves alone and sets their pads, except in
-    // place with the pads already set, where they need nothing
-    return launch_filter_planes_gemm(M, src, src_sel, dst, k0, nplanes, vgrid, s, shift, !(pads_set && src == dst && src_sel == PL_NONE));
+    // The rows the operator leaves alone are copied (and padded) by a light kernel of their own:
+    // done by the operator's blocks, each reserving the product's ~83 KB of shared memory, they
+    // kept the filtered rows' blocks off the SMs (the step's filter time rose by a third).  In
+    // place with the pads already set, those rows need nothing.
+    const long long warps = (long long)(M.nj + 3) * nplanes;
+    if (!(pads_set && src == dst && src_sel == PL_NONE))
+      k_filter_rows_unfiltered<<<zg(epic_blocks(32 * warps, 128), M), 128, 0, s>>>(M, src, src_sel, dst, k0, nplanes, vgrid);
+    return launch_filter_planes_gemm(M, src, src_sel, dst, k0, nplanes, vgrid, s, shift);
   }
   EPIC_LAUNCH_R(fp32, k_filter_planes, grid, row_threads(M), smem, s, M, src, src_sel, dst, k0, vgrid);
   return 0;

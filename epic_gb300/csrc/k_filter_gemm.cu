@@ -91,8 +91,7 @@ __device__ __forceinline__ bool mbar_wait(unsigned mbar, unsigned phase) {
 }  // namespace
 
 // Block = one row j in -1..nj+1 (x), a chunk of 32 planes (y), the member (z).  Rows outside
-// the filtered set are copied from src to dst (when they differ) and get their periodic pads
-// (rows j >= 0), unless copy_rows is 0 (an in-place call whose pads are already set).
+// the filtered set return at once (k_filter_rows_unfiltered copies them).
 //
 // The product runs as a two-stage pipeline over steps t = (K chunk kc, output tile mt): the A
 // (operator) and B (input) tiles are double-buffered in shared memory; while the tensor cores
@@ -101,7 +100,7 @@ __device__ __forceinline__ bool mbar_wait(unsigned mbar, unsigned phase) {
 // its buffer; a buffer is restaged only after the commit of the step that last read it (commits
 // complete in issue order).
 __global__ void __launch_bounds__(FG_THREADS) k_filter_planes_gemm(DevModel M, const double *src, int src_sel, double *dst, int k0,
-                                                                     int nplanes, int vgrid, int shift, int copy_rows) {
+                                                                     int nplanes, int vgrid, int shift) {
   if (epic_member(M, src, dst)) return;
   extern __shared__ __align__(16) unsigned char fg_raw[];
   __shared__ __align__(8) uint64_t mbar[2];
@@ -114,24 +113,7 @@ __global__ void __launch_bounds__(FG_THREADS) k_filter_planes_gemm(DevModel M, c
   const bool valid = vgrid ? (j >= 1 && j <= M.nj) : (j >= 0 && j <= M.nj);
   src += plane_offset(M, src_sel);
   const int n0 = (int)blockIdx.y * FG_N;
-  if (!valid || fabs(M.lat[vgrid ? 2 * j : 2 * j + 1]) < M.lat0) {
-    if (!copy_rows) return;
-    const int w = M.ni + 2, np = min(FG_N, nplanes - n0);
-    if (src != dst)
-      for (int q = (int)threadIdx.x; q < np * w; q += FG_THREADS) {
-        const int n = q / w, i = q - n * w;
-        const int base = M.at(k0 + n0 + n, j, 0);
-        dst[base + i] = src[base + i];
-      }
-    if (j < 0) return;
-    __syncthreads();
-    for (int n = (int)threadIdx.x; n < np; n += FG_THREADS) {
-      const int base = M.at(k0 + n0 + n, j, 0);
-      dst[base] = dst[base + M.ni];
-      dst[base + M.ni + 1] = dst[base + 1];
-    }
-    return;
-  }
+  if (!valid || fabs(M.lat[vgrid ? 2 * j : 2 * j + 1]) < M.lat0) return;
   const int tid = (int)threadIdx.x, warp = tid >> 5;
   const uint32_t tcols = (uint32_t)(mtiles * FG_N);   // 32, 64, 128 or 256: a power of 2
 
@@ -279,10 +261,9 @@ size_t filter_gemm_smem_bytes(int ni) {
 bool filter_gemm_usable(const DevModel &M) { return M.fkern_h && M.ni % FG_M == 0 && M.ni <= 8 * FG_M; }
 
 int launch_filter_planes_gemm(const DevModel &M, const double *src, int src_sel, double *dst, int k0, int nplanes, int vgrid, cudaStream_t s,
-                              int shift, int copy_rows) {
+                              int shift) {
   dim3 grid(M.nj + 3, (nplanes + FG_N - 1) / FG_N);
-  k_filter_planes_gemm<<<zg(grid, M), FG_THREADS, filter_gemm_smem_bytes(M.ni), s>>>(M, src, src_sel, dst, k0, nplanes, vgrid, shift,
-                                                                                      copy_rows);
+  k_filter_planes_gemm<<<zg(grid, M), FG_THREADS, filter_gemm_smem_bytes(M.ni), s>>>(M, src, src_sel, dst, k0, nplanes, vgrid, shift);
   return 0;
 }
 

@@ -47,9 +47,8 @@ int launch_hsu_zonal(const DevModel &M, double *buff, int kind, int kstart, cuda
 int filter_kernels_init(int ni);
 // k_filter_gemm.cu -- the plane filter as a tcgen05 (3xTF32) operator product, mixed form
 bool filter_gemm_usable(const DevModel &M);
-// copy_rows: also copy the rows the operator leaves alone (and set their pads)
 int launch_filter_planes_gemm(const DevModel &M, const double *src, int src_sel, double *dst, int k0, int nplanes, int vgrid, cudaStream_t s,
-                              int shift, int copy_rows);
+                              int shift = 0);
 int filter_gemm_init(int ni);
 
 // k_column_acc.cu -- set_p2etc and store_pgrad_vars (column part) of the mixed form, with the
