@@ -192,6 +192,37 @@ def cpu_reference(name, nsteps, warm, procs, advection="hsu", grids=1, scales=No
     return grids * cfg.cells * nsteps / wall, wall
 
 
+def host_link_gbs(torch, nbytes: int = 1 << 30, reps: int = 3) -> dict:
+    """Pinned host <-> device copy bandwidth of this machine (GB/s): one direction at a time, then both
+    at once on two streams -- what bounds the end-to-end number, whose state crosses twice a step."""
+    h_up = torch.empty(nbytes // 8, dtype=torch.float64, pin_memory=True)
+    h_dn = torch.empty_like(h_up, pin_memory=True)
+    d_up = torch.empty(nbytes // 8, dtype=torch.float64, device="cuda")
+    d_dn = torch.empty_like(d_up)
+    s1, s2 = torch.cuda.Stream(), torch.cuda.Stream()
+
+    def timed(fn):
+        fn()
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        for _ in range(reps):
+            fn()
+        torch.cuda.synchronize()
+        return (time.perf_counter() - t0) / reps
+
+    def both():
+        with torch.cuda.stream(s1):
+            d_up.copy_(h_up, non_blocking=True)
+        with torch.cuda.stream(s2):
+            h_dn.copy_(d_dn, non_blocking=True)
+
+    t_up = timed(lambda: d_up.copy_(h_up, non_blocking=True))
+    t_dn = timed(lambda: h_dn.copy_(d_dn, non_blocking=True))
+    t_both = timed(both)
+    del h_up, h_dn, d_up, d_dn
+    return {"h2d": nbytes / t_up / 1e9, "d2h": nbytes / t_dn / 1e9, "both_directions": 2 * nbytes / t_both / 1e9}
+
+
 def workload_config(args, cfg, nmem, ws):
     """The `config` object of both arms' lines: the workload only (shape, members, time step,
     schemes, state), so that the GPU arm and the reference arm name the same one."""
@@ -592,6 +623,7 @@ def run_gpu_ensemble(args):
     e2e_s = (time.perf_counter() - t0) / e2e_steps
     e2e_val = ws * cells / e2e_s
     host_bytes = sum(h.nbytes for h in hosts)
+    link = host_link_gbs(torch)
     state_gb = sum(m.device_bytes for m in members) / 1e9
     batch.close()
     for m in members:
@@ -611,7 +643,12 @@ def run_gpu_ensemble(args):
                                          "update", "column", "pointwise", "row_filter",
                                          "hsu_meridional_form (1 fused march, 2 four passes)"]},
             "clocks": clocks,
-            "e2e": {"value": e2e_val, "unit": "cell-steps/s", "h2d_bytes_per_step": host_bytes, "d2h_bytes_per_step": host_bytes},
+            "e2e": {"value": e2e_val, "unit": "cell-steps/s", "h2d_bytes_per_step": host_bytes, "d2h_bytes_per_step": host_bytes,
+                    "ms_per_step": e2e_s * 1e3, "host_link_gbs": link,
+                    "link_bound_ms_per_step": 2e3 * host_bytes / (link["both_directions"] * 1e9) if link.get("both_directions") else None,
+                    "note": "state copied up and down every step in 8 sub-batches on their own streams, copies of one "
+                            "overlapping the kernels of the others; host_link_gbs is one pinned copy of the state's size "
+                            "alone in each direction and both at once on this box"},
             "gpu_launches": launches,
             "roofline": roof,
             "roofline_store_pgrad_vars": roof_column,

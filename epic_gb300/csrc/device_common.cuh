@@ -65,7 +65,10 @@ struct DevModel {
   const double *coslat4;                    // pow(coslat[j], 4.) correctly rounded (t_rad's cos^4)
   const MathTable *lt;                      // double-double tables for cr_log/cr_exp/cr_pow
   const float *twf;                         // the twiddles rounded to float (mixed form)
-  const float *fkern_h, *fkern_v;           // circulant filter kernels per row (mixed form, tensor-core filter)
+  const void *fop_map;                      // tensor-core filter (mixed form): the TMA tensor map of the
+                                            // operator tiles of the filtered rows (k_filter_gemm.cu), or null
+  const int *fop_slot;                      // their slot of each row j = -1..nj+1, h rows then v rows; -1
+                                            // where the row is not filtered
   const float2 *exp2tab;                    // 2^(j/32), j = 0..31, as double-floats (exp_df)
   float2 dfc[DFC_COUNT];                    // kappa, 1/kappa, kappa+1, the hybrid-coordinate constants
                                             // and log(press0) as double-floats (hi, lo)
@@ -91,6 +94,7 @@ struct DevModel {
                        // pointer arguments field by field); the launch description then carries
                        // the largest sizes of its members, and member 0's arrays
   long long reloc_n3;  // a launch description's field size of member 0 (whose arrays it carries)
+  int fop_shared;      // a batch whose members all filter with member 0's operator tiles (same grid)
   char *pool_base;   // start of the model's device pool (state, scratch and tables)
   // launch shapes (host side only): threads per block of each kernel group, set by the
   // autotuner; they change no result (every tuned kernel is pointwise or per row)
@@ -134,16 +138,17 @@ __device__ __forceinline__ P *relocate_field(const DevModel &from, const DevMode
 // array by array when they do not.  Returns true when the model is halted (a step found a fatal
 // error): the kernel then returns at once.  Ctl::halted changes only in k_itime_advance, between
 // steps, so every thread of a launch reads the same value.
+template <class P>
+__device__ __forceinline__ P *member_ptr(const DevModel &M, const DevModel &mem, P *p) {
+  if (!p) return p;
+  if (M.hetero) return relocate_field(M, mem, p);
+  return (P *)(mem.pool_base + ((const char *)p - M.pool_base));
+}
 template <class... P>
 __device__ __forceinline__ bool epic_member(DevModel &M, P *&...ptrs) {
   if (M.batch) {
     const DevModel &mem = M.batch[blockIdx.z];
-    if (M.hetero) {
-      ((ptrs = ptrs ? relocate_field(M, mem, ptrs) : ptrs), ...);
-    } else {
-      const char *from = M.pool_base, *to = mem.pool_base;
-      ((ptrs = ptrs ? (P *)(to + ((const char *)ptrs - from)) : ptrs), ...);
-    }
+    ((ptrs = member_ptr(M, mem, ptrs)), ...);
     M = mem;
   }
   return M.ctl->halted != 0;
@@ -161,6 +166,38 @@ __device__ __forceinline__ int fcmp(double x1, double x2) {
   const double delta = ldexp(DBL_EPSILON, e);
   const double d = x1 - x2;
   return d > delta ? 1 : (d < -delta ? -1 : 0);
+}
+
+// THETA2 at an isentropic layer (set_p2etc, K > k_sigma-1) interpolates linearly in the table
+// (sigmatheta[2K+1], THETA(K)), K = nk down to k_sigma-1, at sigmatheta[2K] (linint after
+// find_place_in_table, epic_funcs_diag.c:3553-3561, epic_funcs_util.c:636-648,2908-2976).  The interval
+// found depends on the vertical grid alone: a column kernel finds it once per level for the whole
+// block (theta2_intervals, before its first barrier) instead of once per column -- the search's
+// fcmp calls are binary64 operations.  kay indexes the ascending table x = sigmatheta[2(nk-kay)+1].
+__device__ __forceinline__ int theta2_interval(const DevModel &M, int k) {
+  const int nk = M.nk, nkay = nk - (M.k_sigma - 1) + 1;
+  const double sg = M.sgth[2 * k];
+  auto X = [&](int kay) { return M.sgth[2 * (nk - kay) + 1]; };
+  if (fcmp(sg, X(0)) <= 0) return 0;
+  if (fcmp(sg, X(nkay - 1)) >= 0) return nkay - 2;
+  int il = -1, iu = nkay;
+  while (iu - il > 1) {
+    const int im = (iu + il) >> 1;
+    if (fcmp(sg, X(im)) >= 0) il = im; else iu = im;
+  }
+  return il;
+}
+// the intervals of levels k_sigma..nk, and for the binary32 forms (w != nullptr) the weights
+// (sigmatheta[2k] - x0) / (x1 - x0) rounded to binary32
+__device__ __forceinline__ void theta2_intervals(const DevModel &M, int *kay, float *w) {
+  for (int k = M.k_sigma + (int)threadIdx.x; k <= M.nk; k += (int)blockDim.x) {
+    const int q = theta2_interval(M, k);
+    kay[k] = q;
+    if (w) {
+      const double x0 = M.sgth[2 * (M.nk - q) + 1], x1 = M.sgth[2 * (M.nk - q - 1) + 1];
+      w[k] = (float)((M.sgth[2 * k] - x0) / (x1 - x0));
+    }
+  }
 }
 
 // get_sigma / get_p_sigma / g_sigma / f_sigma / return_sigmatheta, epic_funcs_diag.c:1238-1314,1751-1770
@@ -239,6 +276,52 @@ __device__ __forceinline__ double f2d(float f) {
   return __hiloint2double((int)(hi | (w & 0x80000000u)), (int)lo);
 }
 
+// ---- binary64 <-> double-float without the FP64 unit ----
+//
+// The double-float form of x is (hi, lo) = (RN32(x), RN32(x - hi)) and its binary64 value is
+// RN64(hi + lo): one FP64 subtraction or addition each, at the FP64 unit's rate.  The mixed
+// form's column kernels convert several values per level, so both are computed on the integer
+// and FP32 pipes instead, with the same bits: the residual x - hi is the part of x's 53-bit
+// significand below hi's rounding point, an integer r (|r| <= 2^28) in units of x's last place,
+// rounded to binary32 by one fused multiply-add of two exact halves; hi + lo moves hi's binary64
+// significand by lo in units of its last place, rounded to nearest-even by the conversion to
+// integer (in the binade below a power of two when lo takes hi towards zero, whose unit is half
+// as large; a normalised lo, |lo| <= ulp32(hi)/2, never takes the sum out of those binades).
+// Magnitudes below 2^-74 (5e-23, far below any value of the model's fields but exact zeros) keep
+// binary32 precision: lo is zero there, and a hi that small converts without its lo.
+__device__ __forceinline__ dfl d2df(double x) {
+  const unsigned hi = (unsigned)__double2hiint(x), lo = (unsigned)__double2loint(x);
+  const unsigned a = hi & 0x7fffffffu;
+  const unsigned half = 0x0fffffffu + ((lo >> 29) & 1u);   // d2f's rounding increment
+  const unsigned long long v = (((unsigned long long)hi << 32) | lo) + half;
+  unsigned u = (__funnelshift_l((unsigned)v, (unsigned)(v >> 32), 3) - (896u << 23)) | (hi & 0x80000000u);
+  if (a - 0x38100000u >= 0x0fe00000u)
+    u = (hi & 0x80000000u) | (a < 0x38100000u ? 0u : ((a | (lo != 0u)) > 0x7ff00000u ? 0x7fc00000u : 0x7f800000u));
+  // x - hi in units of x's last place: the 29 bits below the rounding point, less the carry
+  const int r = (int)((unsigned)v & 0x1fffffffu) - (int)half;
+  const int rs = (int)hi < 0 ? -r : r;
+  // rs = 64 q + b with |q| <= 2^22 and 0 <= b < 64, both exact in binary32 by the 1.5 2^23 and
+  // 2^23 shifts; lo = RN32(rs 2^(E-1075)), E the binary64 exponent field, normal for E >= 949
+  const float fq = __uint_as_float(0x4B400000u + (unsigned)(rs >> 6)) - 12582912.f;
+  const float fb = __uint_as_float(0x4B000000u + ((unsigned)rs & 63u)) - 8388608.f;
+  const unsigned e = a >> 20;
+  const float sc = e - 949u < 202u ? __uint_as_float((e - 948u) << 23) : 0.f;
+  return dfl(__uint_as_float(u), fmaf(fq, 64.f * sc, fb * sc));
+}
+__device__ __forceinline__ double df2d(dfl x) {
+  const unsigned wh = __float_as_uint(x.hi), wl = __float_as_uint(x.lo), ah = wh & 0x7fffffffu, eh = ah >> 23;
+  // lo towards zero from a power of two: the binade below, its unit half as large
+  const unsigned down = (ah & 0x007fffffu) == 0u && ((wl ^ wh) & 0x80000000u) && (wl & 0x7fffffffu) ? 1u : 0u;
+  const bool ok = eh - 52u - down < 202u - down;   // 2^-74 <= |hi| (2^-73 going down), finite
+  // lo in units of the last place of hi's binary64 significand: lo 2^(52 - (eh - 127) + down)
+  const float sc = __uint_as_float(((ok ? 306u - eh : 127u) + down) << 23);
+  const int k = ok ? __float2int_rn(x.lo * sc) : 0;
+  unsigned long long mag = ((unsigned long long)ah << 29) + (896ull << 52);
+  mag = ah >= 0x7f800000u ? mag + (896ull << 52) : (ah < 0x00800000u ? 0ull : mag);   // f2d's cases
+  mag += (long long)((int)wh < 0 ? -k : k);
+  return __longlong_as_double((long long)(mag | ((unsigned long long)(wh & 0x80000000u) << 32)));
+}
+
 // ---- compute-type helpers for kernels instantiated in FP64 (R = double: the drop-in form,
 // bit-identical to the reference's arithmetic) and FP32 (R = float: the mixed form) ----
 
@@ -246,17 +329,14 @@ __device__ __forceinline__ double f2d(float f) {
 template <class R> __device__ __forceinline__ R cv(double x);
 template <> __device__ __forceinline__ double cv<double>(double x) { return x; }
 template <> __device__ __forceinline__ float cv<float>(double x) { return d2f(x); }
-template <> __device__ __forceinline__ dfl cv<dfl>(double x) {
-  const float h = d2f(x);
-  return dfl(h, d2f(x - f2d(h)));
-}
+template <> __device__ __forceinline__ dfl cv<dfl>(double x) { return d2df(x); }
 // a model constant in the compute type: the double-float ones come split from the host (the
 // same bits as cv<dfl> of the binary64 value), the others by cv
 template <class R> __device__ __forceinline__ R mconst(const DevModel &, int, double v) { return cv<R>(v); }
 template <> __device__ __forceinline__ dfl mconst<dfl>(const DevModel &M, int q, double) { return dfl(M.dfc[q].x, M.dfc[q].y); }
 __device__ __forceinline__ double to_d(double x) { return x; }
 __device__ __forceinline__ double to_d(float x) { return f2d(x); }
-__device__ __forceinline__ double to_d(dfl x) { return f2d(x.hi) + f2d(x.lo); }
+__device__ __forceinline__ double to_d(dfl x) { return df2d(x); }
 
 template <class R> __device__ __forceinline__ R rmax(R x, R y) { return x > y ? x : y; }
 template <class R> __device__ __forceinline__ R rmin(R x, R y) { return x < y ? x : y; }
@@ -382,8 +462,8 @@ __device__ __forceinline__ void flag_error(Ctl *c, int code, int k, int j, int i
 // write the two fields before it (store_pgrad_vars and set_p2etc of stages 19 and 11, and the
 // polar rows of GZ3 in uv_pgrad itself) to the pressure gradient.
 __device__ __forceinline__ void put_split(double *work, long long x, double v) {
-  const float hi = d2f(v);
-  reinterpret_cast<float2 *>(work)[x] = make_float2(hi, d2f(v - f2d(hi)));
+  const dfl d = d2df(v);
+  reinterpret_cast<float2 *>(work)[x] = make_float2(d.hi, d.lo);
 }
 
 // Zonal periodicity of one row: pads i = 0 and i = ni+1 (bc_lateral, src/single/s_epic_functions.c:55-59).

@@ -25,6 +25,8 @@ struct epic_model {
   cudaStream_t stream = nullptr;
   char *pool = nullptr;
   size_t pool_bytes = 0;
+  void *fop = nullptr;               // the tensor-core filter's operator tiles, slot table and tensor map
+  uint64_t fop_hash = 0;             // equal for models with the same operator
   bool uploaded = false;
   cudaGraphExec_t run_graph = nullptr;
   bool graph_failed = false;
@@ -306,15 +308,15 @@ size_t model_pool_bytes(const epic_grid &g) {
   return rnd(sizeof(Ctl)) + (n_state3 + n_scratch3) * rnd(n3 * 8) + 3 * rnd(n2 * 8) + rnd((size_t)(g.nj + 3) * (g.nk + 2) * 3 * 8) +
          rnd(ni1 * 8) + 10 * rnd(nj1 * 8) + 3 * rnd(nk1 * 8) + rnd((g.nk + 2) * 8) + rnd((g.k_sponge + 1) * 8) +
          2 * rnd(3 * (g.nj + 2) * 8) + rnd(ntw * 8) + rnd(ntw * 4) + 2 * rnd((g.nj + 1) * 8) + rnd(sizeof(epic::MathTable)) +
-         2 * rnd((size_t)(g.nj + 3) * g.ni * 4) + rnd(32 * sizeof(float2)) + 4096;
+         rnd(32 * sizeof(float2)) + 4096;
 }
 
 }  // namespace
 
 extern "C" int64_t epic_model_bytes(const epic_grid *g, int32_t precision) {
-  (void)precision;   // both forms store the state in binary64
   if (!g || g->ni < 4 || g->nj < 3 || g->nk < 3) return -1;
-  return (int64_t)model_pool_bytes(*g);
+  // both forms store the state in binary64; the mixed ones add the tensor-core filter's operator
+  return (int64_t)(model_pool_bytes(*g) + (epic::filter_operator_wanted(*g, precision) ? epic::filter_operator_bytes(*g) : 0));
 }
 
 extern "C" const char *epic_last_error(void) { return epic::error_buffer(); }
@@ -429,7 +431,6 @@ extern "C" int epic_model_create(const epic_grid *g, int32_t precision, epic_mod
   double *hc = carve<double>(p, 3 * (g->nj + 2)), *vc = carve<double>(p, 3 * (g->nj + 2));
   double *tw = carve<double>(p, T.tw.size());
   float *twf = carve<float>(p, T.tw.size());
-  float *fkh = carve<float>(p, (size_t)(g->nj + 3) * g->ni), *fkv = carve<float>(p, (size_t)(g->nj + 3) * g->ni);
   double *coslat = carve<double>(p, g->nj + 1);
   double *coslat4 = carve<double>(p, g->nj + 1);
   epic::MathTable *lt = carve<epic::MathTable>(p, 1);
@@ -458,15 +459,6 @@ extern "C" int epic_model_create(const epic_grid *g, int32_t precision, epic_mod
   up(tw, T.tw.data(), T.tw.size());
   std::vector<float> twf_host(T.tw.begin(), T.tw.end());
   cudaMemcpyAsync(twf, twf_host.data(), twf_host.size() * sizeof(float), cudaMemcpyHostToDevice, m->stream);
-  std::vector<float> fk_host;
-  if (precision != EPIC_PREC_FP64) {   // circulant kernels of the tensor-core filter
-    fk_host.assign(2 * (size_t)(g->nj + 3) * g->ni, 0.f);
-    epic::fill_filter_kernels(g->ni, g->nj, T.high_lat_h.data(), T.high_lat_pv.data(), L.iadim, fk_host.data(),
-                              fk_host.data() + (size_t)(g->nj + 3) * g->ni);
-    const size_t half = (size_t)(g->nj + 3) * g->ni;
-    cudaMemcpyAsync(fkh, fk_host.data(), half * sizeof(float), cudaMemcpyHostToDevice, m->stream);
-    cudaMemcpyAsync(fkv, fk_host.data() + half, half * sizeof(float), cudaMemcpyHostToDevice, m->stream);
-  }
   // cos of the h-row latitudes with the host libm (t_rad and temp_eq use them)
   std::vector<double> cl(g->nj + 1);
   for (int J = 0; J <= g->nj; J++) cl[J] = cos(g->lat[2 * J + 1] * kDeg);
@@ -494,8 +486,15 @@ extern "C" int epic_model_create(const epic_grid *g, int32_t precision, epic_mod
   d.mn_inv = j1[8];
   d.sgth = sg; d.dsgth = ds; d.dsgth_inv = dsi; d.h_min = hmin; d.t_sponge_inv = tsp;
   d.high_lat_h = hlh; d.high_lat_pv = hlpv; d.h_coef = hc; d.v_coef = vc; d.tw = tw; d.twf = twf;
-  d.fkern_h = precision != EPIC_PREC_FP64 ? fkh : nullptr;
-  d.fkern_v = precision != EPIC_PREC_FP64 ? fkv : nullptr;
+  d.fop_map = nullptr;
+  d.fop_slot = nullptr;
+  if (epic::filter_operator_wanted(*g, precision)) {   // the tensor-core filter's operator tiles
+    const char *why = nullptr;
+    if (epic::filter_operator_create(*g, T.high_lat_h.data(), T.high_lat_pv.data(), L.iadim, m->stream, d, &m->fop, &m->fop_hash, &why)) {
+      epic_model_destroy(m);
+      return set_error(EPIC_ERR_NOMEM, "epic_model_create: %s", why);
+    }
+  }
   epic::filter_kernels_init(g->ni);
   epic::column_kernels_init(g->nk);
   epic::column_acc_kernels_init();
@@ -522,6 +521,7 @@ extern "C" void epic_model_destroy(epic_model *m) {
   if (m->snap_ctl) cudaFreeHost(m->snap_ctl);
   if (m->stream) cudaStreamSynchronize(m->stream);
   if (m->pool) cudaFree(m->pool);
+  if (m->fop) cudaFree(m->fop);
   if (m->stream) cudaStreamDestroy(m->stream);
   delete m;
 }
@@ -852,6 +852,9 @@ extern "C" int epic_batch_create(epic_model *const *members, int32_t n, epic_bat
     d.n2 = std::max(d.n2, m.n2);
     d.n3 = std::max(d.n3, m.n3);
   }
+  // one operator for all: a CTA of the filter serves several members with member 0's tiles
+  d.fop_shared = !d.hetero && d.fop_map != nullptr;
+  for (int i = 1; i < n && d.fop_shared; i++) d.fop_shared = members[i]->fop_hash == members[0]->fop_hash;
   d.batch = b->dev_members;
   d.nbatch = n;
   *out = b;

@@ -401,6 +401,8 @@ __global__ void __launch_bounds__(CT_THREADS) k_set_p2etc(DevModel M, int update
   const int nk = M.nk, ks = M.k_sigma, L = nk + 1;
   const long long n2 = M.n2;
   double *P = sm, *HL = P + 32 * L, *TH = HL + 32 * L, *PP = TH + 32 * L;
+  __shared__ int s_kay[EPIC_MAX_NK + 1];
+  if (update_theta) theta2_intervals(M, s_kay, nullptr);
   const double g = M.grav[2 * c.j + 1];
   if (c.valid)   // stage H2 (in HL until the prefix sum is done) and THETA
     for (int k = c.warp; k <= nk; k += CT_WARPS) {
@@ -474,23 +476,12 @@ __global__ void __launch_bounds__(CT_THREADS) k_set_p2etc(DevModel M, int update
     } else if (k == ks - 1) {
       t2 = .5 * (CT(TH, ks - 1) + CT(TH, ks - 2));
     } else {
-      // linint on the table (sigmatheta[2K+1], THETA(K)), K = nk down to k_sigma-1;
-      // find_place_in_table on ascending x = sigmatheta[2(nk-kay)+1]
-      const int nkay = nk - (ks - 1) + 1;
+      // linint on the table (sigmatheta[2K+1], THETA(K)), K = nk down to k_sigma-1, in the
+      // interval theta2_intervals found for this level
       const double sg = M.sgth[2 * k];
       auto X = [&](int kay) { return M.sgth[2 * (nk - kay) + 1]; };
       auto Y = [&](int kay) { return CT(TH, nk - kay); };
-      int kay;
-      if (fcmp(sg, X(0)) <= 0) kay = 0;
-      else if (fcmp(sg, X(nkay - 1)) >= 0) kay = nkay - 2;
-      else {
-        int il = -1, iu = nkay;
-        while (iu - il > 1) {
-          const int im = (iu + il) >> 1;
-          if (fcmp(sg, X(im)) >= 0) il = im; else iu = im;
-        }
-        kay = il;
-      }
+      const int kay = s_kay[k];
       const double dx = X(kay + 1) - X(kay);
       t2 = Y(kay) + (Y(kay + 1) - Y(kay)) * (sg - X(kay)) / dx;
     }
@@ -618,6 +609,9 @@ __device__ __forceinline__ double layer_p_mixed(const DevModel &M, double top, d
 __global__ void __launch_bounds__(CT_THREADS, 3) k_set_p2etc_mixed(DevModel M, int update_theta, int layers) {
   if (epic_member(M)) return;
   extern __shared__ double sm[];
+  __shared__ int s_kay[EPIC_MAX_NK + 1];
+  __shared__ float s_w[EPIC_MAX_NK + 1];
+  if (update_theta && layers) theta2_intervals(M, s_kay, s_w);
   const ColTile c = col_tile(M);
   const int nk = M.nk, ks = M.k_sigma, L = nk + 1;
   const long long n2 = M.n2;
@@ -717,23 +711,9 @@ __global__ void __launch_bounds__(CT_THREADS, 3) k_set_p2etc_mixed(DevModel M, i
       t2 = f2d((d2f(M.sgth[2 * k]) - fs) / gs);
     } else if (k == ks - 1) {
       t2 = .5 * (CT(TH, ks - 1) + CT(TH, ks - 2));
-    } else {
-      const int nkay = nk - (ks - 1) + 1;
-      const double sg = M.sgth[2 * k];
-      auto X = [&](int kay) { return M.sgth[2 * (nk - kay) + 1]; };
-      auto Y = [&](int kay) { return CT(TH, nk - kay); };
-      int kay;
-      if (fcmp(sg, X(0)) <= 0) kay = 0;
-      else if (fcmp(sg, X(nkay - 1)) >= 0) kay = nkay - 2;
-      else {
-        int il = -1, iu = nkay;
-        while (iu - il > 1) {
-          const int im = (iu + il) >> 1;
-          if (fcmp(sg, X(im)) >= 0) il = im; else iu = im;
-        }
-        kay = il;
-      }
-      t2 = Y(kay) + (Y(kay + 1) - Y(kay)) * (sg - X(kay)) / (X(kay + 1) - X(kay));
+    } else {   // linint in binary32 with the block's interval and weight of this level
+      const float y0 = d2f(CT(TH, nk - s_kay[k])), y1 = d2f(CT(TH, nk - s_kay[k] - 1));
+      t2 = f2d(y0 + (y1 - y0) * s_w[k]);
     }
     M.theta2[x] = t2;
   }

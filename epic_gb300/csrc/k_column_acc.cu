@@ -52,6 +52,9 @@ __device__ __forceinline__ double theta_acc(const DevModel &M, double sg, dfl si
 __global__ void __launch_bounds__(CT_THREADS, 3) k_set_p2etc_acc(DevModel M, int update_theta, int layers) {
   if (epic_member(M)) return;
   extern __shared__ double sm[];
+  __shared__ int s_kay[EPIC_MAX_NK + 1];
+  __shared__ float s_w[EPIC_MAX_NK + 1];
+  if (update_theta && layers) theta2_intervals(M, s_kay, s_w);
   const ColTile c = col_tile(M);
   const int nk = M.nk, ks = M.k_sigma, L = nk + 1;
   const long long n2 = M.n2;
@@ -152,23 +155,10 @@ __global__ void __launch_bounds__(CT_THREADS, 3) k_set_p2etc_acc(DevModel M, int
       t2 = f2d((d2f(M.sgth[2 * k]) - fs) / gs);
     } else if (k == ks - 1) {
       t2 = .5 * (CT(TH, ks - 1) + CT(TH, ks - 2));
-    } else {
-      const int nkay = nk - (ks - 1) + 1;
-      const double sg = M.sgth[2 * k];
-      auto X = [&](int kay) { return M.sgth[2 * (nk - kay) + 1]; };
-      auto Y = [&](int kay) { return CT(TH, nk - kay); };
-      int kay;
-      if (fcmp(sg, X(0)) <= 0) kay = 0;
-      else if (fcmp(sg, X(nkay - 1)) >= 0) kay = nkay - 2;
-      else {
-        int il = -1, iu = nkay;
-        while (iu - il > 1) {
-          const int im = (iu + il) >> 1;
-          if (fcmp(sg, X(im)) >= 0) il = im; else iu = im;
-        }
-        kay = il;
-      }
-      t2 = Y(kay) + (Y(kay + 1) - Y(kay)) * (sg - X(kay)) / (X(kay + 1) - X(kay));
+    } else {   // linint in binary32 with the block's interval and weight of this level (THETA2
+               // feeds the Richardson number alone)
+      const float y0 = d2f(CT(TH, nk - s_kay[k])), y1 = d2f(CT(TH, nk - s_kay[k] - 1));
+      t2 = f2d(y0 + (y1 - y0) * s_w[k]);
     }
     M.theta2[x] = t2;
   }

@@ -315,8 +315,8 @@ struct VarzInterval {
   float2 z0, c2, c3;   // double-float coefficients of the cubic in the distance from the knot
 };
 __device__ __forceinline__ float2 split_df(double v) {
-  const float hi = d2f(v);
-  return make_float2(hi, d2f(v - f2d(hi)));
+  const dfl d = d2df(v);
+  return make_float2(d.hi, d.lo);
 }
 __device__ __forceinline__ void varz_intervals_mixed(const Trip *t, int n, int index, double *knot, VarzInterval *iv) {
   for (int q = threadIdx.x; q < n; q += blockDim.x) {

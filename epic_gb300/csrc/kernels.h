@@ -2,6 +2,7 @@
 #pragma once
 #include <cuda_runtime.h>
 #include "device_common.cuh"
+#include "epic_gb300.h"
 
 namespace epic {
 
@@ -58,6 +59,10 @@ __global__ void k_pgrad_vars_column_acc(DevModel M);
 __global__ void k_gz3_column_acc(DevModel M);   // GZ3 alone (the call before the filtered-GZ copy)
 int column_acc_kernels_init();
 void fill_filter_kernels(int ni, int nj, const double *hl_h, const double *hl_pv, long long iadim, float *fh, float *fv);
+bool filter_operator_wanted(const epic_grid &g, int precision);
+size_t filter_operator_bytes(const epic_grid &g);
+int filter_operator_create(const epic_grid &g, const double *hl_h, const double *hl_pv, long long iadim, cudaStream_t s, DevModel &d,
+                           void **mem, uint64_t *hash, const char **why);
 size_t twiddle_doubles(int ni);
 void fill_twiddles(int ni, double *tw);
 

@@ -205,8 +205,10 @@ int64_t epic_model_device_bytes(const epic_model *m);
  * state, stream and kernels stay there.  No counterpart in the reference. */
 int32_t epic_model_device(const epic_model *m);
 
-/* Bytes of device memory epic_model_create would take for this grid (-1 for a bad grid); for
- * admission by memory budget.  No counterpart in the reference. */
+/* Bytes of device memory epic_model_create would take for this grid and precision form (-1 for
+ * a bad grid): the pool, plus for the mixed forms at ni a multiple of 128 the tensor-core
+ * filter's operator tiles (ni/32 x 32 KB per filtered row); for admission by memory budget.  No
+ * counterpart in the reference. */
 int64_t epic_model_bytes(const epic_grid *grid, int32_t precision);
 
 /*

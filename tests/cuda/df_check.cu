@@ -35,6 +35,35 @@ __global__ void k_check(int n, const float2 *tab, unsigned long long *worst) {
   for (int q = 0; q < 6; q++) atomicMax(worst + q, as_ull(e[q]));   // non-negative doubles order as integers
 }
 
+// d2df and df2d (device_common.cuh) against the FP64-unit formulas they replace, bit for bit:
+// binary64 values of every exponent from 2^-74 to 2^127 with random significands (and every
+// eighth one a binary32 value plus a tie or near-tie residual), and double-floats from products
+// and sums, plus powers of two with a lo of the opposite sign (the binade-below case).
+// Counts the mismatches of each; any at all fails.
+__global__ void k_conv(int n, unsigned long long *bad) {
+  const int t = blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= n) return;
+  const unsigned long long h = (unsigned long long)(uni(t, 7) * 18446744073709551616.0);
+  const unsigned e = 949u + (unsigned)(uni(t, 8) * 202.);
+  unsigned long long bits = ((unsigned long long)(uni(t, 9) < .5) << 63) | ((unsigned long long)e << 52) |
+                            (h & 0x000fffffffffffffull);
+  if ((t & 7) == 0) bits = (bits & ~0x1fffffffull) | (0x10000000ull ^ (h >> 60));   // residual at or near half
+  const double x = __longlong_as_double((long long)bits);
+  const dfl d = d2df(x);
+  const float rh = d2f(x), rl = d2f(x - f2d(rh));
+  if (__float_as_uint(d.hi) != __float_as_uint(rh) || __float_as_uint(d.lo) != __float_as_uint(rl)) atomicAdd(bad, 1ull);
+  const double y = 1e3 * uni(t, 10) + 1e-3;
+  dfl q[4] = {d, cv<dfl>(y) * d, d + cv<dfl>(y), dfl(0.f, 0.f)};
+  // a power of two with lo taking it towards zero
+  const float p2 = ldexpf(1.f, (int)(uni(t, 11) * 200.) - 90), sg = uni(t, 12) < .5 ? 1.f : -1.f;
+  q[3] = dfl(sg * p2, -sg * p2 * (float)(uni(t, 13) * 5.9604644775390625e-08));   // |lo| < ulp(hi)/2
+  for (int m = 0; m < 4; m++) {
+    const double want = f2d(q[m].hi) + f2d(q[m].lo);
+    if (fabs(q[m].hi) < 2.2e-22f || fabs(q[m].hi) > 1.7e38f) continue;   // outside the documented range
+    if (__double_as_longlong(df2d(q[m])) != __double_as_longlong(want)) atomicAdd(bad + 1 + (m == 3), 1ull);
+  }
+}
+
 int main() {
   float2 host_tab[32];
   for (int j = 0; j < 32; j++) {
@@ -50,6 +79,12 @@ int main() {
   const int n = 1 << 22;
   k_check<<<(n + 255) / 256, 256>>>(n, tab, worst);
   if (cudaMemcpy(hw, worst, sizeof(hw), cudaMemcpyDeviceToHost) != cudaSuccess) return 2;
+  unsigned long long *cbad = nullptr, hc[3] = {0, 0, 0};
+  if (cudaMalloc(&cbad, sizeof(hc)) != cudaSuccess) return 2;
+  cudaMemset(cbad, 0, sizeof(hc));
+  k_conv<<<(n + 255) / 256, 256>>>(n, cbad);
+  if (cudaMemcpy(hc, cbad, sizeof(hc), cudaMemcpyDeviceToHost) != cudaSuccess) return 2;
+  printf("d2df mismatches %llu, df2d mismatches %llu (binade below a power of two: %llu) of %d\n", hc[0], hc[1], hc[2], n);
   const char *name[6] = {"mul", "div", "sub (abs / max(a,b))", "exp", "log (abs / max(1,|y|))", "log near 1 (abs)"};
   const double bound[6] = {2e-13, 2e-13, 2e-13, 2e-13, 2e-13, 2e-13};
   int bad = 0;
@@ -59,5 +94,5 @@ int main() {
     printf("%-18s max error %.3e (bound %.0e)\n", name[q], v, bound[q]);
     bad |= !(v < bound[q]);
   }
-  return bad;
+  return bad | (hc[0] + hc[1] + hc[2] != 0);
 }

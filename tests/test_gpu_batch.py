@@ -270,13 +270,15 @@ def test_batch_members_on_one_device(gpu):
     b.sync()
 
 
-def test_halted_member_stops_and_reports(gpu):
+@pytest.mark.parametrize("shape", [(32, 16, 10), (128, 64, 10)], ids=["fft_filter", "tensor_filter"])
+def test_halted_member_stops_and_reports(gpu, shape):
     """A member whose state makes the reference stop (a negative potential temperature in one cell:
     GZ3 not monotonic in store_pgrad_vars, found by the priming call) halts after the step in which
     the error is seen: its state and itime stop changing and every sync reports it, while the other
-    member of the batch keeps stepping."""
+    member of the batch keeps stepping (at 128 x 64 the two share the tensor-core filter's CTAs,
+    which must leave the halted member's planes alone)."""
     from epic_gb300 import Fields
-    members = [_member(90 + q, 1.0, EPIC_PREC_MIXED) for q in range(2)]
+    members = [_member(90 + q, 1.0, EPIC_PREC_MIXED, shape=shape) for q in range(2)]
     ga, f, bad = members[1]
     broken = f.copy()
     broken.theta[10, 5, 5] = -1.0
@@ -288,14 +290,14 @@ def test_halted_member_stops_and_reports(gpu):
         b.sync()
     good = members[0][2]
     g0 = good.download()
-    h0 = Fields(32, 16, 10, f.uv_scheme)
+    h0 = Fields(*shape, f.uv_scheme)
     with pytest.raises(EpicError, match="GZ3 not monotonic"):
         bad.download(h0)
     b.run(2)
     with pytest.raises(EpicError, match="member 1"):
         b.sync()
     g1 = good.download()
-    h1 = Fields(32, 16, 10, f.uv_scheme)
+    h1 = Fields(*shape, f.uv_scheme)
     with pytest.raises(EpicError):
         bad.download(h1)
     assert g1.struct.itime == g0.struct.itime + 2

@@ -1,7 +1,9 @@
 """The integer-pipe binary64 <-> binary32 conversions that the mixed form uses on its state
 (d2f, f2d in epic_gb300/csrc/device_common.cuh) give the hardware conversions' bits: every
 binary32 value, 2^32 hashed binary64 values and every rounding boundary of each binary32
-exponent (tests/cuda/conversions_check.cu, compiled here with nvcc)."""
+exponent (tests/cuda/conversions_check.cu, compiled here with nvcc); and the host's TF32 rounding
+of the tensor-core filter's operator tiles gives cvt.rna.tf32.f32's bits for every finite normal
+binary32 value."""
 import os
 import shutil
 import subprocess
@@ -20,4 +22,4 @@ def test_conversions_bit_exact(gpu, tmp_path):
                     os.path.join(HERE, "cuda", "conversions_check.cu")], check=True)
     r = subprocess.run([exe], capture_output=True, text=True, timeout=300)
     assert r.returncode == 0, r.stdout + r.stderr
-    assert "mismatches d2f=0 f2d=0" in r.stdout
+    assert "mismatches d2f=0 f2d=0 tf32=0" in r.stdout

@@ -1,8 +1,8 @@
 """The zonal filter of whole planes on the tensor cores (k_filter_planes_gemm, the mixed form's
 path for ni a multiple of 128) against the FP64 form's FFT filter: the diagnostics that
 store_diag filters (PV3 from the filtered V, DIV_UV3 from the filtered U and V) after one call
-of the stage on the same state, for one (ni = 128) and two (ni = 256) 128-point output tiles per
-row.  3xTF32 products keep FP32 accuracy, so the two agree to FP32 level (measured on a GB300:
+of the stage on the same state, for one (ni = 128), two (ni = 256) and four (ni = 512) 128-point
+output tiles per row.  3xTF32 products keep FP32 accuracy, so the two agree to FP32 level (measured on a GB300:
 PV3 ~8e-8, DIV_UV3 ~4e-7 relative L2); the bounds leave a factor ~10."""
 import pytest
 
@@ -13,7 +13,7 @@ pytestmark = pytest.mark.gpu
 STORE_DIAG = 16
 
 
-@pytest.mark.parametrize("shape,dt", [((128, 64, 10), 150), ((256, 128, 10), 120)])
+@pytest.mark.parametrize("shape,dt", [((128, 64, 10), 150), ((256, 128, 10), 120), ((512, 256, 10), 60)])
 def test_tensor_core_filter_matches_fp64(gpu, shape, dt):
     ni, nj, nk = shape
     ga, f = hs_setup(HSConfig(ni=ni, nj=nj, nk=nk, dt=dt, seed=5))
