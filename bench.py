@@ -520,7 +520,7 @@ def serving_summary(precision, seed=3, nreq=24):
 
 def ensemble_rate(cfg, nmem, precision, args, torch, rank):
     """Cell-steps/s of one ensemble in a given form (tuned, primed, timed like the headline)."""
-    from epic_gb300 import EPIC_SYNC_DIAGS_ONLY, Batch
+    from epic_gb300 import EPIC_IO_ALL, EPIC_IO_STATE, EPIC_SYNC_DIAGS_ONLY, Batch
     members = _members(cfg, nmem, precision, torch_seed=7 + rank)
     starts = [m.download() for m in members]
     batch = Batch(members)
@@ -612,17 +612,24 @@ def run_gpu_ensemble(args):
     roof = batch_roofline(batch, cfg, nmem, stream, torch, stage=12)
     roof_column = batch_roofline(batch, cfg, nmem, stream, torch, stage=19)
 
-    # end to end: every member's state uploaded from pinned host memory and downloaded, each step
+    # end to end: every member's prognostic state (u, v, the tendency planes, hdry, theta) uploaded
+    # from pinned host memory and downloaded, each step; and, beside it, every array of the state
     hosts = [m.download().copy(pinned=True) for m in members]
     e2e_steps = max(1, min(args.steps, 6))
-    batch.step_host(hosts, 1, groups=E2E_GROUPS)   # first call builds the sub-batch graphs
-    barrier()
-    t0 = time.perf_counter()
-    batch.step_host(hosts, e2e_steps, groups=E2E_GROUPS)
-    torch.cuda.synchronize()
-    e2e_s = (time.perf_counter() - t0) / e2e_steps
+
+    def e2e_run(io):
+        batch.step_host(hosts, 1, groups=E2E_GROUPS, io=io)   # the first call builds the sub-batch graphs
+        barrier()
+        t0 = time.perf_counter()
+        batch.step_host(hosts, e2e_steps, groups=E2E_GROUPS, io=io)
+        torch.cuda.synchronize()
+        return (time.perf_counter() - t0) / e2e_steps
+
+    e2e_s = e2e_run(EPIC_IO_STATE)
     e2e_val = ws * cells / e2e_s
+    e2e_all_s = e2e_run(EPIC_IO_ALL)
     host_bytes = sum(h.nbytes for h in hosts)
+    state_bytes = sum(h.state_nbytes for h in hosts)
     link = host_link_gbs(torch)
     state_gb = sum(m.device_bytes for m in members) / 1e9
     batch.close()
@@ -643,12 +650,17 @@ def run_gpu_ensemble(args):
                                          "update", "column", "pointwise", "row_filter",
                                          "hsu_meridional_form (1 fused march, 2 four passes)"]},
             "clocks": clocks,
-            "e2e": {"value": e2e_val, "unit": "cell-steps/s", "h2d_bytes_per_step": host_bytes, "d2h_bytes_per_step": host_bytes,
+            "e2e": {"value": e2e_val, "unit": "cell-steps/s", "h2d_bytes_per_step": state_bytes, "d2h_bytes_per_step": state_bytes,
                     "ms_per_step": e2e_s * 1e3, "host_link_gbs": link,
-                    "link_bound_ms_per_step": 2e3 * host_bytes / (link["both_directions"] * 1e9) if link.get("both_directions") else None,
-                    "note": "state copied up and down every step in 8 sub-batches on their own streams, copies of one "
-                            "overlapping the kernels of the others; host_link_gbs is one pinned copy of the state's size "
-                            "alone in each direction and both at once on this box"},
+                    "link_bound_ms_per_step": 2e3 * state_bytes / (link["both_directions"] * 1e9) if link.get("both_directions") else None,
+                    "all_arrays": {"value": ws * cells / e2e_all_s, "ms_per_step": e2e_all_s * 1e3, "h2d_bytes_per_step": host_bytes,
+                                   "d2h_bytes_per_step": host_bytes,
+                                   "link_bound_ms_per_step": 2e3 * host_bytes / (link["both_directions"] * 1e9) if link.get("both_directions") else None},
+                    "note": "Batch.step_host with EPIC_IO_STATE: every step uploads each member's prognostic arrays (u, v, the three "
+                            "AB3 tendency planes of each, hdry, theta) from pinned host memory, steps, and downloads them, in 8 "
+                            "sub-batches on their own streams (copies of one overlap the kernels of the others); the diagnostics "
+                            "stay on the device, which recomputes them. all_arrays moves every array of the state each way "
+                            "(EPIC_IO_ALL). host_link_gbs: one pinned copy alone in each direction and both at once on this box"},
             "gpu_launches": launches,
             "roofline": roof,
             "roofline_store_pgrad_vars": roof_column,

@@ -17,7 +17,7 @@ import os
 
 import numpy as np
 
-from .abi import (EPIC_ADV_AKIMA, EPIC_ADV_HSU, EPIC_PREC_FP64, EPIC_PREC_MIXED, EPIC_PREC_MIXED_FAST, EPIC_PROFILE_HS_EQ,
+from .abi import (EPIC_ADV_AKIMA, EPIC_ADV_HSU, EPIC_IO_ALL, EPIC_IO_STATE, EPIC_PREC_FP64, EPIC_PREC_MIXED, EPIC_PREC_MIXED_FAST, EPIC_PROFILE_HS_EQ,
                   EPIC_PROFILE_N2, EPIC_PROFILE_TABLE, EPIC_STEP_PROGS_AND_SYNC_DIAGS, EPIC_SYNC_DIAGS_ONLY, EPIC_UV_AB3, EPIC_UV_LEAPFROG,
                   EpicFields, EpicGrid, EpicHsParams, EpicJetParams, Fields, GridArrays, HSConfig, JetConfig, Layout)
 
@@ -79,7 +79,7 @@ def load_library(path: str | None = None) -> C.CDLL:
     lib.epic_batch_autotune.argtypes = [C.c_void_p, C.c_int32, C.POINTER(C.c_int32)]
     for name in ("epic_batch_upload", "epic_batch_download"):
         getattr(lib, name).argtypes = [C.c_void_p, C.POINTER(C.POINTER(EpicFields))]
-    lib.epic_batch_step_host.argtypes = [C.c_void_p, C.POINTER(C.POINTER(EpicFields)), C.c_int32, C.c_int32]
+    lib.epic_batch_step_host.argtypes = [C.c_void_p, C.POINTER(C.POINTER(EpicFields)), C.c_int32, C.c_int32, C.c_int32]
     for name in ("epic_batch_set_tuning", "epic_model_set_tuning"):
         getattr(lib, name).argtypes = [C.c_void_p, C.POINTER(C.c_int32)]
     lib.epic_hs_grid_build.argtypes = [C.POINTER(EpicHsParams), C.POINTER(EpicGrid), C.POINTER(C.c_double),
@@ -261,9 +261,11 @@ class Batch:
         _check(self.lib.epic_batch_download(self._h, self._ptrs(fields)), "epic_batch_download")
         return fields
 
-    def step_host(self, fields: list[Fields], nsteps: int = 1, groups: int = 4) -> list[Fields]:
-        """End-to-end steps with host-resident (pinned) state, copies overlapped with kernels."""
-        _check(self.lib.epic_batch_step_host(self._h, self._ptrs(fields), groups, nsteps), "epic_batch_step_host")
+    def step_host(self, fields: list[Fields], nsteps: int = 1, groups: int = 4, io: int = 0) -> list[Fields]:
+        """End-to-end steps with host-resident (pinned) state, copies overlapped with kernels.
+        io = EPIC_IO_ALL (0) moves every array each way, EPIC_IO_STATE (1) the prognostic arrays
+        (u, v, dudt, dvdt, hdry, theta) only and leaves the diagnostics on the device."""
+        _check(self.lib.epic_batch_step_host(self._h, self._ptrs(fields), groups, nsteps, io), "epic_batch_step_host")
         return fields
 
     def autotune(self, trial_steps: int = 3) -> list[int]:

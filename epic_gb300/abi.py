@@ -23,6 +23,8 @@ EPIC_ADV_AKIMA = 1
 EPIC_PROFILE_HS_EQ = 0
 EPIC_PROFILE_N2 = 1
 EPIC_PROFILE_TABLE = 2
+EPIC_IO_ALL = 0
+EPIC_IO_STATE = 1
 
 _dp = C.POINTER(C.c_double)
 
@@ -203,6 +205,11 @@ class Fields:
     @property
     def nbytes(self) -> int:
         return int(sum(a.nbytes for a in self.arrays.values()))
+
+    @property
+    def state_nbytes(self) -> int:
+        """Bytes of the prognostic arrays (u, v, dudt, dvdt, hdry, theta): what EPIC_IO_STATE moves."""
+        return int(sum(self.arrays[k].nbytes for k in ("u", "v", "dudt", "dvdt", "hdry", "theta")))
 
     def wind(self, name: str) -> np.ndarray:
         """Current value plane of u or v (grid.it_uv: plane 0 for AB3, IT_ZERO for leapfrog)."""

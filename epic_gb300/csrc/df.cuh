@@ -62,7 +62,12 @@ __device__ __forceinline__ bool operator<=(dfl a, dfl b) { return !(a > b); }
 using ::fabs;   // the binary32/binary64 overloads stay visible beside this one
 __device__ __forceinline__ dfl fabs(dfl a) { return a.hi < 0.f || (a.hi == 0.f && a.lo < 0.f) ? -a : a; }
 
-__device__ __forceinline__ dfl df_ldexp(dfl a, int e) { return dfl(ldexpf(a.hi, e), ldexpf(a.lo, e)); }
+// a 2^e for -126 <= e <= 127: the scale is a normal binary32 power of two, so each part is one
+// exactly rounded multiplication (the value ldexpf gives, without its range handling)
+__device__ __forceinline__ dfl df_ldexp(dfl a, int e) {
+  const float s = __int_as_float((e + 127) << 23);
+  return dfl(a.hi * s, a.lo * s);
+}
 
 // ---- exp and log (relative error ~1e-13 over the arguments the model uses) ----
 //
@@ -85,10 +90,12 @@ __device__ __forceinline__ dfl exp_df(dfl x, const float2 *tab) {
   const float2 t = __ldg(tab + (n & 31));
   return df_ldexp(dfl(t.x, t.y) * p, n >> 5);
 }
-// log: one Newton step y0 + x exp(-y0) - 1 from the binary32 logarithm y0 (quadratic: the
-// error of y0, ~2^-23 |y|, becomes ~2^-47 |y|^2).  x > 0, normal.
+// log: one Newton step y0 + x exp(-y0) - 1 from the hardware's approximate logarithm y0
+// (__logf: lg2.approx times ln 2, absolute error ~1e-7 for arguments near 1 and relative error
+// a few 2^-23 elsewhere); the step is quadratic, so that error leaves ~1e-14.  x > 0 with
+// 2^-120 < x < 2^120 (exp_df's range for -y0).
 __device__ __forceinline__ dfl log_df(dfl x, const float2 *tab) {
-  const float y0 = logf(x.hi);
+  const float y0 = __logf(x.hi);
   const dfl t = x * exp_df(dfl(-y0, 0.f), tab);
   return dfl(y0, 0.f) + (t - dfl(1.f, 0.f));
 }

@@ -543,7 +543,14 @@ bool host_state_packed(const DevModel &d, const double *const *fld) {
   return true;
 }
 
-int enqueue_upload(epic_model *m, const epic_fields *f, cudaStream_t s, Ctl *c, bool with_ctl = true) {
+// Planes of the state region that a copy moves: all of it, or (state_only) the prognostic
+// prefix u, v, dudt, dvdt, hdry, theta -- the arrays a step advances and reads from the step
+// before; the other 18 fields are diagnostics the step recomputes before it reads them (P3's top
+// row and GZ_SURFACE are constants of the run).
+int state_arrays(bool state_only) { return state_only ? 6 : 24; }
+size_t state_planes(const DevModel &d, bool state_only) { return (size_t)(2 * d.nvp + 2 * d.ntp + (state_only ? 2 : 20)); }
+
+int enqueue_upload(epic_model *m, const epic_fields *f, cudaStream_t s, Ctl *c, bool with_ctl = true, bool state_only = false) {
   if (!f->u || !f->v || !f->dudt || !f->dvdt || !f->hdry || !f->theta || !f->p3 || !f->gz_surface || !f->u_spinup)
     return set_error(EPIC_ERR_ARG, "epic_model_upload: a required field pointer is NULL");
   DevModel &d = m->d;
@@ -553,12 +560,13 @@ int enqueue_upload(epic_model *m, const epic_fields *f, cudaStream_t s, Ctl *c, 
   double *dst[] = {d.u, d.v, d.dudt, d.dvdt, d.hdry, d.theta, d.p3, d.h3, d.p2, d.theta2, d.t2, d.t3, d.rho2,
                    d.rho3, d.exner3, d.gz3, d.mont3, d.heat3, d.pv3, d.ri2, d.div_uv3, d.w3, d.dzdt3, d.u_spinup};
   if (host_state_packed(d, src)) {
-    EPIC_CUDA_CHECK(cudaMemcpyAsync(d.u, f->u, (size_t)(2 * d.nvp + 2 * d.ntp + 20) * b3, cudaMemcpyHostToDevice, s));
+    EPIC_CUDA_CHECK(cudaMemcpyAsync(d.u, f->u, state_planes(d, state_only) * b3, cudaMemcpyHostToDevice, s));
   } else {
-    for (int i = 0; i < 24; i++)
+    for (int i = 0; i < state_arrays(state_only); i++)
       if (src[i]) EPIC_CUDA_CHECK(cudaMemcpyAsync(dst[i], src[i], (i < 2 ? d.nvp : (i < 4 ? d.ntp : 1)) * b3, cudaMemcpyHostToDevice, s));
   }
-  EPIC_CUDA_CHECK(cudaMemcpyAsync(d.gz_surface, f->gz_surface, (size_t)d.n2 * sizeof(double), cudaMemcpyHostToDevice, s));
+  if (!state_only)
+    EPIC_CUDA_CHECK(cudaMemcpyAsync(d.gz_surface, f->gz_surface, (size_t)d.n2 * sizeof(double), cudaMemcpyHostToDevice, s));
   if (!with_ctl) return EPIC_OK;
   memset(c, 0, sizeof(*c));
   c->it_zero = f->it_zero; c->it_minus1 = f->it_minus1; c->it_minus2 = f->it_minus2;
@@ -577,7 +585,7 @@ int enqueue_upload(epic_model *m, const epic_fields *f, cudaStream_t s, Ctl *c, 
 }
 
 // The copies of epic_model_download, enqueued on stream s; *c receives the control block.
-int enqueue_download(epic_model *m, epic_fields *f, cudaStream_t s, Ctl *c) {
+int enqueue_download(epic_model *m, epic_fields *f, cudaStream_t s, Ctl *c, bool state_only = false) {
   DevModel &d = m->d;
   const size_t b3 = (size_t)d.n3 * sizeof(double);
   double *dst[] = {f->u, f->v, f->dudt, f->dvdt, f->hdry, f->theta, f->p3, f->h3, f->p2, f->theta2, f->t2, f->t3, f->rho2,
@@ -585,12 +593,12 @@ int enqueue_download(epic_model *m, epic_fields *f, cudaStream_t s, Ctl *c) {
   const double *src[] = {d.u, d.v, d.dudt, d.dvdt, d.hdry, d.theta, d.p3, d.h3, d.p2, d.theta2, d.t2, d.t3, d.rho2,
                          d.rho3, d.exner3, d.gz3, d.mont3, d.heat3, d.pv3, d.ri2, d.div_uv3, d.w3, d.dzdt3, d.u_spinup};
   if (host_state_packed(d, dst)) {
-    EPIC_CUDA_CHECK(cudaMemcpyAsync(f->u, d.u, (size_t)(2 * d.nvp + 2 * d.ntp + 20) * b3, cudaMemcpyDeviceToHost, s));
+    EPIC_CUDA_CHECK(cudaMemcpyAsync(f->u, d.u, state_planes(d, state_only) * b3, cudaMemcpyDeviceToHost, s));
   } else {
-    for (int i = 0; i < 24; i++)
+    for (int i = 0; i < state_arrays(state_only); i++)
       if (dst[i]) EPIC_CUDA_CHECK(cudaMemcpyAsync(dst[i], src[i], (i < 2 ? d.nvp : (i < 4 ? d.ntp : 1)) * b3, cudaMemcpyDeviceToHost, s));
   }
-  if (f->gz_surface) EPIC_CUDA_CHECK(cudaMemcpyAsync(f->gz_surface, d.gz_surface, (size_t)d.n2 * sizeof(double), cudaMemcpyDeviceToHost, s));
+  if (f->gz_surface && !state_only) EPIC_CUDA_CHECK(cudaMemcpyAsync(f->gz_surface, d.gz_surface, (size_t)d.n2 * sizeof(double), cudaMemcpyDeviceToHost, s));
   EPIC_CUDA_CHECK(cudaMemcpyAsync(c, d.ctl, sizeof(Ctl), cudaMemcpyDeviceToHost, s));
   return EPIC_OK;
 }
@@ -1143,8 +1151,14 @@ extern "C" int epic_model_snapshot_wait(epic_model *m) {
 // sub-batches, each with its own stream and captured graph, so one group's copies overlap the
 // others' kernels and the two copy directions overlap each other.
 
-extern "C" int epic_batch_step_host(epic_batch *b, epic_fields *const *f, int32_t groups, int32_t nsteps) {
+extern "C" int epic_batch_step_host(epic_batch *b, epic_fields *const *f, int32_t groups, int32_t nsteps, int32_t io) {
   if (!b || !f) return set_error(EPIC_ERR_ARG, "epic_batch_step_host: NULL argument");
+  if (io != EPIC_IO_ALL && io != EPIC_IO_STATE) return set_error(EPIC_ERR_ARG, "epic_batch_step_host: io=%d", io);
+  const bool state_only = io == EPIC_IO_STATE;
+  if (state_only)
+    for (size_t i = 0; i < b->members.size(); i++)
+      if (!b->members[i]->uploaded)
+        return set_error(EPIC_ERR_STATE, "epic_batch_step_host: member %zu has no state on the device (EPIC_IO_STATE moves the prognostic arrays only)", i);
   const int n = (int)b->members.size();
   if (groups < 1) groups = 1;
   if (groups > n) groups = n;
@@ -1179,7 +1193,7 @@ extern "C" int epic_batch_step_host(epic_batch *b, epic_fields *const *f, int32_
       for (auto *m : g->members) {
         // after the first step the host arrays hold exactly what the device state was, and the
         // device's control block (time-plane indices, itime) is already the one they belong to
-        int rc = enqueue_upload(m, f[idx], g->stream, &ctl[2 * idx], step == 0);
+        int rc = enqueue_upload(m, f[idx], g->stream, &ctl[2 * idx], step == 0, state_only);
         if (rc) return rc;
         m->uploaded = true;
         idx++;
@@ -1195,7 +1209,7 @@ extern "C" int epic_batch_step_host(epic_batch *b, epic_fields *const *f, int32_
         if (rc) return rc;
       }
       for (int q = lo; q < idx; q++) {
-        int rc = enqueue_download(b->members[q], f[q], g->stream, &ctl[2 * q + 1]);
+        int rc = enqueue_download(b->members[q], f[q], g->stream, &ctl[2 * q + 1], state_only);
         if (rc) return rc;
       }
     }

@@ -256,8 +256,15 @@ int  epic_batch_download(epic_batch *b, epic_fields *const *f);
  * be pinned host memory; when a member's 3-D arrays sit back to back in the order u, v, dudt,
  * dvdt, hdry, theta, p3, h3, p2, theta2, t2, t3, rho2, rho3, exner3, gz3, mont3, heat3, pv3, ri2,
  * div_uv3, w3, dzdt3, u_spinup, its state moves with one copy each way (any layout works).
+ * io = EPIC_IO_ALL moves every array (and GZ_SURFACE) each way; EPIC_IO_STATE moves the
+ * prognostic arrays u, v, dudt, dvdt, hdry, theta only -- what a step advances and carries from
+ * the step before -- and leaves the diagnostic fields on the device, which recomputes them from
+ * those (every member must have been uploaded; epic_batch_download fetches the diagnostics when
+ * they are wanted, e.g. before a save).
  */
-int  epic_batch_step_host(epic_batch *b, epic_fields *const *f, int32_t groups, int32_t nsteps);
+#define EPIC_IO_ALL   0
+#define EPIC_IO_STATE 1
+int  epic_batch_step_host(epic_batch *b, epic_fields *const *f, int32_t groups, int32_t nsteps, int32_t io);
 int  epic_batch_sync(epic_batch *b);                       /* wait; first member error, if any */
 int  epic_batch_query(epic_batch *b);   /* 1: work queued on the batch finished, 0: still running */
 void *epic_batch_stream(epic_batch *b);

@@ -3,7 +3,7 @@ exactly the bits it gets when stepped alone, in both precision forms."""
 import numpy as np
 import pytest
 
-from epic_gb300 import (EPIC_ADV_AKIMA, EPIC_PREC_FP64, EPIC_PREC_MIXED, EPIC_PREC_MIXED_FAST, EPIC_SYNC_DIAGS_ONLY, EPIC_UV_AB3, EPIC_UV_LEAPFROG, Batch,
+from epic_gb300 import (EPIC_ADV_AKIMA, EPIC_IO_ALL, EPIC_IO_STATE, EPIC_PREC_FP64, EPIC_PREC_MIXED, EPIC_PREC_MIXED_FAST, EPIC_SYNC_DIAGS_ONLY, EPIC_UV_AB3, EPIC_UV_LEAPFROG, Batch,
                         EpicError, HSConfig, Model, hs_setup)
 
 pytestmark = pytest.mark.gpu
@@ -171,17 +171,24 @@ def test_batch_upload_download_match_members(gpu):
         assert g.struct.itime == w.struct.itime
 
 
+PROGNOSTIC = ("u", "v", "dudt", "dvdt", "hdry", "theta")
+
+
+@pytest.mark.parametrize("io", [EPIC_IO_ALL, EPIC_IO_STATE], ids=["all", "state"])
 @pytest.mark.parametrize("groups", [1, 2, 3])
-def test_batch_step_host_pipeline(gpu, groups):
+def test_batch_step_host_pipeline(gpu, groups, io):
     """The pipelined end-to-end step (host-resident state, sub-batches on their own streams)
-    gives every member the bits it gets stepped alone."""
+    gives every member the bits it gets stepped alone: every array with EPIC_IO_ALL; with
+    EPIC_IO_STATE the prognostic arrays that move each step, and the diagnostics left on the
+    device once they are downloaded."""
     members = [_member(60 + q, 1.0 - 0.04 * q, EPIC_PREC_MIXED) for q in range(3)]
     b = Batch([m for _, _, m in members])
     b.timestep(EPIC_SYNC_DIAGS_ONLY)
     b.sync()
     hosts = [m.download().copy(pinned=True) for _, _, m in members]
-    b.step_host(hosts, 4, groups=groups)
-    for (ga, f, _), h in zip(members, hosts):
+    b.step_host(hosts, 4, groups=groups, io=io)
+    diags = [m.download() for _, _, m in members]
+    for (ga, f, _), h, dg in zip(members, hosts, diags):
         alone = Model(ga, EPIC_PREC_MIXED)
         alone.upload(f)
         alone.timestep(EPIC_SYNC_DIAGS_ONLY)
@@ -189,8 +196,18 @@ def test_batch_step_host_pipeline(gpu, groups):
         alone.sync()
         w = alone.download()
         for k in w.arrays:
-            assert np.array_equal(h.arrays[k], w.arrays[k]), (groups, k)
+            got = h.arrays[k] if io == EPIC_IO_ALL or k in PROGNOSTIC else dg.arrays[k]
+            assert np.array_equal(got, w.arrays[k]), (groups, k)
         assert h.struct.itime == w.struct.itime
+
+
+def test_state_io_needs_uploaded_members(gpu):
+    """EPIC_IO_STATE moves the prognostic arrays only, so it refuses members with no state."""
+    ga, f = hs_setup(HSConfig(ni=32, nj=16, nk=10, dt=300, seed=3))
+    fresh = Model(ga, EPIC_PREC_MIXED)
+    b = Batch([fresh])
+    with pytest.raises(EpicError, match="no state on the device"):
+        b.step_host([f.copy(pinned=True)], 1, groups=1, io=EPIC_IO_STATE)
 
 
 # 26 members of 128x64x20: the UNITY and HDRY passes of the meridional Hsu advection cover
