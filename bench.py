@@ -520,7 +520,7 @@ def serving_summary(precision, seed=3, nreq=24):
 
 def ensemble_rate(cfg, nmem, precision, args, torch, rank):
     """Cell-steps/s of one ensemble in a given form (tuned, primed, timed like the headline)."""
-    from epic_gb300 import EPIC_IO_ALL, EPIC_IO_STATE, EPIC_SYNC_DIAGS_ONLY, Batch
+    from epic_gb300 import EPIC_SYNC_DIAGS_ONLY, Batch
     members = _members(cfg, nmem, precision, torch_seed=7 + rank)
     starts = [m.download() for m in members]
     batch = Batch(members)
@@ -551,7 +551,7 @@ def ensemble_rate(cfg, nmem, precision, args, torch, rank):
 
 def run_gpu_ensemble(args):
     import torch
-    from epic_gb300 import EPIC_PREC_FP64, EPIC_PREC_MIXED, EPIC_SYNC_DIAGS_ONLY, Batch
+    from epic_gb300 import EPIC_IO_ALL, EPIC_IO_STATE, EPIC_PREC_FP64, EPIC_PREC_MIXED, EPIC_SYNC_DIAGS_ONLY, Batch
     ws, rank, local = _dist()
     torch.cuda.set_device(local)
     if ws > 1:
