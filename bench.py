@@ -502,14 +502,20 @@ def cfg2_error(precision, steps=240):
     return out
 
 
-def serving_summary(precision, seed=3, nreq=24):
-    """The serving loop on a seeded Poisson stream (20 requests/s) of Held-Suarez runs of the shapes
-    of SERVE_SHAPES, each lasting U[0.25, 2] simulated days."""
+def serving_summary(precision, seed=3, nreq=24, jet_frac=0.0):
+    """The serving loop on a seeded Poisson stream (20 requests/s) of runs of the shapes of
+    SERVE_SHAPES, each lasting U[0.25, 2] simulated days: Held-Suarez runs, and a fraction
+    jet_frac of zonal-jet runs (dt 60 s)."""
     from epic_gb300.serving import RunServer, latency_summary, poisson_requests
-    reqs = poisson_requests(nreq, 20.0, seed, sorted(SERVE_SHAPES), dt_of=lambda s: SERVE_SHAPES[s], days_range=(0.25, 2.0))
+    reqs = poisson_requests(nreq, 20.0, seed, sorted(SERVE_SHAPES), dt_of=lambda s: SERVE_SHAPES[s], days_range=(0.25, 2.0),
+                            jet_frac=jet_frac, jet_dt_of=lambda s: 60)
     res = RunServer(hbm_budget=40 << 30, precision=precision, round_steps=16).serve(reqs)
     out = latency_summary(res)
-    out.update({"arrivals": "Poisson, 20 requests/s, seed 3", "states": "Held-Suarez column at rest with seeded theta noise",
+    states = "Held-Suarez column at rest with seeded theta noise"
+    if jet_frac > 0.0:
+        states += (f"; {sum(r.cfg.state == 'jet' for r in reqs)} of the {nreq} requests in the balanced zonal-jet state on "
+                   "the constant-N^2 sounding at dt 60 s")
+    out.update({"arrivals": f"Poisson, 20 requests/s, seed {seed}", "states": states,
                 "shapes": [list(k) + [v] for k, v in sorted(SERVE_SHAPES.items())],
                 "durations": "uniform 0.25-2 simulated days (steps = days * 86400 / dt)", "hbm_budget_gb": 40,
                 "batching": "runs of one launch class (layers, schemes, form, filter path) share a batch, sizes and dt may differ",
@@ -687,6 +693,7 @@ def run_gpu_ensemble(args):
                                          ensemble_error=ensemble_error(torch, _prec("fast"), cfg, nmem),
                                          note="EPIC_PREC_MIXED_FAST ensemble, same workload and timing")
             out["serving"] = serving_summary(precision)
+            out["serving_with_jets"] = serving_summary(precision, seed=11, jet_frac=0.5)
     if ws > 1:
         import torch.distributed as dist
         dist.barrier()

@@ -132,7 +132,7 @@ class RunServer:
     round_steps: int = 16                # most steps a class advances per scheduling pass
     keep_fields: bool = False            # keep each result's full state (else a checksum)
     size_ratio: int = 16                 # runs share a batch only in one power of this in cells (0: any)
-    allow_jets: bool = False             # serve jet-state requests (see submit)
+    allow_jets: bool = True              # serve jet-state requests (a server may refuse them)
     backend: object = field(default_factory=DeviceBackend)
     waiting: list = field(default_factory=list)
     prepared: dict = field(default_factory=dict)    # rid -> (grid, initial fields, device bytes)
