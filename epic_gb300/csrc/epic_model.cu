@@ -26,6 +26,7 @@ struct epic_model {
   char *pool = nullptr;
   size_t pool_bytes = 0;
   void *fop = nullptr;               // the tensor-core filter's operator tiles, slot table and tensor map
+                                     // (shared by the models of one grid on one device)
   uint64_t fop_hash = 0;             // equal for models with the same operator
   bool uploaded = false;
   cudaGraphExec_t run_graph = nullptr;
@@ -521,7 +522,7 @@ extern "C" void epic_model_destroy(epic_model *m) {
   if (m->snap_ctl) cudaFreeHost(m->snap_ctl);
   if (m->stream) cudaStreamSynchronize(m->stream);
   if (m->pool) cudaFree(m->pool);
-  if (m->fop) cudaFree(m->fop);
+  if (m->fop) epic::filter_operator_release(m->fop);
   if (m->stream) cudaStreamDestroy(m->stream);
   delete m;
 }

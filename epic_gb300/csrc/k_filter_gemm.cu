@@ -36,6 +36,7 @@
 // and returns.
 #include <cmath>
 #include <cstring>
+#include <mutex>
 #include <vector>
 #include <cuda.h>
 #include <cudaTypedefs.h>
@@ -427,7 +428,36 @@ size_t filter_operator_bytes(const epic_grid &g) {
 // ((s ni/32 + t) 2 + h) 128.  They are copied into one device allocation with the slot table and
 // the TMA tensor map that describes them (2-D: 32 FP32 per row, boxes of 32 x 128 with the
 // 128-byte swizzle of the kernel's operand layout).  hash identifies the operator (equal hashes:
-// the same tiles), so that a batch of one grid lets its members share member 0's copy.
+// the same tiles): models of one grid on one device share one allocation (released by
+// filter_operator_release when its last model goes), and a batch of them filters with member 0's.
+namespace {
+// Operators are shared between the models of one grid on one device: a process-wide table of the
+// allocations, keyed by device and hash, counted by the models that use them.
+struct OperatorCopy {
+  int device;
+  uint64_t hash;
+  void *base;
+  const void *map;
+  const int *slot;
+  int users;
+};
+std::mutex g_op_mu;
+std::vector<OperatorCopy> g_ops;
+}  // namespace
+
+void filter_operator_release(void *mem) {
+  if (!mem) return;
+  std::lock_guard<std::mutex> lock(g_op_mu);
+  for (size_t q = 0; q < g_ops.size(); q++)
+    if (g_ops[q].base == mem) {
+      if (--g_ops[q].users == 0) {
+        cudaFree(g_ops[q].base);
+        g_ops.erase(g_ops.begin() + (long)q);
+      }
+      return;
+    }
+}
+
 int filter_operator_create(const epic_grid &g, const double *hl_h, const double *hl_pv, long long iadim, cudaStream_t s, DevModel &d,
                            void **mem, uint64_t *hash, const char **why) {
   *mem = nullptr;
@@ -436,6 +466,27 @@ int filter_operator_create(const epic_grid &g, const double *hl_h, const double 
   const int nslots = filter_slots(g, slot);
   std::vector<float> fh((size_t)(g.nj + 3) * ni), fv((size_t)(g.nj + 3) * ni);
   fill_filter_kernels(ni, g.nj, hl_h, hl_pv, iadim, fh.data(), fv.data());
+  uint64_t hs = 1469598103934665603ull;   // FNV-1a over everything the tiles are made of
+  auto mix = [&](const void *p, size_t n) {
+    const unsigned char *c = static_cast<const unsigned char *>(p);
+    for (size_t q = 0; q < n; q++) hs = (hs ^ c[q]) * 1099511628211ull;
+  };
+  mix(&ni, sizeof ni);
+  mix(slot.data(), slot.size() * sizeof(int));
+  mix(fh.data(), fh.size() * sizeof(float));
+  mix(fv.data(), fv.size() * sizeof(float));
+  *hash = hs;
+  int device = -1;
+  cudaGetDevice(&device);
+  std::lock_guard<std::mutex> lock(g_op_mu);
+  for (auto &c : g_ops)
+    if (c.device == device && c.hash == hs) {   // a model of the same grid made it already
+      c.users++;
+      d.fop_map = c.map;
+      d.fop_slot = c.slot;
+      *mem = c.base;
+      return 0;
+    }
   const size_t tile_floats = (size_t)FG_M * FG_KC;
   std::vector<float> tiles((size_t)(nslots > 0 ? nslots : 1) * ntiles * 2 * tile_floats, 0.f);
   for (int gr = 0; gr < 2; gr++)
@@ -453,17 +504,6 @@ int filter_operator_create(const epic_grid &g, const double *hl_h, const double 
           }
       }
     }
-  uint64_t hs = 1469598103934665603ull;
-  auto mix = [&](const void *p, size_t n) {
-    const unsigned char *c = static_cast<const unsigned char *>(p);
-    for (size_t q = 0; q < n; q++) hs = (hs ^ c[q]) * 1099511628211ull;
-  };
-  mix(&ni, sizeof ni);
-  mix(slot.data(), slot.size() * sizeof(int));
-  mix(fh.data(), fh.size() * sizeof(float));
-  mix(fv.data(), fv.size() * sizeof(float));
-  *hash = hs;
-
   const size_t tile_bytes = tiles.size() * sizeof(float), slot_bytes = ((slot.size() * sizeof(int) + 255) / 256) * 256;
   char *base = nullptr;
   if (cudaMalloc(&base, tile_bytes + 1024 + slot_bytes + 256) != cudaSuccess) {
@@ -509,6 +549,7 @@ int filter_operator_create(const epic_grid &g, const double *hl_h, const double 
   d.fop_map = map_d;
   d.fop_slot = slot_d;
   *mem = base;
+  g_ops.push_back({device, hs, base, map_d, slot_d, 1});
   return 0;
 }
 

@@ -63,6 +63,7 @@ bool filter_operator_wanted(const epic_grid &g, int precision);
 size_t filter_operator_bytes(const epic_grid &g);
 int filter_operator_create(const epic_grid &g, const double *hl_h, const double *hl_pv, long long iadim, cudaStream_t s, DevModel &d,
                            void **mem, uint64_t *hash, const char **why);
+void filter_operator_release(void *mem);
 size_t twiddle_doubles(int ni);
 void fill_twiddles(int ni, double *tw);
 
