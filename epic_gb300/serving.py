@@ -292,4 +292,6 @@ def latency_summary(results: list[RunResult]) -> dict:
     cells = sum(r.shape[0] * r.shape[1] * r.shape[2] * r.steps for r in done)
     return {"requests": len(results), "completed": len(done), "ended_by_model_error": len(results) - len(done),
             "p50_s": float(np.percentile(lat, 50)), "p99_s": float(np.percentile(lat, 99)),
-            "makespan_s": makespan, "aggregate_cell_steps_per_s": cells / makespan}
+            "makespan_s": makespan, "aggregate_cell_steps_per_s": cells / makespan,
+            "errors": [{"rid": r.rid, "shape": list(r.shape), "steps": r.steps, "error": (r.error or "")[-160:]}
+                       for r in results if r.error is not None]}
