@@ -502,6 +502,40 @@ def cfg2_error(precision, steps=240):
     return out
 
 
+def serving_accuracy(reqs, res, precision, max_runs=6, max_ni=128):
+    """The mixed form's error against FP64 on the stream's own requests: the first `max_runs`
+    completed requests with ni <= max_ni, each run alone in both forms for its steps (a served run
+    equals itself run alone bit for bit, tests/test_gpu_serving.py); relative L2 over interior
+    cells per prognostic, the largest over those runs."""
+    sys.path.insert(0, os.path.join(ROOT, "tests"))
+    from compare import PROGNOSTIC, field_errors
+    from epic_gb300 import EPIC_PREC_FP64, EPIC_SYNC_DIAGS_ONLY, Model, hs_setup
+    done = {r.rid for r in res if r.error is None}
+    picked = [q for q in reqs if q.rid in done and q.cfg.ni <= max_ni][:max_runs]
+    worst = {k: 0.0 for k in PROGNOSTIC}
+    runs = []
+    for q in picked:
+        ga, f = hs_setup(q.cfg)
+        ga.struct.hs_kf *= q.kf_scale
+        out = []
+        for prec in (EPIC_PREC_FP64, precision):
+            m = Model(ga, prec)
+            m.upload(f)
+            m.timestep(EPIC_SYNC_DIAGS_ONLY)
+            m.run(q.steps)
+            m.sync()
+            out.append(m.download())
+            m.close()
+        e = {k: v[0] for k, v in field_errors(out[1], out[0], PROGNOSTIC).items()}
+        runs.append({"rid": q.rid, "shape": [q.cfg.ni, q.cfg.nj, q.cfg.nk], "state": q.cfg.state, "steps": q.steps,
+                     "days": q.steps * q.cfg.dt / 86400.0, "rel_l2": e})
+        for k in worst:
+            worst[k] = max(worst[k], e[k])
+    return {"max_rel_l2": worst, "runs": runs,
+            "case": f"the first {len(picked)} completed requests with ni <= {max_ni}, each run alone in FP64 and the "
+                    "mixed form for its whole duration; relative L2 over interior cells vs FP64"}
+
+
 def serving_summary(precision, seed=3, nreq=24, jet_frac=0.0):
     """The serving loop on a seeded Poisson stream (20 requests/s) of runs of the shapes of
     SERVE_SHAPES, each lasting U[0.25, 2] simulated days: Held-Suarez runs, and a fraction
@@ -511,6 +545,7 @@ def serving_summary(precision, seed=3, nreq=24, jet_frac=0.0):
                             jet_frac=jet_frac, jet_dt_of=lambda s: 60)
     res = RunServer(hbm_budget=40 << 30, precision=precision, round_steps=16).serve(reqs)
     out = latency_summary(res)
+    out["accuracy"] = serving_accuracy(reqs, res, precision)
     states = "Held-Suarez column at rest with seeded theta noise"
     if jet_frac > 0.0:
         states += (f"; {sum(r.cfg.state == 'jet' for r in reqs)} of the {nreq} requests in the balanced zonal-jet state on "

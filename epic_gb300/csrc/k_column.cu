@@ -606,7 +606,7 @@ __device__ __forceinline__ double layer_p_mixed(const DevModel &M, double top, d
 
 // layers = 0: P3 and HDRY only (the call inside advection, whose P2 and H3 stage 11 rewrites
 // before anything reads them)
-__global__ void __launch_bounds__(CT_THREADS, 3) k_set_p2etc_mixed(DevModel M, int update_theta, int layers) {
+__global__ void __launch_bounds__(CT_THREADS, 4) k_set_p2etc_mixed(DevModel M, int update_theta, int layers) {
   if (epic_member(M)) return;
   extern __shared__ double sm[];
   __shared__ int s_kay[EPIC_MAX_NK + 1];
@@ -723,7 +723,7 @@ __global__ void __launch_bounds__(CT_THREADS, 3) k_set_p2etc_mixed(DevModel M, i
 // copy; that call's T3, EXNER3, RHO3, T2, RHO2, MONT3 and DZDT3 are rewritten by the call after
 // set_p2etc (stage 19) before anything reads them, and that call reads this GZ3 as the old one.
 template <bool FULL>
-__global__ void __launch_bounds__(CT_THREADS, 3) k_pgrad_vars_column_mixed(DevModel M) {
+__global__ void __launch_bounds__(CT_THREADS, 4) k_pgrad_vars_column_mixed(DevModel M) {
   if (epic_member(M)) return;
   extern __shared__ double sm[];
   __shared__ double s_rho2_1[32];

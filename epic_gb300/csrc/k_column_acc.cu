@@ -49,7 +49,7 @@ __device__ __forceinline__ double theta_acc(const DevModel &M, double sg, dfl si
 
 // layers = 0: only P3, HDRY and the interfaces' logarithms (lp3) -- the call inside advection,
 // whose P2, H3 and THETA2 stage 11 recomputes before anything reads them.
-__global__ void __launch_bounds__(CT_THREADS, 3) k_set_p2etc_acc(DevModel M, int update_theta, int layers) {
+__global__ void __launch_bounds__(CT_THREADS, 4) k_set_p2etc_acc(DevModel M, int update_theta, int layers) {
   if (epic_member(M)) return;
   extern __shared__ double sm[];
   __shared__ int s_kay[EPIC_MAX_NK + 1];
@@ -298,11 +298,11 @@ __device__ __forceinline__ void pgrad_vars_column_acc(DevModel &M) {
   }
 }
 
-__global__ void __launch_bounds__(CT_THREADS, 3) k_pgrad_vars_column_acc(DevModel M) {
+__global__ void __launch_bounds__(CT_THREADS, 4) k_pgrad_vars_column_acc(DevModel M) {
   if (epic_member(M)) return;
   pgrad_vars_column_acc<true>(M);
 }
-__global__ void __launch_bounds__(CT_THREADS, 3) k_gz3_column_acc(DevModel M) {
+__global__ void __launch_bounds__(CT_THREADS, 4) k_gz3_column_acc(DevModel M) {
   if (epic_member(M)) return;
   pgrad_vars_column_acc<false>(M);
 }
