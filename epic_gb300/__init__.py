@@ -114,6 +114,7 @@ def hs_setup(cfg: HSConfig) -> tuple[GridArrays, Fields]:
     dp = C.POINTER(C.c_double)
     _check(lib.epic_hs_grid_build(C.byref(p), C.byref(ga.struct), ga.p_ref.ctypes.data_as(dp),
                                   ga.theta_ref.ctypes.data_as(dp)), "epic_hs_grid_build")
+    ga.struct.gas_giant = int(cfg.gas_giant)
     f = Fields(cfg.ni, cfg.nj, cfg.nk, cfg.uv_scheme)
     if cfg.state == "jet":
         jp = cfg.jet.params()

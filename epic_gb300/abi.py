@@ -34,7 +34,7 @@ class EpicGrid(C.Structure):
         ("ni", C.c_int32), ("nj", C.c_int32), ("nk", C.c_int32), ("dt", C.c_int32),
         ("uv_scheme", C.c_int32), ("k_sigma", C.c_int32), ("k_sponge", C.c_int32),
         ("newt_cool_on", C.c_int32), ("newt_cool_adjust", C.c_int32), ("drag_v", C.c_int32),
-        ("drag_zonal_avg", C.c_int32), ("jtp", C.c_int32), ("advection_scheme", C.c_int32), ("pad1", C.c_int32),
+        ("drag_zonal_avg", C.c_int32), ("jtp", C.c_int32), ("advection_scheme", C.c_int32), ("gas_giant", C.c_int32),
         ("dln", C.c_double), ("dlt", C.c_double), ("dy0", C.c_double),
         ("globe_latbot", C.c_double), ("globe_lattop", C.c_double), ("press0", C.c_double),
         ("topo_scale", C.c_double), ("prandtl", C.c_double), ("tau_drag", C.c_double),
@@ -275,6 +275,9 @@ class HSConfig:
     # EPIC_PROFILE_TABLE: the sounding as (pressures [Pa], temperatures [K]), e.g. the reference's
     # t_vs_p.held_suarez (tests/golden/sounding/t_vs_p_held_suarez.npz)
     table: tuple | None = None
+    # the gas-giant lower boundary: GZ_SURFACE from gradient balance with the bottom layer's
+    # zonal-mean U in every store_pgrad_vars (planet->type "gas-giant"), instead of the terrain
+    gas_giant: bool = False
     extra: dict = field(default_factory=dict)
 
     def params(self) -> EpicHsParams:

@@ -72,6 +72,8 @@ struct DevModel {
   const float2 *exp2tab;                    // 2^(j/32), j = 0..31, as double-floats (exp_df)
   float2 dfc[DFC_COUNT];                    // kappa, 1/kappa, kappa+1, the hybrid-coordinate constants
                                             // and log(press0) as double-floats (hi, lo)
+  int gas_giant;                            // planet->type "gas-giant": GZ_SURFACE from gz_from_u in store_pgrad_vars
+  int jtp;                                  // grid.jtp: the row where gz_from_u puts GZ_SURFACE's zero
   int mixed;                                // FP32 stencils, advection, hyperviscosity, filter, physics
   int col64;                                // mixed, with the vertical pressure/geopotential integration
                                             // (set_p2etc, store_pgrad_vars) and the pressure gradient in FP64

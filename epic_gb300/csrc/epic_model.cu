@@ -329,6 +329,8 @@ extern "C" int epic_model_create(const epic_grid *g, int32_t precision, epic_mod
     return set_error(EPIC_ERR_ARG, "precision form %d not available", precision);
   if (g->ni < 4 || (g->ni & (g->ni - 1)) || g->ni > EPIC_MAX_NI) return set_error(EPIC_ERR_ARG, "ni=%d: need a power of 2 in [4,%d]", g->ni, EPIC_MAX_NI);
   if (g->nj < 3 || g->nk < 3 || g->nk > EPIC_MAX_NK) return set_error(EPIC_ERR_ARG, "nj=%d nk=%d out of range", g->nj, g->nk);
+  if (g->gas_giant && (g->jtp < 0 || g->jtp > g->nj))
+    return set_error(EPIC_ERR_ARG, "gas giant: jtp=%d outside the rows 0..%d", g->jtp, g->nj);
   if (3. * (g->ni + 2) * (g->nj + 3) * (g->nk + 2) >= 2147483648.)
     return set_error(EPIC_ERR_ARG, "grid %dx%dx%d too large: a field's offsets must fit in 32 bits", g->ni, g->nj, g->nk);
   if (g->globe_latbot != -90. || g->globe_lattop != 90.) return set_error(EPIC_ERR_ARG, "only the full globe is supported");
@@ -366,6 +368,8 @@ extern "C" int epic_model_create(const epic_grid *g, int32_t precision, epic_mod
   d.kappa = g->kappa; d.cp = g->cp; d.cpr = g->cpr; d.rgas = g->rgas;
   d.mu_dry = 1. / (g->rgas / 8.314472e+3);
   d.hs_kf = g->hs_kf; d.lat0 = g->lat0;
+  d.gas_giant = g->gas_giant != 0;
+  d.jtp = g->jtp;
   d.mixed = precision != EPIC_PREC_FP64;
   d.col64 = precision == EPIC_PREC_MIXED;
   d.cr = precision == EPIC_PREC_FP64;
@@ -801,6 +805,7 @@ bool batch_compatible(const DevModel &a, const DevModel &b, const char **why) {
            a.drag_zonal_avg != b.drag_zonal_avg || a.lat0 != b.lat0)
     *why = "physics options";
   else if ((a.nudiv == 0.) != (b.nudiv == 0.)) *why = "divergence damping on/off";
+  else if (a.gas_giant != b.gas_giant) *why = "lower boundary (gas giant or terrain)";
   else if (tensor_filter(a) != tensor_filter(b)) *why = "zonal filter path (ni a multiple of 128 or not)";
   else
     for (int i = 0; i < 9; i++)

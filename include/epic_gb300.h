@@ -65,7 +65,8 @@ extern "C" {
  * make_arrays() (src/shared/epic_funcs_diag.c:577-1074): half-level index jj = 0..2*(nj+1),
  * ii = 0..2*(ni+1), kk = 0..2*(nk+1).  Only the full globe (latbot = -90, lattop = 90) with
  * Held-Suarez physics (planet "held_suarez", x_h2 = 0, ideal gas, nq = 0, turbulence "off",
- * Hsu advection) is supported; anything else returns EPIC_ERR_ARG.
+ * Hsu or Akima advection), with the terrestrial or the gas-giant lower boundary (gas_giant), is
+ * supported; anything else returns EPIC_ERR_ARG.
  */
 typedef struct epic_grid {
   int32_t ni, nj, nk;          /* grid.ni, grid.nj, grid.nk                                     */
@@ -79,7 +80,9 @@ typedef struct epic_grid {
   int32_t drag_zonal_avg;      /* grid.drag_zonal_avg                                           */
   int32_t jtp;                 /* grid.jtp                                                      */
   int32_t advection_scheme;    /* EPIC_ADV_HSU or EPIC_ADV_AKIMA, for THETA and HDRY alike      */
-  int32_t pad1;
+  int32_t gas_giant;           /* planet->type "gas-giant": store_pgrad_vars sets GZ_SURFACE in
+                                  gradient balance with the bottom layer's zonal-mean U (gz_from_u,
+                                  zero at J = jtp); 0 for "terrestrial" (GZ_SURFACE is the terrain) */
   double  dln, dlt, dy0;       /* grid.dln, grid.dlt [deg], grid.dy0 [m]                        */
   double  globe_latbot, globe_lattop;
   double  press0;              /* grid.press0 [Pa]                                              */

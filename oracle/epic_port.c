@@ -752,6 +752,89 @@ static void set_p2etc(ep_model *M, int update_theta) {
 }
 
 /* store_pgrad_vars, epic_funcs_diag.c:3595-3950 (terrestrial, fpara off) */
+/* get_kin (Sadourney 1975 with the Suarez-Takacs blend), epic_funcs_diag.c:2694-2846 */
+static double get_kin(const ep_model *M, const double *u2d, const double *v2d, int J, int I) {
+  const int jj = 2 * J;
+  double u2 = A2(u2d, J, I), u4 = A2(u2d, J, I + 1), v2 = A2(v2d, J, I), v4 = A2(v2d, J + 1, I), kin_c, kin_s;
+  kin_c = (u2 * u2 + u4 * u4 + M->mn[jj + 1] * (v2 * v2 * M->mn_inv[jj] + v4 * v4 * M->mn_inv[jj + 2])) * .25;
+  if (J == 0 || J == NJ) return kin_c;
+  u2 = .5 * (A2(u2d, J + 1, I) + A2(u2d, J - 1, I));
+  u4 = .5 * (A2(u2d, J + 1, I + 1) + A2(u2d, J - 1, I + 1));
+  v2 = .5 * (A2(v2d, J, I + 1) + A2(v2d, J, I - 1));
+  v4 = .5 * (A2(v2d, J + 1, I + 1) + A2(v2d, J + 1, I - 1));
+  kin_s = (u2 * u2 + u4 * u4 + M->mn[jj + 1] * (v2 * v2 * M->mn_inv[jj] + v4 * v4 * M->mn_inv[jj + 2])) * .25;
+  return (5. / 6.) * kin_c + (1. / 6.) * kin_s;
+}
+
+/* The gas-giant lower boundary of store_pgrad_vars (epic_funcs_diag.c:3779-3811): zonal means of U,
+ * P3 and RHO3 at K = nk, then gz_from_u (:4460-4612) with gz0 = 0 at J = grid.jtp: the absolute
+ * vorticity of the zonally symmetric bottom wind (vorticity(ON_SIGMATHETA, ABSOLUTE), :4131-4444,
+ * written into PV3(nk+1) as the reference does, where its PV macros read it), the meridional
+ * integral of -(zeta+f) u dy - dp/rho, and GZ_SURFACE = Bernoulli function - kinetic energy on
+ * every row 0..nj. */
+static void gas_giant_gz_surface(ep_model *M) {
+  int J, I;
+  const int K = KHI, j0 = M->g.jtp;
+  const double *U = M->u + (long)M->it_uv * M->n3;
+  double *u1d = calloc(NJ + 1, sizeof(double)), *p1d = calloc(NJ + 1, sizeof(double)), *rho1d = calloc(NJ + 1, sizeof(double));
+  double *udy = calloc(NJ + 1, sizeof(double)), *pvhudy = calloc(NJ + 1, sizeof(double)), *bern = calloc(NJ + 1, sizeof(double));
+  double *u2d = calloc(M->n2, sizeof(double)), *v2d = calloc(M->n2, sizeof(double));
+  double *pv = M->pv3 + (long)(K + 1) * M->n2;
+  double ze, pv_pole, kin0;
+  for (J = 0; J <= NJ; J++) {
+    for (I = 1; I <= NI; I++) {
+      u1d[J] += A3(U, K, J, I);
+      p1d[J] += A3(M->p3, K, J, I);
+      rho1d[J] += A3(M->rho3, K, J, I);
+    }
+    u1d[J] /= NI;
+    p1d[J] /= NI;
+    rho1d[J] /= NI;
+  }
+  for (J = 0; J <= NJ; J++)
+    for (I = 0; I <= NI + 1; I++) A2(u2d, J, I) = u1d[J];
+  for (J = 1; J <= NJ; J++) {
+    const double f2j = M->f[2 * J], m2j = M->m[2 * J], n2j = M->n[2 * J];
+    const double m_m1_inv = 1. / M->m[2 * J - 1], m_p1_inv = 1. / M->m[2 * J + 1];
+    for (I = 1; I <= NI; I++) {
+      ze = m2j * ((A2(v2d, J, I) - A2(v2d, J, I - 1)) + n2j * (A2(u2d, J - 1, I) * m_m1_inv - A2(u2d, J, I) * m_p1_inv));
+      A2(pv, J, I) = (ze + f2j);
+    }
+  }
+  ze = 0.;
+  for (I = 1; I <= NI; I++) ze -= A2(u2d, 0, I);
+  ze *= M->mn[0] / ((M->m[1]) * (double)(NI));
+  pv_pole = ze + M->f[0];
+  for (I = 1; I <= NI; I++) A2(pv, 0, I) = pv_pole;
+  ze = 0.;
+  for (I = 1; I <= NI; I++) ze += A2(u2d, NJ, I);
+  ze *= M->mn[2 * (NJ + 1)] / ((M->m[2 * NJ + 1]) * (double)(NI));
+  pv_pole = ze + M->f[2 * (NJ + 1)];
+  for (I = 1; I <= NI; I++) A2(pv, NJ + 1, I) = pv_pole;
+  bc2(M, pv);
+  I = 1;
+  for (J = 0; J <= NJ; J++) udy[J] = A2(u2d, J, I) / M->n[2 * J + 1];
+  for (J = 1; J <= NJ; J++) {
+    /* the Sadourney PV averages of include/epic_pv_schemes.h:55-61 around the v point */
+    const double al = (A2(pv, J - 1, I) + A2(pv, J, I) + A2(pv, J, I + 1));
+    const double be = (A2(pv, J, I) + A2(pv, J, I + 1) + A2(pv, J - 1, I + 1));
+    const double ga = (A2(pv, J, I) + A2(pv, J, I + 1) + A2(pv, J + 1, I + 1));
+    const double de = (A2(pv, J, I) + A2(pv, J + 1, I) + A2(pv, J, I + 1));
+    pvhudy[J] = (ga * udy[J] + de * udy[J] + al * udy[J - 1] + be * udy[J - 1]) * (1. / 12.);
+    pvhudy[J] += (p1d[J] - p1d[J - 1]) * 2. / (rho1d[J] + rho1d[J - 1]);
+  }
+  kin0 = 0.;
+  if (j0 >= 0 && j0 <= NJ) kin0 = get_kin(M, u2d, v2d, j0, 1);
+  bern[j0] = 0. + kin0;
+  for (J = j0 + 1; J <= NJ; J++) bern[J] = bern[J - 1] - pvhudy[J];
+  for (J = j0 - 1; J >= 0; J--) bern[J] = bern[J + 1] + pvhudy[J + 1];
+  for (J = 0; J <= NJ; J++) {
+    const double gz = bern[J] - get_kin(M, u2d, v2d, J, 1);
+    for (I = 0; I <= NI + 1; I++) A2(M->gz_surface, J, I) = gz;
+  }
+  free(u1d); free(p1d); free(rho1d); free(udy); free(pvhudy); free(bern); free(u2d); free(v2d);
+}
+
 static int store_pgrad_vars(ep_model *M) {
   int K, J, I, jj;
   double theta, pressure, temperature, mu = M->mu_dry, dtg_inv, gdx_inv3, gdy_inv2, gdy_inv4;
@@ -786,6 +869,7 @@ static int store_pgrad_vars(ep_model *M) {
       A3(M->theta2, 0, J, I) = M->sgth[0];
       A3(M->t2, 0, J, I) = A3(M->t3, 0, J, I);
     }
+  if (M->g.gas_giant) gas_giant_gz_surface(M);
   for (J = 0; J <= NJ; J++)
     for (I = 0; I <= NI + 1; I++) {
       A3(M->gz3, KHI, J, I) = M->g.topo_scale * A2(M->gz_surface, J, I);

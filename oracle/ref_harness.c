@@ -44,6 +44,9 @@ int ref_init(const epic_grid *g, const epic_fields *f) {
 
   planet = (planetspec *)malloc(sizeof(planetspec));
   *planet = held_suarez;
+  /* the gas-giant lower boundary on the same planet: store_pgrad_vars then takes GZ_SURFACE
+   * from gz_from_u (epic_funcs_diag.c:3779-3811) */
+  if (g->gas_giant) strcpy(planet->type, "gas-giant");
   if (planet->re != g->re || planet->rp != g->rp || planet->cp != g->cp || planet->rgas != g->rgas ||
       planet->kappa != g->kappa || planet->cpr != g->cpr || planet->kinvisc != g->kinvisc)
     return -2;

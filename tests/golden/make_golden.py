@@ -19,7 +19,7 @@ sys.path.insert(0, os.path.dirname(os.path.dirname(HERE)))
 from epic_gb300 import EPIC_ADV_AKIMA, EPIC_PROFILE_N2, EPIC_UV_AB3, EPIC_UV_LEAPFROG, HSConfig, hs_setup  # noqa: E402
 from oracle_lib import reference_available, run_reference, fields_to_dict  # noqa: E402
 
-SAVED = ("u", "v", "hdry", "theta", "p3", "gz3", "pv3", "w3", "heat3", "div_uv3")
+SAVED = ("u", "v", "hdry", "theta", "p3", "gz3", "pv3", "w3", "heat3", "div_uv3", "gz_surface")
 CASES = {
     "hs32x16x10_ab3": (HSConfig(ni=32, nj=16, nk=10, dt=300, uv_scheme=EPIC_UV_AB3, seed=11), [("sync", 0), ("step", 1), ("step", 4)]),
     "hs32x16x10_leapfrog": (HSConfig(ni=32, nj=16, nk=10, dt=300, uv_scheme=EPIC_UV_LEAPFROG, seed=12), [("sync", 0), ("step", 1), ("step", 2)]),
@@ -28,6 +28,9 @@ CASES = {
                              [("sync", 0), ("step", 1), ("step", 4)]),
     "jet32x16x10_ab3": (HSConfig(ni=32, nj=16, nk=10, dt=300, uv_scheme=EPIC_UV_AB3, seed=15, profile=EPIC_PROFILE_N2, state="jet"),
                         [("sync", 0), ("step", 1), ("step", 4)]),
+    # the jets over the gas-giant lower boundary (planet->type "gas-giant": GZ_SURFACE from gz_from_u)
+    "jetgg32x16x10_ab3": (HSConfig(ni=32, nj=16, nk=10, dt=300, uv_scheme=EPIC_UV_AB3, seed=16, profile=EPIC_PROFILE_N2, state="jet",
+                                   gas_giant=True), [("sync", 0), ("step", 1), ("step", 4)]),
 }
 
 

@@ -188,10 +188,12 @@ def test_one_day_at_member_shape(gpu, form, case):
     _check(_run(a, b, DAY), BOUNDS[(form, case)])
 
 
+@pytest.mark.parametrize("gas_giant", [False, True], ids=["terrain", "gas_giant"])
 @pytest.mark.parametrize("form", FORMS)
-def test_jets_one_day(gpu, form):
-    """The balanced zonal-jet state on the constant-N^2 sounding, one day."""
-    ga, f = hs_setup(HSConfig(ni=64, nj=32, nk=10, dt=300, seed=0, profile=EPIC_PROFILE_N2, state="jet"))
+def test_jets_one_day(gpu, form, gas_giant):
+    """The balanced zonal-jet state on the constant-N^2 sounding, one day; over the terrestrial
+    and over the gas-giant lower boundary (GZ_SURFACE from gz_from_u, binary64 in every form)."""
+    ga, f = hs_setup(HSConfig(ni=64, nj=32, nk=10, dt=300, seed=0, profile=EPIC_PROFILE_N2, state="jet", gas_giant=gas_giant))
     a, b = _pair(ga, f, True, FORMS[form])
     _check(_run(a, b, DAY), BOUNDS[(form, "jet")])
 
