@@ -51,10 +51,12 @@ ENSEMBLE = {"ens64": 64}
 E2E_GROUPS = 8   # sub-batches of the end-to-end pipeline (copies of one overlap kernels of others)
 # Serving stream: shapes and the time step each runs with for two simulated days (the mixed form
 # from the Held-Suarez column at rest; a sweep of time steps per shape kept the largest that did
-# not stop with non-monotonic GZ3 within two days).  256x128 and 512x256 with 20 or 32 layers stop
-# within two days at every time step tried (down to 60 s and 30 s): left out.
+# not stop with non-monotonic GZ3 within two days for three seeds and k_f scaled by 0.9 and 1.1 --
+# 128x64x32 stops at 120 s with the weaker drag, and at 100 s for some seeds).  256x128 and
+# 512x256 with 20 or 32 layers stop within two days at every time step tried (down to 60 s and
+# 30 s): left out.
 SERVE_SHAPES = {(64, 32, 10): 300, (64, 32, 20): 240, (64, 32, 32): 300, (128, 64, 10): 240, (128, 64, 20): 120,
-                (128, 64, 32): 120, (256, 128, 10): 120, (512, 256, 10): 60}
+                (128, 64, 32): 90, (256, 128, 10): 120, (512, 256, 10): 60}
 METRIC = "cell-steps/s"
 
 
@@ -752,7 +754,12 @@ ROOF_STAGES = {
 # the stage's kernels from one ncu capture of an 8-member launch at 128x64x20 (cold L2; writes
 # still resident in L2 when a kernel ends are not counted), divided by 8
 # (profiles/traffic_stages_mixed_ensemble8_128x64x20.md).  Scaled by the members of the launch.
-ROOF_TRAFFIC_PER_MEMBER = {19: 176.4e6 / 8, 12: 111.0e6 / 8}
+ROOF_TRAFFIC_PER_MEMBER = {19: 184.7e6 / 8, 12: 86.4e6 / 8}
+# Issue fraction of each roofline stage (smsp__issue_active, duration-weighted over the stage's
+# kernels, one ncu capture of an 8-member step at 128x64x20,
+# profiles/kernels_hbm_issue_mixed_ensemble8_128x64x20.md): the bound these kernels meet, beside
+# the HBM fraction they do not
+ROOF_ISSUE = {12: 0.826, 19: 0.609}
 ROOF_TRAFFIC_SHAPE = (128, 64, 20)
 
 
@@ -782,6 +789,9 @@ def batch_roofline(batch, cfg, nmem, stream, torch, stage=19):
     return {"kernel": label, "bound": "hbm", "achieved": ach, "peak": peaks["hbm_gbs"], "unit": "GB/s",
             "frac": ach / peaks["hbm_gbs"], "peak_source": peaks["source"] + " (burst copy)", "algorithmic_bytes": alg,
             "launch_ms": dur * 1e3, "traffic": traffic,
+            "issue_frac": ROOF_ISSUE.get(stage),
+            "issue_source": "ncu smsp__issue_active of the stage's kernels, duration-weighted, one 8-member step at "
+                            "128x64x20 (a constant of that capture)" if stage in ROOF_ISSUE else None,
             "traffic_source": "ncu dram__bytes_read.sum + dram__bytes_write.sum of the stage's kernels, one 8-member launch "
                               "at 128x64x20 scaled by members" if traffic else None, "note": note}
 
