@@ -23,6 +23,7 @@ Stated error (relative L2 per field vs FP64, dt 300 s), measured on a GB300:
   fast   128x64x20  1 day from rest                   9.5e-4   1.7e-3   2.0e-5   1.2e-7
   mixed  64x32x10   zonal jets, 1 day                 3.4e-7   8.9e-7   1.7e-8   3.4e-9
   fast   64x32x10   zonal jets, 1 day                 3.6e-6   1.8e-5   1.4e-7   3.8e-8
+  mixed  64x32x10   jets, gas-giant boundary, 1 day   3.7e-7   7.3e-7   1.1e-7   4.1e-9
 
 (128x64x20 is the ensemble member shape: ni = 128 takes the tensor-core filter; its FP64 run
 stays stable for about two days, so its spin-up is one day.)
@@ -59,6 +60,11 @@ BOUNDS = {
     ("fast", "member_rest"): {"u": 3e-3, "v": 5e-3, "hdry": 6e-5, "theta": 4e-7},
     ("mixed", "jet"): {"u": 1.2e-6, "v": 3e-6, "hdry": 6e-8, "theta": 1e-8},
     ("fast", "jet"): {"u": 1.2e-5, "v": 6e-5, "hdry": 5e-7, "theta": 1.2e-7},
+    # the jets over the gas-giant lower boundary: GZ_SURFACE follows the bottom wind, whose
+    # rounding then moves the whole column (mixed, measured: U 3.7e-7, V 7.3e-7, HDRY 1.1e-7,
+    # THETA 4.1e-9)
+    ("mixed", "jet-gg"): {"u": 8e-7, "v": 1.5e-6, "hdry": 2.2e-7, "theta": 1e-8},
+    ("fast", "jet-gg"): {"u": 1.2e-5, "v": 6e-5, "hdry": 2e-6, "theta": 1.2e-7},
     ("fast", "spun_up"): {"u": 1e-4, "v": 2e-3, "hdry": 1e-6, "theta": 1e-7},
     ("fast", "rest"): {"u": 1e-3, "v": 3e-3, "hdry": 1e-6, "theta": 1e-7},
     ("fast", "leapfrog"): {"u": 6e-3, "v": 3e-3, "hdry": 1e-6, "theta": 1e-7},
@@ -195,7 +201,7 @@ def test_jets_one_day(gpu, form, gas_giant):
     and over the gas-giant lower boundary (GZ_SURFACE from gz_from_u, binary64 in every form)."""
     ga, f = hs_setup(HSConfig(ni=64, nj=32, nk=10, dt=300, seed=0, profile=EPIC_PROFILE_N2, state="jet", gas_giant=gas_giant))
     a, b = _pair(ga, f, True, FORMS[form])
-    _check(_run(a, b, DAY), BOUNDS[(form, "jet")])
+    _check(_run(a, b, DAY), BOUNDS[(form, "jet-gg" if gas_giant else "jet")])
 
 
 # The mixed form's error bound of the configuration: relative L2 <= 1e-4 per prognostic after one
