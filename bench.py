@@ -45,6 +45,7 @@ WORKLOADS = {
     "hs256": (256, 128, 32, 60),
     "hs512": (512, 256, 40, 60),
     "jet256": (256, 128, 32, 60),  # balanced zonal jets on the constant-N^2 sounding
+    "jet256gg": (256, 128, 32, 60),  # the same over the gas-giant lower boundary (gz_from_u)
     "ens64": (128, 64, 20, 300),   # per member; 64 members
 }
 ENSEMBLE = {"ens64": 64}
@@ -69,7 +70,7 @@ def _workload_cfg(name, seed=0, advection="hsu"):
     ni, nj, nk, dt = WORKLOADS[name]
     if name.startswith("jet"):
         return HSConfig(ni=ni, nj=nj, nk=nk, dt=dt, seed=seed, advection_scheme=ADVECTION[advection], profile=EPIC_PROFILE_N2,
-                        state="jet")
+                        state="jet", gas_giant=name.endswith("gg"))
     return HSConfig(ni=ni, nj=nj, nk=nk, dt=dt, seed=seed, advection_scheme=ADVECTION[advection])
 
 
@@ -238,6 +239,7 @@ def workload_config(args, cfg, nmem, ws):
                 f"{ADVECTION_NAME[args.advection]}, nu4=0.5 max, seeded 0.1 K noise and +/-10% k_f per member")
     else:
         what = (("Zonal jets on the Held-Suarez planet " if cfg.state == "jet" else "Held-Suarez ") +
+                ("over the gas-giant lower boundary (GZ_SURFACE from gz_from_u) " if cfg.gas_giant else "") +
                 f"{cfg.ni}x{cfg.nj}x{cfg.nk}, dt={cfg.dt}s, AB3, {ADVECTION_NAME[args.advection]}, nu4=0.5 max")
     return {"workload": what, "ni": cfg.ni, "nj": cfg.nj, "nk": cfg.nk, "dt": cfg.dt, "members": nmem,
             "advection": args.advection, "parallelism": f"replicas{ws}", "state": state,
