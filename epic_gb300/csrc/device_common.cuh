@@ -31,6 +31,7 @@ struct Ctl {
   int err_code, err_k, err_j, err_i;   // first model error (0 = none)
   double err_val;
   double ab[2][3];                     // Adams-Bashforth coefficients chosen for u, v this step
+  float2 abf[2][3];                    // the same as double-floats (the mixed forms' update)
   int lf_first[2];                     // leapfrog: forward (Euler) first step for u, v
   int halted;                          // set between steps once err_code is set: every kernel of the
                                        // model then returns at entry (the reference stops the run at

@@ -1002,21 +1002,33 @@ int launch_set_p2etc(const DevModel &M, int update_theta, cudaStream_t s, bool e
 // -(zeta+f) u dy - dp/rho from J = jtp (the Sadourney averages of include/epic_pv_schemes.h:55-61
 // around the v point) and subtracts get_kin.  Every row of the reference's arrays is uniform in I,
 // so each row's values are computed once and written across it.
+//
+// RHO3 at K = nk comes first, one thread per cell (k_gz_rho_bottom: the binary64 power is costly
+// on this GPU's FP64 unit, and one block evaluating a row's worth per thread held the step up for
+// milliseconds); the column kernel that follows writes the same plane again.
+__global__ void k_gz_rho_bottom(DevModel M) {
+  if (epic_member(M)) return;
+  const int t = (int)(blockIdx.x * blockDim.x + threadIdx.x);
+  if (t >= (M.nj + 1) * M.ni) return;
+  const int J = t / M.ni, I = 1 + t - J * M.ni;
+  const int x = M.at(M.nk, J, I);
+  const double p = M.p3[x];
+  M.rho3[x] = return_density(p, return_temp(M, p, M.theta[x]), M.mu_dry);
+}
+
 __global__ void __launch_bounds__(256) k_gz_from_u(DevModel M) {
   if (epic_member(M)) return;
   extern __shared__ double gg[];
   const int nj = M.nj, ni = M.ni, K = M.nk, j0 = M.jtp;
   double *u1d = gg, *p1d = u1d + (nj + 1), *rho1d = p1d + (nj + 1), *pvr = rho1d + (nj + 1), *gz = pvr + (nj + 2);
   const double *U = M.u + plane_offset(M, PL_UV);
-  const double mu = M.mu_dry;
   for (int J = (int)threadIdx.x; J <= nj; J += (int)blockDim.x) {
     double su = 0., sp = 0., sr = 0.;
     for (int I = 1; I <= ni; I++) {
       const int x = M.at(K, J, I);
-      const double p = M.p3[x];
       su += U[x];
-      sp += p;
-      sr += return_density(p, return_temp(M, p, M.theta[x]), mu);
+      sp += M.p3[x];
+      sr += M.rho3[x];
     }
     u1d[J] = su / ni;
     p1d[J] = sp / ni;
@@ -1084,8 +1096,10 @@ __global__ void __launch_bounds__(256) k_gz_from_u(DevModel M) {
 }
 
 int launch_store_pgrad_vars(const DevModel &M, cudaStream_t s, bool early) {
-  if (M.gas_giant)
+  if (M.gas_giant) {
+    k_gz_rho_bottom<<<zg(epic_blocks((long long)(M.nj + 1) * M.ni, 256), M), 256, 0, s>>>(M);
     k_gz_from_u<<<zg(1, M), 256, (size_t)(5 * M.nj + 6) * sizeof(double), s>>>(M);
+  }
   if (M.mixed && early) {   // GZ3 alone: no DZDT3, so no horizontal part either
     if (M.col64) k_gz3_column_acc<<<zg(ntile_blocks(M), M), CT_THREADS, tile_smem(M, 5), s>>>(M);
     else k_pgrad_vars_column_mixed<false><<<zg(ntile_blocks(M), M), CT_THREADS, tile_smem(M, 5), s>>>(M);

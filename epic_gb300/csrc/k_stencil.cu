@@ -275,26 +275,57 @@ __device__ __forceinline__ LonFace<R> lon_face(const DevModel &M, const R (&z)[3
   return f;
 }
 
+// Rows shared by a block (ni divides the block: the launcher sizes the shared memory for it):
+// each cell computes its east face once and takes its west face from the cell to its left --
+// for i = 1 from the row's last cell, whose face at column ni equals the face at the periodic
+// column 0 bit for bit (the fields' pad columns are copies).  The faces of one row then need one
+// reference: the double-float form shifts by the row's value at i = 1 instead of each cell's own
+// (its differences keep ~48 bits either way); the binary32 form keeps its per-cell reference and
+// computes both faces.
 template <class R>
 __global__ void k_pgrad_lon(DevModel M) {
   if (epic_member(M)) return;
   Cell c;
-  if (!cell3(M, 1, M.nk - 1, 0, M.nj + 1, c)) return;
+  const bool share = !std::is_same_v<R, float> && (blockDim.x % (unsigned)M.ni) == 0u;
+  const bool valid = cell3(M, 1, M.nk - 1, 0, M.nj + 1, c);
+  if (!share && !valid) return;
   const int k = c.k, j = c.j, i = c.i;
   const R DLOGZ_TOL = R(1.e-2);
-  const PgradRef<R> ref(M, k, j, i);
-  R z[3][3][2], p[2][2];
+  LonFace<R> w, e;
+  if (share) {
+    extern __shared__ __align__(16) unsigned char pg_smem[];
+    LonFace<R> *faces = reinterpret_cast<LonFace<R> *>(pg_smem);
+    if (valid) {
+      const PgradRef<R> ref(M, k, j, 1);
+      R z[3][3][2], p[2][2];
 #pragma unroll
-  for (int a = 0; a < 3; a++)
+      for (int a = 0; a < 3; a++)
 #pragma unroll
-    for (int b = 0; b < 3; b++)
+        for (int b = 0; b < 3; b++) z[a][b][1] = z[a][b][0] = ref.z(M.at(k + a - 1, j + b - 1, i));
 #pragma unroll
-      for (int q = 0; q < 2; q++) z[a][b][q] = ref.z(M.at(k + a - 1, j + b - 1, i + q - 1));
+      for (int a = 0; a < 2; a++) p[a][1] = p[a][0] = ref.p(M.at(k + a, j, i));
+      e = lon_face<R>(M, z, p, 1, i);
+      faces[threadIdx.x] = e;
+    }
+    __syncthreads();
+    if (!valid) return;
+    w = faces[i == 1 ? threadIdx.x + (unsigned)M.ni - 1u : threadIdx.x - 1u];
+  } else {
+    const PgradRef<R> ref(M, k, j, i);
+    R z[3][3][2], p[2][2];
 #pragma unroll
-  for (int a = 0; a < 2; a++)
+    for (int a = 0; a < 3; a++)
 #pragma unroll
-    for (int q = 0; q < 2; q++) p[a][q] = ref.p(M.at(k + a, j, i + q - 1));
-  const LonFace<R> w = lon_face<R>(M, z, p, 0, i - 1), e = lon_face<R>(M, z, p, 1, i);
+      for (int b = 0; b < 3; b++)
+#pragma unroll
+        for (int q = 0; q < 2; q++) z[a][b][q] = ref.z(M.at(k + a - 1, j + b - 1, i + q - 1));
+#pragma unroll
+    for (int a = 0; a < 2; a++)
+#pragma unroll
+      for (int q = 0; q < 2; q++) p[a][q] = ref.p(M.at(k + a, j, i + q - 1));
+    w = lon_face<R>(M, z, p, 0, i - 1);
+    e = lon_face<R>(M, z, p, 1, i);
+  }
   const R rho = Pow2{.5f} * (cv<R>(M.rho3[M.at(k, j, i)]) + cv<R>(M.rho3[M.at(k, j, i - 1)]));
   const R rlns = cv<R>(M.rln[2 * j]), rlnn = cv<R>(M.rln[2 * j + 2]);
   R a1 = e.ztne + e.ztse, a2 = w.ztne + w.ztse;
@@ -1003,6 +1034,10 @@ __global__ void k_uv_decide(DevModel M) {
         if (ten[(long long)c->it_minus1 * M.n3 + cell] == DBL_MAX) { ab[0] = 1.; ab[1] = 0.; ab[2] = 0.; }
         else { ab[0] = 3. / 2.; ab[1] = -1. / 2.; ab[2] = 0.; }
       } else { ab[0] = 23. / 12.; ab[1] = -16. / 12.; ab[2] = 5. / 12.; }
+      for (int q = 0; q < 3; q++) {
+        const dfl d = d2df(ab[q]);
+        c->abf[w][q] = make_float2(d.hi, d.lo);
+      }
     } else {
       c->lf_first[w] = val[(long long)c->it_minus1 * M.n3 + cell] == DBL_MAX;
     }
@@ -1023,7 +1058,19 @@ __global__ void k_uv_update(DevModel M) {
   const double *ten = w == 0 ? M.dudt : M.dvdt;
   const long long x = M.at(k, j, i), base = M.at(k, j, 0);
   const double DT = M.dt;
-  if (M.uv_scheme == EPIC_UV_AB3) {
+  if (M.uv_scheme == EPIC_UV_AB3 && M.mixed) {
+    // the mixed forms: the Adams-Bashforth sum in double-float on the integer and FP32 pipes
+    // (~1e-14 of the increment) added to the binary64 wind -- one FP64 addition a point instead
+    // of seven, which had put this kernel at the FP64 unit's rate
+    // (a zero coefficient -- the first steps -- drops its term: the planes not yet written hold
+    // the DBL_MAX marker, which has no binary32 part)
+    const float2 *ab = c->abf[w];
+    double *X = val + (long long)c->it_uv * M.n3;
+    dfl s = dfl(ab[0].x, ab[0].y) * d2df(ten[(long long)c->it_zero * M.n3 + x]);
+    if (ab[1].x != 0.f) s += dfl(ab[1].x, ab[1].y) * d2df(ten[(long long)c->it_minus1 * M.n3 + x]);
+    if (ab[2].x != 0.f) s += dfl(ab[2].x, ab[2].y) * d2df(ten[(long long)c->it_minus2 * M.n3 + x]);
+    write_with_pads(X, M, base, i, X[x] + df2d(dfl(d2f(M.dt), 0.f) * s));
+  } else if (M.uv_scheme == EPIC_UV_AB3) {
     const double *ab = c->ab[w];
     double *X = val + (long long)c->it_uv * M.n3;
     const double v = X[x] + DT * (ab[0] * ten[(long long)c->it_zero * M.n3 + x] + ab[1] * ten[(long long)c->it_minus1 * M.n3 + x] +
@@ -1101,17 +1148,20 @@ int launch_uv_core(const DevModel &M, cudaStream_t s) {
   return 0;
 }
 
+// k_pgrad_lon's face exchange: one face per thread of the block
+static size_t lon_smem(const DevModel &M, size_t face_bytes) { return (size_t)TB(M, TB_PGRAD) * face_bytes; }
+
 int launch_uv_pgrad(const DevModel &M, cudaStream_t s) {
   k_gz_pole_rows<<<zg(M.nk + 1, M), 128, 0, s>>>(M);
   // FP64 form: binary64; mixed: double-float on the splits; fast mixed: binary32 on the splits
   const dim3 glon = zg(cells_blocks(M, M.nk - 1, M.nj + 1, TB(M, TB_PGRAD)), M), glat = zg(cells_blocks(M, M.nk - 1, M.nj, TB(M, TB_PGRAD)), M);
   if (!M.mixed) {
-    k_pgrad_lon<double><<<glon, TB(M, TB_PGRAD), 0, s>>>(M);
+    k_pgrad_lon<double><<<glon, TB(M, TB_PGRAD), lon_smem(M, sizeof(LonFace<double>)), s>>>(M);
     k_pgrad_lat<double><<<glat, TB(M, TB_PGRAD), 0, s>>>(M);
     return 0;
   }
   if (M.col64) {
-    k_pgrad_lon<dfl><<<glon, TB(M, TB_PGRAD), 0, s>>>(M);
+    k_pgrad_lon<dfl><<<glon, TB(M, TB_PGRAD), lon_smem(M, sizeof(LonFace<dfl>)), s>>>(M);
     k_pgrad_lat<dfl><<<glat, TB(M, TB_PGRAD), 0, s>>>(M);
   } else {
     k_pgrad_lon<float><<<glon, TB(M, TB_PGRAD), 0, s>>>(M);
