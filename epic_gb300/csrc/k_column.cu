@@ -998,9 +998,9 @@ int launch_set_p2etc(const DevModel &M, int update_theta, cudaStream_t s, bool e
 // kernel of store_pgrad_vars evaluates it, which the reference has just stored when it takes the
 // means); the absolute vorticity of the zonally symmetric wind (vorticity(ON_SIGMATHETA,
 // ABSOLUTE), :4131-4444, v = 0), written into PV3(nk+1) as the reference does (its PV averages
-// read it there, and store_diag leaves that level alone); then one thread integrates
-// -(zeta+f) u dy - dp/rho from J = jtp (the Sadourney averages of include/epic_pv_schemes.h:55-61
-// around the v point) and subtracts get_kin.  Every row of the reference's arrays is uniform in I,
+// read it there, and store_diag leaves that level alone); each row's increment of the Bernoulli
+// function, (zeta+f) u dy (the Sadourney averages of include/epic_pv_schemes.h:55-61 around the v
+// point) plus dp/rho, and its get_kin; then one thread sums the increments from J = jtp.  Every row of the reference's arrays is uniform in I,
 // so each row's values are computed once and written across it.
 //
 // RHO3 at K = nk comes first, one thread per cell (k_gz_rho_bottom: the binary64 power is costly
@@ -1021,6 +1021,7 @@ __global__ void __launch_bounds__(256) k_gz_from_u(DevModel M) {
   extern __shared__ double gg[];
   const int nj = M.nj, ni = M.ni, K = M.nk, j0 = M.jtp;
   double *u1d = gg, *p1d = u1d + (nj + 1), *rho1d = p1d + (nj + 1), *pvr = rho1d + (nj + 1), *gz = pvr + (nj + 2);
+  double *kin = gz + (nj + 1), *pvh = kin + (nj + 1);
   const double *U = M.u + plane_offset(M, PL_UV);
   for (int J = (int)threadIdx.x; J <= nj; J += (int)blockDim.x) {
     double su = 0., sp = 0., sr = 0.;
@@ -1056,36 +1057,40 @@ __global__ void __launch_bounds__(256) k_gz_from_u(DevModel M) {
     pvr[J] = pv;
   }
   __syncthreads();
-  if (threadIdx.x == 0) {
-    // get_kin (Sadourney 1975 with the Suarez-Takacs blend, epic_funcs_diag.c:2694-2846) of the
-    // zonally symmetric wind at row J, v = 0
-    auto kin = [&](int J) {
-      const int jj = 2 * J;
-      double u2 = u1d[J], u4 = u1d[J], v2 = zero, v4 = zero;
-      const double kin_c = (u2 * u2 + u4 * u4 + M.mn[jj + 1] * (v2 * v2 * M.mn_inv[jj] + v4 * v4 * M.mn_inv[jj + 2])) * .25;
-      if (J == 0 || J == nj) return kin_c;
+  // get_kin (Sadourney 1975 with the Suarez-Takacs blend, epic_funcs_diag.c:2694-2846) of the
+  // zonally symmetric wind at every row, v = 0, and the increments of the Bernoulli function,
+  // (zeta+f) u dy plus the pressure term, one row per thread
+  for (int J = (int)threadIdx.x; J <= nj; J += (int)blockDim.x) {
+    const int jj = 2 * J;
+    double u2 = u1d[J], u4 = u1d[J], v2 = zero, v4 = zero;
+    const double kin_c = (u2 * u2 + u4 * u4 + M.mn[jj + 1] * (v2 * v2 * M.mn_inv[jj] + v4 * v4 * M.mn_inv[jj + 2])) * .25;
+    if (J == 0 || J == nj) {
+      kin[J] = kin_c;
+    } else {
       u2 = .5 * (u1d[J + 1] + u1d[J - 1]);
       u4 = .5 * (u1d[J + 1] + u1d[J - 1]);
       v2 = .5 * (zero + zero);
       v4 = .5 * (zero + zero);
       const double kin_s = (u2 * u2 + u4 * u4 + M.mn[jj + 1] * (v2 * v2 * M.mn_inv[jj] + v4 * v4 * M.mn_inv[jj + 2])) * .25;
-      return (5. / 6.) * kin_c + (1. / 6.) * kin_s;
-    };
-    // (zeta+f) u dy + the pressure term, accumulated into GZ's row array as the Bernoulli function
-    auto pvhudy = [&](int J) {
+      kin[J] = (5. / 6.) * kin_c + (1. / 6.) * kin_s;
+    }
+    if (J >= 1) {
       const double udy = u1d[J] / M.n[2 * J + 1], udym = u1d[J - 1] / M.n[2 * J - 1];
       const double al = (pvr[J - 1] + pvr[J] + pvr[J]), be = (pvr[J] + pvr[J] + pvr[J - 1]);
       const double ga = (pvr[J] + pvr[J] + pvr[J + 1]), de = (pvr[J] + pvr[J + 1] + pvr[J]);
       double v = (ga * udy + de * udy + al * udym + be * udym) * (1. / 12.);
       v += (p1d[J] - p1d[J - 1]) * 2. / (rho1d[J] + rho1d[J - 1]);
-      return v;
-    };
-    const double kin0 = (j0 >= 0 && j0 <= nj) ? kin(j0) : 0.;
-    gz[j0] = 0. + kin0;
-    for (int J = j0 + 1; J <= nj; J++) gz[J] = gz[J - 1] - pvhudy(J);
-    for (int J = j0 - 1; J >= 0; J--) gz[J] = gz[J + 1] + pvhudy(J + 1);
-    for (int J = 0; J <= nj; J++) gz[J] = gz[J] - kin(J);
+      pvh[J] = v;
+    }
   }
+  __syncthreads();
+  if (threadIdx.x == 0) {   // the integral from J = jtp, in the reference's order
+    gz[j0] = 0. + kin[j0];
+    for (int J = j0 + 1; J <= nj; J++) gz[J] = gz[J - 1] - pvh[J];
+    for (int J = j0 - 1; J >= 0; J--) gz[J] = gz[J + 1] + pvh[J + 1];
+  }
+  __syncthreads();
+  for (int J = (int)threadIdx.x; J <= nj; J += (int)blockDim.x) gz[J] = gz[J] - kin[J];
   __syncthreads();
   double *pv3 = M.pv3 + (long long)(K + 1) * M.n2;
   for (int t = (int)threadIdx.x; t < (nj + 2) * (ni + 2); t += (int)blockDim.x) {
@@ -1098,7 +1103,7 @@ __global__ void __launch_bounds__(256) k_gz_from_u(DevModel M) {
 int launch_store_pgrad_vars(const DevModel &M, cudaStream_t s, bool early) {
   if (M.gas_giant) {
     k_gz_rho_bottom<<<zg(epic_blocks((long long)(M.nj + 1) * M.ni, 256), M), 256, 0, s>>>(M);
-    k_gz_from_u<<<zg(1, M), 256, (size_t)(5 * M.nj + 6) * sizeof(double), s>>>(M);
+    k_gz_from_u<<<zg(1, M), 256, (size_t)(7 * M.nj + 8) * sizeof(double), s>>>(M);
   }
   if (M.mixed && early) {   // GZ3 alone: no DZDT3, so no horizontal part either
     if (M.col64) k_gz3_column_acc<<<zg(ntile_blocks(M), M), CT_THREADS, tile_smem(M, 5), s>>>(M);

@@ -207,11 +207,12 @@ __global__ void __launch_bounds__(FG_THREADS) k_filter_planes_gemm(DevModel M, c
   const uint32_t idesc = idesc_tf32(N);
 
   // B[n][e] = x_n(kc + e + 1) - x1_n, zero in idle columns: N/16 16-byte chunks (4 values each)
-  // per thread and K chunk, loaded into registers one chunk ahead
+  // per thread and K chunk, loaded into registers two chunks ahead (two register sets, the chunks
+  // taken in pairs), so that a chunk's loads have two chunks' products to arrive in
   constexpr int BQMAX = FG_NMAX * FG_KC / 4 / FG_THREADS;   // 4
   const int nq = N * (FG_KC / 4) / FG_THREADS;
-  double bnext[BQMAX][4];
-  auto load_b = [&](int kc) {
+  double breg0[BQMAX][4], breg1[BQMAX][4];
+  auto load_b = [&](int kc, double (&bn)[BQMAX][4]) {
 #pragma unroll
     for (int u = 0; u < BQMAX; u++) {
       if (u >= nq) break;
@@ -221,21 +222,23 @@ __global__ void __launch_bounds__(FG_THREADS) k_filter_planes_gemm(DevModel M, c
         const double *row = s_src[s_colg[n]] + base + kc + e0 + 1;
         const double c = s_x1[n];
 #pragma unroll
-        for (int v = 0; v < 4; v++) bnext[u][v] = row[v] - c;
+        for (int v = 0; v < 4; v++) bn[u][v] = row[v] - c;
       } else {
 #pragma unroll
-        for (int v = 0; v < 4; v++) bnext[u][v] = 0.;
+        for (int v = 0; v < 4; v++) bn[u][v] = 0.;
       }
     }
   };
-  load_b(0);
-  int t = 0, last_tma = -1, last_commit = -1;
-  for (; t < nsteps; t++) {
-    const int c = t / mtiles, mt = t - c * mtiles, kc = c * FG_KC, abuf = t & 1, bbuf = c & 1;
+  load_b(0, breg0);
+  if (nchunks > 1) load_b(FG_KC, breg1);
+  int last_tma = -1, last_commit = -1;
+  // step t = (K chunk c, output tile mt); false once the CTA must stop
+  auto step = [&](int c, int mt, double (&bn)[BQMAX][4]) -> bool {
+    const int t = c * mtiles + mt, kc = c * FG_KC, abuf = t & 1, bbuf = c & 1;
     // both buffers were last read by the products of step t-2 or earlier
     if (t >= 2 && !mbar_wait(bars_s + 8 * abuf, (unsigned)(((t - 2) >> 1) & 1))) atomicExch(&fail, 1);
     __syncthreads();
-    if (fail) break;
+    if (fail) return false;
     const unsigned a_hi_s = a_s + abuf * 2 * FG_A_BYTES, a_lo_s = a_hi_s + FG_A_BYTES;
     const unsigned b_hi_s = b_s + bbuf * 2 * b_bytes, b_lo_s = b_hi_s + b_bytes;
     if (tid == 0) {
@@ -248,13 +251,13 @@ __global__ void __launch_bounds__(FG_THREADS) k_filter_planes_gemm(DevModel M, c
       tma_tile(a_lo_s, opm.fop_map, y + FG_M, tb);
       last_tma = t;
     }
-    if (mt == 0) {   // the planes' tile of this K chunk
+    if (mt == 0) {   // the planes' tile of this K chunk, then the loads of chunk c+2 into its registers
       unsigned char *bh = fg_smem + (b_hi_s - smem_s), *bl = bh + b_bytes;
 #pragma unroll
       for (int u = 0; u < BQMAX; u++) {
         if (u >= nq) break;
         const int q = tid + u * FG_THREADS, n = q / (FG_KC / 4), e0 = 4 * (q % (FG_KC / 4));
-        const float b0 = d2f(bnext[u][0]), b1 = d2f(bnext[u][1]), b2 = d2f(bnext[u][2]), b3 = d2f(bnext[u][3]);
+        const float b0 = d2f(bn[u][0]), b1 = d2f(bn[u][1]), b2 = d2f(bn[u][2]), b3 = d2f(bn[u][3]);
         const float4 hv = make_float4(tf32_hi(b0), tf32_hi(b1), tf32_hi(b2), tf32_hi(b3));
         const float4 lv = make_float4(b0 - hv.x, b1 - hv.y, b2 - hv.z, b3 - hv.w);
         const unsigned off = sw128(n, e0);
@@ -262,6 +265,7 @@ __global__ void __launch_bounds__(FG_THREADS) k_filter_planes_gemm(DevModel M, c
         *reinterpret_cast<float4 *>(bl + off) = lv;
       }
       asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+      if (c + 2 < nchunks) load_b(kc + 2 * FG_KC, bn);
     }
     __syncthreads();
     if (tid == 0) {
@@ -282,8 +286,12 @@ __global__ void __launch_bounds__(FG_THREADS) k_filter_planes_gemm(DevModel M, c
         last_commit = t;
       }
     }
-    // the next K chunk's inputs travel while the products run
-    if (mt == mtiles - 1 && c + 1 < nchunks) load_b(kc + FG_KC);
+    return true;
+  };
+  bool going = true;
+  for (int c = 0; c < nchunks && going; c += 2) {   // nchunks = ni/32 is even
+    for (int mt = 0; mt < mtiles && going; mt++) going = step(c, mt, breg0);
+    for (int mt = 0; mt < mtiles && going; mt++) going = step(c + 1, mt, breg1);
   }
   // drain: the last commit covers every earlier one; an operator copy whose wait gave up is
   // waited for again (both bounded), so that nothing writes this CTA's shared or tensor memory

@@ -42,6 +42,34 @@ def test_batch_equals_members_alone(gpu, precision, scheme, adv):
     assert batch.kernels_per_step > 0
 
 
+@pytest.mark.parametrize("precision", [EPIC_PREC_FP64, EPIC_PREC_MIXED])
+def test_gas_giant_batch_equals_members_alone(gpu, precision):
+    """Jets over the gas-giant lower boundary (GZ_SURFACE from gz_from_u every store_pgrad_vars),
+    members of two sizes in one batch: each equals itself stepped alone."""
+    from epic_gb300 import EPIC_PROFILE_N2
+    members = []
+    for q, shape in enumerate([(32, 16, 10), (64, 32, 10), (32, 16, 10)]):
+        ni, nj, nk = shape
+        ga, f = hs_setup(HSConfig(ni=ni, nj=nj, nk=nk, dt=300, seed=40 + q, state="jet", profile=EPIC_PROFILE_N2, gas_giant=True))
+        m = Model(ga, precision)
+        m.upload(f)
+        members.append((ga, f, m))
+    batch = Batch([m for _, _, m in members])
+    batch.timestep(EPIC_SYNC_DIAGS_ONLY)
+    batch.run(5)
+    batch.sync()
+    for ga, f, m in members:
+        alone = Model(ga, precision)
+        alone.upload(f)
+        alone.timestep(EPIC_SYNC_DIAGS_ONLY)
+        alone.run(5)
+        alone.sync()
+        a, b = m.download(), alone.download()
+        for k in a.arrays:
+            assert np.array_equal(a.arrays[k], b.arrays[k]), k
+        assert np.abs(a.arrays["gz_surface"]).max() > 0.
+
+
 def test_batch_rejects_incompatible_members(gpu):
     """Members must share the layers, the precision form and, in the mixed forms, the zonal
     filter's path (tensor cores for ni a multiple of 128); ni, nj and dt may differ."""
@@ -59,6 +87,11 @@ def test_batch_rejects_incompatible_members(gpu):
         Batch([c, d])
     with pytest.raises(EpicError, match="filter path"):
         Batch([c, e])
+    ga, fg = hs_setup(HSConfig(ni=32, nj=16, nk=10, dt=300, seed=7, gas_giant=True))
+    g = Model(ga, EPIC_PREC_FP64)
+    g.upload(fg)
+    with pytest.raises(EpicError, match="lower boundary"):
+        Batch([a, g])
     Batch([a, f]).close()   # sizes alone may differ
 
 
