@@ -1000,8 +1000,9 @@ int launch_set_p2etc(const DevModel &M, int update_theta, cudaStream_t s, bool e
 // ABSOLUTE), :4131-4444, v = 0), written into PV3(nk+1) as the reference does (its PV averages
 // read it there, and store_diag leaves that level alone); each row's increment of the Bernoulli
 // function, (zeta+f) u dy (the Sadourney averages of include/epic_pv_schemes.h:55-61 around the v
-// point) plus dp/rho, and its get_kin; then one thread sums the increments from J = jtp.  Every row of the reference's arrays is uniform in I,
-// so each row's values are computed once and written across it.
+// point) plus dp/rho, and its get_kin; then one thread sums the increments from J = jtp.  Every
+// row of the reference's arrays is uniform in I, so each row's values are computed once and
+// written across it.
 //
 // RHO3 at K = nk comes first, one thread per cell (k_gz_rho_bottom: the binary64 power is costly
 // on this GPU's FP64 unit, and one block evaluating a row's worth per thread held the step up for

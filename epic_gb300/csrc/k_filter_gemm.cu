@@ -132,7 +132,7 @@ __device__ __forceinline__ bool mbar_wait(unsigned mbar, unsigned phase) {
 // a buffer is refilled only after the commit of the step that last read it (commits complete in
 // issue order).
 __global__ void __launch_bounds__(FG_THREADS) k_filter_planes_gemm(DevModel M, const double *src, int src_sel, double *dst, int k0,
-                                                                     int nplanes, int vgrid, int shift, int pc, int G, int N) {
+                                                                     int nplanes, int vgrid, int shift, int pc, int G, int N, int msplit) {
   extern __shared__ __align__(16) unsigned char fg_raw[];
   __shared__ __align__(8) uint64_t bars[4];   // products of buffer 0 / 1 done; operator tiles of buffer 0 / 1 landed
   __shared__ uint32_t tmem_base;
@@ -145,13 +145,18 @@ __global__ void __launch_bounds__(FG_THREADS) k_filter_planes_gemm(DevModel M, c
   const int tid = (int)threadIdx.x, warp = tid >> 5;
   const int j = (int)blockIdx.x - 1;
   const int nch = (nplanes + pc - 1) / pc;
-  const int chunk = (int)blockIdx.y % nch, q0 = ((int)blockIdx.y / nch) * G;
+  const int yq = (int)blockIdx.y / msplit, msi = (int)blockIdx.y - yq * msplit;
+  const int chunk = yq % nch, q0 = (yq / nch) * G;
   const int members = M.batch ? M.nbatch : 1;
   // geometry: a one-member CTA takes its member's own (batches of mixed sizes); the members of
   // a larger group share the launch's
   const DevModel &Mg = M.batch ? M.batch[q0] : M;
   const DevModel &opm = M.fop_shared ? M : Mg;
-  const int ni = Mg.ni, mtiles = ni / FG_M, nchunks = ni / FG_KC, nsteps = nchunks * mtiles, ntiles = ni / FG_KC;
+  const int ni = Mg.ni, mtiles = ni / FG_M, nchunks = ni / FG_KC, ntiles = ni / FG_KC;
+  // this CTA's output tiles: msplit CTAs share a row's mtiles (a member narrower than the launch
+  // may leave some of them without a tile)
+  const int mts = mtiles >= msplit ? mtiles / msplit : 1, mt0 = msi * mts;
+  if (mt0 >= mtiles) return;
   if (j > Mg.nj + 1) return;   // a member with fewer rows than the launch
   const int slot = opm.fop_slot[vgrid * (Mg.nj + 3) + j + 1];
   if (slot < 0) return;
@@ -189,7 +194,7 @@ __global__ void __launch_bounds__(FG_THREADS) k_filter_planes_gemm(DevModel M, c
   const unsigned smem_s = (unsigned)__cvta_generic_to_shared(fg_smem);
   const unsigned a_s = smem_s, b_s = smem_s + 4 * FG_A_BYTES;
   const unsigned bars_s = (unsigned)__cvta_generic_to_shared(&bars[0]);
-  const uint32_t tcols = (uint32_t)(mtiles * N) <= 32 ? 32u : 1u << (32 - __clz(mtiles * N - 1));   // a power of 2 >= 32
+  const uint32_t tcols = (uint32_t)(mts * N) <= 32 ? 32u : 1u << (32 - __clz(mts * N - 1));   // a power of 2 >= 32
   if (tid == 0) {
     fail = 0;
     for (int b = 0; b < 4; b++) asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(bars_s + 8 * b));
@@ -234,7 +239,7 @@ __global__ void __launch_bounds__(FG_THREADS) k_filter_planes_gemm(DevModel M, c
   int last_tma = -1, last_commit = -1;
   // step t = (K chunk c, output tile mt); false once the CTA must stop
   auto step = [&](int c, int mt, double (&bn)[BQMAX][4]) -> bool {
-    const int t = c * mtiles + mt, kc = c * FG_KC, abuf = t & 1, bbuf = c & 1;
+    const int t = c * mts + (mt - mt0), kc = c * FG_KC, abuf = t & 1, bbuf = c & 1;
     // both buffers were last read by the products of step t-2 or earlier
     if (t >= 2 && !mbar_wait(bars_s + 8 * abuf, (unsigned)(((t - 2) >> 1) & 1))) atomicExch(&fail, 1);
     __syncthreads();
@@ -251,7 +256,7 @@ __global__ void __launch_bounds__(FG_THREADS) k_filter_planes_gemm(DevModel M, c
       tma_tile(a_lo_s, opm.fop_map, y + FG_M, tb);
       last_tma = t;
     }
-    if (mt == 0) {   // the planes' tile of this K chunk, then the loads of chunk c+2 into its registers
+    if (mt == mt0) {   // the planes' tile of this K chunk, then the loads of chunk c+2 into its registers
       unsigned char *bh = fg_smem + (b_hi_s - smem_s), *bl = bh + b_bytes;
 #pragma unroll
       for (int u = 0; u < BQMAX; u++) {
@@ -274,7 +279,7 @@ __global__ void __launch_bounds__(FG_THREADS) k_filter_planes_gemm(DevModel M, c
       } else {
         last_tma = -1;
         asm volatile("tcgen05.fence::after_thread_sync;");
-        const uint32_t d_mt = dtmem + (uint32_t)(mt * N);
+        const uint32_t d_mt = dtmem + (uint32_t)((mt - mt0) * N);
         for (int ks = 0; ks < FG_KC / 8; ks++) {   // K = 8 TF32 (32 bytes) per instruction
           const unsigned koff = (unsigned)ks * 32;
           const uint32_t acc = (kc > 0 || ks > 0) ? 1u : 0u;
@@ -290,8 +295,8 @@ __global__ void __launch_bounds__(FG_THREADS) k_filter_planes_gemm(DevModel M, c
   };
   bool going = true;
   for (int c = 0; c < nchunks && going; c += 2) {   // nchunks = ni/32 is even
-    for (int mt = 0; mt < mtiles && going; mt++) going = step(c, mt, breg0);
-    for (int mt = 0; mt < mtiles && going; mt++) going = step(c + 1, mt, breg1);
+    for (int mt = mt0; mt < mt0 + mts && going; mt++) going = step(c, mt, breg0);
+    for (int mt = mt0; mt < mt0 + mts && going; mt++) going = step(c + 1, mt, breg1);
   }
   // drain: the last commit covers every earlier one; an operator copy whose wait gave up is
   // waited for again (both bounded), so that nothing writes this CTA's shared or tensor memory
@@ -308,11 +313,11 @@ __global__ void __launch_bounds__(FG_THREADS) k_filter_planes_gemm(DevModel M, c
   asm volatile("tcgen05.fence::after_thread_sync;");
   if (!fail) {
     const int lane = tid & 31;
-    for (int mt = 0; mt < mtiles; mt++)
+    for (int mt = mt0; mt < mt0 + mts; mt++)
       for (int cg = 0; cg < N; cg += 32) {
         // warp w reads tensor-memory lanes 32w..32w+31: output point 128 mt + 32w + lane, columns cg..cg+31
         uint32_t r[32];
-        const uint32_t taddr = dtmem + ((uint32_t)(warp * 32) << 16) + (uint32_t)(mt * N + cg);
+        const uint32_t taddr = dtmem + ((uint32_t)(warp * 32) << 16) + (uint32_t)((mt - mt0) * N + cg);
         asm volatile(
             "tcgen05.ld.sync.aligned.32x32b.x32.b32 {%0, %1, %2, %3, %4, %5, %6, %7, %8, %9, %10, %11, %12, %13, %14, %15, "
             "%16, %17, %18, %19, %20, %21, %22, %23, %24, %25, %26, %27, %28, %29, %30, %31}, [%32];"
@@ -344,6 +349,8 @@ __global__ void __launch_bounds__(FG_THREADS) k_filter_planes_gemm(DevModel M, c
 // alignment slack of the swizzle atoms
 size_t filter_gemm_smem_bytes(int n) { return 1024 + 4 * (size_t)FG_A_BYTES + 4 * (size_t)n * FG_KC * 4; }
 
+static int g_sms = 0;   // SMs of the device (filter_gemm_init, at model creation: not during a graph capture)
+
 bool filter_gemm_usable(const DevModel &M) { return M.fop_map && M.ni % FG_M == 0 && M.ni <= 8 * FG_M; }
 
 // Columns per CTA: up to 64 (32 at ni = 1024), so that two CTAs fit an SM in shared memory
@@ -359,12 +366,24 @@ int launch_filter_planes_gemm(const DevModel &M, const double *src, int src_sel,
   if (G > members) G = members;
   const int N = ((G * pc + 31) / 32) * 32;
   const int groups = (members + G - 1) / G;
-  dim3 grid((unsigned)(M.nj + 3), (unsigned)(nch * groups), 1u);
-  k_filter_planes_gemm<<<grid, FG_THREADS, filter_gemm_smem_bytes(N), s>>>(M, src, src_sel, dst, k0, nplanes, vgrid, shift, pc, G, N);
+  // Few members (a single model): about half of the nj+3 rows are filtered, and one CTA per
+  // (row, group, plane chunk) leaves SMs idle while each CTA walks all its output tiles; split a
+  // row's 128-point output tiles over up to mtiles CTAs (each tile's sums are unchanged) until
+  // there are two CTAs with work per SM
+  const int sms = g_sms > 0 ? g_sms : 152;
+  const int mtiles = M.ni / FG_M;
+  const long long working = (long long)(M.nj + 3) / 2 * nch * groups;
+  int msplit = 1;
+  while (2 * msplit <= mtiles && working * msplit < 2LL * sms) msplit *= 2;
+  dim3 grid((unsigned)(M.nj + 3), (unsigned)(nch * groups * msplit), 1u);
+  k_filter_planes_gemm<<<grid, FG_THREADS, filter_gemm_smem_bytes(N), s>>>(M, src, src_sel, dst, k0, nplanes, vgrid, shift, pc, G, N,
+                                                                          msplit);
   return 0;
 }
 
 int filter_gemm_init(int) {
+  int dev = 0;
+  if (g_sms == 0 && cudaGetDevice(&dev) == cudaSuccess) cudaDeviceGetAttribute(&g_sms, cudaDevAttrMultiProcessorCount, dev);
   return cudaFuncSetAttribute(k_filter_planes_gemm, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)filter_gemm_smem_bytes(FG_NMAX)) ==
                  cudaSuccess
              ? 0
