@@ -369,12 +369,14 @@ int launch_filter_planes_gemm(const DevModel &M, const double *src, int src_sel,
   // Few members (a single model): about half of the nj+3 rows are filtered, and one CTA per
   // (row, group, plane chunk) leaves SMs idle while each CTA walks all its output tiles; split a
   // row's 128-point output tiles over up to mtiles CTAs (each tile's sums are unchanged) until
-  // there are two CTAs with work per SM
+  // there are two CTAs with work per SM.  Not in place: a CTA writes its tiles while the others
+  // of its row still read the whole row.
   const int sms = g_sms > 0 ? g_sms : 152;
   const int mtiles = M.ni / FG_M;
   const long long working = (long long)(M.nj + 3) / 2 * nch * groups;
   int msplit = 1;
-  while (2 * msplit <= mtiles && working * msplit < 2LL * sms) msplit *= 2;
+  if (src != dst)
+    while (2 * msplit <= mtiles && working * msplit < 2LL * sms) msplit *= 2;
   dim3 grid((unsigned)(M.nj + 3), (unsigned)(nch * groups * msplit), 1u);
   k_filter_planes_gemm<<<grid, FG_THREADS, filter_gemm_smem_bytes(N), s>>>(M, src, src_sel, dst, k0, nplanes, vgrid, shift, pc, G, N,
                                                                           msplit);

@@ -204,6 +204,26 @@ def test_jets_one_day(gpu, form, gas_giant):
     _check(_run(a, b, DAY), BOUNDS[(form, "jet-gg" if gas_giant else "jet")])
 
 
+@pytest.mark.parametrize("shape,dt,steps", [((256, 128, 10), 120, 240), ((512, 256, 10), 60, 120)])
+def test_wide_grids_follow_fp64(gpu, shape, dt, steps):
+    """Single models wide enough for two and four 128-point output tiles per row of the
+    tensor-core filter (whose launcher spreads a row's tiles over several CTAs when only a few
+    members fill the GPU, for calls that do not filter in place): the mixed form stays near FP64
+    over hours, and repeats itself bit for bit."""
+    ni, nj, nk = shape
+    ga, f = hs_setup(HSConfig(ni=ni, nj=nj, nk=nk, dt=dt, seed=2))
+    a, b = _pair(ga, f, True, EPIC_PREC_MIXED)
+    _check(_run(a, b, steps), {"u": 2e-4, "v": 2e-4, "hdry": 1e-6, "theta": 1e-8})
+    c = Model(ga, EPIC_PREC_MIXED)
+    c.upload(f)
+    c.timestep(EPIC_SYNC_DIAGS_ONLY)
+    c.run(steps)
+    c.sync()
+    x, y = b.download(), c.download()
+    for k in x.arrays:
+        assert np.array_equal(x.arrays[k], y.arrays[k]), k
+
+
 # The mixed form's error bound of the configuration: relative L2 <= 1e-4 per prognostic after one
 # simulated day, for every member of the ensemble (measured over the members' interior cells).
 NORTH_STAR_BOUND = 1e-4
