@@ -994,9 +994,9 @@ int launch_set_p2etc(const DevModel &M, int update_theta, cudaStream_t s, bool e
 // The gas-giant lower boundary of store_pgrad_vars (epic_funcs_diag.c:3779-3811) with gz_from_u
 // (:4460-4612): GZ_SURFACE in gradient balance with the zonal means of the bottom layer's U and of
 // P3 and RHO3 at K = nk, zero (gz0) at J = jtp.  One block per member, in binary64 in every form
-// and in the reference's order: each row's zonal sums by one thread (RHO3 evaluated as the column
-// kernel of store_pgrad_vars evaluates it, which the reference has just stored when it takes the
-// means); the absolute vorticity of the zonally symmetric wind (vorticity(ON_SIGMATHETA,
+// and in the reference's order: the rows' zonal means (k_gz_means below, RHO3 evaluated as the
+// column kernel of store_pgrad_vars evaluates it, which the reference has just stored when it
+// takes the means); the absolute vorticity of the zonally symmetric wind (vorticity(ON_SIGMATHETA,
 // ABSOLUTE), :4131-4444, v = 0), written into PV3(nk+1) as the reference does (its PV averages
 // read it there, and store_diag leaves that level alone); each row's increment of the Bernoulli
 // function, (zeta+f) u dy (the Sadourney averages of include/epic_pv_schemes.h:55-61 around the v
@@ -1004,17 +1004,30 @@ int launch_set_p2etc(const DevModel &M, int update_theta, cudaStream_t s, bool e
 // row of the reference's arrays is uniform in I, so each row's values are computed once and
 // written across it.
 //
-// RHO3 at K = nk comes first, one thread per cell (k_gz_rho_bottom: the binary64 power is costly
-// on this GPU's FP64 unit, and one block evaluating a row's worth per thread held the step up for
-// milliseconds); the column kernel that follows writes the same plane again.
-__global__ void k_gz_rho_bottom(DevModel M) {
+// The zonal means come first (k_gz_means, one block per row: RHO3 evaluated one thread per cell
+// -- the binary64 power is costly on this GPU's FP64 unit -- and each mean summed from shared
+// memory by one thread in the reference's order); they wait in the first three columns of
+// PV3(nk+1), which k_gz_from_u then rewrites whole.
+__global__ void __launch_bounds__(256) k_gz_means(DevModel M) {
   if (epic_member(M)) return;
-  const int t = (int)(blockIdx.x * blockDim.x + threadIdx.x);
-  if (t >= (M.nj + 1) * M.ni) return;
-  const int J = t / M.ni, I = 1 + t - J * M.ni;
-  const int x = M.at(M.nk, J, I);
-  const double p = M.p3[x];
-  M.rho3[x] = return_density(p, return_temp(M, p, M.theta[x]), M.mu_dry);
+  extern __shared__ double gm[];
+  const int J = (int)blockIdx.x, ni = M.ni, K = M.nk;
+  if (J > M.nj) return;   // a member with fewer rows than the launch
+  const double *U = M.u + plane_offset(M, PL_UV);
+  for (int I = 1 + (int)threadIdx.x; I <= ni; I += (int)blockDim.x) {
+    const int x = M.at(K, J, I);
+    const double p = M.p3[x];
+    gm[I - 1] = U[x];
+    gm[ni + I - 1] = p;
+    gm[2 * ni + I - 1] = return_density(p, return_temp(M, p, M.theta[x]), M.mu_dry);
+  }
+  __syncthreads();
+  if (threadIdx.x < 3) {
+    const double *v = gm + threadIdx.x * ni;
+    double sum = 0.;
+    for (int I = 0; I < ni; I++) sum += v[I];
+    M.pv3[(long long)(K + 1) * M.n2 + M.at2(J, (int)threadIdx.x)] = sum / ni;
+  }
 }
 
 __global__ void __launch_bounds__(256) k_gz_from_u(DevModel M) {
@@ -1023,18 +1036,11 @@ __global__ void __launch_bounds__(256) k_gz_from_u(DevModel M) {
   const int nj = M.nj, ni = M.ni, K = M.nk, j0 = M.jtp;
   double *u1d = gg, *p1d = u1d + (nj + 1), *rho1d = p1d + (nj + 1), *pvr = rho1d + (nj + 1), *gz = pvr + (nj + 2);
   double *kin = gz + (nj + 1), *pvh = kin + (nj + 1);
-  const double *U = M.u + plane_offset(M, PL_UV);
+  const double *means = M.pv3 + (long long)(K + 1) * M.n2;   // k_gz_means
   for (int J = (int)threadIdx.x; J <= nj; J += (int)blockDim.x) {
-    double su = 0., sp = 0., sr = 0.;
-    for (int I = 1; I <= ni; I++) {
-      const int x = M.at(K, J, I);
-      su += U[x];
-      sp += M.p3[x];
-      sr += M.rho3[x];
-    }
-    u1d[J] = su / ni;
-    p1d[J] = sp / ni;
-    rho1d[J] = sr / ni;
+    u1d[J] = means[M.at2(J, 0)];
+    p1d[J] = means[M.at2(J, 1)];
+    rho1d[J] = means[M.at2(J, 2)];
   }
   __syncthreads();
   const double zero = 0.;   // v: the reference's zero array, its operations kept
@@ -1103,7 +1109,7 @@ __global__ void __launch_bounds__(256) k_gz_from_u(DevModel M) {
 
 int launch_store_pgrad_vars(const DevModel &M, cudaStream_t s, bool early) {
   if (M.gas_giant) {
-    k_gz_rho_bottom<<<zg(epic_blocks((long long)(M.nj + 1) * M.ni, 256), M), 256, 0, s>>>(M);
+    k_gz_means<<<zg(M.nj + 1, M), 256, (size_t)3 * M.ni * sizeof(double), s>>>(M);
     k_gz_from_u<<<zg(1, M), 256, (size_t)(7 * M.nj + 8) * sizeof(double), s>>>(M);
   }
   if (M.mixed && early) {   // GZ3 alone: no DZDT3, so no horizontal part either

@@ -297,10 +297,12 @@ __global__ void k_varz_tables(DevModel M, const double *buff, int sel, int index
   }
 }
 
-// The mixed forms' profile: var(gz) to binary64 accuracy as the knot value (binary64) plus the
-// cubic's increment from the knot, evaluated in double-float on the binary64 distance gz - x_knot
-// with the cubic's coefficients computed in binary64 and split into double-floats, and the
-// filtered deviation added back to it in binary64 -- the field itself is never rounded to FP32.
+// The mixed forms' profile: var(gz) to double-float accuracy (~48 bits) as the knot value plus the
+// cubic's increment from the knot, evaluated in double-float on the distance gz - x_knot (gz and
+// x_knot converted to double-floats on the integer pipe), with the cubic's coefficients computed
+// in binary64 and split into double-floats; the deviation buff - var is formed in double-float
+// and the filtered deviation added back to var in binary64 -- the field itself is never rounded
+// to FP32, and the profile's own 48-bit rounding cancels between subtracting and adding it back.
 // The profile has to be this accurate: out = var + F(buff - var) = buff - (I - F)(buff - var), so a
 // rounding error of the profile that varies from column to column (an FP32 increment's does)
 // passes the filter's high-wavenumber part (I - F) straight into THETA and HDRY on every filtered
@@ -309,7 +311,7 @@ __global__ void k_varz_tables(DevModel M, const double *buff, int sel, int index
 // interpolated in log space: knot value exp(y) times exp(increment).  The knot values and the
 // coefficients are tabulated once per row (varz_intervals_mixed); the interval is found in FP32
 // (next to a knot either neighbouring cubic gives the same value, the pieces joining with their
-// first derivative), the distance from its knot in binary64.
+// first derivative), the distance from its knot in double-float.
 struct VarzInterval {
   float x, pad;
   float2 z0, c2, c3;   // double-float coefficients of the cubic in the distance from the knot
@@ -336,9 +338,9 @@ __device__ __forceinline__ void varz_intervals_mixed(const Trip *t, int n, int i
     iv[q] = v;
   }
 }
-__device__ __forceinline__ double varz_profile_mixed(const Trip *t, const double *knot, const VarzInterval *iv, int n, int index,
-                                                     double gzd, const float2 *exp2tab) {
-  const float g = d2f(gzd);
+__device__ __forceinline__ dfl varz_profile_mixed(const Trip *t, const double *knot, const VarzInterval *iv, int n, int index,
+                                                  dfl gzd, const float2 *exp2tab) {
+  const float g = gzd.hi;
   int kay;
   if (g <= iv[0].x) kay = 0;
   else if (g >= iv[n - 1].x) kay = n - 2;
@@ -353,10 +355,9 @@ __device__ __forceinline__ double varz_profile_mixed(const Trip *t, const double
   // a NaN argument fails every comparison: keep the interval index inside the table
   kay = kay < 0 ? 0 : (kay > n - 2 ? n - 2 : kay);
   const VarzInterval v = iv[kay];
-  const float2 xs = split_df(gzd - t[kay].x);
-  const dfl xx(xs.x, xs.y);
+  const dfl xx = gzd - d2df(t[kay].x);
   const dfl inc = xx * (dfl(v.z0.x, v.z0.y) + xx * (dfl(v.c2.x, v.c2.y) + xx * dfl(v.c3.x, v.c3.y)));
-  return index == 2 ? knot[kay] * to_d(exp_df(inc, exp2tab)) : knot[kay] + to_d(inc);
+  return index == 2 ? d2df(knot[kay]) * exp_df(inc, exp2tab) : d2df(knot[kay]) + inc;
 }
 
 // The rest of the THREEDIM zonal_filter: subtract var(gz), filter, add it back.
@@ -387,17 +388,20 @@ __global__ void k_varz_filter_rows(DevModel M, double *buff, int sel, int index,
     load_twiddles(M, fs);
     varz_intervals_mixed(t, n, index, knot, iv);
     __syncthreads();
+    // the profile's argument, its value and the deviation in double-float (integer and FP32
+    // pipes: this kernel had the FP64 unit half busy); the deviation is filtered in binary32 and
+    // added back to the profile in binary64 below, the profile's own rounding cancelling
     for (int i = threadIdx.x + 1; i <= M.ni; i += blockDim.x) {
-      double gzd;
+      dfl gzd;
       switch (index) {
-        case 0: gzd = .5 * (gz[M.at(k, j, i)] + gz[M.at(k, j, i - 1)]); break;
-        case 1: gzd = .5 * (gz[M.at(k, j, i)] + gz[M.at(k, j - 1, i)]); break;
-        case 2: gzd = .5 * (gz[M.at(k, j, i)] + gz[M.at(k - 1, j, i)]); break;
-        default: gzd = gz[M.at(k, j, i)]; break;
+        case 0: gzd = df_ldexp(d2df(gz[M.at(k, j, i)]) + d2df(gz[M.at(k, j, i - 1)]), -1); break;
+        case 1: gzd = df_ldexp(d2df(gz[M.at(k, j, i)]) + d2df(gz[M.at(k, j - 1, i)]), -1); break;
+        case 2: gzd = df_ldexp(d2df(gz[M.at(k, j, i)]) + d2df(gz[M.at(k - 1, j, i)]), -1); break;
+        default: gzd = d2df(gz[M.at(k, j, i)]); break;
       }
-      const double v = varz_profile_mixed(t, knot, iv, n, index, gzd, M.exp2tab);
-      vzd[i] = v;
-      x[i] = d2f(buff[base + i] - v);
+      const dfl v = varz_profile_mixed(t, knot, iv, n, index, gzd, M.exp2tab);
+      vzd[i] = df2d(v);
+      x[i] = (d2df(buff[base + i]) - v).hi;
     }
     __syncthreads();
     filter_row_smem(M, x, vgrid ? M.high_lat_pv : M.high_lat_h, M.at2(j, 0), fs);
