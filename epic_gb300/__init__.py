@@ -115,6 +115,10 @@ def hs_setup(cfg: HSConfig) -> tuple[GridArrays, Fields]:
     _check(lib.epic_hs_grid_build(C.byref(p), C.byref(ga.struct), ga.p_ref.ctypes.data_as(dp),
                                   ga.theta_ref.ctypes.data_as(dp)), "epic_hs_grid_build")
     ga.struct.gas_giant = int(cfg.gas_giant)
+    if cfg.x_h2 > 0.0:   # thermo_setup's cp/R of the mixture (epic_funcs_diag.c:5893-5898), x_3 the rest
+        x3 = max(0.0, 1.0 - cfg.x_h2 - cfg.x_he)
+        ga.struct.x_h2, ga.struct.x_he, ga.struct.x_3 = cfg.x_h2, cfg.x_he, x3
+        ga.struct.cpr = (2.5 * cfg.x_h2 + 2.5 * cfg.x_he + 3.5 * x3) / (cfg.x_h2 + cfg.x_he + x3)
     f = Fields(cfg.ni, cfg.nj, cfg.nk, cfg.uv_scheme)
     if cfg.state == "jet":
         jp = cfg.jet.params()

@@ -44,6 +44,7 @@ class EpicGrid(C.Structure):
         ("nu", C.c_double * 9),
         ("re", C.c_double), ("rp", C.c_double), ("cp", C.c_double), ("rgas", C.c_double),
         ("kappa", C.c_double), ("cpr", C.c_double), ("kinvisc", C.c_double), ("lat0", C.c_double), ("hs_kf", C.c_double),
+        ("x_h2", C.c_double), ("x_he", C.c_double), ("x_3", C.c_double),
         ("lon", _dp), ("lat", _dp), ("rln", _dp), ("rlt", _dp), ("f", _dp), ("m", _dp), ("n", _dp),
         ("mn", _dp), ("g", _dp), ("sigmatheta", _dp), ("dsgth", _dp), ("dsgth_inv", _dp),
         ("h_min", _dp), ("t_sponge_inv", _dp),
@@ -278,6 +279,9 @@ class HSConfig:
     # the gas-giant lower boundary: GZ_SURFACE from gradient balance with the bottom layer's
     # zonal-mean U in every store_pgrad_vars (planet->type "gas-giant"), instead of the terrain
     gas_giant: bool = False
+    # hydrogen thermodynamics (FP64 form): mole fractions of H2 and He; 0 keeps the ideal gas
+    x_h2: float = 0.0
+    x_he: float = 0.0
     extra: dict = field(default_factory=dict)
 
     def params(self) -> EpicHsParams:

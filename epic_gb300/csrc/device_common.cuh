@@ -73,6 +73,8 @@ struct DevModel {
   const float2 *exp2tab;                    // 2^(j/32), j = 0..31, as double-floats (exp_df)
   float2 dfc[DFC_COUNT];                    // kappa, 1/kappa, kappa+1, the hybrid-coordinate constants
                                             // and log(press0) as double-floats (hi, lo)
+  double x_h2, x_he, x_3;                   // hydrogen thermodynamics when x_h2 > 0 (FP64 form)
+  const double *thermo;                     // thermo_setup's tables (thermo_tables in epic_model.cu)
   int gas_giant;                            // planet->type "gas-giant": GZ_SURFACE from gz_from_u in store_pgrad_vars
   int jtp;                                  // grid.jtp: the row where gz_from_u puts GZ_SURFACE's zero
   int mixed;                                // FP32 stencils, advection, hyperviscosity, filter, physics
@@ -239,10 +241,63 @@ __device__ __forceinline__ double return_sigmatheta(const DevModel &M, double th
   const double s = get_sigma(M, pbot, p, ptop);
   return f_sigma(M, s) + g_sigma(M, s) * theta;
 }
-// return_temp (x_h2 = 0), return_density (ideal gas), return_enthalpy (cpr*T*rgas)
-__device__ __forceinline__ double return_temp(const DevModel &M, double p, double theta) { return theta * xpow(M, p / M.press0, M.kappa); }
+// return_density (ideal gas); return_temp and return_enthalpy below (the ideal gas, or hydrogen)
+// The hydrogen thermodynamics of thermo_setup's tables (x_h2 > 0; normal hydrogen, fpara = 0.25,
+// the para fraction the reference takes when the fpara tracer is off, epic_funcs_diag.c:3709;
+// ideal equation of state).  Layout of DevModel::thermo: T(fp, theta_mean) [16][128], the ortho
+// and para enthalpies [2][128], the temperature grid [128], the mean potential temperature grid
+// [128], the para fractions [16].
+constexpr int TH_M = 128, TH_N = 16;
+constexpr double TH_FP = 0.25;
+__device__ __forceinline__ const double *th_t(const DevModel &M) { return M.thermo; }
+__device__ __forceinline__ const double *th_h(const DevModel &M, int q) { return M.thermo + TH_N * TH_M + q * TH_M; }
+__device__ __forceinline__ const double *th_tgrid(const DevModel &M) { return M.thermo + TH_N * TH_M + 2 * TH_M; }
+__device__ __forceinline__ const double *th_thgrid(const DevModel &M) { return M.thermo + TH_N * TH_M + 3 * TH_M; }
+__device__ __forceinline__ const double *th_fpdat(const DevModel &M) { return M.thermo + TH_N * TH_M + 4 * TH_M; }
+
+// return_temp, epic_funcs_diag.c:6112-6210: the ideal relation, or with hydrogen the table of
+// temperature against para fraction and mean potential temperature (bilinear)
+__device__ __forceinline__ double return_temp(const DevModel &M, double p, double theta) {
+  if (M.x_h2 == 0.) return theta * xpow(M, p / M.press0, M.kappa);
+  const double theta1 = theta * xpow(M, p / M.press0, M.kappa);
+  if (theta1 <= 20.) return theta1;
+  if (theta1 >= 600.)
+    return xexp(M, (M.cpr * xlog(M, theta1) - 2.5 * M.x_h2 * ((1. - TH_FP) * -2.105769 + TH_FP * -1.666421)) /
+                       (2.5 * M.x_he + 3.5 * (1. - M.x_he)));
+  const double *fpdat = th_fpdat(M), *thg = th_thgrid(M), *t = th_t(M);
+  const double en = (double)(TH_N - 1) * (TH_FP - fpdat[0]) / (fpdat[TH_N - 1] - fpdat[0]);
+  int n = (int)en;
+  double ffp, fth;
+  if (n > TH_N - 2) { n = TH_N - 2; ffp = 1.; }
+  else if (n < 0) { n = 0; ffp = 0.; }
+  else ffp = fmod(en, 1.);
+  const double em = (double)(TH_M - 1) * (theta1 - thg[0]) / (thg[TH_M - 1] - thg[0]);
+  int m = (int)em;
+  if (m > TH_M - 2) { m = TH_M - 2; fth = 1.; }
+  else if (m < 0) { m = 0; fth = 0.; }
+  else fth = fmod(em, 1.);
+  return t[n * TH_M + m] * (1. - fth) * (1. - ffp) + t[(n + 1) * TH_M + m] * (1. - fth) * (ffp) +
+         t[n * TH_M + m + 1] * (fth) * (1. - ffp) + t[(n + 1) * TH_M + m + 1] * (fth) * (ffp);
+}
 __device__ __forceinline__ double return_density(double p, double t, double mu) { return p * mu / (8.314472e+3 * t); }
-__device__ __forceinline__ double return_enthalpy(const DevModel &M, double t) { return (M.cpr * t) * M.rgas; }
+__device__ __forceinline__ double return_enthalpy(const DevModel &M, double t) {
+  if (M.x_h2 == 0. || t <= 20.) return (M.cpr * t) * M.rgas;
+  double enthalpy;
+  if (t > 500.) {   // hydrogen above the table, epic_funcs_diag.c:6699-6712
+    const double ho = 1545.3790 + 3.5 * (t - 500.), hp = 1720.3776 + 3.5 * (t - 500.);
+    enthalpy = (M.x_h2) * ((1. - TH_FP) * ho + TH_FP * hp) + (M.x_he * 2.5 + M.x_3 * 3.5) * t;
+  } else {          // :6713-6735
+    const double *tg = th_tgrid(M), *ho = th_h(M, 0), *hp = th_h(M, 1);
+    const double em = (double)(TH_M - 1) * (t - tg[0]) / (tg[TH_M - 1] - tg[0]);
+    int m = (int)em;
+    double fract;
+    if (m == TH_M - 1) { m--; fract = 1.; }
+    else fract = fmod(em, 1.);
+    const double h0 = (1. - fract) * ho[m] + (fract) * ho[m + 1], h1 = (1. - fract) * hp[m] + (fract) * hp[m + 1];
+    enthalpy = (M.x_h2) * ((1. - TH_FP) * h0 + (TH_FP) * h1) + (M.x_he * 2.5 + M.x_3 * 3.5) * t;
+  }
+  return enthalpy * M.rgas;
+}
 // onto_kk(P2_INDEX) at a layer, epic_funcs_diag.c:2601-2618
 __device__ __forceinline__ double layer_p(const DevModel &M, double top, double bot) {
   if (fcmp(bot, top) == 0) return .5 * (bot + top);

@@ -296,6 +296,87 @@ int model_error(const Ctl &c) {
                    c.err_k, c.err_j, c.err_i, c.err_val);
 }
 
+// thermo_setup's hydrogen tables (epic_funcs_diag.c:5864-6105) in DevModel::thermo's layout, with
+// the correctly rounded log/exp/pow the FP64 form's kernels use (dd_math.cuh, host-compiled).
+// Per temperature T_i = 500 (i+1)/128 K: the rotational partition sums of ortho and para H2
+// (Dowling et al. 1998, appendix A), their enthalpies and potential temperatures; per para
+// fraction n/15: the temperature on the mean potential temperature grid 20..600 K, inverted by
+// linear interpolation (where the reference's search runs off the end of its arrays, the last
+// interval extrapolates: mean potential temperatures the runs do not reach).
+void thermo_tables(const epic_grid &g, const epic::MathTable &lt, std::vector<double> &out) {
+  constexpr int NM = epic::TH_M, NN = epic::TH_N;
+  auto xlog = [&](double x) { return epic::cr_log(x, lt); };
+  auto xexp = [&](double x) { return epic::cr_exp(x, lt); };
+  const double xh2 = g.x_h2, xhe = g.x_he, x3 = g.x_3;
+  const double cpr = (2.5 * xh2 + 2.5 * xhe + 3.5 * x3) / (xh2 + xhe + x3);
+  const double t0 = 1., p0 = 1.e+5, theta = 87.567, ndeg[2] = {3., 1.}, ln2 = 0.69314718055994530942;
+  const double c1 = xlog(1.3806503e-23 * t0 / p0 *
+                         epic::cr_pow(2. * M_PI * (1.67262158e-27 / 6.62606876e-34) * (1.3806503e-23 * t0 / 6.62606876e-34), 1.5, lt));
+  const double c2 = xlog(9.), p = p0;
+  std::vector<double> temp(NM), tho(NM), thp(NM), tvec(NM), thvec(NM), aa(NM);
+  out.assign((size_t)NN * NM + 4 * NM + NN, 0.);
+  double *T = out.data(), *HO = T + NN * NM, *HP = HO + NM, *TG = HP + NM, *THG = TG + NM, *FP = THG + NM;
+  for (int i = 0; i < NM; i++) {
+    const double temperature = 500. * (double)(i + 1) / (double)NM;
+    double ho, hp, pottempo, pottempp;
+    if (temperature < 10.) {   // placeholders of the reference below 10 K
+      ho = 2.5 * temperature;
+      hp = 2.5 * temperature;
+      pottempo = temperature;
+      pottempp = temperature;
+    } else {
+      double y = theta / temperature, z[3][2] = {{0., 0.}, {0., 0.}, {0., 0.}}, term = 0., a[7];
+      y = y < 30. ? y : 30.;
+      for (int j = 1; j <= 50; j++) {
+        const int jn[2] = {2 * j - 1, 2 * j - 2};
+        for (int n = 0; n < 2; n++) {
+          term = ndeg[n] * (2 * jn[n] + 1) * xexp(-jn[n] * (jn[n] + 1) * y);
+          for (int m = 0; m < 3; m++) {
+            z[m][n] += term;
+            if (m < 2) term *= jn[n] * (jn[n] + 1);
+          }
+        }
+        if (j > 1 && term < 1.e-20) break;
+      }
+      for (int n = 0; n < 2; n++) {
+        a[n + 1] = theta * z[1][n] / z[0][n];
+        a[n + 5] = xlog(z[0][n]);
+      }
+      ho = a[1] + 2.5 * temperature - 2. * theta;
+      hp = a[2] + 2.5 * temperature;
+      const double so = -xlog(p / p0) + 2.5 * xlog(temperature) + 1.5 * ln2 + c1 + (ho + 2. * theta) / temperature + a[5];
+      const double sp = -xlog(p / p0) + 2.5 * xlog(temperature) + 1.5 * ln2 + c1 + hp / temperature + a[6];
+      pottempo = xexp(0.4 * (so - c2 - 1.5 * ln2 - c1 - 2.5));
+      pottempp = xexp(0.4 * (sp - 1.5 * ln2 - c1 - 2.5));
+    }
+    temp[i] = temperature;
+    tho[i] = pottempo;
+    thp[i] = pottempp;
+    HO[i] = ho;
+    HP[i] = hp;
+    TG[i] = temperature;
+  }
+  for (int m = 0; m < NM; m++) THG[m] = (20. * (double)(NM - (m + 1)) + 600. * (double)(m)) / (double)(NM - 1);
+  for (int n = 0; n < NN; n++) {
+    FP[n] = ((double)(n)) / (double)(NN - 1);
+    for (int i = 0; i < NM; i++) {
+      const double thetaln = (xh2 * 2.5 * ((1. - FP[n]) * xlog(tho[i]) + (FP[n]) * xlog(thp[i])) + (xhe * 2.5 + x3 * 3.5) * xlog(temp[i])) / cpr;
+      thvec[i] = xexp(thetaln);
+      tvec[i] = temp[i];
+    }
+    for (int j = 0; j < NM; j++) aa[j] = tvec[j];
+    tvec[NM - 1] = aa[NM - 1];
+    for (int i = 0; i < NM; i++) {
+      int j = 1;
+      for (; j < NM; j++)
+        if (thvec[j] >= THG[i]) break;
+      if (j == NM) j = NM - 1;
+      tvec[i] = aa[j - 1] + (aa[j] - aa[j - 1]) * (THG[i] - thvec[j - 1]) / (thvec[j] - thvec[j - 1]);
+    }
+    for (int m = 0; m < NM; m++) T[n * NM + m] = tvec[m];
+  }
+}
+
 // Device bytes of a model's pool: state, scratch and tables, carved in 256-byte units.
 size_t model_pool_bytes(const epic_grid &g) {
   const epic::Layout L(g.ni, g.nj, g.nk);
@@ -309,7 +390,7 @@ size_t model_pool_bytes(const epic_grid &g) {
   return rnd(sizeof(Ctl)) + (n_state3 + n_scratch3) * rnd(n3 * 8) + 3 * rnd(n2 * 8) + rnd((size_t)(g.nj + 3) * (g.nk + 2) * 3 * 8) +
          rnd(ni1 * 8) + 10 * rnd(nj1 * 8) + 3 * rnd(nk1 * 8) + rnd((g.nk + 2) * 8) + rnd((g.k_sponge + 1) * 8) +
          2 * rnd(3 * (g.nj + 2) * 8) + rnd(ntw * 8) + rnd(ntw * 4) + 2 * rnd((g.nj + 1) * 8) + rnd(sizeof(epic::MathTable)) +
-         rnd(32 * sizeof(float2)) + 4096;
+         rnd(32 * sizeof(float2)) + rnd(((size_t)epic::TH_N * epic::TH_M + 4 * epic::TH_M + epic::TH_N) * 8) + 4096;
 }
 
 }  // namespace
@@ -329,6 +410,8 @@ extern "C" int epic_model_create(const epic_grid *g, int32_t precision, epic_mod
     return set_error(EPIC_ERR_ARG, "precision form %d not available", precision);
   if (g->ni < 4 || (g->ni & (g->ni - 1)) || g->ni > EPIC_MAX_NI) return set_error(EPIC_ERR_ARG, "ni=%d: need a power of 2 in [4,%d]", g->ni, EPIC_MAX_NI);
   if (g->nj < 3 || g->nk < 3 || g->nk > EPIC_MAX_NK) return set_error(EPIC_ERR_ARG, "nj=%d nk=%d out of range", g->nj, g->nk);
+  if (g->x_h2 < 0. || (g->x_h2 > 0. && precision != EPIC_PREC_FP64))
+    return set_error(EPIC_ERR_ARG, "x_h2=%g: hydrogen thermodynamics are in the FP64 form only", g->x_h2);
   if (g->gas_giant && (g->jtp < 0 || g->jtp > g->nj))
     return set_error(EPIC_ERR_ARG, "gas giant: jtp=%d outside the rows 0..%d", g->jtp, g->nj);
   if (3. * (g->ni + 2) * (g->nj + 3) * (g->nk + 2) >= 2147483648.)
@@ -440,6 +523,7 @@ extern "C" int epic_model_create(const epic_grid *g, int32_t precision, epic_mod
   double *coslat4 = carve<double>(p, g->nj + 1);
   epic::MathTable *lt = carve<epic::MathTable>(p, 1);
   float2 *exp2tab = carve<float2>(p, 32);
+  double *thermo_d = carve<double>(p, (size_t)epic::TH_N * epic::TH_M + 4 * epic::TH_M + epic::TH_N);
   if ((size_t)(p - m->pool) > bytes) {
     epic_model_destroy(m);
     return set_error(EPIC_ERR_NOMEM, "internal pool layout overflow");
@@ -475,6 +559,13 @@ extern "C" int epic_model_create(const epic_grid *g, int32_t precision, epic_mod
   for (int J = 0; J <= g->nj; J++) cl4[J] = epic::cr_pow(cl[J], 4., host_lt[0]);
   up(coslat4, cl4.data(), cl4.size());
   cudaMemcpyAsync(lt, host_lt.data(), sizeof(epic::MathTable), cudaMemcpyHostToDevice, m->stream);
+  std::vector<double> thermo_host;   // hydrogen thermodynamics (x_h2 > 0)
+  if (g->x_h2 > 0.) {
+    thermo_tables(*g, host_lt[0], thermo_host);
+    cudaMemcpyAsync(thermo_d, thermo_host.data(), thermo_host.size() * sizeof(double), cudaMemcpyHostToDevice, m->stream);
+  }
+  d.thermo = thermo_d;
+  d.x_h2 = g->x_h2; d.x_he = g->x_he; d.x_3 = g->x_3;
   // 2^(j/32) as double-floats for the double-float exponential of the mixed form
   std::vector<float2> e2(32);
   for (int q = 0; q < 32; q++) {
@@ -806,6 +897,7 @@ bool batch_compatible(const DevModel &a, const DevModel &b, const char **why) {
     *why = "physics options";
   else if ((a.nudiv == 0.) != (b.nudiv == 0.)) *why = "divergence damping on/off";
   else if (a.gas_giant != b.gas_giant) *why = "lower boundary (gas giant or terrain)";
+  else if ((a.x_h2 > 0.) != (b.x_h2 > 0.)) *why = "thermodynamics (hydrogen tables or ideal cp)";
   else if (tensor_filter(a) != tensor_filter(b)) *why = "zonal filter path (ni a multiple of 128 or not)";
   else
     for (int i = 0; i < 9; i++)

@@ -96,6 +96,13 @@ typedef struct epic_grid {
   double  lat0;                /* filter/taper latitude [deg]; the reference's LAT0 is 45      */
   double  hs_kf;               /* Held-Suarez PBL drag rate k_f [1/s]; the reference hard-codes
                                   HELD_SUAREZ_PBL_NU0 = 1/86400 (epic_timestep.c:1292)         */
+  double  x_h2, x_he, x_3;     /* planet->x_h2, x_he, x_3: mole fractions of molecular hydrogen,
+                                  helium and the rest.  x_h2 > 0 takes the reference's hydrogen
+                                  thermodynamics (thermo_setup's ortho/para tables, normal
+                                  hydrogen, fpara = 0.25: return_temp and return_enthalpy by table
+                                  interpolation); cpr must then be thermo_setup's
+                                  (2.5 x_h2 + 2.5 x_he + 3.5 x_3) / (x_h2 + x_he + x_3).  FP64
+                                  form only.                                                    */
   const double *lon;           /* [2*(ni+1)+1]                                                  */
   const double *lat, *rln, *rlt, *f, *m, *n, *mn, *g;   /* [2*(nj+1)+1]                         */
   const double *sigmatheta, *dsgth, *dsgth_inv;         /* [2*(nk+1)+1]                         */

@@ -46,6 +46,8 @@ struct ep_model {
   /* hsu_advection column buffers (static in the reference) */
   double *wm, *wp, *w_a, *w_a_pred, *w_a_min, *w_ff, *w_a_diff1, *w_a_diff2, *w_aaa;
   double coef[9], max_nu[9], m0, n0, mu_dry, eps13;
+  /* hydrogen thermodynamics (x_h2 > 0): thermo_setup's tables */
+  double th_t[16][128], th_array[5][128], th_tgrid[128], th_thetagrid[128], th_fpdat[16];
   int it_zero, it_minus1, it_minus2, it_uv, it_uv_dis, it_uv_tend;
   long itime, model_time;
   int uploaded;
@@ -298,13 +300,157 @@ static double return_sigmatheta(const ep_model *M, double theta, double p, doubl
   sigma = get_sigma(pbot, p, ptop);
   return f_sigma(M, sigma) + g_sigma(M, sigma) * theta;
 }
-/* return_temp with x_h2 = 0, :6146-6152 */
-static double return_temp(const ep_model *M, double p, double theta) { return theta * pow(p / M->g.press0, M->g.kappa); }
+/* Hydrogen thermodynamics (x_h2 > 0), after thermo_setup (epic_funcs_diag.c:5864-6105): per
+ * temperature T_i = 500 (i+1)/128 K the rotational partition sums of ortho and para H2 (Dowling et
+ * al. 1998, appendix A), their enthalpies, curly F, the equilibrium para fraction and the ortho and
+ * para potential temperatures; then, for 16 para fractions, the temperature on a grid of mean
+ * potential temperatures 20..600 K by linear interpolation of the inverted relation.  Where the
+ * reference's inversion search does not find a bracketing entry it reads one past its arrays; here
+ * the last interval extrapolates (those entries belong to mean potential temperatures the runs never
+ * reach). */
+#define MDIM_TH 128
+#define NDIM_TH 16
+#define THLO_TH 20.
+#define THHI_TH 600.
+#define CCOLN_TH -2.105769
+#define CCPLN_TH -1.666421
+#define CPRH2 2.5
+#define CPRHE 2.5
+#define CPR3 3.5
+#define FPARA_NORMAL 0.25   /* the para fraction when the fpara tracer is off, epic_funcs_diag.c:3709 */
+static void thermo_setup(ep_model *M) {
+  const double xh2 = M->g.x_h2, xhe = M->g.x_he, x3 = M->g.x_3;
+  const double cpr = (CPRH2 * xh2 + CPRHE * xhe + CPR3 * x3) / (xh2 + xhe + x3);
+  const double t0 = 1., p0 = 1.e+5, theta = 87.567, ndeg[2] = {3., 1.};
+  const double c1 = log(1.3806503e-23 * t0 / p0 * pow(2. * M_PI * (1.67262158e-27 / 6.62606876e-34) * (1.3806503e-23 * t0 / 6.62606876e-34), 1.5));
+  const double c2 = log(9.);
+  const double p = p0;
+  double temp[MDIM_TH], tho[MDIM_TH], thp[MDIM_TH], tvec[MDIM_TH], thvec[MDIM_TH], aa[MDIM_TH];
+  int i, j, m, n;
+  for (i = 0; i < MDIM_TH; i++) {
+    const double temperature = 500. * (double)(i + 1) / (double)MDIM_TH;
+    double ho, hp, pottempo, pottempp, ff, a[8];
+    if (temperature < 10.) {
+      ho = CPRH2 * temperature;
+      hp = CPRH2 * temperature;
+      pottempo = temperature;
+      pottempp = temperature;
+      a[0] = 1.; a[1] = 175.1340; a[2] = 0.; a[3] = 0.; a[4] = 0.; a[5] = 0.; a[6] = 0.; a[7] = 0.;
+      ff = 0.;
+    } else {
+      double y = theta / temperature, z[3][2], term = 0., den, so, sp;
+      int jn[2];
+      y = dmin(y, 30.);
+      for (n = 0; n < 2; n++)
+        for (m = 0; m < 3; m++) z[m][n] = 0.;
+      for (j = 1; j <= 50; j++) {
+        jn[0] = 2 * j - 1;
+        jn[1] = jn[0] - 1;
+        for (n = 0; n < 2; n++) {
+          term = ndeg[n] * (2 * jn[n] + 1) * exp(-jn[n] * (jn[n] + 1) * y);
+          for (m = 0; m < 3; m++) {
+            z[m][n] += term;
+            if (m < 2) term *= jn[n] * (jn[n] + 1);
+          }
+        }
+        if (j > 1 && term < 1.e-20) break;
+      }
+      den = z[0][0] + z[0][1];
+      a[0] = z[0][1] / den;
+      for (n = 0; n < 2; n++) {
+        a[n + 1] = theta * z[1][n] / z[0][n];
+        a[n + 3] = y * y * (z[0][n] * z[2][n] - z[1][n] * z[1][n]) / (z[0][n] * z[0][n]);
+        a[n + 5] = log(z[0][n]);
+      }
+      a[7] = (1. - a[0]) * a[3] + a[0] * a[4] + (a[2] - a[1]) * y / temperature * (z[1][1] * z[0][0] - z[0][1] * z[1][0]) / (den * den);
+      ho = a[1] + CPRH2 * temperature - 2. * theta;
+      hp = a[2] + CPRH2 * temperature;
+      so = -log(p / p0) + 2.5 * log(temperature) + 1.5 * M_LN2 + c1 + (ho + 2. * theta) / temperature + a[5];
+      sp = -log(p / p0) + 2.5 * log(temperature) + 1.5 * M_LN2 + c1 + hp / temperature + a[6];
+      pottempo = exp(0.4 * (so - c2 - 1.5 * M_LN2 - c1 - 2.5));
+      pottempp = exp(0.4 * (sp - 1.5 * M_LN2 - c1 - 2.5));
+      ff = -(so - c2 - 1.5 * M_LN2 - c1 - 2.5 - ho / temperature) + (sp - 1.5 * M_LN2 - c1 - 2.5 - hp / temperature);
+      ff *= temperature;
+    }
+    temp[i] = temperature;
+    tho[i] = pottempo;
+    thp[i] = pottempp;
+    M->th_array[0][i] = ho;
+    M->th_array[1][i] = hp;
+    M->th_array[2][i] = ff;
+    M->th_array[3][i] = a[0];
+    M->th_array[4][i] = a[1] - a[2];
+    M->th_tgrid[i] = temperature;
+  }
+  for (m = 0; m < MDIM_TH; m++)
+    M->th_thetagrid[m] = (THLO_TH * (double)(MDIM_TH - (m + 1)) + THHI_TH * (double)(m)) / (double)(MDIM_TH - 1);
+  for (n = 0; n < NDIM_TH; n++) {
+    M->th_fpdat[n] = ((double)(n)) / (double)(NDIM_TH - 1);
+    for (i = 0; i < MDIM_TH; i++) {
+      const double thetaln = (xh2 * CPRH2 * ((1. - M->th_fpdat[n]) * log(tho[i]) + (M->th_fpdat[n]) * log(thp[i])) +
+                              (xhe * CPRHE + x3 * CPR3) * log(temp[i])) / cpr;
+      thvec[i] = exp(thetaln);
+      tvec[i] = temp[i];
+    }
+    for (j = 0; j < MDIM_TH; j++) aa[j] = tvec[j];
+    tvec[MDIM_TH - 1] = aa[MDIM_TH - 1];
+    for (i = 0; i < MDIM_TH; i++) {
+      for (j = 1; j < MDIM_TH; j++)
+        if (thvec[j] >= M->th_thetagrid[i]) break;
+      if (j == MDIM_TH) j = MDIM_TH - 1;
+      tvec[i] = aa[j - 1] + (aa[j] - aa[j - 1]) * (M->th_thetagrid[i] - thvec[j - 1]) / (thvec[j] - thvec[j - 1]);
+    }
+    for (m = 0; m < MDIM_TH; m++) M->th_t[n][m] = tvec[m];
+  }
+}
+
+/* return_temp, :6112-6210: x_h2 = 0 the ideal relation; x_h2 > 0 the table of thermo_setup at
+ * fp = 0.25 (bilinear in fp and the mean potential temperature), ideal equation of state */
+static double return_temp(const ep_model *M, double p, double theta) {
+  double theta1, en, em, fract_fp, fract_theta;
+  int n, m;
+  if (M->g.x_h2 == 0.) return theta * pow(p / M->g.press0, M->g.kappa);
+  theta1 = theta * pow(p / M->g.press0, M->g.kappa);
+  if (theta1 <= THLO_TH) return theta1;
+  if (theta1 >= THHI_TH)
+    return exp((M->g.cpr * log(theta1) - CPRH2 * M->g.x_h2 * ((1. - FPARA_NORMAL) * CCOLN_TH + FPARA_NORMAL * CCPLN_TH)) /
+               (CPRHE * M->g.x_he + CPR3 * (1. - M->g.x_he)));
+  en = (double)(NDIM_TH - 1) * (FPARA_NORMAL - M->th_fpdat[0]) / (M->th_fpdat[NDIM_TH - 1] - M->th_fpdat[0]);
+  n = (int)en;
+  if (n > NDIM_TH - 2) { n = NDIM_TH - 2; fract_fp = 1.; }
+  else if (n < 0) { n = 0; fract_fp = 0.; }
+  else fract_fp = fmod(en, 1.);
+  em = (double)(MDIM_TH - 1) * (theta1 - M->th_thetagrid[0]) / (M->th_thetagrid[MDIM_TH - 1] - M->th_thetagrid[0]);
+  m = (int)em;
+  if (m > MDIM_TH - 2) { m = MDIM_TH - 2; fract_theta = 1.; }
+  else if (m < 0) { m = 0; fract_theta = 0.; }
+  else fract_theta = fmod(em, 1.);
+  return M->th_t[n][m] * (1. - fract_theta) * (1. - fract_fp) + M->th_t[n + 1][m] * (1. - fract_theta) * (fract_fp) +
+         M->th_t[n][m + 1] * (fract_theta) * (1. - fract_fp) + M->th_t[n + 1][m + 1] * (fract_theta) * (fract_fp);
+}
 /* return_density, ideal gas, :6353-6385 */
 static double return_density(double p, double temperature, double mu) { return p * mu / (R_GAS * temperature); }
-/* return_enthalpy with x_h2 = 0: cpr*T*rgas, :6678-6746 */
+/* return_enthalpy, :6652-6746: x_h2 = 0 cpr*T*rgas; x_h2 > 0 the ortho/para enthalpies of
+ * thermo_setup's table at fp = 0.25, ideal equation of state */
 static double return_enthalpy(const ep_model *M, double temperature) {
-  double enthalpy = M->g.cpr * temperature;
+  double enthalpy;
+  if (M->g.x_h2 == 0.) {
+    enthalpy = M->g.cpr * temperature;
+  } else if (temperature <= 20.) {   /* hydrogen, :6692-6740, fp = 0.25, ideal */
+    enthalpy = M->g.cpr * temperature;
+  } else if (temperature > 500.) {
+    const double ho = 1545.3790 + 3.5 * (temperature - 500.), hp = 1720.3776 + 3.5 * (temperature - 500.);
+    enthalpy = (M->g.x_h2) * ((1. - FPARA_NORMAL) * ho + FPARA_NORMAL * hp) + (M->g.x_he * 2.5 + M->g.x_3 * 3.5) * temperature;
+  } else {
+    const double em = (double)(MDIM_TH - 1) * (temperature - M->th_tgrid[0]) / (M->th_tgrid[MDIM_TH - 1] - M->th_tgrid[0]);
+    int m = (int)em;
+    double fract, h0, h1;
+    if (m == MDIM_TH - 1) { m--; fract = 1.; }
+    else fract = fmod(em, 1.);
+    h0 = (1. - fract) * M->th_array[0][m] + (fract) * M->th_array[0][m + 1];
+    h1 = (1. - fract) * M->th_array[1][m] + (fract) * M->th_array[1][m + 1];
+    enthalpy = (M->g.x_h2) * ((1. - FPARA_NORMAL) * h0 + (FPARA_NORMAL) * h1) + (M->g.x_he * 2.5 + M->g.x_3 * 3.5) * temperature;
+  }
   return enthalpy * M->g.rgas;
 }
 /* onto_kk for P2_INDEX at a layer, :2601-2618 */
@@ -2266,6 +2412,7 @@ ep_model *ep_create(const epic_grid *g) {
   eps *= 2.;
   M->eps13 = pow(eps, 1. / 3.);
   M->mu_dry = 1. / (M->g.rgas / R_GAS);
+  if (M->g.x_h2 > 0.) thermo_setup(M);
   {
     /* set_max_nu, epic_subgrid.c:82-158 */
     double dt = (double)g->dt, dy2 = g->dy0 * g->dy0;

@@ -47,6 +47,14 @@ int ref_init(const epic_grid *g, const epic_fields *f) {
   /* the gas-giant lower boundary on the same planet: store_pgrad_vars then takes GZ_SURFACE
    * from gz_from_u (epic_funcs_diag.c:3779-3811) */
   if (g->gas_giant) strcpy(planet->type, "gas-giant");
+  /* hydrogen thermodynamics on the same planet: the composition, then the reference's own
+   * thermo_setup (its tables and cpr), as its initialisation calls it */
+  if (g->x_h2 > 0.) {
+    planet->x_h2 = g->x_h2;
+    planet->x_he = g->x_he;
+    planet->x_3 = g->x_3;
+    thermo_setup(planet, &planet->cpr);
+  }
   if (planet->re != g->re || planet->rp != g->rp || planet->cp != g->cp || planet->rgas != g->rgas ||
       planet->kappa != g->kappa || planet->cpr != g->cpr || planet->kinvisc != g->kinvisc)
     return -2;

@@ -92,6 +92,13 @@ def test_batch_rejects_incompatible_members(gpu):
     g.upload(fg)
     with pytest.raises(EpicError, match="lower boundary"):
         Batch([a, g])
+    gh, fh = hs_setup(HSConfig(ni=32, nj=16, nk=10, dt=300, seed=7, x_h2=0.864, x_he=0.136))
+    h = Model(gh, EPIC_PREC_FP64)
+    h.upload(fh)
+    with pytest.raises(EpicError, match="thermodynamics"):
+        Batch([a, h])
+    with pytest.raises(EpicError, match="x_h2"):   # hydrogen tables are in the FP64 form only
+        Model(gh, EPIC_PREC_MIXED)
     Batch([a, f]).close()   # sizes alone may differ
 
 

@@ -52,9 +52,13 @@ def _differing(a, b):
 
 def _state(state):
     """HSConfig keywords of a named state: "hs" (the column at rest), "jet" (the balanced jets);
-    "-gg" adds the gas-giant lower boundary (GZ_SURFACE from gz_from_u)."""
+    "-gg" adds the gas-giant lower boundary (GZ_SURFACE from gz_from_u), "-h2" a hydrogen-helium
+    atmosphere (thermo_setup's tables)."""
+    extra = {}
+    if state.endswith("-h2"):
+        state, extra = state[:-3], {"x_h2": 0.864, "x_he": 0.136}
     base = state[:-3] if state.endswith("-gg") else state
-    return {"state": base, "profile": EPIC_PROFILE_N2 if base == "jet" else 0, "gas_giant": state.endswith("-gg")}
+    return {"state": base, "profile": EPIC_PROFILE_N2 if base == "jet" else 0, "gas_giant": state.endswith("-gg"), **extra}
 
 
 def _stage_by_stage(cfg):
@@ -77,7 +81,8 @@ def _stage_by_stage(cfg):
     assert not failures, "\n".join(failures)
 
 
-@pytest.mark.parametrize("adv,state", [(EPIC_ADV_HSU, "hs"), (EPIC_ADV_AKIMA, "hs"), (EPIC_ADV_HSU, "jet"), (EPIC_ADV_HSU, "jet-gg")])
+@pytest.mark.parametrize("adv,state", [(EPIC_ADV_HSU, "hs"), (EPIC_ADV_AKIMA, "hs"), (EPIC_ADV_HSU, "jet"), (EPIC_ADV_HSU, "jet-gg"),
+                                       (EPIC_ADV_HSU, "hs-h2"), (EPIC_ADV_HSU, "jet-gg-h2")])
 @pytest.mark.parametrize("scheme", [EPIC_UV_AB3, EPIC_UV_LEAPFROG])
 def test_stage_by_stage(gpu, scheme, adv, state):
     """Each reference function on the path, GPU vs the correctly rounded restatement, bit for
@@ -92,7 +97,8 @@ def test_stage_by_stage_divergence_damping(gpu, scheme):
     _stage_by_stage(HSConfig(ni=32, nj=16, nk=10, dt=300, uv_scheme=scheme, seed=5, nudiv=0.5))
 
 
-@pytest.mark.parametrize("adv,state", [(EPIC_ADV_HSU, "hs"), (EPIC_ADV_AKIMA, "hs"), (EPIC_ADV_HSU, "jet"), (EPIC_ADV_HSU, "jet-gg")])
+@pytest.mark.parametrize("adv,state", [(EPIC_ADV_HSU, "hs"), (EPIC_ADV_AKIMA, "hs"), (EPIC_ADV_HSU, "jet"), (EPIC_ADV_HSU, "jet-gg"),
+                                       (EPIC_ADV_HSU, "hs-h2")])
 @pytest.mark.parametrize("scheme", [EPIC_UV_AB3, EPIC_UV_LEAPFROG])
 def test_steps_bitwise(gpu, scheme, adv, state):
     """Ten graph-replayed steps at 64x32x20 equal the correctly rounded restatement bit for bit."""
@@ -128,7 +134,9 @@ def test_sync_diags(gpu):
                                                           (EPIC_UV_AB3, 200, 1e-8, EPIC_ADV_HSU, "hs"),
                                                           (EPIC_UV_AB3, 100, 1e-8, EPIC_ADV_HSU, "hs-nudiv"),
                                                           (EPIC_UV_AB3, 1, 1e-11, EPIC_ADV_HSU, "jet-gg"),
-                                                          (EPIC_UV_AB3, 100, 1e-8, EPIC_ADV_HSU, "jet-gg")])
+                                                          (EPIC_UV_AB3, 100, 1e-8, EPIC_ADV_HSU, "jet-gg"),
+                                                          (EPIC_UV_AB3, 1, 1e-11, EPIC_ADV_HSU, "hs-h2"),
+                                                          (EPIC_UV_AB3, 100, 1e-8, EPIC_ADV_HSU, "hs-h2")])
 def test_full_step(gpu, scheme, nsteps, tol, adv, state):
     """The 64x32x10 configuration (Held-Suarez column or zonal jets; "hs-nudiv": the column with
     divergence damping, nudiv_nondim = 0.5; "jet-gg": the jets over the gas-giant lower
