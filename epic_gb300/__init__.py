@@ -18,8 +18,8 @@ import os
 import numpy as np
 
 from .abi import (EPIC_ADV_AKIMA, EPIC_ADV_HSU, EPIC_IO_ALL, EPIC_IO_STATE, EPIC_PREC_FP64, EPIC_PREC_MIXED, EPIC_PREC_MIXED_FAST, EPIC_PROFILE_HS_EQ,
-                  EPIC_PROFILE_N2, EPIC_PROFILE_TABLE, EPIC_STEP_PROGS_AND_SYNC_DIAGS, EPIC_SYNC_DIAGS_ONLY, EPIC_UV_AB3, EPIC_UV_LEAPFROG,
-                  EpicFields, EpicGrid, EpicHsParams, EpicJetParams, Fields, GridArrays, HSConfig, JetConfig, Layout)
+                  EPIC_PROFILE_N2, EPIC_PROFILE_TABLE, EPIC_STEP_PROGS_AND_SYNC_DIAGS, EPIC_SYNC_DIAGS_ONLY, EPIC_TURB_OFF,
+                  EPIC_TURB_SA_DES, EPIC_UV_AB3, EPIC_UV_LEAPFROG, TURB_FIELDS, EpicFields, EpicGrid, EpicHsParams, EpicJetParams, Fields, GridArrays, HSConfig, JetConfig, Layout)
 
 TUNE_GROUPS = 10   # EPIC_TUNE_GROUPS
 TUNE_HSU_MERID_VARIANT = 9   # table entry: 0 automatic, 1 fused march, 2 four passes
@@ -119,7 +119,13 @@ def hs_setup(cfg: HSConfig) -> tuple[GridArrays, Fields]:
         x3 = max(0.0, 1.0 - cfg.x_h2 - cfg.x_he)
         ga.struct.x_h2, ga.struct.x_he, ga.struct.x_3 = cfg.x_h2, cfg.x_he, x3
         ga.struct.cpr = (2.5 * cfg.x_h2 + 2.5 * cfg.x_he + 3.5 * x3) / (cfg.x_h2 + cfg.x_he + x3)
-    f = Fields(cfg.ni, cfg.nj, cfg.nk, cfg.uv_scheme)
+    # planet->dynvisc of the Held-Suarez planet (epic_globals.c:242-253)
+    ga.struct.dynvisc = 1.718e-5
+    if cfg.turbulence:
+        ga.struct.turbulence = EPIC_TURB_SA_DES
+        ga.struct.diffusion_direction = cfg.diffusion_direction
+        ga.struct.stability_factor = cfg.stability_factor
+    f = Fields(cfg.ni, cfg.nj, cfg.nk, cfg.uv_scheme, turbulence=cfg.turbulence)
     if cfg.state == "jet":
         jp = cfg.jet.params()
         _check(lib.epic_jet_initial_state(C.byref(ga.struct), C.byref(p), C.byref(jp), C.c_uint64(cfg.seed),
@@ -129,6 +135,8 @@ def hs_setup(cfg: HSConfig) -> tuple[GridArrays, Fields]:
                                          C.byref(f.struct)), "epic_hs_initial_state")
     else:
         raise ValueError(f"unknown initial state {cfg.state!r}")
+    if cfg.turbulence:   # init_subgrid, epic_subgrid.c:2127-2160
+        f.nu_turb[...] = ga.struct.kinvisc * 20.0
     return ga, f
 
 
@@ -305,4 +313,4 @@ class Batch:
 
 __all__ = ["Model", "Batch", "model_bytes", "hs_setup", "load_library", "EpicError", "HSConfig", "Fields", "GridArrays", "Layout",
            "EPIC_ADV_AKIMA", "EPIC_ADV_HSU", "EPIC_PREC_FP64", "EPIC_PREC_MIXED", "EPIC_PREC_MIXED_FAST", "EPIC_STEP_PROGS_AND_SYNC_DIAGS", "EPIC_SYNC_DIAGS_ONLY",
-           "EPIC_UV_AB3", "EPIC_UV_LEAPFROG", "LIB_PATH", "TUNE_GROUPS", "TUNE_HSU_MERID_VARIANT", "np"]
+           "EPIC_UV_AB3", "EPIC_UV_LEAPFROG", "EPIC_TURB_OFF", "EPIC_TURB_SA_DES", "TURB_FIELDS", "LIB_PATH", "TUNE_GROUPS", "TUNE_HSU_MERID_VARIANT", "np"]

@@ -25,6 +25,11 @@ EPIC_PROFILE_N2 = 1
 EPIC_PROFILE_TABLE = 2
 EPIC_IO_ALL = 0
 EPIC_IO_STATE = 1
+EPIC_TURB_OFF = 0
+EPIC_TURB_SA_DES = 1
+EPIC_DIFFUSION_HORIZONTAL_AND_VERTICAL = 1
+EPIC_DIFFUSION_JUST_HORIZONTAL = 2
+EPIC_DIFFUSION_JUST_VERTICAL = 3
 
 _dp = C.POINTER(C.c_double)
 
@@ -45,6 +50,8 @@ class EpicGrid(C.Structure):
         ("re", C.c_double), ("rp", C.c_double), ("cp", C.c_double), ("rgas", C.c_double),
         ("kappa", C.c_double), ("cpr", C.c_double), ("kinvisc", C.c_double), ("lat0", C.c_double), ("hs_kf", C.c_double),
         ("x_h2", C.c_double), ("x_he", C.c_double), ("x_3", C.c_double),
+        ("dynvisc", C.c_double), ("turbulence", C.c_int32), ("diffusion_direction", C.c_int32),
+        ("stability_factor", C.c_int32), ("pad1", C.c_int32),
         ("lon", _dp), ("lat", _dp), ("rln", _dp), ("rlt", _dp), ("f", _dp), ("m", _dp), ("n", _dp),
         ("mn", _dp), ("g", _dp), ("sigmatheta", _dp), ("dsgth", _dp), ("dsgth_inv", _dp),
         ("h_min", _dp), ("t_sponge_inv", _dp),
@@ -54,6 +61,8 @@ class EpicGrid(C.Structure):
 FIELD_NAMES_3D = ["hdry", "theta", "p3", "h3", "p2", "theta2", "t2", "t3", "rho2", "rho3", "exner3",
                   "gz3", "mont3", "heat3", "pv3", "ri2", "div_uv3", "w3", "dzdt3", "u_spinup"]
 PROGNOSTIC = ["u", "v", "hdry", "theta"]
+# the turbulence closure's arrays (allocated by Fields(turbulence=True) only)
+TURB_FIELDS = ["nu_turb", "diffusion_coef_uv", "diffusion_coef_theta", "diffusion_coef_mass"]
 
 
 class EpicFields(C.Structure):
@@ -61,7 +70,8 @@ class EpicFields(C.Structure):
                 + [(n, _dp) for n in FIELD_NAMES_3D]
                 + [("gz_surface", _dp),
                    ("it_zero", C.c_int32), ("it_minus1", C.c_int32), ("it_minus2", C.c_int32),
-                   ("pad0", C.c_int32), ("itime", C.c_int64), ("model_time", C.c_int64)])
+                   ("pad0", C.c_int32), ("itime", C.c_int64), ("model_time", C.c_int64)]
+                + [(n, _dp) for n in TURB_FIELDS])
 
 
 class EpicHsParams(C.Structure):
@@ -166,9 +176,10 @@ class Fields:
     are views of one block, back to back in the library's order (u, v, dudt, dvdt, then
     FIELD_NAMES_3D), so that the library moves a whole state with one copy."""
 
-    def __init__(self, ni: int, nj: int, nk: int, uv_scheme: int, pinned: bool = False):
+    def __init__(self, ni: int, nj: int, nk: int, uv_scheme: int, pinned: bool = False, turbulence: bool = False):
         self.layout = Layout(ni, nj, nk)
         self.uv_scheme = uv_scheme
+        self.turbulence = turbulence
         nvp, ntp = (1, 3) if uv_scheme == EPIC_UV_AB3 else (2, 1)
         s3 = self.layout.shape3
         n3 = int(np.prod(s3))
@@ -184,6 +195,10 @@ class Fields:
             off += cnt
         self._block = block
         self.arrays["gz_surface"] = zeros(self.layout.shape2)
+        if turbulence:
+            tb = zeros((len(TURB_FIELDS) * n3,))
+            for q, name in enumerate(TURB_FIELDS):
+                self.arrays[name] = tb[q * n3:(q + 1) * n3].reshape(s3)
         self.struct = EpicFields()
         for k, a in self.arrays.items():
             setattr(self.struct, k, _ptr(a))
@@ -196,7 +211,8 @@ class Fields:
         raise AttributeError(name)
 
     def copy(self, pinned: bool = False) -> "Fields":
-        out = Fields(self.layout.ni, self.layout.nj, self.layout.nk, self.uv_scheme, pinned=pinned)
+        out = Fields(self.layout.ni, self.layout.nj, self.layout.nk, self.uv_scheme, pinned=pinned,
+                     turbulence=self.turbulence)
         for k, a in self.arrays.items():
             out.arrays[k][...] = a
         for name in ("it_zero", "it_minus1", "it_minus2", "itime", "model_time"):
@@ -209,8 +225,10 @@ class Fields:
 
     @property
     def state_nbytes(self) -> int:
-        """Bytes of the prognostic arrays (u, v, dudt, dvdt, hdry, theta): what EPIC_IO_STATE moves."""
-        return int(sum(self.arrays[k].nbytes for k in ("u", "v", "dudt", "dvdt", "hdry", "theta")))
+        """Bytes of the prognostic arrays (u, v, dudt, dvdt, hdry, theta, and nu_turb with the
+        turbulence closure): what EPIC_IO_STATE moves."""
+        keys = ("u", "v", "dudt", "dvdt", "hdry", "theta") + (("nu_turb",) if self.turbulence else ())
+        return int(sum(self.arrays[k].nbytes for k in keys))
 
     def wind(self, name: str) -> np.ndarray:
         """Current value plane of u or v (grid.it_uv: plane 0 for AB3, IT_ZERO for leapfrog)."""
@@ -282,6 +300,12 @@ class HSConfig:
     # hydrogen thermodynamics (FP64 form): mole fractions of H2 and He; 0 keeps the ideal gas
     x_h2: float = 0.0
     x_he: float = 0.0
+    # the Spalart-Allmaras DES turbulence closure (FP64 form): NU_TURB starts at 20 kinvisc
+    # everywhere (init_subgrid), the diffusivities at zero; direction and stability factor as
+    # grid.diffusion_direction and grid.stability_factor (1 = "Collins et al. (2004)")
+    turbulence: bool = False
+    diffusion_direction: int = EPIC_DIFFUSION_HORIZONTAL_AND_VERTICAL
+    stability_factor: int = 1
     extra: dict = field(default_factory=dict)
 
     def params(self) -> EpicHsParams:

@@ -106,12 +106,29 @@ constexpr int LOG_K0 = 724;       // c = k/1024, k = 724 .. 1448 covers m in [sq
 constexpr int LOG_N = 725;
 constexpr int EXP_N = 1024;
 
+constexpr int ATAN_N = 33;       // atan(k/32), k = 0 .. 32
+
+// atan(x) for 0 <= x <= 1 to 2^-106 by Euler's series
+// atan(x) = sum_n (2^2n (n!)^2 / (2n+1)!) x^(2n+1) / (1+x^2)^(n+1), whose ratio x^2/(1+x^2) <= 1/2.
+inline dd slow_atan(dd x) {
+  const dd x2 = dd_mul(x, x);
+  const dd den = dd_add_d(x2, 1.);
+  const dd y = dd_div(x2, den);
+  dd term = dd_div(x, den), sum = term;
+  for (int n = 1; n < 130; n++) {
+    term = dd_div(dd_mul(dd_mul(term, y), {(double)(2 * n), 0.}), {(double)(2 * n + 1), 0.});
+    sum = dd_add(sum, term);
+  }
+  return sum;
+}
+
 struct MathTable {
   dd ln2;                  // ln 2
   dd ln2_1024;             // ln 2 / 1024
   dd logc[LOG_N];          // log(k/1024)
   double invc[LOG_N];      // 1024/k rounded
   dd exp2j[EXP_N];         // 2^(j/1024)
+  dd atanc[ATAN_N];        // atan(k/32)
 };
 
 inline void fill_math_table(MathTable &t) {
@@ -124,6 +141,7 @@ inline void fill_math_table(MathTable &t) {
     t.invc[i] = 1. / c;
   }
   for (int j = 0; j < EXP_N; j++) t.exp2j[j] = slow_exp(dd_mul_d(t.ln2_1024, (double)j));
+  for (int k = 0; k < ATAN_N; k++) t.atanc[k] = slow_atan({(double)k / 32., 0.});
 }
 
 // log(x) in double-double, x > 0 finite and normal.  Relative error ~2^-84.
@@ -304,6 +322,58 @@ __host__ __device__ __forceinline__ double cr_pow(double x, double y, const Math
   if (round_test(v, fabs(v.hi) * (0x1p-69 + fabs(yl.hi) * 0x1p-68), r)) return r * pow2i(q);
   const dd ls = dd_mul_d(dd_log(x, T), y);
   return dd_exp_round(ls, T);
+}
+
+// ---- atan and cos (the turbulence closure's wall function and fv1 inversion) ----
+//
+// One double-double evaluation to ~2^-100, rounded once: the correctly rounded value except
+// within ~2^-100 of a rounding boundary, and the same bits on the host and the device.
+
+// atan(t) for a double-double 0 <= t <= 1: t = c + d with c = k/32 from the table,
+// atan(t) = atan(c) + atan(r), r = (t - c) / (1 + t c), |r| < 1/63, and
+// atan(r) = r (1 - r^2 (1/3 - r^2 (1/5 - r^2 (1/7 - r^2 (1/9 - r^2/11 + r^4/13 - r^6/15))))), the
+// innermost bracket in double (the r^17 term is below 2^-100 |r|).
+__host__ __device__ __forceinline__ dd dd_atan_unit(dd t, const MathTable &T) {
+  const int k = (int)rint(t.hi * 32.);
+  const double c = (double)k * (1. / 32.);
+  const dd r = dd_div(dd_add_d(t, -c), dd_add_d(dd_mul_d(t, c), 1.));
+  const dd r2 = dd_mul(r, r);
+  const double x2 = r2.hi;
+  const double tail = x2 * (1. / 9. - x2 * (1. / 11. - x2 * (1. / 13. - x2 * (1. / 15.))));
+  // Horner in double-double: 1 - r2 (1/3 - r2 (1/5 - r2 (1/7 - tail)))
+  dd h = dd_add_d(dd_div({1., 0.}, {7., 0.}), -tail);
+  h = dd_sub(dd_div({1., 0.}, {5., 0.}), dd_mul(r2, h));
+  h = dd_sub(dd_div({1., 0.}, {3., 0.}), dd_mul(r2, h));
+  h = dd_sub({1., 0.}, dd_mul(r2, h));
+  return dd_add(T.atanc[k], dd_mul(r, h));
+}
+
+__host__ __device__ __forceinline__ double cr_atan(double x, const MathTable &T) {
+  if (!(fabs(x) < INFINITY) || x == 0.) return atan(x);
+  const double a = fabs(x);
+  dd v;
+  if (a <= 1.) {
+    v = dd_atan_unit({a, 0.}, T);
+  } else {   // atan(a) = pi/2 - atan(1/a), pi/2 = 2 atan(1)
+    const dd half_pi = {2. * T.atanc[ATAN_N - 1].hi, 2. * T.atanc[ATAN_N - 1].lo};
+    v = dd_sub(half_pi, dd_atan_unit(dd_div({1., 0.}, {a, 0.}), T));
+  }
+  const double r = v.hi + v.lo;
+  return x < 0. ? -r : r;
+}
+
+// cos(x) for |x| < 1 by its Taylor series to x^30/30! in double-double (Horner:
+// 1 - x^2/(1*2) (1 - x^2/(3*4) (1 - ...))); other arguments go to the library's cos.
+__host__ __device__ __forceinline__ double cr_cos(double x, const MathTable &T) {
+  (void)T;
+  if (!(fabs(x) < 1.)) return cos(x);
+  const dd x2 = two_prod(x, x);
+  dd s = {1., 0.};
+  for (int n = 15; n >= 1; n--) {
+    const double q = (double)((2 * n - 1) * (2 * n));
+    s = dd_sub({1., 0.}, dd_div(dd_mul(x2, s), {q, 0.}));
+  }
+  return s.hi + s.lo;
 }
 
 }  // namespace epic

@@ -42,6 +42,14 @@ extern "C" {
 #define EPIC_ADV_HSU   0   /* "Predictor-corrector (Hsu, Konor, and Arakawa)" */
 #define EPIC_ADV_AKIMA 1   /* "Monotonized, 4th-order centered (Akima)"       */
 
+/* grid.turbulence_scheme (src/shared/epic_initial.c:153-155) and grid.diffusion_direction
+ * (include/epic.h:290-292) */
+#define EPIC_TURB_OFF    0   /* "off"                  */
+#define EPIC_TURB_SA_DES 1   /* "Spalart-Allmaras DES" */
+#define EPIC_DIFFUSION_HORIZONTAL_AND_VERTICAL 1
+#define EPIC_DIFFUSION_JUST_HORIZONTAL         2
+#define EPIC_DIFFUSION_JUST_VERTICAL           3
+
 /* Precision forms accepted by epic_model_create(). */
 #define EPIC_PREC_FP64  0    /* every kernel in binary64 (the drop-in form)                    */
 #define EPIC_PREC_MIXED 1    /* stencils/advection/hyperviscosity/filter/physics in binary32;
@@ -103,6 +111,15 @@ typedef struct epic_grid {
                                   interpolation); cpr must then be thermo_setup's
                                   (2.5 x_h2 + 2.5 x_he + 3.5 x_3) / (x_h2 + x_he + x_3).  FP64
                                   form only.                                                    */
+  double  dynvisc;             /* planet->dynvisc [kg/m/s] (the turbulence closure's molecular
+                                  viscosity of the winds)                                       */
+  int32_t turbulence;          /* grid.turbulence_scheme: EPIC_TURB_OFF or EPIC_TURB_SA_DES
+                                  (Spalart-Allmaras DES: source_sink_turb, the subgrid diffusion
+                                  of THETA, NU_TURB and the winds, epic_subgrid.c).  FP64 form only */
+  int32_t diffusion_direction; /* grid.diffusion_direction: EPIC_DIFFUSION_* (1 horizontal and
+                                  vertical, 2 horizontal only, 3 vertical only)                 */
+  int32_t stability_factor;    /* grid.stability_factor: 0 "off", 1 "Collins et al. (2004)"    */
+  int32_t pad1;
   const double *lon;           /* [2*(ni+1)+1]                                                  */
   const double *lat, *rln, *rlt, *f, *m, *n, *mn, *g;   /* [2*(nj+1)+1]                         */
   const double *sigmatheta, *dsgth, *dsgth_inv;         /* [2*(nk+1)+1]                         */
@@ -126,6 +143,11 @@ typedef struct epic_fields {
   int32_t pad0;
   int64_t itime;               /* grid.itime                                                    */
   int64_t model_time;          /* var.model_time [s]                                            */
+  /* The turbulence closure's arrays (read only when epic_grid.turbulence is on): NU_TURB, the
+   * Spalart-Allmaras working viscosity on the layer interfaces (prognostic), and the eddy
+   * diffusivities that store_diag's set_diffusion_coef leaves for the next step
+   * (DIFFUSION_COEF_UV, _THETA, _MASS).  On upload a NULL diffusivity uploads zeros. */
+  double *nu_turb, *diffusion_coef_uv, *diffusion_coef_theta, *diffusion_coef_mass;
 } epic_fields;
 
 typedef struct epic_model epic_model;

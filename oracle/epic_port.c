@@ -46,6 +46,12 @@ struct ep_model {
   /* hsu_advection column buffers (static in the reference) */
   double *wm, *wp, *w_a, *w_a_pred, *w_a_min, *w_ff, *w_a_diff1, *w_a_diff2, *w_aaa;
   double coef[9], max_nu[9], m0, n0, mu_dry, eps13;
+  /* turbulence closure (g.turbulence): NU_TURB, the eddy diffusivities, column buffers of
+   * crank_nicolson and the band solver, and the first error a wall function meets */
+  double *nu_turb, *dc_uv, *dc_theta, *dc_mass;
+  double *cz, *ca, *cd, *crho, *cans, *sf0, *sf2, *ri, *tb, *tl, *tr, *taorig, *tal;
+  int *tindex;
+  char turb_err[160];
   /* hydrogen thermodynamics (x_h2 > 0): thermo_setup's tables */
   double th_t[16][128], th_array[5][128], th_tgrid[128], th_thetagrid[128], th_fpdat[16];
   int it_zero, it_minus1, it_minus2, it_uv, it_uv_dis, it_uv_tend;
@@ -73,6 +79,14 @@ static int fail(ep_model *M, const char *fmt, ...) {
 #define NJ (M->nj)
 #define NI (M->ni)
 #define LAT0 (M->g.lat0)
+/* the turbulence closure (epic_grid.turbulence, grid.diffusion_direction) */
+#define KINVISC (M->g.kinvisc)
+#define SA_CV1_3 (7.1 * 7.1 * 7.1)
+#define TURB_ON(M) ((M)->g.turbulence == EPIC_TURB_SA_DES)
+#define DIFF_HORIZONTAL(M) ((M)->g.diffusion_direction == EPIC_DIFFUSION_HORIZONTAL_AND_VERTICAL || \
+                            (M)->g.diffusion_direction == EPIC_DIFFUSION_JUST_HORIZONTAL)
+#define DIFF_VERTICAL(M) ((M)->g.diffusion_direction == EPIC_DIFFUSION_HORIZONTAL_AND_VERTICAL || \
+                          (M)->g.diffusion_direction == EPIC_DIFFUSION_JUST_VERTICAL)
 
 static inline double dmax(double x, double y) { return x > y ? x : y; }  /* MAX, include/epic.h:144 */
 static inline double dmin(double x, double y) { return x < y ? x : y; }  /* MIN, include/epic.h:138 */
@@ -492,7 +506,7 @@ static void bc3(const ep_model *M, double *a) {
 /* Zonal filter, src/shared/epic_adjust.c:102-480                                            */
 /* ---------------------------------------------------------------------------------------- */
 
-enum { IDX_U = 0, IDX_V = 1, IDX_HDRY = 2, IDX_THETA = 3, IDX_OTHER = 4 };
+enum { IDX_U = 0, IDX_V = 1, IDX_HDRY = 2, IDX_THETA = 3, IDX_OTHER = 4, IDX_NU = 5 };
 
 static void filter_tables(ep_model *M) { /* the initialisation block, epic_adjust.c:132-241 */
   double lat0 = M->g.lat0 * DEG, rln0, rlt0, r, tmp0, tmp1, re = M->g.re, rp = M->g.rp;
@@ -615,8 +629,14 @@ static int zonal_filter_3d(ep_model *M, int index, double *buff) {
           table[kay].y = A3(buff, K, J, I);
         }
         break;
-      default:
-        return fail(M, "zonal_filter_3d: index %d", index);
+      default:   /* NU_TURB and the other interface variables, epic_adjust.c:369-387 */
+        kstart = 0; kend = KHI;
+        for (K = kend; K >= kstart; K--) {
+          kay = kend - K;
+          table[kay].x = A3(gz, K, J, I);
+          table[kay].y = A3(buff, K, J, I);
+        }
+        break;
     }
     n = kend - kstart + 1;
     if (spline_pchip(n, table) != 0) return fail(M, "spline_pchip: x not increasing (J=%d)", J);
@@ -1504,10 +1524,14 @@ static void uv_drag(ep_model *M) {
 }
 
 /* hsu_advection(is, buff3d, HORIZONTAL_AND_VERTICAL), epic_flux.c:652-1488.
- * kind: IDX_OTHER = P3_INDEX (unity), IDX_THETA, IDX_HDRY. */
+ * kind: IDX_OTHER = P3_INDEX (unity), IDX_THETA, IDX_HDRY, IDX_NU = NU_TURB_INDEX.  NU_TURB is
+ * loaded, moved by the interface velocities and updated as an interface variable, but its
+ * predictor and corrector fluxes take the layer variables' form (the reference's
+ * `is == HDRY_INDEX || is == NU_TURB_INDEX` branches, :876-960), with floor NU_TURB_MIN. */
 static void hsu_advection(ep_model *M, int kind, double *buff) {
   const double ep = EP_EPS_HSU;
-  const int layer = (kind == IDX_HDRY);
+  const int layer = (kind == IDX_HDRY), nu = (kind == IDX_NU), layer_flux = layer || nu;
+  const double nu_min = 1.e-3 * M->g.kinvisc;   /* NU_TURB_MIN, include/epic_subgrid.h:40 */
   const int k_first = (kind == IDX_THETA) ? M->g.k_sigma - 1 : 1;
   int K, J, I;
   double *wm = M->wm, *wp = M->wp, *w_a = M->w_a, *pred = M->w_a_pred, *amin = M->w_a_min, *w_ff = M->w_ff;
@@ -1518,6 +1542,8 @@ static void hsu_advection(ep_model *M, int kind, double *buff) {
   /* Vertical advection, column by column (:717-1052). */
   if (layer) for (K = k_first; K <= KHI; K++) amin[K] = M->h_min[K];
   else for (K = k_first - 1; K <= KHI; K++) amin[K] = 0.;
+  /* NU_TURB sets entries 1 .. nk; entry 0 keeps the 0 of the calls before it */
+  if (nu) for (K = k_first; K <= KHI; K++) amin[K] = nu_min;
   for (J = 0; J <= NJ; J++)
     for (I = 0; I <= NI + 1; I++) {
       if (layer) for (K = k_first; K <= KHI; K++) w_a[K] = A3(buff, K, J, I);
@@ -1537,7 +1563,7 @@ static void hsu_advection(ep_model *M, int kind, double *buff) {
         }
       }
       /* predictor */
-      if (layer) {
+      if (layer_flux) {
         w_ff[k_first - 1] = 0.;
         w_ff[KHI] = 0.;
         for (K = k_first; K < KHI; K++) w_ff[K] = wp[K] * w_a[K + 1] + wm[K] * w_a[K];
@@ -1555,7 +1581,7 @@ static void hsu_advection(ep_model *M, int kind, double *buff) {
         }
       }
       /* corrector */
-      if (layer) {
+      if (layer_flux) {
         for (K = k_first; K < KHI; K++) w_ff[K] = .5 * (wp[K] * (pred[K] + w_a[K + 1]) + wm[K] * (pred[K + 1] + w_a[K]));
         for (K = k_first; K <= KHI; K++) {
           if (K == 1) {
@@ -1628,6 +1654,7 @@ static void hsu_advection(ep_model *M, int kind, double *buff) {
         }
         w_ff[KHI + 1] = 0.;
       }
+      if (nu) w_ff[KHI + 1] = 0.;   /* the reference's static entry, left 0 by the THETA call */
       if (layer) {
         for (K = k_first; K <= KHI; K++) {
           da = (w_ff[K] - w_ff[K - 1]) * M->dsgth_inv[2 * K] * DT;
@@ -1646,7 +1673,7 @@ static void hsu_advection(ep_model *M, int kind, double *buff) {
     double *a, *vm = M->b2d[0], *vp = M->b2d[1], *v2d = M->b2d[2], *ff = M->b2d[4], *ap = M->b2d[5];
     double *ad1, *ad2, *aa, mi, mn1, vhatp, vhatm;
     if (kind == IDX_THETA && K <= M->g.k_sigma - 2) continue;
-    a_min = layer ? M->h_min[K] : 0.;
+    a_min = layer ? M->h_min[K] : (nu ? nu_min : 0.);
     a = buff + K * M->n2;
     memset(vm, 0, M->n2 * sizeof(double));
     memset(vp, 0, M->n2 * sizeof(double));
@@ -1749,7 +1776,7 @@ static void hsu_advection(ep_model *M, int kind, double *buff) {
     double *a = M->b2d[6], *um = M->b2d[0], *up = M->b2d[1], *u2d = M->b2d[2], *ff = M->b2d[4], *ap = M->b2d[5];
     double *ad1, *ad2, *aa, n_inv, mn1, uhatp, uhatm;
     if (kind == IDX_THETA && K <= M->g.k_sigma - 2) continue;
-    a_min = layer ? M->h_min[K] : 0.;
+    a_min = layer ? M->h_min[K] : (nu ? nu_min : 0.);
     memcpy(a, buff + K * M->n2, M->n2 * sizeof(double));
     zonal_filter_2d(M, IDX_OTHER, a);
     memset(um, 0, M->n2 * sizeof(double));
@@ -1844,7 +1871,7 @@ static double akima_dela(double d0, double d1) {   /* harmonic mean of like-sign
   return (tmp > 0.) ? 2. * tmp / (d0 + d1) : 0.;
 }
 static void akima_advection(ep_model *M, int kind, double *buff) {
-  const int layer = (kind == IDX_HDRY);
+  const int layer = (kind == IDX_HDRY), nu = (kind == IDX_NU);
   const int k_first = (kind == IDX_THETA) ? M->g.k_sigma - 1 : 1;
   int K, J, I;
   double *w = M->wm, *w_a = M->w_a, *w_deltaa = M->w_a_diff1, *w_dela = M->w_a_diff2, *w_ff = M->w_ff;
@@ -1868,6 +1895,21 @@ static void akima_advection(ep_model *M, int kind, double *buff) {
         }
         w_ff[KHI] = 0.;           /* mass_flux_bot */
         for (K = k_first; K <= KHI; K++) A3(buff, K, J, I) += (w_ff[K] - w_ff[K - 1]) * M->dsgth_inv[2 * K] * DT;
+      } else if (nu) {   /* NU_TURB: interface velocities and update, the layer form of the flux (:1687-1706) */
+        for (K = k_first; K <= KHI; K++)
+          w[K] = (K == 1 || K == KHI) ? 0. : .5 * (A3(M->w3, K, J, I) + A3(M->w3, K - 1, J, I));
+        w_deltaa[k_first - 1] = 0.;
+        for (K = k_first; K < KHI; K++) w_deltaa[K] = w_a[K] - w_a[K + 1];
+        w_deltaa[KHI] = 0.;
+        for (K = k_first; K <= KHI; K++) w_dela[K] = akima_dela(w_deltaa[K], w_deltaa[K - 1]);
+        w_ff[k_first - 1] = 0.;
+        for (K = k_first; K < KHI; K++) {
+          aval = .5 * (w_a[K] + w_a[K + 1]) - (w_dela[K] - w_dela[K + 1]) / 6.;
+          w_ff[K] = w[K] * aval;
+        }
+        w_ff[KHI] = 0.;
+        w_ff[KHI + 1] = 0.;   /* the reference's static entry, left 0 by the THETA call */
+        for (K = k_first; K <= KHI; K++) A3(buff, K, J, I) += (w_ff[K + 1] - w_ff[K]) * M->dsgth_inv[2 * K + 1] * DT;
       } else {
         for (K = k_first; K <= KHI; K++)
           w[K] = (K == 1 || K == KHI) ? 0. : .5 * (A3(M->w3, K, J, I) + A3(M->w3, K - 1, J, I));
@@ -1981,6 +2023,18 @@ static void advection(ep_model *M) {
   for (K = M->g.k_sigma - 1; K <= KHI + 1; K++)
     for (J = 0; J <= NJ; J++)
       for (I = 0; I <= NI + 1; I++) A3(M->theta, K, J, I) -= A3(M->old, K, J, I) * (A3(M->unity, K, J, I) - 1.);
+  if (TURB_ON(M)) {   /* NU_TURB with the same scheme (UNITY stands), before HDRY, epic_flux.c:540-600 */
+    for (K = 0; K <= KHI + 1; K++)
+      for (J = 0; J <= NJ; J++)
+        for (I = 0; I <= NI + 1; I++) A3(M->old, K, J, I) = A3(M->nu_turb, K, J, I);
+    advect(M, IDX_NU, M->nu_turb);
+    for (K = 0; K <= KHI + 1; K++)
+      for (J = 0; J <= NJ; J++)
+        for (I = 0; I <= NI + 1; I++) {
+          A3(M->nu_turb, K, J, I) -= A3(M->old, K, J, I) * (A3(M->unity, K, J, I) - 1.);
+          A3(M->nu_turb, K, J, I) = dmax(1.e-4 * M->g.kinvisc, A3(M->nu_turb, K, J, I));
+        }
+  }
   advect(M, IDX_HDRY, M->hdry);
   restore_mass(M);
   set_p2etc(M, 0);
@@ -2270,6 +2324,751 @@ static void uv_update(ep_model *M) {
 }
 
 /* ---------------------------------------------------------------------------------------- */
+/* Turbulence closure, Spalart-Allmaras DES: src/shared/epic_subgrid.c:207-590 (the diffusion */
+/* parts), 1236-1488, 1493-1790, 1889-2080, 2127-3228; crank_nicolson and the band solver,   */
+/* src/shared/epic_funcs_util.c:2994-3400, 3643-3787                                         */
+/* ---------------------------------------------------------------------------------------- */
+
+/* The libepicport_cr.so build routes these two to the correctly rounded ones of the kernels. */
+#ifndef EP_TURB_ATAN
+#define EP_TURB_ATAN atan
+#define EP_TURB_COS cos
+#endif
+enum { WALL_U, WALL_V, WALL_H };   /* law_of_the_wall's grids: U_INDEX, V_INDEX, the h-grid default */
+
+static double limit_range(double lo, double x, double hi) { return x < lo ? lo : (x > hi ? hi : x); } /* LIMIT_RANGE, include/epic.h:147 */
+
+static void turb_error(ep_model *M, const char *what, int J, int I, double v) {
+  if (!M->turb_err[0]) snprintf(M->turb_err, sizeof(M->turb_err), "%s (J=%d, I=%d): %g", what, J, I, v);
+}
+
+/* D_WALL as dwall_SA sets it before each use, epic_subgrid.c:2716-2770 */
+static double d_wall(const ep_model *M, int K, int J, int I) {
+  if (M->g.gas_giant) return DBL_MAX;
+  return (A3(M->gz3, K, J, I) - M->g.topo_scale * A2(M->gz_surface, J, I)) / M->grav[2 * J + 1];
+}
+
+/* delta_SA, :2774-2808 */
+static double delta_sa(const ep_model *M, int K, int J, int I) {
+  const int jj = 2 * J + 1;
+  double dx = 1. / M->m[jj], dy = 1. / M->n[jj], dz, delta;
+  if (K < M->nk) dz = (A3(M->gz3, K - 1, J, I) - A3(M->gz3, K + 1, J, I)) / M->grav[jj];
+  else dz = (A3(M->gz3, K - 1, J, I) - A3(M->gz3, M->nk, J, I)) / M->grav[jj];
+  delta = dmin(dx, dy);
+  return dmin(delta, dz);
+}
+
+/* func_utau, :3112-3165: the wall law's residual u+(y+) - u_tan/u_tau */
+static double func_utau(ep_model *M, double u_tau, double u_tan, double dwall) {
+  const double C = 5., const1 = 0.127, const2 = 1. / .41, const3 = 0.41 * 1.43e-3, one_third = 1. / 3.,
+               sqrt_one_third = sqrt(1. / 3.), pi_six = M_PI / 6.;
+  double u_plus = 0., y_plus, yy;
+  if (u_tau != 0.) u_plus = u_tan / u_tau;
+  else turb_error(M, "func_utau: u_tau = 0", -1, -1, u_tau);
+  y_plus = fabs(u_tau * dwall / KINVISC);
+  if (u_plus < 0.1) return 1.e+20;
+  if (y_plus < 5.) return y_plus - u_plus;
+  if (y_plus < 70.) {
+    yy = const1 * y_plus;
+    return (one_third * log((1. + yy) / (sqrt(yy * (yy - 1.) + 1.))) +
+            sqrt_one_third * (EP_TURB_ATAN(sqrt_one_third * (2. * yy - 1.)) + pi_six)) / const1 +
+           .25 * const2 * log(1. + const3 * pow(y_plus, 4.)) - u_plus;
+  }
+  return const2 * log(y_plus) + C - u_plus;
+}
+
+/* law_of_the_wall, :2995-3105: the eddy viscosity next to the wall from the secant solution of
+ * the wall law for the friction velocity (index: WALL_U, WALL_V or the h-grid WALL_H) */
+static double law_of_the_wall(ep_model *M, int K, int J, int I, int index, double t_vis, double u_tan) {
+  const double tol = 1.e-6;
+  double dwall, dwall_inv = 0., u_tau = 0., x1, x2, xl, dx, fl, f, rts, swap;
+  int iter;
+  (void)t_vis;   /* the reference scales t_vis by fv1 and then leaves it unused */
+  if (M->g.gas_giant) return 1.0e-4 * KINVISC;
+  if (index == WALL_U) dwall = 0.5 * (d_wall(M, K, J, I) + d_wall(M, K, J, I - 1));
+  else if (index == WALL_V)
+    dwall = 0.5 * M->m[2 * J] * (d_wall(M, K, J, I) / M->m[2 * J + 1] + d_wall(M, K, J - 1, I) / M->m[2 * J - 1]);
+  else dwall = d_wall(M, K, J, I);
+  if (dwall * u_tan < 0.00023) return 0.01 * KINVISC;
+  if (dwall > 0.) dwall_inv = 1. / dwall;
+  else turb_error(M, "law_of_the_wall: dwall <= 0", J, I, dwall);
+  x1 = sqrt(KINVISC * (1. + 0.01) * u_tan * dwall_inv);
+  x2 = sqrt(KINVISC * (1. + 20.) * u_tan * dwall_inv);
+  fl = func_utau(M, x1, u_tan, dwall);
+  f = func_utau(M, x2, u_tan, dwall);
+  if (fabs(fl) < fabs(f)) {
+    rts = x1; xl = x2; swap = fl; fl = f; f = swap;
+  } else {
+    xl = x1; rts = x2;
+  }
+  for (iter = 0; iter < 30; iter++) {
+    dx = (xl - rts) * f / (f - fl);
+    xl = rts;
+    fl = f;
+    rts += dx;
+    f = func_utau(M, rts, u_tan, dwall);
+    if (f > .99e+20) return 0.01 * KINVISC;
+    if (fabs(dx) < tol || f == 0.0) {
+      u_tau = rts;
+      break;
+    }
+  }
+  if (iter < 30) return dmax((u_tau * u_tau * dwall / u_tan) - KINVISC, 0.01 * KINVISC);
+  return 20. * KINVISC;
+}
+
+/* invert_fv1, :3172-3226: the working viscosity nu~ from an eddy viscosity (fitted fv1) */
+static double invert_fv1(ep_model *M, double t_vis) {
+  const double pi_factor = M_PI * 0.5 / 30.0;
+  double chi, fv1;
+  if (t_vis < 0.) turb_error(M, "invert_fv1: t_vis < 0", -1, -1, t_vis);
+  chi = t_vis / KINVISC;
+  if (chi > 30) return t_vis;
+  if (chi < 0.4) return KINVISC * pow(chi * SA_CV1_3, .25);
+  fv1 = EP_TURB_COS(pi_factor * pow(chi, 0.35));
+  fv1 = 1.0 - fv1 * fv1;
+  return KINVISC * chi / fv1;
+}
+
+/* tau_surface, :2819-2988: the wall stress under the wind component `index` (WALL_U, WALL_V)
+ * or for NU_TURB (WALL_H), from layer K = nk-1 */
+static void tau_surface(ep_model *M, int index, double *tau_wall) {
+  const int K = M->nk - 1;
+  const double *U = M->u + (long)M->it_uv * M->n3, *V = M->v + (long)M->it_uv * M->n3;
+  const double *u2d = U + K * M->n2, *v2d = V + K * M->n2;
+  double *kie = M->b2d[1], rho, nu_turb, dz, kin, u_tan, dc;
+  int J, I;
+  memset(kie, 0, M->n2 * sizeof(double));
+  for (J = 0; J <= NJ; J++)
+    for (I = 1; I <= NI; I++) A2(kie, J, I) = get_kin(M, u2d, v2d, J, I);
+  bc2(M, kie);
+  if (M->g.gas_giant) {
+    for (J = 0; J <= NJ; J++)
+      for (I = 1; I <= NI; I++) A2(tau_wall, J, I) = 0.;
+  } else if (index == WALL_U) {
+    for (J = 0; J <= NJ; J++)
+      for (I = 1; I <= NI; I++) {
+        rho = .5 * (A3(M->rho3, K, J, I) + A3(M->rho3, K, J, I - 1));
+        nu_turb = .5 * (A3(M->nu_turb, K, J, I) + A3(M->nu_turb, K, J, I - 1));
+        dz = .5 * (A3(M->gz3, K, J, I) + A3(M->gz3, K, J, I - 1) - A3(M->gz3, K + 1, J, I) - A3(M->gz3, K + 1, J, I - 1)) /
+             M->grav[2 * J + 1];
+        kin = .5 * (A2(kie, J, I) + A2(kie, J, I - 1));
+        u_tan = sqrt(2. * kin);
+        dc = law_of_the_wall(M, K, J, I, WALL_U, nu_turb, u_tan);
+        A2(tau_wall, J, I) = (M->g.dynvisc + rho * dc) * (A3(U, K, J, I) - 0.) / dz;
+      }
+  } else if (index == WALL_V) {
+    for (J = 1; J <= NJ; J++)
+      for (I = 1; I <= NI; I++) {
+        rho = .5 * (A3(M->rho3, K, J, I) + A3(M->rho3, K, J - 1, I));
+        nu_turb = .5 * (A3(M->nu_turb, K, J, I) + A3(M->nu_turb, K, J - 1, I));
+        dz = .5 * (A3(M->gz3, K, J, I) + A3(M->gz3, K, J - 1, I) - A3(M->gz3, K + 1, J, I) - A3(M->gz3, K + 1, J - 1, I)) /
+             M->grav[2 * J];
+        kin = .5 * (A2(kie, J, I) + A2(kie, J - 1, I));
+        u_tan = sqrt(2. * kin);
+        dc = law_of_the_wall(M, K, J, I, WALL_V, nu_turb, u_tan);
+        A2(tau_wall, J, I) = (M->g.dynvisc + rho * dc) * (A3(V, K, J, I) - 0.) / dz;
+      }
+  } else {
+    for (J = 0; J <= NJ; J++)
+      for (I = 1; I <= NI; I++) {
+        rho = A3(M->rho3, K, J, I);
+        nu_turb = A3(M->nu_turb, K, J, I);
+        dz = (A3(M->gz3, K, J, I) - A3(M->gz3, K + 1, J, I)) / M->grav[2 * J + 1];
+        kin = get_kin(M, u2d, v2d, J, I);
+        u_tan = sqrt(2. * kin);
+        dc = law_of_the_wall(M, K, J, I, WALL_H, nu_turb, u_tan);
+        nu_turb = invert_fv1(M, dc);
+        A2(tau_wall, J, I) = (M->g.dynvisc + rho * nu_turb) * (u_tan - 0.) / dz;
+      }
+  }
+  bc2(M, tau_wall);
+}
+
+/* set_diffusion_coef, :2171-2302 (inside store_diag).  Note that it leaves DIFFUSION_COEF_UV
+ * zero above the bottom layer: the winds' turbulent viscosity acts only at K = nk. */
+static void set_diffusion_coef(ep_model *M) {
+  const int kend = M->g.gas_giant ? KHI : KHI - 1;
+  const double *U = M->u + (long)M->it_uv_dis * M->n3, *V = M->v + (long)M->it_uv_dis * M->n3;
+  double max_nu2, chi3, fv1, turb, nu_turb, kin, u_tan;
+  int K, J, I;
+  for (K = 1; K <= kend; K++)
+    for (J = 0; J <= NJ; J++) {
+      max_nu2 = M->max_nu[2] * dmin(1., pow(M->g.dy0 * M->m[2 * J + 1], -2.));
+      for (I = 0; I <= NI + 1; I++) {
+        chi3 = A3(M->nu_turb, K, J, I) / KINVISC;
+        chi3 *= chi3 * chi3;
+        fv1 = chi3 / (chi3 + SA_CV1_3);
+        turb = fv1 * A3(M->nu_turb, K, J, I);
+        A3(M->dc_theta, K, J, I) = limit_range(0., turb, max_nu2);
+        A3(M->dc_mass, K, J, I) = limit_range(0., turb, max_nu2);
+      }
+    }
+  if (!M->g.gas_giant) {
+    K = KHI - 1;
+    for (J = 0; J <= NJ; J++) {
+      max_nu2 = M->max_nu[2] * dmin(1., pow(M->g.dy0 * M->m[2 * J + 1], -2.));
+      for (I = 1; I <= NI; I++) {
+        nu_turb = A3(M->nu_turb, K, J, I);
+        kin = get_kin(M, U + K * M->n2, V + K * M->n2, J, I);
+        u_tan = sqrt(2. * kin);
+        turb = law_of_the_wall(M, K, J, I, WALL_H, nu_turb, u_tan);
+        A3(M->dc_uv, KHI, J, I) = limit_range(0., turb + KINVISC, max_nu2);
+        A3(M->dc_theta, KHI, J, I) = limit_range(0., turb, max_nu2);
+        A3(M->dc_mass, KHI, J, I) = limit_range(0., turb, max_nu2);
+      }
+    }
+  }
+  bc3(M, M->dc_uv);
+  bc3(M, M->dc_theta);
+  bc3(M, M->dc_mass);
+}
+
+/* stability_factor, :2309-2415, over kk = 1 .. 2 nk + 1 */
+static void stability_factor(ep_model *M, int J, int I, double *sf) {
+  const double max_ri = 100.;
+  double *Ri = M->ri, slope;
+  int K, kk;
+  if (!M->g.stability_factor) {
+    for (kk = 1; kk <= 2 * KHI + 1; kk++) sf[kk] = 1.;
+    return;
+  }
+  Ri[1] = limit_range(-max_ri, A3(M->ri2, 1, J, I), max_ri);
+  for (K = 1; K < KHI; K++) {
+    kk = 2 * K;
+    Ri[kk] = limit_range(-max_ri, A3(M->ri2, K, J, I), max_ri);
+    Ri[kk + 1] = limit_range(-max_ri, .5 * (A3(M->ri2, K, J, I) + A3(M->ri2, K + 1, J, I)), max_ri);
+  }
+  kk = 2 * KHI;
+  Ri[kk] = limit_range(-max_ri, A3(M->ri2, KHI, J, I), max_ri);
+  Ri[kk + 1] = Ri[kk];
+  for (kk = 1; kk <= 2 * KHI; kk++) {
+    slope = Ri[kk + 1] - Ri[kk];
+    if (-slope > .9 * max_ri) Ri[kk + 1] = 0.;
+  }
+  for (kk = 1; kk <= 2 * KHI + 1; kk++) {
+    if (Ri[kk] > 0.) sf[kk] = 1. / (1. + 10. * Ri[kk] * (1. + 8. * Ri[kk]));
+    else sf[kk] = sqrt(1. - 18. * Ri[kk]);
+  }
+}
+
+/* get_brunt2 on the interface kk = 2K+1, 1 <= K < nk (np = 1, fpara off, Held-Suarez cp),
+ * epic_funcs_diag.c:2885-3075 */
+static double brunt2_iface(const ep_model *M, int K, int J, int I) {
+  double pressure = A3(M->p3, K, J, I), temperature = A3(M->t3, K, J, I), density = A3(M->rho3, K, J, I);
+  double cp = 1004., mu = M->mu_dry, deltap, deltaT, drho_dp_T, drho_dT_p, Drho_Dp, g;
+  deltap = 0.001 * pressure;
+  deltaT = 0.001 * temperature;
+  drho_dp_T = (return_density(pressure + deltap, temperature, mu) - return_density(pressure - deltap, temperature, mu)) /
+              (2. * deltap);
+  drho_dT_p = (return_density(pressure, temperature + deltaT, mu) - return_density(pressure, temperature - deltaT, mu)) /
+              (2. * deltaT);
+  Drho_Dp = (A3(M->rho2, K + 1, J, I) - A3(M->rho2, K, J, I)) / (A3(M->p2, K + 1, J, I) - A3(M->p2, K, J, I));
+  g = M->grav[2 * J + 1];
+  return g * g * (Drho_Dp - drho_dp_T + temperature / (cp * density * density) * drho_dT_p * drho_dT_p);
+}
+
+/* source_sink_SA, :2434-2711: production, gradient, destruction and buoyancy terms of the
+ * Spalart-Allmaras equation.  NU_TURB is updated in place in K, J, I order, so each point reads
+ * the new values of its K-1, J-1 and I-1 neighbours and the old ones of K+1, J+1, I+1. */
+static void source_sink_sa(ep_model *M) {
+  const double cw2 = 0.3, cw3_6 = pow(2., 6.), cb1 = 0.1355, cb2 = 0.622, sigma = 2. / 3., kappa = 0.41,
+               kappa_2 = kappa * kappa, cw1 = (cb1 / kappa_2) + ((1. + cb2) / sigma), C_DES = 0.65, nu_turb_limiter = 3000.;
+  const double *U = M->u + (long)M->it_uv_dis * M->n3, *V = M->v + (long)M->it_uv_dis * M->n3;
+  double *u2d = M->b2d[0], *v2d = M->b2d[1], *NU = M->nu_turb;
+  double mn_v, mn_u, m_2jp1, n_2jp1, n_2jp2, n_2j, delta, d_tilda, dz_inv, chi, fv1, fv2, s11, s22, s33, s12, s13, s23;
+  double u_var1, u_var3, v_var1, v_var3, w_var1, w_var3, h_rho, S, tmp1, tmp2, S_tilda, dnudt, r_sa, g_sa, fw, brunt2, brunt;
+  int K, J, I, kk, jj;
+  for (K = 1; K < KHI; K++) {
+    kk = 2 * K + 1;
+    memset(u2d, 0, M->n2 * sizeof(double));
+    memset(v2d, 0, M->n2 * sizeof(double));
+    /* U onto the v-grid; zero at the poles (the edge rows of the globe) */
+    for (J = 1; J <= NJ; J++) {
+      jj = 2 * J;
+      mn_v = .5 / (1. / M->mn[jj - 1] + 1. / M->mn[jj + 1]);
+      for (I = 1; I <= NI; I++)
+        A2(u2d, J, I) = ((A3(U, K, J, I) + A3(U, K, J, I + 1)) * (1. / M->mn[jj + 1]) +
+                         (A3(U, K, J - 1, I) + A3(U, K, J - 1, I + 1)) * (1. / M->mn[jj - 1])) * mn_v;
+    }
+    for (I = 1; I <= NI; I++) A2(u2d, 0, I) = 0.;
+    for (I = 1; I <= NI; I++) A2(u2d, NJ + 1, I) = 0.;
+    bc2(M, u2d);
+    /* V onto the u-grid */
+    for (J = 0; J <= NJ; J++) {
+      jj = 2 * J;
+      mn_u = .5 / (1. / M->mn[jj] + 1. / M->mn[jj + 2]);
+      for (I = 1; I <= NI; I++)
+        A2(v2d, J, I) = ((A3(V, K, J, I) + A3(V, K, J, I - 1)) * (1. / M->mn[jj]) +
+                         (A3(V, K, J + 1, I) + A3(V, K, J + 1, I - 1)) * (1. / M->mn[jj + 2])) * mn_u;
+    }
+    bc2(M, v2d);
+    for (J = 0; J <= NJ; J++) {
+      jj = 2 * J;
+      m_2jp1 = M->m[jj + 1];
+      n_2jp1 = M->n[jj + 1];
+      n_2jp2 = M->n[jj + 2];
+      n_2j = M->n[jj];
+      for (I = 1; I <= NI; I++) {
+        delta = delta_sa(M, K, J, I);
+        d_tilda = dmin(d_wall(M, K, J, I), C_DES * delta);
+        dz_inv = M->grav[jj + 1] / (A3(M->gz3, K - 1, J, I) - A3(M->gz3, K + 1, J, I));
+        chi = A3(NU, K, J, I) / KINVISC;
+        fv1 = pow(chi, 3.) / (pow(chi, 3.) + SA_CV1_3);
+        fv2 = 1. - (chi / (1. + chi * fv1));
+        s11 = (A3(U, K, J, I + 1) - A3(U, K, J, I)) * m_2jp1;
+        s22 = (A3(V, K, J + 1, I) - A3(V, K, J, I)) * n_2jp1;
+        s33 = (A3(M->w3, K - 1, J, I) - A3(M->w3, K + 1, J, I)) / (M->sgth[kk - 2] - M->sgth[kk + 2]);
+        s12 = .5 * ((A2(u2d, J + 1, I) - A2(u2d, J, I)) * n_2jp1 + (A2(v2d, J, I + 1) - A2(v2d, J, I)) * m_2jp1);
+        u_var3 = 0.5 * (A3(U, K + 1, J, I) + A3(U, K + 1, J, I + 1));
+        u_var1 = 0.5 * (A3(U, K - 1, J, I) + A3(U, K - 1, J, I + 1));
+        w_var3 = 0.5 * (A3(M->w3, K, J, I) + A3(M->w3, K, J, I + 1));
+        w_var1 = 0.5 * (A3(M->w3, K, J, I) + A3(M->w3, K, J, I - 1));
+        h_rho = A3(M->h3, K, J, I) / A3(M->rho3, K, J, I);
+        s13 = .5 * ((u_var1 - u_var3) * dz_inv + h_rho * (w_var3 - w_var1) * m_2jp1);
+        v_var3 = 0.5 * (A3(V, K + 1, J, I) + A3(V, K + 1, J + 1, I));
+        v_var1 = 0.5 * (A3(V, K - 1, J, I) + A3(V, K - 1, J + 1, I));
+        w_var3 = 0.5 * (A3(M->w3, K, J, I) + A3(M->w3, K, J + 1, I));
+        w_var1 = 0.5 * (A3(M->w3, K, J, I) + A3(M->w3, K, J - 1, I));
+        s23 = .5 * ((v_var1 - v_var3) * dz_inv + h_rho * (w_var3 - w_var1) * n_2jp1);
+        S = sqrt(2. * (s11 * s11 + s22 * s22 + s33 * s33 + 2. * (s12 * s12 + s13 * s13 + s23 * s23)));
+        tmp1 = kappa_2 * d_tilda * d_tilda;
+        S_tilda = S + (A3(NU, K, J, I) * fv2) / tmp1;
+        tmp2 = S_tilda * tmp1;
+        dnudt = cb1 * S_tilda * A3(NU, K, J, I);
+        dnudt += (cb2 / sigma) * pow(((A3(NU, K, J, I + 1) - A3(NU, K, J, I - 1)) * m_2jp1 * .5), 2.);
+        dnudt += (cb2 / sigma) * pow(.5 * ((A3(NU, K, J + 1, I) - A3(NU, K, J, I)) * n_2jp2 +
+                                           (A3(NU, K, J, I) - A3(NU, K, J - 1, I)) * n_2j), 2.);
+        dnudt += (cb2 / sigma) * pow(((A3(NU, K - 1, J, I) - A3(NU, K + 1, J, I)) * dz_inv), 2.);
+        fw = 1.;
+        if (tmp2 != 0.) {
+          r_sa = A3(NU, K, J, I) / tmp2;
+          if (r_sa < 0.) turb_error(M, "source_sink_SA: r_sa < 0", J, I, r_sa);
+          else if (r_sa < 10.) {
+            g_sa = r_sa + cw2 * (pow(r_sa, 6.) - r_sa);
+            fw = g_sa * pow(((1. + cw3_6) / (pow(g_sa, 6.) + cw3_6)), (1. / 6.));
+          }
+        }
+        dnudt -= cw1 * fw * pow((A3(NU, K, J, I) / d_tilda), 2.);
+        brunt2 = brunt2_iface(M, K, J, I);
+        brunt = sqrt(fabs(brunt2));
+        if (brunt2 < 0.) dnudt -= A3(NU, K, J, I) * exp(-A3(NU, K, J, I) / nu_turb_limiter) * brunt2 / brunt;
+        A3(NU, K, J, I) += DT * dnudt;
+        A3(NU, K, J, I) = dmax(1.e-4 * KINVISC, A3(NU, K, J, I));
+      }
+    }
+  }
+  /* the solid-surface block: the reference computes law_of_the_wall and invert_fv1 for K = nk-1
+   * and then overwrites NU_TURB(nk) with MAX(1e-4 kinvisc, NU_TURB(nk-1)), :2690-2704 */
+  if (!M->g.gas_giant)
+    for (J = 0; J <= NJ; J++)
+      for (I = 1; I <= NI; I++) A3(NU, KHI, J, I) = dmax(1.e-4 * KINVISC, A3(NU, KHI - 1, J, I));
+  bc3(M, NU);
+}
+
+/* restore_mass(NU_TURB_INDEX), epic_adjust.c:80-88 */
+static void restore_nu_turb(ep_model *M) {
+  int K, J, I;
+  for (K = 0; K <= KHI + 1; K++)
+    for (J = 0; J <= NJ; J++)
+      for (I = 0; I <= NI + 1; I++) A3(M->nu_turb, K, J, I) = dmax(1.e-4 * KINVISC, A3(M->nu_turb, K, J, I));
+}
+
+/* laplacian_h, epic_subgrid.c:423-583: DIFF_COEF times the Laplacian of an h-grid plane, with the
+ * zonal filter on a copy of hh before d/dx and on the x-flux before its divergence */
+static void laplacian_h(ep_model *M, const double *hh, const double *diff_coef, double *lph) {
+  double *gh1 = M->b2d[3], *gh2 = M->b2d[4], *buffji = M->b2d[5], m_2jp1, n_2jp1, m_2j_inv, m_2jp2_inv;
+  int J, I;
+  memset(gh1, 0, M->n2 * sizeof(double));
+  memset(gh2, 0, M->n2 * sizeof(double));
+  memcpy(buffji, hh, M->n2 * sizeof(double));
+  zonal_filter_2d(M, IDX_OTHER, buffji);
+  for (J = 0; J <= NJ; J++)
+    for (I = 1; I <= NI; I++) A2(gh1, J, I) = M->m[2 * J + 1] * (A2(buffji, J, I) - A2(buffji, J, I - 1));
+  for (J = 1; J <= NJ; J++)
+    for (I = 1; I <= NI; I++) A2(gh2, J, I) = M->n[2 * J] * (A2(hh, J, I) - A2(hh, J - 1, I));
+  bc2(M, gh1);
+  bc2(M, gh2);
+  for (J = 0; J <= NJ; J++)
+    for (I = 1; I <= NI; I++) A2(gh1, J, I) *= .5 * (A2(diff_coef, J, I) + A2(diff_coef, J, I - 1));
+  bc2(M, gh1);
+  for (J = 1; J <= NJ; J++)
+    for (I = 1; I <= NI; I++) A2(gh2, J, I) *= .5 * (A2(diff_coef, J, I) + A2(diff_coef, J - 1, I));
+  bc2(M, gh2);
+  zonal_filter_2d(M, IDX_U, gh1);
+  for (J = 0; J <= NJ; J++) {
+    m_2jp1 = M->m[2 * J + 1];
+    n_2jp1 = M->n[2 * J + 1];
+    m_2j_inv = (J == 0) ? 0. : 1. / M->m[2 * J];
+    m_2jp2_inv = (J == NJ) ? 0. : 1. / M->m[2 * J + 2];
+    for (I = 1; I <= NI; I++)
+      A2(lph, J, I) = m_2jp1 * ((A2(gh1, J, I + 1) - A2(gh1, J, I)) +
+                                n_2jp1 * (A2(gh2, J + 1, I) * m_2jp2_inv - A2(gh2, J, I) * m_2j_inv));
+  }
+  bc2(M, lph);
+}
+
+/* scalar_horizontal_diffusion, :275-415: THETA (interfaces k_sigma-1 .. nk), set_p2etc, NU_TURB
+ * (interfaces 1 .. nk) */
+static void scalar_horizontal_diffusion(ep_model *M) {
+  const double sigma_inv = 3. / 2., dt = DT;
+  double *hh = M->b2d[0], *lph = M->b2d[1], *dc = M->b2d[2];
+  int K, J, I;
+  for (K = M->g.k_sigma - 1; K <= KHI; K++) {
+    for (J = 0; J <= NJ; J++)
+      for (I = 0; I <= NI + 1; I++) {
+        A2(hh, J, I) = A3(M->theta, K, J, I);
+        A2(dc, J, I) = A3(M->dc_theta, K, J, I);
+      }
+    laplacian_h(M, hh, dc, lph);
+    for (J = 0; J <= NJ; J++)
+      for (I = 0; I <= NI + 1; I++) A3(M->theta, K, J, I) += dt * A2(lph, J, I);
+  }
+  set_p2etc(M, 1);
+  for (K = 1; K <= KHI; K++) {
+    for (J = 0; J <= NJ; J++)
+      for (I = 0; I <= NI + 1; I++) {
+        A2(hh, J, I) = A3(M->nu_turb, K, J, I);
+        A2(dc, J, I) = sigma_inv * (KINVISC + A3(M->nu_turb, K, J, I));
+      }
+    laplacian_h(M, hh, dc, lph);
+    for (J = 0; J <= NJ; J++)
+      for (I = 0; I <= NI + 1; I++) A3(M->nu_turb, K, J, I) += dt * A2(lph, J, I);
+  }
+  restore_nu_turb(M);
+}
+
+/* band_decomp / band_back_sub for m1 = m2 = 1 (Numerical Recipes' bandec/banbks with partial
+ * pivoting, zero-based), epic_funcs_util.c:3130-3260: A[i][0..2] holds row i's band */
+static void band_decomp3(int n, double (*A)[3], double *al, int *index) {
+  int i, j, k, l = 1;
+  double tmp;
+  A[0][0] = A[0][1]; A[0][1] = A[0][2]; A[0][2] = 0.;
+  for (k = 0; k < n; k++) {
+    tmp = A[k][0];
+    i = k;
+    if (l < n) l++;
+    for (j = k + 1; j < l; j++)
+      if (fabs(A[j][0]) > fabs(tmp)) { tmp = A[j][0]; i = j; }
+    index[k] = i;
+    if (tmp == 0.) A[k][0] = 1.e-20;
+    if (i != k)
+      for (j = 0; j < 3; j++) { tmp = A[k][j]; A[k][j] = A[i][j]; A[i][j] = tmp; }
+    for (i = k + 1; i < l; i++) {
+      tmp = A[i][0] / A[k][0];
+      al[k] = tmp;
+      for (j = 1; j < 3; j++) A[i][j - 1] = A[i][j] - tmp * A[k][j];
+      A[i][2] = 0.;
+    }
+  }
+}
+static void band_back_sub3(int n, double (*A)[3], const double *al, const int *index, double *b) {
+  int i, k, l = 1;
+  double tmp;
+  for (k = 0; k < n; k++) {
+    i = index[k];
+    if (i != k) { tmp = b[k]; b[k] = b[i]; b[i] = tmp; }
+    if (l < n) l++;
+    for (i = k + 1; i < l; i++) b[i] -= al[k] * b[k];
+  }
+  l = 1;
+  for (i = n - 1; i >= 0; i--) {
+    tmp = b[i];
+    for (k = 1; k < l; k++) tmp -= A[i][k] * b[k + i];
+    b[i] = tmp / A[i][0];
+    if (l < 3) l++;
+  }
+}
+
+/* crank_nicolson, epic_funcs_util.c:3643-3787, with tridiag(WITH_PIVOTING) (:2994-3120):
+ * band_decomp, band_back_sub and one band_improve pass (:3330-3400).  Arrays z, A, mu, rho and
+ * ans are indexed 0 .. n+1; A[0] or A[n+1] above .99e20 marks a no-flux end.  Returns nonzero
+ * if z is not increasing where it is used. */
+static int crank_nicolson(ep_model *M, int n, double dt, const double *z, const double *A, const double *mu,
+                          const double *rho, double *ans) {
+  double (*Ab)[3] = (double (*)[3])M->tb, (*Ao)[3] = (double (*)[3])M->taorig, *a = M->tl, *b = M->tl + (n + 2),
+         *c = M->tl + 2 * (n + 2), *r = M->tr, *al = M->tal, coeff1, coeff3, factor, sdp;
+  int j, jstart = A[0] > .99e+20 ? 2 : 1, jend = A[n + 1] > .99e+20 ? n : n + 1, i, k, jj;
+  for (j = jstart; j <= jend; j++)
+    if (z[j] <= z[j - 1]) return 1;
+  coeff3 = (A[0] > .99e+20) ? 0. : mu[0] / (z[1] - z[0]);
+  a[0] = 0.;
+  c[n - 1] = 0.;
+  for (j = 1; j <= n; j++) {
+    coeff1 = coeff3;
+    if (j == 1) {
+      coeff3 = mu[j] / (z[j + 1] - z[j]);
+      factor = rho ? dt / (rho[j] * (z[j + 1] - z[j - 1])) : dt / (z[j + 1] - z[j - 1]);
+      b[j - 1] = 1. + (coeff1 + coeff3) * factor;
+      c[j - 1] = -coeff3 * factor;
+      r[j - 1] = 2. * A[j - 1] * coeff1 * factor + A[j] * (1. - (coeff1 + coeff3) * factor) + A[j + 1] * coeff3 * factor;
+    } else if (j == n) {
+      coeff3 = (A[n + 1] > .99e+20) ? 0. : mu[j] / (z[j + 1] - z[j]);
+      factor = rho ? dt / (rho[j] * (z[j + 1] - z[j - 1])) : dt / (z[j + 1] - z[j - 1]);
+      a[j - 1] = -coeff1 * factor;
+      b[j - 1] = 1. + (coeff1 + coeff3) * factor;
+      r[j - 1] = A[j - 1] * coeff1 * factor + A[j] * (1. - (coeff1 + coeff3) * factor) + 2. * A[j + 1] * coeff3 * factor;
+    } else {
+      coeff3 = mu[j] / (z[j + 1] - z[j]);
+      factor = rho ? dt / (rho[j] * (z[j + 1] - z[j - 1])) : dt / (z[j + 1] - z[j - 1]);
+      a[j - 1] = -coeff1 * factor;
+      b[j - 1] = 1. + (coeff1 + coeff3) * factor;
+      c[j - 1] = -coeff3 * factor;
+      r[j - 1] = A[j - 1] * coeff1 * factor + A[j] * (1. - (coeff1 + coeff3) * factor) + A[j + 1] * coeff3 * factor;
+    }
+  }
+  for (j = 0; j < n; j++) {
+    Ab[j][2] = Ao[j][2] = c[j];
+    Ab[j][1] = Ao[j][1] = b[j];
+    Ab[j][0] = Ao[j][0] = a[j];
+  }
+  band_decomp3(n, Ab, al, M->tindex);
+  for (j = 0; j < n; j++) ans[j + 1] = r[j];
+  band_back_sub3(n, Ab, al, M->tindex, ans + 1);
+  /* band_improve: residual of the original band matrix in double, one correction */
+  for (i = 0; i < n; i++) {
+    k = i - 1;
+    jj = n - k < 3 ? n - k : 3;
+    sdp = -r[i];
+    for (j = k < 0 ? -k : 0; j < jj; j++) sdp += Ao[i][j] * ans[1 + j + k];
+    M->cd[i] = sdp;
+  }
+  band_back_sub3(n, Ab, al, M->tindex, M->cd);
+  for (i = 0; i < n; i++) ans[i + 1] -= M->cd[i];
+  return 0;
+}
+
+/* scalar_vertical_diffusion, :1273-1488: THETA below k_sigma, set_p2etc, NU_TURB with the wall
+ * stress at the bottom (implicit Crank-Nicolson in z = GZ3/g) */
+static int scalar_vertical_diffusion(ep_model *M) {
+  const double sigma_inv = 3. / 2.;
+  double *tau_wall = M->b2d[0], *zee = M->cz, *aaa = M->ca, *dee = M->crho, *ans = M->cans, *sf = M->sf2, gi;
+  int K, J, I, kay, n;
+  memset(tau_wall, 0, M->n2 * sizeof(double));
+  for (J = 0; J <= NJ; J++)
+    for (I = 1; I <= NI; I++) {
+      gi = M->grav[2 * J + 1];
+      stability_factor(M, J, I, sf);
+      aaa[0] = 1.e+20;
+      zee[0] = A3(M->gz3, KHI, J, I) / gi;
+      for (K = KHI; K >= M->g.k_sigma - 2; K--) {
+        kay = KHI - K + 1;
+        aaa[kay] = A3(M->theta, K, J, I);
+        zee[kay] = A3(M->gz3, K, J, I) / gi;
+      }
+      for (K = KHI; K > M->g.k_sigma - 2; K--) {
+        kay = KHI - K + 1;
+        dee[kay] = sf[2 * K] * .5 * (A3(M->dc_theta, K, J, I) + A3(M->dc_theta, K - 1, J, I));
+      }
+      n = KHI - M->g.k_sigma + 2;
+      if (crank_nicolson(M, n, DT, zee, aaa, dee, NULL, ans)) return fail(M, "crank_nicolson: z not increasing (THETA, J=%d, I=%d)", J, I);
+      for (K = KHI; K >= M->g.k_sigma - 1; K--) A3(M->theta, K, J, I) = ans[KHI - K + 1];
+    }
+  bc3(M, M->theta);
+  set_p2etc(M, 1);
+  tau_surface(M, WALL_H, tau_wall);
+  for (J = 0; J <= NJ; J++)
+    for (I = 1; I <= NI; I++) {
+      gi = M->grav[2 * J + 1];
+      aaa[KHI + 2] = 1.e+20;
+      zee[KHI + 2] = (A3(M->gz3, 0, J, I) + (A3(M->gz3, 0, J, I) - A3(M->gz3, 1, J, I))) / gi;
+      for (K = KHI; K >= 0; K--) {
+        kay = KHI - K + 1;
+        aaa[kay] = A3(M->nu_turb, K, J, I);
+        zee[kay] = A3(M->gz3, K, J, I) / gi;
+      }
+      for (K = KHI; K > 0; K--) {
+        kay = KHI - K + 1;
+        dee[kay] = sigma_inv * (KINVISC + .5 * (A3(M->nu_turb, K, J, I) + A3(M->nu_turb, K - 1, J, I)));
+      }
+      zee[0] = (A3(M->gz3, KHI, J, I) - (A3(M->gz3, KHI - 1, J, I) - A3(M->gz3, KHI, J, I))) / gi;
+      dee[0] = dee[1];
+      aaa[0] = aaa[1] - A2(tau_wall, J, I) * (zee[1] - zee[0]) / dee[0];
+      if (crank_nicolson(M, KHI + 1, DT, zee, aaa, dee, NULL, ans)) return fail(M, "crank_nicolson: z not increasing (NU_TURB, J=%d, I=%d)", J, I);
+      for (K = KHI; K >= 0; K--) A3(M->nu_turb, K, J, I) = ans[KHI - K + 1];
+    }
+  bc3(M, M->nu_turb);
+  restore_nu_turb(M);
+  return 0;
+}
+
+/* uv_horizontal_diffusion, :1571-1787: the horizontal-gradient viscous stresses of the winds
+ * (Tannehill, Anderson and Pletcher 1997) into DUDT, DVDT */
+static void uv_horizontal_diffusion(ep_model *M) {
+  double *tau11 = M->b2d[0], *tau22 = M->b2d[1], *tau33 = M->b2d[2], *tau12 = M->b2d[3], *coeffd = M->b2d[4],
+         *h_rho = M->b2d[5], *uu = M->b2d[6], *vv = M->b2d[7];
+  double *DU = M->dudt + (long)M->it_uv_tend * M->n3, *DV = M->dvdt + (long)M->it_uv_tend * M->n3;
+  const double *U = M->u + (long)M->it_uv_dis * M->n3, *V = M->v + (long)M->it_uv_dis * M->n3;
+  double rln_inv, m_2jp1, m_2j, n_2jp2, n_2jp1, n_2j, e11, e22, e33, e12, coeff, ze, h_inv;
+  int K, J, I, jj;
+  for (K = 1; K < KHI; K++) {
+    for (J = 0; J <= NJ; J++)
+      for (I = 0; I <= NI + 1; I++) {
+        A2(coeffd, J, I) = M->g.dynvisc + A3(M->rho3, K, J, I) * A3(M->dc_uv, K, J, I);
+        A2(h_rho, J, I) = A3(M->h3, K, J, I) / A3(M->rho3, K, J, I);
+      }
+    memcpy(uu, U + K * M->n2, M->n2 * sizeof(double));
+    memcpy(vv, V + K * M->n2, M->n2 * sizeof(double));
+    zonal_filter_2d(M, IDX_OTHER, coeffd);
+    zonal_filter_2d(M, IDX_OTHER, h_rho);
+    zonal_filter_2d(M, IDX_U, uu);
+    zonal_filter_2d(M, IDX_V, vv);
+    for (J = 0; J <= NJ; J++) {
+      jj = 2 * J;
+      rln_inv = 1. / M->rln[jj + 1];
+      m_2jp1 = M->m[jj + 1];
+      m_2j = M->m[jj];
+      n_2jp2 = M->n[jj + 2];
+      n_2jp1 = M->n[jj + 1];
+      n_2j = M->n[jj];
+      (void)m_2j;
+      for (I = 1; I <= NI; I++) {
+        e11 = (A2(uu, J, I + 1) - A2(uu, J, I)) * m_2jp1 +
+              .5 * (A2(vv, J, I) + A2(vv, J + 1, I)) * rln_inv * (M->rln[jj + 2] - M->rln[jj]) * n_2jp1;
+        e22 = (A2(vv, J + 1, I) - A2(vv, J, I)) * n_2jp1;
+        coeff = .5 / A2(h_rho, J, I);
+        e33 = coeff * (A2(uu, J, I + 1) * (A2(h_rho, J, I + 1) - A2(h_rho, J, I)) * m_2jp1 +
+                       A2(uu, J, I) * (A2(h_rho, J, I) - A2(h_rho, J, I - 1)) * m_2jp1);
+        if (A2(vv, J + 1, I) != 0.) e33 += coeff * A2(vv, J + 1, I) * (A2(h_rho, J + 1, I) - A2(h_rho, J, I)) * n_2jp2;
+        if (A2(vv, J, I) != 0.) e33 += coeff * A2(vv, J, I) * (A2(h_rho, J, I) - A2(h_rho, J - 1, I)) * n_2j;
+        coeff = A2(h_rho, J, I) * (2. / 3.) * A2(coeffd, J, I);
+        A2(tau11, J, I) = coeff * (2. * e11 - e22 - e33);
+        A2(tau22, J, I) = coeff * (2. * e22 - e11 - e33);
+        A2(tau33, J, I) = (coeff / A2(h_rho, J, I)) * (2. * e33 - e11 - e22);
+      }
+    }
+    bc2(M, tau11);
+    bc2(M, tau22);
+    bc2(M, tau33);
+    /* TAU12 at the poles: vorticity(ON_SIGMATHETA, RELATIVE, uu, vv) there (epic_funcs_diag.c:
+     * 4279-4290, 4357-4379), times minus the row's mean of COEFFD H_RHO */
+    ze = 0.;
+    for (I = 1; I <= NI; I++) ze -= A2(uu, 0, I);
+    ze *= M->mn[0] / ((M->m[1]) * (double)(NI));
+    for (I = 1; I <= NI; I++) A2(tau12, 0, I) = ze;
+    ze = 0.;
+    for (I = 1; I <= NI; I++) ze += A2(uu, NJ, I);
+    ze *= M->mn[2 * (NJ + 1)] / (M->m[2 * NJ + 1] * (double)(NI));
+    for (I = 1; I <= NI; I++) A2(tau12, NJ + 1, I) = ze;
+    coeff = 0.;
+    for (I = 1; I <= NI; I++) coeff += A2(coeffd, NJ, I) * A2(h_rho, NJ, I);
+    coeff /= NI;
+    for (I = 1; I <= NI; I++) A2(tau12, NJ + 1, I) *= -coeff;
+    coeff = 0.;
+    for (I = 1; I <= NI; I++) coeff += A2(coeffd, 0, I) * A2(h_rho, 0, I);
+    coeff /= NI;
+    for (I = 1; I <= NI; I++) A2(tau12, 0, I) *= -coeff;
+    for (J = 1; J <= NJ; J++) {
+      jj = 2 * J;
+      m_2j = M->m[jj];
+      n_2j = M->n[jj];
+      for (I = 1; I <= NI; I++) {
+        e12 = (A2(vv, J, I) - A2(vv, J, I - 1)) * m_2j +
+              M->rln[jj] * (A2(uu, J, I) / M->rln[jj + 1] - A2(uu, J - 1, I) / M->rln[jj - 1]) * n_2j;
+        coeff = .25 * (A2(coeffd, J, I) * A2(h_rho, J, I) + A2(coeffd, J, I - 1) * A2(h_rho, J, I - 1) +
+                       A2(coeffd, J - 1, I) * A2(h_rho, J - 1, I) + A2(coeffd, J - 1, I - 1) * A2(h_rho, J - 1, I - 1));
+        A2(tau12, J, I) = coeff * e12;
+      }
+    }
+    bc2(M, tau12);
+    for (J = 0; J <= NJ; J++) {
+      jj = 2 * J;
+      rln_inv = 1. / M->rln[jj + 1];
+      m_2jp1 = M->m[jj + 1];
+      n_2jp1 = M->n[jj + 1];
+      for (I = 1; I <= NI; I++) {
+        h_inv = 2. / (A3(M->hdry, K, J, I) + A3(M->hdry, K, J, I - 1));
+        A3(DU, K, J, I) += h_inv * (m_2jp1 * (A2(tau11, J, I) - A2(tau11, J, I - 1)) +
+                                    n_2jp1 * rln_inv * (M->rln[jj + 2] * A2(tau12, J + 1, I) - M->rln[jj] * A2(tau12, J, I) +
+                                                        .5 * (A2(tau12, J + 1, I) + A2(tau12, J, I)) * (M->rln[jj + 2] - M->rln[jj])) -
+                                    .5 * (A2(tau33, J, I) + A2(tau33, J, I - 1)) * m_2jp1 * (A2(h_rho, J, I) - A2(h_rho, J, I - 1)));
+      }
+    }
+    for (J = 1; J <= NJ; J++) {
+      jj = 2 * J;
+      rln_inv = 1. / M->rln[jj];
+      m_2j = M->m[jj];
+      n_2j = M->n[jj];
+      for (I = 1; I <= NI; I++) {
+        h_inv = 2. / (A3(M->hdry, K, J, I) + A3(M->hdry, K, J - 1, I));
+        A3(DV, K, J, I) += h_inv * (m_2j * (A2(tau12, J, I) - A2(tau12, J, I - 1)) -
+                                    n_2j * rln_inv * (M->rln[jj + 1] * A2(tau22, J, I) - M->rln[jj - 1] * A2(tau22, J - 1, I) -
+                                                      .5 * (A2(tau11, J, I) + A2(tau11, J - 1, I)) * (M->rln[jj + 1] - M->rln[jj - 1])) -
+                                    .5 * (A2(tau33, J, I) + A2(tau33, J - 1, I)) * n_2j * (A2(h_rho, J, I) - A2(h_rho, J - 1, I)));
+      }
+    }
+  }
+}
+
+/* uv_vertical_diffusion, :1940-2075: implicit vertical viscosity of U and V (layers 1 .. nk-1)
+ * with the wall stress below, after the time step (plane it_uv) */
+static int uv_vertical_diffusion(ep_model *M) {
+  double *tau_wall = M->b2d[0], *zee = M->cz, *aaa = M->ca, *rho = M->crho, *ans = M->cans, *sf0 = M->sf0,
+         *sf2 = M->sf2, *U = M->u + (long)M->it_uv * M->n3, *V = M->v + (long)M->it_uv * M->n3, gi;
+  double *mu_b = M->cd + (KHI + 3);   /* crank_nicolson's band_improve residual reuses cd[0..n) */
+  int K, J, I, kay;
+  memset(tau_wall, 0, M->n2 * sizeof(double));
+  tau_surface(M, WALL_U, tau_wall);
+  for (J = 0; J <= NJ; J++)
+    for (I = 1; I <= NI; I++) {
+      gi = M->grav[2 * J + 1];
+      stability_factor(M, J, I, sf2);
+      stability_factor(M, J, I - 1, sf0);
+      aaa[KHI] = 1.e+20;
+      zee[KHI] = .5 * (A3(M->gz3, 0, J, I) + A3(M->gz3, 0, J, I - 1)) / gi;
+      for (K = KHI - 1; K >= 1; K--) {
+        kay = KHI - K;
+        aaa[kay] = A3(U, K, J, I);
+        zee[kay] = .5 * (A3(M->gz3, K, J, I) + A3(M->gz3, K, J, I - 1)) / gi;
+        rho[kay] = .5 * (A3(M->rho3, K, J, I) + A3(M->rho3, K, J, I - 1));
+      }
+      for (K = KHI - 1; K >= 1; K--) {
+        kay = KHI - K;
+        mu_b[kay] = M->g.dynvisc + .5 * (sf2[2 * K] * A3(M->rho2, K, J, I) * .5 * (A3(M->dc_uv, K - 1, J, I) + A3(M->dc_uv, K, J, I)) +
+                                         sf0[2 * K] * A3(M->rho2, K, J, I - 1) * .5 * (A3(M->dc_uv, K - 1, J, I - 1) + A3(M->dc_uv, K, J, I - 1)));
+      }
+      zee[0] = .5 * (A3(M->gz3, KHI, J, I) + A3(M->gz3, KHI, J, I - 1)) / gi;
+      mu_b[0] = mu_b[1];
+      aaa[0] = aaa[1] - A2(tau_wall, J, I) * (zee[1] - zee[0]) / mu_b[0];
+      if (crank_nicolson(M, KHI - 1, DT, zee, aaa, mu_b, rho, ans)) return fail(M, "crank_nicolson: z not increasing (U, J=%d, I=%d)", J, I);
+      for (K = KHI - 1; K >= 1; K--) A3(U, K, J, I) = ans[KHI - K];
+    }
+  bc3(M, U);
+  tau_surface(M, WALL_V, tau_wall);
+  for (J = 1; J <= NJ; J++)
+    for (I = 1; I <= NI; I++) {
+      gi = M->grav[2 * J];
+      stability_factor(M, J, I, sf2);
+      stability_factor(M, J - 1, I, sf0);
+      aaa[KHI] = 1.e+20;
+      zee[KHI] = .5 * (A3(M->gz3, 0, J, I) + A3(M->gz3, 0, J - 1, I)) / gi;
+      for (K = KHI - 1; K >= 1; K--) {
+        kay = KHI - K;
+        aaa[kay] = A3(V, K, J, I);
+        zee[kay] = .5 * (A3(M->gz3, K, J, I) + A3(M->gz3, K, J - 1, I)) / gi;
+        rho[kay] = .5 * (A3(M->rho3, K, J, I) + A3(M->rho3, K, J - 1, I));
+      }
+      for (K = KHI - 1; K >= 1; K--) {
+        kay = KHI - K;
+        mu_b[kay] = M->g.dynvisc + .5 * (sf2[2 * K] * A3(M->rho2, K, J, I) * .5 * (A3(M->dc_uv, K - 1, J, I) + A3(M->dc_uv, K, J, I)) +
+                                         sf0[2 * K] * A3(M->rho2, K, J - 1, I) * .5 * (A3(M->dc_uv, K - 1, J - 1, I) + A3(M->dc_uv, K, J - 1, I)));
+      }
+      zee[0] = .5 * (A3(M->gz3, KHI, J, I) + A3(M->gz3, KHI, J - 1, I)) / gi;
+      mu_b[0] = mu_b[1];
+      aaa[0] = aaa[1] - A2(tau_wall, J, I) * (zee[1] - zee[0]) / mu_b[0];
+      if (crank_nicolson(M, KHI - 1, DT, zee, aaa, mu_b, rho, ans)) return fail(M, "crank_nicolson: z not increasing (V, J=%d, I=%d)", J, I);
+      for (K = KHI - 1; K >= 1; K--) A3(V, K, J, I) = ans[KHI - K];
+    }
+  bc3(M, V);
+  return 0;
+}
+
+static int turb_check(ep_model *M) {
+  if (M->turb_err[0]) return fail(M, "%s", M->turb_err);
+  return 0;
+}
+
+/* ---------------------------------------------------------------------------------------- */
 /* Driver                                                                                   */
 /* ---------------------------------------------------------------------------------------- */
 
@@ -2290,6 +3089,11 @@ int ep_stage(ep_model *M, int stage) {
       restore_mass(M);
       meridional_hyperviscosity(M, IDX_THETA, M->theta);
       zonal_hyperviscosity(M, IDX_THETA, M->theta);
+      if (TURB_ON(M)) {
+        meridional_hyperviscosity(M, IDX_OTHER, M->nu_turb);
+        zonal_hyperviscosity(M, IDX_OTHER, M->nu_turb);
+        restore_nu_turb(M);
+      }
       break;
     case EP_ST_ADVECTION: advection(M); break;
     case EP_ST_PGRAD_VARS: rc = store_pgrad_vars(M); break;
@@ -2302,6 +3106,10 @@ int ep_stage(ep_model *M, int stage) {
       rc = zonal_filter_3d(M, IDX_HDRY, M->hdry);
       if (!rc) restore_mass(M);
       if (!rc) rc = zonal_filter_3d(M, IDX_THETA, M->theta);
+      if (!rc && TURB_ON(M)) {
+        rc = zonal_filter_3d(M, IDX_OTHER, M->nu_turb);
+        if (!rc) restore_nu_turb(M);
+      }
       break;
     case EP_ST_P2ETC_UPDATE: set_p2etc(M, 1); break;
     case EP_ST_UV_PGRAD: uv_pgrad_fv(M); break;
@@ -2313,11 +3121,20 @@ int ep_stage(ep_model *M, int stage) {
       zonal_hyperviscosity(M, IDX_U, M->u + (long)M->it_uv * M->n3);
       zonal_hyperviscosity(M, IDX_V, M->v + (long)M->it_uv * M->n3);
       break;
-    case EP_ST_STORE_DIAG: store_diag(M); break;
+    case EP_ST_STORE_DIAG:
+      store_diag(M);
+      if (TURB_ON(M)) set_diffusion_coef(M);
+      break;
     case EP_ST_CALC_HEATING: calc_heating(M); break;
     case EP_ST_P2ETC_NOUPDATE: set_p2etc(M, 0); break;
+    case EP_ST_TURB_SOURCE: source_sink_sa(M); break;
+    case EP_ST_SCALAR_HDIFF: scalar_horizontal_diffusion(M); break;
+    case EP_ST_SCALAR_VDIFF: rc = scalar_vertical_diffusion(M); break;
+    case EP_ST_UV_HDIFF: uv_horizontal_diffusion(M); break;
+    case EP_ST_UV_VDIFF: rc = uv_vertical_diffusion(M); break;
     default: return fail(M, "unknown stage %d", stage);
   }
+  if (!rc && TURB_ON(M)) rc = turb_check(M);
   return rc;
 }
 
@@ -2328,8 +3145,26 @@ int ep_timestep(ep_model *M, int action) {
                              EP_ST_FILTER_MASS, EP_ST_P2ETC_UPDATE, EP_ST_PGRAD_VARS, EP_ST_UV_PGRAD, EP_ST_DIV_DAMP,
                              EP_ST_UV_UPDATE, EP_ST_UV_HYPERVISC, -1, EP_ST_STORE_DIAG, EP_ST_CALC_HEATING};
   static const int sync[] = {EP_ST_P2ETC_UPDATE, EP_ST_PGRAD_VARS, EP_ST_STORE_DIAG, EP_ST_CALC_HEATING, EP_ST_CALC_W};
+  /* with the turbulence closure (timestep, epic_timestep.c:130-290; the subgrid wrappers
+   * scalar_horizontal_subgrid, scalar_vertical_subgrid, uv_horizontal_subgrid and
+   * uv_vertical_subgrid, epic_subgrid.c:207,1241,1493,1894, choose by diffusion_direction) */
+  int turb[40], nt = 0;
   if (!M->uploaded) return fail(M, "timestep before upload");
-  if (action == EPIC_STEP_PROGS_AND_SYNC_DIAGS) {
+  if (action == EPIC_STEP_PROGS_AND_SYNC_DIAGS && TURB_ON(M)) {
+    for (s = 0; s < (int)(sizeof(step) / sizeof(step[0])); s++) {
+      if (step[s] == EP_ST_UV_CORE) turb[nt++] = EP_ST_TURB_SOURCE;
+      if (step[s] == EP_ST_SCALAR_HSUB && DIFF_HORIZONTAL(M)) turb[nt++] = EP_ST_SCALAR_HDIFF;
+      if (step[s] == EP_ST_DIV_DAMP && DIFF_HORIZONTAL(M)) turb[nt++] = EP_ST_UV_HDIFF;
+      if (step[s] == EP_ST_UV_HYPERVISC && DIFF_VERTICAL(M)) turb[nt++] = EP_ST_UV_VDIFF;
+      turb[nt++] = step[s];
+      if (step[s] == EP_ST_SCALAR_HSUB && DIFF_VERTICAL(M)) turb[nt++] = EP_ST_SCALAR_VDIFF;
+    }
+    for (s = 0; s < nt; s++) {
+      if (turb[s] < 0) { M->model_time += M->g.dt; continue; }
+      rc = ep_stage(M, turb[s]);
+      if (rc) return rc;
+    }
+  } else if (action == EPIC_STEP_PROGS_AND_SYNC_DIAGS) {
     for (s = 0; s < (int)(sizeof(step) / sizeof(step[0])); s++) {
       if (step[s] < 0) { M->model_time += M->g.dt; continue; }
       rc = ep_stage(M, step[s]);
@@ -2413,6 +3248,20 @@ ep_model *ep_create(const epic_grid *g) {
   M->eps13 = pow(eps, 1. / 3.);
   M->mu_dry = 1. / (M->g.rgas / R_GAS);
   if (M->g.x_h2 > 0.) thermo_setup(M);
+  if (g->turbulence != EPIC_TURB_OFF) {
+    const int nc = g->nk + 3;
+    if (g->turbulence != EPIC_TURB_SA_DES || g->diffusion_direction < 1 || g->diffusion_direction > 3) {
+      snprintf(create_err, sizeof(create_err), "turbulence=%d, diffusion_direction=%d", g->turbulence, g->diffusion_direction);
+      free(M);
+      return NULL;
+    }
+    M->nu_turb = dup1(NULL, M->n3); M->dc_uv = dup1(NULL, M->n3); M->dc_theta = dup1(NULL, M->n3); M->dc_mass = dup1(NULL, M->n3);
+    M->cz = dup1(NULL, nc); M->ca = dup1(NULL, nc); M->cd = dup1(NULL, 2 * nc); M->crho = dup1(NULL, nc);
+    M->cans = dup1(NULL, nc); M->sf0 = dup1(NULL, 2 * nc); M->sf2 = dup1(NULL, 2 * nc); M->ri = dup1(NULL, 2 * nc);
+    M->tb = dup1(NULL, 3 * nc); M->taorig = dup1(NULL, 3 * nc); M->tl = dup1(NULL, 3 * nc); M->tr = dup1(NULL, nc);
+    M->tal = dup1(NULL, nc);
+    M->tindex = (int *)calloc(nc, sizeof(int));
+  }
   {
     /* set_max_nu, epic_subgrid.c:82-158 */
     double dt = (double)g->dt, dy2 = g->dy0 * g->dy0;
@@ -2443,6 +3292,12 @@ void ep_destroy(ep_model *M) {
   for (i = 0; i < (int)(sizeof(ps) / sizeof(ps[0])); i++) free(*ps[i]);
   for (i = 0; i < 8; i++) free(M->b2d[i]);
   free(M->table); free(M->h_coef); free(M->v_coef);
+  {
+    double *turb[] = {M->nu_turb, M->dc_uv, M->dc_theta, M->dc_mass, M->cz, M->ca, M->cd, M->crho, M->cans, M->sf0,
+                      M->sf2, M->ri, M->tb, M->taorig, M->tl, M->tr, M->tal};
+    for (i = 0; i < (int)(sizeof(turb) / sizeof(turb[0])); i++) free(turb[i]);
+    free(M->tindex);
+  }
   free(M);
 }
 
@@ -2464,6 +3319,14 @@ int ep_upload(ep_model *M, const epic_fields *f) {
   UP3(h3); UP3(p2); UP3(theta2); UP3(t2); UP3(t3); UP3(rho2); UP3(rho3); UP3(exner3); UP3(gz3); UP3(mont3); UP3(heat3);
   UP3(pv3); UP3(ri2); UP3(div_uv3); UP3(w3); UP3(dzdt3);
 #undef UP3
+  if (TURB_ON(M)) {
+    if (!f->nu_turb) return fail(M, "ep_upload: the turbulence closure needs nu_turb");
+    memcpy(M->nu_turb, f->nu_turb, M->n3 * sizeof(double));
+#define UPT(x, y) do { if (f->y) memcpy(M->x, f->y, M->n3 * sizeof(double)); else memset(M->x, 0, M->n3 * sizeof(double)); } while (0)
+    UPT(dc_uv, diffusion_coef_uv); UPT(dc_theta, diffusion_coef_theta); UPT(dc_mass, diffusion_coef_mass);
+#undef UPT
+    M->turb_err[0] = 0;
+  }
   M->it_zero = f->it_zero; M->it_minus1 = f->it_minus1; M->it_minus2 = f->it_minus2;
   M->itime = (long)f->itime;
   M->model_time = (long)f->model_time;
@@ -2482,6 +3345,10 @@ int ep_download(ep_model *M, epic_fields *f) {
   CP3(f->exner3, M->exner3); CP3(f->gz3, M->gz3); CP3(f->mont3, M->mont3); CP3(f->heat3, M->heat3); CP3(f->pv3, M->pv3);
   CP3(f->ri2, M->ri2); CP3(f->div_uv3, M->div_uv3); CP3(f->w3, M->w3); CP3(f->dzdt3, M->dzdt3); CP3(f->u_spinup, M->u_spinup);
   if (f->gz_surface) memcpy(f->gz_surface, M->gz_surface, M->n2 * sizeof(double));
+  if (TURB_ON(M)) {
+    CP3(f->nu_turb, M->nu_turb); CP3(f->diffusion_coef_uv, M->dc_uv); CP3(f->diffusion_coef_theta, M->dc_theta);
+    CP3(f->diffusion_coef_mass, M->dc_mass);
+  }
   f->it_zero = M->it_zero; f->it_minus1 = M->it_minus1; f->it_minus2 = M->it_minus2;
   f->itime = M->itime;
   f->model_time = M->model_time;

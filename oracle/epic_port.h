@@ -40,7 +40,14 @@ enum ep_stage {
   EP_ST_STORE_DIAG = 16,     /* store_diag                                  epic_funcs_diag.c:3963 */
   EP_ST_CALC_HEATING = 17,   /* calc_heating                                epic_funcs_diag.c:4793 */
   EP_ST_P2ETC_NOUPDATE = 18, /* set_p2etc(DONT_UPDATE_THETA)                epic_funcs_diag.c:3352 */
-  EP_ST_COUNT = 19
+  EP_ST_COUNT = 19,
+  /* the turbulence closure (epic_grid.turbulence on); with it, stage 5 adds NU_TURB's
+   * hyperviscosity, stage 10 NU_TURB's 3-D filter and stage 16 set_diffusion_coef */
+  EP_ST_TURB_SOURCE = 21,    /* source_sink_turb (source_sink_SA)           epic_subgrid.c:2434    */
+  EP_ST_SCALAR_HDIFF = 22,   /* scalar_horizontal_diffusion                 epic_subgrid.c:275     */
+  EP_ST_SCALAR_VDIFF = 23,   /* scalar_vertical_diffusion                   epic_subgrid.c:1273    */
+  EP_ST_UV_HDIFF = 24,       /* uv_horizontal_diffusion                     epic_subgrid.c:1571    */
+  EP_ST_UV_VDIFF = 25        /* uv_vertical_diffusion                       epic_subgrid.c:1940    */
 };
 
 ep_model  *ep_create(const epic_grid *g);

@@ -56,18 +56,22 @@ int ref_init(const epic_grid *g, const epic_fields *f) {
     thermo_setup(planet, &planet->cpr);
   }
   if (planet->re != g->re || planet->rp != g->rp || planet->cp != g->cp || planet->rgas != g->rgas ||
-      planet->kappa != g->kappa || planet->cpr != g->cpr || planet->kinvisc != g->kinvisc)
+      planet->kappa != g->kappa || planet->cpr != g->cpr || planet->kinvisc != g->kinvisc ||
+      (g->turbulence && planet->dynvisc != g->dynvisc))
     return -2;
 
   /* What var_read(SIZE_DATA) and (POST_SIZE_DATA) supply for a held_suarez epic.nc. */
   strcpy(grid.geometry, "globe");
   strcpy(grid.uv_timestep_scheme, g->uv_scheme == EPIC_UV_AB3 ? "3rd-order Adams-Bashforth" : "Leapfrog (Asselin filtered)");
-  strcpy(grid.turbulence_scheme, "off");
+  strcpy(grid.turbulence_scheme, g->turbulence == EPIC_TURB_SA_DES ? "Spalart-Allmaras DES" : "off");
+  grid.diffusion_direction = g->diffusion_direction;
+  strcpy(grid.stability_factor, g->stability_factor ? "Collins et al. (2004)" : "off");
   strcpy(grid.eos, "ideal");
   strcpy(grid.advection_scheme, g->advection_scheme == EPIC_ADV_AKIMA ? "Monotonized, 4th-order centered (Akima)"
                                                                       : "Predictor-corrector (Hsu, Konor, and Arakawa)");
   strcpy(var.theta.advection_scheme, grid.advection_scheme);
   strcpy(var.hdry.advection_scheme, grid.advection_scheme);
+  strcpy(var.nu_turb.advection_scheme, grid.advection_scheme);
   grid.nk = g->nk; grid.nj = g->nj; grid.ni = g->ni; grid.dt = g->dt;
   grid.wrap[0] = 1; grid.wrap[1] = 0; grid.wrap[2] = 0;
   grid.pad[0] = grid.pad[1] = grid.pad[2] = 1;
@@ -85,8 +89,9 @@ int ref_init(const epic_grid *g, const epic_fields *f) {
   for (I = 0; I <= MAX_NU_ORDER; I++) grid.nu[I] = g->nu[I];
   grid.itime = 0;
   var.on_list[U_INDEX] = var.on_list[V_INDEX] = var.on_list[HDRY_INDEX] = var.on_list[THETA_INDEX] = 1;
+  if (g->turbulence == EPIC_TURB_SA_DES) var.on_list[NU_TURB_INDEX] = 1;
 
-  make_arrays(planet);
+  make_arrays(planet);   /* with the turbulence scheme on, this also allocates D_WALL (make_arrays_subgrid) */
   for (I = 0; I < NUM_WORKING_BUFFERS; I++) ref_buff2d[I] = fvector(0, Nelem2d - 1, "ref_harness");
   if (grid.t_sponge_inv == NULL) grid.t_sponge_inv = fvector(0, grid.k_sponge, "ref_harness");
   for (K = 0; K <= grid.k_sponge; K++) grid.t_sponge_inv[K] = g->t_sponge_inv[K];
@@ -129,6 +134,13 @@ int ref_init(const epic_grid *g, const epic_fields *f) {
   memcpy(var.p3.value, f->p3, Nelem3d * sizeof(double));
   memcpy(var.gz_surface.value, f->gz_surface, Nelem2d * sizeof(double));
   memcpy(var.u_spinup.value, f->u_spinup, Nelem3d * sizeof(double));
+  if (g->turbulence == EPIC_TURB_SA_DES) {
+    if (!f->nu_turb || !var.nu_turb.value) return -3;
+    memcpy(var.nu_turb.value, f->nu_turb, Nelem3d * sizeof(double));
+    if (f->diffusion_coef_uv) memcpy(var.diffusion_coef_uv.value, f->diffusion_coef_uv, Nelem3d * sizeof(double));
+    if (f->diffusion_coef_theta) memcpy(var.diffusion_coef_theta.value, f->diffusion_coef_theta, Nelem3d * sizeof(double));
+    if (f->diffusion_coef_mass) memcpy(var.diffusion_coef_mass.value, f->diffusion_coef_mass, Nelem3d * sizeof(double));
+  }
   IT_ZERO = f->it_zero; IT_MINUS1 = f->it_minus1; IT_MINUS2 = f->it_minus2;
   grid.itime = f->itime;
   var.model_time = (time_t)f->model_time;
@@ -188,6 +200,10 @@ int ref_get(epic_fields *f) {
   cp3(f->ri2, var.ri2.value); cp3(f->div_uv3, var.div_uv3.value); cp3(f->w3, var.w3.value);
   cp3(f->dzdt3, var.dzdt3.value); cp3(f->u_spinup, var.u_spinup.value);
   if (f->gz_surface) memcpy(f->gz_surface, var.gz_surface.value, Nelem2d * sizeof(double));
+  if (var.nu_turb.on) {
+    cp3(f->nu_turb, var.nu_turb.value); cp3(f->diffusion_coef_uv, var.diffusion_coef_uv.value);
+    cp3(f->diffusion_coef_theta, var.diffusion_coef_theta.value); cp3(f->diffusion_coef_mass, var.diffusion_coef_mass.value);
+  }
   f->it_zero = IT_ZERO; f->it_minus1 = IT_MINUS1; f->it_minus2 = IT_MINUS2;
   f->itime = (int64_t)grid.itime;
   f->model_time = (int64_t)var.model_time;

@@ -71,6 +71,7 @@ class Port:
         self.lib = port_lib(cr_libm)
         self.layout = grid.layout
         self.uv_scheme = grid.struct.uv_scheme
+        self.turbulence = bool(grid.struct.turbulence)
         h = self.lib.ep_create(C.byref(grid.struct))
         if not h:
             raise RuntimeError("ep_create: " + self.lib.ep_create_error().decode())
@@ -84,7 +85,7 @@ class Port:
         self._chk(self.lib.ep_upload(self.h, C.byref(f.struct)), "ep_upload")
 
     def download(self) -> Fields:
-        f = Fields(self.layout.ni, self.layout.nj, self.layout.nk, self.uv_scheme)
+        f = Fields(self.layout.ni, self.layout.nj, self.layout.nk, self.uv_scheme, turbulence=self.turbulence)
         self._chk(self.lib.ep_download(self.h, C.byref(f.struct)), "ep_download")
         return f
 
@@ -112,7 +113,7 @@ def fields_to_dict(f: Fields) -> dict:
 
 
 def dict_to_fields(d: dict, ni, nj, nk, uv_scheme) -> Fields:
-    f = Fields(ni, nj, nk, uv_scheme)
+    f = Fields(ni, nj, nk, uv_scheme, turbulence="nu_turb" in d)
     for k in f.arrays:
         f.arrays[k][...] = d[k]
     for n in ("it_zero", "it_minus1", "it_minus2", "itime", "model_time"):
@@ -146,7 +147,7 @@ def _ref_worker(grid_arrays: dict, grid_scalars: dict, fields: dict, dims, sched
                 lib.ref_timestep(EPIC_SYNC_DIAGS_ONLY)
             else:
                 lib.ref_run(n)
-            g = Fields(ni, nj, nk, scheme)
+            g = Fields(ni, nj, nk, scheme, turbulence=bool(ga.struct.turbulence))
             lib.ref_get(C.byref(g.struct))
             out.append(fields_to_dict(g))
         q.put(("ok", list(geo), out))
@@ -162,7 +163,14 @@ def run_reference(ga: GridArrays, f: Fields, schedule) -> tuple[list, list]:
     p = ctx.Process(target=_ref_worker, args=({k: v.copy() for k, v in ga.arrays.items()}, ga.scalars(),
                                                fields_to_dict(f), dims, schedule, q))
     p.start()
-    status, geo, out = q.get(timeout=1800)
+    import queue
+    while True:   # a reference that exits (its epic_error) reports nothing: stop waiting then
+        try:
+            status, geo, out = q.get(timeout=5)
+            break
+        except queue.Empty:
+            if not p.is_alive():
+                raise RuntimeError(f"the reference process ended with exit code {p.exitcode} before reporting")
     p.join(60)
     if status != "ok":
         raise RuntimeError(geo)

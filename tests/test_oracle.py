@@ -169,6 +169,35 @@ def test_hydrogen_thermodynamics_match_reference(scheme, state):
             assert np.array_equal(got.arrays[k], want.arrays[k]), f"snapshot {i}: field {k} differs"
 
 
+@pytest.mark.parametrize("scheme,state,gg,direction", [(EPIC_UV_AB3, "jet", False, 1), (EPIC_UV_LEAPFROG, "hs", False, 1),
+                                                       (EPIC_UV_AB3, "jet", True, 1), (EPIC_UV_AB3, "jet", False, 2),
+                                                       (EPIC_UV_AB3, "jet", False, 3)])
+def test_turbulence_matches_reference(scheme, state, gg, direction):
+    """The Spalart-Allmaras DES closure (source_sink_turb, the horizontal and vertical subgrid
+    diffusion of THETA, NU_TURB and the winds, set_diffusion_coef in store_diag) on the
+    Held-Suarez planet, terrestrial or gas-giant: the restatement against the reference's step,
+    every field (NU_TURB and the diffusivities included) bit for bit after every step."""
+    if not reference_available():
+        pytest.skip("reference source tree not present on this host")
+    cfg = HSConfig(ni=32, nj=16, nk=10, dt=300, uv_scheme=scheme, seed=9, state=state,
+                   profile=EPIC_PROFILE_N2 if state == "jet" else 0, gas_giant=gg, turbulence=True,
+                   diffusion_direction=direction)
+    ga, f = hs_setup(cfg)
+    sched = [("sync", 0)] + [("step", 1)] * 6
+    geo, snaps = run_reference(ga, f, sched)
+    port = Port(ga)
+    port.upload(f)
+    for i, (what, n) in enumerate(sched):
+        if what == "sync":
+            port.timestep(EPIC_SYNC_DIAGS_ONLY)
+        else:
+            port.run(n)
+        got = port.download()
+        want = dict_to_fields(snaps[i], 32, 16, 10, scheme)
+        for k in got.arrays:
+            assert np.array_equal(got.arrays[k], want.arrays[k]), f"snapshot {i}: field {k} differs"
+
+
 @pytest.mark.parametrize("seed", [0, 1, 2])
 def test_libm_rounding_floor_at_64x32x10(seed):
     """The CUDA kernels equal the restatement with correctly rounded log/exp/pow bit for bit (the
