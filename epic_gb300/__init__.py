@@ -172,7 +172,7 @@ class Model:
 
     def download(self, f: Fields | None = None) -> Fields:
         if f is None:
-            f = Fields(self.layout.ni, self.layout.nj, self.layout.nk, self.uv_scheme)
+            f = Fields(self.layout.ni, self.layout.nj, self.layout.nk, self.uv_scheme, turbulence=bool(self.grid.struct.turbulence))
         _check(self.lib.epic_model_download(self._h, C.byref(f.struct)), "epic_model_download")
         return f
 
@@ -277,7 +277,8 @@ class Batch:
     def step_host(self, fields: list[Fields], nsteps: int = 1, groups: int = 4, io: int = 0) -> list[Fields]:
         """End-to-end steps with host-resident (pinned) state, copies overlapped with kernels.
         io = EPIC_IO_ALL (0) moves every array each way, EPIC_IO_STATE (1) the prognostic arrays
-        (u, v, dudt, dvdt, hdry, theta) only and leaves the diagnostics on the device."""
+        (u, v, dudt, dvdt, hdry, theta, and nu_turb with the turbulence closure) only and leaves the
+        diagnostics on the device."""
         _check(self.lib.epic_batch_step_host(self._h, self._ptrs(fields), groups, nsteps, io), "epic_batch_step_host")
         return fields
 

@@ -17,7 +17,7 @@ ROOT = os.path.dirname(HERE)
 SRC = os.path.join(HERE, "csrc")
 OUT = os.path.join(HERE, "_lib")
 LIB = os.path.join(OUT, "libepic_gb300.so")
-SOURCES = ["epic_model.cu", "k_filter.cu", "k_filter_gemm.cu", "k_column.cu", "k_column_acc.cu", "k_stencil.cu", "epic_setup.cpp",
+SOURCES = ["epic_model.cu", "k_filter.cu", "k_filter_gemm.cu", "k_column.cu", "k_column_acc.cu", "k_stencil.cu", "k_turb.cu", "epic_setup.cpp",
            "epic_dropin.cpp"]
 ARCH = "-gencode=arch=compute_103a,code=sm_103a"
 

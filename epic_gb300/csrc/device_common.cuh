@@ -18,6 +18,7 @@ enum TuneGroup { TB_UV_CORE = 0, TB_PGRAD, TB_HSU, TB_VISC, TB_DIAG, TB_UPDATE, 
 
 #define EPIC_MAX_NK 126      // column kernels keep per-column arrays of nk+2 entries
 #define EPIC_MAX_NI 1024     // row kernels keep one row of ni entries in shared memory
+#define EPIC_TURB_MAX_NK 64  // the turbulence closure's column solves keep nk+3 entries per array
 
 namespace epic {
 
@@ -38,7 +39,8 @@ struct Ctl {
                                        // its first epic_error); cleared by an upload
 };
 
-enum ErrCode { ERR_NONE = 0, ERR_GZ_MONOTONE = 1, ERR_CALC_W_P = 2, ERR_PCHIP_X = 3, ERR_NONFINITE = 4, ERR_TIMEOUT = 5 };
+enum ErrCode { ERR_NONE = 0, ERR_GZ_MONOTONE = 1, ERR_CALC_W_P = 2, ERR_PCHIP_X = 3, ERR_NONFINITE = 4, ERR_TIMEOUT = 5,
+               ERR_TURB = 6 };
 
 // double-float constants of the mixed form (DevModel::dfc), split on the host
 enum { DFC_KAPPA, DFC_KAPPA_INV, DFC_KAPPA1, DFC_SIGMA_SIGMA, DFC_ZETA0, DFC_ZETA1, DFC_G_COEFF, DFC_ALPHA, DFC_LOG_P0,
@@ -77,6 +79,14 @@ struct DevModel {
   const double *thermo;                     // thermo_setup's tables (thermo_tables in epic_model.cu)
   int gas_giant;                            // planet->type "gas-giant": GZ_SURFACE from gz_from_u in store_pgrad_vars
   int jtp;                                  // grid.jtp: the row where gz_from_u puts GZ_SURFACE's zero
+  // the Spalart-Allmaras DES turbulence closure (FP64 form; k_turb.cu)
+  int turb;                                 // epic_grid.turbulence on
+  int turb_h, turb_v;                       // horizontal / vertical subgrid diffusion (grid.diffusion_direction)
+  int stab;                                 // grid.stability_factor "Collins et al. (2004)" (else "off")
+  double kinvisc, dynvisc, max_nu2;         // planet->kinvisc, planet->dynvisc, set_max_nu's max_nu[2]
+  double *nu_turb, *dc_uv, *dc_theta, *dc_mass;   // NU_TURB and DIFFUSION_COEF_UV, _THETA, _MASS
+  double *turb_pole;                        // scratch: the polar TAU12 rows of uv_horizontal_diffusion
+  const double *turb_maxnu2;                // set_diffusion_coef's taper max_nu[2] MIN(1, (dy0 m)^-2), j = 0..nj
   int mixed;                                // FP32 stencils, advection, hyperviscosity, filter, physics
   int col64;                                // mixed, with the vertical pressure/geopotential integration
                                             // (set_p2etc, store_pgrad_vars) and the pressure gradient in FP64
@@ -508,6 +518,22 @@ __device__ __forceinline__ int find_place_in_table(int n, const Trip *t, double 
   return il;
 }
 
+// get_kin (the Suarez-Takacs blend for the Sadourney scheme, epic_funcs_diag.c:2694-2847) at h-point
+// (j, i) of the layer planes Uk, Vk
+template <class R>
+__device__ __forceinline__ R kin_at(const DevModel &M, const double *Uk, const double *Vk, int j, int i) {
+  const int jj = 2 * j;
+  const R mn1 = cv<R>(M.mn[jj + 1]), mni0 = cv<R>(M.mn_inv[jj]), mni2 = cv<R>(M.mn_inv[jj + 2]);
+  R u2 = cv<R>(Uk[M.at2(j, i)]), u4 = cv<R>(Uk[M.at2(j, i + 1)]), v2 = cv<R>(Vk[M.at2(j, i)]), v4 = cv<R>(Vk[M.at2(j + 1, i)]);
+  const R kin_c = (u2 * u2 + u4 * u4 + mn1 * (v2 * v2 * mni0 + v4 * v4 * mni2)) * R(.25);
+  if (j == 0 || j == M.nj) return kin_c;
+  u2 = R(.5) * (cv<R>(Uk[M.at2(j + 1, i)]) + cv<R>(Uk[M.at2(j - 1, i)]));
+  u4 = R(.5) * (cv<R>(Uk[M.at2(j + 1, i + 1)]) + cv<R>(Uk[M.at2(j - 1, i + 1)]));
+  v2 = R(.5) * (cv<R>(Vk[M.at2(j, i + 1)]) + cv<R>(Vk[M.at2(j, i - 1)]));
+  v4 = R(.5) * (cv<R>(Vk[M.at2(j + 1, i + 1)]) + cv<R>(Vk[M.at2(j + 1, i - 1)]));
+  const R kin_s = (u2 * u2 + u4 * u4 + mn1 * (v2 * v2 * mni0 + v4 * v4 * mni2)) * R(.25);
+  return (R(5.) / R(6.)) * kin_c + (R(1.) / R(6.)) * kin_s;
+}
 // Record the first model error (the reference would epic_error() and exit).
 __device__ __forceinline__ void flag_error(Ctl *c, int code, int k, int j, int i, double v) {
   if (atomicCAS(&c->err_code, 0, code) == 0) {

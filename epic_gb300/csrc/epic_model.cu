@@ -162,6 +162,11 @@ int run_stage_on(const DevModel &M, cudaStream_t s, int stage) {
       launch_zonal_hyperviscosity(M, 2, M.hdry, PL_NONE, s);   // then restore_mass, in the same kernel
       launch_meridional_hyperviscosity(M, 3, M.theta, PL_NONE, s);
       launch_zonal_hyperviscosity(M, 3, M.theta, PL_NONE, s);
+      if (M.turb) {   // NU_TURB (layers 1..nk on the h-grid), then restore_mass(NU_TURB_INDEX)
+        launch_meridional_hyperviscosity(M, 4, M.nu_turb, PL_NONE, s);
+        launch_zonal_hyperviscosity(M, 4, M.nu_turb, PL_NONE, s);
+        launch_restore_nu(M, s);
+      }
       break;
     case 6: {
       // advection(), epic_flux.c:346-637: UNITY, THETA and HDRY with the grid's scheme
@@ -177,6 +182,13 @@ int run_stage_on(const DevModel &M, cudaStream_t s, int stage) {
       meridional(M, M.theta, 1, s);
       zonal(M, M.theta, 0, M.k_sigma - 1, s);
       launch_advection_prep(M, 2, s);
+      if (M.turb) {   // NU_TURB with the same scheme (UNITY stands), before HDRY, epic_flux.c:540-600
+        launch_advection_prep(M, 3, s);
+        vertical(M, M.nu_turb, 3, s);
+        meridional(M, M.nu_turb, 3, s);
+        zonal(M, M.nu_turb, 2, 1, s);
+        launch_advection_prep(M, 4, s);
+      }
       vertical(M, M.hdry, 2, s);
       meridional(M, M.hdry, 2, s);
       zonal(M, M.hdry, 1, 1, s);   // then restore_mass, in the same kernel
@@ -208,6 +220,10 @@ int run_stage_on(const DevModel &M, cudaStream_t s, int stage) {
     case 10:
       launch_varz_filter(M, M.hdry, PL_NONE, 2, 1, M.nk, s);   // then restore_mass, in the same kernel
       launch_varz_filter(M, M.theta, PL_NONE, 3, M.k_sigma - 1, M.nk, s);
+      if (M.turb) {   // NU_TURB (interfaces 0..nk), then restore_mass(NU_TURB_INDEX)
+        launch_varz_filter(M, M.nu_turb, PL_NONE, 4, 0, M.nk, s);
+        launch_restore_nu(M, s);
+      }
       break;
     case 11: launch_set_p2etc(M, 1, s); break;
     case 12: launch_uv_pgrad(M, s); break;
@@ -219,11 +235,20 @@ int run_stage_on(const DevModel &M, cudaStream_t s, int stage) {
       launch_zonal_hyperviscosity(M, 0, M.u, PL_UV, s);
       launch_zonal_hyperviscosity(M, 1, M.v, PL_UV, s);
       break;
-    case 16: launch_store_diag(M, s); break;
+    case 16:
+      launch_store_diag(M, s);
+      if (M.turb) launch_set_diffusion_coef(M, s);
+      break;
     case 17: launch_calc_heating(M, s); break;
     case 18: launch_set_p2etc(M, 0, s); break;
     case 20: launch_calc_w(M, s, true); break;   // stages 1 and 2 in one pass over the columns
     case 19: launch_store_pgrad_vars(M, s); break;   // after stage 11: what the pressure gradient reads
+    // the turbulence closure (epic_subgrid.c)
+    case 21: if (M.turb) launch_source_sink_turb(M, s); break;
+    case 22: if (M.turb) launch_scalar_hdiff(M, s); break;
+    case 23: if (M.turb) launch_scalar_vdiff(M, s); break;
+    case 24: if (M.turb) launch_uv_hdiff(M, s); break;
+    case 25: if (M.turb) launch_uv_vdiff(M, s); break;
     default: return set_error(EPIC_ERR_ARG, "unknown stage %d", stage);
   }
   return check_launch("stage launch");
@@ -233,7 +258,17 @@ int run_stage(epic_model *m, int stage) { return run_stage_on(m->d, m->stream, s
 
 int enqueue_step_on(const DevModel &M, cudaStream_t s) {
   static const int step[] = {0, 20, 3, 4, 5, 6, 7, 8, 9, 10, 11, 19, 12, 13, 14, 15, 16, 17};
-  for (int st : step) {
+  // with the turbulence closure (timestep, epic_timestep.c:130-290): source_sink_turb after
+  // calc_w; the scalar subgrid diffusion around the scalars' hyperviscosity; uv_horizontal_subgrid
+  // before divergence damping, uv_vertical_subgrid after the time update (grid.diffusion_direction
+  // chooses which diffusions run)
+  static const int step_turb[] = {0, 20, 21, 3, 4, 22, 5, 23, 6, 7, 8, 9, 10, 11, 19, 12, 24, 13, 14, 25, 15, 16, 17};
+  const int *seq = M.turb ? step_turb : step;
+  const int n = M.turb ? (int)(sizeof(step_turb) / sizeof(int)) : (int)(sizeof(step) / sizeof(int));
+  for (int q = 0; q < n; q++) {
+    const int st = seq[q];
+    if ((st == 22 || st == 24) && !M.turb_h) continue;
+    if ((st == 23 || st == 25) && !M.turb_v) continue;
     int rc = run_stage_on(M, s, st);
     if (rc) return rc;
   }
@@ -291,8 +326,9 @@ int model_error(const Ctl &c) {
   if (c.err_code == 0) return EPIC_OK;
   static const char *what[] = {"", "store_pgrad_vars: GZ3 not monotonic", "calc_w: p2 >= p4",
                                "zonal_filter: spline_pchip x not increasing", "non-finite value",
-                               "tensor-core filter: product completion not signalled in time"};
-  return set_error(EPIC_ERR_MODEL, "%s at (k=%d, j=%d, i=%d), value %g", c.err_code < 6 ? what[c.err_code] : "model error",
+                               "tensor-core filter: product completion not signalled in time",
+                               "turbulence closure (u_tau = 0, r_sa < 0, dwall <= 0, t_vis < 0 or z not increasing)"};
+  return set_error(EPIC_ERR_MODEL, "%s at (k=%d, j=%d, i=%d), value %g", c.err_code < 7 ? what[c.err_code] : "model error",
                    c.err_k, c.err_j, c.err_i, c.err_val);
 }
 
@@ -390,7 +426,8 @@ size_t model_pool_bytes(const epic_grid &g) {
   return rnd(sizeof(Ctl)) + (n_state3 + n_scratch3) * rnd(n3 * 8) + 3 * rnd(n2 * 8) + rnd((size_t)(g.nj + 3) * (g.nk + 2) * 3 * 8) +
          rnd(ni1 * 8) + 10 * rnd(nj1 * 8) + 3 * rnd(nk1 * 8) + rnd((g.nk + 2) * 8) + rnd((g.k_sponge + 1) * 8) +
          2 * rnd(3 * (g.nj + 2) * 8) + rnd(ntw * 8) + rnd(ntw * 4) + 2 * rnd((g.nj + 1) * 8) + rnd(sizeof(epic::MathTable)) +
-         rnd(32 * sizeof(float2)) + rnd(((size_t)epic::TH_N * epic::TH_M + 4 * epic::TH_M + epic::TH_N) * 8) + 4096;
+         rnd(32 * sizeof(float2)) + rnd(((size_t)epic::TH_N * epic::TH_M + 4 * epic::TH_M + epic::TH_N) * 8) +
+         (g.turbulence ? 4 * rnd(n3 * 8) + rnd(2 * (size_t)(g.nk + 2) * 8) + rnd((size_t)(g.nj + 1) * 8) : 0) + 4096;
 }
 
 }  // namespace
@@ -412,6 +449,14 @@ extern "C" int epic_model_create(const epic_grid *g, int32_t precision, epic_mod
   if (g->nj < 3 || g->nk < 3 || g->nk > EPIC_MAX_NK) return set_error(EPIC_ERR_ARG, "nj=%d nk=%d out of range", g->nj, g->nk);
   if (g->x_h2 < 0. || (g->x_h2 > 0. && precision != EPIC_PREC_FP64))
     return set_error(EPIC_ERR_ARG, "x_h2=%g: hydrogen thermodynamics are in the FP64 form only", g->x_h2);
+  if (g->turbulence != EPIC_TURB_OFF) {
+    if (g->turbulence != EPIC_TURB_SA_DES) return set_error(EPIC_ERR_ARG, "turbulence=%d", g->turbulence);
+    if (precision != EPIC_PREC_FP64) return set_error(EPIC_ERR_ARG, "the turbulence closure is in the FP64 form only");
+    if (g->diffusion_direction < EPIC_DIFFUSION_HORIZONTAL_AND_VERTICAL || g->diffusion_direction > EPIC_DIFFUSION_JUST_VERTICAL)
+      return set_error(EPIC_ERR_ARG, "diffusion_direction=%d", g->diffusion_direction);
+    if (g->nk > EPIC_TURB_MAX_NK) return set_error(EPIC_ERR_ARG, "turbulence closure: nk=%d above %d", g->nk, EPIC_TURB_MAX_NK);
+    if (!(g->kinvisc > 0.)) return set_error(EPIC_ERR_ARG, "turbulence closure: kinvisc=%g", g->kinvisc);
+  }
   if (g->gas_giant && (g->jtp < 0 || g->jtp > g->nj))
     return set_error(EPIC_ERR_ARG, "gas giant: jtp=%d outside the rows 0..%d", g->jtp, g->nj);
   if (3. * (g->ni + 2) * (g->nj + 3) * (g->nk + 2) >= 2147483648.)
@@ -453,6 +498,14 @@ extern "C" int epic_model_create(const epic_grid *g, int32_t precision, epic_mod
   d.hs_kf = g->hs_kf; d.lat0 = g->lat0;
   d.gas_giant = g->gas_giant != 0;
   d.jtp = g->jtp;
+  d.turb = g->turbulence == EPIC_TURB_SA_DES;
+  d.turb_h = d.turb && (g->diffusion_direction == EPIC_DIFFUSION_HORIZONTAL_AND_VERTICAL ||
+                        g->diffusion_direction == EPIC_DIFFUSION_JUST_HORIZONTAL);
+  d.turb_v = d.turb && (g->diffusion_direction == EPIC_DIFFUSION_HORIZONTAL_AND_VERTICAL ||
+                        g->diffusion_direction == EPIC_DIFFUSION_JUST_VERTICAL);
+  d.stab = g->stability_factor != 0;
+  d.kinvisc = g->kinvisc;
+  d.dynvisc = g->dynvisc;
   d.mixed = precision != EPIC_PREC_FP64;
   d.col64 = precision == EPIC_PREC_MIXED;
   d.cr = precision == EPIC_PREC_FP64;
@@ -524,6 +577,14 @@ extern "C" int epic_model_create(const epic_grid *g, int32_t precision, epic_mod
   epic::MathTable *lt = carve<epic::MathTable>(p, 1);
   float2 *exp2tab = carve<float2>(p, 32);
   double *thermo_d = carve<double>(p, (size_t)epic::TH_N * epic::TH_M + 4 * epic::TH_M + epic::TH_N);
+  if (d.turb) {   // the turbulence closure: NU_TURB, the three diffusivities, scratch and a row table
+    d.nu_turb = carve<double>(p, n3);
+    d.dc_uv = carve<double>(p, n3);
+    d.dc_theta = carve<double>(p, n3);
+    d.dc_mass = carve<double>(p, n3);
+    d.turb_pole = carve<double>(p, 2 * (size_t)(g->nk + 2));
+    d.turb_maxnu2 = carve<double>(p, (size_t)g->nj + 1);
+  }
   if ((size_t)(p - m->pool) > bytes) {
     epic_model_destroy(m);
     return set_error(EPIC_ERR_NOMEM, "internal pool layout overflow");
@@ -566,6 +627,18 @@ extern "C" int epic_model_create(const epic_grid *g, int32_t precision, epic_mod
   }
   d.thermo = thermo_d;
   d.x_h2 = g->x_h2; d.x_he = g->x_he; d.x_3 = g->x_3;
+  std::vector<double> maxnu2;
+  if (d.turb) {
+    // set_diffusion_coef's taper of max_nu[2] per row, MIN(1, pow(dy0 m, -2)) with the device's
+    // correctly rounded pow (host-compiled)
+    maxnu2.resize(g->nj + 1);
+    for (int J = 0; J <= g->nj; J++) {
+      const double p2 = epic::cr_pow(g->dy0 * g->m[2 * J + 1], -2., host_lt[0]);
+      maxnu2[J] = T.max_nu[2] * (1. < p2 ? 1. : p2);
+    }
+    cudaMemcpyAsync((void *)d.turb_maxnu2, maxnu2.data(), maxnu2.size() * sizeof(double), cudaMemcpyHostToDevice, m->stream);
+    d.max_nu2 = T.max_nu[2];
+  }
   // 2^(j/32) as double-floats for the double-float exponential of the mixed form
   std::vector<float2> e2(32);
   for (int q = 0; q < 32; q++) {
@@ -663,6 +736,18 @@ int enqueue_upload(epic_model *m, const epic_fields *f, cudaStream_t s, Ctl *c, 
   }
   if (!state_only)
     EPIC_CUDA_CHECK(cudaMemcpyAsync(d.gz_surface, f->gz_surface, (size_t)d.n2 * sizeof(double), cudaMemcpyHostToDevice, s));
+  if (d.turb) {   // NU_TURB is prognostic; the diffusivities are the previous step's store_diag's
+    if (!f->nu_turb) return set_error(EPIC_ERR_ARG, "epic_model_upload: the turbulence closure needs nu_turb");
+    EPIC_CUDA_CHECK(cudaMemcpyAsync(d.nu_turb, f->nu_turb, b3, cudaMemcpyHostToDevice, s));
+    if (!state_only) {
+      const double *tsrc[] = {f->diffusion_coef_uv, f->diffusion_coef_theta, f->diffusion_coef_mass};
+      double *tdst[] = {d.dc_uv, d.dc_theta, d.dc_mass};
+      for (int q = 0; q < 3; q++) {
+        if (tsrc[q]) EPIC_CUDA_CHECK(cudaMemcpyAsync(tdst[q], tsrc[q], b3, cudaMemcpyHostToDevice, s));
+        else EPIC_CUDA_CHECK(cudaMemsetAsync(tdst[q], 0, b3, s));
+      }
+    }
+  }
   if (!with_ctl) return EPIC_OK;
   memset(c, 0, sizeof(*c));
   c->it_zero = f->it_zero; c->it_minus1 = f->it_minus1; c->it_minus2 = f->it_minus2;
@@ -695,6 +780,15 @@ int enqueue_download(epic_model *m, epic_fields *f, cudaStream_t s, Ctl *c, bool
       if (dst[i]) EPIC_CUDA_CHECK(cudaMemcpyAsync(dst[i], src[i], (i < 2 ? d.nvp : (i < 4 ? d.ntp : 1)) * b3, cudaMemcpyDeviceToHost, s));
   }
   if (f->gz_surface && !state_only) EPIC_CUDA_CHECK(cudaMemcpyAsync(f->gz_surface, d.gz_surface, (size_t)d.n2 * sizeof(double), cudaMemcpyDeviceToHost, s));
+  if (d.turb) {
+    if (f->nu_turb) EPIC_CUDA_CHECK(cudaMemcpyAsync(f->nu_turb, d.nu_turb, b3, cudaMemcpyDeviceToHost, s));
+    if (!state_only) {
+      double *tdst[] = {f->diffusion_coef_uv, f->diffusion_coef_theta, f->diffusion_coef_mass};
+      const double *tsrc[] = {d.dc_uv, d.dc_theta, d.dc_mass};
+      for (int q = 0; q < 3; q++)
+        if (tdst[q]) EPIC_CUDA_CHECK(cudaMemcpyAsync(tdst[q], tsrc[q], b3, cudaMemcpyDeviceToHost, s));
+    }
+  }
   EPIC_CUDA_CHECK(cudaMemcpyAsync(c, d.ctl, sizeof(Ctl), cudaMemcpyDeviceToHost, s));
   return EPIC_OK;
 }
@@ -898,6 +992,8 @@ bool batch_compatible(const DevModel &a, const DevModel &b, const char **why) {
   else if ((a.nudiv == 0.) != (b.nudiv == 0.)) *why = "divergence damping on/off";
   else if (a.gas_giant != b.gas_giant) *why = "lower boundary (gas giant or terrain)";
   else if ((a.x_h2 > 0.) != (b.x_h2 > 0.)) *why = "thermodynamics (hydrogen tables or ideal cp)";
+  else if (a.turb != b.turb || a.turb_h != b.turb_h || a.turb_v != b.turb_v)
+    *why = "turbulence closure (on/off, diffusion directions)";
   else if (tensor_filter(a) != tensor_filter(b)) *why = "zonal filter path (ni a multiple of 128 or not)";
   else
     for (int i = 0; i < 9; i++)
@@ -915,6 +1011,10 @@ extern "C" int epic_batch_create(epic_model *const *members, int32_t n, epic_bat
     const char *why = nullptr;
     if (!batch_compatible(members[0]->d, members[i]->d, &why))
       return set_error(EPIC_ERR_ARG, "epic_batch_create: member %d differs from member 0 in %s", i, why);
+    // the turbulence arrays lie outside the regions a launch over members of different sizes moves
+    // its pointer arguments between (relocate_field)
+    if (members[0]->d.turb && (members[i]->d.ni != members[0]->d.ni || members[i]->d.nj != members[0]->d.nj))
+      return set_error(EPIC_ERR_ARG, "epic_batch_create: the turbulence closure batches members of one grid size only (member %d)", i);
     for (int q = 0; q < i; q++)
       if (members[q] == members[i]) return set_error(EPIC_ERR_ARG, "epic_batch_create: member %d repeats member %d", i, q);
     // every kernel of the batch reads and writes each member's pool: all on one device
@@ -1199,27 +1299,35 @@ extern "C" int epic_model_snapshot_begin(epic_model *m, epic_fields *f) {
   if (rc) return rc;
   const DevModel &d = m->d;
   const size_t sb = state_region_bytes(d), gb = (size_t)d.n2 * sizeof(double);
+  const size_t tb = d.turb ? 4 * (size_t)d.n3 * sizeof(double) : 0;   // NU_TURB and the diffusivities
   if (!m->snap) {
     EPIC_CUDA_CHECK(cudaStreamCreateWithFlags(&m->copy_stream, cudaStreamNonBlocking));
     EPIC_CUDA_CHECK(cudaEventCreateWithFlags(&m->snap_taken, cudaEventDisableTiming));
     EPIC_CUDA_CHECK(cudaEventCreateWithFlags(&m->snap_done, cudaEventDisableTiming));
     EPIC_CUDA_CHECK(cudaMallocHost(&m->snap_ctl, sizeof(Ctl)));
-    cudaError_t e = cudaMalloc(&m->snap, sb + gb + sizeof(Ctl));
+    cudaError_t e = cudaMalloc(&m->snap, sb + gb + sizeof(Ctl) + tb);
     if (e != cudaSuccess) {
       m->snap = nullptr;
       return set_error(EPIC_ERR_NOMEM, "snapshot buffer: %s", cudaGetErrorString(e));
     }
   }
-  char *s_state = m->snap, *s_gzs = m->snap + sb, *s_ctl = s_gzs + gb;
+  char *s_state = m->snap, *s_gzs = m->snap + sb, *s_ctl = s_gzs + gb, *s_turb = s_ctl + sizeof(Ctl);
+  const size_t b3 = (size_t)d.n3 * sizeof(double);
   // in stream order, between the steps already enqueued and the ones that follow
   EPIC_CUDA_CHECK(cudaMemcpyAsync(s_state, d.u, sb, cudaMemcpyDeviceToDevice, m->stream));
   EPIC_CUDA_CHECK(cudaMemcpyAsync(s_gzs, d.gz_surface, gb, cudaMemcpyDeviceToDevice, m->stream));
   EPIC_CUDA_CHECK(cudaMemcpyAsync(s_ctl, d.ctl, sizeof(Ctl), cudaMemcpyDeviceToDevice, m->stream));
+  const double *turb_src[] = {d.nu_turb, d.dc_uv, d.dc_theta, d.dc_mass};
+  double *turb_dst[] = {f->nu_turb, f->diffusion_coef_uv, f->diffusion_coef_theta, f->diffusion_coef_mass};
+  if (d.turb)
+    for (int q = 0; q < 4; q++) EPIC_CUDA_CHECK(cudaMemcpyAsync(s_turb + q * b3, turb_src[q], b3, cudaMemcpyDeviceToDevice, m->stream));
   EPIC_CUDA_CHECK(cudaEventRecord(m->snap_taken, m->stream));
   EPIC_CUDA_CHECK(cudaStreamWaitEvent(m->copy_stream, m->snap_taken, 0));
   auto at = [&](const double *dev) { return s_state + ((const char *)dev - (const char *)d.u); };
-  const size_t b3 = (size_t)d.n3 * sizeof(double);
   cudaStream_t cs = m->copy_stream;
+  if (d.turb)
+    for (int q = 0; q < 4; q++)
+      if (turb_dst[q]) EPIC_CUDA_CHECK(cudaMemcpyAsync(turb_dst[q], s_turb + q * b3, b3, cudaMemcpyDeviceToHost, cs));
   if (f->u) EPIC_CUDA_CHECK(cudaMemcpyAsync(f->u, at(d.u), d.nvp * b3, cudaMemcpyDeviceToHost, cs));
   if (f->v) EPIC_CUDA_CHECK(cudaMemcpyAsync(f->v, at(d.v), d.nvp * b3, cudaMemcpyDeviceToHost, cs));
   if (f->dudt) EPIC_CUDA_CHECK(cudaMemcpyAsync(f->dudt, at(d.dudt), d.ntp * b3, cudaMemcpyDeviceToHost, cs));

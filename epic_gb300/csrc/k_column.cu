@@ -176,7 +176,9 @@ __global__ void k_uv_drag(DevModel M) {
 }
 
 // Vertical pass of hsu_advection, epic_flux.c:717-1052.  kind: 0 = unity (P3_INDEX),
-// 1 = THETA, 2 = HDRY.  A column tile (32 columns j = 0..nj, i = 0..ni+1 per block): every pass
+// 1 = THETA, 2 = HDRY, 3 = NU_TURB (loaded, moved by the interface velocities and updated as an
+// interface variable, with the layer variables' predictor and corrector, :876-960, and the floor
+// NU_TURB_MIN).  A column tile (32 columns j = 0..nj, i = 0..ni+1 per block): every pass
 // of the predictor-corrector is pointwise in k given the previous pass, so the levels are
 // spread over the warps with a barrier between passes; d1, d2 and the smoothness weights are
 // recomputed where used (the same expressions, so the same values).  Shared arrays [k][lane]:
@@ -189,22 +191,31 @@ __global__ void __launch_bounds__(CT_THREADS) k_hsu_vertical(DevModel M, double 
   const ColTile c = col_tile(M);
   const int nk = M.nk, L = nk + 2;
   const long long n2 = M.n2;
-  const bool layer = kind == 2;
+  const bool layer = kind == 2, nuk = kind == 3;
   const int kf = kind == 1 ? M.k_sigma - 1 : 1;
   const R ep = R(1.e-10), DT = cv<R>(M.dt);
   R *WA = sm, *WM = WA + 32 * L, *WP = WM + 32 * L, *PR = WP + 32 * L, *FF = PR + 32 * L;
-  auto amin = [&](int k) { return layer ? cv<R>(M.h_min[k]) : R(0.); };
+  auto amin = [&](int k) { return layer ? cv<R>(M.h_min[k]) : (nuk && k >= 1 ? cv<R>(1.e-3 * M.kinvisc) : R(0.)); };
   auto dsi = [&](int kk) { return cv<R>(M.dsgth_inv[kk]); };
   auto wa = [&](int k) { return CT(WA, k); };
   if (c.valid)
     for (int k = (layer ? kf : kf - 1) + c.warp; k <= nk; k += CT_WARPS) CT(WA, k) = cv<R>(buff[c.base + k * n2]);
-  if (layer) {
-    if (c.valid)
+  if (layer || nuk) {
+    if (c.valid && layer)
       for (int k = kf - 1 + c.warp; k <= nk; k += CT_WARPS) {
         const R w = cv<R>(M.w3[c.base + k * n2]);
         CT(WM, k) = rmin(R(0.), w);
         CT(WP, k) = rmax(R(0.), w);
       }
+    if (c.valid && nuk) {
+      for (int k = kf + c.warp; k <= nk; k += CT_WARPS) {
+        const R w = (k == 1 || k == nk) ? R(0.) : R(.5) * (cv<R>(M.w3[c.base + k * n2]) + cv<R>(M.w3[c.base + (k - 1) * n2]));
+        CT(WM, k) = rmin(R(0.), w);
+        CT(WP, k) = rmax(R(0.), w);
+      }
+      // entry 0 is never loaded for NU_TURB; the corrector reads it only against d2(1) = 0
+      if (c.warp == 0) { CT(WM, 0) = R(0.); CT(WP, 0) = R(0.); }
+    }
     __syncthreads();
     if (c.valid)
       for (int k = kf - 1 + c.warp; k <= nk; k += CT_WARPS)
@@ -242,10 +253,16 @@ __global__ void __launch_bounds__(CT_THREADS) k_hsu_vertical(DevModel M, double 
         CT(FF, k) = f;
       }
     __syncthreads();
-    if (c.valid)
+    if (c.valid && layer)
       for (int k = kf + c.warp; k <= nk; k += CT_WARPS) {
         const long long x = c.base + k * n2;
         buff[x] = buff[x] + to_d((CT(FF, k) - CT(FF, k - 1)) * dsi(2 * k) * DT);
+      }
+    if (c.valid && nuk)   // the interface update; w_ff[nk+1] is the 0 the THETA call left there
+      for (int k = kf + c.warp; k <= nk; k += CT_WARPS) {
+        const long long x = c.base + k * n2;
+        const R ffk1 = k == nk ? R(0.) : CT(FF, k + 1);
+        buff[x] = buff[x] + to_d((ffk1 - CT(FF, k)) * dsi(2 * k + 1) * DT);
       }
   } else {
     if (c.valid)
@@ -324,7 +341,7 @@ __global__ void __launch_bounds__(CT_THREADS) k_akima_vertical(DevModel M, doubl
   const ColTile c = col_tile(M);
   const int nk = M.nk, L = nk + 2;
   const long long n2 = M.n2;
-  const bool layer = kind == 2;
+  const bool layer = kind == 2, nuk = kind == 3;   // NU_TURB: the layer form of the flux (:1687-1706)
   const int kf = kind == 1 ? M.k_sigma - 1 : 1;
   const R DT = cv<R>(M.dt);
   R *WA = sm, *W = WA + 32 * L, *DL = W + 32 * L, *FF = DL + 32 * L;
@@ -338,7 +355,7 @@ __global__ void __launch_bounds__(CT_THREADS) k_akima_vertical(DevModel M, doubl
         CT(W, k) = (k == 1 || k == nk) ? R(0.) : R(.5) * (cv<R>(M.w3[c.base + k * n2]) + cv<R>(M.w3[c.base + (k - 1) * n2]));
   }
   __syncthreads();
-  if (layer) {
+  if (layer || nuk) {
     // deltaa(k) = a(k) - a(k+1) for kf <= k < nk, 0 at kf-1 and nk
     auto deltaa = [&](int k) { return (k < kf || k >= nk) ? R(0.) : wa(k) - wa(k + 1); };
     if (c.valid)
@@ -351,10 +368,16 @@ __global__ void __launch_bounds__(CT_THREADS) k_akima_vertical(DevModel M, doubl
         CT(FF, k) = CT(W, k) * aval;
       }
     __syncthreads();
-    if (c.valid)
+    if (c.valid && layer)
       for (int k = kf + c.warp; k <= nk; k += CT_WARPS) {
         const long long x = c.base + k * n2;
         buff[x] = buff[x] + to_d((CT(FF, k) - CT(FF, k - 1)) * cv<R>(M.dsgth_inv[2 * k]) * DT);
+      }
+    if (c.valid && nuk)   // the interface update; w_ff[nk+1] is the 0 the THETA call left there
+      for (int k = kf + c.warp; k <= nk; k += CT_WARPS) {
+        const long long x = c.base + k * n2;
+        const R ffk1 = k == nk ? R(0.) : CT(FF, k + 1);
+        buff[x] = buff[x] + to_d((ffk1 - CT(FF, k)) * cv<R>(M.dsgth_inv[2 * k + 1]) * DT);
       }
   } else {
     // deltaa(k) = a(k-1) - a(k) for kf <= k <= nk
@@ -949,6 +972,8 @@ __global__ void k_advection_prep(DevModel M, int phase) {
   const int k = (int)q;
   const long long x = M.at(k, 0, 0) + (t - q * w);
   if (phase == 0) M.unity[x] = 1.;
+  else if (phase == 3) M.old[x] = M.nu_turb[x];   // NU_TURB, epic_flux.c:569-600
+  else if (phase == 4) M.nu_turb[x] = dmaxr(1.e-4 * M.kinvisc, M.nu_turb[x] - M.old[x] * (M.unity[x] - 1.));
   else if (k >= M.k_sigma - 1) {
     if (phase == 1) M.old[x] = M.theta[x];
     else M.theta[x] -= M.old[x] * (M.unity[x] - 1.);

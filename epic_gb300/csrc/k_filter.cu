@@ -460,7 +460,8 @@ __global__ void k_varz_filter_rows(DevModel M, double *buff, int sel, int index,
 
 // Zonal pass of hsu_advection (epic_flux.c:1316-1484) for one row: the fluxes come from a
 // zonally filtered copy of the row, the update goes to the unfiltered field.
-// kind: 0 = interface variable (unity, THETA), 1 = HDRY (layer; u averaged to the layer).
+// kind: 0 = interface variable (unity, THETA), 1 = HDRY (layer; u averaged to the layer),
+// 2 = NU_TURB (interface variable with the floor NU_TURB_MIN).
 template <class R>
 __global__ void k_hsu_zonal(DevModel M, double *buff, int kind, int kstart) {
   if (epic_member(M, buff)) return;
@@ -473,7 +474,7 @@ __global__ void k_hsu_zonal(DevModel M, double *buff, int kind, int kstart) {
   R *a = sm, *um = a + W, *up = um + W, *ff = up + W, *ap = ff + W, *d1 = ap + W, *d2 = d1 + W, *aa = d2 + W;
   FilterSmem<R> fs = carve_filter(aa + W, ni);
   const R ep = R(1.e-10), DT = cv<R>(M.dt);
-  const R a_min = kind == 1 ? cv<R>(M.h_min[k]) : R(0.);
+  const R a_min = kind == 1 ? cv<R>(M.h_min[k]) : (kind == 2 ? cv<R>(1.e-3 * M.kinvisc) : R(0.));
   const long long base = M.at(k, j, 0);
   const bool filt = row_is_filtered(M, j, 0);
   if (filt) load_twiddles(M, fs);

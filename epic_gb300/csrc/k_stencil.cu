@@ -57,20 +57,6 @@ __global__ void k_zero_tend(DevModel M) {
 // epic_funcs_diag.c:2694-2847) and the PV averages of include/epic_pv_schemes.h:48-61.
 // ---------------------------------------------------------------------------------------------
 
-template <class R>
-__device__ __forceinline__ R kin_at(const DevModel &M, const double *Uk, const double *Vk, int j, int i) {
-  const int jj = 2 * j;
-  const R mn1 = cv<R>(M.mn[jj + 1]), mni0 = cv<R>(M.mn_inv[jj]), mni2 = cv<R>(M.mn_inv[jj + 2]);
-  R u2 = cv<R>(Uk[M.at2(j, i)]), u4 = cv<R>(Uk[M.at2(j, i + 1)]), v2 = cv<R>(Vk[M.at2(j, i)]), v4 = cv<R>(Vk[M.at2(j + 1, i)]);
-  const R kin_c = (u2 * u2 + u4 * u4 + mn1 * (v2 * v2 * mni0 + v4 * v4 * mni2)) * R(.25);
-  if (j == 0 || j == M.nj) return kin_c;
-  u2 = R(.5) * (cv<R>(Uk[M.at2(j + 1, i)]) + cv<R>(Uk[M.at2(j - 1, i)]));
-  u4 = R(.5) * (cv<R>(Uk[M.at2(j + 1, i + 1)]) + cv<R>(Uk[M.at2(j - 1, i + 1)]));
-  v2 = R(.5) * (cv<R>(Vk[M.at2(j, i + 1)]) + cv<R>(Vk[M.at2(j, i - 1)]));
-  v4 = R(.5) * (cv<R>(Vk[M.at2(j + 1, i + 1)]) + cv<R>(Vk[M.at2(j + 1, i - 1)]));
-  const R kin_s = (u2 * u2 + u4 * u4 + mn1 * (v2 * v2 * mni0 + v4 * v4 * mni2)) * R(.25);
-  return (R(5.) / R(6.)) * kin_c + (R(1.) / R(6.)) * kin_s;
-}
 // UH(j,i) for j = 0..nj (0 above), periodic in i
 template <class R>
 __device__ __forceinline__ R uh_at(const DevModel &M, const double *Uk, const double *Hk, int j, int i) {
@@ -472,7 +458,7 @@ __global__ void k_pgrad_lat(DevModel M) {
 
 // ---------------------------------------------------------------------------------------------
 // Meridional pass of hsu_advection, epic_flux.c:1060-1310.  kind: 0/1 interface (unity,
-// THETA), 2 = HDRY (v averaged to the layer).  Four launches over all planes k0..nk.
+// THETA), 2 = HDRY (v averaged to the layer), 3 = NU_TURB (interface, floor NU_TURB_MIN).  Four launches over all planes k0..nk.
 // ---------------------------------------------------------------------------------------------
 
 template <class R>
@@ -521,7 +507,7 @@ __global__ void k_hsu_merid_corr(DevModel M, const double *A, int kind, int k0) 
   R ffv = R(0.);
   if (j >= 1 && j <= nj) {
     const R ep = R(1.e-10), DT = cv<R>(M.dt);
-    const R a_min = kind == 2 ? cv<R>(M.h_min[k]) : R(0.);
+    const R a_min = kind == 2 ? cv<R>(M.h_min[k]) : (kind == 3 ? cv<R>(1.e-3 * M.kinvisc) : R(0.));
     const double *V = M.v + plane_offset(M, PL_UV);
     const double *AP = M.work2;
     auto a = [&](int jj) { return cv<R>(A[M.at(k, jj, i)]); };
@@ -582,7 +568,7 @@ __global__ void k_hsu_meridional(DevModel M, double *A, int kind, int k0) {
   const int nj = M.nj;
   const double *V = M.v + plane_offset(M, PL_UV);
   const R ep = R(1.e-10), DT = cv<R>(M.dt);
-  const R a_min = kind == 2 ? cv<R>(M.h_min[k]) : R(0.);
+  const R a_min = kind == 2 ? cv<R>(M.h_min[k]) : (kind == 3 ? cv<R>(1.e-3 * M.kinvisc) : R(0.));
   auto ld = [&](int jj) { return A[M.at(k, jj, i)]; };
   auto ff_of = [&](int jj, R vm, R vp, R am1, R a0) { return (jj >= 1 && jj <= nj) ? vp * am1 + vm * a0 : R(0.); };
   auto ap_of = [&](int jj, double ad, R ff0, R ff1) { return cv<R>(ad + to_d((ff0 - ff1) * cv<R>(M.mn[2 * jj + 1]) * DT)); };

@@ -106,4 +106,16 @@ int launch_store_diag(const DevModel &M, cudaStream_t s);
 int launch_itime_advance(const DevModel &M, cudaStream_t s);
 int launch_set_itime(const DevModel &M, long long itime, cudaStream_t s);
 
+// k_turb.cu -- the Spalart-Allmaras DES turbulence closure (FP64 form): source_sink_turb,
+// scalar_horizontal_diffusion (with its set_p2etc), scalar_vertical_diffusion (with its
+// set_p2etc), uv_horizontal_diffusion, uv_vertical_diffusion, set_diffusion_coef, and
+// restore_mass(NU_TURB_INDEX); scratch work0..3 and the model's turbulence arrays
+int launch_source_sink_turb(const DevModel &M, cudaStream_t s);
+int launch_scalar_hdiff(const DevModel &M, cudaStream_t s);
+int launch_scalar_vdiff(const DevModel &M, cudaStream_t s);
+int launch_uv_hdiff(const DevModel &M, cudaStream_t s);
+int launch_uv_vdiff(const DevModel &M, cudaStream_t s);
+int launch_set_diffusion_coef(const DevModel &M, cudaStream_t s);
+int launch_restore_nu(const DevModel &M, cudaStream_t s);
+
 }  // namespace epic

@@ -3,8 +3,8 @@ exactly the bits it gets when stepped alone, in both precision forms."""
 import numpy as np
 import pytest
 
-from epic_gb300 import (EPIC_ADV_AKIMA, EPIC_IO_ALL, EPIC_IO_STATE, EPIC_PREC_FP64, EPIC_PREC_MIXED, EPIC_PREC_MIXED_FAST, EPIC_SYNC_DIAGS_ONLY, EPIC_UV_AB3, EPIC_UV_LEAPFROG, Batch,
-                        EpicError, HSConfig, Model, hs_setup)
+from epic_gb300 import (EPIC_ADV_AKIMA, EPIC_IO_ALL, EPIC_IO_STATE, EPIC_PREC_FP64, EPIC_PREC_MIXED, EPIC_PREC_MIXED_FAST, EPIC_PROFILE_N2,
+                        EPIC_SYNC_DIAGS_ONLY, EPIC_UV_AB3, EPIC_UV_LEAPFROG, Batch, EpicError, HSConfig, Model, hs_setup)
 
 pytestmark = pytest.mark.gpu
 
@@ -99,7 +99,46 @@ def test_batch_rejects_incompatible_members(gpu):
         Batch([a, h])
     with pytest.raises(EpicError, match="x_h2"):   # hydrogen tables are in the FP64 form only
         Model(gh, EPIC_PREC_MIXED)
+    gt, ft = hs_setup(HSConfig(ni=32, nj=16, nk=10, dt=300, seed=7, turbulence=True))
+    t1 = Model(gt, EPIC_PREC_FP64)
+    t1.upload(ft)
+    with pytest.raises(EpicError, match="turbulence"):
+        Batch([a, t1])
+    with pytest.raises(EpicError, match="turbulence"):   # the closure is in the FP64 form only
+        Model(gt, EPIC_PREC_MIXED)
+    gt2, ft2 = hs_setup(HSConfig(ni=64, nj=32, nk=10, dt=300, seed=8, turbulence=True))
+    t2 = Model(gt2, EPIC_PREC_FP64)
+    t2.upload(ft2)
+    with pytest.raises(EpicError, match="one grid size"):
+        Batch([t1, t2])
     Batch([a, f]).close()   # sizes alone may differ
+
+
+def test_turbulence_batch_equals_members_alone(gpu):
+    """Three members with the turbulence closure (zonal jets, different seeds and time steps) in
+    one batch: every member equals the same member stepped alone, bit for bit."""
+    cfgs = [HSConfig(ni=32, nj=16, nk=10, dt=dt, seed=60 + q, state="jet", profile=EPIC_PROFILE_N2, turbulence=True)
+            for q, dt in enumerate((300, 300, 150))]
+    alone, models, fields = [], [], []
+    for cfg in cfgs:
+        ga, f = hs_setup(cfg)
+        m = Model(ga, EPIC_PREC_FP64)
+        m.upload(f)
+        m.timestep(EPIC_SYNC_DIAGS_ONLY)
+        m.run(5)
+        m.sync()
+        alone.append(m.download())
+        b = Model(ga, EPIC_PREC_FP64)
+        b.upload(f)
+        models.append(b)
+        fields.append(f)
+    batch = Batch(models)
+    batch.timestep(EPIC_SYNC_DIAGS_ONLY)
+    batch.run(5)
+    out = batch.download([f.copy() for f in fields])
+    for q in range(3):
+        for k in alone[q].arrays:
+            assert np.array_equal(out[q].arrays[k], alone[q].arrays[k]), (q, k)
 
 
 # Batches whose members differ in ni, nj and dt: one launch per kernel for all of them, each

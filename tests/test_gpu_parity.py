@@ -24,7 +24,11 @@ STEP_STAGES = [0, 1, 2, 3, 4, 5, 6, 7, 8, 9, 10, 11, 7, 12, 13, 14, 15, 16, 17]
 STAGE_NAMES = {0: "zero_tend", 1: "source_sink", 2: "calc_w", 3: "uv_core", 4: "uv_drag", 5: "scalar_hypervisc",
                6: "advection", 7: "store_pgrad_vars", 8: "gz_filter", 9: "filter_tend_3d", 10: "filter_mass_3d",
                11: "set_p2etc", 12: "uv_pgrad", 13: "div_damp", 14: "uv_update", 15: "uv_hypervisc",
-               16: "store_diag", 17: "calc_heating", 18: "set_p2etc_noupdate"}
+               16: "store_diag", 17: "calc_heating", 18: "set_p2etc_noupdate", 21: "source_sink_turb",
+               22: "scalar_horizontal_diffusion", 23: "scalar_vertical_diffusion", 24: "uv_horizontal_diffusion",
+               25: "uv_vertical_diffusion"}
+# the step with the turbulence closure (diffusion in both directions)
+STEP_STAGES_TURB = [0, 1, 2, 21, 3, 4, 22, 5, 23, 6, 7, 8, 9, 10, 11, 7, 12, 24, 13, 14, 25, 15, 16, 17]
 
 
 def _pair(cfg, cr_libm=False):
@@ -53,10 +57,12 @@ def _differing(a, b):
 def _state(state):
     """HSConfig keywords of a named state: "hs" (the column at rest), "jet" (the balanced jets);
     "-gg" adds the gas-giant lower boundary (GZ_SURFACE from gz_from_u), "-h2" a hydrogen-helium
-    atmosphere (thermo_setup's tables)."""
+    atmosphere (thermo_setup's tables), "-sa" the Spalart-Allmaras DES turbulence closure."""
     extra = {}
+    if state.endswith("-sa"):
+        state, extra = state[:-3], {"turbulence": True}
     if state.endswith("-h2"):
-        state, extra = state[:-3], {"x_h2": 0.864, "x_he": 0.136}
+        state, extra = state[:-3], {**extra, "x_h2": 0.864, "x_he": 0.136}
     base = state[:-3] if state.endswith("-gg") else state
     return {"state": base, "profile": EPIC_PROFILE_N2 if base == "jet" else 0, "gas_giant": state.endswith("-gg"), **extra}
 
@@ -68,7 +74,7 @@ def _stage_by_stage(cfg):
     model = Model(ga)
     model.upload(f)
     failures = []
-    for st in STEP_STAGES + [18]:
+    for st in (STEP_STAGES_TURB if cfg.turbulence else STEP_STAGES) + [18]:
         port.stage(st)
         model.run_stage(st)
         model.sync()
@@ -90,6 +96,30 @@ def test_stage_by_stage(gpu, scheme, adv, state):
     _stage_by_stage(HSConfig(ni=32, nj=16, nk=10, dt=300, uv_scheme=scheme, seed=3, advection_scheme=adv, **_state(state)))
 
 
+@pytest.mark.parametrize("adv,state", [(EPIC_ADV_HSU, "hs-sa"), (EPIC_ADV_AKIMA, "hs-sa"), (EPIC_ADV_HSU, "jet-sa"),
+                                       (EPIC_ADV_HSU, "jet-gg-sa")])
+@pytest.mark.parametrize("scheme", [EPIC_UV_AB3, EPIC_UV_LEAPFROG])
+def test_stage_by_stage_turbulence(gpu, scheme, adv, state):
+    """The turbulence closure's stages (source_sink_turb, the scalar and wind subgrid diffusions)
+    and the ones it changes (NU_TURB's hyperviscosity, advection and 3-D filter, set_diffusion_coef
+    in store_diag), GPU vs the correctly rounded restatement, bit for bit."""
+    _stage_by_stage(HSConfig(ni=32, nj=16, nk=10, dt=300, uv_scheme=scheme, seed=3, advection_scheme=adv, **_state(state)))
+
+
+@pytest.mark.parametrize("direction", [2, 3])
+def test_turbulence_one_direction_steps(gpu, direction):
+    """grid.diffusion_direction 2 (horizontal only) and 3 (vertical only): ten steps bit for bit."""
+    cfg = HSConfig(ni=32, nj=16, nk=10, dt=300, seed=4, turbulence=True, diffusion_direction=direction, **_state("jet"))
+    ga, f, port, model = _pair(cfg, cr_libm=True)
+    port.timestep(EPIC_SYNC_DIAGS_ONLY)
+    port.run(10)
+    model.timestep(EPIC_SYNC_DIAGS_ONLY)
+    model.run(10)
+    model.sync()
+    diff = _differing(model.download(), port.download())
+    assert not diff, diff
+
+
 @pytest.mark.parametrize("scheme", [EPIC_UV_AB3, EPIC_UV_LEAPFROG])
 def test_stage_by_stage_divergence_damping(gpu, scheme):
     """As above with nudiv_nondim = 0.5, so that divergence_damping (epic_subgrid.c:1792-1885,
@@ -98,7 +128,8 @@ def test_stage_by_stage_divergence_damping(gpu, scheme):
 
 
 @pytest.mark.parametrize("adv,state", [(EPIC_ADV_HSU, "hs"), (EPIC_ADV_AKIMA, "hs"), (EPIC_ADV_HSU, "jet"), (EPIC_ADV_HSU, "jet-gg"),
-                                       (EPIC_ADV_HSU, "hs-h2")])
+                                       (EPIC_ADV_HSU, "hs-h2"), (EPIC_ADV_HSU, "jet-sa"), (EPIC_ADV_AKIMA, "jet-sa"),
+                                       (EPIC_ADV_HSU, "jet-gg-sa")])
 @pytest.mark.parametrize("scheme", [EPIC_UV_AB3, EPIC_UV_LEAPFROG])
 def test_steps_bitwise(gpu, scheme, adv, state):
     """Ten graph-replayed steps at 64x32x20 equal the correctly rounded restatement bit for bit."""
@@ -136,7 +167,9 @@ def test_sync_diags(gpu):
                                                           (EPIC_UV_AB3, 1, 1e-11, EPIC_ADV_HSU, "jet-gg"),
                                                           (EPIC_UV_AB3, 100, 1e-8, EPIC_ADV_HSU, "jet-gg"),
                                                           (EPIC_UV_AB3, 1, 1e-11, EPIC_ADV_HSU, "hs-h2"),
-                                                          (EPIC_UV_AB3, 100, 1e-8, EPIC_ADV_HSU, "hs-h2")])
+                                                          (EPIC_UV_AB3, 100, 1e-8, EPIC_ADV_HSU, "hs-h2"),
+                                                          (EPIC_UV_AB3, 1, 1e-11, EPIC_ADV_HSU, "jet-sa"),
+                                                          (EPIC_UV_AB3, 100, 1e-8, EPIC_ADV_HSU, "jet-sa")])
 def test_full_step(gpu, scheme, nsteps, tol, adv, state):
     """The 64x32x10 configuration (Held-Suarez column or zonal jets; "hs-nudiv": the column with
     divergence damping, nudiv_nondim = 0.5; "jet-gg": the jets over the gas-giant lower
