@@ -220,14 +220,17 @@ __device__ void band_back_sub3(int n, double (*A)[3], const double *al, const in
 
 // crank_nicolson (epic_funcs_util.c:3643-3787) with tridiag(WITH_PIVOTING): band_decomp,
 // band_back_sub and one band_improve pass (:2994-3120, :3330-3400).  z, A, mu, rho (may be null)
-// and ans are indexed 0..n+1; A[0] or A[n+1] above .99e20 marks a no-flux end.  Returns false if
-// z does not increase where it is used (the reference exits).
-__device__ bool crank_nicolson(int n, double dt, const double *z, const double *A, const double *mu, const double *rho, double *ans) {
+// and ans are indexed 0..n+1; A[0] or A[n+1] above .99e20 marks a no-flux end.  Returns 0, or the
+// first index j where z does not increase (z[j] <= z[j-1]; the reference exits there).
+// Kept out of line: inlined into the column kernels (nvcc 13.0, sm_103a), the callers' store of
+// the no-flux marker A[0] = 1e20 into their local array was not seen by the solver's read of it
+// (measured: every column then took the flux branch); a call makes the arrays' stores complete.
+__device__ __noinline__ int crank_nicolson(int n, double dt, const double *z, const double *A, const double *mu, const double *rho, double *ans) {
   double a[TN], b[TN], c[TN], r[TN], Ab[TN][3], al[TN];
   int idx[TN];
   const int jstart = A[0] > .99e+20 ? 2 : 1, jend = A[n + 1] > .99e+20 ? n : n + 1;
   for (int j = jstart; j <= jend; j++)
-    if (z[j] <= z[j - 1]) return false;
+    if (z[j] <= z[j - 1]) return j;
   double coeff3 = (A[0] > .99e+20) ? 0. : mu[0] / (z[1] - z[0]), coeff1, factor;
   a[0] = 0.;
   c[n - 1] = 0.;
@@ -273,7 +276,7 @@ __device__ bool crank_nicolson(int n, double dt, const double *z, const double *
   }
   band_back_sub3(n, Ab, al, idx, res);
   for (int i = 0; i < n; i++) ans[i + 1] -= res[i];
-  return true;
+  return 0;
 }
 
 // ---------------------------------------------------------------------------------------------
@@ -500,8 +503,8 @@ __global__ void __launch_bounds__(64) k_theta_vdiff(DevModel M) {
   }
   for (int k = nk; k > ks - 2; k--)
     dee[nk - k + 1] = sf[k] * .5 * (M.dc_theta[M.at(k, j, i)] + M.dc_theta[M.at(k - 1, j, i)]);
-  if (!crank_nicolson(nk - ks + 2, M.dt, z, A, dee, nullptr, ans)) {
-    flag_error(M.ctl, ERR_TURB, 0, j, i, 0.);
+  if (const int bad = crank_nicolson(nk - ks + 2, M.dt, z, A, dee, nullptr, ans)) {   // THETA: z[bad] - z[bad-1] recorded
+    flag_error(M.ctl, ERR_TURB, nk - bad + 1, j, i, z[bad] - z[bad - 1]);
     return;
   }
   for (int k = nk; k >= ks - 1; k--) write_with_pads(M.theta, M, M.at(k, j, 0), i, ans[nk - k + 1]);
@@ -528,8 +531,8 @@ __global__ void __launch_bounds__(64) k_nu_vdiff(DevModel M) {
   z[0] = (gz(nk) - (gz(nk - 1) - gz(nk))) / gi;
   dee[0] = dee[1];
   A[0] = A[1] - tw * (z[1] - z[0]) / dee[0];
-  if (!crank_nicolson(nk + 1, M.dt, z, A, dee, nullptr, ans)) {
-    flag_error(M.ctl, ERR_TURB, 0, j, i, 1.);
+  if (const int bad = crank_nicolson(nk + 1, M.dt, z, A, dee, nullptr, ans)) {
+    flag_error(M.ctl, ERR_TURB, nk - bad + 1, j, i, z[bad] - z[bad - 1]);
     return;
   }
   for (int k = nk; k >= 0; k--) write_with_pads(M.nu_turb, M, M.at(k, j, 0), i, ans[nk - k + 1]);
@@ -578,8 +581,8 @@ __global__ void __launch_bounds__(64) k_wind_vdiff(DevModel M, int comp, const d
   z[0] = gzm(nk) / gi;
   mu[0] = mu[1];
   A[0] = A[1] - tw[M.at2(j, i)] * (z[1] - z[0]) / mu[0];
-  if (!crank_nicolson(nk - 1, M.dt, z, A, mu, rho, ans)) {
-    flag_error(M.ctl, ERR_TURB, 0, j, i, 2. + comp);
+  if (const int bad = crank_nicolson(nk - 1, M.dt, z, A, mu, rho, ans)) {
+    flag_error(M.ctl, ERR_TURB, nk - bad, j, i, z[bad] - z[bad - 1]);
     return;
   }
   for (int k = nk - 1; k >= 1; k--) write_with_pads(W, M, M.at(k, j, 0), i, ans[nk - k]);
