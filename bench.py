@@ -1,7 +1,8 @@
 """Throughput of the GB300 EPIC timestep() on synthetic Held-Suarez states.
 
     python bench.py [--gpus N] [--steps K] [--warmup W] [--impl gb300|reference]
-                    [--workload ens64|hs64|hs128|hs256|hs512] [--precision mixed|fast|fp64]
+                    [--workload ens64|hs64|hs128|hs256|hs512|jet256|jet256gg|hs128sa|jet128sa]
+                    [--precision mixed|fast|fp64]
                     [--no-cpu-baseline] [--no-extras]
 
 A step is one timestep(STEP_PROGS_AND_SYNC_DIAGS) of every grid in the workload.  metric =
@@ -46,6 +47,8 @@ WORKLOADS = {
     "hs512": (512, 256, 40, 60),
     "jet256": (256, 128, 32, 60),  # balanced zonal jets on the constant-N^2 sounding
     "jet256gg": (256, 128, 32, 60),  # the same over the gas-giant lower boundary (gz_from_u)
+    "hs128sa": (128, 64, 20, 300),   # the Held-Suarez column with the Spalart-Allmaras DES closure (FP64)
+    "jet128sa": (128, 64, 20, 300),  # the balanced jets with the Spalart-Allmaras DES closure (FP64)
     "ens64": (128, 64, 20, 300),   # per member; 64 members
 }
 ENSEMBLE = {"ens64": 64}
@@ -68,10 +71,11 @@ ADVECTION_NAME = {"hsu": "Hsu-Konor-Arakawa advection", "akima": "Akima advectio
 def _workload_cfg(name, seed=0, advection="hsu"):
     from epic_gb300 import EPIC_PROFILE_N2, HSConfig
     ni, nj, nk, dt = WORKLOADS[name]
+    turb = name.endswith("sa")
     if name.startswith("jet"):
         return HSConfig(ni=ni, nj=nj, nk=nk, dt=dt, seed=seed, advection_scheme=ADVECTION[advection], profile=EPIC_PROFILE_N2,
-                        state="jet", gas_giant=name.endswith("gg"))
-    return HSConfig(ni=ni, nj=nj, nk=nk, dt=dt, seed=seed, advection_scheme=ADVECTION[advection])
+                        state="jet", gas_giant=name.endswith("gg"), turbulence=turb)
+    return HSConfig(ni=ni, nj=nj, nk=nk, dt=dt, seed=seed, advection_scheme=ADVECTION[advection], turbulence=turb)
 
 
 def algorithmic_bytes_per_step(cfg, word=8):
@@ -240,6 +244,7 @@ def workload_config(args, cfg, nmem, ws):
     else:
         what = (("Zonal jets on the Held-Suarez planet " if cfg.state == "jet" else "Held-Suarez ") +
                 ("over the gas-giant lower boundary (GZ_SURFACE from gz_from_u) " if cfg.gas_giant else "") +
+                ("with the Spalart-Allmaras DES turbulence closure " if cfg.turbulence else "") +
                 f"{cfg.ni}x{cfg.nj}x{cfg.nk}, dt={cfg.dt}s, AB3, {ADVECTION_NAME[args.advection]}, nu4=0.5 max")
     return {"workload": what, "ni": cfg.ni, "nj": cfg.nj, "nk": cfg.nk, "dt": cfg.dt, "members": nmem,
             "advection": args.advection, "parallelism": f"replicas{ws}", "state": state,

@@ -289,7 +289,7 @@ __host__ __device__ __forceinline__ double cr_exp(double x, const MathTable &T) 
 // separate cr_pow / cr_log call.
 __host__ __device__ __forceinline__ double cr_pow(double x, double y, const MathTable &T);
 __host__ __device__ __forceinline__ double cr_log_pow(double x, double y, const MathTable &T, double &lg) {
-  if (!(x > 0.) || !(x < INFINITY) || x < 2.2250738585072014e-308 || x == 1. || y == 0. || !(fabs(y) < 1e6)) {
+  if (!(x > 0.) || !(x < INFINITY) || x < 2.2250738585072014e-308 || x == 1. || y == 0. || y == 2. || !(fabs(y) < 1e6)) {
     lg = cr_log(x, T);
     return cr_pow(x, y, T);
   }
@@ -309,6 +309,7 @@ __host__ __device__ __forceinline__ double cr_log_pow(double x, double y, const 
 
 __host__ __device__ __forceinline__ double cr_pow(double x, double y, const MathTable &T) {
   if (y == 0. || x == 1.) return 1.;
+  if (y == 2.) return x * x;   // the square rounded once: the correctly rounded x^2 for every x
   if (!(x > 0.) || !(x < INFINITY) || x < 2.2250738585072014e-308 || !(fabs(y) < 1e6)) return pow(x, y);
   const dd l = fast_log(x, T);
   dd yl = two_prod(y, l.hi);

@@ -298,8 +298,11 @@ __device__ double brunt2_iface(const DevModel &M, int k, int j, int i) {
   return g * g * (Drho_Dp - drho_dp_T + temperature / (cp * density * density) * drho_dT_p * drho_dT_p);
 }
 
-// The NU_TURB-free part at every point k = 1..nk-1, j = 0..nj, i = 1..ni: the strain magnitude S
-// (work0), d~ = min(D_WALL, C_DES delta_SA) (work1), 1/dz (work2) and N^2 (work3).
+// Everything of a point's update but the three gradient terms, at every point k = 1..nk-1,
+// j = 0..nj, i = 1..ni: the terms that read only the point's own NU_TURB (which the sweep has not
+// changed when it reaches the point) and the NU_TURB-free strain, wall distance and buoyancy.
+// work0 = the production cb1 S~ NU, work1 = the destruction cw1 fw (NU/d~)^2, work3 = the buoyancy
+// term (0 where N^2 >= 0, which subtracts nothing), work2 = 1/dz.
 __global__ void k_sa_prep(DevModel M) {
   if (epic_member(M)) return;
   const unsigned t = blockIdx.x * blockDim.x + threadIdx.x;
@@ -307,6 +310,9 @@ __global__ void k_sa_prep(DevModel M) {
   if (t >= (unsigned)(M.nk - 1) * nr * ni) return;
   const unsigned r = t / ni, q = r / nr;
   const int i = 1 + (int)(t - r * ni), j = (int)(r - q * nr), k = 1 + (int)q;
+  const double cw2 = 0.3, cw3_6 = 64., cb1 = 0.1355, cb2 = 0.622, sigma = 2. / 3., kappa = 0.41;
+  const double kappa_2 = kappa * kappa, cw1 = (cb1 / kappa_2) + ((1. + cb2) / sigma), nu_turb_limiter = 3000.;
+  const MathTable &T = *M.lt;
   const long long off = plane_offset(M, PL_UV_DIS);
   const double *U = M.u + off, *V = M.v + off;
   auto u = [&](int kk, int jj, int ii) { return U[M.at(kk, jj, ii)]; };
@@ -350,30 +356,9 @@ __global__ void k_sa_prep(DevModel M) {
   w_var3 = 0.5 * (w3(k, j, i) + w3(k, j + 1, i));
   w_var1 = 0.5 * (w3(k, j, i) + w3(k, j - 1, i));
   const double s23 = .5 * ((v_var1 - v_var3) * dz_inv + h_rho * (w_var3 - w_var1) * n_2jp1);
-  M.work0[x] = sqrt(2. * (s11 * s11 + s22 * s22 + s33 * s33 + 2. * (s12 * s12 + s13 * s13 + s23 * s23)));
-  M.work1[x] = d_tilda;
-  M.work2[x] = dz_inv;
-  M.work3[x] = brunt2_iface(M, k, j, i);
-}
-
-// One wavefront k + j + i = d of the in-place NU_TURB update
-__global__ void k_sa_wave(DevModel M, int d) {
-  if (epic_member(M)) return;
-  const int nr = M.nj + 1;
-  const int t = (int)(blockIdx.x * blockDim.x + threadIdx.x);
-  if (t >= (M.nk - 1) * nr) return;
-  const int k = 1 + t / nr, j = t - (k - 1) * nr, i = d - k - j;
-  if (i < 1 || i > M.ni) return;
-  const double cw2 = 0.3, cw3_6 = 64., cb1 = 0.1355, cb2 = 0.622, sigma = 2. / 3., kappa = 0.41;
-  const double kappa_2 = kappa * kappa, cw1 = (cb1 / kappa_2) + ((1. + cb2) / sigma), nu_turb_limiter = 3000.;
-  const MathTable &T = *M.lt;
-  double *NU = M.nu_turb;
-  auto nut = [&](int kk, int jj, int ii) { return NU[M.at(kk, jj, ii)]; };
-  const long long x = M.at(k, j, i);
-  const double S = M.work0[x], d_tilda = M.work1[x], dz_inv = M.work2[x], brunt2 = M.work3[x];
-  const int jj = 2 * j;
-  const double m_2jp1 = M.m[jj + 1], n_2jp2 = M.n[jj + 2], n_2j = M.n[jj];
-  const double nu = NU[x];
+  const double S = sqrt(2. * (s11 * s11 + s22 * s22 + s33 * s33 + 2. * (s12 * s12 + s13 * s13 + s23 * s23)));
+  // the point's own NU_TURB terms
+  const double nu = M.nu_turb[x];
   const double chi = nu / M.kinvisc;
   const double chi3 = cr_pow(chi, 3., T);
   const double fv1 = chi3 / (chi3 + SA_CV1_3);
@@ -381,10 +366,6 @@ __global__ void k_sa_wave(DevModel M, int d) {
   const double tmp1 = kappa_2 * d_tilda * d_tilda;
   const double S_tilda = S + (nu * fv2) / tmp1;
   const double tmp2 = S_tilda * tmp1;
-  double dnudt = cb1 * S_tilda * nu;
-  dnudt += (cb2 / sigma) * cr_pow(((nut(k, j, i + 1) - nut(k, j, i - 1)) * m_2jp1 * .5), 2., T);
-  dnudt += (cb2 / sigma) * cr_pow(.5 * ((nut(k, j + 1, i) - nu) * n_2jp2 + (nu - nut(k, j - 1, i)) * n_2j), 2., T);
-  dnudt += (cb2 / sigma) * cr_pow(((nut(k - 1, j, i) - nut(k + 1, j, i)) * dz_inv), 2., T);
   double fw = 1.;
   if (tmp2 != 0.) {
     const double r_sa = nu / tmp2;
@@ -394,9 +375,40 @@ __global__ void k_sa_wave(DevModel M, int d) {
       fw = g_sa * cr_pow(((1. + cw3_6) / (cr_pow(g_sa, 6., T) + cw3_6)), (1. / 6.), T);
     }
   }
-  dnudt -= cw1 * fw * cr_pow((nu / d_tilda), 2., T);
+  const double brunt2 = brunt2_iface(M, k, j, i);
   const double brunt = sqrt(fabs(brunt2));
-  if (brunt2 < 0.) dnudt -= nu * cr_exp(-nu / nu_turb_limiter, T) * brunt2 / brunt;
+  M.work0[x] = cb1 * S_tilda * nu;
+  M.work1[x] = cw1 * fw * cr_pow((nu / d_tilda), 2., T);
+  M.work2[x] = dz_inv;
+  M.work3[x] = brunt2 < 0. ? nu * cr_exp(-nu / nu_turb_limiter, T) * brunt2 / brunt : 0.;
+}
+
+// One wavefront k + j + i = d of the in-place NU_TURB update: the three gradient terms from the
+// neighbours (new at k-1, j-1, i-1; old at k+1, j+1, i+1), summed in the reference's order between
+// the point's own terms
+__global__ void k_sa_wave(DevModel M, int d) {
+  if (epic_member(M)) return;
+  const int nr = M.nj + 1;
+  const int t = (int)(blockIdx.x * blockDim.x + threadIdx.x);
+  if (t >= (M.nk - 1) * nr) return;
+  const int k = 1 + t / nr, j = t - (k - 1) * nr, i = d - k - j;
+  if (i < 1 || i > M.ni) return;
+  const double cb2 = 0.622, sigma = 2. / 3.;
+  double *NU = M.nu_turb;
+  auto nut = [&](int kk, int jj, int ii) { return NU[M.at(kk, jj, ii)]; };
+  const long long x = M.at(k, j, i);
+  const int jj = 2 * j;
+  const double m_2jp1 = M.m[jj + 1], n_2jp2 = M.n[jj + 2], n_2j = M.n[jj];
+  const double nu = NU[x];
+  const double g1 = (nut(k, j, i + 1) - nut(k, j, i - 1)) * m_2jp1 * .5;
+  const double g2 = .5 * ((nut(k, j + 1, i) - nu) * n_2jp2 + (nu - nut(k, j - 1, i)) * n_2j);
+  const double g3 = (nut(k - 1, j, i) - nut(k + 1, j, i)) * M.work2[x];
+  double dnudt = M.work0[x];
+  dnudt += (cb2 / sigma) * (g1 * g1);   // pow(g, 2.), the correctly rounded square
+  dnudt += (cb2 / sigma) * (g2 * g2);
+  dnudt += (cb2 / sigma) * (g3 * g3);
+  dnudt -= M.work1[x];
+  dnudt -= M.work3[x];
   NU[x] = dmaxr(1.e-4 * M.kinvisc, nu + M.dt * dnudt);
 }
 
