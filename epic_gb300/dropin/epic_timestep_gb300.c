@@ -55,7 +55,15 @@ static void grid_from_globals(planetspec *planet) {
   g.hybrid_alpha = grid.hybrid_alpha;  g.sigma_sigma = grid.sigma_sigma;
   for (i = 0; i <= MAX_NU_ORDER && i < 9; i++) g.nu[i] = grid.nu[i];
   g.re = planet->re;  g.rp = planet->rp;  g.cp = planet->cp;  g.rgas = planet->rgas;
-  g.kappa = planet->kappa;  g.cpr = planet->cpr;  g.kinvisc = planet->kinvisc;
+  g.kappa = planet->kappa;  g.cpr = planet->cpr;  g.kinvisc = planet->kinvisc;  g.dynvisc = planet->dynvisc;
+  /* the gas-giant lower boundary (store_pgrad_vars' gz_from_u, epic_funcs_diag.c:3779-3811) and the
+   * hydrogen thermodynamics (thermo_setup's tables when planet->x_h2 > 0; cpr is thermo_setup's) */
+  g.gas_giant = strcmp(planet->type, "gas-giant") == 0;
+  g.x_h2 = planet->x_h2;  g.x_he = planet->x_he;  g.x_3 = planet->x_3;
+  /* the turbulence closure (epic_subgrid.c), as the reference's initial program chose it */
+  g.turbulence = strcmp(grid.turbulence_scheme, "Spalart-Allmaras DES") == 0 ? EPIC_TURB_SA_DES : EPIC_TURB_OFF;
+  g.diffusion_direction = grid.diffusion_direction;
+  g.stability_factor = strcmp(grid.stability_factor, "Collins et al. (2004)") == 0;
   g.lat0 = LAT0;
   g.hs_kf = 1. / (24. * 60. * 60.);   /* HELD_SUAREZ_PBL_NU0, epic_timestep.c:1292 */
   g.lon = grid.lon;  g.lat = grid.lat;  g.rln = grid.rln;  g.rlt = grid.rlt;  g.f = grid.f;
@@ -73,6 +81,10 @@ static void fields_from_var(void) {
   f.gz3 = var.gz3.value;  f.mont3 = var.mont3.value;  f.heat3 = var.heat3.value;  f.pv3 = var.pv3.value;
   f.ri2 = var.ri2.value;  f.div_uv3 = var.div_uv3.value;  f.w3 = var.w3.value;  f.dzdt3 = var.dzdt3.value;
   f.u_spinup = var.u_spinup.value;  f.gz_surface = var.gz_surface.value;
+  if (var.nu_turb.on) {   /* NU_TURB and the diffusivities store_diag leaves for the next step */
+    f.nu_turb = var.nu_turb.value;  f.diffusion_coef_uv = var.diffusion_coef_uv.value;
+    f.diffusion_coef_theta = var.diffusion_coef_theta.value;  f.diffusion_coef_mass = var.diffusion_coef_mass.value;
+  }
   f.it_zero = IT_ZERO;  f.it_minus1 = IT_MINUS1;  f.it_minus2 = IT_MINUS2;
   f.itime = (int64_t)grid.itime;  f.model_time = (int64_t)var.model_time;
 }

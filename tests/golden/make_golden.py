@@ -31,6 +31,12 @@ CASES = {
     # the jets over the gas-giant lower boundary (planet->type "gas-giant": GZ_SURFACE from gz_from_u)
     "jetgg32x16x10_ab3": (HSConfig(ni=32, nj=16, nk=10, dt=300, uv_scheme=EPIC_UV_AB3, seed=16, profile=EPIC_PROFILE_N2, state="jet",
                                    gas_giant=True), [("sync", 0), ("step", 1), ("step", 4)]),
+    # the jets with the Spalart-Allmaras DES turbulence closure (grid.turbulence_scheme on)
+    "jetsa32x16x10_ab3": (HSConfig(ni=32, nj=16, nk=10, dt=300, uv_scheme=EPIC_UV_AB3, seed=17, profile=EPIC_PROFILE_N2, state="jet",
+                                   turbulence=True), [("sync", 0), ("step", 1), ("step", 4)]),
+    # the column in a hydrogen-helium atmosphere (thermo_setup's tables, x_h2 = 0.864, x_he = 0.136)
+    "hsh2_32x16x10_ab3": (HSConfig(ni=32, nj=16, nk=10, dt=300, uv_scheme=EPIC_UV_AB3, seed=18, x_h2=0.864, x_he=0.136),
+                          [("sync", 0), ("step", 1), ("step", 4)]),
 }
 
 
@@ -43,7 +49,7 @@ def make(name, cfg, schedule):
     for k, v in ga.scalars().items():
         out["scalar_" + k] = np.array(v)
     d = fields_to_dict(f)
-    for k in ("u", "v", "dudt", "dvdt", "hdry", "theta", "p3", "gz_surface", "u_spinup"):
+    for k in ("u", "v", "dudt", "dvdt", "hdry", "theta", "p3", "gz_surface", "u_spinup") + (("nu_turb",) if cfg.turbulence else ()):
         out["in_" + k] = d[k]
     for n in ("it_zero", "it_minus1", "it_minus2", "itime", "model_time"):
         out["in_" + n] = np.array(d[n])
@@ -51,7 +57,7 @@ def make(name, cfg, schedule):
     for (what, n), s in zip(schedule, snaps):
         steps_done += n
         tag = "sync" if what == "sync" else f"step{steps_done}"
-        for k in SAVED:
+        for k in SAVED + (("nu_turb", "diffusion_coef_theta", "diffusion_coef_uv") if cfg.turbulence else ()):
             out[f"{tag}_{k}"] = s[k]
         for n2 in ("it_zero", "it_minus1", "it_minus2", "itime", "model_time"):
             out[f"{tag}_{n2}"] = np.array(s[n2])

@@ -39,8 +39,9 @@ def grid_from_fixture(z) -> GridArrays:
 
 
 def inputs_from_fixture(z, ga) -> Fields:
-    f = Fields(ga.layout.ni, ga.layout.nj, ga.layout.nk, int(z["scalar_uv_scheme"]))
-    for k in ("u", "v", "dudt", "dvdt", "hdry", "theta", "p3", "gz_surface", "u_spinup"):
+    turb = "in_nu_turb" in z.files   # fixtures of the turbulence closure
+    f = Fields(ga.layout.ni, ga.layout.nj, ga.layout.nk, int(z["scalar_uv_scheme"]), turbulence=turb)
+    for k in ("u", "v", "dudt", "dvdt", "hdry", "theta", "p3", "gz_surface", "u_spinup") + (("nu_turb",) if turb else ()):
         f.arrays[k][...] = z["in_" + k]
     for n in ("it_zero", "it_minus1", "it_minus2", "itime", "model_time"):
         setattr(f.struct, n, int(z["in_" + n]))
@@ -56,6 +57,7 @@ def snapshots(z):
 def compare_snapshot(f: Fields, z, tag, tol):
     bad = {}
     extra = ("gz_surface",) if f"{tag}_gz_surface" in z.files else ()   # fixtures of the gas-giant boundary
+    extra += tuple(k for k in ("nu_turb", "diffusion_coef_theta", "diffusion_coef_uv") if f"{tag}_{k}" in z.files)
     for k in ("u", "v", "hdry", "theta", "p3", "gz3", "pv3", "w3", "heat3", "div_uv3") + extra:
         want = z[f"{tag}_{k}"]
         got = f.arrays[k]
