@@ -65,6 +65,7 @@ def load_library(path: str | None = None) -> C.CDLL:
     lib.epic_model_filter_mass_noalloc.argtypes = [C.c_void_p]
     lib.epic_model_snapshot_begin.argtypes = [C.c_void_p, C.POINTER(EpicFields)]
     lib.epic_model_snapshot_wait.argtypes = [C.c_void_p]
+    lib.epic_model_cfl_dt.argtypes = [C.c_void_p, C.POINTER(C.c_int32), C.POINTER(C.c_double)]
     lib.epic_batch_create.argtypes = [C.POINTER(C.c_void_p), C.c_int32, C.POINTER(C.c_void_p)]
     lib.epic_batch_destroy.argtypes = [C.c_void_p]
     lib.epic_batch_destroy.restype = None
@@ -184,6 +185,13 @@ class Model:
 
     def run_stage(self, stage: int) -> None:
         _check(self.lib.epic_model_run_stage(self._h, stage), "epic_model_run_stage")
+
+    def cfl_dt(self) -> tuple[int, tuple[float, float, float]]:
+        """cfl_dt of the device state: (the int time step var_write stores, (cflx, cfly, cflz))."""
+        dt = C.c_int32()
+        c = (C.c_double * 3)()
+        _check(self.lib.epic_model_cfl_dt(self._h, C.byref(dt), c), "epic_model_cfl_dt")
+        return int(dt.value), tuple(c)
 
     def sync(self) -> None:
         _check(self.lib.epic_model_sync(self._h), "epic_model_sync")

@@ -851,6 +851,28 @@ extern "C" int epic_model_run(epic_model *m, int32_t nsteps) {
   return check_launch("epic_model_run");
 }
 
+extern "C" int epic_model_cfl_dt(epic_model *m, int32_t *dt_out, double *cfl) {
+  if (!m || !dt_out) return set_error(EPIC_ERR_ARG, "epic_model_cfl_dt: NULL argument");
+  if (!m->uploaded) return set_error(EPIC_ERR_STATE, "cfl_dt before upload");
+  unsigned long long *lim = nullptr, host[3];
+  EPIC_CUDA_CHECK(cudaMallocAsync((void **)&lim, 3 * sizeof(unsigned long long), m->stream));
+  double big[3] = {DBL_MAX, DBL_MAX, DBL_MAX};
+  EPIC_CUDA_CHECK(cudaMemcpyAsync(lim, big, sizeof(big), cudaMemcpyHostToDevice, m->stream));
+  epic::launch_cfl_dt(m->d, lim, m->stream);
+  int rc = check_launch("cfl_dt");
+  EPIC_CUDA_CHECK(cudaMemcpyAsync(host, lim, sizeof(host), cudaMemcpyDeviceToHost, m->stream));
+  EPIC_CUDA_CHECK(cudaFreeAsync(lim, m->stream));
+  EPIC_CUDA_CHECK(cudaStreamSynchronize(m->stream));
+  if (rc) return rc;
+  double c[3];
+  memcpy(c, host, sizeof(c));
+  double dt = c[0] < c[1] ? c[0] : c[1];   // MIN(cflx, cfly), then MIN(., cflz)
+  dt = dt < c[2] ? dt : c[2];
+  *dt_out = (int32_t)dt;
+  if (cfl) memcpy(cfl, c, sizeof(c));
+  return EPIC_OK;
+}
+
 extern "C" int epic_model_sync(epic_model *m) {
   if (!m) return set_error(EPIC_ERR_ARG, "epic_model_sync: NULL model");
   EPIC_CUDA_CHECK(cudaStreamSynchronize(m->stream));

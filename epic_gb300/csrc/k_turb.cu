@@ -749,7 +749,59 @@ __global__ void k_dc_bottom(DevModel M) {
 
 inline unsigned nblk(long long n, int th) { return (unsigned)((n + th - 1) / th); }
 
+// cfl_dt (epic_funcs_diag.c:4884-5022): the minimum of each direction's limit over the grid, by
+// an atomic minimum on the bits of the positive binary64 limits (their order is the integers');
+// a minimum does not depend on the order of its operands, so the result is the reference's
+__global__ void k_cfl(DevModel M, unsigned long long *lim) {
+  if (epic_member(M, lim)) return;
+  const unsigned t = blockIdx.x * blockDim.x + threadIdx.x;
+  const unsigned ni = (unsigned)M.ni, nr = (unsigned)(M.nj + 1);
+  double cx = DBL_MAX, cy = DBL_MAX, cz = DBL_MAX;
+  if (t < (unsigned)M.nk * nr * ni) {
+    const unsigned r = t / ni, q = r / nr;
+    const int i = 1 + (int)(t - r * ni), j = (int)(r - q * nr), k = 1 + (int)q;
+    const long long off = plane_offset(M, PL_UV);
+    const double *U = M.u + off, *V = M.v + off;
+    const double dz = M.dsgth[2 * k];
+    double w = M.w3[M.at(k - 1, j, i)];
+    if (w > 0.) cz = dminr(cz, dz / w);
+    w = M.w3[M.at(k, j, i)];
+    if (w < 0.) cz = dminr(cz, -dz / w);
+    if (j >= 1) {
+      const double dy = 1. / M.n[2 * j + 1];
+      const double cs = sqrt(M.rgas * .5 * (M.t3[M.at(k, j, i)] + M.t3[M.at(k, j - 1, i)]) / (1. - M.kappa));
+      double v = V[M.at(k, j + 1, i)] + cs;
+      if (v > 0.) cy = dminr(cy, dy / v);
+      v = V[M.at(k, j, i)] - cs;
+      if (v < 0.) cy = dminr(cy, -dy / v);
+    }
+    if (fabs(M.lat[2 * j + 1]) <= M.lat0) {
+      const double dx = 1. / M.m[2 * j + 1];
+      const double cs = sqrt(M.rgas * .5 * (M.t3[M.at(k, j, i)] + M.t3[M.at(k, j, i - 1)]) / (1. - M.kappa));
+      double u = U[M.at(k, j, i + 1)] + cs;
+      if (u > 0.) cx = dminr(cx, dx / u);
+      u = U[M.at(k, j, i)] - cs;
+      if (u < 0.) cx = dminr(cx, -dx / u);
+    }
+  }
+  for (int o = 16; o > 0; o >>= 1) {
+    cx = dminr(cx, __shfl_xor_sync(0xffffffffu, cx, o));
+    cy = dminr(cy, __shfl_xor_sync(0xffffffffu, cy, o));
+    cz = dminr(cz, __shfl_xor_sync(0xffffffffu, cz, o));
+  }
+  if ((threadIdx.x & 31) == 0) {
+    atomicMin(&lim[0], (unsigned long long)__double_as_longlong(cx));
+    atomicMin(&lim[1], (unsigned long long)__double_as_longlong(cy));
+    atomicMin(&lim[2], (unsigned long long)__double_as_longlong(cz));
+  }
+}
+
 }  // namespace
+
+int launch_cfl_dt(const DevModel &M, unsigned long long *lim, cudaStream_t s) {
+  k_cfl<<<zg(nblk((long long)M.nk * (M.nj + 1) * M.ni, 128), M), 128, 0, s>>>(M, lim);
+  return 0;
+}
 
 // ---- launchers ----
 

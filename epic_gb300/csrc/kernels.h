@@ -117,5 +117,8 @@ int launch_uv_hdiff(const DevModel &M, cudaStream_t s);
 int launch_uv_vdiff(const DevModel &M, cudaStream_t s);
 int launch_set_diffusion_coef(const DevModel &M, cudaStream_t s);
 int launch_restore_nu(const DevModel &M, cudaStream_t s);
+// cfl_dt's three limits as the bits of positive binary64 values, minimised into lim[0..2]
+// (x, y, z), which the caller sets to DBL_MAX's bits first
+int launch_cfl_dt(const DevModel &M, unsigned long long *lim, cudaStream_t s);
 
 }  // namespace epic

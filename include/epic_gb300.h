@@ -218,6 +218,16 @@ int  epic_model_snapshot_begin(epic_model *m, epic_fields *f);
 int  epic_model_snapshot_wait(epic_model *m);
 
 /*
+ * cfl_dt(planet), src/shared/epic_funcs_diag.c:4884-5022, on the device state as the work already
+ * enqueued leaves it: the largest time step [s] the vertical, meridional and zonal advection
+ * allow (sound speed for the horizontal gravity waves; the zonal limit only equatorward of the
+ * filter latitude), truncated to int -- what var_write() stores as grid.cfl_dt before a save
+ * (src/shared/epic_funcs_io.c:1772).  cfl (may be NULL) receives the three limits before the
+ * truncation: cflx, cfly, cflz.  Waits for the model's queued work.
+ */
+int  epic_model_cfl_dt(epic_model *m, int32_t *dt_out, double *cfl);
+
+/*
  * End-to-end form of the drop-in: upload f, run nsteps (after a SYNC_DIAGS_ONLY call when
  * prime != 0), download into f.  This is what a reference-side timestep() wrapper does.
  */

@@ -3355,5 +3355,50 @@ int ep_download(ep_model *M, epic_fields *f) {
   return 0;
 }
 
+/* cfl_dt, epic_funcs_diag.c:4884-5022 (the limits before the truncation into cfl[0..2]: x, y, z) */
+int ep_cfl_dt(ep_model *M, double *cfl) {
+  const double *U = M->u + (long)M->it_uv * M->n3, *V = M->v + (long)M->it_uv * M->n3;
+  double cflx = DBL_MAX, cfly = DBL_MAX, cflz = DBL_MAX, u, v, w, cs, dx, dy, dz, dt;
+  int K, J, I;
+  for (K = 1; K <= KHI; K++) {
+    dz = M->dsgth[2 * K];
+    for (J = 0; J <= NJ; J++)
+      for (I = 1; I <= NI; I++) {
+        w = A3(M->w3, K - 1, J, I);
+        if (w > 0.) cflz = dmin(cflz, dz / w);
+        w = A3(M->w3, K, J, I);
+        if (w < 0.) cflz = dmin(cflz, -dz / w);
+      }
+  }
+  for (J = 1; J <= NJ; J++) {
+    dy = 1. / M->n[2 * J + 1];
+    for (I = 1; I <= NI; I++)
+      for (K = 1; K <= KHI; K++) {
+        cs = sqrt(M->g.rgas * .5 * (A3(M->t3, K, J, I) + A3(M->t3, K, J - 1, I)) / (1. - M->g.kappa));
+        v = A3(V, K, J + 1, I) + cs;
+        if (v > 0.) cfly = dmin(cfly, dy / v);
+        v = A3(V, K, J, I) - cs;
+        if (v < 0.) cfly = dmin(cfly, -dy / v);
+      }
+  }
+  for (J = 0; J <= NJ; J++) {
+    if (fabs(M->lat[2 * J + 1]) <= LAT0) {
+      dx = 1. / M->m[2 * J + 1];
+      for (I = 1; I <= NI; I++)
+        for (K = 1; K <= KHI; K++) {
+          cs = sqrt(M->g.rgas * .5 * (A3(M->t3, K, J, I) + A3(M->t3, K, J, I - 1)) / (1. - M->g.kappa));
+          u = A3(U, K, J, I + 1) + cs;
+          if (u > 0.) cflx = dmin(cflx, dx / u);
+          u = A3(U, K, J, I) - cs;
+          if (u < 0.) cflx = dmin(cflx, -dx / u);
+        }
+    }
+  }
+  if (cfl) { cfl[0] = cflx; cfl[1] = cfly; cfl[2] = cflz; }
+  dt = dmin(cflx, cfly);
+  dt = dmin(dt, cflz);
+  return (int)dt;
+}
+
 const char *ep_error(const ep_model *M) { return M->err; }
 const char *ep_create_error(void) { return create_err; }

@@ -55,6 +55,7 @@ void       ep_destroy(ep_model *m);
 int        ep_upload(ep_model *m, const epic_fields *f);
 int        ep_download(ep_model *m, epic_fields *f);
 int        ep_timestep(ep_model *m, int action);
+int        ep_cfl_dt(ep_model *m, double *cfl);   /* cfl_dt; cfl (may be NULL) = the x, y, z limits */
 int        ep_run(ep_model *m, int nsteps);
 int        ep_stage(ep_model *m, int stage);
 const char *ep_error(const ep_model *m);

@@ -181,6 +181,9 @@ int ref_run(int nsteps) {
   return 0;
 }
 
+/* The reference's cfl_dt(planet) on its current state (var_write calls it before a save). */
+int ref_cfl_dt(void) { return ref_ready ? cfl_dt(planet) : -1; }
+
 static void cp3(double *dst, const double *src) { if (dst) memcpy(dst, src, Nelem3d * sizeof(double)); }
 
 int ref_get(epic_fields *f) {

@@ -57,6 +57,7 @@ def port_lib(cr_libm: bool = False) -> C.CDLL:
             getattr(lib, n).argtypes = [C.c_void_p, C.POINTER(EpicFields)]
         for n in ("ep_timestep", "ep_run", "ep_stage"):
             getattr(lib, n).argtypes = [C.c_void_p, C.c_int]
+        lib.ep_cfl_dt.argtypes = [C.c_void_p, C.POINTER(C.c_double)]
         lib.ep_error.restype = C.c_char_p
         lib.ep_error.argtypes = [C.c_void_p]
         lib.ep_create_error.restype = C.c_char_p
@@ -97,6 +98,12 @@ class Port:
 
     def stage(self, s: int):
         self._chk(self.lib.ep_stage(self.h, s), "ep_stage")
+
+    def cfl_dt(self):
+        """cfl_dt of the current state: (the int time step, (cflx, cfly, cflz))."""
+        c = (C.c_double * 3)()
+        dt = self.lib.ep_cfl_dt(self.h, c)
+        return int(dt), tuple(c)
 
     def __del__(self):
         try:
@@ -149,7 +156,9 @@ def _ref_worker(grid_arrays: dict, grid_scalars: dict, fields: dict, dims, sched
                 lib.ref_run(n)
             g = Fields(ni, nj, nk, scheme, turbulence=bool(ga.struct.turbulence))
             lib.ref_get(C.byref(g.struct))
-            out.append(fields_to_dict(g))
+            d = fields_to_dict(g)
+            d["cfl_dt"] = int(lib.ref_cfl_dt())
+            out.append(d)
         q.put(("ok", list(geo), out))
     except Exception as e:  # pragma: no cover - reported to the parent
         q.put(("err", repr(e), None))

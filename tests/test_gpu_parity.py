@@ -144,6 +144,22 @@ def test_steps_bitwise(gpu, scheme, adv, state):
     assert not diff, diff
 
 
+@pytest.mark.parametrize("state", ["hs", "jet", "jet-sa"])
+def test_cfl_dt(gpu, state):
+    """cfl_dt on the device (a minimum over the grid, order-free) equals the restatement's three
+    limits bit for bit, after the synchronising call and after steps."""
+    cfg = HSConfig(ni=64, nj=32, nk=10, dt=300, seed=6, **_state(state))
+    ga, f, port, model = _pair(cfg, cr_libm=True)
+    port.timestep(EPIC_SYNC_DIAGS_ONLY)
+    model.timestep(EPIC_SYNC_DIAGS_ONLY)
+    assert model.cfl_dt() == port.cfl_dt()
+    port.run(5)
+    model.run(5)
+    got, want = model.cfl_dt(), port.cfl_dt()
+    assert got == want, (got, want)
+    assert 0 < got[0] < 10 ** 6
+
+
 def test_sync_diags(gpu):
     cfg = HSConfig(ni=64, nj=32, nk=10, dt=300)
     ga, f, port, model = _pair(cfg)

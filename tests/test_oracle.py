@@ -200,6 +200,27 @@ def test_turbulence_matches_reference(scheme, state, gg, direction):
             assert np.array_equal(got.arrays[k], want.arrays[k]), f"snapshot {i}: field {k} differs"
 
 
+@pytest.mark.parametrize("state,scheme", [("hs", EPIC_UV_AB3), ("jet", EPIC_UV_AB3), ("jet", EPIC_UV_LEAPFROG)])
+def test_cfl_dt_matches_reference(state, scheme):
+    """cfl_dt (the time step var_write stores before a save) of the restatement against the
+    reference's, after the synchronising call and after steps."""
+    if not reference_available():
+        pytest.skip("reference source tree not present on this host")
+    cfg = HSConfig(ni=32, nj=16, nk=10, dt=300, uv_scheme=scheme, seed=21, state=state,
+                   profile=EPIC_PROFILE_N2 if state == "jet" else 0)
+    ga, f = hs_setup(cfg)
+    sched = [("sync", 0), ("step", 1), ("step", 3)]
+    geo, snaps = run_reference(ga, f, sched)
+    port = Port(ga)
+    port.upload(f)
+    for i, (what, n) in enumerate(sched):
+        if what == "sync":
+            port.timestep(EPIC_SYNC_DIAGS_ONLY)
+        else:
+            port.run(n)
+        assert port.cfl_dt()[0] == snaps[i]["cfl_dt"], (i, port.cfl_dt(), snaps[i]["cfl_dt"])
+
+
 @pytest.mark.parametrize("seed", [0, 1, 2])
 def test_libm_rounding_floor_at_64x32x10(seed):
     """The CUDA kernels equal the restatement with correctly rounded log/exp/pow bit for bit (the
