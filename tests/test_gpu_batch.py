@@ -280,6 +280,37 @@ def test_batch_step_host_pipeline(gpu, groups, io):
         assert h.struct.itime == w.struct.itime
 
 
+@pytest.mark.parametrize("io", [EPIC_IO_ALL, EPIC_IO_STATE], ids=["all", "state"])
+def test_turbulence_step_host_pipeline(gpu, io):
+    """The pipelined end-to-end step with the turbulence closure: NU_TURB moves with the
+    prognostic arrays (EPIC_IO_STATE), the diffusivities stay on the device; every member equals
+    the same member stepped alone, bit for bit."""
+    cfgs = [HSConfig(ni=32, nj=16, nk=10, dt=300, seed=70 + q, state="jet", profile=EPIC_PROFILE_N2, turbulence=True)
+            for q in range(3)]
+    members = []
+    for cfg in cfgs:
+        ga, f = hs_setup(cfg)
+        m = Model(ga, EPIC_PREC_FP64)
+        m.upload(f)
+        members.append((ga, f, m))
+    b = Batch([m for _, _, m in members])
+    b.timestep(EPIC_SYNC_DIAGS_ONLY)
+    b.sync()
+    hosts = [m.download().copy(pinned=True) for _, _, m in members]
+    b.step_host(hosts, 3, groups=2, io=io)
+    diags = [m.download() for _, _, m in members]
+    for (ga, f, _), h, dg in zip(members, hosts, diags):
+        alone = Model(ga, EPIC_PREC_FP64)
+        alone.upload(f)
+        alone.timestep(EPIC_SYNC_DIAGS_ONLY)
+        alone.run(3)
+        alone.sync()
+        w = alone.download()
+        for k in w.arrays:
+            got = h.arrays[k] if io == EPIC_IO_ALL or k in PROGNOSTIC + ("nu_turb",) else dg.arrays[k]
+            assert np.array_equal(got, w.arrays[k]), (io, k)
+
+
 def test_state_io_needs_uploaded_members(gpu):
     """EPIC_IO_STATE moves the prognostic arrays only, so it refuses members with no state."""
     ga, f = hs_setup(HSConfig(ni=32, nj=16, nk=10, dt=300, seed=3))

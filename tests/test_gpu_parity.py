@@ -97,7 +97,7 @@ def test_stage_by_stage(gpu, scheme, adv, state):
 
 
 @pytest.mark.parametrize("adv,state", [(EPIC_ADV_HSU, "hs-sa"), (EPIC_ADV_AKIMA, "hs-sa"), (EPIC_ADV_HSU, "jet-sa"),
-                                       (EPIC_ADV_HSU, "jet-gg-sa")])
+                                       (EPIC_ADV_HSU, "jet-gg-sa"), (EPIC_ADV_HSU, "jet-gg-h2-sa")])
 @pytest.mark.parametrize("scheme", [EPIC_UV_AB3, EPIC_UV_LEAPFROG])
 def test_stage_by_stage_turbulence(gpu, scheme, adv, state):
     """The turbulence closure's stages (source_sink_turb, the scalar and wind subgrid diffusions)

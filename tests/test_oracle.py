@@ -171,19 +171,19 @@ def test_hydrogen_thermodynamics_match_reference(scheme, state):
             assert np.array_equal(got.arrays[k], want.arrays[k]), f"snapshot {i}: field {k} differs"
 
 
-@pytest.mark.parametrize("scheme,state,gg,direction", [(EPIC_UV_AB3, "jet", False, 1), (EPIC_UV_LEAPFROG, "hs", False, 1),
-                                                       (EPIC_UV_AB3, "jet", True, 1), (EPIC_UV_AB3, "jet", False, 2),
-                                                       (EPIC_UV_AB3, "jet", False, 3)])
-def test_turbulence_matches_reference(scheme, state, gg, direction):
+@pytest.mark.parametrize("scheme,state,gg,direction,h2", [(EPIC_UV_AB3, "jet", False, 1, 0.), (EPIC_UV_LEAPFROG, "hs", False, 1, 0.),
+                                                          (EPIC_UV_AB3, "jet", True, 1, 0.), (EPIC_UV_AB3, "jet", False, 2, 0.),
+                                                          (EPIC_UV_AB3, "jet", False, 3, 0.), (EPIC_UV_AB3, "jet", True, 1, 0.864)])
+def test_turbulence_matches_reference(scheme, state, gg, direction, h2):
     """The Spalart-Allmaras DES closure (source_sink_turb, the horizontal and vertical subgrid
     diffusion of THETA, NU_TURB and the winds, set_diffusion_coef in store_diag) on the
-    Held-Suarez planet, terrestrial or gas-giant: the restatement against the reference's step,
+    Held-Suarez planet, terrestrial or gas-giant, ideal or hydrogen-helium: the restatement against the reference's step,
     every field (NU_TURB and the diffusivities included) bit for bit after every step."""
     if not reference_available():
         pytest.skip("reference source tree not present on this host")
     cfg = HSConfig(ni=32, nj=16, nk=10, dt=300, uv_scheme=scheme, seed=9, state=state,
                    profile=EPIC_PROFILE_N2 if state == "jet" else 0, gas_giant=gg, turbulence=True,
-                   diffusion_direction=direction)
+                   diffusion_direction=direction, x_h2=h2, x_he=0.136 if h2 else 0.)
     ga, f = hs_setup(cfg)
     sched = [("sync", 0)] + [("step", 1)] * 6
     geo, snaps = run_reference(ga, f, sched)
