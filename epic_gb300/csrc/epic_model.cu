@@ -926,21 +926,14 @@ static __device__ __align__(256) double g_noalloc_ptable[3 * EPIC_NOALLOC_TABLE_
 
 namespace {
 
-constexpr int kNoallocMaxDevices = 64;
-std::mutex g_noalloc_mu;
-double *g_noalloc_addr[kNoallocMaxDevices] = {nullptr};
-
-// Address of g_noalloc_ptable on device `dev`, which must be current.  Resolved once per device.
+// Address of g_noalloc_ptable in the current context, looked up on every call (no allocation):
+// a context torn down and made again (cudaDeviceReset) reloads the module, possibly elsewhere.
 int noalloc_table(int dev, double **out) {
-  if (dev < 0 || dev >= kNoallocMaxDevices) return set_error(EPIC_ERR_ARG, "device %d out of range", dev);
-  std::lock_guard<std::mutex> lock(g_noalloc_mu);
-  if (!g_noalloc_addr[dev]) {
-    void *p = nullptr;
-    const cudaError_t e = cudaGetSymbolAddress(&p, g_noalloc_ptable);
-    if (e != cudaSuccess || !p) return set_error(EPIC_ERR_CUDA, "cudaGetSymbolAddress: %s", cudaGetErrorString(e));
-    g_noalloc_addr[dev] = static_cast<double *>(p);
-  }
-  *out = g_noalloc_addr[dev];
+  (void)dev;
+  void *p = nullptr;
+  const cudaError_t e = cudaGetSymbolAddress(&p, g_noalloc_ptable);
+  if (e != cudaSuccess || !p) return set_error(EPIC_ERR_CUDA, "cudaGetSymbolAddress: %s", cudaGetErrorString(e));
+  *out = static_cast<double *>(p);
   return EPIC_OK;
 }
 
