@@ -124,9 +124,10 @@ struct DevModel {
 // A pointer into member 0's arrays, moved to the same place in member `to`'s arrays.  The pool of
 // a model (epic_model_create) packs the state arrays back to back as planes of n3 values (u and v
 // value planes, the tendency planes, then the single fields), and carves the scratch volumes gz,
-// unity, old, work0..3 one after another, each rounded up to 256 bytes; so the plane (or volume)
-// index and the offset inside it follow from the address by integer arithmetic, and map to the
-// member's pool with its own n3.  A pointer outside both regions (a table) is returned as is.
+// unity, old, work0..3 one after another, each rounded up to 256 bytes (and, with the turbulence
+// closure, NU_TURB and the three diffusivities the same way); so the plane (or volume) index and
+// the offset inside it follow from the address by integer arithmetic, and map to the member's
+// pool with its own n3.  A pointer outside these regions (a table) is returned as is.
 __host__ __device__ __forceinline__ long long scratch_stride(long long n3) { return ((n3 * 8 + 255) / 256) * 256; }
 template <class P>
 __device__ __forceinline__ P *relocate_field(const DevModel &from, const DevModel &to, P *p) {
@@ -137,6 +138,13 @@ __device__ __forceinline__ P *relocate_field(const DevModel &from, const DevMode
   if (c >= s0 && c < s0 + 7 * st0) {
     const long long o = c - s0, q = o / st0;
     return reinterpret_cast<P *>(reinterpret_cast<char *>(to.gz) + q * scratch_stride(to.n3) + (o - q * st0));
+  }
+  if (from.nu_turb) {   // the turbulence closure's four volumes (NU_TURB, the diffusivities), one stride apart
+    const char *t0 = reinterpret_cast<const char *>(from.nu_turb);
+    if (c >= t0 && c < t0 + 4 * st0) {
+      const long long o = c - t0, q = o / st0;
+      return reinterpret_cast<P *>(reinterpret_cast<char *>(to.nu_turb) + q * scratch_stride(to.n3) + (o - q * st0));
+    }
   }
   const char *b0 = reinterpret_cast<const char *>(from.u);
   const long long planes = 2LL * from.nvp + 2LL * from.ntp + 20;

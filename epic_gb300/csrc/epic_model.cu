@@ -577,11 +577,16 @@ extern "C" int epic_model_create(const epic_grid *g, int32_t precision, epic_mod
   epic::MathTable *lt = carve<epic::MathTable>(p, 1);
   float2 *exp2tab = carve<float2>(p, 32);
   double *thermo_d = carve<double>(p, (size_t)epic::TH_N * epic::TH_M + 4 * epic::TH_M + epic::TH_N);
-  if (d.turb) {   // the turbulence closure: NU_TURB, the three diffusivities, scratch and a row table
+  if (d.turb) {   // the turbulence closure: NU_TURB, the three diffusivities (one stride apart, as
+                  // relocate_field expects), scratch and a row table
     d.nu_turb = carve<double>(p, n3);
     d.dc_uv = carve<double>(p, n3);
     d.dc_theta = carve<double>(p, n3);
     d.dc_mass = carve<double>(p, n3);
+    if ((const char *)d.dc_mass - (const char *)d.nu_turb != 3 * epic::scratch_stride(d.n3)) {
+      epic_model_destroy(m);
+      return set_error(EPIC_ERR_STATE, "internal pool layout of the turbulence arrays differs from the batch relocation's");
+    }
     d.turb_pole = carve<double>(p, 2 * (size_t)(g->nk + 2));
     d.turb_maxnu2 = carve<double>(p, (size_t)g->nj + 1);
   }
@@ -1026,10 +1031,6 @@ extern "C" int epic_batch_create(epic_model *const *members, int32_t n, epic_bat
     const char *why = nullptr;
     if (!batch_compatible(members[0]->d, members[i]->d, &why))
       return set_error(EPIC_ERR_ARG, "epic_batch_create: member %d differs from member 0 in %s", i, why);
-    // the turbulence arrays lie outside the regions a launch over members of different sizes moves
-    // its pointer arguments between (relocate_field)
-    if (members[0]->d.turb && (members[i]->d.ni != members[0]->d.ni || members[i]->d.nj != members[0]->d.nj))
-      return set_error(EPIC_ERR_ARG, "epic_batch_create: the turbulence closure batches members of one grid size only (member %d)", i);
     for (int q = 0; q < i; q++)
       if (members[q] == members[i]) return set_error(EPIC_ERR_ARG, "epic_batch_create: member %d repeats member %d", i, q);
     // every kernel of the batch reads and writes each member's pool: all on one device

@@ -106,19 +106,17 @@ def test_batch_rejects_incompatible_members(gpu):
         Batch([a, t1])
     with pytest.raises(EpicError, match="turbulence"):   # the closure is in the FP64 form only
         Model(gt, EPIC_PREC_MIXED)
-    gt2, ft2 = hs_setup(HSConfig(ni=64, nj=32, nk=10, dt=300, seed=8, turbulence=True))
-    t2 = Model(gt2, EPIC_PREC_FP64)
-    t2.upload(ft2)
-    with pytest.raises(EpicError, match="one grid size"):
-        Batch([t1, t2])
     Batch([a, f]).close()   # sizes alone may differ
 
 
-def test_turbulence_batch_equals_members_alone(gpu):
-    """Three members with the turbulence closure (zonal jets, different seeds and time steps) in
-    one batch: every member equals the same member stepped alone, bit for bit."""
-    cfgs = [HSConfig(ni=32, nj=16, nk=10, dt=dt, seed=60 + q, state="jet", profile=EPIC_PROFILE_N2, turbulence=True)
-            for q, dt in enumerate((300, 300, 150))]
+@pytest.mark.parametrize("shapes", [[(32, 16, 300), (32, 16, 300), (32, 16, 150)], [(32, 16, 300), (64, 32, 300), (64, 48, 150)]],
+                         ids=["same_size", "uneven"])
+def test_turbulence_batch_equals_members_alone(gpu, shapes):
+    """Three members with the turbulence closure (zonal jets, different seeds and time steps; of
+    one size, or of different ni, nj, dt) in one batch: every member equals the same member
+    stepped alone, bit for bit."""
+    cfgs = [HSConfig(ni=ni, nj=nj, nk=10, dt=dt, seed=60 + q, state="jet", profile=EPIC_PROFILE_N2, turbulence=True)
+            for q, (ni, nj, dt) in enumerate(shapes)]
     alone, models, fields = [], [], []
     for cfg in cfgs:
         ga, f = hs_setup(cfg)
