@@ -297,7 +297,7 @@ class HSConfig:
     # the gas-giant lower boundary: GZ_SURFACE from gradient balance with the bottom layer's
     # zonal-mean U in every store_pgrad_vars (planet->type "gas-giant"), instead of the terrain
     gas_giant: bool = False
-    # hydrogen thermodynamics (FP64 form): mole fractions of H2 and He; 0 keeps the ideal gas
+    # hydrogen thermodynamics (every form): mole fractions of H2 and He; 0 keeps the ideal gas
     x_h2: float = 0.0
     x_he: float = 0.0
     # the Spalart-Allmaras DES turbulence closure (FP64 form): NU_TURB starts at 20 kinvisc

@@ -447,8 +447,7 @@ extern "C" int epic_model_create(const epic_grid *g, int32_t precision, epic_mod
     return set_error(EPIC_ERR_ARG, "precision form %d not available", precision);
   if (g->ni < 4 || (g->ni & (g->ni - 1)) || g->ni > EPIC_MAX_NI) return set_error(EPIC_ERR_ARG, "ni=%d: need a power of 2 in [4,%d]", g->ni, EPIC_MAX_NI);
   if (g->nj < 3 || g->nk < 3 || g->nk > EPIC_MAX_NK) return set_error(EPIC_ERR_ARG, "nj=%d nk=%d out of range", g->nj, g->nk);
-  if (g->x_h2 < 0. || (g->x_h2 > 0. && precision != EPIC_PREC_FP64))
-    return set_error(EPIC_ERR_ARG, "x_h2=%g: hydrogen thermodynamics are in the FP64 form only", g->x_h2);
+  if (g->x_h2 < 0.) return set_error(EPIC_ERR_ARG, "x_h2=%g: negative", g->x_h2);
   if (g->turbulence != EPIC_TURB_OFF) {
     if (g->turbulence != EPIC_TURB_SA_DES) return set_error(EPIC_ERR_ARG, "turbulence=%d", g->turbulence);
     if (precision != EPIC_PREC_FP64) return set_error(EPIC_ERR_ARG, "the turbulence closure is in the FP64 form only");

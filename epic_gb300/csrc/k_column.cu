@@ -745,7 +745,9 @@ __global__ void __launch_bounds__(CT_THREADS, 4) k_set_p2etc_mixed(DevModel M, i
 // FULL = false: GZ3 alone (and its monotonicity check), for the call before the filtered-GZ
 // copy; that call's T3, EXNER3, RHO3, T2, RHO2, MONT3 and DZDT3 are rewritten by the call after
 // set_p2etc (stage 19) before anything reads them, and that call reads this GZ3 as the old one.
-template <bool FULL>
+// H2: the hydrogen thermodynamics (x_h2 > 0): T3, T2 and MONT3's enthalpy from thermo_setup's
+// tables in binary64, EXNER3 = cp T3 / THETA (epic_funcs_diag.c:3698, :3717).
+template <bool FULL, bool H2>
 __global__ void __launch_bounds__(CT_THREADS, 4) k_pgrad_vars_column_mixed(DevModel M) {
   if (epic_member(M)) return;
   extern __shared__ double sm[];
@@ -764,21 +766,35 @@ __global__ void __launch_bounds__(CT_THREADS, 4) k_pgrad_vars_column_mixed(DevMo
   // is that of the FP32 power, 1e-7, either way), stored in binary64
   auto level = [&](int k, double theta, double p, double pr, double th2) {
       const long long x = c.base + k * n2;
-      const float pf = powf(d2f(p) * p0_inv, kap);
-      const float t3f = d2f(theta) * pf;
-      const double t3 = f2d(t3f);
-      const double rho = f2d(d2f(p) * mu_over_r / t3f);
+      float pf = 0.f;
+      double t3, rho;
+      if (H2) {
+        t3 = return_temp(M, p, theta);
+        rho = return_density(p, t3, mu);
+      } else {
+        pf = powf(d2f(p) * p0_inv, kap);
+        const float t3f = d2f(theta) * pf;
+        t3 = f2d(t3f);
+        rho = f2d(d2f(p) * mu_over_r / t3f);
+      }
       CT(P, k) = p;
       CT(R, k) = rho;
       CT(T3, k) = t3;
       if (!FULL) return;
       M.t3[x] = t3;
-      M.exner3[x] = f2d(cpf * pf);
+      M.exner3[x] = H2 ? M.cp * t3 / theta : f2d(cpf * pf);
       M.rho3[x] = rho;
       if (k >= 1) {
-        const float t2f = d2f(th2) * powf(d2f(pr) * p0_inv, kap);
-        M.t2[x] = f2d(t2f);
-        const double r2 = f2d(d2f(pr) * mu_over_r / t2f);
+        double r2;
+        if (H2) {
+          const double t2 = return_temp(M, pr, th2);
+          M.t2[x] = t2;
+          r2 = return_density(pr, t2, mu);
+        } else {
+          const float t2f = d2f(th2) * powf(d2f(pr) * p0_inv, kap);
+          M.t2[x] = f2d(t2f);
+          r2 = f2d(d2f(pr) * mu_over_r / t2f);
+        }
         M.rho2[x] = r2;
         if (k == 1) s_rho2_1[c.lane] = r2;
       }
@@ -856,7 +872,8 @@ __global__ void __launch_bounds__(CT_THREADS, 4) k_pgrad_vars_column_mixed(DevMo
     const double gzk = CT(GZ, k);
     M.gz3[x] = gzk;
     put_split(M.work1, x, gzk);
-    M.mont3[x] = f2d(d2f(gzk) + cprf * d2f(CT(T3, k)) * rgasf);   // GZ3 + return_enthalpy
+    if (H2) M.mont3[x] = gzk + return_enthalpy(M, CT(T3, k));
+    else M.mont3[x] = f2d(d2f(gzk) + cprf * d2f(CT(T3, k)) * rgasf);   // GZ3 + return_enthalpy
     if (interior && k >= 1) {
       float dz = 0.f;
       if (itime > 1) dz = d2f(old - gzk) * dtg_inv;
@@ -1137,14 +1154,17 @@ int launch_store_pgrad_vars(const DevModel &M, cudaStream_t s, bool early) {
     k_gz_means<<<zg(M.nj + 1, M), 256, (size_t)3 * M.ni * sizeof(double), s>>>(M);
     k_gz_from_u<<<zg(1, M), 256, (size_t)(7 * M.nj + 8) * sizeof(double), s>>>(M);
   }
+  const dim3 grid = zg(ntile_blocks(M), M);
+  const size_t smem = tile_smem(M, 5);
+  const bool h2 = M.x_h2 != 0.;
   if (M.mixed && early) {   // GZ3 alone: no DZDT3, so no horizontal part either
-    if (M.col64) k_gz3_column_acc<<<zg(ntile_blocks(M), M), CT_THREADS, tile_smem(M, 5), s>>>(M);
-    else k_pgrad_vars_column_mixed<false><<<zg(ntile_blocks(M), M), CT_THREADS, tile_smem(M, 5), s>>>(M);
+    if (M.col64) (h2 ? k_gz3_column_acc_h2 : k_gz3_column_acc)<<<grid, CT_THREADS, smem, s>>>(M);
+    else (h2 ? k_pgrad_vars_column_mixed<false, true> : k_pgrad_vars_column_mixed<false, false>)<<<grid, CT_THREADS, smem, s>>>(M);
     return 0;
   }
-  if (M.col64) k_pgrad_vars_column_acc<<<zg(ntile_blocks(M), M), CT_THREADS, tile_smem(M, 5), s>>>(M);
-  else if (M.mixed) k_pgrad_vars_column_mixed<true><<<zg(ntile_blocks(M), M), CT_THREADS, tile_smem(M, 5), s>>>(M);
-  else k_pgrad_vars_column<<<zg(ntile_blocks(M), M), CT_THREADS, tile_smem(M, 5), s>>>(M);
+  if (M.col64) (h2 ? k_pgrad_vars_column_acc_h2 : k_pgrad_vars_column_acc)<<<grid, CT_THREADS, smem, s>>>(M);
+  else if (M.mixed) (h2 ? k_pgrad_vars_column_mixed<true, true> : k_pgrad_vars_column_mixed<true, false>)<<<grid, CT_THREADS, smem, s>>>(M);
+  else k_pgrad_vars_column<<<grid, CT_THREADS, smem, s>>>(M);
   EPIC_LAUNCH_R(M.mixed, k_pgrad_dzdt, epic_blocks((long long)M.nk * (M.nj + 1) * M.ni, TB(M, TB_UPDATE)), TB(M, TB_UPDATE), 0, s, M);
   return 0;
 }
@@ -1169,8 +1189,10 @@ int column_kernels_init(int) {
       cudaFuncSetAttribute(k_set_p2etc, cudaFuncAttributeMaxDynamicSharedMemorySize, big) != cudaSuccess ||
       cudaFuncSetAttribute(k_pgrad_vars_column, cudaFuncAttributeMaxDynamicSharedMemorySize, big) != cudaSuccess ||
       cudaFuncSetAttribute(k_set_p2etc_mixed, cudaFuncAttributeMaxDynamicSharedMemorySize, big) != cudaSuccess ||
-      cudaFuncSetAttribute(k_pgrad_vars_column_mixed<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, big) != cudaSuccess ||
-      cudaFuncSetAttribute(k_pgrad_vars_column_mixed<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, big) != cudaSuccess ||
+      cudaFuncSetAttribute(k_pgrad_vars_column_mixed<true, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, big) != cudaSuccess ||
+      cudaFuncSetAttribute(k_pgrad_vars_column_mixed<false, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, big) != cudaSuccess ||
+      cudaFuncSetAttribute(k_pgrad_vars_column_mixed<true, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, big) != cudaSuccess ||
+      cudaFuncSetAttribute(k_pgrad_vars_column_mixed<false, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, big) != cudaSuccess ||
       cudaFuncSetAttribute(k_hsu_vertical<double>, cudaFuncAttributeMaxDynamicSharedMemorySize, hv) != cudaSuccess ||
       cudaFuncSetAttribute(k_hsu_vertical<float>, cudaFuncAttributeMaxDynamicSharedMemorySize, hv) != cudaSuccess ||
       cudaFuncSetAttribute(k_akima_vertical<double>, cudaFuncAttributeMaxDynamicSharedMemorySize, hv) != cudaSuccess ||

@@ -166,7 +166,10 @@ __global__ void __launch_bounds__(CT_THREADS, 4) k_set_p2etc_acc(DevModel M, int
 
 // FULL = false: GZ3 alone (with its monotonicity check) -- the call before the filtered-GZ
 // copy, whose other outputs the call after stage 11 rewrites before anything reads them.
-template <bool FULL>
+// H2: the hydrogen thermodynamics (x_h2 > 0): T3, T2 and the enthalpy of MONT3 from thermo_setup's
+// tables in binary64 (return_temp, return_enthalpy), EXNER3 = cp T3 / THETA as the reference
+// stores it (epic_funcs_diag.c:3698, :3717); the ideal-gas power (p/p0)^kappa is then not T3/THETA.
+template <bool FULL, bool H2>
 __device__ __forceinline__ void pgrad_vars_column_acc(DevModel &M) {
   extern __shared__ double sm[];
   __shared__ double s_rho2_1[32];
@@ -183,19 +186,28 @@ __device__ __forceinline__ void pgrad_vars_column_acc(DevModel &M) {
   auto level = [&](int k, double theta, double p, double pr, double th2, float2 lpk) {
     const long long x = c.base + k * n2;
     const dfl Pk = cv<dfl>(p);
-    const dfl pi = exp_df(kap * (dfl(lpk.x, lpk.y) - lp0), tab);   // (p/p0)^kappa
+    const double t3d = H2 ? return_temp(M, p, theta) : 0.;
+    const dfl pi = H2 ? dfl(0.f, 0.f) : exp_df(kap * (dfl(lpk.x, lpk.y) - lp0), tab);   // (p/p0)^kappa
     CT(LP, k) = lpk;
-    const dfl t3 = cv<dfl>(theta) * pi;
+    const dfl t3 = H2 ? cv<dfl>(t3d) : cv<dfl>(theta) * pi;
     const double rho = to_d(Pk * mu_over_r / t3);
     if (FULL) {
       M.t3[x] = to_d(t3);
-      M.exner3[x] = f2d(cpf * pi.hi);
+      M.exner3[x] = H2 ? M.cp * t3d / theta : f2d(cpf * pi.hi);
       M.rho3[x] = rho;
     }
     CT(P, k) = p;
     CT(R, k) = rho;
     CT(T3, k) = make_float2(t3.hi, t3.lo);
     if (FULL && k >= 1) {   // the layer's T2, RHO2: read by the Richardson number only
+      if (H2) {
+        const double t2 = return_temp(M, pr, th2);
+        M.t2[x] = t2;
+        const double r2 = return_density(pr, t2, M.mu_dry);
+        M.rho2[x] = r2;
+        if (k == 1) s_rho2_1[c.lane] = r2;
+        return;
+      }
       const float t2f = d2f(th2) * powf(d2f(pr) * p0_inv.hi, kap.hi);
       M.t2[x] = f2d(t2f);
       const double r2 = f2d(d2f(pr) * mu_over_r.hi / t2f);
@@ -267,7 +279,8 @@ __device__ __forceinline__ void pgrad_vars_column_acc(DevModel &M) {
     M.gz3[x] = gzk;
     if (FULL) {
       put_split(M.work1, x, gzk);
-      M.mont3[x] = f2d(d2f(gzk) + cprf * CT(T3, k).x * rgasf);
+      if (H2) M.mont3[x] = gzk + return_enthalpy(M, to_d(t3df(k)));
+      else M.mont3[x] = f2d(d2f(gzk) + cprf * CT(T3, k).x * rgasf);
     }
     if (interior && k >= 1) {
       if (FULL) {
@@ -300,18 +313,29 @@ __device__ __forceinline__ void pgrad_vars_column_acc(DevModel &M) {
 
 __global__ void __launch_bounds__(CT_THREADS, 4) k_pgrad_vars_column_acc(DevModel M) {
   if (epic_member(M)) return;
-  pgrad_vars_column_acc<true>(M);
+  pgrad_vars_column_acc<true, false>(M);
 }
 __global__ void __launch_bounds__(CT_THREADS, 4) k_gz3_column_acc(DevModel M) {
   if (epic_member(M)) return;
-  pgrad_vars_column_acc<false>(M);
+  pgrad_vars_column_acc<false, false>(M);
+}
+// the same with hydrogen thermodynamics (their binary64 table interpolation needs more registers)
+__global__ void __launch_bounds__(CT_THREADS) k_pgrad_vars_column_acc_h2(DevModel M) {
+  if (epic_member(M)) return;
+  pgrad_vars_column_acc<true, true>(M);
+}
+__global__ void __launch_bounds__(CT_THREADS) k_gz3_column_acc_h2(DevModel M) {
+  if (epic_member(M)) return;
+  pgrad_vars_column_acc<false, true>(M);
 }
 
 int column_acc_kernels_init() {
   const int big = (int)(5 * 32 * (EPIC_MAX_NK + 1) * sizeof(double));
   if (cudaFuncSetAttribute(k_set_p2etc_acc, cudaFuncAttributeMaxDynamicSharedMemorySize, big) != cudaSuccess ||
       cudaFuncSetAttribute(k_pgrad_vars_column_acc, cudaFuncAttributeMaxDynamicSharedMemorySize, big) != cudaSuccess ||
-      cudaFuncSetAttribute(k_gz3_column_acc, cudaFuncAttributeMaxDynamicSharedMemorySize, big) != cudaSuccess)
+      cudaFuncSetAttribute(k_gz3_column_acc, cudaFuncAttributeMaxDynamicSharedMemorySize, big) != cudaSuccess ||
+      cudaFuncSetAttribute(k_pgrad_vars_column_acc_h2, cudaFuncAttributeMaxDynamicSharedMemorySize, big) != cudaSuccess ||
+      cudaFuncSetAttribute(k_gz3_column_acc_h2, cudaFuncAttributeMaxDynamicSharedMemorySize, big) != cudaSuccess)
     return -1;
   return 0;
 }

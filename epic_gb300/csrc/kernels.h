@@ -57,6 +57,8 @@ int filter_gemm_init(int ni);
 __global__ void k_set_p2etc_acc(DevModel M, int update_theta, int layers);
 __global__ void k_pgrad_vars_column_acc(DevModel M);
 __global__ void k_gz3_column_acc(DevModel M);   // GZ3 alone (the call before the filtered-GZ copy)
+__global__ void k_pgrad_vars_column_acc_h2(DevModel M);   // the two above with hydrogen thermodynamics
+__global__ void k_gz3_column_acc_h2(DevModel M);
 int column_acc_kernels_init();
 void fill_filter_kernels(int ni, int nj, const double *hl_h, const double *hl_pv, long long iadim, float *fh, float *fv);
 bool filter_operator_wanted(const epic_grid &g, int precision);

@@ -109,8 +109,8 @@ typedef struct epic_grid {
                                   thermodynamics (thermo_setup's ortho/para tables, normal
                                   hydrogen, fpara = 0.25: return_temp and return_enthalpy by table
                                   interpolation); cpr must then be thermo_setup's
-                                  (2.5 x_h2 + 2.5 x_he + 3.5 x_3) / (x_h2 + x_he + x_3).  FP64
-                                  form only.                                                    */
+                                  (2.5 x_h2 + 2.5 x_he + 3.5 x_3) / (x_h2 + x_he + x_3).  Every
+                                  precision form (the tables are read in binary64).             */
   double  dynvisc;             /* planet->dynvisc [kg/m/s] (the turbulence closure's molecular
                                   viscosity of the winds)                                       */
   int32_t turbulence;          /* grid.turbulence_scheme: EPIC_TURB_OFF or EPIC_TURB_SA_DES

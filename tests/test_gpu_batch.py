@@ -97,8 +97,6 @@ def test_batch_rejects_incompatible_members(gpu):
     h.upload(fh)
     with pytest.raises(EpicError, match="thermodynamics"):
         Batch([a, h])
-    with pytest.raises(EpicError, match="x_h2"):   # hydrogen tables are in the FP64 form only
-        Model(gh, EPIC_PREC_MIXED)
     gt, ft = hs_setup(HSConfig(ni=32, nj=16, nk=10, dt=300, seed=7, turbulence=True))
     t1 = Model(gt, EPIC_PREC_FP64)
     t1.upload(ft)

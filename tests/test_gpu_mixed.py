@@ -24,6 +24,8 @@ Stated error (relative L2 per field vs FP64, dt 300 s), measured on a GB300:
   mixed  64x32x10   zonal jets, 1 day                 3.4e-7   8.9e-7   1.7e-8   3.4e-9
   fast   64x32x10   zonal jets, 1 day                 3.6e-6   1.8e-5   1.4e-7   3.8e-8
   mixed  64x32x10   jets, gas-giant boundary, 1 day   3.7e-7   7.3e-7   1.1e-7   4.1e-9
+  mixed  64x32x10   same with hydrogen, dt 150, 1 day 3.7e-7   6.7e-7   1.6e-7   3.9e-9
+  fast   64x32x10   same with hydrogen, dt 150, 1 day 3.3e-6   5.6e-6   2.7e-7   3.7e-8
 
 (128x64x20 is the ensemble member shape: ni = 128 takes the tensor-core filter; its FP64 run
 stays stable for about two days, so its spin-up is one day.)
@@ -65,6 +67,10 @@ BOUNDS = {
     # THETA 4.1e-9)
     ("mixed", "jet-gg"): {"u": 8e-7, "v": 1.5e-6, "hdry": 2.2e-7, "theta": 1e-8},
     ("fast", "jet-gg"): {"u": 1.2e-5, "v": 6e-5, "hdry": 2e-6, "theta": 1.2e-7},
+    # the same with the hydrogen-helium thermodynamics, dt 150 (measured: mixed U 3.7e-7, V 6.7e-7,
+    # HDRY 1.6e-7, THETA 3.9e-9; fast U 3.3e-6, V 5.6e-6, HDRY 2.7e-7, THETA 3.7e-8)
+    ("mixed", "jet-gg-h2"): {"u": 8e-7, "v": 1.5e-6, "hdry": 3.5e-7, "theta": 1e-8},
+    ("fast", "jet-gg-h2"): {"u": 8e-6, "v": 1.5e-5, "hdry": 6e-7, "theta": 8e-8},
     ("fast", "spun_up"): {"u": 1e-4, "v": 2e-3, "hdry": 1e-6, "theta": 1e-7},
     ("fast", "rest"): {"u": 1e-3, "v": 3e-3, "hdry": 1e-6, "theta": 1e-7},
     ("fast", "leapfrog"): {"u": 6e-3, "v": 3e-3, "hdry": 1e-6, "theta": 1e-7},
@@ -202,6 +208,20 @@ def test_jets_one_day(gpu, form, gas_giant):
     ga, f = hs_setup(HSConfig(ni=64, nj=32, nk=10, dt=300, seed=0, profile=EPIC_PROFILE_N2, state="jet", gas_giant=gas_giant))
     a, b = _pair(ga, f, True, FORMS[form])
     _check(_run(a, b, DAY), BOUNDS[(form, "jet-gg" if gas_giant else "jet")])
+
+
+@pytest.mark.parametrize("form", FORMS)
+def test_hydrogen_jets_one_day(gpu, form):
+    """The zonal jets over the gas-giant lower boundary with the hydrogen-helium thermodynamics
+    (x_h2 = 0.864, x_he = 0.136: T3, T2 and the enthalpy of MONT3 from thermo_setup's tables, in
+    binary64 in every form), one day against the FP64 form; dt 150 s (at dt 300 s the FP64 step,
+    as the reference's, stops with non-monotonic GZ3 after 250 steps)."""
+    ga, f = hs_setup(HSConfig(ni=64, nj=32, nk=10, dt=150, seed=0, profile=EPIC_PROFILE_N2, state="jet", gas_giant=True,
+                              x_h2=0.864, x_he=0.136))
+    a, b = _pair(ga, f, True, FORMS[form])
+    e = _run(a, b, 2 * DAY)
+    print(form, "jet-gg-h2", {k: float(v[0]) for k, v in e.items()})
+    _check(e, BOUNDS[(form, "jet-gg-h2")])
 
 
 @pytest.mark.parametrize("shape,dt,steps", [((256, 128, 10), 120, 240), ((512, 256, 10), 60, 120)])
