@@ -1,7 +1,7 @@
 """Throughput of the GB300 EPIC timestep() on synthetic Held-Suarez states.
 
     python bench.py [--gpus N] [--steps K] [--warmup W] [--impl gb300|reference]
-                    [--workload ens64|hs64|hs128|hs256|hs512|jet256|jet256gg|hs128sa|jet128sa]
+                    [--workload ens64|hs64|hs128|hs256|hs512|jet256|jet256gg|jet256ggh2|hs128sa|jet128sa]
                     [--precision mixed|fast|fp64]
                     [--no-cpu-baseline] [--no-extras]
 
@@ -47,6 +47,7 @@ WORKLOADS = {
     "hs512": (512, 256, 40, 60),
     "jet256": (256, 128, 32, 60),  # balanced zonal jets on the constant-N^2 sounding
     "jet256gg": (256, 128, 32, 60),  # the same over the gas-giant lower boundary (gz_from_u)
+    "jet256ggh2": (256, 128, 32, 60),  # and with the hydrogen-helium thermodynamics (thermo_setup's tables)
     "hs128sa": (128, 64, 20, 300),   # the Held-Suarez column with the Spalart-Allmaras DES closure (FP64)
     "jet128sa": (128, 64, 20, 300),  # the balanced jets with the Spalart-Allmaras DES closure (FP64)
     "ens64": (128, 64, 20, 300),   # per member; 64 members
@@ -72,9 +73,10 @@ def _workload_cfg(name, seed=0, advection="hsu"):
     from epic_gb300 import EPIC_PROFILE_N2, HSConfig
     ni, nj, nk, dt = WORKLOADS[name]
     turb = name.endswith("sa")
+    h2 = {"x_h2": 0.864, "x_he": 0.136} if name.endswith("h2") else {}
     if name.startswith("jet"):
         return HSConfig(ni=ni, nj=nj, nk=nk, dt=dt, seed=seed, advection_scheme=ADVECTION[advection], profile=EPIC_PROFILE_N2,
-                        state="jet", gas_giant=name.endswith("gg"), turbulence=turb)
+                        state="jet", gas_giant="gg" in name, turbulence=turb, **h2)
     return HSConfig(ni=ni, nj=nj, nk=nk, dt=dt, seed=seed, advection_scheme=ADVECTION[advection], turbulence=turb)
 
 
@@ -244,6 +246,7 @@ def workload_config(args, cfg, nmem, ws):
     else:
         what = (("Zonal jets on the Held-Suarez planet " if cfg.state == "jet" else "Held-Suarez ") +
                 ("over the gas-giant lower boundary (GZ_SURFACE from gz_from_u) " if cfg.gas_giant else "") +
+                ("with the hydrogen-helium thermodynamics (x_h2 0.864, x_he 0.136, normal hydrogen) " if cfg.x_h2 > 0 else "") +
                 ("with the Spalart-Allmaras DES turbulence closure " if cfg.turbulence else "") +
                 f"{cfg.ni}x{cfg.nj}x{cfg.nk}, dt={cfg.dt}s, AB3, {ADVECTION_NAME[args.advection]}, nu4=0.5 max")
     return {"workload": what, "ni": cfg.ni, "nj": cfg.nj, "nk": cfg.nk, "dt": cfg.dt, "members": nmem,

@@ -274,10 +274,10 @@ __device__ __forceinline__ const double *th_thgrid(const DevModel &M) { return M
 __device__ __forceinline__ const double *th_fpdat(const DevModel &M) { return M.thermo + TH_N * TH_M + 4 * TH_M; }
 
 // return_temp, epic_funcs_diag.c:6112-6210: the ideal relation, or with hydrogen the table of
-// temperature against para fraction and mean potential temperature (bilinear)
-__device__ __forceinline__ double return_temp(const DevModel &M, double p, double theta) {
-  if (M.x_h2 == 0.) return theta * xpow(M, p / M.press0, M.kappa);
-  const double theta1 = theta * xpow(M, p / M.press0, M.kappa);
+// temperature against para fraction and mean potential temperature (bilinear).  The hydrogen
+// part, from the ideal-gas temperature theta1 = theta (p/p0)^kappa (which the mixed forms' column
+// kernels evaluate with their own power):
+__device__ __forceinline__ double hydrogen_temp(const DevModel &M, double theta1) {
   if (theta1 <= 20.) return theta1;
   if (theta1 >= 600.)
     return xexp(M, (M.cpr * xlog(M, theta1) - 2.5 * M.x_h2 * ((1. - TH_FP) * -2.105769 + TH_FP * -1.666421)) /
@@ -296,6 +296,10 @@ __device__ __forceinline__ double return_temp(const DevModel &M, double p, doubl
   else fth = fmod(em, 1.);
   return t[n * TH_M + m] * (1. - fth) * (1. - ffp) + t[(n + 1) * TH_M + m] * (1. - fth) * (ffp) +
          t[n * TH_M + m + 1] * (fth) * (1. - ffp) + t[(n + 1) * TH_M + m + 1] * (fth) * (ffp);
+}
+__device__ __forceinline__ double return_temp(const DevModel &M, double p, double theta) {
+  if (M.x_h2 == 0.) return theta * xpow(M, p / M.press0, M.kappa);
+  return hydrogen_temp(M, theta * xpow(M, p / M.press0, M.kappa));
 }
 __device__ __forceinline__ double return_density(double p, double t, double mu) { return p * mu / (8.314472e+3 * t); }
 __device__ __forceinline__ double return_enthalpy(const DevModel &M, double t) {

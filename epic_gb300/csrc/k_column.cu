@@ -768,11 +768,11 @@ __global__ void __launch_bounds__(CT_THREADS, 4) k_pgrad_vars_column_mixed(DevMo
       const long long x = c.base + k * n2;
       float pf = 0.f;
       double t3, rho;
-      if (H2) {
-        t3 = return_temp(M, p, theta);
+      pf = powf(d2f(p) * p0_inv, kap);
+      if (H2) {   // the table at the binary32 ideal-gas temperature
+        t3 = hydrogen_temp(M, f2d(d2f(theta) * pf));
         rho = return_density(p, t3, mu);
       } else {
-        pf = powf(d2f(p) * p0_inv, kap);
         const float t3f = d2f(theta) * pf;
         t3 = f2d(t3f);
         rho = f2d(d2f(p) * mu_over_r / t3f);
@@ -787,7 +787,7 @@ __global__ void __launch_bounds__(CT_THREADS, 4) k_pgrad_vars_column_mixed(DevMo
       if (k >= 1) {
         double r2;
         if (H2) {
-          const double t2 = return_temp(M, pr, th2);
+          const double t2 = hydrogen_temp(M, f2d(d2f(th2) * powf(d2f(pr) * p0_inv, kap)));
           M.t2[x] = t2;
           r2 = return_density(pr, t2, mu);
         } else {

@@ -167,7 +167,8 @@ __global__ void __launch_bounds__(CT_THREADS, 4) k_set_p2etc_acc(DevModel M, int
 // FULL = false: GZ3 alone (with its monotonicity check) -- the call before the filtered-GZ
 // copy, whose other outputs the call after stage 11 rewrites before anything reads them.
 // H2: the hydrogen thermodynamics (x_h2 > 0): T3, T2 and the enthalpy of MONT3 from thermo_setup's
-// tables in binary64 (return_temp, return_enthalpy), EXNER3 = cp T3 / THETA as the reference
+// tables in binary64 (hydrogen_temp of the ideal-gas temperature this kernel evaluates anyway,
+// return_enthalpy), EXNER3 = cp T3 / THETA as the reference
 // stores it (epic_funcs_diag.c:3698, :3717); the ideal-gas power (p/p0)^kappa is then not T3/THETA.
 template <bool FULL, bool H2>
 __device__ __forceinline__ void pgrad_vars_column_acc(DevModel &M) {
@@ -186,8 +187,8 @@ __device__ __forceinline__ void pgrad_vars_column_acc(DevModel &M) {
   auto level = [&](int k, double theta, double p, double pr, double th2, float2 lpk) {
     const long long x = c.base + k * n2;
     const dfl Pk = cv<dfl>(p);
-    const double t3d = H2 ? return_temp(M, p, theta) : 0.;
-    const dfl pi = H2 ? dfl(0.f, 0.f) : exp_df(kap * (dfl(lpk.x, lpk.y) - lp0), tab);   // (p/p0)^kappa
+    const dfl pi = exp_df(kap * (dfl(lpk.x, lpk.y) - lp0), tab);   // (p/p0)^kappa
+    const double t3d = H2 ? hydrogen_temp(M, to_d(cv<dfl>(theta) * pi)) : 0.;
     CT(LP, k) = lpk;
     const dfl t3 = H2 ? cv<dfl>(t3d) : cv<dfl>(theta) * pi;
     const double rho = to_d(Pk * mu_over_r / t3);
@@ -200,8 +201,8 @@ __device__ __forceinline__ void pgrad_vars_column_acc(DevModel &M) {
     CT(R, k) = rho;
     CT(T3, k) = make_float2(t3.hi, t3.lo);
     if (FULL && k >= 1) {   // the layer's T2, RHO2: read by the Richardson number only
-      if (H2) {
-        const double t2 = return_temp(M, pr, th2);
+      if (H2) {   // T2 from the binary32 power, as the ideal gas's
+        const double t2 = hydrogen_temp(M, f2d(d2f(th2) * powf(d2f(pr) * p0_inv.hi, kap.hi)));
         M.t2[x] = t2;
         const double r2 = return_density(pr, t2, M.mu_dry);
         M.rho2[x] = r2;
