@@ -77,14 +77,17 @@ class _Active:
 def launch_class(cfg: HSConfig, k_sigma: int, precision: int, size_ratio: int = 16) -> tuple:
     """What the members of one Batch must share (epic_batch_create): layers and the pure-sigma
     split, schemes, precision form, which viscosity orders and whether divergence damping act,
-    the filter latitude, and in the mixed forms whether ni takes the tensor-core filter -- plus a
+    the filter latitude, the lower boundary (gas giant or terrain), the thermodynamics (hydrogen
+    tables or the ideal gas), the turbulence closure and its diffusion directions, and in the
+    mixed forms whether ni takes the tensor-core filter -- plus a
     size bucket: a batch's step takes as long as its largest member's, so runs are batched only
     with runs whose cell count lies in the same power of size_ratio (0 batches every size of a
     class together)."""
     tensor_filter = precision != EPIC_PREC_FP64 and cfg.ni % 128 == 0 and cfg.ni <= 1024
     bucket = int(math.log(cfg.ni * cfg.nj * cfg.nk, size_ratio)) if size_ratio > 1 else 0
     return (cfg.nk, k_sigma, cfg.uv_scheme, cfg.advection_scheme, precision, tensor_filter, cfg.nu4 > 0, cfg.nu6 > 0,
-            cfg.nu8 > 0, cfg.nudiv != 0, cfg.lat0, bucket)
+            cfg.nu8 > 0, cfg.nudiv != 0, cfg.lat0, cfg.gas_giant, cfg.x_h2 > 0,
+            cfg.diffusion_direction if cfg.turbulence else None, bucket)
 
 
 def state_checksum(f: Fields) -> float:

@@ -8,6 +8,7 @@ import numpy as np
 import pytest
 
 from epic_gb300 import HSConfig
+from epic_gb300.abi import EPIC_DIFFUSION_JUST_VERTICAL
 from epic_gb300.serving import RunRequest, RunServer, latency_summary
 
 
@@ -148,6 +149,20 @@ def test_durations_in_simulated_days():
         days = r.steps * r.cfg.dt / 86400.0
         assert 0.25 - 1e-3 <= days <= 2.0 + 1e-3
     assert all(np.diff([r.arrival for r in reqs]) > 0)
+
+
+def test_launch_class_separates_physics_a_batch_must_share():
+    """Runs over the gas-giant boundary, with the hydrogen tables or with the turbulence closure
+    (per diffusion direction) each form their own launch class (epic_batch_create refuses to mix
+    them); the seed, drag scale and initial state do not split a class."""
+    from epic_gb300.serving import launch_class
+    base = HSConfig(ni=32, nj=16, nk=10)
+    variants = [HSConfig(ni=32, nj=16, nk=10, gas_giant=True), HSConfig(ni=32, nj=16, nk=10, x_h2=0.864, x_he=0.136),
+                HSConfig(ni=32, nj=16, nk=10, turbulence=True),
+                HSConfig(ni=32, nj=16, nk=10, turbulence=True, diffusion_direction=EPIC_DIFFUSION_JUST_VERTICAL)]
+    keys = [launch_class(c, 10, 0) for c in [base] + variants]
+    assert len(set(keys)) == len(keys)
+    assert launch_class(HSConfig(ni=32, nj=16, nk=10, seed=5, state="jet"), 10, 0) == keys[0]
 
 
 def test_size_buckets_keep_small_runs_out_of_large_batches():
